@@ -1,0 +1,115 @@
+/*
+ * simpimc_gb300 — C interface of the GB300 path-integral Monte Carlo action/estimator library.
+ *
+ * One context = one simulation (path, actions, moves, observables, algorithm loop) on one GPU,
+ * built from a simpimc XML input. Every call returns PIMC_OK (0) or a negative PIMC_ERR_* code;
+ * pimc_last_error() gives the message of the last failing call on that context. No call exits
+ * the process, traps the device or throws across this boundary.
+ *
+ * Path buffers crossing the boundary are host arrays in the reference's bead order
+ * (species_class.h:236-244, "init_type=File all_beads=1"): pos[g][b][d] with g the particle index
+ * over all species in declaration order, b the time slice, d the Cartesian component.
+ *
+ * Each entry point names the reference interface it replaces (paths inside etano/simpimc).
+ */
+#ifndef SIMPIMC_GB300_H_
+#define SIMPIMC_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PIMC_OK 0
+#define PIMC_ERR_ARG (-1)         /* invalid argument (index, range, null pointer) */
+#define PIMC_ERR_INPUT (-2)       /* malformed XML, missing attribute or table file */
+#define PIMC_ERR_CUDA (-3)        /* CUDA runtime failure */
+#define PIMC_ERR_TIMEOUT (-4)     /* a bounded device wait expired */
+#define PIMC_ERR_NONFINITE (-5)   /* non-finite coordinate or action difference */
+#define PIMC_ERR_UNSUPPORTED (-6) /* input uses a feature outside this library */
+#define PIMC_ERR_STATE (-7)       /* call not valid in the current state */
+
+typedef struct pimc_ctx pimc_ctx;
+
+typedef struct pimc_info {
+    uint32_t n_d, n_bead, n_species, n_total, n_k, n_actions, n_moves, n_observables;
+    double beta, tau, L, volume;
+    int32_t pbc;
+} pimc_info;
+
+/* Framework + Simulation construction (src/framework/framework_class.h:87-128,
+ * src/framework/simulation_class.h:16-39). `base_dir` resolves relative table paths; `chain`
+ * selects the independent random stream (the reference's clone index, framework_class.h:96). */
+int pimc_create(const char* xml_text, const char* base_dir, int device, uint32_t chain, pimc_ctx** out);
+void pimc_destroy(pimc_ctx* ctx);
+const char* pimc_last_error(const pimc_ctx* ctx);
+int pimc_get_info(pimc_ctx* ctx, pimc_info* out);
+/* Overrides the <RNG seed> (framework_class.h:132-147). */
+int pimc_set_seed(pimc_ctx* ctx, uint32_t seed);
+/* Names: kind 0 species, 1 action, 2 move, 3 observable. */
+int pimc_get_name(pimc_ctx* ctx, int kind, uint32_t index, char* buf, size_t cap);
+int pimc_species_info(pimc_ctx* ctx, uint32_t species, uint32_t* n_part, uint32_t* offset, double* lambda);
+
+/* Path state: Bead::SetR / StoreR and Species::InitRhoK (bead_class.h:255-302,
+ * species_class.h:236-244,380-403). which: 0 the stored ("old") copy, 1 the working ("new") copy,
+ * 2 both (then the per-slice charge densities are recomputed from the positions). */
+int pimc_set_path(pimc_ctx* ctx, int which, const double* pos);
+int pimc_get_path(pimc_ctx* ctx, int which, double* pos);
+/* Per-slice charge density of a species, [n_bead][n_k][re, im] (species_class.h:23,428). */
+int pimc_get_rho_k(pimc_ctx* ctx, uint32_t species, double* out);
+/* Stored half-space k-vectors [n_k][n_d] (k_space_class.h:33-80). */
+int pimc_get_kvecs(pimc_ctx* ctx, double* out);
+
+/* Action interface (src/actions/action_class.h:37-52). Particles are (species, index) pairs as
+ * in the reference's std::vector<std::pair<std::shared_ptr<Species>, uint32_t>>. mode 0 reads the
+ * stored copy (OLD_MODE), 1 the working copy (NEW_MODE, bead_class.h:204-206). */
+/* Action::GetAction (action_class.h:43) */
+int pimc_get_action(pimc_ctx* ctx, uint32_t action, uint32_t b0, uint32_t b1, const uint32_t* species, const uint32_t* particles,
+                    uint32_t n_particles, uint32_t level, int mode, double* out);
+/* Action::GetActionGradient (action_class.h:46); out has n_d entries. */
+int pimc_get_action_gradient(pimc_ctx* ctx, uint32_t action, uint32_t b0, uint32_t b1, const uint32_t* species,
+                             const uint32_t* particles, uint32_t n_particles, uint32_t level, int mode, double* out);
+/* Action::DActionDBeta (action_class.h:37) */
+int pimc_dactiondbeta(pimc_ctx* ctx, uint32_t action, double* out);
+/* Action::Potential (action_class.h:52) */
+int pimc_potential(pimc_ctx* ctx, uint32_t action, double* out);
+/* Action::VirialEnergy (action_class.h:40) */
+int pimc_virial_energy(pimc_ctx* ctx, uint32_t action, double window, double* out);
+
+/* Moves: Move::DoEvent repeated (move_class.h:277-293, bisect_class.h:24-139). Runs n attempts
+ * of move `move` on the device in one launch. */
+int pimc_move_attempts(pimc_ctx* ctx, uint32_t move, uint64_t n);
+/* A schedule of moves, (moves[i], counts[i]) in order, repeated n_rep times, in one launch
+ * (the body of a Loop of Move events, loop_class.h:269-274). */
+int pimc_sweep(pimc_ctx* ctx, const uint32_t* moves, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep);
+/* out[5] = {total attempts, attempts in block, accepts in block, total accepts, total attempts
+ * that reached the level-0 test} (counters of move_class.h:226-228). */
+int pimc_move_stats(pimc_ctx* ctx, uint32_t move, uint64_t* out);
+
+/* Observables: Observable::DoEvent / Write (observable_class.h:421-432). pimc_observable_block
+ * returns the normalised values Write() would append (energy_class.h:232-325,
+ * pair_correlation_class.h:89-123, structure_factor_class.h:195-211) and resets the block. */
+int pimc_observable_accumulate(pimc_ctx* ctx, uint32_t observable);
+int pimc_observable_block(pimc_ctx* ctx, uint32_t observable, double* out, size_t cap, size_t* n);
+
+/* Simulation::Run (simulation_class.h:42-45): the XML <Algorithm> loop. Block values are kept
+ * per observable and read back with pimc_get_block. */
+int pimc_run(pimc_ctx* ctx);
+int pimc_n_blocks(pimc_ctx* ctx, uint32_t observable, size_t* n);
+int pimc_get_block(pimc_ctx* ctx, uint32_t observable, size_t block, double* out, size_t cap, size_t* n);
+
+/* Synchronises the context stream and reports any device-side error (timeout, non-finite). */
+int pimc_synchronize(pimc_ctx* ctx);
+/* Tuning: CTAs of the cooperative sweep (0 = automatic) and the device wait limit. */
+int pimc_set_sweep_grid(pimc_ctx* ctx, int grid);
+int pimc_set_timeout_ns(pimc_ctx* ctx, uint64_t ns);
+/* CUDA stream of the context (cudaStream_t), for callers that enqueue their own work. */
+void* pimc_stream(pimc_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SIMPIMC_GB300_H_ */

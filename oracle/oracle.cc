@@ -1,0 +1,1704 @@
+// ORACLE — test infrastructure only. Nothing in the product library links, loads or calls this file;
+// it is the CPU checker used by tests/, the smoke check and the bench's CPU-baseline leg.
+//
+// A plain C++/FP64 restatement of simpimc's action/move/estimator hot path, written to follow the
+// reference's own loops and quirks one for one. Each class cites the reference file:line it restates.
+// The reference itself cannot be built here: it needs the scaffold submodule (empty), Armadillo,
+// HDF5, einspline (fetched from an unpinned master tarball) and MPI. Its repository holds no unit
+// tests, fixtures or golden vectors for this path. Parity is therefore pinned through known answers
+// instead: the exact discrete-path energy of harmonic oscillators (the reference's inputs/sho case
+// and the trapped-particle configuration), Philox known-answer vectors, natural-spline identities
+// and independent Ewald sums (tests/test_oracle_*.py).
+//
+// Deliberate, documented departures (each one also listed in the design doc):
+//  * einspline's natural-BC cubic B-splines are represented as the (identical) natural cubic
+//    interpolating spline; arguments are clamped to the grid.
+//  * The scaffold RNG is replaced by the Philox draw protocol shared with the GPU path.
+//  * k-vectors are enumerated lexicographically (the reference's GenCombPermK order is unavailable);
+//    only the summation order differs.
+//  * Open boundaries (pbc=0) skip k-space setup (the reference divides by L=0 there).
+//  * Permutations are not modelled: beads link to the same particle on neighbouring slices.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <ctime>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../simpimc_gb300/src/framework/input.h"
+#include "../simpimc_gb300/src/framework/table_io.h"
+
+namespace orc {
+
+using pimc::Input;
+using pimc::InputError;
+using pimc::TableFile;
+typedef std::complex<double> cplx;
+
+// ---------------------------------------------------------------------------------------------
+// Philox4x32-10, written out independently of the product's copy (same published algorithm).
+struct RNG4 {
+    uint32_t w[4];
+};
+
+static RNG4 philox(uint32_t c[4], uint32_t k0, uint32_t k1) {
+    uint32_t x0 = c[0], x1 = c[1], x2 = c[2], x3 = c[3];
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * x0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * x2;
+        uint32_t y0 = (uint32_t)(p1 >> 32) ^ x1 ^ k0;
+        uint32_t y1 = (uint32_t)p1;
+        uint32_t y2 = (uint32_t)(p0 >> 32) ^ x3 ^ k1;
+        uint32_t y3 = (uint32_t)p0;
+        x0 = y0;
+        x1 = y1;
+        x2 = y2;
+        x3 = y3;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    RNG4 o = {{x0, x1, x2, x3}};
+    return o;
+}
+
+struct Stream {
+    uint32_t seed, chain, move;
+    uint64_t attempt;
+    RNG4 block(uint32_t b) const {
+        uint32_t c[4] = {(uint32_t)attempt, (uint32_t)(attempt >> 32), move, b};
+        return philox(c, seed, chain);
+    }
+};
+
+static double u53(uint32_t a, uint32_t b) { return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0); }
+static uint32_t uidx(uint32_t w, uint32_t n) { return (uint32_t)(((uint64_t)w * n) >> 32); }
+static void boxmuller(const RNG4& w, double& z0, double& z1) {
+    double u0 = u53(w.w[0], w.w[1]), u1 = u53(w.w[2], w.w[3]);
+    double r = std::sqrt(-2.0 * std::log(1.0 - u0));
+    double th = 6.283185307179586 * u1;
+    z0 = r * std::cos(th);
+    z1 = r * std::sin(th);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Natural cubic interpolating spline (stands in for einspline UBspline_1d_d / NUBspline_1d_d with
+// {NATURAL, NATURAL} boundary conditions: free_spline_class.h:177-180, bare_pair_action_class.h:36-67).
+struct Spline {
+    std::vector<double> x, y, m;  // knots, values, second derivatives
+    bool uniform = false;
+    double x0 = 0., dx = 1.;
+
+    void Build(const std::vector<double>& xs, const std::vector<double>& ys, bool is_uniform) {
+        x = xs;
+        y = ys;
+        uniform = is_uniform;
+        size_t n = x.size();
+        m.assign(n, 0.);
+        if (uniform) {
+            x0 = x[0];
+            dx = (x[n - 1] - x[0]) / (double)(n - 1);
+        }
+        if (n < 3) return;
+        std::vector<double> c(n, 0.), d(n, 0.);
+        // Thomas algorithm on rows 1..n-2 with m_0 = m_{n-1} = 0.
+        for (size_t i = 1; i + 1 < n; ++i) {
+            double h0 = x[i] - x[i - 1], h1 = x[i + 1] - x[i];
+            double a = h0, b = 2. * (h0 + h1), cc = h1;
+            double r = 6. * ((y[i + 1] - y[i]) / h1 - (y[i] - y[i - 1]) / h0);
+            if (i > 1) {
+                b -= a * c[i - 1];
+                r -= a * d[i - 1];
+            }
+            c[i] = cc / b;
+            d[i] = r / b;
+        }
+        m[n - 2] = d[n - 2];
+        for (size_t i = n - 2; i-- > 1;) m[i] = d[i] - c[i] * m[i + 1];
+    }
+
+    size_t Interval(double& t) const {
+        size_t n = x.size();
+        if (t < x[0]) t = x[0];
+        if (t > x[n - 1]) t = x[n - 1];
+        size_t i;
+        if (uniform) {
+            double f = std::floor((t - x0) / dx);
+            i = f < 0. ? 0 : (size_t)f;
+            if (i > n - 2) i = n - 2;
+        } else {
+            i = (size_t)(std::upper_bound(x.begin(), x.end(), t) - x.begin());
+            i = i == 0 ? 0 : i - 1;
+            if (i > n - 2) i = n - 2;
+        }
+        return i;
+    }
+
+    double Eval(double t) const {
+        size_t i = Interval(t);
+        double h = x[i + 1] - x[i];
+        double A = (x[i + 1] - t) / h, B = 1. - A;
+        return A * y[i] + B * y[i + 1] + ((A * A * A - A) * m[i] + (B * B * B - B) * m[i + 1]) * h * h / 6.;
+    }
+
+    void EvalVG(double t, double& v, double& g) const {
+        size_t i = Interval(t);
+        double h = x[i + 1] - x[i];
+        double A = (x[i + 1] - t) / h, B = 1. - A;
+        v = A * y[i] + B * y[i + 1] + ((A * A * A - A) * m[i] + (B * B * B - B) * m[i + 1]) * h * h / 6.;
+        g = (y[i + 1] - y[i]) / h + (-(3. * A * A - 1.) * m[i] + (3. * B * B - 1.) * m[i + 1]) * h / 6.;
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
+// KSpace (src/data_structures/k_space_class.h:5-95).
+struct KSpace {
+    double cutoff = 0.;
+    double L = 0.;
+    uint32_t n_d = 3;
+    std::vector<double> mags;
+    std::vector<std::vector<double>> vecs;
+    std::vector<std::vector<int>> indices;
+    std::vector<double> box;
+    std::vector<int> max_index;
+    std::vector<std::vector<cplx>> c_k;
+
+    // k_space_class.h:17-30 — half-space selection.
+    bool Include(const std::vector<double>& k, double k_cut) const {
+        double k2 = 0.;
+        for (double x : k) k2 += x * x;
+        if (k2 < k_cut * k_cut && k2 != 0.) {
+            if (k[0] > 0.) return true;
+            if (n_d >= 2 && (k[0] == 0. && k[1] > 0.)) return true;
+            if (n_d >= 3 && (k[0] == 0. && k[1] == 0. && k[2] > 0.)) return true;
+            return false;
+        }
+        return false;
+    }
+
+    // k_space_class.h:33-80. Enumeration order is lexicographic in (n_0, n_1, n_2).
+    void Setup(double k_cut) {
+        if (L == 0.) return;  // open boundaries: no k-space
+        if (k_cut <= cutoff) return;
+        vecs.clear();
+        indices.clear();
+        mags.clear();
+        cutoff = k_cut;
+        box.assign(n_d, 2. * M_PI / L);
+        max_index.assign(n_d, 0);
+        for (uint32_t d = 0; d < n_d; ++d) max_index[d] = (int)(uint32_t)std::ceil(1.1 * k_cut / box[d]);
+        c_k.assign(n_d, {});
+        for (uint32_t d = 0; d < n_d; ++d) c_k[d].assign(2 * max_index[d] + 1, cplx(0., 0.));
+        std::vector<int> n(n_d, 0);
+        std::vector<int> lo(n_d), hi(n_d);
+        for (uint32_t d = 0; d < n_d; ++d) {
+            lo[d] = -max_index[d];
+            hi[d] = max_index[d];
+        }
+        for (uint32_t d = 0; d < n_d; ++d) n[d] = lo[d];
+        for (;;) {
+            std::vector<double> k(n_d);
+            std::vector<int> ki(n_d);
+            for (uint32_t d = 0; d < n_d; ++d) {
+                k[d] = n[d] * box[d];
+                ki[d] = max_index[d] + n[d];
+            }
+            if (Include(k, k_cut)) {
+                double k2 = 0.;
+                for (double x : k) k2 += x * x;
+                vecs.push_back(k);
+                indices.push_back(ki);
+                mags.push_back(std::sqrt(k2));
+            }
+            int d = (int)n_d - 1;
+            while (d >= 0) {
+                if (++n[d] <= hi[d]) break;
+                n[d] = lo[d];
+                --d;
+            }
+            if (d < 0) break;
+        }
+    }
+
+    // k_space_class.h:83-94.
+    void CalcC(const double* r) {
+        for (uint32_t d = 0; d < box.size(); ++d) {
+            double phi = r[d] * box[d];
+            cplx t(std::cos(phi), std::sin(phi));
+            int m = max_index[d];
+            c_k[d][m] = 1.;
+            for (int k = 1; k <= m; ++k) {
+                c_k[d][m + k] = t * c_k[d][m + k - 1];
+                c_k[d][m - k] = std::conj(c_k[d][m + k]);
+            }
+        }
+    }
+
+    size_t K() const { return vecs.size(); }
+};
+
+enum Mode { OLD_MODE = 0, NEW_MODE = 1 };
+
+struct Path;
+
+// ---------------------------------------------------------------------------------------------
+// Species (src/data_structures/species_class.h:7-446) with the bead grid of bead_class.h.
+struct Species {
+    std::string name;
+    uint32_t s_i = 0, n_part = 0, n_bead = 0, n_d = 3, offset = 0;
+    double lambda = 0.;
+    bool fermi = false, fixed_node = false;
+    bool need_update_rho_k = true;
+    // Per-slice charge densities and their copies (species_class.h:23-24): [b][k].
+    std::vector<cplx> rho_k, rho_k_c;
+    // Per-bead charge densities and their copies (bead_class.h:218-219): [p][b][k].
+    std::vector<cplx> bead_rho_k, bead_rho_k_c;
+    uint32_t bead_loop(uint32_t b) const { return b >= n_bead ? b - n_bead : b; }  // species_class.h:101
+};
+
+struct Path {
+    uint32_t n_d = 3, n_bead = 0;
+    double beta = 0., L = 0., iL = 0., vol = 1., tau = 0.;
+    bool pbc = true;
+    Mode mode = NEW_MODE;
+    KSpace ks;
+    std::vector<Species> species;
+    uint32_t n_total = 0;
+    std::vector<double> r, r_c;  // positions (new) and copies (old): [n_total][n_bead][n_d]
+
+    Path(const Input& in) {
+        // path_class.h:25-62
+        Input sys = in.GetChild("System");
+        n_d = sys.GetAttribute<uint32_t>("n_d");
+        n_bead = sys.GetAttribute<uint32_t>("n_bead");
+        beta = sys.GetAttribute<double>("beta");
+        pbc = sys.GetAttribute<bool>("pbc", true);
+        L = sys.GetAttribute<double>("L", 0.);
+        if (n_d < 1 || n_d > 3) throw InputError("n_d must be 1, 2 or 3");
+        if (n_bead < 2) throw InputError("n_bead must be at least 2");
+        if (pbc) {
+            if (!(L > 0.)) throw InputError("pbc=1 needs a positive L");
+            iL = 1. / L;
+            vol = std::pow(L, n_d);
+        } else {
+            L = 0.;
+            iL = 0.;
+            vol = 1.;
+        }
+        tau = beta / (1. * n_bead);
+        ks.n_d = n_d;
+        ks.L = L;
+        ks.cutoff = 0.;
+        if (pbc) ks.Setup(sys.GetAttribute<double>("k_cut", 2. * M_PI / L));
+        for (auto& sin : in.GetChild("Particles").GetChildList("Species")) {
+            Species s;
+            s.name = sin.GetAttribute<std::string>("name");
+            s.n_part = sin.GetAttribute<uint32_t>("n_part");
+            s.lambda = sin.GetAttribute<double>("lambda");
+            s.fermi = sin.GetAttribute<bool>("fermi", false);
+            s.fixed_node = sin.GetAttribute<bool>("fixed_node", false);
+            s.s_i = (uint32_t)species.size();
+            s.n_bead = n_bead;
+            s.n_d = n_d;
+            s.offset = n_total;
+            n_total += s.n_part;
+            species.push_back(s);
+        }
+        r.assign((size_t)n_total * n_bead * n_d, 0.);
+        r_c = r;
+    }
+
+    Species& GetSpecies(const std::string& nm) {
+        for (auto& s : species)
+            if (s.name == nm) return s;
+        throw InputError("no species named '" + nm + "'");
+    }
+
+    size_t Idx(const Species& s, uint32_t p, uint32_t b) const { return (((size_t)(s.offset + p)) * n_bead + s.bead_loop(b)) * n_d; }
+    double* GetR(const Species& s, uint32_t p, uint32_t b) { return (mode == NEW_MODE ? r.data() : r_c.data()) + Idx(s, p, b); }
+    double* GetRMode(const Species& s, uint32_t p, uint32_t b, Mode m) { return (m == NEW_MODE ? r.data() : r_c.data()) + Idx(s, p, b); }
+
+    // path_class.h:131-134
+    void PutInBox(double* x) const {
+        for (uint32_t d = 0; d < n_d; ++d) x[d] -= std::nearbyint(x[d] * iL) * L;
+    }
+    // path_class.h:108-112
+    void Dr(const double* r0, const double* r1, double* dr) const {
+        for (uint32_t d = 0; d < n_d; ++d) dr[d] = r0[d] - r1[d];
+        PutInBox(dr);
+    }
+    // path_class.h:137-150
+    void DrDrpDrrp(uint32_t b0, uint32_t b1, const Species& s0, const Species& s1, uint32_t p0, uint32_t p1, double& r_mag,
+                   double& r_p_mag, double& r_r_p_mag) {
+        double rv[3], rp[3], rrp[3];
+        const double* a0 = GetR(s1, p1, b0);
+        const double* c0 = GetR(s0, p0, b0);
+        const double* a1 = GetR(s1, p1, b1);
+        const double* c1 = GetR(s0, p0, b1);
+        for (uint32_t d = 0; d < n_d; ++d) {
+            rv[d] = a0[d] - c0[d];
+            rp[d] = a1[d] - c1[d];
+        }
+        for (uint32_t d = 0; d < n_d; ++d) {
+            rv[d] -= std::nearbyint(rv[d] * iL) * L;
+            rp[d] += std::nearbyint((rv[d] - rp[d]) * iL) * L;
+        }
+        for (uint32_t d = 0; d < n_d; ++d) rrp[d] = rv[d] - rp[d];
+        for (uint32_t d = 0; d < n_d; ++d) rrp[d] -= std::nearbyint(rrp[d] * iL) * L;
+        double a = 0., b = 0., c = 0.;
+        for (uint32_t d = 0; d < n_d; ++d) {
+            a += rv[d] * rv[d];
+            b += rp[d] * rp[d];
+            c += rrp[d] * rrp[d];
+        }
+        r_mag = std::sqrt(a);
+        r_p_mag = std::sqrt(b);
+        r_r_p_mag = std::sqrt(c);
+    }
+
+    // bead_class.h:323-331 — rho_k of one bead from the current-mode position.
+    void CalcBeadRhoK(Species& s, uint32_t p, uint32_t b, cplx* out) {
+        ks.CalcC(GetR(s, p, b));
+        for (size_t k = 0; k < ks.K(); ++k) {
+            cplx f = 1.;
+            for (uint32_t d = 0; d < ks.n_d; ++d) f *= ks.c_k[d][ks.indices[k][d]];
+            out[k] = f;
+        }
+    }
+
+    cplx* BeadRhoK(Species& s, uint32_t p, uint32_t b, Mode m) {
+        size_t K = ks.K();
+        size_t off = ((size_t)p * n_bead + s.bead_loop(b)) * K;
+        return (m == NEW_MODE ? s.bead_rho_k.data() : s.bead_rho_k_c.data()) + off;
+    }
+
+    // species_class.h:380-403
+    void InitRhoK(Species& s) {
+        size_t K = ks.K();
+        s.rho_k.assign((size_t)n_bead * K, cplx(0., 0.));
+        s.bead_rho_k.assign((size_t)s.n_part * n_bead * K, cplx(0., 0.));
+        if (K == 0) {
+            s.rho_k_c = s.rho_k;
+            s.bead_rho_k_c = s.bead_rho_k;
+            return;
+        }
+        Mode keep = mode;
+        mode = NEW_MODE;
+        for (uint32_t b = 0; b < n_bead; ++b)
+            for (uint32_t p = 0; p < s.n_part; ++p) CalcBeadRhoK(s, p, b, BeadRhoK(s, p, b, NEW_MODE));
+        for (uint32_t b = 0; b < n_bead; ++b)
+            for (uint32_t p = 0; p < s.n_part; ++p) {
+                const cplx* br = BeadRhoK(s, p, b, NEW_MODE);
+                cplx* sr = &s.rho_k[(size_t)b * K];
+                for (size_t k = 0; k < K; ++k) sr[k] += br[k];
+            }
+        s.rho_k_c = s.rho_k;
+        s.bead_rho_k_c = s.bead_rho_k;
+        mode = keep;
+    }
+
+    // species_class.h:406-425 (NEW mode only)
+    void UpdateRhoK(Species& s, uint32_t b0, uint32_t b1, const std::vector<uint32_t>& parts, uint32_t level) {
+        size_t K = ks.K();
+        uint32_t skip = 1u << level;
+        for (uint32_t b = b0; b < b1; b += skip) {
+            uint32_t bb = s.bead_loop(b);
+            std::copy(s.rho_k_c.begin() + (size_t)bb * K, s.rho_k_c.begin() + (size_t)(bb + 1) * K, s.rho_k.begin() + (size_t)bb * K);
+        }
+        for (uint32_t p : parts) {
+            for (uint32_t b = b0; b < b1; b += skip) {
+                cplx* nw = BeadRhoK(s, p, b, NEW_MODE);
+                CalcBeadRhoK(s, p, b, nw);
+                const cplx* od = BeadRhoK(s, p, b, OLD_MODE);
+                cplx* sr = &s.rho_k[(size_t)s.bead_loop(b) * K];
+                for (size_t k = 0; k < K; ++k) sr[k] += nw[k] - od[k];
+            }
+        }
+        s.need_update_rho_k = false;
+    }
+
+    const std::vector<cplx>& GetRhoK(const Species& s) const { return mode == NEW_MODE ? s.rho_k : s.rho_k_c; }
+};
+
+typedef std::vector<std::pair<uint32_t, uint32_t>> Particles;  // (species index, particle index)
+
+static double CMag2(const cplx& a, const cplx& b) { return a.real() * b.real() + a.imag() * b.imag(); }
+
+// ---------------------------------------------------------------------------------------------
+// FreeSpline (src/actions/free_spline_class.h:25-122).
+struct FreeSpline {
+    double i_4_lambda_tau = 0., i_4_lambda_tau_tau = 0.;
+    Spline image_action, d_image_action_d_tau;
+    bool has_dtau = false;
+
+    FreeSpline() {}
+    FreeSpline(double L, uint32_t n_images, double lambda, double tau, bool use_tau_derivative) {
+        i_4_lambda_tau = 1. / (4. * lambda * tau);
+        i_4_lambda_tau_tau = 1. / (4. * lambda * tau * tau);
+        double t_l = L == 0. ? 1000. : L;
+        const uint32_t num = 10000;
+        double start = -t_l / 2., end = t_l / 2.;
+        double dr = (end - start) / (num - 1);
+        std::vector<double> xs(num), ia(num, 0.), dia(num, 0.);
+        for (uint32_t i = 0; i < num; ++i) {
+            double r = start + i * dr;
+            xs[i] = r;
+            double r2 = r * r * i_4_lambda_tau;
+            for (uint32_t image = 1; image <= n_images; ++image) {
+                double rp = r + image * t_l;
+                double dp = r2 - rp * rp * i_4_lambda_tau;
+                double ep = std::exp(dp);
+                double rm = r - image * t_l;
+                double dm = r2 - rm * rm * i_4_lambda_tau;
+                double em = std::exp(dm);
+                ia[i] += ep + em;
+                if (use_tau_derivative) dia[i] += (dp * ep + dm * em) / tau;
+            }
+            if (use_tau_derivative) dia[i] = dia[i] / (1. + ia[i]);
+            ia[i] = -std::log1p(ia[i]);
+        }
+        image_action.Build(xs, ia, true);
+        if (use_tau_derivative) {
+            d_image_action_d_tau.Build(xs, dia, true);
+            has_dtau = true;
+        }
+    }
+
+    double GetLogRhoFree(const double* r, uint32_t n_d) const {
+        double tot = 0., r2 = 0.;
+        for (uint32_t d = 0; d < n_d; ++d) {
+            tot -= image_action.Eval(r[d]);
+            r2 += r[d] * r[d];
+        }
+        return tot - r2 * i_4_lambda_tau;
+    }
+    double GetDLogRhoFreeDTau(const double* r, uint32_t n_d) const {
+        double tot = 0., r2 = 0.;
+        for (uint32_t d = 0; d < n_d; ++d) {
+            tot -= d_image_action_d_tau.Eval(r[d]);
+            r2 += r[d] * r[d];
+        }
+        return tot - r2 * i_4_lambda_tau_tau;
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
+// Action base (src/actions/action_class.h:7-74).
+struct Action {
+    Path& path;
+    std::string name, type;
+    int n_images = 0;
+    uint32_t max_level = 0;
+    bool is_importance_weight = false;
+    std::vector<uint32_t> species_list;
+
+    Action(Path& p, const Input& in) : path(p) {
+        name = in.GetAttribute<std::string>("name");
+        type = in.GetAttribute<std::string>("type");
+        n_images = in.GetAttribute<int>("n_images", 0);
+        max_level = in.GetAttribute<uint32_t>("max_level", 0);
+    }
+    virtual ~Action() {}
+    virtual double DActionDBeta() { return 0.; }
+    virtual double VirialEnergy(double) { return DActionDBeta(); }
+    virtual double GetAction(uint32_t, uint32_t, const Particles&, uint32_t) { return 0.; }
+    virtual void GetActionGradient(uint32_t, uint32_t, const Particles&, uint32_t, double* g) {
+        for (uint32_t d = 0; d < path.n_d; ++d) g[d] = 0.;
+    }
+    virtual double Potential() { return 0.; }
+    virtual void Accept() {}
+    virtual void Reject() {}
+};
+
+// src/actions/single_action/single_action_class.h:245-262
+struct SingleAction : Action {
+    double i_4_lambda_tau;
+    Species* species;
+    SingleAction(Path& p, const Input& in) : Action(p, in) {
+        species = &p.GetSpecies(in.GetAttribute<std::string>("species"));
+        i_4_lambda_tau = 1. / (4. * species->lambda * p.tau);
+        species_list.push_back(species->s_i);
+    }
+};
+
+// src/actions/single_action/kinetic_class.h:10-169
+struct Kinetic : SingleAction {
+    double d_action_d_beta_const;
+    std::vector<FreeSpline> rho_free_splines;
+
+    Kinetic(Path& p, const Input& in) : SingleAction(p, in) {
+        d_action_d_beta_const = species->n_part * species->n_bead * p.n_d / (2. * p.tau);
+        // kinetic_class.h:16-24
+        uint32_t n_spline = species->n_bead / 2 + (species->n_bead % 2) + 1;
+        rho_free_splines.resize(n_spline);
+        rho_free_splines[0] = FreeSpline(p.L, n_images, species->lambda, p.tau, true);
+        for (uint32_t i = 1; i < n_spline; ++i) rho_free_splines[i] = FreeSpline(p.L, n_images, species->lambda, p.tau * (i + 1), false);
+    }
+
+    // kinetic_class.h:35-45
+    double DActionDBeta() override {
+        double tot = d_action_d_beta_const;
+        double dr[3];
+        for (uint32_t b = 0; b < species->n_bead; ++b)
+            for (uint32_t p = 0; p < species->n_part; ++p) {
+                path.Dr(path.GetR(*species, p, b), path.GetR(*species, p, b + 1), dr);
+                tot += rho_free_splines[0].GetDLogRhoFreeDTau(dr, path.n_d);
+            }
+        return tot;
+    }
+
+    // kinetic_class.h:48-102
+    double VirialEnergy(double window) override {
+        uint32_t n_d = path.n_d, M = species->n_bead;
+        double tot = d_action_d_beta_const / window;
+        for (uint32_t p = 0; p < species->n_part; ++p) {
+            uint32_t b0 = 0, b1 = 1, b2 = 2 % M;
+            double dr1[3], drL[3], t[3];
+            path.Dr(path.GetR(*species, p, b1), path.GetR(*species, p, b0), dr1);
+            for (uint32_t d = 0; d < n_d; ++d) drL[d] = dr1[d];
+            for (uint32_t s = 1; s < window; ++s) {
+                path.Dr(path.GetR(*species, p, b2), path.GetR(*species, p, b1), t);
+                for (uint32_t d = 0; d < n_d; ++d) drL[d] += t[d];
+                b1 = b2;
+                b2 = (b2 + 1) % M;
+            }
+            double dot = 0.;
+            for (uint32_t d = 0; d < n_d; ++d) dot += drL[d] * dr1[d];
+            tot -= dot * i_4_lambda_tau / (window * path.tau);
+            for (uint32_t b = 1; b < M; ++b) {
+                for (uint32_t d = 0; d < n_d; ++d) drL[d] -= dr1[d];
+                path.Dr(path.GetR(*species, p, b2), path.GetR(*species, p, b1), t);
+                for (uint32_t d = 0; d < n_d; ++d) drL[d] += t[d];
+                b0 = (b0 + 1) % M;
+                path.Dr(path.GetR(*species, p, (b0 + 1) % M), path.GetR(*species, p, b0), dr1);
+                b1 = b2;
+                b2 = (b2 + 1) % M;
+                dot = 0.;
+                for (uint32_t d = 0; d < n_d; ++d) dot += drL[d] * dr1[d];
+                tot -= dot * i_4_lambda_tau / (window * path.tau);
+            }
+        }
+        return tot;
+    }
+
+    // kinetic_class.h:105-122 (beads link to the same particle: no permutations)
+    double GetAction(uint32_t b0, uint32_t b1, const Particles& parts, uint32_t level) override {
+        uint32_t skip = 1u << level;
+        uint32_t M = species->n_bead;
+        double tot = 0., dr[3];
+        for (auto& pr : parts) {
+            if (pr.first != species->s_i) continue;
+            uint32_t a = b0 % M, end = b1 % M;
+            while (a != end) {
+                uint32_t nx = (a + skip) % M;
+                path.Dr(path.GetR(*species, pr.second, a), path.GetR(*species, pr.second, nx), dr);
+                tot -= rho_free_splines[skip - 1].GetLogRhoFree(dr, path.n_d);
+                a = nx;
+            }
+        }
+        return tot;
+    }
+
+    // kinetic_class.h:125-144
+    void GetActionGradient(uint32_t b0, uint32_t b1, const Particles& parts, uint32_t level, double* g) override {
+        uint32_t skip = 1u << level;
+        uint32_t M = species->n_bead, n_d = path.n_d;
+        double i4 = i_4_lambda_tau / skip;
+        double tot[3] = {0., 0., 0.}, t[3];
+        for (auto& pr : parts) {
+            if (pr.first != species->s_i) continue;
+            uint32_t a = b0 % M, end = b1 % M;
+            while (a != end) {
+                uint32_t pv = (a + M - (skip % M)) % M;
+                uint32_t nx = (a + skip) % M;
+                path.Dr(path.GetR(*species, pr.second, pv), path.GetR(*species, pr.second, a), t);
+                for (uint32_t d = 0; d < n_d; ++d) tot[d] -= t[d];
+                path.Dr(path.GetR(*species, pr.second, a), path.GetR(*species, pr.second, nx), t);
+                for (uint32_t d = 0; d < n_d; ++d) tot[d] += t[d];
+                a = nx;
+            }
+        }
+        for (uint32_t d = 0; d < n_d; ++d) g[d] = 2. * i4 * tot[d];
+    }
+};
+
+// src/actions/single_action/trap_class.h:7-65
+struct Trap : SingleAction {
+    double omega, cofactor_a, cofactor_b;
+    Trap(Path& p, const Input& in) : SingleAction(p, in) {
+        omega = in.GetAttribute<double>("omega");
+        cofactor_a = 0.5 * p.tau * omega * omega * (1. + p.tau * p.tau * omega * omega / 12.);
+        cofactor_b = 0.5 * omega * omega * (1. + 3. * p.tau * p.tau * omega * omega / 12.);
+    }
+    double DActionDBeta() override {
+        double tot = 0.;
+        for (uint32_t p = 0; p < species->n_part; ++p)
+            for (uint32_t b = 0; b < species->n_bead; ++b) {
+                const double* r = path.GetR(*species, p, b);
+                for (uint32_t d = 0; d < path.n_d; ++d) tot += r[d] * r[d];
+            }
+        return cofactor_b * tot;
+    }
+    double GetAction(uint32_t b0, uint32_t b1, const Particles& parts, uint32_t level) override {
+        if (level > max_level) return 0.;
+        bool check = false;
+        for (auto& pr : parts)
+            if (pr.first == species->s_i) check = true;
+        if (!check) return 0.;
+        uint32_t skip = 1u << level;
+        double tot = 0.;
+        for (auto& pr : parts)
+            for (uint32_t b = b0; b < b1; b += skip) {
+                const double* r = path.GetR(*species, pr.second, b);
+                for (uint32_t d = 0; d < path.n_d; ++d) tot += r[d] * r[d];
+            }
+        return cofactor_a * skip * tot;
+    }
+};
+
+// src/actions/pair_action/pair_action_class.h:12-420
+struct PairAction : Action {
+    bool is_constant, is_first_time = true, use_long_range;
+    double dUdB_constant = 0., k_cut = 0., potential_constant = 0.;
+    Species *species_a, *species_b;
+
+    PairAction(Path& p, const Input& in) : Action(p, in) {
+        species_a = &p.GetSpecies(in.GetAttribute<std::string>("species_a"));
+        species_list.push_back(species_a->s_i);
+        species_b = &p.GetSpecies(in.GetAttribute<std::string>("species_b"));
+        species_list.push_back(species_b->s_i);
+        use_long_range = in.GetAttribute<bool>("use_long_range", false);
+        if (use_long_range) {
+            if (!p.pbc) throw InputError("use_long_range needs periodic boundaries");
+            k_cut = in.GetAttribute<double>("k_cut", p.ks.cutoff);
+            p.ks.Setup(k_cut);
+        }
+        is_constant = (species_a == species_b) && (species_a->n_part == 1 || species_a->lambda == 0.);
+    }
+
+    virtual double CalcV(double r, double rp, uint32_t level) = 0;
+    virtual double CalcVLong() = 0;
+    virtual double CalcU(double r, double rp, double s, uint32_t level) = 0;
+    virtual double CalcULong(uint32_t b0, uint32_t b1, uint32_t level) = 0;
+    virtual double CalcdUdBeta(double r, double rp, double s, uint32_t level) = 0;
+    virtual double CalcdUdBetaLong() = 0;
+
+    static void SetLimits(double rmin, double rmax, double& r, double& rp) {
+        if (r > rmax) r = rmax;
+        else if (r < rmin) r = rmin;
+        if (rp > rmax) rp = rmax;
+        else if (rp < rmin) rp = rmin;
+    }
+
+    // pair_action_class.h:45-59
+    std::vector<std::pair<uint32_t, uint32_t>> AllPairs() const {
+        std::vector<std::pair<uint32_t, uint32_t>> pp;
+        if (species_a == species_b) {
+            for (uint32_t p = 0; p + 1 < species_a->n_part; ++p)
+                for (uint32_t q = p + 1; q < species_b->n_part; ++q) pp.push_back({p, q});
+        } else {
+            for (uint32_t p = 0; p < species_a->n_part; ++p)
+                for (uint32_t q = 0; q < species_b->n_part; ++q) pp.push_back({p, q});
+        }
+        return pp;
+    }
+
+    // pair_action_class.h:62-114
+    void GenPairs(const Particles& parts, std::vector<uint32_t>& pa, std::vector<uint32_t>& pb, std::vector<std::pair<uint32_t, uint32_t>>& pp) {
+        for (auto& pr : parts) {
+            if (pr.first == species_a->s_i) pa.push_back(pr.second);
+            else if (pr.first == species_b->s_i) pb.push_back(pr.second);
+        }
+        uint32_t n_a = (uint32_t)pa.size(), n_b = (uint32_t)pb.size();
+        if (n_a == 0 && n_b == 0) return;
+        std::vector<uint32_t> oa, ob;
+        for (uint32_t i = 0; i < species_a->n_part; ++i)
+            if (std::find(pa.begin(), pa.end(), i) == pa.end()) oa.push_back(i);
+        for (uint32_t i = 0; i < species_b->n_part; ++i)
+            if (std::find(pb.begin(), pb.end(), i) == pb.end()) ob.push_back(i);
+        if (species_a == species_b) {
+            for (auto p : pa)
+                for (auto q : oa) pp.push_back({p, q});
+            for (uint32_t p = 0; p + 1 < n_a; ++p)
+                for (uint32_t q = p + 1; q < n_a; ++q) pp.push_back({pa[p], pa[q]});
+        } else {
+            for (auto p : pa)
+                for (auto q : ob) pp.push_back({p, q});
+            for (auto p : pb)
+                for (auto q : oa) pp.push_back({q, p});
+            for (auto p : pa)
+                for (auto q : pb) pp.push_back({p, q});
+        }
+    }
+
+    // pair_action_class.h:135-155 (central differences, eps = 1e-4)
+    void CalcGradientU(uint32_t bi, uint32_t bj, uint32_t pi, uint32_t pj, uint32_t level, double* tot) {
+        double* rr = path.GetR(*species_a, pi, bi);
+        double r0[3];
+        for (uint32_t d = 0; d < path.n_d; ++d) r0[d] = rr[d];
+        const double eps = 1.e-4;
+        double a, b, c;
+        for (uint32_t d = 0; d < path.n_d; ++d) {
+            rr[d] = r0[d] + eps;
+            path.DrDrpDrrp(bi, bj, *species_a, *species_b, pi, pj, a, b, c);
+            double f1 = CalcU(a, b, c, level);
+            rr[d] = r0[d] - eps;
+            path.DrDrpDrrp(bi, bj, *species_a, *species_b, pi, pj, a, b, c);
+            double f2 = CalcU(a, b, c, level);
+            tot[d] = (f1 - f2) / (2. * eps);
+            rr[d] = r0[d];
+        }
+    }
+    virtual void CalcGradientULong(uint32_t, uint32_t, uint32_t, uint32_t, double* g) {
+        for (uint32_t d = 0; d < path.n_d; ++d) g[d] = 0.;
+    }
+
+    // pair_action_class.h:241-264
+    double DActionDBeta() override {
+        if (is_constant && !is_first_time) return dUdB_constant;
+        double tot = 0.;
+        auto pp = AllPairs();
+        for (size_t i = 0; i < pp.size(); ++i)
+            for (uint32_t b = 0; b < species_a->n_bead; ++b) {
+                double a, bb, c;
+                path.DrDrpDrrp(b, b + 1, *species_a, *species_b, pp[i].first, pp[i].second, a, bb, c);
+                tot += CalcdUdBeta(a, bb, c, 0);
+            }
+        if (use_long_range) tot += CalcdUdBetaLong();
+        if (is_first_time) {
+            is_first_time = false;
+            dUdB_constant = tot;
+        }
+        return tot;
+    }
+
+    // pair_action_class.h:267-302
+    double GetAction(uint32_t b0, uint32_t b1, const Particles& parts, uint32_t level) override {
+        if (level > max_level || is_constant) return 0.;
+        std::vector<uint32_t> pa, pb;
+        std::vector<std::pair<uint32_t, uint32_t>> pp;
+        GenPairs(parts, pa, pb, pp);
+        if (pp.empty()) return 0.;
+        uint32_t skip = 1u << level;
+        double tot = 0.;
+        for (uint32_t b = b0; b < b1; b += skip) {
+            uint32_t bj = b + skip;
+            for (auto& pr : pp) {
+                double a, bb, c;
+                path.DrDrpDrrp(b, bj, *species_a, *species_b, pr.first, pr.second, a, bb, c);
+                tot += CalcU(a, bb, c, level);
+            }
+        }
+        if (use_long_range) {
+            if (species_a->need_update_rho_k && path.mode == NEW_MODE) path.UpdateRhoK(*species_a, b0, b1, pa, level);
+            if (species_b->need_update_rho_k && path.mode == NEW_MODE) path.UpdateRhoK(*species_b, b0, b1, pb, level);
+            tot += CalcULong(b0, b1, level);
+        }
+        return tot;
+    }
+
+    // pair_action_class.h:305-337
+    void GetActionGradient(uint32_t b0, uint32_t b1, const Particles& parts, uint32_t level, double* g) override {
+        for (uint32_t d = 0; d < path.n_d; ++d) g[d] = 0.;
+        if (level > max_level || is_constant) return;
+        std::vector<uint32_t> pa, pb;
+        std::vector<std::pair<uint32_t, uint32_t>> pp;
+        GenPairs(parts, pa, pb, pp);
+        if (pp.empty()) return;
+        uint32_t skip = 1u << level;
+        double t[3];
+        for (uint32_t b = b0; b < b1; b += skip) {
+            uint32_t bj = b + skip;
+            uint32_t bk = b - skip + species_a->n_bead;
+            for (auto& pr : pp) {
+                CalcGradientU(b, bj, pr.first, pr.second, level, t);
+                for (uint32_t d = 0; d < path.n_d; ++d) g[d] += t[d];
+                CalcGradientU(b, bk, pr.first, pr.second, level, t);
+                for (uint32_t d = 0; d < path.n_d; ++d) g[d] += t[d];
+            }
+        }
+        if (use_long_range) {
+            for (auto& pr : pp) {
+                CalcGradientULong(b0, b1, pr.first, level, t);
+                for (uint32_t d = 0; d < path.n_d; ++d) g[d] += t[d];
+            }
+        }
+    }
+
+    // pair_action_class.h:369-395
+    double Potential() override {
+        if (is_constant && !is_first_time) return potential_constant;
+        double tot = 0.;
+        auto pp = AllPairs();
+        double dr[3];
+        for (size_t i = 0; i < pp.size(); ++i)
+            for (uint32_t b = 0; b < species_a->n_bead; ++b) {
+                path.Dr(path.GetR(*species_a, pp[i].first, b), path.GetR(*species_b, pp[i].second, b), dr);
+                double rm = 0.;
+                for (uint32_t d = 0; d < path.n_d; ++d) rm += dr[d] * dr[d];
+                rm = std::sqrt(rm);
+                path.Dr(path.GetR(*species_a, pp[i].first, b + 1), path.GetR(*species_b, pp[i].second, b + 1), dr);
+                double rpm = 0.;
+                for (uint32_t d = 0; d < path.n_d; ++d) rpm += dr[d] * dr[d];
+                rpm = std::sqrt(rpm);
+                tot += CalcV(rm, rpm, 0);
+            }
+        if (use_long_range) tot += CalcVLong();
+        if (is_first_time) {
+            is_first_time = false;
+            potential_constant = tot;
+        }
+        return tot;
+    }
+
+    void Accept() override {
+        if (use_long_range) {
+            species_a->need_update_rho_k = true;
+            species_b->need_update_rho_k = true;
+        }
+    }
+    void Reject() override { Accept(); }
+};
+
+static bool fequal(double a, double b, double tol) { return std::fabs(a - b) < tol; }
+
+// src/actions/pair_action/bare_pair_action_class.h:7-183
+struct BarePairAction : PairAction {
+    bool is_coulomb;
+    double r_v_min, r_v_max, r_v_long_min = 0., r_v_long_max = 0., v_long_k_0 = 0., v_long_r_0 = 0.;
+    Spline v_r_spline, v_long_r_spline;
+    std::vector<double> v_long_k;
+
+    BarePairAction(Path& p, const Input& in, const std::string& base_dir) : PairAction(p, in) {
+        std::string file = in.GetAttribute<std::string>("file");
+        if (!file.empty() && file[0] != '/' && !base_dir.empty()) file = base_dir + "/" + file;
+        TableFile t = TableFile::Load(file);
+        is_coulomb = in.GetAttribute<bool>("is_coulomb", false);
+        const auto& r = t.Vec("v/diag/r");
+        const auto& v = t.Vec("v/diag/v_r");
+        if ((size_t)t.Scalar("v/diag/n_r") != r.size() || r.size() != v.size() || r.size() < 2)
+            throw InputError("table '" + file + "': inconsistent v/diag grid");
+        v_r_spline.Build(r, v, false);
+        r_v_min = r.front();
+        r_v_max = r.back();
+        if (use_long_range) {
+            const auto& rl = t.Vec("v/diag/r_long");
+            const auto& vl = t.Vec("v/diag/v_long_r");
+            v_long_r_0 = t.Scalar("v/diag/v_long_r_0");
+            v_long_r_spline.Build(rl, vl, false);
+            r_v_long_min = rl.front();
+            r_v_long_max = rl.back();
+            const auto& kv = t.Vec("v/diag/k");
+            const auto& vk = t.Vec("v/diag/v_long_k");
+            v_long_k_0 = t.Scalar("v/diag/v_long_k_0");
+            v_long_k.assign(p.ks.K(), 0.);
+            for (size_t k = 0; k < p.ks.K(); ++k)
+                for (size_t j = 0; j < kv.size(); ++j)
+                    if (fequal(p.ks.mags[k], kv[j], 1.e-8)) v_long_k[k] = vk[j];
+        }
+        if (species_a == species_b) {
+            v_long_k_0 *= 0.5 * species_a->n_part * species_b->n_part * p.n_bead;
+            v_long_r_0 *= -0.5 * species_a->n_part * p.n_bead;
+        } else {
+            v_long_k_0 *= species_a->n_part * species_b->n_part * p.n_bead;
+            v_long_r_0 *= 0.;
+        }
+    }
+
+    double CalcV(double r, double rp, uint32_t) override {
+        SetLimits(r_v_min, r_v_max, r, rp);
+        double v = 0.;
+        if (is_coulomb) v += (0.5 / r) + (0.5 / rp);
+        else v += 0.5 * v_r_spline.Eval(r) + 0.5 * v_r_spline.Eval(rp);
+        if (use_long_range) {
+            SetLimits(r_v_long_min, r_v_long_max, r, rp);
+            v -= 0.5 * v_long_r_spline.Eval(r);
+            v -= 0.5 * v_long_r_spline.Eval(rp);
+        }
+        return v;
+    }
+
+    double CalcVLong() override {
+        const auto& ra = path.GetRhoK(*species_a);
+        const auto& rb = path.GetRhoK(*species_b);
+        size_t K = path.ks.K();
+        double tot = 0.;
+        for (size_t k = 0; k < K; ++k)
+            for (uint32_t b = 0; b < path.n_bead; ++b) tot += CMag2(ra[(size_t)b * K + k], rb[(size_t)b * K + k]) * v_long_k[k];
+        if (species_a != species_b) tot *= 2.;
+        return tot + v_long_k_0 + v_long_r_0;
+    }
+
+    double CalcU(double r, double rp, double, uint32_t level) override {
+        uint32_t skip = 1u >> level;  // bare_pair_action_class.h:147 (sic)
+        double level_tau = skip * path.tau;
+        return level_tau * CalcV(r, rp, level);
+    }
+
+    double CalcULong(uint32_t b0, uint32_t b1, uint32_t level) override {
+        const auto& ra = path.GetRhoK(*species_a);
+        const auto& rb = path.GetRhoK(*species_b);
+        size_t K = path.ks.K();
+        uint32_t skip = 1u << level;
+        double tot = 0.;
+        for (size_t k = 0; k < K; ++k)
+            for (uint32_t b = b0; b < b1; b += skip)
+                tot += v_long_k[k] * CMag2(ra[(size_t)species_a->bead_loop(b) * K + k], rb[(size_t)species_b->bead_loop(b) * K + k]);
+        if (species_a != species_b) tot *= 2.;
+        return skip * path.tau * tot;
+    }
+
+    double CalcdUdBeta(double r, double rp, double, uint32_t level) override { return CalcV(r, rp, level); }
+    double CalcdUdBetaLong() override { return CalcVLong(); }
+};
+
+// ---------------------------------------------------------------------------------------------
+// Moves: Bisect (src/events/moves/single_species_move/bisect/bisect_class.h:8-214).
+struct Move {
+    std::string name, type;
+    uint64_t n_accept = 0, n_attempt = 0;
+    uint64_t attempt_counter = 0;
+    virtual ~Move() {}
+    virtual bool Attempt() = 0;
+    virtual void Accept() = 0;
+    virtual void Reject() = 0;
+    virtual void ResetBlock() {}
+    void DoEvent() {
+        n_attempt++;
+        if (Attempt()) {
+            n_accept++;
+            Accept();
+        } else
+            Reject();
+        attempt_counter++;
+    }
+};
+
+struct Bisect : Move {
+    Path& path;
+    Species* species;
+    std::vector<Action*> action_list;
+    uint32_t n_level, n_bisect_beads, bead0 = 0, bead1 = 0, move_index, seed, chain;
+    int n_images;
+    bool adaptive;
+    double target_ratio = 0., i_4_lambda_tau;
+    bool first_block = true;
+    std::vector<FreeSpline> rho_free_splines;
+    std::vector<std::pair<uint32_t, uint32_t>> affected;  // (particle, bead) in species
+
+    Bisect(Path& p, std::vector<std::unique_ptr<Action>>& actions, const Input& in, uint32_t idx, uint32_t sd, uint32_t ch)
+        : path(p), move_index(idx), seed(sd), chain(ch) {
+        name = in.GetAttribute<std::string>("name");
+        type = in.GetAttribute<std::string>("type");
+        species = &p.GetSpecies(in.GetAttribute<std::string>("species"));
+        i_4_lambda_tau = 1. / (4. * species->lambda * p.tau);
+        for (auto& a : actions)  // move_class.h:27-31
+            if (std::find(a->species_list.begin(), a->species_list.end(), species->s_i) != a->species_list.end())
+                action_list.push_back(a.get());
+        n_level = in.GetAttribute<uint32_t>("n_level");
+        n_images = in.GetAttribute<int>("n_images", 0);
+        adaptive = in.GetAttribute<bool>("adaptive", false);
+        if (adaptive) target_ratio = in.GetAttribute<double>("target_ratio");
+        n_bisect_beads = 1u << n_level;
+        if (n_bisect_beads > species->n_bead) throw InputError("bisection segment longer than the path");
+        uint32_t n_spline = (uint32_t)std::floor(std::log2((double)species->n_bead));
+        for (uint32_t i = 0; i < n_spline; ++i)
+            rho_free_splines.emplace_back(p.L, n_images, species->lambda, 0.5 * p.tau * (1u << i), false);
+    }
+
+    // bisect_class.h:142-155
+    void ResetBlock() override {
+        if (!first_block && adaptive && n_attempt > 0) {
+            double ratio = (double)n_accept / (double)n_attempt;
+            if (ratio < target_ratio && n_level > 1) n_level--;
+            else if ((1u << n_level) < species->n_bead / 2) n_level++;
+            n_bisect_beads = 1u << n_level;
+        }
+        first_block = false;
+        n_accept = 0;
+        n_attempt = 0;
+    }
+
+    // bisect_class.h:39-124
+    bool Attempt() override {
+        Stream st{seed, chain, move_index, attempt_counter};
+        RNG4 w0 = st.block(0);
+        uint32_t p_i = uidx(w0.w[0], species->n_part);
+        bead0 = uidx(w0.w[1], species->n_bead);
+        bead1 = bead0 + n_bisect_beads;
+        uint32_t M = species->n_bead, n_d = path.n_d;
+        affected.clear();
+        for (uint32_t i = 0; i <= n_bisect_beads; ++i) affected.push_back({p_i, (bead0 + i) % M});
+        Particles parts;
+        parts.push_back({species->s_i, p_i});
+
+        double prev_action_change = 0.;
+        uint32_t mid_counter = 0;
+        for (int level_i = (int)n_level - 1; level_i >= 0; --level_i) {
+            uint32_t skip = 1u << level_i;
+            double level_tau = path.tau * skip;
+            double sigma = std::sqrt(species->lambda * level_tau);
+            double old_lsp = 0., new_lsp = 0.;
+            for (uint32_t a = 0; a < n_bisect_beads; a += 2 * skip) {
+                uint32_t ba = (bead0 + a) % M, bb = (bead0 + a + skip) % M, bc = (bead0 + a + 2 * skip) % M;
+                double rbar[3], delta[3];
+                // Old sampling: RBar(c, a) = r_a + 0.5 Dr(c, a) in OLD mode (path_class.h:124)
+                {
+                    const double* ra = path.GetRMode(*species, p_i, ba, OLD_MODE);
+                    const double* rc = path.GetRMode(*species, p_i, bc, OLD_MODE);
+                    const double* rb = path.GetRMode(*species, p_i, bb, OLD_MODE);
+                    double t[3];
+                    path.Dr(rc, ra, t);
+                    for (uint32_t d = 0; d < n_d; ++d) rbar[d] = ra[d] + 0.5 * t[d];
+                    path.Dr(rb, rbar, delta);
+                    old_lsp += rho_free_splines[level_i].GetLogRhoFree(delta, n_d);
+                }
+                // New sampling
+                {
+                    double z[4];
+                    boxmuller(st.block(1u + 2u * mid_counter), z[0], z[1]);
+                    boxmuller(st.block(2u + 2u * mid_counter), z[2], z[3]);
+                    mid_counter++;
+                    for (uint32_t d = 0; d < n_d; ++d) delta[d] = 0. + sigma * z[d];
+                    path.PutInBox(delta);
+                    const double* ra = path.GetRMode(*species, p_i, ba, NEW_MODE);
+                    const double* rc = path.GetRMode(*species, p_i, bc, NEW_MODE);
+                    double t[3];
+                    path.Dr(rc, ra, t);
+                    for (uint32_t d = 0; d < n_d; ++d) rbar[d] = ra[d] + 0.5 * t[d];
+                    double* rb = path.GetRMode(*species, p_i, bb, NEW_MODE);
+                    for (uint32_t d = 0; d < n_d; ++d) rb[d] = rbar[d] + delta[d];
+                    new_lsp += rho_free_splines[level_i].GetLogRhoFree(delta, n_d);
+                }
+            }
+            double old_action = 0., new_action = 0.;
+            for (Action* a : action_list) {
+                path.mode = OLD_MODE;
+                old_action += a->GetAction(bead0, bead1, parts, (uint32_t)level_i);
+                path.mode = NEW_MODE;
+                new_action += a->GetAction(bead0, bead1, parts, (uint32_t)level_i);
+            }
+            double log_sample_ratio = -new_lsp + old_lsp;
+            double current = new_action - old_action;
+            double log_accept = log_sample_ratio - current + prev_action_change;
+            RNG4 wu = st.block(1u + 2u * (n_bisect_beads - 1u) + (n_level - 1u - (uint32_t)level_i));
+            double u = u53(wu.w[0], wu.w[1]);
+            if (log_accept < std::log(u)) return false;
+            prev_action_change = current;
+        }
+        return true;
+    }
+
+    // bisect_class.h:24-36
+    void Accept() override {
+        size_t K = path.ks.K();
+        for (auto& pb : affected) {
+            double* r = path.GetRMode(*species, pb.first, pb.second, NEW_MODE);
+            double* rc = path.GetRMode(*species, pb.first, pb.second, OLD_MODE);
+            std::copy(r, r + path.n_d, rc);
+            if (K) {
+                cplx* nw = path.BeadRhoK(*species, pb.first, pb.second, NEW_MODE);
+                cplx* od = path.BeadRhoK(*species, pb.first, pb.second, OLD_MODE);
+                std::copy(nw, nw + K, od);
+            }
+        }
+        if (K)
+            for (uint32_t b = bead0; b < bead1; ++b) {
+                uint32_t bb = species->bead_loop(b);
+                std::copy(species->rho_k.begin() + (size_t)bb * K, species->rho_k.begin() + (size_t)(bb + 1) * K, species->rho_k_c.begin() + (size_t)bb * K);
+            }
+        for (Action* a : action_list) a->Accept();
+    }
+
+    // bisect_class.h:127-139
+    void Reject() override {
+        size_t K = path.ks.K();
+        for (auto& pb : affected) {
+            double* r = path.GetRMode(*species, pb.first, pb.second, NEW_MODE);
+            double* rc = path.GetRMode(*species, pb.first, pb.second, OLD_MODE);
+            std::copy(rc, rc + path.n_d, r);
+            if (K) {
+                cplx* nw = path.BeadRhoK(*species, pb.first, pb.second, NEW_MODE);
+                cplx* od = path.BeadRhoK(*species, pb.first, pb.second, OLD_MODE);
+                std::copy(od, od + K, nw);
+            }
+        }
+        if (K)
+            for (uint32_t b = bead0; b < bead1; ++b) {
+                uint32_t bb = species->bead_loop(b);
+                std::copy(species->rho_k_c.begin() + (size_t)bb * K, species->rho_k_c.begin() + (size_t)(bb + 1) * K, species->rho_k.begin() + (size_t)bb * K);
+            }
+        for (Action* a : action_list) a->Reject();
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
+// Observables (src/events/observables/*).
+struct Observable {
+    std::string name, type;
+    uint32_t n_measure = 0, skip = 1;
+    virtual ~Observable() {}
+    virtual void Accumulate() = 0;
+    virtual void Reset() = 0;
+    // Normalised block values in the order the reference writes them; returns count.
+    virtual std::vector<double> Block() = 0;
+};
+
+// energy_class.h:7-326 (thermal / virial; potentials optional; no per-sector split)
+struct Energy : Observable {
+    Path& path;
+    std::vector<std::unique_ptr<Action>>& actions;
+    bool measure_potential, use_thermal, use_virial;
+    uint32_t virial_window_size = 0;
+    std::vector<double> energies, potentials;
+
+    Energy(Path& p, std::vector<std::unique_ptr<Action>>& a, const Input& in) : path(p), actions(a) {
+        name = in.GetAttribute<std::string>("name");
+        type = in.GetAttribute<std::string>("type");
+        skip = in.GetAttribute<uint32_t>("skip", 1);
+        measure_potential = in.GetAttribute<bool>("measure_potential", false);
+        use_virial = in.GetAttribute<bool>("use_virial_estimator", false);
+        if (use_virial) {
+            virial_window_size = in.GetAttribute<uint32_t>("virial_window_size", p.n_bead);
+            use_thermal = in.GetAttribute<bool>("use_thermal_estimator", false);
+        } else
+            use_thermal = in.GetAttribute<bool>("use_thermal_estimator", true);
+        energies.assign(actions.size(), 0.);
+        potentials.assign(actions.size(), 0.);
+    }
+
+    double Thermal(double cof) {
+        double tot = 0.;
+        for (size_t i = 0; i < actions.size(); ++i) {
+            if (actions[i]->is_importance_weight) continue;
+            double e = actions[i]->DActionDBeta();
+            energies[i] += cof * e;
+            tot += e;
+        }
+        return tot;
+    }
+
+    // energy_class.h:36-116
+    double Virial(double cof) {
+        double ke = 0.;
+        for (auto& a : actions)
+            if (a->type == "Kinetic") ke += a->VirialEnergy(virial_window_size);
+        for (auto& s : path.species) {
+            if (!(s.lambda > 0.)) continue;
+            double centroid = 0.;
+            for (uint32_t p = 0; p < s.n_part; ++p) {
+                Particles parts{{s.s_i, p}};
+                for (uint32_t b = 0; b < path.n_bead; ++b) {
+                    double dr[3], g[3];
+                    path.Dr(path.GetR(s, p, b), path.GetR(s, p, 0), dr);
+                    for (size_t i = 0; i < actions.size(); ++i) {
+                        if (actions[i]->is_importance_weight || actions[i]->type == "Kinetic") continue;
+                        actions[i]->GetActionGradient(b, b + 1, parts, 0, g);
+                        for (uint32_t d = 0; d < path.n_d; ++d) centroid += g[d] * dr[d];
+                    }
+                }
+            }
+            ke += centroid / (2. * path.tau);
+            for (size_t i = 0; i < actions.size(); ++i)
+                if (actions[i]->type == "Kinetic")
+                    for (uint32_t sp : actions[i]->species_list)
+                        if (sp == s.s_i) energies[i] += cof * ke;
+        }
+        double ie = 0.;
+        for (size_t i = 0; i < actions.size(); ++i) {
+            if (actions[i]->is_importance_weight || actions[i]->type == "Kinetic") continue;
+            double e = actions[i]->DActionDBeta();
+            energies[i] += cof * e;
+            ie += e;
+        }
+        return ke + ie;
+    }
+
+    void Accumulate() override {
+        path.mode = NEW_MODE;
+        double cof = 1.;  // sign * importance weight (no fermions, no importance actions)
+        if (use_thermal) Thermal(cof);
+        else if (use_virial) Virial(cof);
+        if (measure_potential)
+            for (size_t i = 0; i < actions.size(); ++i)
+                if (!actions[i]->is_importance_weight) potentials[i] += cof * actions[i]->Potential();
+        n_measure++;
+    }
+    void Reset() override {
+        n_measure = 0;
+        std::fill(energies.begin(), energies.end(), 0.);
+        std::fill(potentials.begin(), potentials.end(), 0.);
+    }
+    // [total, per-action energies..., (v_total, per-action potentials...)] / (M * n_measure)
+    std::vector<double> Block() override {
+        std::vector<double> out;
+        if (n_measure == 0) return out;
+        double norm = (double)path.n_bead * n_measure;
+        double E = 0.;
+        std::vector<double> e(energies.size());
+        for (size_t i = 0; i < e.size(); ++i) {
+            e[i] = energies[i] / norm;
+            E += e[i];
+        }
+        out.push_back(E);
+        out.insert(out.end(), e.begin(), e.end());
+        if (measure_potential) {
+            double V = 0.;
+            std::vector<double> v(potentials.size());
+            for (size_t i = 0; i < v.size(); ++i) {
+                v[i] = potentials[i] / norm;
+                V += v[i];
+            }
+            out.push_back(V);
+            out.insert(out.end(), v.begin(), v.end());
+        }
+        Reset();
+        return out;
+    }
+};
+
+// pair_correlation_class.h:7-124
+struct PairCorrelation : Observable {
+    Path& path;
+    Species *sa, *sb;
+    std::vector<std::pair<uint32_t, uint32_t>> pairs;
+    double r_min, r_max, dr, d_ir;
+    uint32_t n_r;
+    std::vector<double> gr, rs;
+
+    PairCorrelation(Path& p, const Input& in) : path(p) {
+        name = in.GetAttribute<std::string>("name");
+        type = in.GetAttribute<std::string>("type");
+        skip = in.GetAttribute<uint32_t>("skip", 1);
+        sa = &p.GetSpecies(in.GetAttribute<std::string>("species_a"));
+        sb = &p.GetSpecies(in.GetAttribute<std::string>("species_b"));
+        if (sa == sb) {
+            for (uint32_t i = 0; i + 1 < sa->n_part; ++i)
+                for (uint32_t j = i + 1; j < sb->n_part; ++j) pairs.push_back({i, j});
+        } else {
+            for (uint32_t i = 0; i < sa->n_part; ++i)
+                for (uint32_t j = 0; j < sb->n_part; ++j) pairs.push_back({i, j});
+        }
+        r_min = in.GetAttribute<double>("r_min", 0.);
+        r_max = in.GetAttribute<double>("r_max", p.L / 2.);
+        n_r = in.GetAttribute<uint32_t>("n_r", 100);
+        if (n_r < 2) throw InputError("n_r must be at least 2");
+        dr = (r_max - r_min) / (n_r - 1.);  // observable_class.h:357-366
+        d_ir = 1. / dr;
+        rs.resize(n_r);
+        for (uint32_t i = 0; i < n_r; ++i) rs[i] = r_min + i * dr;
+        gr.assign(n_r, 0.);
+    }
+    // observable_class.h:384-390
+    uint32_t ReverseMap(double r) const { return (uint32_t)std::nearbyint((r - r_min) * d_ir - 0.5); }
+    void Accumulate() override {
+        path.mode = NEW_MODE;
+        double cof = 1.;
+        double t[3];
+        for (uint32_t b = 0; b < path.n_bead; ++b)
+            for (auto& pr : pairs) {
+                path.Dr(path.GetR(*sa, pr.first, b), path.GetR(*sb, pr.second, b), t);
+                double m = 0.;
+                for (uint32_t d = 0; d < path.n_d; ++d) m += t[d] * t[d];
+                uint32_t i = ReverseMap(std::sqrt(m));
+                if (i < n_r) gr[i] = gr[i] + 1. * cof;
+            }
+        n_measure++;
+    }
+    void Reset() override {
+        n_measure = 0;
+        std::fill(gr.begin(), gr.end(), 0.);
+    }
+    std::vector<double> Block() override {
+        std::vector<double> out;
+        if (n_measure == 0) return out;
+        double norm;
+        if (sa == sb) norm = 0.5 * n_measure * sa->n_part * (sb->n_part - 1) * path.n_bead / path.vol;
+        else norm = (double)n_measure * sa->n_part * sb->n_part * path.n_bead / path.vol;
+        out.resize(n_r);
+        for (uint32_t i = 0; i < n_r; ++i) {
+            double r1 = rs[i];
+            double r2 = (i < n_r - 1) ? rs[i + 1] : (2. * rs[i] - rs[i - 1]);
+            double bin_vol;
+            if (path.n_d == 3) bin_vol = 4. * M_PI / 3. * (r2 * r2 * r2 - r1 * r1 * r1);
+            else if (path.n_d == 2) bin_vol = M_PI * (r2 * r2 - r1 * r1);
+            else bin_vol = r2 - r1;
+            out[i] = gr[i] / (bin_vol * norm);
+        }
+        Reset();
+        return out;
+    }
+};
+
+// structure_factor_class.h:7-212
+struct StructureFactor : Observable {
+    Path& path;
+    Species *sa, *sb;
+    double k_cut;
+    std::vector<double> sk;
+
+    StructureFactor(Path& p, const Input& in) : path(p) {
+        name = in.GetAttribute<std::string>("name");
+        type = in.GetAttribute<std::string>("type");
+        skip = in.GetAttribute<uint32_t>("skip", 1);
+        sa = &p.GetSpecies(in.GetAttribute<std::string>("species_a"));
+        sb = &p.GetSpecies(in.GetAttribute<std::string>("species_b"));
+        if (!p.pbc) throw InputError("StructureFactor needs periodic boundaries");
+        k_cut = in.GetAttribute<double>("k_cut", p.ks.cutoff);
+        p.ks.Setup(k_cut);
+    }
+    void Init() { sk.assign(path.ks.K(), 0.); }
+    void Accumulate() override {
+        path.mode = NEW_MODE;
+        const auto& ra = path.GetRhoK(*sa);
+        const auto& rb = path.GetRhoK(*sb);
+        size_t K = path.ks.K();
+        for (size_t k = 0; k < K; ++k)
+            if (path.ks.mags[k] < k_cut)
+                for (uint32_t b = 0; b < path.n_bead; ++b) sk[k] += 1. * CMag2(ra[(size_t)b * K + k], rb[(size_t)b * K + k]);
+        n_measure++;
+    }
+    void Reset() override {
+        n_measure = 0;
+        std::fill(sk.begin(), sk.end(), 0.);
+    }
+    std::vector<double> Block() override {
+        std::vector<double> out;
+        if (n_measure == 0) return out;
+        double norm = (double)n_measure * path.n_bead * sa->n_part * sb->n_part;
+        out.resize(sk.size());
+        for (size_t k = 0; k < sk.size(); ++k) out[k] = sk[k] / norm;
+        Reset();
+        return out;
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
+// Simulation (src/framework/simulation_class.h:8-46) with the Loop/Write events (loop_class.h).
+struct LoopNode {
+    int kind = 0;  // 0 loop, 1 move, 2 observable, 3 write
+    uint32_t index = 0;
+    uint64_t n_steps = 1;
+    std::vector<LoopNode> children;
+};
+
+struct Simulation {
+    std::string base_dir;
+    uint32_t seed = 12345, chain = 0;
+    std::unique_ptr<Path> path;
+    std::vector<std::unique_ptr<Action>> actions;
+    std::vector<std::unique_ptr<Move>> moves;
+    std::vector<std::unique_ptr<Observable>> observables;
+    std::vector<uint64_t> obs_calls;
+    LoopNode main_loop;
+    std::vector<std::vector<std::vector<double>>> blocks;  // per observable, per block
+
+    Simulation(const Input& in, const std::string& bd, uint32_t chain_id) : base_dir(bd), chain(chain_id) {
+        Input rng = in.GetChild("RNG");
+        seed = rng.IsNull() ? (uint32_t)time(nullptr) : (uint32_t)rng.GetAttribute<int>("seed", (int)time(nullptr));
+        path.reset(new Path(in));
+        for (auto& a : in.GetChild("Actions").GetChildList("Action")) {
+            std::string t = a.GetAttribute<std::string>("type");
+            if (t == "Kinetic") actions.emplace_back(new Kinetic(*path, a));
+            else if (t == "HarmonicTrap") actions.emplace_back(new Trap(*path, a));
+            else if (t == "BarePairAction") actions.emplace_back(new BarePairAction(*path, a, base_dir));
+            else throw InputError("unsupported action type '" + t + "'");
+        }
+        uint32_t mi = 0;
+        for (auto& m : in.GetChild("Moves").GetChildList("Move")) {
+            std::string t = m.GetAttribute<std::string>("type");
+            if (t == "Bisect") moves.emplace_back(new Bisect(*path, actions, m, mi, seed, chain));
+            else throw InputError("unsupported move type '" + t + "'");
+            ++mi;
+        }
+        for (auto& o : in.GetChild("Observables").GetChildList("Observable")) {
+            std::string t = o.GetAttribute<std::string>("type");
+            if (t == "Energy") observables.emplace_back(new Energy(*path, actions, o));
+            else if (t == "PairCorrelation") observables.emplace_back(new PairCorrelation(*path, o));
+            else if (t == "StructureFactor") observables.emplace_back(new StructureFactor(*path, o));
+            else if (t == "Time" || t == "PathDump") continue;  // bookkeeping only
+            else throw InputError("unsupported observable type '" + t + "'");
+        }
+        obs_calls.assign(observables.size(), 0);
+        blocks.resize(observables.size());
+        // The reference sizes each long-range table at construction (bare_pair_action_class.h:79) and
+        // would read past it if a later element grew the k-vector set; refuse that input instead.
+        for (auto& a : actions)
+            if (a->type == "BarePairAction") {
+                auto* b = static_cast<BarePairAction*>(a.get());
+                if (b->use_long_range && b->v_long_k.size() != path->ks.K())
+                    throw InputError("k_cut of action '" + b->name + "' is below a later k_cut; order the largest first");
+            }
+        for (auto& o : observables)
+            if (o->type == "StructureFactor") static_cast<StructureFactor*>(o.get())->Init();
+        for (auto& s : path->species) path->InitRhoK(s);
+        Input alg = in.GetChild("Algorithm");
+        main_loop.kind = 0;
+        main_loop.n_steps = 1;
+        ReadLoop(alg, main_loop);
+    }
+
+    void ReadLoop(const Input& in, LoopNode& node) {
+        for (auto& c : in.GetChildList()) {
+            const std::string& t = c.GetName();
+            LoopNode ch;
+            if (t == "Move" || t == "Observable") {
+                std::string nm = c.GetAttribute<std::string>("name");
+                bool found = false;
+                if (t == "Move") {
+                    for (size_t i = 0; i < moves.size(); ++i)
+                        if (moves[i]->name == nm) {
+                            ch.kind = 1;
+                            ch.index = (uint32_t)i;
+                            found = true;
+                        }
+                } else {
+                    for (size_t i = 0; i < observables.size(); ++i)
+                        if (observables[i]->name == nm) {
+                            ch.kind = 2;
+                            ch.index = (uint32_t)i;
+                            found = true;
+                        }
+                }
+                if (!found) continue;  // loop_class.h:254-258 warns and skips
+            } else if (t == "Write") {
+                ch.kind = 3;
+            } else if (t == "Loop") {
+                ch.kind = 0;
+                ch.n_steps = (uint64_t)c.GetAttribute<int>("n_step");
+                ReadLoop(c, ch);
+            } else
+                continue;
+            node.children.push_back(ch);
+        }
+    }
+
+    void Write() {
+        for (size_t i = 0; i < observables.size(); ++i) {
+            auto v = observables[i]->Block();
+            if (!v.empty()) blocks[i].push_back(v);
+        }
+        for (auto& m : moves) m->ResetBlock();
+    }
+
+    void RunNode(const LoopNode& n) {
+        for (uint64_t s = 0; s < n.n_steps; ++s)
+            for (auto& c : n.children) {
+                if (c.kind == 0) RunNode(c);
+                else if (c.kind == 1) moves[c.index]->DoEvent();
+                else if (c.kind == 2)
+                    observables[c.index]->Accumulate();  // observable_class.h:421-429 ignores `skip`
+                else
+                    Write();
+            }
+    }
+};
+
+}  // namespace orc
+
+// =============================================================================================
+// C interface used by the tests (ctypes) and by the bench's CPU-baseline leg.
+namespace {
+thread_local std::string g_err;
+int fail(const std::exception& e) {
+    g_err = e.what();
+    return -1;
+}
+orc::Simulation* S(void* h) { return static_cast<orc::Simulation*>(h); }
+orc::Particles parts_of(const uint32_t* sp, const uint32_t* p, uint32_t n) {
+    orc::Particles out;
+    for (uint32_t i = 0; i < n; ++i) out.push_back({sp[i], p[i]});
+    return out;
+}
+}  // namespace
+
+extern "C" {
+
+const char* oracle_last_error() { return g_err.c_str(); }
+
+int oracle_create(const char* xml_text, const char* base_dir, uint32_t chain, void** out) {
+    try {
+        pimc::Input in = pimc::Input::FromString(xml_text);
+        *out = new orc::Simulation(in, base_dir ? base_dir : "", chain);
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+}
+
+void oracle_destroy(void* h) { delete S(h); }
+
+// [n_d, n_bead, n_species, n_total, K, n_actions, n_moves, n_observables]
+int oracle_info(void* h, uint32_t* out) {
+    auto* s = S(h);
+    out[0] = s->path->n_d;
+    out[1] = s->path->n_bead;
+    out[2] = (uint32_t)s->path->species.size();
+    out[3] = s->path->n_total;
+    out[4] = (uint32_t)s->path->ks.K();
+    out[5] = (uint32_t)s->actions.size();
+    out[6] = (uint32_t)s->moves.size();
+    out[7] = (uint32_t)s->observables.size();
+    return 0;
+}
+
+int oracle_seed(void* h, uint32_t seed) {
+    auto* s = S(h);
+    s->seed = seed;
+    for (auto& m : s->moves) static_cast<orc::Bisect*>(m.get())->seed = seed;
+    return 0;
+}
+
+// which: 0 = old copy, 1 = new copy, 2 = both (then charge densities are re-initialised).
+int oracle_set_path(void* h, int which, const double* pos) {
+    auto* s = S(h);
+    size_t n = s->path->r.size();
+    if (which == 1 || which == 2) std::copy(pos, pos + n, s->path->r.begin());
+    if (which == 0 || which == 2) std::copy(pos, pos + n, s->path->r_c.begin());
+    if (which == 2)
+        for (auto& sp : s->path->species) sp.need_update_rho_k = true;
+    if (which == 2)
+        for (auto& sp : s->path->species) s->path->InitRhoK(sp);
+    return 0;
+}
+
+int oracle_get_path(void* h, int which, double* pos) {
+    auto* s = S(h);
+    const auto& v = which == 0 ? s->path->r_c : s->path->r;
+    std::copy(v.begin(), v.end(), pos);
+    return 0;
+}
+
+int oracle_kvecs(void* h, double* out) {
+    auto* s = S(h);
+    for (size_t k = 0; k < s->path->ks.K(); ++k)
+        for (uint32_t d = 0; d < s->path->n_d; ++d) out[k * s->path->n_d + d] = s->path->ks.vecs[k][d];
+    return 0;
+}
+
+int oracle_get_rho_k(void* h, uint32_t species, int which, double* out) {
+    auto* s = S(h);
+    const auto& sp = s->path->species.at(species);
+    const auto& v = which == 0 ? sp.rho_k_c : sp.rho_k;
+    for (size_t i = 0; i < v.size(); ++i) {
+        out[2 * i] = v[i].real();
+        out[2 * i + 1] = v[i].imag();
+    }
+    return 0;
+}
+
+int oracle_get_action(void* h, uint32_t a, uint32_t b0, uint32_t b1, const uint32_t* sp, const uint32_t* p, uint32_t n, uint32_t level,
+                      int mode, double* out) {
+    try {
+        auto* s = S(h);
+        s->path->mode = mode ? orc::NEW_MODE : orc::OLD_MODE;
+        *out = s->actions.at(a)->GetAction(b0, b1, parts_of(sp, p, n), level);
+        s->path->mode = orc::NEW_MODE;
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+}
+
+int oracle_get_action_gradient(void* h, uint32_t a, uint32_t b0, uint32_t b1, const uint32_t* sp, const uint32_t* p, uint32_t n,
+                               uint32_t level, int mode, double* out) {
+    try {
+        auto* s = S(h);
+        s->path->mode = mode ? orc::NEW_MODE : orc::OLD_MODE;
+        s->actions.at(a)->GetActionGradient(b0, b1, parts_of(sp, p, n), level, out);
+        s->path->mode = orc::NEW_MODE;
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+}
+
+// Mark every species' charge density as needing an update (the state after Accept/Reject).
+int oracle_reset_rho_k_latch(void* h) {
+    for (auto& sp : S(h)->path->species) sp.need_update_rho_k = true;
+    return 0;
+}
+
+int oracle_dactiondbeta(void* h, uint32_t a, double* out) {
+    auto* s = S(h);
+    s->path->mode = orc::NEW_MODE;
+    *out = s->actions.at(a)->DActionDBeta();
+    return 0;
+}
+
+int oracle_potential(void* h, uint32_t a, double* out) {
+    auto* s = S(h);
+    s->path->mode = orc::NEW_MODE;
+    *out = s->actions.at(a)->Potential();
+    return 0;
+}
+
+int oracle_virial_energy(void* h, uint32_t a, double window, double* out) {
+    auto* s = S(h);
+    s->path->mode = orc::NEW_MODE;
+    *out = s->actions.at(a)->VirialEnergy(window);
+    return 0;
+}
+
+int oracle_move_attempts(void* h, uint32_t m, uint64_t n) {
+    auto* s = S(h);
+    for (uint64_t i = 0; i < n; ++i) s->moves.at(m)->DoEvent();
+    return 0;
+}
+
+int oracle_move_stats(void* h, uint32_t m, uint64_t* out) {
+    // {total attempts, attempts in the current block, accepts in the current block}
+    auto* mv = S(h)->moves.at(m).get();
+    out[0] = mv->attempt_counter;
+    out[1] = mv->n_attempt;
+    out[2] = mv->n_accept;
+    return 0;
+}
+
+int oracle_obs_accumulate(void* h, uint32_t o) {
+    S(h)->observables.at(o)->Accumulate();
+    return 0;
+}
+
+// Normalised block of observable o (the values its Write() would append); resets it.
+int oracle_obs_block(void* h, uint32_t o, double* out, uint64_t cap, uint64_t* n) {
+    auto v = S(h)->observables.at(o)->Block();
+    *n = v.size();
+    for (size_t i = 0; i < v.size() && i < cap; ++i) out[i] = v[i];
+    return 0;
+}
+
+// Runs the input's Algorithm loop; block values are collected per observable.
+int oracle_run(void* h) {
+    try {
+        auto* s = S(h);
+        s->RunNode(s->main_loop);
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+}
+
+int oracle_n_blocks(void* h, uint32_t o, uint64_t* n) {
+    *n = S(h)->blocks.at(o).size();
+    return 0;
+}
+
+int oracle_get_block(void* h, uint32_t o, uint64_t blk, double* out, uint64_t cap, uint64_t* n) {
+    const auto& v = S(h)->blocks.at(o).at(blk);
+    *n = v.size();
+    for (size_t i = 0; i < v.size() && i < cap; ++i) out[i] = v[i];
+    return 0;
+}
+
+int oracle_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {
+    uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
+    orc::RNG4 r = orc::philox(c, key[0], key[1]);
+    for (int i = 0; i < 4; ++i) out[i] = r.w[i];
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,272 @@
+"""simpimc_gb300: GB300 (sm_103a) path-integral Monte Carlo action/estimator library.
+
+Python binding of the C interface in include/simpimc_gb300.h (ctypes, no torch types). The
+`Simulation` class mirrors the reference's Simulation/Action/Move/Observable surface:
+``get_action`` is Action::GetAction, ``dactiondbeta`` is Action::DActionDBeta, ``move_attempts``
+is Move::DoEvent repeated, ``observable_block`` is Observable::Write, ``run`` is Simulation::Run.
+
+There is no CPU fallback: if the CUDA library has not been built, importing the binding's
+library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+__all__ = ["Simulation", "PimcError", "load_library", "LIB_PATH"]
+
+LIB_PATH = Path(__file__).resolve().parent / "lib" / "libsimpimc_gb300.so"
+
+_ERRORS = {
+    -1: "PIMC_ERR_ARG",
+    -2: "PIMC_ERR_INPUT",
+    -3: "PIMC_ERR_CUDA",
+    -4: "PIMC_ERR_TIMEOUT",
+    -5: "PIMC_ERR_NONFINITE",
+    -6: "PIMC_ERR_UNSUPPORTED",
+    -7: "PIMC_ERR_STATE",
+}
+
+
+class PimcError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class _Info(C.Structure):
+    _fields_ = [("n_d", C.c_uint32), ("n_bead", C.c_uint32), ("n_species", C.c_uint32), ("n_total", C.c_uint32),
+                ("n_k", C.c_uint32), ("n_actions", C.c_uint32), ("n_moves", C.c_uint32), ("n_observables", C.c_uint32),
+                ("beta", C.c_double), ("tau", C.c_double), ("L", C.c_double), ("volume", C.c_double), ("pbc", C.c_int32)]
+
+
+# Exported symbols and argtypes (kept in step with include/simpimc_gb300.h).
+_P = C.c_void_p
+_U32P = C.POINTER(C.c_uint32)
+_U64P = C.POINTER(C.c_uint64)
+_DP = C.POINTER(C.c_double)
+_SZP = C.POINTER(C.c_size_t)
+SIGNATURES = {
+    "pimc_create": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_uint32, C.POINTER(_P)]),
+    "pimc_destroy": (None, [_P]),
+    "pimc_last_error": (C.c_char_p, [_P]),
+    "pimc_get_info": (C.c_int, [_P, C.POINTER(_Info)]),
+    "pimc_set_seed": (C.c_int, [_P, C.c_uint32]),
+    "pimc_get_name": (C.c_int, [_P, C.c_int, C.c_uint32, C.c_char_p, C.c_size_t]),
+    "pimc_species_info": (C.c_int, [_P, C.c_uint32, _U32P, _U32P, _DP]),
+    "pimc_set_path": (C.c_int, [_P, C.c_int, _DP]),
+    "pimc_get_path": (C.c_int, [_P, C.c_int, _DP]),
+    "pimc_get_rho_k": (C.c_int, [_P, C.c_uint32, _DP]),
+    "pimc_get_kvecs": (C.c_int, [_P, _DP]),
+    "pimc_get_action": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _U32P, _U32P, C.c_uint32, C.c_uint32, C.c_int, _DP]),
+    "pimc_get_action_gradient": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _U32P, _U32P, C.c_uint32, C.c_uint32, C.c_int, _DP]),
+    "pimc_dactiondbeta": (C.c_int, [_P, C.c_uint32, _DP]),
+    "pimc_potential": (C.c_int, [_P, C.c_uint32, _DP]),
+    "pimc_virial_energy": (C.c_int, [_P, C.c_uint32, C.c_double, _DP]),
+    "pimc_move_attempts": (C.c_int, [_P, C.c_uint32, C.c_uint64]),
+    "pimc_sweep": (C.c_int, [_P, _U32P, _U64P, C.c_uint32, C.c_uint64]),
+    "pimc_move_stats": (C.c_int, [_P, C.c_uint32, _U64P]),
+    "pimc_observable_accumulate": (C.c_int, [_P, C.c_uint32]),
+    "pimc_observable_block": (C.c_int, [_P, C.c_uint32, _DP, C.c_size_t, _SZP]),
+    "pimc_run": (C.c_int, [_P]),
+    "pimc_n_blocks": (C.c_int, [_P, C.c_uint32, _SZP]),
+    "pimc_get_block": (C.c_int, [_P, C.c_uint32, C.c_size_t, _DP, C.c_size_t, _SZP]),
+    "pimc_synchronize": (C.c_int, [_P]),
+    "pimc_set_sweep_grid": (C.c_int, [_P, C.c_int]),
+    "pimc_set_timeout_ns": (C.c_int, [_P, C.c_uint64]),
+    "pimc_stream": (_P, [_P]),
+}
+
+_lib = None
+
+
+def load_library(path: os.PathLike | None = None):
+    """Load the CUDA library (raises if it has not been built: there is no fallback)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"simpimc_gb300 CUDA library not built: {p} is missing (run __graft_entry__.build())")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_DP)
+
+
+class Simulation:
+    """One simulation on one GPU, built from a simpimc XML input."""
+
+    def __init__(self, xml: str, base_dir: str | os.PathLike = ".", device: int = 0, chain: int = 0):
+        self._lib = load_library()
+        h = _P()
+        rc = self._lib.pimc_create(xml.encode(), str(base_dir).encode(), device, chain, C.byref(h))
+        if rc != 0:
+            raise PimcError(rc, self._lib.pimc_last_error(None).decode())
+        self._h = h
+        info = _Info()
+        self._check(self._lib.pimc_get_info(self._h, C.byref(info)))
+        self.n_d, self.n_bead, self.n_species = info.n_d, info.n_bead, info.n_species
+        self.n_total, self.n_k = info.n_total, info.n_k
+        self.n_actions, self.n_moves, self.n_observables = info.n_actions, info.n_moves, info.n_observables
+        self.beta, self.tau, self.L, self.volume, self.pbc = info.beta, info.tau, info.L, info.volume, bool(info.pbc)
+
+    # -- plumbing -------------------------------------------------------------------------------
+    def _check(self, rc: int):
+        if rc != 0:
+            raise PimcError(rc, self._lib.pimc_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.pimc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def name(self, kind: int, index: int) -> str:
+        buf = C.create_string_buffer(256)
+        self._check(self._lib.pimc_get_name(self._h, kind, index, buf, 256))
+        return buf.value.decode()
+
+    def species_info(self, s: int):
+        n, off, lam = C.c_uint32(), C.c_uint32(), C.c_double()
+        self._check(self._lib.pimc_species_info(self._h, s, C.byref(n), C.byref(off), C.byref(lam)))
+        return n.value, off.value, lam.value
+
+    def set_seed(self, seed: int):
+        self._check(self._lib.pimc_set_seed(self._h, seed))
+
+    def set_sweep_grid(self, grid: int):
+        self._check(self._lib.pimc_set_sweep_grid(self._h, grid))
+
+    def set_timeout_ns(self, ns: int):
+        self._check(self._lib.pimc_set_timeout_ns(self._h, ns))
+
+    def synchronize(self):
+        self._check(self._lib.pimc_synchronize(self._h))
+
+    # -- path -----------------------------------------------------------------------------------
+    @property
+    def path_shape(self):
+        return (self.n_total, self.n_bead, self.n_d)
+
+    def set_path(self, pos: np.ndarray, which: int = 2):
+        a = np.ascontiguousarray(pos, dtype=np.float64)
+        if a.shape != self.path_shape:
+            raise ValueError(f"path must have shape {self.path_shape}, got {a.shape}")
+        self._check(self._lib.pimc_set_path(self._h, which, _dp(a)))
+
+    def get_path(self, which: int = 1) -> np.ndarray:
+        a = np.empty(self.path_shape, dtype=np.float64)
+        self._check(self._lib.pimc_get_path(self._h, which, _dp(a)))
+        return a
+
+    def rho_k(self, species: int) -> np.ndarray:
+        a = np.empty((self.n_bead, self.n_k, 2), dtype=np.float64)
+        self._check(self._lib.pimc_get_rho_k(self._h, species, _dp(a)))
+        return a[..., 0] + 1j * a[..., 1]
+
+    def kvecs(self) -> np.ndarray:
+        a = np.empty((self.n_k, self.n_d), dtype=np.float64)
+        if self.n_k:
+            self._check(self._lib.pimc_get_kvecs(self._h, _dp(a)))
+        return a
+
+    # -- actions --------------------------------------------------------------------------------
+    @staticmethod
+    def _parts(particles):
+        sp = np.array([p[0] for p in particles], dtype=np.uint32)
+        pi = np.array([p[1] for p in particles], dtype=np.uint32)
+        return sp, pi
+
+    def get_action(self, action: int, b0: int, b1: int, particles, level: int = 0, mode: int = 1) -> float:
+        sp, pi = self._parts(particles)
+        out = C.c_double()
+        self._check(self._lib.pimc_get_action(self._h, action, b0, b1, sp.ctypes.data_as(_U32P), pi.ctypes.data_as(_U32P),
+                                              len(sp), level, mode, C.byref(out)))
+        return out.value
+
+    def get_action_gradient(self, action: int, b0: int, b1: int, particles, level: int = 0, mode: int = 1) -> np.ndarray:
+        sp, pi = self._parts(particles)
+        out = np.zeros(self.n_d, dtype=np.float64)
+        self._check(self._lib.pimc_get_action_gradient(self._h, action, b0, b1, sp.ctypes.data_as(_U32P), pi.ctypes.data_as(_U32P),
+                                                       len(sp), level, mode, _dp(out)))
+        return out
+
+    def dactiondbeta(self, action: int) -> float:
+        out = C.c_double()
+        self._check(self._lib.pimc_dactiondbeta(self._h, action, C.byref(out)))
+        return out.value
+
+    def potential(self, action: int) -> float:
+        out = C.c_double()
+        self._check(self._lib.pimc_potential(self._h, action, C.byref(out)))
+        return out.value
+
+    def virial_energy(self, action: int, window: float) -> float:
+        out = C.c_double()
+        self._check(self._lib.pimc_virial_energy(self._h, action, float(window), C.byref(out)))
+        return out.value
+
+    # -- moves, observables, run ----------------------------------------------------------------
+    def move_attempts(self, move: int, n: int):
+        self._check(self._lib.pimc_move_attempts(self._h, move, n))
+
+    def sweep(self, moves, counts, n_rep: int = 1):
+        mv = np.ascontiguousarray(moves, dtype=np.uint32)
+        ct = np.ascontiguousarray(counts, dtype=np.uint64)
+        self._check(self._lib.pimc_sweep(self._h, mv.ctypes.data_as(_U32P), ct.ctypes.data_as(_U64P), len(mv), n_rep))
+
+    def move_stats(self, move: int):
+        """(total attempts, attempts in block, accepts in block)."""
+        return self.move_counters(move)[:3]
+
+    def move_counters(self, move: int):
+        """(total attempts, block attempts, block accepts, total accepts, total level-0 tests)."""
+        out = np.zeros(5, dtype=np.uint64)
+        self._check(self._lib.pimc_move_stats(self._h, move, out.ctypes.data_as(_U64P)))
+        return tuple(int(x) for x in out)
+
+    def observable_accumulate(self, obs: int):
+        self._check(self._lib.pimc_observable_accumulate(self._h, obs))
+
+    def observable_block(self, obs: int, cap: int = 1 << 20) -> np.ndarray:
+        out = np.zeros(cap, dtype=np.float64)
+        n = C.c_size_t()
+        self._check(self._lib.pimc_observable_block(self._h, obs, _dp(out), cap, C.byref(n)))
+        return out[: n.value].copy()
+
+    def run(self):
+        self._check(self._lib.pimc_run(self._h))
+
+    def blocks(self, obs: int, cap: int = 1 << 20) -> list[np.ndarray]:
+        n = C.c_size_t()
+        self._check(self._lib.pimc_n_blocks(self._h, obs, C.byref(n)))
+        out = []
+        buf = np.zeros(cap, dtype=np.float64)
+        for b in range(n.value):
+            m = C.c_size_t()
+            self._check(self._lib.pimc_get_block(self._h, obs, b, _dp(buf), cap, C.byref(m)))
+            out.append(buf[: m.value].copy())
+        return out

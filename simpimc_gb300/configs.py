@@ -1,0 +1,126 @@
+"""XML inputs, pair-action tables and seeded initial paths for the benchmark systems.
+
+Each builder returns ``(xml_text, initial_path)``; tables are written into ``workdir``. The
+systems follow the reference's input format (inputs/*.xml): <System>, <Particles>, <Actions>,
+<Moves>, <Observables>, <Algorithm>.
+
+* ``trapped_coulomb``: N distinguishable unit-mass particles in an isotropic 3-D harmonic trap
+  with bare Coulomb repulsion (primitive action tau*V), open boundaries; beads i.i.d. N(0, 1).
+* ``electron_gas``: N Boltzmannon electrons (half up, half down) in a periodic cube at density
+  r_s, Coulomb split into a short-range primitive part and an Ewald long-range k-sum; beads
+  uniform in the box.
+"""
+from __future__ import annotations
+
+import math
+from pathlib import Path
+
+import numpy as np
+
+from .tables import coulomb_table
+
+
+def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_level=3, seed=1234, coulomb=True,
+                    n_step_inner=100, n_step_outer=10, gr_bins=200, gr_rmax=5.0, virial=False, path_seed=None):
+    workdir = Path(workdir)
+    workdir.mkdir(parents=True, exist_ok=True)
+    tab = workdir / "coulomb_open.pat"
+    coulomb_table(tab, z_ab=1.0, L=0.0)
+    pair = (f'<Action name="Coulomb" type="BarePairAction" file="{tab.name}" is_coulomb="1" species_a="e" '
+            f'species_b="e" max_level="0" use_long_range="0" />') if coulomb else ""
+    energy = ('<Observable name="Energy" type="Energy" use_virial_estimator="1" />' if virial
+              else '<Observable name="Energy" type="Energy" />')
+    xml = f"""<Input>
+  <RNG seed="{seed}" />
+  <IO output_prefix="trap" />
+  <Parallel procs_per_group="1" />
+  <System n_d="3" n_bead="{n_bead}" beta="{beta}" pbc="0" />
+  <Particles>
+    <Species name="e" n_part="{n_part}" lambda="0.5" fermi="0" init_type="File" file_name="init.xyz" all_beads="1" />
+  </Particles>
+  <Actions>
+    <Action name="Kinetic" type="Kinetic" n_images="0" species="e" />
+    <Action name="Trap" type="HarmonicTrap" species="e" omega="{omega}" max_level="0" />
+    {pair}
+  </Actions>
+  <Moves>
+    <Move name="Bisect" type="Bisect" species="e" n_level="{n_level}" />
+  </Moves>
+  <Observables>
+    {energy}
+    <Observable name="gr" type="PairCorrelation" species_a="e" species_b="e" r_min="0." r_max="{gr_rmax}" n_r="{gr_bins}" />
+  </Observables>
+  <Algorithm>
+    <Loop n_step="{n_step_outer}">
+      <Loop n_step="{n_step_inner}">
+        <Move name="Bisect" />
+        <Observable name="Energy" />
+        <Observable name="gr" />
+      </Loop>
+      <Write />
+    </Loop>
+  </Algorithm>
+</Input>
+"""
+    rng = np.random.default_rng(seed if path_seed is None else path_seed)
+    path = rng.standard_normal((n_part, n_bead, 3))
+    return xml, path
+
+
+def electron_gas(workdir, *, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_units=12.0, n_level=4, seed=4321,
+                 n_step_inner=10, n_step_outer=4, path_seed=None, structure_factor=False):
+    workdir = Path(workdir)
+    workdir.mkdir(parents=True, exist_ok=True)
+    L = (4.0 * math.pi * n_part / 3.0) ** (1.0 / 3.0) * rs
+    k_cut = k_cut_units * 2.0 * math.pi / L
+    tab = workdir / f"coulomb_ewald_{n_part}_{rs}.pat"
+    coulomb_table(tab, z_ab=1.0, L=L, k_cut=k_cut)
+    n_up = n_part // 2
+    n_dn = n_part - n_up
+    sk = ('<Observable name="sk" type="StructureFactor" species_a="eU" species_b="eU" />' if structure_factor else "")
+    xml = f"""<Input>
+  <RNG seed="{seed}" />
+  <IO output_prefix="egas" />
+  <Parallel procs_per_group="1" />
+  <System n_d="3" n_bead="{n_bead}" beta="{beta}" L="{L!r}" pbc="1" k_cut="{k_cut!r}" />
+  <Particles>
+    <Species name="eU" n_part="{n_up}" lambda="0.5" fermi="0" init_type="File" file_name="init.xyz" all_beads="1" />
+    <Species name="eD" n_part="{n_dn}" lambda="0.5" fermi="0" init_type="File" file_name="init.xyz" all_beads="1" />
+  </Particles>
+  <Actions>
+    <Action name="KineticU" type="Kinetic" n_images="0" species="eU" />
+    <Action name="KineticD" type="Kinetic" n_images="0" species="eD" />
+    <Action name="CoulombUU" type="BarePairAction" file="{tab.name}" is_coulomb="1" species_a="eU" species_b="eU" max_level="0" use_long_range="1" />
+    <Action name="CoulombDD" type="BarePairAction" file="{tab.name}" is_coulomb="1" species_a="eD" species_b="eD" max_level="0" use_long_range="1" />
+    <Action name="CoulombUD" type="BarePairAction" file="{tab.name}" is_coulomb="1" species_a="eU" species_b="eD" max_level="0" use_long_range="1" />
+  </Actions>
+  <Moves>
+    <Move name="BisectU" type="Bisect" species="eU" n_level="{n_level}" />
+    <Move name="BisectD" type="Bisect" species="eD" n_level="{n_level}" />
+  </Moves>
+  <Observables>
+    <Observable name="Energy" type="Energy" />
+    <Observable name="gr" type="PairCorrelation" species_a="eU" species_b="eD" n_r="100" />
+    {sk}
+  </Observables>
+  <Algorithm>
+    <Loop n_step="{n_step_outer}">
+      <Loop n_step="{n_step_inner}">
+        <Move name="BisectU" />
+        <Move name="BisectD" />
+        <Observable name="Energy" />
+      </Loop>
+      <Write />
+    </Loop>
+  </Algorithm>
+</Input>
+"""
+    rng = np.random.default_rng(seed if path_seed is None else path_seed)
+    path = rng.uniform(-L / 2, L / 2, size=(n_part, n_bead, 3))
+    return xml, path
+
+
+def sweep_schedule(sim_or_counts, n_bisect_beads: int, n_bead: int):
+    """One sweep: N_s * ceil(M / 2^l) attempts of each species' bisection move, in move order."""
+    counts = [n * math.ceil(n_bead / n_bisect_beads) for n in sim_or_counts]
+    return list(range(len(counts))), counts

@@ -1,0 +1,181 @@
+// Host-side owner of one simulation on one GPU: the counterpart of the reference's Simulation
+// (src/framework/simulation_class.h:8-46), which owns the Path, the actions, the moves and the
+// observables. Here the path, tables and accumulators live in device memory and every
+// action/move/observable call launches a kernel on the context's stream.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../data_structures/system.h"
+#include "input.h"
+
+namespace pimc {
+
+struct PimcError : std::runtime_error {
+    int code;
+    PimcError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+// Status codes returned through the C interface (mirrored in include/simpimc_gb300.h).
+enum : int {
+    kOk = 0,
+    kErrArg = -1,
+    kErrInput = -2,
+    kErrCuda = -3,
+    kErrTimeout = -4,
+    kErrNonFinite = -5,
+    kErrUnsupported = -6,
+    kErrState = -7,
+};
+
+void CudaCheck(cudaError_t e, const char* what);
+
+/// Owning device allocation.
+struct DeviceBuffer {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    DeviceBuffer() = default;
+    explicit DeviceBuffer(size_t n);
+    ~DeviceBuffer();
+    DeviceBuffer(const DeviceBuffer&) = delete;
+    DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+    template <class T>
+    T* as() const { return static_cast<T*>(ptr); }
+};
+
+struct ActionHost {
+    std::string name, type;
+    int kind = 0;   // 0 kinetic, 1 trap, 2 bare pair
+    int index = 0;  // into SystemDev::{kinetic,trap,pair}
+    std::vector<uint32_t> species_list;
+    bool is_importance_weight = false;
+    // PairAction::is_first_time / dUdB_constant / potential_constant (pair_action_class.h:14-19)
+    bool is_first_time = true;
+    double dUdB_constant = 0., potential_constant = 0.;
+};
+
+struct MoveHost {
+    std::string name, type;
+    MoveDev dev;
+    bool adaptive = false;
+    double target_ratio = 0.;
+    bool first_block = true;
+    uint64_t attempts = 0;       // total attempts (Philox attempt counter)
+    uint64_t block_attempt = 0;  // counters since the last Write (move_class.h:253-256)
+    uint64_t block_accept = 0;
+    double last_ratio = 0.;      // acceptance ratio of the last completed block
+    uint64_t total_accept = 0;   // accepted attempts since construction
+    uint64_t total_level0 = 0;   // attempts whose proposal reached the level-0 evaluation
+};
+
+struct ObservableHost {
+    std::string name, type;
+    int kind = 0;  // 0 energy, 1 pair correlation, 2 structure factor, 3 ignored bookkeeping
+    uint64_t n_measure = 0;
+    // Energy (energy_class.h:7-326)
+    bool measure_potential = false, use_thermal = true, use_virial = false;
+    uint32_t virial_window = 0;
+    std::vector<double> energies, potentials;
+    // PairCorrelation (pair_correlation_class.h:7-124)
+    uint32_t sa = 0, sb = 0, n_r = 0;
+    double r_min = 0., r_max = 0., dr = 0., d_ir = 0.;
+    std::unique_ptr<DeviceBuffer> hist;  // unsigned long long [n_r]
+    // StructureFactor (structure_factor_class.h:7-212)
+    double k_cut = 0.;
+    std::unique_ptr<DeviceBuffer> sk;    // double [K]
+};
+
+struct LoopNode {
+    int kind = 0;  // 0 loop, 1 move, 2 observable, 3 write
+    uint32_t index = 0;
+    uint64_t n_steps = 1;
+    std::vector<LoopNode> children;
+};
+
+class Context {
+   public:
+    Context(const Input& in, const std::string& base_dir, int device, uint32_t chain);
+    ~Context();
+
+    // --- path state (path_class.h / species_class.h) ---
+    void SetPath(int which, const double* host_pos);  // [n_total][M][n_d]; which 0 old, 1 new, 2 both
+    void GetPath(int which, double* host_pos);
+    void InitRhoK();                                   // species_class.h:380-403 for every kept species
+    void GetRhoK(uint32_t species, double* out);       // [M][K][2]
+    void GetKVecs(double* out);                        // [K][n_d]
+
+    // --- Action interface (action_class.h:37-52) ---
+    double GetAction(uint32_t a, uint32_t b0, uint32_t b1, const uint32_t* sp, const uint32_t* p, uint32_t n, uint32_t level, int mode);
+    void GetActionGradient(uint32_t a, uint32_t b0, uint32_t b1, const uint32_t* sp, const uint32_t* p, uint32_t n, uint32_t level,
+                           int mode, double* out);
+    double DActionDBeta(uint32_t a);
+    double Potential(uint32_t a);
+    double VirialEnergy(uint32_t a, double window);
+    double VirialCentroid(uint32_t species);  // centroid term of energy_class.h:78-94 (before / 2 tau)
+
+    // --- moves, observables, algorithm ---
+    void MoveAttempts(uint32_t m, uint64_t n);
+    void Sweep(const uint32_t* moves, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep);
+    void ObservableAccumulate(uint32_t o);
+    std::vector<double> ObservableBlock(uint32_t o);
+    void Run();
+    void RunNode(const LoopNode& n);
+    void WriteBlock();
+
+    // --- configuration ---
+    SystemDev sys;
+    int device = 0;
+    int n_sm = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t seed = 12345, chain = 0;
+    uint64_t timeout_ns = 2000000000ull;
+    int sweep_grid = 0;       // CTAs of the cooperative sweep (0 = automatic)
+    int last_grid_ = 0;       // CTAs of the most recent sweep launch
+    std::vector<std::string> species_names;
+    std::vector<ActionHost> actions;
+    std::vector<MoveHost> moves;
+    std::vector<ObservableHost> observables;
+    LoopNode main_loop;
+    std::vector<std::vector<std::vector<double>>> blocks;  // per observable, per block
+    std::vector<double> kmags;                             // |k| per stored k-vector
+    double kcutoff = 0.;                                   // KSpace::cutoff after all setups
+    std::vector<std::vector<int>> kint;                    // integer k indices per stored k-vector
+    int rho_slots = 0;
+    std::string base_dir;
+
+   private:
+    std::vector<std::unique_ptr<DeviceBuffer>> keep_;  // tables owned for the context lifetime
+    std::unique_ptr<DeviceBuffer> pos_, pos_new_, rho_, kidx_;
+    std::unique_ptr<DeviceBuffer> partials_, result_, bar_, err_, pairs_, rho_tmp_, parts_, kmag_dev_, sched_, accepts_;
+    size_t partials_cap_ = 0, pairs_cap_ = 0, rho_tmp_cap_ = 0, parts_cap_ = 0;
+
+    template <class T>
+    T* Upload(const std::vector<T>& v);
+    void BuildPath(const Input& in);
+    void BuildActions(const Input& in);
+    void BuildMoves(const Input& in);
+    void BuildObservables(const Input& in);
+    void ReadLoop(const Input& in, LoopNode& node);
+    CubicTable BuildCubic(const std::vector<double>& x, const std::vector<double>& y, bool uniform);
+    void FreeSplineTable(double L, uint32_t n_images, double lambda, double tau, bool want_dtau, CubicTable* image, CubicTable* dtau);
+
+   public:
+    // scratch helpers used by the kernel launch wrappers
+    double* Partials(size_t n);
+    double* Result() { return result_->as<double>(); }
+    unsigned long long* Barrier() { return bar_->as<unsigned long long>(); }
+    int* ErrWord() { return err_->as<int>(); }
+    uint32_t* Pairs(size_t n_pairs);
+    double2* RhoTmp(size_t n);
+    uint32_t* Parts(size_t n);
+    void CheckDeviceError();
+    void Sync();
+};
+
+}  // namespace pimc

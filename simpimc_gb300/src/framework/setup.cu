@@ -1,0 +1,592 @@
+// XML-driven construction of a Context: path, k-space, tables, actions, moves, observables and the
+// algorithm loop. Follows the construction order of the reference's Simulation
+// (src/framework/simulation_class.h:16-39) and Path (src/data_structures/path_class.h:25-69).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <ctime>
+
+#include "context.h"
+#include "table_io.h"
+
+namespace pimc {
+
+void CudaCheck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw PimcError(kErrCuda, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+DeviceBuffer::DeviceBuffer(size_t n) : bytes(n) {
+    if (n == 0) n = 16;
+    CudaCheck(cudaMalloc(&ptr, n), "cudaMalloc");
+    CudaCheck(cudaMemset(ptr, 0, n), "cudaMemset");
+}
+
+DeviceBuffer::~DeviceBuffer() {
+    if (ptr) cudaFree(ptr);
+}
+
+template <class T>
+T* Context::Upload(const std::vector<T>& v) {
+    keep_.emplace_back(new DeviceBuffer(v.size() * sizeof(T)));
+    if (!v.empty()) CudaCheck(cudaMemcpy(keep_.back()->ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "upload");
+    return keep_.back()->as<T>();
+}
+
+// Natural cubic interpolating spline (second derivatives zero at both ends), the function that
+// einspline's {NATURAL, NATURAL} B-spline interpolants represent. Solved by the tridiagonal
+// (Thomas) recurrence and stored as one polynomial per interval.
+CubicTable Context::BuildCubic(const std::vector<double>& x, const std::vector<double>& y, bool uniform) {
+    const size_t n = x.size();
+    if (n < 2 || y.size() != n) throw PimcError(kErrInput, "spline needs at least two matching knots");
+    for (size_t i = 1; i < n; ++i)
+        if (!(x[i] > x[i - 1])) throw PimcError(kErrInput, "spline knots must increase");
+    std::vector<double> m(n, 0.);
+    if (n >= 3) {
+        std::vector<double> cp(n, 0.), dp(n, 0.);
+        for (size_t i = 1; i + 1 < n; ++i) {
+            const double h0 = x[i] - x[i - 1], h1 = x[i + 1] - x[i];
+            double diag = 2. * (h0 + h1);
+            double rhs = 6. * ((y[i + 1] - y[i]) / h1 - (y[i] - y[i - 1]) / h0);
+            if (i > 1) {
+                diag -= h0 * cp[i - 1];
+                rhs -= h0 * dp[i - 1];
+            }
+            cp[i] = h1 / diag;
+            dp[i] = rhs / diag;
+        }
+        m[n - 2] = dp[n - 2];
+        for (size_t i = n - 2; i-- > 1;) m[i] = dp[i] - cp[i] * m[i + 1];
+    }
+    std::vector<Cubic4> c(n - 1);
+    for (size_t i = 0; i + 1 < n; ++i) {
+        const double h = x[i + 1] - x[i];
+        c[i].c0 = y[i];
+        c[i].c1 = (y[i + 1] - y[i]) / h - h * (2. * m[i] + m[i + 1]) / 6.;
+        c[i].c2 = 0.5 * m[i];
+        c[i].c3 = (m[i + 1] - m[i]) / (6. * h);
+    }
+    CubicTable t;
+    t.n = (int32_t)n;
+    t.x0 = x.front();
+    t.x1 = x.back();
+    t.uniform = uniform ? 1 : 0;
+    t.x = Upload(x);
+    t.c = Upload(c);
+    if (uniform) {
+        t.inv_dx = (double)(n - 1) / (x.back() - x.front());
+    } else {
+        // Buckets of equal width over [x0, x1]; each stores the interval holding its left edge.
+        const int nb = (int)std::min<size_t>(4 * n, 1u << 20);
+        t.n_bucket = nb;
+        t.inv_dx = nb / (x.back() - x.front());
+        std::vector<int32_t> bk(nb);
+        size_t i = 0;
+        for (int j = 0; j < nb; ++j) {
+            const double xl = x.front() + j / t.inv_dx;
+            while (i + 2 < n && x[i + 1] <= xl) ++i;
+            bk[j] = (int32_t)i;
+        }
+        t.bucket = Upload(bk);
+    }
+    return t;
+}
+
+// FreeSpline (src/actions/free_spline_class.h:25-68): periodic-image part of the free-particle
+// action on a 10000-point uniform grid spanning one box length (1000 for open boundaries).
+void Context::FreeSplineTable(double L, uint32_t n_images, double lambda, double tau, bool want_dtau, CubicTable* image,
+                              CubicTable* dtau) {
+    const double i4lt = 1. / (4. * lambda * tau);
+    const double t_l = L == 0. ? 1000. : L;
+    const uint32_t num = 10000;
+    const double start = -t_l / 2., end = t_l / 2., dr = (end - start) / (num - 1);
+    std::vector<double> xs(num), ia(num, 0.), dia(num, 0.);
+    for (uint32_t i = 0; i < num; ++i) {
+        const double r = start + i * dr;
+        xs[i] = r;
+        const double r2 = r * r * i4lt;
+        for (uint32_t im = 1; im <= n_images; ++im) {
+            const double rp = r + im * t_l, rm = r - im * t_l;
+            const double dp = r2 - rp * rp * i4lt, dm = r2 - rm * rm * i4lt;
+            const double ep = std::exp(dp), em = std::exp(dm);
+            ia[i] += ep + em;
+            if (want_dtau) dia[i] += (dp * ep + dm * em) / tau;
+        }
+        if (want_dtau) dia[i] = dia[i] / (1. + ia[i]);
+        ia[i] = -std::log1p(ia[i]);
+    }
+    *image = BuildCubic(xs, ia, true);
+    if (want_dtau) *dtau = BuildCubic(xs, dia, true);
+}
+
+void Context::BuildPath(const Input& in) {
+    Input sysin = in.GetChild("System");
+    if (sysin.IsNull()) throw PimcError(kErrInput, "input has no <System> element");
+    sys.n_d = sysin.GetAttribute<uint32_t>("n_d");
+    sys.M = sysin.GetAttribute<uint32_t>("n_bead");
+    sys.beta = sysin.GetAttribute<double>("beta");
+    sys.pbc = sysin.GetAttribute<bool>("pbc", true) ? 1 : 0;
+    sys.L = sysin.GetAttribute<double>("L", 0.);
+    if (sys.n_d < 1 || sys.n_d > 3) throw PimcError(kErrInput, "n_d must be 1, 2 or 3");
+    if (sys.M < 2) throw PimcError(kErrInput, "n_bead must be at least 2");
+    if (!(sys.beta > 0.)) throw PimcError(kErrInput, "beta must be positive");
+    if (sys.pbc) {
+        if (!(sys.L > 0.)) throw PimcError(kErrInput, "pbc=1 needs a positive L");
+        sys.iL = 1. / sys.L;
+        sys.vol = std::pow(sys.L, sys.n_d);
+    } else {
+        sys.L = 0.;
+        sys.iL = 0.;
+        sys.vol = 1.;
+    }
+    sys.tau = sys.beta / (1. * sys.M);
+    for (auto& s : in.GetChild("Particles").GetChildList("Species")) {
+        if (sys.S >= (uint32_t)kMaxSpecies) throw PimcError(kErrUnsupported, "too many species");
+        const uint32_t n = s.GetAttribute<uint32_t>("n_part");
+        const double lam = s.GetAttribute<double>("lambda");
+        if (n == 0) throw PimcError(kErrInput, "species with n_part = 0");
+        if (s.GetAttribute<bool>("fermi", false) || s.GetAttribute<bool>("fixed_node", false))
+            throw PimcError(kErrUnsupported, "fermion / fixed-node species are not supported");
+        species_names.push_back(s.GetAttribute<std::string>("name"));
+        sys.sp_off[sys.S] = sys.n_total;
+        sys.sp_n[sys.S] = n;
+        sys.sp_lambda[sys.S] = lam;
+        sys.sp_rho[sys.S] = -1;
+        sys.n_total += n;
+        sys.S++;
+    }
+    if (sys.S == 0) throw PimcError(kErrInput, "input declares no species");
+    sys.n_pad = (sys.n_total + 31u) & ~31u;
+    pos_.reset(new DeviceBuffer((size_t)sys.M * 3 * sys.n_pad * sizeof(double)));
+    pos_new_.reset(new DeviceBuffer((size_t)sys.M * 3 * sys.n_pad * sizeof(double)));
+    sys.pos = pos_->as<double>();
+    sys.pos_new = pos_new_->as<double>();
+}
+
+static uint32_t SpeciesIndex(const std::vector<std::string>& names, const std::string& n) {
+    for (size_t i = 0; i < names.size(); ++i)
+        if (names[i] == n) return (uint32_t)i;
+    throw PimcError(kErrInput, "no species named '" + n + "'");
+}
+
+namespace {
+
+// KSpace::Include / Setup (k_space_class.h:17-80); lexicographic enumeration of the index box.
+struct KSet {
+    double cutoff = 0.;
+    int max_index[3] = {0, 0, 0};
+    std::vector<std::vector<int>> n;
+    std::vector<double> mags;
+
+    void Setup(double k_cut, double L, uint32_t n_d) {
+        if (L == 0. || k_cut <= cutoff) return;
+        cutoff = k_cut;
+        n.clear();
+        mags.clear();
+        const double box = 2. * M_PI / L;
+        for (uint32_t d = 0; d < n_d; ++d) max_index[d] = (int)(uint32_t)std::ceil(1.1 * k_cut / box);
+        std::vector<int> v(n_d);
+        for (uint32_t d = 0; d < n_d; ++d) v[d] = -max_index[d];
+        for (;;) {
+            double k[3] = {0., 0., 0.}, k2 = 0.;
+            for (uint32_t d = 0; d < n_d; ++d) {
+                k[d] = v[d] * box;
+                k2 += k[d] * k[d];
+            }
+            bool inc = false;
+            if (k2 < k_cut * k_cut && k2 != 0.) {
+                if (k[0] > 0.) inc = true;
+                else if (n_d >= 2 && k[0] == 0. && k[1] > 0.) inc = true;
+                else if (n_d >= 3 && k[0] == 0. && k[1] == 0. && k[2] > 0.) inc = true;
+            }
+            if (inc) {
+                n.push_back(v);
+                mags.push_back(std::sqrt(k2));
+            }
+            int d = (int)n_d - 1;
+            while (d >= 0) {
+                if (++v[d] <= max_index[d]) break;
+                v[d] = -max_index[d];
+                --d;
+            }
+            if (d < 0) break;
+        }
+    }
+};
+
+}  // namespace
+
+void Context::BuildActions(const Input& in) {
+    // k-space: the System cutoff, then every long-range action and structure factor may raise it
+    // (path_class.h:58-62, pair_action_class.h:216-222, structure_factor_class.h:175-180).
+    KSet ks;
+    Input sysin = in.GetChild("System");
+    if (sys.pbc) ks.Setup(sysin.GetAttribute<double>("k_cut", 2. * M_PI / sys.L), sys.L, sys.n_d);
+    auto alist = in.GetChild("Actions").GetChildList("Action");
+    bool long_range_seen = false;
+    for (const auto& a : alist) {
+        if (a.GetAttribute<std::string>("type") == "BarePairAction" && a.GetAttribute<bool>("use_long_range", false)) {
+            if (!sys.pbc) throw PimcError(kErrInput, "use_long_range needs periodic boundaries");
+            const double before = ks.cutoff;
+            ks.Setup(a.GetAttribute<double>("k_cut", ks.cutoff), sys.L, sys.n_d);
+            // A later, larger cutoff would outgrow the tables of earlier long-range actions.
+            if (long_range_seen && ks.cutoff != before)
+                throw PimcError(kErrInput, "k_cut of a long-range action grows after an earlier one; order the largest first");
+            long_range_seen = true;
+        }
+    }
+    for (auto& o : in.GetChild("Observables").GetChildList("Observable"))
+        if (o.GetAttribute<std::string>("type") == "StructureFactor") {
+            if (!sys.pbc) throw PimcError(kErrInput, "StructureFactor needs periodic boundaries");
+            const double before = ks.cutoff;
+            ks.Setup(o.GetAttribute<double>("k_cut", ks.cutoff), sys.L, sys.n_d);
+            if (long_range_seen && ks.cutoff != before)
+                throw PimcError(kErrInput, "StructureFactor k_cut exceeds a long-range action's k_cut");
+        }
+    kcutoff = ks.cutoff;
+    sys.K = (uint32_t)ks.n.size();
+    for (int d = 0; d < 3; ++d) sys.max_index[d] = ks.max_index[d];
+    for (uint32_t d = 0; d < 3; ++d) sys.box[d] = sys.pbc ? 2. * M_PI / sys.L : 0.;
+    kmags = ks.mags;
+    kint = ks.n;
+    std::vector<int32_t> packed(sys.K);
+    for (uint32_t k = 0; k < sys.K; ++k) {
+        int v[3] = {0, 0, 0};
+        for (uint32_t d = 0; d < sys.n_d; ++d) v[d] = ks.n[k][d];
+        if (std::abs(v[0]) > 127 || std::abs(v[1]) > 127 || std::abs(v[2]) > 127) throw PimcError(kErrUnsupported, "k index beyond 127");
+        packed[k] = PackK(v[0], v[1], v[2]);
+    }
+    if (sys.K) sys.kidx = Upload(packed);
+
+    for (auto& a : alist) {
+        ActionHost h;
+        h.name = a.GetAttribute<std::string>("name");
+        h.type = a.GetAttribute<std::string>("type");
+        const int n_images = a.GetAttribute<int>("n_images", 0);
+        const uint32_t max_level = a.GetAttribute<uint32_t>("max_level", 0);
+        if (h.type == "Kinetic") {
+            if (sys.n_kinetic >= kMaxKinetic) throw PimcError(kErrUnsupported, "too many kinetic actions");
+            KineticDev& k = sys.kinetic[sys.n_kinetic];
+            k.species = SpeciesIndex(species_names, a.GetAttribute<std::string>("species"));
+            const double lam = sys.sp_lambda[k.species];
+            if (!(lam > 0.)) throw PimcError(kErrInput, "Kinetic action on a species with lambda = 0");
+            k.has_images = n_images > 0 ? 1 : 0;
+            k.i4lt = 1. / (4. * lam * sys.tau);
+            k.i4ltt = 1. / (4. * lam * sys.tau * sys.tau);
+            k.d_action_d_beta_const = sys.sp_n[k.species] * sys.M * sys.n_d / (2. * sys.tau);
+            // kinetic_class.h:16-24: spline i holds tau (i + 1); the bisection uses skip = 2^l.
+            const uint32_t n_spline = sys.M / 2 + (sys.M % 2) + 1;
+            for (int l = 0; l < kMaxLevels && (1u << l) <= n_spline; ++l) {
+                k.i4lt_level[l] = 1. / (4. * lam * (sys.tau * (1u << l)));
+                FreeSplineTable(sys.L, (uint32_t)std::max(n_images, 0), lam, sys.tau * (1u << l), l == 0, &k.image[l],
+                                l == 0 ? &k.d_image_d_tau : nullptr);
+            }
+            h.kind = 0;
+            h.index = sys.n_kinetic++;
+            h.species_list.push_back(k.species);
+        } else if (h.type == "HarmonicTrap") {
+            if (sys.n_trap >= kMaxTrap) throw PimcError(kErrUnsupported, "too many trap actions");
+            TrapDev& t = sys.trap[sys.n_trap];
+            t.species = SpeciesIndex(species_names, a.GetAttribute<std::string>("species"));
+            t.max_level = max_level;
+            const double om = a.GetAttribute<double>("omega");
+            t.cofactor_a = 0.5 * sys.tau * om * om * (1. + sys.tau * sys.tau * om * om / 12.);
+            t.cofactor_b = 0.5 * om * om * (1. + 3. * sys.tau * sys.tau * om * om / 12.);
+            h.kind = 1;
+            h.index = sys.n_trap++;
+            h.species_list.push_back(t.species);
+        } else if (h.type == "BarePairAction") {
+            if (sys.n_pair >= kMaxPair) throw PimcError(kErrUnsupported, "too many pair actions");
+            PairDev& p = sys.pair[sys.n_pair];
+            p.sa = SpeciesIndex(species_names, a.GetAttribute<std::string>("species_a"));
+            p.sb = SpeciesIndex(species_names, a.GetAttribute<std::string>("species_b"));
+            p.max_level = max_level;
+            p.use_long_range = a.GetAttribute<bool>("use_long_range", false) ? 1 : 0;
+            p.is_coulomb = a.GetAttribute<bool>("is_coulomb", false) ? 1 : 0;
+            p.is_constant = (p.sa == p.sb) && (sys.sp_n[p.sa] == 1 || sys.sp_lambda[p.sa] == 0.);
+            std::string file = a.GetAttribute<std::string>("file");
+            if (!file.empty() && file[0] != '/' && !base_dir.empty()) file = base_dir + "/" + file;
+            TableFile tf = TableFile::Load(file);
+            const auto& r = tf.Vec("v/diag/r");
+            const auto& v = tf.Vec("v/diag/v_r");
+            if ((size_t)tf.Scalar("v/diag/n_r") != r.size() || r.size() != v.size())
+                throw PimcError(kErrInput, "table '" + file + "': inconsistent v/diag grid");
+            p.v_r = BuildCubic(r, v, false);
+            p.r_v_min = r.front();
+            p.r_v_max = r.back();
+            double vk0 = 0., vr0 = 0.;
+            if (p.use_long_range) {
+                const auto& rl = tf.Vec("v/diag/r_long");
+                const auto& vl = tf.Vec("v/diag/v_long_r");
+                vr0 = tf.Scalar("v/diag/v_long_r_0");
+                p.v_long_r = BuildCubic(rl, vl, false);
+                p.r_vl_min = rl.front();
+                p.r_vl_max = rl.back();
+                const auto& kv = tf.Vec("v/diag/k");
+                const auto& vkv = tf.Vec("v/diag/v_long_k");
+                vk0 = tf.Scalar("v/diag/v_long_k_0");
+                // bare_pair_action_class.h:79-85: match every stored |k| against the table.
+                std::vector<double> vk(sys.K, 0.);
+                for (uint32_t k = 0; k < sys.K; ++k)
+                    for (size_t j = 0; j < kv.size(); ++j)
+                        if (std::fabs(kmags[k] - kv[j]) < 1.e-8) vk[k] = vkv[j];
+                p.v_long_k = Upload(vk);
+                sys.sp_rho[p.sa] = sys.sp_rho[p.sb] = 0;  // marked; slots assigned below
+            }
+            // bare_pair_action_class.h:89-95
+            if (p.sa == p.sb) {
+                vk0 *= 0.5 * sys.sp_n[p.sa] * sys.sp_n[p.sb] * sys.M;
+                vr0 *= -0.5 * sys.sp_n[p.sa] * sys.M;
+            } else {
+                vk0 *= (double)sys.sp_n[p.sa] * sys.sp_n[p.sb] * sys.M;
+                vr0 *= 0.;
+            }
+            p.v_long_k_0 = vk0;
+            p.v_long_r_0 = vr0;
+            h.kind = 2;
+            h.index = sys.n_pair++;
+            h.species_list.push_back(p.sa);
+            h.species_list.push_back(p.sb);
+        } else {
+            throw PimcError(kErrUnsupported, "unsupported action type '" + h.type + "'");
+        }
+        actions.push_back(h);
+    }
+}
+
+void Context::BuildMoves(const Input& in) {
+    for (auto& m : in.GetChild("Moves").GetChildList("Move")) {
+        MoveHost h;
+        h.name = m.GetAttribute<std::string>("name");
+        h.type = m.GetAttribute<std::string>("type");
+        if (h.type != "Bisect") throw PimcError(kErrUnsupported, "unsupported move type '" + h.type + "'");
+        if (moves.size() >= (size_t)kMaxMoves) throw PimcError(kErrUnsupported, "too many moves");
+        MoveDev& d = h.dev;
+        d.species = SpeciesIndex(species_names, m.GetAttribute<std::string>("species"));
+        d.n_level = m.GetAttribute<uint32_t>("n_level");
+        d.lambda = sys.sp_lambda[d.species];
+        if (!(d.lambda > 0.)) throw PimcError(kErrInput, "Bisect on a species with lambda = 0");
+        if (d.n_level < 1 || (1u << d.n_level) > sys.M || d.n_level > (uint32_t)kMaxLevels)
+            throw PimcError(kErrInput, "bisection level out of range for n_bead");
+        const int n_images = m.GetAttribute<int>("n_images", 0);
+        d.has_images = n_images > 0 ? 1 : 0;
+        h.adaptive = m.GetAttribute<bool>("adaptive", false);
+        if (h.adaptive) h.target_ratio = m.GetAttribute<double>("target_ratio");
+        // bisect_class.h:158-163: sampling propagator at tau' = tau 2^l / 2.
+        const uint32_t n_spline = (uint32_t)std::floor(std::log2((double)sys.M));
+        for (uint32_t l = 0; l < n_spline && l < (uint32_t)kMaxLevels; ++l) {
+            const double tl = 0.5 * sys.tau * (1u << l);
+            d.i4lt_sample[l] = 1. / (4. * d.lambda * tl);
+            if (d.has_images) FreeSplineTable(sys.L, (uint32_t)n_images, d.lambda, tl, false, &d.sample_image[l], nullptr);
+        }
+        // move_class.h:27-31: every action whose species list holds the move's species.
+        for (auto& a : actions) {
+            if (std::find(a.species_list.begin(), a.species_list.end(), d.species) == a.species_list.end()) continue;
+            if (a.kind == 0) d.kinetic[d.n_kinetic++] = a.index;
+            else if (a.kind == 1) d.trap[d.n_trap++] = a.index;
+            else d.pair[d.n_pair++] = a.index;
+        }
+        moves.push_back(h);
+    }
+}
+
+void Context::BuildObservables(const Input& in) {
+    for (auto& o : in.GetChild("Observables").GetChildList("Observable")) {
+        ObservableHost h;
+        h.name = o.GetAttribute<std::string>("name");
+        h.type = o.GetAttribute<std::string>("type");
+        if (h.type == "Energy") {
+            h.kind = 0;
+            h.measure_potential = o.GetAttribute<bool>("measure_potential", false);
+            h.use_virial = o.GetAttribute<bool>("use_virial_estimator", false);
+            if (h.use_virial) {
+                h.virial_window = o.GetAttribute<uint32_t>("virial_window_size", sys.M);
+                h.use_thermal = o.GetAttribute<bool>("use_thermal_estimator", false);
+            } else {
+                h.use_thermal = o.GetAttribute<bool>("use_thermal_estimator", true);
+            }
+            h.energies.assign(actions.size(), 0.);
+            h.potentials.assign(actions.size(), 0.);
+        } else if (h.type == "PairCorrelation") {
+            h.kind = 1;
+            h.sa = SpeciesIndex(species_names, o.GetAttribute<std::string>("species_a"));
+            h.sb = SpeciesIndex(species_names, o.GetAttribute<std::string>("species_b"));
+            h.r_min = o.GetAttribute<double>("r_min", 0.);
+            h.r_max = o.GetAttribute<double>("r_max", sys.L / 2.);
+            h.n_r = o.GetAttribute<uint32_t>("n_r", 100);
+            if (h.n_r < 2) throw PimcError(kErrInput, "n_r must be at least 2");
+            h.dr = (h.r_max - h.r_min) / (h.n_r - 1.);
+            h.d_ir = 1. / h.dr;
+            h.hist.reset(new DeviceBuffer(h.n_r * sizeof(unsigned long long)));
+        } else if (h.type == "StructureFactor") {
+            h.kind = 2;
+            h.sa = SpeciesIndex(species_names, o.GetAttribute<std::string>("species_a"));
+            h.sb = SpeciesIndex(species_names, o.GetAttribute<std::string>("species_b"));
+            h.k_cut = o.GetAttribute<double>("k_cut", kcutoff);
+            sys.sp_rho[h.sa] = sys.sp_rho[h.sb] = 0;
+            h.sk.reset(new DeviceBuffer(std::max<size_t>(sys.K, 1) * sizeof(double)));
+        } else if (h.type == "Time" || h.type == "PathDump") {
+            h.kind = 3;
+        } else {
+            throw PimcError(kErrUnsupported, "unsupported observable type '" + h.type + "'");
+        }
+        observables.push_back(std::move(h));
+    }
+}
+
+void Context::ReadLoop(const Input& in, LoopNode& node) {
+    // loop_class.h:248-266
+    for (auto& c : in.GetChildList()) {
+        const std::string& t = c.GetName();
+        LoopNode ch;
+        if (t == "Move" || t == "Observable") {
+            const std::string nm = c.GetAttribute<std::string>("name");
+            bool found = false;
+            if (t == "Move") {
+                for (size_t i = 0; i < moves.size(); ++i)
+                    if (moves[i].name == nm) { ch.kind = 1; ch.index = (uint32_t)i; found = true; }
+            } else {
+                for (size_t i = 0; i < observables.size(); ++i)
+                    if (observables[i].name == nm) { ch.kind = 2; ch.index = (uint32_t)i; found = true; }
+            }
+            if (!found) continue;
+        } else if (t == "Write") {
+            ch.kind = 3;
+        } else if (t == "Loop") {
+            ch.kind = 0;
+            ch.n_steps = (uint64_t)c.GetAttribute<int>("n_step");
+            ReadLoop(c, ch);
+        } else {
+            continue;
+        }
+        node.children.push_back(std::move(ch));
+    }
+}
+
+Context::Context(const Input& in, const std::string& bd, int dev, uint32_t ch) : device(dev), chain(ch), base_dir(bd) {
+    CudaCheck(cudaSetDevice(device), "cudaSetDevice");
+    CudaCheck(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, device), "device attribute");
+    CudaCheck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream create");
+    Input rng = in.GetChild("RNG");
+    seed = rng.IsNull() ? (uint32_t)time(nullptr) : (uint32_t)rng.GetAttribute<int>("seed", (int)time(nullptr));
+    BuildPath(in);
+    BuildActions(in);
+    BuildMoves(in);
+    BuildObservables(in);
+    // Charge-density slots for species that need them.
+    for (uint32_t s = 0; s < sys.S; ++s)
+        if (sys.sp_rho[s] == 0) sys.sp_rho[s] = rho_slots++;
+        else sys.sp_rho[s] = -1;
+    if (rho_slots && sys.K) {
+        rho_.reset(new DeviceBuffer((size_t)rho_slots * sys.M * sys.K * sizeof(double2)));
+        sys.rho_k = rho_->as<double2>();
+    }
+    partials_.reset(new DeviceBuffer(4096 * sizeof(double)));
+    partials_cap_ = 4096;
+    result_.reset(new DeviceBuffer(64 * sizeof(double)));
+    bar_.reset(new DeviceBuffer(64));
+    err_.reset(new DeviceBuffer(64));
+    blocks.resize(observables.size());
+    Input alg = in.GetChild("Algorithm");
+    main_loop.kind = 0;
+    main_loop.n_steps = 1;
+    ReadLoop(alg, main_loop);
+    InitRhoK();
+}
+
+Context::~Context() {
+    if (stream) {
+        cudaStreamSynchronize(stream);
+        cudaStreamDestroy(stream);
+    }
+}
+
+double* Context::Partials(size_t n) {
+    if (n > partials_cap_) {
+        partials_.reset(new DeviceBuffer(n * sizeof(double)));
+        partials_cap_ = n;
+    }
+    return partials_->as<double>();
+}
+
+uint32_t* Context::Pairs(size_t n_pairs) {
+    if (2 * n_pairs > pairs_cap_) {
+        pairs_.reset(new DeviceBuffer(2 * n_pairs * sizeof(uint32_t)));
+        pairs_cap_ = 2 * n_pairs;
+    }
+    return pairs_->as<uint32_t>();
+}
+
+double2* Context::RhoTmp(size_t n) {
+    if (n > rho_tmp_cap_) {
+        rho_tmp_.reset(new DeviceBuffer(n * sizeof(double2)));
+        rho_tmp_cap_ = n;
+    }
+    return rho_tmp_->as<double2>();
+}
+
+uint32_t* Context::Parts(size_t n) {
+    if (n > parts_cap_) {
+        parts_.reset(new DeviceBuffer(n * sizeof(uint32_t)));
+        parts_cap_ = n;
+    }
+    return parts_->as<uint32_t>();
+}
+
+void Context::Sync() { CudaCheck(cudaStreamSynchronize(stream), "stream synchronize"); }
+
+void Context::CheckDeviceError() {
+    int e = 0;
+    CudaCheck(cudaMemcpyAsync(&e, err_->ptr, sizeof(int), cudaMemcpyDeviceToHost, stream), "read error word");
+    Sync();
+    if (e != 0) {
+        int zero = 0;
+        CudaCheck(cudaMemcpyAsync(err_->ptr, &zero, sizeof(int), cudaMemcpyHostToDevice, stream), "clear error word");
+        Sync();
+        if (e == kDevErrTimeout) throw PimcError(kErrTimeout, "device wait timed out (grid barrier)");
+        if (e == kDevErrNonFinite) throw PimcError(kErrNonFinite, "non-finite value in the path");
+        throw PimcError(kErrState, "device reported error " + std::to_string(e));
+    }
+}
+
+void Context::SetPath(int which, const double* h) {
+    const uint32_t M = sys.M, n_d = sys.n_d, np = sys.n_pad;
+    std::vector<double> buf((size_t)M * 3 * np, 0.);
+    for (uint32_t g = 0; g < sys.n_total; ++g)
+        for (uint32_t b = 0; b < M; ++b)
+            for (uint32_t d = 0; d < n_d; ++d) {
+                const double v = h[((size_t)g * M + b) * n_d + d];
+                if (!std::isfinite(v)) throw PimcError(kErrNonFinite, "non-finite bead coordinate");
+                buf[((size_t)b * 3 + d) * np + g] = v;
+            }
+    if (which == 0 || which == 2) CudaCheck(cudaMemcpyAsync(sys.pos, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice, stream), "set path");
+    if (which == 1 || which == 2) CudaCheck(cudaMemcpyAsync(sys.pos_new, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice, stream), "set path");
+    Sync();
+    if (which == 2) {
+        for (auto& a : actions) a.is_first_time = true;
+        InitRhoK();
+    }
+}
+
+void Context::GetPath(int which, double* h) {
+    const uint32_t M = sys.M, n_d = sys.n_d, np = sys.n_pad;
+    std::vector<double> buf((size_t)M * 3 * np);
+    CudaCheck(cudaMemcpyAsync(buf.data(), which == 0 ? sys.pos : sys.pos_new, buf.size() * sizeof(double), cudaMemcpyDeviceToHost, stream), "get path");
+    Sync();
+    for (uint32_t g = 0; g < sys.n_total; ++g)
+        for (uint32_t b = 0; b < M; ++b)
+            for (uint32_t d = 0; d < n_d; ++d) h[((size_t)g * M + b) * n_d + d] = buf[((size_t)b * 3 + d) * np + g];
+}
+
+void Context::GetRhoK(uint32_t s, double* out) {
+    if (s >= sys.S || sys.sp_rho[s] < 0 || !sys.rho_k) throw PimcError(kErrArg, "species keeps no charge density");
+    const size_t n = (size_t)sys.M * sys.K;
+    CudaCheck(cudaMemcpyAsync(out, sys.rho_k + (size_t)sys.sp_rho[s] * n, n * sizeof(double2), cudaMemcpyDeviceToHost, stream), "get rho_k");
+    Sync();
+}
+
+void Context::GetKVecs(double* out) {
+    for (uint32_t k = 0; k < sys.K; ++k)
+        for (uint32_t d = 0; d < sys.n_d; ++d) out[(size_t)k * sys.n_d + d] = kint[k][d] * sys.box[d];
+}
+
+}  // namespace pimc

@@ -1,0 +1,792 @@
+// Action-interface and estimator kernels: GetAction / GetActionGradient for one action on a path
+// segment, DActionDBeta, Potential, VirialEnergy, the virial centroid term, the charge-density
+// initialisation and the g(r) / S(k) accumulators.
+//
+// Every scalar result is a deterministic two-pass reduction (fixed per-block tree, then one warp
+// over the block partials in block order), so repeated calls on the same state agree bit for bit.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "../framework/context.h"
+#include "actions.cuh"
+
+namespace pimc {
+
+namespace {
+
+constexpr int kSumThreads = 256;
+
+template <int N, class F>
+__global__ void __launch_bounds__(kSumThreads) SumItemsKernel(uint64_t n, F f, double* __restrict__ partials) {
+    __shared__ double red[kSumThreads / 32];
+    double acc[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) acc[j] = 0.;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        double v[N];
+        f(i, v);
+#pragma unroll
+        for (int j = 0; j < N; ++j) acc[j] += v[j];
+    }
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        const double s = BlockSum(acc[j], red);
+        if (threadIdx.x == 0) partials[(size_t)blockIdx.x * N + j] = s;
+    }
+}
+
+template <int N>
+__global__ void FinalSumKernel(const double* __restrict__ partials, int nb, double* __restrict__ out) {
+    const int lane = threadIdx.x;
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        double t = 0.;
+        for (int b = lane; b < nb; b += 32) t += partials[(size_t)b * N + j];
+        t = WarpSum(t);
+        if (lane == 0) out[j] = t;
+    }
+}
+
+/// Sum f(i) over i in [0, n) for N-component items; result copied to host `out`.
+template <int N, class F>
+void SumItems(Context& c, uint64_t n, F f, double* out) {
+    for (int j = 0; j < N; ++j) out[j] = 0.;
+    if (n == 0) return;
+    const uint64_t want = (n + kSumThreads - 1) / kSumThreads;
+    const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)c.n_sm * 8));
+    double* part = c.Partials((size_t)blocks * N);
+    SumItemsKernel<N><<<blocks, kSumThreads, 0, c.stream>>>(n, f, part);
+    CudaCheck(cudaGetLastError(), "sum kernel launch");
+    FinalSumKernel<N><<<1, 32, 0, c.stream>>>(part, blocks, c.Result());
+    CudaCheck(cudaGetLastError(), "final sum launch");
+    CudaCheck(cudaMemcpyAsync(out, c.Result(), N * sizeof(double), cudaMemcpyDeviceToHost, c.stream), "read result");
+    c.Sync();
+}
+
+__device__ __forceinline__ uint32_t BeadLoop(uint32_t b, uint32_t M) { return b >= M ? b - M : b; }
+
+// InitRhoK (species_class.h:380-403): rho(b, k) = sum over particles in index order of the bead
+// phases. One block per (slot, slice); particles are processed in chunks whose phase tables are
+// staged in shared memory.
+constexpr int kRhoChunk = 16;
+
+__global__ void InitRhoKernel(const SystemDev sys, const int* __restrict__ slot_species) {
+    extern __shared__ double2 tab[];  // [kRhoChunk][3][stride]
+    const int slot = blockIdx.y;
+    const uint32_t b = blockIdx.x;
+    const uint32_t s = (uint32_t)slot_species[slot];
+    const int stride = max(max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
+    double2* rho = sys.rho_k + ((size_t)slot * sys.M + b) * sys.K;
+    for (uint32_t k = threadIdx.x; k < sys.K; k += blockDim.x) rho[k] = make_double2(0., 0.);
+    const uint32_t np = sys.sp_n[s];
+    for (uint32_t p0 = 0; p0 < np; p0 += kRhoChunk) {
+        const uint32_t cnt = min((uint32_t)kRhoChunk, np - p0);
+        __syncthreads();
+        for (uint32_t t = threadIdx.x; t < cnt * sys.n_d; t += blockDim.x) {
+            const uint32_t pi = t / sys.n_d, d = t % sys.n_d;
+            const double x = PosAt(sys.pos, sys.n_pad, b, d, sys.sp_off[s] + p0 + pi);
+            PhaseRow(x, sys.box[d], sys.max_index[d], tab + ((size_t)pi * 3 + d) * stride);
+        }
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < sys.K; k += blockDim.x) {
+            const int32_t pk = sys.kidx[k];
+            double2 acc = rho[k];
+            for (uint32_t pi = 0; pi < cnt; ++pi) {
+                const double2 e = PhaseProduct(tab + (size_t)pi * 3 * stride, stride, sys.n_d, pk);
+                acc.x += e.x;
+                acc.y += e.y;
+            }
+            rho[k] = acc;
+        }
+    }
+}
+
+// Per-slice densities of a proposal (species_class.h:406-425 in NEW mode): for each slice of the
+// segment, the committed density plus (new - old) phases of the listed particles, in list order.
+__global__ void ProposalRhoKernel(const SystemDev sys, uint32_t species, const uint32_t* __restrict__ parts, uint32_t n_parts,
+                                  uint32_t b0, uint32_t skip, double2* __restrict__ out) {
+    extern __shared__ double2 tab[];  // [2][3][stride]
+    const uint32_t j = blockIdx.x;
+    const uint32_t b = BeadLoop(b0 + j * skip, sys.M);
+    const int stride = max(max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
+    const double2* committed = sys.rho_k + ((size_t)sys.sp_rho[species] * sys.M + b) * sys.K;
+    double2* dst = out + (size_t)j * sys.K;
+    for (uint32_t k = threadIdx.x; k < sys.K; k += blockDim.x) dst[k] = committed[k];
+    for (uint32_t q = 0; q < n_parts; ++q) {
+        const uint32_t g = sys.sp_off[species] + parts[q];
+        __syncthreads();
+        if (threadIdx.x < 2 * sys.n_d) {
+            const uint32_t which = threadIdx.x / sys.n_d, d = threadIdx.x % sys.n_d;
+            const double x = PosAt(which ? sys.pos_new : sys.pos, sys.n_pad, b, d, g);
+            PhaseRow(x, sys.box[d], sys.max_index[d], tab + ((size_t)which * 3 + d) * stride);
+        }
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < sys.K; k += blockDim.x) {
+            const int32_t pk = sys.kidx[k];
+            const double2 en = PhaseProduct(tab + (size_t)3 * stride, stride, sys.n_d, pk);
+            const double2 eo = PhaseProduct(tab, stride, sys.n_d, pk);
+            double2 v = dst[k];
+            v.x += en.x - eo.x;
+            v.y += en.y - eo.y;
+            dst[k] = v;
+        }
+    }
+}
+
+// g(r) histogram (pair_correlation_class.h:15-28): shared-memory counts, then global atomics.
+__global__ void PairCorrelationKernel(const SystemDev sys, uint32_t sa, uint32_t sb, double r_min, double d_ir, uint32_t n_r,
+                                      unsigned long long* __restrict__ hist) {
+    extern __shared__ unsigned int counts[];
+    for (uint32_t i = threadIdx.x; i < n_r; i += blockDim.x) counts[i] = 0u;
+    __syncthreads();
+    const uint32_t na = sys.sp_n[sa], nb = sys.sp_n[sb];
+    const uint64_t n_items = (uint64_t)sys.M * na * nb;
+    for (uint64_t it = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; it < n_items; it += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = (uint32_t)(it / ((uint64_t)na * nb));
+        const uint32_t rem = (uint32_t)(it % ((uint64_t)na * nb));
+        const uint32_t p = rem / nb, q = rem % nb;
+        if (sa == sb && q <= p) continue;
+        double ra[3], rb[3];
+        LoadBead(sys.pos, sys.n_pad, sys.n_d, b, sys.sp_off[sa] + p, ra);
+        LoadBead(sys.pos, sys.n_pad, sys.n_d, b, sys.sp_off[sb] + q, rb);
+        const double r = DistMinImage(ra, rb, sys.n_d, sys.L, sys.iL);
+        // observable_class.h:384-390; a negative index wraps as the reference's unsigned cast does.
+        const uint32_t i = (uint32_t)(long long)rint((r - r_min) * d_ir - 0.5);
+        if (i < n_r) atomicAdd(&counts[i], 1u);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n_r; i += blockDim.x)
+        if (counts[i]) atomicAdd(&hist[i], (unsigned long long)counts[i]);
+}
+
+// S(k) accumulation (structure_factor_class.h:15-32) in the reference's order: one thread per k
+// adds the slice terms one by one into the running sum.
+__global__ void StructureFactorKernel(const SystemDev sys, const double* __restrict__ kmag, double k_cut, uint32_t slot_a,
+                                      uint32_t slot_b, double* __restrict__ sk) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= sys.K || !(kmag[k] < k_cut)) return;
+    const double2* ra = sys.rho_k + (size_t)slot_a * sys.M * sys.K;
+    const double2* rb = sys.rho_k + (size_t)slot_b * sys.M * sys.K;
+    double acc = sk[k];
+    for (uint32_t b = 0; b < sys.M; ++b) {
+        const double2 a = ra[(size_t)b * sys.K + k], c = rb[(size_t)b * sys.K + k];
+        acc += 1. * (a.x * c.x + a.y * c.y);
+    }
+    sk[k] = acc;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+void Context::InitRhoK() {
+    if (!rho_slots || !sys.K) return;
+    std::vector<int> slot_species(rho_slots, 0);
+    for (uint32_t s = 0; s < sys.S; ++s)
+        if (sys.sp_rho[s] >= 0) slot_species[sys.sp_rho[s]] = (int)s;
+    uint32_t* dss = Parts(rho_slots);
+    CudaCheck(cudaMemcpyAsync(dss, slot_species.data(), rho_slots * sizeof(int), cudaMemcpyHostToDevice, stream), "slot upload");
+    const int stride = std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
+    const size_t smem = (size_t)kRhoChunk * 3 * stride * sizeof(double2);
+    InitRhoKernel<<<dim3(sys.M, rho_slots), 256, smem, stream>>>(sys, reinterpret_cast<const int*>(dss));
+    CudaCheck(cudaGetLastError(), "init rho_k launch");
+    Sync();
+}
+
+static void SpeciesParticles(const Context& c, uint32_t s, const uint32_t* sp, const uint32_t* p, uint32_t n, std::vector<uint32_t>& out) {
+    for (uint32_t i = 0; i < n; ++i)
+        if (sp[i] == s) {
+            if (p[i] >= c.sys.sp_n[s]) throw PimcError(kErrArg, "particle index out of range");
+            out.push_back(p[i]);
+        }
+}
+
+// PairAction::GenerateParticlePairs (pair_action_class.h:62-114).
+static void GenPairs(const Context& c, const PairDev& pa, const uint32_t* sp, const uint32_t* p, uint32_t n, std::vector<uint32_t>& pa_list,
+                     std::vector<uint32_t>& pb_list, std::vector<uint32_t>& pairs) {
+    for (uint32_t i = 0; i < n; ++i) {
+        if (sp[i] >= c.sys.S || p[i] >= c.sys.sp_n[sp[i]]) throw PimcError(kErrArg, "particle out of range");
+        if (sp[i] == pa.sa) pa_list.push_back(p[i]);
+        else if (sp[i] == pa.sb) pb_list.push_back(p[i]);
+    }
+    if (pa_list.empty() && pb_list.empty()) return;
+    std::vector<uint32_t> oa, ob;
+    for (uint32_t i = 0; i < c.sys.sp_n[pa.sa]; ++i)
+        if (std::find(pa_list.begin(), pa_list.end(), i) == pa_list.end()) oa.push_back(i);
+    for (uint32_t i = 0; i < c.sys.sp_n[pa.sb]; ++i)
+        if (std::find(pb_list.begin(), pb_list.end(), i) == pb_list.end()) ob.push_back(i);
+    auto add = [&](uint32_t x, uint32_t y) {
+        pairs.push_back(x);
+        pairs.push_back(y);
+    };
+    if (pa.sa == pa.sb) {
+        for (auto x : pa_list)
+            for (auto y : oa) add(x, y);
+        for (size_t i = 0; i + 1 < pa_list.size(); ++i)
+            for (size_t j = i + 1; j < pa_list.size(); ++j) add(pa_list[i], pa_list[j]);
+    } else {
+        for (auto x : pa_list)
+            for (auto y : ob) add(x, y);
+        for (auto x : pb_list)
+            for (auto y : oa) add(y, x);
+        for (auto x : pa_list)
+            for (auto y : pb_list) add(x, y);
+    }
+}
+
+static uint32_t CountLinks(uint32_t b0, uint32_t b1, uint32_t skip, uint32_t M) {
+    const uint32_t a0 = b0 % M, end = b1 % M;
+    uint32_t a = a0, n = 0;
+    while (a != end) {
+        a = (a + skip) % M;
+        if (++n > M) throw PimcError(kErrArg, "segment end is not reachable at this level");
+    }
+    return n;
+}
+
+double Context::GetAction(uint32_t ai, uint32_t b0, uint32_t b1, const uint32_t* sp, const uint32_t* p, uint32_t n, uint32_t level, int mode) {
+    if (ai >= actions.size()) throw PimcError(kErrArg, "action index out of range");
+    if (level >= (uint32_t)kMaxLevels) throw PimcError(kErrArg, "level out of range");
+    if (b1 < b0 || b0 >= sys.M || b1 - b0 > sys.M) throw PimcError(kErrArg, "slice range out of bounds");
+    const ActionHost& ah = actions[ai];
+    const double* pos = mode ? sys.pos_new : sys.pos;
+    const uint32_t M = sys.M, n_d = sys.n_d, np = sys.n_pad;
+    const double L = sys.L, iL = sys.iL;
+    const uint32_t skip = 1u << level;
+    double out = 0.;
+    if (ah.kind == 0) {
+        const KineticDev k = sys.kinetic[ah.index];
+        if (k.image[level].n == 0) throw PimcError(kErrArg, "no kinetic spline for this level");
+        std::vector<uint32_t> list;
+        SpeciesParticles(*this, k.species, sp, p, n, list);
+        const uint32_t nl = CountLinks(b0, b1, skip, M);
+        if (list.empty() || nl == 0) return 0.;
+        uint32_t* dl = Parts(list.size());
+        for (auto& x : list) x += sys.sp_off[k.species];
+        CudaCheck(cudaMemcpyAsync(dl, list.data(), list.size() * 4, cudaMemcpyHostToDevice, stream), "parts upload");
+        const uint32_t a0 = b0 % M;
+        const double i4 = k.i4lt_level[level];
+        SumItems<1>(*this, (uint64_t)list.size() * nl, [=] __device__(uint64_t i, double* v) {
+            const uint32_t g = dl[i / nl], j = (uint32_t)(i % nl);
+            const uint32_t a = (a0 + j * skip) % M, nx = (a + skip) % M;
+            double dr[3];
+            for (uint32_t d = 0; d < n_d; ++d) dr[d] = MinImage(PosAt(pos, np, a, d, g) - PosAt(pos, np, nx, d, g), L, iL);
+            v[0] = -LogRhoFree(dr, n_d, i4, &k.image[level], k.has_images);
+        }, &out);
+        return out;
+    }
+    if (ah.kind == 1) {
+        const TrapDev t = sys.trap[ah.index];
+        if (level > t.max_level) return 0.;
+        bool check = false;
+        for (uint32_t i = 0; i < n; ++i) check |= (sp[i] == t.species);
+        if (!check) return 0.;
+        // trap_class.h:224-229 reads the trap species' bead with every listed particle's index.
+        std::vector<uint32_t> list;
+        for (uint32_t i = 0; i < n; ++i) {
+            if (p[i] >= sys.sp_n[t.species]) throw PimcError(kErrArg, "particle index out of range for the trap species");
+            list.push_back(sys.sp_off[t.species] + p[i]);
+        }
+        const uint32_t ns = b1 > b0 ? (b1 - b0 + skip - 1) / skip : 0;
+        if (ns == 0) return 0.;
+        uint32_t* dl = Parts(list.size());
+        CudaCheck(cudaMemcpyAsync(dl, list.data(), list.size() * 4, cudaMemcpyHostToDevice, stream), "parts upload");
+        SumItems<1>(*this, (uint64_t)list.size() * ns, [=] __device__(uint64_t i, double* v) {
+            const uint32_t g = dl[i / ns], j = (uint32_t)(i % ns);
+            const uint32_t b = BeadLoop(b0 + j * skip, M);
+            double s = 0.;
+            for (uint32_t d = 0; d < n_d; ++d) {
+                const double x = PosAt(pos, np, b, d, g);
+                s += x * x;
+            }
+            v[0] = s;
+        }, &out);
+        return t.cofactor_a * skip * out;
+    }
+    // Bare pair action (pair_action_class.h:267-302).
+    const PairDev pa = sys.pair[ah.index];
+    if (level > pa.max_level || pa.is_constant) return 0.;
+    std::vector<uint32_t> la, lb, pairs;
+    GenPairs(*this, pa, sp, p, n, la, lb, pairs);
+    const uint32_t npairs = (uint32_t)(pairs.size() / 2);
+    if (npairs == 0) return 0.;
+    uint32_t* dp = Pairs(npairs);
+    CudaCheck(cudaMemcpyAsync(dp, pairs.data(), pairs.size() * 4, cudaMemcpyHostToDevice, stream), "pairs upload");
+    const uint32_t ns = (b1 - b0 + skip - 1) / skip;
+    const uint32_t offa = sys.sp_off[pa.sa], offb = sys.sp_off[pa.sb];
+    const double tau = sys.tau;
+    double tot = 0.;
+    SumItems<1>(*this, (uint64_t)ns * npairs, [=] __device__(uint64_t i, double* v) {
+        const uint32_t j = (uint32_t)(i / npairs), q = (uint32_t)(i % npairs);
+        const uint32_t bi = BeadLoop(b0 + j * skip, M), bj = BeadLoop(b0 + j * skip + skip, M);
+        double A0[3], C0[3], A1[3], C1[3];
+        LoadBead(pos, np, n_d, bi, offb + dp[2 * q + 1], A0);
+        LoadBead(pos, np, n_d, bi, offa + dp[2 * q], C0);
+        LoadBead(pos, np, n_d, bj, offb + dp[2 * q + 1], A1);
+        LoadBead(pos, np, n_d, bj, offa + dp[2 * q], C1);
+        double r, rp, s;
+        DrDrpDrrp(A0, C0, A1, C1, n_d, L, iL, r, rp, s);
+        v[0] = PairU(pa, r, rp, level, tau);
+    }, &tot);
+    if (pa.use_long_range) {
+        const uint32_t K = sys.K;
+        const int stride = std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
+        const double2* ra;
+        const double2* rb;
+        if (mode) {
+            double2* tmp = RhoTmp((size_t)2 * ns * K);
+            const std::vector<uint32_t>* lists[2] = {&la, &lb};
+            const uint32_t spc[2] = {pa.sa, pa.sb};
+            // A homologous action has one species: its updated density serves as both factors
+            // (species_a and species_b are the same object in pair_action_class.h:294-298).
+            const int n_species = pa.sa == pa.sb ? 1 : 2;
+            for (int x = 0; x < n_species; ++x) {
+                uint32_t* dl = Parts(std::max<size_t>(1, lists[x]->size()));
+                if (!lists[x]->empty())
+                    CudaCheck(cudaMemcpyAsync(dl, lists[x]->data(), lists[x]->size() * 4, cudaMemcpyHostToDevice, stream), "parts upload");
+                ProposalRhoKernel<<<ns, 256, (size_t)2 * 3 * stride * sizeof(double2), stream>>>(sys, spc[x], dl, (uint32_t)lists[x]->size(), b0,
+                                                                                               skip, tmp + (size_t)x * ns * K);
+                CudaCheck(cudaGetLastError(), "proposal rho launch");
+                Sync();  // `Parts` is reused by the next species
+            }
+            ra = tmp;
+            rb = n_species == 1 ? tmp : tmp + (size_t)ns * K;
+        } else {
+            ra = rb = nullptr;
+        }
+        const double2* rho = sys.rho_k;
+        const int slot_a = sys.sp_rho[pa.sa], slot_b = sys.sp_rho[pa.sb];
+        const double* vk = pa.v_long_k;
+        double lr = 0.;
+        SumItems<1>(*this, (uint64_t)K * ns, [=] __device__(uint64_t i, double* v) {
+            const uint32_t k = (uint32_t)(i / ns), j = (uint32_t)(i % ns);
+            double2 a, c;
+            if (ra) {
+                a = ra[(size_t)j * K + k];
+                c = rb[(size_t)j * K + k];
+            } else {
+                const uint32_t b = BeadLoop(b0 + j * skip, M);
+                a = rho[((size_t)slot_a * M + b) * K + k];
+                c = rho[((size_t)slot_b * M + b) * K + k];
+            }
+            v[0] = vk[k] * (a.x * c.x + a.y * c.y);
+        }, &lr);
+        if (pa.sa != pa.sb) lr *= 2.;
+        tot += skip * sys.tau * lr;
+    }
+    return tot;
+}
+
+void Context::GetActionGradient(uint32_t ai, uint32_t b0, uint32_t b1, const uint32_t* sp, const uint32_t* p, uint32_t n, uint32_t level,
+                                int mode, double* g) {
+    if (ai >= actions.size()) throw PimcError(kErrArg, "action index out of range");
+    if (level >= (uint32_t)kMaxLevels) throw PimcError(kErrArg, "level out of range");
+    if (b1 < b0 || b0 >= sys.M || b1 - b0 > sys.M) throw PimcError(kErrArg, "slice range out of bounds");
+    for (uint32_t d = 0; d < 3; ++d) g[d] = 0.;
+    const ActionHost& ah = actions[ai];
+    const double* pos = mode ? sys.pos_new : sys.pos;
+    const uint32_t M = sys.M, n_d = sys.n_d, np = sys.n_pad;
+    const double L = sys.L, iL = sys.iL;
+    const uint32_t skip = 1u << level;
+    if (ah.kind == 0) {
+        // kinetic_class.h:125-144
+        const KineticDev k = sys.kinetic[ah.index];
+        std::vector<uint32_t> list;
+        SpeciesParticles(*this, k.species, sp, p, n, list);
+        const uint32_t nl = CountLinks(b0, b1, skip, M);
+        if (list.empty() || nl == 0) return;
+        for (auto& x : list) x += sys.sp_off[k.species];
+        uint32_t* dl = Parts(list.size());
+        CudaCheck(cudaMemcpyAsync(dl, list.data(), list.size() * 4, cudaMemcpyHostToDevice, stream), "parts upload");
+        const uint32_t a0 = b0 % M;
+        double t[3];
+        SumItems<3>(*this, (uint64_t)list.size() * nl, [=] __device__(uint64_t i, double* v) {
+            const uint32_t gg = dl[i / nl], j = (uint32_t)(i % nl);
+            const uint32_t a = (a0 + j * skip) % M, nx = (a + skip) % M, pv = (a + M - (skip % M)) % M;
+            for (uint32_t d = 0; d < 3; ++d) {
+                if (d >= n_d) {
+                    v[d] = 0.;
+                    continue;
+                }
+                const double ra = PosAt(pos, np, a, d, gg);
+                const double dprev = MinImage(PosAt(pos, np, pv, d, gg) - ra, L, iL);
+                const double dnext = MinImage(ra - PosAt(pos, np, nx, d, gg), L, iL);
+                v[d] = -dprev + dnext;
+            }
+        }, t);
+        const double i4 = k.i4lt / skip;
+        for (uint32_t d = 0; d < n_d; ++d) g[d] = 2. * i4 * t[d];
+        return;
+    }
+    if (ah.kind == 1) return;  // trap_class.h has no gradient: the base class returns zeros.
+    const PairDev pa = sys.pair[ah.index];
+    if (level > pa.max_level || pa.is_constant) return;
+    std::vector<uint32_t> la, lb, pairs;
+    GenPairs(*this, pa, sp, p, n, la, lb, pairs);
+    const uint32_t npairs = (uint32_t)(pairs.size() / 2);
+    if (npairs == 0) return;
+    uint32_t* dp = Pairs(npairs);
+    CudaCheck(cudaMemcpyAsync(dp, pairs.data(), pairs.size() * 4, cudaMemcpyHostToDevice, stream), "pairs upload");
+    const uint32_t ns = (b1 - b0 + skip - 1) / skip;
+    const uint32_t offa = sys.sp_off[pa.sa], offb = sys.sp_off[pa.sb];
+    const double tau = sys.tau;
+    // pair_action_class.h:135-155 central differences on the first particle's bead, links to
+    // b + skip and to b - skip (+M), eps = 1e-4. The Bare action has no long-range gradient.
+    SumItems<3>(*this, (uint64_t)ns * npairs * 2, [=] __device__(uint64_t i, double* v) {
+        const uint32_t link = (uint32_t)(i & 1u);
+        const uint64_t ii = i >> 1;
+        const uint32_t j = (uint32_t)(ii / npairs), q = (uint32_t)(ii % npairs);
+        const uint32_t braw = b0 + j * skip;
+        const uint32_t bi = BeadLoop(braw, M);
+        const uint32_t bo = link == 0 ? BeadLoop(braw + skip, M) : BeadLoop(braw - skip + M, M);
+        double A0[3], C0[3], A1[3], C1[3];
+        LoadBead(pos, np, n_d, bi, offb + dp[2 * q + 1], A0);
+        LoadBead(pos, np, n_d, bi, offa + dp[2 * q], C0);
+        LoadBead(pos, np, n_d, bo, offb + dp[2 * q + 1], A1);
+        LoadBead(pos, np, n_d, bo, offa + dp[2 * q], C1);
+        const double eps = 1.e-4;
+        for (uint32_t d = 0; d < 3; ++d) {
+            if (d >= n_d) {
+                v[d] = 0.;
+                continue;
+            }
+            const double c0 = C0[d];
+            double r, rp, s;
+            C0[d] = c0 + eps;
+            DrDrpDrrp(A0, C0, A1, C1, n_d, L, iL, r, rp, s);
+            const double f1 = PairU(pa, r, rp, level, tau);
+            C0[d] = c0 - eps;
+            DrDrpDrrp(A0, C0, A1, C1, n_d, L, iL, r, rp, s);
+            const double f2 = PairU(pa, r, rp, level, tau);
+            C0[d] = c0;
+            v[d] = (f1 - f2) / (2. * eps);
+        }
+    }, g);
+}
+
+double Context::DActionDBeta(uint32_t ai) {
+    if (ai >= actions.size()) throw PimcError(kErrArg, "action index out of range");
+    ActionHost& ah = actions[ai];
+    const double* pos = sys.pos;
+    const uint32_t M = sys.M, n_d = sys.n_d, np = sys.n_pad;
+    const double L = sys.L, iL = sys.iL;
+    double out = 0.;
+    if (ah.kind == 0) {
+        // kinetic_class.h:35-45
+        const KineticDev k = sys.kinetic[ah.index];
+        const uint32_t N = sys.sp_n[k.species], off = sys.sp_off[k.species];
+        SumItems<1>(*this, (uint64_t)N * M, [=] __device__(uint64_t i, double* v) {
+            const uint32_t g = off + (uint32_t)(i / M), b = (uint32_t)(i % M), bn = (b + 1) % M;
+            double tot = 0., r2 = 0.;
+            for (uint32_t d = 0; d < n_d; ++d) {
+                const double x = MinImage(PosAt(pos, np, b, d, g) - PosAt(pos, np, bn, d, g), L, iL);
+                if (k.has_images) tot -= EvalCubic(k.d_image_d_tau, x);
+                r2 += x * x;
+            }
+            v[0] = tot - r2 * k.i4ltt;
+        }, &out);
+        return k.d_action_d_beta_const + out;
+    }
+    if (ah.kind == 1) {
+        const TrapDev t = sys.trap[ah.index];
+        const uint32_t N = sys.sp_n[t.species], off = sys.sp_off[t.species];
+        SumItems<1>(*this, (uint64_t)N * M, [=] __device__(uint64_t i, double* v) {
+            const uint32_t g = off + (uint32_t)(i / M), b = (uint32_t)(i % M);
+            double s = 0.;
+            for (uint32_t d = 0; d < n_d; ++d) {
+                const double x = PosAt(pos, np, b, d, g);
+                s += x * x;
+            }
+            v[0] = s;
+        }, &out);
+        return t.cofactor_b * out;
+    }
+    // pair_action_class.h:241-264 with the constant-action cache.
+    const PairDev pa = sys.pair[ah.index];
+    if (pa.is_constant && !ah.is_first_time) return ah.dUdB_constant;
+    const uint32_t na = sys.sp_n[pa.sa], nb = sys.sp_n[pa.sb], offa = sys.sp_off[pa.sa], offb = sys.sp_off[pa.sb];
+    const bool hom = pa.sa == pa.sb;
+    SumItems<1>(*this, (uint64_t)na * nb * M, [=] __device__(uint64_t i, double* v) {
+        const uint32_t b = (uint32_t)(i % M);
+        const uint64_t pq = i / M;
+        const uint32_t x = (uint32_t)(pq / nb), y = (uint32_t)(pq % nb);
+        v[0] = 0.;
+        if (hom && y <= x) return;
+        const uint32_t bn = (b + 1) % M;
+        double A0[3], C0[3], A1[3], C1[3];
+        LoadBead(pos, np, n_d, b, offb + y, A0);
+        LoadBead(pos, np, n_d, b, offa + x, C0);
+        LoadBead(pos, np, n_d, bn, offb + y, A1);
+        LoadBead(pos, np, n_d, bn, offa + x, C1);
+        double r, rp, s;
+        DrDrpDrrp(A0, C0, A1, C1, n_d, L, iL, r, rp, s);
+        v[0] = PairV(pa, r, rp);
+    }, &out);
+    if (pa.use_long_range) {
+        const uint32_t K = sys.K;
+        const double2* ra = sys.rho_k + (size_t)sys.sp_rho[pa.sa] * M * K;
+        const double2* rb = sys.rho_k + (size_t)sys.sp_rho[pa.sb] * M * K;
+        const double* vk = pa.v_long_k;
+        double lr = 0.;
+        SumItems<1>(*this, (uint64_t)K * M, [=] __device__(uint64_t i, double* v) {
+            const uint32_t k = (uint32_t)(i / M), b = (uint32_t)(i % M);
+            const double2 a = ra[(size_t)b * K + k], c = rb[(size_t)b * K + k];
+            v[0] = (a.x * c.x + a.y * c.y) * vk[k];
+        }, &lr);
+        if (!hom) lr *= 2.;
+        out += lr + pa.v_long_k_0 + pa.v_long_r_0;
+    }
+    if (ah.is_first_time) {
+        ah.is_first_time = false;
+        ah.dUdB_constant = out;
+    }
+    return out;
+}
+
+double Context::Potential(uint32_t ai) {
+    if (ai >= actions.size()) throw PimcError(kErrArg, "action index out of range");
+    ActionHost& ah = actions[ai];
+    if (ah.kind != 2) return 0.;  // Kinetic and Trap keep Action::Potential() = 0 (action_class.h:52)
+    const PairDev pa = sys.pair[ah.index];
+    if (pa.is_constant && !ah.is_first_time) return ah.potential_constant;
+    const double* pos = sys.pos;
+    const uint32_t M = sys.M, n_d = sys.n_d, np = sys.n_pad;
+    const double L = sys.L, iL = sys.iL;
+    const uint32_t na = sys.sp_n[pa.sa], nb = sys.sp_n[pa.sb], offa = sys.sp_off[pa.sa], offb = sys.sp_off[pa.sb];
+    const bool hom = pa.sa == pa.sb;
+    double out = 0.;
+    SumItems<1>(*this, (uint64_t)na * nb * M, [=] __device__(uint64_t i, double* v) {
+        const uint32_t b = (uint32_t)(i % M);
+        const uint64_t pq = i / M;
+        const uint32_t x = (uint32_t)(pq / nb), y = (uint32_t)(pq % nb);
+        v[0] = 0.;
+        if (hom && y <= x) return;
+        const uint32_t bn = (b + 1) % M;
+        double a[3], c[3];
+        LoadBead(pos, np, n_d, b, offa + x, a);
+        LoadBead(pos, np, n_d, b, offb + y, c);
+        const double r = DistMinImage(a, c, n_d, L, iL);
+        LoadBead(pos, np, n_d, bn, offa + x, a);
+        LoadBead(pos, np, n_d, bn, offb + y, c);
+        const double rp = DistMinImage(a, c, n_d, L, iL);
+        v[0] = PairV(pa, r, rp);
+    }, &out);
+    if (pa.use_long_range) {
+        const uint32_t K = sys.K;
+        const double2* ra = sys.rho_k + (size_t)sys.sp_rho[pa.sa] * M * K;
+        const double2* rb = sys.rho_k + (size_t)sys.sp_rho[pa.sb] * M * K;
+        const double* vk = pa.v_long_k;
+        double lr = 0.;
+        SumItems<1>(*this, (uint64_t)K * M, [=] __device__(uint64_t i, double* v) {
+            const uint32_t k = (uint32_t)(i / M), b = (uint32_t)(i % M);
+            const double2 a = ra[(size_t)b * K + k], c = rb[(size_t)b * K + k];
+            v[0] = (a.x * c.x + a.y * c.y) * vk[k];
+        }, &lr);
+        if (!hom) lr *= 2.;
+        out += lr + pa.v_long_k_0 + pa.v_long_r_0;
+    }
+    if (ah.is_first_time) {
+        ah.is_first_time = false;
+        ah.potential_constant = out;
+    }
+    return out;
+}
+
+double Context::VirialEnergy(uint32_t ai, double window) {
+    if (ai >= actions.size()) throw PimcError(kErrArg, "action index out of range");
+    const ActionHost& ah = actions[ai];
+    if (ah.kind != 0) return DActionDBeta(ai);  // action_class.h:40
+    // kinetic_class.h:48-102 with each window sum formed directly.
+    const KineticDev k = sys.kinetic[ah.index];
+    const uint32_t N = sys.sp_n[k.species], off = sys.sp_off[k.species];
+    const double* pos = sys.pos;
+    const uint32_t M = sys.M, n_d = sys.n_d, np = sys.n_pad;
+    const double L = sys.L, iL = sys.iL;
+    const uint32_t W = window < 1. ? 1u : (uint32_t)std::ceil(window);
+    double out = 0.;
+    SumItems<1>(*this, (uint64_t)N * M, [=] __device__(uint64_t i, double* v) {
+        const uint32_t g = off + (uint32_t)(i / M), b = (uint32_t)(i % M);
+        double dr1[3] = {0., 0., 0.}, drl[3] = {0., 0., 0.};
+        for (uint32_t d = 0; d < n_d; ++d) dr1[d] = MinImage(PosAt(pos, np, (b + 1) % M, d, g) - PosAt(pos, np, b, d, g), L, iL);
+        for (uint32_t w = 0; w < W; ++w) {
+            const uint32_t x = (b + w) % M, y = (b + w + 1) % M;
+            for (uint32_t d = 0; d < n_d; ++d) drl[d] += MinImage(PosAt(pos, np, y, d, g) - PosAt(pos, np, x, d, g), L, iL);
+        }
+        double dot = 0.;
+        for (uint32_t d = 0; d < n_d; ++d) dot += drl[d] * dr1[d];
+        v[0] = dot;
+    }, &out);
+    return k.d_action_d_beta_const / window - out * k.i4lt / (window * sys.tau);
+}
+
+double Context::VirialCentroid(uint32_t s) {
+    // energy_class.h:81-94: sum over particles and slices of grad S(b, b+1, {p}) . (r_pb - r_p0)
+    // for every non-kinetic action; only pair actions have gradients here.
+    const double* pos = sys.pos;
+    const uint32_t M = sys.M, n_d = sys.n_d, np = sys.n_pad;
+    const double L = sys.L, iL = sys.iL, tau = sys.tau;
+    double total = 0.;
+    for (const auto& ah : actions) {
+        if (ah.kind != 2 || ah.is_importance_weight) continue;
+        const PairDev pa = sys.pair[ah.index];
+        if (pa.is_constant) continue;
+        if (pa.sa != s && pa.sb != s) continue;
+        const uint32_t ns = sys.sp_n[s];
+        // Partners: homologous q != p (pair (p, q)); s == sa: q in sb (pair (p, q));
+        // s == sb: q in sa (pair (q, p), the gradient is taken on q).
+        const bool hom = pa.sa == pa.sb;
+        const bool s_is_a = pa.sa == s;
+        const uint32_t other = hom ? s : (s_is_a ? pa.sb : pa.sa);
+        const uint32_t nq = sys.sp_n[other];
+        const uint32_t offs = sys.sp_off[s], offo = sys.sp_off[other];
+        double part = 0.;
+        SumItems<1>(*this, (uint64_t)ns * M * nq * 2, [=] __device__(uint64_t i, double* v) {
+            const uint32_t link = (uint32_t)(i & 1u);
+            uint64_t ii = i >> 1;
+            const uint32_t q = (uint32_t)(ii % nq);
+            ii /= nq;
+            const uint32_t b = (uint32_t)(ii % M), pp = (uint32_t)(ii / M);
+            v[0] = 0.;
+            if (hom && q == pp) return;
+            // first (species a) and second (species b) particle of the pair
+            const uint32_t ga = (hom || s_is_a) ? offs + pp : offo + q;
+            const uint32_t gb = (hom || s_is_a) ? offo + q : offs + pp;
+            const uint32_t bo = link == 0 ? (b + 1) % M : (b + M - 1) % M;
+            double A0[3], C0[3], A1[3], C1[3];
+            LoadBead(pos, np, n_d, b, gb, A0);
+            LoadBead(pos, np, n_d, b, ga, C0);
+            LoadBead(pos, np, n_d, bo, gb, A1);
+            LoadBead(pos, np, n_d, bo, ga, C1);
+            const double eps = 1.e-4;
+            double dot = 0.;
+            for (uint32_t d = 0; d < n_d; ++d) {
+                const double c0 = C0[d];
+                double r, rp, sd;
+                C0[d] = c0 + eps;
+                DrDrpDrrp(A0, C0, A1, C1, n_d, L, iL, r, rp, sd);
+                const double f1 = PairU(pa, r, rp, 0, tau);
+                C0[d] = c0 - eps;
+                DrDrpDrrp(A0, C0, A1, C1, n_d, L, iL, r, rp, sd);
+                const double f2 = PairU(pa, r, rp, 0, tau);
+                C0[d] = c0;
+                const double gd = (f1 - f2) / (2. * eps);
+                const double dr = MinImage(PosAt(pos, np, b, d, offs + pp) - PosAt(pos, np, 0, d, offs + pp), L, iL);
+                dot += gd * dr;
+            }
+            v[0] = dot;
+        }, &part);
+        total += part;
+    }
+    return total;
+}
+
+void Context::ObservableAccumulate(uint32_t oi) {
+    if (oi >= observables.size()) throw PimcError(kErrArg, "observable index out of range");
+    ObservableHost& o = observables[oi];
+    if (o.kind == 3) return;
+    if (o.kind == 0) {
+        // energy_class.h:133-161 (sign and importance weight are 1 for these species)
+        const double cof = 1.;
+        if (o.use_thermal) {
+            for (size_t i = 0; i < actions.size(); ++i)
+                if (!actions[i].is_importance_weight) o.energies[i] += cof * DActionDBeta((uint32_t)i);
+        } else if (o.use_virial) {
+            double ke = 0.;
+            for (size_t i = 0; i < actions.size(); ++i)
+                if (actions[i].kind == 0) ke += VirialEnergy((uint32_t)i, (double)o.virial_window);
+            for (uint32_t s = 0; s < sys.S; ++s) {
+                if (!(sys.sp_lambda[s] > 0.)) continue;
+                ke += VirialCentroid(s) / (2. * sys.tau);
+                for (size_t i = 0; i < actions.size(); ++i)
+                    if (actions[i].kind == 0)
+                        for (uint32_t x : actions[i].species_list)
+                            if (x == s) o.energies[i] += cof * ke;
+            }
+            for (size_t i = 0; i < actions.size(); ++i)
+                if (!actions[i].is_importance_weight && actions[i].kind != 0) o.energies[i] += cof * DActionDBeta((uint32_t)i);
+        }
+        if (o.measure_potential)
+            for (size_t i = 0; i < actions.size(); ++i)
+                if (!actions[i].is_importance_weight) o.potentials[i] += cof * Potential((uint32_t)i);
+    } else if (o.kind == 1) {
+        const int blocks = n_sm * 2;
+        PairCorrelationKernel<<<blocks, 256, o.n_r * sizeof(unsigned int), stream>>>(sys, o.sa, o.sb, o.r_min, o.d_ir, o.n_r,
+                                                                                    o.hist->as<unsigned long long>());
+        CudaCheck(cudaGetLastError(), "g(r) launch");
+    } else if (o.kind == 2) {
+        if (sys.K) {
+            if (!kmag_dev_) {  // |k| of every stored k-vector, uploaded on first use
+                kmag_dev_.reset(new DeviceBuffer(sys.K * sizeof(double)));
+                CudaCheck(cudaMemcpy(kmag_dev_->ptr, kmags.data(), sys.K * sizeof(double), cudaMemcpyHostToDevice), "kmag upload");
+            }
+            const double* dk = kmag_dev_->as<double>();
+            StructureFactorKernel<<<(sys.K + 255) / 256, 256, 0, stream>>>(sys, dk, o.k_cut, (uint32_t)sys.sp_rho[o.sa], (uint32_t)sys.sp_rho[o.sb],
+                                                                           o.sk->as<double>());
+            CudaCheck(cudaGetLastError(), "S(k) launch");
+        }
+    }
+    o.n_measure++;
+}
+
+std::vector<double> Context::ObservableBlock(uint32_t oi) {
+    if (oi >= observables.size()) throw PimcError(kErrArg, "observable index out of range");
+    ObservableHost& o = observables[oi];
+    std::vector<double> out;
+    if (o.kind == 3 || o.n_measure == 0) return out;
+    Sync();
+    if (o.kind == 0) {
+        // energy_class.h:232-253
+        const double norm = (double)sys.M * o.n_measure;
+        double E = 0.;
+        std::vector<double> e(o.energies.size());
+        for (size_t i = 0; i < e.size(); ++i) {
+            e[i] = o.energies[i] / norm;
+            E += e[i];
+        }
+        out.push_back(E);
+        out.insert(out.end(), e.begin(), e.end());
+        if (o.measure_potential) {
+            double V = 0.;
+            std::vector<double> v(o.potentials.size());
+            for (size_t i = 0; i < v.size(); ++i) {
+                v[i] = o.potentials[i] / norm;
+                V += v[i];
+            }
+            out.push_back(V);
+            out.insert(out.end(), v.begin(), v.end());
+        }
+        std::fill(o.energies.begin(), o.energies.end(), 0.);
+        std::fill(o.potentials.begin(), o.potentials.end(), 0.);
+    } else if (o.kind == 1) {
+        // pair_correlation_class.h:89-123
+        std::vector<unsigned long long> h(o.n_r);
+        CudaCheck(cudaMemcpy(h.data(), o.hist->ptr, o.n_r * sizeof(unsigned long long), cudaMemcpyDeviceToHost), "read g(r)");
+        CudaCheck(cudaMemset(o.hist->ptr, 0, o.n_r * sizeof(unsigned long long)), "reset g(r)");
+        const double na = sys.sp_n[o.sa], nb = sys.sp_n[o.sb];
+        const double norm = o.sa == o.sb ? 0.5 * o.n_measure * na * (nb - 1) * sys.M / sys.vol : (double)o.n_measure * na * nb * sys.M / sys.vol;
+        out.resize(o.n_r);
+        for (uint32_t i = 0; i < o.n_r; ++i) {
+            const double r1 = o.r_min + i * o.dr;
+            const double r2 = (i < o.n_r - 1) ? o.r_min + (i + 1) * o.dr : (2. * r1 - (o.r_min + (i - 1) * o.dr));
+            double bin_vol;
+            if (sys.n_d == 3) bin_vol = 4. * M_PI / 3. * (r2 * r2 * r2 - r1 * r1 * r1);
+            else if (sys.n_d == 2) bin_vol = M_PI * (r2 * r2 - r1 * r1);
+            else bin_vol = r2 - r1;
+            out[i] = (double)h[i] / (bin_vol * norm);
+        }
+    } else if (o.kind == 2) {
+        std::vector<double> sk(sys.K);
+        if (sys.K) {
+            CudaCheck(cudaMemcpy(sk.data(), o.sk->ptr, sys.K * sizeof(double), cudaMemcpyDeviceToHost), "read S(k)");
+            CudaCheck(cudaMemset(o.sk->ptr, 0, sys.K * sizeof(double)), "reset S(k)");
+        }
+        const double norm = (double)o.n_measure * sys.M * sys.sp_n[o.sa] * sys.sp_n[o.sb];
+        out.resize(sys.K);
+        for (uint32_t k = 0; k < sys.K; ++k) out[k] = sk[k] / norm;
+    }
+    o.n_measure = 0;
+    return out;
+}
+
+}  // namespace pimc
