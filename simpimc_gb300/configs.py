@@ -115,8 +115,10 @@ def electron_gas(workdir, *, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_unit
   </Algorithm>
 </Input>
 """
+    # Classical start as the reference's init_type="Random" (species_class.h:262-272): one uniform
+    # point in the box per particle, shared by all of its beads.
     rng = np.random.default_rng(seed if path_seed is None else path_seed)
-    path = rng.uniform(-L / 2, L / 2, size=(n_part, n_bead, 3))
+    path = np.repeat(rng.uniform(-L / 2, L / 2, size=(n_part, 1, 3)), n_bead, axis=1)
     return xml, path
 
 
