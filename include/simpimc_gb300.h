@@ -68,6 +68,14 @@ int pimc_get_kvecs(pimc_ctx* ctx, double* out);
 /* Action::GetAction (action_class.h:43) */
 int pimc_get_action(pimc_ctx* ctx, uint32_t action, uint32_t b0, uint32_t b1, const uint32_t* species, const uint32_t* particles,
                     uint32_t n_particles, uint32_t level, int mode, double* out);
+/* Same value as pimc_get_action for a pair action, computed without any device allocation
+ * during the call: for host programs that give all GPU memory to their own pool or may not
+ * allocate where they call from. All temporaries live in one 4 MiB array fixed in the library
+ * (held on every GPU that loads it); larger requests fail with PIMC_ERR_ARG. Calls share that
+ * array, so calls whose GPU work overlaps race; the first call on a device looks up the array's
+ * address and should come before any stream capture. No counterpart in the reference. */
+int pimc_get_action_noalloc(pimc_ctx* ctx, uint32_t action, uint32_t b0, uint32_t b1, const uint32_t* species,
+                            const uint32_t* particles, uint32_t n_particles, uint32_t level, int mode, double* out);
 /* Action::GetActionGradient (action_class.h:46); out has n_d entries. */
 int pimc_get_action_gradient(pimc_ctx* ctx, uint32_t action, uint32_t b0, uint32_t b1, const uint32_t* species,
                              const uint32_t* particles, uint32_t n_particles, uint32_t level, int mode, double* out);

@@ -4,12 +4,7 @@
 #include <string>
 
 #include "../../include/simpimc_gb300.h"
-#include "framework/context.h"
-
-struct pimc_ctx {
-    std::unique_ptr<pimc::Context> c;
-    std::string err;
-};
+#include "capi_internal.h"
 
 namespace {
 
