@@ -25,7 +25,7 @@ def build(force: bool = False) -> Path:
     LIB.parent.mkdir(exist_ok=True)
     if force or not LIB.exists() or any(d.stat().st_mtime > LIB.stat().st_mtime for d in DEPS):
         cxx = os.environ.get("CXX") or shutil.which("g++") or "c++"
-        cmd = [cxx, "-std=c++17", "-O3", "-fPIC", "-shared", "-fopenmp", str(SRC), "-o", str(LIB)]
+        cmd = [cxx, "-std=c++17", "-O3", "-ffp-contract=off", "-fPIC", "-shared", str(SRC), "-o", str(LIB)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"oracle build failed:\n{r.stderr}")

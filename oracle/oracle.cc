@@ -74,14 +74,73 @@ struct Stream {
     }
 };
 
-static double u53(uint32_t a, uint32_t b) { return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0); }
 static uint32_t uidx(uint32_t w, uint32_t n) { return (uint32_t)(((uint64_t)w * n) >> 32); }
-static void boxmuller(const RNG4& w, double& z0, double& z1) {
-    double u0 = u53(w.w[0], w.w[1]), u1 = u53(w.w[2], w.w[3]);
-    double r = std::sqrt(-2.0 * std::log(1.0 - u0));
-    double th = 6.283185307179586 * u1;
-    z0 = r * std::cos(th);
-    z1 = r * std::sin(th);
+
+// The move's exactly specified binary32 transforms (this file is compiled with
+// -ffp-contract=off; every fused multiply-add is an explicit fmaf): a 24-bit uniform, the
+// logarithm by m in [sqrt(1/2), sqrt(2)) and 2 atanh((m-1)/(m+1)), sin/cos of 2 pi u by quadrant
+// reduction and Taylor polynomials, Box-Muller normals.
+static float u24(uint32_t w) { return (float)(w >> 8) * (1.0f / 16777216.0f); }
+
+static float logf_spec(float x) {
+    if (x == 0.f) return -INFINITY;
+    uint32_t b;
+    std::memcpy(&b, &x, 4);
+    int e = (int)((b >> 23) & 0xffu) - 126;
+    uint32_t mb = (b & 0x007fffffu) | 0x3f000000u;
+    float m;
+    std::memcpy(&m, &mb, 4);
+    if (m < 0.70710678f) {
+        m = m + m;
+        e -= 1;
+    }
+    const float f = m - 1.0f;
+    const float s = f / (2.0f + f);
+    const float s2 = s * s;
+    float p = std::fmaf(s2, 1.0f / 9.0f, 1.0f / 7.0f);
+    p = std::fmaf(s2, p, 1.0f / 5.0f);
+    p = std::fmaf(s2, p, 1.0f / 3.0f);
+    p = s2 * p;
+    const float two_s = s + s;
+    const float lm = std::fmaf(two_s, p, two_s);
+    const float ef = (float)e;
+    return std::fmaf(ef, 0.693145751953125f, std::fmaf(ef, 1.428606765330187e-06f, lm));
+}
+
+static void sincos2pi_spec(float u, float& s, float& c) {
+    const float v = u * 4.0f;
+    const float q = std::floor(v);
+    const float f = v - q;
+    const int qi = (int)q & 3;
+    const float t = (f - 0.5f) * 1.57079637f;
+    const float t2 = t * t;
+    float ps = std::fmaf(t2, 1.0f / 362880.0f, -1.0f / 5040.0f);
+    ps = std::fmaf(t2, ps, 1.0f / 120.0f);
+    ps = std::fmaf(t2, ps, -1.0f / 6.0f);
+    ps = t2 * ps;
+    const float st = std::fmaf(t, ps, t);
+    float pc = std::fmaf(t2, -1.0f / 3628800.0f, 1.0f / 40320.0f);
+    pc = std::fmaf(t2, pc, -1.0f / 720.0f);
+    pc = std::fmaf(t2, pc, 1.0f / 24.0f);
+    pc = std::fmaf(t2, pc, -0.5f);
+    const float ct = std::fmaf(t2, pc, 1.0f);
+    const float sp = (st + ct) * 0.70710678f;
+    const float cp = (ct - st) * 0.70710678f;
+    switch (qi) {
+        case 0: s = sp; c = cp; break;
+        case 1: s = cp; c = -sp; break;
+        case 2: s = -sp; c = -cp; break;
+        default: s = -cp; c = sp; break;
+    }
+}
+
+static void boxmuller(uint32_t w0, uint32_t w1, float& z0, float& z1) {
+    const float u0 = u24(w0), u1 = u24(w1);
+    const float r = std::sqrt(-2.0f * logf_spec(1.0f - u0));
+    float s, c;
+    sincos2pi_spec(u1, s, c);
+    z0 = r * c;
+    z1 = r * s;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1058,11 +1117,12 @@ struct Bisect : Move {
                 }
                 // New sampling
                 {
-                    double z[4];
-                    boxmuller(st.block(1u + 2u * mid_counter), z[0], z[1]);
-                    boxmuller(st.block(2u + 2u * mid_counter), z[2], z[3]);
+                    float z[4];
+                    RNG4 wz = st.block(1u + mid_counter);
+                    boxmuller(wz.w[0], wz.w[1], z[0], z[1]);
+                    boxmuller(wz.w[2], wz.w[3], z[2], z[3]);
                     mid_counter++;
-                    for (uint32_t d = 0; d < n_d; ++d) delta[d] = 0. + sigma * z[d];
+                    for (uint32_t d = 0; d < n_d; ++d) delta[d] = 0. + sigma * (double)z[d];
                     path.PutInBox(delta);
                     const double* ra = path.GetRMode(*species, p_i, ba, NEW_MODE);
                     const double* rc = path.GetRMode(*species, p_i, bc, NEW_MODE);
@@ -1084,9 +1144,8 @@ struct Bisect : Move {
             double log_sample_ratio = -new_lsp + old_lsp;
             double current = new_action - old_action;
             double log_accept = log_sample_ratio - current + prev_action_change;
-            RNG4 wu = st.block(1u + 2u * (n_bisect_beads - 1u) + (n_level - 1u - (uint32_t)level_i));
-            double u = u53(wu.w[0], wu.w[1]);
-            if (log_accept < std::log(u)) return false;
+            RNG4 wu = st.block(1u + (n_bisect_beads - 1u) + (n_level - 1u - (uint32_t)level_i));
+            if (log_accept < (double)logf_spec(u24(wu.w[0]))) return false;
             prev_action_change = current;
         }
         return true;

@@ -78,7 +78,10 @@ SIGNATURES = {
     "pimc_set_sweep_grid": (C.c_int, [_P, C.c_int]),
     "pimc_set_timeout_ns": (C.c_int, [_P, C.c_uint64]),
     "pimc_stream": (_P, [_P]),
+    "pimc_sweep_timing": (C.c_int, [_P, C.c_int, _U64P]),
 }
+
+SWEEP_PHASES = ("segment+rng", "sampling", "level terms", "grid work", "grid barrier", "final sum", "decision", "commit")
 
 _lib = None
 
@@ -165,6 +168,13 @@ class Simulation:
 
     def synchronize(self):
         self._check(self._lib.pimc_synchronize(self._h))
+
+    def sweep_timing(self, enable: int = -1) -> dict:
+        """Per-phase cycles of the sweep kernel's block 0 since the last reset (tracing aid);
+        enable=1/0 switches recording on/off and resets the sums."""
+        out = np.zeros(len(SWEEP_PHASES), dtype=np.uint64)
+        self._check(self._lib.pimc_sweep_timing(self._h, enable, out.ctypes.data_as(_U64P)))
+        return dict(zip(SWEEP_PHASES, (int(x) for x in out)))
 
     # -- path -----------------------------------------------------------------------------------
     @property

@@ -10,9 +10,9 @@
 //
 // Stream layout of one bisection attempt with n_bisect = 2^n_level beads:
 //   block 0                       words 0,1 -> particle index, first bead (multiply-high ranges)
-//   blocks 1+2i, 2+2i             3 normal deviates for the i-th resampled bead, in generation
+//   block 1+i                     3 normal deviates for the i-th resampled bead, in generation
 //                                 order (top level first, left to right within a level)
-//   block 1+2(n_bisect-1)+li      words 0,1 -> acceptance uniform of level li (0 = top level)
+//   block 1+(n_bisect-1)+li       word 0 -> acceptance uniform of level li (0 = top level)
 #pragma once
 
 #include <cmath>
@@ -87,26 +87,127 @@ struct MoveStream {
     }
 };
 
-/// Two standard normal deviates from one Philox block (Box-Muller on 53-bit uniforms).
-PIMC_HD void BoxMuller(const Philox4& w, double& z0, double& z1) {
-    const double u0 = Uniform53(w.v[0], w.v[1]);
-    const double u1 = Uniform53(w.v[2], w.v[3]);
-    const double r = sqrt(-2.0 * log(1.0 - u0));
-    const double th = 6.283185307179586 * u1;
-    z0 = r * cos(th);
-    z1 = r * sin(th);
+// ---------------------------------------------------------------------------------------------
+// Exactly specified single-precision transforms. Every operation below is an IEEE-754 binary32
+// operation with round-to-nearest and no contraction (explicit intrinsics on the device; the CPU
+// checker compiles its restatement with -ffp-contract=off), so the GPU and any CPU produce the
+// same bits. Methods: logarithm by reduction to m in [sqrt(1/2), sqrt(2)) and the series
+// log m = 2 atanh((m-1)/(m+1)); sine/cosine of 2*pi*u by quadrant reduction in turns and Taylor
+// polynomials on [-pi/4, pi/4]; normals by the Box-Muller transform.
+
+#if defined(__CUDA_ARCH__)
+#define PIMC_FADD(a, b) __fadd_rn(a, b)
+#define PIMC_FSUB(a, b) __fsub_rn(a, b)
+#define PIMC_FMUL(a, b) __fmul_rn(a, b)
+#define PIMC_FDIV(a, b) __fdiv_rn(a, b)
+#define PIMC_FFMA(a, b, c) __fmaf_rn(a, b, c)
+#define PIMC_FSQRT(a) __fsqrt_rn(a)
+#else
+#define PIMC_FADD(a, b) ((a) + (b))
+#define PIMC_FSUB(a, b) ((a) - (b))
+#define PIMC_FMUL(a, b) ((a) * (b))
+#define PIMC_FDIV(a, b) ((a) / (b))
+#define PIMC_FFMA(a, b, c) fmaf(a, b, c)
+#define PIMC_FSQRT(a) sqrtf(a)
+#endif
+
+PIMC_HD uint32_t FloatBits(float x) {
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(x);
+#else
+    uint32_t b;
+    __builtin_memcpy(&b, &x, 4);
+    return b;
+#endif
 }
 
-/// The three normal deviates of resampled bead i of an attempt.
-PIMC_HD void BisectNormals(const MoveStream& s, uint32_t i, double z[3]) {
-    double z3;
-    BoxMuller(s.Block(1u + 2u * i), z[0], z[1]);
-    BoxMuller(s.Block(2u + 2u * i), z[2], z3);
+PIMC_HD float BitsFloat(uint32_t b) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(b);
+#else
+    float x;
+    __builtin_memcpy(&x, &b, 4);
+    return x;
+#endif
 }
 
-PIMC_HD double BisectAcceptUniform(const MoveStream& s, uint32_t n_bisect, uint32_t level_index) {
-    Philox4 w = s.Block(1u + 2u * (n_bisect - 1u) + level_index);
-    return Uniform53(w.v[0], w.v[1]);
+/// 24-bit uniform in [0, 1), exact in binary32.
+PIMC_HD float U24(uint32_t w) { return (float)(w >> 8) * (1.0f / 16777216.0f); }
+
+/// Natural logarithm of a normal binary32 x in (0, 1]; -inf for 0.
+PIMC_HD float LogF(float x) {
+    if (x == 0.f) return -INFINITY;
+    const uint32_t b = FloatBits(x);
+    int e = (int)((b >> 23) & 0xffu) - 126;  // x = m 2^e, m in [1/2, 1)
+    float m = BitsFloat((b & 0x007fffffu) | 0x3f000000u);
+    if (m < 0.70710678f) {
+        m = PIMC_FADD(m, m);
+        e -= 1;
+    }
+    const float f = PIMC_FSUB(m, 1.0f);  // exact
+    const float s = PIMC_FDIV(f, PIMC_FADD(2.0f, f));
+    const float s2 = PIMC_FMUL(s, s);
+    float p = PIMC_FFMA(s2, 1.0f / 9.0f, 1.0f / 7.0f);
+    p = PIMC_FFMA(s2, p, 1.0f / 5.0f);
+    p = PIMC_FFMA(s2, p, 1.0f / 3.0f);
+    p = PIMC_FMUL(s2, p);
+    const float two_s = PIMC_FADD(s, s);
+    const float lm = PIMC_FFMA(two_s, p, two_s);
+    const float ef = (float)e;
+    return PIMC_FFMA(ef, 0.693145751953125f, PIMC_FFMA(ef, 1.428606765330187e-06f, lm));
+}
+
+/// sin and cos of 2 pi u for u in [0, 1).
+PIMC_HD void SinCos2PiF(float u, float& s, float& c) {
+    const float v = PIMC_FMUL(u, 4.0f);
+    const float q = floorf(v);
+    const float f = PIMC_FSUB(v, q);
+    const int qi = (int)q & 3;
+    const float t = PIMC_FMUL(PIMC_FSUB(f, 0.5f), 1.57079637f);
+    const float t2 = PIMC_FMUL(t, t);
+    float ps = PIMC_FFMA(t2, 1.0f / 362880.0f, -1.0f / 5040.0f);
+    ps = PIMC_FFMA(t2, ps, 1.0f / 120.0f);
+    ps = PIMC_FFMA(t2, ps, -1.0f / 6.0f);
+    ps = PIMC_FMUL(t2, ps);
+    const float st = PIMC_FFMA(t, ps, t);
+    float pc = PIMC_FFMA(t2, -1.0f / 3628800.0f, 1.0f / 40320.0f);
+    pc = PIMC_FFMA(t2, pc, -1.0f / 720.0f);
+    pc = PIMC_FFMA(t2, pc, 1.0f / 24.0f);
+    pc = PIMC_FFMA(t2, pc, -0.5f);
+    const float ct = PIMC_FFMA(t2, pc, 1.0f);
+    const float sp = PIMC_FMUL(PIMC_FADD(st, ct), 0.70710678f);  // sin(pi/4 + t)
+    const float cp = PIMC_FMUL(PIMC_FSUB(ct, st), 0.70710678f);  // cos(pi/4 + t)
+    switch (qi) {
+        case 0: s = sp; c = cp; break;
+        case 1: s = cp; c = -sp; break;
+        case 2: s = -sp; c = -cp; break;
+        default: s = -cp; c = sp; break;
+    }
+}
+
+/// Two standard normal deviates from two Philox words (Box-Muller on 24-bit uniforms; the
+/// radius is bounded by sqrt(48 ln 2) = 5.77, a tail cut at probability 1e-8).
+PIMC_HD void BoxMullerF(uint32_t w0, uint32_t w1, float& z0, float& z1) {
+    const float u0 = U24(w0), u1 = U24(w1);
+    const float r = PIMC_FSQRT(PIMC_FMUL(-2.0f, LogF(PIMC_FSUB(1.0f, u0))));
+    float s, c;
+    SinCos2PiF(u1, s, c);
+    z0 = PIMC_FMUL(r, c);
+    z1 = PIMC_FMUL(r, s);
+}
+
+/// The three normal deviates of resampled bead i of an attempt (one Philox block per bead).
+PIMC_HD void BisectNormals(const MoveStream& st, uint32_t i, float z[3]) {
+    const Philox4 w = st.Block(1u + i);
+    float z3;
+    BoxMullerF(w.v[0], w.v[1], z[0], z[1]);
+    BoxMullerF(w.v[2], w.v[3], z[2], z3);
+}
+
+/// log of the acceptance uniform of level index li (0 = top level) of an attempt.
+PIMC_HD float BisectLogU(const MoveStream& st, uint32_t n_bisect, uint32_t level_index) {
+    const Philox4 w = st.Block(1u + (n_bisect - 1u) + level_index);
+    return LogF(U24(w.v[0]));
 }
 
 }  // namespace pimc

@@ -33,6 +33,10 @@ constexpr int kMaxMoves = 8;
 constexpr int kMaxLevels = 12;   // bisection levels / kinetic spline levels (skip = 2^l)
 constexpr int kMaxSegment = 1 << kMaxLevels;
 
+// Phases of one bisection attempt timed by the sweep kernel's optional tracing: segment and random
+// numbers, sampling chain, per-level terms, grid work, grid barrier, final sum, decision, commit.
+constexpr int kSweepPhases = 8;
+
 // Error word values written by kernels (read back by the host as PIMC_ERR_*).
 constexpr int kDevErrTimeout = 1;
 constexpr int kDevErrNonFinite = 2;

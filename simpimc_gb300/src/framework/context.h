@@ -137,6 +137,8 @@ class Context {
     uint64_t timeout_ns = 2000000000ull;
     int sweep_grid = 0;       // CTAs of the cooperative sweep (0 = automatic)
     int last_grid_ = 0;       // CTAs of the most recent sweep launch
+    bool phase_timing = false;  // record per-phase cycles of block 0 in the sweep kernel
+    std::unique_ptr<DeviceBuffer> phase_buf;  // unsigned long long [kSweepPhases]
     std::vector<std::string> species_names;
     std::vector<ActionHost> actions;
     std::vector<MoveHost> moves;
@@ -149,8 +151,35 @@ class Context {
     int rho_slots = 0;
     std::string base_dir;
 
+    // Double-float mirrors of the path state used by the sweep kernel (positions as (hi, lo)
+    // float pairs, per-slice densities as (re.hi, re.lo, im.hi, im.lo)). Exactly one of the two
+    // representations may be newer than the other; Ensure* converts on demand.
+    void EnsureDD();
+    void EnsureFP64();
+    bool dd_valid = false;
+    bool fp64_valid = true;
+    // Host copies of every spline table, keyed by the device coefficient pointer, so the sweep
+    // can build double-float versions of the same tables.
+    struct HostCubic {
+        std::vector<double> x;
+        std::vector<Cubic4> c;
+        std::vector<int32_t> bucket;
+    };
+    std::vector<std::pair<const Cubic4*, HostCubic>> host_cubics;
+    std::vector<std::vector<double>> host_vk;  // v_long_k per pair action (empty without long range)
+
    private:
     std::vector<std::unique_ptr<DeviceBuffer>> keep_;  // tables owned for the context lifetime
+    std::unique_ptr<DeviceBuffer> pos_dd_, rho_dd_, sweep_desc_, sweep_tables_;
+    bool sweep_tables_built_ = false;
+    std::vector<uint32_t> desc_levels_;  // bisection levels the uploaded move descriptors were built for
+    struct StageTable {
+        const void* x;  // float2 knots
+        const void* c;  // float4 coefficients
+        uint32_t n;
+    };
+    std::vector<StageTable> stage_tables_;  // spline tables the sweep may copy into shared memory
+    void BuildSweepTables();
     std::unique_ptr<DeviceBuffer> pos_, pos_new_, rho_, kidx_;
     std::unique_ptr<DeviceBuffer> partials_, result_, bar_, err_, pairs_, rho_tmp_, parts_, kmag_dev_, sched_, accepts_;
     size_t partials_cap_ = 0, pairs_cap_ = 0, rho_tmp_cap_ = 0, parts_cap_ = 0;

@@ -87,7 +87,10 @@ CubicTable Context::BuildCubic(const std::vector<double>& x, const std::vector<d
             bk[j] = (int32_t)i;
         }
         t.bucket = Upload(bk);
+        host_cubics.push_back({t.c, HostCubic{x, c, bk}});
+        return t;
     }
+    host_cubics.push_back({t.c, HostCubic{x, c, {}}});
     return t;
 }
 
@@ -330,6 +333,8 @@ void Context::BuildActions(const Input& in) {
                     for (size_t j = 0; j < kv.size(); ++j)
                         if (std::fabs(kmags[k] - kv[j]) < 1.e-8) vk[k] = vkv[j];
                 p.v_long_k = Upload(vk);
+                host_vk.resize(sys.n_pair + 1);
+                host_vk[sys.n_pair] = vk;
                 sys.sp_rho[p.sa] = sys.sp_rho[p.sb] = 0;  // marked; slots assigned below
             }
             // bare_pair_action_class.h:89-95
@@ -558,9 +563,12 @@ void Context::SetPath(int which, const double* h) {
                 if (!std::isfinite(v)) throw PimcError(kErrNonFinite, "non-finite bead coordinate");
                 buf[((size_t)b * 3 + d) * np + g] = v;
             }
+    if (which != 2) EnsureFP64();  // a partial update applies on top of the current state
     if (which == 0 || which == 2) CudaCheck(cudaMemcpyAsync(sys.pos, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice, stream), "set path");
     if (which == 1 || which == 2) CudaCheck(cudaMemcpyAsync(sys.pos_new, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice, stream), "set path");
     Sync();
+    fp64_valid = true;
+    if (which != 1) dd_valid = false;
     if (which == 2) {
         for (auto& a : actions) a.is_first_time = true;
         InitRhoK();
@@ -568,6 +576,7 @@ void Context::SetPath(int which, const double* h) {
 }
 
 void Context::GetPath(int which, double* h) {
+    EnsureFP64();
     const uint32_t M = sys.M, n_d = sys.n_d, np = sys.n_pad;
     std::vector<double> buf((size_t)M * 3 * np);
     CudaCheck(cudaMemcpyAsync(buf.data(), which == 0 ? sys.pos : sys.pos_new, buf.size() * sizeof(double), cudaMemcpyDeviceToHost, stream), "get path");
@@ -579,6 +588,7 @@ void Context::GetPath(int which, double* h) {
 
 void Context::GetRhoK(uint32_t s, double* out) {
     if (s >= sys.S || sys.sp_rho[s] < 0 || !sys.rho_k) throw PimcError(kErrArg, "species keeps no charge density");
+    EnsureFP64();
     const size_t n = (size_t)sys.M * sys.K;
     CudaCheck(cudaMemcpyAsync(out, sys.rho_k + (size_t)sys.sp_rho[s] * n, n * sizeof(double2), cudaMemcpyDeviceToHost, stream), "get rho_k");
     Sync();

@@ -162,21 +162,22 @@ __device__ __forceinline__ bool GridBarrier(unsigned long long* ctr, uint64_t ge
     __syncthreads();
     if (threadIdx.x == 0) {
         const uint64_t target = gen * (uint64_t)gridDim.x;
-        __threadfence();
-        atomicAdd(ctr, 1ull);
+        // Release-ordered arrival: this thread's earlier global writes (the block's partial) are
+        // visible to any block that observes the incremented counter with an acquire load.
+        asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(ctr), "l"(1ull) : "memory");
         const uint64_t t0 = GlobalTimerNs();
         uint32_t iters = 0;
         int ok = 1;
         for (;;) {
             if (LoadAcquire(ctr) >= target) break;
-            if (LoadVolatile(err) != 0) { ok = 0; break; }
             ++iters;
-            if ((iters & 255u) == 0u && (GlobalTimerNs() - t0 > timeout_ns || iters > (1u << 30))) {
+            if ((iters & 63u) == 0u && LoadVolatile(err) != 0) { ok = 0; break; }
+            if ((iters & 1023u) == 0u && (GlobalTimerNs() - t0 > timeout_ns || iters > (1u << 30))) {
                 atomicCAS(err, 0, kDevErrTimeout);
                 ok = 0;
                 break;
             }
-            __nanosleep(20);
+            if (iters > 4096u) __nanosleep(32);
         }
         s_ok = ok;
     }

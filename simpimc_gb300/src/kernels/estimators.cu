@@ -192,6 +192,7 @@ void Context::InitRhoK() {
     InitRhoKernel<<<dim3(sys.M, rho_slots), 256, smem, stream>>>(sys, reinterpret_cast<const int*>(dss));
     CudaCheck(cudaGetLastError(), "init rho_k launch");
     Sync();
+    dd_valid = false;
 }
 
 static void SpeciesParticles(const Context& c, uint32_t s, const uint32_t* sp, const uint32_t* p, uint32_t n, std::vector<uint32_t>& out) {
@@ -246,6 +247,7 @@ static uint32_t CountLinks(uint32_t b0, uint32_t b1, uint32_t skip, uint32_t M) 
 }
 
 double Context::GetAction(uint32_t ai, uint32_t b0, uint32_t b1, const uint32_t* sp, const uint32_t* p, uint32_t n, uint32_t level, int mode) {
+    EnsureFP64();
     if (ai >= actions.size()) throw PimcError(kErrArg, "action index out of range");
     if (level >= (uint32_t)kMaxLevels) throw PimcError(kErrArg, "level out of range");
     if (b1 < b0 || b0 >= sys.M || b1 - b0 > sys.M) throw PimcError(kErrArg, "slice range out of bounds");
@@ -380,6 +382,7 @@ double Context::GetAction(uint32_t ai, uint32_t b0, uint32_t b1, const uint32_t*
 
 void Context::GetActionGradient(uint32_t ai, uint32_t b0, uint32_t b1, const uint32_t* sp, const uint32_t* p, uint32_t n, uint32_t level,
                                 int mode, double* g) {
+    EnsureFP64();
     if (ai >= actions.size()) throw PimcError(kErrArg, "action index out of range");
     if (level >= (uint32_t)kMaxLevels) throw PimcError(kErrArg, "level out of range");
     if (b1 < b0 || b0 >= sys.M || b1 - b0 > sys.M) throw PimcError(kErrArg, "slice range out of bounds");
@@ -466,6 +469,7 @@ void Context::GetActionGradient(uint32_t ai, uint32_t b0, uint32_t b1, const uin
 }
 
 double Context::DActionDBeta(uint32_t ai) {
+    EnsureFP64();
     if (ai >= actions.size()) throw PimcError(kErrArg, "action index out of range");
     ActionHost& ah = actions[ai];
     const double* pos = sys.pos;
@@ -545,6 +549,7 @@ double Context::DActionDBeta(uint32_t ai) {
 }
 
 double Context::Potential(uint32_t ai) {
+    EnsureFP64();
     if (ai >= actions.size()) throw PimcError(kErrArg, "action index out of range");
     ActionHost& ah = actions[ai];
     if (ah.kind != 2) return 0.;  // Kinetic and Trap keep Action::Potential() = 0 (action_class.h:52)
@@ -594,6 +599,7 @@ double Context::Potential(uint32_t ai) {
 }
 
 double Context::VirialEnergy(uint32_t ai, double window) {
+    EnsureFP64();
     if (ai >= actions.size()) throw PimcError(kErrArg, "action index out of range");
     const ActionHost& ah = actions[ai];
     if (ah.kind != 0) return DActionDBeta(ai);  // action_class.h:40
@@ -621,6 +627,7 @@ double Context::VirialEnergy(uint32_t ai, double window) {
 }
 
 double Context::VirialCentroid(uint32_t s) {
+    EnsureFP64();
     // energy_class.h:81-94: sum over particles and slices of grad S(b, b+1, {p}) . (r_pb - r_p0)
     // for every non-kinetic action; only pair actions have gradients here.
     const double* pos = sys.pos;
@@ -682,6 +689,7 @@ double Context::VirialCentroid(uint32_t s) {
 }
 
 void Context::ObservableAccumulate(uint32_t oi) {
+    EnsureFP64();
     if (oi >= observables.size()) throw PimcError(kErrArg, "observable index out of range");
     ObservableHost& o = observables[oi];
     if (o.kind == 3) return;

@@ -2,383 +2,916 @@
 // calls (src/events/moves/single_species_move/bisect/bisect_class.h:39-124) for one chain, with
 // the accept/reject commits of bisect_class.h:24-36,127-139, without returning to the host.
 //
-// Work split of one attempt across the grid (G blocks, all co-resident):
-//  * Sampling, the kinetic action and the trap action touch at most 2^n_level beads of one
-//    particle. Every block computes them redundantly from the same Philox stream, so every block
-//    holds the identical proposal in shared memory and no communication is needed for them.
-//  * The pair links of the moved particle (partners x slices) are spread over all threads of the
-//    grid; the Ewald k-sum over the segment is split by ownership: block c owns the slices with
-//    b mod R == c mod R and the k-vectors of chunk c / R. A block only ever reads and writes the
-//    charge densities it owns, so commits need no synchronisation.
-//  * Block partial sums are double-buffered in global memory; one bounded grid barrier per level
-//    that has grid-wide work; every block then reduces the partials in the same order and takes
-//    the same Metropolis decision.
-//  * Accepted positions are written by every block (identical values), so each block's later
-//    reads see either its own store or an identical one.
+// Arithmetic: double-float (df64.cuh). GB300 issues FP64 at 1/64 of the FP32 rate, so the kernel
+// keeps the path, the charge densities and every action term as float pairs (48-bit significand)
+// and never touches the FP64 pipe on its critical path. Results agree with the FP64 oracle to
+// ~1e-13 relative; the random numbers are exactly specified binary32 transforms (philox.h) that
+// the oracle reproduces bit for bit.
+//
+// One attempt, all co-resident blocks in lock step:
+//  1. Every block decodes the same particle/first bead, loads the segment and draws all normals
+//     and acceptance logarithms of the attempt in parallel.
+//  2. Warp 0 samples every level top-down (the chain of midpoints is inherently sequential);
+//     meanwhile other warps build the phase tables of the old positions on this block's slices.
+//  3. In parallel: one warp per level reduces that level's sampling log-probabilities, kinetic
+//     and trap differences; other warps build the new-position phase tables.
+//  4. All threads: pair links of the moved particle (spread over the grid) and the Ewald
+//     differences of the owned (slice, k-chunk) cells; block partial -> one bounded grid barrier
+//     -> every block sums the partials in the same order.
+//  5. Thread 0 replays the reference's per-level Metropolis tests from the precomputed terms
+//     (levels below a rejection are discarded), identically in every block.
+//  6. On acceptance every block writes the resampled beads (identical values) and updates the
+//     charge densities it owns.
+// Levels above 0 are computed speculatively: the random numbers of an attempt are indexed per
+// bead, so drawing them all up front changes nothing.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "../common/philox.h"
 #include "../framework/context.h"
 #include "actions.cuh"
+#include "df64.cuh"
 
 namespace pimc {
 
+struct CubicDD {
+    const float2* x = nullptr;       // knots (hi, lo)
+    const float4* c = nullptr;       // per interval two float4: (c0, c1), (c2, c3) as (hi, lo) pairs
+    const int32_t* bucket = nullptr;
+    int32_t n = 0, n_bucket = 0, uniform = 0, pad = 0;
+    float x0f = 0.f, inv_dxf = 0.f;
+    dd x0{0.f, 0.f}, x1{0.f, 0.f};
+};
+
+struct PairDD {
+    uint32_t sa, sb;
+    int32_t is_coulomb, use_lr, is_constant, max_level;
+    int32_t slot_a, slot_b;
+    dd rvmin, rvmax, rvlmin, rvlmax;
+    CubicDD v_r, v_long_r;
+    const float2* vk;  // [K]
+};
+
+constexpr int kMoveKinetic = 2;
+
+struct MoveDD {
+    uint32_t species, n_level;
+    int32_t has_images, n_kin, n_trap, n_pair;
+    dd sigma[kMaxLevels], i4s[kMaxLevels];
+    CubicDD sample_image[kMaxLevels];
+    int32_t kin_has_images[kMoveKinetic];
+    dd kin_i4[kMoveKinetic][kMaxLevels];
+    CubicDD kin_image[kMoveKinetic][kMaxLevels];
+    uint32_t trap_max_level[kMaxTrap];
+    dd trap_cofa[kMaxTrap];
+    int32_t pair[kMaxPair];
+};
+
 struct SweepArgs {
-    SystemDev sys;
-    MoveDev moves[kMaxMoves];
+    uint32_t n_d, M, n_pad, K;
+    dd L, iL, tau, two_pi;
+    uint32_t sp_off[kMaxSpecies], sp_n[kMaxSpecies];
+    int32_t max_index[3];
+    float2* pos;              // [M][3][n_pad]
+    float4* rho;              // [slots][M][K]
+    const int32_t* kidx;      // [K]
+    const float4* phase256;   // exp(2 pi i j / 256), j = 0..255
+    const MoveDD* moves;
+    const PairDD* pairs;
     uint64_t attempt_base[kMaxMoves];
     const uint32_t* sched_move;
     const uint64_t* sched_count;
     uint32_t n_entries;
     uint64_t n_rep;
     uint32_t seed, chain;
-    uint32_t R, Q;              // ownership: residue classes of slices, chunks of k
-    uint32_t seg_cap;           // capacity of the shared segment arrays (beads)
-    int32_t tab_stride;         // phase-table row length
-    unsigned long long* accepts;  // [2][kMaxMoves]: accepted attempts, attempts reaching level 0
+    uint32_t R, Q;            // ownership: slice residue classes, k chunks
+    uint32_t seg_cap;         // segment capacity in beads (2^max_level + 1)
+    uint32_t tab_stride;      // phase-table row length (max_index + 1)
+    uint32_t slices_per_cta;  // owned slices per attempt (segment length / R)
+    unsigned long long* counters;  // [2][kMaxMoves]: accepts, attempts reaching level 0
     unsigned long long* bar;
     int* err;
-    double* partials;             // [2][gridDim.x]
+    float2* partials;         // [2][gridDim.x]
     uint64_t timeout_ns;
+    unsigned long long* phase_cycles;  // optional [kSweepPhases]: block 0's cycles per phase, summed
+    // Shared-memory staging (byte offsets into the dynamic shared block).
+    uint32_t n_moves, n_pairs;
+    uint32_t off_moves, off_pairs, off_phase, off_work;
+    uint32_t n_stage;
+    const float2* stage_x[kMaxPair];
+    const float4* stage_c[kMaxPair];
+    uint32_t stage_n[kMaxPair], stage_off_x[kMaxPair], stage_off_c[kMaxPair];
 };
 
 namespace {
 
-__device__ __forceinline__ uint32_t Wrap(uint32_t b, uint32_t M) { return b >= M ? b - M : b; }
+constexpr int kThreads = 512;
+constexpr int kWarps = kThreads / 32;
+constexpr int kDeltaCache = 4;
+constexpr uint32_t kMaxOwned = 8;
 
-constexpr int kSweepThreads = 256;
+__device__ __forceinline__ dd LoadDD(const float2* p) {
+    const float2 v = *p;
+    return dd{v.x, v.y};
+}
 
-__global__ void __launch_bounds__(kSweepThreads) BisectSweepKernel(const __grid_constant__ SweepArgs a) {
-    extern __shared__ double smem[];
-    const SystemDev& sys = a.sys;
-    const uint32_t n_d = sys.n_d, M = sys.M, np = sys.n_pad;
-    const double L = sys.L, iL = sys.iL;
-    double* seg_old = smem;                          // [seg_cap][3]
-    double* seg_new = seg_old + 3 * a.seg_cap;       // [seg_cap][3]
-    double* red = seg_new + 3 * a.seg_cap;           // [32]
-    double2* tab = reinterpret_cast<double2*>(red + 32);  // [2][3][tab_stride]
-    __shared__ double s_small, s_lsp_old, s_lsp_new, s_total, s_dS;
-    __shared__ int s_reject;
+__device__ __forceinline__ dd EvalCubicDD(const CubicDD& t, dd x) {
+    x = Min(Max(x, t.x0), t.x1);
+    int i;
+    if (t.uniform) {
+        i = (int)floorf(__fmul_rn(__fsub_rn(x.hi, t.x0f), t.inv_dxf));
+        i = min(max(i, 0), t.n - 2);
+    } else {
+        int j = (int)floorf(__fmul_rn(__fsub_rn(x.hi, t.x0f), t.inv_dxf));
+        j = min(max(j, 0), t.n_bucket - 1);
+        i = t.bucket[j];
+    }
+    while (i < t.n - 2 && !Less(x, LoadDD(&t.x[i + 1]))) ++i;
+    while (i > 0 && Less(x, LoadDD(&t.x[i]))) --i;
+    const float4 a = t.c[2 * i], b = t.c[2 * i + 1];
+    const dd u = Sub(x, LoadDD(&t.x[i]));
+    const dd v = Add(dd{a.z, a.w}, Mul(u, Add(dd{b.x, b.y}, Mul(u, dd{b.z, b.w}))));
+    return Add(dd{a.x, a.y}, Mul(u, v));
+}
+
+/// Sum over dimensions of the image-spline values.
+__device__ __forceinline__ dd ImageSum(const CubicDD& t, const dd* dr, uint32_t n_d) {
+    dd s{0.f, 0.f};
+    for (uint32_t d = 0; d < n_d; ++d) s = Add(s, EvalCubicDD(t, dr[d]));
+    return s;
+}
+
+/// BarePairAction::CalcV (bare_pair_action_class.h:99-123) in double-float.
+__device__ __forceinline__ dd PairVDD(const PairDD& pa, dd r, dd rp) {
+    r = Min(Max(r, pa.rvmin), pa.rvmax);
+    rp = Min(Max(rp, pa.rvmin), pa.rvmax);
+    dd v;
+    if (pa.is_coulomb) {
+        v = Add(Scale2(Div(DD(1.f), r), 0.5f), Scale2(Div(DD(1.f), rp), 0.5f));
+    } else {
+        v = Add(Scale2(EvalCubicDD(pa.v_r, r), 0.5f), Scale2(EvalCubicDD(pa.v_r, rp), 0.5f));
+    }
+    if (pa.use_lr) {
+        r = Min(Max(r, pa.rvlmin), pa.rvlmax);
+        rp = Min(Max(rp, pa.rvlmin), pa.rvlmax);
+        v = Sub(v, Scale2(EvalCubicDD(pa.v_long_r, r), 0.5f));
+        v = Sub(v, Scale2(EvalCubicDD(pa.v_long_r, rp), 0.5f));
+    }
+    return v;
+}
+
+/// Path::DrDrpDrrp (path_class.h:137-150) magnitudes |r|, |r'| in double-float.
+__device__ __forceinline__ void DrDrpDD(const dd* A0, const dd* C0, const dd* A1, const dd* C1, uint32_t n_d, dd L, dd iL, dd& r,
+                                        dd& rp) {
+    dd a{0.f, 0.f}, b{0.f, 0.f};
+    for (uint32_t d = 0; d < n_d; ++d) {
+        const dd rv = MinImageDD(Sub(A0[d], C0[d]), L, iL);
+        dd rq = Sub(A1[d], C1[d]);
+        const float n = Rint(Mul(Sub(rv, rq), iL));
+        if (n != 0.f) rq = Add(rq, MulF(L, n));
+        a = Add(a, Sqr(rv));
+        b = Add(b, Sqr(rq));
+    }
+    r = Sqrt(a);
+    rp = Sqrt(b);
+}
+
+/// exp(2 pi i n t) for the turn count t = x / L of one coordinate: n t is reduced modulo 1, its
+/// nearest 1/256 of a turn read from a table and the residue (|eps| <= pi/256) expanded in Taylor
+/// series to eps^7 in double-float.
+__device__ __forceinline__ ddc PhaseDD(dd x, int n, dd iL, dd two_pi, const float4* tab256) {
+    if (n == 0) return ddc{DD(1.f), DD(0.f)};
+    dd t = Mul(x, iL);
+    t = Sub(t, DD(Rint(t)));
+    dd a = MulF(t, (float)n);
+    a = Sub(a, DD(Rint(a)));
+    const float jf = rintf(__fmul_rn(a.hi, 256.f));
+    const dd g = Sub(a, DD(__fmul_rn(jf, 1.f / 256.f)));
+    const dd eps = Mul(g, two_pi);
+    const dd e2 = Sqr(eps);
+    const dd neg_inv6{-0.16666667f, 4.9670538e-09f};  // -1/6 as a float pair
+    const dd ps = Add(neg_inv6, MulF(e2, __fmaf_rn(e2.hi, -1.f / 5040.f, 1.f / 120.f)));
+    const dd sn = Add(eps, Mul(eps, Mul(e2, ps)));
+    const dd pc = AddF(MulF(e2, __fmaf_rn(e2.hi, -1.f / 720.f, 1.f / 24.f)), -0.5f);
+    const dd cs = AddF(Mul(e2, pc), 1.f);
+    const int j = ((int)jf + 256) & 255;
+    const ddc T = Unpack(tab256[j]);
+    return CMulDD(T, ddc{cs, sn});
+}
+
+/// Product over dimensions of the per-dimension phases from tables [3][stride].
+__device__ __forceinline__ ddc PhaseProductDD(const ddc* tab, uint32_t stride, uint32_t n_d, int32_t packed) {
+    ddc f{DD(1.f), DD(0.f)};
+    for (uint32_t d = 0; d < n_d; ++d) {
+        const int n = KIdx(packed, (int)d);
+        ddc c = tab[d * stride + (n < 0 ? -n : n)];
+        if (n < 0) c.im = Neg(c.im);
+        f = d == 0 ? c : CMulDD(f, c);
+    }
+    return f;
+}
+
+/// Generation index of the first midpoint of level lvl (levels are sampled from n_level - 1 down).
+__device__ __forceinline__ uint32_t LevelFirst(uint32_t nl, int lvl, uint32_t B) {
+    uint32_t first = 0;
+    for (int l = (int)nl - 1; l > lvl; --l) first += B / (2u << l);
+    return first;
+}
+
+/// Level sums of one copy of the segment (warp-cooperative; every lane receives the totals):
+///   lsp   = sampling log-probability of the copy's midpoints, -i4s |d|^2 - images(d)
+///           (free_spline_class.h:189-197 with tau' = tau 2^l / 2, bisect_class.h:85-94);
+///   small = kinetic action of the links j -> j + skip (kinetic_class.h:105-122) plus the trap
+///           action of slices j at stride skip (trap_class.h:37-61, when lvl <= max_level).
+__device__ __forceinline__ void LevelSums(const MoveDD& mv, int lvl, uint32_t B, const dd* seg, const dd* disp, uint32_t first, uint32_t n_d,
+                                          dd L, dd iL, int lane, dd& lsp, dd& small) {
+    const uint32_t skip = 1u << lvl, nm = B / (2 * skip);
+    dd sp{0.f, 0.f}, sm{0.f, 0.f};
+    for (uint32_t t = lane; t < nm; t += 32) {
+        dd q{0.f, 0.f};
+        for (uint32_t d = 0; d < n_d; ++d) q = Add(q, Sqr(disp[3 * (first + t) + d]));
+        dd v = Mul(q, mv.i4s[lvl]);
+        if (mv.has_images) v = Add(v, ImageSum(mv.sample_image[lvl], &disp[3 * (first + t)], n_d));
+        sp = Add(sp, v);
+    }
+    for (int ki = 0; ki < mv.n_kin; ++ki)
+        for (uint32_t j = lane * skip; j < B; j += 32 * skip) {
+            dd dr[3];
+            dd q{0.f, 0.f};
+            for (uint32_t d = 0; d < n_d; ++d) {
+                dr[d] = MinImageDD(Sub(seg[3 * j + d], seg[3 * (j + skip) + d]), L, iL);
+                q = Add(q, Sqr(dr[d]));
+            }
+            dd v = Mul(q, mv.kin_i4[ki][lvl]);
+            if (mv.kin_has_images[ki]) v = Add(v, ImageSum(mv.kin_image[ki][lvl], dr, n_d));
+            sm = Add(sm, v);
+        }
+    for (int ti = 0; ti < mv.n_trap; ++ti) {
+        if ((uint32_t)lvl > mv.trap_max_level[ti]) continue;
+        dd acc{0.f, 0.f};
+        for (uint32_t j = lane * skip; j < B; j += 32 * skip)
+            for (uint32_t d = 0; d < n_d; ++d) acc = Add(acc, Sqr(seg[3 * j + d]));
+        sm = Add(sm, MulF(Mul(acc, mv.trap_cofa[ti]), (float)skip));
+    }
+    lsp = Neg(WarpSumDD(sp));
+    small = WarpSumDD(sm);
+}
+
+__device__ __forceinline__ void CopyWords(void* dst, const void* src, uint32_t bytes) {
+    uint32_t* d = static_cast<uint32_t*>(dst);
+    const uint32_t* s = static_cast<const uint32_t*>(src);
+    for (uint32_t i = threadIdx.x; i < bytes / 4; i += blockDim.x) d[i] = s[i];
+}
+
+__global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_constant__ SweepArgs a) {
+    extern __shared__ float4 smem4[];
+    const uint32_t n_d = a.n_d, M = a.M, np = a.n_pad, K = a.K;
+    const uint32_t cap = a.seg_cap, stride = a.tab_stride;
+    // Launch-invariant data staged in shared memory once: move and pair descriptors, the phase
+    // table and (when they fit) the long-range spline tables.
+    char* sbase = reinterpret_cast<char*>(smem4);
+    MoveDD* s_moves = reinterpret_cast<MoveDD*>(sbase + a.off_moves);
+    PairDD* s_pairs = reinterpret_cast<PairDD*>(sbase + a.off_pairs);
+    float4* s_phase = reinterpret_cast<float4*>(sbase + a.off_phase);
+    CopyWords(s_moves, a.moves, a.n_moves * (uint32_t)sizeof(MoveDD));
+    CopyWords(s_pairs, a.pairs, a.n_pairs * (uint32_t)sizeof(PairDD));
+    CopyWords(s_phase, a.phase256, 256 * (uint32_t)sizeof(float4));
+    for (uint32_t j = 0; j < a.n_stage; ++j) {
+        CopyWords(sbase + a.stage_off_x[j], a.stage_x[j], a.stage_n[j] * (uint32_t)sizeof(float2));
+        CopyWords(sbase + a.stage_off_c[j], a.stage_c[j], 2 * (a.stage_n[j] - 1) * (uint32_t)sizeof(float4));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (uint32_t i = 0; i < a.n_pairs; ++i)
+            for (uint32_t j = 0; j < a.n_stage; ++j) {
+                CubicDD* t[2] = {&s_pairs[i].v_long_r, &s_pairs[i].v_r};
+                for (CubicDD* c : t)
+                    if (c->x == a.stage_x[j]) {
+                        c->x = reinterpret_cast<const float2*>(sbase + a.stage_off_x[j]);
+                        c->c = reinterpret_cast<const float4*>(sbase + a.stage_off_c[j]);
+                    }
+            }
+    __syncthreads();
+    ddc* tab_old = reinterpret_cast<ddc*>(sbase + a.off_work);          // [spc][3][stride]
+    ddc* tab_new = tab_old + (size_t)a.slices_per_cta * 3 * stride;       // [spc][3][stride]
+    dd* seg_old = reinterpret_cast<dd*>(tab_new + (size_t)a.slices_per_cta * 3 * stride);  // [cap][3]
+    dd* seg_new = seg_old + 3 * cap;                                      // [cap][3]
+    dd* d_old = seg_new + 3 * cap;                                        // [cap][3] sampling displacements
+    dd* d_new = d_old + 3 * cap;                                          // [cap][3]
+    float* zs = reinterpret_cast<float*>(d_new + 3 * cap);                // [cap][3] normals
+    float* logu = zs + 3 * cap;                                           // [kMaxLevels]
+    __shared__ dd s_lvl_diff[kMaxLevels], s_lvl_small[kMaxLevels];
+    __shared__ dd s_old_lsp[kMaxLevels], s_old_small[kMaxLevels];
+    __shared__ dd s_red[kWarps];
+    __shared__ dd s_big;
+    __shared__ int s_result;
+    __shared__ uint32_t s_slice_jj[kMaxOwned];
+    __shared__ uint32_t s_n_own;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t G = gridDim.x, cta = blockIdx.x;
     const uint32_t r_own = cta % a.R, q_own = cta / a.R;
     const bool owns_k = q_own < a.Q;
-    const uint32_t k_lo = owns_k ? (uint32_t)(((uint64_t)sys.K * q_own) / a.Q) : 0u;
-    const uint32_t k_hi = owns_k ? (uint32_t)(((uint64_t)sys.K * (q_own + 1)) / a.Q) : 0u;
-    const int stride = a.tab_stride;
+    const uint32_t k_lo = owns_k ? (uint32_t)(((uint64_t)K * q_own) / a.Q) : 0u;
+    const uint32_t k_hi = owns_k ? (uint32_t)(((uint64_t)K * (q_own + 1)) / a.Q) : 0u;
 
     uint64_t ctr[kMaxMoves];
-    for (int m = 0; m < kMaxMoves; ++m) ctr[m] = a.attempt_base[m];
-    unsigned long long my_accepts[kMaxMoves], my_reach0[kMaxMoves];
-    for (int m = 0; m < kMaxMoves; ++m) my_accepts[m] = my_reach0[m] = 0ull;
+    unsigned long long n_acc[kMaxMoves], n_l0[kMaxMoves];
+    for (int m = 0; m < kMaxMoves; ++m) {
+        ctr[m] = a.attempt_base[m];
+        n_acc[m] = n_l0[m] = 0ull;
+    }
     uint64_t nbar = 0;
+    // Optional phase timing of block 0 (tracing aid; the work done is identical either way).
+    const bool timing = a.phase_cycles != nullptr && cta == 0 && tid == 0;
+    unsigned long long ph[kSweepPhases] = {0ull};
+    long long t_prev = clock64();
+#define PIMC_PHASE(i)                             \
+    if (timing) {                                 \
+        const long long t_now = clock64();        \
+        ph[i] += (unsigned long long)(t_now - t_prev); \
+        t_prev = t_now;                           \
+    }
 
     for (uint64_t rep = 0; rep < a.n_rep; ++rep) {
         for (uint32_t e = 0; e < a.n_entries; ++e) {
             const uint32_t m = a.sched_move[e];
-            const uint64_t count = a.sched_count[e];
-            const MoveDev& mv = a.moves[m];
-            const uint32_t s = mv.species, B = 1u << mv.n_level;
-            const uint32_t g_off = sys.sp_off[s];
-            const int slot_s = sys.sp_rho[s];
-            for (uint64_t c = 0; c < count; ++c) {
+            const MoveDD& mv = s_moves[m];
+            const uint32_t s = mv.species, nl = mv.n_level, B = 1u << nl;
+            const uint32_t g_off = a.sp_off[s];
+            bool any_lr = false, grid_work = false;
+            int slot_s = -1;
+            for (int pi = 0; pi < mv.n_pair; ++pi) {
+                const PairDD& pa = s_pairs[mv.pair[pi]];
+                if (!pa.is_constant) grid_work = true;
+                if (pa.use_lr && !pa.is_constant) {
+                    any_lr = true;
+                    slot_s = pa.sa == s ? pa.slot_a : pa.slot_b;
+                }
+            }
+            for (uint64_t c = 0, count = a.sched_count[e]; c < count; ++c) {
                 const MoveStream st{a.seed, a.chain, m, ctr[m]};
                 ctr[m] += 1;
                 const Philox4 w0 = st.Block(0);
-                const uint32_t p = UniformIndex(w0.v[0], sys.sp_n[s]);
+                const uint32_t p = UniformIndex(w0.v[0], a.sp_n[s]);
                 const uint32_t bead0 = UniformIndex(w0.v[1], M);
                 const uint32_t g = g_off + p;
 
-                // Segment bead0 .. bead0 + B (wrapping), old and new copies.
+                // ---- 1. segment, random numbers, owned slices -------------------------------
                 for (uint32_t i = tid; i < (B + 1) * 3; i += blockDim.x) {
                     const uint32_t j = i / 3, d = i % 3;
-                    const double v = d < n_d ? PosAt(sys.pos, np, (bead0 + j) % M, d, g) : 0.;
+                    dd v{0.f, 0.f};
+                    if (d < n_d) v = LoadDD(&a.pos[((size_t)((bead0 + j) % M) * 3 + d) * np + g]);
                     seg_old[i] = v;
                     seg_new[i] = v;
                 }
+                for (uint32_t i = tid; i < B - 1; i += blockDim.x) BisectNormals(st, i, &zs[3 * i]);
+                if (tid < (int)nl) logu[tid] = BisectLogU(st, B, (uint32_t)tid);
+                if (tid == 0) {
+                    uint32_t n = 0;
+                    if (owns_k && any_lr)
+                        for (uint32_t jj = 1; jj < B && n < kMaxOwned; ++jj)
+                            if (((bead0 + jj) % M) % a.R == r_own) s_slice_jj[n++] = jj;
+                    s_n_own = n;
+                }
                 __syncthreads();
+                PIMC_PHASE(0);
+                const uint32_t n_own = s_n_own;
 
-                double prev_dS = 0.;
-                bool accepted = true;
-                uint32_t mid = 0;
-                for (int lvl = (int)mv.n_level - 1; lvl >= 0; --lvl) {
-                    const uint32_t skip = 1u << lvl;
-                    const uint32_t nm = B / (2 * skip);
-                    // (1) Sampling, kinetic and trap terms: warp 0 of every block.
-                    if (warp == 0) {
-                        const double level_tau = sys.tau * skip;
-                        const double sigma = sqrt(mv.lambda * level_tau);
-                        const double i4s = mv.i4lt_sample[lvl];
-                        double lo = 0., ln = 0.;
-                        for (uint32_t mm = lane; mm < nm; mm += 32) {
+                // ---- 2. sampling chain (warp 0) || old phase tables (other warps) ----------
+                if (warp == 0) {
+                    uint32_t mid = 0;
+                    for (int lvl = (int)nl - 1; lvl >= 0; --lvl) {
+                        const uint32_t skip = 1u << lvl, nm = B / (2 * skip);
+                        const dd sigma = mv.sigma[lvl];
+                        for (uint32_t t = lane; t < nm * n_d; t += 32) {
+                            const uint32_t mm = t / n_d, d = t % n_d;
                             const uint32_t ja = mm * 2 * skip, jb = ja + skip, jc = ja + 2 * skip;
-                            double dold[3] = {0., 0., 0.}, dnew[3] = {0., 0., 0.};
-                            double z[3];
-                            BisectNormals(st, mid + mm, z);
-                            for (uint32_t d = 0; d < n_d; ++d) {
-                                const double ra = seg_old[3 * ja + d], rc = seg_old[3 * jc + d];
-                                const double rbar = ra + 0.5 * MinImage(rc - ra, L, iL);
-                                dold[d] = MinImage(seg_old[3 * jb + d] - rbar, L, iL);
-                                const double na = seg_new[3 * ja + d], nc = seg_new[3 * jc + d];
-                                const double nbar = na + 0.5 * MinImage(nc - na, L, iL);
-                                dnew[d] = MinImage(0. + sigma * z[d], L, iL);
-                                seg_new[3 * jb + d] = nbar + dnew[d];
-                            }
-                            lo += LogRhoFree(dold, n_d, i4s, &mv.sample_image[lvl], mv.has_images);
-                            ln += LogRhoFree(dnew, n_d, i4s, &mv.sample_image[lvl], mv.has_images);
+                            // Path::RBar (path_class.h:124) on the working copy.
+                            const dd na = seg_new[3 * ja + d], nc = seg_new[3 * jc + d];
+                            const dd nbar2 = Add(na, Scale2(MinImageDD(Sub(nc, na), a.L, a.iL), 0.5f));
+                            const dd dn = MinImageDD(MulF(sigma, zs[3 * (mid + mm) + d]), a.L, a.iL);
+                            d_new[3 * (mid + mm) + d] = dn;
+                            seg_new[3 * jb + d] = Add(nbar2, dn);
                         }
-                        lo = WarpSum(lo);
-                        ln = WarpSum(ln);
+                        mid += nm;
                         __syncwarp();
-                        double small = 0.;
-                        // Kinetic action at this level (kinetic_class.h:105-122): links j -> j + skip.
-                        for (int ki = 0; ki < mv.n_kinetic; ++ki) {
-                            const KineticDev& kd = sys.kinetic[mv.kinetic[ki]];
-                            const double i4 = kd.i4lt_level[lvl];
-                            for (uint32_t j = lane * skip; j < B; j += 32 * skip) {
-                                double dro[3] = {0., 0., 0.}, drn[3] = {0., 0., 0.};
-                                for (uint32_t d = 0; d < n_d; ++d) {
-                                    dro[d] = MinImage(seg_old[3 * j + d] - seg_old[3 * (j + skip) + d], L, iL);
-                                    drn[d] = MinImage(seg_new[3 * j + d] - seg_new[3 * (j + skip) + d], L, iL);
-                                }
-                                small += -LogRhoFree(drn, n_d, i4, &kd.image[lvl], kd.has_images) +
-                                         LogRhoFree(dro, n_d, i4, &kd.image[lvl], kd.has_images);
-                            }
-                        }
-                        // Harmonic trap (trap_class.h:37-61): slices [bead0, bead1) at stride skip.
-                        for (int ti = 0; ti < mv.n_trap; ++ti) {
-                            const TrapDev& td = sys.trap[mv.trap[ti]];
-                            if ((uint32_t)lvl > td.max_level) continue;
-                            double acc = 0.;
-                            for (uint32_t j = lane * skip; j < B; j += 32 * skip)
-                                for (uint32_t d = 0; d < n_d; ++d)
-                                    acc += seg_new[3 * j + d] * seg_new[3 * j + d] - seg_old[3 * j + d] * seg_old[3 * j + d];
-                            small += td.cofactor_a * skip * acc;
-                        }
-                        small = WarpSum(small);
-                        if (lane == 0) {
-                            s_small = small;
-                            s_lsp_old = lo;
-                            s_lsp_new = ln;
-                        }
                     }
-                    mid += nm;
-                    __syncthreads();
+                } else if (warp <= (int)nl) {
+                    // Everything of the stored copy is known before sampling: its displacements from
+                    // the midpoints and its level sums (warp 1 + level).
+                    const int lvl = warp - 1;
+                    const uint32_t skip = 1u << lvl, nm = B / (2 * skip), first = LevelFirst(nl, lvl, B);
+                    for (uint32_t t = lane; t < nm * n_d; t += 32) {
+                        const uint32_t mm = t / n_d, d = t % n_d;
+                        const uint32_t ja = mm * 2 * skip, jb = ja + skip, jc = ja + 2 * skip;
+                        const dd ra = seg_old[3 * ja + d], rc = seg_old[3 * jc + d];
+                        const dd rbar = Add(ra, Scale2(MinImageDD(Sub(rc, ra), a.L, a.iL), 0.5f));
+                        d_old[3 * (first + mm) + d] = MinImageDD(Sub(seg_old[3 * jb + d], rbar), a.L, a.iL);
+                    }
+                    __syncwarp();
+                    dd lsp, sm;
+                    LevelSums(mv, lvl, B, seg_old, d_old, first, n_d, a.L, a.iL, lane, lsp, sm);
+                    if (lane == 0) {
+                        s_old_lsp[lvl] = lsp;
+                        s_old_small[lvl] = sm;
+                    }
+                } else {
+                    const int w0 = (int)nl + 1;
+                    for (uint32_t task = warp - w0; task < n_own * 3; task += kWarps - w0) {
+                        const uint32_t si = task / 3, d = task % 3;
+                        if (d < n_d)
+                            for (int n = lane; n <= a.max_index[d]; n += 32)
+                                tab_old[(si * 3 + d) * stride + n] = PhaseDD(seg_old[3 * s_slice_jj[si] + d], n, a.iL, a.two_pi, s_phase);
+                    }
+                }
+                __syncthreads();
+                PIMC_PHASE(1);
 
-                    // (2) Pair links and Ewald sums: the whole grid.
-                    bool grid_work = false;
+                // ---- 3. per-level sums of the working copy || new phase tables -------------
+                if (warp < (int)nl) {
+                    const int lvl = warp;
+                    dd lsp, sm;
+                    LevelSums(mv, lvl, B, seg_new, d_new, LevelFirst(nl, lvl, B), n_d, a.L, a.iL, lane, lsp, sm);
+                    if (lane == 0) {
+                        s_lvl_diff[lvl] = Sub(s_old_lsp[lvl], lsp);     // old log-prob - new log-prob
+                        s_lvl_small[lvl] = Sub(sm, s_old_small[lvl]);   // new action - old action
+                    }
+                } else {
+                    const int w0 = (int)nl;
+                    for (uint32_t task = warp - w0; task < n_own * 3; task += kWarps - w0) {
+                        const uint32_t si = task / 3, d = task % 3;
+                        if (d < n_d)
+                            for (int n = lane; n <= a.max_index[d]; n += 32)
+                                tab_new[(si * 3 + d) * stride + n] = PhaseDD(seg_new[3 * s_slice_jj[si] + d], n, a.iL, a.two_pi, s_phase);
+                    }
+                }
+                __syncthreads();
+                PIMC_PHASE(2);
+
+                // ---- 4. level-0 grid work: pair links + owned Ewald cells -------------------
+                ddc delta_cache[kDeltaCache];
+                if (grid_work) {
+                    dd acc{0.f, 0.f};
+                    // Pair links (pair_action_class.h:280-290): one (link, old|new) evaluation per
+                    // thread, consecutive evaluations on different blocks so that no block carries
+                    // more than a few of these latency-bound chains.
+                    uint32_t offs[kMaxPair + 1];
+                    uint32_t n_eval = 0;
                     for (int pi = 0; pi < mv.n_pair; ++pi) {
-                        const PairDev& pa = sys.pair[mv.pair[pi]];
-                        if ((uint32_t)lvl <= pa.max_level && !pa.is_constant && (lvl == 0 || pa.use_long_range)) grid_work = true;
+                        const PairDD& pa = s_pairs[mv.pair[pi]];
+                        offs[pi] = n_eval;
+                        if (pa.is_constant) continue;
+                        const uint32_t other = pa.sa == pa.sb ? s : (pa.sa == s ? pa.sb : pa.sa);
+                        n_eval += 2u * (pa.sa == pa.sb ? a.sp_n[s] - 1 : a.sp_n[other]) * B;
                     }
-                    double big = 0.;
-                    if (grid_work) {
-                        double acc = 0.;
-                        const uint64_t gtid = (uint64_t)cta * blockDim.x + tid, gstride = (uint64_t)G * blockDim.x;
-                        // Pair links (pair_action_class.h:280-290); CalcU is zero above level 0.
-                        if (lvl == 0) {
+                    offs[mv.n_pair] = n_eval;
+                    const uint32_t gstride = G * blockDim.x;
+                    for (uint32_t it = (uint32_t)tid * G + cta; it < n_eval; it += gstride) {
+                        int pi = 0;
+                        while (it >= offs[pi + 1]) ++pi;
+                        const PairDD& pa = s_pairs[mv.pair[pi]];
+                        const bool hom = pa.sa == pa.sb;
+                        const uint32_t other = hom ? s : (pa.sa == s ? pa.sb : pa.sa);
+                        const bool moved_is_a = hom || pa.sa == s;
+                        uint32_t local = it - offs[pi];
+                        const bool is_new = (local & 1u) != 0u;
+                        local >>= 1;
+                        const uint32_t jj = local % B;
+                        uint32_t qq = local / B;
+                        if (hom && qq >= p) ++qq;
+                        const uint32_t gq = a.sp_off[other] + qq;
+                        const uint32_t bi = (bead0 + jj) % M, bj = (bead0 + jj + 1) % M;
+                        dd Q0[3], Q1[3];
+                        for (uint32_t d = 0; d < n_d; ++d) {
+                            Q0[d] = LoadDD(&a.pos[((size_t)bi * 3 + d) * np + gq]);
+                            Q1[d] = LoadDD(&a.pos[((size_t)bj * 3 + d) * np + gq]);
+                        }
+                        const dd* sg = is_new ? seg_new : seg_old;
+                        dd r, rp;
+                        if (moved_is_a) DrDrpDD(Q0, &sg[3 * jj], Q1, &sg[3 * (jj + 1)], n_d, a.L, a.iL, r, rp);
+                        else DrDrpDD(&sg[3 * jj], Q0, &sg[3 * (jj + 1)], Q1, n_d, a.L, a.iL, r, rp);
+                        const dd u = Mul(a.tau, PairVDD(pa, r, rp));  // CalcU = tau V at level 0
+                        acc = Add(acc, is_new ? u : Neg(u));
+                    }
+                    if (any_lr) {
+                        const uint32_t nk = k_hi - k_lo;
+                        dd lr{0.f, 0.f};
+                        uint32_t ci = 0;
+                        for (uint32_t it = tid; it < n_own * nk; it += blockDim.x, ++ci) {
+                            const uint32_t si = it / nk, k = k_lo + it % nk;
+                            const uint32_t b = (bead0 + s_slice_jj[si]) % M;
+                            const int32_t pk = a.kidx[k];
+                            const ddc en = PhaseProductDD(tab_new + (size_t)si * 3 * stride, stride, n_d, pk);
+                            const ddc eo = PhaseProductDD(tab_old + (size_t)si * 3 * stride, stride, n_d, pk);
+                            const ddc dl = CSub(en, eo);
+                            if (ci < kDeltaCache) delta_cache[ci] = dl;
+                            const ddc rho = Unpack(a.rho[((size_t)slot_s * M + b) * K + k]);
                             for (int pi = 0; pi < mv.n_pair; ++pi) {
-                                const PairDev& pa = sys.pair[mv.pair[pi]];
-                                if (pa.is_constant) continue;
-                                const bool hom = pa.sa == pa.sb;
-                                const uint32_t other = hom ? s : (pa.sa == s ? pa.sb : pa.sa);
-                                const uint32_t n_partner = hom ? sys.sp_n[s] - 1 : sys.sp_n[other];
-                                const uint64_t n_items = (uint64_t)n_partner * B;
-                                const bool moved_is_a = hom || pa.sa == s;
-                                for (uint64_t it = gtid; it < n_items; it += gstride) {
-                                    const uint32_t jj = (uint32_t)(it % B);
-                                    uint32_t qq = (uint32_t)(it / B);
-                                    if (hom && qq >= p) ++qq;
-                                    const uint32_t gq = sys.sp_off[other] + qq;
-                                    const uint32_t bi = (bead0 + jj) % M, bj = (bead0 + jj + 1) % M;
-                                    double Q0[3], Q1[3];
-                                    LoadBead(sys.pos, np, n_d, bi, gq, Q0);
-                                    LoadBead(sys.pos, np, n_d, bj, gq, Q1);
-                                    double r, rp, sd, uo, un;
-                                    if (moved_is_a) {
-                                        DrDrpDrrp(Q0, &seg_old[3 * jj], Q1, &seg_old[3 * (jj + 1)], n_d, L, iL, r, rp, sd);
-                                        uo = PairU(pa, r, rp, 0, sys.tau);
-                                        DrDrpDrrp(Q0, &seg_new[3 * jj], Q1, &seg_new[3 * (jj + 1)], n_d, L, iL, r, rp, sd);
-                                        un = PairU(pa, r, rp, 0, sys.tau);
-                                    } else {
-                                        DrDrpDrrp(&seg_old[3 * jj], Q0, &seg_old[3 * (jj + 1)], Q1, n_d, L, iL, r, rp, sd);
-                                        uo = PairU(pa, r, rp, 0, sys.tau);
-                                        DrDrpDrrp(&seg_new[3 * jj], Q0, &seg_new[3 * (jj + 1)], Q1, n_d, L, iL, r, rp, sd);
-                                        un = PairU(pa, r, rp, 0, sys.tau);
-                                    }
-                                    acc += un - uo;
+                                const PairDD& pa = s_pairs[mv.pair[pi]];
+                                if (!pa.use_lr || pa.is_constant) continue;
+                                const float2 vkf = pa.vk[k];
+                                const dd vk{vkf.x, vkf.y};
+                                if (pa.sa == pa.sb) {
+                                    // |rho + D|^2 - |rho|^2 = D.re (2 rho.re + D.re) + D.im (2 rho.im + D.im)
+                                    const dd t = Add(Mul(dl.re, Add(Scale2(rho.re, 2.f), dl.re)), Mul(dl.im, Add(Scale2(rho.im, 2.f), dl.im)));
+                                    lr = Add(lr, Mul(vk, t));
+                                } else {
+                                    const int slot_o = pa.sa == s ? pa.slot_b : pa.slot_a;
+                                    const ddc ro = Unpack(a.rho[((size_t)slot_o * M + b) * K + k]);
+                                    const dd t = Add(Mul(dl.re, ro.re), Mul(dl.im, ro.im));
+                                    lr = Add(lr, Scale2(Mul(vk, t), 2.f));
                                 }
                             }
                         }
-                        // Ewald sums over the owned slices and k-vectors (bare_pair_action_class.h:153-172).
-                        bool any_lr = false;
-                        for (int pi = 0; pi < mv.n_pair; ++pi) {
-                            const PairDev& pa = sys.pair[mv.pair[pi]];
-                            if (pa.use_long_range && (uint32_t)lvl <= pa.max_level && !pa.is_constant) any_lr = true;
-                        }
-                        if (any_lr && owns_k && slot_s >= 0) {
-                            double lr = 0.;
-                            for (uint32_t jj = skip; jj < B; jj += skip) {
-                                const uint32_t b = (bead0 + jj) % M;
-                                if (b % a.R != r_own) continue;
-                                __syncthreads();
-                                if (tid < 2 * (int)n_d) {
-                                    const int which = tid / n_d, d = tid % n_d;
-                                    const double x = which ? seg_new[3 * jj + d] : seg_old[3 * jj + d];
-                                    PhaseRow(x, sys.box[d], sys.max_index[d], tab + ((size_t)which * 3 + d) * stride);
-                                }
-                                __syncthreads();
-                                const double2* rs = sys.rho_k + ((size_t)slot_s * M + b) * sys.K;
-                                for (uint32_t k = k_lo + tid; k < k_hi; k += blockDim.x) {
-                                    const int32_t pk = sys.kidx[k];
-                                    const double2 en = PhaseProduct(tab + 3 * stride, stride, n_d, pk);
-                                    const double2 eo = PhaseProduct(tab, stride, n_d, pk);
-                                    const double dx = en.x - eo.x, dy = en.y - eo.y;
-                                    const double2 rho = rs[k];
-                                    for (int pi = 0; pi < mv.n_pair; ++pi) {
-                                        const PairDev& pa = sys.pair[mv.pair[pi]];
-                                        if (!pa.use_long_range || (uint32_t)lvl > pa.max_level || pa.is_constant) continue;
-                                        const double vk = pa.v_long_k[k];
-                                        if (pa.sa == pa.sb) {
-                                            lr += vk * (dx * (2. * rho.x + dx) + dy * (2. * rho.y + dy));
-                                        } else {
-                                            const uint32_t o = pa.sa == s ? pa.sb : pa.sa;
-                                            const double2 ro = sys.rho_k[((size_t)sys.sp_rho[o] * M + b) * sys.K + k];
-                                            lr += 2. * vk * (dx * ro.x + dy * ro.y);
-                                        }
-                                    }
-                                }
-                            }
-                            acc += skip * sys.tau * lr;
-                        }
-                        // Grid reduction: block partial -> barrier -> identical ordered sum everywhere.
-                        const double bsum = BlockSum(acc, red);
-                        ++nbar;
-                        if (tid == 0) __stcg(&a.partials[(nbar & 1ull) * G + cta], bsum);
-                        if (!GridBarrier(a.bar, nbar, a.err, a.timeout_ns)) return;
-                        if (warp == 0) {
-                            double t = 0.;
-                            for (uint32_t c2 = lane; c2 < G; c2 += 32) t += __ldcg(&a.partials[(nbar & 1ull) * G + c2]);
-                            t = WarpSum(t);
-                            if (lane == 0) s_total = t;
-                        }
-                        __syncthreads();
-                        big = s_total;
+                        acc = Add(acc, Mul(a.tau, lr));
                     }
-
-                    // (3) Metropolis test (bisect_class.h:110-117), identical in every block.
-                    if (lvl == 0) my_reach0[m] += 1;
-                    if (tid == 0) {
-                        const double dS = s_small + big;
-                        const double log_sample_ratio = -s_lsp_new + s_lsp_old;
-                        const double log_accept = log_sample_ratio - dS + prev_dS;
-                        const double u = BisectAcceptUniform(st, B, mv.n_level - 1u - (uint32_t)lvl);
-                        int rej = log_accept < log(u) ? 1 : 0;
-                        if (!isfinite(log_accept)) {
-                            atomicCAS(a.err, 0, kDevErrNonFinite);
-                            rej = 2;
+                    // block sum (fixed order) -> partial -> grid barrier -> ordered total
+                    ++nbar;
+                    const dd v = WarpSumDD(acc);
+                    if (lane == 0) s_red[warp] = v;
+                    __syncthreads();
+                    PIMC_PHASE(3);
+                    if (warp == 0) {
+                        dd t = lane < kWarps ? s_red[lane] : dd{0.f, 0.f};
+                        t = WarpSumDD(t);
+                        if (lane == 0) __stcg(&a.partials[(nbar & 1ull) * G + cta], make_float2(t.hi, t.lo));
+                    }
+                    if (!GridBarrier(a.bar, nbar, a.err, a.timeout_ns)) return;
+                    PIMC_PHASE(4);
+                    if (warp == 0) {
+                        dd t{0.f, 0.f};
+                        for (uint32_t c2 = lane; c2 < G; c2 += 32) {
+                            const float2 pv = __ldcg(&a.partials[(nbar & 1ull) * G + c2]);
+                            t = Add(t, dd{pv.x, pv.y});
                         }
-                        s_reject = rej;
-                        s_dS = dS;
+                        t = WarpSumDD(t);
+                        if (lane == 0) s_big = t;
                     }
                     __syncthreads();
-                    const int rej = s_reject;
-                    const double dS_level = s_dS;
-                    __syncthreads();
-                    if (rej == 2) return;
-                    if (rej) {
-                        accepted = false;
-                        break;
-                    }
-                    prev_dS = dS_level;
+                    PIMC_PHASE(5);
+                } else if (tid == 0) {
+                    s_big = dd{0.f, 0.f};
                 }
 
-                if (accepted) {
-                    // bisect_class.h:24-36: commit the resampled beads (both copies).
+                // ---- 5. Metropolis tests of every level (bisect_class.h:110-117) ------------
+                // Level l's test reads only its own action change and the one of level l + 1 (the
+                // reference's prev_action_change), so lane l evaluates level l and the top-most
+                // failing level decides, as the reference's top-down loop would.
+                if (warp == 0) {
+                    const int lvl = lane;
+                    bool fail = false, bad = false;
+                    if (lvl < (int)nl) {
+                        dd dS = s_lvl_small[lvl];
+                        if (lvl == 0) dS = Add(dS, s_big);
+                        const dd prev = lvl + 1 < (int)nl ? s_lvl_small[lvl + 1] : dd{0.f, 0.f};
+                        const dd log_accept = Add(Sub(s_lvl_diff[lvl], dS), prev);
+                        bad = !isfinite(log_accept.hi);
+                        fail = bad || Less(log_accept, DD(logu[nl - 1 - lvl]));
+                    }
+                    const unsigned fm = __ballot_sync(0xffffffffu, fail);
+                    const unsigned bm = __ballot_sync(0xffffffffu, bad);
+                    if (lane == 0) {
+                        int res = 1, top = -1;
+                        if (fm) {
+                            top = 31 - __clz(fm);
+                            res = (bm >> top) & 1u ? 2 : 0;
+                            if (res == 2) atomicCAS(a.err, 0, kDevErrNonFinite);
+                        }
+                        s_result = res | ((top <= 0) ? 4 : 0);  // bit 2: the attempt reached level 0
+                    }
+                }
+                __syncthreads();
+                PIMC_PHASE(6);
+                const int res = s_result & 3;
+                if (res == 2) return;
+                if (s_result & 4) n_l0[m] += 1;
+
+                // ---- 6. commit ---------------------------------------------------------------
+                if (res == 1) {
                     for (uint32_t i = tid; i < (B - 1) * n_d; i += blockDim.x) {
                         const uint32_t j = 1 + i / n_d, d = i % n_d;
-                        const size_t idx = ((size_t)((bead0 + j) % M) * 3 + d) * np + g;
-                        sys.pos[idx] = seg_new[3 * j + d];
-                        sys.pos_new[idx] = seg_new[3 * j + d];
+                        const dd v = seg_new[3 * j + d];
+                        a.pos[((size_t)((bead0 + j) % M) * 3 + d) * np + g] = make_float2(v.hi, v.lo);
                     }
-                    // Per-slice charge densities (species_class.h:406-425 then StoreRhoK): only when a
-                    // long-range action of this move updated them.
-                    bool any_lr = false;
-                    for (int pi = 0; pi < mv.n_pair; ++pi) {
-                        const PairDev& pa = sys.pair[mv.pair[pi]];
-                        if (pa.use_long_range && !pa.is_constant) any_lr = true;
-                    }
-                    if (any_lr && owns_k && slot_s >= 0) {
-                        for (uint32_t jj = 1; jj < B; ++jj) {
-                            const uint32_t b = (bead0 + jj) % M;
-                            if (b % a.R != r_own) continue;
-                            __syncthreads();
-                            if (tid < 2 * (int)n_d) {
-                                const int which = tid / n_d, d = tid % n_d;
-                                const double x = which ? seg_new[3 * jj + d] : seg_old[3 * jj + d];
-                                PhaseRow(x, sys.box[d], sys.max_index[d], tab + ((size_t)which * 3 + d) * stride);
+                    if (any_lr) {
+                        const uint32_t nk = k_hi - k_lo;
+                        uint32_t ci = 0;
+                        for (uint32_t it = tid; it < n_own * nk; it += blockDim.x, ++ci) {
+                            const uint32_t si = it / nk, k = k_lo + it % nk;
+                            const uint32_t b = (bead0 + s_slice_jj[si]) % M;
+                            ddc dl;
+                            if (ci < kDeltaCache) {
+                                dl = delta_cache[ci];
+                            } else {
+                                const int32_t pk = a.kidx[k];
+                                dl = CSub(PhaseProductDD(tab_new + (size_t)si * 3 * stride, stride, n_d, pk),
+                                          PhaseProductDD(tab_old + (size_t)si * 3 * stride, stride, n_d, pk));
                             }
-                            __syncthreads();
-                            double2* rs = sys.rho_k + ((size_t)slot_s * M + b) * sys.K;
-                            for (uint32_t k = k_lo + tid; k < k_hi; k += blockDim.x) {
-                                const int32_t pk = sys.kidx[k];
-                                const double2 en = PhaseProduct(tab + 3 * stride, stride, n_d, pk);
-                                const double2 eo = PhaseProduct(tab, stride, n_d, pk);
-                                double2 v = rs[k];
-                                v.x += en.x - eo.x;
-                                v.y += en.y - eo.y;
-                                rs[k] = v;
-                            }
+                            float4* cell = &a.rho[((size_t)slot_s * M + b) * K + k];
+                            *cell = Pack(CAdd(Unpack(*cell), dl));
                         }
                     }
-                    my_accepts[m] += 1;
+                    n_acc[m] += 1;
                 }
                 __syncthreads();
+                PIMC_PHASE(7);
             }
         }
     }
-    if (cta == 0 && tid == 0)
-        for (int m = 0; m < kMaxMoves; ++m)
-            {
-                a.accepts[m] += my_accepts[m];
-                a.accepts[kMaxMoves + m] += my_reach0[m];
-            }
+#undef PIMC_PHASE
+    if (cta == 0 && tid == 0) {
+        for (int m = 0; m < kMaxMoves; ++m) {
+            a.counters[m] += n_acc[m];
+            a.counters[kMaxMoves + m] += n_l0[m];
+        }
+        if (timing)
+            for (int i = 0; i < kSweepPhases; ++i) a.phase_cycles[i] += ph[i];
+    }
+}
+
+// Conversions between the FP64 state and its double-float mirror.
+__global__ void ToDDKernel(const double* __restrict__ pos, float2* __restrict__ pos_dd, size_t n_pos, const double2* __restrict__ rho,
+                           float4* __restrict__ rho_dd, size_t n_rho) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_pos + n_rho; i += (size_t)gridDim.x * blockDim.x) {
+        if (i < n_pos) {
+            float h, l;
+            SplitDouble(pos[i], h, l);
+            pos_dd[i] = make_float2(h, l);
+        } else {
+            const double2 v = rho[i - n_pos];
+            float x0, x1, y0, y1;
+            SplitDouble(v.x, x0, x1);
+            SplitDouble(v.y, y0, y1);
+            rho_dd[i - n_pos] = make_float4(x0, x1, y0, y1);
+        }
+    }
+}
+
+__global__ void FromDDKernel(const float2* __restrict__ pos_dd, double* __restrict__ pos, double* __restrict__ pos_new, size_t n_pos,
+                             const float4* __restrict__ rho_dd, double2* __restrict__ rho, size_t n_rho) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_pos + n_rho; i += (size_t)gridDim.x * blockDim.x) {
+        if (i < n_pos) {
+            const float2 v = pos_dd[i];
+            const double x = (double)v.x + (double)v.y;
+            pos[i] = x;
+            pos_new[i] = x;
+        } else {
+            const float4 v = rho_dd[i - n_pos];
+            rho[i - n_pos] = make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+        }
+    }
+}
+
+void Split(double x, dd& out) {
+    float h, l;
+    SplitDouble(x, h, l);
+    out = dd{h, l};
 }
 
 }  // namespace
 
 // ---------------------------------------------------------------------------------------------
 
+void Context::EnsureDD() {
+    if (dd_valid) return;
+    const size_t n_pos = (size_t)sys.M * 3 * sys.n_pad;
+    const size_t n_rho = (rho_slots && sys.K) ? (size_t)rho_slots * sys.M * sys.K : 0;
+    if (!pos_dd_) pos_dd_.reset(new DeviceBuffer(n_pos * sizeof(float2)));
+    if (!rho_dd_) rho_dd_.reset(new DeviceBuffer(std::max<size_t>(n_rho, 1) * sizeof(float4)));
+    ToDDKernel<<<n_sm * 4, 256, 0, stream>>>(sys.pos, pos_dd_->as<float2>(), n_pos, sys.rho_k, rho_dd_->as<float4>(), n_rho);
+    CudaCheck(cudaGetLastError(), "to-dd launch");
+    dd_valid = true;
+}
+
+void Context::EnsureFP64() {
+    if (fp64_valid) return;
+    const size_t n_pos = (size_t)sys.M * 3 * sys.n_pad;
+    const size_t n_rho = (rho_slots && sys.K) ? (size_t)rho_slots * sys.M * sys.K : 0;
+    FromDDKernel<<<n_sm * 4, 256, 0, stream>>>(pos_dd_->as<float2>(), sys.pos, sys.pos_new, n_pos, rho_dd_->as<float4>(), sys.rho_k, n_rho);
+    CudaCheck(cudaGetLastError(), "from-dd launch");
+    Sync();
+    fp64_valid = true;
+}
+
+static CubicDD MakeCubicDD(Context& c, const CubicTable& t, std::vector<std::unique_ptr<DeviceBuffer>>& keep) {
+    CubicDD o;
+    if (!t.c) return o;
+    const Context::HostCubic* h = nullptr;
+    for (auto& kv : c.host_cubics)
+        if (kv.first == t.c) h = &kv.second;
+    if (!h) throw PimcError(kErrState, "spline table without host copy");
+    std::vector<float2> x(h->x.size());
+    for (size_t i = 0; i < x.size(); ++i) {
+        float hi, lo;
+        SplitDouble(h->x[i], hi, lo);
+        x[i] = make_float2(hi, lo);
+    }
+    std::vector<float4> cf(2 * h->c.size());
+    for (size_t i = 0; i < h->c.size(); ++i) {
+        float a0, a1, b0, b1, c0, c1, d0, d1;
+        SplitDouble(h->c[i].c0, a0, a1);
+        SplitDouble(h->c[i].c1, b0, b1);
+        SplitDouble(h->c[i].c2, c0, c1);
+        SplitDouble(h->c[i].c3, d0, d1);
+        cf[2 * i] = make_float4(a0, a1, b0, b1);
+        cf[2 * i + 1] = make_float4(c0, c1, d0, d1);
+    }
+    keep.emplace_back(new DeviceBuffer(x.size() * sizeof(float2)));
+    CudaCheck(cudaMemcpy(keep.back()->ptr, x.data(), x.size() * sizeof(float2), cudaMemcpyHostToDevice), "dd knots");
+    o.x = keep.back()->as<float2>();
+    keep.emplace_back(new DeviceBuffer(cf.size() * sizeof(float4)));
+    CudaCheck(cudaMemcpy(keep.back()->ptr, cf.data(), cf.size() * sizeof(float4), cudaMemcpyHostToDevice), "dd coefficients");
+    o.c = keep.back()->as<float4>();
+    o.bucket = t.bucket;
+    o.n = t.n;
+    o.n_bucket = t.n_bucket;
+    o.uniform = t.uniform;
+    o.x0f = (float)t.x0;
+    o.inv_dxf = (float)t.inv_dx;
+    // A grid whose spacing is uniform to within a quarter step locates its interval arithmetically
+    // (the evaluator's scan corrects the estimate by one either way), skipping the bucket table.
+    if (!o.uniform && h->x.size() >= 2) {
+        const double step = (h->x.back() - h->x.front()) / (double)(h->x.size() - 1);
+        bool near_uniform = step > 0.;
+        for (size_t i = 0; near_uniform && i + 1 < h->x.size(); ++i)
+            near_uniform = std::fabs((h->x[i + 1] - h->x[i]) - step) <= 0.25 * step;
+        if (near_uniform) {
+            o.uniform = 1;
+            o.inv_dxf = (float)(1. / step);
+        }
+    }
+    Split(t.x0, o.x0);
+    Split(t.x1, o.x1);
+    return o;
+}
+
+void Context::BuildSweepTables() {
+    if (sweep_tables_built_) return;
+    std::vector<float4> tab(256);
+    for (int j = 0; j < 256; ++j) {
+        const double th = 2. * M_PI * j / 256.;
+        float a0, a1, b0, b1;
+        SplitDouble(std::cos(th), a0, a1);
+        SplitDouble(std::sin(th), b0, b1);
+        tab[j] = make_float4(a0, a1, b0, b1);
+    }
+    sweep_tables_.reset(new DeviceBuffer(sizeof(float4) * 256 + sizeof(PairDD) * kMaxPair));
+    CudaCheck(cudaMemcpy(sweep_tables_->ptr, tab.data(), sizeof(float4) * 256, cudaMemcpyHostToDevice), "phase table");
+    std::vector<PairDD> pd(kMaxPair);
+    // Identical tables (one file read by several pair actions) share one device copy.
+    std::vector<std::pair<const HostCubic*, CubicDD>> made;
+    auto make = [&](const CubicTable& t) -> CubicDD {
+        const HostCubic* h = nullptr;
+        for (auto& kv : host_cubics)
+            if (kv.first == t.c) h = &kv.second;
+        for (auto& mk : made)
+            if (h && mk.first->x == h->x && mk.first->c.size() == h->c.size() &&
+                std::memcmp(mk.first->c.data(), h->c.data(), h->c.size() * sizeof(Cubic4)) == 0)
+                return mk.second;
+        CubicDD o = MakeCubicDD(*this, t, keep_);
+        if (h) made.push_back({h, o});
+        return o;
+    };
+    for (int i = 0; i < sys.n_pair; ++i) {
+        const PairDev& p = sys.pair[i];
+        PairDD& q = pd[i];
+        q.sa = p.sa;
+        q.sb = p.sb;
+        q.is_coulomb = p.is_coulomb;
+        q.use_lr = p.use_long_range;
+        q.is_constant = p.is_constant;
+        q.max_level = (int32_t)p.max_level;
+        q.slot_a = sys.sp_rho[p.sa];
+        q.slot_b = sys.sp_rho[p.sb];
+        Split(p.r_v_min, q.rvmin);
+        Split(p.r_v_max, q.rvmax);
+        Split(p.r_vl_min, q.rvlmin);
+        Split(p.r_vl_max, q.rvlmax);
+        q.v_r = make(p.v_r);
+        q.v_long_r = p.use_long_range ? make(p.v_long_r) : CubicDD();
+        q.vk = nullptr;
+        if (p.use_long_range) {
+            std::vector<float2> vk(sys.K);
+            for (uint32_t k = 0; k < sys.K; ++k) {
+                float hi, lo;
+                SplitDouble(host_vk[i][k], hi, lo);
+                vk[k] = make_float2(hi, lo);
+            }
+            keep_.emplace_back(new DeviceBuffer(sys.K * sizeof(float2)));
+            CudaCheck(cudaMemcpy(keep_.back()->ptr, vk.data(), sys.K * sizeof(float2), cudaMemcpyHostToDevice), "dd vk");
+            q.vk = keep_.back()->as<float2>();
+        }
+    }
+    CudaCheck(cudaMemcpy(sweep_tables_->as<char>() + sizeof(float4) * 256, pd.data(), sizeof(PairDD) * kMaxPair, cudaMemcpyHostToDevice),
+              "pair descriptors");
+    // Tables worth staging in shared memory: the pair actions' spline tables, once each.
+    stage_tables_.clear();
+    for (int i = 0; i < sys.n_pair; ++i) {
+        const CubicDD* ts[2] = {&pd[i].v_long_r, &pd[i].v_r};
+        const bool used[2] = {pd[i].use_lr != 0, pd[i].is_coulomb == 0};
+        for (int j = 0; j < 2; ++j) {
+            if (!used[j] || !ts[j]->x) continue;
+            bool seen = false;
+            for (auto& st : stage_tables_) seen |= (st.x == ts[j]->x);
+            if (!seen) stage_tables_.push_back(StageTable{ts[j]->x, ts[j]->c, (uint32_t)ts[j]->n});
+        }
+    }
+    // Double-float sampling/kinetic spline tables are built per move (they depend on n_images).
+    sweep_tables_built_ = true;
+}
+
 void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep) {
     if (n_entries == 0 || n_rep == 0) return;
+    if (n_entries > 1024) throw PimcError(kErrArg, "schedule longer than 1024 entries");
     for (uint32_t e = 0; e < n_entries; ++e)
         if (mv[e] >= moves.size()) throw PimcError(kErrArg, "move index out of range");
-    static_assert(sizeof(SweepArgs) < 30000, "sweep arguments exceed the kernel parameter space");
-    SweepArgs* args = new SweepArgs();
-    std::unique_ptr<SweepArgs> guard(args);
-    args->sys = sys;
+    BuildSweepTables();
+    // Move descriptors, rebuilt when a level changes (adaptive bisection between blocks).
     uint32_t max_level = 1;
     for (size_t m = 0; m < moves.size(); ++m) {
-        args->moves[m] = moves[m].dev;
-        args->attempt_base[m] = moves[m].attempts;
-        max_level = std::max(max_level, moves[m].dev.n_level);
+        const MoveDev& d = moves[m].dev;
+        if (d.n_level > 8) throw PimcError(kErrUnsupported, "bisection level above 8 in the sweep kernel");
+        max_level = std::max(max_level, d.n_level);
+        for (int i = 0; i < d.n_pair; ++i) {
+            const PairDev& p = sys.pair[d.pair[i]];
+            if (p.use_long_range && p.max_level > 0)
+                throw PimcError(kErrUnsupported, "long-range pair action with max_level > 0 in the sweep kernel");
+        }
+        if (d.n_kinetic > kMoveKinetic) throw PimcError(kErrUnsupported, "more than two kinetic actions on one species");
     }
-    if (max_level > 10) throw PimcError(kErrUnsupported, "bisection level above 10 in the sweep kernel");
-    // Schedule upload (entries then counts).
-    std::vector<uint32_t> sm(mv, mv + n_entries);
-    std::vector<uint64_t> sc(counts, counts + n_entries);
-    if (!sched_) {
-        sched_.reset(new DeviceBuffer(1024 * 12));
-        accepts_.reset(new DeviceBuffer(2 * kMaxMoves * sizeof(unsigned long long)));
+    std::vector<uint32_t> levels(moves.size());
+    for (size_t m = 0; m < moves.size(); ++m) levels[m] = moves[m].dev.n_level;
+    if (!sweep_desc_) sweep_desc_.reset(new DeviceBuffer(sizeof(MoveDD) * kMaxMoves + 4096 + 8192 + 2 * kMaxMoves * 8));
+    char* base = sweep_desc_->as<char>();
+    MoveDD* dmoves = reinterpret_cast<MoveDD*>(base);
+    uint32_t* dsm = reinterpret_cast<uint32_t*>(base + sizeof(MoveDD) * kMaxMoves);
+    uint64_t* dsc = reinterpret_cast<uint64_t*>(base + sizeof(MoveDD) * kMaxMoves + 4096);
+    unsigned long long* dcount = reinterpret_cast<unsigned long long*>(base + sizeof(MoveDD) * kMaxMoves + 4096 + 8192);
+    if (levels != desc_levels_) {
+        std::vector<MoveDD> md(kMaxMoves, MoveDD{});
+        for (size_t m = 0; m < moves.size(); ++m) {
+            const MoveDev& d = moves[m].dev;
+            MoveDD& o = md[m];
+            o.species = d.species;
+            o.n_level = d.n_level;
+            o.has_images = d.has_images;
+            for (uint32_t l = 0; l < d.n_level; ++l) {
+                Split(std::sqrt(d.lambda * (sys.tau * (1u << l))), o.sigma[l]);
+                Split(d.i4lt_sample[l], o.i4s[l]);
+                o.sample_image[l] = d.has_images ? MakeCubicDD(*this, d.sample_image[l], keep_) : CubicDD();
+            }
+            o.n_kin = d.n_kinetic;
+            for (int i = 0; i < d.n_kinetic; ++i) {
+                const KineticDev& k = sys.kinetic[d.kinetic[i]];
+                o.kin_has_images[i] = k.has_images;
+                for (uint32_t l = 0; l < d.n_level; ++l) {
+                    if (k.image[l].n == 0) throw PimcError(kErrInput, "kinetic spline missing for a bisection level");
+                    Split(k.i4lt_level[l], o.kin_i4[i][l]);
+                    o.kin_image[i][l] = k.has_images ? MakeCubicDD(*this, k.image[l], keep_) : CubicDD();
+                }
+            }
+            o.n_trap = d.n_trap;
+            for (int i = 0; i < d.n_trap; ++i) {
+                o.trap_max_level[i] = sys.trap[d.trap[i]].max_level;
+                Split(sys.trap[d.trap[i]].cofactor_a, o.trap_cofa[i]);
+            }
+            o.n_pair = d.n_pair;
+            for (int i = 0; i < d.n_pair; ++i) o.pair[i] = d.pair[i];
+        }
+        CudaCheck(cudaMemcpyAsync(dmoves, md.data(), sizeof(MoveDD) * kMaxMoves, cudaMemcpyHostToDevice, stream), "move descriptors");
+        Sync();
+        desc_levels_ = levels;
     }
-    if (n_entries > 1024) throw PimcError(kErrArg, "schedule longer than 1024 entries");
-    uint32_t* dsm = sched_->as<uint32_t>();
-    uint64_t* dsc = reinterpret_cast<uint64_t*>(sched_->as<char>() + 4096);
-    CudaCheck(cudaMemcpyAsync(dsm, sm.data(), n_entries * 4, cudaMemcpyHostToDevice, stream), "schedule upload");
-    CudaCheck(cudaMemcpyAsync(dsc, sc.data(), n_entries * 8, cudaMemcpyHostToDevice, stream), "schedule upload");
+    CudaCheck(cudaMemcpyAsync(dsm, mv, n_entries * 4, cudaMemcpyHostToDevice, stream), "schedule");
+    CudaCheck(cudaMemcpyAsync(dsc, counts, n_entries * 8, cudaMemcpyHostToDevice, stream), "schedule");
+    CudaCheck(cudaMemsetAsync(dcount, 0, 2 * kMaxMoves * 8, stream), "counters");
+    EnsureDD();
+
+    SweepArgs* args = new SweepArgs();
+    std::unique_ptr<SweepArgs> guard(args);
+    args->n_d = sys.n_d;
+    args->M = sys.M;
+    args->n_pad = sys.n_pad;
+    args->K = sys.K;
+    Split(sys.L, args->L);
+    Split(sys.iL, args->iL);
+    Split(sys.tau, args->tau);
+    Split(2. * M_PI, args->two_pi);
+    for (int s = 0; s < kMaxSpecies; ++s) {
+        args->sp_off[s] = sys.sp_off[s];
+        args->sp_n[s] = sys.sp_n[s];
+    }
+    for (int d = 0; d < 3; ++d) args->max_index[d] = sys.max_index[d];
+    args->pos = pos_dd_->as<float2>();
+    args->rho = rho_dd_->as<float4>();
+    args->kidx = sys.kidx;
+    args->phase256 = sweep_tables_->as<float4>();
+    args->moves = dmoves;
+    args->pairs = reinterpret_cast<const PairDD*>(sweep_tables_->as<char>() + sizeof(float4) * 256);
+    for (size_t m = 0; m < moves.size(); ++m) args->attempt_base[m] = moves[m].attempts;
     args->sched_move = dsm;
     args->sched_count = dsc;
     args->n_entries = n_entries;
@@ -386,41 +919,76 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
     args->seed = seed;
     args->chain = chain;
     args->seg_cap = (1u << max_level) + 1;
-    args->tab_stride = std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
-    const size_t smem = (size_t)2 * 3 * args->seg_cap * sizeof(double) + 32 * sizeof(double) + (size_t)2 * 3 * args->tab_stride * sizeof(double2);
-    CudaCheck(cudaFuncSetAttribute(BisectSweepKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attribute");
-    int occ = 0;
-    CudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, BisectSweepKernel, kSweepThreads, smem), "occupancy");
-    if (occ < 1) throw PimcError(kErrCuda, "sweep kernel cannot be resident");
-    int G = sweep_grid > 0 ? std::min(sweep_grid, occ * n_sm) : std::min(occ, 2) * n_sm;
-    // Ownership of slices: R residue classes (a power of two up to the segment length).
+    args->tab_stride = (uint32_t)std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
+
+    const int G = sweep_grid > 0 ? sweep_grid : n_sm;
     uint32_t R = 1;
     while (R * 2 <= (1u << max_level) && R * 2 <= (uint32_t)G) R *= 2;
+    const uint32_t spc = std::max<uint32_t>(1, (1u << max_level) / R);
+    if (spc > kMaxOwned) throw PimcError(kErrUnsupported, "too few blocks for the segment length");
     args->R = R;
     args->Q = std::max<uint32_t>(1, (uint32_t)G / R);
-    args->accepts = accepts_->as<unsigned long long>();
+    args->slices_per_cta = spc;
+    // Shared layout: [move descriptors][pair descriptors][phase table][staged splines][work area].
+    auto align16 = [](size_t x) { return (x + 15) & ~size_t(15); };
+    const size_t work = (size_t)2 * spc * 3 * args->tab_stride * sizeof(ddc) + (size_t)4 * 3 * args->seg_cap * sizeof(dd) +
+                        (size_t)3 * args->seg_cap * sizeof(float) + kMaxLevels * sizeof(float);
+    size_t off = 0;
+    args->n_moves = (uint32_t)moves.size();
+    args->n_pairs = (uint32_t)sys.n_pair;
+    args->off_moves = (uint32_t)off;
+    off = align16(off + moves.size() * sizeof(MoveDD));
+    args->off_pairs = (uint32_t)off;
+    off = align16(off + (size_t)sys.n_pair * sizeof(PairDD));
+    args->off_phase = (uint32_t)off;
+    off += 256 * sizeof(float4);
+    const size_t smem_cap = 200 * 1024;
+    args->n_stage = 0;
+    for (const auto& st : stage_tables_) {
+        const size_t bx = align16((size_t)st.n * sizeof(float2)), bc = (size_t)2 * (st.n - 1) * sizeof(float4);
+        if (off + bx + bc + work > smem_cap || args->n_stage >= (uint32_t)kMaxPair) continue;  // stays in global memory
+        const uint32_t j = args->n_stage++;
+        args->stage_x[j] = static_cast<const float2*>(st.x);
+        args->stage_c[j] = static_cast<const float4*>(st.c);
+        args->stage_n[j] = st.n;
+        args->stage_off_x[j] = (uint32_t)off;
+        args->stage_off_c[j] = (uint32_t)(off + bx);
+        off = align16(off + bx + bc);
+    }
+    args->off_work = (uint32_t)off;
+    const size_t smem = off + work;
+    CudaCheck(cudaFuncSetAttribute(BisectSweepKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attribute");
+    int occ = 0;
+    CudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, BisectSweepKernel, kThreads, smem), "occupancy");
+    if (occ < 1) throw PimcError(kErrCuda, "sweep kernel cannot be resident");
+    if (G > occ * n_sm) throw PimcError(kErrArg, "sweep grid larger than the co-resident limit");
+    args->counters = dcount;
     args->bar = Barrier();
     args->err = ErrWord();
-    args->partials = Partials((size_t)2 * G);
+    args->partials = reinterpret_cast<float2*>(Partials((size_t)2 * G));
     args->timeout_ns = timeout_ns;
-    CudaCheck(cudaMemsetAsync(accepts_->ptr, 0, 2 * kMaxMoves * sizeof(unsigned long long), stream), "reset accepts");
+    args->phase_cycles = nullptr;
+    if (phase_timing) {
+        if (!phase_buf) phase_buf.reset(new DeviceBuffer(kSweepPhases * sizeof(unsigned long long)));
+        args->phase_cycles = phase_buf->as<unsigned long long>();
+    }
     CudaCheck(cudaMemsetAsync(Barrier(), 0, sizeof(unsigned long long), stream), "reset barrier");
     void* kargs[] = {args};
-    CudaCheck(cudaLaunchCooperativeKernel((void*)BisectSweepKernel, dim3(G), dim3(kSweepThreads), kargs, smem, stream), "sweep launch");
-    std::vector<unsigned long long> acc(2 * kMaxMoves);
-    CudaCheck(cudaMemcpyAsync(acc.data(), accepts_->ptr, 2 * kMaxMoves * sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream), "read accepts");
+    CudaCheck(cudaLaunchCooperativeKernel((void*)BisectSweepKernel, dim3(G), dim3(kThreads), kargs, smem, stream), "sweep launch");
+    fp64_valid = false;
+    std::vector<unsigned long long> cnt(2 * kMaxMoves);
+    CudaCheck(cudaMemcpyAsync(cnt.data(), dcount, 2 * kMaxMoves * 8, cudaMemcpyDeviceToHost, stream), "read counters");
     Sync();
     CheckDeviceError();
-    // Host bookkeeping of the attempt counters (they define the Philox streams).
     std::vector<uint64_t> per_move(moves.size(), 0);
     for (uint32_t e = 0; e < n_entries; ++e) per_move[mv[e]] += counts[e];
     for (size_t m = 0; m < moves.size(); ++m) {
         const uint64_t n = per_move[m] * n_rep;
         moves[m].attempts += n;
         moves[m].block_attempt += n;
-        moves[m].block_accept += acc[m];
-        moves[m].total_accept += acc[m];
-        moves[m].total_level0 += acc[kMaxMoves + m];
+        moves[m].block_accept += cnt[m];
+        moves[m].total_accept += cnt[m];
+        moves[m].total_level0 += cnt[kMaxMoves + m];
     }
     last_grid_ = G;
 }
@@ -449,9 +1017,8 @@ void Context::WriteBlock() {
     }
 }
 
-// Loop::DoEvent (loop_class.h:269-274). Consecutive move events are batched into one launch.
+// Loop::DoEvent (loop_class.h:269-274). Consecutive move events run as one launch.
 void Context::RunNode(const LoopNode& n) {
-    // A loop body made only of moves runs as one sweep schedule repeated n_steps times.
     bool only_moves = !n.children.empty();
     for (auto& c : n.children) only_moves &= (c.kind == 1);
     if (only_moves) {

@@ -140,6 +140,7 @@ double GetActionNoAlloc(pimc::Context& c, uint32_t ai, uint32_t b0, uint32_t b1,
     if (b1 < b0 || b0 >= c.sys.M || b1 - b0 > c.sys.M) throw PimcError(PIMC_ERR_ARG, "slice range out of bounds");
     const pimc::ActionHost& ah = c.actions[ai];
     if (ah.kind != 2) throw PimcError(PIMC_ERR_UNSUPPORTED, "pimc_get_action_noalloc evaluates pair actions only");
+    c.EnsureFP64();  // a conversion kernel when a sweep ran since the last FP64 read; no allocation
     const pimc::SystemDev& sys = c.sys;
     const pimc::PairDev pa = sys.pair[ah.index];
     if (level > pa.max_level || pa.is_constant) return 0.;

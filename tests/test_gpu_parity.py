@@ -170,5 +170,8 @@ def test_observables_blocks(tmp_path, gpu_lib, oracle_mod):
             c.observable_accumulate(o)
     eg, ec = g.observable_block(0), c.observable_block(0)
     assert eg.shape == ec.shape and close(eg, ec, 1e-8), (eg, ec)
+    # g(r): integer bin counts must agree exactly; the shell-volume normalisation is host FP64 and
+    # may differ in the last bit with the compilers' contraction choices.
     hg, hc = g.observable_block(1), c.observable_block(1)
-    np.testing.assert_array_equal(hg, hc)
+    np.testing.assert_array_equal(hg == 0, hc == 0)
+    np.testing.assert_allclose(hg, hc, rtol=1e-13, atol=0)
