@@ -120,6 +120,17 @@ def algorithmic_bytes(sim, counters_before, counters_after, n_k):
     return total
 
 
+def reduce_max_over_ranks(values, dist=None, device=None):
+    """Element-wise maximum of per-rank timings: the slowest replica sets the job time. Chains are
+    independent replicas (no data exchange), so this is the only collective of the benchmark."""
+    if dist is None or not dist.is_initialized():
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 def run_ours(args):
     import torch
     from simpimc_gb300 import Simulation
@@ -182,10 +193,7 @@ def run_ours(args):
         sampler.terminate()
         sampler.wait()
 
-    ms_t = torch.tensor([ms, e2e_ms], dtype=torch.float64, device=f"cuda:{local}")
-    if dist:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms_max, e2e_max = float(ms_t[0]), float(ms_t[1])
+    ms_max, e2e_max = reduce_max_over_ranks([ms, e2e_ms], dist, device=f"cuda:{local}")
     total_moves = bead_moves_per_step * args.steps * world
     value = total_moves / (ms_max / 1e3)
     e2e_value = total_moves / (e2e_max / 1e3)

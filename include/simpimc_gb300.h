@@ -117,9 +117,12 @@ int pimc_set_timeout_ns(pimc_ctx* ctx, uint64_t ns);
 void* pimc_stream(pimc_ctx* ctx);
 /* Sweep tracing, the device-side analogue of the reference's per-event timers (move_class.h:61-77,
  * time_class.h:38-68): cycles spent by block 0 in the 8 phases of each attempt (segment and random
- * numbers, sampling, per-level terms, grid work, grid barrier, final sum, decision, commit).
- * `cycles` (8 entries, may be NULL) receives the sums since the last reset; `enable` >= 0 switches
- * recording on/off and resets the sums (-1 leaves both as they are). */
+ * numbers, sampling, per-level terms, grid work, grid barrier, final sum, decision, commit),
+ * followed by the slowest warp of each of 8 roles inside phases 2-4 (sampling chain, stored-copy
+ * level sums, old phase tables, stored-copy pair links, working-copy level sums, new phase tables,
+ * old Ewald phases, grid-phase pair links and Ewald cells). `cycles` (16 entries, may be NULL)
+ * receives the sums since the last reset; `enable` >= 0 switches recording on/off and resets the
+ * sums (-1 leaves both as they are). */
 int pimc_sweep_timing(pimc_ctx* ctx, int enable, uint64_t* cycles);
 
 #ifdef __cplusplus

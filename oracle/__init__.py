@@ -76,6 +76,22 @@ def lib():
     return _lib
 
 
+def bisect_draws(seed, chain, move, attempt, n_part, n_bead, n_level):
+    """(particle, first bead), normals [(2^l - 1), 3] and per-level log-uniforms of one attempt."""
+    L = lib()
+    fn = L.oracle_bisect_draws
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, _U32P,
+                   C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    B = 1 << n_level
+    pb = np.zeros(2, dtype=np.uint32)
+    z = np.zeros((B - 1, 3), dtype=np.float32)
+    lu = np.zeros(n_level, dtype=np.float32)
+    fn(seed, chain, move, attempt, n_part, n_bead, n_level, pb.ctypes.data_as(_U32P), z.ctypes.data_as(C.POINTER(C.c_float)),
+       lu.ctypes.data_as(C.POINTER(C.c_float)))
+    return pb, z, lu
+
+
 def philox(ctr, key):
     c = np.ascontiguousarray(ctr, dtype=np.uint32)
     k = np.ascontiguousarray(key, dtype=np.uint32)

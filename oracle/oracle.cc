@@ -1753,6 +1753,25 @@ int oracle_get_block(void* h, uint32_t o, uint64_t blk, double* out, uint64_t ca
     return 0;
 }
 
+// Draws of one bisection attempt: p, bead0, the 3 normals of each of the (n_bisect - 1) beads and
+// the acceptance logarithm of each level, as the move consumes them.
+int oracle_bisect_draws(uint32_t seed, uint32_t chain, uint32_t move, uint64_t attempt, uint32_t n_part, uint32_t n_bead, uint32_t n_level,
+                        uint32_t* pb, float* z, float* logu) {
+    orc::Stream st{seed, chain, move, attempt};
+    orc::RNG4 w0 = st.block(0);
+    pb[0] = orc::uidx(w0.w[0], n_part);
+    pb[1] = orc::uidx(w0.w[1], n_bead);
+    const uint32_t B = 1u << n_level;
+    for (uint32_t i = 0; i + 1 < B; ++i) {
+        orc::RNG4 w = st.block(1u + i);
+        float z3;
+        orc::boxmuller(w.w[0], w.w[1], z[3 * i], z[3 * i + 1]);
+        orc::boxmuller(w.w[2], w.w[3], z[3 * i + 2], z3);
+    }
+    for (uint32_t li = 0; li < n_level; ++li) logu[li] = orc::logf_spec(orc::u24(st.block(1u + (B - 1u) + li).w[0]));
+    return 0;
+}
+
 int oracle_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {
     uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
     orc::RNG4 r = orc::philox(c, key[0], key[1]);

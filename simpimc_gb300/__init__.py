@@ -81,7 +81,9 @@ SIGNATURES = {
     "pimc_sweep_timing": (C.c_int, [_P, C.c_int, _U64P]),
 }
 
-SWEEP_PHASES = ("segment+rng", "sampling", "level terms", "grid work", "grid barrier", "final sum", "decision", "commit")
+SWEEP_PHASES = ("segment+rng", "sampling", "level terms", "grid work", "grid barrier", "final sum", "decision", "commit",
+                "role:sampling chain", "role:stored level sums", "role:old tables", "role:stored pair links",
+                "role:working level sums", "role:new tables", "role:old Ewald phases", "role:grid pair+Ewald")
 
 _lib = None
 

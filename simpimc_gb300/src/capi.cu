@@ -231,15 +231,15 @@ void* pimc_stream(pimc_ctx* ctx) { return ctx && ctx->c ? (void*)ctx->c->stream 
 int pimc_sweep_timing(pimc_ctx* ctx, int enable, uint64_t* cycles) {
     return Guard(ctx, [&](pimc::Context& c) {
         if (cycles) {
-            for (int i = 0; i < pimc::kSweepPhases; ++i) cycles[i] = 0;
+            for (int i = 0; i < pimc::kSweepTimingSlots; ++i) cycles[i] = 0;
             if (c.phase_buf) {
-                pimc::CudaCheck(cudaMemcpy(cycles, c.phase_buf->ptr, pimc::kSweepPhases * sizeof(uint64_t), cudaMemcpyDeviceToHost),
+                pimc::CudaCheck(cudaMemcpy(cycles, c.phase_buf->ptr, pimc::kSweepTimingSlots * sizeof(uint64_t), cudaMemcpyDeviceToHost),
                                 "read phase timing");
             }
         }
         if (enable >= 0) {
             c.phase_timing = enable != 0;
-            if (c.phase_buf) pimc::CudaCheck(cudaMemset(c.phase_buf->ptr, 0, pimc::kSweepPhases * sizeof(uint64_t)), "reset phase timing");
+            if (c.phase_buf) pimc::CudaCheck(cudaMemset(c.phase_buf->ptr, 0, pimc::kSweepTimingSlots * sizeof(uint64_t)), "reset phase timing");
         }
     });
 }

@@ -36,6 +36,11 @@ constexpr int kMaxSegment = 1 << kMaxLevels;
 // Phases of one bisection attempt timed by the sweep kernel's optional tracing: segment and random
 // numbers, sampling chain, per-level terms, grid work, grid barrier, final sum, decision, commit.
 constexpr int kSweepPhases = 8;
+// Extra tracing slots: the slowest warp of each role inside phases 2-4 (cycles from the phase
+// start): sampling chain, stored-copy level sums, old phase tables, stored-copy pair links,
+// working-copy level sums, new phase tables, old Ewald phases, grid-phase pair links + Ewald cells.
+constexpr int kSweepRoles = 8;
+constexpr int kSweepTimingSlots = kSweepPhases + kSweepRoles;
 
 // Error word values written by kernels (read back by the host as PIMC_ERR_*).
 constexpr int kDevErrTimeout = 1;

@@ -49,8 +49,17 @@ __device__ __forceinline__ dd TwoProd(float a, float b) {
     return dd{p, e};
 }
 
-/// Accurate df64 addition (IEEE-style: both error terms carried).
+/// df64 addition in the "sloppy" form of the double-double libraries: TwoSum of the high parts,
+/// low parts added, one renormalisation. Its error is within a few units of 2^-46 of |a| + |b|,
+/// which is the accuracy every use here needs (sums of positions, distances and action terms).
 __device__ __forceinline__ dd Add(dd a, dd b) {
+    dd s = TwoSum(a.hi, b.hi);
+    s.lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+    return FastTwoSum(s.hi, s.lo);
+}
+
+/// df64 addition carrying both error terms (for long accumulations of cancelling terms).
+__device__ __forceinline__ dd AddAccurate(dd a, dd b) {
     dd s = TwoSum(a.hi, b.hi);
     dd t = TwoSum(a.lo, b.lo);
     s.lo = __fadd_rn(s.lo, t.hi);
@@ -160,6 +169,20 @@ __device__ __forceinline__ dd WarpSumDD(dd v) {
         v = Add(v, w);
     }
     return v;
+}
+
+/// Two warp-wide df64 sums in one shuffle tree (the two chains interleave).
+__device__ __forceinline__ void WarpSum2DD(dd& a, dd& b) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        dd wa, wb;
+        wa.hi = __shfl_xor_sync(0xffffffffu, a.hi, o);
+        wa.lo = __shfl_xor_sync(0xffffffffu, a.lo, o);
+        wb.hi = __shfl_xor_sync(0xffffffffu, b.hi, o);
+        wb.lo = __shfl_xor_sync(0xffffffffu, b.lo, o);
+        a = Add(a, wa);
+        b = Add(b, wb);
+    }
 }
 
 }  // namespace pimc

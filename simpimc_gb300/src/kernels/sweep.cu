@@ -94,6 +94,7 @@ struct SweepArgs {
     unsigned long long* bar;
     int* err;
     float2* partials;         // [2][gridDim.x]
+    float4* level_out;        // [2][kMaxLevels]: (diff, small) of each level from its designated block
     uint64_t timeout_ns;
     unsigned long long* phase_cycles;  // optional [kSweepPhases]: block 0's cycles per phase, summed
     // Shared-memory staging (byte offsets into the dynamic shared block).
@@ -255,8 +256,66 @@ __device__ __forceinline__ void LevelSums(const MoveDD& mv, int lvl, uint32_t B,
             for (uint32_t d = 0; d < n_d; ++d) acc = Add(acc, Sqr(seg[3 * j + d]));
         sm = Add(sm, MulF(Mul(acc, mv.trap_cofa[ti]), (float)skip));
     }
-    lsp = Neg(WarpSumDD(sp));
-    small = WarpSumDD(sm);
+    WarpSum2DD(sp, sm);
+    lsp = Neg(sp);
+    small = sm;
+}
+
+__device__ __forceinline__ dd ShflXorDD(dd v, int m) {
+    return dd{__shfl_xor_sync(0xffffffffu, v.hi, m), __shfl_xor_sync(0xffffffffu, v.lo, m)};
+}
+
+/// One radius' share of BarePairAction::CalcV (bare_pair_action_class.h:99-123):
+/// 1/(2r) (or v(r)/2 from the table) minus v_long(r)/2, with the reference's clamps.
+__device__ __forceinline__ dd PairHalfV(const PairDD& pa, dd r) {
+    r = Min(Max(r, pa.rvmin), pa.rvmax);
+    dd v = pa.is_coulomb ? Scale2(Div(DD(1.f), r), 0.5f) : Scale2(EvalCubicDD(pa.v_r, r), 0.5f);
+    if (pa.use_lr) v = Sub(v, Scale2(EvalCubicDD(pa.v_long_r, Min(Max(r, pa.rvlmin), pa.rvlmax)), 0.5f));
+    return v;
+}
+
+/// U = tau V of pair link l (level 0) for one copy of the moved particle's segment, evaluated by a
+/// quad of lanes: lanes 0-2 take one Cartesian component of Path::DrDrpDrrp (path_class.h:137-150)
+/// each, lanes 0 and 1 then take r and r'. Every lane of the warp must call it; the result is
+/// returned on lane 0 of the quad (zero elsewhere and for invalid links).
+__device__ __forceinline__ dd PairLinkU4(const PairDD* s_pairs, const MoveDD& mv, const uint32_t* link_off, uint32_t l, bool valid, int ql,
+                                         uint32_t s, uint32_t p, uint32_t B, uint32_t bead0, uint32_t M, uint32_t np, uint32_t n_d,
+                                         const uint32_t* sp_off, const float2* pos, const dd* seg, dd L, dd iL, dd tau) {
+    dd rv2{0.f, 0.f}, rq2{0.f, 0.f};
+    int pi = 0;
+    if (valid) {
+        while (l >= link_off[pi + 1]) ++pi;
+        const PairDD& pa = s_pairs[mv.pair[pi]];
+        const bool hom = pa.sa == pa.sb;
+        const uint32_t other = hom ? s : (pa.sa == s ? pa.sb : pa.sa);
+        const uint32_t local = l - link_off[pi];
+        const uint32_t jj = local % B;
+        uint32_t qq = local / B;
+        if (hom && qq >= p) ++qq;
+        const uint32_t gq = sp_off[other] + qq;
+        if ((uint32_t)ql < n_d) {
+            const uint32_t d = ql;
+            const dd q0 = LoadDD(&pos[((size_t)((bead0 + jj) % M) * 3 + d) * np + gq]);
+            const dd q1 = LoadDD(&pos[((size_t)((bead0 + jj + 1) % M) * 3 + d) * np + gq]);
+            const dd m0 = seg[3 * jj + d], m1 = seg[3 * (jj + 1) + d];
+            // r = second - first particle; the moved particle is first unless it is species b.
+            const bool moved_first = hom || pa.sa == s;
+            const dd rv = MinImageDD(moved_first ? Sub(q0, m0) : Sub(m0, q0), L, iL);
+            dd rq = moved_first ? Sub(q1, m1) : Sub(m1, q1);
+            const float n = Rint(Mul(Sub(rv, rq), iL));
+            if (n != 0.f) rq = Add(rq, MulF(L, n));
+            rv2 = Sqr(rv);
+            rq2 = Sqr(rq);
+        }
+    }
+    rv2 = Add(rv2, ShflXorDD(rv2, 1));
+    rv2 = Add(rv2, ShflXorDD(rv2, 2));
+    rq2 = Add(rq2, ShflXorDD(rq2, 1));
+    rq2 = Add(rq2, ShflXorDD(rq2, 2));
+    dd f{0.f, 0.f};
+    if (valid && ql < 2) f = PairHalfV(s_pairs[mv.pair[pi]], Sqrt(ql == 0 ? rv2 : rq2));
+    f = Add(f, ShflXorDD(f, 1));
+    return (valid && ql == 0) ? Mul(tau, f) : dd{0.f, 0.f};
 }
 
 __device__ __forceinline__ void CopyWords(void* dst, const void* src, uint32_t bytes) {
@@ -326,14 +385,20 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
     uint64_t nbar = 0;
     // Optional phase timing of block 0 (tracing aid; the work done is identical either way).
     const bool timing = a.phase_cycles != nullptr && cta == 0 && tid == 0;
-    unsigned long long ph[kSweepPhases] = {0ull};
+    unsigned long long ph[kSweepTimingSlots] = {0ull};
     long long t_prev = clock64();
+    const bool timing_cta = a.phase_cycles != nullptr && cta == 0;
+    __shared__ unsigned long long s_role_max[kSweepRoles];
+    if (timing_cta && tid < kSweepRoles) s_role_max[tid] = 0ull;
 #define PIMC_PHASE(i)                             \
     if (timing) {                                 \
         const long long t_now = clock64();        \
         ph[i] += (unsigned long long)(t_now - t_prev); \
         t_prev = t_now;                           \
     }
+#define PIMC_ROLE_BEGIN(v) const long long v = timing_cta ? clock64() : 0ll
+#define PIMC_ROLE_END(v, r)                                                                         \
+    if (timing_cta && lane == 0) atomicMax(&s_role_max[r], (unsigned long long)(clock64() - v))
 
     for (uint64_t rep = 0; rep < a.n_rep; ++rep) {
         for (uint32_t e = 0; e < a.n_entries; ++e) {
@@ -342,15 +407,36 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
             const uint32_t s = mv.species, nl = mv.n_level, B = 1u << nl;
             const uint32_t g_off = a.sp_off[s];
             bool any_lr = false, grid_work = false;
-            int slot_s = -1;
+            int slot_s = -1, slot_o_first = -1;
+            uint32_t n_links = 0;  // pair links of the moved particle over the segment, all pair actions
+            uint32_t link_off[kMaxPair + 1];
             for (int pi = 0; pi < mv.n_pair; ++pi) {
                 const PairDD& pa = s_pairs[mv.pair[pi]];
-                if (!pa.is_constant) grid_work = true;
+                link_off[pi] = n_links;
+                if (!pa.is_constant) {
+                    grid_work = true;
+                    const uint32_t other = pa.sa == pa.sb ? s : (pa.sa == s ? pa.sb : pa.sa);
+                    n_links += (pa.sa == pa.sb ? a.sp_n[s] - 1 : a.sp_n[other]) * B;
+                }
                 if (pa.use_lr && !pa.is_constant) {
                     any_lr = true;
                     slot_s = pa.sa == s ? pa.slot_a : pa.slot_b;
+                    if (pa.sa != pa.sb && slot_o_first < 0) slot_o_first = pa.sa == s ? pa.slot_b : pa.slot_a;
                 }
             }
+            link_off[mv.n_pair] = n_links;
+            // Pair link l is evaluated by block l mod G, lane quad 127 - (l / G) mod 128: links fill
+            // the top warps first, which are idle while the sampling chain runs.
+            const uint32_t n_quads = blockDim.x / 4;
+            const int qlane = tid & 3;
+            const uint32_t link_stride = G * n_quads;
+            const uint32_t link_first = cta + G * (n_quads - 1 - (uint32_t)(tid >> 2));
+            // Warp-uniform trip count of the link loop (all lanes join the quad shuffles).
+            const uint32_t warp_first = cta + G * (n_quads - 1 - (uint32_t)((warp * 32 + 31) >> 2));
+            const uint32_t link_rounds = warp_first < n_links ? (n_links - warp_first + link_stride - 1) / link_stride : 0u;
+            // Designated blocks for the per-level sums when the attempt has a grid phase: the last
+            // n_level blocks, one level each (published with the grid barrier).
+            const int my_level = (grid_work && cta + nl >= G) ? (int)(G - 1 - cta) : -1;
             for (uint64_t c = 0, count = a.sched_count[e]; c < count; ++c) {
                 const MoveStream st{a.seed, a.chain, m, ctr[m]};
                 ctr[m] += 1;
@@ -359,28 +445,61 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                 const uint32_t bead0 = UniformIndex(w0.v[1], M);
                 const uint32_t g = g_off + p;
 
-                // ---- 1. segment, random numbers, owned slices -------------------------------
-                for (uint32_t i = tid; i < (B + 1) * 3; i += blockDim.x) {
-                    const uint32_t j = i / 3, d = i % 3;
-                    dd v{0.f, 0.f};
-                    if (d < n_d) v = LoadDD(&a.pos[((size_t)((bead0 + j) % M) * 3 + d) * np + g]);
-                    seg_old[i] = v;
-                    seg_new[i] = v;
-                }
-                for (uint32_t i = tid; i < B - 1; i += blockDim.x) BisectNormals(st, i, &zs[3 * i]);
-                if (tid < (int)nl) logu[tid] = BisectLogU(st, B, (uint32_t)tid);
-                if (tid == 0) {
+                // ---- 1. segment (warps 0-1), normals (warps 2-3), acceptance logarithms (warp 4),
+                //         owned slices (warp 5), all in parallel ---------------------------------
+                if (warp < 2) {
+                    for (uint32_t i = tid; i < (B + 1) * 3; i += 64) {
+                        const uint32_t j = i / 3, d = i % 3;
+                        dd v{0.f, 0.f};
+                        if (d < n_d) v = LoadDD(&a.pos[((size_t)((bead0 + j) % M) * 3 + d) * np + g]);
+                        seg_old[i] = v;
+                        seg_new[i] = v;
+                    }
+                } else if (warp < 4) {
+                    for (uint32_t i = tid - 64; i < B - 1; i += 64) BisectNormals(st, i, &zs[3 * i]);
+                } else if (warp == 4) {
+                    if (lane < (int)nl) logu[lane] = BisectLogU(st, B, (uint32_t)lane);
+                } else if (warp == 5) {
                     uint32_t n = 0;
                     if (owns_k && any_lr)
-                        for (uint32_t jj = 1; jj < B && n < kMaxOwned; ++jj)
-                            if (((bead0 + jj) % M) % a.R == r_own) s_slice_jj[n++] = jj;
-                    s_n_own = n;
+                        for (uint32_t j0 = 1; j0 < B; j0 += 32) {
+                            const uint32_t jj = j0 + lane;
+                            const bool mine = jj < B && ((bead0 + jj) % M) % a.R == r_own;
+                            const unsigned mask = __ballot_sync(0xffffffffu, mine);
+                            if (mine) {
+                                const uint32_t slot = n + __popc(mask & ((1u << lane) - 1u));
+                                if (slot < kMaxOwned) s_slice_jj[slot] = jj;
+                            }
+                            n += __popc(mask);
+                        }
+                    if (lane == 0) s_n_own = n < kMaxOwned ? n : kMaxOwned;
                 }
                 __syncthreads();
                 PIMC_PHASE(0);
                 const uint32_t n_own = s_n_own;
+                // Prefetch the Ewald cells of this thread's first owned item: the loads overlap with
+                // the sampling phases and are consumed in the grid phase.
+                const uint32_t nk_own = k_hi - k_lo;
+                float4 pre_rho = make_float4(0.f, 0.f, 0.f, 0.f), pre_rho_o = pre_rho;
+                if (any_lr && (uint32_t)tid < n_own * nk_own) {
+                    const uint32_t k = k_lo + tid % nk_own;
+                    const uint32_t b = (bead0 + s_slice_jj[tid / nk_own]) % M;
+                    pre_rho = a.rho[((size_t)slot_s * M + b) * K + k];
+                    if (slot_o_first >= 0) pre_rho_o = a.rho[((size_t)slot_o_first * M + b) * K + k];
+                }
+                dd pair_old{0.f, 0.f};  // stored copy's pair links of this lane's quad (quad lane 0)
+                bool old_done = false;
+                ddc pre_eo{{0.f, 0.f}, {0.f, 0.f}};
+                bool eo_done = false;
+                PIMC_ROLE_BEGIN(rt2);
+                // Warp roles: level sums run in one warp of a designated block when the attempt has
+                // a grid phase (published through the barrier), in one warp per level otherwise.
+                const int n_lvl_w = my_level >= 0 ? 1 : (grid_work ? 0 : (int)nl);
 
-                // ---- 2. sampling chain (warp 0) || old phase tables (other warps) ----------
+                // ---- 2. sampling chain (warp 0) || stored-copy level sums || old phase tables
+                //         || stored-copy pair links -------------------------------------------
+                const int w_tab2 = 1 + n_lvl_w;
+                const int n_tw2 = any_lr ? min((int)(n_own * 3), kWarps - w_tab2 - 1) : 0;
                 if (warp == 0) {
                     uint32_t mid = 0;
                     for (int lvl = (int)nl - 1; lvl >= 0; --lvl) {
@@ -399,10 +518,11 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                         mid += nm;
                         __syncwarp();
                     }
-                } else if (warp <= (int)nl) {
+                    PIMC_ROLE_END(rt2, 0);
+                } else if (warp < w_tab2) {
                     // Everything of the stored copy is known before sampling: its displacements from
-                    // the midpoints and its level sums (warp 1 + level).
-                    const int lvl = warp - 1;
+                    // the midpoints and its level sums.
+                    const int lvl = my_level >= 0 ? my_level : warp - 1;
                     const uint32_t skip = 1u << lvl, nm = B / (2 * skip), first = LevelFirst(nl, lvl, B);
                     for (uint32_t t = lane; t < nm * n_d; t += 32) {
                         const uint32_t mm = t / n_d, d = t % n_d;
@@ -418,86 +538,86 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                         s_old_lsp[lvl] = lsp;
                         s_old_small[lvl] = sm;
                     }
-                } else {
-                    const int w0 = (int)nl + 1;
-                    for (uint32_t task = warp - w0; task < n_own * 3; task += kWarps - w0) {
+                    PIMC_ROLE_END(rt2, 1);
+                } else if (warp < w_tab2 + n_tw2) {
+                    for (uint32_t task = warp - w_tab2; task < n_own * 3; task += n_tw2) {
                         const uint32_t si = task / 3, d = task % 3;
                         if (d < n_d)
                             for (int n = lane; n <= a.max_index[d]; n += 32)
                                 tab_old[(si * 3 + d) * stride + n] = PhaseDD(seg_old[3 * s_slice_jj[si] + d], n, a.iL, a.two_pi, s_phase);
                     }
+                    PIMC_ROLE_END(rt2, 2);
+                } else if (grid_work) {
+                    // Pair links of the stored copy (they do not depend on the sampling).
+                    for (uint32_t r = 0; r < link_rounds; ++r) {
+                        const uint32_t l = link_first + r * link_stride;
+                        pair_old = Add(pair_old, PairLinkU4(s_pairs, mv, link_off, l, l < n_links, qlane, s, p, B, bead0, M, np, n_d, a.sp_off,
+                                                            a.pos, seg_old, a.L, a.iL, a.tau));
+                    }
+                    old_done = true;
+                    PIMC_ROLE_END(rt2, 3);
                 }
                 __syncthreads();
                 PIMC_PHASE(1);
+                PIMC_ROLE_BEGIN(rt3);
 
                 // ---- 3. per-level sums of the working copy || new phase tables -------------
-                if (warp < (int)nl) {
-                    const int lvl = warp;
+                const int n_tw3 = any_lr ? min((int)(n_own * 3), kWarps - n_lvl_w - 1) : 0;
+                if (warp < n_lvl_w) {
+                    const int lvl = my_level >= 0 ? my_level : warp;
                     dd lsp, sm;
                     LevelSums(mv, lvl, B, seg_new, d_new, LevelFirst(nl, lvl, B), n_d, a.L, a.iL, lane, lsp, sm);
                     if (lane == 0) {
-                        s_lvl_diff[lvl] = Sub(s_old_lsp[lvl], lsp);     // old log-prob - new log-prob
-                        s_lvl_small[lvl] = Sub(sm, s_old_small[lvl]);   // new action - old action
+                        const dd diff = Sub(s_old_lsp[lvl], lsp);   // old log-prob - new log-prob
+                        const dd small = Sub(sm, s_old_small[lvl]); // new action - old action
+                        if (my_level >= 0) {
+                            // published with this attempt's grid barrier (generation nbar + 1)
+                            __stcg(&a.level_out[((nbar + 1) & 1ull) * kMaxLevels + lvl], make_float4(diff.hi, diff.lo, small.hi, small.lo));
+                        } else {
+                            s_lvl_diff[lvl] = diff;
+                            s_lvl_small[lvl] = small;
+                        }
                     }
+                    PIMC_ROLE_END(rt3, 4);
                 } else {
-                    const int w0 = (int)nl;
-                    for (uint32_t task = warp - w0; task < n_own * 3; task += kWarps - w0) {
-                        const uint32_t si = task / 3, d = task % 3;
-                        if (d < n_d)
-                            for (int n = lane; n <= a.max_index[d]; n += 32)
-                                tab_new[(si * 3 + d) * stride + n] = PhaseDD(seg_new[3 * s_slice_jj[si] + d], n, a.iL, a.two_pi, s_phase);
+                    const int w0 = n_lvl_w;
+                    const int n_tw = n_tw3;
+                    if (warp < w0 + n_tw) {
+                        for (uint32_t task = warp - w0; task < n_own * 3; task += n_tw) {
+                            const uint32_t si = task / 3, d = task % 3;
+                            if (d < n_d)
+                                for (int n = lane; n <= a.max_index[d]; n += 32)
+                                    tab_new[(si * 3 + d) * stride + n] = PhaseDD(seg_new[3 * s_slice_jj[si] + d], n, a.iL, a.two_pi, s_phase);
+                        }
+                        PIMC_ROLE_END(rt3, 5);
+                    } else if (any_lr && (uint32_t)tid < n_own * nk_own) {
+                        // Old-position phase of this thread's first Ewald cell (tables built above).
+                        pre_eo = PhaseProductDD(tab_old + (size_t)(tid / nk_own) * 3 * stride, stride, n_d, a.kidx[k_lo + tid % nk_own]);
+                        eo_done = true;
+                        PIMC_ROLE_END(rt3, 6);
                     }
                 }
                 __syncthreads();
                 PIMC_PHASE(2);
+                PIMC_ROLE_BEGIN(rt4);
 
                 // ---- 4. level-0 grid work: pair links + owned Ewald cells -------------------
                 ddc delta_cache[kDeltaCache];
                 if (grid_work) {
+                    // Pair links (pair_action_class.h:280-290), CalcU = tau V at level 0: the working
+                    // copy here; the stored copy was summed during sampling by free warps.
                     dd acc{0.f, 0.f};
-                    // Pair links (pair_action_class.h:280-290): one (link, old|new) evaluation per
-                    // thread, consecutive evaluations on different blocks so that no block carries
-                    // more than a few of these latency-bound chains.
-                    uint32_t offs[kMaxPair + 1];
-                    uint32_t n_eval = 0;
-                    for (int pi = 0; pi < mv.n_pair; ++pi) {
-                        const PairDD& pa = s_pairs[mv.pair[pi]];
-                        offs[pi] = n_eval;
-                        if (pa.is_constant) continue;
-                        const uint32_t other = pa.sa == pa.sb ? s : (pa.sa == s ? pa.sb : pa.sa);
-                        n_eval += 2u * (pa.sa == pa.sb ? a.sp_n[s] - 1 : a.sp_n[other]) * B;
+                    for (uint32_t r = 0; r < link_rounds; ++r) {
+                        const uint32_t l = link_first + r * link_stride;
+                        acc = Add(acc, PairLinkU4(s_pairs, mv, link_off, l, l < n_links, qlane, s, p, B, bead0, M, np, n_d, a.sp_off, a.pos,
+                                                  seg_new, a.L, a.iL, a.tau));
+                        if (!old_done)
+                            acc = Sub(acc, PairLinkU4(s_pairs, mv, link_off, l, l < n_links, qlane, s, p, B, bead0, M, np, n_d, a.sp_off, a.pos,
+                                                      seg_old, a.L, a.iL, a.tau));
                     }
-                    offs[mv.n_pair] = n_eval;
-                    const uint32_t gstride = G * blockDim.x;
-                    for (uint32_t it = (uint32_t)tid * G + cta; it < n_eval; it += gstride) {
-                        int pi = 0;
-                        while (it >= offs[pi + 1]) ++pi;
-                        const PairDD& pa = s_pairs[mv.pair[pi]];
-                        const bool hom = pa.sa == pa.sb;
-                        const uint32_t other = hom ? s : (pa.sa == s ? pa.sb : pa.sa);
-                        const bool moved_is_a = hom || pa.sa == s;
-                        uint32_t local = it - offs[pi];
-                        const bool is_new = (local & 1u) != 0u;
-                        local >>= 1;
-                        const uint32_t jj = local % B;
-                        uint32_t qq = local / B;
-                        if (hom && qq >= p) ++qq;
-                        const uint32_t gq = a.sp_off[other] + qq;
-                        const uint32_t bi = (bead0 + jj) % M, bj = (bead0 + jj + 1) % M;
-                        dd Q0[3], Q1[3];
-                        for (uint32_t d = 0; d < n_d; ++d) {
-                            Q0[d] = LoadDD(&a.pos[((size_t)bi * 3 + d) * np + gq]);
-                            Q1[d] = LoadDD(&a.pos[((size_t)bj * 3 + d) * np + gq]);
-                        }
-                        const dd* sg = is_new ? seg_new : seg_old;
-                        dd r, rp;
-                        if (moved_is_a) DrDrpDD(Q0, &sg[3 * jj], Q1, &sg[3 * (jj + 1)], n_d, a.L, a.iL, r, rp);
-                        else DrDrpDD(&sg[3 * jj], Q0, &sg[3 * (jj + 1)], Q1, n_d, a.L, a.iL, r, rp);
-                        const dd u = Mul(a.tau, PairVDD(pa, r, rp));  // CalcU = tau V at level 0
-                        acc = Add(acc, is_new ? u : Neg(u));
-                    }
+                    if (old_done) acc = Sub(acc, pair_old);
                     if (any_lr) {
-                        const uint32_t nk = k_hi - k_lo;
+                        const uint32_t nk = nk_own;
                         dd lr{0.f, 0.f};
                         uint32_t ci = 0;
                         for (uint32_t it = tid; it < n_own * nk; it += blockDim.x, ++ci) {
@@ -505,10 +625,10 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                             const uint32_t b = (bead0 + s_slice_jj[si]) % M;
                             const int32_t pk = a.kidx[k];
                             const ddc en = PhaseProductDD(tab_new + (size_t)si * 3 * stride, stride, n_d, pk);
-                            const ddc eo = PhaseProductDD(tab_old + (size_t)si * 3 * stride, stride, n_d, pk);
+                            const ddc eo = (ci == 0 && eo_done) ? pre_eo : PhaseProductDD(tab_old + (size_t)si * 3 * stride, stride, n_d, pk);
                             const ddc dl = CSub(en, eo);
                             if (ci < kDeltaCache) delta_cache[ci] = dl;
-                            const ddc rho = Unpack(a.rho[((size_t)slot_s * M + b) * K + k]);
+                            const ddc rho = Unpack(ci == 0 ? pre_rho : a.rho[((size_t)slot_s * M + b) * K + k]);
                             for (int pi = 0; pi < mv.n_pair; ++pi) {
                                 const PairDD& pa = s_pairs[mv.pair[pi]];
                                 if (!pa.use_lr || pa.is_constant) continue;
@@ -520,7 +640,8 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                                     lr = Add(lr, Mul(vk, t));
                                 } else {
                                     const int slot_o = pa.sa == s ? pa.slot_b : pa.slot_a;
-                                    const ddc ro = Unpack(a.rho[((size_t)slot_o * M + b) * K + k]);
+                                    const ddc ro = Unpack((ci == 0 && slot_o == slot_o_first) ? pre_rho_o
+                                                                                              : a.rho[((size_t)slot_o * M + b) * K + k]);
                                     const dd t = Add(Mul(dl.re, ro.re), Mul(dl.im, ro.im));
                                     lr = Add(lr, Scale2(Mul(vk, t), 2.f));
                                 }
@@ -528,6 +649,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                         }
                         acc = Add(acc, Mul(a.tau, lr));
                     }
+                    PIMC_ROLE_END(rt4, 7);
                     // block sum (fixed order) -> partial -> grid barrier -> ordered total
                     ++nbar;
                     const dd v = WarpSumDD(acc);
@@ -549,6 +671,12 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                         }
                         t = WarpSumDD(t);
                         if (lane == 0) s_big = t;
+                        if (lane < (int)nl) {
+                            // level sums from the designated blocks (written before their arrival)
+                            const float4 v = __ldcg(&a.level_out[(nbar & 1ull) * kMaxLevels + lane]);
+                            s_lvl_diff[lane] = dd{v.x, v.y};
+                            s_lvl_small[lane] = dd{v.z, v.w};
+                        }
                     }
                     __syncthreads();
                     PIMC_PHASE(5);
@@ -618,17 +746,24 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                 }
                 __syncthreads();
                 PIMC_PHASE(7);
+                if (timing)
+                    for (int r = 0; r < kSweepRoles; ++r) {
+                        ph[kSweepPhases + r] += s_role_max[r];
+                        s_role_max[r] = 0ull;
+                    }
             }
         }
     }
 #undef PIMC_PHASE
+#undef PIMC_ROLE_BEGIN
+#undef PIMC_ROLE_END
     if (cta == 0 && tid == 0) {
         for (int m = 0; m < kMaxMoves; ++m) {
             a.counters[m] += n_acc[m];
             a.counters[kMaxMoves + m] += n_l0[m];
         }
         if (timing)
-            for (int i = 0; i < kSweepPhases; ++i) a.phase_cycles[i] += ph[i];
+            for (int i = 0; i < kSweepTimingSlots; ++i) a.phase_cycles[i] += ph[i];
     }
 }
 
@@ -922,6 +1057,7 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
     args->tab_stride = (uint32_t)std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
 
     const int G = sweep_grid > 0 ? sweep_grid : n_sm;
+    if ((uint32_t)G < max_level) throw PimcError(kErrArg, "sweep grid smaller than the bisection level count");
     uint32_t R = 1;
     while (R * 2 <= (1u << max_level) && R * 2 <= (uint32_t)G) R *= 2;
     const uint32_t spc = std::max<uint32_t>(1, (1u << max_level) / R);
@@ -965,11 +1101,13 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
     args->counters = dcount;
     args->bar = Barrier();
     args->err = ErrWord();
-    args->partials = reinterpret_cast<float2*>(Partials((size_t)2 * G));
+    double* scratch = Partials((size_t)2 * G + 4 * kMaxLevels);
+    args->partials = reinterpret_cast<float2*>(scratch);
+    args->level_out = reinterpret_cast<float4*>(scratch + (size_t)2 * G);
     args->timeout_ns = timeout_ns;
     args->phase_cycles = nullptr;
     if (phase_timing) {
-        if (!phase_buf) phase_buf.reset(new DeviceBuffer(kSweepPhases * sizeof(unsigned long long)));
+        if (!phase_buf) phase_buf.reset(new DeviceBuffer(kSweepTimingSlots * sizeof(unsigned long long)));
         args->phase_cycles = phase_buf->as<unsigned long long>();
     }
     CudaCheck(cudaMemsetAsync(Barrier(), 0, sizeof(unsigned long long), stream), "reset barrier");

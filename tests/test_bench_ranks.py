@@ -1,0 +1,59 @@
+"""Multi-process (replica) logic of bench.py on CPU: world size 2 over gloo on 127.0.0.1.
+
+Chains are independent Markov chains, one per GPU (the reference's MPI clones,
+framework_class.h:44-53): the only collective is the maximum of the per-rank timings."""
+import os
+import socket
+
+import pytest
+
+torch = pytest.importorskip("torch")
+import torch.distributed as dist  # noqa: E402
+import torch.multiprocessing as mp  # noqa: E402
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _worker(rank, world, port, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+    out[rank] = bench.reduce_max_over_ranks([1.0 + rank, 10.0 - rank, 3.0], dist)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_reduce_max_over_two_ranks():
+    ctx = mp.get_context("spawn")
+    manager = ctx.Manager()
+    out = manager.dict()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, out)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    assert out[0] == out[1] == [2.0, 10.0, 3.0]
+
+
+def test_single_process_is_identity():
+    import bench
+    assert bench.reduce_max_over_ranks([1.5, 2.5]) == [1.5, 2.5]
+
+
+def test_reference_arm_non_zero_rank_exits_quietly(monkeypatch, capsys):
+    import bench
+    monkeypatch.setenv("RANK", "1")
+
+    class A:
+        steps, warmup = 1, 3
+
+    bench.run_reference(A())
+    assert capsys.readouterr().out == ""
