@@ -125,6 +125,52 @@ void* pimc_stream(pimc_ctx* ctx);
  * sums (-1 leaves both as they are). */
 int pimc_sweep_timing(pimc_ctx* ctx, int enable, uint64_t* cycles);
 
+/* ---------------------------------------------------------------------------------------------
+ * Batched independent chains. The reference obtains several Markov chains only as MPI clones,
+ * one process each with its own seed, input and output (framework_class.h:44-53,84-99); this
+ * handle runs many chains, one XML input each, in one persistent launch per call. Chain i draws
+ * from the same counter-based stream as a single-chain context created with chain = i, so it
+ * replays that context's Markov chain up to FP32 rounding (positions and per-term actions in
+ * FP32, sums in double-float, estimator values in FP64).
+ * Supported inputs: one 3-D species, Kinetic (n_images 0), optional HarmonicTrap, optional
+ * BarePairAction is_coulomb=1 without long range within the species, one fixed-level Bisect with
+ * n_level <= 5; anything else returns PIMC_ERR_UNSUPPORTED. */
+typedef struct pimc_batch pimc_batch;
+
+int pimc_batch_create(const char* const* xml_texts, uint32_t n_chains, const char* base_dir, int device, pimc_batch** out);
+void pimc_batch_destroy(pimc_batch* b);
+const char* pimc_batch_last_error(const pimc_batch* b); /* NULL handle: last failed create */
+/* out4 = {n_part, n_bead, n_level, warps of its pair tile}. */
+int pimc_batch_chain_info(pimc_batch* b, uint32_t chain, uint32_t* out4);
+/* One chain's path, pos[p][b][d] as for pimc_set_path (stored as FP32). */
+int pimc_batch_set_path(pimc_batch* b, uint32_t chain, const double* pos);
+int pimc_batch_get_path(pimc_batch* b, uint32_t chain, double* pos);
+/* n bisection attempts (Move::DoEvent, move_class.h:277-293) on every chain. */
+int pimc_batch_attempts(pimc_batch* b, uint64_t n);
+/* n sweeps on every chain; a sweep of a chain is n_part * ceil(n_bead / 2^n_level) attempts. */
+int pimc_batch_sweeps(pimc_batch* b, uint64_t n);
+/* One thermal energy measurement on every chain (Energy::Accumulate, energy_class.h:36-58). */
+int pimc_batch_measure(pimc_batch* b);
+/* n_cycles replays of a CUDA graph holding `sweeps_per_measure` sweeps and one measurement. */
+int pimc_batch_run(pimc_batch* b, uint64_t n_cycles, uint64_t sweeps_per_measure);
+int pimc_batch_sync(pimc_batch* b);
+/* Energy series of one chain: out[m][4] = {E, kinetic, trap, pair} per measurement, each already
+ * divided by n_bead as in Energy::Write (energy_class.h:232-253); at most `cap` rows (the device
+ * keeps the first 4096); *n_measure = measurements since the last reset. */
+int pimc_batch_energy(pimc_batch* b, uint32_t chain, double* out, uint64_t cap, uint64_t* n_measure);
+int pimc_batch_reset_energy(pimc_batch* b);
+/* Per-chain attempt and acceptance counters (arrays of n_chains; either may be NULL). */
+int pimc_batch_counters(pimc_batch* b, uint64_t* attempts, uint64_t* accepts);
+/* Pair tile: a chain gets ceil((n_part-1)(2^n_level-1) / (32 items_per_lane)) warps, at most
+ * max_warps (<= 16). pimc_batch_autotune times `trial_sweeps` sweeps of every candidate on a
+ * saved copy of the chains' state, restores it, and keeps the fastest tile. */
+int pimc_batch_set_tiles(pimc_batch* b, uint32_t items_per_lane, uint32_t max_warps);
+int pimc_batch_autotune(pimc_batch* b, uint32_t trial_sweeps, uint32_t* items_per_lane, uint32_t* max_warps, double* sec_per_sweep);
+/* out4 = {n_chains, bead moves per sweep of all chains, kernels launched so far, series rows kept}. */
+int pimc_batch_stats(pimc_batch* b, uint64_t* out4);
+/* CUDA stream of the batch (cudaStream_t). */
+int pimc_batch_stream(pimc_batch* b, void** stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -16,7 +16,7 @@ from pathlib import Path
 
 import numpy as np
 
-__all__ = ["Simulation", "PimcError", "load_library", "LIB_PATH"]
+__all__ = ["Simulation", "ChainBatch", "PimcError", "load_library", "LIB_PATH"]
 
 LIB_PATH = Path(__file__).resolve().parent / "lib" / "libsimpimc_gb300.so"
 
@@ -79,6 +79,24 @@ SIGNATURES = {
     "pimc_set_timeout_ns": (C.c_int, [_P, C.c_uint64]),
     "pimc_stream": (_P, [_P]),
     "pimc_sweep_timing": (C.c_int, [_P, C.c_int, _U64P]),
+    "pimc_batch_create": (C.c_int, [C.POINTER(C.c_char_p), C.c_uint32, C.c_char_p, C.c_int, C.POINTER(_P)]),
+    "pimc_batch_destroy": (None, [_P]),
+    "pimc_batch_last_error": (C.c_char_p, [_P]),
+    "pimc_batch_chain_info": (C.c_int, [_P, C.c_uint32, _U32P]),
+    "pimc_batch_set_path": (C.c_int, [_P, C.c_uint32, _DP]),
+    "pimc_batch_get_path": (C.c_int, [_P, C.c_uint32, _DP]),
+    "pimc_batch_attempts": (C.c_int, [_P, C.c_uint64]),
+    "pimc_batch_sweeps": (C.c_int, [_P, C.c_uint64]),
+    "pimc_batch_measure": (C.c_int, [_P]),
+    "pimc_batch_run": (C.c_int, [_P, C.c_uint64, C.c_uint64]),
+    "pimc_batch_sync": (C.c_int, [_P]),
+    "pimc_batch_energy": (C.c_int, [_P, C.c_uint32, _DP, C.c_uint64, _U64P]),
+    "pimc_batch_reset_energy": (C.c_int, [_P]),
+    "pimc_batch_counters": (C.c_int, [_P, _U64P, _U64P]),
+    "pimc_batch_set_tiles": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
+    "pimc_batch_autotune": (C.c_int, [_P, C.c_uint32, _U32P, _U32P, _DP]),
+    "pimc_batch_stats": (C.c_int, [_P, _U64P]),
+    "pimc_batch_stream": (C.c_int, [_P, C.POINTER(_P)]),
 }
 
 SWEEP_PHASES = ("segment+rng", "sampling", "level terms", "grid work", "grid barrier", "final sum", "decision", "commit",
@@ -282,3 +300,109 @@ class Simulation:
             self._check(self._lib.pimc_get_block(self._h, obs, b, _dp(buf), cap, C.byref(m)))
             out.append(buf[: m.value].copy())
         return out
+
+
+class ChainBatch:
+    """Many independent chains on one GPU (one XML input per chain; chain i replays the
+    single-chain context created with ``chain=i`` up to FP32 rounding)."""
+
+    def __init__(self, xmls, base_dir: str | os.PathLike = ".", device: int = 0):
+        self._lib = load_library()
+        arr = (C.c_char_p * len(xmls))(*[x.encode() for x in xmls])
+        h = _P()
+        rc = self._lib.pimc_batch_create(arr, len(xmls), str(base_dir).encode(), device, C.byref(h))
+        if rc != 0:
+            raise PimcError(rc, self._lib.pimc_batch_last_error(None).decode())
+        self._h = h
+        self.n_chains = len(xmls)
+        self.shapes = [self.chain_info(i)[:3] for i in range(self.n_chains)]
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise PimcError(rc, self._lib.pimc_batch_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.pimc_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def chain_info(self, chain: int):
+        """(n_part, n_bead, n_level, warps of the chain's pair tile)."""
+        out = np.zeros(4, dtype=np.uint32)
+        self._check(self._lib.pimc_batch_chain_info(self._h, chain, out.ctypes.data_as(_U32P)))
+        return tuple(int(x) for x in out)
+
+    def set_path(self, chain: int, pos: np.ndarray):
+        n, m, _ = self.shapes[chain]
+        a = np.ascontiguousarray(pos, dtype=np.float64)
+        if a.shape != (n, m, 3):
+            raise ValueError(f"path shape {a.shape} != {(n, m, 3)}")
+        self._check(self._lib.pimc_batch_set_path(self._h, chain, _dp(a)))
+
+    def get_path(self, chain: int) -> np.ndarray:
+        n, m, _ = self.shapes[chain]
+        out = np.zeros((n, m, 3), dtype=np.float64)
+        self._check(self._lib.pimc_batch_get_path(self._h, chain, _dp(out)))
+        return out
+
+    def attempts(self, n: int):
+        self._check(self._lib.pimc_batch_attempts(self._h, n))
+
+    def sweeps(self, n: int):
+        self._check(self._lib.pimc_batch_sweeps(self._h, n))
+
+    def measure(self):
+        self._check(self._lib.pimc_batch_measure(self._h))
+
+    def run(self, n_cycles: int, sweeps_per_measure: int = 1):
+        self._check(self._lib.pimc_batch_run(self._h, n_cycles, sweeps_per_measure))
+
+    def synchronize(self):
+        self._check(self._lib.pimc_batch_sync(self._h))
+
+    def energy(self, chain: int, cap: int = 4096) -> tuple[np.ndarray, int]:
+        """(series[m, 4] of {E, kinetic, trap, pair} per measurement, measurements since reset)."""
+        out = np.zeros((cap, 4), dtype=np.float64)
+        n = C.c_uint64()
+        self._check(self._lib.pimc_batch_energy(self._h, chain, _dp(out), cap, C.byref(n)))
+        return out[: min(n.value, cap)].copy(), int(n.value)
+
+    def reset_energy(self):
+        self._check(self._lib.pimc_batch_reset_energy(self._h))
+
+    def counters(self):
+        att = np.zeros(self.n_chains, dtype=np.uint64)
+        acc = np.zeros(self.n_chains, dtype=np.uint64)
+        self._check(self._lib.pimc_batch_counters(self._h, att.ctypes.data_as(_U64P), acc.ctypes.data_as(_U64P)))
+        return att, acc
+
+    def set_tiles(self, items_per_lane: int, max_warps: int):
+        self._check(self._lib.pimc_batch_set_tiles(self._h, items_per_lane, max_warps))
+
+    def autotune(self, trial_sweeps: int = 2):
+        ipl, mw, sec = C.c_uint32(), C.c_uint32(), C.c_double()
+        self._check(self._lib.pimc_batch_autotune(self._h, trial_sweeps, C.byref(ipl), C.byref(mw), C.byref(sec)))
+        return int(ipl.value), int(mw.value), float(sec.value)
+
+    def stats(self) -> dict:
+        out = np.zeros(4, dtype=np.uint64)
+        self._check(self._lib.pimc_batch_stats(self._h, out.ctypes.data_as(_U64P)))
+        return {"n_chains": int(out[0]), "bead_moves_per_sweep": int(out[1]), "kernel_launches": int(out[2]),
+                "series_cap": int(out[3])}
+
+    def stream(self) -> int:
+        s = _P()
+        self._check(self._lib.pimc_batch_stream(self._h, C.byref(s)))
+        return int(s.value or 0)

@@ -27,6 +27,7 @@ SOURCES = [
     SRC / "framework" / "setup.cu",
     SRC / "kernels" / "estimators.cu",
     SRC / "kernels" / "sweep.cu",
+    SRC / "kernels" / "batch.cu",
     SRC / "noalloc.cu",
 ]
 

@@ -21,11 +21,13 @@ from .tables import coulomb_table
 
 
 def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_level=3, seed=1234, coulomb=True,
-                    n_step_inner=100, n_step_outer=10, gr_bins=200, gr_rmax=5.0, virial=False, path_seed=None):
+                    n_step_inner=100, n_step_outer=10, gr_bins=200, gr_rmax=5.0, virial=False, path_seed=None,
+                    write_table=True):
     workdir = Path(workdir)
     workdir.mkdir(parents=True, exist_ok=True)
     tab = workdir / "coulomb_open.pat"
-    coulomb_table(tab, z_ab=1.0, L=0.0)
+    if write_table or not tab.exists():
+        coulomb_table(tab, z_ab=1.0, L=0.0)
     pair = (f'<Action name="Coulomb" type="BarePairAction" file="{tab.name}" is_coulomb="1" species_a="e" '
             f'species_b="e" max_level="0" use_long_range="0" />') if coulomb else ""
     energy = ('<Observable name="Energy" type="Energy" use_virial_estimator="1" />' if virial
@@ -120,6 +122,22 @@ def electron_gas(workdir, *, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_unit
     rng = np.random.default_rng(seed if path_seed is None else path_seed)
     path = np.repeat(rng.uniform(-L / 2, L / 2, size=(n_part, 1, 3)), n_bead, axis=1)
     return xml, path
+
+
+def batched_trap_chains(workdir, *, n_chains=256, seed0=1000, n_range=(16, 128), bead_choices=(32, 64, 128),
+                        n_level=3, beta=2.0, omega=1.0):
+    """Independent trapped Coulomb chains with uneven sizes: chain c has seed ``seed0 + c``,
+    N drawn uniformly from ``n_range`` (inclusive) and M from ``bead_choices`` by a generator
+    seeded with ``seed0``; beads i.i.d. N(0, 1) from the chain's seed. Returns a list of
+    ``(xml_text, initial_path)``."""
+    rng = np.random.default_rng(seed0)
+    ns = rng.integers(n_range[0], n_range[1] + 1, size=n_chains)
+    ms = rng.choice(np.asarray(bead_choices), size=n_chains)
+    out = []
+    for c in range(n_chains):
+        out.append(trapped_coulomb(workdir, n_part=int(ns[c]), n_bead=int(ms[c]), n_level=n_level, beta=beta,
+                                   omega=omega, seed=seed0 + c, write_table=(c == 0)))
+    return out
 
 
 def sweep_schedule(sim_or_counts, n_bisect_beads: int, n_bead: int):

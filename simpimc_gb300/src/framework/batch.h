@@ -1,0 +1,104 @@
+// Many independent Markov chains advanced together on one GPU.
+//
+// The reference runs one chain per process and gets more chains from MPI clones, each with its
+// own seed and output (src/framework/framework_class.h:44-53,84-99). Here the chains are the
+// batch dimension of one persistent launch: thread block c runs chain order[c], with as many
+// warps as that chain's pair tile needs; chains may differ in particle number, slice number,
+// bisection level and seed. A measurement cycle (sweeps, then one energy measurement per chain)
+// is captured once as a CUDA graph and replayed; the per-chain attempt counters and estimator
+// series live in device memory, so replays advance the chains without host work.
+//
+// Supported chains (anything else is rejected at creation): one species in three dimensions;
+// Kinetic (n_images 0); optional HarmonicTrap; optional BarePairAction with is_coulomb=1 and no
+// long-range part between the species and itself; one non-adaptive Bisect move with n_level <= 5;
+// open or periodic boundaries.
+//
+// Arithmetic: positions and per-term action values in FP32; every sum of terms in double-float
+// (FP32 pairs, 2^-46 relative rounding); each Metropolis level decision, which adds the level's
+// action difference to the previous level's and compares with the log-uniform draw, in FP64;
+// estimator values and block sums in FP64.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "context.h"
+
+namespace pimc {
+
+constexpr uint32_t kBatchMaxLevels = 5;        // segment of at most 32 beads
+constexpr uint32_t kBatchMaxWarps = 16;        // warps per chain (block size 512)
+constexpr uint32_t kBatchSeriesComponents = 4; // E, kinetic, trap, pair (each / M)
+
+/// Per-chain parameters read by the batched kernels.
+struct ChainDev {
+    uint32_t n_part, n_bead, n_pad, n_level;  // B = 2^n_level beads per segment
+    uint32_t seed, chain_id, n_warps, move;   // Philox keys; warps used; move index in its input
+    uint64_t pos_off;                         // first float4 of the chain's [n_bead][n_pad] block
+    uint64_t attempts_per_sweep;              // n_part * ceil(n_bead / B)
+    float L, iL, lambda, tau;
+    float sigma[kBatchMaxLevels];        // sqrt(lambda tau 2^l): sampling width at level l
+    float i4lt_sample[kBatchMaxLevels];  // 1/(4 lambda (tau 2^l / 2)): sampling density at level l
+    float i4lt_level[kBatchMaxLevels];   // 1/(4 lambda tau 2^l): kinetic action at level l
+    int32_t pbc, has_trap, has_pair, trap_max_level;
+    float trap_cofa, r2_min, r2_max, pad1;  // pair clamp r in [r_min, r_max] as r^2
+    double trap_cofb, kin_const, i4ltt;     // DActionDBeta constants (trap_class.h, kinetic_class.h)
+};
+
+/// Host view of one chain's input.
+struct ChainSpec {
+    uint32_t n_part = 0, n_bead = 0, n_level = 0, seed = 0, move = 0;
+    double beta = 0., tau = 0., L = 0., lambda = 0., omega = 0., r_min = 0., r_max = 0.;
+    bool pbc = true, has_trap = false, has_pair = false;
+    uint32_t trap_max_level = 0;
+};
+
+/// Parses one chain's XML input (the reference's format) into a ChainSpec; throws PimcError
+/// (kErrUnsupported) for inputs outside the supported subset.
+ChainSpec ParseChain(const std::string& xml, const std::string& base_dir);
+
+class ChainBatch {
+   public:
+    ChainBatch(const std::vector<std::string>& xml, const std::string& base_dir, int device);
+    ~ChainBatch();
+    ChainBatch(const ChainBatch&) = delete;
+    ChainBatch& operator=(const ChainBatch&) = delete;
+
+    void SetPath(uint32_t chain, const double* pos);  // [n_part][n_bead][3]
+    void GetPath(uint32_t chain, double* pos);
+    void Attempts(uint64_t n);                // n bisection attempts on every chain
+    void Sweeps(uint64_t n);                  // n sweeps on every chain (one launch)
+    void Measure();                           // one energy measurement on every chain
+    void Run(uint64_t n_cycles, uint64_t sweeps_per_measure);  // graph-replayed cycles
+    uint64_t ReadEnergy(uint32_t chain, double* out, uint64_t cap);  // series [n][4]
+    void ResetEnergy();
+    void ReadCounters(uint64_t* attempts, uint64_t* accepts);
+    void SetTiles(uint32_t items_per_lane, uint32_t max_warps);
+    double Autotune(uint32_t trial_sweeps);   // returns the best trial's seconds per sweep
+    void Sync();
+
+    uint32_t n_chains = 0, series_cap = 0;
+    int device = 0, n_sm = 0;
+    uint32_t items_per_lane = 8, max_warps = 8;
+    cudaStream_t stream = nullptr;
+    std::vector<ChainSpec> specs;
+    std::vector<ChainDev> chains;
+    std::vector<uint32_t> order;   // block -> chain, most expensive first
+    uint64_t bead_moves_per_sweep = 0;
+    uint64_t kernel_launches = 0;
+
+   private:
+    void Upload();
+    void LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts);
+    void LaunchMeasure();
+    void ResetGraph();
+    std::unique_ptr<DeviceBuffer> pos_, chains_dev_, order_dev_, att_, acc_, series_, n_meas_, err_;
+    cudaGraphExec_t graph_ = nullptr;
+    uint64_t graph_sweeps_ = 0;
+};
+
+}  // namespace pimc

@@ -1,0 +1,855 @@
+// Batched independent chains: one thread block per chain, bisection sweeps and the thermal
+// energy estimator for trapped / bare-Coulomb systems in FP32 with double-float sums.
+//
+// Algorithm per attempt (the reference's Bisect::Attempt, src/events/moves/single_species_move/
+// bisect/bisect_class.h:39-124, with its actions Kinetic kinetic_class.h:105-122, HarmonicTrap
+// trap_class.h:40-62 and BarePairAction bare_pair_action_class.h:133-149 / pair_action_class.h:
+// 267-302): draw particle and first bead; resample the 2^l - 1 inner beads level by level from
+// the free-particle distribution; at every level compare the level's action difference plus the
+// sampling ratio (minus the previous level's action difference) with a log-uniform draw; accept
+// the segment only if every level passes. The draws come from the same counter-based stream as
+// the single-chain path, so a chain replays the FP64 path's Markov chain up to FP32 rounding.
+//
+// Work split inside a chain's warp group (G warps, T = 32 G lanes):
+//   warp 0   draws the normals / uniforms, loads the moved particle's segment, samples the new
+//            beads (lanes 0-2, one per dimension), evaluates the old-path sampling, kinetic and
+//            trap sums (lanes 3-5), and takes every level decision;
+//   all      evaluate the pair differences of the moved particle against the others on the
+//            segment's inner slices (items (slice, other particle), coalesced float4 loads of the
+//            other particles issued at the top of the attempt), reduce them in double-float.
+// Pair terms are zero above level 0 (the primitive action's `1 >> level` factor,
+// bare_pair_action_class.h:147), so upper levels are decided before the pair work and a rejection
+// there skips it.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <ctime>
+#include <numeric>
+
+#include "../../../include/simpimc_gb300.h"
+#include "../common/philox.h"
+#include "../framework/batch.h"
+#include "../framework/input.h"
+#include "../framework/table_io.h"
+#include "df64.cuh"
+
+namespace pimc {
+namespace {
+
+struct BatchArgs {
+    float4* pos;
+    const ChainDev* chains;
+    const uint32_t* order;
+    uint64_t* attempts;  // per chain: attempt counter of its Bisect move
+    uint64_t* accepts;
+    double* series;      // [chain][series_cap][kBatchSeriesComponents]
+    uint64_t* n_meas;    // per chain
+    int* err;
+    uint32_t series_cap;
+};
+
+constexpr uint32_t kMaxB = 1u << kBatchMaxLevels;  // 32
+constexpr uint32_t kPrefetch = 4;                  // pair items loaded ahead per lane
+
+/// Barrier over the chain's warp group (named barrier 1; a warp-level barrier for one warp).
+__device__ __forceinline__ void GroupSync(uint32_t n_warps) {
+    if (n_warps == 1) __syncwarp();
+    else asm volatile("bar.sync 1, %0;" ::"r"(n_warps * 32u) : "memory");
+}
+
+__device__ __forceinline__ float MinImg(float d, int pbc, float L, float iL) {
+    return pbc ? __fsub_rn(d, __fmul_rn(L, rintf(__fmul_rn(d, iL)))) : d;
+}
+
+/// Exact i / d for i * d < 2^32 with m = ceil(2^32 / d).
+__device__ __forceinline__ uint32_t FastDiv(uint32_t i, uint32_t m) { return __umulhi(i, m); }
+
+__device__ __forceinline__ dd AddSq(dd acc, float x) { return Add(acc, TwoProd(x, x)); }
+
+__device__ __forceinline__ dd ShflDownDD(dd v, int o) {
+    return dd{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+}
+
+/// Sampling sums of one side (new: lanes 0-2, old: lanes 3-5) for one dimension, all levels.
+/// Writes per level: [0] sum of squared sampling displacements, [1] kinetic |dr|^2 sum,
+/// [2] trap r^2 sum (if the trap acts at that level).
+__device__ __forceinline__ void SideSums(const ChainDev& c, bool is_new, uint32_t d, uint32_t NL, uint32_t B, float* s_pos,
+                                         const float* s_old, const float* s_z, dd (*s_dim)[2][3][3]) {
+    const int pbc = c.pbc;
+    const float L = c.L, iL = c.iL;
+    for (int li = (int)NL - 1; li >= 0; --li) {
+        const uint32_t skip = 1u << li;
+        dd samp = DD(0.f);
+        const uint32_t i0 = (B >> (li + 1)) - 1u;  // beads sampled on the levels above
+        for (uint32_t a = 0; a < B; a += 2 * skip) {
+            const float ra = s_pos[3 * a + d], rc = s_pos[3 * (a + 2 * skip) + d];
+            const float rbar = __fadd_rn(ra, __fmul_rn(0.5f, MinImg(__fsub_rn(rc, ra), pbc, L, iL)));
+            if (is_new) {
+                const float delta = MinImg(__fmul_rn(c.sigma[li], s_z[3 * (i0 + a / (2 * skip)) + d]), pbc, L, iL);
+                s_pos[3 * (a + skip) + d] = __fadd_rn(rbar, delta);
+                samp = AddSq(samp, delta);
+            } else {
+                const float delta = MinImg(__fsub_rn(s_old[3 * (a + skip) + d], rbar), pbc, L, iL);
+                samp = AddSq(samp, delta);
+            }
+        }
+        // A segment spanning the whole ring (B == M) has no kinetic links: the reference walks from
+        // the first bead to GetNextBead(B), which is the first bead itself (kinetic_class.h:111-117).
+        const bool kin_links = B != c.n_bead;
+        dd kin = DD(0.f), trap = DD(0.f);
+        for (uint32_t k = 0; k < B; k += skip) {
+            const float x = s_pos[3 * k + d];
+            if (kin_links) kin = AddSq(kin, MinImg(__fsub_rn(x, s_pos[3 * (k + skip) + d]), pbc, L, iL));
+            trap = AddSq(trap, x);
+        }
+        const uint32_t side = is_new ? 0u : 1u;
+        s_dim[li][side][0][d] = samp;
+        s_dim[li][side][1][d] = kin;
+        s_dim[li][side][2][d] = trap;
+    }
+}
+
+__global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArgs a, uint64_t n_sweeps, uint64_t n_attempts) {
+    const uint32_t ci = a.order[blockIdx.x];
+    const ChainDev& c = a.chains[ci];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t G = c.n_warps;
+    if (warp >= G) return;
+    const uint32_t T = G * 32u, t = threadIdx.x;
+    const uint32_t N = c.n_part, M = c.n_bead, NL = c.n_level, B = 1u << NL, n_pad = c.n_pad;
+    const int pbc = c.pbc;
+    const float L = c.L, iL = c.iL;
+    float4* __restrict__ pos = a.pos + c.pos_off;
+
+    __shared__ float s_old[3 * (kMaxB + 1)], s_new[3 * (kMaxB + 1)], s_z[3 * (kMaxB - 1)];
+    __shared__ float s_logu[kBatchMaxLevels];
+    __shared__ dd s_dim[kBatchMaxLevels][2][3][3];
+    __shared__ dd s_part[kBatchMaxWarps];
+    __shared__ dd s_base0;  // level-0 log acceptance without the pair term
+    __shared__ int s_upper_ok;
+
+    // Pair items: (inner slice k in 1..B-1) x (other particle); item i -> k = 1 + i / (N-1).
+    const uint32_t nm1 = N > 1 ? N - 1 : 1;
+    const uint32_t n_items = c.has_pair && N > 1 ? (N - 1) * (B - 1) : 0u;
+    const uint32_t magic = (uint32_t)((0x100000000ull + nm1 - 1) / nm1);
+
+    uint64_t att = a.attempts[ci], acc = a.accepts[ci];
+    const uint64_t n_att = n_sweeps ? n_sweeps * c.attempts_per_sweep : n_attempts;
+    for (uint64_t it = 0; it < n_att; ++it, ++att) {
+        const MoveStream st{c.seed, c.chain_id, c.move, att};
+        const Philox4 w0 = st.Block(0);
+        const uint32_t p = UniformIndex(w0.v[0], N), b0 = UniformIndex(w0.v[1], M);
+
+        // Issue the first pair items' loads now; they complete while warp 0 samples.
+        float4 pre[kPrefetch];
+#pragma unroll
+        for (uint32_t j = 0; j < kPrefetch; ++j) {
+            const uint32_t i = t + j * T;
+            if (i < n_items) {
+                const uint32_t k = FastDiv(i, magic), qq = i - k * nm1;
+                const uint32_t q = qq + (qq >= p ? 1u : 0u);
+                const uint32_t b = (b0 + 1u + k) % M;
+                pre[j] = pos[(size_t)b * n_pad + q];
+            }
+        }
+
+        if (warp == 0) {
+            for (uint32_t j = lane; j < (B - 1) + NL; j += 32) {
+                if (j < B - 1) {
+                    float z[3];
+                    BisectNormals(st, j, z);
+                    s_z[3 * j] = z[0];
+                    s_z[3 * j + 1] = z[1];
+                    s_z[3 * j + 2] = z[2];
+                } else {
+                    const uint32_t li = j - (B - 1);  // 0 = top level
+                    s_logu[NL - 1 - li] = BisectLogU(st, B, li);
+                }
+            }
+            for (uint32_t k = lane; k <= B; k += 32) {
+                const float4 r = pos[(size_t)((b0 + k) % M) * n_pad + p];
+                s_old[3 * k] = s_new[3 * k] = r.x;
+                s_old[3 * k + 1] = s_new[3 * k + 1] = r.y;
+                s_old[3 * k + 2] = s_new[3 * k + 2] = r.z;
+            }
+            __syncwarp();
+            if (lane < 3) SideSums(c, true, lane, NL, B, s_new, s_old, s_z, s_dim);
+            else if (lane < 6) SideSums(c, false, lane - 3, NL, B, s_old, s_old, s_z, s_dim);
+            __syncwarp();
+            // Lane li assembles level li: log_accept = i4s (sum_new dz^2 - sum_old dz^2)
+            //   - [i4l (kin_new - kin_old) + cofa 2^li (trap_new - trap_old)] + dS_{li+1}.
+            dd dS = DD(0.f), lsr = DD(0.f);
+            if (lane < NL) {
+                const uint32_t li = lane;
+                dd v[2][3];
+#pragma unroll
+                for (int s = 0; s < 2; ++s)
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) v[s][q] = Add(Add(s_dim[li][s][q][0], s_dim[li][s][q][1]), s_dim[li][s][q][2]);
+                lsr = MulF(Sub(v[0][0], v[1][0]), c.i4lt_sample[li]);
+                dS = MulF(Sub(v[0][1], v[1][1]), c.i4lt_level[li]);
+                if (c.has_trap && (int)li <= c.trap_max_level)
+                    dS = Add(dS, MulF(Sub(v[0][2], v[1][2]), __fmul_rn(c.trap_cofa, (float)(1u << li))));
+            }
+            const dd prev = ShflDownDD(dS, 1);
+            dd la = Sub(lsr, dS);
+            if (lane + 1 < NL) la = Add(la, prev);
+            if (!isfinite(la.hi)) la.hi = -INFINITY;
+            const bool fail = lane >= 1 && lane < NL && Less(la, DD(s_logu[lane]));
+            const unsigned fails = __ballot_sync(0xffffffffu, fail);
+            if (lane == 0) {
+                s_upper_ok = fails == 0u;
+                s_base0 = la;
+            }
+        }
+        GroupSync(G);
+        const bool upper_ok = s_upper_ok != 0;
+
+        if (upper_ok && n_items) {
+            dd acc_u = DD(0.f);
+            for (uint32_t base = t; base < n_items; base += kPrefetch * T) {
+#pragma unroll
+                for (uint32_t j = 0; j < kPrefetch; ++j) {
+                    const uint32_t i = base + j * T;
+                    if (i < n_items) {
+                        const uint32_t k = FastDiv(i, magic);
+                        float4 rq;
+                        if (base == t) {
+                            rq = pre[j];
+                        } else {
+                            const uint32_t qq = i - k * nm1;
+                            const uint32_t q = qq + (qq >= p ? 1u : 0u);
+                            rq = pos[(size_t)((b0 + 1u + k) % M) * n_pad + q];
+                        }
+                        const float* ro = s_old + 3 * (k + 1);
+                        const float* rn = s_new + 3 * (k + 1);
+                        const float ox = MinImg(__fsub_rn(ro[0], rq.x), pbc, L, iL);
+                        const float oy = MinImg(__fsub_rn(ro[1], rq.y), pbc, L, iL);
+                        const float oz = MinImg(__fsub_rn(ro[2], rq.z), pbc, L, iL);
+                        const float nx = MinImg(__fsub_rn(rn[0], rq.x), pbc, L, iL);
+                        const float ny = MinImg(__fsub_rn(rn[1], rq.y), pbc, L, iL);
+                        const float nz = MinImg(__fsub_rn(rn[2], rq.z), pbc, L, iL);
+                        float r2o = __fmaf_rn(ox, ox, __fmaf_rn(oy, oy, __fmul_rn(oz, oz)));
+                        float r2n = __fmaf_rn(nx, nx, __fmaf_rn(ny, ny, __fmul_rn(nz, nz)));
+                        r2o = fminf(fmaxf(r2o, c.r2_min), c.r2_max);
+                        r2n = fminf(fmaxf(r2n, c.r2_min), c.r2_max);
+                        acc_u = AddF(acc_u, __fsub_rn(rsqrtf(r2n), rsqrtf(r2o)));
+                    }
+                }
+            }
+            acc_u = WarpSumDD(acc_u);
+            if (lane == 0) s_part[warp] = acc_u;
+        }
+        GroupSync(G);
+
+        if (warp == 0) {
+            bool accepted = upper_ok;
+            if (upper_ok) {
+                // Level 0: pair action difference tau * sum (1/r_new - 1/r_old) over inner slices
+                // (each inner slice closes two links with weight 1/2; the segment ends cancel).
+                dd u = DD(0.f);
+                if (n_items)
+                    for (uint32_t w = 0; w < G; ++w) u = Add(u, s_part[w]);
+                dd la0 = Sub(s_base0, MulF(u, c.tau));
+                if (!isfinite(la0.hi)) la0.hi = -INFINITY;
+                accepted = !Less(la0, DD(s_logu[0]));
+            }
+            if (accepted)
+                for (uint32_t k = 1 + lane; k < B; k += 32)
+                    pos[(size_t)((b0 + k) % M) * n_pad + p] = make_float4(s_new[3 * k], s_new[3 * k + 1], s_new[3 * k + 2], 0.f);
+            acc += accepted ? 1u : 0u;
+        }
+        GroupSync(G);
+    }
+    if (t == 0) {
+        a.attempts[ci] = att;
+        a.accepts[ci] = acc;
+    }
+}
+
+/// Thermal energy estimator of one chain (Energy::Accumulate with use_thermal, energy_class.h:
+/// 36-58): the sum of the actions' DActionDBeta divided by M, per action:
+///   Kinetic       N M D / (2 tau) - sum_{p,b} |r_{b+1} - r_b|^2 / (4 lambda tau^2)  kinetic_class.h:35-45
+///   HarmonicTrap  cofactor_b sum_{p,b} r^2                                         trap_class.h:20-35
+///   Coulomb       sum_{p<q} sum_b (1/r_b + 1/r_{b+1}) / 2                          pair_action_class.h:241-264
+__global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchEnergyKernel(BatchArgs a) {
+    const uint32_t ci = a.order[blockIdx.x];
+    const ChainDev& c = a.chains[ci];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t G = c.n_warps;
+    if (warp >= G) return;
+    const uint32_t T = G * 32u, t = threadIdx.x;
+    const uint32_t N = c.n_part, M = c.n_bead, n_pad = c.n_pad;
+    const int pbc = c.pbc;
+    const float L = c.L, iL = c.iL;
+    const float4* __restrict__ pos = a.pos + c.pos_off;
+    __shared__ dd s_red[3][kBatchMaxWarps];
+
+    dd kin = DD(0.f), trap = DD(0.f), pair = DD(0.f);
+    for (uint32_t i = t; i < N * M; i += T) {
+        const uint32_t b = i / N, pp = i - b * N;
+        const float4 r = pos[(size_t)b * n_pad + pp];
+        const float4 r1 = pos[(size_t)((b + 1) % M) * n_pad + pp];
+        // |r_{b+1} - r_b|^2 with exact differences (TwoSum) and products (TwoProd).
+        dd dx = TwoSum(r1.x, -r.x), dy = TwoSum(r1.y, -r.y), dz = TwoSum(r1.z, -r.z);
+        if (pbc) {
+            dx = Sub(dx, DD(__fmul_rn(L, rintf(__fmul_rn(dx.hi, iL)))));
+            dy = Sub(dy, DD(__fmul_rn(L, rintf(__fmul_rn(dy.hi, iL)))));
+            dz = Sub(dz, DD(__fmul_rn(L, rintf(__fmul_rn(dz.hi, iL)))));
+        }
+        kin = Add(kin, Add(Add(Sqr(dx), Sqr(dy)), Sqr(dz)));
+        trap = AddSq(AddSq(AddSq(trap, r.x), r.y), r.z);
+    }
+    if (c.has_pair && N > 1) {
+        // Unordered pairs of one slice: (p, p + o mod N) for o = 1 .. (N-1)/2, plus o = N/2 for
+        // p < N/2 when N is even; every lane gets the same share of pairs.
+        const uint32_t half = (N - 1) / 2, n_main = N * half;
+        const uint32_t n_pairs = N * (N - 1) / 2;
+        for (uint32_t b = 0; b < M; ++b) {
+            const float4* row = pos + (size_t)b * n_pad;
+            for (uint32_t j = t; j < n_pairs; j += T) {
+                uint32_t pp, o;
+                if (j < n_main) {
+                    o = 1 + j / N;
+                    pp = j - (o - 1) * N;
+                } else {
+                    pp = j - n_main;
+                    o = N / 2;
+                }
+                uint32_t q = pp + o;
+                if (q >= N) q -= N;
+                const float4 r = row[pp], s = row[q];
+                const float x = MinImg(__fsub_rn(r.x, s.x), pbc, L, iL);
+                const float y = MinImg(__fsub_rn(r.y, s.y), pbc, L, iL);
+                const float z = MinImg(__fsub_rn(r.z, s.z), pbc, L, iL);
+                float r2 = __fmaf_rn(x, x, __fmaf_rn(y, y, __fmul_rn(z, z)));
+                r2 = fminf(fmaxf(r2, c.r2_min), c.r2_max);
+                pair = AddF(pair, rsqrtf(r2));
+            }
+        }
+    }
+    kin = WarpSumDD(kin);
+    trap = WarpSumDD(trap);
+    pair = WarpSumDD(pair);
+    if (lane == 0) {
+        s_red[0][warp] = kin;
+        s_red[1][warp] = trap;
+        s_red[2][warp] = pair;
+    }
+    GroupSync(G);
+    if (t == 0) {
+        dd k = DD(0.f), tr = DD(0.f), pr = DD(0.f);
+        for (uint32_t w = 0; w < G; ++w) {
+            k = Add(k, s_red[0][w]);
+            tr = Add(tr, s_red[1][w]);
+            pr = Add(pr, s_red[2][w]);
+        }
+        const double inv_m = 1.0 / (double)M;
+        const double e_kin = (c.kin_const - c.i4ltt * ToDouble(k)) * inv_m;
+        const double e_trap = c.has_trap ? c.trap_cofb * ToDouble(tr) * inv_m : 0.;
+        const double e_pair = ToDouble(pr) * inv_m;
+        const uint64_t n = a.n_meas[ci];
+        if (!isfinite(e_kin + e_trap + e_pair)) atomicOr(a.err, kDevErrNonFinite);
+        if (n < a.series_cap) {
+            double* out = a.series + ((size_t)ci * a.series_cap + n) * kBatchSeriesComponents;
+            out[0] = e_kin + e_trap + e_pair;
+            out[1] = e_kin;
+            out[2] = e_trap;
+            out[3] = e_pair;
+        }
+        a.n_meas[ci] = n + 1;
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+// Host side.
+
+ChainSpec ParseChain(const std::string& xml, const std::string& base_dir) {
+    ChainSpec s;
+    const Input in = Input::FromString(xml);
+    const Input rng = in.GetChild("RNG");
+    s.seed = rng.IsNull() ? (uint32_t)time(nullptr) : (uint32_t)rng.GetAttribute<int>("seed", (int)time(nullptr));
+    const Input sys = in.GetChild("System");
+    if (sys.IsNull()) throw PimcError(kErrInput, "input has no <System> element");
+    if (sys.GetAttribute<uint32_t>("n_d") != 3) throw PimcError(kErrUnsupported, "batched chains need n_d = 3");
+    s.n_bead = sys.GetAttribute<uint32_t>("n_bead");
+    s.beta = sys.GetAttribute<double>("beta");
+    s.pbc = sys.GetAttribute<bool>("pbc", true);  // path_class.h:29 defaults to periodic
+    s.L = s.pbc ? sys.GetAttribute<double>("L") : 0.;
+    if (s.n_bead < 2 || !(s.beta > 0.) || (s.pbc && !(s.L > 0.))) throw PimcError(kErrInput, "bad <System> parameters");
+    s.tau = s.beta / s.n_bead;
+    const auto species = in.GetChild("Particles").GetChildList("Species");
+    if (species.size() != 1) throw PimcError(kErrUnsupported, "batched chains need exactly one species");
+    const std::string sp = species[0].GetAttribute<std::string>("name");
+    s.n_part = species[0].GetAttribute<uint32_t>("n_part");
+    s.lambda = species[0].GetAttribute<double>("lambda");
+    if (species[0].GetAttribute<bool>("fermi", false) || species[0].GetAttribute<bool>("fixed_node", false))
+        throw PimcError(kErrUnsupported, "batched chains are Boltzmannons");
+    if (s.n_part < 1 || !(s.lambda > 0.)) throw PimcError(kErrInput, "bad <Species> parameters");
+    if (s.n_part > 4096 || s.n_bead > 65536) throw PimcError(kErrUnsupported, "batched chains: n_part <= 4096, n_bead <= 65536");
+    bool has_kinetic = false;
+    for (const Input& a : in.GetChild("Actions").GetChildList("Action")) {
+        const std::string type = a.GetAttribute<std::string>("type");
+        if (type == "Kinetic") {
+            if (a.GetAttribute<std::string>("species") != sp || a.GetAttribute<int>("n_images", 0) != 0)
+                throw PimcError(kErrUnsupported, "batched Kinetic action: one species, n_images = 0");
+            has_kinetic = true;
+        } else if (type == "HarmonicTrap") {
+            if (a.GetAttribute<std::string>("species") != sp) throw PimcError(kErrInput, "trap on an unknown species");
+            s.has_trap = true;
+            s.omega = a.GetAttribute<double>("omega");
+            s.trap_max_level = a.GetAttribute<uint32_t>("max_level", 0);
+        } else if (type == "BarePairAction") {
+            if (a.GetAttribute<std::string>("species_a") != sp || a.GetAttribute<std::string>("species_b") != sp ||
+                !a.GetAttribute<bool>("is_coulomb", false) || a.GetAttribute<bool>("use_long_range", false))
+                throw PimcError(kErrUnsupported, "batched pair action: bare Coulomb within the species, no long range");
+            std::string file = a.GetAttribute<std::string>("file");
+            if (!file.empty() && file[0] != '/' && !base_dir.empty()) file = base_dir + "/" + file;
+            const TableFile tf = TableFile::Load(file);
+            const auto& r = tf.Vec("v/diag/r");
+            if (r.size() < 2) throw PimcError(kErrInput, "table '" + file + "': empty r grid");
+            s.has_pair = true;
+            s.r_min = r.front();
+            s.r_max = r.back();
+        } else {
+            throw PimcError(kErrUnsupported, "batched chains do not support action type '" + type + "'");
+        }
+    }
+    if (!has_kinetic) throw PimcError(kErrUnsupported, "batched chains need a Kinetic action");
+    const auto moves = in.GetChild("Moves").GetChildList("Move");
+    if (moves.size() != 1 || moves[0].GetAttribute<std::string>("type") != "Bisect")
+        throw PimcError(kErrUnsupported, "batched chains need exactly one Bisect move");
+    if (moves[0].GetAttribute<std::string>("species") != sp) throw PimcError(kErrInput, "Bisect on an unknown species");
+    if (moves[0].GetAttribute<bool>("adaptive", false) || moves[0].GetAttribute<int>("n_images", 0) != 0)
+        throw PimcError(kErrUnsupported, "batched Bisect: fixed level, n_images = 0");
+    s.n_level = moves[0].GetAttribute<uint32_t>("n_level");
+    if (s.n_level < 1 || s.n_level > kBatchMaxLevels) throw PimcError(kErrUnsupported, "batched Bisect needs 1 <= n_level <= 5");
+    if ((1u << s.n_level) > s.n_bead) throw PimcError(kErrInput, "bisection segment longer than the path");
+    s.move = 0;
+    return s;
+}
+
+ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& base_dir, int dev) : device(dev) {
+    if (xml.empty()) throw PimcError(kErrArg, "no chains");
+    n_chains = (uint32_t)xml.size();
+    for (const auto& x : xml) specs.push_back(ParseChain(x, base_dir));  // input errors before any CUDA call
+    CudaCheck(cudaSetDevice(device), "cudaSetDevice");
+    CudaCheck(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, device), "device attribute");
+    chains.resize(n_chains);
+    uint64_t off = 0;
+    for (uint32_t i = 0; i < n_chains; ++i) {
+        const ChainSpec& s = specs[i];
+        ChainDev& c = chains[i];
+        std::memset(&c, 0, sizeof(c));
+        c.n_part = s.n_part;
+        c.n_bead = s.n_bead;
+        c.n_pad = (s.n_part + 7u) & ~7u;
+        c.n_level = s.n_level;
+        c.seed = s.seed;
+        c.chain_id = i;
+        c.move = s.move;
+        c.pos_off = off;
+        off += (uint64_t)c.n_pad * c.n_bead;
+        const uint32_t B = 1u << s.n_level;
+        c.attempts_per_sweep = (uint64_t)s.n_part * ((s.n_bead + B - 1) / B);
+        c.L = (float)s.L;
+        c.iL = s.pbc ? (float)(1. / s.L) : 0.f;
+        c.lambda = (float)s.lambda;
+        c.tau = (float)s.tau;
+        for (uint32_t l = 0; l < s.n_level; ++l) {
+            const double lt = s.tau * (double)(1u << l);
+            c.sigma[l] = (float)std::sqrt(s.lambda * lt);
+            c.i4lt_sample[l] = (float)(1. / (4. * s.lambda * 0.5 * lt));
+            c.i4lt_level[l] = (float)(1. / (4. * s.lambda * lt));
+        }
+        c.pbc = s.pbc ? 1 : 0;
+        c.has_trap = s.has_trap ? 1 : 0;
+        c.has_pair = s.has_pair ? 1 : 0;
+        c.trap_max_level = (int32_t)s.trap_max_level;
+        const double w2 = s.omega * s.omega, t2 = s.tau * s.tau;
+        c.trap_cofa = (float)(0.5 * s.tau * w2 * (1. + t2 * w2 / 12.));  // trap_class.h:14-15
+        c.trap_cofb = 0.5 * w2 * (1. + 3. * t2 * w2 / 12.);
+        c.r2_min = (float)(s.r_min * s.r_min);
+        c.r2_max = (float)(s.r_max * s.r_max);
+        c.kin_const = (double)s.n_part * s.n_bead * 3. / (2. * s.tau);  // kinetic_class.h:13
+        c.i4ltt = 1. / (4. * s.lambda * s.tau * s.tau);
+        bead_moves_per_sweep += c.attempts_per_sweep * (B - 1);
+    }
+    series_cap = 4096;
+    CudaCheck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream create");
+    pos_.reset(new DeviceBuffer(off * sizeof(float4)));
+    CudaCheck(cudaMemset(pos_->ptr, 0, off * sizeof(float4)), "memset");
+    chains_dev_.reset(new DeviceBuffer(n_chains * sizeof(ChainDev)));
+    order_dev_.reset(new DeviceBuffer(n_chains * sizeof(uint32_t)));
+    att_.reset(new DeviceBuffer(n_chains * sizeof(uint64_t)));
+    acc_.reset(new DeviceBuffer(n_chains * sizeof(uint64_t)));
+    n_meas_.reset(new DeviceBuffer(n_chains * sizeof(uint64_t)));
+    series_.reset(new DeviceBuffer((size_t)n_chains * series_cap * kBatchSeriesComponents * sizeof(double)));
+    err_.reset(new DeviceBuffer(sizeof(int)));
+    CudaCheck(cudaMemset(att_->ptr, 0, n_chains * sizeof(uint64_t)), "memset");
+    CudaCheck(cudaMemset(acc_->ptr, 0, n_chains * sizeof(uint64_t)), "memset");
+    CudaCheck(cudaMemset(n_meas_->ptr, 0, n_chains * sizeof(uint64_t)), "memset");
+    CudaCheck(cudaMemset(err_->ptr, 0, sizeof(int)), "memset");
+    SetTiles(items_per_lane, max_warps);
+}
+
+ChainBatch::~ChainBatch() {
+    if (graph_) cudaGraphExecDestroy(graph_);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+void ChainBatch::ResetGraph() {
+    if (graph_) cudaGraphExecDestroy(graph_);
+    graph_ = nullptr;
+    graph_sweeps_ = 0;
+}
+
+/// Pair tile: chain c gets ceil((N-1)(B-1) / (32 items_per_lane)) warps, at most max_warps.
+/// Blocks are ordered by descending work so the longest chains start first.
+void ChainBatch::SetTiles(uint32_t ipl, uint32_t mw) {
+    if (ipl < 1 || mw < 1 || mw > kBatchMaxWarps) throw PimcError(kErrArg, "tile: items_per_lane >= 1, 1 <= max_warps <= 16");
+    items_per_lane = ipl;
+    max_warps = mw;
+    for (auto& c : chains) {
+        const uint64_t items = (uint64_t)(c.n_part > 1 ? c.n_part - 1 : 1) * ((1u << c.n_level) - 1);
+        const uint64_t g = (items + 32ull * ipl - 1) / (32ull * ipl);
+        c.n_warps = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(g, mw));
+    }
+    order.resize(n_chains);
+    std::iota(order.begin(), order.end(), 0u);
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+        const double wx = (double)chains[x].attempts_per_sweep * chains[x].n_part;
+        const double wy = (double)chains[y].attempts_per_sweep * chains[y].n_part;
+        return wx > wy;
+    });
+    Upload();
+    ResetGraph();
+}
+
+void ChainBatch::Upload() {
+    CudaCheck(cudaMemcpyAsync(chains_dev_->ptr, chains.data(), n_chains * sizeof(ChainDev), cudaMemcpyHostToDevice, stream), "upload chains");
+    CudaCheck(cudaMemcpyAsync(order_dev_->ptr, order.data(), n_chains * sizeof(uint32_t), cudaMemcpyHostToDevice, stream), "upload order");
+    CudaCheck(cudaStreamSynchronize(stream), "sync");
+}
+
+void ChainBatch::SetPath(uint32_t chain, const double* p) {
+    if (chain >= n_chains || !p) throw PimcError(kErrArg, "bad chain or null path");
+    const ChainDev& c = chains[chain];
+    std::vector<float4> h((size_t)c.n_bead * c.n_pad, make_float4(0.f, 0.f, 0.f, 0.f));
+    for (uint32_t i = 0; i < c.n_part; ++i)
+        for (uint32_t b = 0; b < c.n_bead; ++b) {
+            const double* r = p + ((size_t)i * c.n_bead + b) * 3;
+            if (!std::isfinite(r[0]) || !std::isfinite(r[1]) || !std::isfinite(r[2])) throw PimcError(kErrArg, "non-finite position");
+            h[(size_t)b * c.n_pad + i] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.f);
+        }
+    CudaCheck(cudaMemcpyAsync(pos_->as<float4>() + c.pos_off, h.data(), h.size() * sizeof(float4), cudaMemcpyHostToDevice, stream), "set path");
+    CudaCheck(cudaStreamSynchronize(stream), "sync");
+}
+
+void ChainBatch::GetPath(uint32_t chain, double* p) {
+    if (chain >= n_chains || !p) throw PimcError(kErrArg, "bad chain or null path");
+    const ChainDev& c = chains[chain];
+    std::vector<float4> h((size_t)c.n_bead * c.n_pad);
+    CudaCheck(cudaMemcpyAsync(h.data(), pos_->as<float4>() + c.pos_off, h.size() * sizeof(float4), cudaMemcpyDeviceToHost, stream), "get path");
+    CudaCheck(cudaStreamSynchronize(stream), "sync");
+    for (uint32_t i = 0; i < c.n_part; ++i)
+        for (uint32_t b = 0; b < c.n_bead; ++b) {
+            const float4 r = h[(size_t)b * c.n_pad + i];
+            double* o = p + ((size_t)i * c.n_bead + b) * 3;
+            o[0] = r.x;
+            o[1] = r.y;
+            o[2] = r.z;
+        }
+}
+
+namespace {
+BatchArgs MakeArgs(DeviceBuffer& pos, DeviceBuffer& ch, DeviceBuffer& ord, DeviceBuffer& att, DeviceBuffer& acc, DeviceBuffer& ser,
+                   DeviceBuffer& nm, DeviceBuffer& err, uint32_t cap) {
+    return BatchArgs{pos.as<float4>(), ch.as<ChainDev>(), ord.as<uint32_t>(), att.as<uint64_t>(), acc.as<uint64_t>(),
+                     ser.as<double>(), nm.as<uint64_t>(), err.as<int>(), cap};
+}
+}  // namespace
+
+void ChainBatch::LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts) {
+    uint32_t warps = 1;
+    for (const auto& c : chains) warps = std::max(warps, c.n_warps);
+    const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *err_, series_cap);
+    BatchSweepKernel<<<n_chains, warps * 32, 0, stream>>>(a, n_sweeps, n_attempts);
+    CudaCheck(cudaGetLastError(), "batch sweep launch");
+    ++kernel_launches;
+}
+
+void ChainBatch::LaunchMeasure() {
+    uint32_t warps = 1;
+    for (const auto& c : chains) warps = std::max(warps, c.n_warps);
+    const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *err_, series_cap);
+    BatchEnergyKernel<<<n_chains, warps * 32, 0, stream>>>(a);
+    CudaCheck(cudaGetLastError(), "batch energy launch");
+    ++kernel_launches;
+}
+
+void ChainBatch::Attempts(uint64_t n) {
+    if (n) LaunchSweep(0, n);
+}
+
+void ChainBatch::Sweeps(uint64_t n) {
+    if (n) LaunchSweep(n, 0);
+}
+
+void ChainBatch::Measure() { LaunchMeasure(); }
+
+void ChainBatch::Run(uint64_t n_cycles, uint64_t spm) {
+    if (spm == 0) throw PimcError(kErrArg, "sweeps_per_measure must be positive");
+    if (!graph_ || graph_sweeps_ != spm) {
+        ResetGraph();
+        cudaGraph_t g = nullptr;
+        CudaCheck(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        const uint64_t before = kernel_launches;
+        LaunchSweep(spm, 0);
+        LaunchMeasure();
+        kernel_launches = before;
+        CudaCheck(cudaStreamEndCapture(stream, &g), "end capture");
+        const cudaError_t e = cudaGraphInstantiate(&graph_, g, 0);
+        cudaGraphDestroy(g);
+        CudaCheck(e, "graph instantiate");
+        graph_sweeps_ = spm;
+    }
+    for (uint64_t i = 0; i < n_cycles; ++i) {
+        CudaCheck(cudaGraphLaunch(graph_, stream), "graph launch");
+        kernel_launches += 2;
+    }
+}
+
+void ChainBatch::Sync() {
+    CudaCheck(cudaStreamSynchronize(stream), "sync");
+    int e = 0;
+    CudaCheck(cudaMemcpy(&e, err_->ptr, sizeof(int), cudaMemcpyDeviceToHost), "read error word");
+    if (e & kDevErrNonFinite) throw PimcError(kErrNonFinite, "non-finite energy in a batched chain");
+}
+
+uint64_t ChainBatch::ReadEnergy(uint32_t chain, double* out, uint64_t cap) {
+    if (chain >= n_chains) throw PimcError(kErrArg, "bad chain");
+    Sync();
+    uint64_t n = 0;
+    CudaCheck(cudaMemcpy(&n, n_meas_->as<uint64_t>() + chain, sizeof(uint64_t), cudaMemcpyDeviceToHost), "read n");
+    const uint64_t kept = std::min<uint64_t>(n, series_cap);
+    if (out && cap) {
+        const uint64_t m = std::min(kept, cap);
+        CudaCheck(cudaMemcpy(out, series_->as<double>() + (size_t)chain * series_cap * kBatchSeriesComponents,
+                             m * kBatchSeriesComponents * sizeof(double), cudaMemcpyDeviceToHost),
+                  "read series");
+    }
+    return n;
+}
+
+void ChainBatch::ResetEnergy() {
+    CudaCheck(cudaMemsetAsync(n_meas_->ptr, 0, n_chains * sizeof(uint64_t), stream), "reset");
+    CudaCheck(cudaStreamSynchronize(stream), "sync");
+}
+
+void ChainBatch::ReadCounters(uint64_t* attempts, uint64_t* accepts) {
+    Sync();
+    if (attempts) CudaCheck(cudaMemcpy(attempts, att_->ptr, n_chains * sizeof(uint64_t), cudaMemcpyDeviceToHost), "read attempts");
+    if (accepts) CudaCheck(cudaMemcpy(accepts, acc_->ptr, n_chains * sizeof(uint64_t), cudaMemcpyDeviceToHost), "read accepts");
+}
+
+/// Times trial sweeps for every (items_per_lane, max_warps) candidate on a copy of the chains'
+/// state, restores the state after each trial and keeps the fastest tile.
+double ChainBatch::Autotune(uint32_t trial_sweeps) {
+    if (trial_sweeps == 0) trial_sweeps = 1;
+    DeviceBuffer pos_save(pos_->bytes), att_save(att_->bytes), acc_save(acc_->bytes);
+    auto copy = [&](DeviceBuffer& dst, const DeviceBuffer& src) {
+        CudaCheck(cudaMemcpyAsync(dst.ptr, src.ptr, src.bytes, cudaMemcpyDeviceToDevice, stream), "state copy");
+    };
+    copy(pos_save, *pos_);
+    copy(att_save, *att_);
+    copy(acc_save, *acc_);
+    cudaEvent_t e0, e1;
+    CudaCheck(cudaEventCreate(&e0), "event");
+    CudaCheck(cudaEventCreate(&e1), "event");
+    const uint32_t ipls[] = {2, 4, 8, 16};
+    const uint32_t mws[] = {2, 4, 8, 16};
+    double best = 1e300;
+    uint32_t best_ipl = items_per_lane, best_mw = max_warps;
+    for (uint32_t ipl : ipls)
+        for (uint32_t mw : mws) {
+            SetTiles(ipl, mw);
+            LaunchSweep(1, 0);  // warm-up of this shape
+            CudaCheck(cudaEventRecord(e0, stream), "event");
+            LaunchSweep(trial_sweeps, 0);
+            CudaCheck(cudaEventRecord(e1, stream), "event");
+            CudaCheck(cudaEventSynchronize(e1), "event sync");
+            float ms = 0.f;
+            CudaCheck(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+            const double sec = ms * 1e-3 / trial_sweeps;
+            if (sec < best) {
+                best = sec;
+                best_ipl = ipl;
+                best_mw = mw;
+            }
+            copy(*pos_, pos_save);
+            copy(*att_, att_save);
+            copy(*acc_, acc_save);
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    SetTiles(best_ipl, best_mw);
+    CudaCheck(cudaStreamSynchronize(stream), "sync");
+    return best;
+}
+
+}  // namespace pimc
+
+// ---------------------------------------------------------------------------------------------
+// C interface.
+
+struct pimc_batch {
+    std::unique_ptr<pimc::ChainBatch> b;
+    std::string err;
+};
+
+namespace {
+thread_local std::string g_batch_create_error;
+
+template <class F>
+int BatchGuard(pimc_batch* h, F f) {
+    if (!h || !h->b) return PIMC_ERR_ARG;
+    try {
+        f(*h->b);
+        return PIMC_OK;
+    } catch (const pimc::PimcError& e) {
+        h->err = e.what();
+        return e.code;
+    } catch (const pimc::InputError& e) {
+        h->err = e.what();
+        return PIMC_ERR_INPUT;
+    } catch (const std::exception& e) {
+        h->err = e.what();
+        return PIMC_ERR_STATE;
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int pimc_batch_create(const char* const* xml_texts, uint32_t n_chains, const char* base_dir, int device, pimc_batch** out) {
+    if (!xml_texts || !out || n_chains == 0) return PIMC_ERR_ARG;
+    *out = nullptr;
+    try {
+        std::vector<std::string> xml;
+        for (uint32_t i = 0; i < n_chains; ++i) {
+            if (!xml_texts[i]) return PIMC_ERR_ARG;
+            xml.emplace_back(xml_texts[i]);
+        }
+        auto* h = new pimc_batch();
+        try {
+            h->b.reset(new pimc::ChainBatch(xml, base_dir ? base_dir : "", device));
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+        return PIMC_OK;
+    } catch (const pimc::PimcError& e) {
+        g_batch_create_error = e.what();
+        return e.code;
+    } catch (const pimc::InputError& e) {
+        g_batch_create_error = e.what();
+        return PIMC_ERR_INPUT;
+    } catch (const std::exception& e) {
+        g_batch_create_error = e.what();
+        return PIMC_ERR_STATE;
+    }
+}
+
+void pimc_batch_destroy(pimc_batch* b) { delete b; }
+
+const char* pimc_batch_last_error(const pimc_batch* b) { return b ? b->err.c_str() : g_batch_create_error.c_str(); }
+
+int pimc_batch_chain_info(pimc_batch* h, uint32_t chain, uint32_t* out4) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) {
+        if (chain >= b.n_chains || !out4) throw pimc::PimcError(pimc::kErrArg, "bad chain or null output");
+        const auto& c = b.chains[chain];
+        out4[0] = c.n_part;
+        out4[1] = c.n_bead;
+        out4[2] = c.n_level;
+        out4[3] = c.n_warps;
+    });
+}
+
+int pimc_batch_set_path(pimc_batch* h, uint32_t chain, const double* pos) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.SetPath(chain, pos); });
+}
+
+int pimc_batch_get_path(pimc_batch* h, uint32_t chain, double* pos) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.GetPath(chain, pos); });
+}
+
+int pimc_batch_attempts(pimc_batch* h, uint64_t n) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.Attempts(n); });
+}
+
+int pimc_batch_sweeps(pimc_batch* h, uint64_t n) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.Sweeps(n); });
+}
+
+int pimc_batch_measure(pimc_batch* h) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.Measure(); });
+}
+
+int pimc_batch_run(pimc_batch* h, uint64_t n_cycles, uint64_t sweeps_per_measure) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.Run(n_cycles, sweeps_per_measure); });
+}
+
+int pimc_batch_sync(pimc_batch* h) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.Sync(); });
+}
+
+int pimc_batch_energy(pimc_batch* h, uint32_t chain, double* out, uint64_t cap, uint64_t* n_measure) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) {
+        const uint64_t n = b.ReadEnergy(chain, out, cap);
+        if (n_measure) *n_measure = n;
+    });
+}
+
+int pimc_batch_reset_energy(pimc_batch* h) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.ResetEnergy(); });
+}
+
+int pimc_batch_counters(pimc_batch* h, uint64_t* attempts, uint64_t* accepts) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.ReadCounters(attempts, accepts); });
+}
+
+int pimc_batch_set_tiles(pimc_batch* h, uint32_t items_per_lane, uint32_t max_warps) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.SetTiles(items_per_lane, max_warps); });
+}
+
+int pimc_batch_autotune(pimc_batch* h, uint32_t trial_sweeps, uint32_t* items_per_lane, uint32_t* max_warps, double* sec_per_sweep) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) {
+        const double s = b.Autotune(trial_sweeps);
+        if (items_per_lane) *items_per_lane = b.items_per_lane;
+        if (max_warps) *max_warps = b.max_warps;
+        if (sec_per_sweep) *sec_per_sweep = s;
+    });
+}
+
+int pimc_batch_stats(pimc_batch* h, uint64_t* out4) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) {
+        if (!out4) throw pimc::PimcError(pimc::kErrArg, "null output");
+        out4[0] = b.n_chains;
+        out4[1] = b.bead_moves_per_sweep;
+        out4[2] = b.kernel_launches;
+        out4[3] = b.series_cap;
+    });
+}
+
+int pimc_batch_stream(pimc_batch* h, void** stream) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) {
+        if (!stream) throw pimc::PimcError(pimc::kErrArg, "null output");
+        *stream = (void*)b.stream;
+    });
+}
+
+}  // extern "C"

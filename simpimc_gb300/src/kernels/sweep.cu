@@ -226,8 +226,10 @@ __device__ __forceinline__ uint32_t LevelFirst(uint32_t nl, int lvl, uint32_t B)
 ///           (free_spline_class.h:189-197 with tau' = tau 2^l / 2, bisect_class.h:85-94);
 ///   small = kinetic action of the links j -> j + skip (kinetic_class.h:105-122) plus the trap
 ///           action of slices j at stride skip (trap_class.h:37-61, when lvl <= max_level).
-__device__ __forceinline__ void LevelSums(const MoveDD& mv, int lvl, uint32_t B, const dd* seg, const dd* disp, uint32_t first, uint32_t n_d,
-                                          dd L, dd iL, int lane, dd& lsp, dd& small) {
+/// A segment spanning the whole ring (B == M) has no kinetic links: the reference walks from the
+/// first bead to GetNextBead(B), which is the first bead itself (kinetic_class.h:111-117).
+__device__ __forceinline__ void LevelSums(const MoveDD& mv, int lvl, uint32_t B, bool kin_links, const dd* seg, const dd* disp,
+                                          uint32_t first, uint32_t n_d, dd L, dd iL, int lane, dd& lsp, dd& small) {
     const uint32_t skip = 1u << lvl, nm = B / (2 * skip);
     dd sp{0.f, 0.f}, sm{0.f, 0.f};
     for (uint32_t t = lane; t < nm; t += 32) {
@@ -237,7 +239,7 @@ __device__ __forceinline__ void LevelSums(const MoveDD& mv, int lvl, uint32_t B,
         if (mv.has_images) v = Add(v, ImageSum(mv.sample_image[lvl], &disp[3 * (first + t)], n_d));
         sp = Add(sp, v);
     }
-    for (int ki = 0; ki < mv.n_kin; ++ki)
+    for (int ki = 0; ki < (kin_links ? mv.n_kin : 0); ++ki)
         for (uint32_t j = lane * skip; j < B; j += 32 * skip) {
             dd dr[3];
             dd q{0.f, 0.f};
@@ -533,7 +535,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                     }
                     __syncwarp();
                     dd lsp, sm;
-                    LevelSums(mv, lvl, B, seg_old, d_old, first, n_d, a.L, a.iL, lane, lsp, sm);
+                    LevelSums(mv, lvl, B, B != M, seg_old, d_old, first, n_d, a.L, a.iL, lane, lsp, sm);
                     if (lane == 0) {
                         s_old_lsp[lvl] = lsp;
                         s_old_small[lvl] = sm;
@@ -566,7 +568,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                 if (warp < n_lvl_w) {
                     const int lvl = my_level >= 0 ? my_level : warp;
                     dd lsp, sm;
-                    LevelSums(mv, lvl, B, seg_new, d_new, LevelFirst(nl, lvl, B), n_d, a.L, a.iL, lane, lsp, sm);
+                    LevelSums(mv, lvl, B, B != M, seg_new, d_new, LevelFirst(nl, lvl, B), n_d, a.L, a.iL, lane, lsp, sm);
                     if (lane == 0) {
                         const dd diff = Sub(s_old_lsp[lvl], lsp);   // old log-prob - new log-prob
                         const dd small = Sub(sm, s_old_small[lvl]); // new action - old action

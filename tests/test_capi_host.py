@@ -60,3 +60,22 @@ def test_binding_fails_loudly_without_library(tmp_path):
     import simpimc_gb300
     with pytest.raises(RuntimeError, match="not built"):
         simpimc_gb300.load_library(tmp_path / "missing.so")
+
+
+@pytest.mark.parametrize("edit,code", [
+    (('n_images="0"', 'n_images="2"'), -6),                           # Kinetic with periodic images
+    (('type="Bisect"', 'type="Bisect" adaptive="1" target_ratio="0.5"'), -6),
+    (('n_level="2"', 'n_level="6"'), -6),                              # segment beyond 32 beads
+    (('n_bead="8"', 'n_bead="2"'), -2),                                # segment longer than the path
+    (('is_coulomb="1"', 'is_coulomb="0"'), -6),
+])
+def test_batch_rejects_inputs_before_device_work(lib, tmp_path, edit, code):
+    """Chain inputs are parsed before any CUDA call, so these errors are reported without a GPU."""
+    import simpimc_gb300
+    from simpimc_gb300.configs import trapped_coulomb
+    xml, _ = trapped_coulomb(tmp_path, n_part=4, n_bead=8, n_level=2, seed=1)
+    bad = xml.replace(*edit)
+    assert bad != xml
+    with pytest.raises(simpimc_gb300.PimcError) as e:
+        simpimc_gb300.ChainBatch([xml, bad], base_dir=tmp_path)
+    assert e.value.code == code, str(e.value)

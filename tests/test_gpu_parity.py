@@ -137,6 +137,20 @@ def test_trap_bisection_replay(tmp_path, gpu_lib, oracle_mod):
         assert close(g.dactiondbeta(a), c.dactiondbeta(a), 1e-9)
 
 
+def test_full_ring_bisection_replay(tmp_path, gpu_lib, oracle_mod):
+    """A segment of 2^l = M beads: the reference's kinetic walk from the first bead to the bead
+    M slices later stops at once (same bead), so only trap, pair and sampling terms decide."""
+    xml, path = trapped_coulomb(tmp_path, n_part=5, n_bead=8, n_level=3, seed=23)
+    g = Simulation(xml, base_dir=tmp_path)
+    c = oracle_mod.OracleSim(xml, base_dir=tmp_path)
+    g.set_path(path)
+    c.set_path(path)
+    g.move_attempts(0, 400)
+    c.move_attempts(0, 400)
+    assert g.move_stats(0) == c.move_stats(0)
+    assert np.max(np.abs(g.get_path(1) - c.get_path(1))) < 1e-9
+
+
 def test_egas_bisection_replay(tmp_path, gpu_lib, oracle_mod):
     xml, path = electron_gas(tmp_path, n_part=14, n_bead=16, n_level=2, rs=2.0, k_cut_units=4.0, seed=9)
     g = Simulation(xml, base_dir=tmp_path)
