@@ -70,63 +70,88 @@ __device__ __forceinline__ dd ShflDownDD(dd v, int o) {
     return dd{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
 }
 
-/// Sampling sums of one side (new: lanes 0-2, old: lanes 3-5) for one dimension, all levels.
-/// Writes per level: [0] sum of squared sampling displacements, [1] kinetic |dr|^2 sum,
-/// [2] trap r^2 sum (if the trap acts at that level).
-__device__ __forceinline__ void SideSums(const ChainDev& c, bool is_new, uint32_t d, uint32_t NL, uint32_t B, float* s_pos,
-                                         const float* s_old, const float* s_z, dd (*s_dim)[2][3][3]) {
-    const int pbc = c.pbc;
-    const float L = c.L, iL = c.iL;
-    for (int li = (int)NL - 1; li >= 0; --li) {
-        const uint32_t skip = 1u << li;
-        dd samp = DD(0.f);
-        const uint32_t i0 = (B >> (li + 1)) - 1u;  // beads sampled on the levels above
-        for (uint32_t a = 0; a < B; a += 2 * skip) {
-            const float ra = s_pos[3 * a + d], rc = s_pos[3 * (a + 2 * skip) + d];
-            const float rbar = __fadd_rn(ra, __fmul_rn(0.5f, MinImg(__fsub_rn(rc, ra), pbc, L, iL)));
-            if (is_new) {
-                const float delta = MinImg(__fmul_rn(c.sigma[li], s_z[3 * (i0 + a / (2 * skip)) + d]), pbc, L, iL);
-                s_pos[3 * (a + skip) + d] = __fadd_rn(rbar, delta);
-                samp = AddSq(samp, delta);
-            } else {
-                const float delta = MinImg(__fsub_rn(s_old[3 * (a + skip) + d], rbar), pbc, L, iL);
-                samp = AddSq(samp, delta);
-            }
+/// Cascaded compensated sum (Neumaier / Ogita-Rump-Oishi Sum2): the running sum carries one FP32
+/// add per term on its dependency chain; the TwoSum errors gather in a separate FP32 word. The
+/// result is as accurate as a sum formed in twice the working precision.
+struct Comp {
+    float s, c;
+};
+
+__device__ __forceinline__ void CompAdd(Comp& a, float x) {
+    const float t = __fadd_rn(a.s, x);
+    const float bp = __fsub_rn(t, a.s);
+    const float e = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(x, bp));
+    a.s = t;
+    a.c = __fadd_rn(a.c, e);
+}
+
+__device__ __forceinline__ dd CompDD(Comp a) { return TwoSum(a.s, a.c); }
+
+__device__ __forceinline__ float Sq3(float x, float y, float z) { return __fmaf_rn(x, x, __fmaf_rn(y, y, __fmul_rn(z, z))); }
+
+__device__ __forceinline__ uint32_t Wrap(uint32_t s, uint32_t M) { return s >= M ? s - M : s; }  // s < 2M
+
+// Per-level term table of warp 0: q = 0 new sampling |delta|^2, 1 old sampling, 2 new kinetic
+// |dr|^2, 3 old kinetic, 4 new trap r^2, 5 old trap; index = position of the term within its level.
+constexpr int kTermKinds = 6;
+
+/// Draws of one attempt (particle, first bead, normals, log-uniforms; philox.h stream layout) and
+/// the moved particle's segment, by one warp into one of two shared buffers.
+__device__ __forceinline__ void DrawAttempt(const MoveStream& st, uint32_t lane, uint32_t N, uint32_t M, uint32_t B, uint32_t NL, uint32_t n_pad,
+                                            const float4* __restrict__ pos, float* z, float* logu, float4* seg, uint32_t* pb) {
+    const Philox4 w0 = st.Block(0);
+    const uint32_t p = UniformIndex(w0.v[0], N), b0 = UniformIndex(w0.v[1], M);
+    if (lane <= B) seg[lane] = pos[(size_t)Wrap(b0 + lane, M) * n_pad + p];
+    if (B == 32 && lane == 0) seg[32] = pos[(size_t)Wrap(b0 + 32u, M) * n_pad + p];
+    if (lane == 0) {
+        pb[0] = p;
+        pb[1] = b0;
+    }
+    for (uint32_t j = lane; j < (B - 1) + NL; j += 32) {
+        if (j < B - 1) {
+            float zz[3];
+            BisectNormals(st, j, zz);
+            z[3 * j] = zz[0];
+            z[3 * j + 1] = zz[1];
+            z[3 * j + 2] = zz[2];
+        } else {
+            const uint32_t li = j - (B - 1);  // 0 = top level
+            logu[NL - 1 - li] = BisectLogU(st, B, li);
         }
-        // A segment spanning the whole ring (B == M) has no kinetic links: the reference walks from
-        // the first bead to GetNextBead(B), which is the first bead itself (kinetic_class.h:111-117).
-        const bool kin_links = B != c.n_bead;
-        dd kin = DD(0.f), trap = DD(0.f);
-        for (uint32_t k = 0; k < B; k += skip) {
-            const float x = s_pos[3 * k + d];
-            if (kin_links) kin = AddSq(kin, MinImg(__fsub_rn(x, s_pos[3 * (k + skip) + d]), pbc, L, iL));
-            trap = AddSq(trap, x);
-        }
-        const uint32_t side = is_new ? 0u : 1u;
-        s_dim[li][side][0][d] = samp;
-        s_dim[li][side][1][d] = kin;
-        s_dim[li][side][2][d] = trap;
     }
 }
 
 __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArgs a, uint64_t n_sweeps, uint64_t n_attempts) {
     const uint32_t ci = a.order[blockIdx.x];
-    const ChainDev& c = a.chains[ci];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint32_t G = c.n_warps;
+    const uint32_t G = a.chains[ci].n_warps;
     if (warp >= G) return;
     const uint32_t T = G * 32u, t = threadIdx.x;
-    const uint32_t N = c.n_part, M = c.n_bead, NL = c.n_level, B = 1u << NL, n_pad = c.n_pad;
-    const int pbc = c.pbc;
-    const float L = c.L, iL = c.iL;
-    float4* __restrict__ pos = a.pos + c.pos_off;
 
-    __shared__ float s_old[3 * (kMaxB + 1)], s_new[3 * (kMaxB + 1)], s_z[3 * (kMaxB - 1)];
-    __shared__ float s_logu[kBatchMaxLevels];
-    __shared__ dd s_dim[kBatchMaxLevels][2][3][3];
+    __shared__ ChainDev s_c;
+    __shared__ float s_z[2][3 * (kMaxB - 1)];
+    __shared__ float s_logu[2][kBatchMaxLevels];
+    __shared__ float4 s_seg[2][kMaxB + 1];
+    __shared__ uint32_t s_pb[2][2];
+    __shared__ float s_old[3 * (kMaxB + 1)], s_new[3 * (kMaxB + 1)];
+    __shared__ float s_terms[kBatchMaxLevels][kTermKinds][kMaxB];
+    __shared__ dd s_sum[kBatchMaxLevels][kTermKinds];
     __shared__ dd s_part[kBatchMaxWarps];
     __shared__ dd s_base0;  // level-0 log acceptance without the pair term
     __shared__ int s_upper_ok;
+
+    {
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(a.chains + ci);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(&s_c);
+        for (uint32_t i = t; i < sizeof(ChainDev) / 4; i += T) dst[i] = src[i];
+    }
+    GroupSync(G);
+    const ChainDev& c = s_c;
+    const uint32_t N = c.n_part, M = c.n_bead, NL = c.n_level, B = 1u << NL, n_pad = c.n_pad;
+    const int pbc = c.pbc;
+    const float L = c.L, iL = c.iL;
+    const bool kin_links = B != M;  // whole-ring segment: no kinetic links (kinetic_class.h:111-117)
+    float4* __restrict__ pos = a.pos + c.pos_off;
 
     // Pair items: (inner slice k in 1..B-1) x (other particle); item i -> k = 1 + i / (N-1).
     const uint32_t nm1 = N > 1 ? N - 1 : 1;
@@ -135,12 +160,26 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArg
 
     uint64_t att = a.attempts[ci], acc = a.accepts[ci];
     const uint64_t n_att = n_sweeps ? n_sweeps * c.attempts_per_sweep : n_attempts;
-    for (uint64_t it = 0; it < n_att; ++it, ++att) {
-        const MoveStream st{c.seed, c.chain_id, c.move, att};
-        const Philox4 w0 = st.Block(0);
-        const uint32_t p = UniformIndex(w0.v[0], N), b0 = UniformIndex(w0.v[1], M);
+    // With two or more warps, warp 1 draws attempt k+1 (and loads its segment) while warp 0
+    // works on attempt k; a segment loaded before attempt k's commit is patched from warp 0's
+    // registers when both attempts move the same particle.
+    const bool ahead = G >= 2;
+    if (ahead && warp == 1 && n_att > 0)
+        DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, att}, lane, N, M, B, NL, n_pad, pos, s_z[att & 1], s_logu[att & 1], s_seg[att & 1],
+                    s_pb[att & 1]);
+    GroupSync(G);
 
-        // Issue the first pair items' loads now; they complete while warp 0 samples.
+    float nx = 0.f, ny = 0.f, nz = 0.f;  // warp 0, lane k: new position of bead k of the last attempt
+    uint32_t p_prev = 0xffffffffu, b0_prev = 0;
+    bool acc_prev = false;
+    for (uint64_t it = 0; it < n_att; ++it, ++att) {
+        const uint32_t buf = (uint32_t)(att & 1);
+        if (!ahead) {
+            DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, att}, lane, N, M, B, NL, n_pad, pos, s_z[buf], s_logu[buf], s_seg[buf], s_pb[buf]);
+            __syncwarp();
+        }
+        const uint32_t p = s_pb[buf][0], b0 = s_pb[buf][1];
+
         float4 pre[kPrefetch];
 #pragma unroll
         for (uint32_t j = 0; j < kPrefetch; ++j) {
@@ -148,65 +187,175 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArg
             if (i < n_items) {
                 const uint32_t k = FastDiv(i, magic), qq = i - k * nm1;
                 const uint32_t q = qq + (qq >= p ? 1u : 0u);
-                const uint32_t b = (b0 + 1u + k) % M;
-                pre[j] = pos[(size_t)b * n_pad + q];
+                pre[j] = pos[(size_t)Wrap(b0 + 1u + k, M) * n_pad + q];
             }
         }
 
         if (warp == 0) {
-            for (uint32_t j = lane; j < (B - 1) + NL; j += 32) {
-                if (j < B - 1) {
-                    float z[3];
-                    BisectNormals(st, j, z);
-                    s_z[3 * j] = z[0];
-                    s_z[3 * j + 1] = z[1];
-                    s_z[3 * j + 2] = z[2];
-                } else {
-                    const uint32_t li = j - (B - 1);  // 0 = top level
-                    s_logu[NL - 1 - li] = BisectLogU(st, B, li);
+            // Old segment: lane k holds bead k; every lane holds the last bead B.
+            const float4 sv = s_seg[buf][lane <= B ? lane : B];
+            const float4 se = s_seg[buf][B];
+            float ox = sv.x, oy = sv.y, oz = sv.z, ex = se.x, ey = se.y, ez = se.z;
+            if (ahead && acc_prev && p == p_prev) {
+                // Beads of this segment inside the last accepted segment: take the committed values.
+                const uint32_t off = Wrap(Wrap(b0 + (lane <= B ? lane : B), M) + M - b0_prev, M);
+                const uint32_t off_e = Wrap(Wrap(b0 + B, M) + M - b0_prev, M);
+                const bool in = off >= 1 && off < B, in_e = off_e >= 1 && off_e < B;
+                const float px = __shfl_sync(0xffffffffu, nx, in ? off : 0), py = __shfl_sync(0xffffffffu, ny, in ? off : 0),
+                            pz = __shfl_sync(0xffffffffu, nz, in ? off : 0);
+                const float qx = __shfl_sync(0xffffffffu, nx, in_e ? off_e : 0), qy = __shfl_sync(0xffffffffu, ny, in_e ? off_e : 0),
+                            qz = __shfl_sync(0xffffffffu, nz, in_e ? off_e : 0);
+                if (in) {
+                    ox = px;
+                    oy = py;
+                    oz = pz;
+                }
+                if (in_e) {
+                    ex = qx;
+                    ey = qy;
+                    ez = qz;
                 }
             }
-            for (uint32_t k = lane; k <= B; k += 32) {
-                const float4 r = pos[(size_t)((b0 + k) % M) * n_pad + p];
-                s_old[3 * k] = s_new[3 * k] = r.x;
-                s_old[3 * k + 1] = s_new[3 * k + 1] = r.y;
-                s_old[3 * k + 2] = s_new[3 * k + 2] = r.z;
+            // Sampling, level by level (bisect_class.h:77-107): bead k = 2^l (2m + 1) is resampled
+            // on level l from beads k -+ 2^l; positions travel by shuffles.
+            const float* zb = s_z[buf];
+            const uint32_t lk = lane == 0 ? 31u : (uint32_t)(__ffs(lane) - 1);  // level of bead `lane`
+            nx = ox;
+            ny = oy;
+            nz = oz;
+            float dn2 = 0.f;
+            for (int li = (int)NL - 1; li >= 0; --li) {
+                const uint32_t skip = 1u << li;
+                const bool mine = lane < B && lk == (uint32_t)li;
+                const uint32_t sa = mine ? lane - skip : lane, sc = mine ? lane + skip : lane;
+                const float ax = __shfl_sync(0xffffffffu, nx, sa & 31u), ay = __shfl_sync(0xffffffffu, ny, sa & 31u),
+                            az = __shfl_sync(0xffffffffu, nz, sa & 31u);
+                float cx = __shfl_sync(0xffffffffu, nx, sc & 31u), cy = __shfl_sync(0xffffffffu, ny, sc & 31u),
+                      cz = __shfl_sync(0xffffffffu, nz, sc & 31u);
+                if (sc == 32u) {
+                    cx = ex;
+                    cy = ey;
+                    cz = ez;
+                }
+                if (mine) {
+                    const uint32_t zi = 3 * ((B >> (li + 1)) - 1u + (lane >> (li + 1)));
+                    const float sg = c.sigma[li];
+                    const float dx = MinImg(__fmul_rn(sg, zb[zi]), pbc, L, iL), dy = MinImg(__fmul_rn(sg, zb[zi + 1]), pbc, L, iL),
+                                dz = MinImg(__fmul_rn(sg, zb[zi + 2]), pbc, L, iL);
+                    nx = __fadd_rn(__fadd_rn(ax, __fmul_rn(0.5f, MinImg(__fsub_rn(cx, ax), pbc, L, iL))), dx);
+                    ny = __fadd_rn(__fadd_rn(ay, __fmul_rn(0.5f, MinImg(__fsub_rn(cy, ay), pbc, L, iL))), dy);
+                    nz = __fadd_rn(__fadd_rn(az, __fmul_rn(0.5f, MinImg(__fsub_rn(cz, az), pbc, L, iL))), dz);
+                    dn2 = Sq3(dx, dy, dz);
+                }
+            }
+            // Old sampling displacements of every level at once.
+            {
+                const bool inner = lane >= 1 && lane < B;
+                const uint32_t skip = inner ? (1u << lk) : 0u;
+                const uint32_t sa = inner ? lane - skip : lane, sc = inner ? lane + skip : lane;
+                const float ax = __shfl_sync(0xffffffffu, ox, sa & 31u), ay = __shfl_sync(0xffffffffu, oy, sa & 31u),
+                            az = __shfl_sync(0xffffffffu, oz, sa & 31u);
+                float cx = __shfl_sync(0xffffffffu, ox, sc & 31u), cy = __shfl_sync(0xffffffffu, oy, sc & 31u),
+                      cz = __shfl_sync(0xffffffffu, oz, sc & 31u);
+                if (sc == 32u) {
+                    cx = ex;
+                    cy = ey;
+                    cz = ez;
+                }
+                if (inner) {
+                    const float bx = __fadd_rn(ax, __fmul_rn(0.5f, MinImg(__fsub_rn(cx, ax), pbc, L, iL)));
+                    const float by = __fadd_rn(ay, __fmul_rn(0.5f, MinImg(__fsub_rn(cy, ay), pbc, L, iL)));
+                    const float bz = __fadd_rn(az, __fmul_rn(0.5f, MinImg(__fsub_rn(cz, az), pbc, L, iL)));
+                    const uint32_t m = lane >> (lk + 1);
+                    s_terms[lk][0][m] = dn2;
+                    s_terms[lk][1][m] = Sq3(MinImg(__fsub_rn(ox, bx), pbc, L, iL), MinImg(__fsub_rn(oy, by), pbc, L, iL),
+                                            MinImg(__fsub_rn(oz, bz), pbc, L, iL));
+                }
+            }
+            // Kinetic links k -> k + 2^l and trap slices k of every level (k a multiple of 2^l).
+            for (uint32_t li = 0; li < NL; ++li) {
+                const uint32_t skip = 1u << li;
+                const bool mine = lane < B && (lane & (skip - 1u)) == 0u;
+                const uint32_t sc = mine ? lane + skip : lane;
+                float cx = __shfl_sync(0xffffffffu, nx, sc & 31u), cy = __shfl_sync(0xffffffffu, ny, sc & 31u),
+                      cz = __shfl_sync(0xffffffffu, nz, sc & 31u);
+                float dx = __shfl_sync(0xffffffffu, ox, sc & 31u), dy = __shfl_sync(0xffffffffu, oy, sc & 31u),
+                      dz = __shfl_sync(0xffffffffu, oz, sc & 31u);
+                if (sc == 32u) {
+                    cx = dx = ex;
+                    cy = dy = ey;
+                    cz = dz = ez;
+                }
+                if (mine) {
+                    const uint32_t idx = lane >> li;
+                    s_terms[li][2][idx] = kin_links ? Sq3(MinImg(__fsub_rn(nx, cx), pbc, L, iL), MinImg(__fsub_rn(ny, cy), pbc, L, iL),
+                                                          MinImg(__fsub_rn(nz, cz), pbc, L, iL))
+                                                    : 0.f;
+                    s_terms[li][3][idx] = kin_links ? Sq3(MinImg(__fsub_rn(ox, dx), pbc, L, iL), MinImg(__fsub_rn(oy, dy), pbc, L, iL),
+                                                          MinImg(__fsub_rn(oz, dz), pbc, L, iL))
+                                                    : 0.f;
+                    s_terms[li][4][idx] = Sq3(nx, ny, nz);
+                    s_terms[li][5][idx] = Sq3(ox, oy, oz);
+                }
+            }
+            // Segment copies for the pair work of all warps.
+            if (lane <= B) {
+                s_old[3 * lane] = ox;
+                s_old[3 * lane + 1] = oy;
+                s_old[3 * lane + 2] = oz;
+                s_new[3 * lane] = nx;
+                s_new[3 * lane + 1] = ny;
+                s_new[3 * lane + 2] = nz;
+            }
+            if (B == 32 && lane == 0) {
+                s_old[96] = s_new[96] = ex;
+                s_old[97] = s_new[97] = ey;
+                s_old[98] = s_new[98] = ez;
             }
             __syncwarp();
-            if (lane < 3) SideSums(c, true, lane, NL, B, s_new, s_old, s_z, s_dim);
-            else if (lane < 6) SideSums(c, false, lane - 3, NL, B, s_old, s_old, s_z, s_dim);
+            // One lane per (level, kind) forms the compensated sum of its terms.
+            if (lane < NL * kTermKinds) {
+                const uint32_t li = lane / kTermKinds, q = lane - li * kTermKinds;
+                const uint32_t n = q < 2 ? (B >> (li + 1)) : (B >> li);
+                float v[kMaxB];
+#pragma unroll
+                for (uint32_t j = 0; j < kMaxB; ++j) v[j] = j < n ? s_terms[li][q][j] : 0.f;
+                Comp s{0.f, 0.f};
+#pragma unroll
+                for (uint32_t j = 0; j < kMaxB; ++j)
+                    if (j < n) CompAdd(s, v[j]);
+                s_sum[li][q] = CompDD(s);
+            }
             __syncwarp();
-            // Lane li assembles level li: log_accept = i4s (sum_new dz^2 - sum_old dz^2)
+            // Lane li assembles level li: log_accept = i4s (sum_new - sum_old of |delta|^2)
             //   - [i4l (kin_new - kin_old) + cofa 2^li (trap_new - trap_old)] + dS_{li+1}.
             dd dS = DD(0.f), lsr = DD(0.f);
             if (lane < NL) {
                 const uint32_t li = lane;
-                dd v[2][3];
-#pragma unroll
-                for (int s = 0; s < 2; ++s)
-#pragma unroll
-                    for (int q = 0; q < 3; ++q) v[s][q] = Add(Add(s_dim[li][s][q][0], s_dim[li][s][q][1]), s_dim[li][s][q][2]);
-                lsr = MulF(Sub(v[0][0], v[1][0]), c.i4lt_sample[li]);
-                dS = MulF(Sub(v[0][1], v[1][1]), c.i4lt_level[li]);
+                lsr = MulF(Sub(s_sum[li][0], s_sum[li][1]), c.i4lt_sample[li]);
+                dS = MulF(Sub(s_sum[li][2], s_sum[li][3]), c.i4lt_level[li]);
                 if (c.has_trap && (int)li <= c.trap_max_level)
-                    dS = Add(dS, MulF(Sub(v[0][2], v[1][2]), __fmul_rn(c.trap_cofa, (float)(1u << li))));
+                    dS = Add(dS, MulF(Sub(s_sum[li][4], s_sum[li][5]), __fmul_rn(c.trap_cofa, (float)(1u << li))));
             }
             const dd prev = ShflDownDD(dS, 1);
             dd la = Sub(lsr, dS);
             if (lane + 1 < NL) la = Add(la, prev);
             if (!isfinite(la.hi)) la.hi = -INFINITY;
-            const bool fail = lane >= 1 && lane < NL && Less(la, DD(s_logu[lane]));
+            const bool fail = lane >= 1 && lane < NL && Less(la, DD(s_logu[buf][lane]));
             const unsigned fails = __ballot_sync(0xffffffffu, fail);
             if (lane == 0) {
                 s_upper_ok = fails == 0u;
                 s_base0 = la;
             }
+        } else if (ahead && warp == 1 && it + 1 < n_att) {
+            DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, att + 1}, lane, N, M, B, NL, n_pad, pos, s_z[buf ^ 1u], s_logu[buf ^ 1u],
+                        s_seg[buf ^ 1u], s_pb[buf ^ 1u]);
         }
         GroupSync(G);
         const bool upper_ok = s_upper_ok != 0;
 
         if (upper_ok && n_items) {
-            dd acc_u = DD(0.f);
+            Comp acc_u{0.f, 0.f};
             for (uint32_t base = t; base < n_items; base += kPrefetch * T) {
 #pragma unroll
                 for (uint32_t j = 0; j < kPrefetch; ++j) {
@@ -219,26 +368,22 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArg
                         } else {
                             const uint32_t qq = i - k * nm1;
                             const uint32_t q = qq + (qq >= p ? 1u : 0u);
-                            rq = pos[(size_t)((b0 + 1u + k) % M) * n_pad + q];
+                            rq = pos[(size_t)Wrap(b0 + 1u + k, M) * n_pad + q];
                         }
                         const float* ro = s_old + 3 * (k + 1);
                         const float* rn = s_new + 3 * (k + 1);
-                        const float ox = MinImg(__fsub_rn(ro[0], rq.x), pbc, L, iL);
-                        const float oy = MinImg(__fsub_rn(ro[1], rq.y), pbc, L, iL);
-                        const float oz = MinImg(__fsub_rn(ro[2], rq.z), pbc, L, iL);
-                        const float nx = MinImg(__fsub_rn(rn[0], rq.x), pbc, L, iL);
-                        const float ny = MinImg(__fsub_rn(rn[1], rq.y), pbc, L, iL);
-                        const float nz = MinImg(__fsub_rn(rn[2], rq.z), pbc, L, iL);
-                        float r2o = __fmaf_rn(ox, ox, __fmaf_rn(oy, oy, __fmul_rn(oz, oz)));
-                        float r2n = __fmaf_rn(nx, nx, __fmaf_rn(ny, ny, __fmul_rn(nz, nz)));
+                        float r2o = Sq3(MinImg(__fsub_rn(ro[0], rq.x), pbc, L, iL), MinImg(__fsub_rn(ro[1], rq.y), pbc, L, iL),
+                                        MinImg(__fsub_rn(ro[2], rq.z), pbc, L, iL));
+                        float r2n = Sq3(MinImg(__fsub_rn(rn[0], rq.x), pbc, L, iL), MinImg(__fsub_rn(rn[1], rq.y), pbc, L, iL),
+                                        MinImg(__fsub_rn(rn[2], rq.z), pbc, L, iL));
                         r2o = fminf(fmaxf(r2o, c.r2_min), c.r2_max);
                         r2n = fminf(fmaxf(r2n, c.r2_min), c.r2_max);
-                        acc_u = AddF(acc_u, __fsub_rn(rsqrtf(r2n), rsqrtf(r2o)));
+                        CompAdd(acc_u, __fsub_rn(rsqrtf(r2n), rsqrtf(r2o)));
                     }
                 }
             }
-            acc_u = WarpSumDD(acc_u);
-            if (lane == 0) s_part[warp] = acc_u;
+            const dd u = WarpSumDD(CompDD(acc_u));
+            if (lane == 0) s_part[warp] = u;
         }
         GroupSync(G);
 
@@ -248,16 +393,16 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArg
                 // Level 0: pair action difference tau * sum (1/r_new - 1/r_old) over inner slices
                 // (each inner slice closes two links with weight 1/2; the segment ends cancel).
                 dd u = DD(0.f);
-                if (n_items)
-                    for (uint32_t w = 0; w < G; ++w) u = Add(u, s_part[w]);
+                if (n_items) u = WarpSumDD(lane < G ? s_part[lane] : DD(0.f));
                 dd la0 = Sub(s_base0, MulF(u, c.tau));
                 if (!isfinite(la0.hi)) la0.hi = -INFINITY;
-                accepted = !Less(la0, DD(s_logu[0]));
+                accepted = !Less(la0, DD(s_logu[buf][0]));
             }
-            if (accepted)
-                for (uint32_t k = 1 + lane; k < B; k += 32)
-                    pos[(size_t)((b0 + k) % M) * n_pad + p] = make_float4(s_new[3 * k], s_new[3 * k + 1], s_new[3 * k + 2], 0.f);
+            if (accepted && lane >= 1 && lane < B) pos[(size_t)Wrap(b0 + lane, M) * n_pad + p] = make_float4(nx, ny, nz, 0.f);
             acc += accepted ? 1u : 0u;
+            acc_prev = accepted;
+            p_prev = p;
+            b0_prev = b0;
         }
         GroupSync(G);
     }
