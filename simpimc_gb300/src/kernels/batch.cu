@@ -85,15 +85,35 @@ __device__ __forceinline__ void CompAdd(Comp& a, float x) {
     a.c = __fadd_rn(a.c, e);
 }
 
+/// Merge of two compensated partial sums (TwoSum of the sums, errors added).
+__device__ __forceinline__ Comp CompMerge(Comp a, Comp b) {
+    const dd s = TwoSum(a.s, b.s);
+    return Comp{s.hi, __fadd_rn(__fadd_rn(a.c, b.c), s.lo)};
+}
+
+/// Butterfly reduction over the lanes whose xor distance is below 2^log2_width; every lane of a
+/// group receives the same total (TwoSum and FP32 addition are commutative).
+__device__ __forceinline__ Comp CompWarpSum(Comp v, int width) {
+    for (int o = width >> 1; o > 0; o >>= 1) {
+        const Comp w{__shfl_xor_sync(0xffffffffu, v.s, o), __shfl_xor_sync(0xffffffffu, v.c, o)};
+        v = CompMerge(v, w);
+    }
+    return v;
+}
+
 __device__ __forceinline__ dd CompDD(Comp a) { return TwoSum(a.s, a.c); }
 
 __device__ __forceinline__ float Sq3(float x, float y, float z) { return __fmaf_rn(x, x, __fmaf_rn(y, y, __fmul_rn(z, z))); }
 
 __device__ __forceinline__ uint32_t Wrap(uint32_t s, uint32_t M) { return s >= M ? s - M : s; }  // s < 2M
 
-// Per-level term table of warp 0: q = 0 new sampling |delta|^2, 1 old sampling, 2 new kinetic
-// |dr|^2, 3 old kinetic, 4 new trap r^2, 5 old trap; index = position of the term within its level.
-constexpr int kTermKinds = 6;
+template <bool kPbc>
+__device__ __forceinline__ float Img(float d, float L, float iL) {
+    if constexpr (kPbc) return __fsub_rn(d, __fmul_rn(L, rintf(__fmul_rn(d, iL))));
+    else return d;
+}
+
+constexpr uint32_t kItems = 4;  // pair items per lane kept in registers (more are loaded in the loop)
 
 /// Draws of one attempt (particle, first bead, normals, log-uniforms; philox.h stream layout) and
 /// the moved particle's segment, by one warp into one of two shared buffers.
@@ -121,42 +141,41 @@ __device__ __forceinline__ void DrawAttempt(const MoveStream& st, uint32_t lane,
     }
 }
 
-__global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArgs a, uint64_t n_sweeps, uint64_t n_attempts) {
-    const uint32_t ci = a.order[blockIdx.x];
+struct SweepShared {
+    ChainDev c;
+    float z[2][3 * (kMaxB - 1)];
+    float logu[2][kBatchMaxLevels];
+    float4 seg[2][kMaxB + 1];
+    uint32_t pb[2][2];
+    float old_[3 * (kMaxB + 1)], new_[3 * (kMaxB + 1)];
+    Comp part[kBatchMaxWarps];
+    dd base0;  // level-0 log acceptance without the pair term
+    int upper_ok;
+};
+
+template <bool kPbc>
+__device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_t ci, uint32_t G, uint64_t n_sweeps, uint64_t n_attempts) {
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint32_t G = a.chains[ci].n_warps;
-    if (warp >= G) return;
     const uint32_t T = G * 32u, t = threadIdx.x;
-
-    __shared__ ChainDev s_c;
-    __shared__ float s_z[2][3 * (kMaxB - 1)];
-    __shared__ float s_logu[2][kBatchMaxLevels];
-    __shared__ float4 s_seg[2][kMaxB + 1];
-    __shared__ uint32_t s_pb[2][2];
-    __shared__ float s_old[3 * (kMaxB + 1)], s_new[3 * (kMaxB + 1)];
-    __shared__ float s_terms[kBatchMaxLevels][kTermKinds][kMaxB];
-    __shared__ dd s_sum[kBatchMaxLevels][kTermKinds];
-    __shared__ dd s_part[kBatchMaxWarps];
-    __shared__ dd s_base0;  // level-0 log acceptance without the pair term
-    __shared__ int s_upper_ok;
-
-    {
-        const uint32_t* src = reinterpret_cast<const uint32_t*>(a.chains + ci);
-        uint32_t* dst = reinterpret_cast<uint32_t*>(&s_c);
-        for (uint32_t i = t; i < sizeof(ChainDev) / 4; i += T) dst[i] = src[i];
-    }
-    GroupSync(G);
-    const ChainDev& c = s_c;
+    const ChainDev& c = sh.c;
     const uint32_t N = c.n_part, M = c.n_bead, NL = c.n_level, B = 1u << NL, n_pad = c.n_pad;
-    const int pbc = c.pbc;
     const float L = c.L, iL = c.iL;
     const bool kin_links = B != M;  // whole-ring segment: no kinetic links (kinetic_class.h:111-117)
     float4* __restrict__ pos = a.pos + c.pos_off;
 
-    // Pair items: (inner slice k in 1..B-1) x (other particle); item i -> k = 1 + i / (N-1).
+    // Pair items: (inner slice k in 1..B-1) x (other particle); item i -> k = 1 + i / (N-1). The
+    // decomposition of this lane's first kItems items does not depend on the attempt.
     const uint32_t nm1 = N > 1 ? N - 1 : 1;
     const uint32_t n_items = c.has_pair && N > 1 ? (N - 1) * (B - 1) : 0u;
     const uint32_t magic = (uint32_t)((0x100000000ull + nm1 - 1) / nm1);
+    uint32_t it_k[kItems], it_q[kItems];
+#pragma unroll
+    for (uint32_t j = 0; j < kItems; ++j) {
+        const uint32_t i = t + j * T;
+        it_k[j] = FastDiv(i, magic);
+        it_q[j] = i - it_k[j] * nm1;
+    }
+    const float r2_min = c.r2_min, r2_max = c.r2_max, tau = c.tau;
 
     uint64_t att = a.attempts[ci], acc = a.accepts[ci];
     const uint64_t n_att = n_sweeps ? n_sweeps * c.attempts_per_sweep : n_attempts;
@@ -165,8 +184,8 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArg
     // registers when both attempts move the same particle.
     const bool ahead = G >= 2;
     if (ahead && warp == 1 && n_att > 0)
-        DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, att}, lane, N, M, B, NL, n_pad, pos, s_z[att & 1], s_logu[att & 1], s_seg[att & 1],
-                    s_pb[att & 1]);
+        DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, att}, lane, N, M, B, NL, n_pad, pos, sh.z[att & 1], sh.logu[att & 1], sh.seg[att & 1],
+                    sh.pb[att & 1]);
     GroupSync(G);
 
     float nx = 0.f, ny = 0.f, nz = 0.f;  // warp 0, lane k: new position of bead k of the last attempt
@@ -175,26 +194,20 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArg
     for (uint64_t it = 0; it < n_att; ++it, ++att) {
         const uint32_t buf = (uint32_t)(att & 1);
         if (!ahead) {
-            DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, att}, lane, N, M, B, NL, n_pad, pos, s_z[buf], s_logu[buf], s_seg[buf], s_pb[buf]);
+            DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, att}, lane, N, M, B, NL, n_pad, pos, sh.z[buf], sh.logu[buf], sh.seg[buf], sh.pb[buf]);
             __syncwarp();
         }
-        const uint32_t p = s_pb[buf][0], b0 = s_pb[buf][1];
+        const uint32_t p = sh.pb[buf][0], b0 = sh.pb[buf][1];
 
-        float4 pre[kPrefetch];
+        float4 pre[kItems];
 #pragma unroll
-        for (uint32_t j = 0; j < kPrefetch; ++j) {
-            const uint32_t i = t + j * T;
-            if (i < n_items) {
-                const uint32_t k = FastDiv(i, magic), qq = i - k * nm1;
-                const uint32_t q = qq + (qq >= p ? 1u : 0u);
-                pre[j] = pos[(size_t)Wrap(b0 + 1u + k, M) * n_pad + q];
-            }
-        }
+        for (uint32_t j = 0; j < kItems; ++j)
+            if (t + j * T < n_items) pre[j] = pos[(size_t)Wrap(b0 + 1u + it_k[j], M) * n_pad + it_q[j] + (it_q[j] >= p ? 1u : 0u)];
 
         if (warp == 0) {
             // Old segment: lane k holds bead k; every lane holds the last bead B.
-            const float4 sv = s_seg[buf][lane <= B ? lane : B];
-            const float4 se = s_seg[buf][B];
+            const float4 sv = sh.seg[buf][lane <= B ? lane : B];
+            const float4 se = sh.seg[buf][B];
             float ox = sv.x, oy = sv.y, oz = sv.z, ex = se.x, ey = se.y, ez = se.z;
             if (ahead && acc_prev && p == p_prev) {
                 // Beads of this segment inside the last accepted segment: take the committed values.
@@ -218,7 +231,8 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArg
             }
             // Sampling, level by level (bisect_class.h:77-107): bead k = 2^l (2m + 1) is resampled
             // on level l from beads k -+ 2^l; positions travel by shuffles.
-            const float* zb = s_z[buf];
+            const float* zb = sh.z[buf];
+            const bool inner = lane >= 1 && lane < B;
             const uint32_t lk = lane == 0 ? 31u : (uint32_t)(__ffs(lane) - 1);  // level of bead `lane`
             nx = ox;
             ny = oy;
@@ -226,7 +240,7 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArg
             float dn2 = 0.f;
             for (int li = (int)NL - 1; li >= 0; --li) {
                 const uint32_t skip = 1u << li;
-                const bool mine = lane < B && lk == (uint32_t)li;
+                const bool mine = inner && lk == (uint32_t)li;
                 const uint32_t sa = mine ? lane - skip : lane, sc = mine ? lane + skip : lane;
                 const float ax = __shfl_sync(0xffffffffu, nx, sa & 31u), ay = __shfl_sync(0xffffffffu, ny, sa & 31u),
                             az = __shfl_sync(0xffffffffu, nz, sa & 31u);
@@ -240,17 +254,17 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArg
                 if (mine) {
                     const uint32_t zi = 3 * ((B >> (li + 1)) - 1u + (lane >> (li + 1)));
                     const float sg = c.sigma[li];
-                    const float dx = MinImg(__fmul_rn(sg, zb[zi]), pbc, L, iL), dy = MinImg(__fmul_rn(sg, zb[zi + 1]), pbc, L, iL),
-                                dz = MinImg(__fmul_rn(sg, zb[zi + 2]), pbc, L, iL);
-                    nx = __fadd_rn(__fadd_rn(ax, __fmul_rn(0.5f, MinImg(__fsub_rn(cx, ax), pbc, L, iL))), dx);
-                    ny = __fadd_rn(__fadd_rn(ay, __fmul_rn(0.5f, MinImg(__fsub_rn(cy, ay), pbc, L, iL))), dy);
-                    nz = __fadd_rn(__fadd_rn(az, __fmul_rn(0.5f, MinImg(__fsub_rn(cz, az), pbc, L, iL))), dz);
+                    const float dx = Img<kPbc>(__fmul_rn(sg, zb[zi]), L, iL), dy = Img<kPbc>(__fmul_rn(sg, zb[zi + 1]), L, iL),
+                                dz = Img<kPbc>(__fmul_rn(sg, zb[zi + 2]), L, iL);
+                    nx = __fadd_rn(__fadd_rn(ax, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cx, ax), L, iL))), dx);
+                    ny = __fadd_rn(__fadd_rn(ay, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cy, ay), L, iL))), dy);
+                    nz = __fadd_rn(__fadd_rn(az, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cz, az), L, iL))), dz);
                     dn2 = Sq3(dx, dy, dz);
                 }
             }
-            // Old sampling displacements of every level at once.
+            // Old sampling displacement of bead `lane` on its level.
+            float samp = 0.f;
             {
-                const bool inner = lane >= 1 && lane < B;
                 const uint32_t skip = inner ? (1u << lk) : 0u;
                 const uint32_t sa = inner ? lane - skip : lane, sc = inner ? lane + skip : lane;
                 const float ax = __shfl_sync(0xffffffffu, ox, sa & 31u), ay = __shfl_sync(0xffffffffu, oy, sa & 31u),
@@ -263,127 +277,111 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArg
                     cz = ez;
                 }
                 if (inner) {
-                    const float bx = __fadd_rn(ax, __fmul_rn(0.5f, MinImg(__fsub_rn(cx, ax), pbc, L, iL)));
-                    const float by = __fadd_rn(ay, __fmul_rn(0.5f, MinImg(__fsub_rn(cy, ay), pbc, L, iL)));
-                    const float bz = __fadd_rn(az, __fmul_rn(0.5f, MinImg(__fsub_rn(cz, az), pbc, L, iL)));
-                    const uint32_t m = lane >> (lk + 1);
-                    s_terms[lk][0][m] = dn2;
-                    s_terms[lk][1][m] = Sq3(MinImg(__fsub_rn(ox, bx), pbc, L, iL), MinImg(__fsub_rn(oy, by), pbc, L, iL),
-                                            MinImg(__fsub_rn(oz, bz), pbc, L, iL));
+                    const float bx = __fadd_rn(ax, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cx, ax), L, iL)));
+                    const float by = __fadd_rn(ay, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cy, ay), L, iL)));
+                    const float bz = __fadd_rn(az, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cz, az), L, iL)));
+                    const float do2 = Sq3(Img<kPbc>(__fsub_rn(ox, bx), L, iL), Img<kPbc>(__fsub_rn(oy, by), L, iL), Img<kPbc>(__fsub_rn(oz, bz), L, iL));
+                    samp = __fmul_rn(c.i4lt_sample[lk], __fsub_rn(dn2, do2));  // log sample ratio term
                 }
             }
-            // Kinetic links k -> k + 2^l and trap slices k of every level (k a multiple of 2^l).
-            for (uint32_t li = 0; li < NL; ++li) {
-                const uint32_t skip = 1u << li;
-                const bool mine = lane < B && (lane & (skip - 1u)) == 0u;
-                const uint32_t sc = mine ? lane + skip : lane;
-                float cx = __shfl_sync(0xffffffffu, nx, sc & 31u), cy = __shfl_sync(0xffffffffu, ny, sc & 31u),
-                      cz = __shfl_sync(0xffffffffu, nz, sc & 31u);
-                float dx = __shfl_sync(0xffffffffu, ox, sc & 31u), dy = __shfl_sync(0xffffffffu, oy, sc & 31u),
-                      dz = __shfl_sync(0xffffffffu, oz, sc & 31u);
-                if (sc == 32u) {
-                    cx = dx = ex;
-                    cy = dy = ey;
-                    cz = dz = ez;
+            // Per level l and lane k (a multiple of 2^l): the action change of link k -> k + 2^l
+            // (kinetic) and slice k (trap); the level's totals come from one compensated butterfly
+            // each for  D_l = sum of action changes  and  R_l = sampling ratio - D_l.
+            Comp Dl[kBatchMaxLevels], Rl[kBatchMaxLevels];
+#pragma unroll
+            for (uint32_t li = 0; li < kBatchMaxLevels; ++li) {
+                float dterm = 0.f;
+                if (li < NL) {
+                    const uint32_t skip = 1u << li;
+                    const bool mine = lane < B && (lane & (skip - 1u)) == 0u;
+                    const uint32_t sc = mine ? lane + skip : lane;
+                    float cx = __shfl_sync(0xffffffffu, nx, sc & 31u), cy = __shfl_sync(0xffffffffu, ny, sc & 31u),
+                          cz = __shfl_sync(0xffffffffu, nz, sc & 31u);
+                    float dx = __shfl_sync(0xffffffffu, ox, sc & 31u), dy = __shfl_sync(0xffffffffu, oy, sc & 31u),
+                          dz = __shfl_sync(0xffffffffu, oz, sc & 31u);
+                    if (sc == 32u) {
+                        cx = dx = ex;
+                        cy = dy = ey;
+                        cz = dz = ez;
+                    }
+                    if (mine) {
+                        if (kin_links) {
+                            const float kn = Sq3(Img<kPbc>(__fsub_rn(nx, cx), L, iL), Img<kPbc>(__fsub_rn(ny, cy), L, iL), Img<kPbc>(__fsub_rn(nz, cz), L, iL));
+                            const float ko = Sq3(Img<kPbc>(__fsub_rn(ox, dx), L, iL), Img<kPbc>(__fsub_rn(oy, dy), L, iL), Img<kPbc>(__fsub_rn(oz, dz), L, iL));
+                            dterm = __fmul_rn(c.i4lt_level[li], __fsub_rn(kn, ko));
+                        }
+                        if (c.has_trap && (int)li <= c.trap_max_level)
+                            dterm = __fadd_rn(dterm, __fmul_rn(__fmul_rn(c.trap_cofa, (float)skip), __fsub_rn(Sq3(nx, ny, nz), Sq3(ox, oy, oz))));
+                    }
                 }
-                if (mine) {
-                    const uint32_t idx = lane >> li;
-                    s_terms[li][2][idx] = kin_links ? Sq3(MinImg(__fsub_rn(nx, cx), pbc, L, iL), MinImg(__fsub_rn(ny, cy), pbc, L, iL),
-                                                          MinImg(__fsub_rn(nz, cz), pbc, L, iL))
-                                                    : 0.f;
-                    s_terms[li][3][idx] = kin_links ? Sq3(MinImg(__fsub_rn(ox, dx), pbc, L, iL), MinImg(__fsub_rn(oy, dy), pbc, L, iL),
-                                                          MinImg(__fsub_rn(oz, dz), pbc, L, iL))
-                                                    : 0.f;
-                    s_terms[li][4][idx] = Sq3(nx, ny, nz);
-                    s_terms[li][5][idx] = Sq3(ox, oy, oz);
-                }
+                Dl[li] = Comp{dterm, 0.f};
+                Rl[li] = Comp{__fsub_rn(inner && lk == li ? samp : 0.f, dterm), 0.f};
             }
+#pragma unroll
+            for (uint32_t li = 0; li < kBatchMaxLevels; ++li)
+                if (li < NL) {
+                    Dl[li] = CompWarpSum(Dl[li], 32);
+                    Rl[li] = CompWarpSum(Rl[li], 32);
+                }
             // Segment copies for the pair work of all warps.
             if (lane <= B) {
-                s_old[3 * lane] = ox;
-                s_old[3 * lane + 1] = oy;
-                s_old[3 * lane + 2] = oz;
-                s_new[3 * lane] = nx;
-                s_new[3 * lane + 1] = ny;
-                s_new[3 * lane + 2] = nz;
+                sh.old_[3 * lane] = ox;
+                sh.old_[3 * lane + 1] = oy;
+                sh.old_[3 * lane + 2] = oz;
+                sh.new_[3 * lane] = nx;
+                sh.new_[3 * lane + 1] = ny;
+                sh.new_[3 * lane + 2] = nz;
             }
             if (B == 32 && lane == 0) {
-                s_old[96] = s_new[96] = ex;
-                s_old[97] = s_new[97] = ey;
-                s_old[98] = s_new[98] = ez;
+                sh.old_[96] = sh.new_[96] = ex;
+                sh.old_[97] = sh.new_[97] = ey;
+                sh.old_[98] = sh.new_[98] = ez;
             }
-            __syncwarp();
-            // One lane per (level, kind) forms the compensated sum of its terms.
-            if (lane < NL * kTermKinds) {
-                const uint32_t li = lane / kTermKinds, q = lane - li * kTermKinds;
-                const uint32_t n = q < 2 ? (B >> (li + 1)) : (B >> li);
-                float v[kMaxB];
+            // Level l passes if  R_l + D_{l+1} >= log u_l  (bisect_class.h:110-121); every lane
+            // holds every level's totals, so lane l tests level l.
+            bool fail = false;
+            dd base0 = DD(0.f);
 #pragma unroll
-                for (uint32_t j = 0; j < kMaxB; ++j) v[j] = j < n ? s_terms[li][q][j] : 0.f;
-                Comp s{0.f, 0.f};
-#pragma unroll
-                for (uint32_t j = 0; j < kMaxB; ++j)
-                    if (j < n) CompAdd(s, v[j]);
-                s_sum[li][q] = CompDD(s);
-            }
-            __syncwarp();
-            // Lane li assembles level li: log_accept = i4s (sum_new - sum_old of |delta|^2)
-            //   - [i4l (kin_new - kin_old) + cofa 2^li (trap_new - trap_old)] + dS_{li+1}.
-            dd dS = DD(0.f), lsr = DD(0.f);
-            if (lane < NL) {
-                const uint32_t li = lane;
-                lsr = MulF(Sub(s_sum[li][0], s_sum[li][1]), c.i4lt_sample[li]);
-                dS = MulF(Sub(s_sum[li][2], s_sum[li][3]), c.i4lt_level[li]);
-                if (c.has_trap && (int)li <= c.trap_max_level)
-                    dS = Add(dS, MulF(Sub(s_sum[li][4], s_sum[li][5]), __fmul_rn(c.trap_cofa, (float)(1u << li))));
-            }
-            const dd prev = ShflDownDD(dS, 1);
-            dd la = Sub(lsr, dS);
-            if (lane + 1 < NL) la = Add(la, prev);
-            if (!isfinite(la.hi)) la.hi = -INFINITY;
-            const bool fail = lane >= 1 && lane < NL && Less(la, DD(s_logu[buf][lane]));
+            for (uint32_t li = 0; li < kBatchMaxLevels; ++li)
+                if (li < NL) {
+                    dd la = CompDD(Rl[li]);
+                    if (li + 1 < NL) la = Add(la, CompDD(Dl[li + 1]));
+                    if (!isfinite(la.hi)) la.hi = -INFINITY;
+                    if (li == 0) base0 = la;
+                    else if (lane == li) fail = Less(la, DD(sh.logu[buf][li]));
+                }
             const unsigned fails = __ballot_sync(0xffffffffu, fail);
             if (lane == 0) {
-                s_upper_ok = fails == 0u;
-                s_base0 = la;
+                sh.upper_ok = fails == 0u;
+                sh.base0 = base0;
             }
         } else if (ahead && warp == 1 && it + 1 < n_att) {
-            DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, att + 1}, lane, N, M, B, NL, n_pad, pos, s_z[buf ^ 1u], s_logu[buf ^ 1u],
-                        s_seg[buf ^ 1u], s_pb[buf ^ 1u]);
+            DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, att + 1}, lane, N, M, B, NL, n_pad, pos, sh.z[buf ^ 1u], sh.logu[buf ^ 1u],
+                        sh.seg[buf ^ 1u], sh.pb[buf ^ 1u]);
         }
         GroupSync(G);
-        const bool upper_ok = s_upper_ok != 0;
+        const bool upper_ok = sh.upper_ok != 0;
 
         if (upper_ok && n_items) {
             Comp acc_u{0.f, 0.f};
-            for (uint32_t base = t; base < n_items; base += kPrefetch * T) {
+            auto item = [&](uint32_t k, float4 rq) {
+                const float* ro = sh.old_ + 3 * (k + 1);
+                const float* rn = sh.new_ + 3 * (k + 1);
+                float r2o = Sq3(Img<kPbc>(__fsub_rn(ro[0], rq.x), L, iL), Img<kPbc>(__fsub_rn(ro[1], rq.y), L, iL), Img<kPbc>(__fsub_rn(ro[2], rq.z), L, iL));
+                float r2n = Sq3(Img<kPbc>(__fsub_rn(rn[0], rq.x), L, iL), Img<kPbc>(__fsub_rn(rn[1], rq.y), L, iL), Img<kPbc>(__fsub_rn(rn[2], rq.z), L, iL));
+                r2o = fminf(fmaxf(r2o, r2_min), r2_max);
+                r2n = fminf(fmaxf(r2n, r2_min), r2_max);
+                CompAdd(acc_u, __fsub_rn(rsqrtf(r2n), rsqrtf(r2o)));
+            };
 #pragma unroll
-                for (uint32_t j = 0; j < kPrefetch; ++j) {
-                    const uint32_t i = base + j * T;
-                    if (i < n_items) {
-                        const uint32_t k = FastDiv(i, magic);
-                        float4 rq;
-                        if (base == t) {
-                            rq = pre[j];
-                        } else {
-                            const uint32_t qq = i - k * nm1;
-                            const uint32_t q = qq + (qq >= p ? 1u : 0u);
-                            rq = pos[(size_t)Wrap(b0 + 1u + k, M) * n_pad + q];
-                        }
-                        const float* ro = s_old + 3 * (k + 1);
-                        const float* rn = s_new + 3 * (k + 1);
-                        float r2o = Sq3(MinImg(__fsub_rn(ro[0], rq.x), pbc, L, iL), MinImg(__fsub_rn(ro[1], rq.y), pbc, L, iL),
-                                        MinImg(__fsub_rn(ro[2], rq.z), pbc, L, iL));
-                        float r2n = Sq3(MinImg(__fsub_rn(rn[0], rq.x), pbc, L, iL), MinImg(__fsub_rn(rn[1], rq.y), pbc, L, iL),
-                                        MinImg(__fsub_rn(rn[2], rq.z), pbc, L, iL));
-                        r2o = fminf(fmaxf(r2o, c.r2_min), c.r2_max);
-                        r2n = fminf(fmaxf(r2n, c.r2_min), c.r2_max);
-                        CompAdd(acc_u, __fsub_rn(rsqrtf(r2n), rsqrtf(r2o)));
-                    }
-                }
+            for (uint32_t j = 0; j < kItems; ++j)
+                if (t + j * T < n_items) item(it_k[j], pre[j]);
+            for (uint32_t i = t + kItems * T; i < n_items; i += T) {
+                const uint32_t k = FastDiv(i, magic), qq = i - k * nm1;
+                item(k, pos[(size_t)Wrap(b0 + 1u + k, M) * n_pad + qq + (qq >= p ? 1u : 0u)]);
             }
-            const dd u = WarpSumDD(CompDD(acc_u));
-            if (lane == 0) s_part[warp] = u;
+            const Comp u = CompWarpSum(acc_u, 32);
+            if (lane == 0) sh.part[warp] = u;
         }
         GroupSync(G);
 
@@ -393,10 +391,10 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArg
                 // Level 0: pair action difference tau * sum (1/r_new - 1/r_old) over inner slices
                 // (each inner slice closes two links with weight 1/2; the segment ends cancel).
                 dd u = DD(0.f);
-                if (n_items) u = WarpSumDD(lane < G ? s_part[lane] : DD(0.f));
-                dd la0 = Sub(s_base0, MulF(u, c.tau));
+                if (n_items) u = CompDD(CompWarpSum(lane < G ? sh.part[lane] : Comp{0.f, 0.f}, 32));  // same total on every lane
+                dd la0 = Sub(sh.base0, MulF(u, tau));
                 if (!isfinite(la0.hi)) la0.hi = -INFINITY;
-                accepted = !Less(la0, DD(s_logu[buf][0]));
+                accepted = !Less(la0, DD(sh.logu[buf][0]));
             }
             if (accepted && lane >= 1 && lane < B) pos[(size_t)Wrap(b0 + lane, M) * n_pad + p] = make_float4(nx, ny, nz, 0.f);
             acc += accepted ? 1u : 0u;
@@ -410,6 +408,22 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArg
         a.attempts[ci] = att;
         a.accepts[ci] = acc;
     }
+}
+
+__global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArgs a, uint64_t n_sweeps, uint64_t n_attempts) {
+    const uint32_t ci = a.order[blockIdx.x];
+    const uint32_t warp = threadIdx.x >> 5;
+    const uint32_t G = a.chains[ci].n_warps;
+    if (warp >= G) return;
+    __shared__ SweepShared sh;
+    {
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(a.chains + ci);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(&sh.c);
+        for (uint32_t i = threadIdx.x; i < sizeof(ChainDev) / 4; i += G * 32u) dst[i] = src[i];
+    }
+    GroupSync(G);
+    if (sh.c.pbc) SweepChain<true>(sh, a, ci, G, n_sweeps, n_attempts);
+    else SweepChain<false>(sh, a, ci, G, n_sweeps, n_attempts);
 }
 
 /// Thermal energy estimator of one chain (Energy::Accumulate with use_thermal, energy_class.h:
