@@ -1,21 +1,30 @@
 #!/usr/bin/env python3
-"""Benchmark: bead-moves/s of the bisection sweep on the 66-electron gas (one GB300).
+"""Benchmark: bead-moves/s of path-integral Monte Carlo bisection sweeps on one GB300.
 
-Workload (one "step" = one sweep): N = 66 Boltzmannon electrons (33 up, 33 down) in a periodic
-cube at r_s = 2 (L = 13.0289), beta = 8, M = 128 slices, Coulomb as primitive short-range part
-plus an Ewald k-sum with |k| < 12 (2 pi / L) (3561 stored half-space k-vectors), bisection
-level 4 (2^4 - 1 = 15 resampled beads per attempt), FP64. A sweep is N_s * M / 2^4 attempts of
-each species' move, alternating up/down as the reference's Loop of Move events does:
-528 attempts = 7920 bead-moves. Synthetic data: beads uniform in the box from a fixed seed,
-then untimed warm-up sweeps.
+Headline workload (one "step" = one measurement cycle, replayed as a CUDA graph: one sweep of
+every chain, then one thermal-energy measurement of every chain): 256 independent chains of
+distinguishable unit-mass particles in an isotropic 3-D harmonic trap (omega = 1) with bare
+Coulomb repulsion (primitive action), open boundaries, beta = 2; chain c has seed 1000 + c,
+N drawn uniformly from {16..128} and M from {32, 64, 128} by a generator seeded with 1000;
+bisection level 3 (7 resampled beads per attempt); a sweep of a chain is N ceil(M / 8) attempts.
+FP32 positions and action terms, compensated sums, double-float acceptance, FP64 estimators.
+Synthetic data: beads i.i.d. N(0, 1) from each chain's seed, then untimed warm-up cycles.
+
+Also reported on the same line:
+  plain_same_system  the single-chain FP64 sweep kernel run on a sample of the same chains, one
+                     chain at a time (what the batched kernel replaces);
+  energy_gate        per-chain energies and blocking error bars of the batched FP32 chains
+                     against the single-chain FP64 path on the same chains and seeds;
+  plain_electron_gas the single-chain FP64 kernel on the 66-electron gas (r_s = 2, beta = 8,
+                     M = 128, Ewald |k| < 12 (2 pi / L), 3561 half-space k-vectors, level 4).
 
 Arms:
-  (default)          the CUDA library: `value` = device-timed sweeps with the path resident in
-                     HBM; `e2e` = the same sweeps through the C interface with the path uploaded
-                     from and downloaded to host memory every step.
+  (default)          the CUDA library. `value` = device-timed cycles with the paths resident in
+                     HBM; `e2e` = the same cycles through the C interface with every chain's path
+                     uploaded from and downloaded to host memory and the energies read back.
   --impl reference   the CPU restatement of the reference hot path (the reference itself does not
-                     build here: its scaffold/einspline/Armadillo/HDF5 dependencies are absent),
-                     one independent chain per host thread, on a bounded sample per step.
+                     build here: its scaffold/einspline/Armadillo/HDF5 dependencies are absent) on
+                     the same chains, one chain per host thread, on a bounded sample per step.
 """
 from __future__ import annotations
 
@@ -36,27 +45,17 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-N_PART, RS, BETA, N_BEAD, K_UNITS, N_LEVEL = 66, 2.0, 8.0, 128, 12.0, 4
 METRIC = "bead-moves/s"
-WORKLOAD = "electron gas N=66 (33+33) r_s=2 beta=8 M=128 Ewald |k|<12(2pi/L) bisection level 4, FP64, single chain"
+N_CHAINS, SEED0, CHAIN_LEVEL = 256, 1000, 3
+WORKLOAD = ("256 independent harmonic-trap Coulomb chains (omega=1, beta=2, open), N~U{16..128}, M in {32,64,128}, "
+            "bisection level 3, seeds 1000+c; one step = one sweep of every chain + one energy measurement (CUDA graph); "
+            "FP32 action terms, compensated sums, double-float acceptance")
+EGAS = dict(n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_units=12.0, n_level=4)
 
 
-def workload(tmp):
-    from simpimc_gb300.configs import electron_gas
-    xml, path = electron_gas(tmp, n_part=N_PART, rs=RS, beta=BETA, n_bead=N_BEAD, k_cut_units=K_UNITS, n_level=N_LEVEL,
-                             seed=20261203)
-    n_up = N_PART // 2
-    reps = n_up * math.ceil(N_BEAD / (1 << N_LEVEL))  # per-species attempts per sweep
-    return xml, path, reps
-
-
-def base_config(extra=None):
-    cfg = {"workload": WORKLOAD, "n_part": N_PART, "r_s": RS, "beta": BETA, "n_bead": N_BEAD, "k_cut": "12*2pi/L",
-           "n_k_half_space": None, "bisection_level": N_LEVEL, "attempts_per_step": 2 * N_PART // 2 * math.ceil(N_BEAD / 16),
-           "bead_moves_per_attempt": (1 << N_LEVEL) - 1, "parallelism": "replicas (independent chains per GPU)"}
-    if extra:
-        cfg.update(extra)
-    return cfg
+def chains_workload(tmp):
+    from simpimc_gb300.configs import batched_trap_chains
+    return batched_trap_chains(tmp, n_chains=N_CHAINS, seed0=SEED0, n_level=CHAIN_LEVEL)
 
 
 def clocks_sampler(out_path):
@@ -93,7 +92,7 @@ def clocks_summary(path, device):
     return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def measured_peaks():
+def measured_hbm_peak():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
@@ -101,23 +100,16 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def algorithmic_bytes(sim, counters_before, counters_after, n_k):
-    """Bytes one sweep touches once each (8-byte doubles): the moved particle's segment
-    (read, and written twice on accept), the partners' positions on the segment, and the
-    per-slice charge densities of the segment: read for the moved species and the other species
-    of the cross action, written for the moved species on accept."""
-    B = 1 << N_LEVEL
-    D = 3
-    total = 0
-    for m in range(sim.n_moves):
-        a0, _, _, acc0, l00 = counters_before[m]
-        a1, _, _, acc1, l01 = counters_after[m]
-        att, acc, lv0 = a1 - a0, acc1 - acc0, l01 - l00
-        seg = (B + 1) * D * 8
-        total += att * seg
-        total += lv0 * ((N_PART - 1) * (B + 1) * D * 8 + B * n_k * 16 * 2)
-        total += acc * ((B - 1) * n_k * 16 + 2 * (B - 1) * D * 8)
-    return total
+def blocking_error(x):
+    """Standard error of the mean of a correlated series by Flyvbjerg-Petersen blocking: the
+    largest naive error over the halving levels that keep at least 16 blocks."""
+    x = np.asarray(x, dtype=np.float64)
+    best = 0.0
+    while x.size >= 16:
+        best = max(best, float(np.std(x, ddof=1) / math.sqrt(x.size)))
+        n = x.size // 2
+        x = 0.5 * (x[0:2 * n:2] + x[1:2 * n:2])
+    return best
 
 
 def reduce_max_over_ranks(values, dist=None, device=None):
@@ -131,9 +123,153 @@ def reduce_max_over_ranks(values, dist=None, device=None):
     return [float(x) for x in t]
 
 
-def run_ours(args):
+def batch_algorithmic_bytes(batch, att, acc):
+    """Bytes one sweep launch touches once each (float4 = 16 B per bead): the moved particle's
+    2^l + 1 beads and every other particle's beads on the 2^l - 1 inner slices (loaded for every
+    attempt), plus the 2^l - 1 beads written back on acceptance."""
+    total = 0
+    for c, (n, m, lvl) in enumerate(batch.shapes):
+        B = 1 << lvl
+        total += int(att[c]) * ((B + 1) + (n - 1) * (B - 1)) * 16 + int(acc[c]) * (B - 1) * 16
+    return total
+
+
+def time_plain_chains(items, tmp, local, sample, sweeps=2):
+    """The single-chain FP64 sweep kernel on `sample` chains, one after the other (device time)."""
     import torch
     from simpimc_gb300 import Simulation
+    moves, secs = 0, 0.0
+    for c in sample:
+        xml, path = items[c]
+        s = Simulation(xml, base_dir=tmp, device=local, chain=c)
+        s.set_path(path)
+        reps = s.species_info(0)[0] * math.ceil(s.n_bead / (1 << CHAIN_LEVEL))
+        st = torch.cuda.ExternalStream(s._lib.pimc_stream(s._h), device=torch.device("cuda", local))
+        s.sweep([0], [1], reps)  # warm-up
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        s.sweep([0], [1], reps * sweeps)
+        e1.record(st)
+        e1.synchronize()
+        secs += e0.elapsed_time(e1) / 1e3
+        moves += reps * sweeps * ((1 << CHAIN_LEVEL) - 1)
+        s.close()
+    return moves, secs
+
+
+def energy_gate(items, tmp, local, chains, sweeps):
+    """Batched FP32 chains against the single-chain FP64 path on the same chains and seeds: per
+    chain the mean energy and its blocking error bar over `sweeps` measurements."""
+    from simpimc_gb300 import ChainBatch, Simulation
+    sub = [items[c] for c in chains]
+    b = ChainBatch([x for x, _ in sub], base_dir=tmp, device=local)
+    # The batch numbers its chains 0..k-1; the FP64 contexts use the same chain indices.
+    for i, (_, p) in enumerate(sub):
+        b.set_path(i, p)
+    b.run(sweeps, 1)
+    rows = []
+    for i, (xml, p) in enumerate(sub):
+        e32, n = b.energy(i, cap=sweeps)
+        s = Simulation(xml, base_dir=tmp, device=local, chain=i)
+        s.set_path(p)
+        reps = s.species_info(0)[0] * math.ceil(s.n_bead / (1 << CHAIN_LEVEL))
+        e64 = []
+        for _ in range(sweeps):
+            s.sweep([0], [1], reps)
+            s.observable_accumulate(0)
+            e64.append(s.observable_block(0)[0])
+        s.close()
+        a32, a64 = e32[:, 0], np.asarray(e64)
+        err32, err64 = blocking_error(a32), blocking_error(a64)
+        rows.append({"chain": chains[i], "shape": list(b.shapes[i][:2]), "E_fp32": float(a32.mean()), "err_fp32": err32,
+                     "E_fp64": float(a64.mean()), "err_fp64": err64,
+                     "err_ratio": err32 / err64 if err64 > 0 else None,
+                     "max_abs_diff_per_measurement": float(np.max(np.abs(a32 - a64)))})
+    b.close()
+    ratios = [r["err_ratio"] for r in rows if r["err_ratio"]]
+    return {"sweeps": sweeps, "chains": rows,
+            "max_err_ratio_deviation": max(abs(r - 1.0) for r in ratios) if ratios else None,
+            "note": "chain i of the batch and the FP64 context with chain=i draw the same random stream"}
+
+
+def egas_plain(local, steps, warmup, tmp, flush):
+    """The single-chain FP64 sweep kernel on the 66-electron gas: device time, e2e, bytes."""
+    import torch
+    from simpimc_gb300 import Simulation
+    from simpimc_gb300.configs import electron_gas
+    xml, path = electron_gas(tmp, seed=20261203, **EGAS)
+    sim = Simulation(xml, base_dir=tmp, device=local, chain=0)
+    sim.set_path(path)
+    st = torch.cuda.ExternalStream(sim._lib.pimc_stream(sim._h), device=torch.device("cuda", local))
+    B = 1 << EGAS["n_level"]
+    reps = EGAS["n_part"] // 2 * math.ceil(EGAS["n_bead"] / B)
+    for _ in range(warmup):
+        sim.sweep([0, 1], [1, 1], reps)
+    c0 = [sim.move_counters(m) for m in range(sim.n_moves)]
+    ms = 0.0
+    for _ in range(steps):
+        with torch.cuda.stream(st):
+            flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        sim.sweep([0, 1], [1, 1], reps)
+        e1.record(st)
+        e1.synchronize()
+        ms += e0.elapsed_time(e1)
+    c1 = [sim.move_counters(m) for m in range(sim.n_moves)]
+    host = sim.get_path(1)
+    e2e_ms = 0.0
+    for _ in range(steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.set_path(host)
+        sim.sweep([0, 1], [1, 1], reps)
+        host = sim.get_path(1)
+        e2e_ms += (time.perf_counter() - t0) * 1e3
+    moves = 2 * reps * (B - 1) * steps
+    n_k = sim.n_k
+    att = sum(c1[m][0] - c0[m][0] for m in range(2))
+    acc = sum(c1[m][3] - c0[m][3] for m in range(2))
+    lv0 = sum(c1[m][4] - c0[m][4] for m in range(2))
+    n = EGAS["n_part"]
+    alg = (att * (B + 1) * 24 + lv0 * ((n - 1) * (B + 1) * 24 + B * n_k * 32) + acc * ((B - 1) * n_k * 16 + 2 * (B - 1) * 24)) / steps
+    peak, kind = measured_hbm_peak()
+    achieved = alg / (ms / steps / 1e3) / 1e9
+    out = {"workload": "electron gas N=66 (33+33) r_s=2 beta=8 M=128 Ewald |k|<12(2pi/L) bisection level 4, FP64-grade, single chain",
+           "value": moves / (ms / 1e3), "unit": METRIC, "ms_per_sweep": ms / steps, "n_k_half_space": n_k,
+           "acceptance": acc / max(att, 1),
+           "e2e": {"value": moves / (e2e_ms / 1e3), "unit": METRIC, "h2d_bytes_per_step": n * EGAS["n_bead"] * 24,
+                   "d2h_bytes_per_step": n * EGAS["n_bead"] * 24},
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                        "peak_kind": kind, "kernel": "BisectSweepKernel", "algorithmic_bytes_per_launch": alg}}
+    return out, xml, host, reps
+
+
+def cpu_oracle_chains(items, tmp, seconds, chains):
+    """The oracle on one host core, cycling through `chains` in chunks of attempts."""
+    import oracle
+    oracle.build()
+    sims = []
+    for c in chains:
+        xml, p = items[c]
+        o = oracle.OracleSim(xml, base_dir=tmp, chain=c)
+        o.set_path(p)
+        sims.append(o)
+    moves, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        for o in sims:
+            o.move_attempts(0, 64)
+            moves += 64 * ((1 << CHAIN_LEVEL) - 1)
+    el = time.perf_counter() - t0
+    for o in sims:
+        o.close()
+    return moves, el
+
+
+def run_ours(args):
+    import torch
+    from simpimc_gb300 import ChainBatch
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -144,18 +280,19 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     tmp = tempfile.mkdtemp(prefix="pimc_bench_")
-    xml, path, reps = workload(tmp)
-    sim = Simulation(xml, base_dir=tmp, device=local, chain=rank)
-    sim.set_path(path)
-    stream = torch.cuda.ExternalStream(sim._lib.pimc_stream(sim._h), device=torch.device("cuda", local))
-    moves, counts = [0, 1], [1, 1]
-    B = 1 << N_LEVEL
-    bead_moves_per_step = 2 * reps * (B - 1)
-
-    for _ in range(args.warmup):
-        sim.sweep(moves, counts, reps)
+    items = chains_workload(tmp)
+    flat0 = np.concatenate([p.ravel() for _, p in items])
+    batch = ChainBatch([x for x, _ in items], base_dir=tmp, device=local)
+    batch.set_paths(flat0)
+    stream = torch.cuda.ExternalStream(batch.stream(), device=torch.device("cuda", local))
+    per_sweep = batch.stats()["bead_moves_per_sweep"]
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
-    counters0 = [sim.move_counters(m) for m in range(sim.n_moves)]
+
+    ipl, mw, tune_s = batch.autotune(2)
+    batch.run(args.warmup, 1)
+    batch.synchronize()
+    att0, acc0 = batch.counters()
+    launches0 = batch.stats()["kernel_launches"]
     clk_file = Path(tmp) / "clocks.csv"
     sampler = clocks_sampler(clk_file) if rank == 0 else None
     if dist:
@@ -166,70 +303,97 @@ def run_ours(args):
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()  # L2 flush between timed steps (untimed)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-        sim.sweep(moves, counts, reps)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        batch.run(1, 1)
         e1.record(stream)
         e1.synchronize()
         ms += e0.elapsed_time(e1)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t_wall
-    counters1 = [sim.move_counters(m) for m in range(sim.n_moves)]
+    launches = batch.stats()["kernel_launches"] - launches0
+    att1, acc1 = batch.counters()
 
-    # e2e: host buffers in, sweep, host buffers out, every step, through the C interface.
-    host_path = sim.get_path(1)
+    # Sweep kernel alone (for its roofline): one launch per step, same flush.
+    k_ms = 0.0
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        batch.sweeps(1)
+        e1.record(stream)
+        e1.synchronize()
+        k_ms += e0.elapsed_time(e1)
+    att2, acc2 = batch.counters()
+
+    # e2e: every chain's path from host memory, one cycle, energies and paths back, every step.
+    host = batch.get_paths()
     e2e_ms = 0.0
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        sim.set_path(host_path)
-        sim.sweep(moves, counts, reps)
-        host_path = sim.get_path(1)
+        batch.set_paths(host)
+        batch.run(1, 1)
+        energies = batch.last_energy()
+        host = batch.get_paths()
         e2e_ms += (time.perf_counter() - t0) * 1e3
     if sampler:
         sampler.terminate()
         sampler.wait()
+    assert np.all(np.isfinite(energies))
 
-    ms_max, e2e_max = reduce_max_over_ranks([ms, e2e_ms], dist, device=f"cuda:{local}")
-    total_moves = bead_moves_per_step * args.steps * world
-    value = total_moves / (ms_max / 1e3)
-    e2e_value = total_moves / (e2e_max / 1e3)
+    ms_max, e2e_max, k_max = reduce_max_over_ranks([ms, e2e_ms, k_ms], dist, device=f"cuda:{local}")
+    value = per_sweep * args.steps * world / (ms_max / 1e3)
+    e2e_value = per_sweep * args.steps * world / (e2e_max / 1e3)
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return
 
-    acc = sum(counters1[m][3] - counters0[m][3] for m in range(sim.n_moves))
-    att = sum(counters1[m][0] - counters0[m][0] for m in range(sim.n_moves))
-    lv0 = sum(counters1[m][4] - counters0[m][4] for m in range(sim.n_moves))
-    peak, peak_kind = measured_peaks()
-    alg = algorithmic_bytes(sim, counters0, counters1, sim.n_k) / args.steps
-    achieved = alg / (ms_max / args.steps / 1e3) / 1e9
+    peak, peak_kind = measured_hbm_peak()
+    alg = batch_algorithmic_bytes(batch, att2 - att1, acc2 - acc1) / args.steps
+    achieved = alg / (k_max / args.steps / 1e3) / 1e9
     traffic = None
-    tf = ROOT / "profiles" / "sweep_traffic.json"
+    tf = ROOT / "profiles" / "batch_sweep_traffic.json"
     if tf.exists():
         traffic = json.loads(tf.read_text()).get("dram_bytes_per_sweep")
-
-    cpu = cpu_baseline(xml, tmp, host_path, reps) if not args.no_cpu_baseline else None
-    path_bytes = N_PART * N_BEAD * 3 * 8
+    sample = list(range(0, N_CHAINS, N_CHAINS // 8))
+    pm, psec = time_plain_chains(items, tmp, local, sample)
+    plain = {"value": pm / psec, "unit": METRIC, "chains": sample,
+             "note": "single-chain FP64 sweep kernel, one chain after another, device time"}
+    cheap = sorted(range(N_CHAINS), key=lambda c: batch.shapes[c][0] ** 2 * batch.shapes[c][1])[:4]
+    gate = energy_gate(items, tmp, local, chains=cheap, sweeps=args.gate_sweeps)
+    eg, _, _, _ = egas_plain(local, args.steps, args.warmup, tmp, flush)
+    cpu = None
+    if not args.no_cpu_baseline:
+        moves, el = cpu_oracle_chains(items, tmp, 12.0, sample)
+        cpu = {"value": moves / el, "unit": METRIC, "cores": 1, "kind": "port",
+               "sample": f"{moves // 7} bisection attempts ({el:.1f} s) on chains {sample}, round robin in chunks of 64"}
+    path_bytes_h2d = sum(((n + 7) & ~7) * m * 16 for n, m, _ in batch.shapes)  # the float4 staging copy
     line = {
-        "metric": METRIC, "value": value, "unit": "bead-moves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded uniform beads, warmed up)",
-        "config": base_config({"n_k_half_space": sim.n_k, "l2": "256 MB flush between timed steps",
-                               "acceptance": acc / max(att, 1), "level0_fraction": lv0 / max(att, 1),
-                               "sweep_grid_ctas": None}),
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Gaussian beads per chain, warmed up)",
+        "config": {"workload": WORKLOAD, "n_chains": N_CHAINS, "bead_moves_per_step": per_sweep,
+                   "tile": {"items_per_lane": ipl, "max_warps": mw, "autotune_s_per_sweep": tune_s},
+                   "acceptance": float((acc1 - acc0).sum() / max((att1 - att0).sum(), 1)),
+                   "l2": "256 MB flush between timed steps", "parallelism": "replicas (independent chains per GPU)"},
         "clocks": clocks_summary(clk_file, local),
-        "e2e": {"value": e2e_value, "unit": "bead-moves/s", "h2d_bytes_per_step": path_bytes, "d2h_bytes_per_step": path_bytes,
-                "note": "pimc_set_path (upload + charge-density rebuild) + pimc_sweep + pimc_get_path per step"},
-        "gpu_launches": args.steps,
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": path_bytes_h2d,
+                "d2h_bytes_per_step": path_bytes_h2d + N_CHAINS * 4 * 8,
+                "note": "pimc_batch_set_paths + pimc_batch_run(1 cycle) + pimc_batch_last_energy + pimc_batch_get_paths per step"},
+        "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "BisectSweepKernel", "algorithmic_bytes_per_launch": alg},
+                     "traffic": traffic, "peak_kind": peak_kind, "kernel": "BatchSweepKernel",
+                     "algorithmic_bytes_per_launch": alg, "ms_per_launch": k_max / args.steps},
         "cpu_baseline": cpu,
+        "plain_same_system": plain,
+        "speedup_vs_plain_same_system": value / plain["value"],
+        "energy_gate": gate,
+        "plain_electron_gas": eg,
         "wall_s": wall,
     }
     print(json.dumps(line))
@@ -237,31 +401,22 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def _oracle_sample(xml, tmp, path, seconds, chain, reps, results, idx):
+def _oracle_worker(items, tmp, chains, seconds, results, idx):
     import oracle
-    o = oracle.OracleSim(xml, base_dir=tmp, chain=chain)
-    o.set_path(path)
-    B = 1 << N_LEVEL
-    done = 0
-    t0 = time.perf_counter()
-    chunk = 8
+    sims = []
+    for c in chains:
+        xml, p = items[c]
+        o = oracle.OracleSim(xml, base_dir=tmp, chain=c)
+        o.set_path(p)
+        sims.append(o)
+    moves, t0 = 0, time.perf_counter()
     while time.perf_counter() - t0 < seconds:
-        for _ in range(chunk):
-            o.move_attempts(0, 1)
-            o.move_attempts(1, 1)
-        done += 2 * chunk
-    el = time.perf_counter() - t0
-    results[idx] = (done * (B - 1), el)
-    o.close()
-
-
-def cpu_baseline(xml, tmp, path, reps, seconds=12.0):
-    """The oracle on one host core, from the GPU run's warmed-up path, for a bounded time."""
-    res = [None]
-    _oracle_sample(xml, tmp, path, seconds, 0, reps, res, 0)
-    moves, el = res[0]
-    return {"value": moves / el, "unit": "bead-moves/s", "cores": 1, "kind": "port",
-            "sample": f"{moves // ((1 << N_LEVEL) - 1)} alternating up/down bisection attempts ({el:.1f} s) from the warmed-up GPU path"}
+        for o in sims:
+            o.move_attempts(0, 64)
+            moves += 64 * ((1 << CHAIN_LEVEL) - 1)
+    results[idx] = (moves, time.perf_counter() - t0)
+    for o in sims:
+        o.close()
 
 
 def run_reference(args):
@@ -271,39 +426,33 @@ def run_reference(args):
     import oracle
     oracle.build()
     tmp = tempfile.mkdtemp(prefix="pimc_ref_")
-    xml, path, reps = workload(tmp)
+    items = chains_workload(tmp)
     threads = max(1, os.cpu_count() or 1)
-    # Warm-up (untimed): equilibrate one chain briefly, then give every thread that path.
-    o = oracle.OracleSim(xml, base_dir=tmp, chain=0)
-    o.set_path(path)
-    for _ in range(max(1, args.warmup)):
-        for _ in range(16):
-            o.move_attempts(0, 1)
-            o.move_attempts(1, 1)
-    start = o.get_path(1)
-    o.close()
     per_step_s = 4.0
+    for _ in range(args.warmup):  # untimed: start-up of every thread's chains
+        _oracle_worker(items, tmp, [0], 0.05, [None], 0)
     total_moves, total_s = 0, 0.0
     for _ in range(args.steps):
         res = [None] * threads
-        ths = [threading.Thread(target=_oracle_sample, args=(xml, tmp, start, per_step_s, i + 1, reps, res, i)) for i in range(threads)]
+        groups = [list(range(i, N_CHAINS, threads)) for i in range(threads)]
+        ths = [threading.Thread(target=_oracle_worker, args=(items, tmp, groups[i], per_step_s, res, i)) for i in range(threads)]
         t0 = time.perf_counter()
         for t in ths:
             t.start()
         for t in ths:
             t.join()
-        el = time.perf_counter() - t0
+        total_s += time.perf_counter() - t0
         total_moves += sum(r[0] for r in res)
-        total_s += el
     value = total_moves / total_s
     line = {
-        "metric": METRIC, "value": value, "unit": "bead-moves/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform beads)",
-        "config": base_config({"l2": "n/a (host)"}), "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": "bead-moves/s", "cores": threads, "kind": "port",
-                         "sample": f"{threads} independent chains x {per_step_s:.0f} s per step (CPU restatement; the reference's own build needs absent dependencies)"},
-        "e2e": {"value": value, "unit": "bead-moves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian beads per chain)",
+        "config": {"workload": WORKLOAD, "n_chains": N_CHAINS, "l2": "n/a (host)"}, "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                         "sample": f"{threads} threads, each cycling through its share of the 256 chains for {per_step_s:.0f} s per "
+                                   "step (CPU restatement; the reference's own build needs absent dependencies)"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
 
@@ -315,6 +464,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--gate-sweeps", type=int, default=400)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

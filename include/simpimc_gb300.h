@@ -145,6 +145,10 @@ int pimc_batch_chain_info(pimc_batch* b, uint32_t chain, uint32_t* out4);
 /* One chain's path, pos[p][b][d] as for pimc_set_path (stored as FP32). */
 int pimc_batch_set_path(pimc_batch* b, uint32_t chain, const double* pos);
 int pimc_batch_get_path(pimc_batch* b, uint32_t chain, double* pos);
+/* Every chain's path in one transfer: the chains' [n_part][n_bead][3] arrays concatenated in chain
+ * order (staged through pinned host memory, one copy each way). */
+int pimc_batch_set_paths(pimc_batch* b, const double* all);
+int pimc_batch_get_paths(pimc_batch* b, double* all);
 /* n bisection attempts (Move::DoEvent, move_class.h:277-293) on every chain. */
 int pimc_batch_attempts(pimc_batch* b, uint64_t n);
 /* n sweeps on every chain; a sweep of a chain is n_part * ceil(n_bead / 2^n_level) attempts. */
@@ -159,6 +163,8 @@ int pimc_batch_sync(pimc_batch* b);
  * keeps the first 4096); *n_measure = measurements since the last reset. */
 int pimc_batch_energy(pimc_batch* b, uint32_t chain, double* out, uint64_t cap, uint64_t* n_measure);
 int pimc_batch_reset_energy(pimc_batch* b);
+/* The latest measurement of every chain, out[n_chains][4] = {E, kinetic, trap, pair}. */
+int pimc_batch_last_energy(pimc_batch* b, double* out);
 /* Per-chain attempt and acceptance counters (arrays of n_chains; either may be NULL). */
 int pimc_batch_counters(pimc_batch* b, uint64_t* attempts, uint64_t* accepts);
 /* Pair tile: a chain gets ceil((n_part-1)(2^n_level-1) / (32 items_per_lane)) warps, at most

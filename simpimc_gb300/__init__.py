@@ -85,6 +85,9 @@ SIGNATURES = {
     "pimc_batch_chain_info": (C.c_int, [_P, C.c_uint32, _U32P]),
     "pimc_batch_set_path": (C.c_int, [_P, C.c_uint32, _DP]),
     "pimc_batch_get_path": (C.c_int, [_P, C.c_uint32, _DP]),
+    "pimc_batch_set_paths": (C.c_int, [_P, _DP]),
+    "pimc_batch_get_paths": (C.c_int, [_P, _DP]),
+    "pimc_batch_last_energy": (C.c_int, [_P, _DP]),
     "pimc_batch_attempts": (C.c_int, [_P, C.c_uint64]),
     "pimc_batch_sweeps": (C.c_int, [_P, C.c_uint64]),
     "pimc_batch_measure": (C.c_int, [_P]),
@@ -355,6 +358,23 @@ class ChainBatch:
         n, m, _ = self.shapes[chain]
         out = np.zeros((n, m, 3), dtype=np.float64)
         self._check(self._lib.pimc_batch_get_path(self._h, chain, _dp(out)))
+        return out
+
+    def set_paths(self, flat: np.ndarray):
+        """Every chain's path at once: the chains' (n_part, n_bead, 3) arrays concatenated."""
+        a = np.ascontiguousarray(flat, dtype=np.float64).ravel()
+        if a.size != sum(n * m * 3 for n, m, _ in self.shapes):
+            raise ValueError("flat path size does not match the chains")
+        self._check(self._lib.pimc_batch_set_paths(self._h, _dp(a)))
+
+    def get_paths(self) -> np.ndarray:
+        out = np.zeros(sum(n * m * 3 for n, m, _ in self.shapes), dtype=np.float64)
+        self._check(self._lib.pimc_batch_get_paths(self._h, _dp(out)))
+        return out
+
+    def last_energy(self) -> np.ndarray:
+        out = np.zeros((self.n_chains, 4), dtype=np.float64)
+        self._check(self._lib.pimc_batch_last_energy(self._h, _dp(out)))
         return out
 
     def attempts(self, n: int):

@@ -1,0 +1,52 @@
+"""Small fixed workloads for profiler captures (one warm-up launch, then the launches to capture).
+
+    python -m simpimc_gb300.profile_cases batch   # 256 uneven trapped-Coulomb chains: 1 + 1 sweep launches
+    python -m simpimc_gb300.profile_cases egas    # 66-electron gas: 1 + 1 sweep launches (528 attempts each)
+
+Each case holds well under 100 MB on the device, so a capture of the second launch
+(`-k regex:<Kernel> -s 1 -c 1`) ends in seconds.
+"""
+from __future__ import annotations
+
+import math
+import sys
+import tempfile
+
+import numpy as np
+
+
+def batch_case(d):
+    from . import ChainBatch
+    from .configs import batched_trap_chains
+    items = batched_trap_chains(d, n_chains=256, seed0=1000, n_level=3)
+    b = ChainBatch([x for x, _ in items], base_dir=d)
+    b.set_paths(np.concatenate([p.ravel() for _, p in items]))
+    b.set_tiles(2, 16)
+    b.sweeps(1)
+    b.sweeps(1)
+    b.synchronize()
+    att, acc = b.counters()
+    print(f"batch ok: {int(att.sum())} attempts, acceptance {acc.sum() / att.sum():.4f}")
+
+
+def egas_case(d):
+    from . import Simulation
+    from .configs import electron_gas
+    xml, path = electron_gas(d, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_units=12.0, n_level=4, seed=20261203)
+    s = Simulation(xml, base_dir=d)
+    s.set_path(path)
+    reps = 33 * math.ceil(128 / 16)
+    s.sweep([0, 1], [1, 1], reps)
+    s.sweep([0, 1], [1, 1], reps)
+    s.synchronize()
+    print(f"egas ok: {s.move_counters(0)[0] + s.move_counters(1)[0]} attempts")
+
+
+def main(argv):
+    case = argv[1] if len(argv) > 1 else "batch"
+    with tempfile.TemporaryDirectory() as d:
+        {"batch": batch_case, "egas": egas_case}[case](d)
+
+
+if __name__ == "__main__":
+    main(sys.argv)

@@ -13,10 +13,13 @@
 // long-range part between the species and itself; one non-adaptive Bisect move with n_level <= 5;
 // open or periodic boundaries.
 //
-// Arithmetic: positions and per-term action values in FP32; every sum of terms in double-float
-// (FP32 pairs, 2^-46 relative rounding); each Metropolis level decision, which adds the level's
-// action difference to the previous level's and compares with the log-uniform draw, in FP64;
-// estimator values and block sums in FP64.
+// Arithmetic: positions and per-term action values in FP32; every sum of terms compensated
+// (cascaded TwoSum, as accurate as a sum in twice the working precision); the per-level
+// acceptance accumulation (sampling ratio minus this level's action change plus the previous
+// level's) and its comparison with the log-uniform draw in double-float (FP32 pairs, 48-bit
+// significand): each FP64 instruction holds GB300's FP64 pipe (2 lanes per SM per clock) for a
+// whole warp, and the double-float result is within 1e-13 of the FP64 one. Estimator values and
+// block sums are FP64.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -70,6 +73,9 @@ class ChainBatch {
 
     void SetPath(uint32_t chain, const double* pos);  // [n_part][n_bead][3]
     void GetPath(uint32_t chain, double* pos);
+    void SetPaths(const double* all);  // every chain's path, concatenated in chain order
+    void GetPaths(double* all);
+    void LastEnergy(double* out);      // [n_chains][4]: the latest measurement of every chain
     void Attempts(uint64_t n);                // n bisection attempts on every chain
     void Sweeps(uint64_t n);                  // n sweeps on every chain (one launch)
     void Measure();                           // one energy measurement on every chain
@@ -83,12 +89,13 @@ class ChainBatch {
 
     uint32_t n_chains = 0, series_cap = 0;
     int device = 0, n_sm = 0;
-    uint32_t items_per_lane = 8, max_warps = 8;
+    uint32_t items_per_lane = 2, max_warps = 16;  // pair tile (the autotuner's usual choice)
     cudaStream_t stream = nullptr;
     std::vector<ChainSpec> specs;
     std::vector<ChainDev> chains;
     std::vector<uint32_t> order;   // block -> chain, most expensive first
     uint64_t bead_moves_per_sweep = 0;
+    uint64_t path_doubles = 0;  // sum of n_part * n_bead * 3 over the chains
     uint64_t kernel_launches = 0;
 
    private:
@@ -96,7 +103,9 @@ class ChainBatch {
     void LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts);
     void LaunchMeasure();
     void ResetGraph();
-    std::unique_ptr<DeviceBuffer> pos_, chains_dev_, order_dev_, att_, acc_, series_, n_meas_, err_;
+    std::unique_ptr<DeviceBuffer> pos_, chains_dev_, order_dev_, att_, acc_, series_, n_meas_, err_, last_;
+    float4* staging_ = nullptr;  // pinned host mirror of pos_ for bulk transfers
+    size_t pos_float4 = 0;
     cudaGraphExec_t graph_ = nullptr;
     uint64_t graph_sweeps_ = 0;
 };

@@ -44,6 +44,7 @@ struct BatchArgs {
     uint64_t* accepts;
     double* series;      // [chain][series_cap][kBatchSeriesComponents]
     uint64_t* n_meas;    // per chain
+    double* last;        // [chain][kBatchSeriesComponents]: latest measurement
     int* err;
     uint32_t series_cap;
 };
@@ -509,6 +510,11 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchEnergyKernel(BatchAr
         const double e_pair = ToDouble(pr) * inv_m;
         const uint64_t n = a.n_meas[ci];
         if (!isfinite(e_kin + e_trap + e_pair)) atomicOr(a.err, kDevErrNonFinite);
+        double* last = a.last + (size_t)ci * kBatchSeriesComponents;
+        last[0] = e_kin + e_trap + e_pair;
+        last[1] = e_kin;
+        last[2] = e_trap;
+        last[3] = e_pair;
         if (n < a.series_cap) {
             double* out = a.series + ((size_t)ci * a.series_cap + n) * kBatchSeriesComponents;
             out[0] = e_kin + e_trap + e_pair;
@@ -635,11 +641,17 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
         c.kin_const = (double)s.n_part * s.n_bead * 3. / (2. * s.tau);  // kinetic_class.h:13
         c.i4ltt = 1. / (4. * s.lambda * s.tau * s.tau);
         bead_moves_per_sweep += c.attempts_per_sweep * (B - 1);
+        path_doubles += (uint64_t)s.n_part * s.n_bead * 3;
     }
     series_cap = 4096;
     CudaCheck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream create");
     pos_.reset(new DeviceBuffer(off * sizeof(float4)));
+    pos_float4 = off;
     CudaCheck(cudaMemset(pos_->ptr, 0, off * sizeof(float4)), "memset");
+    CudaCheck(cudaMallocHost(&staging_, off * sizeof(float4)), "pinned staging");
+    std::memset(staging_, 0, off * sizeof(float4));
+    last_.reset(new DeviceBuffer((size_t)n_chains * kBatchSeriesComponents * sizeof(double)));
+    CudaCheck(cudaMemset(last_->ptr, 0, last_->bytes), "memset");
     chains_dev_.reset(new DeviceBuffer(n_chains * sizeof(ChainDev)));
     order_dev_.reset(new DeviceBuffer(n_chains * sizeof(uint32_t)));
     att_.reset(new DeviceBuffer(n_chains * sizeof(uint64_t)));
@@ -656,6 +668,7 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
 
 ChainBatch::~ChainBatch() {
     if (graph_) cudaGraphExecDestroy(graph_);
+    if (staging_) cudaFreeHost(staging_);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -723,18 +736,63 @@ void ChainBatch::GetPath(uint32_t chain, double* p) {
         }
 }
 
+/// Every chain's path in one transfer: converted into the pinned float4 mirror, then one copy.
+void ChainBatch::SetPaths(const double* all) {
+    if (!all) throw PimcError(kErrArg, "null paths");
+    const double* src = all;
+    for (uint32_t ci = 0; ci < n_chains; ++ci) {
+        const ChainDev& c = chains[ci];
+        float4* dst = staging_ + c.pos_off;
+        for (uint32_t i = 0; i < c.n_part; ++i)
+            for (uint32_t b = 0; b < c.n_bead; ++b) {
+                const double* r = src + ((size_t)i * c.n_bead + b) * 3;
+                if (!std::isfinite(r[0]) || !std::isfinite(r[1]) || !std::isfinite(r[2])) throw PimcError(kErrArg, "non-finite position");
+                dst[(size_t)b * c.n_pad + i] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.f);
+            }
+        src += (size_t)c.n_part * c.n_bead * 3;
+    }
+    CudaCheck(cudaMemcpyAsync(pos_->ptr, staging_, pos_float4 * sizeof(float4), cudaMemcpyHostToDevice, stream), "set paths");
+    CudaCheck(cudaStreamSynchronize(stream), "sync");
+}
+
+void ChainBatch::GetPaths(double* all) {
+    if (!all) throw PimcError(kErrArg, "null paths");
+    CudaCheck(cudaMemcpyAsync(staging_, pos_->ptr, pos_float4 * sizeof(float4), cudaMemcpyDeviceToHost, stream), "get paths");
+    CudaCheck(cudaStreamSynchronize(stream), "sync");
+    double* dst = all;
+    for (uint32_t ci = 0; ci < n_chains; ++ci) {
+        const ChainDev& c = chains[ci];
+        const float4* src = staging_ + c.pos_off;
+        for (uint32_t i = 0; i < c.n_part; ++i)
+            for (uint32_t b = 0; b < c.n_bead; ++b) {
+                const float4 r = src[(size_t)b * c.n_pad + i];
+                double* o = dst + ((size_t)i * c.n_bead + b) * 3;
+                o[0] = r.x;
+                o[1] = r.y;
+                o[2] = r.z;
+            }
+        dst += (size_t)c.n_part * c.n_bead * 3;
+    }
+}
+
+void ChainBatch::LastEnergy(double* out) {
+    if (!out) throw PimcError(kErrArg, "null output");
+    CudaCheck(cudaMemcpyAsync(out, last_->ptr, last_->bytes, cudaMemcpyDeviceToHost, stream), "last energy");
+    Sync();
+}
+
 namespace {
 BatchArgs MakeArgs(DeviceBuffer& pos, DeviceBuffer& ch, DeviceBuffer& ord, DeviceBuffer& att, DeviceBuffer& acc, DeviceBuffer& ser,
-                   DeviceBuffer& nm, DeviceBuffer& err, uint32_t cap) {
+                   DeviceBuffer& nm, DeviceBuffer& last, DeviceBuffer& err, uint32_t cap) {
     return BatchArgs{pos.as<float4>(), ch.as<ChainDev>(), ord.as<uint32_t>(), att.as<uint64_t>(), acc.as<uint64_t>(),
-                     ser.as<double>(), nm.as<uint64_t>(), err.as<int>(), cap};
+                     ser.as<double>(), nm.as<uint64_t>(), last.as<double>(), err.as<int>(), cap};
 }
 }  // namespace
 
 void ChainBatch::LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts) {
     uint32_t warps = 1;
     for (const auto& c : chains) warps = std::max(warps, c.n_warps);
-    const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *err_, series_cap);
+    const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, series_cap);
     BatchSweepKernel<<<n_chains, warps * 32, 0, stream>>>(a, n_sweeps, n_attempts);
     CudaCheck(cudaGetLastError(), "batch sweep launch");
     ++kernel_launches;
@@ -743,7 +801,7 @@ void ChainBatch::LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts) {
 void ChainBatch::LaunchMeasure() {
     uint32_t warps = 1;
     for (const auto& c : chains) warps = std::max(warps, c.n_warps);
-    const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *err_, series_cap);
+    const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, series_cap);
     BatchEnergyKernel<<<n_chains, warps * 32, 0, stream>>>(a);
     CudaCheck(cudaGetLastError(), "batch energy launch");
     ++kernel_launches;
@@ -944,6 +1002,18 @@ int pimc_batch_set_path(pimc_batch* h, uint32_t chain, const double* pos) {
 
 int pimc_batch_get_path(pimc_batch* h, uint32_t chain, double* pos) {
     return BatchGuard(h, [&](pimc::ChainBatch& b) { b.GetPath(chain, pos); });
+}
+
+int pimc_batch_set_paths(pimc_batch* h, const double* all) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.SetPaths(all); });
+}
+
+int pimc_batch_get_paths(pimc_batch* h, double* all) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.GetPaths(all); });
+}
+
+int pimc_batch_last_energy(pimc_batch* h, double* out) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.LastEnergy(out); });
 }
 
 int pimc_batch_attempts(pimc_batch* h, uint64_t n) {
