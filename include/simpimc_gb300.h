@@ -79,6 +79,20 @@ int pimc_get_action_noalloc(pimc_ctx* ctx, uint32_t action, uint32_t b0, uint32_
 /* Action::GetActionGradient (action_class.h:46); out has n_d entries. */
 int pimc_get_action_gradient(pimc_ctx* ctx, uint32_t action, uint32_t b0, uint32_t b1, const uint32_t* species,
                              const uint32_t* particles, uint32_t n_particles, uint32_t level, int mode, double* out);
+/* Exact ("adjoint") counterparts, level 0, FP64. The whole-ring action of one action (action >= 0)
+ * or of every action (action = -1): every link b -> b+1 of every particle of its species, the
+ * trap on every slice, every pair on every slice and, for Ewald actions, the k-space sum
+ * tau sum_b sum_k v_k Re(rho_a conj(rho_b)) (x2 between different species) from densities of the
+ * chosen copy. pimc_action_gradient_path returns its gradient dS/dR, grad[p][b][d] in the path
+ * order, with the trap and Ewald forces the reference leaves out (pair_action_class.h:305-337,
+ * trap_class.h) and the analytic pair derivative in place of its eps = 1e-4 central differences
+ * (pair_action_class.h:135-155). pimc_get_action_gradient_exact is Action::GetActionGradient
+ * (action_class.h:46) from that gradient: the sum over the listed particles of the action's species
+ * and slices b0..b1-1 of dS/dr. No reference counterpart for the first two. */
+int pimc_total_action(pimc_ctx* ctx, int action, int mode, double* out);
+int pimc_action_gradient_path(pimc_ctx* ctx, int action, int mode, double* grad);
+int pimc_get_action_gradient_exact(pimc_ctx* ctx, uint32_t action, uint32_t b0, uint32_t b1, const uint32_t* species,
+                                   const uint32_t* particles, uint32_t n_particles, uint32_t level, int mode, double* out);
 /* Action::DActionDBeta (action_class.h:37) */
 int pimc_dactiondbeta(pimc_ctx* ctx, uint32_t action, double* out);
 /* Action::Potential (action_class.h:52) */
@@ -87,7 +101,10 @@ int pimc_potential(pimc_ctx* ctx, uint32_t action, double* out);
 int pimc_virial_energy(pimc_ctx* ctx, uint32_t action, double window, double* out);
 
 /* Moves: Move::DoEvent repeated (move_class.h:277-293, bisect_class.h:24-139). Runs n attempts
- * of move `move` on the device in one launch. */
+ * of move `move` on the device in one launch. Besides Bisect, a <Move type="HMC" step_size="0.01"
+ * n_steps="10" [species="..."]/> (no reference counterpart) moves the whole path of one or every
+ * species by hybrid Monte Carlo: Gaussian momenta, leapfrog on S(R) + |P|^2/2 with the exact
+ * gradient, Metropolis on the energy change. */
 int pimc_move_attempts(pimc_ctx* ctx, uint32_t move, uint64_t n);
 /* A schedule of moves, (moves[i], counts[i]) in order, repeated n_rep times, in one launch
  * (the body of a Loop of Move events, loop_class.h:269-274). */

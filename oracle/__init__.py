@@ -61,6 +61,8 @@ def lib():
             "oracle_potential": [C.c_void_p, C.c_uint32, _DP],
             "oracle_virial_energy": [C.c_void_p, C.c_uint32, C.c_double, _DP],
             "oracle_move_attempts": [C.c_void_p, C.c_uint32, C.c_uint64],
+            "oracle_total_action": [C.c_void_p, C.c_int, C.c_int, _DP],
+            "oracle_action_gradient_path": [C.c_void_p, C.c_int, C.c_int, _DP],
             "oracle_move_stats": [C.c_void_p, C.c_uint32, _U64P],
             "oracle_obs_accumulate": [C.c_void_p, C.c_uint32],
             "oracle_obs_block": [C.c_void_p, C.c_uint32, _DP, C.c_uint64, _U64P],
@@ -193,6 +195,17 @@ class OracleSim:
         out = C.c_double()
         self._ok(self._L.oracle_virial_energy(self._h, action, float(window), C.byref(out)))
         return out.value
+
+    def total_action(self, action=-1, mode=0):
+        out = C.c_double()
+        self._ok(self._L.oracle_total_action(self._h, action, mode, C.byref(out)))
+        return out.value
+
+    def action_gradient_path(self, action=-1, mode=0):
+        n_total, n_bead, n_d = self.n_total, self.n_bead, self.n_d
+        out = np.zeros((n_total, n_bead, n_d), dtype=np.float64)
+        self._ok(self._L.oracle_action_gradient_path(self._h, action, mode, out.ctypes.data_as(_DP)))
+        return out
 
     def move_attempts(self, move, n):
         self._ok(self._L.oracle_move_attempts(self._h, move, n))

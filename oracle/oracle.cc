@@ -1016,6 +1016,216 @@ struct BarePairAction : PairAction {
 
 // ---------------------------------------------------------------------------------------------
 // Moves: Bisect (src/events/moves/single_species_move/bisect/bisect_class.h:8-214).
+// ---------------------------------------------------------------------------------------------
+// Whole-ring action at level 0 and its exact gradient (checker for the library's
+// pimc_total_action / pimc_action_gradient_path and the HMC move built on them). Definitions:
+//   Kinetic  sum_{p,b} -log rho_free(r_{p,b+1} - r_{p,b})        (kinetic_class.h:105-122)
+//   Trap     cofactor_a sum_{p,b} |r_{p,b}|^2                       (trap_class.h:40-62)
+//   Bare     tau sum_pairs sum_b V(|d_b|), d_b the minimum image of r_q - r_p on slice b, V the
+//            clamped per-bead potential of CalcV (bare_pair_action_class.h:98-111), plus the Ewald
+//            sum tau sum_b sum_k v_k Re(rho_a conj(rho_b)) (x2 for a != b, bare_pair_action_class.h:152-165)
+// The gradient is the analytic derivative of each term.
+static bool SelectedAction(const Action& a, int sel, int i) {
+    if (a.is_importance_weight) return false;
+    if (sel >= 0) return sel == i;
+    if (sel == -2) return a.type != "Kinetic";
+    return true;
+}
+
+static const double* RAt(const Path& path, const double* R, uint32_t g, uint32_t b) {
+    return R + ((size_t)g * path.n_bead + (b % path.n_bead)) * path.n_d;
+}
+
+static void WholeRho(Path& path, const double* R, std::vector<std::vector<cplx>>& rho) {
+    const size_t K = path.ks.K();
+    rho.assign(path.species.size(), {});
+    if (!K) return;
+    for (auto& s : path.species) {
+        auto& out = rho[s.s_i];
+        out.assign((size_t)path.n_bead * K, cplx(0., 0.));
+        for (uint32_t b = 0; b < path.n_bead; ++b)
+            for (uint32_t p = 0; p < s.n_part; ++p) {
+                path.ks.CalcC(RAt(path, R, s.offset + p, b));
+                for (size_t k = 0; k < K; ++k) {
+                    cplx f = 1.;
+                    for (uint32_t d = 0; d < path.n_d; ++d) f *= path.ks.c_k[d][path.ks.indices[k][d]];
+                    out[(size_t)b * K + k] += f;
+                }
+            }
+    }
+}
+
+// Value and slope of a spline, zero slope outside its grid (where Eval holds the end value).
+static void SplineVG(const Spline& sp, double t, double& v, double& g) {
+    const bool in = t >= sp.x.front() && t <= sp.x.back();
+    sp.EvalVG(t, v, g);
+    if (!in) g = 0.;
+}
+
+static void KineticTerms(Kinetic& k, double* d, uint32_t nd, double& phi, double* dphi) {
+    const FreeSpline& fs = k.rho_free_splines[0];
+    phi = 0.;
+    for (uint32_t c = 0; c < nd; ++c) {
+        double v = 0., g = 0.;
+        if (k.n_images > 0) SplineVG(fs.image_action, d[c], v, g);
+        phi += v + d[c] * d[c] * fs.i_4_lambda_tau;
+        dphi[c] = g + 2. * d[c] * fs.i_4_lambda_tau;
+    }
+}
+
+static void BareVBead(const BarePairAction& a, double r, double& v, double& dv) {
+    const bool in1 = r >= a.r_v_min && r <= a.r_v_max;
+    const double r1 = std::min(std::max(r, a.r_v_min), a.r_v_max);
+    if (a.is_coulomb) {
+        v = 1. / r1;
+        dv = in1 ? -1. / (r1 * r1) : 0.;
+    } else {
+        double g;
+        a.v_r_spline.EvalVG(r1, v, g);
+        dv = in1 ? g : 0.;
+    }
+    if (a.use_long_range) {
+        const bool in2 = r1 >= a.r_v_long_min && r1 <= a.r_v_long_max;
+        const double r2 = std::min(std::max(r1, a.r_v_long_min), a.r_v_long_max);
+        double vl, gl;
+        a.v_long_r_spline.EvalVG(r2, vl, gl);
+        v -= vl;
+        if (in1 && in2) dv -= gl;
+    }
+}
+
+static double WholeAction(Path& path, std::vector<std::unique_ptr<Action>>& actions, int sel, const double* R) {
+    const uint32_t M = path.n_bead, nd = path.n_d;
+    std::vector<std::vector<cplx>> rho;
+    bool have_rho = false;
+    double total = 0.;
+    for (size_t i = 0; i < actions.size(); ++i) {
+        Action* a = actions[i].get();
+        if (!SelectedAction(*a, sel, (int)i)) continue;
+        if (auto* k = dynamic_cast<Kinetic*>(a)) {
+            const Species& s = *k->species;
+            for (uint32_t p = 0; p < s.n_part; ++p)
+                for (uint32_t b = 0; b < M; ++b) {
+                    double d[3], dphi[3], phi;
+                    path.Dr(RAt(path, R, s.offset + p, b + 1), RAt(path, R, s.offset + p, b), d);
+                    KineticTerms(*k, d, nd, phi, dphi);
+                    total += phi;
+                }
+        } else if (auto* t = dynamic_cast<Trap*>(a)) {
+            const Species& s = *t->species;
+            for (uint32_t p = 0; p < s.n_part; ++p)
+                for (uint32_t b = 0; b < M; ++b) {
+                    const double* r = RAt(path, R, s.offset + p, b);
+                    double r2 = 0.;
+                    for (uint32_t c = 0; c < nd; ++c) r2 += r[c] * r[c];
+                    total += t->cofactor_a * r2;
+                }
+        } else if (auto* bp = dynamic_cast<BarePairAction*>(a)) {
+            if (bp->is_constant) continue;
+            for (auto& pr : bp->AllPairs()) {
+                const uint32_t ga = bp->species_a->offset + pr.first, gb = bp->species_b->offset + pr.second;
+                for (uint32_t b = 0; b < M; ++b) {
+                    double d[3], r2 = 0., v, dv;
+                    path.Dr(RAt(path, R, gb, b), RAt(path, R, ga, b), d);
+                    for (uint32_t c = 0; c < nd; ++c) r2 += d[c] * d[c];
+                    BareVBead(*bp, std::sqrt(r2), v, dv);
+                    total += path.tau * v;
+                }
+            }
+            if (bp->use_long_range) {
+                if (!have_rho) {
+                    WholeRho(path, R, rho);
+                    have_rho = true;
+                }
+                const auto& ra = rho[bp->species_a->s_i];
+                const auto& rb = rho[bp->species_b->s_i];
+                const size_t K = path.ks.K();
+                double lr = 0.;
+                for (uint32_t b = 0; b < M; ++b)
+                    for (size_t k = 0; k < K; ++k) lr += bp->v_long_k[k] * CMag2(ra[(size_t)b * K + k], rb[(size_t)b * K + k]);
+                total += (bp->species_a == bp->species_b ? 1. : 2.) * path.tau * lr;
+            }
+        }
+    }
+    return total;
+}
+
+static void WholeGradient(Path& path, std::vector<std::unique_ptr<Action>>& actions, int sel, const double* R, double* G) {
+    const uint32_t M = path.n_bead, nd = path.n_d;
+    std::fill(G, G + (size_t)path.n_total * M * nd, 0.);
+    auto gat = [&](uint32_t g, uint32_t b) { return G + ((size_t)g * M + (b % M)) * nd; };
+    std::vector<std::vector<cplx>> rho;
+    bool have_rho = false;
+    for (size_t i = 0; i < actions.size(); ++i) {
+        Action* a = actions[i].get();
+        if (!SelectedAction(*a, sel, (int)i)) continue;
+        if (auto* k = dynamic_cast<Kinetic*>(a)) {
+            const Species& s = *k->species;
+            for (uint32_t p = 0; p < s.n_part; ++p)
+                for (uint32_t b = 0; b < M; ++b) {
+                    const uint32_t g = s.offset + p;
+                    double d[3], dphi[3], phi;
+                    path.Dr(RAt(path, R, g, b + 1), RAt(path, R, g, b), d);  // link b -> b+1
+                    KineticTerms(*k, d, nd, phi, dphi);
+                    for (uint32_t c = 0; c < nd; ++c) {
+                        gat(g, b + 1)[c] += dphi[c];
+                        gat(g, b)[c] -= dphi[c];
+                    }
+                }
+        } else if (auto* t = dynamic_cast<Trap*>(a)) {
+            const Species& s = *t->species;
+            for (uint32_t p = 0; p < s.n_part; ++p)
+                for (uint32_t b = 0; b < M; ++b) {
+                    const double* r = RAt(path, R, s.offset + p, b);
+                    for (uint32_t c = 0; c < nd; ++c) gat(s.offset + p, b)[c] += 2. * t->cofactor_a * r[c];
+                }
+        } else if (auto* bp = dynamic_cast<BarePairAction*>(a)) {
+            if (bp->is_constant) continue;
+            for (auto& pr : bp->AllPairs()) {
+                const uint32_t ga = bp->species_a->offset + pr.first, gb = bp->species_b->offset + pr.second;
+                for (uint32_t b = 0; b < M; ++b) {
+                    double d[3], r2 = 0., v, dv;
+                    path.Dr(RAt(path, R, ga, b), RAt(path, R, gb, b), d);  // r_a - r_b
+                    for (uint32_t c = 0; c < nd; ++c) r2 += d[c] * d[c];
+                    const double r = std::sqrt(r2);
+                    BareVBead(*bp, r, v, dv);
+                    if (r > 0.)
+                        for (uint32_t c = 0; c < nd; ++c) {
+                            const double f = path.tau * dv * d[c] / r;
+                            gat(ga, b)[c] += f;
+                            gat(gb, b)[c] -= f;
+                        }
+                }
+            }
+            if (bp->use_long_range) {
+                if (!have_rho) {
+                    WholeRho(path, R, rho);
+                    have_rho = true;
+                }
+                const size_t K = path.ks.K();
+                auto force = [&](const Species& s, const std::vector<cplx>& other) {
+                    for (uint32_t p = 0; p < s.n_part; ++p)
+                        for (uint32_t b = 0; b < M; ++b) {
+                            path.ks.CalcC(RAt(path, R, s.offset + p, b));
+                            double acc[3] = {0., 0., 0.};
+                            for (size_t k = 0; k < K; ++k) {
+                                cplx e = 1.;
+                                for (uint32_t c = 0; c < nd; ++c) e *= path.ks.c_k[c][path.ks.indices[k][c]];
+                                const double f = bp->v_long_k[k] * std::imag(std::conj(other[(size_t)b * K + k]) * e);
+                                for (uint32_t c = 0; c < nd; ++c) acc[c] += f * path.ks.vecs[k][c];
+                            }
+                            for (uint32_t c = 0; c < nd; ++c) gat(s.offset + p, b)[c] += -2. * path.tau * acc[c];
+                        }
+                };
+                const Species& sa = *bp->species_a;
+                const Species& sb = *bp->species_b;
+                force(sa, rho[sb.s_i]);
+                if (&sa != &sb) force(sb, rho[sa.s_i]);
+            }
+        }
+    }
+}
+
 struct Move {
     std::string name, type;
     uint64_t n_accept = 0, n_attempt = 0;
@@ -1196,6 +1406,73 @@ struct Bisect : Move {
 
 // ---------------------------------------------------------------------------------------------
 // Observables (src/events/observables/*).
+// Hybrid Monte Carlo of the whole path (the library's <Move type="HMC">): momenta N(0, 1) per
+// coordinate of the moving particles in path order, normal j from Philox block 1 + j/4 (two
+// Box-Muller pairs per block), leapfrog on H = S(R) + |P|^2/2 with the exact gradient, accepted
+// when -dH >= log u with u from block 0, word 0.
+struct HMC : Move {
+    Path& path;
+    std::vector<std::unique_ptr<Action>>& actions;
+    uint32_t move_index, seed, chain, n_steps;
+    double eps;
+    int species = -1;
+    std::vector<double> prop;
+
+    HMC(Path& p, std::vector<std::unique_ptr<Action>>& a, const Input& in, uint32_t idx, uint32_t sd, uint32_t ch)
+        : path(p), actions(a), move_index(idx), seed(sd), chain(ch) {
+        name = in.GetAttribute<std::string>("name");
+        type = in.GetAttribute<std::string>("type");
+        eps = in.GetAttribute<double>("step_size", 0.01);
+        n_steps = in.GetAttribute<uint32_t>("n_steps", 10);
+        const std::string sp = in.GetAttribute<std::string>("species", "");
+        if (!sp.empty()) species = (int)p.GetSpecies(sp).s_i;
+    }
+
+    bool Attempt() override {
+        Stream st{seed, chain, move_index, attempt_counter};
+        const uint32_t M = path.n_bead, nd = path.n_d;
+        std::vector<double> R(path.r_c), P(R.size(), 0.), G(R.size(), 0.);
+        uint64_t j = 0;
+        for (auto& s : path.species) {
+            if (species >= 0 && (uint32_t)species != s.s_i) continue;
+            for (uint32_t p = 0; p < s.n_part; ++p)
+                for (uint32_t b = 0; b < M; ++b)
+                    for (uint32_t d = 0; d < nd; ++d, ++j) {
+                        RNG4 w = st.block(1u + (uint32_t)(j >> 2));
+                        float z0, z1;
+                        if ((j & 3u) < 2) boxmuller(w.w[0], w.w[1], z0, z1);
+                        else boxmuller(w.w[2], w.w[3], z0, z1);
+                        P[((size_t)(s.offset + p) * M + b) * nd + d] = (double)((j & 1u) ? z1 : z0);
+                    }
+        }
+        auto kin = [&]() {
+            double k = 0.;
+            for (double x : P) k += 0.5 * x * x;
+            return k;
+        };
+        const double h0 = WholeAction(path, actions, -1, R.data()) + kin();
+        WholeGradient(path, actions, -1, R.data(), G.data());
+        for (size_t i = 0; i < P.size(); ++i) P[i] -= 0.5 * eps * G[i];
+        for (uint32_t s = 0; s < n_steps; ++s) {
+            for (size_t i = 0; i < R.size(); ++i) R[i] += eps * P[i];
+            WholeGradient(path, actions, -1, R.data(), G.data());
+            const double f = s + 1 == n_steps ? 0.5 * eps : eps;
+            for (size_t i = 0; i < P.size(); ++i) P[i] -= f * G[i];
+        }
+        const double h1 = WholeAction(path, actions, -1, R.data()) + kin();
+        const double log_accept = -(h1 - h0);
+        const double logu = (double)logf_spec(u24(st.block(0).w[0]));
+        prop.swap(R);
+        return std::isfinite(log_accept) && !(log_accept < logu);
+    }
+    void Accept() override {
+        path.r = prop;
+        path.r_c = prop;
+        for (auto& s : path.species) path.InitRhoK(s);
+    }
+    void Reject() override {}
+};
+
 struct Observable {
     std::string name, type;
     uint32_t n_measure = 0, skip = 1;
@@ -1210,7 +1487,7 @@ struct Observable {
 struct Energy : Observable {
     Path& path;
     std::vector<std::unique_ptr<Action>>& actions;
-    bool measure_potential, use_thermal, use_virial;
+    bool measure_potential, use_thermal, use_virial, use_adjoint = false;
     uint32_t virial_window_size = 0;
     std::vector<double> energies, potentials;
 
@@ -1220,6 +1497,7 @@ struct Energy : Observable {
         skip = in.GetAttribute<uint32_t>("skip", 1);
         measure_potential = in.GetAttribute<bool>("measure_potential", false);
         use_virial = in.GetAttribute<bool>("use_virial_estimator", false);
+        use_adjoint = in.GetAttribute<bool>("use_adjoint_gradient", false);
         if (use_virial) {
             virial_window_size = in.GetAttribute<uint32_t>("virial_window_size", p.n_bead);
             use_thermal = in.GetAttribute<bool>("use_thermal_estimator", false);
@@ -1245,10 +1523,24 @@ struct Energy : Observable {
         double ke = 0.;
         for (auto& a : actions)
             if (a->type == "Kinetic") ke += a->VirialEnergy(virial_window_size);
+        std::vector<double> G;
+        if (use_adjoint) {  // exact gradient of every non-kinetic action, trap and Ewald forces included
+            G.assign((size_t)path.n_total * path.n_bead * path.n_d, 0.);
+            WholeGradient(path, actions, -2, path.r.data(), G.data());
+        }
         for (auto& s : path.species) {
             if (!(s.lambda > 0.)) continue;
             double centroid = 0.;
-            for (uint32_t p = 0; p < s.n_part; ++p) {
+            if (use_adjoint) {
+                for (uint32_t p = 0; p < s.n_part; ++p)
+                    for (uint32_t b = 0; b < path.n_bead; ++b) {
+                        double dr[3];
+                        path.Dr(path.GetR(s, p, b), path.GetR(s, p, 0), dr);
+                        const double* g = G.data() + ((size_t)(s.offset + p) * path.n_bead + b) * path.n_d;
+                        for (uint32_t d = 0; d < path.n_d; ++d) centroid += g[d] * dr[d];
+                    }
+            }
+            for (uint32_t p = 0; p < s.n_part && !use_adjoint; ++p) {
                 Particles parts{{s.s_i, p}};
                 for (uint32_t b = 0; b < path.n_bead; ++b) {
                     double dr[3], g[3];
@@ -1470,6 +1762,7 @@ struct Simulation {
         for (auto& m : in.GetChild("Moves").GetChildList("Move")) {
             std::string t = m.GetAttribute<std::string>("type");
             if (t == "Bisect") moves.emplace_back(new Bisect(*path, actions, m, mi, seed, chain));
+            else if (t == "HMC") moves.emplace_back(new HMC(*path, actions, m, mi, seed, chain));
             else throw InputError("unsupported move type '" + t + "'");
             ++mi;
         }
@@ -1700,6 +1993,28 @@ int oracle_virial_energy(void* h, uint32_t a, double window, double* out) {
     s->path->mode = orc::NEW_MODE;
     *out = s->actions.at(a)->VirialEnergy(window);
     return 0;
+}
+
+// Whole-ring action (action >= 0, or -1 for every action) and its exact gradient [n_total][M][n_d]
+// on the stored (mode 0) or working (mode 1) copy.
+int oracle_total_action(void* h, int a, int mode, double* out) {
+    try {
+        auto* s = S(h);
+        *out = orc::WholeAction(*s->path, s->actions, a, mode ? s->path->r.data() : s->path->r_c.data());
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+}
+
+int oracle_action_gradient_path(void* h, int a, int mode, double* out) {
+    try {
+        auto* s = S(h);
+        orc::WholeGradient(*s->path, s->actions, a, mode ? s->path->r.data() : s->path->r_c.data(), out);
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
 }
 
 int oracle_move_attempts(void* h, uint32_t m, uint64_t n) {

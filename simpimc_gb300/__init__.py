@@ -63,6 +63,9 @@ SIGNATURES = {
     "pimc_get_kvecs": (C.c_int, [_P, _DP]),
     "pimc_get_action": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _U32P, _U32P, C.c_uint32, C.c_uint32, C.c_int, _DP]),
     "pimc_get_action_gradient": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _U32P, _U32P, C.c_uint32, C.c_uint32, C.c_int, _DP]),
+    "pimc_get_action_gradient_exact": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _U32P, _U32P, C.c_uint32, C.c_uint32, C.c_int, _DP]),
+    "pimc_total_action": (C.c_int, [_P, C.c_int, C.c_int, _DP]),
+    "pimc_action_gradient_path": (C.c_int, [_P, C.c_int, C.c_int, _DP]),
     "pimc_dactiondbeta": (C.c_int, [_P, C.c_uint32, _DP]),
     "pimc_potential": (C.c_int, [_P, C.c_uint32, _DP]),
     "pimc_virial_energy": (C.c_int, [_P, C.c_uint32, C.c_double, _DP]),
@@ -245,6 +248,25 @@ class Simulation:
         out = np.zeros(self.n_d, dtype=np.float64)
         self._check(self._lib.pimc_get_action_gradient(self._h, action, b0, b1, sp.ctypes.data_as(_U32P), pi.ctypes.data_as(_U32P),
                                                        len(sp), level, mode, _dp(out)))
+        return out
+
+    def get_action_gradient_exact(self, action: int, b0: int, b1: int, particles, level: int = 0, mode: int = 1) -> np.ndarray:
+        sp, p = self._parts(particles)
+        out = np.zeros(self.n_d, dtype=np.float64)
+        self._check(self._lib.pimc_get_action_gradient_exact(self._h, action, b0, b1, sp.ctypes.data_as(_U32P), p.ctypes.data_as(_U32P),
+                                                             len(particles), level, mode, _dp(out)))
+        return out
+
+    def total_action(self, action: int = -1, mode: int = 0) -> float:
+        """Whole-ring action at level 0 of one action, or of every action (-1)."""
+        out = C.c_double()
+        self._check(self._lib.pimc_total_action(self._h, action, mode, C.byref(out)))
+        return out.value
+
+    def action_gradient_path(self, action: int = -1, mode: int = 0) -> np.ndarray:
+        """Exact dS/dR of total_action, shaped like the path (n_total, n_bead, n_d)."""
+        out = np.zeros((self.n_total, self.n_bead, self.n_d), dtype=np.float64)
+        self._check(self._lib.pimc_action_gradient_path(self._h, action, mode, _dp(out)))
         return out
 
     def dactiondbeta(self, action: int) -> float:

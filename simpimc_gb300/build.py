@@ -28,6 +28,7 @@ SOURCES = [
     SRC / "kernels" / "estimators.cu",
     SRC / "kernels" / "sweep.cu",
     SRC / "kernels" / "batch.cu",
+    SRC / "kernels" / "adjoint.cu",
     SRC / "noalloc.cu",
 ]
 

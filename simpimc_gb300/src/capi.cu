@@ -139,6 +139,26 @@ int pimc_get_action_gradient(pimc_ctx* ctx, uint32_t action, uint32_t b0, uint32
     });
 }
 
+int pimc_get_action_gradient_exact(pimc_ctx* ctx, uint32_t action, uint32_t b0, uint32_t b1, const uint32_t* species,
+                                   const uint32_t* particles, uint32_t n_particles, uint32_t level, int mode, double* out) {
+    if (!out || (n_particles && (!species || !particles))) return PIMC_ERR_ARG;
+    return Guard(ctx, [&](pimc::Context& c) {
+        double g[3];
+        c.ActionGradientAdjoint(action, b0, b1, species, particles, n_particles, level, mode, g);
+        for (uint32_t d = 0; d < c.sys.n_d; ++d) out[d] = g[d];
+    });
+}
+
+int pimc_total_action(pimc_ctx* ctx, int action, int mode, double* out) {
+    if (!out) return PIMC_ERR_ARG;
+    return Guard(ctx, [&](pimc::Context& c) { *out = c.TotalAction(action, mode); });
+}
+
+int pimc_action_gradient_path(pimc_ctx* ctx, int action, int mode, double* grad) {
+    if (!grad) return PIMC_ERR_ARG;
+    return Guard(ctx, [&](pimc::Context& c) { c.ActionGradientPath(action, mode, grad); });
+}
+
 int pimc_dactiondbeta(pimc_ctx* ctx, uint32_t action, double* out) {
     if (!out) return PIMC_ERR_ARG;
     return Guard(ctx, [&](pimc::Context& c) { *out = c.DActionDBeta(action); });

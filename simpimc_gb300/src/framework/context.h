@@ -72,6 +72,12 @@ struct MoveHost {
     double last_ratio = 0.;      // acceptance ratio of the last completed block
     uint64_t total_accept = 0;   // accepted attempts since construction
     uint64_t total_level0 = 0;   // attempts whose proposal reached the level-0 evaluation
+    // Hybrid Monte Carlo move (no reference counterpart): leapfrog on the whole path driven by
+    // the adjoint gradient of the total action.
+    int kind = 0;                // 0 Bisect, 1 HMC
+    double hmc_step = 0.01;
+    uint32_t hmc_steps = 10;
+    int hmc_species = -1;        // -1: every species moves
 };
 
 struct ObservableHost {
@@ -80,6 +86,7 @@ struct ObservableHost {
     uint64_t n_measure = 0;
     // Energy (energy_class.h:7-326)
     bool measure_potential = false, use_thermal = true, use_virial = false;
+    bool use_adjoint = false;  // virial centroid from the adjoint gradient of every non-kinetic action
     uint32_t virial_window = 0;
     std::vector<double> energies, potentials;
     // PairCorrelation (pair_correlation_class.h:7-124)
@@ -107,6 +114,7 @@ class Context {
     void SetPath(int which, const double* host_pos);  // [n_total][M][n_d]; which 0 old, 1 new, 2 both
     void GetPath(int which, double* host_pos);
     void InitRhoK();                                   // species_class.h:380-403 for every kept species
+    void ComputeRho(const double* pos, double2* out);  // the same densities of any position copy into `out`
     void GetRhoK(uint32_t species, double* out);       // [M][K][2]
     void GetKVecs(double* out);                        // [K][n_d]
 
@@ -118,6 +126,18 @@ class Context {
     double Potential(uint32_t a);
     double VirialEnergy(uint32_t a, double window);
     double VirialCentroid(uint32_t species);  // centroid term of energy_class.h:78-94 (before / 2 tau)
+
+    // --- adjoint: the whole-ring action at level 0 and its exact gradient dS/dR ---
+    double TotalAction(int a, int mode);                          // action a, or every action for a = -1
+    void ActionGradientPath(int a, int mode, double* host_grad);  // [n_total][M][n_d]
+    void ActionGradientAdjoint(uint32_t a, uint32_t b0, uint32_t b1, const uint32_t* sp, const uint32_t* p, uint32_t n,
+                               uint32_t level, int mode, double* out);
+    double VirialCentroidAdjoint(uint32_t species);
+    void HmcAttempts(uint32_t m, uint64_t n);
+    // Device-side pieces (a >= 0 one action, -1 every action, -2 every non-kinetic action).
+    double TotalActionDev(int a, const double* pos, const double2* rho);
+    void GradientDev(int a, const double* pos, const double2* rho, double* grad);  // [M][3][n_pad], overwritten
+    const double2* ScratchRho(const double* pos);                                    // densities of `pos`
 
     // --- moves, observables, algorithm ---
     void MoveAttempts(uint32_t m, uint64_t n);
@@ -181,6 +201,7 @@ class Context {
     std::vector<StageTable> stage_tables_;  // spline tables the sweep may copy into shared memory
     void BuildSweepTables();
     std::unique_ptr<DeviceBuffer> pos_, pos_new_, rho_, kidx_;
+    std::unique_ptr<DeviceBuffer> grad_, mom_, pos_save_, rho_scratch_;  // adjoint / HMC work arrays
     std::unique_ptr<DeviceBuffer> partials_, result_, bar_, err_, pairs_, rho_tmp_, parts_, kmag_dev_, sched_, accepts_;
     size_t partials_cap_ = 0, pairs_cap_ = 0, rho_tmp_cap_ = 0, parts_cap_ = 0;
 

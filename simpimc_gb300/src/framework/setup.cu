@@ -363,8 +363,19 @@ void Context::BuildMoves(const Input& in) {
         MoveHost h;
         h.name = m.GetAttribute<std::string>("name");
         h.type = m.GetAttribute<std::string>("type");
-        if (h.type != "Bisect") throw PimcError(kErrUnsupported, "unsupported move type '" + h.type + "'");
         if (moves.size() >= (size_t)kMaxMoves) throw PimcError(kErrUnsupported, "too many moves");
+        if (h.type == "HMC") {
+            // Hybrid Monte Carlo of the whole path (no reference counterpart).
+            h.kind = 1;
+            h.hmc_step = m.GetAttribute<double>("step_size", 0.01);
+            h.hmc_steps = m.GetAttribute<uint32_t>("n_steps", 10);
+            const std::string sp = m.GetAttribute<std::string>("species", "");
+            h.hmc_species = sp.empty() ? -1 : (int)SpeciesIndex(species_names, sp);
+            if (!(h.hmc_step > 0.) || h.hmc_steps == 0) throw PimcError(kErrInput, "HMC needs step_size > 0 and n_steps > 0");
+            moves.push_back(h);
+            continue;
+        }
+        if (h.type != "Bisect") throw PimcError(kErrUnsupported, "unsupported move type '" + h.type + "'");
         MoveDev& d = h.dev;
         d.species = SpeciesIndex(species_names, m.GetAttribute<std::string>("species"));
         d.n_level = m.GetAttribute<uint32_t>("n_level");
@@ -403,6 +414,7 @@ void Context::BuildObservables(const Input& in) {
             h.kind = 0;
             h.measure_potential = o.GetAttribute<bool>("measure_potential", false);
             h.use_virial = o.GetAttribute<bool>("use_virial_estimator", false);
+            h.use_adjoint = o.GetAttribute<bool>("use_adjoint_gradient", false);
             if (h.use_virial) {
                 h.virial_window = o.GetAttribute<uint32_t>("virial_window_size", sys.M);
                 h.use_thermal = o.GetAttribute<bool>("use_thermal_estimator", false);

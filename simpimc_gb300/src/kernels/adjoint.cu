@@ -1,0 +1,449 @@
+// Exact gradient dS/dR of the whole-ring action at level 0 (the "adjoint" of the action
+// evaluation), the total action it differentiates, the virial centroid term built on it, and a
+// hybrid Monte Carlo path move driven by it. FP64 throughout.
+//
+// The action of one species' path, summed over every link b -> b+1 of the ring (level 0):
+//   Kinetic        sum_b phi(r_{b+1} - r_b),  phi(d) = sum_c image(d_c) + |d|^2 / (4 lambda tau)
+//                  (kinetic_class.h:105-122 with the free-particle splines of free_spline_class.h)
+//   HarmonicTrap   cofactor_a sum_b |r_b|^2                                   (trap_class.h:40-62)
+//   BarePairAction sum_pairs sum_b tau (V(r_b) + V(r_{b+1})) / 2  (pair_action_class.h:267-302,
+//                  bare_pair_action_class.h:98-149; V clamped to the table's grid) plus, with the
+//                  Ewald split, tau sum_b sum_k v_k Re(rho_a(k,b) conj(rho_b(k,b))) (x 2 for a != b)
+// The reference differentiates only parts of this (kinetic_class.h:125-144 exactly; the pair
+// short-range part by central differences with eps = 1e-4, pair_action_class.h:135-155; the trap
+// and the Ewald part not at all). Here every term has its analytic derivative:
+//   kinetic   dS/dr_b = phi'(r_b - r_{b-1}) - phi'(r_{b+1} - r_b)
+//   trap      2 cofactor_a r_b
+//   pair      tau sum_q V'(|r_pq|) r_pq / |r_pq|      (zero where the table clamps V flat)
+//   Ewald     -2 tau sum_k v_k k Im(conj(rho_other(k,b)) exp(i k.r_b))
+// where rho_other is the partner species' density (the own species' for a homologous action).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "../common/philox.h"
+#include "../framework/context.h"
+#include "actions.cuh"
+#include "reduce.cuh"
+
+namespace pimc {
+namespace {
+
+/// d/dx of EvalCubic: zero outside the grid, where EvalCubic holds the end value.
+__device__ __forceinline__ double EvalCubicDeriv(const CubicTable& t, double x) {
+    if (x < t.x0 || x > t.x1) return 0.;
+    int i;
+    if (t.uniform) {
+        i = (int)floor((x - t.x0) * t.inv_dx);
+        i = min(max(i, 0), t.n - 2);
+    } else {
+        int j = (int)floor((x - t.x0) * t.inv_dx);
+        j = min(max(j, 0), t.n_bucket - 1);
+        i = t.bucket[j];
+        while (i < t.n - 2 && __ldg(&t.x[i + 1]) <= x) ++i;
+    }
+    const Cubic4 c = t.c[i];
+    const double u = x - __ldg(&t.x[i]);
+    return c.c1 + u * (2. * c.c2 + 3. * u * c.c3);
+}
+
+/// Per-bead pair potential V(r) of the primitive action (one half of CalcV's two ends) and dV/dr,
+/// with the reference's two clamps (bare_pair_action_class.h:98-111).
+__device__ __forceinline__ void PairVBead(const PairDev& pa, double r, double& v, double& dv) {
+    const bool in1 = r >= pa.r_v_min && r <= pa.r_v_max;
+    const double r1 = fmin(fmax(r, pa.r_v_min), pa.r_v_max);
+    if (pa.is_coulomb) {
+        v = 1. / r1;
+        dv = in1 ? -1. / (r1 * r1) : 0.;
+    } else {
+        v = EvalCubic(pa.v_r, r1);
+        dv = in1 ? EvalCubicDeriv(pa.v_r, r1) : 0.;
+    }
+    if (pa.use_long_range) {
+        const bool in2 = r1 >= pa.r_vl_min && r1 <= pa.r_vl_max;
+        const double r2 = fmin(fmax(r1, pa.r_vl_min), pa.r_vl_max);
+        v -= EvalCubic(pa.v_long_r, r2);
+        if (in1 && in2) dv -= EvalCubicDeriv(pa.v_long_r, r2);
+    }
+}
+
+__device__ __forceinline__ size_t GIdx(uint32_t b, uint32_t d, uint32_t g, uint32_t np) { return ((size_t)b * 3 + d) * np + g; }
+
+__global__ void KineticGradKernel(const SystemDev sys, const double* __restrict__ pos, const KineticDev k, double* __restrict__ grad) {
+    const uint32_t ns = sys.sp_n[k.species], M = sys.M, np = sys.n_pad, off = sys.sp_off[k.species];
+    const double i4lt = k.i4lt_level[0];
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (uint64_t)ns * M; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = (uint32_t)(i / ns), g = off + (uint32_t)(i % ns);
+        const uint32_t bm = b == 0 ? M - 1 : b - 1, bp = b + 1 == M ? 0 : b + 1;
+        for (uint32_t d = 0; d < sys.n_d; ++d) {
+            const double x = PosAt(pos, np, b, d, g);
+            const double dm = MinImage(x - PosAt(pos, np, bm, d, g), sys.L, sys.iL);
+            const double dp = MinImage(PosAt(pos, np, bp, d, g) - x, sys.L, sys.iL);
+            double fm = 2. * dm * i4lt, fp = 2. * dp * i4lt;
+            if (k.has_images) {
+                fm += EvalCubicDeriv(k.image[0], dm);
+                fp += EvalCubicDeriv(k.image[0], dp);
+            }
+            grad[GIdx(b, d, g, np)] += fm - fp;
+        }
+    }
+}
+
+__global__ void TrapGradKernel(const SystemDev sys, const double* __restrict__ pos, const TrapDev t, double* __restrict__ grad) {
+    const uint32_t ns = sys.sp_n[t.species], M = sys.M, np = sys.n_pad, off = sys.sp_off[t.species];
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (uint64_t)ns * M; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = (uint32_t)(i / ns), g = off + (uint32_t)(i % ns);
+        for (uint32_t d = 0; d < sys.n_d; ++d) grad[GIdx(b, d, g, np)] += 2. * t.cofactor_a * PosAt(pos, np, b, d, g);
+    }
+}
+
+/// Short-range pair forces: one thread per (slice, particle of either species of the action).
+__global__ void PairGradKernel(const SystemDev sys, const double* __restrict__ pos, const PairDev pa, double* __restrict__ grad) {
+    const uint32_t na = sys.sp_n[pa.sa], nb = sys.sp_n[pa.sb], M = sys.M, np = sys.n_pad, n_d = sys.n_d;
+    const bool hom = pa.sa == pa.sb;
+    const uint32_t ng = hom ? na : na + nb;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (uint64_t)ng * M; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = (uint32_t)(i / ng), j = (uint32_t)(i % ng);
+        const bool in_a = j < na;
+        const uint32_t g = in_a ? sys.sp_off[pa.sa] + j : sys.sp_off[pa.sb] + (j - na);
+        const uint32_t q0 = in_a ? sys.sp_off[pa.sb] : sys.sp_off[pa.sa];
+        const uint32_t nq = in_a ? nb : na;
+        double rg[3], G[3] = {0., 0., 0.};
+        for (uint32_t d = 0; d < n_d; ++d) rg[d] = PosAt(pos, np, b, d, g);
+        for (uint32_t qi = 0; qi < nq; ++qi) {
+            const uint32_t q = q0 + qi;
+            if (q == g) continue;
+            double dr[3], r2 = 0.;
+            for (uint32_t d = 0; d < n_d; ++d) {
+                dr[d] = MinImage(rg[d] - PosAt(pos, np, b, d, q), sys.L, sys.iL);
+                r2 += dr[d] * dr[d];
+            }
+            const double r = sqrt(r2);
+            double v, dv;
+            PairVBead(pa, r, v, dv);
+            if (r > 0.) {
+                const double f = sys.tau * dv / r;
+                for (uint32_t d = 0; d < n_d; ++d) G[d] += f * dr[d];
+            }
+        }
+        for (uint32_t d = 0; d < n_d; ++d) grad[GIdx(b, d, g, np)] += G[d];
+    }
+}
+
+/// Ewald forces: one warp per (slice, particle), lanes over the stored k-vectors; the particle's
+/// per-dimension phase rows sit in shared memory.
+__global__ void EwaldGradKernel(const SystemDev sys, const double* __restrict__ pos, const PairDev pa, const double2* __restrict__ rho_a,
+                                const double2* __restrict__ rho_b, double* __restrict__ grad) {
+    extern __shared__ double2 tab[];  // [warps][3][stride]
+    const int stride = max(max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
+    const uint32_t warps = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    double2* my = tab + (size_t)w * 3 * stride;
+    const uint32_t na = sys.sp_n[pa.sa], nb = sys.sp_n[pa.sb], M = sys.M, np = sys.n_pad, K = sys.K, n_d = sys.n_d;
+    const bool hom = pa.sa == pa.sb;
+    const uint32_t ng = hom ? na : na + nb;
+    for (uint64_t it = (uint64_t)blockIdx.x * warps + w; it < (uint64_t)ng * M; it += (uint64_t)gridDim.x * warps) {
+        const uint32_t b = (uint32_t)(it / ng), j = (uint32_t)(it % ng);
+        const bool in_a = j < na;
+        const uint32_t g = in_a ? sys.sp_off[pa.sa] + j : sys.sp_off[pa.sb] + (j - na);
+        const double2* rho = (in_a ? rho_b : rho_a) + (size_t)b * K;
+        __syncwarp();
+        if (lane < n_d) PhaseRow(PosAt(pos, np, b, lane, g), sys.box[lane], sys.max_index[lane], my + (size_t)lane * stride);
+        __syncwarp();
+        double acc[3] = {0., 0., 0.};
+        for (uint32_t k = lane; k < K; k += 32) {
+            const int32_t pk = sys.kidx[k];
+            const double2 e = PhaseProduct(my, stride, n_d, pk);
+            const double2 rk = rho[k];
+            const double f = pa.v_long_k[k] * (rk.x * e.y - rk.y * e.x);  // v_k Im(conj(rho) e)
+            for (uint32_t d = 0; d < n_d; ++d) acc[d] += f * (double)KIdx(pk, (int)d) * sys.box[d];
+        }
+        for (uint32_t d = 0; d < n_d; ++d) {
+            const double s = WarpSum(acc[d]);
+            if (lane == 0) grad[GIdx(b, d, g, np)] += -2. * sys.tau * s;
+        }
+    }
+}
+
+/// HMC momenta: standard normals for every coordinate of the moving particles, in the path order
+/// (moving particle, slice, dimension); normal j is component j % 4 of Philox block 1 + j / 4
+/// of the attempt's stream (two Box-Muller pairs per block).
+__global__ void HmcMomentaKernel(const SystemDev sys, MoveStream st, const uint32_t* __restrict__ moving, uint32_t n_moving,
+                                 double* __restrict__ mom) {
+    const uint32_t M = sys.M, np = sys.n_pad, n_d = sys.n_d;
+    const uint64_t n = (uint64_t)n_moving * M * n_d;
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t d = (uint32_t)(j % n_d), b = (uint32_t)((j / n_d) % M), gi = (uint32_t)(j / ((uint64_t)n_d * M));
+        const Philox4 w = st.Block(1u + (uint32_t)(j >> 2));
+        float z0, z1;
+        const uint32_t c = (uint32_t)(j & 3u);
+        if (c < 2) BoxMullerF(w.v[0], w.v[1], z0, z1);
+        else BoxMullerF(w.v[2], w.v[3], z0, z1);
+        mom[GIdx(b, d, moving[gi], np)] = (double)((c & 1u) ? z1 : z0);
+    }
+}
+
+__global__ void AxpyKernel(double* __restrict__ y, const double* __restrict__ x, double a, uint64_t n) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) y[i] += a * x[i];
+}
+
+int Blocks(const Context& c, uint64_t n, int threads) {
+    const uint64_t want = (n + threads - 1) / threads;
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)c.n_sm * 16));
+}
+
+}  // namespace
+
+const double2* Context::ScratchRho(const double* pos) {
+    if (!rho_slots || !sys.K) return nullptr;
+    const size_t n = (size_t)rho_slots * sys.M * sys.K;
+    if (!rho_scratch_ || rho_scratch_->bytes < n * sizeof(double2)) rho_scratch_.reset(new DeviceBuffer(n * sizeof(double2)));
+    ComputeRho(pos, rho_scratch_->as<double2>());
+    return rho_scratch_->as<double2>();
+}
+
+/// Selection: a >= 0 one action, -1 every action, -2 every non-kinetic action.
+static bool Selected(const ActionHost& ah, int sel, int i) {
+    if (ah.is_importance_weight) return false;
+    if (sel >= 0) return sel == i;
+    if (sel == -2) return ah.kind != 0;
+    return true;
+}
+
+double Context::TotalActionDev(int a, const double* pos, const double2* rho) {
+    const uint32_t M = sys.M, np = sys.n_pad, n_d = sys.n_d;
+    const double L = sys.L, iL = sys.iL, tau = sys.tau;
+    double total = 0.;
+    for (size_t i = 0; i < actions.size(); ++i) {
+        const ActionHost& ah = actions[i];
+        if (!Selected(ah, a, (int)i)) continue;
+        double part = 0.;
+        if (ah.kind == 0) {
+            const KineticDev k = sys.kinetic[ah.index];
+            const uint32_t ns = sys.sp_n[k.species], off = sys.sp_off[k.species];
+            const double i4lt = k.i4lt_level[0];
+            SumItems<1>(*this, (uint64_t)ns * M, [=] __device__(uint64_t it, double* v) {
+                const uint32_t b = (uint32_t)(it / ns), g = off + (uint32_t)(it % ns), bp = b + 1 == M ? 0 : b + 1;
+                double dr[3];
+                for (uint32_t d = 0; d < n_d; ++d) dr[d] = MinImage(PosAt(pos, np, bp, d, g) - PosAt(pos, np, b, d, g), L, iL);
+                v[0] = -LogRhoFree(dr, n_d, i4lt, &k.image[0], k.has_images);
+            }, &part);
+        } else if (ah.kind == 1) {
+            const TrapDev t = sys.trap[ah.index];
+            const uint32_t ns = sys.sp_n[t.species], off = sys.sp_off[t.species];
+            SumItems<1>(*this, (uint64_t)ns * M, [=] __device__(uint64_t it, double* v) {
+                const uint32_t b = (uint32_t)(it / ns), g = off + (uint32_t)(it % ns);
+                double s = 0.;
+                for (uint32_t d = 0; d < n_d; ++d) {
+                    const double x = PosAt(pos, np, b, d, g);
+                    s += x * x;
+                }
+                v[0] = t.cofactor_a * s;
+            }, &part);
+        } else {
+            const PairDev pa = sys.pair[ah.index];
+            if (pa.is_constant) continue;  // pair_action_class.h:268
+            const uint32_t na = sys.sp_n[pa.sa], nb = sys.sp_n[pa.sb], oa = sys.sp_off[pa.sa], ob = sys.sp_off[pa.sb];
+            const bool hom = pa.sa == pa.sb;
+            // tau V(|d_b|) per pair and slice, d_b the minimum image on that slice: the two half
+            // links of CalcU that meet at a bead, with each end's distance taken as its own minimum
+            // image (the function PairGradKernel differentiates).
+            SumItems<1>(*this, (uint64_t)na * nb * M, [=] __device__(uint64_t it, double* v) {
+                const uint32_t q = (uint32_t)(it % nb);
+                const uint64_t r0 = it / nb;
+                const uint32_t p = (uint32_t)(r0 % na), b = (uint32_t)(r0 / na);
+                v[0] = 0.;
+                if (hom && q <= p) return;
+                double r2 = 0.;
+                for (uint32_t d = 0; d < n_d; ++d) {
+                    const double x = MinImage(PosAt(pos, np, b, d, ob + q) - PosAt(pos, np, b, d, oa + p), L, iL);
+                    r2 += x * x;
+                }
+                double vb, dvb;
+                PairVBead(pa, sqrt(r2), vb, dvb);
+                v[0] = tau * vb;
+            }, &part);
+            if (pa.use_long_range && rho) {
+                const double2* ra = rho + (size_t)sys.sp_rho[pa.sa] * M * sys.K;
+                const double2* rb = rho + (size_t)sys.sp_rho[pa.sb] * M * sys.K;
+                const uint32_t K = sys.K;
+                double lr = 0.;
+                SumItems<1>(*this, (uint64_t)M * K, [=] __device__(uint64_t it, double* v) {
+                    const double2 x = ra[it], y = rb[it];
+                    v[0] = pa.v_long_k[it % K] * (x.x * y.x + x.y * y.y);
+                }, &lr);
+                part += (hom ? 1. : 2.) * tau * lr;
+            }
+        }
+        total += part;
+    }
+    return total;
+}
+
+void Context::GradientDev(int a, const double* pos, const double2* rho, double* grad) {
+    const size_t n = (size_t)sys.M * 3 * sys.n_pad;
+    CudaCheck(cudaMemsetAsync(grad, 0, n * sizeof(double), stream), "grad clear");
+    const int th = 256;
+    for (size_t i = 0; i < actions.size(); ++i) {
+        const ActionHost& ah = actions[i];
+        if (!Selected(ah, a, (int)i)) continue;
+        if (ah.kind == 0) {
+            const KineticDev k = sys.kinetic[ah.index];
+            KineticGradKernel<<<Blocks(*this, (uint64_t)sys.sp_n[k.species] * sys.M, th), th, 0, stream>>>(sys, pos, k, grad);
+        } else if (ah.kind == 1) {
+            const TrapDev t = sys.trap[ah.index];
+            TrapGradKernel<<<Blocks(*this, (uint64_t)sys.sp_n[t.species] * sys.M, th), th, 0, stream>>>(sys, pos, t, grad);
+        } else {
+            const PairDev pa = sys.pair[ah.index];
+            if (pa.is_constant) continue;
+            const uint64_t ng = (uint64_t)(pa.sa == pa.sb ? sys.sp_n[pa.sa] : sys.sp_n[pa.sa] + sys.sp_n[pa.sb]) * sys.M;
+            PairGradKernel<<<Blocks(*this, ng, th), th, 0, stream>>>(sys, pos, pa, grad);
+            if (pa.use_long_range && rho && sys.K) {
+                const double2* ra = rho + (size_t)sys.sp_rho[pa.sa] * sys.M * sys.K;
+                const double2* rb = rho + (size_t)sys.sp_rho[pa.sb] * sys.M * sys.K;
+                const int stride = std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
+                const int warps = 8;
+                const size_t smem = (size_t)warps * 3 * stride * sizeof(double2);
+                const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((ng + warps - 1) / warps, (uint64_t)n_sm * 8));
+                EwaldGradKernel<<<blocks, warps * 32, smem, stream>>>(sys, pos, pa, ra, rb, grad);
+            }
+        }
+        CudaCheck(cudaGetLastError(), "gradient launch");
+    }
+}
+
+double Context::TotalAction(int a, int mode) {
+    EnsureFP64();
+    if (a >= (int)actions.size() || a < -1) throw PimcError(kErrArg, "action index out of range");
+    const double* pos = mode ? sys.pos_new : sys.pos;
+    return TotalActionDev(a, pos, ScratchRho(pos));
+}
+
+void Context::ActionGradientPath(int a, int mode, double* host) {
+    EnsureFP64();
+    if (a >= (int)actions.size() || a < -1) throw PimcError(kErrArg, "action index out of range");
+    if (!host) throw PimcError(kErrArg, "null output");
+    const double* pos = mode ? sys.pos_new : sys.pos;
+    const size_t n = (size_t)sys.M * 3 * sys.n_pad;
+    if (!grad_ || grad_->bytes < n * sizeof(double)) grad_.reset(new DeviceBuffer(n * sizeof(double)));
+    GradientDev(a, pos, ScratchRho(pos), grad_->as<double>());
+    std::vector<double> g(n);
+    CudaCheck(cudaMemcpyAsync(g.data(), grad_->ptr, n * sizeof(double), cudaMemcpyDeviceToHost, stream), "gradient download");
+    Sync();
+    for (uint32_t gi = 0; gi < sys.n_total; ++gi)
+        for (uint32_t b = 0; b < sys.M; ++b)
+            for (uint32_t d = 0; d < sys.n_d; ++d) host[((size_t)gi * sys.M + b) * sys.n_d + d] = g[((size_t)b * 3 + d) * sys.n_pad + gi];
+}
+
+/// Action::GetActionGradient with the exact gradient: the sum of dS_a/dr over the listed
+/// particles of the action's species and slices b0 .. b1-1 (level 0 only).
+void Context::ActionGradientAdjoint(uint32_t a, uint32_t b0, uint32_t b1, const uint32_t* sp, const uint32_t* p, uint32_t n, uint32_t level,
+                                    int mode, double* out) {
+    if (a >= actions.size()) throw PimcError(kErrArg, "action index out of range");
+    if (level != 0) throw PimcError(kErrUnsupported, "the exact gradient is defined at level 0");
+    if (b1 < b0) throw PimcError(kErrArg, "b1 < b0");
+    std::vector<double> g((size_t)sys.n_total * sys.M * sys.n_d);
+    ActionGradientPath((int)a, mode, g.data());
+    for (uint32_t d = 0; d < sys.n_d; ++d) out[d] = 0.;
+    const auto& sl = actions[a].species_list;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (sp[i] >= sys.S || p[i] >= sys.sp_n[sp[i]]) throw PimcError(kErrArg, "particle out of range");
+        if (std::find(sl.begin(), sl.end(), sp[i]) == sl.end()) continue;
+        const uint32_t gi = sys.sp_off[sp[i]] + p[i];
+        for (uint32_t b = b0; b < b1; ++b)
+            for (uint32_t d = 0; d < sys.n_d; ++d) out[d] += g[((size_t)gi * sys.M + (b % sys.M)) * sys.n_d + d];
+    }
+}
+
+/// Virial centroid term of energy_class.h:78-94 with the exact gradient of every non-kinetic
+/// action (trap and Ewald forces included): sum over the species' particles and slices of
+/// dS/dr_{p,b} . (r_{p,b} - r_{p,0}).
+double Context::VirialCentroidAdjoint(uint32_t s) {
+    EnsureFP64();
+    const size_t n = (size_t)sys.M * 3 * sys.n_pad;
+    if (!grad_ || grad_->bytes < n * sizeof(double)) grad_.reset(new DeviceBuffer(n * sizeof(double)));
+    double* grad = grad_->as<double>();
+    GradientDev(-2, sys.pos, ScratchRho(sys.pos), grad);
+    const double* pos = sys.pos;
+    const uint32_t ns = sys.sp_n[s], off = sys.sp_off[s], M = sys.M, np = sys.n_pad, n_d = sys.n_d;
+    const double L = sys.L, iL = sys.iL;
+    double total = 0.;
+    SumItems<1>(*this, (uint64_t)ns * M, [=] __device__(uint64_t it, double* v) {
+        const uint32_t b = (uint32_t)(it / ns), g = off + (uint32_t)(it % ns);
+        double s2 = 0.;
+        for (uint32_t d = 0; d < n_d; ++d)
+            s2 += grad[GIdx(b, d, g, np)] * MinImage(PosAt(pos, np, b, d, g) - PosAt(pos, np, 0, d, g), L, iL);
+        v[0] = s2;
+    }, &total);
+    return total;
+}
+
+/// Hybrid Monte Carlo over the whole path of the moving species: momenta P ~ N(0, 1) per
+/// coordinate, `hmc_steps` leapfrog steps of size `hmc_step` on H = S(R) + |P|^2 / 2 with the
+/// exact gradient, accepted with probability min(1, exp(-dH)) against the same log-uniform draw
+/// layout as a bisection level (Philox block 0, word 0).
+void Context::HmcAttempts(uint32_t m, uint64_t n_att) {
+    MoveHost& mh = moves[m];
+    EnsureFP64();
+    const size_t n = (size_t)sys.M * 3 * sys.n_pad;
+    auto ensure = [&](std::unique_ptr<DeviceBuffer>& b) {
+        if (!b || b->bytes < n * sizeof(double)) b.reset(new DeviceBuffer(n * sizeof(double)));
+    };
+    ensure(grad_);
+    ensure(mom_);
+    ensure(pos_save_);
+    double* grad = grad_->as<double>();
+    double* mom = mom_->as<double>();
+    double* pos = sys.pos;
+    std::vector<uint32_t> moving;
+    for (uint32_t s = 0; s < sys.S; ++s)
+        if (mh.hmc_species < 0 || (uint32_t)mh.hmc_species == s)
+            for (uint32_t p = 0; p < sys.sp_n[s]; ++p) moving.push_back(sys.sp_off[s] + p);
+    uint32_t* dmov = Parts(moving.size());
+    CudaCheck(cudaMemcpyAsync(dmov, moving.data(), moving.size() * 4, cudaMemcpyHostToDevice, stream), "moving upload");
+    const double eps = mh.hmc_step;
+    const int th = 256;
+    auto kinetic_energy = [&]() {
+        double k = 0.;
+        SumItems<1>(*this, n, [=] __device__(uint64_t i, double* v) { v[0] = 0.5 * mom[i] * mom[i]; }, &k);
+        return k;
+    };
+    for (uint64_t it = 0; it < n_att; ++it) {
+        const MoveStream st{seed, chain, m, mh.attempts};
+        CudaCheck(cudaMemsetAsync(mom, 0, n * sizeof(double), stream), "momenta clear");
+        const uint64_t nm = (uint64_t)moving.size() * sys.M * sys.n_d;
+        HmcMomentaKernel<<<Blocks(*this, nm, th), th, 0, stream>>>(sys, st, dmov, (uint32_t)moving.size(), mom);
+        CudaCheck(cudaGetLastError(), "momenta launch");
+        CudaCheck(cudaMemcpyAsync(pos_save_->ptr, pos, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "save path");
+        const double h0 = TotalActionDev(-1, pos, ScratchRho(pos)) + kinetic_energy();
+        // Leapfrog: half kick, (drift, kick) x steps with a half final kick.
+        GradientDev(-1, pos, ScratchRho(pos), grad);
+        AxpyKernel<<<Blocks(*this, n, th), th, 0, stream>>>(mom, grad, -0.5 * eps, n);
+        for (uint32_t s = 0; s < mh.hmc_steps; ++s) {
+            AxpyKernel<<<Blocks(*this, n, th), th, 0, stream>>>(pos, mom, eps, n);
+            GradientDev(-1, pos, ScratchRho(pos), grad);
+            AxpyKernel<<<Blocks(*this, n, th), th, 0, stream>>>(mom, grad, s + 1 == mh.hmc_steps ? -0.5 * eps : -eps, n);
+        }
+        CudaCheck(cudaGetLastError(), "leapfrog launch");
+        const double h1 = TotalActionDev(-1, pos, ScratchRho(pos)) + kinetic_energy();
+        const double log_accept = -(h1 - h0);
+        const Philox4 w0 = st.Block(0);
+        const double logu = (double)LogF(U24(w0.v[0]));
+        const bool accept = std::isfinite(log_accept) && !(log_accept < logu);
+        if (accept) {
+            CudaCheck(cudaMemcpyAsync(sys.pos_new, pos, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "commit");
+            InitRhoK();
+            mh.block_accept++;
+            mh.total_accept++;
+        } else {
+            CudaCheck(cudaMemcpyAsync(pos, pos_save_->ptr, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "restore");
+        }
+        mh.attempts++;
+        mh.block_attempt++;
+        mh.total_level0++;
+    }
+    Sync();
+    fp64_valid = true;
+    dd_valid = false;
+}
+
+}  // namespace pimc

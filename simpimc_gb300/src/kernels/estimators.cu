@@ -10,60 +10,11 @@
 
 #include "../framework/context.h"
 #include "actions.cuh"
+#include "reduce.cuh"
 
 namespace pimc {
 
 namespace {
-
-constexpr int kSumThreads = 256;
-
-template <int N, class F>
-__global__ void __launch_bounds__(kSumThreads) SumItemsKernel(uint64_t n, F f, double* __restrict__ partials) {
-    __shared__ double red[kSumThreads / 32];
-    double acc[N];
-#pragma unroll
-    for (int j = 0; j < N; ++j) acc[j] = 0.;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        double v[N];
-        f(i, v);
-#pragma unroll
-        for (int j = 0; j < N; ++j) acc[j] += v[j];
-    }
-#pragma unroll
-    for (int j = 0; j < N; ++j) {
-        const double s = BlockSum(acc[j], red);
-        if (threadIdx.x == 0) partials[(size_t)blockIdx.x * N + j] = s;
-    }
-}
-
-template <int N>
-__global__ void FinalSumKernel(const double* __restrict__ partials, int nb, double* __restrict__ out) {
-    const int lane = threadIdx.x;
-#pragma unroll
-    for (int j = 0; j < N; ++j) {
-        double t = 0.;
-        for (int b = lane; b < nb; b += 32) t += partials[(size_t)b * N + j];
-        t = WarpSum(t);
-        if (lane == 0) out[j] = t;
-    }
-}
-
-/// Sum f(i) over i in [0, n) for N-component items; result copied to host `out`.
-template <int N, class F>
-void SumItems(Context& c, uint64_t n, F f, double* out) {
-    for (int j = 0; j < N; ++j) out[j] = 0.;
-    if (n == 0) return;
-    const uint64_t want = (n + kSumThreads - 1) / kSumThreads;
-    const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)c.n_sm * 8));
-    double* part = c.Partials((size_t)blocks * N);
-    SumItemsKernel<N><<<blocks, kSumThreads, 0, c.stream>>>(n, f, part);
-    CudaCheck(cudaGetLastError(), "sum kernel launch");
-    FinalSumKernel<N><<<1, 32, 0, c.stream>>>(part, blocks, c.Result());
-    CudaCheck(cudaGetLastError(), "final sum launch");
-    CudaCheck(cudaMemcpyAsync(out, c.Result(), N * sizeof(double), cudaMemcpyDeviceToHost, c.stream), "read result");
-    c.Sync();
-}
 
 __device__ __forceinline__ uint32_t BeadLoop(uint32_t b, uint32_t M) { return b >= M ? b - M : b; }
 
@@ -180,7 +131,7 @@ __global__ void StructureFactorKernel(const SystemDev sys, const double* __restr
 }  // namespace
 
 // ---------------------------------------------------------------------------------------------
-void Context::InitRhoK() {
+void Context::ComputeRho(const double* pos, double2* out) {
     if (!rho_slots || !sys.K) return;
     std::vector<int> slot_species(rho_slots, 0);
     for (uint32_t s = 0; s < sys.S; ++s)
@@ -189,9 +140,17 @@ void Context::InitRhoK() {
     CudaCheck(cudaMemcpyAsync(dss, slot_species.data(), rho_slots * sizeof(int), cudaMemcpyHostToDevice, stream), "slot upload");
     const int stride = std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
     const size_t smem = (size_t)kRhoChunk * 3 * stride * sizeof(double2);
-    InitRhoKernel<<<dim3(sys.M, rho_slots), 256, smem, stream>>>(sys, reinterpret_cast<const int*>(dss));
+    SystemDev s2 = sys;
+    s2.pos = const_cast<double*>(pos);
+    s2.rho_k = out;
+    InitRhoKernel<<<dim3(sys.M, rho_slots), 256, smem, stream>>>(s2, reinterpret_cast<const int*>(dss));
     CudaCheck(cudaGetLastError(), "init rho_k launch");
     Sync();
+}
+
+void Context::InitRhoK() {
+    if (!rho_slots || !sys.K) return;
+    ComputeRho(sys.pos, sys.rho_k);
     dd_valid = false;
 }
 
@@ -705,7 +664,7 @@ void Context::ObservableAccumulate(uint32_t oi) {
                 if (actions[i].kind == 0) ke += VirialEnergy((uint32_t)i, (double)o.virial_window);
             for (uint32_t s = 0; s < sys.S; ++s) {
                 if (!(sys.sp_lambda[s] > 0.)) continue;
-                ke += VirialCentroid(s) / (2. * sys.tau);
+                ke += (o.use_adjoint ? VirialCentroidAdjoint(s) : VirialCentroid(s)) / (2. * sys.tau);
                 for (size_t i = 0; i < actions.size(); ++i)
                     if (actions[i].kind == 0)
                         for (uint32_t x : actions[i].species_list)

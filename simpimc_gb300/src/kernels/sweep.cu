@@ -963,8 +963,23 @@ void Context::BuildSweepTables() {
 void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep) {
     if (n_entries == 0 || n_rep == 0) return;
     if (n_entries > 1024) throw PimcError(kErrArg, "schedule longer than 1024 entries");
-    for (uint32_t e = 0; e < n_entries; ++e)
+    bool any_hmc = false;
+    for (uint32_t e = 0; e < n_entries; ++e) {
         if (mv[e] >= moves.size()) throw PimcError(kErrArg, "move index out of range");
+        any_hmc |= moves[mv[e]].kind == 1;
+    }
+    if (any_hmc) {  // HMC moves run their own launches; bisection entries between them keep the sweep kernel
+        for (uint64_t r = 0; r < n_rep; ++r)
+            for (uint32_t e = 0; e < n_entries; ++e) {
+                if (moves[mv[e]].kind == 1) {
+                    HmcAttempts(mv[e], counts[e]);
+                } else {
+                    const uint64_t c1 = counts[e];
+                    Sweep(&mv[e], &c1, 1, 1);
+                }
+            }
+        return;
+    }
     BuildSweepTables();
     // Move descriptors, rebuilt when a level changes (adaptive bisection between blocks).
     uint32_t max_level = 1;

@@ -211,3 +211,56 @@ def test_table_round_trip(tmp_path):
     text = (tmp_path / "t.pat").read_text().split()
     i = text.index("v/diag/v_long_k_0")
     assert float(text[i + 2]) == ds["v/diag/v_long_k_0"]
+
+
+def _fd_check(o, path, coords, h=1e-5):
+    g = o.action_gradient_path()
+    out = []
+    for i in coords:
+        pp = path.copy()
+        pp[i] += h
+        o.set_path(pp)
+        sp = o.total_action()
+        pp[i] -= 2 * h
+        o.set_path(pp)
+        sm = o.total_action()
+        out.append((g[i], (sp - sm) / (2 * h)))
+    o.set_path(path)
+    return out
+
+
+def test_oracle_exact_gradient_matches_central_differences(oracle_mod, tmp_path):
+    """The oracle's analytic dS/dR (kinetic, trap, pair, Ewald) against central differences of
+    its whole-ring action, h = 1e-5: agreement within the O(h^2) truncation."""
+    from simpimc_gb300.configs import electron_gas, trapped_coulomb
+    rng = np.random.default_rng(11)
+    xml, path = trapped_coulomb(tmp_path, n_part=4, n_bead=8, n_level=2, seed=3)
+    o = oracle_mod.OracleSim(xml, base_dir=tmp_path)
+    o.set_path(path)
+    coords = [tuple(int(x) for x in (rng.integers(4), rng.integers(8), rng.integers(3))) for _ in range(6)]
+    for g, fd in _fd_check(o, path, coords):
+        assert abs(g - fd) <= 1e-6 * max(1.0, abs(g)), (g, fd)
+    xml, path = electron_gas(tmp_path, n_part=8, n_bead=8, n_level=2, rs=2.0, k_cut_units=3.0, seed=5)
+    L = (4 * np.pi * 8 / 3) ** (1 / 3) * 2.0
+    path = rng.uniform(-L / 2, L / 2, size=path.shape)
+    o = oracle_mod.OracleSim(xml, base_dir=tmp_path)
+    o.set_path(path)
+    coords = [tuple(int(x) for x in (rng.integers(8), rng.integers(8), rng.integers(3))) for _ in range(6)]
+    for g, fd in _fd_check(o, path, coords):
+        assert abs(g - fd) <= 1e-6 * max(1.0, abs(g)), (g, fd)
+
+
+def test_oracle_hmc_energy_error_shrinks_with_step(oracle_mod, tmp_path):
+    """Leapfrog is second order: the mean |dH| of an HMC trajectory of fixed length falls by ~4x
+    when the step halves, so acceptance approaches 1."""
+    from simpimc_gb300.configs import trapped_coulomb
+    xml, path = trapped_coulomb(tmp_path, n_part=3, n_bead=8, n_level=2, seed=9)
+    rates = []
+    for step, n in ((0.02, 10), (0.01, 20)):
+        x = xml.replace('<Move name="Bisect" type="Bisect" species="e" n_level="2" />',
+                        f'<Move name="HMC" type="HMC" step_size="{step}" n_steps="{n}" />')
+        o = oracle_mod.OracleSim(x, base_dir=tmp_path)
+        o.set_path(path)
+        o.move_attempts(0, 40)
+        rates.append(o.move_stats(0)[2] / 40)
+    assert rates[1] >= rates[0] and rates[1] > 0.5, rates
