@@ -16,7 +16,9 @@ Also reported on the same line:
   energy_gate        per-chain energies and blocking error bars of the batched FP32 chains
                      against the single-chain FP64 path on the same chains and seeds;
   plain_electron_gas the single-chain FP64 kernel on the 66-electron gas (r_s = 2, beta = 8,
-                     M = 128, Ewald |k| < 12 (2 pi / L), 3561 half-space k-vectors, level 4).
+                     M = 128, Ewald |k| < 12 (2 pi / L), 3561 half-space k-vectors, level 4);
+  mixed_precision_large  the N = 1024, M = 512, |k| < 23 (2 pi / L) electron gas in the FP32 mode
+                     and the double-float mode: speed, HBM fraction, energy and S(k) differences.
 
 Arms:
   (default)          the CUDA library. `value` = device-timed cycles with the paths resident in
@@ -246,6 +248,69 @@ def egas_plain(local, steps, warmup, tmp, flush):
     return out, xml, host, reps
 
 
+def large_mixed_precision(local, tmp, sweeps=3):
+    """The large electron gas (r_s = 1, N = 1024 as 512 + 512, beta = 4, M = 512, |k| < 23 (2 pi / L),
+    bisection level 4) in FP32 mode and in the double-float mode from the same start and seeds:
+    device-timed sweeps of each, the FP32 kernel's bytes against the HBM peak, and the energy and
+    S(k) (first 200 |k| shells) differences between the two runs."""
+    import torch
+    from simpimc_gb300 import Simulation
+    from simpimc_gb300.configs import electron_gas
+    xml, path = electron_gas(tmp, n_part=1024, rs=1.0, beta=4.0, n_bead=512, k_cut_units=23.0, n_level=4, seed=777,
+                             structure_factor=True)
+    B = 16
+    reps = 512 * math.ceil(512 / B)
+    runs = {}
+    for bits in (32, 64):
+        s = Simulation(xml, base_dir=tmp, device=local, chain=0)
+        s.set_precision(bits)
+        s.set_path(path)
+        st = torch.cuda.ExternalStream(s._lib.pimc_stream(s._h), device=torch.device("cuda", local))
+        s.sweep([0, 1], [1, 1], reps)  # warm-up sweep
+        c0 = [s.move_counters(m) for m in range(2)]
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        energies = []
+        ms = 0.0
+        for _ in range(sweeps):
+            e0.record(st)
+            s.sweep([0, 1], [1, 1], reps)
+            e1.record(st)
+            e1.synchronize()
+            ms += e0.elapsed_time(e1)
+            s.observable_accumulate(0)
+            energies.append(s.observable_block(0)[0])
+            s.observable_accumulate(2)
+        c1 = [s.move_counters(m) for m in range(2)]
+        sk = s.observable_block(2)
+        kv = s.kvecs()
+        runs[bits] = dict(ms=ms, energies=np.asarray(energies), sk=np.asarray(sk), kmag=np.linalg.norm(kv, axis=1), n_k=s.n_k,
+                          att=sum(c1[m][0] - c0[m][0] for m in range(2)), acc=sum(c1[m][3] - c0[m][3] for m in range(2)),
+                          lv0=sum(c1[m][4] - c0[m][4] for m in range(2)))
+        s.close()
+    r32, r64 = runs[32], runs[64]
+    moves = 2 * reps * (B - 1) * sweeps
+    n_k = r32["n_k"]
+    alg = (r32["att"] * (B + 1) * 24 + r32["lv0"] * (1023 * (B + 1) * 24 + B * n_k * 16) + r32["acc"] * (B - 1) * n_k * 8) / sweeps
+    peak, kind = measured_hbm_peak()
+    achieved = alg / (r32["ms"] / sweeps / 1e3) / 1e9
+    mags = np.round(r32["kmag"], 9)
+    shells = np.unique(mags)[:200]
+    sk_diff = max(float(np.max(np.abs(r32["sk"][mags == m] - r64["sk"][mags == m]))) for m in shells) if r32["sk"].size else None
+    de = r32["energies"] - r64["energies"]
+    return {"workload": "electron gas N=1024 (512+512) r_s=1 beta=4 M=512 Ewald |k|<23(2pi/L) bisection level 4",
+            "n_k_half_space": n_k, "sweeps": sweeps,
+            "fp32": {"value": moves / (r32["ms"] / 1e3), "unit": METRIC, "ms_per_sweep": r32["ms"] / sweeps,
+                     "acceptance": r32["acc"] / max(r32["att"], 1),
+                     "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                                  "peak_kind": kind, "algorithmic_bytes_per_sweep": alg}},
+            "fp64_grade": {"value": moves / (r64["ms"] / 1e3), "unit": METRIC, "ms_per_sweep": r64["ms"] / sweeps,
+                           "acceptance": r64["acc"] / max(r64["att"], 1)},
+            "energy_fp32": r32["energies"].tolist(), "energy_fp64": r64["energies"].tolist(),
+            "energy_max_rel_diff": float(np.max(np.abs(de) / np.abs(r64["energies"]))),
+            "sk_shells": int(len(shells)), "sk_max_abs_diff_200_shells": sk_diff,
+            "note": "same start, seeds and draws; FP32 densities rebuilt from the positions at every sweep call"}
+
+
 def cpu_oracle_chains(items, tmp, seconds, chains):
     """The oracle on one host core, cycling through `chains` in chunks of attempts."""
     import oracle
@@ -367,6 +432,7 @@ def run_ours(args):
     cheap = sorted(range(N_CHAINS), key=lambda c: batch.shapes[c][0] ** 2 * batch.shapes[c][1])[:4]
     gate = energy_gate(items, tmp, local, chains=cheap, sweeps=args.gate_sweeps)
     eg, _, _, _ = egas_plain(local, args.steps, args.warmup, tmp, flush)
+    large = large_mixed_precision(local, tmp) if not args.no_large else None
     cpu = None
     if not args.no_cpu_baseline:
         moves, el = cpu_oracle_chains(items, tmp, 12.0, sample)
@@ -394,6 +460,7 @@ def run_ours(args):
         "speedup_vs_plain_same_system": value / plain["value"],
         "energy_gate": gate,
         "plain_electron_gas": eg,
+        "mixed_precision_large": large,
         "wall_s": wall,
     }
     print(json.dumps(line))
@@ -465,6 +532,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--gate-sweeps", type=int, default=400)
+    ap.add_argument("--no-large", action="store_true", help="skip the N=1024 mixed-precision leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -125,6 +125,12 @@ int pimc_run(pimc_ctx* ctx);
 int pimc_n_blocks(pimc_ctx* ctx, uint32_t observable, size_t* n);
 int pimc_get_block(pimc_ctx* ctx, uint32_t observable, size_t block, double* out, size_t cap, size_t* n);
 
+/* Sweep precision (the reference's build-time PRECISION option, CMakeLists.txt:11-19, as a run-time
+ * switch): 64 (default) keeps positions, per-slice densities and all action terms in double-float;
+ * 32 keeps the per-slice densities, bead phases and Ewald differences in FP32 with compensated sums
+ * (densities rebuilt from the positions at every sweep call), while positions, pair links, level
+ * sums and the acceptance test stay double-float and estimators stay FP64. */
+int pimc_set_precision(pimc_ctx* ctx, int bits);
 /* Synchronises the context stream and reports any device-side error (timeout, non-finite). */
 int pimc_synchronize(pimc_ctx* ctx);
 /* Tuning: CTAs of the cooperative sweep (0 = automatic) and the device wait limit. */

@@ -65,6 +65,7 @@ SIGNATURES = {
     "pimc_get_action_gradient": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _U32P, _U32P, C.c_uint32, C.c_uint32, C.c_int, _DP]),
     "pimc_get_action_gradient_exact": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _U32P, _U32P, C.c_uint32, C.c_uint32, C.c_int, _DP]),
     "pimc_total_action": (C.c_int, [_P, C.c_int, C.c_int, _DP]),
+    "pimc_set_precision": (C.c_int, [_P, C.c_int]),
     "pimc_action_gradient_path": (C.c_int, [_P, C.c_int, C.c_int, _DP]),
     "pimc_dactiondbeta": (C.c_int, [_P, C.c_uint32, _DP]),
     "pimc_potential": (C.c_int, [_P, C.c_uint32, _DP]),
@@ -188,6 +189,10 @@ class Simulation:
 
     def set_sweep_grid(self, grid: int):
         self._check(self._lib.pimc_set_sweep_grid(self._h, grid))
+
+    def set_precision(self, bits: int):
+        """Sweep precision: 64 (double-float densities) or 32 (FP32 densities and phases)."""
+        self._check(self._lib.pimc_set_precision(self._h, bits))
 
     def set_timeout_ns(self, ns: int):
         self._check(self._lib.pimc_set_timeout_ns(self._h, ns))

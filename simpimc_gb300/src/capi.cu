@@ -149,6 +149,10 @@ int pimc_get_action_gradient_exact(pimc_ctx* ctx, uint32_t action, uint32_t b0, 
     });
 }
 
+int pimc_set_precision(pimc_ctx* ctx, int bits) {
+    return Guard(ctx, [&](pimc::Context& c) { c.SetPrecision(bits); });
+}
+
 int pimc_total_action(pimc_ctx* ctx, int action, int mode, double* out) {
     if (!out) return PIMC_ERR_ARG;
     return Guard(ctx, [&](pimc::Context& c) { *out = c.TotalAction(action, mode); });

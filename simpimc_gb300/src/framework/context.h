@@ -176,6 +176,10 @@ class Context {
     // representations may be newer than the other; Ensure* converts on demand.
     void EnsureDD();
     void EnsureFP64();
+    // Sweep precision: 64 keeps the densities in double-float; 32 keeps them (and the bead phases
+    // and Ewald differences) in FP32 with compensated sums, rebuilt from the positions per call.
+    void SetPrecision(int bits);
+    int precision = 64;
     bool dd_valid = false;
     bool fp64_valid = true;
     // Host copies of every spline table, keyed by the device coefficient pointer, so the sweep
@@ -190,7 +194,7 @@ class Context {
 
    private:
     std::vector<std::unique_ptr<DeviceBuffer>> keep_;  // tables owned for the context lifetime
-    std::unique_ptr<DeviceBuffer> pos_dd_, rho_dd_, sweep_desc_, sweep_tables_;
+    std::unique_ptr<DeviceBuffer> pos_dd_, rho_dd_, rho32_, sweep_desc_, sweep_tables_;
     bool sweep_tables_built_ = false;
     std::vector<uint32_t> desc_levels_;  // bisection levels the uploaded move descriptors were built for
     struct StageTable {

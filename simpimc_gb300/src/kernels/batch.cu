@@ -71,27 +71,6 @@ __device__ __forceinline__ dd ShflDownDD(dd v, int o) {
     return dd{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
 }
 
-/// Cascaded compensated sum (Neumaier / Ogita-Rump-Oishi Sum2): the running sum carries one FP32
-/// add per term on its dependency chain; the TwoSum errors gather in a separate FP32 word. The
-/// result is as accurate as a sum formed in twice the working precision.
-struct Comp {
-    float s, c;
-};
-
-__device__ __forceinline__ void CompAdd(Comp& a, float x) {
-    const float t = __fadd_rn(a.s, x);
-    const float bp = __fsub_rn(t, a.s);
-    const float e = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(x, bp));
-    a.s = t;
-    a.c = __fadd_rn(a.c, e);
-}
-
-/// Merge of two compensated partial sums (TwoSum of the sums, errors added).
-__device__ __forceinline__ Comp CompMerge(Comp a, Comp b) {
-    const dd s = TwoSum(a.s, b.s);
-    return Comp{s.hi, __fadd_rn(__fadd_rn(a.c, b.c), s.lo)};
-}
-
 /// Butterfly reduction over the lanes whose xor distance is below 2^log2_width; every lane of a
 /// group receives the same total (TwoSum and FP32 addition are commutative).
 __device__ __forceinline__ Comp CompWarpSum(Comp v, int width) {
@@ -101,8 +80,6 @@ __device__ __forceinline__ Comp CompWarpSum(Comp v, int width) {
     }
     return v;
 }
-
-__device__ __forceinline__ dd CompDD(Comp a) { return TwoSum(a.s, a.c); }
 
 __device__ __forceinline__ float Sq3(float x, float y, float z) { return __fmaf_rn(x, x, __fmaf_rn(y, y, __fmul_rn(z, z))); }
 

@@ -147,6 +147,29 @@ __host__ __device__ __forceinline__ void SplitDouble(double x, float& hi, float&
     lo = (float)(x - (double)hi);
 }
 
+/// Cascaded compensated sum (Neumaier / Ogita-Rump-Oishi Sum2): the running sum carries one FP32
+/// add per term on its dependency chain; the TwoSum errors gather in a separate FP32 word. The
+/// result is as accurate as a sum formed in twice the working precision.
+struct Comp {
+    float s, c;
+};
+
+__device__ __forceinline__ void CompAdd(Comp& a, float x) {
+    const float t = __fadd_rn(a.s, x);
+    const float bp = __fsub_rn(t, a.s);
+    const float e = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(x, bp));
+    a.s = t;
+    a.c = __fadd_rn(a.c, e);
+}
+
+/// Merge of two compensated partial sums (TwoSum of the sums, errors added).
+__device__ __forceinline__ Comp CompMerge(Comp a, Comp b) {
+    const dd s = TwoSum(a.s, b.s);
+    return Comp{s.hi, __fadd_rn(__fadd_rn(a.c, b.c), s.lo)};
+}
+
+__device__ __forceinline__ dd CompDD(Comp a) { return TwoSum(a.s, a.c); }
+
 // Complex df64.
 __device__ __forceinline__ ddc CAdd(ddc a, ddc b) { return ddc{Add(a.re, b.re), Add(a.im, b.im)}; }
 __device__ __forceinline__ ddc CSub(ddc a, ddc b) { return ddc{Sub(a.re, b.re), Sub(a.im, b.im)}; }

@@ -75,7 +75,8 @@ struct SweepArgs {
     uint32_t sp_off[kMaxSpecies], sp_n[kMaxSpecies];
     int32_t max_index[3];
     float2* pos;              // [M][3][n_pad]
-    float4* rho;              // [slots][M][K]
+    float4* rho;              // [slots][M][K] double-float densities
+    float2* rho32;            // [slots][M][K] FP32 densities (FP32 mode)
     const int32_t* kidx;      // [K]
     const float4* phase256;   // exp(2 pi i j / 256), j = 0..255
     const MoveDD* moves;
@@ -214,6 +215,40 @@ __device__ __forceinline__ ddc PhaseProductDD(const ddc* tab, uint32_t stride, u
     return f;
 }
 
+/// FP32 counterpart of PhaseDD: the turn count n x / L is reduced in double-float (so large n x
+/// loses no bits), the residue of at most pi/256 is expanded to fifth order in FP32 and rotated by
+/// the table entry's leading part.
+__device__ __forceinline__ float2 PhaseF(dd x, int n, dd iL, const float4* tab256) {
+    if (n == 0) return make_float2(1.f, 0.f);
+    dd t = Mul(x, iL);
+    t = Sub(t, DD(Rint(t)));
+    dd a = MulF(t, (float)n);
+    a = Sub(a, DD(Rint(a)));
+    const float jf = rintf(__fmul_rn(a.hi, 256.f));
+    const dd g = Sub(a, DD(__fmul_rn(jf, 1.f / 256.f)));
+    const float eps = __fmul_rn(__fadd_rn(g.hi, g.lo), 6.28318531f);
+    const float e2 = __fmul_rn(eps, eps);
+    const float sn = __fmaf_rn(__fmul_rn(eps, e2), __fmaf_rn(e2, 1.f / 120.f, -1.f / 6.f), eps);
+    const float cs = __fmaf_rn(e2, __fmaf_rn(e2, 1.f / 24.f, -0.5f), 1.f);
+    const float4 T = tab256[((int)jf + 256) & 255];  // (re.hi, re.lo, im.hi, im.lo)
+    return make_float2(__fsub_rn(__fmul_rn(T.x, cs), __fmul_rn(T.z, sn)), __fadd_rn(__fmul_rn(T.x, sn), __fmul_rn(T.z, cs)));
+}
+
+__device__ __forceinline__ float2 CMulF(float2 a, float2 b) {
+    return make_float2(__fsub_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fadd_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
+}
+
+__device__ __forceinline__ float2 PhaseProductF(const float2* tab, uint32_t stride, uint32_t n_d, int32_t packed) {
+    float2 f = make_float2(1.f, 0.f);
+    for (uint32_t d = 0; d < n_d; ++d) {
+        const int n = KIdx(packed, (int)d);
+        float2 c = tab[d * stride + (n < 0 ? -n : n)];
+        if (n < 0) c.y = -c.y;
+        f = d == 0 ? c : CMulF(f, c);
+    }
+    return f;
+}
+
 /// Generation index of the first midpoint of level lvl (levels are sampled from n_level - 1 down).
 __device__ __forceinline__ uint32_t LevelFirst(uint32_t nl, int lvl, uint32_t B) {
     uint32_t first = 0;
@@ -326,6 +361,10 @@ __device__ __forceinline__ void CopyWords(void* dst, const void* src, uint32_t b
     for (uint32_t i = threadIdx.x; i < bytes / 4; i += blockDim.x) d[i] = s[i];
 }
 
+/// kF32: FP32 mode. Per-slice densities are FP32 (a.rho32), bead phases are FP32 (PhaseF), and
+/// each thread's Ewald differences are summed with a cascaded compensated sum before they join the
+/// double-float acceptance pipeline; positions, pair links and level sums stay double-float.
+template <bool kF32>
 __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_constant__ SweepArgs a) {
     extern __shared__ float4 smem4[];
     const uint32_t n_d = a.n_d, M = a.M, np = a.n_pad, K = a.K;
@@ -357,6 +396,8 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
     __syncthreads();
     ddc* tab_old = reinterpret_cast<ddc*>(sbase + a.off_work);          // [spc][3][stride]
     ddc* tab_new = tab_old + (size_t)a.slices_per_cta * 3 * stride;       // [spc][3][stride]
+    float2* tf_old = reinterpret_cast<float2*>(tab_old);                  // FP32 mode: same rows, float2 entries
+    float2* tf_new = reinterpret_cast<float2*>(tab_new);
     dd* seg_old = reinterpret_cast<dd*>(tab_new + (size_t)a.slices_per_cta * 3 * stride);  // [cap][3]
     dd* seg_new = seg_old + 3 * cap;                                      // [cap][3]
     dd* d_old = seg_new + 3 * cap;                                        // [cap][3] sampling displacements
@@ -486,12 +527,22 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                 if (any_lr && (uint32_t)tid < n_own * nk_own) {
                     const uint32_t k = k_lo + tid % nk_own;
                     const uint32_t b = (bead0 + s_slice_jj[tid / nk_own]) % M;
-                    pre_rho = a.rho[((size_t)slot_s * M + b) * K + k];
-                    if (slot_o_first >= 0) pre_rho_o = a.rho[((size_t)slot_o_first * M + b) * K + k];
+                    if constexpr (kF32) {
+                        const float2 v = a.rho32[((size_t)slot_s * M + b) * K + k];
+                        pre_rho = make_float4(v.x, v.y, 0.f, 0.f);
+                        if (slot_o_first >= 0) {
+                            const float2 w = a.rho32[((size_t)slot_o_first * M + b) * K + k];
+                            pre_rho_o = make_float4(w.x, w.y, 0.f, 0.f);
+                        }
+                    } else {
+                        pre_rho = a.rho[((size_t)slot_s * M + b) * K + k];
+                        if (slot_o_first >= 0) pre_rho_o = a.rho[((size_t)slot_o_first * M + b) * K + k];
+                    }
                 }
                 dd pair_old{0.f, 0.f};  // stored copy's pair links of this lane's quad (quad lane 0)
                 bool old_done = false;
                 ddc pre_eo{{0.f, 0.f}, {0.f, 0.f}};
+                float2 pre_eo_f = make_float2(0.f, 0.f);
                 bool eo_done = false;
                 PIMC_ROLE_BEGIN(rt2);
                 // Warp roles: level sums run in one warp of a designated block when the attempt has
@@ -546,7 +597,8 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                         const uint32_t si = task / 3, d = task % 3;
                         if (d < n_d)
                             for (int n = lane; n <= a.max_index[d]; n += 32)
-                                tab_old[(si * 3 + d) * stride + n] = PhaseDD(seg_old[3 * s_slice_jj[si] + d], n, a.iL, a.two_pi, s_phase);
+                                if constexpr (kF32) tf_old[(si * 3 + d) * stride + n] = PhaseF(seg_old[3 * s_slice_jj[si] + d], n, a.iL, s_phase);
+                                else tab_old[(si * 3 + d) * stride + n] = PhaseDD(seg_old[3 * s_slice_jj[si] + d], n, a.iL, a.two_pi, s_phase);
                     }
                     PIMC_ROLE_END(rt2, 2);
                 } else if (grid_work) {
@@ -589,12 +641,14 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                             const uint32_t si = task / 3, d = task % 3;
                             if (d < n_d)
                                 for (int n = lane; n <= a.max_index[d]; n += 32)
-                                    tab_new[(si * 3 + d) * stride + n] = PhaseDD(seg_new[3 * s_slice_jj[si] + d], n, a.iL, a.two_pi, s_phase);
+                                    if constexpr (kF32) tf_new[(si * 3 + d) * stride + n] = PhaseF(seg_new[3 * s_slice_jj[si] + d], n, a.iL, s_phase);
+                                    else tab_new[(si * 3 + d) * stride + n] = PhaseDD(seg_new[3 * s_slice_jj[si] + d], n, a.iL, a.two_pi, s_phase);
                         }
                         PIMC_ROLE_END(rt3, 5);
                     } else if (any_lr && (uint32_t)tid < n_own * nk_own) {
                         // Old-position phase of this thread's first Ewald cell (tables built above).
-                        pre_eo = PhaseProductDD(tab_old + (size_t)(tid / nk_own) * 3 * stride, stride, n_d, a.kidx[k_lo + tid % nk_own]);
+                        if constexpr (kF32) pre_eo_f = PhaseProductF(tf_old + (size_t)(tid / nk_own) * 3 * stride, stride, n_d, a.kidx[k_lo + tid % nk_own]);
+                        else pre_eo = PhaseProductDD(tab_old + (size_t)(tid / nk_own) * 3 * stride, stride, n_d, a.kidx[k_lo + tid % nk_own]);
                         eo_done = true;
                         PIMC_ROLE_END(rt3, 6);
                     }
@@ -605,6 +659,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
 
                 // ---- 4. level-0 grid work: pair links + owned Ewald cells -------------------
                 ddc delta_cache[kDeltaCache];
+                float2 delta_f[kDeltaCache];
                 if (grid_work) {
                     // Pair links (pair_action_class.h:280-290), CalcU = tau V at level 0: the working
                     // copy here; the stored copy was summed during sampling by free warps.
@@ -618,7 +673,39 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                                                       seg_old, a.L, a.iL, a.tau));
                     }
                     if (old_done) acc = Sub(acc, pair_old);
-                    if (any_lr) {
+                    if (any_lr && kF32) {
+                        // FP32 mode: the same cells with FP32 phases and densities; each thread's
+                        // terms in a compensated sum, joined to the double-float total once.
+                        const uint32_t nk = nk_own;
+                        Comp lr32{0.f, 0.f};
+                        uint32_t ci = 0;
+                        for (uint32_t it = tid; it < n_own * nk; it += blockDim.x, ++ci) {
+                            const uint32_t si = it / nk, k = k_lo + it % nk;
+                            const uint32_t b = (bead0 + s_slice_jj[si]) % M;
+                            const int32_t pk = a.kidx[k];
+                            const float2 en = PhaseProductF(tf_new + (size_t)si * 3 * stride, stride, n_d, pk);
+                            const float2 eo = (ci == 0 && eo_done) ? pre_eo_f : PhaseProductF(tf_old + (size_t)si * 3 * stride, stride, n_d, pk);
+                            const float2 dl = make_float2(__fsub_rn(en.x, eo.x), __fsub_rn(en.y, eo.y));
+                            if (ci < kDeltaCache) delta_f[ci] = dl;
+                            const float2 rho = ci == 0 ? make_float2(pre_rho.x, pre_rho.y) : a.rho32[((size_t)slot_s * M + b) * K + k];
+                            for (int pi = 0; pi < mv.n_pair; ++pi) {
+                                const PairDD& pa = s_pairs[mv.pair[pi]];
+                                if (!pa.use_lr || pa.is_constant) continue;
+                                const float vk = pa.vk[k].x;
+                                if (pa.sa == pa.sb) {
+                                    const float t = __fmaf_rn(dl.x, __fmaf_rn(2.f, rho.x, dl.x), __fmul_rn(dl.y, __fmaf_rn(2.f, rho.y, dl.y)));
+                                    CompAdd(lr32, __fmul_rn(vk, t));
+                                } else {
+                                    const int slot_o = pa.sa == s ? pa.slot_b : pa.slot_a;
+                                    const float2 ro = (ci == 0 && slot_o == slot_o_first) ? make_float2(pre_rho_o.x, pre_rho_o.y)
+                                                                                          : a.rho32[((size_t)slot_o * M + b) * K + k];
+                                    const float t = __fmaf_rn(dl.x, ro.x, __fmul_rn(dl.y, ro.y));
+                                    CompAdd(lr32, __fmul_rn(2.f * vk, t));
+                                }
+                            }
+                        }
+                        acc = Add(acc, Mul(a.tau, CompDD(lr32)));
+                    } else if (any_lr) {
                         const uint32_t nk = nk_own;
                         dd lr{0.f, 0.f};
                         uint32_t ci = 0;
@@ -732,16 +819,31 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                         for (uint32_t it = tid; it < n_own * nk; it += blockDim.x, ++ci) {
                             const uint32_t si = it / nk, k = k_lo + it % nk;
                             const uint32_t b = (bead0 + s_slice_jj[si]) % M;
-                            ddc dl;
-                            if (ci < kDeltaCache) {
-                                dl = delta_cache[ci];
+                            if constexpr (kF32) {
+                                float2 dl;
+                                if (ci < kDeltaCache) {
+                                    dl = delta_f[ci];
+                                } else {
+                                    const int32_t pk = a.kidx[k];
+                                    const float2 en = PhaseProductF(tf_new + (size_t)si * 3 * stride, stride, n_d, pk);
+                                    const float2 eo = PhaseProductF(tf_old + (size_t)si * 3 * stride, stride, n_d, pk);
+                                    dl = make_float2(__fsub_rn(en.x, eo.x), __fsub_rn(en.y, eo.y));
+                                }
+                                float2* cell = &a.rho32[((size_t)slot_s * M + b) * K + k];
+                                const float2 c0 = *cell;
+                                *cell = make_float2(__fadd_rn(c0.x, dl.x), __fadd_rn(c0.y, dl.y));
                             } else {
-                                const int32_t pk = a.kidx[k];
-                                dl = CSub(PhaseProductDD(tab_new + (size_t)si * 3 * stride, stride, n_d, pk),
-                                          PhaseProductDD(tab_old + (size_t)si * 3 * stride, stride, n_d, pk));
+                                ddc dl;
+                                if (ci < kDeltaCache) {
+                                    dl = delta_cache[ci];
+                                } else {
+                                    const int32_t pk = a.kidx[k];
+                                    dl = CSub(PhaseProductDD(tab_new + (size_t)si * 3 * stride, stride, n_d, pk),
+                                              PhaseProductDD(tab_old + (size_t)si * 3 * stride, stride, n_d, pk));
+                                }
+                                float4* cell = &a.rho[((size_t)slot_s * M + b) * K + k];
+                                *cell = Pack(CAdd(Unpack(*cell), dl));
                             }
-                            float4* cell = &a.rho[((size_t)slot_s * M + b) * K + k];
-                            *cell = Pack(CAdd(Unpack(*cell), dl));
                         }
                     }
                     n_acc[m] += 1;
@@ -802,6 +904,51 @@ __global__ void FromDDKernel(const float2* __restrict__ pos_dd, double* __restri
     }
 }
 
+__global__ void ToF32Kernel(const double2* __restrict__ rho, float2* __restrict__ rho32, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        rho32[i] = make_float2((float)rho[i].x, (float)rho[i].y);
+}
+
+__global__ void FromF32Kernel(const float2* __restrict__ rho32, double2* __restrict__ rho, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        rho[i] = make_double2((double)rho32[i].x, (double)rho32[i].y);
+}
+
+// FP32 densities from the double-float positions (species_class.h:380-403 in FP32 mode): the sum
+// over the species' particles, in particle order, of FP32 bead phases, compensated. One thread
+// per k-vector of a 256-wide chunk, one block per (chunk, slice, slot); the phase rows of
+// kRho32Chunk particles at a time sit in shared memory.
+constexpr uint32_t kRho32Chunk = 64;
+
+__global__ void InitRho32Kernel(const __grid_constant__ SweepArgs a, const int* __restrict__ slot_species) {
+    extern __shared__ float2 ftab[];  // [kRho32Chunk][3][stride]
+    const uint32_t stride = a.tab_stride, n_d = a.n_d, M = a.M, K = a.K, np = a.n_pad;
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y, slot = blockIdx.z;
+    const uint32_t s = (uint32_t)slot_species[slot];
+    const uint32_t ns = a.sp_n[s], off = a.sp_off[s];
+    const int32_t pk = k < K ? a.kidx[k] : 0;
+    Comp re{0.f, 0.f}, im{0.f, 0.f};
+    for (uint32_t p0 = 0; p0 < ns; p0 += kRho32Chunk) {
+        const uint32_t cnt = min(kRho32Chunk, ns - p0);
+        __syncthreads();
+        for (uint32_t t = threadIdx.x; t < cnt * 3 * stride; t += blockDim.x) {
+            const uint32_t pi = t / (3 * stride), rem = t - pi * 3 * stride, d = rem / stride, n = rem - d * stride;
+            if (d < n_d && (int)n <= a.max_index[d]) {
+                const float2 v = a.pos[((size_t)b * 3 + d) * np + off + p0 + pi];
+                ftab[t] = PhaseF(dd{v.x, v.y}, (int)n, a.iL, a.phase256);
+            }
+        }
+        __syncthreads();
+        if (k < K)
+            for (uint32_t pi = 0; pi < cnt; ++pi) {
+                const float2 e = PhaseProductF(ftab + (size_t)pi * 3 * stride, stride, n_d, pk);
+                CompAdd(re, e.x);
+                CompAdd(im, e.y);
+            }
+    }
+    if (k < K) a.rho32[((size_t)slot * M + b) * K + k] = make_float2(__fadd_rn(re.s, re.c), __fadd_rn(im.s, im.c));
+}
+
 void Split(double x, dd& out) {
     float h, l;
     SplitDouble(x, h, l);
@@ -817,17 +964,36 @@ void Context::EnsureDD() {
     const size_t n_pos = (size_t)sys.M * 3 * sys.n_pad;
     const size_t n_rho = (rho_slots && sys.K) ? (size_t)rho_slots * sys.M * sys.K : 0;
     if (!pos_dd_) pos_dd_.reset(new DeviceBuffer(n_pos * sizeof(float2)));
-    if (!rho_dd_) rho_dd_.reset(new DeviceBuffer(std::max<size_t>(n_rho, 1) * sizeof(float4)));
-    ToDDKernel<<<n_sm * 4, 256, 0, stream>>>(sys.pos, pos_dd_->as<float2>(), n_pos, sys.rho_k, rho_dd_->as<float4>(), n_rho);
+    if (precision == 32) {
+        // FP32 mode: the densities are rebuilt from the positions at every sweep call.
+        if (!rho32_) rho32_.reset(new DeviceBuffer(std::max<size_t>(n_rho, 1) * sizeof(float2)));
+        ToDDKernel<<<n_sm * 4, 256, 0, stream>>>(sys.pos, pos_dd_->as<float2>(), n_pos, sys.rho_k, nullptr, 0);
+    } else {
+        if (!rho_dd_) rho_dd_.reset(new DeviceBuffer(std::max<size_t>(n_rho, 1) * sizeof(float4)));
+        ToDDKernel<<<n_sm * 4, 256, 0, stream>>>(sys.pos, pos_dd_->as<float2>(), n_pos, sys.rho_k, rho_dd_->as<float4>(), n_rho);
+    }
     CudaCheck(cudaGetLastError(), "to-dd launch");
     dd_valid = true;
+}
+
+void Context::SetPrecision(int bits) {
+    if (bits != 32 && bits != 64) throw PimcError(kErrArg, "precision must be 32 or 64");
+    if (bits == precision) return;
+    EnsureFP64();
+    precision = bits;
+    dd_valid = false;
 }
 
 void Context::EnsureFP64() {
     if (fp64_valid) return;
     const size_t n_pos = (size_t)sys.M * 3 * sys.n_pad;
     const size_t n_rho = (rho_slots && sys.K) ? (size_t)rho_slots * sys.M * sys.K : 0;
-    FromDDKernel<<<n_sm * 4, 256, 0, stream>>>(pos_dd_->as<float2>(), sys.pos, sys.pos_new, n_pos, rho_dd_->as<float4>(), sys.rho_k, n_rho);
+    if (precision == 32) {
+        FromDDKernel<<<n_sm * 4, 256, 0, stream>>>(pos_dd_->as<float2>(), sys.pos, sys.pos_new, n_pos, nullptr, sys.rho_k, 0);
+        if (n_rho) FromF32Kernel<<<n_sm * 4, 256, 0, stream>>>(rho32_->as<float2>(), sys.rho_k, n_rho);
+    } else {
+        FromDDKernel<<<n_sm * 4, 256, 0, stream>>>(pos_dd_->as<float2>(), sys.pos, sys.pos_new, n_pos, rho_dd_->as<float4>(), sys.rho_k, n_rho);
+    }
     CudaCheck(cudaGetLastError(), "from-dd launch");
     Sync();
     fp64_valid = true;
@@ -1058,7 +1224,8 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
     }
     for (int d = 0; d < 3; ++d) args->max_index[d] = sys.max_index[d];
     args->pos = pos_dd_->as<float2>();
-    args->rho = rho_dd_->as<float4>();
+    args->rho = precision == 32 ? nullptr : rho_dd_->as<float4>();
+    args->rho32 = precision == 32 ? rho32_->as<float2>() : nullptr;
     args->kidx = sys.kidx;
     args->phase256 = sweep_tables_->as<float4>();
     args->moves = dmoves;
@@ -1110,9 +1277,10 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
     }
     args->off_work = (uint32_t)off;
     const size_t smem = off + work;
-    CudaCheck(cudaFuncSetAttribute(BisectSweepKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attribute");
+    const void* kfn = precision == 32 ? (const void*)BisectSweepKernel<true> : (const void*)BisectSweepKernel<false>;
+    CudaCheck(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attribute");
     int occ = 0;
-    CudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, BisectSweepKernel, kThreads, smem), "occupancy");
+    CudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kfn, kThreads, smem), "occupancy");
     if (occ < 1) throw PimcError(kErrCuda, "sweep kernel cannot be resident");
     if (G > occ * n_sm) throw PimcError(kErrArg, "sweep grid larger than the co-resident limit");
     args->counters = dcount;
@@ -1127,9 +1295,21 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
         if (!phase_buf) phase_buf.reset(new DeviceBuffer(kSweepTimingSlots * sizeof(unsigned long long)));
         args->phase_cycles = phase_buf->as<unsigned long long>();
     }
+    if (precision == 32 && rho_slots && sys.K) {
+        // FP32 densities rebuilt from the positions, which bounds the drift of their FP32 updates.
+        std::vector<int> slot_species(rho_slots, 0);
+        for (uint32_t sp = 0; sp < sys.S; ++sp)
+            if (sys.sp_rho[sp] >= 0) slot_species[sys.sp_rho[sp]] = (int)sp;
+        uint32_t* dss = Parts(rho_slots);
+        CudaCheck(cudaMemcpyAsync(dss, slot_species.data(), rho_slots * sizeof(int), cudaMemcpyHostToDevice, stream), "slot upload");
+        const size_t rsm = (size_t)kRho32Chunk * 3 * args->tab_stride * sizeof(float2);
+        CudaCheck(cudaFuncSetAttribute(InitRho32Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm), "smem attribute");
+        InitRho32Kernel<<<dim3((sys.K + 255) / 256, sys.M, rho_slots), 256, rsm, stream>>>(*args, reinterpret_cast<const int*>(dss));
+        CudaCheck(cudaGetLastError(), "rho32 launch");
+    }
     CudaCheck(cudaMemsetAsync(Barrier(), 0, sizeof(unsigned long long), stream), "reset barrier");
     void* kargs[] = {args};
-    CudaCheck(cudaLaunchCooperativeKernel((void*)BisectSweepKernel, dim3(G), dim3(kThreads), kargs, smem, stream), "sweep launch");
+    CudaCheck(cudaLaunchCooperativeKernel(kfn, dim3(G), dim3(kThreads), kargs, smem, stream), "sweep launch");
     fp64_valid = false;
     std::vector<unsigned long long> cnt(2 * kMaxMoves);
     CudaCheck(cudaMemcpyAsync(cnt.data(), dcount, 2 * kMaxMoves * 8, cudaMemcpyDeviceToHost, stream), "read counters");
