@@ -353,7 +353,7 @@ def run_ours(args):
     per_sweep = batch.stats()["bead_moves_per_sweep"]
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
 
-    ipl, mw, tune_s = batch.autotune(2)
+    ipl, mw, wave, tune_s = batch.autotune(2)
     batch.run(args.warmup, 1)
     batch.synchronize()
     att0, acc0 = batch.counters()
@@ -444,7 +444,7 @@ def run_ours(args):
         "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Gaussian beads per chain, warmed up)",
         "config": {"workload": WORKLOAD, "n_chains": N_CHAINS, "bead_moves_per_step": per_sweep,
-                   "tile": {"items_per_lane": ipl, "max_warps": mw, "autotune_s_per_sweep": tune_s},
+                   "tile": {"items_per_lane": ipl, "max_warps": mw, "wave": wave, "autotune_s_per_sweep": tune_s},
                    "acceptance": float((acc1 - acc0).sum() / max((att1 - att0).sum(), 1)),
                    "l2": "256 MB flush between timed steps", "parallelism": "replicas (independent chains per GPU)"},
         "clocks": clocks_summary(clk_file, local),

@@ -190,11 +190,16 @@ int pimc_batch_reset_energy(pimc_batch* b);
 int pimc_batch_last_energy(pimc_batch* b, double* out);
 /* Per-chain attempt and acceptance counters (arrays of n_chains; either may be NULL). */
 int pimc_batch_counters(pimc_batch* b, uint64_t* attempts, uint64_t* accepts);
-/* Pair tile: a chain gets ceil((n_part-1)(2^n_level-1) / (32 items_per_lane)) warps, at most
- * max_warps (<= 16). pimc_batch_autotune times `trial_sweeps` sweeps of every candidate on a
- * saved copy of the chains' state, restores it, and keeps the fastest tile. */
-int pimc_batch_set_tiles(pimc_batch* b, uint32_t items_per_lane, uint32_t max_warps);
-int pimc_batch_autotune(pimc_batch* b, uint32_t trial_sweeps, uint32_t* items_per_lane, uint32_t* max_warps, double* sec_per_sweep);
+/* Tiles: one attempt wants ceil((n_part-1)(2^n_level-1) / (32 items_per_lane)) warps for its pair
+ * items; with wave = 1 a chain gets that many, at most max_warps (<= 16). With wave = W > 1 (<= 4)
+ * a chain runs up to W attempts at once on W groups of such warps (at least 2 each, W times at
+ * most max_warps in all): the longest prefix of its next W draws in which no attempt reads what an
+ * earlier one may change, so the Markov chain is the sequential one. pimc_batch_autotune times
+ * `trial_sweeps` sweeps of every candidate on a saved copy of the chains' state, restores it, and
+ * keeps the fastest. */
+int pimc_batch_set_tiles(pimc_batch* b, uint32_t items_per_lane, uint32_t max_warps, uint32_t wave);
+int pimc_batch_autotune(pimc_batch* b, uint32_t trial_sweeps, uint32_t* items_per_lane, uint32_t* max_warps, uint32_t* wave,
+                        double* sec_per_sweep);
 /* out4 = {n_chains, bead moves per sweep of all chains, kernels launched so far, series rows kept}. */
 int pimc_batch_stats(pimc_batch* b, uint64_t* out4);
 /* CUDA stream of the batch (cudaStream_t). */

@@ -100,8 +100,8 @@ SIGNATURES = {
     "pimc_batch_energy": (C.c_int, [_P, C.c_uint32, _DP, C.c_uint64, _U64P]),
     "pimc_batch_reset_energy": (C.c_int, [_P]),
     "pimc_batch_counters": (C.c_int, [_P, _U64P, _U64P]),
-    "pimc_batch_set_tiles": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
-    "pimc_batch_autotune": (C.c_int, [_P, C.c_uint32, _U32P, _U32P, _DP]),
+    "pimc_batch_set_tiles": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32]),
+    "pimc_batch_autotune": (C.c_int, [_P, C.c_uint32, _U32P, _U32P, _U32P, _DP]),
     "pimc_batch_stats": (C.c_int, [_P, _U64P]),
     "pimc_batch_stream": (C.c_int, [_P, C.POINTER(_P)]),
 }
@@ -435,13 +435,14 @@ class ChainBatch:
         self._check(self._lib.pimc_batch_counters(self._h, att.ctypes.data_as(_U64P), acc.ctypes.data_as(_U64P)))
         return att, acc
 
-    def set_tiles(self, items_per_lane: int, max_warps: int):
-        self._check(self._lib.pimc_batch_set_tiles(self._h, items_per_lane, max_warps))
+    def set_tiles(self, items_per_lane: int, max_warps: int, wave: int = 1):
+        self._check(self._lib.pimc_batch_set_tiles(self._h, items_per_lane, max_warps, wave))
 
     def autotune(self, trial_sweeps: int = 2):
-        ipl, mw, sec = C.c_uint32(), C.c_uint32(), C.c_double()
-        self._check(self._lib.pimc_batch_autotune(self._h, trial_sweeps, C.byref(ipl), C.byref(mw), C.byref(sec)))
-        return int(ipl.value), int(mw.value), float(sec.value)
+        """(items_per_lane, max_warps, wave, seconds per sweep) of the fastest tile, now set."""
+        ipl, mw, wv, sec = C.c_uint32(), C.c_uint32(), C.c_uint32(), C.c_double()
+        self._check(self._lib.pimc_batch_autotune(self._h, trial_sweeps, C.byref(ipl), C.byref(mw), C.byref(wv), C.byref(sec)))
+        return int(ipl.value), int(mw.value), int(wv.value), float(sec.value)
 
     def stats(self) -> dict:
         out = np.zeros(4, dtype=np.uint64)

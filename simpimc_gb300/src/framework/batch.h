@@ -36,11 +36,13 @@ namespace pimc {
 constexpr uint32_t kBatchMaxLevels = 5;        // segment of at most 32 beads
 constexpr uint32_t kBatchMaxWarps = 16;        // warps per chain (block size 512)
 constexpr uint32_t kBatchSeriesComponents = 4; // E, kinetic, trap, pair (each / M)
+constexpr uint32_t kMaxWave = 4;               // attempts of one chain in flight at once
 
 /// Per-chain parameters read by the batched kernels.
 struct ChainDev {
     uint32_t n_part, n_bead, n_pad, n_level;  // B = 2^n_level beads per segment
     uint32_t seed, chain_id, n_warps, move;   // Philox keys; warps used; move index in its input
+    uint32_t n_wave, sub_warps, pad2, pad3;   // attempts in flight per round; warps per attempt
     uint64_t pos_off;                         // first float4 of the chain's [n_bead][n_pad] block
     uint64_t attempts_per_sweep;              // n_part * ceil(n_bead / B)
     float L, iL, lambda, tau;
@@ -83,13 +85,13 @@ class ChainBatch {
     uint64_t ReadEnergy(uint32_t chain, double* out, uint64_t cap);  // series [n][4]
     void ResetEnergy();
     void ReadCounters(uint64_t* attempts, uint64_t* accepts);
-    void SetTiles(uint32_t items_per_lane, uint32_t max_warps);
+    void SetTiles(uint32_t items_per_lane, uint32_t max_warps, uint32_t wave);
     double Autotune(uint32_t trial_sweeps);   // returns the best trial's seconds per sweep
     void Sync();
 
     uint32_t n_chains = 0, series_cap = 0;
     int device = 0, n_sm = 0;
-    uint32_t items_per_lane = 2, max_warps = 16;  // pair tile (the autotuner's usual choice)
+    uint32_t items_per_lane = 2, max_warps = 16, wave = 1;  // pair tile and attempts in flight per chain
     cudaStream_t stream = nullptr;
     std::vector<ChainSpec> specs;
     std::vector<ChainDev> chains;
@@ -105,6 +107,7 @@ class ChainBatch {
     void ResetGraph();
     std::unique_ptr<DeviceBuffer> pos_, chains_dev_, order_dev_, att_, acc_, series_, n_meas_, err_, last_;
     float4* staging_ = nullptr;  // pinned host mirror of pos_ for bulk transfers
+    std::vector<uint64_t> path_off_;  // first double of each chain in the concatenated host layout
     size_t pos_float4 = 0;
     cudaGraphExec_t graph_ = nullptr;
     uint64_t graph_sweeps_ = 0;

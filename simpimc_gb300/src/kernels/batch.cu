@@ -25,6 +25,7 @@
 #include <cstring>
 #include <ctime>
 #include <numeric>
+#include <thread>
 
 #include "../../../include/simpimc_gb300.h"
 #include "../common/philox.h"
@@ -93,14 +94,16 @@ __device__ __forceinline__ float Img(float d, float L, float iL) {
 
 constexpr uint32_t kItems = 4;  // pair items per lane kept in registers (more are loaded in the loop)
 
-/// Draws of one attempt (particle, first bead, normals, log-uniforms; philox.h stream layout) and
-/// the moved particle's segment, by one warp into one of two shared buffers.
+/// Draws of one attempt (particle, first bead, normals, log-uniforms; philox.h stream layout) into
+/// shared buffers, by one warp; with `seg` also the moved particle's segment as it is now.
 __device__ __forceinline__ void DrawAttempt(const MoveStream& st, uint32_t lane, uint32_t N, uint32_t M, uint32_t B, uint32_t NL, uint32_t n_pad,
                                             const float4* __restrict__ pos, float* z, float* logu, float4* seg, uint32_t* pb) {
     const Philox4 w0 = st.Block(0);
     const uint32_t p = UniformIndex(w0.v[0], N), b0 = UniformIndex(w0.v[1], M);
-    if (lane <= B) seg[lane] = pos[(size_t)Wrap(b0 + lane, M) * n_pad + p];
-    if (B == 32 && lane == 0) seg[32] = pos[(size_t)Wrap(b0 + 32u, M) * n_pad + p];
+    if (seg) {
+        if (lane <= B) seg[lane] = pos[(size_t)Wrap(b0 + lane, M) * n_pad + p];
+        if (B == 32 && lane == 0) seg[32] = pos[(size_t)Wrap(b0 + 32u, M) * n_pad + p];
+    }
     if (lane == 0) {
         pb[0] = p;
         pb[1] = b0;
@@ -119,6 +122,183 @@ __device__ __forceinline__ void DrawAttempt(const MoveStream& st, uint32_t lane,
     }
 }
 
+/// Warp work of one attempt (bisect_class.h:39-124 above level 0): lane k enters with bead k of
+/// the old segment (every lane also holds the last bead B in e*), samples the new beads level by
+/// level in registers (bead k = 2^l (2m + 1) from beads k -+ 2^l by shuffles), forms each level's
+/// sampling, kinetic and trap terms, reduces them with one compensated butterfly per level and
+/// quantity, writes both segment copies for the pair work, and tests every level above 0. Returns
+/// with the new bead in n*.
+template <bool kPbc>
+__device__ __forceinline__ void LeaderPhase(const ChainDev& c, uint32_t lane, uint32_t B, uint32_t NL, uint32_t M, float ox, float oy, float oz,
+                                            float ex, float ey, float ez, const float* zb, const float* logu, float* s_old, float* s_new,
+                                            dd* base0_out, int* upper_out, float& nx, float& ny, float& nz) {
+    const float L = c.L, iL = c.iL;
+    const bool kin_links = B != M;  // whole-ring segment: no kinetic links (kinetic_class.h:111-117)
+    const bool inner = lane >= 1 && lane < B;
+    const uint32_t lk = lane == 0 ? 31u : (uint32_t)(__ffs(lane) - 1);  // level of bead `lane`
+    nx = ox;
+    ny = oy;
+    nz = oz;
+    float dn2 = 0.f;
+    for (int li = (int)NL - 1; li >= 0; --li) {
+        const uint32_t skip = 1u << li;
+        const bool mine = inner && lk == (uint32_t)li;
+        const uint32_t sa = mine ? lane - skip : lane, sc = mine ? lane + skip : lane;
+        const float ax = __shfl_sync(0xffffffffu, nx, sa & 31u), ay = __shfl_sync(0xffffffffu, ny, sa & 31u),
+                    az = __shfl_sync(0xffffffffu, nz, sa & 31u);
+        float cx = __shfl_sync(0xffffffffu, nx, sc & 31u), cy = __shfl_sync(0xffffffffu, ny, sc & 31u),
+              cz = __shfl_sync(0xffffffffu, nz, sc & 31u);
+        if (sc == 32u) {
+            cx = ex;
+            cy = ey;
+            cz = ez;
+        }
+        if (mine) {
+            const uint32_t zi = 3 * ((B >> (li + 1)) - 1u + (lane >> (li + 1)));
+            const float sg = c.sigma[li];
+            const float dx = Img<kPbc>(__fmul_rn(sg, zb[zi]), L, iL), dy = Img<kPbc>(__fmul_rn(sg, zb[zi + 1]), L, iL),
+                        dz = Img<kPbc>(__fmul_rn(sg, zb[zi + 2]), L, iL);
+            nx = __fadd_rn(__fadd_rn(ax, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cx, ax), L, iL))), dx);
+            ny = __fadd_rn(__fadd_rn(ay, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cy, ay), L, iL))), dy);
+            nz = __fadd_rn(__fadd_rn(az, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cz, az), L, iL))), dz);
+            dn2 = Sq3(dx, dy, dz);
+        }
+    }
+    // Old sampling displacement of bead `lane` on its level.
+    float samp = 0.f;
+    {
+        const uint32_t skip = inner ? (1u << lk) : 0u;
+        const uint32_t sa = inner ? lane - skip : lane, sc = inner ? lane + skip : lane;
+        const float ax = __shfl_sync(0xffffffffu, ox, sa & 31u), ay = __shfl_sync(0xffffffffu, oy, sa & 31u),
+                    az = __shfl_sync(0xffffffffu, oz, sa & 31u);
+        float cx = __shfl_sync(0xffffffffu, ox, sc & 31u), cy = __shfl_sync(0xffffffffu, oy, sc & 31u),
+              cz = __shfl_sync(0xffffffffu, oz, sc & 31u);
+        if (sc == 32u) {
+            cx = ex;
+            cy = ey;
+            cz = ez;
+        }
+        if (inner) {
+            const float bx = __fadd_rn(ax, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cx, ax), L, iL)));
+            const float by = __fadd_rn(ay, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cy, ay), L, iL)));
+            const float bz = __fadd_rn(az, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cz, az), L, iL)));
+            const float do2 = Sq3(Img<kPbc>(__fsub_rn(ox, bx), L, iL), Img<kPbc>(__fsub_rn(oy, by), L, iL), Img<kPbc>(__fsub_rn(oz, bz), L, iL));
+            samp = __fmul_rn(c.i4lt_sample[lk], __fsub_rn(dn2, do2));  // log sample ratio term
+        }
+    }
+    // Per level l and lane k (a multiple of 2^l): the action change of link k -> k + 2^l
+    // (kinetic) and slice k (trap); the level's totals come from one compensated butterfly each
+    // for  D_l = sum of action changes  and  R_l = sampling ratio - D_l.
+    Comp Dl[kBatchMaxLevels], Rl[kBatchMaxLevels];
+#pragma unroll
+    for (uint32_t li = 0; li < kBatchMaxLevels; ++li) {
+        float dterm = 0.f;
+        if (li < NL) {
+            const uint32_t skip = 1u << li;
+            const bool mine = lane < B && (lane & (skip - 1u)) == 0u;
+            const uint32_t sc = mine ? lane + skip : lane;
+            float cx = __shfl_sync(0xffffffffu, nx, sc & 31u), cy = __shfl_sync(0xffffffffu, ny, sc & 31u),
+                  cz = __shfl_sync(0xffffffffu, nz, sc & 31u);
+            float dx = __shfl_sync(0xffffffffu, ox, sc & 31u), dy = __shfl_sync(0xffffffffu, oy, sc & 31u),
+                  dz = __shfl_sync(0xffffffffu, oz, sc & 31u);
+            if (sc == 32u) {
+                cx = dx = ex;
+                cy = dy = ey;
+                cz = dz = ez;
+            }
+            if (mine) {
+                if (kin_links) {
+                    const float kn = Sq3(Img<kPbc>(__fsub_rn(nx, cx), L, iL), Img<kPbc>(__fsub_rn(ny, cy), L, iL), Img<kPbc>(__fsub_rn(nz, cz), L, iL));
+                    const float ko = Sq3(Img<kPbc>(__fsub_rn(ox, dx), L, iL), Img<kPbc>(__fsub_rn(oy, dy), L, iL), Img<kPbc>(__fsub_rn(oz, dz), L, iL));
+                    dterm = __fmul_rn(c.i4lt_level[li], __fsub_rn(kn, ko));
+                }
+                if (c.has_trap && (int)li <= c.trap_max_level)
+                    dterm = __fadd_rn(dterm, __fmul_rn(__fmul_rn(c.trap_cofa, (float)skip), __fsub_rn(Sq3(nx, ny, nz), Sq3(ox, oy, oz))));
+            }
+        }
+        Dl[li] = Comp{dterm, 0.f};
+        Rl[li] = Comp{__fsub_rn(inner && lk == li ? samp : 0.f, dterm), 0.f};
+    }
+#pragma unroll
+    for (uint32_t li = 0; li < kBatchMaxLevels; ++li)
+        if (li < NL) {
+            Dl[li] = CompWarpSum(Dl[li], 32);
+            Rl[li] = CompWarpSum(Rl[li], 32);
+        }
+    // Segment copies for the pair work.
+    if (lane <= B) {
+        s_old[3 * lane] = ox;
+        s_old[3 * lane + 1] = oy;
+        s_old[3 * lane + 2] = oz;
+        s_new[3 * lane] = nx;
+        s_new[3 * lane + 1] = ny;
+        s_new[3 * lane + 2] = nz;
+    }
+    if (B == 32 && lane == 0) {
+        s_old[96] = s_new[96] = ex;
+        s_old[97] = s_new[97] = ey;
+        s_old[98] = s_new[98] = ez;
+    }
+    // Level l passes if  R_l + D_{l+1} >= log u_l  (bisect_class.h:110-121); every lane holds every
+    // level's totals, so lane l tests level l.
+    bool fail = false;
+    dd base0 = DD(0.f);
+#pragma unroll
+    for (uint32_t li = 0; li < kBatchMaxLevels; ++li)
+        if (li < NL) {
+            dd la = CompDD(Rl[li]);
+            if (li + 1 < NL) la = Add(la, CompDD(Dl[li + 1]));
+            if (!isfinite(la.hi)) la.hi = -INFINITY;
+            if (li == 0) base0 = la;
+            else if (lane == li) fail = Less(la, DD(logu[li]));
+        }
+    const unsigned fails = __ballot_sync(0xffffffffu, fail);
+    if (lane == 0) {
+        *upper_out = fails == 0u;
+        *base0_out = base0;
+    }
+}
+
+/// Pair items of one attempt: (inner slice k in 1..B-1) x (other particle q), item i -> k = i /
+/// (N-1); this lane's first kItems items (attempt-independent decomposition in it_k / it_q,
+/// beads already in pre[]) and any further ones at stride T. Returns the lane's compensated sum
+/// of 1/r_new - 1/r_old (clamped to the table's grid).
+template <bool kPbc>
+__device__ __forceinline__ Comp PairPhase(const ChainDev& c, uint32_t t, uint32_t T, uint32_t n_items, uint32_t magic, uint32_t nm1, uint32_t p,
+                                          uint32_t b0, uint32_t M, uint32_t n_pad, const float4* __restrict__ pos, const uint32_t* it_k,
+                                          const float4* pre, const float* s_old, const float* s_new) {
+    const float L = c.L, iL = c.iL, r2_min = c.r2_min, r2_max = c.r2_max;
+    Comp acc_u{0.f, 0.f};
+    auto item = [&](uint32_t k, float4 rq) {
+        const float* ro = s_old + 3 * (k + 1);
+        const float* rn = s_new + 3 * (k + 1);
+        float r2o = Sq3(Img<kPbc>(__fsub_rn(ro[0], rq.x), L, iL), Img<kPbc>(__fsub_rn(ro[1], rq.y), L, iL), Img<kPbc>(__fsub_rn(ro[2], rq.z), L, iL));
+        float r2n = Sq3(Img<kPbc>(__fsub_rn(rn[0], rq.x), L, iL), Img<kPbc>(__fsub_rn(rn[1], rq.y), L, iL), Img<kPbc>(__fsub_rn(rn[2], rq.z), L, iL));
+        r2o = fminf(fmaxf(r2o, r2_min), r2_max);
+        r2n = fminf(fmaxf(r2n, r2_min), r2_max);
+        CompAdd(acc_u, __fsub_rn(rsqrtf(r2n), rsqrtf(r2o)));
+    };
+#pragma unroll
+    for (uint32_t j = 0; j < kItems; ++j)
+        if (t + j * T < n_items) item(it_k[j], pre[j]);
+    for (uint32_t i = t + kItems * T; i < n_items; i += T) {
+        const uint32_t k = FastDiv(i, magic), qq = i - k * nm1;
+        item(k, pos[(size_t)Wrap(b0 + 1u + k, M) * n_pad + qq + (qq >= p ? 1u : 0u)]);
+    }
+    return acc_u;
+}
+
+/// Level-0 test: pair action difference tau * sum (1/r_new - 1/r_old) over inner slices (each
+/// inner slice closes two links with weight 1/2; the segment ends cancel) joins the level's
+/// double-float total. Every lane of the calling warp gets the same answer.
+__device__ __forceinline__ bool Level0Accepts(const ChainDev& c, uint32_t lane, uint32_t G, const Comp* part, bool has_items, dd base0, float logu0) {
+    dd u = DD(0.f);
+    if (has_items) u = CompDD(CompWarpSum(lane < G ? part[lane] : Comp{0.f, 0.f}, 32));
+    dd la0 = Sub(base0, MulF(u, c.tau));
+    if (!isfinite(la0.hi)) la0.hi = -INFINITY;
+    return !Less(la0, DD(logu0));
+}
+
 struct SweepShared {
     ChainDev c;
     float z[2][3 * (kMaxB - 1)];
@@ -131,18 +311,16 @@ struct SweepShared {
     int upper_ok;
 };
 
+/// One attempt at a time (warp 0 leads; warp 1 draws the next attempt and loads its segment,
+/// which is patched from warp 0's registers when both attempts move the same particle).
 template <bool kPbc>
 __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_t ci, uint32_t G, uint64_t n_sweeps, uint64_t n_attempts) {
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t T = G * 32u, t = threadIdx.x;
     const ChainDev& c = sh.c;
     const uint32_t N = c.n_part, M = c.n_bead, NL = c.n_level, B = 1u << NL, n_pad = c.n_pad;
-    const float L = c.L, iL = c.iL;
-    const bool kin_links = B != M;  // whole-ring segment: no kinetic links (kinetic_class.h:111-117)
     float4* __restrict__ pos = a.pos + c.pos_off;
 
-    // Pair items: (inner slice k in 1..B-1) x (other particle); item i -> k = 1 + i / (N-1). The
-    // decomposition of this lane's first kItems items does not depend on the attempt.
     const uint32_t nm1 = N > 1 ? N - 1 : 1;
     const uint32_t n_items = c.has_pair && N > 1 ? (N - 1) * (B - 1) : 0u;
     const uint32_t magic = (uint32_t)((0x100000000ull + nm1 - 1) / nm1);
@@ -153,13 +331,9 @@ __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_
         it_k[j] = FastDiv(i, magic);
         it_q[j] = i - it_k[j] * nm1;
     }
-    const float r2_min = c.r2_min, r2_max = c.r2_max, tau = c.tau;
 
     uint64_t att = a.attempts[ci], acc = a.accepts[ci];
     const uint64_t n_att = n_sweeps ? n_sweeps * c.attempts_per_sweep : n_attempts;
-    // With two or more warps, warp 1 draws attempt k+1 (and loads its segment) while warp 0
-    // works on attempt k; a segment loaded before attempt k's commit is patched from warp 0's
-    // registers when both attempts move the same particle.
     const bool ahead = G >= 2;
     if (ahead && warp == 1 && n_att > 0)
         DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, att}, lane, N, M, B, NL, n_pad, pos, sh.z[att & 1], sh.logu[att & 1], sh.seg[att & 1],
@@ -183,7 +357,6 @@ __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_
             if (t + j * T < n_items) pre[j] = pos[(size_t)Wrap(b0 + 1u + it_k[j], M) * n_pad + it_q[j] + (it_q[j] >= p ? 1u : 0u)];
 
         if (warp == 0) {
-            // Old segment: lane k holds bead k; every lane holds the last bead B.
             const float4 sv = sh.seg[buf][lane <= B ? lane : B];
             const float4 se = sh.seg[buf][B];
             float ox = sv.x, oy = sv.y, oz = sv.z, ex = se.x, ey = se.y, ez = se.z;
@@ -207,132 +380,8 @@ __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_
                     ez = qz;
                 }
             }
-            // Sampling, level by level (bisect_class.h:77-107): bead k = 2^l (2m + 1) is resampled
-            // on level l from beads k -+ 2^l; positions travel by shuffles.
-            const float* zb = sh.z[buf];
-            const bool inner = lane >= 1 && lane < B;
-            const uint32_t lk = lane == 0 ? 31u : (uint32_t)(__ffs(lane) - 1);  // level of bead `lane`
-            nx = ox;
-            ny = oy;
-            nz = oz;
-            float dn2 = 0.f;
-            for (int li = (int)NL - 1; li >= 0; --li) {
-                const uint32_t skip = 1u << li;
-                const bool mine = inner && lk == (uint32_t)li;
-                const uint32_t sa = mine ? lane - skip : lane, sc = mine ? lane + skip : lane;
-                const float ax = __shfl_sync(0xffffffffu, nx, sa & 31u), ay = __shfl_sync(0xffffffffu, ny, sa & 31u),
-                            az = __shfl_sync(0xffffffffu, nz, sa & 31u);
-                float cx = __shfl_sync(0xffffffffu, nx, sc & 31u), cy = __shfl_sync(0xffffffffu, ny, sc & 31u),
-                      cz = __shfl_sync(0xffffffffu, nz, sc & 31u);
-                if (sc == 32u) {
-                    cx = ex;
-                    cy = ey;
-                    cz = ez;
-                }
-                if (mine) {
-                    const uint32_t zi = 3 * ((B >> (li + 1)) - 1u + (lane >> (li + 1)));
-                    const float sg = c.sigma[li];
-                    const float dx = Img<kPbc>(__fmul_rn(sg, zb[zi]), L, iL), dy = Img<kPbc>(__fmul_rn(sg, zb[zi + 1]), L, iL),
-                                dz = Img<kPbc>(__fmul_rn(sg, zb[zi + 2]), L, iL);
-                    nx = __fadd_rn(__fadd_rn(ax, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cx, ax), L, iL))), dx);
-                    ny = __fadd_rn(__fadd_rn(ay, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cy, ay), L, iL))), dy);
-                    nz = __fadd_rn(__fadd_rn(az, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cz, az), L, iL))), dz);
-                    dn2 = Sq3(dx, dy, dz);
-                }
-            }
-            // Old sampling displacement of bead `lane` on its level.
-            float samp = 0.f;
-            {
-                const uint32_t skip = inner ? (1u << lk) : 0u;
-                const uint32_t sa = inner ? lane - skip : lane, sc = inner ? lane + skip : lane;
-                const float ax = __shfl_sync(0xffffffffu, ox, sa & 31u), ay = __shfl_sync(0xffffffffu, oy, sa & 31u),
-                            az = __shfl_sync(0xffffffffu, oz, sa & 31u);
-                float cx = __shfl_sync(0xffffffffu, ox, sc & 31u), cy = __shfl_sync(0xffffffffu, oy, sc & 31u),
-                      cz = __shfl_sync(0xffffffffu, oz, sc & 31u);
-                if (sc == 32u) {
-                    cx = ex;
-                    cy = ey;
-                    cz = ez;
-                }
-                if (inner) {
-                    const float bx = __fadd_rn(ax, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cx, ax), L, iL)));
-                    const float by = __fadd_rn(ay, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cy, ay), L, iL)));
-                    const float bz = __fadd_rn(az, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cz, az), L, iL)));
-                    const float do2 = Sq3(Img<kPbc>(__fsub_rn(ox, bx), L, iL), Img<kPbc>(__fsub_rn(oy, by), L, iL), Img<kPbc>(__fsub_rn(oz, bz), L, iL));
-                    samp = __fmul_rn(c.i4lt_sample[lk], __fsub_rn(dn2, do2));  // log sample ratio term
-                }
-            }
-            // Per level l and lane k (a multiple of 2^l): the action change of link k -> k + 2^l
-            // (kinetic) and slice k (trap); the level's totals come from one compensated butterfly
-            // each for  D_l = sum of action changes  and  R_l = sampling ratio - D_l.
-            Comp Dl[kBatchMaxLevels], Rl[kBatchMaxLevels];
-#pragma unroll
-            for (uint32_t li = 0; li < kBatchMaxLevels; ++li) {
-                float dterm = 0.f;
-                if (li < NL) {
-                    const uint32_t skip = 1u << li;
-                    const bool mine = lane < B && (lane & (skip - 1u)) == 0u;
-                    const uint32_t sc = mine ? lane + skip : lane;
-                    float cx = __shfl_sync(0xffffffffu, nx, sc & 31u), cy = __shfl_sync(0xffffffffu, ny, sc & 31u),
-                          cz = __shfl_sync(0xffffffffu, nz, sc & 31u);
-                    float dx = __shfl_sync(0xffffffffu, ox, sc & 31u), dy = __shfl_sync(0xffffffffu, oy, sc & 31u),
-                          dz = __shfl_sync(0xffffffffu, oz, sc & 31u);
-                    if (sc == 32u) {
-                        cx = dx = ex;
-                        cy = dy = ey;
-                        cz = dz = ez;
-                    }
-                    if (mine) {
-                        if (kin_links) {
-                            const float kn = Sq3(Img<kPbc>(__fsub_rn(nx, cx), L, iL), Img<kPbc>(__fsub_rn(ny, cy), L, iL), Img<kPbc>(__fsub_rn(nz, cz), L, iL));
-                            const float ko = Sq3(Img<kPbc>(__fsub_rn(ox, dx), L, iL), Img<kPbc>(__fsub_rn(oy, dy), L, iL), Img<kPbc>(__fsub_rn(oz, dz), L, iL));
-                            dterm = __fmul_rn(c.i4lt_level[li], __fsub_rn(kn, ko));
-                        }
-                        if (c.has_trap && (int)li <= c.trap_max_level)
-                            dterm = __fadd_rn(dterm, __fmul_rn(__fmul_rn(c.trap_cofa, (float)skip), __fsub_rn(Sq3(nx, ny, nz), Sq3(ox, oy, oz))));
-                    }
-                }
-                Dl[li] = Comp{dterm, 0.f};
-                Rl[li] = Comp{__fsub_rn(inner && lk == li ? samp : 0.f, dterm), 0.f};
-            }
-#pragma unroll
-            for (uint32_t li = 0; li < kBatchMaxLevels; ++li)
-                if (li < NL) {
-                    Dl[li] = CompWarpSum(Dl[li], 32);
-                    Rl[li] = CompWarpSum(Rl[li], 32);
-                }
-            // Segment copies for the pair work of all warps.
-            if (lane <= B) {
-                sh.old_[3 * lane] = ox;
-                sh.old_[3 * lane + 1] = oy;
-                sh.old_[3 * lane + 2] = oz;
-                sh.new_[3 * lane] = nx;
-                sh.new_[3 * lane + 1] = ny;
-                sh.new_[3 * lane + 2] = nz;
-            }
-            if (B == 32 && lane == 0) {
-                sh.old_[96] = sh.new_[96] = ex;
-                sh.old_[97] = sh.new_[97] = ey;
-                sh.old_[98] = sh.new_[98] = ez;
-            }
-            // Level l passes if  R_l + D_{l+1} >= log u_l  (bisect_class.h:110-121); every lane
-            // holds every level's totals, so lane l tests level l.
-            bool fail = false;
-            dd base0 = DD(0.f);
-#pragma unroll
-            for (uint32_t li = 0; li < kBatchMaxLevels; ++li)
-                if (li < NL) {
-                    dd la = CompDD(Rl[li]);
-                    if (li + 1 < NL) la = Add(la, CompDD(Dl[li + 1]));
-                    if (!isfinite(la.hi)) la.hi = -INFINITY;
-                    if (li == 0) base0 = la;
-                    else if (lane == li) fail = Less(la, DD(sh.logu[buf][li]));
-                }
-            const unsigned fails = __ballot_sync(0xffffffffu, fail);
-            if (lane == 0) {
-                sh.upper_ok = fails == 0u;
-                sh.base0 = base0;
-            }
+            LeaderPhase<kPbc>(c, lane, B, NL, M, ox, oy, oz, ex, ey, ez, sh.z[buf], sh.logu[buf], sh.old_, sh.new_, &sh.base0, &sh.upper_ok,
+                              nx, ny, nz);
         } else if (ahead && warp == 1 && it + 1 < n_att) {
             DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, att + 1}, lane, N, M, B, NL, n_pad, pos, sh.z[buf ^ 1u], sh.logu[buf ^ 1u],
                         sh.seg[buf ^ 1u], sh.pb[buf ^ 1u]);
@@ -341,39 +390,13 @@ __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_
         const bool upper_ok = sh.upper_ok != 0;
 
         if (upper_ok && n_items) {
-            Comp acc_u{0.f, 0.f};
-            auto item = [&](uint32_t k, float4 rq) {
-                const float* ro = sh.old_ + 3 * (k + 1);
-                const float* rn = sh.new_ + 3 * (k + 1);
-                float r2o = Sq3(Img<kPbc>(__fsub_rn(ro[0], rq.x), L, iL), Img<kPbc>(__fsub_rn(ro[1], rq.y), L, iL), Img<kPbc>(__fsub_rn(ro[2], rq.z), L, iL));
-                float r2n = Sq3(Img<kPbc>(__fsub_rn(rn[0], rq.x), L, iL), Img<kPbc>(__fsub_rn(rn[1], rq.y), L, iL), Img<kPbc>(__fsub_rn(rn[2], rq.z), L, iL));
-                r2o = fminf(fmaxf(r2o, r2_min), r2_max);
-                r2n = fminf(fmaxf(r2n, r2_min), r2_max);
-                CompAdd(acc_u, __fsub_rn(rsqrtf(r2n), rsqrtf(r2o)));
-            };
-#pragma unroll
-            for (uint32_t j = 0; j < kItems; ++j)
-                if (t + j * T < n_items) item(it_k[j], pre[j]);
-            for (uint32_t i = t + kItems * T; i < n_items; i += T) {
-                const uint32_t k = FastDiv(i, magic), qq = i - k * nm1;
-                item(k, pos[(size_t)Wrap(b0 + 1u + k, M) * n_pad + qq + (qq >= p ? 1u : 0u)]);
-            }
-            const Comp u = CompWarpSum(acc_u, 32);
+            const Comp u = CompWarpSum(PairPhase<kPbc>(c, t, T, n_items, magic, nm1, p, b0, M, n_pad, pos, it_k, pre, sh.old_, sh.new_), 32);
             if (lane == 0) sh.part[warp] = u;
         }
         GroupSync(G);
 
         if (warp == 0) {
-            bool accepted = upper_ok;
-            if (upper_ok) {
-                // Level 0: pair action difference tau * sum (1/r_new - 1/r_old) over inner slices
-                // (each inner slice closes two links with weight 1/2; the segment ends cancel).
-                dd u = DD(0.f);
-                if (n_items) u = CompDD(CompWarpSum(lane < G ? sh.part[lane] : Comp{0.f, 0.f}, 32));  // same total on every lane
-                dd la0 = Sub(sh.base0, MulF(u, tau));
-                if (!isfinite(la0.hi)) la0.hi = -INFINITY;
-                accepted = !Less(la0, DD(sh.logu[buf][0]));
-            }
+            const bool accepted = upper_ok && Level0Accepts(c, lane, G, sh.part, n_items != 0, sh.base0, sh.logu[buf][0]);
             if (accepted && lane >= 1 && lane < B) pos[(size_t)Wrap(b0 + lane, M) * n_pad + p] = make_float4(nx, ny, nz, 0.f);
             acc += accepted ? 1u : 0u;
             acc_prev = accepted;
@@ -388,20 +411,152 @@ __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Several attempts of one chain at a time. Attempt j (later in the chain) does not see attempt i's
+// changes when they share nothing it reads: a different particle whose inner slices miss i's
+// inner slices (its pair terms read the others only there), or the same particle with its whole
+// segment clear of i's inner slices. A round takes the longest prefix of the next W drawn
+// attempts in which every attempt is clear of all earlier ones; they run concurrently, one per
+// sub-group of warps, and commit disjoint beads. The result is the sequential chain's.
+
+struct WaveShared {
+    ChainDev c;
+    float z[2 * kMaxWave][3 * (kMaxB - 1)];  // ring of drawn attempts, slot = attempt mod 2W
+    float logu[2 * kMaxWave][kBatchMaxLevels];
+    uint32_t pb[2 * kMaxWave][2];
+    float old_[kMaxWave][3 * (kMaxB + 1)], new_[kMaxWave][3 * (kMaxB + 1)];
+    Comp part[kMaxWave][kBatchMaxWarps];
+    dd base0[kMaxWave];
+    int upper_ok[kMaxWave];
+    unsigned int accepts;
+};
+
+__device__ __forceinline__ bool CircOverlap(uint32_t s1, uint32_t l1, uint32_t s2, uint32_t l2, uint32_t M) {
+    return Wrap(s2 + M - s1, M) < l1 || Wrap(s1 + M - s2, M) < l2;
+}
+
+/// Does attempt j (later) read anything attempt i changes?
+__device__ __forceinline__ bool Conflicts(uint32_t pi, uint32_t bi, uint32_t pj, uint32_t bj, uint32_t B, uint32_t M) {
+    const uint32_t si = Wrap(bi + 1u, M);  // inner slices of i: [bi+1, bi+B-1]
+    if (pi == pj) return B + 1 > M || CircOverlap(si, B - 1, bj, B + 1, M);
+    return CircOverlap(si, B - 1, Wrap(bj + 1u, M), B - 1, M);
+}
+
+__device__ __forceinline__ void SubSync(uint32_t id, uint32_t n_warps) {
+    if (n_warps == 1) __syncwarp();
+    else asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n_warps * 32u) : "memory");
+}
+
+template <bool kPbc>
+__device__ __forceinline__ void SweepChainW(WaveShared& sh, BatchArgs a, uint32_t ci, uint64_t n_sweeps, uint64_t n_attempts) {
+    const ChainDev& c = sh.c;
+    const uint32_t W = c.n_wave, Gs = c.sub_warps, G = W * Gs, R = 2 * W;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t sg = warp / Gs, ws = warp - sg * Gs, Ts = Gs * 32u, ts = ws * 32u + lane;
+    const uint32_t N = c.n_part, M = c.n_bead, NL = c.n_level, B = 1u << NL, n_pad = c.n_pad;
+    float4* __restrict__ pos = a.pos + c.pos_off;
+    const uint32_t draw_warp = Gs >= 2 ? 1u : 0u;
+
+    const uint32_t nm1 = N > 1 ? N - 1 : 1;
+    const uint32_t n_items = c.has_pair && N > 1 ? (N - 1) * (B - 1) : 0u;
+    const uint32_t magic = (uint32_t)((0x100000000ull + nm1 - 1) / nm1);
+    uint32_t it_k[kItems], it_q[kItems];
+#pragma unroll
+    for (uint32_t j = 0; j < kItems; ++j) {
+        const uint32_t i = ts + j * Ts;
+        it_k[j] = FastDiv(i, magic);
+        it_q[j] = i - it_k[j] * nm1;
+    }
+
+    uint64_t A = a.attempts[ci];
+    const uint64_t end = A + (n_sweeps ? n_sweeps * c.attempts_per_sweep : n_attempts);
+    if (threadIdx.x == 0) sh.accepts = 0;
+    // Prologue: the first 2W attempts' draws, attempt A + x by sub-group x mod W.
+    if (ws == draw_warp)
+        for (uint64_t x = A + sg; x < end && x < A + R; x += W)
+            DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, x}, lane, N, M, B, NL, n_pad, pos, sh.z[x % R], sh.logu[x % R], nullptr, sh.pb[x % R]);
+    SubSync(15, G);
+
+    while (A < end) {
+        // The round's attempts: the longest conflict-free prefix of the next W (same on all lanes).
+        uint32_t w = 1;
+        for (uint32_t j = 1; j < W && A + j < end; ++j) {
+            const uint32_t* pj = sh.pb[(A + j) % R];
+            bool clear = true;
+            for (uint32_t i = 0; i < j && clear; ++i) {
+                const uint32_t* pi = sh.pb[(A + i) % R];
+                clear = !Conflicts(pi[0], pi[1], pj[0], pj[1], B, M);
+            }
+            if (!clear) break;
+            ++w;
+        }
+        if (sg < w) {
+            const uint64_t x = A + sg;
+            const uint32_t slot = (uint32_t)(x % R);
+            const uint32_t p = sh.pb[slot][0], b0 = sh.pb[slot][1];
+            float4 pre[kItems];
+#pragma unroll
+            for (uint32_t j = 0; j < kItems; ++j)
+                if (ts + j * Ts < n_items) pre[j] = pos[(size_t)Wrap(b0 + 1u + it_k[j], M) * n_pad + it_q[j] + (it_q[j] >= p ? 1u : 0u)];
+            float nx = 0.f, ny = 0.f, nz = 0.f;
+            if (ws == 0) {
+                const float4 sv = pos[(size_t)Wrap(b0 + (lane <= B ? lane : B), M) * n_pad + p];
+                const float4 se = pos[(size_t)Wrap(b0 + B, M) * n_pad + p];
+                LeaderPhase<kPbc>(c, lane, B, NL, M, sv.x, sv.y, sv.z, se.x, se.y, se.z, sh.z[slot], sh.logu[slot], sh.old_[sg], sh.new_[sg],
+                                  &sh.base0[sg], &sh.upper_ok[sg], nx, ny, nz);
+            }
+            // The draw that completes the next window: attempt A + W + sg (its slot is not in use).
+            if (ws == draw_warp && A + W + sg < end) {
+                const uint64_t y = A + W + sg;
+                if (draw_warp == 0) __syncwarp();
+                DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, y}, lane, N, M, B, NL, n_pad, pos, sh.z[y % R], sh.logu[y % R], nullptr, sh.pb[y % R]);
+            }
+            SubSync(1 + sg, Gs);
+            const bool upper_ok = sh.upper_ok[sg] != 0;
+            if (upper_ok && n_items) {
+                const Comp u = CompWarpSum(PairPhase<kPbc>(c, ts, Ts, n_items, magic, nm1, p, b0, M, n_pad, pos, it_k, pre, sh.old_[sg], sh.new_[sg]), 32);
+                if (lane == 0) sh.part[sg][ws] = u;
+            }
+            SubSync(1 + sg, Gs);
+            if (ws == 0) {
+                const bool accepted = upper_ok && Level0Accepts(c, lane, Gs, sh.part[sg], n_items != 0, sh.base0[sg], sh.logu[slot][0]);
+                if (accepted && lane >= 1 && lane < B) pos[(size_t)Wrap(b0 + lane, M) * n_pad + p] = make_float4(nx, ny, nz, 0.f);
+                if (accepted && lane == 0) atomicAdd(&sh.accepts, 1u);
+            }
+        }
+        SubSync(15, G);
+        A += w;
+    }
+    if (threadIdx.x == 0) {
+        a.attempts[ci] = A;
+        a.accepts[ci] += sh.accepts;
+    }
+}
+
+union BatchShared {
+    SweepShared one;
+    WaveShared wave;
+};
+
 __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArgs a, uint64_t n_sweeps, uint64_t n_attempts) {
     const uint32_t ci = a.order[blockIdx.x];
     const uint32_t warp = threadIdx.x >> 5;
     const uint32_t G = a.chains[ci].n_warps;
     if (warp >= G) return;
-    __shared__ SweepShared sh;
+    __shared__ BatchShared sh;
     {
         const uint32_t* src = reinterpret_cast<const uint32_t*>(a.chains + ci);
-        uint32_t* dst = reinterpret_cast<uint32_t*>(&sh.c);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(&sh.one.c);
         for (uint32_t i = threadIdx.x; i < sizeof(ChainDev) / 4; i += G * 32u) dst[i] = src[i];
     }
     GroupSync(G);
-    if (sh.c.pbc) SweepChain<true>(sh, a, ci, G, n_sweeps, n_attempts);
-    else SweepChain<false>(sh, a, ci, G, n_sweeps, n_attempts);
+    if (sh.one.c.n_wave > 1) {
+        if (sh.one.c.pbc) SweepChainW<true>(sh.wave, a, ci, n_sweeps, n_attempts);
+        else SweepChainW<false>(sh.wave, a, ci, n_sweeps, n_attempts);
+    } else {
+        if (sh.one.c.pbc) SweepChain<true>(sh.one, a, ci, G, n_sweeps, n_attempts);
+        else SweepChain<false>(sh.one, a, ci, G, n_sweeps, n_attempts);
+    }
 }
 
 /// Thermal energy estimator of one chain (Energy::Accumulate with use_thermal, energy_class.h:
@@ -618,6 +773,7 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
         c.kin_const = (double)s.n_part * s.n_bead * 3. / (2. * s.tau);  // kinetic_class.h:13
         c.i4ltt = 1. / (4. * s.lambda * s.tau * s.tau);
         bead_moves_per_sweep += c.attempts_per_sweep * (B - 1);
+        path_off_.push_back(path_doubles);
         path_doubles += (uint64_t)s.n_part * s.n_bead * 3;
     }
     series_cap = 4096;
@@ -640,7 +796,7 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
     CudaCheck(cudaMemset(acc_->ptr, 0, n_chains * sizeof(uint64_t)), "memset");
     CudaCheck(cudaMemset(n_meas_->ptr, 0, n_chains * sizeof(uint64_t)), "memset");
     CudaCheck(cudaMemset(err_->ptr, 0, sizeof(int)), "memset");
-    SetTiles(items_per_lane, max_warps);
+    SetTiles(items_per_lane, max_warps, wave);
 }
 
 ChainBatch::~ChainBatch() {
@@ -657,14 +813,27 @@ void ChainBatch::ResetGraph() {
 
 /// Pair tile: chain c gets ceil((N-1)(B-1) / (32 items_per_lane)) warps, at most max_warps.
 /// Blocks are ordered by descending work so the longest chains start first.
-void ChainBatch::SetTiles(uint32_t ipl, uint32_t mw) {
-    if (ipl < 1 || mw < 1 || mw > kBatchMaxWarps) throw PimcError(kErrArg, "tile: items_per_lane >= 1, 1 <= max_warps <= 16");
+void ChainBatch::SetTiles(uint32_t ipl, uint32_t mw, uint32_t wave) {
+    if (ipl < 1 || mw < 1 || mw > kBatchMaxWarps || wave < 1 || wave > kMaxWave)
+        throw PimcError(kErrArg, "tile: items_per_lane >= 1, 1 <= max_warps <= 16, 1 <= wave <= 4");
     items_per_lane = ipl;
     max_warps = mw;
+    this->wave = wave;
     for (auto& c : chains) {
         const uint64_t items = (uint64_t)(c.n_part > 1 ? c.n_part - 1 : 1) * ((1u << c.n_level) - 1);
-        const uint64_t g = (items + 32ull * ipl - 1) / (32ull * ipl);
-        c.n_warps = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(g, mw));
+        const uint64_t g = (items + 32ull * ipl - 1) / (32ull * ipl);  // warps one attempt wants
+        uint32_t W = wave;
+        while (W > 1 && mw / W < 2) --W;  // a concurrent attempt needs a leader and a drawing warp
+        if (W > 1) {
+            const uint32_t gs = (uint32_t)std::max<uint64_t>(2, std::min<uint64_t>(g, mw / W));
+            c.n_wave = W;
+            c.sub_warps = gs;
+            c.n_warps = W * gs;
+        } else {
+            c.n_wave = 1;
+            c.n_warps = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(g, mw));
+            c.sub_warps = c.n_warps;
+        }
     }
     order.resize(n_chains);
     std::iota(order.begin(), order.end(), 0u);
@@ -713,12 +882,33 @@ void ChainBatch::GetPath(uint32_t chain, double* p) {
         }
 }
 
-/// Every chain's path in one transfer: converted into the pinned float4 mirror, then one copy.
+/// Runs f(chain) for every chain on a few host threads (contiguous chain ranges).
+template <class F>
+static void ForChains(uint32_t n_chains, F f) {
+    const uint32_t hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const uint32_t nt = std::min(hw, n_chains);
+    std::vector<std::thread> pool;
+    std::vector<std::exception_ptr> errs(nt);
+    for (uint32_t t = 0; t < nt; ++t)
+        pool.emplace_back([&, t] {
+            try {
+                for (uint32_t ci = t * n_chains / nt; ci < (t + 1) * n_chains / nt; ++ci) f(ci);
+            } catch (...) {
+                errs[t] = std::current_exception();
+            }
+        });
+    for (auto& th : pool) th.join();
+    for (auto& e : errs)
+        if (e) std::rethrow_exception(e);
+}
+
+/// Every chain's path in one transfer: converted into the pinned float4 mirror (host threads over
+/// the chains), then one copy.
 void ChainBatch::SetPaths(const double* all) {
     if (!all) throw PimcError(kErrArg, "null paths");
-    const double* src = all;
-    for (uint32_t ci = 0; ci < n_chains; ++ci) {
+    ForChains(n_chains, [&](uint32_t ci) {
         const ChainDev& c = chains[ci];
+        const double* src = all + path_off_[ci];
         float4* dst = staging_ + c.pos_off;
         for (uint32_t i = 0; i < c.n_part; ++i)
             for (uint32_t b = 0; b < c.n_bead; ++b) {
@@ -726,8 +916,7 @@ void ChainBatch::SetPaths(const double* all) {
                 if (!std::isfinite(r[0]) || !std::isfinite(r[1]) || !std::isfinite(r[2])) throw PimcError(kErrArg, "non-finite position");
                 dst[(size_t)b * c.n_pad + i] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.f);
             }
-        src += (size_t)c.n_part * c.n_bead * 3;
-    }
+    });
     CudaCheck(cudaMemcpyAsync(pos_->ptr, staging_, pos_float4 * sizeof(float4), cudaMemcpyHostToDevice, stream), "set paths");
     CudaCheck(cudaStreamSynchronize(stream), "sync");
 }
@@ -736,10 +925,10 @@ void ChainBatch::GetPaths(double* all) {
     if (!all) throw PimcError(kErrArg, "null paths");
     CudaCheck(cudaMemcpyAsync(staging_, pos_->ptr, pos_float4 * sizeof(float4), cudaMemcpyDeviceToHost, stream), "get paths");
     CudaCheck(cudaStreamSynchronize(stream), "sync");
-    double* dst = all;
-    for (uint32_t ci = 0; ci < n_chains; ++ci) {
+    ForChains(n_chains, [&](uint32_t ci) {
         const ChainDev& c = chains[ci];
         const float4* src = staging_ + c.pos_off;
+        double* dst = all + path_off_[ci];
         for (uint32_t i = 0; i < c.n_part; ++i)
             for (uint32_t b = 0; b < c.n_bead; ++b) {
                 const float4 r = src[(size_t)b * c.n_pad + i];
@@ -748,8 +937,7 @@ void ChainBatch::GetPaths(double* all) {
                 o[1] = r.y;
                 o[2] = r.z;
             }
-        dst += (size_t)c.n_part * c.n_bead * 3;
-    }
+    });
 }
 
 void ChainBatch::LastEnergy(double* out) {
@@ -863,13 +1051,15 @@ double ChainBatch::Autotune(uint32_t trial_sweeps) {
     cudaEvent_t e0, e1;
     CudaCheck(cudaEventCreate(&e0), "event");
     CudaCheck(cudaEventCreate(&e1), "event");
-    const uint32_t ipls[] = {2, 4, 8, 16};
-    const uint32_t mws[] = {2, 4, 8, 16};
+    const uint32_t ipls[] = {2, 4, 8};
+    const uint32_t mws[] = {4, 8, 16};
+    const uint32_t waves[] = {1, 2, 4};
     double best = 1e300;
-    uint32_t best_ipl = items_per_lane, best_mw = max_warps;
+    uint32_t best_ipl = items_per_lane, best_mw = max_warps, best_wave = wave;
+    for (uint32_t wv : waves)
     for (uint32_t ipl : ipls)
         for (uint32_t mw : mws) {
-            SetTiles(ipl, mw);
+            SetTiles(ipl, mw, wv);
             LaunchSweep(1, 0);  // warm-up of this shape
             CudaCheck(cudaEventRecord(e0, stream), "event");
             LaunchSweep(trial_sweeps, 0);
@@ -882,6 +1072,7 @@ double ChainBatch::Autotune(uint32_t trial_sweeps) {
                 best = sec;
                 best_ipl = ipl;
                 best_mw = mw;
+                best_wave = wv;
             }
             copy(*pos_, pos_save);
             copy(*att_, att_save);
@@ -889,7 +1080,7 @@ double ChainBatch::Autotune(uint32_t trial_sweeps) {
         }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    SetTiles(best_ipl, best_mw);
+    SetTiles(best_ipl, best_mw, best_wave);
     CudaCheck(cudaStreamSynchronize(stream), "sync");
     return best;
 }
@@ -1028,15 +1219,17 @@ int pimc_batch_counters(pimc_batch* h, uint64_t* attempts, uint64_t* accepts) {
     return BatchGuard(h, [&](pimc::ChainBatch& b) { b.ReadCounters(attempts, accepts); });
 }
 
-int pimc_batch_set_tiles(pimc_batch* h, uint32_t items_per_lane, uint32_t max_warps) {
-    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.SetTiles(items_per_lane, max_warps); });
+int pimc_batch_set_tiles(pimc_batch* h, uint32_t items_per_lane, uint32_t max_warps, uint32_t wave) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.SetTiles(items_per_lane, max_warps, wave); });
 }
 
-int pimc_batch_autotune(pimc_batch* h, uint32_t trial_sweeps, uint32_t* items_per_lane, uint32_t* max_warps, double* sec_per_sweep) {
+int pimc_batch_autotune(pimc_batch* h, uint32_t trial_sweeps, uint32_t* items_per_lane, uint32_t* max_warps, uint32_t* wave,
+                        double* sec_per_sweep) {
     return BatchGuard(h, [&](pimc::ChainBatch& b) {
         const double s = b.Autotune(trial_sweeps);
         if (items_per_lane) *items_per_lane = b.items_per_lane;
         if (max_warps) *max_warps = b.max_warps;
+        if (wave) *wave = b.wave;
         if (sec_per_sweep) *sec_per_sweep = s;
     });
 }

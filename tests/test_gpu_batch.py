@@ -83,6 +83,27 @@ def test_replay_matches_oracle(chains, oracle_mod):
     b.close()
 
 
+@pytest.mark.parametrize("wave", [2, 4])
+def test_concurrent_attempts_replay_oracle(chains, oracle_mod, wave):
+    """Attempts run several at a time (conflict-free prefixes of the draws) give the sequential
+    chain: the oracle's accept counts and positions."""
+    d, items = chains
+    b = make_batch(d, items)
+    b.set_tiles(2, 16, wave)
+    n_att = 300
+    b.attempts(n_att)
+    att, acc = b.counters()
+    assert np.all(att == n_att)
+    for c, (xml, path) in enumerate(items):
+        o = oracle_mod.OracleSim(xml, base_dir=d, chain=c)
+        o.set_path(path)
+        o.move_attempts(0, n_att)
+        assert int(acc[c]) == int(o.move_stats(0)[2]), (c, wave, int(acc[c]), o.move_stats(0))
+        assert np.max(np.abs(b.get_path(c) - o.get_path())) < 1e-4, (c, wave)
+        o.close()
+    b.close()
+
+
 def test_same_chain_as_fp64_gpu_path(chains):
     """Chain i of the batch and a single-chain FP64 context with chain = i make the same moves."""
     d, items = chains
@@ -129,8 +150,8 @@ def test_autotune_keeps_state(chains):
     b.attempts(50)
     before = [b.get_path(c) for c in range(len(items))]
     att0, acc0 = b.counters()
-    ipl, mw, sec = b.autotune(1)
-    assert ipl >= 1 and 1 <= mw <= 16 and sec > 0
+    ipl, mw, wave, sec = b.autotune(1)
+    assert ipl >= 1 and 1 <= mw <= 16 and 1 <= wave <= 4 and sec > 0
     att1, acc1 = b.counters()
     assert np.array_equal(att0, att1) and np.array_equal(acc0, acc1)
     for c in range(len(items)):
@@ -141,9 +162,9 @@ def test_autotune_keeps_state(chains):
 def test_tile_shape_does_not_change_the_chain(chains):
     d, items = chains
     ref = None
-    for ipl, mw in ((1, 16), (4, 4), (32, 1)):
+    for ipl, mw, wave in ((1, 16, 1), (4, 4, 1), (32, 1, 1), (2, 16, 2), (4, 16, 4), (8, 8, 4)):
         b = make_batch(d, items)
-        b.set_tiles(ipl, mw)
+        b.set_tiles(ipl, mw, wave)
         b.attempts(150)
         _, acc = b.counters()
         paths = [b.get_path(c) for c in range(len(items))]
