@@ -1,10 +1,12 @@
 """Small fixed workloads for profiler captures (one warm-up launch, then the launches to capture).
 
-    python -m simpimc_gb300.profile_cases batch   # 256 uneven trapped-Coulomb chains: 1 + 1 sweep launches
-    python -m simpimc_gb300.profile_cases egas    # 66-electron gas: 1 + 1 sweep launches (528 attempts each)
+    python -m simpimc_gb300.profile_cases batch    # 256 uneven trapped-Coulomb chains: 1 + 1 sweep launches
+    python -m simpimc_gb300.profile_cases egas     # 66-electron gas: 1 + 1 sweep launches (528 attempts each)
+    python -m simpimc_gb300.profile_cases large32  # 1024-electron gas, FP32 mode: 1 + 1 launches of 64 attempts
 
-Each case holds well under 100 MB on the device, so a capture of the second launch
-(`-k regex:<Kernel> -s 1 -c 1`) ends in seconds.
+The first two hold well under 100 MB on the device, the third about 1.3 GB; a capture of the
+second launch (`-k regex:<Kernel> -s 1 -c 1`) ends in seconds (the large case with one or two
+sections rather than the full set).
 """
 from __future__ import annotations
 
@@ -21,7 +23,7 @@ def batch_case(d):
     items = batched_trap_chains(d, n_chains=256, seed0=1000, n_level=3)
     b = ChainBatch([x for x, _ in items], base_dir=d)
     b.set_paths(np.concatenate([p.ravel() for _, p in items]))
-    b.set_tiles(2, 16)
+    b.set_tiles(4, 16, 4)
     b.sweeps(1)
     b.sweeps(1)
     b.synchronize()
@@ -42,10 +44,23 @@ def egas_case(d):
     print(f"egas ok: {s.move_counters(0)[0] + s.move_counters(1)[0]} attempts")
 
 
+def large32_case(d):
+    from . import Simulation
+    from .configs import electron_gas
+    xml, path = electron_gas(d, n_part=1024, rs=1.0, beta=4.0, n_bead=512, k_cut_units=23.0, n_level=4, seed=777)
+    s = Simulation(xml, base_dir=d)
+    s.set_precision(32)
+    s.set_path(path)
+    s.sweep([0, 1], [1, 1], 32)
+    s.sweep([0, 1], [1, 1], 32)
+    s.synchronize()
+    print(f"large32 ok: {s.move_counters(0)[0] + s.move_counters(1)[0]} attempts, {s.n_k} k-vectors")
+
+
 def main(argv):
     case = argv[1] if len(argv) > 1 else "batch"
     with tempfile.TemporaryDirectory() as d:
-        {"batch": batch_case, "egas": egas_case}[case](d)
+        {"batch": batch_case, "egas": egas_case, "large32": large32_case}[case](d)
 
 
 if __name__ == "__main__":

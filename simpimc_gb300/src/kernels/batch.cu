@@ -564,13 +564,13 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArg
 ///   Kinetic       N M D / (2 tau) - sum_{p,b} |r_{b+1} - r_b|^2 / (4 lambda tau^2)  kinetic_class.h:35-45
 ///   HarmonicTrap  cofactor_b sum_{p,b} r^2                                         trap_class.h:20-35
 ///   Coulomb       sum_{p<q} sum_b (1/r_b + 1/r_{b+1}) / 2                          pair_action_class.h:241-264
+/// Every warp of the block works on the chain, whatever its sweep tile.
 __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchEnergyKernel(BatchArgs a) {
     const uint32_t ci = a.order[blockIdx.x];
     const ChainDev& c = a.chains[ci];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint32_t G = c.n_warps;
-    if (warp >= G) return;
-    const uint32_t T = G * 32u, t = threadIdx.x;
+    const uint32_t G = blockDim.x >> 5;
+    const uint32_t T = blockDim.x, t = threadIdx.x;
     const uint32_t N = c.n_part, M = c.n_bead, n_pad = c.n_pad;
     const int pbc = c.pbc;
     const float L = c.L, iL = c.iL;
@@ -628,7 +628,7 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchEnergyKernel(BatchAr
         s_red[1][warp] = trap;
         s_red[2][warp] = pair;
     }
-    GroupSync(G);
+    __syncthreads();
     if (t == 0) {
         dd k = DD(0.f), tr = DD(0.f), pr = DD(0.f);
         for (uint32_t w = 0; w < G; ++w) {
@@ -964,10 +964,8 @@ void ChainBatch::LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts) {
 }
 
 void ChainBatch::LaunchMeasure() {
-    uint32_t warps = 1;
-    for (const auto& c : chains) warps = std::max(warps, c.n_warps);
     const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, series_cap);
-    BatchEnergyKernel<<<n_chains, warps * 32, 0, stream>>>(a);
+    BatchEnergyKernel<<<n_chains, kBatchMaxWarps * 32, 0, stream>>>(a);
     CudaCheck(cudaGetLastError(), "batch energy launch");
     ++kernel_launches;
 }
