@@ -18,7 +18,9 @@ Also reported on the same line:
   plain_electron_gas the single-chain FP64 kernel on the 66-electron gas (r_s = 2, beta = 8,
                      M = 128, Ewald |k| < 12 (2 pi / L), 3561 half-space k-vectors, level 4);
   mixed_precision_large  the N = 1024, M = 512, |k| < 23 (2 pi / L) electron gas in the FP32 mode
-                     and the double-float mode: speed, HBM fraction, energy and S(k) differences.
+                     and the double-float mode: speed, HBM fraction, energy and S(k) differences;
+  hmc_adjoint        the r_s = 4, N = 128, M = 256 electron gas moved by the HMC path move on the
+                     exact gradient: gradient time and whole-path bead-moves/s.
 
 Arms:
   (default)          the CUDA library. `value` = device-timed cycles with the paths resident in
@@ -311,6 +313,50 @@ def large_mixed_precision(local, tmp, sweeps=3):
             "note": "same start, seeds and draws; FP32 densities rebuilt from the positions at every sweep call"}
 
 
+def hmc_adjoint(local, tmp, attempts=4, equil_sweeps=10):
+    """The adjoint workload's system (r_s = 4, N = 128 as 64 + 64, beta = 16, M = 256, |k| < 17 (2 pi / L))
+    moved by the HMC path move (leapfrog step 0.01, 10 steps, every bead of both species per
+    attempt) on the exact gradient: device time per gradient evaluation and per attempt."""
+    import torch
+    from simpimc_gb300 import Simulation
+    from simpimc_gb300.configs import electron_gas
+    xml, path = electron_gas(tmp, n_part=128, rs=4.0, beta=16.0, n_bead=256, k_cut_units=17.0, n_level=4, seed=4242)
+    xml = xml.replace('<Move name="BisectD" type="Bisect" species="eD" n_level="4" />',
+                      '<Move name="BisectD" type="Bisect" species="eD" n_level="4" />\n'
+                      '    <Move name="HMC" type="HMC" step_size="0.01" n_steps="10" />')
+    s = Simulation(xml, base_dir=tmp, device=local, chain=0)
+    # The electron gas's classical start (every bead of a particle at one uniform point), then
+    # bisection sweeps until the paths have spread; HMC from there.
+    s.set_path(path)
+    for _ in range(equil_sweeps):
+        s.sweep([0, 1], [1, 1], 64 * 16)
+    st = torch.cuda.ExternalStream(s._lib.pimc_stream(s._h), device=torch.device("cuda", local))
+    s.action_gradient_path()  # warm-up
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        s.action_gradient_path()
+    grad_s = (time.perf_counter() - t0) / 3
+    s.move_attempts(2, 1)  # warm-up attempt
+    torch.cuda.synchronize()
+    c0 = s.move_counters(2)
+    e0.record(st)
+    s.move_attempts(2, attempts)
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    c1 = s.move_counters(2)
+    beads = 128 * 256
+    out = {"workload": "electron gas N=128 (64+64) r_s=4 beta=16 M=256 Ewald |k|<17(2pi/L), HMC step 0.01 x 10 on the exact gradient",
+           "n_k_half_space": s.n_k, "attempts": attempts, "ms_per_attempt": ms / attempts,
+           "gradient_s_host_timed": grad_s, "acceptance": (c1[3] - c0[3]) / max(c1[0] - c0[0], 1),
+           "value": beads * attempts / (ms / 1e3), "unit": METRIC,
+           "equilibration": f"{equil_sweeps} bisection sweeps (level 4) from the classical start",
+           "note": "one HMC attempt moves all 32768 beads; 11 gradient and 2 whole-ring action evaluations per attempt, FP64"}
+    s.close()
+    return out
+
+
 def cpu_oracle_chains(items, tmp, seconds, chains):
     """The oracle on one host core, cycling through `chains` in chunks of attempts."""
     import oracle
@@ -433,6 +479,7 @@ def run_ours(args):
     gate = energy_gate(items, tmp, local, chains=cheap, sweeps=args.gate_sweeps)
     eg, _, _, _ = egas_plain(local, args.steps, args.warmup, tmp, flush)
     large = large_mixed_precision(local, tmp) if not args.no_large else None
+    hmc = hmc_adjoint(local, tmp) if not args.no_large else None
     cpu = None
     if not args.no_cpu_baseline:
         moves, el = cpu_oracle_chains(items, tmp, 12.0, sample)
@@ -461,6 +508,7 @@ def run_ours(args):
         "energy_gate": gate,
         "plain_electron_gas": eg,
         "mixed_precision_large": large,
+        "hmc_adjoint": hmc,
         "wall_s": wall,
     }
     print(json.dumps(line))

@@ -111,6 +111,9 @@ class ChainBatch {
     size_t pos_float4 = 0;
     cudaGraphExec_t graph_ = nullptr;
     uint64_t graph_sweeps_ = 0;
+    uint32_t launches_per_cycle_ = 3;  // sweep + energy parts + energy finish
+    std::unique_ptr<DeviceBuffer> energy_tasks_, energy_first_, energy_part_;
+    uint32_t n_energy_tasks_ = 0;
 };
 
 }  // namespace pimc

@@ -559,27 +559,34 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArg
     }
 }
 
-/// Thermal energy estimator of one chain (Energy::Accumulate with use_thermal, energy_class.h:
-/// 36-58): the sum of the actions' DActionDBeta divided by M, per action:
+/// Thermal energy estimator (Energy::Accumulate with use_thermal, energy_class.h:36-58): the sum of
+/// the actions' DActionDBeta divided by M, per action:
 ///   Kinetic       N M D / (2 tau) - sum_{p,b} |r_{b+1} - r_b|^2 / (4 lambda tau^2)  kinetic_class.h:35-45
 ///   HarmonicTrap  cofactor_b sum_{p,b} r^2                                         trap_class.h:20-35
 ///   Coulomb       sum_{p<q} sum_b (1/r_b + 1/r_{b+1}) / 2                          pair_action_class.h:241-264
-/// Every warp of the block works on the chain, whatever its sweep tile.
-__global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchEnergyKernel(BatchArgs a) {
-    const uint32_t ci = a.order[blockIdx.x];
-    const ChainDev& c = a.chains[ci];
+/// A chain's slices are split into tasks of kEnergySlices; one block per task forms the task's
+/// three sums, and one warp per chain adds its tasks' sums in task order (deterministic).
+constexpr uint32_t kEnergySlices = 8;
+constexpr uint32_t kEnergyThreads = 256;
+
+struct EnergyTask {
+    uint32_t chain, b0, nb, pad;
+};
+
+__global__ void __launch_bounds__(kEnergyThreads) BatchEnergyPartKernel(BatchArgs a, const EnergyTask* __restrict__ tasks, float2* __restrict__ part) {
+    const EnergyTask tk = tasks[blockIdx.x];
+    const ChainDev& c = a.chains[tk.chain];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint32_t G = blockDim.x >> 5;
     const uint32_t T = blockDim.x, t = threadIdx.x;
     const uint32_t N = c.n_part, M = c.n_bead, n_pad = c.n_pad;
     const int pbc = c.pbc;
     const float L = c.L, iL = c.iL;
     const float4* __restrict__ pos = a.pos + c.pos_off;
-    __shared__ dd s_red[3][kBatchMaxWarps];
+    __shared__ dd s_red[3][kEnergyThreads / 32];
 
     dd kin = DD(0.f), trap = DD(0.f), pair = DD(0.f);
-    for (uint32_t i = t; i < N * M; i += T) {
-        const uint32_t b = i / N, pp = i - b * N;
+    for (uint32_t i = t; i < N * tk.nb; i += T) {
+        const uint32_t b = tk.b0 + i / N, pp = i % N;
         const float4 r = pos[(size_t)b * n_pad + pp];
         const float4 r1 = pos[(size_t)((b + 1) % M) * n_pad + pp];
         // |r_{b+1} - r_b|^2 with exact differences (TwoSum) and products (TwoProd).
@@ -594,31 +601,32 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchEnergyKernel(BatchAr
     }
     if (c.has_pair && N > 1) {
         // Unordered pairs of one slice: (p, p + o mod N) for o = 1 .. (N-1)/2, plus o = N/2 for
-        // p < N/2 when N is even; every lane gets the same share of pairs.
+        // p < N/2 when N is even; items (slice of the task, pair) spread evenly over the block.
         const uint32_t half = (N - 1) / 2, n_main = N * half;
         const uint32_t n_pairs = N * (N - 1) / 2;
-        for (uint32_t b = 0; b < M; ++b) {
-            const float4* row = pos + (size_t)b * n_pad;
-            for (uint32_t j = t; j < n_pairs; j += T) {
-                uint32_t pp, o;
-                if (j < n_main) {
-                    o = 1 + j / N;
-                    pp = j - (o - 1) * N;
-                } else {
-                    pp = j - n_main;
-                    o = N / 2;
-                }
-                uint32_t q = pp + o;
-                if (q >= N) q -= N;
-                const float4 r = row[pp], s = row[q];
-                const float x = MinImg(__fsub_rn(r.x, s.x), pbc, L, iL);
-                const float y = MinImg(__fsub_rn(r.y, s.y), pbc, L, iL);
-                const float z = MinImg(__fsub_rn(r.z, s.z), pbc, L, iL);
-                float r2 = __fmaf_rn(x, x, __fmaf_rn(y, y, __fmul_rn(z, z)));
-                r2 = fminf(fmaxf(r2, c.r2_min), c.r2_max);
-                pair = AddF(pair, rsqrtf(r2));
+        Comp acc{0.f, 0.f};
+        for (uint32_t i = t; i < n_pairs * tk.nb; i += T) {
+            const uint32_t bb = i / n_pairs, j = i - bb * n_pairs;
+            const float4* row = pos + (size_t)(tk.b0 + bb) * n_pad;
+            uint32_t pp, o;
+            if (j < n_main) {
+                o = 1 + j / N;
+                pp = j - (o - 1) * N;
+            } else {
+                pp = j - n_main;
+                o = N / 2;
             }
+            uint32_t q = pp + o;
+            if (q >= N) q -= N;
+            const float4 r = row[pp], s = row[q];
+            const float x = MinImg(__fsub_rn(r.x, s.x), pbc, L, iL);
+            const float y = MinImg(__fsub_rn(r.y, s.y), pbc, L, iL);
+            const float z = MinImg(__fsub_rn(r.z, s.z), pbc, L, iL);
+            float r2 = __fmaf_rn(x, x, __fmaf_rn(y, y, __fmul_rn(z, z)));
+            r2 = fminf(fmaxf(r2, c.r2_min), c.r2_max);
+            CompAdd(acc, rsqrtf(r2));
         }
+        pair = CompDD(acc);
     }
     kin = WarpSumDD(kin);
     trap = WarpSumDD(trap);
@@ -629,33 +637,48 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchEnergyKernel(BatchAr
         s_red[2][warp] = pair;
     }
     __syncthreads();
-    if (t == 0) {
-        dd k = DD(0.f), tr = DD(0.f), pr = DD(0.f);
-        for (uint32_t w = 0; w < G; ++w) {
-            k = Add(k, s_red[0][w]);
-            tr = Add(tr, s_red[1][w]);
-            pr = Add(pr, s_red[2][w]);
-        }
-        const double inv_m = 1.0 / (double)M;
-        const double e_kin = (c.kin_const - c.i4ltt * ToDouble(k)) * inv_m;
-        const double e_trap = c.has_trap ? c.trap_cofb * ToDouble(tr) * inv_m : 0.;
-        const double e_pair = ToDouble(pr) * inv_m;
-        const uint64_t n = a.n_meas[ci];
-        if (!isfinite(e_kin + e_trap + e_pair)) atomicOr(a.err, kDevErrNonFinite);
-        double* last = a.last + (size_t)ci * kBatchSeriesComponents;
-        last[0] = e_kin + e_trap + e_pair;
-        last[1] = e_kin;
-        last[2] = e_trap;
-        last[3] = e_pair;
-        if (n < a.series_cap) {
-            double* out = a.series + ((size_t)ci * a.series_cap + n) * kBatchSeriesComponents;
-            out[0] = e_kin + e_trap + e_pair;
-            out[1] = e_kin;
-            out[2] = e_trap;
-            out[3] = e_pair;
-        }
-        a.n_meas[ci] = n + 1;
+    if (warp == 0) {
+        dd v[3];
+        for (int q = 0; q < 3; ++q) v[q] = WarpSumDD(lane < T / 32 ? s_red[q][lane] : DD(0.f));
+        if (lane == 0)
+            for (int q = 0; q < 3; ++q) part[(size_t)blockIdx.x * 3 + q] = make_float2(v[q].hi, v[q].lo);
     }
+}
+
+/// One warp per chain: its tasks' sums in task order, then E and its parts (FP64) into the
+/// series and the latest-measurement record.
+__global__ void BatchEnergyFinishKernel(BatchArgs a, const uint32_t* __restrict__ first_task, const float2* __restrict__ part, uint32_t n_chains) {
+    const uint32_t ci = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31u;
+    if (ci >= n_chains) return;
+    const ChainDev& c = a.chains[ci];
+    const uint32_t t0 = first_task[ci], t1 = first_task[ci + 1];
+    dd s[3] = {DD(0.f), DD(0.f), DD(0.f)};
+    for (uint32_t t = t0 + lane; t < t1; t += 32)
+        for (int q = 0; q < 3; ++q) {
+            const float2 v = part[(size_t)t * 3 + q];
+            s[q] = Add(s[q], dd{v.x, v.y});
+        }
+    for (int q = 0; q < 3; ++q) s[q] = WarpSumDD(s[q]);
+    if (lane != 0) return;
+    const double inv_m = 1.0 / (double)c.n_bead;
+    const double e_kin = (c.kin_const - c.i4ltt * ToDouble(s[0])) * inv_m;
+    const double e_trap = c.has_trap ? c.trap_cofb * ToDouble(s[1]) * inv_m : 0.;
+    const double e_pair = ToDouble(s[2]) * inv_m;
+    const uint64_t n = a.n_meas[ci];
+    if (!isfinite(e_kin + e_trap + e_pair)) atomicOr(a.err, kDevErrNonFinite);
+    double* last = a.last + (size_t)ci * kBatchSeriesComponents;
+    last[0] = e_kin + e_trap + e_pair;
+    last[1] = e_kin;
+    last[2] = e_trap;
+    last[3] = e_pair;
+    if (n < a.series_cap) {
+        double* out = a.series + ((size_t)ci * a.series_cap + n) * kBatchSeriesComponents;
+        out[0] = e_kin + e_trap + e_pair;
+        out[1] = e_kin;
+        out[2] = e_trap;
+        out[3] = e_pair;
+    }
+    a.n_meas[ci] = n + 1;
 }
 
 }  // namespace
@@ -796,6 +819,21 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
     CudaCheck(cudaMemset(acc_->ptr, 0, n_chains * sizeof(uint64_t)), "memset");
     CudaCheck(cudaMemset(n_meas_->ptr, 0, n_chains * sizeof(uint64_t)), "memset");
     CudaCheck(cudaMemset(err_->ptr, 0, sizeof(int)), "memset");
+    // Energy tasks: kEnergySlices slices of one chain each, chains in index order.
+    std::vector<EnergyTask> tasks;
+    std::vector<uint32_t> first(n_chains + 1, 0);
+    for (uint32_t ci = 0; ci < n_chains; ++ci) {
+        first[ci] = (uint32_t)tasks.size();
+        for (uint32_t b0 = 0; b0 < chains[ci].n_bead; b0 += kEnergySlices)
+            tasks.push_back(EnergyTask{ci, b0, std::min(kEnergySlices, chains[ci].n_bead - b0), 0});
+    }
+    first[n_chains] = (uint32_t)tasks.size();
+    n_energy_tasks_ = (uint32_t)tasks.size();
+    energy_tasks_.reset(new DeviceBuffer(tasks.size() * sizeof(EnergyTask)));
+    energy_first_.reset(new DeviceBuffer(first.size() * sizeof(uint32_t)));
+    energy_part_.reset(new DeviceBuffer(tasks.size() * 3 * sizeof(float2)));
+    CudaCheck(cudaMemcpy(energy_tasks_->ptr, tasks.data(), tasks.size() * sizeof(EnergyTask), cudaMemcpyHostToDevice), "energy tasks");
+    CudaCheck(cudaMemcpy(energy_first_->ptr, first.data(), first.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "energy tasks");
     SetTiles(items_per_lane, max_warps, wave);
 }
 
@@ -965,9 +1003,11 @@ void ChainBatch::LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts) {
 
 void ChainBatch::LaunchMeasure() {
     const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, series_cap);
-    BatchEnergyKernel<<<n_chains, kBatchMaxWarps * 32, 0, stream>>>(a);
+    BatchEnergyPartKernel<<<n_energy_tasks_, kEnergyThreads, 0, stream>>>(a, energy_tasks_->as<EnergyTask>(), energy_part_->as<float2>());
     CudaCheck(cudaGetLastError(), "batch energy launch");
-    ++kernel_launches;
+    BatchEnergyFinishKernel<<<(n_chains + 7) / 8, 256, 0, stream>>>(a, energy_first_->as<uint32_t>(), energy_part_->as<float2>(), n_chains);
+    CudaCheck(cudaGetLastError(), "batch energy launch");
+    kernel_launches += 2;
 }
 
 void ChainBatch::Attempts(uint64_t n) {
@@ -991,6 +1031,7 @@ void ChainBatch::Run(uint64_t n_cycles, uint64_t spm) {
         LaunchMeasure();
         kernel_launches = before;
         CudaCheck(cudaStreamEndCapture(stream, &g), "end capture");
+        launches_per_cycle_ = 3;
         const cudaError_t e = cudaGraphInstantiate(&graph_, g, 0);
         cudaGraphDestroy(g);
         CudaCheck(e, "graph instantiate");
@@ -998,7 +1039,7 @@ void ChainBatch::Run(uint64_t n_cycles, uint64_t spm) {
     }
     for (uint64_t i = 0; i < n_cycles; ++i) {
         CudaCheck(cudaGraphLaunch(graph_, stream), "graph launch");
-        kernel_launches += 2;
+        kernel_launches += launches_per_cycle_;
     }
 }
 
