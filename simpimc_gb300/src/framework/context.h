@@ -135,9 +135,9 @@ class Context {
     double VirialCentroidAdjoint(uint32_t species);
     void HmcAttempts(uint32_t m, uint64_t n);
     // Device-side pieces (a >= 0 one action, -1 every action, -2 every non-kinetic action).
-    double TotalActionDev(int a, const double* pos, const double2* rho);
-    void GradientDev(int a, const double* pos, const double2* rho, double* grad);  // [M][3][n_pad], overwritten
-    const double2* ScratchRho(const double* pos);                                    // densities of `pos`
+    double TotalActionDev(int a, const double* pos, const float4* rho);
+    void GradientDev(int a, const double* pos, const float4* rho, double* grad);  // [M][3][n_pad], overwritten
+    const float4* ScratchRho(const double* pos);                                    // double-float densities of `pos`
 
     // --- moves, observables, algorithm ---
     void MoveAttempts(uint32_t m, uint64_t n);
@@ -205,7 +205,8 @@ class Context {
     std::vector<StageTable> stage_tables_;  // spline tables the sweep may copy into shared memory
     void BuildSweepTables();
     std::unique_ptr<DeviceBuffer> pos_, pos_new_, rho_, kidx_;
-    std::unique_ptr<DeviceBuffer> grad_, mom_, pos_save_, rho_scratch_;  // adjoint / HMC work arrays
+    std::unique_ptr<DeviceBuffer> grad_, mom_, pos_save_, rho_scratch_, phase_tab_;  // adjoint / HMC work arrays
+    std::vector<std::unique_ptr<DeviceBuffer>> adj_vk_;                              // double-float v_k per action
     std::unique_ptr<DeviceBuffer> partials_, result_, bar_, err_, pairs_, rho_tmp_, parts_, kmag_dev_, sched_, accepts_;
     size_t partials_cap_ = 0, pairs_cap_ = 0, rho_tmp_cap_ = 0, parts_cap_ = 0;
 

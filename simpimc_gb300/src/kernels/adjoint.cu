@@ -1,6 +1,6 @@
 // Exact gradient dS/dR of the whole-ring action at level 0 (the "adjoint" of the action
 // evaluation), the total action it differentiates, the virial centroid term built on it, and a
-// hybrid Monte Carlo path move driven by it. FP64 throughout.
+// hybrid Monte Carlo path move driven by it.
 //
 // The action of one species' path, summed over every link b -> b+1 of the ring (level 0):
 //   Kinetic        sum_b phi(r_{b+1} - r_b),  phi(d) = sum_c image(d_c) + |d|^2 / (4 lambda tau)
@@ -17,6 +17,8 @@
 //   pair      tau sum_q V'(|r_pq|) r_pq / |r_pq|      (zero where the table clamps V flat)
 //   Ewald     -2 tau sum_k v_k k Im(conj(rho_other(k,b)) exp(i k.r_b))
 // where rho_other is the partner species' density (the own species' for a homologous action).
+// The densities and the Ewald sums over k run in double-float (FP32 pairs, ~1e-14 relative) on
+// the FP32 pipe; every other term and every total is FP64.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -24,6 +26,7 @@
 #include "../common/philox.h"
 #include "../framework/context.h"
 #include "actions.cuh"
+#include "phase_dd.cuh"
 #include "reduce.cuh"
 
 namespace pimc {
@@ -130,14 +133,47 @@ __global__ void PairGradKernel(const SystemDev sys, const double* __restrict__ p
     }
 }
 
-/// Ewald forces: one warp per (slice, particle), lanes over the stored k-vectors; the particle's
-/// per-dimension phase rows sit in shared memory.
-__global__ void EwaldGradKernel(const SystemDev sys, const double* __restrict__ pos, const PairDev pa, const double2* __restrict__ rho_a,
-                                const double2* __restrict__ rho_b, double* __restrict__ grad) {
-    extern __shared__ double2 tab[];  // [warps][3][stride]
-    const int stride = max(max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
+__device__ __forceinline__ dd SplitDD(double x) {
+    const float h = (float)x;
+    return dd{h, (float)(x - (double)h)};
+}
+
+/// Per-slice densities of every kept species from one position copy, in double-float: one thread
+/// per k-vector of a 128-wide chunk, one block per (chunk, slice, slot), particles in order in
+/// chunks whose phase rows sit in shared memory (species_class.h:380-403).
+constexpr uint32_t kRhoDDChunk = 32;
+
+__global__ void RhoDDKernel(const SystemDev sys, const double* __restrict__ pos, const int* __restrict__ slot_species, const float4* __restrict__ tab256,
+                            dd iL, dd two_pi, float4* __restrict__ rho) {
+    extern __shared__ ddc rtab[];  // [kRhoDDChunk][3][stride]
+    const uint32_t stride = (uint32_t)max(max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y, slot = blockIdx.z;
+    const uint32_t s = (uint32_t)slot_species[slot], ns = sys.sp_n[s], off = sys.sp_off[s], K = sys.K, np = sys.n_pad, n_d = sys.n_d;
+    const int32_t pk = k < K ? sys.kidx[k] : 0;
+    ddc acc{DD(0.f), DD(0.f)};
+    for (uint32_t p0 = 0; p0 < ns; p0 += kRhoDDChunk) {
+        const uint32_t cnt = min(kRhoDDChunk, ns - p0);
+        __syncthreads();
+        for (uint32_t t = threadIdx.x; t < cnt * 3 * stride; t += blockDim.x) {
+            const uint32_t pi = t / (3 * stride), rem = t - pi * 3 * stride, d = rem / stride, n = rem - d * stride;
+            if (d < n_d && (int)n <= sys.max_index[d]) rtab[t] = PhaseDD(SplitDD(PosAt(pos, np, b, d, off + p0 + pi)), (int)n, iL, two_pi, tab256);
+        }
+        __syncthreads();
+        if (k < K)
+            for (uint32_t pi = 0; pi < cnt; ++pi) acc = CAdd(acc, PhaseProductDD(rtab + (size_t)pi * 3 * stride, stride, n_d, pk));
+    }
+    if (k < K) rho[((size_t)slot * sys.M + b) * K + k] = Pack(acc);
+}
+
+/// Ewald forces: one warp per (slice, particle), lanes over the stored k-vectors in double-float;
+/// the particle's per-dimension phase rows sit in shared memory.
+__global__ void EwaldGradDDKernel(const SystemDev sys, const double* __restrict__ pos, const PairDev pa, const float4* __restrict__ rho_a,
+                                  const float4* __restrict__ rho_b, const float2* __restrict__ vk, const float4* __restrict__ tab256, dd iL, dd two_pi,
+                                  double* __restrict__ grad) {
+    extern __shared__ ddc etab[];  // [warps][3][stride]
+    const uint32_t stride = (uint32_t)max(max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
     const uint32_t warps = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    double2* my = tab + (size_t)w * 3 * stride;
+    ddc* my = etab + (size_t)w * 3 * stride;
     const uint32_t na = sys.sp_n[pa.sa], nb = sys.sp_n[pa.sb], M = sys.M, np = sys.n_pad, K = sys.K, n_d = sys.n_d;
     const bool hom = pa.sa == pa.sb;
     const uint32_t ng = hom ? na : na + nb;
@@ -145,21 +181,25 @@ __global__ void EwaldGradKernel(const SystemDev sys, const double* __restrict__ 
         const uint32_t b = (uint32_t)(it / ng), j = (uint32_t)(it % ng);
         const bool in_a = j < na;
         const uint32_t g = in_a ? sys.sp_off[pa.sa] + j : sys.sp_off[pa.sb] + (j - na);
-        const double2* rho = (in_a ? rho_b : rho_a) + (size_t)b * K;
+        const float4* rho = (in_a ? rho_b : rho_a) + (size_t)b * K;
         __syncwarp();
-        if (lane < n_d) PhaseRow(PosAt(pos, np, b, lane, g), sys.box[lane], sys.max_index[lane], my + (size_t)lane * stride);
+        for (uint32_t t = lane; t < 3 * stride; t += 32) {
+            const uint32_t d = t / stride, n = t - d * stride;
+            if (d < n_d && (int)n <= sys.max_index[d]) my[t] = PhaseDD(SplitDD(PosAt(pos, np, b, d, g)), (int)n, iL, two_pi, tab256);
+        }
         __syncwarp();
-        double acc[3] = {0., 0., 0.};
+        dd acc[3] = {DD(0.f), DD(0.f), DD(0.f)};
         for (uint32_t k = lane; k < K; k += 32) {
             const int32_t pk = sys.kidx[k];
-            const double2 e = PhaseProduct(my, stride, n_d, pk);
-            const double2 rk = rho[k];
-            const double f = pa.v_long_k[k] * (rk.x * e.y - rk.y * e.x);  // v_k Im(conj(rho) e)
-            for (uint32_t d = 0; d < n_d; ++d) acc[d] += f * (double)KIdx(pk, (int)d) * sys.box[d];
+            const ddc e = PhaseProductDD(my, stride, n_d, pk);
+            const ddc r = Unpack(rho[k]);
+            const float2 v = vk[k];
+            const dd f = Mul(dd{v.x, v.y}, Sub(Mul(r.re, e.im), Mul(r.im, e.re)));  // v_k Im(conj(rho) e)
+            for (uint32_t d = 0; d < n_d; ++d) acc[d] = Add(acc[d], MulF(f, (float)KIdx(pk, (int)d)));
         }
         for (uint32_t d = 0; d < n_d; ++d) {
-            const double s = WarpSum(acc[d]);
-            if (lane == 0) grad[GIdx(b, d, g, np)] += -2. * sys.tau * s;
+            const dd s = WarpSumDD(acc[d]);
+            if (lane == 0) grad[GIdx(b, d, g, np)] += -2. * sys.tau * sys.box[d] * ToDouble(s);
         }
     }
 }
@@ -193,12 +233,46 @@ int Blocks(const Context& c, uint64_t n, int threads) {
 
 }  // namespace
 
-const double2* Context::ScratchRho(const double* pos) {
+/// Double-float densities of `pos` (adjoint scratch; the committed densities are untouched), and
+/// the double-float tables the adjoint kernels read (phase rows, v_k per long-range action).
+const float4* Context::ScratchRho(const double* pos) {
     if (!rho_slots || !sys.K) return nullptr;
     const size_t n = (size_t)rho_slots * sys.M * sys.K;
-    if (!rho_scratch_ || rho_scratch_->bytes < n * sizeof(double2)) rho_scratch_.reset(new DeviceBuffer(n * sizeof(double2)));
-    ComputeRho(pos, rho_scratch_->as<double2>());
-    return rho_scratch_->as<double2>();
+    if (!rho_scratch_ || rho_scratch_->bytes < n * sizeof(float4)) rho_scratch_.reset(new DeviceBuffer(n * sizeof(float4)));
+    if (!phase_tab_) {
+        std::vector<float4> t(256);
+        PhaseTable256(t.data());
+        phase_tab_.reset(new DeviceBuffer(256 * sizeof(float4)));
+        CudaCheck(cudaMemcpy(phase_tab_->ptr, t.data(), 256 * sizeof(float4), cudaMemcpyHostToDevice), "phase table");
+        adj_vk_.resize(actions.size());
+        for (size_t i = 0; i < actions.size(); ++i) {
+            if (actions[i].kind != 2 || !sys.pair[actions[i].index].use_long_range) continue;
+            const auto& hv = host_vk[actions[i].index];
+            std::vector<float2> v(sys.K);
+            for (uint32_t k = 0; k < sys.K; ++k) {
+                float h, l;
+                SplitDouble(hv[k], h, l);
+                v[k] = make_float2(h, l);
+            }
+            adj_vk_[i].reset(new DeviceBuffer(sys.K * sizeof(float2)));
+            CudaCheck(cudaMemcpy(adj_vk_[i]->ptr, v.data(), sys.K * sizeof(float2), cudaMemcpyHostToDevice), "v_k table");
+        }
+    }
+    std::vector<int> slot_species(rho_slots, 0);
+    for (uint32_t s = 0; s < sys.S; ++s)
+        if (sys.sp_rho[s] >= 0) slot_species[sys.sp_rho[s]] = (int)s;
+    uint32_t* dss = Parts(rho_slots);
+    CudaCheck(cudaMemcpyAsync(dss, slot_species.data(), rho_slots * sizeof(int), cudaMemcpyHostToDevice, stream), "slot upload");
+    const uint32_t stride = (uint32_t)std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
+    const size_t smem = (size_t)kRhoDDChunk * 3 * stride * sizeof(ddc);
+    CudaCheck(cudaFuncSetAttribute(RhoDDKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attribute");
+    dd iL, two_pi;
+    SplitDouble(sys.iL, iL.hi, iL.lo);
+    SplitDouble(2. * M_PI, two_pi.hi, two_pi.lo);
+    RhoDDKernel<<<dim3((sys.K + 127) / 128, sys.M, rho_slots), 128, smem, stream>>>(sys, pos, reinterpret_cast<const int*>(dss),
+                                                                                     phase_tab_->as<float4>(), iL, two_pi, rho_scratch_->as<float4>());
+    CudaCheck(cudaGetLastError(), "rho launch");
+    return rho_scratch_->as<float4>();
 }
 
 /// Selection: a >= 0 one action, -1 every action, -2 every non-kinetic action.
@@ -209,7 +283,7 @@ static bool Selected(const ActionHost& ah, int sel, int i) {
     return true;
 }
 
-double Context::TotalActionDev(int a, const double* pos, const double2* rho) {
+double Context::TotalActionDev(int a, const double* pos, const float4* rho) {
     const uint32_t M = sys.M, np = sys.n_pad, n_d = sys.n_d;
     const double L = sys.L, iL = sys.iL, tau = sys.tau;
     double total = 0.;
@@ -263,13 +337,15 @@ double Context::TotalActionDev(int a, const double* pos, const double2* rho) {
                 v[0] = tau * vb;
             }, &part);
             if (pa.use_long_range && rho) {
-                const double2* ra = rho + (size_t)sys.sp_rho[pa.sa] * M * sys.K;
-                const double2* rb = rho + (size_t)sys.sp_rho[pa.sb] * M * sys.K;
+                const float4* ra = rho + (size_t)sys.sp_rho[pa.sa] * M * sys.K;
+                const float4* rb = rho + (size_t)sys.sp_rho[pa.sb] * M * sys.K;
                 const uint32_t K = sys.K;
                 double lr = 0.;
                 SumItems<1>(*this, (uint64_t)M * K, [=] __device__(uint64_t it, double* v) {
-                    const double2 x = ra[it], y = rb[it];
-                    v[0] = pa.v_long_k[it % K] * (x.x * y.x + x.y * y.y);
+                    const float4 x = ra[it], y = rb[it];
+                    const double xr = (double)x.x + (double)x.y, xi = (double)x.z + (double)x.w;
+                    const double yr = (double)y.x + (double)y.y, yi = (double)y.z + (double)y.w;
+                    v[0] = pa.v_long_k[it % K] * (xr * yr + xi * yi);
                 }, &lr);
                 part += (hom ? 1. : 2.) * tau * lr;
             }
@@ -279,7 +355,7 @@ double Context::TotalActionDev(int a, const double* pos, const double2* rho) {
     return total;
 }
 
-void Context::GradientDev(int a, const double* pos, const double2* rho, double* grad) {
+void Context::GradientDev(int a, const double* pos, const float4* rho, double* grad) {
     const size_t n = (size_t)sys.M * 3 * sys.n_pad;
     CudaCheck(cudaMemsetAsync(grad, 0, n * sizeof(double), stream), "grad clear");
     const int th = 256;
@@ -298,13 +374,17 @@ void Context::GradientDev(int a, const double* pos, const double2* rho, double* 
             const uint64_t ng = (uint64_t)(pa.sa == pa.sb ? sys.sp_n[pa.sa] : sys.sp_n[pa.sa] + sys.sp_n[pa.sb]) * sys.M;
             PairGradKernel<<<Blocks(*this, ng, th), th, 0, stream>>>(sys, pos, pa, grad);
             if (pa.use_long_range && rho && sys.K) {
-                const double2* ra = rho + (size_t)sys.sp_rho[pa.sa] * sys.M * sys.K;
-                const double2* rb = rho + (size_t)sys.sp_rho[pa.sb] * sys.M * sys.K;
+                const float4* ra = rho + (size_t)sys.sp_rho[pa.sa] * sys.M * sys.K;
+                const float4* rb = rho + (size_t)sys.sp_rho[pa.sb] * sys.M * sys.K;
                 const int stride = std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
                 const int warps = 8;
-                const size_t smem = (size_t)warps * 3 * stride * sizeof(double2);
-                const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((ng + warps - 1) / warps, (uint64_t)n_sm * 8));
-                EwaldGradKernel<<<blocks, warps * 32, smem, stream>>>(sys, pos, pa, ra, rb, grad);
+                const size_t smem = (size_t)warps * 3 * stride * sizeof(ddc);
+                const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((ng + warps - 1) / warps, (uint64_t)n_sm * 16));
+                dd iL, two_pi;
+                SplitDouble(sys.iL, iL.hi, iL.lo);
+                SplitDouble(2. * M_PI, two_pi.hi, two_pi.lo);
+                EwaldGradDDKernel<<<blocks, warps * 32, smem, stream>>>(sys, pos, pa, ra, rb, adj_vk_[i]->as<float2>(), phase_tab_->as<float4>(), iL,
+                                                                        two_pi, grad);
             }
         }
         CudaCheck(cudaGetLastError(), "gradient launch");

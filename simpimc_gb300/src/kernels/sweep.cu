@@ -33,6 +33,7 @@
 #include "../framework/context.h"
 #include "actions.cuh"
 #include "df64.cuh"
+#include "phase_dd.cuh"
 
 namespace pimc {
 
@@ -178,41 +179,6 @@ __device__ __forceinline__ void DrDrpDD(const dd* A0, const dd* C0, const dd* A1
     }
     r = Sqrt(a);
     rp = Sqrt(b);
-}
-
-/// exp(2 pi i n t) for the turn count t = x / L of one coordinate: n t is reduced modulo 1, its
-/// nearest 1/256 of a turn read from a table and the residue (|eps| <= pi/256) expanded in Taylor
-/// series to eps^7 in double-float.
-__device__ __forceinline__ ddc PhaseDD(dd x, int n, dd iL, dd two_pi, const float4* tab256) {
-    if (n == 0) return ddc{DD(1.f), DD(0.f)};
-    dd t = Mul(x, iL);
-    t = Sub(t, DD(Rint(t)));
-    dd a = MulF(t, (float)n);
-    a = Sub(a, DD(Rint(a)));
-    const float jf = rintf(__fmul_rn(a.hi, 256.f));
-    const dd g = Sub(a, DD(__fmul_rn(jf, 1.f / 256.f)));
-    const dd eps = Mul(g, two_pi);
-    const dd e2 = Sqr(eps);
-    const dd neg_inv6{-0.16666667f, 4.9670538e-09f};  // -1/6 as a float pair
-    const dd ps = Add(neg_inv6, MulF(e2, __fmaf_rn(e2.hi, -1.f / 5040.f, 1.f / 120.f)));
-    const dd sn = Add(eps, Mul(eps, Mul(e2, ps)));
-    const dd pc = AddF(MulF(e2, __fmaf_rn(e2.hi, -1.f / 720.f, 1.f / 24.f)), -0.5f);
-    const dd cs = AddF(Mul(e2, pc), 1.f);
-    const int j = ((int)jf + 256) & 255;
-    const ddc T = Unpack(tab256[j]);
-    return CMulDD(T, ddc{cs, sn});
-}
-
-/// Product over dimensions of the per-dimension phases from tables [3][stride].
-__device__ __forceinline__ ddc PhaseProductDD(const ddc* tab, uint32_t stride, uint32_t n_d, int32_t packed) {
-    ddc f{DD(1.f), DD(0.f)};
-    for (uint32_t d = 0; d < n_d; ++d) {
-        const int n = KIdx(packed, (int)d);
-        ddc c = tab[d * stride + (n < 0 ? -n : n)];
-        if (n < 0) c.im = Neg(c.im);
-        f = d == 0 ? c : CMulDD(f, c);
-    }
-    return f;
 }
 
 /// FP32 counterpart of PhaseDD: the turn count n x / L is reduced in double-float (so large n x
