@@ -438,8 +438,9 @@ def run_ours(args):
         k_ms += e0.elapsed_time(e1)
     att2, acc2 = batch.counters()
 
-    # e2e: every chain's path from host memory, one cycle, energies and paths back, every step.
-    host = batch.get_paths()
+    # e2e: every chain's path from pinned host memory, one cycle, energies and paths back, every step.
+    host = torch.empty(batch.get_paths().size, dtype=torch.float64, pin_memory=True).numpy()
+    batch.get_paths(out=host)
     e2e_ms = 0.0
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
@@ -449,7 +450,7 @@ def run_ours(args):
         batch.set_paths(host)
         batch.run(1, 1)
         energies = batch.last_energy()
-        host = batch.get_paths()
+        batch.get_paths(out=host)
         e2e_ms += (time.perf_counter() - t0) * 1e3
     if sampler:
         sampler.terminate()
@@ -485,7 +486,7 @@ def run_ours(args):
         moves, el = cpu_oracle_chains(items, tmp, 12.0, sample)
         cpu = {"value": moves / el, "unit": METRIC, "cores": 1, "kind": "port",
                "sample": f"{moves // 7} bisection attempts ({el:.1f} s) on chains {sample}, round robin in chunks of 64"}
-    path_bytes_h2d = sum(((n + 7) & ~7) * m * 16 for n, m, _ in batch.shapes)  # the float4 staging copy
+    path_bytes_h2d = int(host.nbytes)  # every chain's path as doubles, copied as they are
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -497,7 +498,8 @@ def run_ours(args):
         "clocks": clocks_summary(clk_file, local),
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": path_bytes_h2d,
                 "d2h_bytes_per_step": path_bytes_h2d + N_CHAINS * 4 * 8,
-                "note": "pimc_batch_set_paths + pimc_batch_run(1 cycle) + pimc_batch_last_energy + pimc_batch_get_paths per step"},
+                "note": "pimc_batch_set_paths + pimc_batch_run(1 cycle) + pimc_batch_last_energy + pimc_batch_get_paths per step, "
+                        "paths in pinned host memory"},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": peak_kind, "kernel": "BatchSweepKernel",

@@ -169,7 +169,8 @@ int pimc_batch_chain_info(pimc_batch* b, uint32_t chain, uint32_t* out4);
 int pimc_batch_set_path(pimc_batch* b, uint32_t chain, const double* pos);
 int pimc_batch_get_path(pimc_batch* b, uint32_t chain, double* pos);
 /* Every chain's path in one transfer: the chains' [n_part][n_bead][3] arrays concatenated in chain
- * order (staged through pinned host memory, one copy each way). */
+ * order, copied as they are (one copy each way; pinned host memory moves at full link speed) and
+ * laid out on the device. A non-finite coordinate makes set_paths return PIMC_ERR_ARG. */
 int pimc_batch_set_paths(pimc_batch* b, const double* all);
 int pimc_batch_get_paths(pimc_batch* b, double* all);
 /* n bisection attempts (Move::DoEvent, move_class.h:277-293) on every chain. */

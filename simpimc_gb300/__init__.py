@@ -388,14 +388,20 @@ class ChainBatch:
         return out
 
     def set_paths(self, flat: np.ndarray):
-        """Every chain's path at once: the chains' (n_part, n_bead, 3) arrays concatenated."""
+        """Every chain's path at once: the chains' (n_part, n_bead, 3) arrays concatenated (copied
+        as they are; pinned host memory moves at full link speed)."""
         a = np.ascontiguousarray(flat, dtype=np.float64).ravel()
         if a.size != sum(n * m * 3 for n, m, _ in self.shapes):
             raise ValueError("flat path size does not match the chains")
         self._check(self._lib.pimc_batch_set_paths(self._h, _dp(a)))
 
-    def get_paths(self) -> np.ndarray:
-        out = np.zeros(sum(n * m * 3 for n, m, _ in self.shapes), dtype=np.float64)
+    def get_paths(self, out: np.ndarray | None = None) -> np.ndarray:
+        """Every chain's path, concatenated; `out` (float64, contiguous, e.g. pinned) is reused."""
+        n = sum(n * m * 3 for n, m, _ in self.shapes)
+        if out is None:
+            out = np.zeros(n, dtype=np.float64)
+        if out.dtype != np.float64 or out.size != n or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a contiguous float64 array of the concatenated path size")
         self._check(self._lib.pimc_batch_get_paths(self._h, _dp(out)))
         return out
 

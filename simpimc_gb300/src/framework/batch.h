@@ -106,8 +106,8 @@ class ChainBatch {
     void LaunchMeasure();
     void ResetGraph();
     std::unique_ptr<DeviceBuffer> pos_, chains_dev_, order_dev_, att_, acc_, series_, n_meas_, err_, last_;
-    float4* staging_ = nullptr;  // pinned host mirror of pos_ for bulk transfers
     std::vector<uint64_t> path_off_;  // first double of each chain in the concatenated host layout
+    std::unique_ptr<DeviceBuffer> dstage_, path_off_dev_;  // host-layout doubles on the device, offsets
     size_t pos_float4 = 0;
     cudaGraphExec_t graph_ = nullptr;
     uint64_t graph_sweeps_ = 0;

@@ -25,7 +25,6 @@
 #include <cstring>
 #include <ctime>
 #include <numeric>
-#include <thread>
 
 #include "../../../include/simpimc_gb300.h"
 #include "../common/philox.h"
@@ -681,6 +680,38 @@ __global__ void BatchEnergyFinishKernel(BatchArgs a, const uint32_t* __restrict_
     a.n_meas[ci] = n + 1;
 }
 
+/// Host layout (every chain's [n_part][n_bead][3] doubles, concatenated) to the device float4
+/// layout, one block per chain; a non-finite coordinate sets kDevErrNonFinite and is not stored.
+__global__ void HostLayoutToPosKernel(const double* __restrict__ src, const ChainDev* __restrict__ chains, const uint64_t* __restrict__ path_off,
+                                      float4* __restrict__ pos, int* err) {
+    const ChainDev& c = chains[blockIdx.x];
+    const double* in = src + path_off[blockIdx.x];
+    float4* out = pos + c.pos_off;
+    for (uint32_t i = threadIdx.x; i < c.n_part * c.n_bead; i += blockDim.x) {
+        const uint32_t p = i / c.n_bead, b = i - p * c.n_bead;
+        const double x = in[3 * (size_t)i], y = in[3 * (size_t)i + 1], z = in[3 * (size_t)i + 2];
+        if (!isfinite(x) || !isfinite(y) || !isfinite(z)) {
+            atomicOr(err, kDevErrNonFinite);
+            continue;
+        }
+        out[(size_t)b * c.n_pad + p] = make_float4((float)x, (float)y, (float)z, 0.f);
+    }
+}
+
+__global__ void PosToHostLayoutKernel(const float4* __restrict__ pos, const ChainDev* __restrict__ chains, const uint64_t* __restrict__ path_off,
+                                      double* __restrict__ dst) {
+    const ChainDev& c = chains[blockIdx.x];
+    double* out = dst + path_off[blockIdx.x];
+    const float4* in = pos + c.pos_off;
+    for (uint32_t i = threadIdx.x; i < c.n_part * c.n_bead; i += blockDim.x) {
+        const uint32_t p = i / c.n_bead, b = i - p * c.n_bead;
+        const float4 r = in[(size_t)b * c.n_pad + p];
+        out[3 * (size_t)i] = r.x;
+        out[3 * (size_t)i + 1] = r.y;
+        out[3 * (size_t)i + 2] = r.z;
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------------------------
@@ -804,8 +835,9 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
     pos_.reset(new DeviceBuffer(off * sizeof(float4)));
     pos_float4 = off;
     CudaCheck(cudaMemset(pos_->ptr, 0, off * sizeof(float4)), "memset");
-    CudaCheck(cudaMallocHost(&staging_, off * sizeof(float4)), "pinned staging");
-    std::memset(staging_, 0, off * sizeof(float4));
+    dstage_.reset(new DeviceBuffer(std::max<uint64_t>(path_doubles, 1) * sizeof(double)));
+    path_off_dev_.reset(new DeviceBuffer(n_chains * sizeof(uint64_t)));
+    CudaCheck(cudaMemcpy(path_off_dev_->ptr, path_off_.data(), n_chains * sizeof(uint64_t), cudaMemcpyHostToDevice), "path offsets");
     last_.reset(new DeviceBuffer((size_t)n_chains * kBatchSeriesComponents * sizeof(double)));
     CudaCheck(cudaMemset(last_->ptr, 0, last_->bytes), "memset");
     chains_dev_.reset(new DeviceBuffer(n_chains * sizeof(ChainDev)));
@@ -839,7 +871,6 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
 
 ChainBatch::~ChainBatch() {
     if (graph_) cudaGraphExecDestroy(graph_);
-    if (staging_) cudaFreeHost(staging_);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -920,62 +951,31 @@ void ChainBatch::GetPath(uint32_t chain, double* p) {
         }
 }
 
-/// Runs f(chain) for every chain on a few host threads (contiguous chain ranges).
-template <class F>
-static void ForChains(uint32_t n_chains, F f) {
-    const uint32_t hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-    const uint32_t nt = std::min(hw, n_chains);
-    std::vector<std::thread> pool;
-    std::vector<std::exception_ptr> errs(nt);
-    for (uint32_t t = 0; t < nt; ++t)
-        pool.emplace_back([&, t] {
-            try {
-                for (uint32_t ci = t * n_chains / nt; ci < (t + 1) * n_chains / nt; ++ci) f(ci);
-            } catch (...) {
-                errs[t] = std::current_exception();
-            }
-        });
-    for (auto& th : pool) th.join();
-    for (auto& e : errs)
-        if (e) std::rethrow_exception(e);
-}
-
-/// Every chain's path in one transfer: converted into the pinned float4 mirror (host threads over
-/// the chains), then one copy.
+/// Every chain's path in one transfer: the caller's doubles are copied as they are (from pinned
+/// memory at full link speed) and laid out as float4 on the device.
 void ChainBatch::SetPaths(const double* all) {
     if (!all) throw PimcError(kErrArg, "null paths");
-    ForChains(n_chains, [&](uint32_t ci) {
-        const ChainDev& c = chains[ci];
-        const double* src = all + path_off_[ci];
-        float4* dst = staging_ + c.pos_off;
-        for (uint32_t i = 0; i < c.n_part; ++i)
-            for (uint32_t b = 0; b < c.n_bead; ++b) {
-                const double* r = src + ((size_t)i * c.n_bead + b) * 3;
-                if (!std::isfinite(r[0]) || !std::isfinite(r[1]) || !std::isfinite(r[2])) throw PimcError(kErrArg, "non-finite position");
-                dst[(size_t)b * c.n_pad + i] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.f);
-            }
-    });
-    CudaCheck(cudaMemcpyAsync(pos_->ptr, staging_, pos_float4 * sizeof(float4), cudaMemcpyHostToDevice, stream), "set paths");
+    CudaCheck(cudaMemcpyAsync(dstage_->ptr, all, path_doubles * sizeof(double), cudaMemcpyHostToDevice, stream), "set paths");
+    CudaCheck(cudaMemsetAsync(err_->ptr, 0, sizeof(int), stream), "clear error");
+    HostLayoutToPosKernel<<<n_chains, 256, 0, stream>>>(dstage_->as<double>(), chains_dev_->as<ChainDev>(), path_off_dev_->as<uint64_t>(),
+                                                         pos_->as<float4>(), err_->as<int>());
+    CudaCheck(cudaGetLastError(), "path layout launch");
+    int e = 0;
+    CudaCheck(cudaMemcpyAsync(&e, err_->ptr, sizeof(int), cudaMemcpyDeviceToHost, stream), "read error word");
     CudaCheck(cudaStreamSynchronize(stream), "sync");
+    if (e & kDevErrNonFinite) {
+        CudaCheck(cudaMemset(err_->ptr, 0, sizeof(int)), "clear error");
+        throw PimcError(kErrArg, "non-finite position");
+    }
 }
 
 void ChainBatch::GetPaths(double* all) {
     if (!all) throw PimcError(kErrArg, "null paths");
-    CudaCheck(cudaMemcpyAsync(staging_, pos_->ptr, pos_float4 * sizeof(float4), cudaMemcpyDeviceToHost, stream), "get paths");
+    PosToHostLayoutKernel<<<n_chains, 256, 0, stream>>>(pos_->as<float4>(), chains_dev_->as<ChainDev>(), path_off_dev_->as<uint64_t>(),
+                                                         dstage_->as<double>());
+    CudaCheck(cudaGetLastError(), "path layout launch");
+    CudaCheck(cudaMemcpyAsync(all, dstage_->ptr, path_doubles * sizeof(double), cudaMemcpyDeviceToHost, stream), "get paths");
     CudaCheck(cudaStreamSynchronize(stream), "sync");
-    ForChains(n_chains, [&](uint32_t ci) {
-        const ChainDev& c = chains[ci];
-        const float4* src = staging_ + c.pos_off;
-        double* dst = all + path_off_[ci];
-        for (uint32_t i = 0; i < c.n_part; ++i)
-            for (uint32_t b = 0; b < c.n_bead; ++b) {
-                const float4 r = src[(size_t)b * c.n_pad + i];
-                double* o = dst + ((size_t)i * c.n_bead + b) * 3;
-                o[0] = r.x;
-                o[1] = r.y;
-                o[2] = r.z;
-            }
-    });
 }
 
 void ChainBatch::LastEnergy(double* out) {
