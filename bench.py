@@ -104,7 +104,7 @@ def measured_hbm_peak():
     return 6800.0, "fallback"
 
 
-def blocking_error(x):
+def blocking_error(x):  # noqa: D401 (same estimator as simpimc_gb300.stats.blocking_error)
     """Standard error of the mean of a correlated series by Flyvbjerg-Petersen blocking: the
     largest naive error over the halving levels that keep at least 16 blocks."""
     x = np.asarray(x, dtype=np.float64)
