@@ -49,6 +49,8 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+from simpimc_gb300.stats import blocking_error  # noqa: E402
+
 METRIC = "bead-moves/s"
 N_CHAINS, SEED0, CHAIN_LEVEL = 256, 1000, 3
 WORKLOAD = ("256 independent harmonic-trap Coulomb chains (omega=1, beta=2, open), N~U{16..128}, M in {32,64,128}, "
@@ -102,18 +104,6 @@ def measured_hbm_peak():
         d = json.loads(p.read_text())
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
-
-
-def blocking_error(x):  # noqa: D401 (same estimator as simpimc_gb300.stats.blocking_error)
-    """Standard error of the mean of a correlated series by Flyvbjerg-Petersen blocking: the
-    largest naive error over the halving levels that keep at least 16 blocks."""
-    x = np.asarray(x, dtype=np.float64)
-    best = 0.0
-    while x.size >= 16:
-        best = max(best, float(np.std(x, ddof=1) / math.sqrt(x.size)))
-        n = x.size // 2
-        x = 0.5 * (x[0:2 * n:2] + x[1:2 * n:2])
-    return best
 
 
 def reduce_max_over_ranks(values, dist=None, device=None):
