@@ -136,6 +136,14 @@ int pimc_synchronize(pimc_ctx* ctx);
 /* Tuning: CTAs of the cooperative sweep (0 = automatic) and the device wait limit. */
 int pimc_set_sweep_grid(pimc_ctx* ctx, int grid);
 int pimc_set_timeout_ns(pimc_ctx* ctx, uint64_t ns);
+/* Bisection attempts in flight per round of the sweep (1..8; 0, the default, = automatic): the
+ * blocks split into that many groups, and each round runs the longest prefix of the schedule's next
+ * attempts in which no attempt reads what an earlier one may change (no earlier attempt's inner
+ * slices meet its closed segment). The Markov chain is the sequential one, bit for bit. Automatic
+ * takes 2 when a segment's density work (2^max_level slices x k-vectors) is at most 2^17 and 1
+ * otherwise. Schedules with a move that has no pair action, or a segment longer than half the
+ * ring, run one attempt at a time. */
+int pimc_set_sweep_wave(pimc_ctx* ctx, int wave);
 /* CUDA stream of the context (cudaStream_t), for callers that enqueue their own work. */
 void* pimc_stream(pimc_ctx* ctx);
 /* Sweep tracing, the device-side analogue of the reference's per-event timers (move_class.h:61-77,

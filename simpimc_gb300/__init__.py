@@ -81,6 +81,7 @@ SIGNATURES = {
     "pimc_synchronize": (C.c_int, [_P]),
     "pimc_set_sweep_grid": (C.c_int, [_P, C.c_int]),
     "pimc_set_timeout_ns": (C.c_int, [_P, C.c_uint64]),
+    "pimc_set_sweep_wave": (C.c_int, [_P, C.c_int]),
     "pimc_stream": (_P, [_P]),
     "pimc_sweep_timing": (C.c_int, [_P, C.c_int, _U64P]),
     "pimc_batch_create": (C.c_int, [C.POINTER(C.c_char_p), C.c_uint32, C.c_char_p, C.c_int, C.POINTER(_P)]),
@@ -193,6 +194,10 @@ class Simulation:
     def set_precision(self, bits: int):
         """Sweep precision: 64 (double-float densities) or 32 (FP32 densities and phases)."""
         self._check(self._lib.pimc_set_precision(self._h, bits))
+
+    def set_sweep_wave(self, wave: int):
+        """Bisection attempts in flight per round of the sweep (1 = one at a time, 0 = automatic)."""
+        self._check(self._lib.pimc_set_sweep_wave(self._h, wave))
 
     def set_timeout_ns(self, ns: int):
         self._check(self._lib.pimc_set_timeout_ns(self._h, ns))

@@ -246,6 +246,11 @@ int pimc_set_sweep_grid(pimc_ctx* ctx, int grid) {
     return Guard(ctx, [&](pimc::Context& c) { c.sweep_grid = grid < 0 ? 0 : grid; });
 }
 
+int pimc_set_sweep_wave(pimc_ctx* ctx, int wave) {
+    if (wave < 0 || wave > 8) return PIMC_ERR_ARG;
+    return Guard(ctx, [&](pimc::Context& c) { c.sweep_wave = wave; });
+}
+
 int pimc_set_timeout_ns(pimc_ctx* ctx, uint64_t ns) {
     return Guard(ctx, [&](pimc::Context& c) { c.timeout_ns = ns; });
 }

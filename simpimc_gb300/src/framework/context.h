@@ -156,6 +156,7 @@ class Context {
     uint32_t seed = 12345, chain = 0;
     uint64_t timeout_ns = 2000000000ull;
     int sweep_grid = 0;       // CTAs of the cooperative sweep (0 = automatic)
+    int sweep_wave = 0;       // bisection attempts in flight per round of the sweep (0 = automatic)
     int last_grid_ = 0;       // CTAs of the most recent sweep launch
     bool phase_timing = false;  // record per-phase cycles of block 0 in the sweep kernel
     std::unique_ptr<DeviceBuffer> phase_buf;  // unsigned long long [kSweepPhases]
@@ -194,7 +195,7 @@ class Context {
 
    private:
     std::vector<std::unique_ptr<DeviceBuffer>> keep_;  // tables owned for the context lifetime
-    std::unique_ptr<DeviceBuffer> pos_dd_, rho_dd_, rho32_, sweep_desc_, sweep_tables_;
+    std::unique_ptr<DeviceBuffer> pos_dd_, rho_dd_, rho32_, sweep_desc_, sweep_tables_, sched_wave_;
     bool sweep_tables_built_ = false;
     std::vector<uint32_t> desc_levels_;  // bisection levels the uploaded move descriptors were built for
     struct StageTable {

@@ -99,6 +99,14 @@ struct SweepArgs {
     float4* level_out;        // [2][kMaxLevels]: (diff, small) of each level from its designated block
     uint64_t timeout_ns;
     unsigned long long* phase_cycles;  // optional [kSweepPhases]: block 0's cycles per phase, summed
+    // Concurrent attempts: `wave` groups of `group_ctas` blocks; the schedule flattened per
+    // repetition (sched_prefix[e] = attempts before entry e, move_before[e] = attempts of its move
+    // before it, per_rep_move[m] = attempts of move m per repetition).
+    uint32_t wave, group_ctas;
+    uint64_t per_rep;
+    uint64_t per_rep_move[kMaxMoves];
+    const uint64_t* sched_prefix;
+    const uint64_t* move_before;
     // Shared-memory staging (byte offsets into the dynamic shared block).
     uint32_t n_moves, n_pairs;
     uint32_t off_moves, off_pairs, off_phase, off_work;
@@ -114,6 +122,21 @@ constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 constexpr int kDeltaCache = 4;
 constexpr uint32_t kMaxOwned = 8;
+constexpr uint32_t kWaveSlots = 8;  // most attempts in flight in one round
+
+__device__ __forceinline__ bool CircOverlap(uint32_t s1, uint32_t l1, uint32_t s2, uint32_t l2, uint32_t M) {
+    return (s2 + M - s1) % M < l1 || (s1 + M - s2) % M < l2;
+}
+
+/// Does attempt j (later in the schedule) read anything attempt i may change? Attempt i changes
+/// the beads of its particle and the densities of its inner slices. Attempt j reads its own
+/// particle's whole segment and, through its pair links (b, b + 1) for b in [bj, bj + Bj), every
+/// particle on every slice of the closed segment: a link at an end slice takes the other
+/// particle's bead there, and a pair density u(r, r') does not cancel it between the old and new
+/// action. So j conflicts with i whenever i's inner slices meet j's closed segment.
+__device__ __forceinline__ bool Conflicts(uint32_t bi, uint32_t Bi, uint32_t bj, uint32_t Bj, uint32_t M) {
+    return CircOverlap((bi + 1) % M, Bi - 1, bj, Bj + 1, M);
+}
 
 __device__ __forceinline__ dd LoadDD(const float2* p) {
     const float2 v = *p;
@@ -380,7 +403,9 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t G = gridDim.x, cta = blockIdx.x;
-    const uint32_t r_own = cta % a.R, q_own = cta / a.R;
+    // Group of this block (one attempt per group and round) and its place in the group.
+    const uint32_t Gg = a.group_ctas, grp = cta / Gg, lc = cta - grp * Gg;
+    const uint32_t r_own = lc % a.R, q_own = lc / a.R;
     const bool owns_k = q_own < a.Q;
     const uint32_t k_lo = owns_k ? (uint32_t)(((uint64_t)K * q_own) / a.Q) : 0u;
     const uint32_t k_hi = owns_k ? (uint32_t)(((uint64_t)K * (q_own + 1)) / a.Q) : 0u;
@@ -409,9 +434,9 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
 #define PIMC_ROLE_END(v, r)                                                                         \
     if (timing_cta && lane == 0) atomicMax(&s_role_max[r], (unsigned long long)(clock64() - v))
 
-    for (uint64_t rep = 0; rep < a.n_rep; ++rep) {
-        for (uint32_t e = 0; e < a.n_entries; ++e) {
-            const uint32_t m = a.sched_move[e];
+    bool abort = false;
+    // One bisection attempt of move m with Philox counter actr, by this block's group.
+    auto attempt = [&](const uint32_t m, const uint64_t actr) {
             const MoveDD& mv = s_moves[m];
             const uint32_t s = mv.species, nl = mv.n_level, B = 1u << nl;
             const uint32_t g_off = a.sp_off[s];
@@ -434,21 +459,20 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                 }
             }
             link_off[mv.n_pair] = n_links;
-            // Pair link l is evaluated by block l mod G, lane quad 127 - (l / G) mod 128: links fill
-            // the top warps first, which are idle while the sampling chain runs.
+            // Pair link l is evaluated by block l mod Gg of the group, lane quad 127 - (l / Gg) mod
+            // 128: links fill the top warps first, which are idle while the sampling chain runs.
             const uint32_t n_quads = blockDim.x / 4;
             const int qlane = tid & 3;
-            const uint32_t link_stride = G * n_quads;
-            const uint32_t link_first = cta + G * (n_quads - 1 - (uint32_t)(tid >> 2));
+            const uint32_t link_stride = Gg * n_quads;
+            const uint32_t link_first = lc + Gg * (n_quads - 1 - (uint32_t)(tid >> 2));
             // Warp-uniform trip count of the link loop (all lanes join the quad shuffles).
-            const uint32_t warp_first = cta + G * (n_quads - 1 - (uint32_t)((warp * 32 + 31) >> 2));
+            const uint32_t warp_first = lc + Gg * (n_quads - 1 - (uint32_t)((warp * 32 + 31) >> 2));
             const uint32_t link_rounds = warp_first < n_links ? (n_links - warp_first + link_stride - 1) / link_stride : 0u;
             // Designated blocks for the per-level sums when the attempt has a grid phase: the last
-            // n_level blocks, one level each (published with the grid barrier).
-            const int my_level = (grid_work && cta + nl >= G) ? (int)(G - 1 - cta) : -1;
-            for (uint64_t c = 0, count = a.sched_count[e]; c < count; ++c) {
-                const MoveStream st{a.seed, a.chain, m, ctr[m]};
-                ctr[m] += 1;
+            // n_level blocks of the group, one level each (published with the grid barrier).
+            const int my_level = (grid_work && lc + nl >= Gg) ? (int)(Gg - 1 - lc) : -1;
+            {
+                const MoveStream st{a.seed, a.chain, m, actr};
                 const Philox4 w0 = st.Block(0);
                 const uint32_t p = UniformIndex(w0.v[0], a.sp_n[s]);
                 const uint32_t bead0 = UniformIndex(w0.v[1], M);
@@ -592,7 +616,8 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                         const dd small = Sub(sm, s_old_small[lvl]); // new action - old action
                         if (my_level >= 0) {
                             // published with this attempt's grid barrier (generation nbar + 1)
-                            __stcg(&a.level_out[((nbar + 1) & 1ull) * kMaxLevels + lvl], make_float4(diff.hi, diff.lo, small.hi, small.lo));
+                            __stcg(&a.level_out[(((nbar + 1) & 1ull) * kWaveSlots + grp) * kMaxLevels + lvl],
+                                   make_float4(diff.hi, diff.lo, small.hi, small.lo));
                         } else {
                             s_lvl_diff[lvl] = diff;
                             s_lvl_small[lvl] = small;
@@ -716,11 +741,14 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                         t = WarpSumDD(t);
                         if (lane == 0) __stcg(&a.partials[(nbar & 1ull) * G + cta], make_float2(t.hi, t.lo));
                     }
-                    if (!GridBarrier(a.bar, nbar, a.err, a.timeout_ns)) return;
+                    if (!GridBarrier(a.bar, nbar, a.err, a.timeout_ns)) {
+                        abort = true;
+                        return;
+                    }
                     PIMC_PHASE(4);
                     if (warp == 0) {
                         dd t{0.f, 0.f};
-                        for (uint32_t c2 = lane; c2 < G; c2 += 32) {
+                        for (uint32_t c2 = grp * Gg + lane; c2 < (grp + 1) * Gg; c2 += 32) {
                             const float2 pv = __ldcg(&a.partials[(nbar & 1ull) * G + c2]);
                             t = Add(t, dd{pv.x, pv.y});
                         }
@@ -728,7 +756,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                         if (lane == 0) s_big = t;
                         if (lane < (int)nl) {
                             // level sums from the designated blocks (written before their arrival)
-                            const float4 v = __ldcg(&a.level_out[(nbar & 1ull) * kMaxLevels + lane]);
+                            const float4 v = __ldcg(&a.level_out[((nbar & 1ull) * kWaveSlots + grp) * kMaxLevels + lane]);
                             s_lvl_diff[lane] = dd{v.x, v.y};
                             s_lvl_small[lane] = dd{v.z, v.w};
                         }
@@ -769,7 +797,10 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                 __syncthreads();
                 PIMC_PHASE(6);
                 const int res = s_result & 3;
-                if (res == 2) return;
+                if (res == 2) {
+                    abort = true;
+                    return;
+                }
                 if (s_result & 4) n_l0[m] += 1;
 
                 // ---- 6. commit ---------------------------------------------------------------
@@ -822,15 +853,70 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                         s_role_max[r] = 0ull;
                     }
             }
+    };
+
+    if (a.wave <= 1) {
+        for (uint64_t rep = 0; rep < a.n_rep; ++rep)
+            for (uint32_t e = 0; e < a.n_entries; ++e) {
+                const uint32_t m = a.sched_move[e];
+                for (uint64_t c = 0, count = a.sched_count[e]; c < count; ++c) {
+                    attempt(m, ctr[m]);
+                    ctr[m] += 1;
+                    if (abort) return;
+                }
+            }
+    } else {
+        // Rounds of concurrent attempts: the longest prefix of the next `wave` attempts of the
+        // schedule in which no attempt reads what an earlier one may change; group j runs attempt
+        // j (the sequential chain's result), and a second grid barrier makes every commit visible
+        // before the next round reads. Idle groups keep the barrier count.
+        const uint64_t total = a.n_rep * a.per_rep;
+        uint64_t A = 0;
+        while (A < total) {
+            uint32_t wm[kWaveSlots], wb0[kWaveSlots], wB[kWaveSlots];
+            uint64_t wc[kWaveSlots];
+            uint32_t w = 0;
+            for (uint32_t j = 0; j < a.wave && A + j < total; ++j) {
+                const uint64_t x = A + j, rep = x / a.per_rep, r = x - rep * a.per_rep;
+                uint32_t lo = 0, hi = a.n_entries;  // the entry holding position r of a repetition
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (a.sched_prefix[mid] <= r) lo = mid;
+                    else hi = mid;
+                }
+                const uint32_t m = a.sched_move[lo];
+                const uint64_t actr = a.attempt_base[m] + rep * a.per_rep_move[m] + a.move_before[lo] + (r - a.sched_prefix[lo]);
+                const Philox4 w0 = MoveStream{a.seed, a.chain, m, actr}.Block(0);
+                const uint32_t bj = UniformIndex(w0.v[1], M);  // the attempt's first slice
+                const uint32_t Bj = 1u << s_moves[m].n_level;
+                bool clear = true;
+                for (uint32_t i = 0; i < j && clear; ++i) clear = !Conflicts(wb0[i], wB[i], bj, Bj, M);
+                if (!clear) break;
+                wm[j] = m;
+                wc[j] = actr;
+                wb0[j] = bj;
+                wB[j] = Bj;
+                ++w;
+            }
+            if (grp < w) {
+                attempt(wm[grp], wc[grp]);
+                if (abort) return;
+            } else {
+                ++nbar;
+                if (!GridBarrier(a.bar, nbar, a.err, a.timeout_ns)) return;
+            }
+            ++nbar;
+            if (!GridBarrier(a.bar, nbar, a.err, a.timeout_ns)) return;
+            A += w;
         }
     }
 #undef PIMC_PHASE
 #undef PIMC_ROLE_BEGIN
 #undef PIMC_ROLE_END
-    if (cta == 0 && tid == 0) {
+    if (lc == 0 && tid == 0) {  // each group's first block reports its group's attempts
         for (int m = 0; m < kMaxMoves; ++m) {
-            a.counters[m] += n_acc[m];
-            a.counters[kMaxMoves + m] += n_l0[m];
+            atomicAdd(&a.counters[m], n_acc[m]);
+            atomicAdd(&a.counters[kMaxMoves + m], n_l0[m]);
         }
         if (timing)
             for (int i = 0; i < kSweepTimingSlots; ++i) a.phase_cycles[i] += ph[i];
@@ -1206,15 +1292,50 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
     args->seg_cap = (1u << max_level) + 1;
     args->tab_stride = (uint32_t)std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
 
-    const int G = sweep_grid > 0 ? sweep_grid : n_sm;
-    if ((uint32_t)G < max_level) throw PimcError(kErrArg, "sweep grid smaller than the bisection level count");
+    // Concurrent attempts need every scheduled move to have a grid phase (a non-constant pair
+    // action) and segments of at most half the ring; otherwise one attempt at a time. Automatic:
+    // two groups when an attempt's density work is small (66-electron gas, 16 slices x 3.6k
+    // k-vectors: 1.35x faster per sweep), one when it fills the grid (1024 electrons, 16 x 25k:
+    // two and four groups were slower).
+    uint32_t wave = sweep_wave > 0 ? (uint32_t)std::min(sweep_wave, (int)kWaveSlots)
+                                   : ((uint64_t(1) << max_level) * sys.K <= (uint64_t(1) << 17) ? 2u : 1u);
+    for (uint32_t e = 0; e < n_entries; ++e) {
+        const MoveDev& d = moves[mv[e]].dev;
+        bool gw = false;
+        for (int i = 0; i < d.n_pair; ++i) gw |= !sys.pair[d.pair[i]].is_constant;
+        if (!gw || (2u << d.n_level) > sys.M) wave = 1;
+    }
+    const int G0 = sweep_grid > 0 ? sweep_grid : n_sm;
+    const uint32_t Gg = (uint32_t)G0 / wave;
+    const int G = (int)(Gg * wave);
+    if (Gg < max_level + 1) throw PimcError(kErrArg, "sweep grid (per concurrent attempt) smaller than the bisection level count");
     uint32_t R = 1;
-    while (R * 2 <= (1u << max_level) && R * 2 <= (uint32_t)G) R *= 2;
+    while (R * 2 <= (1u << max_level) && R * 2 <= Gg) R *= 2;
     const uint32_t spc = std::max<uint32_t>(1, (1u << max_level) / R);
     if (spc > kMaxOwned) throw PimcError(kErrUnsupported, "too few blocks for the segment length");
     args->R = R;
-    args->Q = std::max<uint32_t>(1, (uint32_t)G / R);
+    args->Q = std::max<uint32_t>(1, Gg / R);
     args->slices_per_cta = spc;
+    args->wave = wave;
+    args->group_ctas = Gg;
+    {
+        // The schedule flattened per repetition, for the rounds' attempt lookup.
+        std::vector<uint64_t> pre(n_entries + 1, 0), before(n_entries, 0);
+        std::vector<uint64_t> per_move(kMaxMoves, 0);
+        for (uint32_t e = 0; e < n_entries; ++e) {
+            pre[e + 1] = pre[e] + counts[e];
+            before[e] = per_move[mv[e]];
+            per_move[mv[e]] += counts[e];
+        }
+        args->per_rep = pre[n_entries];
+        for (int m = 0; m < kMaxMoves; ++m) args->per_rep_move[m] = per_move[m];
+        if (!sched_wave_) sched_wave_.reset(new DeviceBuffer(2 * 1025 * sizeof(uint64_t)));
+        uint64_t* dw = sched_wave_->as<uint64_t>();
+        CudaCheck(cudaMemcpyAsync(dw, pre.data(), pre.size() * 8, cudaMemcpyHostToDevice, stream), "schedule prefix");
+        CudaCheck(cudaMemcpyAsync(dw + 1025, before.data(), before.size() * 8, cudaMemcpyHostToDevice, stream), "schedule prefix");
+        args->sched_prefix = dw;
+        args->move_before = dw + 1025;
+    }
     // Shared layout: [move descriptors][pair descriptors][phase table][staged splines][work area].
     auto align16 = [](size_t x) { return (x + 15) & ~size_t(15); };
     const size_t work = (size_t)2 * spc * 3 * args->tab_stride * sizeof(ddc) + (size_t)4 * 3 * args->seg_cap * sizeof(dd) +
@@ -1252,7 +1373,7 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
     args->counters = dcount;
     args->bar = Barrier();
     args->err = ErrWord();
-    double* scratch = Partials((size_t)2 * G + 4 * kMaxLevels);
+    double* scratch = Partials((size_t)2 * G + 4 * kWaveSlots * kMaxLevels);
     args->partials = reinterpret_cast<float2*>(scratch);
     args->level_out = reinterpret_cast<float4*>(scratch + (size_t)2 * G);
     args->timeout_ns = timeout_ns;

@@ -54,6 +54,11 @@ def test_malformed_input_is_an_error_code(lib):
     assert b"XML parse error" in lib.pimc_last_error(None)
     assert not h.value
     assert lib.pimc_create(None, b".", 0, 0, C.byref(h)) == -1
+    # concurrent-attempt count outside 0..8 is rejected before the context is touched
+    lib.pimc_set_sweep_wave.restype = C.c_int
+    lib.pimc_set_sweep_wave.argtypes = [C.c_void_p, C.c_int]
+    assert lib.pimc_set_sweep_wave(None, 9) == -1
+    assert lib.pimc_set_sweep_wave(None, -1) == -1
 
 
 def test_binding_fails_loudly_without_library(tmp_path):

@@ -170,6 +170,28 @@ def test_egas_bisection_replay(tmp_path, gpu_lib, oracle_mod):
         assert close(g.dactiondbeta(a), c.dactiondbeta(a), 1e-9)
 
 
+@pytest.mark.parametrize("wave", [0, 1, 2, 4, 8])
+def test_concurrent_sweep_replays_oracle(tmp_path, gpu_lib, oracle_mod, wave):
+    """Rounds of conflict-free attempts give the sequential chain for every wave size."""
+    xml, path = electron_gas(tmp_path, n_part=14, n_bead=64, n_level=3, rs=2.0, k_cut_units=4.0, seed=31)
+    g = Simulation(xml, base_dir=tmp_path)
+    c = oracle_mod.OracleSim(xml, base_dir=tmp_path)
+    g.set_sweep_wave(wave)
+    g.set_path(path)
+    c.set_path(path)
+    g.sweep([0, 1], [7, 7], n_rep=12)
+    for _ in range(12):
+        c.move_attempts(0, 7)
+        c.move_attempts(1, 7)
+    for m in range(2):
+        assert g.move_stats(m) == c.move_stats(m), (wave, m)
+    assert np.max(np.abs(g.get_path(1) - c.get_path(1))) < 1e-9
+    for s in range(2):
+        assert np.max(np.abs(g.rho_k(s) - c.rho_k(s))) < 1e-9
+    g.close()
+    c.close()
+
+
 def test_observables_blocks(tmp_path, gpu_lib, oracle_mod):
     xml, path = trapped_coulomb(tmp_path, n_part=6, n_bead=16, n_level=2, seed=3, virial=True)
     g = Simulation(xml, base_dir=tmp_path)
