@@ -42,7 +42,8 @@ constexpr uint32_t kMaxWave = 4;               // attempts of one chain in fligh
 struct ChainDev {
     uint32_t n_part, n_bead, n_pad, n_level;  // B = 2^n_level beads per segment
     uint32_t seed, chain_id, n_warps, move;   // Philox keys; warps used; move index in its input
-    uint32_t n_wave, sub_warps, pad2, pad3;   // attempts in flight per round; warps per attempt
+    uint32_t n_wave, sub_warps, staged, pad3; // attempts in flight per round; warps per attempt;
+                                              // path held in shared memory during a sweep
     uint64_t pos_off;                         // first float4 of the chain's [n_bead][n_pad] block
     uint64_t attempts_per_sweep;              // n_part * ceil(n_bead / B)
     float L, iL, lambda, tau;
@@ -99,6 +100,8 @@ class ChainBatch {
     uint64_t bead_moves_per_sweep = 0;
     uint64_t path_doubles = 0;  // sum of n_part * n_bead * 3 over the chains
     uint64_t kernel_launches = 0;
+    size_t stage_cap = 0;     // shared memory a sweep block may take for a staged path
+    size_t stage_bytes = 0;   // shared memory the sweep launch requests (largest staged path)
 
    private:
     void Upload();

@@ -93,6 +93,35 @@ __device__ __forceinline__ float Img(float d, float L, float iL) {
 
 constexpr uint32_t kItems = 4;  // pair items per lane kept in registers (more are loaded in the loop)
 
+/// A chain's beads during a sweep: the global float4 block [M][n_pad] (slice-major, x y z 0), or,
+/// when kStaged, three coordinate planes [M][N] in shared memory filled at the start of the
+/// launch and written back at its end.
+template <bool kStaged>
+struct PathView {
+    float4* g;
+    float* s;
+    uint32_t n_pad, n, plane;
+    __device__ __forceinline__ float3 Load(uint32_t b, uint32_t q) const {
+        if constexpr (kStaged) {
+            const uint32_t i = b * n + q;
+            return make_float3(s[i], s[plane + i], s[2 * plane + i]);
+        } else {
+            const float4 v = g[(size_t)b * n_pad + q];
+            return make_float3(v.x, v.y, v.z);
+        }
+    }
+    __device__ __forceinline__ void Store(uint32_t b, uint32_t q, float x, float y, float z) const {
+        if constexpr (kStaged) {
+            const uint32_t i = b * n + q;
+            s[i] = x;
+            s[plane + i] = y;
+            s[2 * plane + i] = z;
+        } else {
+            g[(size_t)b * n_pad + q] = make_float4(x, y, z, 0.f);
+        }
+    }
+};
+
 /// Draws of one attempt (particle, first bead, normals, log-uniforms; philox.h stream layout) into
 /// shared buffers, by one warp; with `seg` also the moved particle's segment as it is now.
 __device__ __forceinline__ void DrawAttempt(const MoveStream& st, uint32_t lane, uint32_t N, uint32_t M, uint32_t B, uint32_t NL, uint32_t n_pad,
@@ -123,22 +152,33 @@ __device__ __forceinline__ void DrawAttempt(const MoveStream& st, uint32_t lane,
 
 /// Warp work of one attempt (bisect_class.h:39-124 above level 0): lane k enters with bead k of
 /// the old segment (every lane also holds the last bead B in e*), samples the new beads level by
-/// level in registers (bead k = 2^l (2m + 1) from beads k -+ 2^l by shuffles), forms each level's
-/// sampling, kinetic and trap terms, reduces them with one compensated butterfly per level and
-/// quantity, writes both segment copies for the pair work, and tests every level above 0. Returns
-/// with the new bead in n*.
-template <bool kPbc>
-__device__ __forceinline__ void LeaderPhase(const ChainDev& c, uint32_t lane, uint32_t B, uint32_t NL, uint32_t M, float ox, float oy, float oz,
-                                            float ex, float ey, float ez, const float* zb, const float* logu, float* s_old, float* s_new,
-                                            dd* base0_out, int* upper_out, float& nx, float& ny, float& nz) {
+/// level in registers (bead k = 2^l (2m + 1) from beads k -+ 2^l by shuffles), writes both segment
+/// copies for the pair work, forms each level's sampling, kinetic and trap terms (the link's far
+/// bead from those copies), reduces them with compensated butterflies over the B lanes that hold
+/// terms (all levels in step, so their latencies overlap), and tests every level above 0, lane l
+/// deciding level l. Returns with the new bead in n*.
+template <bool kPbc, uint32_t NL>
+__device__ __forceinline__ void LeaderPhaseL(const ChainDev& c, uint32_t lane, uint32_t M, float ox, float oy, float oz, float ex, float ey,
+                                             float ez, const float* zb, const float* logu, float* s_old, float* s_new, dd* base0_out,
+                                             int* upper_out, float& nx, float& ny, float& nz) {
+    constexpr uint32_t B = 1u << NL;
     const float L = c.L, iL = c.iL;
     const bool kin_links = B != M;  // whole-ring segment: no kinetic links (kinetic_class.h:111-117)
     const bool inner = lane >= 1 && lane < B;
     const uint32_t lk = lane == 0 ? 31u : (uint32_t)(__ffs(lane) - 1);  // level of bead `lane`
+    // An inner bead is drawn once, on its own level: its scaled normal displacement.
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    if (inner) {
+        const uint32_t zi = 3 * ((B >> (lk + 1)) - 1u + (lane >> (lk + 1)));
+        const float sg = c.sigma[lk];
+        gx = Img<kPbc>(__fmul_rn(sg, zb[zi]), L, iL);
+        gy = Img<kPbc>(__fmul_rn(sg, zb[zi + 1]), L, iL);
+        gz = Img<kPbc>(__fmul_rn(sg, zb[zi + 2]), L, iL);
+    }
     nx = ox;
     ny = oy;
     nz = oz;
-    float dn2 = 0.f;
+#pragma unroll
     for (int li = (int)NL - 1; li >= 0; --li) {
         const uint32_t skip = 1u << li;
         const bool mine = inner && lk == (uint32_t)li;
@@ -153,15 +193,25 @@ __device__ __forceinline__ void LeaderPhase(const ChainDev& c, uint32_t lane, ui
             cz = ez;
         }
         if (mine) {
-            const uint32_t zi = 3 * ((B >> (li + 1)) - 1u + (lane >> (li + 1)));
-            const float sg = c.sigma[li];
-            const float dx = Img<kPbc>(__fmul_rn(sg, zb[zi]), L, iL), dy = Img<kPbc>(__fmul_rn(sg, zb[zi + 1]), L, iL),
-                        dz = Img<kPbc>(__fmul_rn(sg, zb[zi + 2]), L, iL);
-            nx = __fadd_rn(__fadd_rn(ax, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cx, ax), L, iL))), dx);
-            ny = __fadd_rn(__fadd_rn(ay, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cy, ay), L, iL))), dy);
-            nz = __fadd_rn(__fadd_rn(az, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cz, az), L, iL))), dz);
-            dn2 = Sq3(dx, dy, dz);
+            nx = __fadd_rn(__fadd_rn(ax, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cx, ax), L, iL))), gx);
+            ny = __fadd_rn(__fadd_rn(ay, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cy, ay), L, iL))), gy);
+            nz = __fadd_rn(__fadd_rn(az, __fmul_rn(0.5f, Img<kPbc>(__fsub_rn(cz, az), L, iL))), gz);
         }
+    }
+    const float dn2 = inner ? Sq3(gx, gy, gz) : 0.f;
+    // Segment copies for the pair work and for the links below (bead 32 of a 32-bead segment is e).
+    if (lane <= B) {
+        s_old[3 * lane] = ox;
+        s_old[3 * lane + 1] = oy;
+        s_old[3 * lane + 2] = oz;
+        s_new[3 * lane] = nx;
+        s_new[3 * lane + 1] = ny;
+        s_new[3 * lane + 2] = nz;
+    }
+    if (B == 32 && lane == 0) {
+        s_old[96] = s_new[96] = ex;
+        s_old[97] = s_new[97] = ey;
+        s_old[98] = s_new[98] = ez;
     }
     // Old sampling displacement of bead `lane` on its level.
     float samp = 0.f;
@@ -185,76 +235,72 @@ __device__ __forceinline__ void LeaderPhase(const ChainDev& c, uint32_t lane, ui
             samp = __fmul_rn(c.i4lt_sample[lk], __fsub_rn(dn2, do2));  // log sample ratio term
         }
     }
+    __syncwarp();
     // Per level l and lane k (a multiple of 2^l): the action change of link k -> k + 2^l
     // (kinetic) and slice k (trap); the level's totals come from one compensated butterfly each
     // for  D_l = sum of action changes  and  R_l = sampling ratio - D_l.
-    Comp Dl[kBatchMaxLevels], Rl[kBatchMaxLevels];
+    Comp Dl[NL + 1], Rl[NL];
+    Dl[NL] = Comp{0.f, 0.f};
 #pragma unroll
-    for (uint32_t li = 0; li < kBatchMaxLevels; ++li) {
+    for (uint32_t li = 0; li < NL; ++li) {
         float dterm = 0.f;
-        if (li < NL) {
-            const uint32_t skip = 1u << li;
-            const bool mine = lane < B && (lane & (skip - 1u)) == 0u;
-            const uint32_t sc = mine ? lane + skip : lane;
-            float cx = __shfl_sync(0xffffffffu, nx, sc & 31u), cy = __shfl_sync(0xffffffffu, ny, sc & 31u),
-                  cz = __shfl_sync(0xffffffffu, nz, sc & 31u);
-            float dx = __shfl_sync(0xffffffffu, ox, sc & 31u), dy = __shfl_sync(0xffffffffu, oy, sc & 31u),
-                  dz = __shfl_sync(0xffffffffu, oz, sc & 31u);
-            if (sc == 32u) {
-                cx = dx = ex;
-                cy = dy = ey;
-                cz = dz = ez;
+        const uint32_t skip = 1u << li;
+        if (lane < B && (lane & (skip - 1u)) == 0u) {
+            const float* cn = s_new + 3 * (lane + skip);
+            const float* co = s_old + 3 * (lane + skip);
+            if (kin_links) {
+                const float kn = Sq3(Img<kPbc>(__fsub_rn(nx, cn[0]), L, iL), Img<kPbc>(__fsub_rn(ny, cn[1]), L, iL), Img<kPbc>(__fsub_rn(nz, cn[2]), L, iL));
+                const float ko = Sq3(Img<kPbc>(__fsub_rn(ox, co[0]), L, iL), Img<kPbc>(__fsub_rn(oy, co[1]), L, iL), Img<kPbc>(__fsub_rn(oz, co[2]), L, iL));
+                dterm = __fmul_rn(c.i4lt_level[li], __fsub_rn(kn, ko));
             }
-            if (mine) {
-                if (kin_links) {
-                    const float kn = Sq3(Img<kPbc>(__fsub_rn(nx, cx), L, iL), Img<kPbc>(__fsub_rn(ny, cy), L, iL), Img<kPbc>(__fsub_rn(nz, cz), L, iL));
-                    const float ko = Sq3(Img<kPbc>(__fsub_rn(ox, dx), L, iL), Img<kPbc>(__fsub_rn(oy, dy), L, iL), Img<kPbc>(__fsub_rn(oz, dz), L, iL));
-                    dterm = __fmul_rn(c.i4lt_level[li], __fsub_rn(kn, ko));
-                }
-                if (c.has_trap && (int)li <= c.trap_max_level)
-                    dterm = __fadd_rn(dterm, __fmul_rn(__fmul_rn(c.trap_cofa, (float)skip), __fsub_rn(Sq3(nx, ny, nz), Sq3(ox, oy, oz))));
-            }
+            if (c.has_trap && (int)li <= c.trap_max_level)
+                dterm = __fadd_rn(dterm, __fmul_rn(__fmul_rn(c.trap_cofa, (float)skip), __fsub_rn(Sq3(nx, ny, nz), Sq3(ox, oy, oz))));
         }
         Dl[li] = Comp{dterm, 0.f};
         Rl[li] = Comp{__fsub_rn(inner && lk == li ? samp : 0.f, dterm), 0.f};
     }
+    // Every term sits on a lane below B, so a butterfly over B lanes gives those lanes the totals
+    // (the wider one would only merge zeros, which leave a compensated pair unchanged).
 #pragma unroll
-    for (uint32_t li = 0; li < kBatchMaxLevels; ++li)
-        if (li < NL) {
-            Dl[li] = CompWarpSum(Dl[li], 32);
-            Rl[li] = CompWarpSum(Rl[li], 32);
-        }
-    // Segment copies for the pair work.
-    if (lane <= B) {
-        s_old[3 * lane] = ox;
-        s_old[3 * lane + 1] = oy;
-        s_old[3 * lane + 2] = oz;
-        s_new[3 * lane] = nx;
-        s_new[3 * lane + 1] = ny;
-        s_new[3 * lane + 2] = nz;
-    }
-    if (B == 32 && lane == 0) {
-        s_old[96] = s_new[96] = ex;
-        s_old[97] = s_new[97] = ey;
-        s_old[98] = s_new[98] = ez;
-    }
-    // Level l passes if  R_l + D_{l+1} >= log u_l  (bisect_class.h:110-121); every lane holds every
-    // level's totals, so lane l tests level l.
-    bool fail = false;
-    dd base0 = DD(0.f);
+    for (uint32_t o = B >> 1; o > 0; o >>= 1) {
 #pragma unroll
-    for (uint32_t li = 0; li < kBatchMaxLevels; ++li)
-        if (li < NL) {
-            dd la = CompDD(Rl[li]);
-            if (li + 1 < NL) la = Add(la, CompDD(Dl[li + 1]));
-            if (!isfinite(la.hi)) la.hi = -INFINITY;
-            if (li == 0) base0 = la;
-            else if (lane == li) fail = Less(la, DD(logu[li]));
+        for (uint32_t li = 0; li < NL; ++li) {
+            const Comp dw{__shfl_xor_sync(0xffffffffu, Dl[li].s, o), __shfl_xor_sync(0xffffffffu, Dl[li].c, o)};
+            const Comp rw{__shfl_xor_sync(0xffffffffu, Rl[li].s, o), __shfl_xor_sync(0xffffffffu, Rl[li].c, o)};
+            Dl[li] = CompMerge(Dl[li], dw);
+            Rl[li] = CompMerge(Rl[li], rw);
         }
+    }
+    // Level l passes if  R_l + D_{l+1} >= log u_l  (bisect_class.h:110-121); lane l tests level l
+    // and lane 0 keeps level 0's value for the pair test.
+    Comp rs = Rl[0], dn = Dl[1];
+#pragma unroll
+    for (uint32_t li = 1; li < NL; ++li)
+        if (lane == li) {
+            rs = Rl[li];
+            dn = Dl[li + 1];
+        }
+    dd la = CompDD(rs);
+    if (lane + 1 < NL) la = Add(la, CompDD(dn));
+    if (!isfinite(la.hi)) la.hi = -INFINITY;
+    const bool fail = lane >= 1 && lane < NL && Less(la, DD(logu[lane]));
     const unsigned fails = __ballot_sync(0xffffffffu, fail);
     if (lane == 0) {
         *upper_out = fails == 0u;
-        *base0_out = base0;
+        *base0_out = la;
+    }
+}
+
+template <bool kPbc>
+__device__ __forceinline__ void LeaderPhase(const ChainDev& c, uint32_t lane, uint32_t NL, uint32_t M, float ox, float oy, float oz, float ex,
+                                            float ey, float ez, const float* zb, const float* logu, float* s_old, float* s_new, dd* base0_out,
+                                            int* upper_out, float& nx, float& ny, float& nz) {
+    switch (NL) {
+        case 1: LeaderPhaseL<kPbc, 1>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_old, s_new, base0_out, upper_out, nx, ny, nz); break;
+        case 2: LeaderPhaseL<kPbc, 2>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_old, s_new, base0_out, upper_out, nx, ny, nz); break;
+        case 3: LeaderPhaseL<kPbc, 3>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_old, s_new, base0_out, upper_out, nx, ny, nz); break;
+        case 4: LeaderPhaseL<kPbc, 4>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_old, s_new, base0_out, upper_out, nx, ny, nz); break;
+        default: LeaderPhaseL<kPbc, 5>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_old, s_new, base0_out, upper_out, nx, ny, nz); break;
     }
 }
 
@@ -262,13 +308,13 @@ __device__ __forceinline__ void LeaderPhase(const ChainDev& c, uint32_t lane, ui
 /// (N-1); this lane's first kItems items (attempt-independent decomposition in it_k / it_q,
 /// beads already in pre[]) and any further ones at stride T. Returns the lane's compensated sum
 /// of 1/r_new - 1/r_old (clamped to the table's grid).
-template <bool kPbc>
+template <bool kPbc, bool kStaged>
 __device__ __forceinline__ Comp PairPhase(const ChainDev& c, uint32_t t, uint32_t T, uint32_t n_items, uint32_t magic, uint32_t nm1, uint32_t p,
-                                          uint32_t b0, uint32_t M, uint32_t n_pad, const float4* __restrict__ pos, const uint32_t* it_k,
-                                          const float4* pre, const float* s_old, const float* s_new) {
+                                          uint32_t b0, uint32_t M, const PathView<kStaged>& path, const uint32_t* it_k, const float3* pre,
+                                          const float* s_old, const float* s_new) {
     const float L = c.L, iL = c.iL, r2_min = c.r2_min, r2_max = c.r2_max;
     Comp acc_u{0.f, 0.f};
-    auto item = [&](uint32_t k, float4 rq) {
+    auto item = [&](uint32_t k, float3 rq) {
         const float* ro = s_old + 3 * (k + 1);
         const float* rn = s_new + 3 * (k + 1);
         float r2o = Sq3(Img<kPbc>(__fsub_rn(ro[0], rq.x), L, iL), Img<kPbc>(__fsub_rn(ro[1], rq.y), L, iL), Img<kPbc>(__fsub_rn(ro[2], rq.z), L, iL));
@@ -282,20 +328,25 @@ __device__ __forceinline__ Comp PairPhase(const ChainDev& c, uint32_t t, uint32_
         if (t + j * T < n_items) item(it_k[j], pre[j]);
     for (uint32_t i = t + kItems * T; i < n_items; i += T) {
         const uint32_t k = FastDiv(i, magic), qq = i - k * nm1;
-        item(k, pos[(size_t)Wrap(b0 + 1u + k, M) * n_pad + qq + (qq >= p ? 1u : 0u)]);
+        item(k, path.Load(Wrap(b0 + 1u + k, M), qq + (qq >= p ? 1u : 0u)));
     }
     return acc_u;
 }
 
 /// Level-0 test: pair action difference tau * sum (1/r_new - 1/r_old) over inner slices (each
 /// inner slice closes two links with weight 1/2; the segment ends cancel) joins the level's
-/// double-float total. Every lane of the calling warp gets the same answer.
+/// double-float total. Lane 0 decides (the G warp partials merged over the smallest power-of-two
+/// lane group that holds them) and every lane of the calling warp gets its answer.
 __device__ __forceinline__ bool Level0Accepts(const ChainDev& c, uint32_t lane, uint32_t G, const Comp* part, bool has_items, dd base0, float logu0) {
     dd u = DD(0.f);
-    if (has_items) u = CompDD(CompWarpSum(lane < G ? part[lane] : Comp{0.f, 0.f}, 32));
+    if (has_items) {
+        int width = 1;
+        while (width < (int)G) width <<= 1;
+        u = CompDD(CompWarpSum(lane < G ? part[lane] : Comp{0.f, 0.f}, width));
+    }
     dd la0 = Sub(base0, MulF(u, c.tau));
     if (!isfinite(la0.hi)) la0.hi = -INFINITY;
-    return !Less(la0, DD(logu0));
+    return __shfl_sync(0xffffffffu, (int)!Less(la0, DD(logu0)), 0) != 0;
 }
 
 struct SweepShared {
@@ -319,6 +370,7 @@ __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_
     const ChainDev& c = sh.c;
     const uint32_t N = c.n_part, M = c.n_bead, NL = c.n_level, B = 1u << NL, n_pad = c.n_pad;
     float4* __restrict__ pos = a.pos + c.pos_off;
+    const PathView<false> gpath{pos, nullptr, n_pad, N, 0u};
 
     const uint32_t nm1 = N > 1 ? N - 1 : 1;
     const uint32_t n_items = c.has_pair && N > 1 ? (N - 1) * (B - 1) : 0u;
@@ -350,10 +402,10 @@ __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_
         }
         const uint32_t p = sh.pb[buf][0], b0 = sh.pb[buf][1];
 
-        float4 pre[kItems];
+        float3 pre[kItems];
 #pragma unroll
         for (uint32_t j = 0; j < kItems; ++j)
-            if (t + j * T < n_items) pre[j] = pos[(size_t)Wrap(b0 + 1u + it_k[j], M) * n_pad + it_q[j] + (it_q[j] >= p ? 1u : 0u)];
+            if (t + j * T < n_items) pre[j] = gpath.Load(Wrap(b0 + 1u + it_k[j], M), it_q[j] + (it_q[j] >= p ? 1u : 0u));
 
         if (warp == 0) {
             const float4 sv = sh.seg[buf][lane <= B ? lane : B];
@@ -379,7 +431,7 @@ __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_
                     ez = qz;
                 }
             }
-            LeaderPhase<kPbc>(c, lane, B, NL, M, ox, oy, oz, ex, ey, ez, sh.z[buf], sh.logu[buf], sh.old_, sh.new_, &sh.base0, &sh.upper_ok,
+            LeaderPhase<kPbc>(c, lane, NL, M, ox, oy, oz, ex, ey, ez, sh.z[buf], sh.logu[buf], sh.old_, sh.new_, &sh.base0, &sh.upper_ok,
                               nx, ny, nz);
         } else if (ahead && warp == 1 && it + 1 < n_att) {
             DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, att + 1}, lane, N, M, B, NL, n_pad, pos, sh.z[buf ^ 1u], sh.logu[buf ^ 1u],
@@ -389,7 +441,7 @@ __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_
         const bool upper_ok = sh.upper_ok != 0;
 
         if (upper_ok && n_items) {
-            const Comp u = CompWarpSum(PairPhase<kPbc>(c, t, T, n_items, magic, nm1, p, b0, M, n_pad, pos, it_k, pre, sh.old_, sh.new_), 32);
+            const Comp u = CompWarpSum(PairPhase<kPbc, false>(c, t, T, n_items, magic, nm1, p, b0, M, gpath, it_k, pre, sh.old_, sh.new_), 32);
             if (lane == 0) sh.part[warp] = u;
         }
         GroupSync(G);
@@ -418,11 +470,14 @@ __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_
 // attempts in which every attempt is clear of all earlier ones; they run concurrently, one per
 // sub-group of warps, and commit disjoint beads. The result is the sequential chain's.
 
+constexpr uint32_t kRing = 2 * kMaxWave;  // ring of drawn attempts, slot = attempt mod kRing
+static_assert((kRing & (kRing - 1)) == 0, "the drawn-attempt ring is indexed by a mask");
+
 struct WaveShared {
     ChainDev c;
-    float z[2 * kMaxWave][3 * (kMaxB - 1)];  // ring of drawn attempts, slot = attempt mod 2W
-    float logu[2 * kMaxWave][kBatchMaxLevels];
-    uint32_t pb[2 * kMaxWave][2];
+    float z[kRing][3 * (kMaxB - 1)];
+    float logu[kRing][kBatchMaxLevels];
+    uint32_t pb[kRing][2];
     float old_[kMaxWave][3 * (kMaxB + 1)], new_[kMaxWave][3 * (kMaxB + 1)];
     Comp part[kMaxWave][kBatchMaxWarps];
     dd base0[kMaxWave];
@@ -441,20 +496,38 @@ __device__ __forceinline__ bool Conflicts(uint32_t pi, uint32_t bi, uint32_t pj,
     return CircOverlap(si, B - 1, Wrap(bj + 1u, M), B - 1, M);
 }
 
+/// Pairs (i, j), i < j < kMaxWave, in the order k = j (j - 1) / 2 + i; PairJ(k) = j. Pairs of a
+/// smaller j come first, so the lowest conflicting pair names the first attempt that conflicts.
+constexpr uint32_t kPairsMax = kMaxWave * (kMaxWave - 1) / 2;
+static_assert(kMaxWave == 4, "PairJ covers the pairs of a window of four");
+__device__ __forceinline__ uint32_t PairJ(uint32_t k) { return 1u + (k >= 1u ? 1u : 0u) + (k >= 3u ? 1u : 0u); }
+
 __device__ __forceinline__ void SubSync(uint32_t id, uint32_t n_warps) {
     if (n_warps == 1) __syncwarp();
     else asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n_warps * 32u) : "memory");
 }
 
-template <bool kPbc>
-__device__ __forceinline__ void SweepChainW(WaveShared& sh, BatchArgs a, uint32_t ci, uint64_t n_sweeps, uint64_t n_attempts) {
+template <bool kPbc, bool kStaged>
+__device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchArgs a, uint32_t ci, uint64_t n_sweeps, uint64_t n_attempts) {
     const ChainDev& c = sh.c;
-    const uint32_t W = c.n_wave, Gs = c.sub_warps, G = W * Gs, R = 2 * W;
+    const uint32_t W = c.n_wave, Gs = c.sub_warps, G = W * Gs;
+    constexpr uint32_t kMask = kRing - 1;  // 2W <= kRing: the window and the next one never share a slot
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint32_t sg = warp / Gs, ws = warp - sg * Gs, Ts = Gs * 32u, ts = ws * 32u + lane;
+    // Warp w belongs to sub-group w mod W: the leaders (warps 0..W-1), whose phases are the
+    // serial part of a round, sit on different SM sub-partitions.
+    const uint32_t sg = warp % W, ws = warp / W, Ts = Gs * 32u, ts = ws * 32u + lane;
     const uint32_t N = c.n_part, M = c.n_bead, NL = c.n_level, B = 1u << NL, n_pad = c.n_pad;
     float4* __restrict__ pos = a.pos + c.pos_off;
     const uint32_t draw_warp = Gs >= 2 ? 1u : 0u;
+    const PathView<kStaged> path{pos, stage, n_pad, N, N * M};
+    if constexpr (kStaged)  // the path into shared memory (visible after the prologue's barrier)
+        for (uint32_t i = threadIdx.x; i < N * M; i += G * 32u) {
+            const uint32_t b = i / N, q = i - b * N;
+            const float4 v = pos[(size_t)b * n_pad + q];
+            stage[i] = v.x;
+            stage[N * M + i] = v.y;
+            stage[2 * N * M + i] = v.z;
+        }
 
     const uint32_t nm1 = N > 1 ? N - 1 : 1;
     const uint32_t n_items = c.has_pair && N > 1 ? (N - 1) * (B - 1) : 0u;
@@ -472,60 +545,78 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, BatchArgs a, uint32_
     if (threadIdx.x == 0) sh.accepts = 0;
     // Prologue: the first 2W attempts' draws, attempt A + x by sub-group x mod W.
     if (ws == draw_warp)
-        for (uint64_t x = A + sg; x < end && x < A + R; x += W)
-            DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, x}, lane, N, M, B, NL, n_pad, pos, sh.z[x % R], sh.logu[x % R], nullptr, sh.pb[x % R]);
+        for (uint64_t x = A + sg; x < end && x < A + 2 * W; x += W) {
+            const uint32_t sl = (uint32_t)x & kMask;
+            DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, x}, lane, N, M, B, NL, n_pad, pos, sh.z[sl], sh.logu[sl], nullptr, sh.pb[sl]);
+        }
     SubSync(15, G);
 
     while (A < end) {
+        // Attempt A + sg's beads, loaded before the round's prefix is known (the previous round's
+        // commits are visible after its closing barrier; unused if the prefix stops earlier).
+        const uint32_t a0 = (uint32_t)A & kMask;
+        const bool drawn = A + sg < end;
+        const uint32_t slot = (a0 + sg) & kMask;
+        const uint32_t p = drawn ? sh.pb[slot][0] : 0u, b0 = drawn ? sh.pb[slot][1] : 0u;
+        float3 pre[kItems];
+#pragma unroll
+        for (uint32_t j = 0; j < kItems; ++j)
+            if (drawn && ts + j * Ts < n_items) pre[j] = path.Load(Wrap(b0 + 1u + it_k[j], M), it_q[j] + (it_q[j] >= p ? 1u : 0u));
+        float3 sv = make_float3(0.f, 0.f, 0.f), se = sv;
+        if (drawn && ws == 0) {
+            sv = path.Load(Wrap(b0 + (lane <= B ? lane : B), M), p);
+            se = path.Load(Wrap(b0 + B, M), p);
+        }
         // The round's attempts: the longest conflict-free prefix of the next W (same on all lanes).
-        uint32_t w = 1;
-        for (uint32_t j = 1; j < W && A + j < end; ++j) {
-            const uint32_t* pj = sh.pb[(A + j) % R];
-            bool clear = true;
-            for (uint32_t i = 0; i < j && clear; ++i) {
-                const uint32_t* pi = sh.pb[(A + i) % R];
-                clear = !Conflicts(pi[0], pi[1], pj[0], pj[1], B, M);
+        // Lane k tests pair k = j (j - 1) / 2 + i (i < j < W) and one ballot collects them.
+        const uint32_t left = end - A < (uint64_t)W ? (uint32_t)(end - A) : W;
+        uint32_t w = left;
+        if (left > 1) {
+            bool hit = false;
+            if (lane < kPairsMax) {
+                const uint32_t j = PairJ(lane), i = lane - j * (j - 1) / 2;
+                if (j < left) {
+                    const uint32_t* pi = sh.pb[(a0 + i) & kMask];
+                    const uint32_t* pj = sh.pb[(a0 + j) & kMask];
+                    hit = Conflicts(pi[0], pi[1], pj[0], pj[1], B, M);
+                }
             }
-            if (!clear) break;
-            ++w;
+            const unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (m) w = PairJ((uint32_t)__ffs(m) - 1u);  // the first later attempt that conflicts ends the prefix
         }
         if (sg < w) {
-            const uint64_t x = A + sg;
-            const uint32_t slot = (uint32_t)(x % R);
-            const uint32_t p = sh.pb[slot][0], b0 = sh.pb[slot][1];
-            float4 pre[kItems];
-#pragma unroll
-            for (uint32_t j = 0; j < kItems; ++j)
-                if (ts + j * Ts < n_items) pre[j] = pos[(size_t)Wrap(b0 + 1u + it_k[j], M) * n_pad + it_q[j] + (it_q[j] >= p ? 1u : 0u)];
             float nx = 0.f, ny = 0.f, nz = 0.f;
-            if (ws == 0) {
-                const float4 sv = pos[(size_t)Wrap(b0 + (lane <= B ? lane : B), M) * n_pad + p];
-                const float4 se = pos[(size_t)Wrap(b0 + B, M) * n_pad + p];
-                LeaderPhase<kPbc>(c, lane, B, NL, M, sv.x, sv.y, sv.z, se.x, se.y, se.z, sh.z[slot], sh.logu[slot], sh.old_[sg], sh.new_[sg],
+            if (ws == 0)
+                LeaderPhase<kPbc>(c, lane, NL, M, sv.x, sv.y, sv.z, se.x, se.y, se.z, sh.z[slot], sh.logu[slot], sh.old_[sg], sh.new_[sg],
                                   &sh.base0[sg], &sh.upper_ok[sg], nx, ny, nz);
-            }
             // The draw that completes the next window: attempt A + W + sg (its slot is not in use).
             if (ws == draw_warp && A + W + sg < end) {
                 const uint64_t y = A + W + sg;
+                const uint32_t sl = (uint32_t)y & kMask;
                 if (draw_warp == 0) __syncwarp();
-                DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, y}, lane, N, M, B, NL, n_pad, pos, sh.z[y % R], sh.logu[y % R], nullptr, sh.pb[y % R]);
+                DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, y}, lane, N, M, B, NL, n_pad, pos, sh.z[sl], sh.logu[sl], nullptr, sh.pb[sl]);
             }
             SubSync(1 + sg, Gs);
             const bool upper_ok = sh.upper_ok[sg] != 0;
             if (upper_ok && n_items) {
-                const Comp u = CompWarpSum(PairPhase<kPbc>(c, ts, Ts, n_items, magic, nm1, p, b0, M, n_pad, pos, it_k, pre, sh.old_[sg], sh.new_[sg]), 32);
+                const Comp u = CompWarpSum(PairPhase<kPbc, kStaged>(c, ts, Ts, n_items, magic, nm1, p, b0, M, path, it_k, pre, sh.old_[sg], sh.new_[sg]), 32);
                 if (lane == 0) sh.part[sg][ws] = u;
             }
             SubSync(1 + sg, Gs);
             if (ws == 0) {
                 const bool accepted = upper_ok && Level0Accepts(c, lane, Gs, sh.part[sg], n_items != 0, sh.base0[sg], sh.logu[slot][0]);
-                if (accepted && lane >= 1 && lane < B) pos[(size_t)Wrap(b0 + lane, M) * n_pad + p] = make_float4(nx, ny, nz, 0.f);
+                if (accepted && lane >= 1 && lane < B) path.Store(Wrap(b0 + lane, M), p, nx, ny, nz);
                 if (accepted && lane == 0) atomicAdd(&sh.accepts, 1u);
             }
         }
         SubSync(15, G);
         A += w;
     }
+    if constexpr (kStaged)  // every round ended with a block barrier: all commits are visible
+        for (uint32_t i = threadIdx.x; i < N * M; i += G * 32u) {
+            const uint32_t b = i / N, q = i - b * N;
+            pos[(size_t)b * n_pad + q] = make_float4(stage[i], stage[N * M + i], stage[2 * N * M + i], 0.f);
+        }
     if (threadIdx.x == 0) {
         a.attempts[ci] = A;
         a.accepts[ci] += sh.accepts;
@@ -543,6 +634,7 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArg
     const uint32_t G = a.chains[ci].n_warps;
     if (warp >= G) return;
     __shared__ BatchShared sh;
+    extern __shared__ float4 batch_stage[];  // staged path planes (chains with `staged` set)
     {
         const uint32_t* src = reinterpret_cast<const uint32_t*>(a.chains + ci);
         uint32_t* dst = reinterpret_cast<uint32_t*>(&sh.one.c);
@@ -550,8 +642,14 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArg
     }
     GroupSync(G);
     if (sh.one.c.n_wave > 1) {
-        if (sh.one.c.pbc) SweepChainW<true>(sh.wave, a, ci, n_sweeps, n_attempts);
-        else SweepChainW<false>(sh.wave, a, ci, n_sweeps, n_attempts);
+        float* stage = reinterpret_cast<float*>(batch_stage);
+        if (sh.one.c.staged) {
+            if (sh.one.c.pbc) SweepChainW<true, true>(sh.wave, stage, a, ci, n_sweeps, n_attempts);
+            else SweepChainW<false, true>(sh.wave, stage, a, ci, n_sweeps, n_attempts);
+        } else {
+            if (sh.one.c.pbc) SweepChainW<true, false>(sh.wave, stage, a, ci, n_sweeps, n_attempts);
+            else SweepChainW<false, false>(sh.wave, stage, a, ci, n_sweeps, n_attempts);
+        }
     } else {
         if (sh.one.c.pbc) SweepChain<true>(sh.one, a, ci, G, n_sweeps, n_attempts);
         else SweepChain<false>(sh.one, a, ci, G, n_sweeps, n_attempts);
@@ -788,6 +886,14 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
     for (const auto& x : xml) specs.push_back(ParseChain(x, base_dir));  // input errors before any CUDA call
     CudaCheck(cudaSetDevice(device), "cudaSetDevice");
     CudaCheck(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, device), "device attribute");
+    {
+        // Shared memory left for a staged path next to the kernel's static shared memory.
+        int optin = 0;
+        cudaFuncAttributes fa{};
+        CudaCheck(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "device attribute");
+        CudaCheck(cudaFuncGetAttributes(&fa, BatchSweepKernel), "kernel attributes");
+        stage_cap = (size_t)optin > fa.sharedSizeBytes ? (size_t)optin - fa.sharedSizeBytes : 0;
+    }
     chains.resize(n_chains);
     uint64_t off = 0;
     for (uint32_t i = 0; i < n_chains; ++i) {
@@ -898,12 +1004,20 @@ void ChainBatch::SetTiles(uint32_t ipl, uint32_t mw, uint32_t wave) {
             c.n_wave = W;
             c.sub_warps = gs;
             c.n_warps = W * gs;
+            // The path in shared memory (three FP32 planes) when it fits next to the static part.
+            c.staged = (size_t)12 * c.n_part * c.n_bead <= stage_cap ? 1u : 0u;
         } else {
             c.n_wave = 1;
             c.n_warps = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(g, mw));
             c.sub_warps = c.n_warps;
+            c.staged = 0;
         }
     }
+    stage_bytes = 0;
+    for (const auto& c : chains)
+        if (c.staged) stage_bytes = std::max(stage_bytes, (size_t)12 * c.n_part * c.n_bead);
+    stage_bytes = (stage_bytes + 15) & ~size_t(15);
+    CudaCheck(cudaFuncSetAttribute(BatchSweepKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_bytes), "smem attribute");
     order.resize(n_chains);
     std::iota(order.begin(), order.end(), 0u);
     std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
@@ -996,7 +1110,7 @@ void ChainBatch::LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts) {
     uint32_t warps = 1;
     for (const auto& c : chains) warps = std::max(warps, c.n_warps);
     const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, series_cap);
-    BatchSweepKernel<<<n_chains, warps * 32, 0, stream>>>(a, n_sweeps, n_attempts);
+    BatchSweepKernel<<<n_chains, warps * 32, stage_bytes, stream>>>(a, n_sweeps, n_attempts);
     CudaCheck(cudaGetLastError(), "batch sweep launch");
     ++kernel_launches;
 }
