@@ -91,6 +91,45 @@ __device__ __forceinline__ float Img(float d, float L, float iL) {
     else return d;
 }
 
+// Paired FP32 arithmetic (sub/mul/fma.rn.f32x2): each half rounds as the scalar operation does,
+// so a pair of (old, new) terms costs one instruction and keeps the scalar results.
+__device__ __forceinline__ unsigned long long Pk2(float2 v) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(v.x), "f"(v.y));
+    return r;
+}
+__device__ __forceinline__ float2 Un2(unsigned long long r) {
+    float2 v;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(r));
+    return v;
+}
+__device__ __forceinline__ float2 Sub2(float2 a, float2 b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(Pk2(a)), "l"(Pk2(b)));
+    return Un2(r);
+}
+__device__ __forceinline__ float2 Mul2(float2 a, float2 b) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(Pk2(a)), "l"(Pk2(b)));
+    return Un2(r);
+}
+__device__ __forceinline__ float2 Fma2(float2 a, float2 b, float2 c) {
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(Pk2(a)), "l"(Pk2(b)), "l"(Pk2(c)));
+    return Un2(r);
+}
+/// Img on both halves: d - L rint(d / L) with the scalar version's roundings.
+template <bool kPbc>
+__device__ __forceinline__ float2 Img2(float2 d, float L, float iL) {
+    if constexpr (kPbc) {
+        const float2 t = Mul2(d, make_float2(iL, iL));
+        return Sub2(d, Mul2(make_float2(L, L), make_float2(rintf(t.x), rintf(t.y))));
+    } else {
+        return d;
+    }
+}
+__device__ __forceinline__ float2 Sq3x2(float2 x, float2 y, float2 z) { return Fma2(x, x, Fma2(y, y, Mul2(z, z))); }
+
 constexpr uint32_t kItems = 4;  // pair items per lane kept in registers (more are loaded in the loop)
 
 /// A chain's beads during a sweep: the global float4 block [M][n_pad] (slice-major, x y z 0), or,
@@ -159,7 +198,7 @@ __device__ __forceinline__ void DrawAttempt(const MoveStream& st, uint32_t lane,
 /// deciding level l. Returns with the new bead in n*.
 template <bool kPbc, uint32_t NL>
 __device__ __forceinline__ void LeaderPhaseL(const ChainDev& c, uint32_t lane, uint32_t M, float ox, float oy, float oz, float ex, float ey,
-                                             float ez, const float* zb, const float* logu, float* s_old, float* s_new, dd* base0_out,
+                                             float ez, const float* zb, const float* logu, float2* s_on, dd* base0_out,
                                              int* upper_out, float& nx, float& ny, float& nz) {
     constexpr uint32_t B = 1u << NL;
     const float L = c.L, iL = c.iL;
@@ -201,17 +240,14 @@ __device__ __forceinline__ void LeaderPhaseL(const ChainDev& c, uint32_t lane, u
     const float dn2 = inner ? Sq3(gx, gy, gz) : 0.f;
     // Segment copies for the pair work and for the links below (bead 32 of a 32-bead segment is e).
     if (lane <= B) {
-        s_old[3 * lane] = ox;
-        s_old[3 * lane + 1] = oy;
-        s_old[3 * lane + 2] = oz;
-        s_new[3 * lane] = nx;
-        s_new[3 * lane + 1] = ny;
-        s_new[3 * lane + 2] = nz;
+        s_on[3 * lane] = make_float2(ox, nx);
+        s_on[3 * lane + 1] = make_float2(oy, ny);
+        s_on[3 * lane + 2] = make_float2(oz, nz);
     }
     if (B == 32 && lane == 0) {
-        s_old[96] = s_new[96] = ex;
-        s_old[97] = s_new[97] = ey;
-        s_old[98] = s_new[98] = ez;
+        s_on[96] = make_float2(ex, ex);
+        s_on[97] = make_float2(ey, ey);
+        s_on[98] = make_float2(ez, ez);
     }
     // Old sampling displacement of bead `lane` on its level.
     float samp = 0.f;
@@ -241,20 +277,20 @@ __device__ __forceinline__ void LeaderPhaseL(const ChainDev& c, uint32_t lane, u
     // for  D_l = sum of action changes  and  R_l = sampling ratio - D_l.
     Comp Dl[NL + 1], Rl[NL];
     Dl[NL] = Comp{0.f, 0.f};
+    const float2 t2 = Sq3x2(make_float2(ox, nx), make_float2(oy, ny), make_float2(oz, nz));  // |r|^2 old, new
 #pragma unroll
     for (uint32_t li = 0; li < NL; ++li) {
         float dterm = 0.f;
         const uint32_t skip = 1u << li;
         if (lane < B && (lane & (skip - 1u)) == 0u) {
-            const float* cn = s_new + 3 * (lane + skip);
-            const float* co = s_old + 3 * (lane + skip);
+            const float2* cf = s_on + 3 * (lane + skip);  // far bead of the link, (old, new)
             if (kin_links) {
-                const float kn = Sq3(Img<kPbc>(__fsub_rn(nx, cn[0]), L, iL), Img<kPbc>(__fsub_rn(ny, cn[1]), L, iL), Img<kPbc>(__fsub_rn(nz, cn[2]), L, iL));
-                const float ko = Sq3(Img<kPbc>(__fsub_rn(ox, co[0]), L, iL), Img<kPbc>(__fsub_rn(oy, co[1]), L, iL), Img<kPbc>(__fsub_rn(oz, co[2]), L, iL));
-                dterm = __fmul_rn(c.i4lt_level[li], __fsub_rn(kn, ko));
+                const float2 k2 = Sq3x2(Img2<kPbc>(Sub2(make_float2(ox, nx), cf[0]), L, iL), Img2<kPbc>(Sub2(make_float2(oy, ny), cf[1]), L, iL),
+                                        Img2<kPbc>(Sub2(make_float2(oz, nz), cf[2]), L, iL));
+                dterm = __fmul_rn(c.i4lt_level[li], __fsub_rn(k2.y, k2.x));
             }
             if (c.has_trap && (int)li <= c.trap_max_level)
-                dterm = __fadd_rn(dterm, __fmul_rn(__fmul_rn(c.trap_cofa, (float)skip), __fsub_rn(Sq3(nx, ny, nz), Sq3(ox, oy, oz))));
+                dterm = __fadd_rn(dterm, __fmul_rn(__fmul_rn(c.trap_cofa, (float)skip), __fsub_rn(t2.y, t2.x)));
         }
         Dl[li] = Comp{dterm, 0.f};
         Rl[li] = Comp{__fsub_rn(inner && lk == li ? samp : 0.f, dterm), 0.f};
@@ -293,14 +329,14 @@ __device__ __forceinline__ void LeaderPhaseL(const ChainDev& c, uint32_t lane, u
 
 template <bool kPbc>
 __device__ __forceinline__ void LeaderPhase(const ChainDev& c, uint32_t lane, uint32_t NL, uint32_t M, float ox, float oy, float oz, float ex,
-                                            float ey, float ez, const float* zb, const float* logu, float* s_old, float* s_new, dd* base0_out,
+                                            float ey, float ez, const float* zb, const float* logu, float2* s_on, dd* base0_out,
                                             int* upper_out, float& nx, float& ny, float& nz) {
     switch (NL) {
-        case 1: LeaderPhaseL<kPbc, 1>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_old, s_new, base0_out, upper_out, nx, ny, nz); break;
-        case 2: LeaderPhaseL<kPbc, 2>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_old, s_new, base0_out, upper_out, nx, ny, nz); break;
-        case 3: LeaderPhaseL<kPbc, 3>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_old, s_new, base0_out, upper_out, nx, ny, nz); break;
-        case 4: LeaderPhaseL<kPbc, 4>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_old, s_new, base0_out, upper_out, nx, ny, nz); break;
-        default: LeaderPhaseL<kPbc, 5>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_old, s_new, base0_out, upper_out, nx, ny, nz); break;
+        case 1: LeaderPhaseL<kPbc, 1>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_on, base0_out, upper_out, nx, ny, nz); break;
+        case 2: LeaderPhaseL<kPbc, 2>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_on, base0_out, upper_out, nx, ny, nz); break;
+        case 3: LeaderPhaseL<kPbc, 3>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_on, base0_out, upper_out, nx, ny, nz); break;
+        case 4: LeaderPhaseL<kPbc, 4>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_on, base0_out, upper_out, nx, ny, nz); break;
+        default: LeaderPhaseL<kPbc, 5>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_on, base0_out, upper_out, nx, ny, nz); break;
     }
 }
 
@@ -311,24 +347,31 @@ __device__ __forceinline__ void LeaderPhase(const ChainDev& c, uint32_t lane, ui
 template <bool kPbc, bool kStaged>
 __device__ __forceinline__ Comp PairPhase(const ChainDev& c, uint32_t t, uint32_t T, uint32_t n_items, uint32_t magic, uint32_t nm1, uint32_t p,
                                           uint32_t b0, uint32_t M, const PathView<kStaged>& path, const uint32_t* it_k, const float3* pre,
-                                          const float* s_old, const float* s_new) {
+                                          const float2* s_on) {
     const float L = c.L, iL = c.iL, r2_min = c.r2_min, r2_max = c.r2_max;
     Comp acc_u{0.f, 0.f};
     auto item = [&](uint32_t k, float3 rq) {
-        const float* ro = s_old + 3 * (k + 1);
-        const float* rn = s_new + 3 * (k + 1);
-        float r2o = Sq3(Img<kPbc>(__fsub_rn(ro[0], rq.x), L, iL), Img<kPbc>(__fsub_rn(ro[1], rq.y), L, iL), Img<kPbc>(__fsub_rn(ro[2], rq.z), L, iL));
-        float r2n = Sq3(Img<kPbc>(__fsub_rn(rn[0], rq.x), L, iL), Img<kPbc>(__fsub_rn(rn[1], rq.y), L, iL), Img<kPbc>(__fsub_rn(rn[2], rq.z), L, iL));
-        r2o = fminf(fmaxf(r2o, r2_min), r2_max);
-        r2n = fminf(fmaxf(r2n, r2_min), r2_max);
+        const float2* on = s_on + 3 * (k + 1);  // inner bead k + 1, (old, new)
+        const float2 r2 = Sq3x2(Img2<kPbc>(Sub2(on[0], make_float2(rq.x, rq.x)), L, iL), Img2<kPbc>(Sub2(on[1], make_float2(rq.y, rq.y)), L, iL),
+                                Img2<kPbc>(Sub2(on[2], make_float2(rq.z, rq.z)), L, iL));
+        const float r2o = fminf(fmaxf(r2.x, r2_min), r2_max);
+        const float r2n = fminf(fmaxf(r2.y, r2_min), r2_max);
         CompAdd(acc_u, __fsub_rn(rsqrtf(r2n), rsqrtf(r2o)));
     };
+    if constexpr (kStaged) {  // beads in shared memory: no prefetch, loads batched by the unrolled loop
+#pragma unroll 4
+        for (uint32_t i = t; i < n_items; i += T) {
+            const uint32_t k = FastDiv(i, magic), qq = i - k * nm1;
+            item(k, path.Load(Wrap(b0 + 1u + k, M), qq + (qq >= p ? 1u : 0u)));
+        }
+    } else {
 #pragma unroll
-    for (uint32_t j = 0; j < kItems; ++j)
-        if (t + j * T < n_items) item(it_k[j], pre[j]);
-    for (uint32_t i = t + kItems * T; i < n_items; i += T) {
-        const uint32_t k = FastDiv(i, magic), qq = i - k * nm1;
-        item(k, path.Load(Wrap(b0 + 1u + k, M), qq + (qq >= p ? 1u : 0u)));
+        for (uint32_t j = 0; j < kItems; ++j)
+            if (t + j * T < n_items) item(it_k[j], pre[j]);
+        for (uint32_t i = t + kItems * T; i < n_items; i += T) {
+            const uint32_t k = FastDiv(i, magic), qq = i - k * nm1;
+            item(k, path.Load(Wrap(b0 + 1u + k, M), qq + (qq >= p ? 1u : 0u)));
+        }
     }
     return acc_u;
 }
@@ -355,7 +398,7 @@ struct SweepShared {
     float logu[2][kBatchMaxLevels];
     float4 seg[2][kMaxB + 1];
     uint32_t pb[2][2];
-    float old_[3 * (kMaxB + 1)], new_[3 * (kMaxB + 1)];
+    float2 on_[3 * (kMaxB + 1)];  // the attempt's segment, (old, new) per coordinate
     Comp part[kBatchMaxWarps];
     dd base0;  // level-0 log acceptance without the pair term
     int upper_ok;
@@ -431,7 +474,7 @@ __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_
                     ez = qz;
                 }
             }
-            LeaderPhase<kPbc>(c, lane, NL, M, ox, oy, oz, ex, ey, ez, sh.z[buf], sh.logu[buf], sh.old_, sh.new_, &sh.base0, &sh.upper_ok,
+            LeaderPhase<kPbc>(c, lane, NL, M, ox, oy, oz, ex, ey, ez, sh.z[buf], sh.logu[buf], sh.on_, &sh.base0, &sh.upper_ok,
                               nx, ny, nz);
         } else if (ahead && warp == 1 && it + 1 < n_att) {
             DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, att + 1}, lane, N, M, B, NL, n_pad, pos, sh.z[buf ^ 1u], sh.logu[buf ^ 1u],
@@ -441,7 +484,7 @@ __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_
         const bool upper_ok = sh.upper_ok != 0;
 
         if (upper_ok && n_items) {
-            const Comp u = CompWarpSum(PairPhase<kPbc, false>(c, t, T, n_items, magic, nm1, p, b0, M, gpath, it_k, pre, sh.old_, sh.new_), 32);
+            const Comp u = CompWarpSum(PairPhase<kPbc, false>(c, t, T, n_items, magic, nm1, p, b0, M, gpath, it_k, pre, sh.on_), 32);
             if (lane == 0) sh.part[warp] = u;
         }
         GroupSync(G);
@@ -478,7 +521,7 @@ struct WaveShared {
     float z[kRing][3 * (kMaxB - 1)];
     float logu[kRing][kBatchMaxLevels];
     uint32_t pb[kRing][2];
-    float old_[kMaxWave][3 * (kMaxB + 1)], new_[kMaxWave][3 * (kMaxB + 1)];
+    float2 on_[kMaxWave][3 * (kMaxB + 1)];
     Comp part[kMaxWave][kBatchMaxWarps];
     dd base0[kMaxWave];
     int upper_ok[kMaxWave];
@@ -559,9 +602,11 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
         const uint32_t slot = (a0 + sg) & kMask;
         const uint32_t p = drawn ? sh.pb[slot][0] : 0u, b0 = drawn ? sh.pb[slot][1] : 0u;
         float3 pre[kItems];
+        if constexpr (!kStaged) {  // global beads: the first items' partners in flight during the leader
 #pragma unroll
-        for (uint32_t j = 0; j < kItems; ++j)
-            if (drawn && ts + j * Ts < n_items) pre[j] = path.Load(Wrap(b0 + 1u + it_k[j], M), it_q[j] + (it_q[j] >= p ? 1u : 0u));
+            for (uint32_t j = 0; j < kItems; ++j)
+                if (drawn && ts + j * Ts < n_items) pre[j] = path.Load(Wrap(b0 + 1u + it_k[j], M), it_q[j] + (it_q[j] >= p ? 1u : 0u));
+        }
         float3 sv = make_float3(0.f, 0.f, 0.f), se = sv;
         if (drawn && ws == 0) {
             sv = path.Load(Wrap(b0 + (lane <= B ? lane : B), M), p);
@@ -587,7 +632,7 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
         if (sg < w) {
             float nx = 0.f, ny = 0.f, nz = 0.f;
             if (ws == 0)
-                LeaderPhase<kPbc>(c, lane, NL, M, sv.x, sv.y, sv.z, se.x, se.y, se.z, sh.z[slot], sh.logu[slot], sh.old_[sg], sh.new_[sg],
+                LeaderPhase<kPbc>(c, lane, NL, M, sv.x, sv.y, sv.z, se.x, se.y, se.z, sh.z[slot], sh.logu[slot], sh.on_[sg],
                                   &sh.base0[sg], &sh.upper_ok[sg], nx, ny, nz);
             // The draw that completes the next window: attempt A + W + sg (its slot is not in use).
             if (ws == draw_warp && A + W + sg < end) {
@@ -599,7 +644,7 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
             SubSync(1 + sg, Gs);
             const bool upper_ok = sh.upper_ok[sg] != 0;
             if (upper_ok && n_items) {
-                const Comp u = CompWarpSum(PairPhase<kPbc, kStaged>(c, ts, Ts, n_items, magic, nm1, p, b0, M, path, it_k, pre, sh.old_[sg], sh.new_[sg]), 32);
+                const Comp u = CompWarpSum(PairPhase<kPbc, kStaged>(c, ts, Ts, n_items, magic, nm1, p, b0, M, path, it_k, pre, sh.on_[sg]), 32);
                 if (lane == 0) sh.part[sg][ws] = u;
             }
             SubSync(1 + sg, Gs);
