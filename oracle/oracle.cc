@@ -210,6 +210,59 @@ struct Spline {
         v = A * y[i] + B * y[i + 1] + ((A * A * A - A) * m[i] + (B * B * B - B) * m[i + 1]) * h * h / 6.;
         g = (y[i + 1] - y[i]) / h + (-(3. * A * A - 1.) * m[i] + (3. * B * B - 1.) * m[i + 1]) * h / 6.;
     }
+
+    // Value and slope without clamping the argument: outside the knots the edge interval's cubic
+    // continues.
+    void EvalExtVG(double t, double& v, double& g) const {
+        size_t n = x.size();
+        size_t i = (size_t)(std::upper_bound(x.begin(), x.end(), t) - x.begin());
+        i = i == 0 ? 0 : i - 1;
+        if (i > n - 2) i = n - 2;
+        double h = x[i + 1] - x[i];
+        double A = (x[i + 1] - t) / h, B = 1. - A;
+        v = A * y[i] + B * y[i + 1] + ((A * A * A - A) * m[i] + (B * B * B - B) * m[i + 1]) * h * h / 6.;
+        g = (y[i + 1] - y[i]) / h + (-(3. * A * A - 1.) * m[i] + (3. * B * B - 1.) * m[i + 1]) * h / 6.;
+    }
+};
+
+// 2-D natural spline on a rectilinear grid: the tensor product of natural cubic splines that
+// einspline's NUBspline_2d_d with {NATURAL, NATURAL} conditions represents. It is evaluated by its
+// definition as a product of 1-D interpolations: a natural spline along x within every grid row
+// y_j, then a natural spline along y through those row values (and through their x slopes for
+// df/dx). Outside the grid each 1-D spline continues its edge interval's cubic.
+struct Spline2 {
+    std::vector<double> y;
+    std::vector<Spline> rows;  // rows[j]: the spline in x of f(., y_j)
+
+    void Build(const std::vector<double>& xs, const std::vector<double>& ys, const std::vector<double>& f) {
+        size_t nx = xs.size(), ny = ys.size();
+        if (nx < 2 || ny < 2 || f.size() != nx * ny) throw InputError("2-D spline: inconsistent grid and values");
+        y = ys;
+        rows.assign(ny, Spline());
+        std::vector<double> col(nx);
+        for (size_t j = 0; j < ny; ++j) {
+            for (size_t i = 0; i < nx; ++i) col[i] = f[i * ny + j];  // value (i, j) at i n_y + j
+            rows[j].Build(xs, col, false);
+        }
+    }
+
+    void EvalVG(double xx, double yy, double& f, double& fx, double& fy) const {
+        size_t ny = y.size();
+        std::vector<double> v(ny), dv(ny);
+        for (size_t j = 0; j < ny; ++j) rows[j].EvalExtVG(xx, v[j], dv[j]);
+        Spline sv, sd;
+        sv.Build(y, v, false);
+        sd.Build(y, dv, false);
+        double unused;
+        sv.EvalExtVG(yy, f, fy);
+        sd.EvalExtVG(yy, fx, unused);
+    }
+
+    double Eval(double xx, double yy) const {
+        double f, fx, fy;
+        EvalVG(xx, yy, f, fx, fy);
+        return f;
+    }
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -794,7 +847,7 @@ struct PairAction : Action {
     }
 
     // pair_action_class.h:135-155 (central differences, eps = 1e-4)
-    void CalcGradientU(uint32_t bi, uint32_t bj, uint32_t pi, uint32_t pj, uint32_t level, double* tot) {
+    virtual void CalcGradientU(uint32_t bi, uint32_t bj, uint32_t pi, uint32_t pj, uint32_t level, double* tot) {
         double* rr = path.GetR(*species_a, pi, bi);
         double r0[3];
         for (uint32_t d = 0; d < path.n_d; ++d) r0[d] = rr[d];
@@ -1014,6 +1067,201 @@ struct BarePairAction : PairAction {
     double CalcdUdBetaLong() override { return CalcVLong(); }
 };
 
+// src/actions/pair_action/ilkka_pair_action_class.h:7-433
+struct IlkkaPairAction : PairAction {
+    double r_u_min = 0., r_u_max = 0., r_du_min = 0., r_du_max = 0., r_v_min = 0., r_v_max = 0.;
+    double r_v_long_min = 0., r_v_long_max = 0.;
+    double du_long_k_0 = 0., du_long_r_0 = 0., v_long_k_0 = 0., v_long_r_0 = 0.;
+    std::vector<double> u_long_k, du_long_k, v_long_k;
+    Spline u_long_r_spline, du_long_r_spline, v_r_spline, v_long_r_spline;
+    Spline2 u_xy_spline, du_xy_spline;
+
+    // The k-space datasets hold one value per distinct |k|; each stored k-vector takes the value
+    // of its magnitude (ilkka_pair_action_class.h:308-315).
+    static std::vector<double> ByMagnitude(const Path& p, const std::vector<double>& kv, const std::vector<double>& vals) {
+        std::vector<double> out(p.ks.K(), 0.);
+        for (size_t k = 0; k < p.ks.K(); ++k)
+            for (size_t j = 0; j < kv.size(); ++j)
+                if (fequal(p.ks.mags[k], kv[j], 1.e-8)) out[k] = vals[j];
+        return out;
+    }
+
+    IlkkaPairAction(Path& p, const Input& in, const std::string& base_dir) : PairAction(p, in) {
+        std::string file = in.GetAttribute<std::string>("file");
+        if (!file.empty() && file[0] != '/' && !base_dir.empty()) file = base_dir + "/" + file;
+        TableFile t = TableFile::Load(file);
+        auto grid2 = [&](const std::string& g, const std::string& f, Spline2& sp) {
+            const auto& x = t.Vec(g + "/off_diag/x");
+            const auto& y = t.Vec(g + "/off_diag/y");
+            if ((size_t)t.Scalar(g + "/off_diag/n_x") != x.size() || (size_t)t.Scalar(g + "/off_diag/n_y") != y.size())
+                throw InputError("table '" + file + "': inconsistent " + g + "/off_diag grid");
+            sp.Build(x, y, t.Vec(g + "/off_diag/" + f));
+        };
+        grid2("u", "u_xy", u_xy_spline);  // :266-280
+        if (use_long_range) {             // :282-316
+            const auto& r = t.Vec("u/diag/r_long");
+            u_long_r_spline.Build(r, t.Vec("u/diag/u_long_r"), false);
+            r_u_min = r.front();
+            r_u_max = r.back();
+            u_long_k = ByMagnitude(p, t.Vec("u/diag/k"), t.Vec("u/diag/u_long_k"));
+        }
+        grid2("du", "du_xy", du_xy_spline);  // :318-332
+        if (use_long_range) {                // :334-368
+            const auto& r = t.Vec("du/diag/r_long");
+            du_long_r_spline.Build(r, t.Vec("du/diag/du_long_r"), false);
+            du_long_r_0 = t.Scalar("du/diag/du_long_r_0");
+            r_du_min = r.front();
+            r_du_max = r.back();
+            du_long_k = ByMagnitude(p, t.Vec("du/diag/k"), t.Vec("du/diag/du_long_k"));
+            du_long_k_0 = t.Scalar("du/diag/du_long_k_0");
+        }
+        {  // :370-382
+            const auto& r = t.Vec("v/diag/r");
+            v_r_spline.Build(r, t.Vec("v/diag/v_r"), false);
+            r_v_min = r.front();
+            r_v_max = r.back();
+        }
+        if (use_long_range) {  // :384-418
+            const auto& r = t.Vec("v/diag/r_long");
+            v_long_r_spline.Build(r, t.Vec("v/diag/v_long_r"), false);
+            v_long_r_0 = t.Scalar("v/diag/v_long_r_0");
+            r_v_long_min = r.front();
+            r_v_long_max = r.back();
+            v_long_k = ByMagnitude(p, t.Vec("v/diag/k"), t.Vec("v/diag/v_long_k"));
+            v_long_k_0 = t.Scalar("v/diag/v_long_k_0");
+        }
+        if (species_a == species_b) {  // :420-431
+            du_long_k_0 *= 0.5 * species_a->n_part * species_b->n_part * p.n_bead;
+            du_long_r_0 *= -0.5 * species_a->n_part * p.n_bead;
+            v_long_k_0 *= 0.5 * species_a->n_part * species_b->n_part * p.n_bead;
+            v_long_r_0 *= -0.5 * species_a->n_part * p.n_bead;
+        } else {
+            du_long_k_0 *= species_a->n_part * species_b->n_part * p.n_bead;
+            du_long_r_0 *= 0.;
+            v_long_k_0 *= species_a->n_part * species_b->n_part * p.n_bead;
+            v_long_r_0 *= 0.;
+        }
+    }
+
+    // Sum over stored k of coef_k Re(rho_a conj rho_b) over slices [b0, b1) at stride skip, x2 for
+    // two species (:104-122, :151-169).
+    double KSum(const std::vector<double>& coef, uint32_t b0, uint32_t b1, uint32_t skip) {
+        const auto& ra = path.GetRhoK(*species_a);
+        const auto& rb = path.GetRhoK(*species_b);
+        size_t K = path.ks.K();
+        double tot = 0.;
+        for (size_t k = 0; k < K; ++k)
+            for (uint32_t b = b0; b < b1; b += skip)
+                tot += coef[k] * CMag2(ra[(size_t)species_a->bead_loop(b) * K + k], rb[(size_t)species_b->bead_loop(b) * K + k]);
+        if (species_a != species_b) tot *= 2.;
+        return tot;
+    }
+
+    double CalcV(double r, double rp, uint32_t) override {  // :34-54
+        SetLimits(r_v_min, r_v_max, r, rp);
+        double v = 0.5 * v_r_spline.Eval(r) + 0.5 * v_r_spline.Eval(rp);
+        if (use_long_range) {
+            SetLimits(r_v_long_min, r_v_long_max, r, rp);
+            v -= 0.5 * v_long_r_spline.Eval(r);
+            v -= 0.5 * v_long_r_spline.Eval(rp);
+        }
+        return v;
+    }
+    double CalcVLong() override {  // :57-74 (summed in k-major order as the reference's loop)
+        const auto& ra = path.GetRhoK(*species_a);
+        const auto& rb = path.GetRhoK(*species_b);
+        size_t K = path.ks.K();
+        double tot = 0.;
+        for (size_t k = 0; k < K; ++k)
+            for (uint32_t b = 0; b < path.n_bead; ++b) tot += v_long_k[k] * CMag2(ra[(size_t)b * K + k], rb[(size_t)b * K + k]);
+        if (species_a != species_b) tot *= 2.;
+        return tot + v_long_k_0 + v_long_r_0;
+    }
+    double CalcU(double r, double rp, double s, uint32_t) override {  // :77-101
+        double q = 0.5 * (r + rp);
+        double u = u_xy_spline.Eval(q + 0.5 * s, q - 0.5 * s);
+        if (use_long_range) {
+            SetLimits(r_u_min, r_u_max, r, rp);
+            u -= 0.5 * u_long_r_spline.Eval(r);
+            u -= 0.5 * u_long_r_spline.Eval(rp);
+        }
+        return u;
+    }
+    double CalcULong(uint32_t b0, uint32_t b1, uint32_t level) override { return KSum(u_long_k, b0, b1, 1u << level); }  // :104-122
+    double CalcdUdBeta(double r, double rp, double s, uint32_t) override {  // :125-149
+        double q = 0.5 * (r + rp);
+        double du = du_xy_spline.Eval(q + 0.5 * s, q - 0.5 * s);
+        if (use_long_range) {
+            SetLimits(r_du_min, r_du_max, r, rp);
+            du -= 0.5 * du_long_r_spline.Eval(r);
+            du -= 0.5 * du_long_r_spline.Eval(rp);
+        }
+        return du;
+    }
+    double CalcdUdBetaLong() override { return KSum(du_long_k, 0, path.n_bead, 1) + du_long_k_0 + du_long_r_0; }  // :152-169
+
+    // :172-222, the chain rule through (x, y); r is the vector of DrDrpDrrp (second minus first particle).
+    void CalcGradientU(uint32_t bi, uint32_t bj, uint32_t pi, uint32_t pj, uint32_t, double* tot) override {
+        const uint32_t nd = path.n_d;
+        double rv[3], rp[3], rrp[3];
+        const double* a0 = path.GetR(*species_b, pj, bi);
+        const double* c0 = path.GetR(*species_a, pi, bi);
+        const double* a1 = path.GetR(*species_b, pj, bj);
+        const double* c1 = path.GetR(*species_a, pi, bj);
+        for (uint32_t d = 0; d < nd; ++d) {
+            rv[d] = a0[d] - c0[d];
+            rp[d] = a1[d] - c1[d];
+        }
+        for (uint32_t d = 0; d < nd; ++d) {
+            rv[d] -= std::nearbyint(rv[d] * path.iL) * path.L;
+            rp[d] += std::nearbyint((rv[d] - rp[d]) * path.iL) * path.L;
+        }
+        for (uint32_t d = 0; d < nd; ++d) rrp[d] = rv[d] - rp[d];
+        for (uint32_t d = 0; d < nd; ++d) rrp[d] -= std::nearbyint(rrp[d] * path.iL) * path.L;
+        double a = 0., b = 0., c = 0.;
+        for (uint32_t d = 0; d < nd; ++d) {
+            a += rv[d] * rv[d];
+            b += rp[d] * rp[d];
+            c += rrp[d] * rrp[d];
+        }
+        double r_mag = std::sqrt(a), r_p_mag = std::sqrt(b), s_mag = std::sqrt(c);
+        double q = 0.5 * (r_mag + r_p_mag);
+        double u, du_dx, du_dy;
+        u_xy_spline.EvalVG(q + 0.5 * s_mag, q - 0.5 * s_mag, u, du_dx, du_dy);
+        double rh[3], sh[3];
+        for (uint32_t d = 0; d < nd; ++d) {
+            rh[d] = r_mag == 0. ? 0. : rv[d] / r_mag;
+            sh[d] = s_mag == 0. ? 0. : rrp[d] / s_mag;
+        }
+        for (uint32_t d = 0; d < nd; ++d) tot[d] = -0.5 * (du_dx * (rh[d] + sh[d]) + du_dy * (rh[d] - sh[d]));
+        if (use_long_range) {
+            SetLimits(r_u_min, r_u_max, r_mag, r_p_mag);
+            double tu, tdu;
+            u_long_r_spline.EvalVG(r_mag, tu, tdu);
+            for (uint32_t d = 0; d < nd; ++d) tot[d] -= 0.5 * tdu * rh[d];
+        }
+    }
+
+    // :231-249: per-bead densities of p_i (current mode) against species b's slice densities.
+    void CalcGradientULong(uint32_t b0, uint32_t b1, uint32_t pi, uint32_t level, double* g) override {
+        const auto& rb = path.GetRhoK(*species_b);
+        size_t K = path.ks.K();
+        uint32_t skip = 1u << level;
+        double tot[3] = {0., 0., 0.};
+        for (uint32_t b = b0; b < b1; b += skip) {
+            const cplx* ri = path.BeadRhoK(*species_a, pi, b, path.mode);
+            for (size_t k = 0; k < K; ++k) {
+                const cplx& rbk = rb[(size_t)species_b->bead_loop(b) * K + k];
+                double f = u_long_k[k] * (ri[k].real() * rbk.imag() - ri[k].imag() * rbk.real());
+                for (uint32_t d = 0; d < path.n_d; ++d) tot[d] += f * path.ks.vecs[k][d];
+            }
+        }
+        if (species_a != species_b)
+            for (uint32_t d = 0; d < path.n_d; ++d) tot[d] *= 2.;
+        for (uint32_t d = 0; d < path.n_d; ++d) g[d] = tot[d];
+    }
+};
+
 // ---------------------------------------------------------------------------------------------
 // Moves: Bisect (src/events/moves/single_species_move/bisect/bisect_class.h:8-214).
 // ---------------------------------------------------------------------------------------------
@@ -1120,6 +1368,8 @@ static double WholeAction(Path& path, std::vector<std::unique_ptr<Action>>& acti
                     for (uint32_t c = 0; c < nd; ++c) r2 += r[c] * r[c];
                     total += t->cofactor_a * r2;
                 }
+        } else if (dynamic_cast<IlkkaPairAction*>(a)) {
+            throw InputError("the whole-ring action covers Kinetic, HarmonicTrap and BarePairAction");
         } else if (auto* bp = dynamic_cast<BarePairAction*>(a)) {
             if (bp->is_constant) continue;
             for (auto& pr : bp->AllPairs()) {
@@ -1179,6 +1429,8 @@ static void WholeGradient(Path& path, std::vector<std::unique_ptr<Action>>& acti
                     const double* r = RAt(path, R, s.offset + p, b);
                     for (uint32_t c = 0; c < nd; ++c) gat(s.offset + p, b)[c] += 2. * t->cofactor_a * r[c];
                 }
+        } else if (dynamic_cast<IlkkaPairAction*>(a)) {
+            throw InputError("the whole-ring gradient covers Kinetic, HarmonicTrap and BarePairAction");
         } else if (auto* bp = dynamic_cast<BarePairAction*>(a)) {
             if (bp->is_constant) continue;
             for (auto& pr : bp->AllPairs()) {
@@ -1756,6 +2008,7 @@ struct Simulation {
             if (t == "Kinetic") actions.emplace_back(new Kinetic(*path, a));
             else if (t == "HarmonicTrap") actions.emplace_back(new Trap(*path, a));
             else if (t == "BarePairAction") actions.emplace_back(new BarePairAction(*path, a, base_dir));
+            else if (t == "IlkkaPairAction") actions.emplace_back(new IlkkaPairAction(*path, a, base_dir));
             else throw InputError("unsupported action type '" + t + "'");
         }
         uint32_t mi = 0;
@@ -1782,6 +2035,10 @@ struct Simulation {
             if (a->type == "BarePairAction") {
                 auto* b = static_cast<BarePairAction*>(a.get());
                 if (b->use_long_range && b->v_long_k.size() != path->ks.K())
+                    throw InputError("k_cut of action '" + b->name + "' is below a later k_cut; order the largest first");
+            } else if (a->type == "IlkkaPairAction") {
+                auto* b = static_cast<IlkkaPairAction*>(a.get());
+                if (b->use_long_range && b->u_long_k.size() != path->ks.K())
                     throw InputError("k_cut of action '" + b->name + "' is below a later k_cut; order the largest first");
             }
         for (auto& o : observables)

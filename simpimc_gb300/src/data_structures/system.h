@@ -65,6 +65,25 @@ struct CubicTable {
     double inv_dx = 0.;              // uniform: 1/spacing; general: buckets per unit length
 };
 
+/// Knots of one axis of a 2-D table: uniform grids locate the cell arithmetically, general grids
+/// through a bucket table followed by a short forward scan (as CubicTable).
+struct GridDev {
+    const double* x = nullptr;
+    const int32_t* bucket = nullptr;
+    int32_t n = 0, n_bucket = 0, uniform = 0;
+    double x0 = 0., x1 = 0., inv_dx = 0.;
+};
+
+/// Natural bicubic interpolating spline on a rectilinear grid: the tensor product of natural cubic
+/// splines, which is what einspline's NUBspline_2d_d with {NATURAL, NATURAL} conditions represents
+/// (ilkka_pair_action_class.h:264-280). Stored as one bicubic polynomial per cell,
+/// f = sum_{a,b} c[16 cell + 4a + b] u^a v^b with u = x - x_i, v = y - y_j, cell = i (n_y - 1) + j.
+/// Outside the grid the edge cell's polynomial continues (the arguments are not clamped).
+struct BicubicTable {
+    GridDev gx, gy;
+    const double* c = nullptr;
+};
+
 /// Kinetic action of one species (src/actions/single_action/kinetic_class.h:10-169).
 struct KineticDev {
     uint32_t species = 0;
@@ -84,15 +103,28 @@ struct TrapDev {
     double cofactor_a = 0., cofactor_b = 0.;
 };
 
-/// Bare (primitive) pair action (src/actions/pair_action/bare_pair_action_class.h:7-183).
+constexpr int32_t kPairBare = 0;   // BarePairAction (bare_pair_action_class.h:7-183)
+constexpr int32_t kPairIlkka = 1;  // IlkkaPairAction (ilkka_pair_action_class.h:7-433)
+
+/// Pair action: the primitive BarePairAction, or IlkkaPairAction's off-diagonal action u(x, y) of
+/// x = q + s/2, y = q - s/2 (q = (|r| + |r'|)/2, s = |r - r'|) with its tau derivative. Both keep
+/// the potential tables v (Potential; and DActionDBeta of the bare action).
 struct PairDev {
     uint32_t sa = 0, sb = 0;
+    int32_t kind = kPairBare;
     int32_t is_coulomb = 0, use_long_range = 0, is_constant = 0;
     uint32_t max_level = 0;
     double r_v_min = 0., r_v_max = 0., r_vl_min = 0., r_vl_max = 0.;
     double v_long_k_0 = 0., v_long_r_0 = 0.;   // already scaled as in the reference constructor
     CubicTable v_r, v_long_r;
     const double* v_long_k = nullptr;          // [K]
+    // IlkkaPairAction only
+    BicubicTable u_xy, du_xy;
+    CubicTable u_long_r, du_long_r;
+    double r_u_min = 0., r_u_max = 0., r_du_min = 0., r_du_max = 0.;
+    double du_long_k_0 = 0., du_long_r_0 = 0.; // scaled as v_long_k_0 / v_long_r_0
+    const double* u_long_k = nullptr;          // [K]
+    const double* du_long_k = nullptr;         // [K]
 };
 
 /// Bisection move (src/events/moves/single_species_move/bisect/bisect_class.h:8-214) with the

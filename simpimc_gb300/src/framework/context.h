@@ -191,7 +191,15 @@ class Context {
         std::vector<int32_t> bucket;
     };
     std::vector<std::pair<const Cubic4*, HostCubic>> host_cubics;
-    std::vector<std::vector<double>> host_vk;  // v_long_k per pair action (empty without long range)
+    struct HostBicubic {
+        std::vector<double> x, y;
+        std::vector<double> c;  // [cells][16]
+        std::vector<int32_t> bx, by;
+    };
+    std::vector<std::pair<const double*, HostBicubic>> host_bicubics;
+    // Per pair action, the k-space coefficient of its long-range action: v_long_k for the bare action
+    // (multiplied by tau 2^level there), u_long_k / tau for IlkkaPairAction (empty without long range).
+    std::vector<std::vector<double>> host_vk;
 
    private:
     std::vector<std::unique_ptr<DeviceBuffer>> keep_;  // tables owned for the context lifetime
@@ -219,6 +227,7 @@ class Context {
     void BuildObservables(const Input& in);
     void ReadLoop(const Input& in, LoopNode& node);
     CubicTable BuildCubic(const std::vector<double>& x, const std::vector<double>& y, bool uniform);
+    BicubicTable BuildBicubic(const std::vector<double>& x, const std::vector<double>& y, const std::vector<double>& f);
     void FreeSplineTable(double L, uint32_t n_images, double lambda, double tau, bool want_dtau, CubicTable* image, CubicTable* dtau);
 
    public:

@@ -94,6 +94,143 @@ CubicTable Context::BuildCubic(const std::vector<double>& x, const std::vector<d
     return t;
 }
 
+// Second derivatives of the natural cubic spline through (x_i, y_i) (zero at both ends).
+static std::vector<double> NaturalSecond(const std::vector<double>& x, const std::vector<double>& y) {
+    const size_t n = x.size();
+    std::vector<double> m(n, 0.);
+    if (n < 3) return m;
+    std::vector<double> cp(n, 0.), dp(n, 0.);
+    for (size_t i = 1; i + 1 < n; ++i) {
+        const double h0 = x[i] - x[i - 1], h1 = x[i + 1] - x[i];
+        double diag = 2. * (h0 + h1);
+        double rhs = 6. * ((y[i + 1] - y[i]) / h1 - (y[i] - y[i - 1]) / h0);
+        if (i > 1) {
+            diag -= h0 * cp[i - 1];
+            rhs -= h0 * dp[i - 1];
+        }
+        cp[i] = h1 / diag;
+        dp[i] = rhs / diag;
+    }
+    m[n - 2] = dp[n - 2];
+    for (size_t i = n - 2; i-- > 1;) m[i] = dp[i] - cp[i] * m[i + 1];
+    return m;
+}
+
+// First derivatives at the knots of the natural cubic spline through (x_i, y_i).
+static std::vector<double> NaturalSlopes(const std::vector<double>& x, const std::vector<double>& y) {
+    const size_t n = x.size();
+    const std::vector<double> m = NaturalSecond(x, y);
+    std::vector<double> d(n);
+    for (size_t i = 0; i + 1 < n; ++i) {
+        const double h = x[i + 1] - x[i];
+        d[i] = (y[i + 1] - y[i]) / h - h * (2. * m[i] + m[i + 1]) / 6.;
+    }
+    const double h = x[n - 1] - x[n - 2];
+    d[n - 1] = (y[n - 1] - y[n - 2]) / h + h * (m[n - 2] + 2. * m[n - 1]) / 6.;
+    return d;
+}
+
+// Cubic p(t) on [0, h] with p(0) = f0, p(h) = f1, p'(0) = d0, p'(h) = d1: monomial coefficients as
+// rows of H applied to (f0, f1, d0, d1).
+static void HermiteMatrix(double h, double H[4][4]) {
+    const double ih = 1. / h, ih2 = ih * ih;
+    const double rows[4][4] = {{1., 0., 0., 0.},
+                               {0., 0., 1., 0.},
+                               {-3. * ih2, 3. * ih2, -2. * ih, -ih},
+                               {2. * ih2 * ih, -2. * ih2 * ih, ih2, ih2}};
+    for (int a = 0; a < 4; ++a)
+        for (int b = 0; b < 4; ++b) H[a][b] = rows[a][b];
+}
+
+// Knot descriptor with the bucket table of BuildCubic for a general grid (device pointers unset).
+static GridDev MakeGrid(const std::vector<double>& x, std::vector<int32_t>& bk) {
+    const size_t n = x.size();
+    GridDev g;
+    g.n = (int32_t)n;
+    g.x0 = x.front();
+    g.x1 = x.back();
+    const int nb = (int)std::min<size_t>(4 * n, 1u << 20);
+    g.n_bucket = nb;
+    g.inv_dx = nb / (x.back() - x.front());
+    bk.assign(nb, 0);
+    size_t i = 0;
+    for (int j = 0; j < nb; ++j) {
+        const double xl = x.front() + j / g.inv_dx;
+        while (i + 2 < n && x[i + 1] <= xl) ++i;
+        bk[j] = (int32_t)i;
+    }
+    return g;
+}
+
+// Natural bicubic spline through f(x_i, y_j) = f[i n_y + j]. The tensor product of natural cubic
+// splines restricted to a cell is the bicubic Hermite polynomial of its corner values f, df/dx,
+// df/dy and d2f/dxdy, where df/dx at the knots is the slope of each row's natural spline, df/dy
+// that of each column's, and d2f/dxdy the y-slope of the column spline through the row slopes.
+BicubicTable Context::BuildBicubic(const std::vector<double>& x, const std::vector<double>& y, const std::vector<double>& f) {
+    const size_t nx = x.size(), ny = y.size();
+    if (nx < 2 || ny < 2 || f.size() != nx * ny) throw PimcError(kErrInput, "2-D spline needs a full grid of at least 2 x 2 knots");
+    for (size_t i = 1; i < nx; ++i)
+        if (!(x[i] > x[i - 1])) throw PimcError(kErrInput, "spline knots must increase");
+    for (size_t j = 1; j < ny; ++j)
+        if (!(y[j] > y[j - 1])) throw PimcError(kErrInput, "spline knots must increase");
+    std::vector<double> fx(nx * ny), fy(nx * ny), fxy(nx * ny), line;
+    for (size_t j = 0; j < ny; ++j) {  // slopes along x of every row
+        line.resize(nx);
+        for (size_t i = 0; i < nx; ++i) line[i] = f[i * ny + j];
+        const std::vector<double> d = NaturalSlopes(x, line);
+        for (size_t i = 0; i < nx; ++i) fx[i * ny + j] = d[i];
+    }
+    for (size_t i = 0; i < nx; ++i) {  // slopes along y of every column, and of the row slopes
+        const std::vector<double> col(f.begin() + i * ny, f.begin() + (i + 1) * ny);
+        const std::vector<double> dcol(fx.begin() + i * ny, fx.begin() + (i + 1) * ny);
+        const std::vector<double> d = NaturalSlopes(y, col), dd = NaturalSlopes(y, dcol);
+        for (size_t j = 0; j < ny; ++j) {
+            fy[i * ny + j] = d[j];
+            fxy[i * ny + j] = dd[j];
+        }
+    }
+    std::vector<double> c((nx - 1) * (ny - 1) * 16);
+    for (size_t i = 0; i + 1 < nx; ++i)
+        for (size_t j = 0; j + 1 < ny; ++j) {
+            double Hx[4][4], Hy[4][4];
+            HermiteMatrix(x[i + 1] - x[i], Hx);
+            HermiteMatrix(y[j + 1] - y[j], Hy);
+            const size_t a0 = i * ny + j, a1 = (i + 1) * ny + j;
+            const double G[4][4] = {{f[a0], f[a0 + 1], fy[a0], fy[a0 + 1]},
+                                    {f[a1], f[a1 + 1], fy[a1], fy[a1 + 1]},
+                                    {fx[a0], fx[a0 + 1], fxy[a0], fxy[a0 + 1]},
+                                    {fx[a1], fx[a1 + 1], fxy[a1], fxy[a1 + 1]}};
+            double T[4][4];  // Hx G
+            for (int a = 0; a < 4; ++a)
+                for (int b = 0; b < 4; ++b) {
+                    double t = 0.;
+                    for (int k = 0; k < 4; ++k) t += Hx[a][k] * G[k][b];
+                    T[a][b] = t;
+                }
+            double* cell = &c[(i * (ny - 1) + j) * 16];
+            for (int a = 0; a < 4; ++a)
+                for (int b = 0; b < 4; ++b) {  // (Hx G Hy^T)[a][b]
+                    double t = 0.;
+                    for (int k = 0; k < 4; ++k) t += T[a][k] * Hy[b][k];
+                    cell[4 * a + b] = t;
+                }
+        }
+    BicubicTable t;
+    HostBicubic hb;
+    t.gx = MakeGrid(x, hb.bx);
+    t.gx.x = Upload(x);
+    t.gx.bucket = Upload(hb.bx);
+    t.gy = MakeGrid(y, hb.by);
+    t.gy.x = Upload(y);
+    t.gy.bucket = Upload(hb.by);
+    t.c = Upload(c);
+    hb.x = x;
+    hb.y = y;
+    hb.c = c;
+    host_bicubics.push_back({t.c, hb});
+    return t;
+}
+
 // FreeSpline (src/actions/free_spline_class.h:25-68): periodic-image part of the free-particle
 // action on a 10000-point uniform grid spanning one box length (1000 for open boundaries).
 void Context::FreeSplineTable(double L, uint32_t n_images, double lambda, double tau, bool want_dtau, CubicTable* image,
@@ -227,7 +364,8 @@ void Context::BuildActions(const Input& in) {
     auto alist = in.GetChild("Actions").GetChildList("Action");
     bool long_range_seen = false;
     for (const auto& a : alist) {
-        if (a.GetAttribute<std::string>("type") == "BarePairAction" && a.GetAttribute<bool>("use_long_range", false)) {
+        const std::string ty = a.GetAttribute<std::string>("type");
+        if ((ty == "BarePairAction" || ty == "IlkkaPairAction") && a.GetAttribute<bool>("use_long_range", false)) {
             if (!sys.pbc) throw PimcError(kErrInput, "use_long_range needs periodic boundaries");
             const double before = ks.cutoff;
             ks.Setup(a.GetAttribute<double>("k_cut", ks.cutoff), sys.L, sys.n_d);
@@ -345,6 +483,96 @@ void Context::BuildActions(const Input& in) {
                 vk0 *= (double)sys.sp_n[p.sa] * sys.sp_n[p.sb] * sys.M;
                 vr0 *= 0.;
             }
+            p.v_long_k_0 = vk0;
+            p.v_long_r_0 = vr0;
+            h.kind = 2;
+            h.index = sys.n_pair++;
+            h.species_list.push_back(p.sa);
+            h.species_list.push_back(p.sb);
+        } else if (h.type == "IlkkaPairAction") {
+            // ilkka_pair_action_class.h:253-432
+            if (sys.n_pair >= kMaxPair) throw PimcError(kErrUnsupported, "too many pair actions");
+            PairDev& p = sys.pair[sys.n_pair];
+            p.kind = kPairIlkka;
+            p.sa = SpeciesIndex(species_names, a.GetAttribute<std::string>("species_a"));
+            p.sb = SpeciesIndex(species_names, a.GetAttribute<std::string>("species_b"));
+            p.max_level = max_level;
+            p.use_long_range = a.GetAttribute<bool>("use_long_range", false) ? 1 : 0;
+            p.is_coulomb = 0;
+            p.is_constant = (p.sa == p.sb) && (sys.sp_n[p.sa] == 1 || sys.sp_lambda[p.sa] == 0.);
+            std::string file = a.GetAttribute<std::string>("file");
+            if (!file.empty() && file[0] != '/' && !base_dir.empty()) file = base_dir + "/" + file;
+            TableFile tf = TableFile::Load(file);
+            auto grid2 = [&](const std::string& g, const std::string& f) {
+                const auto& x = tf.Vec(g + "/off_diag/x");
+                const auto& y = tf.Vec(g + "/off_diag/y");
+                if ((size_t)tf.Scalar(g + "/off_diag/n_x") != x.size() || (size_t)tf.Scalar(g + "/off_diag/n_y") != y.size())
+                    throw PimcError(kErrInput, "table '" + file + "': inconsistent " + g + "/off_diag grid");
+                return BuildBicubic(x, y, tf.Vec(g + "/off_diag/" + f));
+            };
+            // Each stored k-vector takes the table value of its magnitude (:308-315).
+            auto by_mag = [&](const std::string& kd, const std::string& vd) {
+                const auto& kv = tf.Vec(kd);
+                const auto& vv = tf.Vec(vd);
+                std::vector<double> out(sys.K, 0.);
+                for (uint32_t k = 0; k < sys.K; ++k)
+                    for (size_t j = 0; j < kv.size() && j < vv.size(); ++j)
+                        if (std::fabs(kmags[k] - kv[j]) < 1.e-8) out[k] = vv[j];
+                return out;
+            };
+            p.u_xy = grid2("u", "u_xy");
+            p.du_xy = grid2("du", "du_xy");
+            {
+                const auto& r = tf.Vec("v/diag/r");
+                const auto& v = tf.Vec("v/diag/v_r");
+                if ((size_t)tf.Scalar("v/diag/n_r") != r.size() || r.size() != v.size())
+                    throw PimcError(kErrInput, "table '" + file + "': inconsistent v/diag grid");
+                p.v_r = BuildCubic(r, v, false);
+                p.r_v_min = r.front();
+                p.r_v_max = r.back();
+            }
+            double vk0 = 0., vr0 = 0., dk0 = 0., dr0 = 0.;
+            if (p.use_long_range) {
+                const auto& ru = tf.Vec("u/diag/r_long");
+                p.u_long_r = BuildCubic(ru, tf.Vec("u/diag/u_long_r"), false);
+                p.r_u_min = ru.front();
+                p.r_u_max = ru.back();
+                const auto& rd = tf.Vec("du/diag/r_long");
+                p.du_long_r = BuildCubic(rd, tf.Vec("du/diag/du_long_r"), false);
+                p.r_du_min = rd.front();
+                p.r_du_max = rd.back();
+                dr0 = tf.Scalar("du/diag/du_long_r_0");
+                dk0 = tf.Scalar("du/diag/du_long_k_0");
+                const auto& rv = tf.Vec("v/diag/r_long");
+                p.v_long_r = BuildCubic(rv, tf.Vec("v/diag/v_long_r"), false);
+                p.r_vl_min = rv.front();
+                p.r_vl_max = rv.back();
+                vr0 = tf.Scalar("v/diag/v_long_r_0");
+                vk0 = tf.Scalar("v/diag/v_long_k_0");
+                const std::vector<double> uk = by_mag("u/diag/k", "u/diag/u_long_k");
+                p.u_long_k = Upload(uk);
+                p.du_long_k = Upload(by_mag("du/diag/k", "du/diag/du_long_k"));
+                p.v_long_k = Upload(by_mag("v/diag/k", "v/diag/v_long_k"));
+                // The sweep multiplies every long-range coefficient by tau.
+                std::vector<double> scaled(uk);
+                for (auto& x : scaled) x /= sys.tau;
+                host_vk.resize(sys.n_pair + 1);
+                host_vk[sys.n_pair] = scaled;
+                sys.sp_rho[p.sa] = sys.sp_rho[p.sb] = 0;  // marked; slots assigned below
+            }
+            if (p.sa == p.sb) {  // :420-431
+                dk0 *= 0.5 * sys.sp_n[p.sa] * sys.sp_n[p.sb] * sys.M;
+                dr0 *= -0.5 * sys.sp_n[p.sa] * sys.M;
+                vk0 *= 0.5 * sys.sp_n[p.sa] * sys.sp_n[p.sb] * sys.M;
+                vr0 *= -0.5 * sys.sp_n[p.sa] * sys.M;
+            } else {
+                dk0 *= (double)sys.sp_n[p.sa] * sys.sp_n[p.sb] * sys.M;
+                dr0 *= 0.;
+                vk0 *= (double)sys.sp_n[p.sa] * sys.sp_n[p.sb] * sys.M;
+                vr0 *= 0.;
+            }
+            p.du_long_k_0 = dk0;
+            p.du_long_r_0 = dr0;
             p.v_long_k_0 = vk0;
             p.v_long_r_0 = vr0;
             h.kind = 2;

@@ -26,10 +26,85 @@ __device__ __forceinline__ double PairV(const PairDev& pa, double r, double rp) 
     return v;
 }
 
-/// BarePairAction::CalcU (bare_pair_action_class.h:146-150). The reference scales by
-/// (1 >> level) * tau, i.e. tau at level 0 and zero above; that behaviour is kept.
-__device__ __forceinline__ double PairU(const PairDev& pa, double r, double rp, uint32_t level, double tau) {
+/// CalcU of a link with end distances r, r' and s = |r - r'|.
+///  * BarePairAction (bare_pair_action_class.h:146-150): tau V(r, r') scaled by (1 >> level), i.e.
+///    tau at level 0 and zero above; that behaviour is kept.
+///  * IlkkaPairAction (ilkka_pair_action_class.h:77-101): u(q + s/2, q - s/2), q = (r + r')/2, minus
+///    half the long-range action at each end (clamped to its grid) when the action has an Ewald part.
+__device__ __forceinline__ double PairU(const PairDev& pa, double r, double rp, double s, uint32_t level, double tau) {
+    if (pa.kind == kPairIlkka) {
+        const double q = 0.5 * (r + rp);
+        double u = EvalBicubic(pa.u_xy, q + 0.5 * s, q - 0.5 * s);
+        if (pa.use_long_range) {
+            r = fmin(fmax(r, pa.r_u_min), pa.r_u_max);
+            rp = fmin(fmax(rp, pa.r_u_min), pa.r_u_max);
+            u -= 0.5 * EvalCubic(pa.u_long_r, r);
+            u -= 0.5 * EvalCubic(pa.u_long_r, rp);
+        }
+        return u;
+    }
     return level == 0 ? tau * PairV(pa, r, rp) : 0.;
+}
+
+/// CalcdUdBeta of a link: V(r, r') for the bare action (bare_pair_action_class.h:152-155);
+/// du(q + s/2, q - s/2) minus half the long-range du at each end for IlkkaPairAction
+/// (ilkka_pair_action_class.h:125-149).
+__device__ __forceinline__ double PairdUdBeta(const PairDev& pa, double r, double rp, double s) {
+    if (pa.kind == kPairIlkka) {
+        const double q = 0.5 * (r + rp);
+        double du = EvalBicubic(pa.du_xy, q + 0.5 * s, q - 0.5 * s);
+        if (pa.use_long_range) {
+            r = fmin(fmax(r, pa.r_du_min), pa.r_du_max);
+            rp = fmin(fmax(rp, pa.r_du_min), pa.r_du_max);
+            du -= 0.5 * EvalCubic(pa.du_long_r, r);
+            du -= 0.5 * EvalCubic(pa.du_long_r, rp);
+        }
+        return du;
+    }
+    return PairV(pa, r, rp);
+}
+
+/// IlkkaPairAction::CalcGradientU (ilkka_pair_action_class.h:172-222): the gradient of the link
+/// action with respect to the first particle's bead on the link's first slice, by the chain rule
+/// through (x, y). A0/A1 are the second particle's beads, C0/C1 the first's (Path::DrDrpDrrp).
+__device__ __forceinline__ void IlkkaGradientU(const PairDev& pa, const double* A0, const double* C0, const double* A1, const double* C1,
+                                               uint32_t n_d, double L, double iL, double* g) {
+    double rv[3] = {0., 0., 0.}, rq[3] = {0., 0., 0.}, rr[3] = {0., 0., 0.};
+    double a = 0., b = 0., c = 0.;
+#pragma unroll
+    for (uint32_t d = 0; d < 3; ++d) {
+        if (d < n_d) {
+            rv[d] = A0[d] - C0[d];
+            rq[d] = A1[d] - C1[d];
+            rv[d] -= rint(rv[d] * iL) * L;
+            rq[d] += rint((rv[d] - rq[d]) * iL) * L;
+            rr[d] = rv[d] - rq[d];
+            rr[d] -= rint(rr[d] * iL) * L;
+            a += rv[d] * rv[d];
+            b += rq[d] * rq[d];
+            c += rr[d] * rr[d];
+        }
+    }
+    double r = sqrt(a), rp = sqrt(b);
+    const double s = sqrt(c);
+    const double q = 0.5 * (r + rp);
+    double ux, uy;
+    EvalBicubic(pa.u_xy, q + 0.5 * s, q - 0.5 * s, &ux, &uy);
+    double rh[3], sh[3];
+#pragma unroll
+    for (uint32_t d = 0; d < 3; ++d) {
+        rh[d] = r == 0. ? 0. : rv[d] / r;
+        sh[d] = s == 0. ? 0. : rr[d] / s;
+        g[d] = d < n_d ? -0.5 * (ux * (rh[d] + sh[d]) + uy * (rh[d] - sh[d])) : 0.;
+    }
+    if (pa.use_long_range) {
+        r = fmin(fmax(r, pa.r_u_min), pa.r_u_max);
+        double tu, tdu;
+        EvalCubicVG(pa.u_long_r, r, tu, tdu);
+#pragma unroll
+        for (uint32_t d = 0; d < 3; ++d)
+            if (d < n_d) g[d] -= 0.5 * tdu * rh[d];
+    }
 }
 
 /// Pair potential from two minimum-image distances (PairAction::Potential, pair_action_class.h:369-395).

@@ -283,7 +283,15 @@ static bool Selected(const ActionHost& ah, int sel, int i) {
     return true;
 }
 
+/// The whole-ring action and its exact gradient cover Kinetic, HarmonicTrap and BarePairAction.
+static void RequireAdjointActions(const Context& c, int sel) {
+    for (size_t i = 0; i < c.actions.size(); ++i)
+        if (Selected(c.actions[i], sel, (int)i) && c.actions[i].kind == 2 && c.sys.pair[c.actions[i].index].kind != kPairBare)
+            throw PimcError(kErrUnsupported, "the whole-ring action and its gradient cover Kinetic, HarmonicTrap and BarePairAction");
+}
+
 double Context::TotalActionDev(int a, const double* pos, const float4* rho) {
+    RequireAdjointActions(*this, a);
     const uint32_t M = sys.M, np = sys.n_pad, n_d = sys.n_d;
     const double L = sys.L, iL = sys.iL, tau = sys.tau;
     double total = 0.;
@@ -356,6 +364,7 @@ double Context::TotalActionDev(int a, const double* pos, const float4* rho) {
 }
 
 void Context::GradientDev(int a, const double* pos, const float4* rho, double* grad) {
+    RequireAdjointActions(*this, a);
     const size_t n = (size_t)sys.M * 3 * sys.n_pad;
     CudaCheck(cudaMemsetAsync(grad, 0, n * sizeof(double), stream), "grad clear");
     const int th = 256;

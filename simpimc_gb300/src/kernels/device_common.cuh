@@ -63,6 +63,61 @@ __device__ __forceinline__ double EvalCubic(const CubicTable& t, double x) {
     return c.c0 + u * (c.c1 + u * (c.c2 + u * c.c3));
 }
 
+/// Value and slope of a CubicTable at x clamped to the grid (the slope of the edge interval at an
+/// end, as einspline's _vg evaluation of an argument the caller has clamped).
+__device__ __forceinline__ void EvalCubicVG(const CubicTable& t, double x, double& v, double& g) {
+    x = fmin(fmax(x, t.x0), t.x1);
+    int i;
+    if (t.uniform) {
+        i = (int)floor((x - t.x0) * t.inv_dx);
+        i = min(max(i, 0), t.n - 2);
+    } else {
+        int j = (int)floor((x - t.x0) * t.inv_dx);
+        j = min(max(j, 0), t.n_bucket - 1);
+        i = t.bucket[j];
+        while (i < t.n - 2 && __ldg(&t.x[i + 1]) <= x) ++i;
+    }
+    const Cubic4 c = t.c[i];
+    const double u = x - __ldg(&t.x[i]);
+    v = c.c0 + u * (c.c1 + u * (c.c2 + u * c.c3));
+    g = c.c1 + u * (2. * c.c2 + 3. * u * c.c3);
+}
+
+/// Cell of a 2-D table axis holding x: the last knot at or below x, within [0, n - 2] (so an
+/// argument outside the grid takes the edge cell).
+__device__ __forceinline__ int GridCell(const GridDev& g, double x) {
+    int i;
+    const double xc = fmin(fmax(x, g.x0), g.x1);
+    if (g.uniform) {
+        i = (int)floor((xc - g.x0) * g.inv_dx);
+        i = min(max(i, 0), g.n - 2);
+    } else {
+        int j = (int)floor((xc - g.x0) * g.inv_dx);
+        j = min(max(j, 0), g.n_bucket - 1);
+        i = g.bucket[j];
+        while (i < g.n - 2 && __ldg(&g.x[i + 1]) <= xc) ++i;
+    }
+    return i;
+}
+
+/// Value and partial derivatives of a BicubicTable at (x, y); the cell polynomial is evaluated at
+/// the unclamped arguments.
+__device__ __forceinline__ double EvalBicubic(const BicubicTable& t, double x, double y, double* fx = nullptr, double* fy = nullptr) {
+    const int i = GridCell(t.gx, x), j = GridCell(t.gy, y);
+    const double u = x - __ldg(&t.gx.x[i]), v = y - __ldg(&t.gy.x[j]);
+    const double* c = t.c + ((size_t)i * (t.gy.n - 1) + j) * 16;
+    double row[4], drow[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const double c0 = __ldg(&c[4 * a]), c1 = __ldg(&c[4 * a + 1]), c2 = __ldg(&c[4 * a + 2]), c3 = __ldg(&c[4 * a + 3]);
+        row[a] = c0 + v * (c1 + v * (c2 + v * c3));
+        drow[a] = c1 + v * (2. * c2 + 3. * v * c3);
+    }
+    if (fx) *fx = row[1] + u * (2. * row[2] + 3. * u * row[3]);
+    if (fy) *fy = drow[0] + u * (drow[1] + u * (drow[2] + u * drow[3]));
+    return row[0] + u * (row[1] + u * (row[2] + u * row[3]));
+}
+
 /// Free-particle log density with periodic-image correction (free_spline_class.h:189-197):
 /// -sum_d image(dr_d) - |dr|^2 / (4 lambda tau).
 __device__ __forceinline__ double LogRhoFree(const double* dr, uint32_t n_d, double i4lt, const CubicTable* image, int has_images) {

@@ -128,6 +128,45 @@ __global__ void StructureFactorKernel(const SystemDev sys, const double* __restr
     sk[k] = acc;
 }
 
+// IlkkaPairAction::CalcGradientULong of one bead (ilkka_pair_action_class.h:231-249):
+// sum_k u_long_k k (Re rho_g Im rho_B - Im rho_g Re rho_B), rho_g = exp(i k . r_g) the bead's own
+// density and rho_B species b's density on the slice, x2 for two species. One block per (listed
+// particle, slice); out[(i * n_slices + j) * 3 + d].
+__global__ void IlkkaLongGradKernel(const SystemDev sys, const double* __restrict__ pos, const double* __restrict__ uk,
+                                    const uint32_t* __restrict__ glist, uint32_t n_slices, uint32_t b0, uint32_t skip,
+                                    const double2* __restrict__ rho_b, int rho_b_slice_major, double scale, double* __restrict__ out) {
+    __shared__ double red[3][32];
+    const uint32_t i = blockIdx.x / n_slices, j = blockIdx.x % n_slices;
+    const uint32_t b = (b0 + j * skip) % sys.M, g = glist[i];
+    double r[3];
+    LoadBead(pos, sys.n_pad, sys.n_d, b, g, r);
+    double acc[3] = {0., 0., 0.};
+    for (uint32_t k = threadIdx.x; k < sys.K; k += blockDim.x) {
+        const int32_t pk = sys.kidx[k];
+        double kv[3] = {0., 0., 0.}, kr = 0.;
+        for (uint32_t d = 0; d < sys.n_d; ++d) {
+            kv[d] = KIdx(pk, (int)d) * sys.box[d];
+            kr += kv[d] * r[d];
+        }
+        double sn, cs;
+        sincos(kr, &sn, &cs);
+        const double2 rb = rho_b_slice_major ? rho_b[(size_t)j * sys.K + k] : rho_b[(size_t)b * sys.K + k];
+        const double f = uk[k] * (cs * rb.y - sn * rb.x);
+        for (uint32_t d = 0; d < 3; ++d) acc[d] += f * kv[d];
+    }
+    for (int d = 0; d < 3; ++d) {
+        double v = acc[d];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) red[d][threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double v = 0.;
+        for (uint32_t w = 0; w < (blockDim.x + 31) / 32; ++w) v += red[threadIdx.x][w];
+        out[(size_t)blockIdx.x * 3 + threadIdx.x] = scale * v;
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------------------------
@@ -288,7 +327,7 @@ double Context::GetAction(uint32_t ai, uint32_t b0, uint32_t b1, const uint32_t*
         LoadBead(pos, np, n_d, bj, offa + dp[2 * q], C1);
         double r, rp, s;
         DrDrpDrrp(A0, C0, A1, C1, n_d, L, iL, r, rp, s);
-        v[0] = PairU(pa, r, rp, level, tau);
+        v[0] = PairU(pa, r, rp, s, level, tau);
     }, &tot);
     if (pa.use_long_range) {
         const uint32_t K = sys.K;
@@ -318,7 +357,8 @@ double Context::GetAction(uint32_t ai, uint32_t b0, uint32_t b1, const uint32_t*
         }
         const double2* rho = sys.rho_k;
         const int slot_a = sys.sp_rho[pa.sa], slot_b = sys.sp_rho[pa.sb];
-        const double* vk = pa.v_long_k;
+        // bare: tau 2^level v_long_k (bare_pair_action_class.h:126-144); Ilkka: u_long_k (ilkka_pair_action_class.h:104-122)
+        const double* vk = pa.kind == kPairIlkka ? pa.u_long_k : pa.v_long_k;
         double lr = 0.;
         SumItems<1>(*this, (uint64_t)K * ns, [=] __device__(uint64_t i, double* v) {
             const uint32_t k = (uint32_t)(i / ns), j = (uint32_t)(i % ns);
@@ -334,7 +374,7 @@ double Context::GetAction(uint32_t ai, uint32_t b0, uint32_t b1, const uint32_t*
             v[0] = vk[k] * (a.x * c.x + a.y * c.y);
         }, &lr);
         if (pa.sa != pa.sb) lr *= 2.;
-        tot += skip * sys.tau * lr;
+        tot += pa.kind == kPairIlkka ? lr : skip * sys.tau * lr;
     }
     return tot;
 }
@@ -393,6 +433,64 @@ void Context::GetActionGradient(uint32_t ai, uint32_t b0, uint32_t b1, const uin
     const uint32_t ns = (b1 - b0 + skip - 1) / skip;
     const uint32_t offa = sys.sp_off[pa.sa], offb = sys.sp_off[pa.sb];
     const double tau = sys.tau;
+    if (pa.kind == kPairIlkka) {
+        // pair_action_class.h:318-334 with IlkkaPairAction's analytic link gradient
+        // (ilkka_pair_action_class.h:172-222), links to b + skip and b - skip (+M).
+        SumItems<3>(*this, (uint64_t)ns * npairs * 2, [=] __device__(uint64_t i, double* v) {
+            const uint32_t link = (uint32_t)(i & 1u);
+            const uint64_t ii = i >> 1;
+            const uint32_t j = (uint32_t)(ii / npairs), q = (uint32_t)(ii % npairs);
+            const uint32_t braw = b0 + j * skip;
+            const uint32_t bi = BeadLoop(braw, M);
+            const uint32_t bo = link == 0 ? BeadLoop(braw + skip, M) : BeadLoop(braw - skip + M, M);
+            double A0[3], C0[3], A1[3], C1[3];
+            LoadBead(pos, np, n_d, bi, offb + dp[2 * q + 1], A0);
+            LoadBead(pos, np, n_d, bi, offa + dp[2 * q], C0);
+            LoadBead(pos, np, n_d, bo, offb + dp[2 * q + 1], A1);
+            LoadBead(pos, np, n_d, bo, offa + dp[2 * q], C1);
+            IlkkaGradientU(pa, A0, C0, A1, C1, n_d, L, iL, v);
+        }, g);
+        if (pa.use_long_range && sys.K) {
+            // CalcGradientULong once per pair, on the pair's first particle (pair_action_class.h:331-334;
+            // ilkka_pair_action_class.h:231-249): the listed first particles with their multiplicity.
+            std::vector<uint32_t> firsts(npairs);
+            for (uint32_t q = 0; q < npairs; ++q) firsts[q] = offa + pairs[2 * q];
+            const double2* rb = sys.rho_k + (size_t)sys.sp_rho[pa.sb] * M * sys.K;
+            int slice_major = 0;
+            // One scratch block: [NEW-mode densities of species b, ns x K][per (pair, slice) gradients].
+            const size_t n_rho = mode ? (size_t)ns * sys.K : 0;
+            double2* scratch = RhoTmp(n_rho + ((size_t)npairs * ns * 3 + 1) / 2 + 1);
+            double* outg = reinterpret_cast<double*>(scratch + n_rho);
+            if (mode) {
+                // NEW mode: species b's density with the listed particles at their new positions, as GetAction forms it.
+                const int stride = std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
+                const std::vector<uint32_t>& lst = pa.sa == pa.sb ? la : lb;
+                uint32_t* dl = Parts(std::max<size_t>(1, lst.size()));
+                if (!lst.empty()) CudaCheck(cudaMemcpyAsync(dl, lst.data(), lst.size() * 4, cudaMemcpyHostToDevice, stream), "parts upload");
+                ProposalRhoKernel<<<ns, 256, (size_t)2 * 3 * stride * sizeof(double2), stream>>>(sys, pa.sb, dl, (uint32_t)lst.size(), b0, skip,
+                                                                                               scratch);
+                CudaCheck(cudaGetLastError(), "proposal rho launch");
+                Sync();  // `Parts` is reused below
+                rb = scratch;
+                slice_major = 1;
+            }
+            uint32_t* dg = Parts(firsts.size());
+            CudaCheck(cudaMemcpyAsync(dg, firsts.data(), firsts.size() * 4, cudaMemcpyHostToDevice, stream), "parts upload");
+            IlkkaLongGradKernel<<<npairs * ns, 256, 0, stream>>>(sys, pos, pa.u_long_k, dg, ns, b0, skip, rb, slice_major,
+                                                                pa.sa != pa.sb ? 2. : 1., outg);
+            CudaCheck(cudaGetLastError(), "long-range gradient launch");
+            std::vector<double> hg((size_t)npairs * ns * 3);
+            CudaCheck(cudaMemcpyAsync(hg.data(), outg, hg.size() * sizeof(double), cudaMemcpyDeviceToHost, stream), "read gradient");
+            Sync();
+            for (uint32_t q = 0; q < npairs; ++q)
+                for (uint32_t d = 0; d < n_d; ++d) {
+                    double t = 0.;
+                    for (uint32_t j = 0; j < ns; ++j) t += hg[((size_t)q * ns + j) * 3 + d];
+                    g[d] += t;
+                }
+        }
+        return;
+    }
     // pair_action_class.h:135-155 central differences on the first particle's bead, links to
     // b + skip and to b - skip (+M), eps = 1e-4. The Bare action has no long-range gradient.
     SumItems<3>(*this, (uint64_t)ns * npairs * 2, [=] __device__(uint64_t i, double* v) {
@@ -417,10 +515,10 @@ void Context::GetActionGradient(uint32_t ai, uint32_t b0, uint32_t b1, const uin
             double r, rp, s;
             C0[d] = c0 + eps;
             DrDrpDrrp(A0, C0, A1, C1, n_d, L, iL, r, rp, s);
-            const double f1 = PairU(pa, r, rp, level, tau);
+            const double f1 = PairU(pa, r, rp, s, level, tau);
             C0[d] = c0 - eps;
             DrDrpDrrp(A0, C0, A1, C1, n_d, L, iL, r, rp, s);
-            const double f2 = PairU(pa, r, rp, level, tau);
+            const double f2 = PairU(pa, r, rp, s, level, tau);
             C0[d] = c0;
             v[d] = (f1 - f2) / (2. * eps);
         }
@@ -484,13 +582,15 @@ double Context::DActionDBeta(uint32_t ai) {
         LoadBead(pos, np, n_d, bn, offa + x, C1);
         double r, rp, s;
         DrDrpDrrp(A0, C0, A1, C1, n_d, L, iL, r, rp, s);
-        v[0] = PairV(pa, r, rp);
+        v[0] = PairdUdBeta(pa, r, rp, s);
     }, &out);
     if (pa.use_long_range) {
+        // bare: CalcVLong (bare_pair_action_class.h:126-144); Ilkka: CalcdUdBetaLong (ilkka_pair_action_class.h:152-169)
+        const bool ilkka = pa.kind == kPairIlkka;
         const uint32_t K = sys.K;
         const double2* ra = sys.rho_k + (size_t)sys.sp_rho[pa.sa] * M * K;
         const double2* rb = sys.rho_k + (size_t)sys.sp_rho[pa.sb] * M * K;
-        const double* vk = pa.v_long_k;
+        const double* vk = ilkka ? pa.du_long_k : pa.v_long_k;
         double lr = 0.;
         SumItems<1>(*this, (uint64_t)K * M, [=] __device__(uint64_t i, double* v) {
             const uint32_t k = (uint32_t)(i / M), b = (uint32_t)(i % M);
@@ -498,7 +598,7 @@ double Context::DActionDBeta(uint32_t ai) {
             v[0] = (a.x * c.x + a.y * c.y) * vk[k];
         }, &lr);
         if (!hom) lr *= 2.;
-        out += lr + pa.v_long_k_0 + pa.v_long_r_0;
+        out += ilkka ? lr + pa.du_long_k_0 + pa.du_long_r_0 : lr + pa.v_long_k_0 + pa.v_long_r_0;
     }
     if (ah.is_first_time) {
         ah.is_first_time = false;
@@ -624,17 +724,25 @@ double Context::VirialCentroid(uint32_t s) {
             LoadBead(pos, np, n_d, b, ga, C0);
             LoadBead(pos, np, n_d, bo, gb, A1);
             LoadBead(pos, np, n_d, bo, ga, C1);
-            const double eps = 1.e-4;
             double dot = 0.;
+            if (pa.kind == kPairIlkka) {
+                double gl[3];
+                IlkkaGradientU(pa, A0, C0, A1, C1, n_d, L, iL, gl);
+                for (uint32_t d = 0; d < n_d; ++d)
+                    dot += gl[d] * MinImage(PosAt(pos, np, b, d, offs + pp) - PosAt(pos, np, 0, d, offs + pp), L, iL);
+                v[0] = dot;
+                return;
+            }
+            const double eps = 1.e-4;
             for (uint32_t d = 0; d < n_d; ++d) {
                 const double c0 = C0[d];
                 double r, rp, sd;
                 C0[d] = c0 + eps;
                 DrDrpDrrp(A0, C0, A1, C1, n_d, L, iL, r, rp, sd);
-                const double f1 = PairU(pa, r, rp, 0, tau);
+                const double f1 = PairU(pa, r, rp, sd, 0, tau);
                 C0[d] = c0 - eps;
                 DrDrpDrrp(A0, C0, A1, C1, n_d, L, iL, r, rp, sd);
-                const double f2 = PairU(pa, r, rp, 0, tau);
+                const double f2 = PairU(pa, r, rp, sd, 0, tau);
                 C0[d] = c0;
                 const double gd = (f1 - f2) / (2. * eps);
                 const double dr = MinImage(PosAt(pos, np, b, d, offs + pp) - PosAt(pos, np, 0, d, offs + pp), L, iL);
@@ -643,6 +751,39 @@ double Context::VirialCentroid(uint32_t s) {
             v[0] = dot;
         }, &part);
         total += part;
+        if (pa.kind == kPairIlkka && pa.use_long_range && sys.K) {
+            // CalcGradientULong(b, b + 1, first particle) once per pair (pair_action_class.h:331-334):
+            // the listed particle itself for every partner when it is species a (or the action is
+            // homologous), otherwise every species-a particle once.
+            const uint32_t sa = pa.sa, na = sys.sp_n[sa], offa = sys.sp_off[sa];
+            std::vector<uint32_t> firsts(na);
+            for (uint32_t q = 0; q < na; ++q) firsts[q] = offa + q;
+            double2* scratch = RhoTmp(((size_t)na * M * 3 + 1) / 2 + 1);
+            double* G = reinterpret_cast<double*>(scratch);
+            uint32_t* dg = Parts(na);
+            CudaCheck(cudaMemcpyAsync(dg, firsts.data(), na * 4, cudaMemcpyHostToDevice, stream), "parts upload");
+            IlkkaLongGradKernel<<<na * M, 256, 0, stream>>>(sys, pos, pa.u_long_k, dg, M, 0, 1,
+                                                           sys.rho_k + (size_t)sys.sp_rho[pa.sb] * M * sys.K, 0, hom ? 1. : 2., G);
+            CudaCheck(cudaGetLastError(), "long-range gradient launch");
+            const bool first_is_s = hom || s_is_a;
+            const double mult = hom ? (double)(ns - 1) : (double)sys.sp_n[pa.sb];
+            double lrp = 0.;
+            SumItems<1>(*this, (uint64_t)ns * M, [=] __device__(uint64_t i, double* v) {
+                const uint32_t pp = (uint32_t)(i / M), b = (uint32_t)(i % M);
+                double gsum[3] = {0., 0., 0.};
+                if (first_is_s) {
+                    for (uint32_t d = 0; d < 3; ++d) gsum[d] = mult * G[((size_t)pp * M + b) * 3 + d];
+                } else {
+                    for (uint32_t q = 0; q < na; ++q)
+                        for (uint32_t d = 0; d < 3; ++d) gsum[d] += G[((size_t)q * M + b) * 3 + d];
+                }
+                double dot = 0.;
+                for (uint32_t d = 0; d < n_d; ++d)
+                    dot += gsum[d] * MinImage(PosAt(pos, np, b, d, offs + pp) - PosAt(pos, np, 0, d, offs + pp), L, iL);
+                v[0] = dot;
+            }, &lrp);
+            total += lrp;
+        }
     }
     return total;
 }

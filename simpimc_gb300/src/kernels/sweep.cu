@@ -46,13 +46,30 @@ struct CubicDD {
     dd x0{0.f, 0.f}, x1{0.f, 0.f};
 };
 
+/// Double-float BicubicTable: knots as (hi, lo) pairs, per cell the 16 coefficients as 8 float4 of
+/// (hi, lo) pairs in the order of BicubicTable::c.
+struct BicubicDD {
+    const float2* gx = nullptr;
+    const float2* gy = nullptr;
+    const int32_t* bx = nullptr;
+    const int32_t* by = nullptr;
+    const float4* c = nullptr;
+    int32_t nx = 0, ny = 0, nbx = 0, nby = 0;
+    float x0f = 0.f, inv_dxf = 0.f, y0f = 0.f, inv_dyf = 0.f;
+    dd x0{0.f, 0.f}, x1{0.f, 0.f}, y0{0.f, 0.f}, y1{0.f, 0.f};
+};
+
 struct PairDD {
     uint32_t sa, sb;
-    int32_t is_coulomb, use_lr, is_constant, max_level;
+    int32_t kind, is_coulomb, use_lr, is_constant, max_level;
     int32_t slot_a, slot_b;
     dd rvmin, rvmax, rvlmin, rvlmax;
     CubicDD v_r, v_long_r;
-    const float2* vk;  // [K]
+    const float2* vk;  // [K]: the long-range coefficient the sweep multiplies by tau
+    // IlkkaPairAction
+    BicubicDD u_xy;
+    CubicDD u_long_r;
+    dd rumin, rumax;
 };
 
 constexpr int kMoveKinetic = 2;
@@ -160,6 +177,33 @@ __device__ __forceinline__ dd EvalCubicDD(const CubicDD& t, dd x) {
     const dd u = Sub(x, LoadDD(&t.x[i]));
     const dd v = Add(dd{a.z, a.w}, Mul(u, Add(dd{b.x, b.y}, Mul(u, dd{b.z, b.w}))));
     return Add(dd{a.x, a.y}, Mul(u, v));
+}
+
+/// Cell of one 2-D table axis holding x (the last knot at or below x, within [0, n - 2]).
+__device__ __forceinline__ int GridCellDD(const float2* g, const int32_t* bucket, int n, int nb, float x0f, float inv_dxf, dd x0, dd x1, dd x) {
+    const dd xc = Min(Max(x, x0), x1);
+    int j = (int)floorf(__fmul_rn(__fsub_rn(xc.hi, x0f), inv_dxf));
+    j = min(max(j, 0), nb - 1);
+    int i = bucket[j];
+    while (i < n - 2 && !Less(xc, LoadDD(&g[i + 1]))) ++i;
+    while (i > 0 && Less(xc, LoadDD(&g[i]))) --i;
+    return i;
+}
+
+/// BicubicTable evaluation in double-float: the cell polynomial at the unclamped arguments.
+__device__ __forceinline__ dd EvalBicubicDD(const BicubicDD& t, dd x, dd y) {
+    const int i = GridCellDD(t.gx, t.bx, t.nx, t.nbx, t.x0f, t.inv_dxf, t.x0, t.x1, x);
+    const int j = GridCellDD(t.gy, t.by, t.ny, t.nby, t.y0f, t.inv_dyf, t.y0, t.y1, y);
+    const dd u = Sub(x, LoadDD(&t.gx[i])), v = Sub(y, LoadDD(&t.gy[j]));
+    const float4* c = t.c + ((size_t)i * (t.ny - 1) + j) * 8;
+    dd acc{0.f, 0.f};
+#pragma unroll
+    for (int a = 3; a >= 0; --a) {
+        const float4 p = c[2 * a], q = c[2 * a + 1];  // (c_a0, c_a1), (c_a2, c_a3)
+        const dd row = Add(dd{p.x, p.y}, Mul(v, Add(dd{p.z, p.w}, Mul(v, Add(dd{q.x, q.y}, Mul(v, dd{q.z, q.w}))))));
+        acc = a == 3 ? row : Add(row, Mul(u, acc));
+    }
+    return acc;
 }
 
 /// Sum over dimensions of the image-spline values.
@@ -304,10 +348,14 @@ __device__ __forceinline__ dd PairHalfV(const PairDD& pa, dd r) {
 /// quad of lanes: lanes 0-2 take one Cartesian component of Path::DrDrpDrrp (path_class.h:137-150)
 /// each, lanes 0 and 1 then take r and r'. Every lane of the warp must call it; the result is
 /// returned on lane 0 of the quad (zero elsewhere and for invalid links).
+/// With `ext` (the move has an IlkkaPairAction; uniform over the warp) the quad also forms
+/// s = |r - r'| (min image), and an Ilkka link is u(q + s/2, q - s/2) from lane 0 minus half the
+/// long-range action of r (lane 1) and of r' (lane 2), ilkka_pair_action_class.h:77-101; it is not
+/// scaled by tau.
 __device__ __forceinline__ dd PairLinkU4(const PairDD* s_pairs, const MoveDD& mv, const uint32_t* link_off, uint32_t l, bool valid, int ql,
                                          uint32_t s, uint32_t p, uint32_t B, uint32_t bead0, uint32_t M, uint32_t np, uint32_t n_d,
-                                         const uint32_t* sp_off, const float2* pos, const dd* seg, dd L, dd iL, dd tau) {
-    dd rv2{0.f, 0.f}, rq2{0.f, 0.f};
+                                         const uint32_t* sp_off, const float2* pos, const dd* seg, dd L, dd iL, dd tau, bool ext) {
+    dd rv2{0.f, 0.f}, rq2{0.f, 0.f}, ss2{0.f, 0.f};
     int pi = 0;
     if (valid) {
         while (l >= link_off[pi + 1]) ++pi;
@@ -332,16 +380,41 @@ __device__ __forceinline__ dd PairLinkU4(const PairDD* s_pairs, const MoveDD& mv
             if (n != 0.f) rq = Add(rq, MulF(L, n));
             rv2 = Sqr(rv);
             rq2 = Sqr(rq);
+            if (ext) ss2 = Sqr(MinImageDD(Sub(rv, rq), L, iL));
         }
     }
     rv2 = Add(rv2, ShflXorDD(rv2, 1));
     rv2 = Add(rv2, ShflXorDD(rv2, 2));
     rq2 = Add(rq2, ShflXorDD(rq2, 1));
     rq2 = Add(rq2, ShflXorDD(rq2, 2));
+    if (!ext) {
+        dd f{0.f, 0.f};
+        if (valid && ql < 2) f = PairHalfV(s_pairs[mv.pair[pi]], Sqrt(ql == 0 ? rv2 : rq2));
+        f = Add(f, ShflXorDD(f, 1));
+        return (valid && ql == 0) ? Mul(tau, f) : dd{0.f, 0.f};
+    }
+    ss2 = Add(ss2, ShflXorDD(ss2, 1));
+    ss2 = Add(ss2, ShflXorDD(ss2, 2));
     dd f{0.f, 0.f};
-    if (valid && ql < 2) f = PairHalfV(s_pairs[mv.pair[pi]], Sqrt(ql == 0 ? rv2 : rq2));
+    bool ilkka = false;
+    if (valid) {
+        const PairDD& pa = s_pairs[mv.pair[pi]];
+        ilkka = pa.kind == kPairIlkka;
+        if (!ilkka) {
+            if (ql < 2) f = PairHalfV(pa, Sqrt(ql == 0 ? rv2 : rq2));
+        } else if (ql == 0) {
+            const dd r = Sqrt(rv2), rp = Sqrt(rq2), sl = Sqrt(ss2);
+            const dd q = Scale2(Add(r, rp), 0.5f), hs = Scale2(sl, 0.5f);
+            f = EvalBicubicDD(pa.u_xy, Add(q, hs), Sub(q, hs));
+        } else if (ql < 3 && pa.use_lr) {
+            const dd r = Min(Max(Sqrt(ql == 1 ? rv2 : rq2), pa.rumin), pa.rumax);
+            f = Neg(Scale2(EvalCubicDD(pa.u_long_r, r), 0.5f));
+        }
+    }
     f = Add(f, ShflXorDD(f, 1));
-    return (valid && ql == 0) ? Mul(tau, f) : dd{0.f, 0.f};
+    f = Add(f, ShflXorDD(f, 2));
+    if (!(valid && ql == 0)) return dd{0.f, 0.f};
+    return ilkka ? f : Mul(tau, f);
 }
 
 __device__ __forceinline__ void CopyWords(void* dst, const void* src, uint32_t bytes) {
@@ -375,7 +448,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
     if (threadIdx.x == 0)
         for (uint32_t i = 0; i < a.n_pairs; ++i)
             for (uint32_t j = 0; j < a.n_stage; ++j) {
-                CubicDD* t[2] = {&s_pairs[i].v_long_r, &s_pairs[i].v_r};
+                CubicDD* t[3] = {&s_pairs[i].v_long_r, &s_pairs[i].v_r, &s_pairs[i].u_long_r};
                 for (CubicDD* c : t)
                     if (c->x == a.stage_x[j]) {
                         c->x = reinterpret_cast<const float2*>(sbase + a.stage_off_x[j]);
@@ -440,7 +513,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
             const MoveDD& mv = s_moves[m];
             const uint32_t s = mv.species, nl = mv.n_level, B = 1u << nl;
             const uint32_t g_off = a.sp_off[s];
-            bool any_lr = false, grid_work = false;
+            bool any_lr = false, grid_work = false, ext_links = false;
             int slot_s = -1, slot_o_first = -1;
             uint32_t n_links = 0;  // pair links of the moved particle over the segment, all pair actions
             uint32_t link_off[kMaxPair + 1];
@@ -449,6 +522,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                 link_off[pi] = n_links;
                 if (!pa.is_constant) {
                     grid_work = true;
+                    ext_links |= pa.kind == kPairIlkka;
                     const uint32_t other = pa.sa == pa.sb ? s : (pa.sa == s ? pa.sb : pa.sa);
                     n_links += (pa.sa == pa.sb ? a.sp_n[s] - 1 : a.sp_n[other]) * B;
                 }
@@ -596,7 +670,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                     for (uint32_t r = 0; r < link_rounds; ++r) {
                         const uint32_t l = link_first + r * link_stride;
                         pair_old = Add(pair_old, PairLinkU4(s_pairs, mv, link_off, l, l < n_links, qlane, s, p, B, bead0, M, np, n_d, a.sp_off,
-                                                            a.pos, seg_old, a.L, a.iL, a.tau));
+                                                            a.pos, seg_old, a.L, a.iL, a.tau, ext_links));
                     }
                     old_done = true;
                     PIMC_ROLE_END(rt2, 3);
@@ -658,10 +732,10 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                     for (uint32_t r = 0; r < link_rounds; ++r) {
                         const uint32_t l = link_first + r * link_stride;
                         acc = Add(acc, PairLinkU4(s_pairs, mv, link_off, l, l < n_links, qlane, s, p, B, bead0, M, np, n_d, a.sp_off, a.pos,
-                                                  seg_new, a.L, a.iL, a.tau));
+                                                  seg_new, a.L, a.iL, a.tau, ext_links));
                         if (!old_done)
                             acc = Sub(acc, PairLinkU4(s_pairs, mv, link_off, l, l < n_links, qlane, s, p, B, bead0, M, np, n_d, a.sp_off, a.pos,
-                                                      seg_old, a.L, a.iL, a.tau));
+                                                      seg_old, a.L, a.iL, a.tau, ext_links));
                     }
                     if (old_done) acc = Sub(acc, pair_old);
                     if (any_lr && kF32) {
@@ -1103,6 +1177,53 @@ static CubicDD MakeCubicDD(Context& c, const CubicTable& t, std::vector<std::uni
     return o;
 }
 
+static BicubicDD MakeBicubicDD(Context& c, const BicubicTable& t, std::vector<std::unique_ptr<DeviceBuffer>>& keep) {
+    BicubicDD o;
+    if (!t.c) return o;
+    const Context::HostBicubic* h = nullptr;
+    for (auto& kv : c.host_bicubics)
+        if (kv.first == t.c) h = &kv.second;
+    if (!h) throw PimcError(kErrState, "2-D spline table without host copy");
+    auto knots = [&](const std::vector<double>& x) {
+        std::vector<float2> v(x.size());
+        for (size_t i = 0; i < x.size(); ++i) {
+            float hi, lo;
+            SplitDouble(x[i], hi, lo);
+            v[i] = make_float2(hi, lo);
+        }
+        keep.emplace_back(new DeviceBuffer(v.size() * sizeof(float2)));
+        CudaCheck(cudaMemcpy(keep.back()->ptr, v.data(), v.size() * sizeof(float2), cudaMemcpyHostToDevice), "dd knots");
+        return keep.back()->as<float2>();
+    };
+    o.gx = knots(h->x);
+    o.gy = knots(h->y);
+    std::vector<float4> cf(h->c.size() / 2);
+    for (size_t i = 0; i + 1 < h->c.size(); i += 2) {
+        float a0, a1, b0, b1;
+        SplitDouble(h->c[i], a0, a1);
+        SplitDouble(h->c[i + 1], b0, b1);
+        cf[i / 2] = make_float4(a0, a1, b0, b1);
+    }
+    keep.emplace_back(new DeviceBuffer(cf.size() * sizeof(float4)));
+    CudaCheck(cudaMemcpy(keep.back()->ptr, cf.data(), cf.size() * sizeof(float4), cudaMemcpyHostToDevice), "dd 2-D coefficients");
+    o.c = keep.back()->as<float4>();
+    o.bx = t.gx.bucket;
+    o.by = t.gy.bucket;
+    o.nx = t.gx.n;
+    o.ny = t.gy.n;
+    o.nbx = t.gx.n_bucket;
+    o.nby = t.gy.n_bucket;
+    o.x0f = (float)t.gx.x0;
+    o.inv_dxf = (float)t.gx.inv_dx;
+    o.y0f = (float)t.gy.x0;
+    o.inv_dyf = (float)t.gy.inv_dx;
+    Split(t.gx.x0, o.x0);
+    Split(t.gx.x1, o.x1);
+    Split(t.gy.x0, o.y0);
+    Split(t.gy.x1, o.y1);
+    return o;
+}
+
 void Context::BuildSweepTables() {
     if (sweep_tables_built_) return;
     std::vector<float4> tab(256);
@@ -1135,6 +1256,7 @@ void Context::BuildSweepTables() {
         PairDD& q = pd[i];
         q.sa = p.sa;
         q.sb = p.sb;
+        q.kind = p.kind;
         q.is_coulomb = p.is_coulomb;
         q.use_lr = p.use_long_range;
         q.is_constant = p.is_constant;
@@ -1147,6 +1269,15 @@ void Context::BuildSweepTables() {
         Split(p.r_vl_max, q.rvlmax);
         q.v_r = make(p.v_r);
         q.v_long_r = p.use_long_range ? make(p.v_long_r) : CubicDD();
+        q.u_xy = BicubicDD();
+        q.u_long_r = CubicDD();
+        q.rumin = q.rumax = dd{0.f, 0.f};
+        if (p.kind == kPairIlkka) {
+            q.u_xy = MakeBicubicDD(*this, p.u_xy, keep_);
+            if (p.use_long_range) q.u_long_r = make(p.u_long_r);
+            Split(p.r_u_min, q.rumin);
+            Split(p.r_u_max, q.rumax);
+        }
         q.vk = nullptr;
         if (p.use_long_range) {
             std::vector<float2> vk(sys.K);
@@ -1165,9 +1296,10 @@ void Context::BuildSweepTables() {
     // Tables worth staging in shared memory: the pair actions' spline tables, once each.
     stage_tables_.clear();
     for (int i = 0; i < sys.n_pair; ++i) {
-        const CubicDD* ts[2] = {&pd[i].v_long_r, &pd[i].v_r};
-        const bool used[2] = {pd[i].use_lr != 0, pd[i].is_coulomb == 0};
-        for (int j = 0; j < 2; ++j) {
+        const bool ilkka = pd[i].kind == kPairIlkka;
+        const CubicDD* ts[3] = {&pd[i].v_long_r, &pd[i].v_r, &pd[i].u_long_r};
+        const bool used[3] = {!ilkka && pd[i].use_lr != 0, !ilkka && pd[i].is_coulomb == 0, ilkka && pd[i].use_lr != 0};
+        for (int j = 0; j < 3; ++j) {
             if (!used[j] || !ts[j]->x) continue;
             bool seen = false;
             for (auto& st : stage_tables_) seen |= (st.x == ts[j]->x);

@@ -1,4 +1,4 @@
-"""Pair-action table files for BarePairAction (Coulomb with an optional Ewald long-range split).
+"""Pair-action table files for BarePairAction and IlkkaPairAction (Coulomb, optional Ewald split).
 
 The reference reads these tables from HDF5 files written by its `pagen` generator (an empty
 submodule in the reference repository). This module writes the same datasets
@@ -24,7 +24,7 @@ from pathlib import Path
 
 import numpy as np
 
-__all__ = ["write_table", "coulomb_table", "lattice_k_magnitudes", "ewald_alpha"]
+__all__ = ["write_table", "coulomb_table", "ilkka_table", "lattice_k_magnitudes", "ewald_alpha"]
 
 
 def write_table(path, datasets: dict) -> None:
@@ -81,6 +81,73 @@ def coulomb_table(path, *, z_ab: float = 1.0, L: float = 0.0, k_cut: float = 0.0
             "v/diag/k": k,
             "v/diag/v_long_k": vk,
             "v/diag/v_long_k_0": -z_ab * math.pi / (a * a * vol),
+        })
+    write_table(path, ds)
+    return ds
+
+
+def _ilkka_grid(x_max: float, n: int) -> np.ndarray:
+    """Non-uniform grid on [0, x_max], denser at small distances: x_max t^1.5 for uniform t."""
+    t = np.linspace(0.0, 1.0, n)
+    return x_max * t ** 1.5
+
+
+def ilkka_table(path, *, tau: float, lam: float = 0.5, z_ab: float = 1.0, L: float = 0.0, k_cut: float = 0.0,
+                n_d: int = 3, n_xy: int = 64, xy_max: float | None = None, alpha: float | None = None) -> dict:
+    """Write an IlkkaPairAction table (src/actions/pair_action/ilkka_pair_action_class.h:253-432).
+
+    The reference's tables come from a pair-density squarer that is not part of its repository, so
+    this one is synthetic but smooth and of the right shape. The off-diagonal action is the
+    end-point average of a Gaussian-smeared Coulomb potential at the two 'extremal' distances,
+
+        u(x, y) = tau [phi(x) + phi(y)] / 2,   phi(r) = z erf(r / a) / r,   a = sqrt(4 lambda tau),
+
+    with x = q + s/2, y = q - s/2, q = (|r| + |r'|) / 2, s = |r - r'|: it equals tau phi(r) on the
+    diagonal r = r'. du(x, y) is its tau derivative (a depends on tau). The grids in x and y are
+    equal and non-uniform, and u(x, y) = u(y, x), so the matrix storage order (value (i, j) at
+    i n_y + j here) cannot change the spline. With ``L > 0`` and ``k_cut > 0`` the long-range parts
+    are the Ewald split of BarePairAction's table scaled for the action (u = tau v) and its tau
+    derivative (du = v); ``v/diag`` holds the potential datasets as for BarePairAction.
+    """
+    a = math.sqrt(4.0 * lam * tau)
+    if xy_max is None:
+        xy_max = math.sqrt(n_d) * L if L > 0 else 20.0
+    g = _ilkka_grid(xy_max, n_xy)
+    erf = np.vectorize(math.erf)
+
+    def phi(r):
+        r = np.asarray(r, dtype=np.float64)
+        out = np.empty_like(r)
+        small = r < 1e-8
+        out[small] = z_ab * 2.0 / (a * math.sqrt(math.pi))
+        rr = r[~small]
+        out[~small] = z_ab * erf(rr / a) / rr
+        return out
+
+    def dphi_da(r):
+        r = np.asarray(r, dtype=np.float64)
+        return -z_ab * 2.0 / math.sqrt(math.pi) * np.exp(-(r / a) ** 2) / (a * a)
+
+    X, Y = np.meshgrid(g, g, indexing="ij")
+    u = tau * 0.5 * (phi(X) + phi(Y))
+    # d/dtau [tau Phi(a(tau))] = Phi + tau dPhi/da da/dtau, da/dtau = a / (2 tau)
+    du = 0.5 * (phi(X) + phi(Y)) + 0.5 * a * 0.5 * (dphi_da(X) + dphi_da(Y))
+    ds = {
+        "u/off_diag/n_x": n_xy, "u/off_diag/n_y": n_xy, "u/off_diag/x": g, "u/off_diag/y": g, "u/off_diag/u_xy": u.ravel(),
+        "du/off_diag/n_x": n_xy, "du/off_diag/n_y": n_xy, "du/off_diag/x": g, "du/off_diag/y": g, "du/off_diag/du_xy": du.ravel(),
+    }
+    v = coulomb_table(path, z_ab=z_ab, L=L, k_cut=k_cut, n_d=n_d, alpha=alpha)  # v/diag datasets (file rewritten below)
+    ds.update(v)
+    if L > 0 and k_cut > 0:
+        ds.update({
+            "u/diag/n_r_long": v["v/diag/n_r_long"], "u/diag/r_long": v["v/diag/r_long"],
+            "u/diag/u_long_r": tau * v["v/diag/v_long_r"], "u/diag/u_long_r_0": tau * v["v/diag/v_long_r_0"],
+            "u/diag/n_k": v["v/diag/n_k"], "u/diag/k": v["v/diag/k"],
+            "u/diag/u_long_k": tau * v["v/diag/v_long_k"], "u/diag/u_long_k_0": tau * v["v/diag/v_long_k_0"],
+            "du/diag/n_r_long": v["v/diag/n_r_long"], "du/diag/r_long": v["v/diag/r_long"],
+            "du/diag/du_long_r": v["v/diag/v_long_r"], "du/diag/du_long_r_0": v["v/diag/v_long_r_0"],
+            "du/diag/n_k": v["v/diag/n_k"], "du/diag/k": v["v/diag/k"],
+            "du/diag/du_long_k": v["v/diag/v_long_k"], "du/diag/du_long_k_0": v["v/diag/v_long_k_0"],
         })
     write_table(path, ds)
     return ds
