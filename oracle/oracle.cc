@@ -1262,6 +1262,134 @@ struct IlkkaPairAction : PairAction {
     }
 };
 
+// src/actions/pair_action/david_pair_action_class.h:7-361. The squarer's expansion
+//   U = (u_00(r) + u_00(r'))/2 + sum_{k=1..n} sum_{j=0..k} u_kj(q) z^(2j) s^(2(k-j)),
+// q = (r + r')/2, z = r - r', on one radial grid; component 0 of every multi-spline is the potential.
+// Tables for the time step tau only (max_level 0, the setting of the reference's inputs).
+struct DavidPairAction : PairAction {
+    uint32_t n_order = 0, n_val = 0;
+    double r_min = 0., r_max = 0.;
+    double du_long_k_0 = 0., du_long_r_0 = 0., v_long_k_0 = 0., v_long_r_0 = 0.;
+    std::vector<double> u_long_k, du_long_k, v_long_k;
+    std::vector<Spline> u_kj, du_kj;  // n_val + 1 components
+
+    DavidPairAction(Path& p, const Input& in, const std::string& base_dir) : PairAction(p, in) {
+        n_order = in.GetAttribute<uint32_t>("n_order", 0);  // pair_action_class.h:208
+        if (max_level != 0) throw InputError("DavidPairAction: tables for one time step (max_level 0)");
+        std::string file = in.GetAttribute<std::string>("file");
+        if (!file.empty() && file[0] != '/' && !base_dir.empty()) file = base_dir + "/" + file;
+        TableFile t = TableFile::Load(file);
+        const std::string pre = "u_kj_" + std::to_string(n_order), dpre = "du_kj_dbeta_" + std::to_string(n_order);
+        const auto& grid = t.Vec(pre + "/grid/grid_points");  // :211-232 (a general grid)
+        const size_t n_grid = grid.size();
+        if ((size_t)t.Scalar(pre + "/grid/n_grid_points") != n_grid || n_grid < 2)
+            throw InputError("table '" + file + "': inconsistent grid");
+        r_min = grid.front();
+        r_max = grid.back();
+        const auto& taus = t.Vec(pre + "/taus");  // :234-246
+        bool found = false;
+        for (double x : taus) found |= std::fabs(x - p.tau) < 1.0e-6;
+        if (!found) throw InputError("table '" + file + "': tau of the path not found");
+        const auto& V = t.Vec("potential/data");
+        n_val = 1;
+        for (uint32_t i = 1; i <= n_order; ++i) n_val += 1 + i;  // :252-255
+        auto load = [&](const std::string& key, std::vector<Spline>& out) {  // :257-316
+            const auto& d = t.Vec(key);
+            if (d.size() < (size_t)n_val * n_grid || V.size() != n_grid) throw InputError("table '" + file + "': short " + key);
+            out.assign(n_val + 1, Spline());
+            std::vector<double> col(n_grid);
+            for (uint32_t v = 0; v <= n_val; ++v) {
+                for (size_t g = 0; g < n_grid; ++g) col[g] = v == 0 ? V[g] : d[(v - 1) + g * n_val];
+                out[v].Build(grid, col, false);
+            }
+        };
+        load(pre + "/data", u_kj);
+        load(dpre + "/data", du_kj);
+        if (use_long_range) {  // :318-357
+            const auto& kv = t.Vec("long_range/k_points");
+            const auto& uk = t.Vec("long_range/u_k");
+            const double vol = p.vol;
+            u_long_k.assign(p.ks.K(), 0.);
+            du_long_k.assign(p.ks.K(), 0.);
+            v_long_k.assign(p.ks.K(), 0.);
+            for (size_t i = 0; i < kv.size(); ++i) {
+                const double vk = uk[i] / vol;
+                if (fequal(0., kv[i], 1.e-8)) v_long_k_0 = vk;
+                for (size_t k = 0; k < p.ks.K(); ++k)
+                    if (fequal(p.ks.mags[k], kv[i], 1.e-8)) {
+                        u_long_k[k] = vk * p.tau;
+                        du_long_k[k] = vk;
+                        v_long_k[k] = vk;
+                    }
+            }
+            v_long_r_0 = t.Scalar("squarer/v_image");
+            du_long_r_0 = v_long_r_0;
+            du_long_k_0 = v_long_k_0;
+            if (species_a == species_b) {
+                du_long_k_0 *= 0.5 * species_a->n_part * species_b->n_part * p.n_bead;
+                du_long_r_0 *= -0.5 * species_a->n_part * p.n_bead;
+                v_long_k_0 *= 0.5 * species_a->n_part * species_b->n_part * p.n_bead;
+                v_long_r_0 *= -0.5 * species_a->n_part * p.n_bead;
+            } else {
+                du_long_k_0 *= species_a->n_part * species_b->n_part * p.n_bead;
+                du_long_r_0 *= 0.;
+                v_long_k_0 *= species_a->n_part * species_b->n_part * p.n_bead;
+                v_long_r_0 *= 0.;
+            }
+        }
+    }
+
+    double KSum(const std::vector<double>& coef, uint32_t b0, uint32_t b1, uint32_t skip) {
+        const auto& ra = path.GetRhoK(*species_a);
+        const auto& rb = path.GetRhoK(*species_b);
+        size_t K = path.ks.K();
+        double tot = 0.;
+        for (size_t k = 0; k < K; ++k)
+            for (uint32_t b = b0; b < b1; b += skip)
+                tot += coef[k] * CMag2(ra[(size_t)species_a->bead_loop(b) * K + k], rb[(size_t)species_b->bead_loop(b) * K + k]);
+        if (species_a != species_b) tot *= 2.;
+        return tot;
+    }
+
+    // Off-diagonal sum of the expansion at q with the coefficients of `comp` (:80-99, :146-163).
+    double OffDiagonal(const std::vector<Spline>& comp, double q, double z, double s) const {
+        double z2 = z * z, s2 = s * s, is2 = 1. / s2, s2k = s2, tot = 0.;
+        for (uint32_t k = 1; k <= n_order; ++k) {
+            double z2j = 1., cs = s2k;
+            for (uint32_t j = 0; j <= k; ++j) {
+                tot += comp[k * (k + 1) / 2 + j + 1].Eval(q) * z2j * cs;
+                z2j *= z2;
+                cs *= is2;
+            }
+            s2k *= s2;
+        }
+        return tot;
+    }
+
+    double CalcV(double r, double rp, uint32_t) override {  // :34-47
+        SetLimits(r_min, r_max, r, rp);
+        return 0.5 * (u_kj[0].Eval(r) + u_kj[0].Eval(rp));
+    }
+    double CalcVLong() override { return KSum(v_long_k, 0, path.n_bead, 1) + v_long_k_0 + v_long_r_0; }  // :50-66
+    double CalcU(double r, double rp, double s, uint32_t) override {  // :69-102
+        double q = 0.5 * (r + rp), z = r - rp;
+        SetLimits(r_min, r_max, r, rp);
+        double u = 0.5 * (u_kj[1].Eval(r) + u_kj[1].Eval(rp));
+        if (s > 0.0 && q < r_max) u += OffDiagonal(u_kj, q, z, s);
+        return u;
+    }
+    double CalcULong(uint32_t b0, uint32_t b1, uint32_t level) override { return KSum(u_long_k, b0, b1, 1u << level); }  // :105-123
+    double CalcdUdBeta(double r, double rp, double s, uint32_t) override {  // :126-167
+        double q = 0.5 * (r + rp), z = r - rp;
+        SetLimits(r_min, r_max, r, rp);
+        double v = 0.5 * (du_kj[0].Eval(r) + du_kj[0].Eval(rp));
+        double du = 0.5 * (du_kj[1].Eval(r) + du_kj[1].Eval(rp)) + v;
+        if (s > 0.0 && q < r_max) du += OffDiagonal(du_kj, q, z, s);
+        return du;
+    }
+    double CalcdUdBetaLong() override { return KSum(du_long_k, 0, path.n_bead, 1) + du_long_k_0 + du_long_r_0; }  // :170-186
+};
+
 // ---------------------------------------------------------------------------------------------
 // Moves: Bisect (src/events/moves/single_species_move/bisect/bisect_class.h:8-214).
 // ---------------------------------------------------------------------------------------------
@@ -1368,7 +1496,7 @@ static double WholeAction(Path& path, std::vector<std::unique_ptr<Action>>& acti
                     for (uint32_t c = 0; c < nd; ++c) r2 += r[c] * r[c];
                     total += t->cofactor_a * r2;
                 }
-        } else if (dynamic_cast<IlkkaPairAction*>(a)) {
+        } else if (dynamic_cast<IlkkaPairAction*>(a) || dynamic_cast<DavidPairAction*>(a)) {
             throw InputError("the whole-ring action covers Kinetic, HarmonicTrap and BarePairAction");
         } else if (auto* bp = dynamic_cast<BarePairAction*>(a)) {
             if (bp->is_constant) continue;
@@ -1429,7 +1557,7 @@ static void WholeGradient(Path& path, std::vector<std::unique_ptr<Action>>& acti
                     const double* r = RAt(path, R, s.offset + p, b);
                     for (uint32_t c = 0; c < nd; ++c) gat(s.offset + p, b)[c] += 2. * t->cofactor_a * r[c];
                 }
-        } else if (dynamic_cast<IlkkaPairAction*>(a)) {
+        } else if (dynamic_cast<IlkkaPairAction*>(a) || dynamic_cast<DavidPairAction*>(a)) {
             throw InputError("the whole-ring gradient covers Kinetic, HarmonicTrap and BarePairAction");
         } else if (auto* bp = dynamic_cast<BarePairAction*>(a)) {
             if (bp->is_constant) continue;
@@ -2009,6 +2137,7 @@ struct Simulation {
             else if (t == "HarmonicTrap") actions.emplace_back(new Trap(*path, a));
             else if (t == "BarePairAction") actions.emplace_back(new BarePairAction(*path, a, base_dir));
             else if (t == "IlkkaPairAction") actions.emplace_back(new IlkkaPairAction(*path, a, base_dir));
+            else if (t == "DavidPairAction") actions.emplace_back(new DavidPairAction(*path, a, base_dir));
             else throw InputError("unsupported action type '" + t + "'");
         }
         uint32_t mi = 0;
@@ -2035,6 +2164,10 @@ struct Simulation {
             if (a->type == "BarePairAction") {
                 auto* b = static_cast<BarePairAction*>(a.get());
                 if (b->use_long_range && b->v_long_k.size() != path->ks.K())
+                    throw InputError("k_cut of action '" + b->name + "' is below a later k_cut; order the largest first");
+            } else if (a->type == "DavidPairAction") {
+                auto* b = static_cast<DavidPairAction*>(a.get());
+                if (b->use_long_range && b->u_long_k.size() != path->ks.K())
                     throw InputError("k_cut of action '" + b->name + "' is below a later k_cut; order the largest first");
             } else if (a->type == "IlkkaPairAction") {
                 auto* b = static_cast<IlkkaPairAction*>(a.get());

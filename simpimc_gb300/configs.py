@@ -10,8 +10,9 @@ systems follow the reference's input format (inputs/*.xml): <System>, <Particles
   r_s, Coulomb split into a short-range primitive part and an Ewald long-range k-sum; beads
   uniform in the box.
 
-Both take ``pair="IlkkaPairAction"`` to use the off-diagonal pair action of a synthetic
-``tables.ilkka_table`` instead of the primitive BarePairAction.
+Both take ``pair="IlkkaPairAction"`` or ``pair="DavidPairAction"`` (with ``n_order``) to use the
+off-diagonal pair action of a synthetic ``tables.ilkka_table`` / ``tables.david_table`` instead of
+the primitive BarePairAction.
 """
 from __future__ import annotations
 
@@ -20,15 +21,21 @@ from pathlib import Path
 
 import numpy as np
 
-from .tables import coulomb_table, ilkka_table
+from .tables import coulomb_table, david_table, ilkka_table
 
 
 def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_level=3, seed=1234, coulomb=True,
                     n_step_inner=100, n_step_outer=10, gr_bins=200, gr_rmax=5.0, virial=False, path_seed=None,
-                    write_table=True, pair="BarePairAction"):
+                    write_table=True, pair="BarePairAction", n_order=2):
     workdir = Path(workdir)
     workdir.mkdir(parents=True, exist_ok=True)
-    if pair == "IlkkaPairAction":
+    if pair == "DavidPairAction":
+        tab = workdir / f"david_open_{n_bead}_{beta}_{n_order}.pat"
+        if write_table or not tab.exists():
+            david_table(tab, tau=beta / n_bead, n_order=n_order, lam=0.5, z_ab=1.0, L=0.0)
+        pair_xml = (f'<Action name="Coulomb" type="DavidPairAction" file="{tab.name}" n_order="{n_order}" species_a="e" '
+                    f'species_b="e" max_level="0" use_long_range="0" />')
+    elif pair == "IlkkaPairAction":
         tab = workdir / f"ilkka_open_{n_bead}_{beta}.pat"
         if write_table or not tab.exists():
             ilkka_table(tab, tau=beta / n_bead, lam=0.5, z_ab=1.0, L=0.0)
@@ -81,12 +88,16 @@ def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_leve
 
 
 def electron_gas(workdir, *, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_units=12.0, n_level=4, seed=4321,
-                 n_step_inner=10, n_step_outer=4, path_seed=None, structure_factor=False, pair="BarePairAction"):
+                 n_step_inner=10, n_step_outer=4, path_seed=None, structure_factor=False, pair="BarePairAction", n_order=2):
     workdir = Path(workdir)
     workdir.mkdir(parents=True, exist_ok=True)
     L = (4.0 * math.pi * n_part / 3.0) ** (1.0 / 3.0) * rs
     k_cut = k_cut_units * 2.0 * math.pi / L
-    if pair == "IlkkaPairAction":
+    if pair == "DavidPairAction":
+        tab = workdir / f"david_ewald_{n_part}_{rs}_{n_bead}_{beta}_{n_order}.pat"
+        david_table(tab, tau=beta / n_bead, n_order=n_order, lam=0.5, z_ab=1.0, L=L, k_cut=k_cut)
+        extra = f' n_order="{n_order}"'
+    elif pair == "IlkkaPairAction":
         tab = workdir / f"ilkka_ewald_{n_part}_{rs}_{n_bead}_{beta}.pat"
         ilkka_table(tab, tau=beta / n_bead, lam=0.5, z_ab=1.0, L=L, k_cut=k_cut)
         extra = ""

@@ -84,6 +84,14 @@ struct BicubicTable {
     const double* c = nullptr;
 };
 
+/// Components of a multi-spline on one grid (einspline's multi_NUBspline_1d_d): component m on
+/// interval i is c[i n_comp + m], a natural cubic spline as CubicTable.
+struct MultiCubic {
+    GridDev g;
+    const Cubic4* c = nullptr;
+    int32_t n_comp = 0;
+};
+
 /// Kinetic action of one species (src/actions/single_action/kinetic_class.h:10-169).
 struct KineticDev {
     uint32_t species = 0;
@@ -105,10 +113,13 @@ struct TrapDev {
 
 constexpr int32_t kPairBare = 0;   // BarePairAction (bare_pair_action_class.h:7-183)
 constexpr int32_t kPairIlkka = 1;  // IlkkaPairAction (ilkka_pair_action_class.h:7-433)
+constexpr int32_t kPairDavid = 2;  // DavidPairAction (david_pair_action_class.h:7-361)
 
-/// Pair action: the primitive BarePairAction, or IlkkaPairAction's off-diagonal action u(x, y) of
-/// x = q + s/2, y = q - s/2 (q = (|r| + |r'|)/2, s = |r - r'|) with its tau derivative. Both keep
-/// the potential tables v (Potential; and DActionDBeta of the bare action).
+/// Pair action: the primitive BarePairAction; IlkkaPairAction's off-diagonal action u(x, y) of
+/// x = q + s/2, y = q - s/2 (q = (|r| + |r'|)/2, s = |r - r'|) with its tau derivative; or
+/// DavidPairAction's expansion (u_00(r) + u_00(r'))/2 + sum_kj u_kj(q) z^2j s^2(k-j), z = r - r'.
+/// The bare and Ilkka actions keep the potential tables v (Potential; and DActionDBeta of the bare
+/// action); the David action's potential is component 0 of its multi-splines.
 struct PairDev {
     uint32_t sa = 0, sb = 0;
     int32_t kind = kPairBare;
@@ -123,8 +134,12 @@ struct PairDev {
     CubicTable u_long_r, du_long_r;
     double r_u_min = 0., r_u_max = 0., r_du_min = 0., r_du_max = 0.;
     double du_long_k_0 = 0., du_long_r_0 = 0.; // scaled as v_long_k_0 / v_long_r_0
-    const double* u_long_k = nullptr;          // [K]
-    const double* du_long_k = nullptr;         // [K]
+    const double* u_long_k = nullptr;          // [K] (also DavidPairAction)
+    const double* du_long_k = nullptr;         // [K] (also DavidPairAction)
+    // DavidPairAction only
+    MultiCubic u_kj, du_kj;                    // n_val + 1 components, component 0 the potential
+    uint32_t n_order = 0;
+    double r_d_min = 0., r_d_max = 0.;         // the grid's ends (GetLimits)
 };
 
 /// Bisection move (src/events/moves/single_species_move/bisect/bisect_class.h:8-214) with the

@@ -197,6 +197,13 @@ class Context {
         std::vector<int32_t> bx, by;
     };
     std::vector<std::pair<const double*, HostBicubic>> host_bicubics;
+    struct HostMulti {
+        std::vector<double> x;
+        std::vector<Cubic4> c;  // [interval][component]
+        std::vector<int32_t> bucket;
+        int32_t n_comp;
+    };
+    std::vector<std::pair<const Cubic4*, HostMulti>> host_multis;
     // Per pair action, the k-space coefficient of its long-range action: v_long_k for the bare action
     // (multiplied by tau 2^level there), u_long_k / tau for IlkkaPairAction (empty without long range).
     std::vector<std::vector<double>> host_vk;
@@ -228,6 +235,7 @@ class Context {
     void ReadLoop(const Input& in, LoopNode& node);
     CubicTable BuildCubic(const std::vector<double>& x, const std::vector<double>& y, bool uniform);
     BicubicTable BuildBicubic(const std::vector<double>& x, const std::vector<double>& y, const std::vector<double>& f);
+    MultiCubic BuildMultiCubic(const std::vector<double>& x, const std::vector<std::vector<double>>& comps);
     void FreeSplineTable(double L, uint32_t n_images, double lambda, double tau, bool want_dtau, CubicTable* image, CubicTable* dtau);
 
    public:

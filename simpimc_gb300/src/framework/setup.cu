@@ -231,6 +231,37 @@ BicubicTable Context::BuildBicubic(const std::vector<double>& x, const std::vect
     return t;
 }
 
+// Natural cubic splines of several components on one grid, interleaved per interval.
+MultiCubic Context::BuildMultiCubic(const std::vector<double>& x, const std::vector<std::vector<double>>& comps) {
+    const size_t n = x.size(), nc = comps.size();
+    if (n < 2 || nc == 0) throw PimcError(kErrInput, "multi-spline needs at least two knots and one component");
+    for (size_t i = 1; i < n; ++i)
+        if (!(x[i] > x[i - 1])) throw PimcError(kErrInput, "spline knots must increase");
+    std::vector<Cubic4> c((n - 1) * nc);
+    for (size_t m = 0; m < nc; ++m) {
+        const std::vector<double>& y = comps[m];
+        if (y.size() != n) throw PimcError(kErrInput, "multi-spline component of the wrong length");
+        const std::vector<double> mm = NaturalSecond(x, y);
+        for (size_t i = 0; i + 1 < n; ++i) {
+            const double h = x[i + 1] - x[i];
+            Cubic4& q = c[i * nc + m];
+            q.c0 = y[i];
+            q.c1 = (y[i + 1] - y[i]) / h - h * (2. * mm[i] + mm[i + 1]) / 6.;
+            q.c2 = 0.5 * mm[i];
+            q.c3 = (mm[i + 1] - mm[i]) / (6. * h);
+        }
+    }
+    MultiCubic t;
+    std::vector<int32_t> bk;
+    t.g = MakeGrid(x, bk);
+    t.g.x = Upload(x);
+    t.g.bucket = Upload(bk);
+    t.c = Upload(c);
+    t.n_comp = (int32_t)nc;
+    host_multis.push_back({t.c, HostMulti{x, c, bk, (int32_t)nc}});
+    return t;
+}
+
 // FreeSpline (src/actions/free_spline_class.h:25-68): periodic-image part of the free-particle
 // action on a 10000-point uniform grid spanning one box length (1000 for open boundaries).
 void Context::FreeSplineTable(double L, uint32_t n_images, double lambda, double tau, bool want_dtau, CubicTable* image,
@@ -365,7 +396,7 @@ void Context::BuildActions(const Input& in) {
     bool long_range_seen = false;
     for (const auto& a : alist) {
         const std::string ty = a.GetAttribute<std::string>("type");
-        if ((ty == "BarePairAction" || ty == "IlkkaPairAction") && a.GetAttribute<bool>("use_long_range", false)) {
+        if ((ty == "BarePairAction" || ty == "IlkkaPairAction" || ty == "DavidPairAction") && a.GetAttribute<bool>("use_long_range", false)) {
             if (!sys.pbc) throw PimcError(kErrInput, "use_long_range needs periodic boundaries");
             const double before = ks.cutoff;
             ks.Setup(a.GetAttribute<double>("k_cut", ks.cutoff), sys.L, sys.n_d);
@@ -483,6 +514,90 @@ void Context::BuildActions(const Input& in) {
                 vk0 *= (double)sys.sp_n[p.sa] * sys.sp_n[p.sb] * sys.M;
                 vr0 *= 0.;
             }
+            p.v_long_k_0 = vk0;
+            p.v_long_r_0 = vr0;
+            h.kind = 2;
+            h.index = sys.n_pair++;
+            h.species_list.push_back(p.sa);
+            h.species_list.push_back(p.sb);
+        } else if (h.type == "DavidPairAction") {
+            // david_pair_action_class.h:190-358
+            if (sys.n_pair >= kMaxPair) throw PimcError(kErrUnsupported, "too many pair actions");
+            if (max_level != 0) throw PimcError(kErrUnsupported, "DavidPairAction: tables for one time step (max_level 0)");
+            PairDev& p = sys.pair[sys.n_pair];
+            p.kind = kPairDavid;
+            p.sa = SpeciesIndex(species_names, a.GetAttribute<std::string>("species_a"));
+            p.sb = SpeciesIndex(species_names, a.GetAttribute<std::string>("species_b"));
+            p.max_level = max_level;
+            p.use_long_range = a.GetAttribute<bool>("use_long_range", false) ? 1 : 0;
+            p.is_coulomb = 0;
+            p.is_constant = (p.sa == p.sb) && (sys.sp_n[p.sa] == 1 || sys.sp_lambda[p.sa] == 0.);
+            p.n_order = a.GetAttribute<uint32_t>("n_order", 0);  // pair_action_class.h:208
+            std::string file = a.GetAttribute<std::string>("file");
+            if (!file.empty() && file[0] != '/' && !base_dir.empty()) file = base_dir + "/" + file;
+            TableFile tf = TableFile::Load(file);
+            const std::string pre = "u_kj_" + std::to_string(p.n_order), dpre = "du_kj_dbeta_" + std::to_string(p.n_order);
+            const auto& grid = tf.Vec(pre + "/grid/grid_points");
+            const size_t n_grid = grid.size();
+            if ((size_t)tf.Scalar(pre + "/grid/n_grid_points") != n_grid || n_grid < 2)
+                throw PimcError(kErrInput, "table '" + file + "': inconsistent grid");
+            bool found = false;
+            for (double t : tf.Vec(pre + "/taus")) found |= std::fabs(t - sys.tau) < 1.0e-6;
+            if (!found) throw PimcError(kErrInput, "table '" + file + "': tau of the path not found");
+            const auto& V = tf.Vec("potential/data");
+            uint32_t n_val = 1;
+            for (uint32_t i = 1; i <= p.n_order; ++i) n_val += 1 + i;
+            auto comps = [&](const std::string& key) {
+                const auto& d = tf.Vec(key);
+                if (d.size() < (size_t)n_val * n_grid || V.size() != n_grid) throw PimcError(kErrInput, "table '" + file + "': short " + key);
+                std::vector<std::vector<double>> out(n_val + 1, std::vector<double>(n_grid));
+                for (size_t g = 0; g < n_grid; ++g) {
+                    out[0][g] = V[g];
+                    for (uint32_t v = 1; v <= n_val; ++v) out[v][g] = d[(v - 1) + g * n_val];
+                }
+                return out;
+            };
+            p.u_kj = BuildMultiCubic(grid, comps(pre + "/data"));
+            p.du_kj = BuildMultiCubic(grid, comps(dpre + "/data"));
+            p.r_d_min = grid.front();
+            p.r_d_max = grid.back();
+            double vk0 = 0., vr0 = 0.;
+            if (p.use_long_range) {
+                const auto& kv = tf.Vec("long_range/k_points");
+                const auto& ukv = tf.Vec("long_range/u_k");
+                std::vector<double> uk(sys.K, 0.), duk(sys.K, 0.), vk(sys.K, 0.);
+                for (size_t i = 0; i < kv.size() && i < ukv.size(); ++i) {
+                    const double v = ukv[i] / sys.vol;
+                    if (std::fabs(kv[i]) < 1.e-8) vk0 = v;
+                    for (uint32_t k = 0; k < sys.K; ++k)
+                        if (std::fabs(kmags[k] - kv[i]) < 1.e-8) {
+                            uk[k] = v * sys.tau;
+                            duk[k] = v;
+                            vk[k] = v;
+                        }
+                }
+                vr0 = tf.Scalar("squarer/v_image");
+                p.u_long_k = Upload(uk);
+                p.du_long_k = Upload(duk);
+                p.v_long_k = Upload(vk);
+                host_vk.resize(sys.n_pair + 1);
+                host_vk[sys.n_pair] = vk;  // u_long_k / tau
+                sys.sp_rho[p.sa] = sys.sp_rho[p.sb] = 0;  // marked; slots assigned below
+            }
+            double dk0 = vk0, dr0 = vr0;
+            if (p.sa == p.sb) {  // :340-356
+                dk0 *= 0.5 * sys.sp_n[p.sa] * sys.sp_n[p.sb] * sys.M;
+                dr0 *= -0.5 * sys.sp_n[p.sa] * sys.M;
+                vk0 *= 0.5 * sys.sp_n[p.sa] * sys.sp_n[p.sb] * sys.M;
+                vr0 *= -0.5 * sys.sp_n[p.sa] * sys.M;
+            } else {
+                dk0 *= (double)sys.sp_n[p.sa] * sys.sp_n[p.sb] * sys.M;
+                dr0 *= 0.;
+                vk0 *= (double)sys.sp_n[p.sa] * sys.sp_n[p.sb] * sys.M;
+                vr0 *= 0.;
+            }
+            p.du_long_k_0 = dk0;
+            p.du_long_r_0 = dr0;
             p.v_long_k_0 = vk0;
             p.v_long_r_0 = vr0;
             h.kind = 2;

@@ -5,9 +5,44 @@
 
 namespace pimc {
 
-/// BarePairAction::CalcV (bare_pair_action_class.h:99-123): clamp to the table grid, Coulomb or
-/// spline short-range part, minus the long-range spline when the action has an Ewald part.
+/// DavidPairAction: the endpoint terms of component `diag` at r and r' (clamped to the grid), plus
+/// the off-diagonal expansion sum_{k=1..n} sum_{j=0..k} c_kj(q) z^2j s^2(k-j) at q = (r + r')/2
+/// (clamped) when s > 0 and q < r_max (david_pair_action_class.h:69-102, 126-167). With `add_v` the
+/// potential's endpoint terms (component 0) are added, as CalcdUdBeta does.
+__device__ __forceinline__ double DavidLink(const PairDev& pa, const MultiCubic& t, double r, double rp, double s, bool add_v) {
+    const double q = 0.5 * (r + rp), z = r - rp;
+    double ur, urp;
+    const int i = MultiInterval(t, r, ur), ip = MultiInterval(t, rp, urp);
+    double u = 0.5 * (MultiComp(t, i, ur, 1) + MultiComp(t, ip, urp, 1));
+    if (add_v) u += 0.5 * (MultiComp(t, i, ur, 0) + MultiComp(t, ip, urp, 0));
+    if (s > 0. && q < pa.r_d_max) {
+        double uq;
+        const int iq = MultiInterval(t, q, uq);
+        const double z2 = z * z, s2 = s * s, is2 = 1. / s2;
+        double s2k = s2;
+        for (uint32_t k = 1; k <= pa.n_order; ++k) {
+            double z2j = 1., cs = s2k;
+            for (uint32_t j = 0; j <= k; ++j) {
+                u += MultiComp(t, iq, uq, (int)(k * (k + 1) / 2 + j + 1)) * z2j * cs;
+                z2j *= z2;
+                cs *= is2;
+            }
+            s2k *= s2;
+        }
+    }
+    return u;
+}
+
+/// CalcV of a link. BarePairAction::CalcV (bare_pair_action_class.h:99-123): clamp to the table
+/// grid, Coulomb or spline short-range part, minus the long-range spline when the action has an
+/// Ewald part; IlkkaPairAction::CalcV is the same with its tables (ilkka_pair_action_class.h:34-54);
+/// DavidPairAction::CalcV is the potential component at both ends (david_pair_action_class.h:34-47).
 __device__ __forceinline__ double PairV(const PairDev& pa, double r, double rp) {
+    if (pa.kind == kPairDavid) {
+        double ur, urp;
+        const int i = MultiInterval(pa.u_kj, r, ur), ip = MultiInterval(pa.u_kj, rp, urp);
+        return 0.5 * (MultiComp(pa.u_kj, i, ur, 0) + MultiComp(pa.u_kj, ip, urp, 0));
+    }
     r = fmin(fmax(r, pa.r_v_min), pa.r_v_max);
     rp = fmin(fmax(rp, pa.r_v_min), pa.r_v_max);
     double v = 0.;
@@ -31,7 +66,10 @@ __device__ __forceinline__ double PairV(const PairDev& pa, double r, double rp) 
 ///    tau at level 0 and zero above; that behaviour is kept.
 ///  * IlkkaPairAction (ilkka_pair_action_class.h:77-101): u(q + s/2, q - s/2), q = (r + r')/2, minus
 ///    half the long-range action at each end (clamped to its grid) when the action has an Ewald part.
+///  * DavidPairAction (david_pair_action_class.h:69-102): DavidLink of its action components; the
+///    tables are for the time step tau (max_level 0).
 __device__ __forceinline__ double PairU(const PairDev& pa, double r, double rp, double s, uint32_t level, double tau) {
+    if (pa.kind == kPairDavid) return DavidLink(pa, pa.u_kj, r, rp, s, false);
     if (pa.kind == kPairIlkka) {
         const double q = 0.5 * (r + rp);
         double u = EvalBicubic(pa.u_xy, q + 0.5 * s, q - 0.5 * s);
@@ -50,6 +88,7 @@ __device__ __forceinline__ double PairU(const PairDev& pa, double r, double rp, 
 /// du(q + s/2, q - s/2) minus half the long-range du at each end for IlkkaPairAction
 /// (ilkka_pair_action_class.h:125-149).
 __device__ __forceinline__ double PairdUdBeta(const PairDev& pa, double r, double rp, double s) {
+    if (pa.kind == kPairDavid) return DavidLink(pa, pa.du_kj, r, rp, s, true);
     if (pa.kind == kPairIlkka) {
         const double q = 0.5 * (r + rp);
         double du = EvalBicubic(pa.du_xy, q + 0.5 * s, q - 0.5 * s);

@@ -118,6 +118,20 @@ __device__ __forceinline__ double EvalBicubic(const BicubicTable& t, double x, d
     return row[0] + u * (row[1] + u * (row[2] + u * row[3]));
 }
 
+/// Component m of a MultiCubic on interval i at offset u from the interval's knot.
+__device__ __forceinline__ double MultiComp(const MultiCubic& t, int i, double u, int m) {
+    const Cubic4 c = t.c[(size_t)i * t.n_comp + m];
+    return c.c0 + u * (c.c1 + u * (c.c2 + u * c.c3));
+}
+
+/// Interval of a MultiCubic holding x clamped to the grid, and the offset from its knot.
+__device__ __forceinline__ int MultiInterval(const MultiCubic& t, double x, double& u) {
+    x = fmin(fmax(x, t.g.x0), t.g.x1);
+    const int i = GridCell(t.g, x);
+    u = x - __ldg(&t.g.x[i]);
+    return i;
+}
+
 /// Free-particle log density with periodic-image correction (free_spline_class.h:189-197):
 /// -sum_d image(dr_d) - |dr|^2 / (4 lambda tau).
 __device__ __forceinline__ double LogRhoFree(const double* dr, uint32_t n_d, double i4lt, const CubicTable* image, int has_images) {

@@ -357,8 +357,9 @@ double Context::GetAction(uint32_t ai, uint32_t b0, uint32_t b1, const uint32_t*
         }
         const double2* rho = sys.rho_k;
         const int slot_a = sys.sp_rho[pa.sa], slot_b = sys.sp_rho[pa.sb];
-        // bare: tau 2^level v_long_k (bare_pair_action_class.h:126-144); Ilkka: u_long_k (ilkka_pair_action_class.h:104-122)
-        const double* vk = pa.kind == kPairIlkka ? pa.u_long_k : pa.v_long_k;
+        // bare: tau 2^level v_long_k (bare_pair_action_class.h:126-144); Ilkka and David: u_long_k
+        // (ilkka_pair_action_class.h:104-122, david_pair_action_class.h:105-123)
+        const double* vk = pa.kind != kPairBare ? pa.u_long_k : pa.v_long_k;
         double lr = 0.;
         SumItems<1>(*this, (uint64_t)K * ns, [=] __device__(uint64_t i, double* v) {
             const uint32_t k = (uint32_t)(i / ns), j = (uint32_t)(i % ns);
@@ -374,7 +375,7 @@ double Context::GetAction(uint32_t ai, uint32_t b0, uint32_t b1, const uint32_t*
             v[0] = vk[k] * (a.x * c.x + a.y * c.y);
         }, &lr);
         if (pa.sa != pa.sb) lr *= 2.;
-        tot += pa.kind == kPairIlkka ? lr : skip * sys.tau * lr;
+        tot += pa.kind != kPairBare ? lr : skip * sys.tau * lr;
     }
     return tot;
 }
@@ -585,8 +586,9 @@ double Context::DActionDBeta(uint32_t ai) {
         v[0] = PairdUdBeta(pa, r, rp, s);
     }, &out);
     if (pa.use_long_range) {
-        // bare: CalcVLong (bare_pair_action_class.h:126-144); Ilkka: CalcdUdBetaLong (ilkka_pair_action_class.h:152-169)
-        const bool ilkka = pa.kind == kPairIlkka;
+        // bare: CalcVLong (bare_pair_action_class.h:126-144); Ilkka and David: CalcdUdBetaLong
+        // (ilkka_pair_action_class.h:152-169, david_pair_action_class.h:170-186)
+        const bool ilkka = pa.kind != kPairBare;
         const uint32_t K = sys.K;
         const double2* ra = sys.rho_k + (size_t)sys.sp_rho[pa.sa] * M * K;
         const double2* rb = sys.rho_k + (size_t)sys.sp_rho[pa.sb] * M * K;

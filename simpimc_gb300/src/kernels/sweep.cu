@@ -59,6 +59,17 @@ struct BicubicDD {
     dd x0{0.f, 0.f}, x1{0.f, 0.f}, y0{0.f, 0.f}, y1{0.f, 0.f};
 };
 
+/// Double-float MultiCubic: knots (hi, lo); per interval and component two float4 of (hi, lo)
+/// pairs, (c0, c1) and (c2, c3).
+struct MultiCubicDD {
+    const float2* x = nullptr;
+    const int32_t* bucket = nullptr;
+    const float4* c = nullptr;
+    int32_t n = 0, n_bucket = 0, n_comp = 0, pad = 0;
+    float x0f = 0.f, inv_dxf = 0.f;
+    dd x0{0.f, 0.f}, x1{0.f, 0.f};
+};
+
 struct PairDD {
     uint32_t sa, sb;
     int32_t kind, is_coulomb, use_lr, is_constant, max_level;
@@ -70,6 +81,9 @@ struct PairDD {
     BicubicDD u_xy;
     CubicDD u_long_r;
     dd rumin, rumax;
+    // DavidPairAction
+    MultiCubicDD u_kj;
+    uint32_t n_order;
 };
 
 constexpr int kMoveKinetic = 2;
@@ -204,6 +218,38 @@ __device__ __forceinline__ dd EvalBicubicDD(const BicubicDD& t, dd x, dd y) {
         acc = a == 3 ? row : Add(row, Mul(u, acc));
     }
     return acc;
+}
+
+/// Interval of a MultiCubicDD holding x clamped to the grid, and the offset from its knot.
+__device__ __forceinline__ int MultiIntervalDD(const MultiCubicDD& t, dd x, dd& u) {
+    x = Min(Max(x, t.x0), t.x1);
+    const int i = GridCellDD(t.x, t.bucket, t.n, t.n_bucket, t.x0f, t.inv_dxf, t.x0, t.x1, x);
+    u = Sub(x, LoadDD(&t.x[i]));
+    return i;
+}
+
+__device__ __forceinline__ dd MultiCompDD(const MultiCubicDD& t, int i, dd u, int m) {
+    const float4 a = t.c[2 * ((size_t)i * t.n_comp + m)], b = t.c[2 * ((size_t)i * t.n_comp + m) + 1];
+    const dd v = Add(dd{a.z, a.w}, Mul(u, Add(dd{b.x, b.y}, Mul(u, dd{b.z, b.w}))));
+    return Add(dd{a.x, a.y}, Mul(u, v));
+}
+
+/// DavidPairAction::CalcU's off-diagonal expansion at q (david_pair_action_class.h:80-99).
+__device__ __forceinline__ dd DavidOffDiagDD(const PairDD& pa, dd q, dd z, dd s) {
+    dd uq;
+    const int iq = MultiIntervalDD(pa.u_kj, q, uq);
+    const dd z2 = Sqr(z), s2 = Sqr(s), is2 = Div(DD(1.f), s2);
+    dd s2k = s2, tot{0.f, 0.f};
+    for (uint32_t k = 1; k <= pa.n_order; ++k) {
+        dd z2j = DD(1.f), cs = s2k;
+        for (uint32_t j = 0; j <= k; ++j) {
+            tot = Add(tot, Mul(Mul(MultiCompDD(pa.u_kj, iq, uq, (int)(k * (k + 1) / 2 + j + 1)), z2j), cs));
+            z2j = Mul(z2j, z2);
+            cs = Mul(cs, is2);
+        }
+        s2k = Mul(s2k, s2);
+    }
+    return tot;
 }
 
 /// Sum over dimensions of the image-spline values.
@@ -399,8 +445,19 @@ __device__ __forceinline__ dd PairLinkU4(const PairDD* s_pairs, const MoveDD& mv
     bool ilkka = false;
     if (valid) {
         const PairDD& pa = s_pairs[mv.pair[pi]];
-        ilkka = pa.kind == kPairIlkka;
-        if (!ilkka) {
+        ilkka = pa.kind != kPairBare;  // tables hold the action itself: no tau factor
+        if (pa.kind == kPairDavid) {
+            // endpoint terms on lanes 0 and 1, the off-diagonal expansion on lane 2 (david_pair_action_class.h:69-102)
+            const dd r = Sqrt(rv2), rp = Sqrt(rq2);
+            if (ql < 2) {
+                dd u;
+                const int i = MultiIntervalDD(pa.u_kj, ql == 0 ? r : rp, u);
+                f = Scale2(MultiCompDD(pa.u_kj, i, u, 1), 0.5f);
+            } else if (ql == 2) {
+                const dd sl = Sqrt(ss2), q = Scale2(Add(r, rp), 0.5f);
+                if (sl.hi > 0.f && Less(q, pa.u_kj.x1)) f = DavidOffDiagDD(pa, q, Sub(r, rp), sl);
+            }
+        } else if (!ilkka) {
             if (ql < 2) f = PairHalfV(pa, Sqrt(ql == 0 ? rv2 : rq2));
         } else if (ql == 0) {
             const dd r = Sqrt(rv2), rp = Sqrt(rq2), sl = Sqrt(ss2);
@@ -522,7 +579,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                 link_off[pi] = n_links;
                 if (!pa.is_constant) {
                     grid_work = true;
-                    ext_links |= pa.kind == kPairIlkka;
+                    ext_links |= pa.kind != kPairBare;
                     const uint32_t other = pa.sa == pa.sb ? s : (pa.sa == s ? pa.sb : pa.sa);
                     n_links += (pa.sa == pa.sb ? a.sp_n[s] - 1 : a.sp_n[other]) * B;
                 }
@@ -1177,6 +1234,46 @@ static CubicDD MakeCubicDD(Context& c, const CubicTable& t, std::vector<std::uni
     return o;
 }
 
+static MultiCubicDD MakeMultiCubicDD(Context& c, const MultiCubic& t, std::vector<std::unique_ptr<DeviceBuffer>>& keep) {
+    MultiCubicDD o;
+    if (!t.c) return o;
+    const Context::HostMulti* h = nullptr;
+    for (auto& kv : c.host_multis)
+        if (kv.first == t.c) h = &kv.second;
+    if (!h) throw PimcError(kErrState, "multi-spline table without host copy");
+    std::vector<float2> x(h->x.size());
+    for (size_t i = 0; i < x.size(); ++i) {
+        float hi, lo;
+        SplitDouble(h->x[i], hi, lo);
+        x[i] = make_float2(hi, lo);
+    }
+    std::vector<float4> cf(2 * h->c.size());
+    for (size_t i = 0; i < h->c.size(); ++i) {
+        float a0, a1, b0, b1, c0, c1, d0, d1;
+        SplitDouble(h->c[i].c0, a0, a1);
+        SplitDouble(h->c[i].c1, b0, b1);
+        SplitDouble(h->c[i].c2, c0, c1);
+        SplitDouble(h->c[i].c3, d0, d1);
+        cf[2 * i] = make_float4(a0, a1, b0, b1);
+        cf[2 * i + 1] = make_float4(c0, c1, d0, d1);
+    }
+    keep.emplace_back(new DeviceBuffer(x.size() * sizeof(float2)));
+    CudaCheck(cudaMemcpy(keep.back()->ptr, x.data(), x.size() * sizeof(float2), cudaMemcpyHostToDevice), "dd knots");
+    o.x = keep.back()->as<float2>();
+    keep.emplace_back(new DeviceBuffer(cf.size() * sizeof(float4)));
+    CudaCheck(cudaMemcpy(keep.back()->ptr, cf.data(), cf.size() * sizeof(float4), cudaMemcpyHostToDevice), "dd coefficients");
+    o.c = keep.back()->as<float4>();
+    o.bucket = t.g.bucket;
+    o.n = t.g.n;
+    o.n_bucket = t.g.n_bucket;
+    o.n_comp = t.n_comp;
+    o.x0f = (float)t.g.x0;
+    o.inv_dxf = (float)t.g.inv_dx;
+    Split(t.g.x0, o.x0);
+    Split(t.g.x1, o.x1);
+    return o;
+}
+
 static BicubicDD MakeBicubicDD(Context& c, const BicubicTable& t, std::vector<std::unique_ptr<DeviceBuffer>>& keep) {
     BicubicDD o;
     if (!t.c) return o;
@@ -1272,6 +1369,9 @@ void Context::BuildSweepTables() {
         q.u_xy = BicubicDD();
         q.u_long_r = CubicDD();
         q.rumin = q.rumax = dd{0.f, 0.f};
+        q.u_kj = MultiCubicDD();
+        q.n_order = p.n_order;
+        if (p.kind == kPairDavid) q.u_kj = MakeMultiCubicDD(*this, p.u_kj, keep_);
         if (p.kind == kPairIlkka) {
             q.u_xy = MakeBicubicDD(*this, p.u_xy, keep_);
             if (p.use_long_range) q.u_long_r = make(p.u_long_r);
@@ -1296,9 +1396,9 @@ void Context::BuildSweepTables() {
     // Tables worth staging in shared memory: the pair actions' spline tables, once each.
     stage_tables_.clear();
     for (int i = 0; i < sys.n_pair; ++i) {
-        const bool ilkka = pd[i].kind == kPairIlkka;
+        const bool bare = pd[i].kind == kPairBare, ilkka = pd[i].kind == kPairIlkka;
         const CubicDD* ts[3] = {&pd[i].v_long_r, &pd[i].v_r, &pd[i].u_long_r};
-        const bool used[3] = {!ilkka && pd[i].use_lr != 0, !ilkka && pd[i].is_coulomb == 0, ilkka && pd[i].use_lr != 0};
+        const bool used[3] = {bare && pd[i].use_lr != 0, bare && pd[i].is_coulomb == 0, ilkka && pd[i].use_lr != 0};
         for (int j = 0; j < 3; ++j) {
             if (!used[j] || !ts[j]->x) continue;
             bool seen = false;

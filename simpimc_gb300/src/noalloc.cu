@@ -245,7 +245,7 @@ double GetActionNoAlloc(pimc::Context& c, uint32_t ai, uint32_t b0, uint32_t b1,
         }
         const double2* rho = sys.rho_k;
         const int slot_a = sys.sp_rho[pa.sa], slot_b = sys.sp_rho[pa.sb];
-        const double* vk = pa.kind == pimc::kPairIlkka ? pa.u_long_k : pa.v_long_k;
+        const double* vk = pa.kind != pimc::kPairBare ? pa.u_long_k : pa.v_long_k;
         double lr = NoAllocSum(c, (uint64_t)K * ns, [=] __device__(uint64_t i) -> double {
             const uint32_t k = (uint32_t)(i / ns), j = (uint32_t)(i % ns);
             double2 a, b;
@@ -260,7 +260,7 @@ double GetActionNoAlloc(pimc::Context& c, uint32_t ai, uint32_t b0, uint32_t b1,
             return vk[k] * (a.x * b.x + a.y * b.y);
         }, partials, max_blocks, result);
         if (pa.sa != pa.sb) lr *= 2.;
-        tot += pa.kind == pimc::kPairIlkka ? lr : skip * sys.tau * lr;
+        tot += pa.kind != pimc::kPairBare ? lr : skip * sys.tau * lr;
     }
     return tot;
 }

@@ -24,7 +24,7 @@ from pathlib import Path
 
 import numpy as np
 
-__all__ = ["write_table", "coulomb_table", "ilkka_table", "lattice_k_magnitudes", "ewald_alpha"]
+__all__ = ["write_table", "coulomb_table", "ilkka_table", "david_table", "lattice_k_magnitudes", "ewald_alpha"]
 
 
 def write_table(path, datasets: dict) -> None:
@@ -148,6 +148,68 @@ def ilkka_table(path, *, tau: float, lam: float = 0.5, z_ab: float = 1.0, L: flo
             "du/diag/du_long_r": v["v/diag/v_long_r"], "du/diag/du_long_r_0": v["v/diag/v_long_r_0"],
             "du/diag/n_k": v["v/diag/n_k"], "du/diag/k": v["v/diag/k"],
             "du/diag/du_long_k": v["v/diag/v_long_k"], "du/diag/du_long_k_0": v["v/diag/v_long_k_0"],
+        })
+    write_table(path, ds)
+    return ds
+
+
+def david_table(path, *, tau: float, n_order: int = 2, lam: float = 0.5, z_ab: float = 1.0, L: float = 0.0,
+                k_cut: float = 0.0, n_d: int = 3, n_grid: int = 200, r_max: float | None = None,
+                alpha: float | None = None) -> dict:
+    """Write a DavidPairAction table (src/actions/pair_action/david_pair_action_class.h:190-358).
+
+    The squarer that writes these tables is not part of the reference, so the table is synthetic:
+    a smeared Coulomb potential V(r) = z erf(r / a) / r (a = sqrt(4 lambda tau)), the diagonal action
+    u_00(r) = tau V(r) + tau^2 w(r) with w(r) = z exp(-r^2 / a^2) / (2 a), and off-diagonal
+    coefficients u_kj(q) = tau^k c_kj V(q) / a^(2k) (k = 1..n_order, j = 0..k, c_kj = (-1)^(k+j)
+    / (4^k (j + 1))) of the expansion sum_kj u_kj z^(2j) s^(2(k-j)). The beta derivatives are the
+    tau derivatives at fixed a, with the potential taken out of the diagonal one as in the
+    reference's files (du_00 - V). Datasets, with ``n = n_order``:
+
+    * ``u_kj_n/grid/{start, end, n_grid_points, grid_points}``: a general grid (the reference also
+      reads LOG, LINEAR and LOGLIN grid types, whose knots the points give);
+    * ``u_kj_n/taus``, ``potential/data``;
+    * ``u_kj_n/data`` and ``du_kj_dbeta_n/data``: n_val x n_grid x n_tau values, value index
+      fastest (Armadillo's cube order), n_val = sum_{i=0..n} (i + 1);
+    * with ``L > 0`` and ``k_cut > 0``: ``long_range/{k_cut, n_k, k_points, u_k}`` (V u_k is the
+      k-space Ewald potential, listed with k = 0 for its constant) and ``squarer/v_image``.
+    """
+    a = math.sqrt(4.0 * lam * tau)
+    if r_max is None:
+        r_max = math.sqrt(n_d) * L / 2.0 if L > 0 else 20.0
+    t = np.linspace(0.0, 1.0, n_grid)
+    r = 1.0e-3 + (r_max - 1.0e-3) * t ** 2
+    erf = np.vectorize(math.erf)
+    V = z_ab * erf(r / a) / r
+    w = z_ab * np.exp(-(r / a) ** 2) / (2.0 * a)
+    n_val = sum(i + 1 for i in range(n_order + 1))
+    u = np.zeros((n_val, n_grid))
+    du = np.zeros((n_val, n_grid))
+    u[0] = tau * V + tau * tau * w
+    du[0] = 2.0 * tau * w  # d u_00 / d tau - V
+    for k in range(1, n_order + 1):
+        for j in range(k + 1):
+            c = (-1.0) ** (k + j) / (4.0 ** k * (j + 1))
+            idx = k * (k + 1) // 2 + j
+            u[idx] = tau ** k * c * V / a ** (2 * k)
+            du[idx] = k * tau ** (k - 1) * c * V / a ** (2 * k)
+    pre = f"u_kj_{n_order}"
+    ds = {
+        f"{pre}/grid/start": r[0], f"{pre}/grid/end": r[-1], f"{pre}/grid/n_grid_points": n_grid, f"{pre}/grid/grid_points": r,
+        f"{pre}/taus": tau, "potential/data": V,
+        f"{pre}/data": u.T.ravel(),  # value index fastest
+        f"du_kj_dbeta_{n_order}/data": du.T.ravel(),
+    }
+    if L > 0 and k_cut > 0:
+        al = ewald_alpha(L, k_cut) if alpha is None else alpha
+        vol = L ** n_d
+        k = lattice_k_magnitudes(L, k_cut, n_d)
+        uk = z_ab * 4.0 * math.pi * np.exp(-k * k / (4.0 * al * al)) / (k * k)  # divided by V at load
+        ds.update({
+            "long_range/k_cut": k_cut, "long_range/n_k": k.size + 1,
+            "long_range/k_points": np.concatenate([[0.0], k]),
+            "long_range/u_k": np.concatenate([[-z_ab * math.pi / (al * al)], uk]),
+            "squarer/v_image": z_ab * 2.0 * al / math.sqrt(math.pi),
         })
     write_table(path, ds)
     return ds
