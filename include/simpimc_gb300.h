@@ -122,6 +122,13 @@ int pimc_observable_block(pimc_ctx* ctx, uint32_t observable, double* out, size_
 /* Simulation::Run (simulation_class.h:42-45): the XML <Algorithm> loop. Block values are kept
  * per observable and read back with pimc_get_block. */
 int pimc_run(pimc_ctx* ctx);
+/* The run's output so far (every Write event's move counters and observable blocks, and the path
+ * dumps of PathDump observables) under the reference's HDF5 dataset paths (Moves/<name>/...,
+ * Observables/<name>/..., Observables/<path dump>/<species>/{n_dump, positions, permutation};
+ * move_class.h:45-53, observable_class.h:79-88, path_dump_class.h:28-66), written in the table
+ * container format. A species with init_type="Restart" prefix="P" reads the last path dump of
+ * P.0.pat (P.<chain>.pat with parallel="1") at creation (species_class.h:336-377). */
+int pimc_write_output(pimc_ctx* ctx, const char* path);
 int pimc_n_blocks(pimc_ctx* ctx, uint32_t observable, size_t* n);
 int pimc_get_block(pimc_ctx* ctx, uint32_t observable, size_t block, double* out, size_t cap, size_t* n);
 

@@ -76,6 +76,7 @@ SIGNATURES = {
     "pimc_observable_accumulate": (C.c_int, [_P, C.c_uint32]),
     "pimc_observable_block": (C.c_int, [_P, C.c_uint32, _DP, C.c_size_t, _SZP]),
     "pimc_run": (C.c_int, [_P]),
+    "pimc_write_output": (C.c_int, [_P, C.c_char_p]),
     "pimc_n_blocks": (C.c_int, [_P, C.c_uint32, _SZP]),
     "pimc_get_block": (C.c_int, [_P, C.c_uint32, C.c_size_t, _DP, C.c_size_t, _SZP]),
     "pimc_synchronize": (C.c_int, [_P]),
@@ -324,6 +325,11 @@ class Simulation:
 
     def run(self):
         self._check(self._lib.pimc_run(self._h))
+
+    def write_output(self, path) -> None:
+        """Write the run's output (the reference's dataset paths) to `path`; read it with
+        simpimc_gb300.tables.read_table."""
+        self._check(self._lib.pimc_write_output(self._h, os.fsencode(str(path))))
 
     def blocks(self, obs: int, cap: int = 1 << 20) -> list[np.ndarray]:
         n = C.c_size_t()

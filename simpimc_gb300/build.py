@@ -25,6 +25,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--extended-lambda", "-Xcompiler
 SOURCES = [
     SRC / "capi.cu",
     SRC / "framework" / "setup.cu",
+    SRC / "framework" / "output.cu",
     SRC / "kernels" / "estimators.cu",
     SRC / "kernels" / "sweep.cu",
     SRC / "kernels" / "batch.cu",

@@ -216,6 +216,11 @@ int pimc_run(pimc_ctx* ctx) {
     return Guard(ctx, [&](pimc::Context& c) { c.Run(); });
 }
 
+int pimc_write_output(pimc_ctx* ctx, const char* path) {
+    if (!path) return PIMC_ERR_ARG;
+    return Guard(ctx, [&](pimc::Context& c) { c.WriteOutput(path); });
+}
+
 int pimc_n_blocks(pimc_ctx* ctx, uint32_t observable, size_t* n) {
     if (!n) return PIMC_ERR_ARG;
     return Guard(ctx, [&](pimc::Context& c) {

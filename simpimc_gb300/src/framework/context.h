@@ -72,6 +72,9 @@ struct MoveHost {
     double last_ratio = 0.;      // acceptance ratio of the last completed block
     uint64_t total_accept = 0;   // accepted attempts since construction
     uint64_t total_level0 = 0;   // attempts whose proposal reached the level-0 evaluation
+    // Per Write event (move_class.h:296-310, bisect_class.h:193-213): the block's counters, its
+    // acceptance ratio and the bisection level in force.
+    std::vector<double> out_attempt, out_accept, out_ratio, out_level;
     // Hybrid Monte Carlo move (no reference counterpart): leapfrog on the whole path driven by
     // the adjoint gradient of the total action.
     int kind = 0;                // 0 Bisect, 1 HMC
@@ -82,7 +85,7 @@ struct MoveHost {
 
 struct ObservableHost {
     std::string name, type;
-    int kind = 0;  // 0 energy, 1 pair correlation, 2 structure factor, 3 ignored bookkeeping
+    int kind = 0;  // 0 energy, 1 pair correlation, 2 structure factor, 3 ignored bookkeeping, 4 path dump
     uint64_t n_measure = 0;
     // Energy (energy_class.h:7-326)
     bool measure_potential = false, use_thermal = true, use_virial = false;
@@ -96,6 +99,11 @@ struct ObservableHost {
     // StructureFactor (structure_factor_class.h:7-212)
     double k_cut = 0.;
     std::unique_ptr<DeviceBuffer> sk;    // double [K]
+    // PathDump (path_dump_class.h:7-70): every `skip`-th Write stores each species' positions as
+    // the reference's cube (n_d, n_bead, n_part), column-major, and its permutation (2, n_part).
+    uint32_t skip = 1;
+    uint64_t n_write_calls = 0;
+    std::vector<std::vector<std::vector<double>>> dumps;  // [species][dump] positions
 };
 
 struct LoopNode {
@@ -161,6 +169,16 @@ class Context {
     bool phase_timing = false;  // record per-phase cycles of block 0 in the sweep kernel
     std::unique_ptr<DeviceBuffer> phase_buf;  // unsigned long long [kSweepPhases]
     std::vector<std::string> species_names;
+    // Species initialised from a previous run's path dump (species_class.h:336-377).
+    struct RestartSpec {
+        uint32_t species;
+        std::string file, dump_name;
+    };
+    std::vector<RestartSpec> restarts;
+    void ApplyRestarts();
+    /// The run's output under the reference's dataset paths (Moves/*, Observables/*) in the table
+    /// container format.
+    void WriteOutput(const std::string& path);
     std::vector<ActionHost> actions;
     std::vector<MoveHost> moves;
     std::vector<ObservableHost> observables;

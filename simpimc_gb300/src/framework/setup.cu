@@ -318,6 +318,13 @@ void Context::BuildPath(const Input& in) {
         if (s.GetAttribute<bool>("fermi", false) || s.GetAttribute<bool>("fixed_node", false))
             throw PimcError(kErrUnsupported, "fermion / fixed-node species are not supported");
         species_names.push_back(s.GetAttribute<std::string>("name"));
+        if (s.GetAttribute<std::string>("init_type", "") == "Restart") {
+            // species_class.h:336-345: <prefix>.<proc>.h5 in the reference; the table container here
+            std::string file = s.GetAttribute<std::string>("prefix") + "." +
+                               std::to_string(s.GetAttribute<bool>("parallel", false) ? chain : 0u) + ".pat";
+            if (!file.empty() && file[0] != '/' && !base_dir.empty()) file = base_dir + "/" + file;
+            restarts.push_back(RestartSpec{sys.S, file, s.GetAttribute<std::string>("path_dump_name", "path_dump")});
+        }
         sys.sp_off[sys.S] = sys.n_total;
         sys.sp_n[sys.S] = n;
         sys.sp_lambda[sys.S] = lam;
@@ -784,7 +791,11 @@ void Context::BuildObservables(const Input& in) {
             h.k_cut = o.GetAttribute<double>("k_cut", kcutoff);
             sys.sp_rho[h.sa] = sys.sp_rho[h.sb] = 0;
             h.sk.reset(new DeviceBuffer(std::max<size_t>(sys.K, 1) * sizeof(double)));
-        } else if (h.type == "Time" || h.type == "PathDump") {
+        } else if (h.type == "PathDump") {
+            h.kind = 4;
+            h.skip = std::max(1u, o.GetAttribute<uint32_t>("skip", 1));  // observable_class.h:77
+            h.dumps.resize(sys.S);
+        } else if (h.type == "Time") {
             h.kind = 3;
         } else {
             throw PimcError(kErrUnsupported, "unsupported observable type '" + h.type + "'");
@@ -851,6 +862,7 @@ Context::Context(const Input& in, const std::string& bd, int dev, uint32_t ch) :
     main_loop.n_steps = 1;
     ReadLoop(alg, main_loop);
     InitRhoK();
+    ApplyRestarts();
 }
 
 Context::~Context() {

@@ -12,7 +12,8 @@
 //
 // Each record is "<dataset path> <count>" followed by <count> whitespace-separated numbers.
 // Scalars are records of count 1. Numbers are written with 17 significant digits so that a
-// round trip through the file is exact in double precision.
+// round trip through the file is exact in double precision. A string dataset (the reference's
+// names and type tags) is "<dataset path> str" followed by one line holding the string.
 #pragma once
 
 #include <fstream>
@@ -55,6 +56,18 @@ class TableFile {
             if (h != std::string::npos) line.resize(h);
             std::istringstream ls(line);
             std::string tok;
+            {
+                // "<path> str": the next line is the string value
+                std::istringstream peek(line);
+                std::string k, c, extra;
+                if ((key.empty() || vals.size() >= want) && (peek >> k >> c) && c == "str" && !(peek >> extra)) {
+                    flush();
+                    std::string v;
+                    if (!std::getline(f, v)) throw InputError("table '" + path + "': string dataset '" + k + "' lacks its line");
+                    t.strings_[k] = v;
+                    continue;
+                }
+            }
             while (ls >> tok) {
                 if (!key.empty() && vals.size() < want) {
                     char* end = nullptr;
@@ -79,6 +92,12 @@ class TableFile {
     }
 
     bool Has(const std::string& key) const { return data_.count(key) != 0; }
+    bool HasString(const std::string& key) const { return strings_.count(key) != 0; }
+    const std::string& String(const std::string& key) const {
+        auto it = strings_.find(key);
+        if (it == strings_.end()) throw InputError("table '" + path_ + "' has no string dataset '" + key + "'");
+        return it->second;
+    }
 
     const std::vector<double>& Vec(const std::string& key) const {
         auto it = data_.find(key);
@@ -95,6 +114,7 @@ class TableFile {
    private:
     std::string path_;
     std::map<std::string, std::vector<double>> data_;
+    std::map<std::string, std::string> strings_;
 };
 
 }  // namespace pimc

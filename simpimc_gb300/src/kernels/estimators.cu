@@ -794,7 +794,7 @@ void Context::ObservableAccumulate(uint32_t oi) {
     EnsureFP64();
     if (oi >= observables.size()) throw PimcError(kErrArg, "observable index out of range");
     ObservableHost& o = observables[oi];
-    if (o.kind == 3) return;
+    if (o.kind >= 3) return;  // Time, PathDump: nothing to accumulate
     if (o.kind == 0) {
         // energy_class.h:133-161 (sign and importance weight are 1 for these species)
         const double cof = 1.;
@@ -843,7 +843,7 @@ std::vector<double> Context::ObservableBlock(uint32_t oi) {
     if (oi >= observables.size()) throw PimcError(kErrArg, "observable index out of range");
     ObservableHost& o = observables[oi];
     std::vector<double> out;
-    if (o.kind == 3 || o.n_measure == 0) return out;
+    if (o.kind >= 3 || o.n_measure == 0) return out;
     Sync();
     if (o.kind == 0) {
         // energy_class.h:232-253

@@ -1652,13 +1652,35 @@ void Context::MoveAttempts(uint32_t m, uint64_t n) {
     Sweep(&m, &one, 1, 1);
 }
 
-// Bisect::Reset (bisect_class.h:142-155) and Move::Write/Reset (move_class.h:296-310).
+// Bisect::Reset (bisect_class.h:142-155) and Move::Write/Reset (move_class.h:296-310); PathDump::Write
+// (path_dump_class.h:28-66) on every skip-th call.
 void Context::WriteBlock() {
+    std::vector<double> host;
     for (size_t i = 0; i < observables.size(); ++i) {
+        ObservableHost& o = observables[i];
+        if (o.kind == 4) {
+            if (o.n_write_calls % o.skip == 0) {
+                if (host.empty()) {
+                    host.resize((size_t)sys.n_total * sys.M * sys.n_d);
+                    GetPath(0, host.data());  // [n_total][M][n_d]
+                }
+                for (uint32_t sp = 0; sp < sys.S; ++sp) {
+                    // cube (n_d, n_bead, n_part) column-major: the same order as the host layout
+                    const size_t n = (size_t)sys.sp_n[sp] * sys.M * sys.n_d, off = (size_t)sys.sp_off[sp] * sys.M * sys.n_d;
+                    o.dumps[sp].emplace_back(host.begin() + off, host.begin() + off + n);
+                }
+            }
+            o.n_write_calls++;
+            continue;
+        }
         auto v = ObservableBlock((uint32_t)i);
         if (!v.empty()) blocks[i].push_back(v);
     }
     for (auto& mh : moves) {
+        mh.out_attempt.push_back((double)mh.block_attempt);
+        mh.out_accept.push_back((double)mh.block_accept);
+        mh.out_ratio.push_back(mh.block_attempt ? (double)mh.block_accept / (double)mh.block_attempt : 0.);
+        mh.out_level.push_back((double)mh.dev.n_level);
         mh.last_ratio = mh.block_attempt ? (double)mh.block_accept / (double)mh.block_attempt : 0.;
         if (!mh.first_block && mh.adaptive && mh.block_attempt > 0) {
             const double ratio = (double)mh.block_accept / (double)mh.block_attempt;

@@ -24,18 +24,52 @@ from pathlib import Path
 
 import numpy as np
 
-__all__ = ["write_table", "coulomb_table", "ilkka_table", "david_table", "lattice_k_magnitudes", "ewald_alpha"]
+__all__ = ["write_table", "read_table", "coulomb_table", "ilkka_table", "david_table", "lattice_k_magnitudes", "ewald_alpha"]
 
 
 def write_table(path, datasets: dict) -> None:
-    """Write ``{dataset path: scalar or 1-D array}`` in the table container format."""
+    """Write ``{dataset path: scalar, 1-D array or string}`` in the table container format."""
     lines = ["# pair-action table: '<dataset> <count>' then the values"]
     for key, val in datasets.items():
+        if isinstance(val, str):
+            if "\n" in val:
+                raise ValueError(f"string dataset {key!r} spans lines")
+            lines.append(f"{key} str")
+            lines.append(val)
+            continue
         arr = np.atleast_1d(np.asarray(val, dtype=np.float64))
         lines.append(f"{key} {arr.size}")
         for i in range(0, arr.size, 4):
             lines.append(" ".join(repr(float(x)) for x in arr[i:i + 4]))
     Path(path).write_text("\n".join(lines) + "\n")
+
+
+def read_table(path) -> dict:
+    """Read a container file: ``{dataset path: 1-D float64 array or string}``."""
+    out: dict = {}
+    key, want, vals = None, None, []
+    lines = Path(path).read_text().splitlines()
+    i = 0
+    while i < len(lines):
+        toks = lines[i].split("#", 1)[0].split()
+        i += 1
+        if key is None and len(toks) == 2 and toks[1] == "str":
+            out[toks[0]] = lines[i] if i < len(lines) else ""
+            i += 1
+            continue
+        for tok in toks:
+            if key is None:
+                key = tok
+            elif want is None:
+                want, vals = int(tok), []
+            else:
+                vals.append(float(tok))
+            if key is not None and want is not None and len(vals) == want:
+                out[key] = np.asarray(vals, dtype=np.float64)
+                key, want, vals = None, None, []
+    if key is not None:
+        raise ValueError(f"{path}: dataset {key!r} is incomplete")
+    return out
 
 
 def lattice_k_magnitudes(L: float, k_cut: float, n_d: int = 3) -> np.ndarray:
