@@ -117,6 +117,7 @@ class ChainBatch {
     uint32_t launches_per_cycle_ = 3;  // sweep + energy parts + energy finish
     std::unique_ptr<DeviceBuffer> energy_tasks_, energy_first_, energy_part_;
     uint32_t n_energy_tasks_ = 0;
+    size_t energy_smem_ = 0;  // dynamic shared memory of the energy kernel
 };
 
 }  // namespace pimc

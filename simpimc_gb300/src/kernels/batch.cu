@@ -62,8 +62,10 @@ __device__ __forceinline__ float MinImg(float d, int pbc, float L, float iL) {
     return pbc ? __fsub_rn(d, __fmul_rn(L, rintf(__fmul_rn(d, iL)))) : d;
 }
 
-/// Exact i / d for i * d < 2^32 with m = ceil(2^32 / d).
+/// Exact i / d for i * d < 2^32 with m = ceil(2^32 / d) (d >= 2: for d = 1 the multiplier 2^32
+/// has no 32-bit form; FastDivD handles both).
 __device__ __forceinline__ uint32_t FastDiv(uint32_t i, uint32_t m) { return __umulhi(i, m); }
+__device__ __forceinline__ uint32_t FastDivD(uint32_t i, uint32_t d, uint32_t m) { return d == 1u ? i : __umulhi(i, m); }
 
 __device__ __forceinline__ dd AddSq(dd acc, float x) { return Add(acc, TwoProd(x, x)); }
 
@@ -361,7 +363,7 @@ __device__ __forceinline__ Comp PairPhase(const ChainDev& c, uint32_t t, uint32_
     if constexpr (kStaged) {  // beads in shared memory: no prefetch, loads batched by the unrolled loop
 #pragma unroll 4
         for (uint32_t i = t; i < n_items; i += T) {
-            const uint32_t k = FastDiv(i, magic), qq = i - k * nm1;
+            const uint32_t k = FastDivD(i, nm1, magic), qq = i - k * nm1;
             item(k, path.Load(Wrap(b0 + 1u + k, M), qq + (qq >= p ? 1u : 0u)));
         }
     } else {
@@ -369,7 +371,7 @@ __device__ __forceinline__ Comp PairPhase(const ChainDev& c, uint32_t t, uint32_
         for (uint32_t j = 0; j < kItems; ++j)
             if (t + j * T < n_items) item(it_k[j], pre[j]);
         for (uint32_t i = t + kItems * T; i < n_items; i += T) {
-            const uint32_t k = FastDiv(i, magic), qq = i - k * nm1;
+            const uint32_t k = FastDivD(i, nm1, magic), qq = i - k * nm1;
             item(k, path.Load(Wrap(b0 + 1u + k, M), qq + (qq >= p ? 1u : 0u)));
         }
     }
@@ -422,7 +424,7 @@ __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_
 #pragma unroll
     for (uint32_t j = 0; j < kItems; ++j) {
         const uint32_t i = t + j * T;
-        it_k[j] = FastDiv(i, magic);
+        it_k[j] = FastDivD(i, nm1, magic);
         it_q[j] = i - it_k[j] * nm1;
     }
 
@@ -579,7 +581,7 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
 #pragma unroll
     for (uint32_t j = 0; j < kItems; ++j) {
         const uint32_t i = ts + j * Ts;
-        it_k[j] = FastDiv(i, magic);
+        it_k[j] = FastDivD(i, nm1, magic);
         it_q[j] = i - it_k[j] * nm1;
     }
 
@@ -706,8 +708,9 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArg
 ///   Kinetic       N M D / (2 tau) - sum_{p,b} |r_{b+1} - r_b|^2 / (4 lambda tau^2)  kinetic_class.h:35-45
 ///   HarmonicTrap  cofactor_b sum_{p,b} r^2                                         trap_class.h:20-35
 ///   Coulomb       sum_{p<q} sum_b (1/r_b + 1/r_{b+1}) / 2                          pair_action_class.h:241-264
-/// A chain's slices are split into tasks of kEnergySlices; one block per task forms the task's
-/// three sums, and one warp per chain adds its tasks' sums in task order (deterministic).
+/// A chain's slices are split into tasks of kEnergySlices; one block per task stages the task's
+/// slices (and the next one) in shared memory, forms the task's three sums, and one warp per chain
+/// adds its tasks' sums in task order (deterministic).
 constexpr uint32_t kEnergySlices = 8;
 constexpr uint32_t kEnergyThreads = 256;
 
@@ -725,12 +728,21 @@ __global__ void __launch_bounds__(kEnergyThreads) BatchEnergyPartKernel(BatchArg
     const float L = c.L, iL = c.iL;
     const float4* __restrict__ pos = a.pos + c.pos_off;
     __shared__ dd s_red[3][kEnergyThreads / 32];
+    extern __shared__ float4 s_pos[];  // slices b0 .. b0 + nb of the task, [slot][N]
+    // i / N by FastDiv (i N < 2^32 here); a divisor of 1 has no 32-bit multiplier
+    const uint32_t mN = (uint32_t)((0x100000000ull + N - 1) / N);
+    auto div_n = [&](uint32_t i) { return FastDivD(i, N, mN); };
+    for (uint32_t i = t; i < N * (tk.nb + 1); i += T) {
+        const uint32_t slot = div_n(i), pp = i - slot * N;
+        s_pos[i] = pos[(size_t)((tk.b0 + slot) % M) * n_pad + pp];
+    }
+    __syncthreads();
 
     dd kin = DD(0.f), trap = DD(0.f), pair = DD(0.f);
     for (uint32_t i = t; i < N * tk.nb; i += T) {
-        const uint32_t b = tk.b0 + i / N, pp = i % N;
-        const float4 r = pos[(size_t)b * n_pad + pp];
-        const float4 r1 = pos[(size_t)((b + 1) % M) * n_pad + pp];
+        const uint32_t bb = div_n(i), pp = i - bb * N;
+        const float4 r = s_pos[bb * N + pp];
+        const float4 r1 = s_pos[(bb + 1) * N + pp];
         // |r_{b+1} - r_b|^2 with exact differences (TwoSum) and products (TwoProd).
         dd dx = TwoSum(r1.x, -r.x), dy = TwoSum(r1.y, -r.y), dz = TwoSum(r1.z, -r.z);
         if (pbc) {
@@ -746,13 +758,15 @@ __global__ void __launch_bounds__(kEnergyThreads) BatchEnergyPartKernel(BatchArg
         // p < N/2 when N is even; items (slice of the task, pair) spread evenly over the block.
         const uint32_t half = (N - 1) / 2, n_main = N * half;
         const uint32_t n_pairs = N * (N - 1) / 2;
+        const uint32_t mP = (uint32_t)((0x100000000ull + n_pairs - 1) / n_pairs);
         Comp acc{0.f, 0.f};
+        const bool fast = n_pairs > 1 && (uint64_t)n_pairs * tk.nb * n_pairs < (1ull << 32);  // FastDiv exact below 2^32
         for (uint32_t i = t; i < n_pairs * tk.nb; i += T) {
-            const uint32_t bb = i / n_pairs, j = i - bb * n_pairs;
-            const float4* row = pos + (size_t)(tk.b0 + bb) * n_pad;
+            const uint32_t bb = fast ? FastDiv(i, mP) : i / n_pairs, j = i - bb * n_pairs;
+            const float4* row = s_pos + bb * N;
             uint32_t pp, o;
             if (j < n_main) {
-                o = 1 + j / N;
+                o = 1 + div_n(j);
                 pp = j - (o - 1) * N;
             } else {
                 pp = j - n_main;
@@ -1012,6 +1026,13 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
     }
     first[n_chains] = (uint32_t)tasks.size();
     n_energy_tasks_ = (uint32_t)tasks.size();
+    // Shared memory of the largest task: its slices and the next one, N float4 each.
+    energy_smem_ = 0;
+    for (const auto& t : tasks) energy_smem_ = std::max(energy_smem_, (size_t)(t.nb + 1) * chains[t.chain].n_part * sizeof(float4));
+    int optin_e = 0;
+    CudaCheck(cudaDeviceGetAttribute(&optin_e, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "device attribute");
+    if (energy_smem_ + 4096 > (size_t)optin_e) throw PimcError(kErrUnsupported, "batched chain too large for the energy kernel's shared memory");
+    CudaCheck(cudaFuncSetAttribute(BatchEnergyPartKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)energy_smem_), "smem attribute");
     energy_tasks_.reset(new DeviceBuffer(tasks.size() * sizeof(EnergyTask)));
     energy_first_.reset(new DeviceBuffer(first.size() * sizeof(uint32_t)));
     energy_part_.reset(new DeviceBuffer(tasks.size() * 3 * sizeof(float2)));
@@ -1162,7 +1183,7 @@ void ChainBatch::LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts) {
 
 void ChainBatch::LaunchMeasure() {
     const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, series_cap);
-    BatchEnergyPartKernel<<<n_energy_tasks_, kEnergyThreads, 0, stream>>>(a, energy_tasks_->as<EnergyTask>(), energy_part_->as<float2>());
+    BatchEnergyPartKernel<<<n_energy_tasks_, kEnergyThreads, energy_smem_, stream>>>(a, energy_tasks_->as<EnergyTask>(), energy_part_->as<float2>());
     CudaCheck(cudaGetLastError(), "batch energy launch");
     BatchEnergyFinishKernel<<<(n_chains + 7) / 8, 256, 0, stream>>>(a, energy_first_->as<uint32_t>(), energy_part_->as<float2>(), n_chains);
     CudaCheck(cudaGetLastError(), "batch energy launch");

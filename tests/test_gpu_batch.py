@@ -20,6 +20,7 @@ pytestmark = pytest.mark.gpu
 
 SHAPES = [  # (n_part, n_bead, n_level)
     (2, 8, 1), (5, 16, 2), (16, 32, 3), (33, 32, 3), (40, 64, 4), (17, 128, 5), (64, 32, 3), (9, 8, 3),
+    (2, 16, 3),  # one partner: item and pair indices divide by 1
 ]
 
 
