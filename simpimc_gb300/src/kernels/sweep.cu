@@ -151,7 +151,7 @@ namespace {
 
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
-constexpr int kDeltaCache = 4;
+constexpr int kDeltaCache = 8;
 constexpr uint32_t kMaxOwned = 8;
 constexpr uint32_t kWaveSlots = 8;  // most attempts in flight in one round
 
@@ -801,15 +801,25 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                         const uint32_t nk = nk_own;
                         Comp lr32{0.f, 0.f};
                         uint32_t ci = 0;
+                        // This cell's densities (the first ones were loaded at the top of the
+                        // attempt); the next cell's are requested before this one's arithmetic.
+                        float2 rho_nx = make_float2(pre_rho.x, pre_rho.y), ro_nx = make_float2(pre_rho_o.x, pre_rho_o.y);
                         for (uint32_t it = tid; it < n_own * nk; it += blockDim.x, ++ci) {
                             const uint32_t si = it / nk, k = k_lo + it % nk;
                             const uint32_t b = (bead0 + s_slice_jj[si]) % M;
+                            const float2 rho = rho_nx, ro_first = ro_nx;
+                            if (it + blockDim.x < n_own * nk) {
+                                const uint32_t it2 = it + blockDim.x, si2 = it2 / nk, k2 = k_lo + it2 % nk;
+                                const uint32_t b2 = (bead0 + s_slice_jj[si2]) % M;
+                                rho_nx = a.rho32[((size_t)slot_s * M + b2) * K + k2];
+                                if (slot_o_first >= 0) ro_nx = a.rho32[((size_t)slot_o_first * M + b2) * K + k2];
+                            }
                             const int32_t pk = a.kidx[k];
                             const float2 en = PhaseProductF(tf_new + (size_t)si * 3 * stride, stride, n_d, pk);
                             const float2 eo = (ci == 0 && eo_done) ? pre_eo_f : PhaseProductF(tf_old + (size_t)si * 3 * stride, stride, n_d, pk);
                             const float2 dl = make_float2(__fsub_rn(en.x, eo.x), __fsub_rn(en.y, eo.y));
-                            if (ci < kDeltaCache) delta_f[ci] = dl;
-                            const float2 rho = ci == 0 ? make_float2(pre_rho.x, pre_rho.y) : a.rho32[((size_t)slot_s * M + b) * K + k];
+                            // the committed value of the cell if the attempt is accepted
+                            if (ci < kDeltaCache) delta_f[ci] = make_float2(__fadd_rn(rho.x, dl.x), __fadd_rn(rho.y, dl.y));
                             for (int pi = 0; pi < mv.n_pair; ++pi) {
                                 const PairDD& pa = s_pairs[mv.pair[pi]];
                                 if (!pa.use_lr || pa.is_constant) continue;
@@ -819,8 +829,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                                     CompAdd(lr32, __fmul_rn(vk, t));
                                 } else {
                                     const int slot_o = pa.sa == s ? pa.slot_b : pa.slot_a;
-                                    const float2 ro = (ci == 0 && slot_o == slot_o_first) ? make_float2(pre_rho_o.x, pre_rho_o.y)
-                                                                                          : a.rho32[((size_t)slot_o * M + b) * K + k];
+                                    const float2 ro = slot_o == slot_o_first ? ro_first : a.rho32[((size_t)slot_o * M + b) * K + k];
                                     const float t = __fmaf_rn(dl.x, ro.x, __fmul_rn(dl.y, ro.y));
                                     CompAdd(lr32, __fmul_rn(2.f * vk, t));
                                 }
@@ -838,8 +847,8 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                             const ddc en = PhaseProductDD(tab_new + (size_t)si * 3 * stride, stride, n_d, pk);
                             const ddc eo = (ci == 0 && eo_done) ? pre_eo : PhaseProductDD(tab_old + (size_t)si * 3 * stride, stride, n_d, pk);
                             const ddc dl = CSub(en, eo);
-                            if (ci < kDeltaCache) delta_cache[ci] = dl;
                             const ddc rho = Unpack(ci == 0 ? pre_rho : a.rho[((size_t)slot_s * M + b) * K + k]);
+                            if (ci < kDeltaCache) delta_cache[ci] = CAdd(rho, dl);  // the committed value on acceptance
                             for (int pi = 0; pi < mv.n_pair; ++pi) {
                                 const PairDD& pa = s_pairs[mv.pair[pi]];
                                 if (!pa.use_lr || pa.is_constant) continue;
@@ -947,30 +956,30 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                         for (uint32_t it = tid; it < n_own * nk; it += blockDim.x, ++ci) {
                             const uint32_t si = it / nk, k = k_lo + it % nk;
                             const uint32_t b = (bead0 + s_slice_jj[si]) % M;
+                            // The first kDeltaCache cells of the thread store the value formed in the
+                            // grid phase (the cell as loaded there plus the change); later ones re-form it.
                             if constexpr (kF32) {
-                                float2 dl;
+                                float2* cell = &a.rho32[((size_t)slot_s * M + b) * K + k];
                                 if (ci < kDeltaCache) {
-                                    dl = delta_f[ci];
+                                    *cell = delta_f[ci];
                                 } else {
                                     const int32_t pk = a.kidx[k];
                                     const float2 en = PhaseProductF(tf_new + (size_t)si * 3 * stride, stride, n_d, pk);
                                     const float2 eo = PhaseProductF(tf_old + (size_t)si * 3 * stride, stride, n_d, pk);
-                                    dl = make_float2(__fsub_rn(en.x, eo.x), __fsub_rn(en.y, eo.y));
+                                    const float2 dl = make_float2(__fsub_rn(en.x, eo.x), __fsub_rn(en.y, eo.y));
+                                    const float2 c0 = *cell;
+                                    *cell = make_float2(__fadd_rn(c0.x, dl.x), __fadd_rn(c0.y, dl.y));
                                 }
-                                float2* cell = &a.rho32[((size_t)slot_s * M + b) * K + k];
-                                const float2 c0 = *cell;
-                                *cell = make_float2(__fadd_rn(c0.x, dl.x), __fadd_rn(c0.y, dl.y));
                             } else {
-                                ddc dl;
+                                float4* cell = &a.rho[((size_t)slot_s * M + b) * K + k];
                                 if (ci < kDeltaCache) {
-                                    dl = delta_cache[ci];
+                                    *cell = Pack(delta_cache[ci]);
                                 } else {
                                     const int32_t pk = a.kidx[k];
-                                    dl = CSub(PhaseProductDD(tab_new + (size_t)si * 3 * stride, stride, n_d, pk),
-                                              PhaseProductDD(tab_old + (size_t)si * 3 * stride, stride, n_d, pk));
+                                    const ddc dl = CSub(PhaseProductDD(tab_new + (size_t)si * 3 * stride, stride, n_d, pk),
+                                                        PhaseProductDD(tab_old + (size_t)si * 3 * stride, stride, n_d, pk));
+                                    *cell = Pack(CAdd(Unpack(*cell), dl));
                                 }
-                                float4* cell = &a.rho[((size_t)slot_s * M + b) * K + k];
-                                *cell = Pack(CAdd(Unpack(*cell), dl));
                             }
                         }
                     }
