@@ -10,9 +10,10 @@
 // and the trapped-particle configuration), Philox known-answer vectors, natural-spline identities
 // and independent Ewald sums (tests/test_oracle_*.py).
 //
-// Deliberate, documented departures (each one also listed in the design doc):
+// Deliberate departures from the reference:
 //  * einspline's natural-BC cubic B-splines are represented as the (identical) natural cubic
-//    interpolating spline; arguments are clamped to the grid.
+//    interpolating splines; 1-D table arguments are clamped to the grid, and the 2-D table of
+//    IlkkaPairAction continues its edge cells outside it.
 //  * The scaffold RNG is replaced by the Philox draw protocol shared with the GPU path.
 //  * k-vectors are enumerated lexicographically (the reference's GenCombPermK order is unavailable);
 //    only the summation order differs.
