@@ -113,6 +113,17 @@ int pimc_sweep(pimc_ctx* ctx, const uint32_t* moves, const uint64_t* counts, uin
  * that reached the level-0 test} (counters of move_class.h:226-228). */
 int pimc_move_stats(pimc_ctx* ctx, uint32_t move, uint64_t* out);
 
+/* Path permutation of a species (the bead links at the ring closure, bead_class.h:38-41 after the
+ * relabelling of perm_bisect_class.h:47-56): perm[p] is the particle whose slice-0 bead follows
+ * bead (p, M - 1); species-local indices. pimc_set_perm refuses a non-permutation with
+ * PIMC_ERR_ARG. Permuting moves (PermBisectIterative, PermBisectTable) and the plain bisection of a
+ * species that has one or carries a non-identity permutation run on the permutation kernel. */
+int pimc_get_perm(pimc_ctx* ctx, uint32_t species, uint32_t* perm);
+int pimc_set_perm(pimc_ctx* ctx, uint32_t species, const uint32_t* perm);
+/* Per cycle length 1..N of a permuting move: out[0..N) attempts, out[N..2N) accepts of the current
+ * block (perm_bisect_class.h:25-26, 59-90); N = the move's species particle count. */
+int pimc_perm_stats(pimc_ctx* ctx, uint32_t move, uint64_t* out, size_t cap);
+
 /* Observables: Observable::DoEvent / Write (observable_class.h:421-432). pimc_observable_block
  * returns the normalised values Write() would append (energy_class.h:232-325,
  * pair_correlation_class.h:89-123, structure_factor_class.h:195-211) and resets the block. */

@@ -70,6 +70,9 @@ def lib():
             "oracle_n_blocks": [C.c_void_p, C.c_uint32, _U64P],
             "oracle_get_block": [C.c_void_p, C.c_uint32, C.c_uint64, _DP, C.c_uint64, _U64P],
             "oracle_philox": [_U32P, _U32P, _U32P],
+            "oracle_perm_stats": [C.c_void_p, C.c_uint32, _U64P],
+            "oracle_get_perm": [C.c_void_p, C.c_uint32, _U32P],
+            "oracle_set_perm": [C.c_void_p, C.c_uint32, _U32P],
         }.items():
             fn = getattr(L, name)
             fn.argtypes = args
@@ -214,6 +217,20 @@ class OracleSim:
         out = np.zeros(3, dtype=np.uint64)
         self._L.oracle_move_stats(self._h, move, out.ctypes.data_as(_U64P))
         return int(out[0]), int(out[1]), int(out[2])
+
+    def perm_stats(self, move, n_part):
+        out = np.zeros(2 * n_part, dtype=np.uint64)
+        self._ok(self._L.oracle_perm_stats(self._h, move, out.ctypes.data_as(_U64P)))
+        return out[:n_part].astype(np.int64), out[n_part:].astype(np.int64)
+
+    def get_perm(self, species, n_part):
+        out = np.zeros(n_part, dtype=np.uint32)
+        self._ok(self._L.oracle_get_perm(self._h, species, out.ctypes.data_as(_U32P)))
+        return out.astype(np.int64)
+
+    def set_perm(self, species, perm):
+        pi = np.ascontiguousarray(perm, dtype=np.uint32)
+        self._ok(self._L.oracle_set_perm(self._h, species, pi.ctypes.data_as(_U32P)))
 
     def observable_accumulate(self, obs):
         self._ok(self._L.oracle_obs_accumulate(self._h, obs))

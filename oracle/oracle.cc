@@ -27,6 +27,7 @@
 #include <cstring>
 #include <ctime>
 #include <memory>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -369,6 +370,11 @@ struct Species {
     std::vector<cplx> rho_k, rho_k_c;
     // Per-bead charge densities and their copies (bead_class.h:218-219): [p][b][k].
     std::vector<cplx> bead_rho_k, bead_rho_k_c;
+    // Bead links (bead_class.h:38-41, 98-111): bead (p, b) is followed by bead (nxt[p M + b], b + 1 mod M);
+    // OLD mode reads the copy nxt_c. Between moves every link keeps its particle label except at the
+    // ring closure b = M - 1, which holds the path permutation (AssignParticleLabels,
+    // perm_bisect_class.h:47-56, relabels the beads after an accepted permutation).
+    std::vector<uint32_t> nxt, nxt_c;
     uint32_t bead_loop(uint32_t b) const { return b >= n_bead ? b - n_bead : b; }  // species_class.h:101
 };
 
@@ -422,6 +428,12 @@ struct Path {
         }
         r.assign((size_t)n_total * n_bead * n_d, 0.);
         r_c = r;
+        for (auto& s : species) {
+            s.nxt.resize((size_t)s.n_part * n_bead);
+            for (uint32_t p = 0; p < s.n_part; ++p)
+                for (uint32_t b = 0; b < n_bead; ++b) s.nxt[(size_t)p * n_bead + b] = p;
+            s.nxt_c = s.nxt;
+        }
     }
 
     Species& GetSpecies(const std::string& nm) {
@@ -433,6 +445,62 @@ struct Path {
     size_t Idx(const Species& s, uint32_t p, uint32_t b) const { return (((size_t)(s.offset + p)) * n_bead + s.bead_loop(b)) * n_d; }
     double* GetR(const Species& s, uint32_t p, uint32_t b) { return (mode == NEW_MODE ? r.data() : r_c.data()) + Idx(s, p, b); }
     double* GetRMode(const Species& s, uint32_t p, uint32_t b, Mode m) { return (m == NEW_MODE ? r.data() : r_c.data()) + Idx(s, p, b); }
+
+    // Label of the bead after (p, b) (GetNextBead(1), bead_class.h:22-23, 104).
+    uint32_t NextLabel(const Species& s, uint32_t p, uint32_t b, Mode m) const {
+        return (m == NEW_MODE ? s.nxt : s.nxt_c)[(size_t)p * n_bead + s.bead_loop(b)];
+    }
+    // Label of the bead before (p, b) (GetPrevBead(1)): the bead whose link reaches (p, b).
+    uint32_t PrevLabel(const Species& s, uint32_t p, uint32_t b, Mode m) const {
+        const uint32_t bp = (s.bead_loop(b) + n_bead - 1) % n_bead;
+        for (uint32_t q = 0; q < s.n_part; ++q)
+            if (NextLabel(s, q, bp, m) == p) return q;
+        throw std::logic_error("bead links are not a permutation");
+    }
+    // GetNextBead(n) / GetPrevBead(n) of bead (p, b): returns the label and sets `slice`.
+    uint32_t Walk(const Species& s, uint32_t p, uint32_t b, uint32_t n, Mode m, uint32_t& slice) const {
+        uint32_t q = p, bb = s.bead_loop(b);
+        for (uint32_t i = 0; i < n; ++i) {
+            q = NextLabel(s, q, bb, m);
+            bb = bb + 1 == n_bead ? 0 : bb + 1;
+        }
+        slice = bb;
+        return q;
+    }
+    uint32_t WalkBack(const Species& s, uint32_t p, uint32_t b, uint32_t n, Mode m, uint32_t& slice) const {
+        uint32_t q = p, bb = s.bead_loop(b);
+        for (uint32_t i = 0; i < n; ++i) {
+            q = PrevLabel(s, q, bb, m);
+            bb = bb == 0 ? n_bead - 1 : bb - 1;
+        }
+        slice = bb;
+        return q;
+    }
+    // The path permutation of a species: pi[p] = label of the bead after (p, M - 1).
+    std::vector<uint32_t> Closure(const Species& s) const {
+        std::vector<uint32_t> pi(s.n_part);
+        for (uint32_t p = 0; p < s.n_part; ++p) pi[p] = NextLabel(s, p, n_bead - 1, NEW_MODE);
+        return pi;
+    }
+    // Species::GetSign (species_class.h:149-157) over every species (path_class.h:169-175).
+    int GetSign() const {
+        int sign = 1;
+        for (const auto& s : species) {
+            if (!s.fermi) continue;
+            std::vector<char> seen(s.n_part, 0);
+            for (uint32_t p = 0; p < s.n_part; ++p) {
+                if (seen[p]) continue;
+                uint32_t len = 0, q = p;
+                do {
+                    seen[q] = 1;
+                    q = NextLabel(s, q, n_bead - 1, NEW_MODE);
+                    ++len;
+                } while (q != p);
+                if (!(len % 2)) sign = -sign;
+            }
+        }
+        return sign;
+    }
 
     // path_class.h:131-134
     void PutInBox(double* x) const {
@@ -657,38 +725,47 @@ struct Kinetic : SingleAction {
         double dr[3];
         for (uint32_t b = 0; b < species->n_bead; ++b)
             for (uint32_t p = 0; p < species->n_part; ++p) {
-                path.Dr(path.GetR(*species, p, b), path.GetR(*species, p, b + 1), dr);
+                const uint32_t q = path.NextLabel(*species, p, b, path.mode);
+                path.Dr(path.GetR(*species, p, b), path.GetR(*species, q, b + 1), dr);
                 tot += rho_free_splines[0].GetDLogRhoFreeDTau(dr, path.n_d);
             }
         return tot;
     }
 
-    // kinetic_class.h:48-102
+    // kinetic_class.h:48-102 (beads b_0, b_1, b_2 follow the links)
     double VirialEnergy(double window) override {
         uint32_t n_d = path.n_d, M = species->n_bead;
+        const Mode m = path.mode;
         double tot = d_action_d_beta_const / window;
+        struct B {
+            uint32_t p, b;
+        };
+        auto next = [&](B x) { return B{path.NextLabel(*species, x.p, x.b, m), (x.b + 1) % M}; };
+        auto R = [&](B x) { return path.GetR(*species, x.p, x.b); };
         for (uint32_t p = 0; p < species->n_part; ++p) {
-            uint32_t b0 = 0, b1 = 1, b2 = 2 % M;
+            B b0{p, 0};
+            B b1 = next(b0);
+            B b2 = next(b1);
             double dr1[3], drL[3], t[3];
-            path.Dr(path.GetR(*species, p, b1), path.GetR(*species, p, b0), dr1);
+            path.Dr(R(b1), R(b0), dr1);
             for (uint32_t d = 0; d < n_d; ++d) drL[d] = dr1[d];
             for (uint32_t s = 1; s < window; ++s) {
-                path.Dr(path.GetR(*species, p, b2), path.GetR(*species, p, b1), t);
+                path.Dr(R(b2), R(b1), t);
                 for (uint32_t d = 0; d < n_d; ++d) drL[d] += t[d];
                 b1 = b2;
-                b2 = (b2 + 1) % M;
+                b2 = next(b2);
             }
             double dot = 0.;
             for (uint32_t d = 0; d < n_d; ++d) dot += drL[d] * dr1[d];
             tot -= dot * i_4_lambda_tau / (window * path.tau);
             for (uint32_t b = 1; b < M; ++b) {
                 for (uint32_t d = 0; d < n_d; ++d) drL[d] -= dr1[d];
-                path.Dr(path.GetR(*species, p, b2), path.GetR(*species, p, b1), t);
+                path.Dr(R(b2), R(b1), t);
                 for (uint32_t d = 0; d < n_d; ++d) drL[d] += t[d];
-                b0 = (b0 + 1) % M;
-                path.Dr(path.GetR(*species, p, (b0 + 1) % M), path.GetR(*species, p, b0), dr1);
+                b0 = next(b0);
+                path.Dr(R(next(b0)), R(b0), dr1);
                 b1 = b2;
-                b2 = (b2 + 1) % M;
+                b2 = next(b2);
                 dot = 0.;
                 for (uint32_t d = 0; d < n_d; ++d) dot += drL[d] * dr1[d];
                 tot -= dot * i_4_lambda_tau / (window * path.tau);
@@ -697,20 +774,34 @@ struct Kinetic : SingleAction {
         return tot;
     }
 
-    // kinetic_class.h:105-122 (beads link to the same particle: no permutations)
+    // The walk of kinetic_class.h:112-119: from bead (p, b0) in steps of `skip` along the links until
+    // bead_b = GetNextBead(b1 - b0) of the start; calls f(label, slice, next label, next slice) per link.
+    template <class F>
+    void Links(uint32_t p, uint32_t b0, uint32_t b1, uint32_t skip, F f) {
+        const Mode m = path.mode;
+        uint32_t end_b;
+        const uint32_t end_p = path.Walk(*species, p, b0, b1 - b0, m, end_b);
+        uint32_t ap = p, ab = species->bead_loop(b0 % species->n_bead), guard = 0;
+        while (!(ap == end_p && ab == end_b)) {
+            uint32_t nb;
+            const uint32_t np_ = path.Walk(*species, ap, ab, skip, m, nb);
+            f(ap, ab, np_, nb);
+            ap = np_;
+            ab = nb;
+            if (++guard > species->n_part * species->n_bead) throw std::invalid_argument("segment end is not reachable at this level");
+        }
+    }
+
+    // kinetic_class.h:105-122
     double GetAction(uint32_t b0, uint32_t b1, const Particles& parts, uint32_t level) override {
         uint32_t skip = 1u << level;
-        uint32_t M = species->n_bead;
         double tot = 0., dr[3];
         for (auto& pr : parts) {
             if (pr.first != species->s_i) continue;
-            uint32_t a = b0 % M, end = b1 % M;
-            while (a != end) {
-                uint32_t nx = (a + skip) % M;
-                path.Dr(path.GetR(*species, pr.second, a), path.GetR(*species, pr.second, nx), dr);
+            Links(pr.second, b0, b1, skip, [&](uint32_t ap, uint32_t ab, uint32_t np_, uint32_t nb) {
+                path.Dr(path.GetR(*species, ap, ab), path.GetR(*species, np_, nb), dr);
                 tot -= rho_free_splines[skip - 1].GetLogRhoFree(dr, path.n_d);
-                a = nx;
-            }
+            });
         }
         return tot;
     }
@@ -718,21 +809,19 @@ struct Kinetic : SingleAction {
     // kinetic_class.h:125-144
     void GetActionGradient(uint32_t b0, uint32_t b1, const Particles& parts, uint32_t level, double* g) override {
         uint32_t skip = 1u << level;
-        uint32_t M = species->n_bead, n_d = path.n_d;
+        uint32_t n_d = path.n_d;
         double i4 = i_4_lambda_tau / skip;
         double tot[3] = {0., 0., 0.}, t[3];
         for (auto& pr : parts) {
             if (pr.first != species->s_i) continue;
-            uint32_t a = b0 % M, end = b1 % M;
-            while (a != end) {
-                uint32_t pv = (a + M - (skip % M)) % M;
-                uint32_t nx = (a + skip) % M;
-                path.Dr(path.GetR(*species, pr.second, pv), path.GetR(*species, pr.second, a), t);
+            Links(pr.second, b0, b1, skip, [&](uint32_t ap, uint32_t ab, uint32_t np_, uint32_t nb) {
+                uint32_t pb;
+                const uint32_t pp = path.WalkBack(*species, ap, ab, skip, path.mode, pb);
+                path.Dr(path.GetR(*species, pp, pb), path.GetR(*species, ap, ab), t);
                 for (uint32_t d = 0; d < n_d; ++d) tot[d] -= t[d];
-                path.Dr(path.GetR(*species, pr.second, a), path.GetR(*species, pr.second, nx), t);
+                path.Dr(path.GetR(*species, ap, ab), path.GetR(*species, np_, nb), t);
                 for (uint32_t d = 0; d < n_d; ++d) tot[d] += t[d];
-                a = nx;
-            }
+            });
         }
         for (uint32_t d = 0; d < n_d; ++d) g[d] = 2. * i4 * tot[d];
     }
@@ -1672,68 +1761,91 @@ struct Bisect : Move {
         n_attempt = 0;
     }
 
-    // bisect_class.h:39-124
+    // Sampling of one bisection level along beads lab/sl[0..B] (NEW links) for the bisection, with the
+    // OLD-mode neighbours of the last midpoint taken from old_end (bisect_class.h:74-94,
+    // perm_bisect_iterative_class.h:167-192): accumulates both log sampling probabilities.
+    void SampleLevel(const Stream& st, uint32_t& mid_counter, uint32_t block_base, int level_i, const std::vector<uint32_t>& lab,
+                     const std::vector<uint32_t>& sl, uint32_t old_end_p, uint32_t old_end_b, double& old_lsp, double& new_lsp) {
+        const uint32_t skip = 1u << level_i, n_d = path.n_d;
+        const double sigma = std::sqrt(species->lambda * path.tau * skip);
+        for (uint32_t a = 0; a < n_bisect_beads; a += 2 * skip) {
+            const uint32_t b = a + skip, c = a + 2 * skip;
+            double rbar[3], delta[3], t[3];
+            {
+                const uint32_t cp = c == n_bisect_beads ? old_end_p : lab[c], cb = c == n_bisect_beads ? old_end_b : sl[c];
+                const double* ra = path.GetRMode(*species, lab[a], sl[a], OLD_MODE);
+                const double* rc = path.GetRMode(*species, cp, cb, OLD_MODE);
+                const double* rb = path.GetRMode(*species, lab[b], sl[b], OLD_MODE);
+                path.Dr(rc, ra, t);
+                for (uint32_t d = 0; d < n_d; ++d) rbar[d] = ra[d] + 0.5 * t[d];
+                path.Dr(rb, rbar, delta);
+                old_lsp += rho_free_splines[level_i].GetLogRhoFree(delta, n_d);
+            }
+            {
+                float z[4];
+                RNG4 wz = st.block(block_base + mid_counter);
+                boxmuller(wz.w[0], wz.w[1], z[0], z[1]);
+                boxmuller(wz.w[2], wz.w[3], z[2], z[3]);
+                mid_counter++;
+                for (uint32_t d = 0; d < n_d; ++d) delta[d] = 0. + sigma * (double)z[d];
+                path.PutInBox(delta);
+                const double* ra = path.GetRMode(*species, lab[a], sl[a], NEW_MODE);
+                const double* rc = path.GetRMode(*species, lab[c], sl[c], NEW_MODE);
+                path.Dr(rc, ra, t);
+                for (uint32_t d = 0; d < n_d; ++d) rbar[d] = ra[d] + 0.5 * t[d];
+                double* rb = path.GetRMode(*species, lab[b], sl[b], NEW_MODE);
+                for (uint32_t d = 0; d < n_d; ++d) rb[d] = rbar[d] + delta[d];
+                new_lsp += rho_free_splines[level_i].GetLogRhoFree(delta, n_d);
+            }
+        }
+    }
+
+    // The beads GetNextBead(0..B) of (p, b0) along the NEW links.
+    void Chain(uint32_t p, uint32_t b0, std::vector<uint32_t>& lab, std::vector<uint32_t>& sl) const {
+        lab.resize(n_bisect_beads + 1);
+        sl.resize(n_bisect_beads + 1);
+        lab[0] = p;
+        sl[0] = b0;
+        for (uint32_t t = 0; t < n_bisect_beads; ++t) {
+            lab[t + 1] = path.NextLabel(*species, lab[t], sl[t], NEW_MODE);
+            sl[t + 1] = (sl[t] + 1) % species->n_bead;
+        }
+    }
+
+    double ActionChange(const Particles& parts, int level_i) {
+        double old_action = 0., new_action = 0.;
+        for (Action* a : action_list) {
+            path.mode = OLD_MODE;
+            old_action += a->GetAction(bead0, bead1, parts, (uint32_t)level_i);
+            path.mode = NEW_MODE;
+            new_action += a->GetAction(bead0, bead1, parts, (uint32_t)level_i);
+        }
+        return new_action - old_action;
+    }
+
+    // bisect_class.h:39-124: the segment follows the bead links, and the particle owning the end
+    // bead joins the action's particle list when it differs (:61-64).
     bool Attempt() override {
         Stream st{seed, chain, move_index, attempt_counter};
         RNG4 w0 = st.block(0);
         uint32_t p_i = uidx(w0.w[0], species->n_part);
         bead0 = uidx(w0.w[1], species->n_bead);
         bead1 = bead0 + n_bisect_beads;
-        uint32_t M = species->n_bead, n_d = path.n_d;
+        std::vector<uint32_t> lab, sl;
+        Chain(p_i, bead0, lab, sl);
         affected.clear();
-        for (uint32_t i = 0; i <= n_bisect_beads; ++i) affected.push_back({p_i, (bead0 + i) % M});
+        for (uint32_t i = 0; i <= n_bisect_beads; ++i) affected.push_back({lab[i], sl[i]});
         Particles parts;
         parts.push_back({species->s_i, p_i});
+        if (lab[n_bisect_beads] != p_i) parts.push_back({species->s_i, lab[n_bisect_beads]});
 
         double prev_action_change = 0.;
         uint32_t mid_counter = 0;
         for (int level_i = (int)n_level - 1; level_i >= 0; --level_i) {
-            uint32_t skip = 1u << level_i;
-            double level_tau = path.tau * skip;
-            double sigma = std::sqrt(species->lambda * level_tau);
             double old_lsp = 0., new_lsp = 0.;
-            for (uint32_t a = 0; a < n_bisect_beads; a += 2 * skip) {
-                uint32_t ba = (bead0 + a) % M, bb = (bead0 + a + skip) % M, bc = (bead0 + a + 2 * skip) % M;
-                double rbar[3], delta[3];
-                // Old sampling: RBar(c, a) = r_a + 0.5 Dr(c, a) in OLD mode (path_class.h:124)
-                {
-                    const double* ra = path.GetRMode(*species, p_i, ba, OLD_MODE);
-                    const double* rc = path.GetRMode(*species, p_i, bc, OLD_MODE);
-                    const double* rb = path.GetRMode(*species, p_i, bb, OLD_MODE);
-                    double t[3];
-                    path.Dr(rc, ra, t);
-                    for (uint32_t d = 0; d < n_d; ++d) rbar[d] = ra[d] + 0.5 * t[d];
-                    path.Dr(rb, rbar, delta);
-                    old_lsp += rho_free_splines[level_i].GetLogRhoFree(delta, n_d);
-                }
-                // New sampling
-                {
-                    float z[4];
-                    RNG4 wz = st.block(1u + mid_counter);
-                    boxmuller(wz.w[0], wz.w[1], z[0], z[1]);
-                    boxmuller(wz.w[2], wz.w[3], z[2], z[3]);
-                    mid_counter++;
-                    for (uint32_t d = 0; d < n_d; ++d) delta[d] = 0. + sigma * (double)z[d];
-                    path.PutInBox(delta);
-                    const double* ra = path.GetRMode(*species, p_i, ba, NEW_MODE);
-                    const double* rc = path.GetRMode(*species, p_i, bc, NEW_MODE);
-                    double t[3];
-                    path.Dr(rc, ra, t);
-                    for (uint32_t d = 0; d < n_d; ++d) rbar[d] = ra[d] + 0.5 * t[d];
-                    double* rb = path.GetRMode(*species, p_i, bb, NEW_MODE);
-                    for (uint32_t d = 0; d < n_d; ++d) rb[d] = rbar[d] + delta[d];
-                    new_lsp += rho_free_splines[level_i].GetLogRhoFree(delta, n_d);
-                }
-            }
-            double old_action = 0., new_action = 0.;
-            for (Action* a : action_list) {
-                path.mode = OLD_MODE;
-                old_action += a->GetAction(bead0, bead1, parts, (uint32_t)level_i);
-                path.mode = NEW_MODE;
-                new_action += a->GetAction(bead0, bead1, parts, (uint32_t)level_i);
-            }
+            SampleLevel(st, mid_counter, 1u, level_i, lab, sl, lab[n_bisect_beads], sl[n_bisect_beads], old_lsp, new_lsp);
             double log_sample_ratio = -new_lsp + old_lsp;
-            double current = new_action - old_action;
+            double current = ActionChange(parts, level_i);
             double log_accept = log_sample_ratio - current + prev_action_change;
             RNG4 wu = st.block(1u + (n_bisect_beads - 1u) + (n_level - 1u - (uint32_t)level_i));
             if (log_accept < (double)logf_spec(u24(wu.w[0]))) return false;
@@ -1782,6 +1894,312 @@ struct Bisect : Move {
                 std::copy(species->rho_k_c.begin() + (size_t)bb * K, species->rho_k_c.begin() + (size_t)(bb + 1) * K, species->rho_k.begin() + (size_t)bb * K);
             }
         for (Action* a : action_list) a->Reject();
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
+// Permuting bisection (perm_bisect_class.h:7-133; perm_bisect_iterative_class.h:7-231 builds the
+// cycle particle by particle, perm_bisect_table_class.h:7-240 samples a table of every cycle of
+// n_perm_part particles). Random numbers of attempt a of move m come from Philox blocks
+// (a, m, block) as for the bisection, laid out by the species' particle count N and B = 2^n_level:
+//   block 0                  word 0: first slice; word 1: first particle (iterative); words 2, 3:
+//                            the table's selection uniform (53 bits)
+//   block 1 + j, j < N       step j of the iterative cycle: words 0, 1 the continuation uniform,
+//                            words 2, 3 the choice uniform
+//   block 1 + N + c          midpoint c, in the order level, cycle path, position along the path
+//   block 1 + N + N(B-1) + l the level test of level n_level - 1 - l (word 0, as the bisection)
+//   block 1 + N + N(B-1) + n_level   the table's final test (words 0, 1)
+// Departures: the table variant adds the particles owning the end beads to the action's particle
+// list when the segment passes the ring closure, as the iterative variant does (:141-146 there;
+// the table omits it, which leaves the moved beads beyond the closure out of the label-indexed
+// actions and of the density update); the cycle table enumerates permutations and particle subsets
+// in lexicographic order (GenPerm / GenCombPermK belong to the absent scaffold library); a cycle
+// walk that selects no particle in N steps (only possible by rounding of the running sum) ends
+// the attempt as an unselected cycle; a selection uniform at the table's total picks the last cycle.
+static double u53(uint32_t a, uint32_t b) { return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0); }
+
+struct PermBisect : Bisect {
+    bool table;
+    double epsilon, log_epsilon;
+    uint32_t n_perm_part = 0, n_perm_type = 0, n_perm_part_in = 0;
+    std::vector<uint64_t> perm_attempt, perm_accept;
+    std::vector<double> t;  // [N][N]
+    struct Cycle {
+        double weight = 0., contribution = 0.;
+        uint32_t type = 0;
+        std::vector<uint32_t> part, perm, i_perm;
+    };
+    std::vector<Cycle> all_cycles;
+    Cycle cyc;
+    uint32_t s0 = 0;  // slice of the bead before the permuted link
+
+    PermBisect(Path& p, std::vector<std::unique_ptr<Action>>& actions, const Input& in, uint32_t idx, uint32_t sd, uint32_t ch, bool tbl)
+        : Bisect(p, actions, in, idx, sd, ch), table(tbl) {
+        epsilon = in.GetAttribute<double>("epsilon", 1.e-100);
+        log_epsilon = std::log(epsilon);
+        const uint32_t N = species->n_part;
+        t.assign((size_t)N * N, 0.);
+        perm_attempt.assign(N, 0);
+        perm_accept.assign(N, 0);
+        if (table) {
+            n_perm_part_in = in.GetAttribute<uint32_t>("n_perm_part");
+            BuildCycles();
+        } else
+            n_perm_type = N;
+    }
+
+    // perm_bisect_table_class.h:54-102
+    void BuildCycles() {
+        const uint32_t k = n_perm_part_in, N = species->n_part;
+        if (k < 1 || k > N) throw InputError("n_perm_part must be between 1 and the particle count");
+        std::vector<std::vector<uint32_t>> perms, combs;
+        std::vector<uint32_t> a(k);
+        for (uint32_t i = 0; i < k; ++i) a[i] = i;
+        do perms.push_back(a);
+        while (std::next_permutation(a.begin(), a.end()));
+        n_perm_type = (uint32_t)perms.size();
+        std::vector<uint32_t> c(k);
+        for (uint32_t i = 0; i < k; ++i) c[i] = i;
+        while (true) {
+            combs.push_back(c);
+            int i = (int)k - 1;
+            while (i >= 0 && c[i] == N - k + (uint32_t)i) --i;
+            if (i < 0) break;
+            c[i]++;
+            for (uint32_t j = (uint32_t)i + 1; j < k; ++j) c[j] = c[j - 1] + 1;
+        }
+        for (uint32_t ty = 0; ty < perms.size(); ++ty)
+            for (auto& cb : combs) {
+                Cycle cy;
+                cy.type = ty;
+                cy.part = cb;
+                cy.perm = perms[ty];
+                cy.i_perm.resize(k);
+                for (uint32_t j = 0; j < k; ++j) cy.i_perm[cy.perm[j]] = j;
+                all_cycles.push_back(cy);
+            }
+    }
+
+    // UpdatePermTable (perm_bisect_iterative_class.h:10-29, perm_bisect_table_class.h:31-51): the
+    // free-particle weight from the start bead of i to the end bead (B links on) of j.
+    void UpdateTable() {
+        const uint32_t N = species->n_part;
+        std::vector<uint32_t> ep(N), eb(N);
+        for (uint32_t j = 0; j < N; ++j) ep[j] = path.Walk(*species, j, bead0, n_bisect_beads, NEW_MODE, eb[j]);
+        const double i4 = i_4_lambda_tau / n_bisect_beads;
+        for (uint32_t i = 0; i < N; ++i) {
+            double dii = 0., dr[3];
+            path.Dr(path.GetRMode(*species, i, bead0, NEW_MODE), path.GetRMode(*species, ep[i], eb[i], NEW_MODE), dr);
+            for (uint32_t d = 0; d < path.n_d; ++d) dii += dr[d] * dr[d];
+            for (uint32_t j = 0; j < N; ++j) {
+                path.Dr(path.GetRMode(*species, i, bead0, NEW_MODE), path.GetRMode(*species, ep[j], eb[j], NEW_MODE), dr);
+                double dij = 0.;
+                for (uint32_t d = 0; d < path.n_d; ++d) dij += dr[d] * dr[d];
+                const double ex = table ? (-dij + dii) * i4 : (-dij) * i4;
+                t[(size_t)i * N + j] = ex > log_epsilon ? std::exp(ex) : 0.;
+            }
+        }
+    }
+
+    // perm_bisect_table_class.h:10-28: returns the total weight; fills `order`/`contrib` with the
+    // cycles above epsilon and their running sums.
+    double TableTotal(std::vector<uint32_t>* order, std::vector<double>* contrib) {
+        UpdateTable();
+        const uint32_t N = species->n_part;
+        double total = 0.;
+        for (uint32_t ci = 0; ci < all_cycles.size(); ++ci) {
+            Cycle& c = all_cycles[ci];
+            c.weight = 1.;
+            for (uint32_t i = 0; i < c.part.size(); ++i) c.weight *= t[(size_t)c.part[i] * N + c.part[c.perm[i]]];
+            if (c.weight > epsilon) {
+                total += c.weight;
+                c.contribution = total;
+                if (order) {
+                    order->push_back(ci);
+                    contrib->push_back(total);
+                }
+            }
+        }
+        return total;
+    }
+
+    // perm_bisect_iterative_class.h:32-110
+    bool SelectIterative(const Stream& st, const RNG4& w0) {
+        UpdateTable();
+        const uint32_t N = species->n_part;
+        std::vector<double> tc = t;
+        const uint32_t p0 = uidx(w0.w[1], N);
+        uint32_t p = p0;
+        std::vector<uint32_t> ps;
+        for (uint32_t step = 0;; ++step) {
+            if (step >= N) return false;
+            ps.push_back(p);
+            const size_t n = ps.size();
+            for (size_t i = 0; i < n; ++i) tc[(size_t)p * N + ps[i]] = 0.;
+            tc[(size_t)p * N + p0] = t[(size_t)p * N + p0];
+            double Qp = 0., Qpc = 0.;
+            for (uint32_t i = 0; i < N; ++i) {
+                Qp += t[(size_t)p * N + i];
+                Qpc += tc[(size_t)p * N + i];
+            }
+            const RNG4 w = st.block(1u + step);
+            if (Qpc / Qp < u53(w.w[0], w.w[1])) return false;
+            const double x = u53(w.w[2], w.w[3]);
+            double tQ = 0.;
+            for (uint32_t i = 0; i < N; ++i) {
+                tQ += tc[(size_t)p * N + i] / Qpc;
+                if (tQ > x) {
+                    p = i;
+                    break;
+                }
+            }
+            if (p == p0) break;
+        }
+        const uint32_t n = (uint32_t)ps.size();
+        cyc.weight = 1.;
+        for (uint32_t i = 0; i + 1 < n; ++i) cyc.weight *= t[(size_t)ps[i] * N + ps[i + 1]] / t[(size_t)ps[i] * N + ps[i]];
+        cyc.weight *= t[(size_t)ps[n - 1] * N + ps[0]] / t[(size_t)ps[n - 1] * N + ps[n - 1]];
+        cyc.part = ps;
+        cyc.type = n - 1;
+        cyc.perm.resize(n);
+        cyc.i_perm.resize(n);
+        for (uint32_t i = 0; i < n; ++i) {
+            cyc.perm[i] = (i + 1) % n;
+            cyc.i_perm[i] = (i + n - 1) % n;
+        }
+        return true;
+    }
+
+    bool Attempt() override {
+        Stream st{seed, chain, move_index, attempt_counter};
+        const RNG4 w0 = st.block(0);
+        const uint32_t N = species->n_part, M = species->n_bead, B = n_bisect_beads;
+        bead0 = uidx(w0.w[0], M);
+        bead1 = bead0 + B;
+        const bool roll_over = bead1 > M - 1;
+        n_perm_part = 0;
+        affected.clear();
+        double perm_tot_0 = 0.;
+        if (table) {
+            std::vector<uint32_t> order;
+            std::vector<double> contrib;
+            perm_tot_0 = TableTotal(&order, &contrib);
+            const double x = u53(w0.w[2], w0.w[3]) * perm_tot_0;
+            size_t k = 0;
+            if (!(x < contrib[0])) {  // SelectCycle, perm_bisect_table_class.h:105-119
+                size_t hi = contrib.size(), lo = 0;
+                while (hi - lo > 1) {
+                    const size_t mid = (hi + lo) >> 1;
+                    if (x < contrib[mid]) hi = mid;
+                    else lo = mid;
+                }
+                k = std::min(hi, contrib.size() - 1);
+            }
+            cyc = all_cycles[order[k]];
+        } else if (!SelectIterative(st, w0))
+            return false;
+        const uint32_t n = (uint32_t)cyc.part.size();
+        n_perm_part = n;
+
+        std::vector<std::vector<uint32_t>> lab(n), sl(n);
+        for (uint32_t i = 0; i < n; ++i) Chain(cyc.part[i], bead0, lab[i], sl[i]);
+        Particles parts;
+        for (uint32_t i = 0; i < n; ++i) parts.push_back({species->s_i, cyc.part[i]});
+        if (roll_over) {
+            for (uint32_t i = 0; i < n; ++i) parts.push_back({species->s_i, lab[i][B]});
+            std::sort(parts.begin(), parts.end());
+            parts.erase(std::unique(parts.begin(), parts.end()), parts.end());
+        }
+        // PermuteBeads (perm_bisect_class.h:32-44): the bead before the end of path i now links to
+        // the end bead of path perm(i).
+        s0 = sl[0][B - 1];
+        std::vector<uint32_t> old_end(n);
+        for (uint32_t i = 0; i < n; ++i) old_end[i] = lab[i][B];
+        for (uint32_t i = 0; i < n; ++i) species->nxt[(size_t)lab[i][B - 1] * M + s0] = old_end[cyc.perm[i]];
+        for (uint32_t i = 0; i < n; ++i) lab[i][B] = old_end[cyc.perm[i]];
+        for (uint32_t i = 0; i < n; ++i)
+            for (uint32_t k = 1; k < B; ++k) affected.push_back({lab[i][k], sl[i][k]});
+
+        double prev_action_change = -std::log(cyc.weight);
+        uint32_t mid_counter = 0;
+        const uint32_t base_m = 1u + N, base_u = base_m + N * (B - 1u);
+        for (int level_i = (int)n_level - 1; level_i >= 0; --level_i) {
+            double old_lsp = 0., new_lsp = 0.;
+            for (uint32_t i = 0; i < n; ++i) SampleLevel(st, mid_counter, base_m, level_i, lab[i], sl[i], old_end[i], sl[i][B], old_lsp, new_lsp);
+            const double current = ActionChange(parts, level_i);
+            const double log_accept = -new_lsp + old_lsp - current + prev_action_change;
+            const RNG4 wu = st.block(base_u + (n_level - 1u - (uint32_t)level_i));
+            if (log_accept < (double)logf_spec(u24(wu.w[0]))) return false;
+            prev_action_change = current;
+        }
+        if (table && n < N) {  // perm_bisect_table_class.h:216-225
+            path.mode = NEW_MODE;
+            const double perm_tot_1 = TableTotal(nullptr, nullptr);
+            const RNG4 wf = st.block(base_u + n_level);
+            if (perm_tot_0 / perm_tot_1 < u53(wf.w[0], wf.w[1])) return false;
+        }
+        return true;
+    }
+
+    // AssignParticleLabels (perm_bisect_class.h:47-56): beads after slice s0 take the label of the
+    // path that reaches them from slice s0; their positions, densities and links move with them.
+    void AssignParticleLabels() {
+        const uint32_t N = species->n_part, M = species->n_bead, nd = path.n_d;
+        const size_t K = path.ks.K();
+        std::vector<uint32_t> src((size_t)N * M);
+        for (uint32_t p = 0; p < N; ++p) {
+            uint32_t q = p;
+            for (uint32_t b = s0; b < M; ++b) {
+                src[(size_t)p * M + b] = q;
+                if (b + 1 < M) q = path.NextLabel(*species, q, b, NEW_MODE);
+            }
+        }
+        const std::vector<double> r0 = path.r, rc0 = path.r_c;
+        const std::vector<cplx> k0 = species->bead_rho_k, kc0 = species->bead_rho_k_c;
+        const std::vector<uint32_t> n0 = species->nxt, nc0 = species->nxt_c;
+        for (uint32_t p = 0; p < N; ++p) {
+            for (uint32_t b = s0 + 1; b < M; ++b) {
+                const uint32_t q = src[(size_t)p * M + b];
+                std::copy(r0.begin() + path.Idx(*species, q, b), r0.begin() + path.Idx(*species, q, b) + nd, path.r.begin() + path.Idx(*species, p, b));
+                std::copy(rc0.begin() + path.Idx(*species, q, b), rc0.begin() + path.Idx(*species, q, b) + nd, path.r_c.begin() + path.Idx(*species, p, b));
+                if (K) {
+                    std::copy(k0.begin() + ((size_t)q * M + b) * K, k0.begin() + ((size_t)q * M + b + 1) * K, species->bead_rho_k.begin() + ((size_t)p * M + b) * K);
+                    std::copy(kc0.begin() + ((size_t)q * M + b) * K, kc0.begin() + ((size_t)q * M + b + 1) * K, species->bead_rho_k_c.begin() + ((size_t)p * M + b) * K);
+                }
+            }
+            for (uint32_t b = s0; b + 1 < M; ++b) species->nxt[(size_t)p * M + b] = species->nxt_c[(size_t)p * M + b] = p;
+            const uint32_t q = src[(size_t)p * M + M - 1];
+            species->nxt[(size_t)p * M + M - 1] = n0[(size_t)q * M + M - 1];
+            species->nxt_c[(size_t)p * M + M - 1] = nc0[(size_t)q * M + M - 1];
+        }
+    }
+
+    // perm_bisect_class.h:59-73 (the stores of Bisect::Accept act on the moved beads before their
+    // relabelling, which carries both copies along)
+    void Accept() override {
+        const uint32_t M = species->n_bead;
+        for (uint32_t p = 0; p < species->n_part; ++p) species->nxt_c[(size_t)p * M + s0] = species->nxt[(size_t)p * M + s0];
+        Bisect::Accept();
+        if (n_perm_part > 1) AssignParticleLabels();
+        perm_attempt[n_perm_part - 1]++;
+        perm_accept[n_perm_part - 1]++;
+    }
+
+    // perm_bisect_class.h:75-90
+    void Reject() override {
+        if (n_perm_part > 0) {
+            const uint32_t M = species->n_bead;
+            for (uint32_t p = 0; p < species->n_part; ++p) species->nxt[(size_t)p * M + s0] = species->nxt_c[(size_t)p * M + s0];
+            perm_attempt[n_perm_part - 1]++;
+        }
+        Bisect::Reject();
+    }
+
+    // perm_bisect_class.h:93-97, 119-132 (counters reset at every Write)
+    void ResetBlock() override {
+        Bisect::ResetBlock();
+        std::fill(perm_attempt.begin(), perm_attempt.end(), 0);
+        std::fill(perm_accept.begin(), perm_accept.end(), 0);
     }
 };
 
@@ -1951,7 +2369,7 @@ struct Energy : Observable {
 
     void Accumulate() override {
         path.mode = NEW_MODE;
-        double cof = 1.;  // sign * importance weight (no fermions, no importance actions)
+        double cof = path.GetSign();  // sign * importance weight (no importance-weight actions)
         if (use_thermal) Thermal(cof);
         else if (use_virial) Virial(cof);
         if (measure_potential)
@@ -2028,7 +2446,7 @@ struct PairCorrelation : Observable {
     uint32_t ReverseMap(double r) const { return (uint32_t)std::nearbyint((r - r_min) * d_ir - 0.5); }
     void Accumulate() override {
         path.mode = NEW_MODE;
-        double cof = 1.;
+        double cof = path.GetSign();
         double t[3];
         for (uint32_t b = 0; b < path.n_bead; ++b)
             for (auto& pr : pairs) {
@@ -2085,12 +2503,13 @@ struct StructureFactor : Observable {
     void Init() { sk.assign(path.ks.K(), 0.); }
     void Accumulate() override {
         path.mode = NEW_MODE;
+        const double cof = path.GetSign();
         const auto& ra = path.GetRhoK(*sa);
         const auto& rb = path.GetRhoK(*sb);
         size_t K = path.ks.K();
         for (size_t k = 0; k < K; ++k)
             if (path.ks.mags[k] < k_cut)
-                for (uint32_t b = 0; b < path.n_bead; ++b) sk[k] += 1. * CMag2(ra[(size_t)b * K + k], rb[(size_t)b * K + k]);
+                for (uint32_t b = 0; b < path.n_bead; ++b) sk[k] += cof * CMag2(ra[(size_t)b * K + k], rb[(size_t)b * K + k]);
         n_measure++;
     }
     void Reset() override {
@@ -2103,6 +2522,129 @@ struct StructureFactor : Observable {
         double norm = (double)n_measure * path.n_bead * sa->n_part * sb->n_part;
         out.resize(sk.size());
         for (size_t k = 0; k < sk.size(); ++k) out[k] = sk[k] / norm;
+        Reset();
+        return out;
+    }
+};
+
+// sign_class.h:7-51: the block mean of the path's sign.
+struct SignObs : Observable {
+    Path& path;
+    double sign = 0.;
+    SignObs(Path& p, const Input& in) : path(p) {
+        name = in.GetAttribute<std::string>("name");
+        type = in.GetAttribute<std::string>("type");
+    }
+    void Accumulate() override {
+        sign += path.GetSign();
+        n_measure++;
+    }
+    void Reset() override {
+        n_measure = 0;
+        sign = 0.;
+    }
+    std::vector<double> Block() override {
+        std::vector<double> out;
+        if (n_measure == 0) return out;
+        out.push_back(sign / n_measure);
+        Reset();
+        return out;
+    }
+};
+
+// permutation_class.h:7-119: the normalised histogram of cycle lengths, then the (sector, count)
+// pairs of the block in increasing sector order. Sectors are the partitions of N into cycle
+// lengths, numbered in the order the ascending-composition generation of species_class.h:178-221
+// produces them (the reference's guard there skips the generation, leaving the lookup of :172-175
+// without entries; the numbering it intends is used).
+struct PermutationObs : Observable {
+    Path& path;
+    Species* species;
+    std::vector<double> cycles;
+    std::vector<uint32_t> sectors;
+    std::vector<std::vector<uint32_t>> partitions;
+    PermutationObs(Path& p, const Input& in) : path(p) {
+        name = in.GetAttribute<std::string>("name");
+        type = in.GetAttribute<std::string>("type");
+        species = &p.GetSpecies(in.GetAttribute<std::string>("species"));
+        const uint32_t sector_max = in.GetAttribute<uint32_t>("sector_max", 0);
+        partitions = Partitions(species->n_part, sector_max);
+        cycles.assign(species->n_part, 0.);
+    }
+    // Accelerated ascending-composition generation of the partitions of n (Kelleher and O'Sullivan).
+    static std::vector<std::vector<uint32_t>> Partitions(uint32_t n, uint32_t cap) {
+        std::vector<std::vector<uint32_t>> out;
+        if (n == 0) return out;
+        std::vector<uint32_t> a(n + 1, 0);
+        uint32_t k = 1, y = n - 1;
+        auto room = [&]() { return cap == 0 || out.size() < cap; };
+        while (k != 0 && room()) {
+            uint32_t x = a[k - 1] + 1;
+            k -= 1;
+            while (2 * x <= y) {
+                a[k] = x;
+                y -= x;
+                k += 1;
+            }
+            const uint32_t l = k + 1;
+            while (x <= y && room()) {
+                a[k] = x;
+                a[l] = y;
+                out.emplace_back(a.begin(), a.begin() + k + 2);
+                x += 1;
+                y -= 1;
+            }
+            a[k] = x + y;
+            y = x + y - 1;
+            out.emplace_back(a.begin(), a.begin() + k + 1);
+        }
+        return out;
+    }
+    std::vector<uint32_t> CycleLengths() const {
+        std::vector<uint32_t> out;
+        std::vector<char> seen(species->n_part, 0);
+        for (uint32_t p = 0; p < species->n_part; ++p) {
+            if (seen[p]) continue;
+            uint32_t len = 0, q = p;
+            do {
+                seen[q] = 1;
+                q = path.NextLabel(*species, q, species->n_bead - 1, NEW_MODE);
+                ++len;
+            } while (q != p);
+            out.push_back(len);
+        }
+        return out;
+    }
+    void Accumulate() override {
+        auto c = CycleLengths();
+        for (uint32_t l : c) cycles[l - 1] += 1.;
+        std::sort(c.begin(), c.end());
+        uint32_t sector = (uint32_t)partitions.size();  // not among the first sector_max partitions
+        for (size_t i = 0; i < partitions.size(); ++i)
+            if (partitions[i] == c) sector = (uint32_t)i;
+        sectors.push_back(sector);
+        n_measure++;
+    }
+    void Reset() override {
+        n_measure = 0;
+        std::fill(cycles.begin(), cycles.end(), 0.);
+        sectors.clear();
+    }
+    std::vector<double> Block() override {
+        std::vector<double> out;
+        if (n_measure == 0) return out;
+        double n_cycles = 0.;
+        for (double c : cycles) n_cycles += c;
+        for (double c : cycles) out.push_back(c / n_cycles);
+        std::vector<uint32_t> s = sectors;
+        std::sort(s.begin(), s.end());
+        for (size_t i = 0; i < s.size();) {
+            size_t j = i;
+            while (j < s.size() && s[j] == s[i]) ++j;
+            out.push_back((double)s[i]);
+            out.push_back((double)(j - i));
+            i = j;
+        }
         Reset();
         return out;
     }
@@ -2146,6 +2688,8 @@ struct Simulation {
             std::string t = m.GetAttribute<std::string>("type");
             if (t == "Bisect") moves.emplace_back(new Bisect(*path, actions, m, mi, seed, chain));
             else if (t == "HMC") moves.emplace_back(new HMC(*path, actions, m, mi, seed, chain));
+            else if (t == "PermBisectIterative") moves.emplace_back(new PermBisect(*path, actions, m, mi, seed, chain, false));
+            else if (t == "PermBisectTable") moves.emplace_back(new PermBisect(*path, actions, m, mi, seed, chain, true));
             else throw InputError("unsupported move type '" + t + "'");
             ++mi;
         }
@@ -2154,6 +2698,8 @@ struct Simulation {
             if (t == "Energy") observables.emplace_back(new Energy(*path, actions, o));
             else if (t == "PairCorrelation") observables.emplace_back(new PairCorrelation(*path, o));
             else if (t == "StructureFactor") observables.emplace_back(new StructureFactor(*path, o));
+            else if (t == "Sign") observables.emplace_back(new SignObs(*path, o));
+            else if (t == "Permutation") observables.emplace_back(new PermutationObs(*path, o));
             else if (t == "Time" || t == "PathDump") continue;  // bookkeeping only
             else throw InputError("unsupported observable type '" + t + "'");
         }
@@ -2421,6 +2967,51 @@ int oracle_move_stats(void* h, uint32_t m, uint64_t* out) {
     out[1] = mv->n_attempt;
     out[2] = mv->n_accept;
     return 0;
+}
+
+// Per cycle length n: attempts and accepts of a permuting move in the current block
+// (perm_bisect_class.h:25-26); out[2 N].
+int oracle_perm_stats(void* h, uint32_t m, uint64_t* out) {
+    try {
+        auto* mv = dynamic_cast<orc::PermBisect*>(S(h)->moves.at(m).get());
+        if (!mv) throw std::invalid_argument("not a permuting move");
+        const size_t N = mv->perm_attempt.size();
+        for (size_t i = 0; i < N; ++i) {
+            out[i] = mv->perm_attempt[i];
+            out[N + i] = mv->perm_accept[i];
+        }
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+}
+
+// The path permutation of a species: out[p] = particle whose slice-0 bead follows (p, M - 1).
+int oracle_get_perm(void* h, uint32_t sp, uint32_t* out) {
+    try {
+        auto& path = *S(h)->path;
+        auto pi = path.Closure(path.species.at(sp));
+        std::copy(pi.begin(), pi.end(), out);
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
+}
+
+int oracle_set_perm(void* h, uint32_t sp, const uint32_t* pi) {
+    try {
+        auto& path = *S(h)->path;
+        auto& s = path.species.at(sp);
+        std::vector<char> seen(s.n_part, 0);
+        for (uint32_t p = 0; p < s.n_part; ++p) {
+            if (pi[p] >= s.n_part || seen[pi[p]]) throw std::invalid_argument("not a permutation");
+            seen[pi[p]] = 1;
+        }
+        for (uint32_t p = 0; p < s.n_part; ++p) s.nxt[(size_t)p * s.n_bead + s.n_bead - 1] = s.nxt_c[(size_t)p * s.n_bead + s.n_bead - 1] = pi[p];
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(e);
+    }
 }
 
 int oracle_obs_accumulate(void* h, uint32_t o) {

@@ -73,6 +73,9 @@ SIGNATURES = {
     "pimc_move_attempts": (C.c_int, [_P, C.c_uint32, C.c_uint64]),
     "pimc_sweep": (C.c_int, [_P, _U32P, _U64P, C.c_uint32, C.c_uint64]),
     "pimc_move_stats": (C.c_int, [_P, C.c_uint32, _U64P]),
+    "pimc_get_perm": (C.c_int, [_P, C.c_uint32, _U32P]),
+    "pimc_set_perm": (C.c_int, [_P, C.c_uint32, _U32P]),
+    "pimc_perm_stats": (C.c_int, [_P, C.c_uint32, _U64P, C.c_size_t]),
     "pimc_observable_accumulate": (C.c_int, [_P, C.c_uint32]),
     "pimc_observable_block": (C.c_int, [_P, C.c_uint32, _DP, C.c_size_t, _SZP]),
     "pimc_run": (C.c_int, [_P]),
@@ -303,6 +306,23 @@ class Simulation:
         mv = np.ascontiguousarray(moves, dtype=np.uint32)
         ct = np.ascontiguousarray(counts, dtype=np.uint64)
         self._check(self._lib.pimc_sweep(self._h, mv.ctypes.data_as(_U32P), ct.ctypes.data_as(_U64P), len(mv), n_rep))
+
+    def get_perm(self, species: int):
+        """Path permutation of a species: perm[p] = particle whose slice-0 bead follows (p, M - 1)."""
+        n, _, _ = self.species_info(species)
+        out = np.zeros(n, dtype=np.uint32)
+        self._check(self._lib.pimc_get_perm(self._h, species, out.ctypes.data_as(_U32P)))
+        return out.astype(np.int64)
+
+    def set_perm(self, species: int, perm):
+        pi = np.ascontiguousarray(perm, dtype=np.uint32)
+        self._check(self._lib.pimc_set_perm(self._h, species, pi.ctypes.data_as(_U32P)))
+
+    def perm_stats(self, move: int, n_part: int):
+        """Per cycle length: (attempts, accepts) of a permuting move in the current block."""
+        out = np.zeros(2 * n_part, dtype=np.uint64)
+        self._check(self._lib.pimc_perm_stats(self._h, move, out.ctypes.data_as(_U64P), out.size))
+        return out[:n_part].astype(np.int64), out[n_part:].astype(np.int64)
 
     def move_stats(self, move: int):
         """(total attempts, attempts in block, accepts in block)."""

@@ -30,6 +30,7 @@ SOURCES = [
     SRC / "kernels" / "sweep.cu",
     SRC / "kernels" / "batch.cu",
     SRC / "kernels" / "adjoint.cu",
+    SRC / "kernels" / "perm.cu",
     SRC / "noalloc.cu",
 ]
 

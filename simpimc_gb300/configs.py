@@ -10,7 +10,10 @@ systems follow the reference's input format (inputs/*.xml): <System>, <Particles
   r_s, Coulomb split into a short-range primitive part and an Ewald long-range k-sum; beads
   uniform in the box.
 
-Both take ``pair="IlkkaPairAction"`` or ``pair="DavidPairAction"`` (with ``n_order``) to use the
+* ``trapped_bosons``: N bosons (or sign-weighted fermions) in the same trap, with a permuting
+  bisection (PermBisectIterative or PermBisectTable) beside the plain one; optional Coulomb.
+
+The first two take ``pair="IlkkaPairAction"`` or ``pair="DavidPairAction"`` (with ``n_order``) to use the
 off-diagonal pair action of a synthetic ``tables.ilkka_table`` / ``tables.david_table`` instead of
 the primitive BarePairAction.
 """
@@ -173,3 +176,59 @@ def sweep_schedule(sim_or_counts, n_bisect_beads: int, n_bead: int):
     """One sweep: N_s * ceil(M / 2^l) attempts of each species' bisection move, in move order."""
     counts = [n * math.ceil(n_bead / n_bisect_beads) for n in sim_or_counts]
     return list(range(len(counts))), counts
+
+
+def trapped_bosons(workdir, *, n_part=3, beta=2.0, n_bead=16, omega=1.0, n_level=2, seed=1234, coulomb=False,
+                   perm="PermBisectIterative", n_perm_part=2, fermi=False, n_step_inner=100, n_step_outer=10,
+                   path_seed=None, perm_level=None):
+    """Identical particles with exchange: the permuting move's species carries the path
+    permutation. Observables: Energy (thermal), Permutation (cycle histogram and sectors), Sign."""
+    workdir = Path(workdir)
+    workdir.mkdir(parents=True, exist_ok=True)
+    pair_xml = ""
+    if coulomb:
+        tab = workdir / "coulomb_open.pat"
+        coulomb_table(tab, z_ab=1.0, L=0.0)
+        pair_xml = (f'<Action name="Coulomb" type="BarePairAction" file="{tab.name}" is_coulomb="1" species_a="b" '
+                    f'species_b="b" max_level="0" use_long_range="0" />')
+    extra = f' n_perm_part="{n_perm_part}"' if perm == "PermBisectTable" else ""
+    perm_level = n_level if perm_level is None else perm_level
+    xml = f"""<Input>
+  <RNG seed="{seed}" />
+  <IO output_prefix="bosons" />
+  <Parallel procs_per_group="1" />
+  <System n_d="3" n_bead="{n_bead}" beta="{beta}" pbc="0" />
+  <Particles>
+    <Species name="b" n_part="{n_part}" lambda="0.5" fermi="{int(fermi)}" init_type="File" file_name="init.xyz" all_beads="1" />
+  </Particles>
+  <Actions>
+    <Action name="Kinetic" type="Kinetic" n_images="0" species="b" />
+    <Action name="Trap" type="HarmonicTrap" species="b" omega="{omega}" max_level="0" />
+    {pair_xml}
+  </Actions>
+  <Moves>
+    <Move name="Bisect" type="Bisect" species="b" n_level="{n_level}" />
+    <Move name="Perm" type="{perm}" species="b" n_level="{perm_level}"{extra} />
+  </Moves>
+  <Observables>
+    <Observable name="Energy" type="Energy" />
+    <Observable name="Permutation" type="Permutation" species="b" />
+    <Observable name="Sign" type="Sign" />
+  </Observables>
+  <Algorithm>
+    <Loop n_step="{n_step_outer}">
+      <Loop n_step="{n_step_inner}">
+        <Move name="Bisect" />
+        <Move name="Perm" />
+        <Observable name="Energy" />
+        <Observable name="Permutation" />
+        <Observable name="Sign" />
+      </Loop>
+      <Write />
+    </Loop>
+  </Algorithm>
+</Input>
+"""
+    rng = np.random.default_rng(seed if path_seed is None else path_seed)
+    path = rng.standard_normal((n_part, n_bead, 3))
+    return xml, path

@@ -199,6 +199,31 @@ int pimc_move_stats(pimc_ctx* ctx, uint32_t move, uint64_t* out) {
     });
 }
 
+int pimc_get_perm(pimc_ctx* ctx, uint32_t species, uint32_t* perm) {
+    if (!perm) return PIMC_ERR_ARG;
+    return Guard(ctx, [&](pimc::Context& c) { c.GetPerm(species, perm); });
+}
+
+int pimc_set_perm(pimc_ctx* ctx, uint32_t species, const uint32_t* perm) {
+    if (!perm) return PIMC_ERR_ARG;
+    return Guard(ctx, [&](pimc::Context& c) { c.SetPerm(species, perm); });
+}
+
+int pimc_perm_stats(pimc_ctx* ctx, uint32_t move, uint64_t* out, size_t cap) {
+    if (!out) return PIMC_ERR_ARG;
+    return Guard(ctx, [&](pimc::Context& c) {
+        if (move >= c.moves.size()) throw pimc::PimcError(PIMC_ERR_ARG, "move index out of range");
+        const auto& mh = c.moves[move];
+        if (mh.kind != 2 && mh.kind != 3) throw pimc::PimcError(PIMC_ERR_ARG, "not a permuting move");
+        const size_t N = mh.perm_attempt.size();
+        if (cap < 2 * N) throw pimc::PimcError(PIMC_ERR_ARG, "output shorter than twice the particle count");
+        for (size_t i = 0; i < N; ++i) {
+            out[i] = mh.perm_attempt[i];
+            out[N + i] = mh.perm_accept[i];
+        }
+    });
+}
+
 int pimc_observable_accumulate(pimc_ctx* ctx, uint32_t observable) {
     return Guard(ctx, [&](pimc::Context& c) { c.ObservableAccumulate(observable); });
 }

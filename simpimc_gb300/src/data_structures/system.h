@@ -168,6 +168,11 @@ struct SystemDev {
 
     double* pos = nullptr;      // committed ("old") copy  [M][3][n_pad]
     double* pos_new = nullptr;  // proposal ("new") copy   [M][3][n_pad]
+    // Path permutation at the ring closure: bead (g, M - 1) is followed by bead (perm[g], 0)
+    // (bead_class.h:38-41 links after the relabelling of perm_bisect_class.h:47-56); perm_inv is
+    // its inverse. Identity without exchanges.
+    const uint32_t* perm = nullptr;      // [n_total]
+    const uint32_t* perm_inv = nullptr;  // [n_total]
 
     uint32_t K = 0;
     int32_t max_index[3] = {0, 0, 0};

@@ -77,7 +77,15 @@ struct MoveHost {
     std::vector<double> out_attempt, out_accept, out_ratio, out_level;
     // Hybrid Monte Carlo move (no reference counterpart): leapfrog on the whole path driven by
     // the adjoint gradient of the total action.
-    int kind = 0;                // 0 Bisect, 1 HMC
+    int kind = 0;                // 0 Bisect, 1 HMC, 2 PermBisectIterative, 3 PermBisectTable
+    // Permuting bisection (perm_bisect_class.h:19-29): epsilon of the weight table, per cycle
+    // length the block's attempts and accepts (appended per Write), and for the table variant the
+    // particle subsets and their permutations (lexicographic order) on the device.
+    double perm_epsilon = 1.e-100;
+    uint32_t perm_k = 0, perm_n_comb = 0, perm_n_types = 0, perm_n_type_out = 0;
+    std::vector<uint64_t> perm_attempt, perm_accept;
+    std::vector<std::vector<double>> out_perm_attempt, out_perm_accept;
+    std::shared_ptr<DeviceBuffer> perm_combs, perm_types;
     double hmc_step = 0.01;
     uint32_t hmc_steps = 10;
     int hmc_species = -1;        // -1: every species moves
@@ -85,7 +93,8 @@ struct MoveHost {
 
 struct ObservableHost {
     std::string name, type;
-    int kind = 0;  // 0 energy, 1 pair correlation, 2 structure factor, 3 ignored bookkeeping, 4 path dump
+    int kind = 0;  // 0 energy, 1 pair correlation, 2 structure factor, 3 ignored bookkeeping, 4 path dump,
+                   // 5 sign, 6 permutation
     uint64_t n_measure = 0;
     // Energy (energy_class.h:7-326)
     bool measure_potential = false, use_thermal = true, use_virial = false;
@@ -104,6 +113,14 @@ struct ObservableHost {
     uint32_t skip = 1;
     uint64_t n_write_calls = 0;
     std::vector<std::vector<std::vector<double>>> dumps;  // [species][dump] positions
+    std::vector<std::vector<std::vector<double>>> dump_perms;  // [species][dump] (prev, next) per particle
+    // Sign (sign_class.h:7-51) and Permutation (permutation_class.h:7-119): the block's sign sum,
+    // cycle-length counts and sector of each measurement; the partitions of N in sector order.
+    double sign_sum = 0.;
+    uint32_t species = 0, sector_max = 0;
+    std::vector<double> cycles;
+    std::vector<uint32_t> sectors;
+    std::vector<std::vector<uint32_t>> partitions;
 };
 
 struct LoopNode {
@@ -149,6 +166,21 @@ class Context {
 
     // --- moves, observables, algorithm ---
     void MoveAttempts(uint32_t m, uint64_t n);
+    // Bisection on a species with exchanges (src/kernels/perm.cu): the permuting moves and the
+    // plain bisection of a species that has one or carries a non-identity path permutation.
+    void PermAttempts(uint32_t m, uint64_t n);
+    bool PermutingSpecies(uint32_t s) const;
+    // The path permutation: perm[g] = particle whose slice-0 bead follows bead (g, M - 1), global
+    // indices; the host copy is refreshed after every device update.
+    void SyncPermHost();
+    bool PermIdentity(uint32_t s) const;
+    bool AnyPerm() const;
+    void SetPerm(uint32_t s, const uint32_t* pi);  // species-local indices
+    void GetPerm(uint32_t s, uint32_t* out) const;
+    std::vector<uint32_t> CycleLengths(uint32_t s) const;
+    double PathSign() const;
+    std::vector<uint32_t> perm_host;
+    std::vector<int> species_fermi;
     void Sweep(const uint32_t* moves, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep);
     void ObservableAccumulate(uint32_t o);
     std::vector<double> ObservableBlock(uint32_t o);
@@ -242,6 +274,7 @@ class Context {
     std::unique_ptr<DeviceBuffer> grad_, mom_, pos_save_, rho_scratch_, phase_tab_;  // adjoint / HMC work arrays
     std::vector<std::unique_ptr<DeviceBuffer>> adj_vk_;                              // double-float v_k per action
     std::unique_ptr<DeviceBuffer> partials_, result_, bar_, err_, pairs_, rho_tmp_, parts_, kmag_dev_, sched_, accepts_;
+    std::unique_ptr<DeviceBuffer> perm_, perm_inv_, perm_t_, perm_cyc_, perm_drho_, perm_hold_, perm_cnt_;
     size_t partials_cap_ = 0, pairs_cap_ = 0, rho_tmp_cap_ = 0, parts_cap_ = 0;
 
     template <class T>

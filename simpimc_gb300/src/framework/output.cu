@@ -58,12 +58,20 @@ void Context::WriteOutput(const std::string& path) {
         w.Vec(pre + "n_accept", mh.out_accept);
         w.Vec(pre + "x", mh.out_ratio);
         if (mh.adaptive) w.Vec(pre + "n_level", mh.out_level);
+        if (mh.kind == 2 || mh.kind == 3) {  // perm_bisect_class.h:119-132
+            w.Num(pre + "n_perm_type", (double)mh.perm_n_type_out);
+            std::vector<double> pa, pc;
+            for (const auto& v : mh.out_perm_attempt) pa.insert(pa.end(), v.begin(), v.end());
+            for (const auto& v : mh.out_perm_accept) pc.insert(pc.end(), v.begin(), v.end());
+            w.Vec(pre + "perm_attempt", pa);
+            w.Vec(pre + "perm_accept", pc);
+        }
     }
     for (size_t oi = 0; oi < observables.size(); ++oi) {
         const ObservableHost& o = observables[oi];
         const std::string pre = "Observables/" + o.name + "/";
         w.Str(pre + "type", o.type);
-        w.Str(pre + "data_type", (o.kind == 1 || o.kind == 2) ? "histogram" : "none");
+        w.Str(pre + "data_type", (o.kind == 1 || o.kind == 2) ? "histogram" : (o.kind == 5 ? "scalar" : "none"));
         const auto& bl = blocks[oi];
         if (o.kind == 0) {
             // block layout: E, the per-action energies, then (with measure_potential) V and the potentials
@@ -119,20 +127,41 @@ void Context::WriteOutput(const std::string& path) {
             std::vector<double> y;
             for (const auto& b : bl) y.insert(y.end(), b.begin(), b.end());
             w.Vec(pre + "y", y);
+        } else if (o.kind == 5) {
+            std::vector<double> x;
+            for (const auto& b : bl) x.push_back(b.empty() ? 0. : b[0]);
+            w.Vec(pre + "x", x);
+        } else if (o.kind == 6) {
+            // permutation_class.h:36-73, 89-111
+            const uint32_t n = sys.sp_n[o.species];
+            w.Str(pre + "species", species_names[o.species]);
+            w.Num(pre + "sector_max", (double)o.sector_max);
+            w.Str(pre + "sectors/data_type", "pairs");
+            std::vector<double> xs(o.partitions.size()), poss((size_t)n * o.partitions.size(), 0.);
+            for (size_t i = 0; i < o.partitions.size(); ++i) {
+                xs[i] = (double)i;
+                for (uint32_t len : o.partitions[i]) poss[(size_t)(len - 1) * o.partitions.size() + i] += 1.;  // (n, n_perm) row-major
+            }
+            w.Vec(pre + "sectors/x", xs);
+            w.Vec(pre + "sectors/possPerms", poss);
+            w.Str(pre + "cycles/data_type", "histogram");
+            std::vector<double> cx(n), cy, sy;
+            for (uint32_t i = 0; i < n; ++i) cx[i] = i + 1.;
+            for (const auto& b : bl) {
+                cy.insert(cy.end(), b.begin(), b.begin() + std::min<size_t>(n, b.size()));
+                if (b.size() > n) sy.insert(sy.end(), b.begin() + n, b.end());
+            }
+            w.Vec(pre + "cycles/x", cx);
+            w.Vec(pre + "cycles/y", cy);
+            w.Vec(pre + "sectors/y", sy);
         } else if (o.kind == 4) {
             for (uint32_t sp = 0; sp < sys.S; ++sp) {
                 const std::string spre = pre + species_names[sp] + "/";
                 const auto& dumps = o.dumps[sp];
                 w.Num(spre + "n_dump", (double)dumps.size());
                 std::vector<double> pos, perm;
-                for (const auto& d : dumps) {
-                    pos.insert(pos.end(), d.begin(), d.end());
-                    // no permutations: each bead closes on its own particle
-                    for (uint32_t p = 0; p < sys.sp_n[sp]; ++p) {
-                        perm.push_back((double)p);
-                        perm.push_back((double)p);
-                    }
-                }
+                for (const auto& d : dumps) pos.insert(pos.end(), d.begin(), d.end());
+                for (const auto& d : o.dump_perms[sp]) perm.insert(perm.end(), d.begin(), d.end());
                 w.Vec(spre + "positions", pos);
                 w.Vec(spre + "permutation", perm);
             }
@@ -144,6 +173,8 @@ void Context::WriteOutput(const std::string& path) {
 void Context::ApplyRestarts() {
     if (restarts.empty()) return;
     std::vector<double> host((size_t)sys.n_total * sys.M * sys.n_d, 0.);
+    GetPath(0, host.data());  // species not restarted keep their positions
+    std::vector<std::pair<uint32_t, std::vector<uint32_t>>> new_perms;
     for (const auto& r : restarts) {
         TableFile t = TableFile::Load(r.file);
         const std::string pre = "Observables/" + r.dump_name + "/" + species_names[r.species] + "/";
@@ -152,16 +183,26 @@ void Context::ApplyRestarts() {
         const size_t per = (size_t)sys.sp_n[r.species] * sys.M * sys.n_d;
         if (n_dump == 0 || pos.size() < per * n_dump)
             throw PimcError(kErrInput, "restart file '" + r.file + "': no complete path dump for species " + species_names[r.species]);
+        // the last dump's permutation (species_class.h:366-376): next particle at the closure,
+        // checked against the recorded previous particles
         const auto& perm = t.Vec(pre + "permutation");
-        for (uint32_t p = 0; p < sys.sp_n[r.species]; ++p) {
-            const size_t at = ((size_t)(n_dump - 1) * sys.sp_n[r.species] + p) * 2;
-            if (at + 1 >= perm.size() || perm[at] != p || perm[at + 1] != p)
-                throw PimcError(kErrUnsupported, "restart file '" + r.file + "': permuted paths are not supported");
+        const uint32_t N = sys.sp_n[r.species];
+        std::vector<uint32_t> next(N);
+        for (uint32_t p = 0; p < N; ++p) {
+            const size_t at = ((size_t)(n_dump - 1) * N + p) * 2;
+            if (at + 1 >= perm.size() || !(perm[at + 1] >= 0.) || perm[at + 1] >= N)
+                throw PimcError(kErrInput, "restart file '" + r.file + "': incomplete permutation");
+            next[p] = (uint32_t)perm[at + 1];
         }
+        for (uint32_t p = 0; p < N; ++p)
+            if (perm[((size_t)(n_dump - 1) * N + next[p]) * 2] != p)
+                throw PimcError(kErrInput, "restart file '" + r.file + "': permutation columns disagree");
+        new_perms.push_back({r.species, next});
         // positions(d, p n_bead + b, n_dump - 1) of the reference's cube read (species_class.h:354-364)
         std::copy(pos.begin() + per * (n_dump - 1), pos.begin() + per * n_dump, host.begin() + (size_t)sys.sp_off[r.species] * sys.M * sys.n_d);
     }
     SetPath(2, host.data());
+    for (const auto& np : new_perms) SetPerm(np.first, np.second.data());
 }
 
 }  // namespace pimc

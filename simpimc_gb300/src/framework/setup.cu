@@ -315,8 +315,11 @@ void Context::BuildPath(const Input& in) {
         const uint32_t n = s.GetAttribute<uint32_t>("n_part");
         const double lam = s.GetAttribute<double>("lambda");
         if (n == 0) throw PimcError(kErrInput, "species with n_part = 0");
-        if (s.GetAttribute<bool>("fermi", false) || s.GetAttribute<bool>("fixed_node", false))
-            throw PimcError(kErrUnsupported, "fermion / fixed-node species are not supported");
+        // Fermions are sampled as bosons and measured with the permutation sign (Species::GetSign,
+        // species_class.h:149-157); the fixed-node restriction needs the nodal actions, which are not built.
+        if (s.GetAttribute<bool>("fixed_node", false))
+            throw PimcError(kErrUnsupported, "fixed-node species are not supported (no nodal actions)");
+        species_fermi.push_back(s.GetAttribute<bool>("fermi", false) ? 1 : 0);
         species_names.push_back(s.GetAttribute<std::string>("name"));
         if (s.GetAttribute<std::string>("init_type", "") == "Restart") {
             // species_class.h:336-345: <prefix>.<proc>.h5 in the reference; the table container here
@@ -338,6 +341,14 @@ void Context::BuildPath(const Input& in) {
     pos_new_.reset(new DeviceBuffer((size_t)sys.M * 3 * sys.n_pad * sizeof(double)));
     sys.pos = pos_->as<double>();
     sys.pos_new = pos_new_->as<double>();
+    perm_.reset(new DeviceBuffer(sys.n_total * sizeof(uint32_t)));
+    perm_inv_.reset(new DeviceBuffer(sys.n_total * sizeof(uint32_t)));
+    perm_host.resize(sys.n_total);
+    for (uint32_t g = 0; g < sys.n_total; ++g) perm_host[g] = g;
+    CudaCheck(cudaMemcpy(perm_->ptr, perm_host.data(), sys.n_total * sizeof(uint32_t), cudaMemcpyHostToDevice), "perm upload");
+    CudaCheck(cudaMemcpy(perm_inv_->ptr, perm_host.data(), sys.n_total * sizeof(uint32_t), cudaMemcpyHostToDevice), "perm upload");
+    sys.perm = perm_->as<uint32_t>();
+    sys.perm_inv = perm_inv_->as<uint32_t>();
 }
 
 static uint32_t SpeciesIndex(const std::vector<std::string>& names, const std::string& n) {
@@ -725,7 +736,9 @@ void Context::BuildMoves(const Input& in) {
             moves.push_back(h);
             continue;
         }
-        if (h.type != "Bisect") throw PimcError(kErrUnsupported, "unsupported move type '" + h.type + "'");
+        if (h.type == "PermBisectIterative") h.kind = 2;
+        else if (h.type == "PermBisectTable") h.kind = 3;
+        else if (h.type != "Bisect") throw PimcError(kErrUnsupported, "unsupported move type '" + h.type + "'");
         MoveDev& d = h.dev;
         d.species = SpeciesIndex(species_names, m.GetAttribute<std::string>("species"));
         d.n_level = m.GetAttribute<uint32_t>("n_level");
@@ -750,6 +763,50 @@ void Context::BuildMoves(const Input& in) {
             if (a.kind == 0) d.kinetic[d.n_kinetic++] = a.index;
             else if (a.kind == 1) d.trap[d.n_trap++] = a.index;
             else d.pair[d.n_pair++] = a.index;
+        }
+        if (h.kind == 2 || h.kind == 3) {
+            // perm_bisect_class.h:101-116
+            const uint32_t N = sys.sp_n[d.species];
+            h.perm_epsilon = m.GetAttribute<double>("epsilon", 1.e-100);
+            h.perm_attempt.assign(N, 0);
+            h.perm_accept.assign(N, 0);
+            h.perm_n_type_out = N;  // perm_bisect_iterative_class.h:229
+            for (int i = 0; i < d.n_pair; ++i)
+                if (sys.pair[d.pair[i]].kind != kPairBare)
+                    throw PimcError(kErrUnsupported, "permuting moves take the bare pair action only");
+            if (h.kind == 3) {
+                // BuildCycles (perm_bisect_table_class.h:54-102): every permutation of n_perm_part
+                // particles (lexicographic) over every subset of that size (lexicographic).
+                const uint32_t k = m.GetAttribute<uint32_t>("n_perm_part");
+                if (k < 1 || k > N) throw PimcError(kErrInput, "n_perm_part must be between 1 and the particle count");
+                std::vector<uint32_t> a(k), types, combs;
+                for (uint32_t i = 0; i < k; ++i) a[i] = i;
+                uint32_t n_types = 0, n_comb = 0;
+                do {
+                    types.insert(types.end(), a.begin(), a.end());
+                    ++n_types;
+                } while (std::next_permutation(a.begin(), a.end()));
+                std::vector<uint32_t> c(k);
+                for (uint32_t i = 0; i < k; ++i) c[i] = i;
+                for (;;) {
+                    combs.insert(combs.end(), c.begin(), c.end());
+                    ++n_comb;
+                    if ((size_t)n_comb * n_types > (1u << 24)) throw PimcError(kErrUnsupported, "permutation table above 2^24 cycles");
+                    int i = (int)k - 1;
+                    while (i >= 0 && c[i] == N - k + (uint32_t)i) --i;
+                    if (i < 0) break;
+                    c[i]++;
+                    for (uint32_t j = (uint32_t)i + 1; j < k; ++j) c[j] = c[j - 1] + 1;
+                }
+                h.perm_k = k;
+                h.perm_n_types = n_types;
+                h.perm_n_comb = n_comb;
+                h.perm_n_type_out = n_types;
+                h.perm_types = std::make_shared<DeviceBuffer>(types.size() * sizeof(uint32_t));
+                h.perm_combs = std::make_shared<DeviceBuffer>(combs.size() * sizeof(uint32_t));
+                CudaCheck(cudaMemcpy(h.perm_types->ptr, types.data(), types.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "cycle table upload");
+                CudaCheck(cudaMemcpy(h.perm_combs->ptr, combs.data(), combs.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "cycle table upload");
+            }
         }
         moves.push_back(h);
     }
@@ -795,8 +852,45 @@ void Context::BuildObservables(const Input& in) {
             h.kind = 4;
             h.skip = std::max(1u, o.GetAttribute<uint32_t>("skip", 1));  // observable_class.h:77
             h.dumps.resize(sys.S);
+            h.dump_perms.resize(sys.S);
         } else if (h.type == "Time") {
             h.kind = 3;
+        } else if (h.type == "Sign") {
+            h.kind = 5;
+        } else if (h.type == "Permutation") {
+            // permutation_class.h:33-73; sectors are the partitions of N in the order of the
+            // ascending-composition generation of species_class.h:178-221
+            h.kind = 6;
+            h.species = SpeciesIndex(species_names, o.GetAttribute<std::string>("species"));
+            h.sector_max = o.GetAttribute<uint32_t>("sector_max", 0);
+            const uint32_t n = sys.sp_n[h.species];
+            h.cycles.assign(n, 0.);
+            // Accelerated ascending-composition generation of the partitions of n (Kelleher and
+            // O'Sullivan), stopped after sector_max partitions when sector_max > 0.
+            std::vector<uint32_t> a(n + 1, 0);
+            uint32_t k = 1, y = n - 1;
+            auto room = [&]() { return h.sector_max == 0 || h.partitions.size() < h.sector_max; };
+            while (k != 0 && room()) {
+                uint32_t x = a[k - 1] + 1;
+                k -= 1;
+                while (2 * x <= y) {
+                    a[k] = x;
+                    y -= x;
+                    k += 1;
+                }
+                const uint32_t l = k + 1;
+                while (x <= y && room()) {
+                    a[k] = x;
+                    a[l] = y;
+                    h.partitions.emplace_back(a.begin(), a.begin() + k + 2);
+                    x += 1;
+                    y -= 1;
+                }
+                a[k] = x + y;
+                y = x + y - 1;
+                h.partitions.emplace_back(a.begin(), a.begin() + k + 1);
+                if (h.partitions.size() > (1u << 20)) throw PimcError(kErrUnsupported, "more than 2^20 permutation sectors: set sector_max");
+            }
         } else {
             throw PimcError(kErrUnsupported, "unsupported observable type '" + h.type + "'");
         }

@@ -285,6 +285,8 @@ static bool Selected(const ActionHost& ah, int sel, int i) {
 
 /// The whole-ring action and its exact gradient cover Kinetic, HarmonicTrap and BarePairAction.
 static void RequireAdjointActions(const Context& c, int sel) {
+    if (c.AnyPerm())
+        throw PimcError(kErrUnsupported, "the whole-ring action and its gradient assume paths without exchanges");
     for (size_t i = 0; i < c.actions.size(); ++i)
         if (Selected(c.actions[i], sel, (int)i) && c.actions[i].kind == 2 && c.sys.pair[c.actions[i].index].kind != kPairBare)
             throw PimcError(kErrUnsupported, "the whole-ring action and its gradient cover Kinetic, HarmonicTrap and BarePairAction");

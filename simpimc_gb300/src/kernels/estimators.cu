@@ -87,8 +87,9 @@ __global__ void ProposalRhoKernel(const SystemDev sys, uint32_t species, const u
 }
 
 // g(r) histogram (pair_correlation_class.h:15-28): shared-memory counts, then global atomics.
+// The sign cofactor (pair_correlation_class.h:17) enters as a signed increment of the counts.
 __global__ void PairCorrelationKernel(const SystemDev sys, uint32_t sa, uint32_t sb, double r_min, double d_ir, uint32_t n_r,
-                                      unsigned long long* __restrict__ hist) {
+                                      long long sign, unsigned long long* __restrict__ hist) {
     extern __shared__ unsigned int counts[];
     for (uint32_t i = threadIdx.x; i < n_r; i += blockDim.x) counts[i] = 0u;
     __syncthreads();
@@ -109,13 +110,13 @@ __global__ void PairCorrelationKernel(const SystemDev sys, uint32_t sa, uint32_t
     }
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < n_r; i += blockDim.x)
-        if (counts[i]) atomicAdd(&hist[i], (unsigned long long)counts[i]);
+        if (counts[i]) atomicAdd(&hist[i], (unsigned long long)(sign * (long long)counts[i]));
 }
 
 // S(k) accumulation (structure_factor_class.h:15-32) in the reference's order: one thread per k
 // adds the slice terms one by one into the running sum.
 __global__ void StructureFactorKernel(const SystemDev sys, const double* __restrict__ kmag, double k_cut, uint32_t slot_a,
-                                      uint32_t slot_b, double* __restrict__ sk) {
+                                      uint32_t slot_b, double cofactor, double* __restrict__ sk) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= sys.K || !(kmag[k] < k_cut)) return;
     const double2* ra = sys.rho_k + (size_t)slot_a * sys.M * sys.K;
@@ -123,7 +124,7 @@ __global__ void StructureFactorKernel(const SystemDev sys, const double* __restr
     double acc = sk[k];
     for (uint32_t b = 0; b < sys.M; ++b) {
         const double2 a = ra[(size_t)b * sys.K + k], c = rb[(size_t)b * sys.K + k];
-        acc += 1. * (a.x * c.x + a.y * c.y);
+        acc += cofactor * (a.x * c.x + a.y * c.y);
     }
     sk[k] = acc;
 }
@@ -260,18 +261,32 @@ double Context::GetAction(uint32_t ai, uint32_t b0, uint32_t b1, const uint32_t*
         if (k.image[level].n == 0) throw PimcError(kErrArg, "no kinetic spline for this level");
         std::vector<uint32_t> list;
         SpeciesParticles(*this, k.species, sp, p, n, list);
-        const uint32_t nl = CountLinks(b0, b1, skip, M);
+        const bool exch = !PermIdentity(k.species);
+        uint32_t nl;
+        if (!exch) {
+            nl = CountLinks(b0, b1, skip, M);
+        } else {
+            // links follow the path permutation at the ring closure (kinetic_class.h:112-119)
+            if ((b1 - b0) % skip) throw PimcError(kErrArg, "segment is not a whole number of links at this level");
+            nl = (b1 - b0) / skip;
+        }
         if (list.empty() || nl == 0) return 0.;
         uint32_t* dl = Parts(list.size());
         for (auto& x : list) x += sys.sp_off[k.species];
         CudaCheck(cudaMemcpyAsync(dl, list.data(), list.size() * 4, cudaMemcpyHostToDevice, stream), "parts upload");
         const uint32_t a0 = b0 % M;
         const double i4 = k.i4lt_level[level];
+        const uint32_t* perm = sys.perm;
+        const bool whole = b1 - b0 == M;
         SumItems<1>(*this, (uint64_t)list.size() * nl, [=] __device__(uint64_t i, double* v) {
             const uint32_t g = dl[i / nl], j = (uint32_t)(i % nl);
-            const uint32_t a = (a0 + j * skip) % M, nx = (a + skip) % M;
+            v[0] = 0.;
+            if (exch && whole && perm[g] == g) return;  // the walk's end is its start bead: no links
+            const uint32_t q0 = a0 + j * skip, q1 = q0 + skip;
+            const uint32_t ga = (exch && q0 >= M) ? perm[g] : g, gn = (exch && q1 >= M) ? perm[g] : g;
+            const uint32_t a = q0 % M, nx = q1 % M;
             double dr[3];
-            for (uint32_t d = 0; d < n_d; ++d) dr[d] = MinImage(PosAt(pos, np, a, d, g) - PosAt(pos, np, nx, d, g), L, iL);
+            for (uint32_t d = 0; d < n_d; ++d) dr[d] = MinImage(PosAt(pos, np, a, d, ga) - PosAt(pos, np, nx, d, gn), L, iL);
             v[0] = -LogRhoFree(dr, n_d, i4, &k.image[level], k.has_images);
         }, &out);
         return out;
@@ -397,24 +412,44 @@ void Context::GetActionGradient(uint32_t ai, uint32_t b0, uint32_t b1, const uin
         const KineticDev k = sys.kinetic[ah.index];
         std::vector<uint32_t> list;
         SpeciesParticles(*this, k.species, sp, p, n, list);
-        const uint32_t nl = CountLinks(b0, b1, skip, M);
+        const bool exch = !PermIdentity(k.species);
+        uint32_t nl;
+        if (!exch) {
+            nl = CountLinks(b0, b1, skip, M);
+        } else {
+            if ((b1 - b0) % skip) throw PimcError(kErrArg, "segment is not a whole number of links at this level");
+            nl = (b1 - b0) / skip;
+        }
         if (list.empty() || nl == 0) return;
         for (auto& x : list) x += sys.sp_off[k.species];
         uint32_t* dl = Parts(list.size());
         CudaCheck(cudaMemcpyAsync(dl, list.data(), list.size() * 4, cudaMemcpyHostToDevice, stream), "parts upload");
         const uint32_t a0 = b0 % M;
+        const uint32_t* perm = sys.perm;
+        const uint32_t* perm_inv = sys.perm_inv;
+        const bool whole = b1 - b0 == M;
         double t[3];
         SumItems<3>(*this, (uint64_t)list.size() * nl, [=] __device__(uint64_t i, double* v) {
             const uint32_t gg = dl[i / nl], j = (uint32_t)(i % nl);
-            const uint32_t a = (a0 + j * skip) % M, nx = (a + skip) % M, pv = (a + M - (skip % M)) % M;
+            v[0] = v[1] = v[2] = 0.;
+            if (exch && whole && perm[gg] == gg) return;
+            // GetPrevBead(skip) / GetNextBead(skip) across the ring closure (kinetic_class.h:133-136)
+            const int q = (int)(a0 + j * skip), qp = q - (int)skip, qn = q + (int)skip;
+            auto lab = [&](int x) -> uint32_t {
+                if (!exch) return gg;
+                return x < 0 ? perm_inv[gg] : (x >= (int)M ? perm[gg] : gg);
+            };
+            auto slc = [&](int x) -> uint32_t { return (uint32_t)(((x % (int)M) + (int)M) % (int)M); };
+            const uint32_t a = slc(q), nx = slc(qn), pv = slc(qp);
+            const uint32_t ga = lab(q), gn = lab(qn), gp = lab(qp);
             for (uint32_t d = 0; d < 3; ++d) {
                 if (d >= n_d) {
                     v[d] = 0.;
                     continue;
                 }
-                const double ra = PosAt(pos, np, a, d, gg);
-                const double dprev = MinImage(PosAt(pos, np, pv, d, gg) - ra, L, iL);
-                const double dnext = MinImage(ra - PosAt(pos, np, nx, d, gg), L, iL);
+                const double ra = PosAt(pos, np, a, d, ga);
+                const double dprev = MinImage(PosAt(pos, np, pv, d, gp) - ra, L, iL);
+                const double dnext = MinImage(ra - PosAt(pos, np, nx, d, gn), L, iL);
                 v[d] = -dprev + dnext;
             }
         }, t);
@@ -538,11 +573,13 @@ double Context::DActionDBeta(uint32_t ai) {
         // kinetic_class.h:35-45
         const KineticDev k = sys.kinetic[ah.index];
         const uint32_t N = sys.sp_n[k.species], off = sys.sp_off[k.species];
+        const uint32_t* perm = sys.perm;
         SumItems<1>(*this, (uint64_t)N * M, [=] __device__(uint64_t i, double* v) {
             const uint32_t g = off + (uint32_t)(i / M), b = (uint32_t)(i % M), bn = (b + 1) % M;
+            const uint32_t gn = b + 1 == M ? perm[g] : g;  // GetNextBead(1) across the closure
             double tot = 0., r2 = 0.;
             for (uint32_t d = 0; d < n_d; ++d) {
-                const double x = MinImage(PosAt(pos, np, b, d, g) - PosAt(pos, np, bn, d, g), L, iL);
+                const double x = MinImage(PosAt(pos, np, b, d, g) - PosAt(pos, np, bn, d, gn), L, iL);
                 if (k.has_images) tot -= EvalCubic(k.d_image_d_tau, x);
                 r2 += x * x;
             }
@@ -671,14 +708,18 @@ double Context::VirialEnergy(uint32_t ai, double window) {
     const uint32_t M = sys.M, n_d = sys.n_d, np = sys.n_pad;
     const double L = sys.L, iL = sys.iL;
     const uint32_t W = window < 1. ? 1u : (uint32_t)std::ceil(window);
+    if (W > M && !PermIdentity(k.species)) throw PimcError(kErrArg, "virial window longer than the path of an exchanging species");
+    const uint32_t* perm = sys.perm;
     double out = 0.;
     SumItems<1>(*this, (uint64_t)N * M, [=] __device__(uint64_t i, double* v) {
         const uint32_t g = off + (uint32_t)(i / M), b = (uint32_t)(i % M);
+        // beads b + w of the path through the ring closure (one crossing: b + W < 2M)
+        auto lab = [&](uint32_t x) { return x >= M ? perm[g] : g; };
         double dr1[3] = {0., 0., 0.}, drl[3] = {0., 0., 0.};
-        for (uint32_t d = 0; d < n_d; ++d) dr1[d] = MinImage(PosAt(pos, np, (b + 1) % M, d, g) - PosAt(pos, np, b, d, g), L, iL);
+        for (uint32_t d = 0; d < n_d; ++d) dr1[d] = MinImage(PosAt(pos, np, (b + 1) % M, d, lab(b + 1)) - PosAt(pos, np, b, d, g), L, iL);
         for (uint32_t w = 0; w < W; ++w) {
-            const uint32_t x = (b + w) % M, y = (b + w + 1) % M;
-            for (uint32_t d = 0; d < n_d; ++d) drl[d] += MinImage(PosAt(pos, np, y, d, g) - PosAt(pos, np, x, d, g), L, iL);
+            const uint32_t x = b + w, y = b + w + 1;
+            for (uint32_t d = 0; d < n_d; ++d) drl[d] += MinImage(PosAt(pos, np, y % M, d, lab(y)) - PosAt(pos, np, x % M, d, lab(x)), L, iL);
         }
         double dot = 0.;
         for (uint32_t d = 0; d < n_d; ++d) dot += drl[d] * dr1[d];
@@ -794,10 +835,27 @@ void Context::ObservableAccumulate(uint32_t oi) {
     EnsureFP64();
     if (oi >= observables.size()) throw PimcError(kErrArg, "observable index out of range");
     ObservableHost& o = observables[oi];
-    if (o.kind >= 3) return;  // Time, PathDump: nothing to accumulate
+    if (o.kind == 3 || o.kind == 4) return;  // Time, PathDump: nothing to accumulate
+    // Path::GetSign times the importance weight (1: no importance-weight actions), energy_class.h:135-137
+    const double cof = PathSign();
+    if (o.kind == 5) {  // sign_class.h:12-16
+        o.sign_sum += cof;
+        o.n_measure++;
+        return;
+    }
+    if (o.kind == 6) {  // permutation_class.h:15-22
+        auto c = CycleLengths(o.species);
+        for (uint32_t l : c) o.cycles[l - 1] += 1.;
+        std::sort(c.begin(), c.end());
+        uint32_t sector = (uint32_t)o.partitions.size();
+        for (size_t i = 0; i < o.partitions.size(); ++i)
+            if (o.partitions[i] == c) sector = (uint32_t)i;
+        o.sectors.push_back(sector);
+        o.n_measure++;
+        return;
+    }
     if (o.kind == 0) {
-        // energy_class.h:133-161 (sign and importance weight are 1 for these species)
-        const double cof = 1.;
+        // energy_class.h:133-161
         if (o.use_thermal) {
             for (size_t i = 0; i < actions.size(); ++i)
                 if (!actions[i].is_importance_weight) o.energies[i] += cof * DActionDBeta((uint32_t)i);
@@ -822,7 +880,7 @@ void Context::ObservableAccumulate(uint32_t oi) {
     } else if (o.kind == 1) {
         const int blocks = n_sm * 2;
         PairCorrelationKernel<<<blocks, 256, o.n_r * sizeof(unsigned int), stream>>>(sys, o.sa, o.sb, o.r_min, o.d_ir, o.n_r,
-                                                                                    o.hist->as<unsigned long long>());
+                                                                                    (long long)cof, o.hist->as<unsigned long long>());
         CudaCheck(cudaGetLastError(), "g(r) launch");
     } else if (o.kind == 2) {
         if (sys.K) {
@@ -832,7 +890,7 @@ void Context::ObservableAccumulate(uint32_t oi) {
             }
             const double* dk = kmag_dev_->as<double>();
             StructureFactorKernel<<<(sys.K + 255) / 256, 256, 0, stream>>>(sys, dk, o.k_cut, (uint32_t)sys.sp_rho[o.sa], (uint32_t)sys.sp_rho[o.sb],
-                                                                           o.sk->as<double>());
+                                                                           cof, o.sk->as<double>());
             CudaCheck(cudaGetLastError(), "S(k) launch");
         }
     }
@@ -843,8 +901,34 @@ std::vector<double> Context::ObservableBlock(uint32_t oi) {
     if (oi >= observables.size()) throw PimcError(kErrArg, "observable index out of range");
     ObservableHost& o = observables[oi];
     std::vector<double> out;
-    if (o.kind >= 3 || o.n_measure == 0) return out;
+    if (o.kind == 3 || o.kind == 4 || o.n_measure == 0) return out;
     Sync();
+    if (o.kind == 5) {  // sign_class.h:34-50
+        out.push_back(o.sign_sum / (double)o.n_measure);
+        o.sign_sum = 0.;
+        o.n_measure = 0;
+        return out;
+    }
+    if (o.kind == 6) {
+        // permutation_class.h:76-118: cycle histogram normalised by the number of cycles, then the
+        // block's (sector, count) pairs in increasing sector order
+        double n_cycles = 0.;
+        for (double c : o.cycles) n_cycles += c;
+        for (double c : o.cycles) out.push_back(c / n_cycles);
+        std::vector<uint32_t> sct = o.sectors;
+        std::sort(sct.begin(), sct.end());
+        for (size_t i = 0; i < sct.size();) {
+            size_t j = i;
+            while (j < sct.size() && sct[j] == sct[i]) ++j;
+            out.push_back((double)sct[i]);
+            out.push_back((double)(j - i));
+            i = j;
+        }
+        std::fill(o.cycles.begin(), o.cycles.end(), 0.);
+        o.sectors.clear();
+        o.n_measure = 0;
+        return out;
+    }
     if (o.kind == 0) {
         // energy_class.h:232-253
         const double norm = (double)sys.M * o.n_measure;
@@ -883,7 +967,7 @@ std::vector<double> Context::ObservableBlock(uint32_t oi) {
             if (sys.n_d == 3) bin_vol = 4. * M_PI / 3. * (r2 * r2 * r2 - r1 * r1 * r1);
             else if (sys.n_d == 2) bin_vol = M_PI * (r2 * r2 - r1 * r1);
             else bin_vol = r2 - r1;
-            out[i] = (double)h[i] / (bin_vol * norm);
+            out[i] = (double)(long long)h[i] / (bin_vol * norm);
         }
     } else if (o.kind == 2) {
         std::vector<double> sk(sys.K);

@@ -1422,16 +1422,21 @@ void Context::BuildSweepTables() {
 void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep) {
     if (n_entries == 0 || n_rep == 0) return;
     if (n_entries > 1024) throw PimcError(kErrArg, "schedule longer than 1024 entries");
-    bool any_hmc = false;
+    bool own_launches = false;
+    auto on_perm_kernel = [&](uint32_t m) {
+        return moves[m].kind == 2 || moves[m].kind == 3 || (moves[m].kind == 0 && PermutingSpecies(moves[m].dev.species));
+    };
     for (uint32_t e = 0; e < n_entries; ++e) {
         if (mv[e] >= moves.size()) throw PimcError(kErrArg, "move index out of range");
-        any_hmc |= moves[mv[e]].kind == 1;
+        own_launches |= moves[mv[e]].kind == 1 || on_perm_kernel(mv[e]);
     }
-    if (any_hmc) {  // HMC moves run their own launches; bisection entries between them keep the sweep kernel
+    if (own_launches) {  // HMC and exchanging species run their own launches, entry by entry
         for (uint64_t r = 0; r < n_rep; ++r)
             for (uint32_t e = 0; e < n_entries; ++e) {
                 if (moves[mv[e]].kind == 1) {
                     HmcAttempts(mv[e], counts[e]);
+                } else if (on_perm_kernel(mv[e])) {
+                    PermAttempts(mv[e], counts[e]);
                 } else {
                     const uint64_t c1 = counts[e];
                     Sweep(&mv[e], &c1, 1, 1);
@@ -1677,6 +1682,14 @@ void Context::WriteBlock() {
                     // cube (n_d, n_bead, n_part) column-major: the same order as the host layout
                     const size_t n = (size_t)sys.sp_n[sp] * sys.M * sys.n_d, off = (size_t)sys.sp_off[sp] * sys.M * sys.n_d;
                     o.dumps[sp].emplace_back(host.begin() + off, host.begin() + off + n);
+                    // (prev, next) particle of each path at the ring closure (path_dump_class.h:42-47)
+                    std::vector<double> pm(2 * (size_t)sys.sp_n[sp]);
+                    const uint32_t G0 = sys.sp_off[sp];
+                    for (uint32_t p = 0; p < sys.sp_n[sp]; ++p) {
+                        pm[2 * p + 1] = (double)(perm_host[G0 + p] - G0);
+                        pm[2 * (perm_host[G0 + p] - G0)] = (double)p;
+                    }
+                    o.dump_perms[sp].push_back(pm);
                 }
             }
             o.n_write_calls++;
@@ -1699,6 +1712,12 @@ void Context::WriteBlock() {
         mh.first_block = false;
         mh.block_attempt = 0;
         mh.block_accept = 0;
+        if (mh.kind == 2 || mh.kind == 3) {  // perm_bisect_class.h:119-132
+            mh.out_perm_attempt.emplace_back(mh.perm_attempt.begin(), mh.perm_attempt.end());
+            mh.out_perm_accept.emplace_back(mh.perm_accept.begin(), mh.perm_accept.end());
+            std::fill(mh.perm_attempt.begin(), mh.perm_attempt.end(), 0);
+            std::fill(mh.perm_accept.begin(), mh.perm_accept.end(), 0);
+        }
     }
 }
 

@@ -1,0 +1,188 @@
+"""GPU parity of the permuting bisection (perm_bisect_class.h:7-133, perm_bisect_iterative_class.h:
+7-231, perm_bisect_table_class.h:7-240), the plain bisection of exchanging species, the kinetic
+action across a permuted ring closure, the sign cofactor and the Sign / Permutation observables
+against the FP64 oracle.
+
+The permutation kernel replays the oracle's random streams, so accept counts, per-cycle-length
+counters and the path permutation must agree exactly; positions within 1e-9 (FP64 on both sides,
+different summation order of the action changes); estimator values 1e-10 relative.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from simpimc_gb300 import PimcError, Simulation
+from simpimc_gb300.configs import electron_gas, trapped_bosons, trapped_coulomb
+from simpimc_gb300.tables import read_table
+
+pytestmark = pytest.mark.gpu
+
+
+def close(g, c, rel=1e-10):
+    g = np.asarray(g, dtype=float)
+    c = np.asarray(c, dtype=float)
+    return np.all(np.abs(g - c) <= rel * np.maximum(1.0, np.abs(c)))
+
+
+def replay(g, c, n_part, schedule, n_perm_move=1):
+    for m, chunk in schedule:
+        g.move_attempts(m, chunk)
+        c.move_attempts(m, chunk)
+        assert g.move_stats(m) == c.move_stats(m), (m, chunk)
+        np.testing.assert_array_equal(g.get_perm(0), c.get_perm(0, n_part))
+        assert np.max(np.abs(g.get_path(1) - c.get_path(1))) < 1e-9
+    ga, gc = g.perm_stats(n_perm_move, n_part)
+    ca, cc = c.perm_stats(n_perm_move, n_part)
+    np.testing.assert_array_equal(ga, ca)
+    np.testing.assert_array_equal(gc, cc)
+
+
+@pytest.mark.parametrize("perm,k,coulomb", [("PermBisectIterative", 0, False), ("PermBisectIterative", 0, True),
+                                            ("PermBisectTable", 2, False), ("PermBisectTable", 3, True)])
+def test_perm_bisection_replays_oracle(tmp_path, gpu_lib, oracle_mod, perm, k, coulomb):
+    n = 6
+    xml, path = trapped_bosons(tmp_path, n_part=n, beta=4.0, n_bead=16, n_level=2, perm=perm, n_perm_part=k, coulomb=coulomb,
+                               seed=21)
+    path = path * 0.4  # close paths: exchanges are frequent
+    g = Simulation(xml, base_dir=tmp_path)
+    c = oracle_mod.OracleSim(xml, base_dir=tmp_path)
+    g.set_path(path)
+    c.set_path(path)
+    replay(g, c, n, [(1, 1), (0, 7), (1, 40), (0, 40), (1, 300), (0, 100), (1, 300)])
+    assert sum(c.perm_stats(1, n)[1][1:]) > 0, "no exchange was accepted: the case does not test permutations"
+    for a in range(g.n_actions):
+        assert close(g.dactiondbeta(a), c.dactiondbeta(a)), a
+        assert close(g.virial_energy(a, 16.0), c.virial_energy(a, 16.0), 1e-9), a
+    g.close()
+    c.close()
+
+
+def test_perm_with_long_bisection_and_closure(tmp_path, gpu_lib, oracle_mod):
+    """Segments of half the ring cross the closure often; the relabelling moves slice data."""
+    n = 5
+    xml, path = trapped_bosons(tmp_path, n_part=n, beta=4.0, n_bead=8, n_level=2, perm_level=3, seed=5)
+    path = path * 0.3
+    g = Simulation(xml, base_dir=tmp_path)
+    c = oracle_mod.OracleSim(xml, base_dir=tmp_path)
+    g.set_path(path)
+    c.set_path(path)
+    replay(g, c, n, [(1, 50), (0, 20), (1, 400), (0, 50), (1, 400)])
+    g.close()
+    c.close()
+
+
+def test_perm_ewald_electron_gas(tmp_path, gpu_lib, oracle_mod):
+    """Exchanges of one spin species with the primitive pair action and its Ewald sum: the density
+    update of moved beads on both sides of the closure."""
+    xml, path = electron_gas(tmp_path, n_part=8, n_bead=16, n_level=2, rs=1.0, beta=4.0, k_cut_units=3.0, seed=4)
+    xml = xml.replace('<Move name="BisectD"', '<Move name="PermU" type="PermBisectIterative" species="eU" n_level="2" />\n    <Move name="BisectD"')
+    L = (4.0 * math.pi * 8 / 3.0) ** (1.0 / 3.0) * 1.0
+    rng = np.random.default_rng(2)
+    centre = rng.uniform(-L / 2, L / 2, size=(8, 1, 3))
+    path = centre + 0.2 * rng.standard_normal(path.shape)
+    path -= np.rint(path / L) * L
+    g = Simulation(xml, base_dir=tmp_path)
+    c = oracle_mod.OracleSim(xml, base_dir=tmp_path)
+    pm = 1  # BisectU, PermU, BisectD
+    g.set_path(path)
+    c.set_path(path)
+    for m, chunk in [(pm, 30), (0, 10), (pm, 200), (2, 10), (pm, 200)]:
+        g.move_attempts(m, chunk)
+        c.move_attempts(m, chunk)
+        assert g.move_stats(m) == c.move_stats(m), (m, chunk)
+        assert np.max(np.abs(g.get_path(1) - c.get_path(1))) < 1e-9
+    np.testing.assert_array_equal(g.get_perm(0), c.get_perm(0, 4))
+    for s in range(2):
+        assert np.max(np.abs(g.rho_k(s) - c.rho_k(s))) < 1e-9
+    for a in range(g.n_actions):
+        assert close(g.dactiondbeta(a), c.dactiondbeta(a), 1e-9), a
+    g.close()
+    c.close()
+
+
+def test_kinetic_terms_across_a_set_permutation(tmp_path, gpu_lib, oracle_mod):
+    n = 5
+    xml, path = trapped_bosons(tmp_path, n_part=n, beta=2.0, n_bead=16, n_level=2, seed=9)
+    g = Simulation(xml, base_dir=tmp_path)
+    c = oracle_mod.OracleSim(xml, base_dir=tmp_path)
+    g.set_path(path)
+    c.set_path(path)
+    pi = [3, 0, 4, 1, 2]
+    g.set_perm(0, pi)
+    c.set_perm(0, pi)
+    np.testing.assert_array_equal(g.get_perm(0), pi)
+    assert close(g.dactiondbeta(0), c.dactiondbeta(0))
+    for w in (1.0, 5.0, 16.0):
+        assert close(g.virial_energy(0, w), c.virial_energy(0, w)), w
+    for b0, b1, level in [(12, 20, 0), (12, 20, 1), (14, 18, 1), (0, 16, 0), (15, 16, 0), (0, 16, 2)]:
+        for p in range(n):
+            for mode in (0, 1):
+                assert close(g.get_action(0, b0, b1, [(0, p)], level, mode), c.get_action(0, b0, b1, [(0, p)], level, mode)), (b0, b1, p)
+            assert close(g.get_action_gradient(0, b0, b0 + (1 << level), [(0, p)], level, 0),
+                         c.get_action_gradient(0, b0, b0 + (1 << level), [(0, p)], level, 0)), (b0, p)
+    with pytest.raises(PimcError):
+        g.set_perm(0, [0, 0, 1, 2, 3])
+    with pytest.raises(PimcError):
+        g.total_action()  # the whole-ring paths assume no exchanges
+    g.close()
+    c.close()
+
+
+def test_sign_and_permutation_observables(tmp_path, gpu_lib, oracle_mod):
+    n = 4
+    xml, path = trapped_bosons(tmp_path, n_part=n, beta=4.0, n_bead=16, n_level=2, fermi=True, seed=13)
+    path = path * 0.4
+    g = Simulation(xml, base_dir=tmp_path)
+    c = oracle_mod.OracleSim(xml, base_dir=tmp_path)
+    g.set_path(path)
+    c.set_path(path)
+    for _ in range(30):
+        for sim in (g, c):
+            sim.move_attempts(0, n)
+            sim.move_attempts(1, n)
+            for o in range(3):
+                sim.observable_accumulate(o)
+    for o in range(3):
+        gb, cb = g.observable_block(o), c.observable_block(o)
+        assert gb.shape == cb.shape and close(gb, cb), (o, gb, cb)
+    g.close()
+    c.close()
+
+
+def test_perm_output_and_restart(tmp_path, gpu_lib):
+    n = 5
+    xml, path = trapped_bosons(tmp_path, n_part=n, beta=4.0, n_bead=16, n_level=2, seed=17, n_step_inner=50, n_step_outer=4)
+    xml = xml.replace('<Observable name="Sign" type="Sign" />',
+                      '<Observable name="Sign" type="Sign" />\n    <Observable name="path_dump" type="PathDump" />')
+    g = Simulation(xml, base_dir=tmp_path)
+    g.set_path(path * 0.4)
+    g.run()
+    g.write_output(tmp_path / "bosons.0.pat")
+    d = read_table(tmp_path / "bosons.0.pat")
+    att = d["Moves/Perm/perm_attempt"].reshape(-1, n)
+    acc = d["Moves/Perm/perm_accept"].reshape(-1, n)
+    assert att.shape[0] == 4 and np.all(acc <= att)
+    assert d["Moves/Perm/n_perm_type"][0] == n
+    perm = d["Observables/path_dump/b/permutation"].reshape(-1, n, 2)
+    pi = g.get_perm(0)
+    np.testing.assert_array_equal(perm[-1, :, 1], pi)
+    np.testing.assert_array_equal(perm[-1, pi, 0], np.arange(n))
+    cyc = d["Observables/Permutation/cycles/y"].reshape(4, n)
+    np.testing.assert_allclose(cyc.sum(axis=1), 1.0)
+    xml2 = xml.replace('init_type="File" file_name="init.xyz" all_beads="1"', 'init_type="Restart" prefix="bosons"')
+    r = Simulation(xml2, base_dir=tmp_path)
+    np.testing.assert_array_equal(r.get_perm(0), pi)
+    np.testing.assert_array_equal(r.get_path(0), g.get_path(0))
+    assert r.dactiondbeta(0) == g.dactiondbeta(0)
+    r.close()
+    g.close()
+
+
+def test_perm_refuses_off_diagonal_pair_actions(tmp_path, gpu_lib):
+    xml, path = trapped_coulomb(tmp_path, n_part=4, n_bead=8, n_level=2, seed=2, pair="IlkkaPairAction")
+    xml = xml.replace('<Move name="Bisect" type="Bisect" species="e" n_level="2" />',
+                      '<Move name="Bisect" type="Bisect" species="e" n_level="2" />\n    '
+                      '<Move name="Perm" type="PermBisectIterative" species="e" n_level="2" />')
+    with pytest.raises(PimcError):
+        Simulation(xml, base_dir=tmp_path)
