@@ -771,9 +771,6 @@ void Context::BuildMoves(const Input& in) {
             h.perm_attempt.assign(N, 0);
             h.perm_accept.assign(N, 0);
             h.perm_n_type_out = N;  // perm_bisect_iterative_class.h:229
-            for (int i = 0; i < d.n_pair; ++i)
-                if (sys.pair[d.pair[i]].kind != kPairBare)
-                    throw PimcError(kErrUnsupported, "permuting moves take the bare pair action only");
             if (h.kind == 3) {
                 // BuildCycles (perm_bisect_table_class.h:54-102): every permutation of n_perm_part
                 // particles (lexicographic) over every subset of that size (lexicographic).

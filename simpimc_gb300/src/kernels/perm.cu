@@ -11,12 +11,14 @@
 // cycle (bead B - 1 of path i to the old end bead of path sigma(i)) is held in shared memory.
 //
 // Action changes. Kinetic links follow the paths (pointer semantics of kinetic_class.h:105-122).
-// The trap, the bare pair action and its Ewald part are sums over beads of the label-indexed
-// particle list (trap_class.h:37-61, pair_action_class.h:267-302 with level_tau = tau at level 0
-// and zero above, bare_pair_action_class.h:146-150); every moved bead lies on a listed label
-// (the particle owning the end bead joins the list when the segment passes the closure), so the
-// change of each is a sum over the moved beads. IlkkaPairAction and DavidPairAction links are not
-// separable per bead and are refused for these moves.
+// The trap and the Ewald part are sums over beads of the label-indexed particle list
+// (trap_class.h:37-61, bare_pair_action_class.h:126-144); every moved bead lies on a listed label
+// (the particle owning the end bead joins the list when the segment passes the closure), so their
+// changes are sums over the moved beads. The short-range pair actions are evaluated link by link
+// over the list's labels as PairAction::GetAction does (pair_action_class.h:267-302; the bare
+// action's level_tau is tau at level 0 and zero above, bare_pair_action_class.h:146-150), so the
+// off-diagonal IlkkaPairAction and DavidPairAction links keep the reference's label pairing across
+// the permuted link.
 //
 // One CTA of kPermThreads runs the attempts of one move in order: the N x N table of free-particle
 // weights and the cycle weights in parallel, the cycle selection (iterative walk, or running sum
@@ -145,18 +147,21 @@ __global__ void __launch_bounds__(kPermThreads, 1) PermBisectKernel(const __grid
     const uint32_t B = 1u << mv.n_level, K = s.K;
     const int slot = s.sp_rho[sp];
     const int stride = max(max(s.max_index[0], s.max_index[1]), s.max_index[2]) + 1;
-    // dynamic shared memory: lo_idx[N], hi_idx[N], part[N], sigma[N], lab_lo[N], lab_hi[N],
-    // end_old[N], end_new[N], then the phase rows 2 x 3 x stride double2.
+    // dynamic shared memory: lo_idx[N] (cycle member of a start particle), lpos[N] (place in the
+    // particle list), part[N], sigma[N], lab_lo[N], lab_hi[N], end_old[N], end_new[N], lst[2N]
+    // (the particle list), then the phase rows 2 x 3 x stride double2.
     int* lo_idx = reinterpret_cast<int*>(dyn);
-    int* hi_idx = lo_idx + N;
-    uint32_t* part = reinterpret_cast<uint32_t*>(hi_idx + N);
+    int* lpos = lo_idx + N;
+    uint32_t* part = reinterpret_cast<uint32_t*>(lpos + N);
     uint32_t* sigma = part + N;
     uint32_t* lab_lo = sigma + N;
     uint32_t* lab_hi = lab_lo + N;
     uint32_t* end_old = lab_hi + N;
     uint32_t* end_new = end_old + N;
-    double2* ph = reinterpret_cast<double2*>(reinterpret_cast<uintptr_t>(end_new + N + 3) & ~(uintptr_t)15);
-    for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) lo_idx[i] = hi_idx[i] = -1;
+    uint32_t* lst = end_new + N;
+    double2* ph = reinterpret_cast<double2*>(reinterpret_cast<uintptr_t>(lst + 2 * N + 3) & ~(uintptr_t)15);
+    __shared__ uint32_t s_nlist;
+    for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) lo_idx[i] = lpos[i] = -1;
     const uint32_t base_m = a.variant == kVariantBisect ? 1u : 1u + N;
     const uint32_t base_u = a.variant == kVariantBisect ? 1u + (B - 1u) : base_m + N * (B - 1u);
     __syncthreads();
@@ -284,11 +289,27 @@ __global__ void __launch_bounds__(kPermThreads, 1) PermBisectKernel(const __grid
             lab_hi[m] = a.perm[g];
             end_old[m] = B < tcross ? g : a.perm[g];
             lo_idx[part[m]] = (int)m;
-            hi_idx[a.perm[g] - G0] = (int)m;
         }
         __syncthreads();
         for (uint32_t m = threadIdx.x; m < n; m += blockDim.x) end_new[m] = end_old[sigma[m]];
+        if (threadIdx.x == 0) {
+            // the actions' particle list: the cycle, and the particles owning the end beads when the
+            // segment reaches past the closure (perm_bisect_iterative_class.h:141-146, bisect_class.h:61-64)
+            uint32_t nl = 0;
+            for (uint32_t m = 0; m < n; ++m) {
+                lpos[lab_lo[m] - G0] = (int)nl;
+                lst[nl++] = lab_lo[m];
+            }
+            if (B >= tcross)
+                for (uint32_t m = 0; m < n; ++m)
+                    if (lpos[end_old[m] - G0] < 0) {
+                        lpos[end_old[m] - G0] = (int)nl;
+                        lst[nl++] = end_old[m];
+                    }
+            s_nlist = nl;
+        }
         __syncthreads();
+        const uint32_t nlist = s_nlist;
         auto label = [&](uint32_t m, uint32_t t) -> uint32_t { return t < tcross ? lab_lo[m] : lab_hi[m]; };
         auto slice = [&](uint32_t t) -> uint32_t { return (bead0 + t) % M; };
 
@@ -323,23 +344,30 @@ __global__ void __launch_bounds__(kPermThreads, 1) PermBisectKernel(const __grid
                 new_lsp += LogRhoFree(dl, nd, mv.i4lt_sample[level], &mv.sample_image[level], mv.has_images);
             }
             __syncthreads();
-            // kinetic links along the paths (kinetic_class.h:105-122)
+            // kinetic links along the paths (kinetic_class.h:105-122). A segment of the whole ring
+            // (B = M) whose end bead is its start bead has no link in that mode: the walk to
+            // GetNextBead(M) stops at once.
             for (int ki = 0; ki < mv.n_kinetic; ++ki) {
                 const KineticDev& k = s.kinetic[mv.kinetic[ki]];
                 const uint32_t nl = B / skip;
                 for (uint32_t it = threadIdx.x; it < n * nl; it += blockDim.x) {
                     const uint32_t m = it / nl, j = it % nl, t0 = j * skip, t1 = t0 + skip;
-                    double r0[3], r1[3], dr[3];
-                    LoadR(s.pos, np, nd, slice(t0), label(m, t0), r0);
-                    if (t1 == B) LoadR(s.pos, np, nd, es, end_old[m], r1);
-                    else LoadR(s.pos, np, nd, slice(t1), label(m, t1), r1);
-                    for (uint32_t d = 0; d < nd; ++d) dr[d] = MinImage(r0[d] - r1[d], s.L, s.iL);
-                    const double so = -LogRhoFree(dr, nd, k.i4lt_level[level], &k.image[level], k.has_images);
-                    LoadR(s.pos_new, np, nd, slice(t0), label(m, t0), r0);
-                    if (t1 == B) LoadR(s.pos, np, nd, es, end_new[m], r1);
-                    else LoadR(s.pos_new, np, nd, slice(t1), label(m, t1), r1);
-                    for (uint32_t d = 0; d < nd; ++d) dr[d] = MinImage(r0[d] - r1[d], s.L, s.iL);
-                    const double sn = -LogRhoFree(dr, nd, k.i4lt_level[level], &k.image[level], k.has_images);
+                    const bool old_empty = B == M && end_old[m] == lab_lo[m], new_empty = B == M && end_new[m] == lab_lo[m];
+                    double r0[3], r1[3], dr[3], so = 0., sn = 0.;
+                    if (!old_empty) {
+                        LoadR(s.pos, np, nd, slice(t0), label(m, t0), r0);
+                        if (t1 == B) LoadR(s.pos, np, nd, es, end_old[m], r1);
+                        else LoadR(s.pos, np, nd, slice(t1), label(m, t1), r1);
+                        for (uint32_t d = 0; d < nd; ++d) dr[d] = MinImage(r0[d] - r1[d], s.L, s.iL);
+                        so = -LogRhoFree(dr, nd, k.i4lt_level[level], &k.image[level], k.has_images);
+                    }
+                    if (!new_empty) {
+                        LoadR(s.pos_new, np, nd, slice(t0), label(m, t0), r0);
+                        if (t1 == B) LoadR(s.pos, np, nd, es, end_new[m], r1);
+                        else LoadR(s.pos_new, np, nd, slice(t1), label(m, t1), r1);
+                        for (uint32_t d = 0; d < nd; ++d) dr[d] = MinImage(r0[d] - r1[d], s.L, s.iL);
+                        sn = -LogRhoFree(dr, nd, k.i4lt_level[level], &k.image[level], k.has_images);
+                    }
                     dS += sn - so;
                 }
             }
@@ -359,29 +387,39 @@ __global__ void __launch_bounds__(kPermThreads, 1) PermBisectKernel(const __grid
                     dS += tr.cofactor_a * skip * (sn - so);
                 }
             }
-            // bare pair action: each moved bead against its partners at the same slice
+            // bare pair action over the particle list, link by link with the labels' beads
+            // (PairAction::GetAction, pair_action_class.h:267-302; GenerateParticlePairs :62-114;
+            // Path::DrDrpDrrp, path_class.h:137-150): zero above level 0 (level_tau), and under
+            // periodic boundaries r' is the image nearest r, so the link is not a sum over its ends.
             for (int pi = 0; pi < mv.n_pair; ++pi) {
                 const PairDev& pa = s.pair[mv.pair[pi]];
                 if ((uint32_t)level > pa.max_level || pa.is_constant) continue;
+                if (pa.kind == kPairBare && level != 0) continue;
                 const bool hom = pa.sa == pa.sb;
                 const uint32_t other = hom ? sp : (pa.sa == sp ? pa.sb : pa.sa);
-                const uint32_t nq = s.sp_n[other], goff = s.sp_off[other];
-                if (level == 0) {
-                    for (uint32_t it = threadIdx.x; it < n * ngrid * nq; it += blockDim.x) {
-                        const uint32_t q = it % nq, rest = it / nq, m = rest / ngrid, t = (rest % ngrid + 1u) * skip;
-                        const uint32_t gm = label(m, t), gq = goff + q, b = slice(t);
-                        if (hom && gq == gm) continue;
-                        int mq = -1;
-                        if (hom) mq = t < tcross ? lo_idx[q] : hi_idx[q];
-                        if (mq >= 0 && (uint32_t)mq < m) continue;  // pair of two moved beads: counted once
-                        double ro[3], rn[3], qo[3], qn[3];
-                        LoadR(s.pos, np, nd, b, gm, ro);
-                        LoadR(s.pos_new, np, nd, b, gm, rn);
-                        LoadR(s.pos, np, nd, b, gq, qo);
-                        LoadR(mq >= 0 ? s.pos_new : s.pos, np, nd, b, gq, qn);
-                        const double d_o = DistMinImage(ro, qo, nd, s.L, s.iL), d_n = DistMinImage(rn, qn, nd, s.L, s.iL);
-                        dS += PairU(pa, d_n, d_n, 0., 0u, s.tau) - PairU(pa, d_o, d_o, 0., 0u, s.tau);
+                const uint32_t nq = s.sp_n[other], goff = s.sp_off[other], nlk = B / skip;
+                for (uint32_t it = threadIdx.x; it < nlk * nlist * nq; it += blockDim.x) {
+                    const uint32_t q = it % nq, rest = it / nq, li = rest % nlist, t = (rest / nlist) * skip;
+                    const uint32_t gx = lst[li], gy = goff + q;
+                    if (hom) {
+                        if (gy == gx) continue;
+                        const int ly = lpos[q];
+                        if (ly >= 0 && (uint32_t)ly < li) continue;  // a pair within the list: once
                     }
+                    const uint32_t b = slice(t), bn = slice(t + skip);
+                    double A0[3], C0[3], A1[3], C1[3], r, rp, ss;
+                    LoadR(s.pos, np, nd, b, gy, A0);
+                    LoadR(s.pos, np, nd, b, gx, C0);
+                    LoadR(s.pos, np, nd, bn, gy, A1);
+                    LoadR(s.pos, np, nd, bn, gx, C1);
+                    DrDrpDrrp(A0, C0, A1, C1, nd, s.L, s.iL, r, rp, ss);
+                    const double uo = PairU(pa, r, rp, ss, (uint32_t)level, s.tau);
+                    LoadR(s.pos_new, np, nd, b, gy, A0);
+                    LoadR(s.pos_new, np, nd, b, gx, C0);
+                    LoadR(s.pos_new, np, nd, bn, gy, A1);
+                    LoadR(s.pos_new, np, nd, bn, gx, C1);
+                    DrDrpDrrp(A0, C0, A1, C1, nd, s.L, s.iL, r, rp, ss);
+                    dS += PairU(pa, r, rp, ss, (uint32_t)level, s.tau) - uo;
                 }
             }
             // density change of the moved beads at this level's slices (species_class.h:406-425)
@@ -408,7 +446,9 @@ __global__ void __launch_bounds__(kPermThreads, 1) PermBisectKernel(const __grid
                     }
                 }
                 __syncthreads();
-                // Ewald part of every bare pair action touching the species (bare_pair_action_class.h:126-144)
+                // Ewald part of every pair action touching the species: tau 2^level v_long_k for the
+                // bare action (bare_pair_action_class.h:126-144), u_long_k for IlkkaPairAction and
+                // DavidPairAction (ilkka_pair_action_class.h:104-122, david_pair_action_class.h:105-123)
                 for (int pi = 0; pi < mv.n_pair; ++pi) {
                     const PairDev& pa = s.pair[mv.pair[pi]];
                     if ((uint32_t)level > pa.max_level || pa.is_constant || !pa.use_long_range) continue;
@@ -427,9 +467,9 @@ __global__ void __launch_bounds__(kPermThreads, 1) PermBisectKernel(const __grid
                             const double2 rb = s.rho_k[((size_t)oslot * M + slice(t)) * K + k];
                             dm = (rn.x * rb.x + rn.y * rb.y) - (ro.x * rb.x + ro.y * rb.y);
                         }
-                        part_lr += pa.v_long_k[k] * dm;
+                        part_lr += (pa.kind != kPairBare ? pa.u_long_k[k] : pa.v_long_k[k]) * dm;
                     }
-                    dS += (hom ? 1. : 2.) * skip * s.tau * part_lr;
+                    dS += (hom ? 1. : 2.) * (pa.kind != kPairBare ? 1. : skip * s.tau) * part_lr;
                 }
             }
             // decision (bisect_class.h:103-118)
@@ -520,10 +560,8 @@ __global__ void __launch_bounds__(kPermThreads, 1) PermBisectKernel(const __grid
             }
         }
         __syncthreads();
-        for (uint32_t m = threadIdx.x; m < n; m += blockDim.x) {
-            lo_idx[lab_lo[m] - G0] = -1;
-            hi_idx[lab_hi[m] - G0] = -1;
-        }
+        for (uint32_t m = threadIdx.x; m < n; m += blockDim.x) lo_idx[lab_lo[m] - G0] = -1;
+        for (uint32_t i = threadIdx.x; i < nlist; i += blockDim.x) lpos[lst[i] - G0] = -1;
         __syncthreads();
     }
 }
@@ -608,9 +646,6 @@ void Context::PermAttempts(uint32_t m, uint64_t n_att) {
     MoveHost& mh = moves[m];
     const uint32_t sp = mh.dev.species, N = sys.sp_n[sp], M = sys.M;
     if (N > kPermMaxPart) throw PimcError(kErrUnsupported, "permuting moves support at most 4096 particles per species");
-    for (int i = 0; i < mh.dev.n_pair; ++i)
-        if (sys.pair[mh.dev.pair[i]].kind != kPairBare)
-            throw PimcError(kErrUnsupported, "permuting paths take the bare pair action only (off-diagonal pair links are not per-bead sums)");
     if (n_att == 0) return;
     EnsureFP64();
     const uint32_t B = 1u << mh.dev.n_level;
@@ -650,7 +685,7 @@ void Context::PermAttempts(uint32_t m, uint64_t n_att) {
     a.counters = perm_cnt_->as<unsigned long long>();
     a.err = ErrWord();
     const int stride = std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
-    const size_t smem = (size_t)N * 8 * sizeof(uint32_t) + 32 + (size_t)2 * 3 * stride * sizeof(double2);
+    const size_t smem = (size_t)N * 10 * sizeof(uint32_t) + 32 + (size_t)2 * 3 * stride * sizeof(double2);
     CudaCheck(cudaFuncSetAttribute(PermBisectKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "perm smem attribute");
     CudaCheck(cudaMemsetAsync(perm_cnt_->ptr, 0, (2 + 2 * (size_t)N) * sizeof(unsigned long long), stream), "perm counters");
     (void)B;

@@ -58,10 +58,12 @@ def test_perm_bisection_replays_oracle(tmp_path, gpu_lib, oracle_mod, perm, k, c
     c.close()
 
 
-def test_perm_with_long_bisection_and_closure(tmp_path, gpu_lib, oracle_mod):
-    """Segments of half the ring cross the closure often; the relabelling moves slice data."""
+@pytest.mark.parametrize("n_bead", [16, 8])
+def test_perm_with_long_bisection_and_closure(tmp_path, gpu_lib, oracle_mod, n_bead):
+    """Segments of half the ring, or of the whole ring (the kinetic walk of a segment that ends on
+    its start bead has no link), cross the closure often; the relabelling moves slice data."""
     n = 5
-    xml, path = trapped_bosons(tmp_path, n_part=n, beta=4.0, n_bead=8, n_level=2, perm_level=3, seed=5)
+    xml, path = trapped_bosons(tmp_path, n_part=n, beta=4.0, n_bead=n_bead, n_level=2, perm_level=3, seed=5)
     path = path * 0.3
     g = Simulation(xml, base_dir=tmp_path)
     c = oracle_mod.OracleSim(xml, base_dir=tmp_path)
@@ -75,7 +77,7 @@ def test_perm_with_long_bisection_and_closure(tmp_path, gpu_lib, oracle_mod):
 def test_perm_ewald_electron_gas(tmp_path, gpu_lib, oracle_mod):
     """Exchanges of one spin species with the primitive pair action and its Ewald sum: the density
     update of moved beads on both sides of the closure."""
-    xml, path = electron_gas(tmp_path, n_part=8, n_bead=16, n_level=2, rs=1.0, beta=4.0, k_cut_units=3.0, seed=4)
+    xml, path = electron_gas(tmp_path, n_part=8, n_bead=16, n_level=2, rs=1.0, beta=4.0, k_cut_units=3.3, seed=4)
     xml = xml.replace('<Move name="BisectD"', '<Move name="PermU" type="PermBisectIterative" species="eU" n_level="2" />\n    <Move name="BisectD"')
     L = (4.0 * math.pi * 8 / 3.0) ** (1.0 / 3.0) * 1.0
     rng = np.random.default_rng(2)
@@ -179,10 +181,21 @@ def test_perm_output_and_restart(tmp_path, gpu_lib):
     g.close()
 
 
-def test_perm_refuses_off_diagonal_pair_actions(tmp_path, gpu_lib):
-    xml, path = trapped_coulomb(tmp_path, n_part=4, n_bead=8, n_level=2, seed=2, pair="IlkkaPairAction")
+@pytest.mark.parametrize("pair", ["IlkkaPairAction", "DavidPairAction"])
+def test_perm_off_diagonal_pair_actions(tmp_path, gpu_lib, oracle_mod, pair):
+    """Off-diagonal pair links keep the reference's label pairing across the permuted link."""
+    n = 5
+    xml, path = trapped_coulomb(tmp_path, n_part=n, n_bead=16, n_level=2, seed=2, pair=pair, beta=4.0)
     xml = xml.replace('<Move name="Bisect" type="Bisect" species="e" n_level="2" />',
                       '<Move name="Bisect" type="Bisect" species="e" n_level="2" />\n    '
                       '<Move name="Perm" type="PermBisectIterative" species="e" n_level="2" />')
-    with pytest.raises(PimcError):
-        Simulation(xml, base_dir=tmp_path)
+    g = Simulation(xml, base_dir=tmp_path)
+    c = oracle_mod.OracleSim(xml, base_dir=tmp_path)
+    path = path * 0.5
+    g.set_path(path)
+    c.set_path(path)
+    replay(g, c, n, [(1, 30), (0, 20), (1, 300), (0, 50), (1, 300)])
+    for a in range(g.n_actions):
+        assert close(g.dactiondbeta(a), c.dactiondbeta(a), 1e-9), a
+    g.close()
+    c.close()
