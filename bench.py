@@ -17,6 +17,8 @@ Also reported on the same line:
                      against the single-chain FP64 path on the same chains and seeds;
   plain_electron_gas the single-chain FP64 kernel on the 66-electron gas (r_s = 2, beta = 8,
                      M = 128, Ewald |k| < 12 (2 pi / L), 3561 half-space k-vectors, level 4);
+  exchange_bosons    32 trapped bosons with PermBisectIterative on the permutation kernel, with
+                     the oracle on one core beside it
   mixed_precision_large  the N = 1024, M = 512, |k| < 23 (2 pi / L) electron gas in the FP32 mode
                      and the double-float mode: speed, HBM fraction, energy and S(k) differences;
   hmc_adjoint        the r_s = 4, N = 128, M = 256 electron gas moved by the HMC path move on the
@@ -347,6 +349,63 @@ def hmc_adjoint(local, tmp, attempts=4, equil_sweeps=10):
     return out
 
 
+def exchange_bosons(local, tmp, sweeps=20, cpu_seconds=6.0):
+    """Exchanging bosons on the permutation kernel: N = 32 in the harmonic trap (omega = 1, beta = 4,
+    M = 32), plain bisection and PermBisectIterative at level 3, one sweep = N attempts of each.
+    Bead-moves count 2^l - 1 per plain attempt and (cycle length) x (2^l - 1) per permuting attempt
+    whose cycle was selected. The oracle runs the same chain on one host core beside it."""
+    import torch
+    import oracle
+    from simpimc_gb300 import Simulation
+    from simpimc_gb300.configs import trapped_bosons
+    n, m_beads, lvl = 32, 32, 3
+    B1 = (1 << lvl) - 1
+    xml, path = trapped_bosons(tmp, n_part=n, beta=4.0, n_bead=m_beads, n_level=lvl, seed=77)
+    path = path * 0.4
+    s = Simulation(xml, base_dir=tmp, device=local, chain=0)
+    s.set_path(path)
+    s.sweep([0, 1], [n, n], 5)  # warm-up
+    st = torch.cuda.ExternalStream(s._lib.pimc_stream(s._h), device=torch.device("cuda", local))
+
+    def moved(sim, pstats):
+        att, _ = pstats
+        return sum(int(att[i]) * (i + 1) * B1 for i in range(n))
+
+    b0 = s.move_counters(0)[0]
+    p0 = moved(s, s.perm_stats(1, n))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    s.sweep([0, 1], [n, n], sweeps)
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    beads = (s.move_counters(0)[0] - b0) * B1 + moved(s, s.perm_stats(1, n)) - p0
+    att, acc = s.perm_stats(1, n)
+    cycles = {int(i + 1): [int(att[i]), int(acc[i])] for i in range(n) if att[i]}
+    s.close()
+    oracle.build()
+    o = oracle.OracleSim(xml, base_dir=tmp)
+    o.set_path(path)
+    o.move_attempts(0, n)
+    o.move_attempts(1, n)
+    cb0, cp0 = o.move_stats(0)[0], moved(o, o.perm_stats(1, n))
+    t0, done = time.perf_counter(), 0
+    while time.perf_counter() - t0 < cpu_seconds:
+        o.move_attempts(0, n)
+        o.move_attempts(1, n)
+        done += 1
+    el = time.perf_counter() - t0
+    cbeads = (o.move_stats(0)[0] - cb0) * B1 + moved(o, o.perm_stats(1, n)) - cp0
+    o.close()
+    return {"workload": f"trapped bosons N={n} omega=1 beta=4 M={m_beads}, Bisect + PermBisectIterative at level {lvl}",
+            "sweeps": sweeps, "ms_per_sweep": ms / sweeps, "value": beads / (ms / 1e3), "unit": METRIC,
+            "perm_attempts_accepts_by_cycle_length": cycles,
+            "cpu_oracle_1_core": {"value": cbeads / el, "unit": METRIC, "sweeps": done, "seconds": el},
+            "note": "one CTA per chain runs the attempts in order (PermBisectKernel), FP64; device time of the "
+                    "sweep calls, host gaps between the per-move launches included"}
+
+
 def cpu_oracle_chains(items, tmp, seconds, chains):
     """The oracle on one host core, cycling through `chains` in chunks of attempts."""
     import oracle
@@ -473,6 +532,7 @@ def run_ours(args):
     eg, _, _, _ = egas_plain(local, args.steps, args.warmup, tmp, flush)
     large = large_mixed_precision(local, tmp) if not args.no_large else None
     hmc = hmc_adjoint(local, tmp) if not args.no_large else None
+    exch = exchange_bosons(local, tmp)
     cpu = None
     if not args.no_cpu_baseline:
         moves, el = cpu_oracle_chains(items, tmp, 12.0, sample)
@@ -503,6 +563,7 @@ def run_ours(args):
         "plain_electron_gas": eg,
         "mixed_precision_large": large,
         "hmc_adjoint": hmc,
+        "exchange_bosons": exch,
         "wall_s": wall,
     }
     print(json.dumps(line))

@@ -3,6 +3,7 @@
     python -m simpimc_gb300.profile_cases batch    # 256 uneven trapped-Coulomb chains: 1 + 1 sweep launches
     python -m simpimc_gb300.profile_cases egas     # 66-electron gas: 1 + 1 sweep launches (528 attempts each)
     python -m simpimc_gb300.profile_cases large32  # 1024-electron gas, FP32 mode: 1 + 1 launches of 64 attempts
+    python -m simpimc_gb300.profile_cases bosons   # 32 trapped bosons: Bisect and PermBisectIterative, 1 + 1 sweeps
 
 The first two hold well under 100 MB on the device, the third about 1.3 GB; a capture of the
 second launch (`-k regex:<Kernel> -s 1 -c 1`) ends in seconds (the large case with one or two
@@ -57,10 +58,22 @@ def large32_case(d):
     print(f"large32 ok: {s.move_counters(0)[0] + s.move_counters(1)[0]} attempts, {s.n_k} k-vectors")
 
 
+def bosons_case(d):
+    from . import Simulation
+    from .configs import trapped_bosons
+    xml, path = trapped_bosons(d, n_part=32, beta=4.0, n_bead=32, n_level=3, seed=77)
+    s = Simulation(xml, base_dir=d)
+    s.set_path(path * 0.4)
+    s.sweep([0, 1], [32, 32], 1)
+    s.sweep([0, 1], [32, 32], 1)
+    s.synchronize()
+    print(f"bosons ok: {s.move_counters(0)[0] + s.move_counters(1)[0]} attempts")
+
+
 def main(argv):
     case = argv[1] if len(argv) > 1 else "batch"
     with tempfile.TemporaryDirectory() as d:
-        {"batch": batch_case, "egas": egas_case, "large32": large32_case}[case](d)
+        {"batch": batch_case, "egas": egas_case, "large32": large32_case, "bosons": bosons_case}[case](d)
 
 
 if __name__ == "__main__":

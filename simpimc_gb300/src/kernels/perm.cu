@@ -40,7 +40,8 @@ namespace {
 
 constexpr int kPermThreads = 256;
 constexpr int kVariantBisect = 0, kVariantIterative = 1, kVariantTable = 2;
-constexpr uint32_t kPermMaxPart = 4096;
+constexpr uint32_t kPermMaxPart = 2048;
+constexpr uint32_t kCycleCache = 8192;  // table cycle weights kept in shared memory up to this count
 constexpr uint32_t kPermChunk = 2048;  // attempts per launch
 
 struct PermArgs {
@@ -71,10 +72,36 @@ struct PermShared {
     uint32_t n, bead0, p_first, fail;
     double weight, tot0, tot1;
     Philox4 w0;
-    double red[kPermThreads / 32];
-    double acc[3];
+    double red[3 * (kPermThreads / 32)];
+    double qpc, x;
+    uint32_t p, cont;
     int decide;
 };
+
+// Three block-wide sums at once: warp trees, then every thread adds the warp partials in warp
+// order, so all threads hold the same values.
+__device__ __forceinline__ void BlockSum3(double& a0, double& a1, double& a2, double* red) {
+    a0 = WarpSum(a0);
+    a1 = WarpSum(a1);
+    a2 = WarpSum(a2);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) {
+        red[warp] = a0;
+        red[nw + warp] = a1;
+        red[2 * nw + warp] = a2;
+    }
+    __syncthreads();
+    double t0 = 0., t1 = 0., t2 = 0.;
+    for (int w = 0; w < nw; ++w) {
+        t0 += red[w];
+        t1 += red[nw + w];
+        t2 += red[2 * nw + w];
+    }
+    a0 = t0;
+    a1 = t1;
+    a2 = t2;
+    __syncthreads();
+}
 
 __device__ __forceinline__ void LoadR(const double* __restrict__ pos, uint32_t np, uint32_t n_d, uint32_t b, uint32_t g, double* r) {
 #pragma unroll
@@ -127,14 +154,14 @@ __device__ void BuildTable(const PermArgs& a, uint32_t bead0, uint32_t B, bool r
 }
 
 // Cycle weights of the table (perm_bisect_table_class.h:15-26) into cw.
-__device__ void CycleWeights(const PermArgs& a, uint32_t N) {
+__device__ void CycleWeights(const PermArgs& a, uint32_t N, double* cw) {
     const uint32_t n_cycles = a.n_comb * a.n_types, k = a.k_part;
     for (uint32_t c = threadIdx.x; c < n_cycles; c += blockDim.x) {
         const uint32_t* part = a.combs + (size_t)(c % a.n_comb) * k;
         const uint32_t* pm = a.types + (size_t)(c / a.n_comb) * k;
         double w = 1.;
         for (uint32_t i = 0; i < k; ++i) w *= a.t[(size_t)part[i] * N + part[pm[i]]];
-        a.cw[c] = w;
+        cw[c] = w;
     }
 }
 
@@ -159,7 +186,13 @@ __global__ void __launch_bounds__(kPermThreads, 1) PermBisectKernel(const __grid
     uint32_t* end_old = lab_hi + N;
     uint32_t* end_new = end_old + N;
     uint32_t* lst = end_new + N;
-    double2* ph = reinterpret_cast<double2*>(reinterpret_cast<uintptr_t>(lst + 2 * N + 3) & ~(uintptr_t)15);
+    // rows of the weight table for the cycle walk [2N], the table's cycle weights [kCycleCache]
+    double* row = reinterpret_cast<double*>(reinterpret_cast<uintptr_t>(lst + 2 * N + 1) & ~(uintptr_t)7);
+    const uint32_t n_cycles = a.n_comb * a.n_types;
+    const bool cw_shared = a.variant == kVariantTable && n_cycles <= kCycleCache;
+    double* cws = row + 2 * N;
+    double* cw = cw_shared ? cws : a.cw;
+    double2* ph = reinterpret_cast<double2*>(reinterpret_cast<uintptr_t>(cws + (cw_shared ? n_cycles : 0) + 1) & ~(uintptr_t)15);
     __shared__ uint32_t s_nlist;
     for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) lo_idx[i] = lpos[i] = -1;
     const uint32_t base_m = a.variant == kVariantBisect ? 1u : 1u + N;
@@ -188,40 +221,67 @@ __global__ void __launch_bounds__(kPermThreads, 1) PermBisectKernel(const __grid
             BuildTable(a, bead0, B, a.variant == kVariantTable, nullptr, nullptr);
             __syncthreads();
             if (a.variant == kVariantTable) {
-                CycleWeights(a, N);
+                CycleWeights(a, N, cw);
                 __syncthreads();
             }
-            if (threadIdx.x == 0) {
-                if (a.variant == kVariantIterative) {
-                    // perm_bisect_iterative_class.h:32-110
-                    const uint32_t p0 = sh.p_first;
-                    uint32_t p = p0, n = 0;
-                    bool ok = false;
-                    for (uint32_t step = 0; step < N; ++step) {
-                        part[n++] = p;
-                        for (uint32_t i = 0; i < n; ++i) a.tc[(size_t)p * N + part[i]] = 0.;
-                        a.tc[(size_t)p * N + p0] = a.t[(size_t)p * N + p0];
+            if (a.variant == kVariantIterative && threadIdx.x < 32) {
+                // perm_bisect_iterative_class.h:32-110 on warp 0: the row of the table is staged in
+                // shared memory and its quotients formed by the lanes; lane 0 adds in the
+                // reference's order, so the sums and choices are those of the sequential walk.
+                const uint32_t lane = threadIdx.x, p0 = sh.p_first;
+                double* rt = row;
+                double* rc = row + N;
+                uint32_t p = p0, n = 0;
+                bool ok = false;
+                for (uint32_t step = 0; step < N; ++step) {
+                    if (lane == 0) part[n] = p;
+                    ++n;
+                    __syncwarp();
+                    for (uint32_t i = lane; i < n; i += 32) a.tc[(size_t)p * N + part[i]] = 0.;
+                    __syncwarp();
+                    if (lane == 0) a.tc[(size_t)p * N + p0] = a.t[(size_t)p * N + p0];
+                    __syncwarp();
+                    for (uint32_t i = lane; i < N; i += 32) {
+                        rt[i] = a.t[(size_t)p * N + i];
+                        rc[i] = a.tc[(size_t)p * N + i];
+                    }
+                    __syncwarp();
+                    if (lane == 0) {
                         double Qp = 0., Qpc = 0.;
                         for (uint32_t i = 0; i < N; ++i) {
-                            Qp += a.t[(size_t)p * N + i];
-                            Qpc += a.tc[(size_t)p * N + i];
+                            Qp += rt[i];
+                            Qpc += rc[i];
                         }
                         const Philox4 w = st.Block(1u + step);
-                        if (Qpc / Qp < Uniform53(w.v[0], w.v[1])) break;
-                        const double x = Uniform53(w.v[2], w.v[3]);
+                        sh.cont = !(Qpc / Qp < Uniform53(w.v[0], w.v[1]));
+                        sh.qpc = Qpc;
+                        sh.x = Uniform53(w.v[2], w.v[3]);
+                    }
+                    __syncwarp();
+                    if (!sh.cont) break;
+                    const double qpc = sh.qpc;
+                    for (uint32_t i = lane; i < N; i += 32) rt[i] = rc[i] / qpc;
+                    __syncwarp();
+                    if (lane == 0) {
+                        const double x = sh.x;
                         double tQ = 0.;
                         for (uint32_t i = 0; i < N; ++i) {
-                            tQ += a.tc[(size_t)p * N + i] / Qpc;
+                            tQ += rt[i];
                             if (tQ > x) {
                                 p = i;
                                 break;
                             }
                         }
-                        if (p == p0) {
-                            ok = true;
-                            break;
-                        }
+                        sh.p = p;
                     }
+                    __syncwarp();
+                    p = sh.p;
+                    if (p == p0) {
+                        ok = true;
+                        break;
+                    }
+                }
+                if (lane == 0) {
                     if (!ok) {
                         sh.n = 0;
                         sh.fail = 1;
@@ -233,42 +293,41 @@ __global__ void __launch_bounds__(kPermThreads, 1) PermBisectKernel(const __grid
                         sh.n = n;
                         for (uint32_t i = 0; i < n; ++i) sigma[i] = (i + 1) % n;
                     }
-                } else {
-                    // perm_bisect_table_class.h:10-28, 105-119
-                    const uint32_t n_cycles = a.n_comb * a.n_types;
-                    double total = 0.;
-                    uint32_t kept = 0;
-                    for (uint32_t c = 0; c < n_cycles; ++c) {
-                        const double w = a.cw[c];
-                        if (w > a.epsilon) {
-                            total += w;
-                            a.ccon[kept] = total;
-                            a.cidx[kept] = c;
-                            ++kept;
-                        }
-                    }
-                    const double x = Uniform53(sh.w0.v[2], sh.w0.v[3]) * total;
-                    uint32_t kk = 0;
-                    if (!(x < a.ccon[0])) {
-                        uint32_t hi = kept, lo = 0;
-                        while (hi - lo > 1) {
-                            const uint32_t mid = (hi + lo) >> 1;
-                            if (x < a.ccon[mid]) hi = mid;
-                            else lo = mid;
-                        }
-                        kk = min(hi, kept - 1);
-                    }
-                    const uint32_t c = a.cidx[kk];
-                    const uint32_t* cp = a.combs + (size_t)(c % a.n_comb) * a.k_part;
-                    const uint32_t* pm = a.types + (size_t)(c / a.n_comb) * a.k_part;
-                    for (uint32_t i = 0; i < a.k_part; ++i) {
-                        part[i] = cp[i];
-                        sigma[i] = pm[i];
-                    }
-                    sh.n = a.k_part;
-                    sh.weight = a.cw[c];
-                    sh.tot0 = total;
                 }
+            } else if (a.variant == kVariantTable && threadIdx.x == 0) {
+                // perm_bisect_table_class.h:10-28, 105-119
+                double total = 0.;
+                uint32_t kept = 0;
+                for (uint32_t c = 0; c < n_cycles; ++c) {
+                    const double w = cw[c];
+                    if (w > a.epsilon) {
+                        total += w;
+                        a.ccon[kept] = total;
+                        a.cidx[kept] = c;
+                        ++kept;
+                    }
+                }
+                const double x = Uniform53(sh.w0.v[2], sh.w0.v[3]) * total;
+                uint32_t kk = 0;
+                if (!(x < a.ccon[0])) {
+                    uint32_t hi = kept, lo = 0;
+                    while (hi - lo > 1) {
+                        const uint32_t mid = (hi + lo) >> 1;
+                        if (x < a.ccon[mid]) hi = mid;
+                        else lo = mid;
+                    }
+                    kk = min(hi, kept - 1);
+                }
+                const uint32_t c = a.cidx[kk];
+                const uint32_t* cp = a.combs + (size_t)(c % a.n_comb) * a.k_part;
+                const uint32_t* pm = a.types + (size_t)(c / a.n_comb) * a.k_part;
+                for (uint32_t i = 0; i < a.k_part; ++i) {
+                    part[i] = cp[i];
+                    sigma[i] = pm[i];
+                }
+                sh.n = a.k_part;
+                sh.weight = cw[c];
+                sh.tot0 = total;
             }
         } else if (threadIdx.x == 0) {
             part[0] = sh.p_first;
@@ -473,9 +532,8 @@ __global__ void __launch_bounds__(kPermThreads, 1) PermBisectKernel(const __grid
                 }
             }
             // decision (bisect_class.h:103-118)
-            const double t_old = BlockSum(old_lsp, sh.red);
-            const double t_new = BlockSum(new_lsp, sh.red);
-            const double t_ds = BlockSum(dS, sh.red);
+            BlockSum3(old_lsp, new_lsp, dS, sh.red);
+            const double t_old = old_lsp, t_new = new_lsp, t_ds = dS;
             if (threadIdx.x == 0) {
                 const double la = -t_new + t_old - t_ds + prev;
                 const float lu = LogF(U24(st.Block(base_u + (mv.n_level - 1u - (uint32_t)level)).v[0]));
@@ -498,13 +556,12 @@ __global__ void __launch_bounds__(kPermThreads, 1) PermBisectKernel(const __grid
         if (accepted && a.variant == kVariantTable && n < N) {
             BuildTable(a, bead0, B, true, lo_idx, end_new);
             __syncthreads();
-            CycleWeights(a, N);
+            CycleWeights(a, N, cw);
             __syncthreads();
             if (threadIdx.x == 0) {
-                const uint32_t n_cycles = a.n_comb * a.n_types;
                 double total = 0.;
                 for (uint32_t c = 0; c < n_cycles; ++c)
-                    if (a.cw[c] > a.epsilon) total += a.cw[c];
+                    if (cw[c] > a.epsilon) total += cw[c];
                 const Philox4 w = st.Block(base_u + mv.n_level);
                 sh.decide = !(sh.tot0 / total < Uniform53(w.v[0], w.v[1]));
             }
@@ -645,7 +702,7 @@ bool Context::PermutingSpecies(uint32_t s) const {
 void Context::PermAttempts(uint32_t m, uint64_t n_att) {
     MoveHost& mh = moves[m];
     const uint32_t sp = mh.dev.species, N = sys.sp_n[sp], M = sys.M;
-    if (N > kPermMaxPart) throw PimcError(kErrUnsupported, "permuting moves support at most 4096 particles per species");
+    if (N > kPermMaxPart) throw PimcError(kErrUnsupported, "permuting moves support at most 2048 particles per species");
     if (n_att == 0) return;
     EnsureFP64();
     const uint32_t B = 1u << mh.dev.n_level;
@@ -685,7 +742,9 @@ void Context::PermAttempts(uint32_t m, uint64_t n_att) {
     a.counters = perm_cnt_->as<unsigned long long>();
     a.err = ErrWord();
     const int stride = std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
-    const size_t smem = (size_t)N * 10 * sizeof(uint32_t) + 32 + (size_t)2 * 3 * stride * sizeof(double2);
+    const size_t cyc_smem = (mh.kind == 3 && n_cycles <= kCycleCache) ? n_cycles * sizeof(double) : 0;
+    const size_t smem = (size_t)N * 10 * sizeof(uint32_t) + 16 + (size_t)N * 2 * sizeof(double) + cyc_smem + 16 +
+                        (size_t)2 * 3 * stride * sizeof(double2);
     CudaCheck(cudaFuncSetAttribute(PermBisectKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "perm smem attribute");
     CudaCheck(cudaMemsetAsync(perm_cnt_->ptr, 0, (2 + 2 * (size_t)N) * sizeof(unsigned long long), stream), "perm counters");
     (void)B;
