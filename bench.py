@@ -402,8 +402,51 @@ def exchange_bosons(local, tmp, sweeps=20, cpu_seconds=6.0):
             "sweeps": sweeps, "ms_per_sweep": ms / sweeps, "value": beads / (ms / 1e3), "unit": METRIC,
             "perm_attempts_accepts_by_cycle_length": cycles,
             "cpu_oracle_1_core": {"value": cbeads / el, "unit": METRIC, "sweeps": done, "seconds": el},
-            "note": "one CTA per chain runs the attempts in order (PermBisectKernel), FP64; device time of the "
-                    "sweep calls, host gaps between the per-move launches included"}
+            "note": "one CTA per chain runs the attempts in order (PermBisectKernelDD, double-float); device time of "
+                    "the sweep calls, host gaps between the per-move launches included"}
+
+
+def exchange_bosons_chains(local, tmp, n_chains=152, sweeps=10):
+    """The exchanging-boson chain of exchange_bosons, n_chains independent copies (seeds 77 + c):
+    one context and CUDA stream per chain, each driven by its own host thread, so the one-CTA
+    permutation kernels of different chains run side by side on the SMs. Wall-clock time of all
+    chains' sweeps (host threads started together, device synchronised on both sides)."""
+    import torch
+    from simpimc_gb300 import Simulation
+    from simpimc_gb300.configs import trapped_bosons
+    n, m_beads, lvl = 32, 32, 3
+    B1 = (1 << lvl) - 1
+    sims = []
+    for c in range(n_chains):
+        d = os.path.join(tmp, f"bosons{c}")
+        xml, path = trapped_bosons(d, n_part=n, beta=4.0, n_bead=m_beads, n_level=lvl, seed=77 + c)
+        s = Simulation(xml, base_dir=d, device=local, chain=c)
+        s.set_path(path * 0.4)
+        sims.append(s)
+
+    def run_all(k):
+        ts = [threading.Thread(target=s.sweep, args=([0, 1], [n, n], k)) for s in sims]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+
+    run_all(2)  # warm-up
+    before = [(s.move_counters(0)[0], s.perm_stats(1, n)[0]) for s in sims]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    run_all(sweeps)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    beads = 0
+    for s, (b0, pa0) in zip(sims, before):
+        pa1 = s.perm_stats(1, n)[0]
+        beads += (s.move_counters(0)[0] - b0) * B1 + sum(int(pa1[i] - pa0[i]) * (i + 1) * B1 for i in range(n))
+    for s in sims:
+        s.close()
+    return {"workload": f"{n_chains} independent chains of the exchange_bosons system (seeds 77 + c)", "sweeps_per_chain": sweeps,
+            "seconds": el, "value": beads / el, "unit": METRIC,
+            "note": "one context, stream and host thread per chain; wall-clock time including host launch and counter reads"}
 
 
 def cpu_oracle_chains(items, tmp, seconds, chains):
@@ -533,6 +576,7 @@ def run_ours(args):
     large = large_mixed_precision(local, tmp) if not args.no_large else None
     hmc = hmc_adjoint(local, tmp) if not args.no_large else None
     exch = exchange_bosons(local, tmp)
+    exch["many_chains"] = exchange_bosons_chains(local, tmp)
     cpu = None
     if not args.no_cpu_baseline:
         moves, el = cpu_oracle_chains(items, tmp, 12.0, sample)

@@ -169,6 +169,10 @@ class Context {
     // Bisection on a species with exchanges (src/kernels/perm.cu): the permuting moves and the
     // plain bisection of a species that has one or carries a non-identity path permutation.
     void PermAttempts(uint32_t m, uint64_t n);
+    void PermEnqueue(uint32_t m, uint64_t n);
+    void PermFinish();
+    uint32_t perm_pending_ = 0;  // moves with permutation launches not yet folded into their counters
+    void* MoveDescriptors();  // double-float move descriptors on the device (sweep.cu)
     bool PermutingSpecies(uint32_t s) const;
     // The path permutation: perm[g] = particle whose slice-0 bead follows bead (g, M - 1), global
     // indices; the host copy is refreshed after every device update.
@@ -274,7 +278,7 @@ class Context {
     std::unique_ptr<DeviceBuffer> grad_, mom_, pos_save_, rho_scratch_, phase_tab_;  // adjoint / HMC work arrays
     std::vector<std::unique_ptr<DeviceBuffer>> adj_vk_;                              // double-float v_k per action
     std::unique_ptr<DeviceBuffer> partials_, result_, bar_, err_, pairs_, rho_tmp_, parts_, kmag_dev_, sched_, accepts_;
-    std::unique_ptr<DeviceBuffer> perm_, perm_inv_, perm_t_, perm_cyc_, perm_drho_, perm_hold_, perm_cnt_;
+    std::unique_ptr<DeviceBuffer> perm_, perm_inv_, perm_t_, perm_cyc_, perm_drho_, perm_hold_, perm_cnt_, perm_prop_, perm_segold_;
     size_t partials_cap_ = 0, pairs_cap_ = 0, rho_tmp_cap_ = 0, parts_cap_ = 0;
 
     template <class T>

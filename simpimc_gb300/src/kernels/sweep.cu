@@ -1147,6 +1147,18 @@ void Split(double x, dd& out) {
     out = dd{h, l};
 }
 
+/// The 53-bit uniform of two Philox words (philox.h Uniform53) as a float pair, without FP64:
+/// u 2^53 = (w0 >> 5) 2^26 + (w1 >> 6); the leading 24 bits exactly, the remaining 29 rounded.
+__device__ __forceinline__ void Split53(uint32_t w0, uint32_t w1, dd& u) {
+    const uint32_t A = w0 >> 5, Bw = w1 >> 6;
+    const float hi = __fmul_rn(__uint2float_rn(A >> 3), 5.9604644775390625e-08f);  // 2^-24
+    const unsigned long long R = ((unsigned long long)(A & 7u) << 26) | (unsigned long long)Bw;
+    const float lo = __fmul_rn(__ull2float_rn(R), 1.1102230246251565e-16f);  // 2^-53
+    u = FastTwoSum(hi, lo);
+}
+
+#include "perm_dd.cuh"
+
 }  // namespace
 
 // ---------------------------------------------------------------------------------------------
@@ -1419,53 +1431,18 @@ void Context::BuildSweepTables() {
     sweep_tables_built_ = true;
 }
 
-void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep) {
-    if (n_entries == 0 || n_rep == 0) return;
-    if (n_entries > 1024) throw PimcError(kErrArg, "schedule longer than 1024 entries");
-    bool own_launches = false;
-    auto on_perm_kernel = [&](uint32_t m) {
-        return moves[m].kind == 2 || moves[m].kind == 3 || (moves[m].kind == 0 && PermutingSpecies(moves[m].dev.species));
-    };
-    for (uint32_t e = 0; e < n_entries; ++e) {
-        if (mv[e] >= moves.size()) throw PimcError(kErrArg, "move index out of range");
-        own_launches |= moves[mv[e]].kind == 1 || on_perm_kernel(mv[e]);
-    }
-    if (own_launches) {  // HMC and exchanging species run their own launches, entry by entry
-        for (uint64_t r = 0; r < n_rep; ++r)
-            for (uint32_t e = 0; e < n_entries; ++e) {
-                if (moves[mv[e]].kind == 1) {
-                    HmcAttempts(mv[e], counts[e]);
-                } else if (on_perm_kernel(mv[e])) {
-                    PermAttempts(mv[e], counts[e]);
-                } else {
-                    const uint64_t c1 = counts[e];
-                    Sweep(&mv[e], &c1, 1, 1);
-                }
-            }
-        return;
-    }
+// Double-float move descriptors of every move (sampling and kinetic tables per level, trap
+// cofactors, pair indices) in the sweep's descriptor buffer, rebuilt when a level changes
+// (adaptive bisection between blocks). Returns the buffer: [kMaxMoves] MoveDD, then the schedule
+// and counters the sweep kernel uses.
+void* Context::MoveDescriptors() {
     BuildSweepTables();
-    // Move descriptors, rebuilt when a level changes (adaptive bisection between blocks).
-    uint32_t max_level = 1;
-    for (size_t m = 0; m < moves.size(); ++m) {
-        const MoveDev& d = moves[m].dev;
-        if (d.n_level > 8) throw PimcError(kErrUnsupported, "bisection level above 8 in the sweep kernel");
-        max_level = std::max(max_level, d.n_level);
-        for (int i = 0; i < d.n_pair; ++i) {
-            const PairDev& p = sys.pair[d.pair[i]];
-            if (p.use_long_range && p.max_level > 0)
-                throw PimcError(kErrUnsupported, "long-range pair action with max_level > 0 in the sweep kernel");
-        }
-        if (d.n_kinetic > kMoveKinetic) throw PimcError(kErrUnsupported, "more than two kinetic actions on one species");
-    }
+    for (size_t m = 0; m < moves.size(); ++m)
+        if (moves[m].dev.n_kinetic > kMoveKinetic) throw PimcError(kErrUnsupported, "more than two kinetic actions on one species");
     std::vector<uint32_t> levels(moves.size());
     for (size_t m = 0; m < moves.size(); ++m) levels[m] = moves[m].dev.n_level;
     if (!sweep_desc_) sweep_desc_.reset(new DeviceBuffer(sizeof(MoveDD) * kMaxMoves + 4096 + 8192 + 2 * kMaxMoves * 8));
-    char* base = sweep_desc_->as<char>();
-    MoveDD* dmoves = reinterpret_cast<MoveDD*>(base);
-    uint32_t* dsm = reinterpret_cast<uint32_t*>(base + sizeof(MoveDD) * kMaxMoves);
-    uint64_t* dsc = reinterpret_cast<uint64_t*>(base + sizeof(MoveDD) * kMaxMoves + 4096);
-    unsigned long long* dcount = reinterpret_cast<unsigned long long*>(base + sizeof(MoveDD) * kMaxMoves + 4096 + 8192);
+    MoveDD* dmoves = sweep_desc_->as<MoveDD>();
     if (levels != desc_levels_) {
         std::vector<MoveDD> md(kMaxMoves, MoveDD{});
         for (size_t m = 0; m < moves.size(); ++m) {
@@ -1501,6 +1478,65 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
         Sync();
         desc_levels_ = levels;
     }
+    return sweep_desc_->ptr;
+}
+
+void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep) {
+    if (n_entries == 0 || n_rep == 0) return;
+    if (n_entries > 1024) throw PimcError(kErrArg, "schedule longer than 1024 entries");
+    bool own_launches = false;
+    auto on_perm_kernel = [&](uint32_t m) {
+        return moves[m].kind == 2 || moves[m].kind == 3 || (moves[m].kind == 0 && PermutingSpecies(moves[m].dev.species));
+    };
+    for (uint32_t e = 0; e < n_entries; ++e) {
+        if (mv[e] >= moves.size()) throw PimcError(kErrArg, "move index out of range");
+        own_launches |= moves[mv[e]].kind == 1 || on_perm_kernel(mv[e]);
+    }
+    bool all_perm = true;
+    for (uint32_t e = 0; e < n_entries; ++e) all_perm &= on_perm_kernel(mv[e]);
+    if (all_perm) {  // every entry on the permutation kernel: enqueue them all, wait once
+        try {
+            for (uint64_t r = 0; r < n_rep; ++r)
+                for (uint32_t e = 0; e < n_entries; ++e) PermEnqueue(mv[e], counts[e]);
+        } catch (...) {
+            PermFinish();
+            throw;
+        }
+        PermFinish();
+        return;
+    }
+    if (own_launches) {  // HMC and exchanging species run their own launches, entry by entry
+        for (uint64_t r = 0; r < n_rep; ++r)
+            for (uint32_t e = 0; e < n_entries; ++e) {
+                if (moves[mv[e]].kind == 1) {
+                    HmcAttempts(mv[e], counts[e]);
+                } else if (on_perm_kernel(mv[e])) {
+                    PermAttempts(mv[e], counts[e]);
+                } else {
+                    const uint64_t c1 = counts[e];
+                    Sweep(&mv[e], &c1, 1, 1);
+                }
+            }
+        return;
+    }
+    BuildSweepTables();
+    uint32_t max_level = 1;
+    for (size_t m = 0; m < moves.size(); ++m) {
+        const MoveDev& d = moves[m].dev;
+        if (d.n_level > 8) throw PimcError(kErrUnsupported, "bisection level above 8 in the sweep kernel");
+        max_level = std::max(max_level, d.n_level);
+        for (int i = 0; i < d.n_pair; ++i) {
+            const PairDev& p = sys.pair[d.pair[i]];
+            if (p.use_long_range && p.max_level > 0)
+                throw PimcError(kErrUnsupported, "long-range pair action with max_level > 0 in the sweep kernel");
+        }
+    }
+    char* base = static_cast<char*>(MoveDescriptors());
+    MoveDD* dmoves = reinterpret_cast<MoveDD*>(base);
+    uint32_t* dsm = reinterpret_cast<uint32_t*>(base + sizeof(MoveDD) * kMaxMoves);
+    uint64_t* dsc = reinterpret_cast<uint64_t*>(base + sizeof(MoveDD) * kMaxMoves + 4096);
+    unsigned long long* dcount = reinterpret_cast<unsigned long long*>(base + sizeof(MoveDD) * kMaxMoves + 4096 + 8192);
+
     CudaCheck(cudaMemcpyAsync(dsm, mv, n_entries * 4, cudaMemcpyHostToDevice, stream), "schedule");
     CudaCheck(cudaMemcpyAsync(dsc, counts, n_entries * 8, cudaMemcpyHostToDevice, stream), "schedule");
     CudaCheck(cudaMemsetAsync(dcount, 0, 2 * kMaxMoves * 8, stream), "counters");
@@ -1659,6 +1695,149 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
         moves[m].total_level0 += cnt[kMaxMoves + m];
     }
     last_grid_ = G;
+}
+
+// Attempts of a permuting move, or of the plain bisection of an exchanging species, on the
+// double-float permutation kernel (perm_dd.cuh): one CTA runs them in order, in launches of at
+// most 2048 attempts.
+void Context::PermAttempts(uint32_t m, uint64_t n_att) {
+    PermEnqueue(m, n_att);
+    PermFinish();
+}
+
+// Launches the attempts on the context's stream without waiting; the move's counters accumulate
+// on the device until PermFinish reads them.
+void Context::PermEnqueue(uint32_t m, uint64_t n_att) {
+    MoveHost& mh = moves[m];
+    const uint32_t sp = mh.dev.species, N = sys.sp_n[sp], M = sys.M;
+    if (N > kPermMaxPart) throw PimcError(kErrUnsupported, "exchanging species of at most 512 particles");
+    if (precision == 32 && sys.sp_rho[sp] >= 0 && sys.K)
+        throw PimcError(kErrUnsupported, "the permutation kernel keeps double-float densities: set precision 64");
+    if (n_att == 0) return;
+    const uint32_t B = 1u << mh.dev.n_level;
+    MoveDD* dmoves = static_cast<MoveDD*>(MoveDescriptors());
+    EnsureDD();
+    const size_t n_cycles = (size_t)mh.perm_n_comb * mh.perm_n_types, nc = std::max<size_t>(n_cycles, 1);
+    auto ensure = [](std::unique_ptr<DeviceBuffer>& b, size_t bytes) {
+        if (!b || b->bytes < bytes) b.reset(new DeviceBuffer(std::max<size_t>(bytes, 16)));
+    };
+    ensure(perm_t_, (size_t)N * N * sizeof(float2) * 3);  // [2][N][N] tables (when not shared) and the exponents
+    ensure(perm_segold_, (size_t)N * (B + 1) * 3 * sizeof(float2));
+    ensure(perm_cyc_, nc * (3 * sizeof(float2) + sizeof(uint32_t)));
+    ensure(perm_prop_, (size_t)N * (B + 1) * 3 * sizeof(float2));
+    ensure(perm_drho_, (size_t)(B + 1) * std::max<uint32_t>(sys.K, 1) * sizeof(float4));
+    ensure(perm_hold_, (size_t)N * M * 3 * sizeof(float2));
+    const size_t cnt_stride = 2 + 2 * (size_t)kPermMaxPart;
+    if (!perm_cnt_) {
+        perm_cnt_.reset(new DeviceBuffer(kMaxMoves * cnt_stride * sizeof(unsigned long long)));
+        CudaCheck(cudaMemsetAsync(perm_cnt_->ptr, 0, perm_cnt_->bytes, stream), "perm counters");
+    }
+    PermArgsDD a{};
+    a.n_d = sys.n_d;
+    a.M = M;
+    a.n_pad = sys.n_pad;
+    a.K = sys.K;
+    Split(sys.L, a.L);
+    Split(sys.iL, a.iL);
+    Split(sys.tau, a.tau);
+    Split(2. * M_PI, a.two_pi);
+    Split(std::log(2.), a.ln2);
+    Split(1. / (4. * mh.dev.lambda * sys.tau * B), a.i4B);  // i_4_lambda_tau_n_bisect_beads (bisect_class.h:182)
+    Split(mh.perm_epsilon, a.eps);
+    a.log_eps = (float)std::log(mh.perm_epsilon);
+    for (int s = 0; s < kMaxSpecies; ++s) {
+        a.sp_off[s] = sys.sp_off[s];
+        a.sp_n[s] = sys.sp_n[s];
+        a.sp_rho[s] = sys.sp_rho[s];
+    }
+    for (int d = 0; d < 3; ++d) a.max_index[d] = sys.max_index[d];
+    a.pos = pos_dd_->as<float2>();
+    a.rho = (rho_slots && sys.K) ? rho_dd_->as<float4>() : nullptr;
+    a.kidx = sys.kidx;
+    a.phase256 = sweep_tables_->as<float4>();
+    a.mv = dmoves + m;
+    a.pairs = reinterpret_cast<const PairDD*>(sweep_tables_->as<char>() + sizeof(float4) * 256);
+    a.variant = mh.kind == 2 ? kPermVariantIterative : (mh.kind == 3 ? kPermVariantTable : kPermVariantBisect);
+    a.seed = seed;
+    a.chain = chain;
+    a.move_index = m;
+    a.k_part = mh.perm_k;
+    a.n_comb = mh.perm_n_comb;
+    a.n_types = mh.perm_n_types;
+    a.combs = mh.perm_combs ? mh.perm_combs->as<uint32_t>() : nullptr;
+    a.types = mh.perm_types ? mh.perm_types->as<uint32_t>() : nullptr;
+    a.tg = perm_t_->as<float2>();
+    a.ex = a.tg + (size_t)2 * N * N;
+    a.seg_old_g = perm_segold_->as<float2>();
+    a.cw = perm_cyc_->as<float2>();
+    a.cwl = a.cw + nc;
+    a.ccon = a.cwl + nc;
+    a.cidx = reinterpret_cast<uint32_t*>(a.ccon + nc);
+    a.prop = perm_prop_->as<float2>();
+    a.drho = perm_drho_->as<float4>();
+    a.hold = perm_hold_->as<float2>();
+    a.perm = perm_->as<uint32_t>();
+    a.perm_inv = perm_inv_->as<uint32_t>();
+    a.counters = perm_cnt_->as<unsigned long long>() + m * cnt_stride;
+    a.err = ErrWord();
+    const size_t stride = (size_t)std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
+    const uint32_t cyc_shared = (mh.kind == 3 && n_cycles <= kPermCycleCache) ? (uint32_t)n_cycles : 0u;
+    const size_t smem = PermLayout(N, cyc_shared, mh.kind == 2 && N <= kPermTabShared, (uint32_t)stride).total;
+    // The limit is the device's opt-in maximum, the same value from every context and thread (a
+    // per-launch value would race between host threads driving different contexts).
+    static int smem_optin[64] = {0};
+    int& optin = smem_optin[device & 63];
+    if (!optin) {
+        int v = 0;
+        CudaCheck(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "shared memory limit");
+        cudaFuncAttributes fa;
+        CudaCheck(cudaFuncGetAttributes(&fa, PermBisectKernelDD), "perm kernel attributes");
+        v -= (int)fa.sharedSizeBytes;  // the static part counts against the same limit
+        CudaCheck(cudaFuncSetAttribute(PermBisectKernelDD, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "perm smem attribute");
+        optin = v;
+    }
+    if (smem > (size_t)optin) throw PimcError(kErrUnsupported, "permutation kernel shared memory above the device limit");
+    for (uint64_t done = 0; done < n_att;) {
+        const uint32_t chunk = (uint32_t)std::min<uint64_t>(2048, n_att - done);
+        a.attempt0 = mh.attempts + done;
+        a.n_attempts = chunk;
+        PermBisectKernelDD<<<1, kPermThreads, smem, stream>>>(a);
+        CudaCheck(cudaGetLastError(), "permuting bisection launch");
+        done += chunk;
+    }
+    mh.attempts += n_att;
+    mh.block_attempt += n_att;
+    perm_pending_ |= 1u << m;
+    fp64_valid = false;
+}
+
+// Waits for the enqueued permutation launches, folds their device counters into the moves'
+// counters and refreshes the host copy of the path permutation.
+void Context::PermFinish() {
+    if (!perm_pending_) return;
+    const size_t cnt_stride = 2 + 2 * (size_t)kPermMaxPart;
+    std::vector<unsigned long long> cnt(kMaxMoves * cnt_stride);
+    CudaCheck(cudaMemcpyAsync(cnt.data(), perm_cnt_->ptr, cnt.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream),
+              "read perm counters");
+    CudaCheck(cudaMemsetAsync(perm_cnt_->ptr, 0, perm_cnt_->bytes, stream), "perm counters");
+    SyncPermHost();  // synchronises the stream
+    const uint32_t pending = perm_pending_;
+    perm_pending_ = 0;
+    CheckDeviceError();
+    for (uint32_t m = 0; m < moves.size(); ++m) {
+        if (!(pending & (1u << m))) continue;
+        MoveHost& mh = moves[m];
+        const unsigned long long* c = cnt.data() + m * cnt_stride;
+        const uint32_t N = sys.sp_n[mh.dev.species];
+        mh.block_accept += c[0];
+        mh.total_accept += c[0];
+        mh.total_level0 += c[1];
+        if (mh.kind == 2 || mh.kind == 3)
+            for (uint32_t i = 0; i < N; ++i) {
+                mh.perm_attempt[i] += c[2 + i];
+                mh.perm_accept[i] += c[2 + N + i];
+            }
+    }
 }
 
 void Context::MoveAttempts(uint32_t m, uint64_t n) {
