@@ -406,11 +406,10 @@ def exchange_bosons(local, tmp, sweeps=20, cpu_seconds=6.0):
                     "the sweep calls, host gaps between the per-move launches included"}
 
 
-def exchange_bosons_chains(local, tmp, n_chains=152, sweeps=10):
-    """The exchanging-boson chain of exchange_bosons, n_chains independent copies (seeds 77 + c):
-    one context and CUDA stream per chain, each driven by its own host thread, so the one-CTA
-    permutation kernels of different chains run side by side on the SMs. Wall-clock time of all
-    chains' sweeps (host threads started together, device synchronised on both sides)."""
+def exchange_bosons_chains(local, tmp, n_chains=304, sweeps=10):
+    """The exchanging-boson chain of exchange_bosons, n_chains independent copies (seeds 77 + c),
+    one context per chain, all swept by pimc_sweep_chains: one launch with one CTA per chain.
+    Wall-clock time of the call, device synchronised on both sides."""
     import torch
     from simpimc_gb300 import Simulation
     from simpimc_gb300.configs import trapped_bosons
@@ -424,12 +423,10 @@ def exchange_bosons_chains(local, tmp, n_chains=152, sweeps=10):
         s.set_path(path * 0.4)
         sims.append(s)
 
+    from simpimc_gb300 import sweep_chains
+
     def run_all(k):
-        ts = [threading.Thread(target=s.sweep, args=([0, 1], [n, n], k)) for s in sims]
-        for t in ts:
-            t.start()
-        for t in ts:
-            t.join()
+        sweep_chains(sims, [0, 1], [n, n], k)
 
     run_all(2)  # warm-up
     before = [(s.move_counters(0)[0], s.perm_stats(1, n)[0]) for s in sims]
@@ -446,7 +443,7 @@ def exchange_bosons_chains(local, tmp, n_chains=152, sweeps=10):
         s.close()
     return {"workload": f"{n_chains} independent chains of the exchange_bosons system (seeds 77 + c)", "sweeps_per_chain": sweeps,
             "seconds": el, "value": beads / el, "unit": METRIC,
-            "note": "one context, stream and host thread per chain; wall-clock time including host launch and counter reads"}
+            "note": "pimc_sweep_chains: one launch, one CTA per chain; wall-clock time including argument upload and counter reads"}
 
 
 def cpu_oracle_chains(items, tmp, seconds, chains):

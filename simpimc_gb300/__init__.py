@@ -16,7 +16,7 @@ from pathlib import Path
 
 import numpy as np
 
-__all__ = ["Simulation", "ChainBatch", "PimcError", "load_library", "LIB_PATH"]
+__all__ = ["Simulation", "ChainBatch", "PimcError", "load_library", "LIB_PATH", "sweep_chains"]
 
 LIB_PATH = Path(__file__).resolve().parent / "lib" / "libsimpimc_gb300.so"
 
@@ -74,6 +74,7 @@ SIGNATURES = {
     "pimc_sweep": (C.c_int, [_P, _U32P, _U64P, C.c_uint32, C.c_uint64]),
     "pimc_move_stats": (C.c_int, [_P, C.c_uint32, _U64P]),
     "pimc_get_perm": (C.c_int, [_P, C.c_uint32, _U32P]),
+    "pimc_sweep_chains": (C.c_int, [C.POINTER(_P), C.c_uint32, _U32P, _U64P, C.c_uint32, C.c_uint64]),
     "pimc_set_perm": (C.c_int, [_P, C.c_uint32, _U32P]),
     "pimc_perm_stats": (C.c_int, [_P, C.c_uint32, _U64P, C.c_size_t]),
     "pimc_observable_accumulate": (C.c_int, [_P, C.c_uint32]),
@@ -361,6 +362,18 @@ class Simulation:
             self._check(self._lib.pimc_get_block(self._h, obs, b, _dp(buf), cap, C.byref(m)))
             out.append(buf[: m.value].copy())
         return out
+
+
+def sweep_chains(sims, moves, counts, n_rep: int = 1):
+    """pimc_sweep on many independent chains (Simulation objects of the same input structure on
+    one device): schedules on the permutation kernel run as one launch with one CTA per chain."""
+    if not sims:
+        return
+    lib = sims[0]._lib
+    hs = (_P * len(sims))(*[s._h for s in sims])
+    mv = np.ascontiguousarray(moves, dtype=np.uint32)
+    ct = np.ascontiguousarray(counts, dtype=np.uint64)
+    sims[0]._check(lib.pimc_sweep_chains(hs, len(sims), mv.ctypes.data_as(_U32P), ct.ctypes.data_as(_U64P), len(mv), n_rep))
 
 
 class ChainBatch:

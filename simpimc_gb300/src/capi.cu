@@ -2,8 +2,10 @@
 // each entry point converts them into a status code and keeps the message on the context.
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "../../include/simpimc_gb300.h"
+
 #include "capi_internal.h"
 
 namespace {
@@ -185,6 +187,17 @@ int pimc_move_attempts(pimc_ctx* ctx, uint32_t move, uint64_t n) {
 int pimc_sweep(pimc_ctx* ctx, const uint32_t* moves, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep) {
     if (n_entries && (!moves || !counts)) return PIMC_ERR_ARG;
     return Guard(ctx, [&](pimc::Context& c) { c.Sweep(moves, counts, n_entries, n_rep); });
+}
+
+int pimc_sweep_chains(pimc_ctx** ctxs, uint32_t n_ctx, const uint32_t* moves, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep) {
+    if (!ctxs || n_ctx == 0 || (n_entries && (!moves || !counts))) return PIMC_ERR_ARG;
+    for (uint32_t i = 0; i < n_ctx; ++i)
+        if (!ctxs[i] || !ctxs[i]->c) return PIMC_ERR_ARG;
+    return Guard(ctxs[0], [&](pimc::Context&) {
+        std::vector<pimc::Context*> cs(n_ctx);
+        for (uint32_t i = 0; i < n_ctx; ++i) cs[i] = ctxs[i]->c.get();
+        pimc::SweepChains(cs, moves, counts, n_entries, n_rep);
+    });
 }
 
 int pimc_move_stats(pimc_ctx* ctx, uint32_t move, uint64_t* out) {

@@ -171,6 +171,8 @@ class Context {
     void PermAttempts(uint32_t m, uint64_t n);
     void PermEnqueue(uint32_t m, uint64_t n);
     void PermFinish();
+    void PermPrepare(const uint32_t* mv, uint32_t n_entries);
+    void PermArgs(uint32_t m, void* out, size_t* smem);  // the kernel's arguments for move m (sweep.cu)
     uint32_t perm_pending_ = 0;  // moves with permutation launches not yet folded into their counters
     void* MoveDescriptors();  // double-float move descriptors on the device (sweep.cu)
     bool PermutingSpecies(uint32_t s) const;
@@ -305,5 +307,10 @@ class Context {
     void CheckDeviceError();
     void Sync();
 };
+
+/// The same move schedule (pimc_sweep) on many independent chains, one context each, on one
+/// device: schedules that run on the permutation kernel go to one launch with one CTA per chain;
+/// others run chain after chain.
+void SweepChains(const std::vector<Context*>& cs, const uint32_t* mv, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep);
 
 }  // namespace pimc

@@ -257,9 +257,8 @@ __device__ void CycleWeightsDD(const PermArgsDD& a, uint32_t N, const float2* tt
     }
 }
 
-__global__ void __launch_bounds__(kPermThreads, 1) PermBisectKernelDD(const __grid_constant__ PermArgsDD a) {
-    extern __shared__ __align__(16) unsigned char dyn[];
-    __shared__ PermSharedDD sh;
+/// The attempts attempt0 .. attempt0 + n_attempts - 1 of one move of one chain, by the whole CTA.
+__device__ void PermRun(const PermArgsDD& a, uint64_t attempt0, uint32_t n_attempts, unsigned char* dyn, PermSharedDD& sh) {
     const MoveDD& mv = *a.mv;
     const uint32_t sp = mv.species, N = a.sp_n[sp], G0 = a.sp_off[sp], M = a.M, nd = a.n_d, np = a.n_pad, K = a.K;
     const uint32_t B = 1u << mv.n_level;
@@ -297,8 +296,8 @@ __global__ void __launch_bounds__(kPermThreads, 1) PermBisectKernelDD(const __gr
     const uint32_t base_u = a.variant == kPermVariantBisect ? 1u + (B - 1u) : base_m + N * (B - 1u);
     __syncthreads();
 
-    for (uint32_t at = 0; at < a.n_attempts; ++at) {
-        const MoveStream st{a.seed, a.chain, a.move_index, a.attempt0 + at};
+    for (uint32_t at = 0; at < n_attempts; ++at) {
+        const MoveStream st{a.seed, a.chain, a.move_index, attempt0 + at};
         if (threadIdx.x == 0) {
             const Philox4 w0 = st.Block(0);
             sh.w0 = w0;
@@ -750,4 +749,26 @@ __global__ void __launch_bounds__(kPermThreads, 1) PermBisectKernelDD(const __gr
         __syncthreads();
     }
     if (threadIdx.x == 0 && sh.overflow) atomicCAS(a.err, 0, kDevErrNonFinite);
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kPermThreads, 1) PermBisectKernelDD(const __grid_constant__ PermArgsDD a) {
+    extern __shared__ __align__(16) unsigned char dyn[];
+    __shared__ PermSharedDD sh;
+    PermRun(a, a.attempt0, a.n_attempts, dyn, sh);
+}
+
+/// Many independent chains in one launch, one CTA per chain: chain c runs its schedule
+/// args[c n_entries + e] (e in order) n_rep times; repetition r of entry e starts at attempt
+/// args.attempt0 + r rep_stride[c n_entries + e].
+__global__ void __launch_bounds__(kPermThreads, 2) PermChainsKernelDD(const PermArgsDD* __restrict__ args, const uint64_t* __restrict__ rep_stride,
+                                                                     uint32_t n_entries, uint64_t n_rep) {
+    extern __shared__ __align__(16) unsigned char dyn[];
+    __shared__ PermSharedDD sh;
+    const size_t c = blockIdx.x;
+    for (uint64_t r = 0; r < n_rep; ++r)
+        for (uint32_t e = 0; e < n_entries; ++e) {
+            const PermArgsDD& a = args[c * n_entries + e];
+            PermRun(a, a.attempt0 + r * rep_stride[c * n_entries + e], a.n_attempts, dyn, sh);
+        }
 }

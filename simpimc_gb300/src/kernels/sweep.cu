@@ -1495,6 +1495,7 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
     bool all_perm = true;
     for (uint32_t e = 0; e < n_entries; ++e) all_perm &= on_perm_kernel(mv[e]);
     if (all_perm) {  // every entry on the permutation kernel: enqueue them all, wait once
+        PermPrepare(mv, n_entries);
         try {
             for (uint64_t r = 0; r < n_rep; ++r)
                 for (uint32_t e = 0; e < n_entries; ++e) PermEnqueue(mv[e], counts[e]);
@@ -1697,6 +1698,21 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
     last_grid_ = G;
 }
 
+// The dynamic shared memory limit of the permutation kernels: the device's opt-in maximum less
+// their static part, set once per device to the same value from every context and thread (a
+// per-launch value would race between host threads driving different contexts).
+static int PermSmemOptin(int device) {
+    int v = 0;
+    CudaCheck(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "shared memory limit");
+    cudaFuncAttributes fa, fb;
+    CudaCheck(cudaFuncGetAttributes(&fa, PermBisectKernelDD), "perm kernel attributes");
+    CudaCheck(cudaFuncGetAttributes(&fb, PermChainsKernelDD), "perm kernel attributes");
+    v -= (int)std::max(fa.sharedSizeBytes, fb.sharedSizeBytes);
+    CudaCheck(cudaFuncSetAttribute(PermBisectKernelDD, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "perm smem attribute");
+    CudaCheck(cudaFuncSetAttribute(PermChainsKernelDD, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "perm smem attribute");
+    return v;
+}
+
 // Attempts of a permuting move, or of the plain bisection of an exchanging species, on the
 // double-float permutation kernel (perm_dd.cuh): one CTA runs them in order, in launches of at
 // most 2048 attempts.
@@ -1708,12 +1724,37 @@ void Context::PermAttempts(uint32_t m, uint64_t n_att) {
 // Launches the attempts on the context's stream without waiting; the move's counters accumulate
 // on the device until PermFinish reads them.
 void Context::PermEnqueue(uint32_t m, uint64_t n_att) {
+    if (n_att == 0) return;
+    PermArgsDD a;
+    size_t smem = 0;
+    PermArgs(m, &a, &smem);
+    static int smem_optin[64] = {0};
+    int& optin = smem_optin[device & 63];
+    if (!optin) optin = PermSmemOptin(device);
+    if (smem > (size_t)optin) throw PimcError(kErrUnsupported, "permutation kernel shared memory above the device limit");
+    for (uint64_t done = 0; done < n_att;) {
+        const uint32_t chunk = (uint32_t)std::min<uint64_t>(2048, n_att - done);
+        a.attempt0 = moves[m].attempts + done;
+        a.n_attempts = chunk;
+        PermBisectKernelDD<<<1, kPermThreads, smem, stream>>>(a);
+        CudaCheck(cudaGetLastError(), "permuting bisection launch");
+        done += chunk;
+    }
+    moves[m].attempts += n_att;
+    moves[m].block_attempt += n_att;
+    perm_pending_ |= 1u << m;
+    fp64_valid = false;
+}
+
+// The permutation kernel's arguments for move m (attempt0 / n_attempts left to the caller), with
+// its scratch sized, and the dynamic shared memory a launch needs.
+void Context::PermArgs(uint32_t m, void* out, size_t* smem_out) {
+    PermArgsDD& a = *static_cast<PermArgsDD*>(out);
     MoveHost& mh = moves[m];
     const uint32_t sp = mh.dev.species, N = sys.sp_n[sp], M = sys.M;
     if (N > kPermMaxPart) throw PimcError(kErrUnsupported, "exchanging species of at most 512 particles");
     if (precision == 32 && sys.sp_rho[sp] >= 0 && sys.K)
         throw PimcError(kErrUnsupported, "the permutation kernel keeps double-float densities: set precision 64");
-    if (n_att == 0) return;
     const uint32_t B = 1u << mh.dev.n_level;
     MoveDD* dmoves = static_cast<MoveDD*>(MoveDescriptors());
     EnsureDD();
@@ -1732,7 +1773,7 @@ void Context::PermEnqueue(uint32_t m, uint64_t n_att) {
         perm_cnt_.reset(new DeviceBuffer(kMaxMoves * cnt_stride * sizeof(unsigned long long)));
         CudaCheck(cudaMemsetAsync(perm_cnt_->ptr, 0, perm_cnt_->bytes, stream), "perm counters");
     }
-    PermArgsDD a{};
+    a = PermArgsDD{};
     a.n_d = sys.n_d;
     a.M = M;
     a.n_pad = sys.n_pad;
@@ -1782,33 +1823,78 @@ void Context::PermEnqueue(uint32_t m, uint64_t n_att) {
     a.err = ErrWord();
     const size_t stride = (size_t)std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
     const uint32_t cyc_shared = (mh.kind == 3 && n_cycles <= kPermCycleCache) ? (uint32_t)n_cycles : 0u;
-    const size_t smem = PermLayout(N, cyc_shared, mh.kind == 2 && N <= kPermTabShared, (uint32_t)stride).total;
-    // The limit is the device's opt-in maximum, the same value from every context and thread (a
-    // per-launch value would race between host threads driving different contexts).
+    *smem_out = PermLayout(N, cyc_shared, mh.kind == 2 && N <= kPermTabShared, (uint32_t)stride).total;
+}
+
+// Sizes the permutation kernel's scratch for every move of a schedule before any launch (a later
+// move's larger scratch must not replace buffers an earlier launch still uses).
+void Context::PermPrepare(const uint32_t* mv, uint32_t n_entries) {
+    for (uint32_t e = 0; e < n_entries; ++e) {
+        PermArgsDD a;
+        size_t smem;
+        PermArgs(mv[e], &a, &smem);
+    }
+}
+
+void SweepChains(const std::vector<Context*>& cs, const uint32_t* mv, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep) {
+    if (cs.empty() || n_entries == 0 || n_rep == 0) return;
+    bool all_perm = true;
+    for (Context* c : cs) {
+        if (c->device != cs[0]->device) throw PimcError(kErrArg, "chains on different devices");
+        if (c->moves.size() != cs[0]->moves.size()) throw PimcError(kErrArg, "chains with different move lists");
+        for (uint32_t e = 0; e < n_entries; ++e) {
+            if (mv[e] >= c->moves.size()) throw PimcError(kErrArg, "move index out of range");
+            const MoveHost& mh = c->moves[mv[e]];
+            all_perm &= mh.kind == 2 || mh.kind == 3 || (mh.kind == 0 && c->PermutingSpecies(mh.dev.species));
+            if (counts[e] > (1ull << 31)) throw PimcError(kErrArg, "more than 2^31 attempts in one schedule entry");
+        }
+    }
+    if (!all_perm) {  // chains whose schedules use other kernels: one after another
+        for (Context* c : cs) c->Sweep(mv, counts, n_entries, n_rep);
+        return;
+    }
+    const size_t nc = cs.size();
+    std::vector<PermArgsDD> args(nc * n_entries);
+    std::vector<uint64_t> stride(nc * n_entries);
+    size_t smem = 0;
+    for (size_t ci = 0; ci < nc; ++ci) {
+        Context& c = *cs[ci];
+        c.PermFinish();
+        c.PermPrepare(mv, n_entries);
+        std::vector<uint64_t> per_rep(c.moves.size(), 0), before(c.moves.size(), 0);
+        for (uint32_t e = 0; e < n_entries; ++e) per_rep[mv[e]] += counts[e];
+        for (uint32_t e = 0; e < n_entries; ++e) {
+            size_t sm = 0;
+            PermArgsDD& a = args[ci * n_entries + e];
+            c.PermArgs(mv[e], &a, &sm);
+            smem = std::max(smem, sm);
+            a.attempt0 = c.moves[mv[e]].attempts + before[mv[e]];
+            a.n_attempts = (uint32_t)counts[e];
+            before[mv[e]] += counts[e];
+            stride[ci * n_entries + e] = per_rep[mv[e]];
+        }
+        for (uint32_t e = 0; e < n_entries; ++e) {
+            MoveHost& mh = c.moves[mv[e]];
+            mh.attempts += counts[e] * n_rep;
+            mh.block_attempt += counts[e] * n_rep;
+            c.perm_pending_ |= 1u << mv[e];
+        }
+        c.fp64_valid = false;
+        c.Sync();  // the double-float copies each context prepared on its own stream
+    }
+    Context& c0 = *cs[0];
     static int smem_optin[64] = {0};
-    int& optin = smem_optin[device & 63];
-    if (!optin) {
-        int v = 0;
-        CudaCheck(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "shared memory limit");
-        cudaFuncAttributes fa;
-        CudaCheck(cudaFuncGetAttributes(&fa, PermBisectKernelDD), "perm kernel attributes");
-        v -= (int)fa.sharedSizeBytes;  // the static part counts against the same limit
-        CudaCheck(cudaFuncSetAttribute(PermBisectKernelDD, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "perm smem attribute");
-        optin = v;
-    }
+    int& optin = smem_optin[c0.device & 63];
+    if (!optin) optin = PermSmemOptin(c0.device);
     if (smem > (size_t)optin) throw PimcError(kErrUnsupported, "permutation kernel shared memory above the device limit");
-    for (uint64_t done = 0; done < n_att;) {
-        const uint32_t chunk = (uint32_t)std::min<uint64_t>(2048, n_att - done);
-        a.attempt0 = mh.attempts + done;
-        a.n_attempts = chunk;
-        PermBisectKernelDD<<<1, kPermThreads, smem, stream>>>(a);
-        CudaCheck(cudaGetLastError(), "permuting bisection launch");
-        done += chunk;
-    }
-    mh.attempts += n_att;
-    mh.block_attempt += n_att;
-    perm_pending_ |= 1u << m;
-    fp64_valid = false;
+    DeviceBuffer dargs(args.size() * sizeof(PermArgsDD) + stride.size() * sizeof(uint64_t));
+    CudaCheck(cudaMemcpyAsync(dargs.ptr, args.data(), args.size() * sizeof(PermArgsDD), cudaMemcpyHostToDevice, c0.stream), "chain arguments");
+    uint64_t* dstride = reinterpret_cast<uint64_t*>(dargs.as<char>() + args.size() * sizeof(PermArgsDD));
+    CudaCheck(cudaMemcpyAsync(dstride, stride.data(), stride.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, c0.stream), "chain arguments");
+    PermChainsKernelDD<<<(unsigned)nc, kPermThreads, smem, c0.stream>>>(dargs.as<PermArgsDD>(), dstride, n_entries, n_rep);
+    CudaCheck(cudaGetLastError(), "chains launch");
+    c0.Sync();
+    for (Context* c : cs) c->PermFinish();
 }
 
 // Waits for the enqueued permutation launches, folds their device counters into the moves'

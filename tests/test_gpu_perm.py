@@ -12,7 +12,7 @@ import math
 import numpy as np
 import pytest
 
-from simpimc_gb300 import PimcError, Simulation
+from simpimc_gb300 import PimcError, Simulation, sweep_chains
 from simpimc_gb300.configs import electron_gas, trapped_bosons, trapped_coulomb
 from simpimc_gb300.tables import read_table
 
@@ -199,3 +199,41 @@ def test_perm_off_diagonal_pair_actions(tmp_path, gpu_lib, oracle_mod, pair):
         assert close(g.dactiondbeta(a), c.dactiondbeta(a), 1e-9), a
     g.close()
     c.close()
+
+
+def test_sweep_chains_matches_chain_by_chain(tmp_path, gpu_lib, oracle_mod):
+    """Many chains in one launch (one CTA per chain) give each chain the results of its own sweep
+    calls, bit for bit; one of them replays the oracle."""
+    n, sweeps = 6, 5
+    together, apart, paths, xmls = [], [], [], []
+    for c in range(5):
+        d = tmp_path / f"chain{c}"
+        xml, path = trapped_bosons(d, n_part=n, beta=4.0, n_bead=16, n_level=2, seed=40 + c)
+        xmls.append((xml, d))
+        paths.append(path * 0.4)
+        for lst in (together, apart):
+            s = Simulation(xml, base_dir=d, chain=c)
+            s.set_path(paths[-1])
+            lst.append(s)
+    sweep_chains(together, [0, 1], [n, n], sweeps)
+    for s in apart:
+        s.sweep([0, 1], [n, n], sweeps)
+    for a, b in zip(together, apart):
+        for m in range(2):
+            assert a.move_stats(m) == b.move_stats(m)
+        np.testing.assert_array_equal(a.get_path(0), b.get_path(0))
+        np.testing.assert_array_equal(a.get_perm(0), b.get_perm(0))
+        ga, _ = a.perm_stats(1, n)
+        gb, _ = b.perm_stats(1, n)
+        np.testing.assert_array_equal(ga, gb)
+    xml, d = xmls[3]
+    c = oracle_mod.OracleSim(xml, base_dir=d, chain=3)
+    c.set_path(paths[3])
+    for _ in range(sweeps):
+        c.move_attempts(0, n)
+        c.move_attempts(1, n)
+    assert together[3].move_stats(1) == c.move_stats(1)
+    assert np.max(np.abs(together[3].get_path(1) - c.get_path(1))) < 1e-9
+    c.close()
+    for s in together + apart:
+        s.close()
