@@ -4,6 +4,7 @@
     python -m simpimc_gb300.profile_cases egas     # 66-electron gas: 1 + 1 sweep launches (528 attempts each)
     python -m simpimc_gb300.profile_cases large32  # 1024-electron gas, FP32 mode: 1 + 1 launches of 64 attempts
     python -m simpimc_gb300.profile_cases bosons   # 32 trapped bosons: Bisect and PermBisectIterative, 1 + 1 sweeps
+    python -m simpimc_gb300.profile_cases chains   # 304 such chains: 1 + 1 launches of one sweep each (pimc_sweep_chains)
 
 The first two hold well under 100 MB on the device, the third about 1.3 GB; a capture of the
 second launch (`-k regex:<Kernel> -s 1 -c 1`) ends in seconds (the large case with one or two
@@ -70,10 +71,27 @@ def bosons_case(d):
     print(f"bosons ok: {s.move_counters(0)[0] + s.move_counters(1)[0]} attempts")
 
 
+def chains_case(d):
+    import os
+
+    from . import Simulation, sweep_chains
+    from .configs import trapped_bosons
+    sims = []
+    for c in range(304):
+        dc = os.path.join(d, f"c{c}")
+        xml, path = trapped_bosons(dc, n_part=32, beta=4.0, n_bead=32, n_level=3, seed=77 + c)
+        s = Simulation(xml, base_dir=dc, chain=c)
+        s.set_path(path * 0.4)
+        sims.append(s)
+    sweep_chains(sims, [0, 1], [32, 32], 1)
+    sweep_chains(sims, [0, 1], [32, 32], 1)
+    print(f"chains ok: {sum(s.move_counters(0)[0] + s.move_counters(1)[0] for s in sims)} attempts")
+
+
 def main(argv):
     case = argv[1] if len(argv) > 1 else "batch"
     with tempfile.TemporaryDirectory() as d:
-        {"batch": batch_case, "egas": egas_case, "large32": large32_case, "bosons": bosons_case}[case](d)
+        {"batch": batch_case, "egas": egas_case, "large32": large32_case, "bosons": bosons_case, "chains": chains_case}[case](d)
 
 
 if __name__ == "__main__":
