@@ -406,7 +406,7 @@ def exchange_bosons(local, tmp, sweeps=20, cpu_seconds=6.0):
                     "the sweep calls, host gaps between the per-move launches included"}
 
 
-def exchange_bosons_chains(local, tmp, n_chains=304, sweeps=10):
+def exchange_bosons_chains(local, tmp, n_chains=608, sweeps=10):
     """The exchanging-boson chain of exchange_bosons, n_chains independent copies (seeds 77 + c),
     one context per chain, all swept by pimc_sweep_chains: one launch with one CTA per chain.
     Wall-clock time of the call, device synchronised on both sides."""

@@ -34,11 +34,12 @@
 // move, attempt) streams. No wait spins; every loop is bounded.
 
 constexpr int kPermThreads = 256;
+constexpr int kPermChainThreads = 128;  // many-chain launches: smaller CTAs, four per SM
 constexpr uint32_t kPermMaxPart = 512;      // particles of an exchanging species
 constexpr uint32_t kPermCycleCache = 4096;  // table cycles whose weights stay in shared memory
 constexpr uint32_t kPermTabShared = 64;     // the walk's weight tables stay in shared memory up to N = 64
-constexpr uint32_t kPermSegCap = 1024;      // path beads (n (B + 1)) kept in shared memory
-constexpr uint32_t kPermZCap = 1024;        // midpoints (n (B - 1)) whose normals are drawn up front
+constexpr uint32_t kPermSegCap = 512;       // path beads (n (B + 1)) kept in shared memory
+constexpr uint32_t kPermZCap = 512;         // midpoints (n (B - 1)) whose normals are drawn up front
 constexpr int kPermVariantBisect = 0, kPermVariantIterative = 1, kPermVariantTable = 2;
 
 /// Byte offsets of the kernel's dynamic shared memory: per-particle index arrays [11 N] uint32,
@@ -114,7 +115,7 @@ struct PermSharedDD {
     Philox4 w0;
     dd prev0, tot0, total;
     float lu[kMaxLevels];
-    dd red[3 * (kPermThreads / 32)];
+    dd red[2][3 * (kPermThreads / 32)];
     dd inv_fact[15];
 };
 
@@ -134,6 +135,7 @@ __device__ __forceinline__ dd LoadPos(const float2* pos, uint32_t np, uint32_t b
 }
 
 /// Three block-wide df64 sums: warp trees, then every thread adds the warp partials in warp order.
+/// Callers alternate two red buffers between consecutive calls, so one barrier per call suffices.
 __device__ __forceinline__ void BlockSum3DD(dd& a0, dd& a1, dd& a2, dd* red) {
     WarpSum2DD(a0, a1);
     a2 = WarpSumDD(a2);
@@ -153,7 +155,6 @@ __device__ __forceinline__ void BlockSum3DD(dd& a0, dd& a1, dd& a2, dd* red) {
     a0 = t0;
     a1 = t1;
     a2 = t2;
-    __syncthreads();
 }
 
 /// Free-particle log density of a displacement: -|dr|^2 i4 - images (free_spline_class.h:189-197).
@@ -294,6 +295,7 @@ __device__ void PermRun(const PermArgsDD& a, uint64_t attempt0, uint32_t n_attem
     }
     const uint32_t base_m = a.variant == kPermVariantBisect ? 1u : 1u + N;
     const uint32_t base_u = a.variant == kPermVariantBisect ? 1u + (B - 1u) : base_m + N * (B - 1u);
+    uint32_t red_flip = 0;
     __syncthreads();
 
     for (uint32_t at = 0; at < n_attempts; ++at) {
@@ -446,35 +448,35 @@ __device__ void PermRun(const PermArgsDD& a, uint64_t attempt0, uint32_t n_attem
             __syncthreads();
             continue;
         }
-        // ---- the cycle's paths, their end beads and the actions' particle list ----
+        // ---- the cycle's paths, their end beads, the actions' particle list and the staged beads,
+        // all formed from part, sigma and the committed permutation in one phase ----
+        auto lo_of = [&](uint32_t m) -> uint32_t { return G0 + part[m]; };
+        auto hi_of = [&](uint32_t m) -> uint32_t { return a.perm[G0 + part[m]]; };
+        auto eold_of = [&](uint32_t m) -> uint32_t { return B < tcross ? lo_of(m) : hi_of(m); };
         for (uint32_t m = threadIdx.x; m < n; m += blockDim.x) {
-            const uint32_t g = G0 + part[m];
-            lab_lo[m] = g;
-            lab_hi[m] = a.perm[g];
-            end_old[m] = B < tcross ? g : a.perm[g];
+            lab_lo[m] = lo_of(m);
+            lab_hi[m] = hi_of(m);
+            end_old[m] = eold_of(m);
+            end_new[m] = eold_of(sigma[m]);
             lo_idx[part[m]] = (int)m;
-            hi_idx[a.perm[g] - G0] = (int)m;
+            hi_idx[hi_of(m) - G0] = (int)m;
         }
-        __syncthreads();
-        for (uint32_t m = threadIdx.x; m < n; m += blockDim.x) end_new[m] = end_old[sigma[m]];
         if (threadIdx.x == 0) {
             // the cycle, and the particles owning the end beads when the segment reaches past the
             // closure (perm_bisect_iterative_class.h:141-146, bisect_class.h:61-64)
             uint32_t nl = 0;
             for (uint32_t m = 0; m < n; ++m) {
-                lpos[lab_lo[m] - G0] = (int)nl;
-                lst[nl++] = lab_lo[m];
+                lpos[lo_of(m) - G0] = (int)nl;
+                lst[nl++] = lo_of(m);
             }
             if (B >= tcross)
                 for (uint32_t m = 0; m < n; ++m)
-                    if (lpos[end_old[m] - G0] < 0) {
-                        lpos[end_old[m] - G0] = (int)nl;
-                        lst[nl++] = end_old[m];
+                    if (lpos[eold_of(m) - G0] < 0) {
+                        lpos[eold_of(m) - G0] = (int)nl;
+                        lst[nl++] = eold_of(m);
                     }
             sh.nlist = nl;
         }
-        __syncthreads();
-        const uint32_t nlist = sh.nlist;
         auto label = [&](uint32_t m, uint32_t t) -> uint32_t { return t < tcross ? lab_lo[m] : lab_hi[m]; };
         auto slice = [&](uint32_t t) -> uint32_t { return (bead0 + t) % M; };
         // old and new beads of the paths, offsets 0..B (the old end, the new end)
@@ -485,10 +487,11 @@ __device__ void PermRun(const PermArgsDD& a, uint64_t attempt0, uint32_t n_attem
         auto SN = [&](uint32_t m, uint32_t t, uint32_t d) -> float2* { return &sn[((size_t)m * (B + 1u) + t) * 3 + d]; };
         for (uint32_t it = threadIdx.x; it < n * (B + 1u) * nd; it += blockDim.x) {
             const uint32_t d = it % nd, rest = it / nd, m = rest / (B + 1u), t = rest % (B + 1u);
-            const float2 v = t == B ? a.pos[((size_t)es * 3 + d) * np + end_old[m]] : a.pos[((size_t)slice(t) * 3 + d) * np + label(m, t)];
+            const uint32_t g = t == B ? eold_of(m) : (t < tcross ? lo_of(m) : hi_of(m));
+            const float2 v = a.pos[((size_t)slice(t) * 3 + d) * np + g];
             *SO(m, t, d) = v;
             if (t == 0) *SN(m, 0, d) = v;
-            if (t == B) *SN(m, B, d) = a.pos[((size_t)es * 3 + d) * np + end_new[m]];
+            if (t == B) *SN(m, B, d) = a.pos[((size_t)es * 3 + d) * np + eold_of(sigma[m])];
         }
         // the normals of every midpoint, drawn up front in the order of the reference's loop
         const bool z_up = n * (B - 1u) <= kPermZCap;
@@ -510,6 +513,7 @@ __device__ void PermRun(const PermArgsDD& a, uint64_t attempt0, uint32_t n_attem
             return LoadPos(a.pos, np, b, d, g);
         };
         __syncthreads();
+        const uint32_t nlist = sh.nlist;
 
         bool accepted = true;
         dd prev = sh.prev0;
@@ -656,21 +660,18 @@ __device__ void PermRun(const PermArgsDD& a, uint64_t attempt0, uint32_t n_attem
                     dS = Add(dS, MulF(Mul(a.tau, part_lr), f));
                 }
             }
-            // decision (bisect_class.h:103-118)
-            BlockSum3DD(old_lsp, new_lsp, dS, sh.red);
-            if (threadIdx.x == 0) {
-                const dd la = Add(Sub(Sub(old_lsp, new_lsp), dS), prev);
-                int ok = !Less(la, DD(sh.lu[mv.n_level - 1u - (uint32_t)level]));
-                if (!isfinite(la.hi)) {
-                    atomicCAS(a.err, 0, kDevErrNonFinite);
-                    ok = 0;
-                }
-                if (ok && level == 0) atomicAdd(&a.counters[1], 1ull);
-                sh.decide = ok;
+            // decision (bisect_class.h:103-118), formed by every thread from the same block sums
+            BlockSum3DD(old_lsp, new_lsp, dS, sh.red[red_flip]);
+            red_flip ^= 1u;
+            const dd la = Add(Sub(Sub(old_lsp, new_lsp), dS), prev);
+            bool ok = !Less(la, DD(sh.lu[mv.n_level - 1u - (uint32_t)level]));
+            if (!isfinite(la.hi)) {
+                if (threadIdx.x == 0) atomicCAS(a.err, 0, kDevErrNonFinite);
+                ok = false;
             }
-            __syncthreads();
+            if (ok && level == 0 && threadIdx.x == 0) atomicAdd(&a.counters[1], 1ull);
             prev = dS;
-            if (!sh.decide) {
+            if (!ok) {
                 accepted = false;
                 break;
             }
@@ -758,10 +759,10 @@ __global__ void __launch_bounds__(kPermThreads, 1) PermBisectKernelDD(const __gr
     PermRun(a, a.attempt0, a.n_attempts, dyn, sh);
 }
 
-/// Many independent chains in one launch, one CTA per chain: chain c runs its schedule
+/// Many independent chains in one launch, one CTA of kPermChainThreads per chain: chain c runs its schedule
 /// args[c n_entries + e] (e in order) n_rep times; repetition r of entry e starts at attempt
 /// args.attempt0 + r rep_stride[c n_entries + e].
-__global__ void __launch_bounds__(kPermThreads, 2) PermChainsKernelDD(const PermArgsDD* __restrict__ args, const uint64_t* __restrict__ rep_stride,
+__global__ void __launch_bounds__(kPermChainThreads, 4) PermChainsKernelDD(const PermArgsDD* __restrict__ args, const uint64_t* __restrict__ rep_stride,
                                                                      uint32_t n_entries, uint64_t n_rep) {
     extern __shared__ __align__(16) unsigned char dyn[];
     __shared__ PermSharedDD sh;

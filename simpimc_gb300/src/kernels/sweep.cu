@@ -1891,7 +1891,7 @@ void SweepChains(const std::vector<Context*>& cs, const uint32_t* mv, const uint
     CudaCheck(cudaMemcpyAsync(dargs.ptr, args.data(), args.size() * sizeof(PermArgsDD), cudaMemcpyHostToDevice, c0.stream), "chain arguments");
     uint64_t* dstride = reinterpret_cast<uint64_t*>(dargs.as<char>() + args.size() * sizeof(PermArgsDD));
     CudaCheck(cudaMemcpyAsync(dstride, stride.data(), stride.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, c0.stream), "chain arguments");
-    PermChainsKernelDD<<<(unsigned)nc, kPermThreads, smem, c0.stream>>>(dargs.as<PermArgsDD>(), dstride, n_entries, n_rep);
+    PermChainsKernelDD<<<(unsigned)nc, kPermChainThreads, smem, c0.stream>>>(dargs.as<PermArgsDD>(), dstride, n_entries, n_rep);
     CudaCheck(cudaGetLastError(), "chains launch");
     c0.Sync();
     for (Context* c : cs) c->PermFinish();
