@@ -27,9 +27,11 @@
 // identity for the table variant). exp in double-float reduces the argument by ln 2 and sums the
 // Taylor series to the 14th power; a cycle's log weight is the sum of its exponents.
 //
-// One CTA of kPermThreads runs the attempts of one move in order; the weight table, cycle
-// weights, midpoints, links, beads and density changes are spread over the threads, the cycle
-// walk's sums and choices run in the reference's order on one lane, and block sums are formed in
+// One CTA runs the attempts of one move of one chain in order (PermBisectKernelDD, 256 threads;
+// PermChainsKernelDD runs one chain per CTA of 128 threads, four per SM); the weight table, cycle
+// weights, midpoints, links, beads and density changes are spread over the threads; the cycle
+// walk runs on one warp (row sums by a warp reduction, the choice by a warp scan, in double-float;
+// each decision compares the quantities the reference's loop compares); block sums are formed in
 // a fixed order. Random numbers follow the block layout of the oracle's PermBisect (seed, chain,
 // move, attempt) streams. No wait spins; every loop is bounded.
 
@@ -110,10 +112,10 @@ struct PermArgsDD {
 };
 
 struct PermSharedDD {
-    uint32_t n, bead0, p_first, nlist, p, cont;
+    uint32_t n, bead0, p_first, nlist;
     int decide, overflow;
     Philox4 w0;
-    dd prev0, tot0, total;
+    dd prev0, tot0;
     float lu[kMaxLevels];
     dd red[2][3 * (kPermThreads / 32)];
     dd inv_fact[15];
