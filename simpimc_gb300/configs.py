@@ -180,7 +180,7 @@ def sweep_schedule(sim_or_counts, n_bisect_beads: int, n_bead: int):
 
 def trapped_bosons(workdir, *, n_part=3, beta=2.0, n_bead=16, omega=1.0, n_level=2, seed=1234, coulomb=False,
                    perm="PermBisectIterative", n_perm_part=2, fermi=False, n_step_inner=100, n_step_outer=10,
-                   path_seed=None, perm_level=None):
+                   path_seed=None, perm_level=None, sector_max=0):
     """Identical particles with exchange: the permuting move's species carries the path
     permutation. Observables: Energy (thermal), Permutation (cycle histogram and sectors), Sign."""
     workdir = Path(workdir)
@@ -212,7 +212,7 @@ def trapped_bosons(workdir, *, n_part=3, beta=2.0, n_bead=16, omega=1.0, n_level
   </Moves>
   <Observables>
     <Observable name="Energy" type="Energy" />
-    <Observable name="Permutation" type="Permutation" species="b" />
+    <Observable name="Permutation" type="Permutation" species="b"{f' sector_max="{sector_max}"' if sector_max else ""} />
     <Observable name="Sign" type="Sign" />
   </Observables>
   <Algorithm>

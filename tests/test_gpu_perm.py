@@ -237,3 +237,18 @@ def test_sweep_chains_matches_chain_by_chain(tmp_path, gpu_lib, oracle_mod):
     c.close()
     for s in together + apart:
         s.close()
+
+
+@pytest.mark.parametrize("n,perm,k", [(80, "PermBisectIterative", 0), (20, "PermBisectTable", 3)])
+def test_perm_global_memory_tables(tmp_path, gpu_lib, oracle_mod, n, perm, k):
+    """Weight tables past 64 particles and cycle tables past 4096 cycles (20 choose 3 x 3! = 6840)
+    live in global memory instead of shared memory; the replay is unchanged."""
+    xml, path = trapped_bosons(tmp_path, n_part=n, beta=4.0, n_bead=16, n_level=2, perm=perm, n_perm_part=k, seed=8, sector_max=100)
+    path = path * 0.4
+    g = Simulation(xml, base_dir=tmp_path)
+    c = oracle_mod.OracleSim(xml, base_dir=tmp_path)
+    g.set_path(path)
+    c.set_path(path)
+    replay(g, c, n, [(1, 40), (0, 40), (1, 200)])
+    g.close()
+    c.close()
