@@ -252,3 +252,37 @@ def test_perm_global_memory_tables(tmp_path, gpu_lib, oracle_mod, n, perm, k):
     replay(g, c, n, [(1, 40), (0, 40), (1, 200)])
     g.close()
     c.close()
+
+
+def test_signed_pair_correlation_and_structure_factor(tmp_path, gpu_lib, oracle_mod):
+    """g(r) and S(k) accumulate with the sign cofactor of fermion species (pair_correlation_class.h:17,
+    structure_factor_class.h:17): one exchanging spin species of the electron gas, fermi="1"."""
+    xml, path = electron_gas(tmp_path, n_part=8, n_bead=16, n_level=2, rs=1.0, beta=4.0, k_cut_units=3.3, seed=6, structure_factor=True)
+    xml = xml.replace('<Species name="eU" n_part="4" lambda="0.5" fermi="0"', '<Species name="eU" n_part="4" lambda="0.5" fermi="1"')
+    xml = xml.replace('<Move name="BisectD"', '<Move name="PermU" type="PermBisectIterative" species="eU" n_level="2" />\n    <Move name="BisectD"')
+    xml = xml.replace('</Observables>', '  <Observable name="gr" type="PairCorrelation" species_a="eU" species_b="eU" r_min="0." n_r="40" />\n  </Observables>')
+    assert 'fermi="1"' in xml and "PermU" in xml
+    L = (4.0 * math.pi * 8 / 3.0) ** (1.0 / 3.0)
+    rng = np.random.default_rng(3)
+    path = rng.uniform(-L / 2, L / 2, size=(8, 1, 3)) + 0.2 * rng.standard_normal(path.shape)
+    path -= np.rint(path / L) * L
+    g = Simulation(xml, base_dir=tmp_path)
+    c = oracle_mod.OracleSim(xml, base_dir=tmp_path)
+    g.set_path(path)
+    c.set_path(path)
+    n_obs = g.n_observables
+    signs = []
+    for _ in range(40):
+        for sim in (g, c):
+            sim.move_attempts(1, 8)
+            sim.move_attempts(0, 4)
+            for o in range(n_obs):
+                sim.observable_accumulate(o)
+        pi = g.get_perm(0)
+        signs.append(pi.tolist())
+    assert any(sorted(p) == list(range(4)) and p != list(range(4)) for p in signs), "no exchange happened"
+    for o in range(n_obs):
+        gb, cb = g.observable_block(o), c.observable_block(o)
+        assert gb.shape == cb.shape and close(gb, cb, 1e-9), (o, gb[:8], cb[:8])
+    g.close()
+    c.close()
