@@ -4,7 +4,7 @@
     python -m simpimc_gb300.profile_cases egas     # 66-electron gas: 1 + 1 sweep launches (528 attempts each)
     python -m simpimc_gb300.profile_cases large32  # 1024-electron gas, FP32 mode: 1 + 1 launches of 64 attempts
     python -m simpimc_gb300.profile_cases bosons   # 32 trapped bosons: Bisect and PermBisectIterative, 1 + 1 sweeps
-    python -m simpimc_gb300.profile_cases chains   # 304 such chains: 1 + 1 launches of one sweep each (pimc_sweep_chains)
+    python -m simpimc_gb300.profile_cases chains   # 608 such chains: 1 + 1 launches of one sweep each (pimc_sweep_chains)
 
 The first two hold well under 100 MB on the device, the third about 1.3 GB; a capture of the
 second launch (`-k regex:<Kernel> -s 1 -c 1`) ends in seconds (the large case with one or two
@@ -77,7 +77,7 @@ def chains_case(d):
     from . import Simulation, sweep_chains
     from .configs import trapped_bosons
     sims = []
-    for c in range(304):
+    for c in range(608):
         dc = os.path.join(d, f"c{c}")
         xml, path = trapped_bosons(dc, n_part=32, beta=4.0, n_bead=32, n_level=3, seed=77 + c)
         s = Simulation(xml, base_dir=dc, chain=c)
