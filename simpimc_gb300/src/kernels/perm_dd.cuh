@@ -46,12 +46,24 @@ constexpr int kPermVariantBisect = 0, kPermVariantIterative = 1, kPermVariantTab
 
 /// Byte offsets of the kernel's dynamic shared memory: per-particle index arrays [11 N] uint32,
 /// the walk's rows [2 N] and the table slices [6 N] float2, the cycle weights, the walk's weight
-/// tables [2 N^2] float2, the old and new path beads [2 x 3 kPermSegCap] float2, the normals
-/// [3 kPermZCap] float and the phase rows [6 stride] ddc.
+/// tables [2 N^2] float2, the old and new path beads [2 x 3 seg_cap] float2, the normals
+/// [3 z_cap] float and the phase rows [6 stride] ddc.
 struct PermSmem {
     size_t row, slices, cyc, tab, seg_old, seg_new, z, ph, total;
 };
-__host__ __device__ inline PermSmem PermLayout(uint32_t N, uint32_t cyc_shared, bool tab_shared, uint32_t stride) {
+/// Path beads and midpoints a move can stage: its longest cycle (1 for the bisection, the table's
+/// particle count, N for the walk) times B + 1 and B - 1, capped.
+__host__ __device__ inline uint32_t PermSegCap(int variant, uint32_t N, uint32_t k_part, uint32_t B) {
+    const uint32_t n_max = variant == kPermVariantBisect ? 1u : (variant == kPermVariantTable ? k_part : N);
+    return n_max * (B + 1u) < kPermSegCap ? n_max * (B + 1u) : kPermSegCap;
+}
+__host__ __device__ inline uint32_t PermZCap(int variant, uint32_t N, uint32_t k_part, uint32_t B) {
+    const uint32_t n_max = variant == kPermVariantBisect ? 1u : (variant == kPermVariantTable ? k_part : N);
+    return n_max * (B - 1u) < kPermZCap ? n_max * (B - 1u) : kPermZCap;
+}
+
+__host__ __device__ inline PermSmem PermLayout(uint32_t N, uint32_t cyc_shared, bool tab_shared, uint32_t stride, uint32_t seg_cap,
+                                               uint32_t z_cap) {
     PermSmem o;
     size_t at = (size_t)N * 11 * 4;
     at = (at + 15) & ~(size_t)15;
@@ -64,11 +76,11 @@ __host__ __device__ inline PermSmem PermLayout(uint32_t N, uint32_t cyc_shared, 
     o.tab = at;
     at += tab_shared ? (size_t)2 * N * N * 8 : 0;
     o.seg_old = at;
-    at += (size_t)3 * kPermSegCap * 8;
+    at += (size_t)3 * seg_cap * 8;
     o.seg_new = at;
-    at += (size_t)3 * kPermSegCap * 8;
+    at += (size_t)3 * seg_cap * 8;
     o.z = at;
-    at += (size_t)3 * kPermZCap * 4;
+    at += (size_t)3 * z_cap * 4;
     at = (at + 15) & ~(size_t)15;
     o.ph = at;
     at += (size_t)6 * stride * sizeof(ddc);
@@ -261,8 +273,26 @@ __device__ void CycleWeightsDD(const PermArgsDD& a, uint32_t N, const float2* tt
 }
 
 /// The attempts attempt0 .. attempt0 + n_attempts - 1 of one move of one chain, by the whole CTA.
-__device__ void PermRun(const PermArgsDD& a, uint64_t attempt0, uint32_t n_attempts, unsigned char* dyn, PermSharedDD& sh) {
-    const MoveDD& mv = *a.mv;
+/// Word copy of a descriptor into shared memory by the whole CTA (the caller synchronises).
+__device__ __forceinline__ void CopyToShared(void* dst, const void* src, size_t bytes) {
+    uint32_t* d = static_cast<uint32_t*>(dst);
+    const uint32_t* s = static_cast<const uint32_t*>(src);
+    for (size_t i = threadIdx.x; i < bytes / 4; i += blockDim.x) d[i] = s[i];
+}
+
+__device__ void PermRun(const PermArgsDD& a_in, uint64_t attempt0, uint32_t n_attempts, unsigned char* dyn, PermSharedDD& sh) {
+    // The arguments, the move descriptor and its pair descriptors in shared memory: the phases of an
+    // attempt read them on their dependent chains.
+    __shared__ PermArgsDD s_args;
+    __shared__ MoveDD s_mv;
+    __shared__ PairDD s_pairs[kMaxPair];
+    __syncthreads();  // the previous entry of a many-chain schedule is done with them
+    CopyToShared(&s_args, &a_in, sizeof(PermArgsDD));
+    CopyToShared(&s_mv, a_in.mv, sizeof(MoveDD));
+    __syncthreads();
+    for (int i = 0; i < s_mv.n_pair; ++i) CopyToShared(&s_pairs[i], a_in.pairs + s_mv.pair[i], sizeof(PairDD));
+    const PermArgsDD& a = s_args;
+    const MoveDD& mv = s_mv;
     const uint32_t sp = mv.species, N = a.sp_n[sp], G0 = a.sp_off[sp], M = a.M, nd = a.n_d, np = a.n_pad, K = a.K;
     const uint32_t B = 1u << mv.n_level;
     const int slot = a.sp_rho[sp];
@@ -270,7 +300,8 @@ __device__ void PermRun(const PermArgsDD& a, uint64_t attempt0, uint32_t n_attem
     const uint32_t n_cycles = a.n_comb * a.n_types;
     const bool cw_shared = a.variant == kPermVariantTable && n_cycles <= kPermCycleCache;
     const bool tab_shared = a.variant == kPermVariantIterative && N <= kPermTabShared;
-    const PermSmem L = PermLayout(N, cw_shared ? n_cycles : 0u, tab_shared, stride);
+    const uint32_t seg_cap = PermSegCap(a.variant, N, a.k_part, B), z_cap = PermZCap(a.variant, N, a.k_part, B);
+    const PermSmem L = PermLayout(N, cw_shared ? n_cycles : 0u, tab_shared, stride, seg_cap, z_cap);
     int* lo_idx = reinterpret_cast<int*>(dyn);  // path of a start label
     int* hi_idx = lo_idx + N;                   // path of a label past the closure
     int* lpos = hi_idx + N;                     // place in the particle list
@@ -482,7 +513,7 @@ __device__ void PermRun(const PermArgsDD& a, uint64_t attempt0, uint32_t n_attem
         auto label = [&](uint32_t m, uint32_t t) -> uint32_t { return t < tcross ? lab_lo[m] : lab_hi[m]; };
         auto slice = [&](uint32_t t) -> uint32_t { return (bead0 + t) % M; };
         // old and new beads of the paths, offsets 0..B (the old end, the new end)
-        const bool seg_shared = n * (B + 1u) <= kPermSegCap;
+        const bool seg_shared = n * (B + 1u) <= seg_cap;
         float2* so = seg_shared ? reinterpret_cast<float2*>(dyn + L.seg_old) : a.seg_old_g;
         float2* sn = seg_shared ? reinterpret_cast<float2*>(dyn + L.seg_new) : a.prop;
         auto SO = [&](uint32_t m, uint32_t t, uint32_t d) -> float2* { return &so[((size_t)m * (B + 1u) + t) * 3 + d]; };
@@ -496,7 +527,7 @@ __device__ void PermRun(const PermArgsDD& a, uint64_t attempt0, uint32_t n_attem
             if (t == B) *SN(m, B, d) = a.pos[((size_t)es * 3 + d) * np + eold_of(sigma[m])];
         }
         // the normals of every midpoint, drawn up front in the order of the reference's loop
-        const bool z_up = n * (B - 1u) <= kPermZCap;
+        const bool z_up = n * (B - 1u) <= z_cap;
         if (z_up)
             for (uint32_t c = threadIdx.x; c < n * (B - 1u); c += blockDim.x) {
                 float z[3];
@@ -581,7 +612,7 @@ __device__ void PermRun(const PermArgsDD& a, uint64_t attempt0, uint32_t n_attem
             }
             // pair links over the particle list, label by label (pair_action_class.h:267-302)
             for (int pi = 0; pi < mv.n_pair; ++pi) {
-                const PairDD& pa = a.pairs[mv.pair[pi]];
+                const PairDD& pa = s_pairs[pi];
                 if (level > pa.max_level || pa.is_constant) continue;
                 if (pa.kind == kPairBare && level != 0) continue;  // level_tau = 0
                 const bool hom = pa.sa == pa.sb;
@@ -639,7 +670,7 @@ __device__ void PermRun(const PermArgsDD& a, uint64_t attempt0, uint32_t n_attem
                 // Ewald part: tau 2^level v_long_k (bare) or u_long_k (Ilkka, David) times the change of
                 // CMag2 over the level's slices (bare_pair_action_class.h:126-144)
                 for (int pi = 0; pi < mv.n_pair; ++pi) {
-                    const PairDD& pa = a.pairs[mv.pair[pi]];
+                    const PairDD& pa = s_pairs[pi];
                     if (level > pa.max_level || pa.is_constant || !pa.use_lr || !pa.vk) continue;
                     const bool hom = pa.sa == pa.sb;
                     const int oslot = hom ? slot : a.sp_rho[pa.sa == sp ? pa.sb : pa.sa];

@@ -1823,7 +1823,9 @@ void Context::PermArgs(uint32_t m, void* out, size_t* smem_out) {
     a.err = ErrWord();
     const size_t stride = (size_t)std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
     const uint32_t cyc_shared = (mh.kind == 3 && n_cycles <= kPermCycleCache) ? (uint32_t)n_cycles : 0u;
-    *smem_out = PermLayout(N, cyc_shared, mh.kind == 2 && N <= kPermTabShared, (uint32_t)stride).total;
+    *smem_out = PermLayout(N, cyc_shared, mh.kind == 2 && N <= kPermTabShared, (uint32_t)stride, PermSegCap(a.variant, N, a.k_part, B),
+                           PermZCap(a.variant, N, a.k_part, B))
+                    .total;
 }
 
 // Sizes the permutation kernel's scratch for every move of a schedule before any launch (a later
