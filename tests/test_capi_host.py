@@ -58,6 +58,21 @@ def test_malformed_input_is_an_error_code(lib):
     lib.pimc_set_sweep_wave.restype = C.c_int
     lib.pimc_set_sweep_wave.argtypes = [C.c_void_p, C.c_int]
     assert lib.pimc_set_sweep_wave(None, 9) == -1
+    # the many-chain sweep and the permutation calls check their pointers before any device work
+    lib.pimc_sweep_chains.restype = C.c_int
+    lib.pimc_sweep_chains.argtypes = [C.POINTER(C.c_void_p), C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint64]
+    assert lib.pimc_sweep_chains(None, 1, None, None, 0, 1) == -1
+    arr = (C.c_void_p * 2)(None, None)
+    assert lib.pimc_sweep_chains(arr, 0, None, None, 0, 1) == -1
+    assert lib.pimc_sweep_chains(arr, 2, None, None, 0, 1) == -1
+    for name in ("pimc_get_perm", "pimc_set_perm"):
+        fn = getattr(lib, name)
+        fn.restype = C.c_int
+        fn.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
+        assert fn(None, 0, None) == -1
+    lib.pimc_perm_stats.restype = C.c_int
+    lib.pimc_perm_stats.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_size_t]
+    assert lib.pimc_perm_stats(None, 0, None, 0) == -1
     assert lib.pimc_set_sweep_wave(None, -1) == -1
 
 

@@ -286,3 +286,18 @@ def test_signed_pair_correlation_and_structure_factor(tmp_path, gpu_lib, oracle_
         assert gb.shape == cb.shape and close(gb, cb, 1e-9), (o, gb[:8], cb[:8])
     g.close()
     c.close()
+
+
+def test_sweep_chains_rejects_mismatched_chains(tmp_path, gpu_lib):
+    xml_a, path_a = trapped_bosons(tmp_path / "a", n_part=4, beta=2.0, n_bead=8, n_level=2, seed=1)
+    xml_b, path_b = trapped_coulomb(tmp_path / "b", n_part=4, n_bead=8, n_level=2, seed=2)
+    a = Simulation(xml_a, base_dir=tmp_path / "a")
+    b = Simulation(xml_b, base_dir=tmp_path / "b")
+    a.set_path(path_a)
+    b.set_path(path_b)
+    with pytest.raises(PimcError):
+        sweep_chains([a, b], [0, 1], [4, 4], 1)  # b has one move
+    sweep_chains([b, b], [0], [4], 1)  # chains without exchanges run one after another
+    assert b.move_stats(0)[0] == 8
+    a.close()
+    b.close()
