@@ -129,7 +129,7 @@ struct PermSharedDD {
     Philox4 w0;
     dd prev0, tot0;
     float lu[kMaxLevels];
-    dd red[2][3 * (kPermThreads / 32)];
+    dd lvl[kMaxLevels][3][kPermThreads / 32];  // per level: old / new sampling log densities, action change; per warp
     dd inv_fact[15];
 };
 
@@ -146,29 +146,6 @@ __device__ __forceinline__ dd ExpDD(dd x, dd ln2, const dd* inv_fact) {
 
 __device__ __forceinline__ dd LoadPos(const float2* pos, uint32_t np, uint32_t b, uint32_t d, uint32_t g) {
     return LoadDD(&pos[((size_t)b * 3 + d) * np + g]);
-}
-
-/// Three block-wide df64 sums: warp trees, then every thread adds the warp partials in warp order.
-/// Callers alternate two red buffers between consecutive calls, so one barrier per call suffices.
-__device__ __forceinline__ void BlockSum3DD(dd& a0, dd& a1, dd& a2, dd* red) {
-    WarpSum2DD(a0, a1);
-    a2 = WarpSumDD(a2);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (lane == 0) {
-        red[warp] = a0;
-        red[nw + warp] = a1;
-        red[2 * nw + warp] = a2;
-    }
-    __syncthreads();
-    dd t0{0.f, 0.f}, t1{0.f, 0.f}, t2{0.f, 0.f};
-    for (int w = 0; w < nw; ++w) {
-        t0 = Add(t0, red[w]);
-        t1 = Add(t1, red[nw + w]);
-        t2 = Add(t2, red[2 * nw + w]);
-    }
-    a0 = t0;
-    a1 = t1;
-    a2 = t2;
 }
 
 /// Free-particle log density of a displacement: -|dr|^2 i4 - images (free_spline_class.h:189-197).
@@ -328,7 +305,6 @@ __device__ void PermRun(const PermArgsDD& a_in, uint64_t attempt0, uint32_t n_at
     }
     const uint32_t base_m = a.variant == kPermVariantBisect ? 1u : 1u + N;
     const uint32_t base_u = a.variant == kPermVariantBisect ? 1u + (B - 1u) : base_m + N * (B - 1u);
-    uint32_t red_flip = 0;
     __syncthreads();
 
     for (uint32_t at = 0; at < n_attempts; ++at) {
@@ -548,12 +524,16 @@ __device__ void PermRun(const PermArgsDD& a_in, uint64_t attempt0, uint32_t n_at
         __syncthreads();
         const uint32_t nlist = sh.nlist;
 
-        bool accepted = true;
-        dd prev = sh.prev0;
+        // Every level's terms are formed before the level tests run (the draws of an attempt are
+        // indexed per bead and per level, so the levels below a rejection change nothing): the
+        // midpoints top-down, one barrier per level; then the density changes of the inner beads;
+        // then every level's kinetic, trap, pair and Ewald terms in one pass, reduced per warp and
+        // level; then the tests of bisect_class.h:103-118 in order on one thread.
+        const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
         for (int level = (int)mv.n_level - 1; level >= 0; --level) {
-            const uint32_t skip = 1u << level, nmid = B >> (level + 1), ngrid = B / skip - 1u;
+            const uint32_t skip = 1u << level, nmid = B >> (level + 1);
             const uint32_t off = n * (nmid - 1u);
-            dd old_lsp{0.f, 0.f}, new_lsp{0.f, 0.f}, dS{0.f, 0.f};
+            dd old_lsp{0.f, 0.f}, new_lsp{0.f, 0.f};
             // midpoints (bisect_class.h:74-94 with the old end of each cycle path)
             for (uint32_t it = threadIdx.x; it < n * nmid; it += blockDim.x) {
                 const uint32_t m = it / nmid, q = it % nmid;
@@ -580,7 +560,35 @@ __device__ void PermRun(const PermArgsDD& a_in, uint64_t attempt0, uint32_t n_at
                 old_lsp = Add(old_lsp, LogRhoFreeDD(dl, nd, mv.i4s[level], &mv.sample_image[level], mv.has_images));
                 new_lsp = Add(new_lsp, LogRhoFreeDD(dn, nd, mv.i4s[level], &mv.sample_image[level], mv.has_images));
             }
+            WarpSum2DD(old_lsp, new_lsp);
+            if (lane == 0) {
+                sh.lvl[level][0][warp] = old_lsp;
+                sh.lvl[level][1][warp] = new_lsp;
+            }
             __syncthreads();
+        }
+        // density changes of the inner beads (species_class.h:406-425), from their final positions
+        if (slot >= 0 && K > 0) {
+            for (uint32_t t = 1; t < B; ++t)
+                for (uint32_t m = 0; m < n; ++m) {
+                    for (uint32_t it = threadIdx.x; it < 2u * nd * stride; it += blockDim.x) {
+                        const uint32_t nn = it % stride, rest = it / stride, d = rest % nd, which = rest / nd;
+                        const dd x = which ? LoadDD(SN(m, t, d)) : LoadDD(SO(m, t, d));
+                        ph[((size_t)which * 3 + d) * stride + nn] = PhaseDD(x, (int)nn, a.iL, a.two_pi, a.phase256);
+                    }
+                    __syncthreads();
+                    for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) {
+                        const int32_t pk = a.kidx[k];
+                        const ddc dv = CSub(PhaseProductDD(ph + 3 * stride, stride, nd, pk), PhaseProductDD(ph, stride, nd, pk));
+                        float4* cell = &a.drho[(size_t)t * K + k];
+                        *cell = Pack(m == 0 ? dv : CAdd(Unpack(*cell), dv));
+                    }
+                    __syncthreads();
+                }
+        }
+        for (int level = (int)mv.n_level - 1; level >= 0; --level) {
+            const uint32_t skip = 1u << level, ngrid = B / skip - 1u;
+            dd dS{0.f, 0.f};
             // kinetic links along the paths (kinetic_class.h:105-122)
             for (int ki = 0; ki < mv.n_kin; ++ki) {
                 const uint32_t nl = B / skip;
@@ -646,29 +654,9 @@ __device__ void PermRun(const PermArgsDD& a_in, uint64_t attempt0, uint32_t n_at
                     dS = Add(dS, Sub(PairUDD(pa, r, rp, ss, level, a.tau), uo));
                 }
             }
-            // density change of the moved beads at this level's slices (species_class.h:406-425)
-            if (slot >= 0 && K > 0) {
-                for (uint32_t j = 0; j < ngrid; ++j) {
-                    const uint32_t t = (j + 1u) * skip;
-                    for (uint32_t m = 0; m < n; ++m) {
-                        __syncthreads();
-                        for (uint32_t it = threadIdx.x; it < 2u * nd * stride; it += blockDim.x) {
-                            const uint32_t nn = it % stride, rest = it / stride, d = rest % nd, which = rest / nd;
-                            const dd x = which ? LoadDD(SN(m, t, d)) : LoadDD(SO(m, t, d));
-                            ph[((size_t)which * 3 + d) * stride + nn] = PhaseDD(x, (int)nn, a.iL, a.two_pi, a.phase256);
-                        }
-                        __syncthreads();
-                        for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) {
-                            const int32_t pk = a.kidx[k];
-                            const ddc dv = CSub(PhaseProductDD(ph + 3 * stride, stride, nd, pk), PhaseProductDD(ph, stride, nd, pk));
-                            float4* cell = &a.drho[(size_t)t * K + k];
-                            *cell = Pack(m == 0 ? dv : CAdd(Unpack(*cell), dv));
-                        }
-                    }
-                }
-                __syncthreads();
-                // Ewald part: tau 2^level v_long_k (bare) or u_long_k (Ilkka, David) times the change of
-                // CMag2 over the level's slices (bare_pair_action_class.h:126-144)
+            // Ewald part: tau 2^level v_long_k (bare) or u_long_k (Ilkka, David) times the change of
+            // CMag2 over the level's slices (bare_pair_action_class.h:126-144)
+            if (slot >= 0 && K > 0)
                 for (int pi = 0; pi < mv.n_pair; ++pi) {
                     const PairDD& pa = s_pairs[pi];
                     if (level > pa.max_level || pa.is_constant || !pa.use_lr || !pa.vk) continue;
@@ -692,23 +680,38 @@ __device__ void PermRun(const PermArgsDD& a_in, uint64_t attempt0, uint32_t n_at
                     const float f = (hom ? 1.f : 2.f) * (pa.kind == kPairBare ? (float)skip : 1.f);
                     dS = Add(dS, MulF(Mul(a.tau, part_lr), f));
                 }
-            }
-            // decision (bisect_class.h:103-118), formed by every thread from the same block sums
-            BlockSum3DD(old_lsp, new_lsp, dS, sh.red[red_flip]);
-            red_flip ^= 1u;
-            const dd la = Add(Sub(Sub(old_lsp, new_lsp), dS), prev);
-            bool ok = !Less(la, DD(sh.lu[mv.n_level - 1u - (uint32_t)level]));
-            if (!isfinite(la.hi)) {
-                if (threadIdx.x == 0) atomicCAS(a.err, 0, kDevErrNonFinite);
-                ok = false;
-            }
-            if (ok && level == 0 && threadIdx.x == 0) atomicAdd(&a.counters[1], 1ull);
-            prev = dS;
-            if (!ok) {
-                accepted = false;
-                break;
-            }
+            dS = WarpSumDD(dS);
+            if (lane == 0) sh.lvl[level][2][warp] = dS;
         }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            // lanes add the warp partials of one (level, term) each, in warp order; lane 0 then runs the tests
+            const uint32_t nw = blockDim.x >> 5;
+            for (uint32_t i = lane; i < 3u * mv.n_level; i += 32) {
+                dd t{0.f, 0.f};
+                for (uint32_t w = 0; w < nw; ++w) t = Add(t, sh.lvl[i / 3][i % 3][w]);
+                sh.lvl[i / 3][i % 3][0] = t;
+            }
+            __syncwarp();
+        }
+        if (threadIdx.x == 0) {
+            dd prev = sh.prev0;
+            int ok = 1;
+            for (int level = (int)mv.n_level - 1; level >= 0 && ok; --level) {
+                const dd so = sh.lvl[level][0][0], sn = sh.lvl[level][1][0], ds = sh.lvl[level][2][0];
+                if (level == 0) atomicAdd(&a.counters[1], 1ull);  // the attempt reached the level-0 test
+                const dd la = Add(Sub(Sub(so, sn), ds), prev);
+                ok = !Less(la, DD(sh.lu[mv.n_level - 1u - (uint32_t)level]));
+                if (!isfinite(la.hi)) {
+                    atomicCAS(a.err, 0, kDevErrNonFinite);
+                    ok = 0;
+                }
+                prev = ds;
+            }
+            sh.decide = ok;
+        }
+        __syncthreads();
+        bool accepted = sh.decide != 0;
         // final test of the table with the new end map (perm_bisect_table_class.h:216-225)
         if (accepted && a.variant == kPermVariantTable && n < N) {
             BuildTableDD(a, N, G0, B, tcross, true, lo_idx, end_new, sh.inv_fact, s0, sE, tt, nullptr, &sh.overflow);
