@@ -121,9 +121,11 @@ int pimc_move_stats(pimc_ctx* ctx, uint32_t move, uint64_t* out);
 int pimc_get_perm(pimc_ctx* ctx, uint32_t species, uint32_t* perm);
 int pimc_set_perm(pimc_ctx* ctx, uint32_t species, const uint32_t* perm);
 /* pimc_sweep on n_ctx independent chains (contexts of the same input structure on one device):
- * when every schedule entry runs on the permutation kernel, all chains go to one launch with one
- * CTA per chain (the reference runs one chain per MPI process, framework_class.h:44-53); otherwise
- * the chains run one after another. Errors are reported on ctxs[0]. */
+ * when every schedule entry is a Bisect or permuting move on a species of at most 512 particles
+ * (64-bit mode when the species keeps densities), all chains go to one launch of the permutation
+ * kernel with one CTA per chain, any action set included (the reference runs one chain per MPI
+ * process, framework_class.h:44-53); otherwise the chains run one after another. Errors are
+ * reported on ctxs[0]. */
 int pimc_sweep_chains(pimc_ctx** ctxs, uint32_t n_ctx, const uint32_t* moves, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep);
 /* Per cycle length 1..N of a permuting move: out[0..N) attempts, out[N..2N) accepts of the current
  * block (perm_bisect_class.h:25-26, 59-90); N = the move's species particle count. */

@@ -1841,13 +1841,20 @@ void Context::PermPrepare(const uint32_t* mv, uint32_t n_entries) {
 void SweepChains(const std::vector<Context*>& cs, const uint32_t* mv, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep) {
     if (cs.empty() || n_entries == 0 || n_rep == 0) return;
     bool all_perm = true;
+    for (size_t i = 0; i < cs.size(); ++i)
+        for (size_t j = 0; j < i; ++j)
+            if (cs[i] == cs[j]) throw PimcError(kErrArg, "a chain appears twice");
     for (Context* c : cs) {
         if (c->device != cs[0]->device) throw PimcError(kErrArg, "chains on different devices");
         if (c->moves.size() != cs[0]->moves.size()) throw PimcError(kErrArg, "chains with different move lists");
         for (uint32_t e = 0; e < n_entries; ++e) {
             if (mv[e] >= c->moves.size()) throw PimcError(kErrArg, "move index out of range");
             const MoveHost& mh = c->moves[mv[e]];
-            all_perm &= mh.kind == 2 || mh.kind == 3 || (mh.kind == 0 && c->PermutingSpecies(mh.dev.species));
+            // every bisection and permuting move fits the one-CTA kernel (its plain variant replays the
+            // sweep kernel's draws); HMC, species above kPermMaxPart and the FP32 density mode do not
+            const uint32_t sp = mh.dev.species;
+            all_perm &= (mh.kind == 0 || mh.kind == 2 || mh.kind == 3) && c->sys.sp_n[sp] <= kPermMaxPart &&
+                        !(c->precision == 32 && c->sys.sp_rho[sp] >= 0 && c->sys.K);
             if (counts[e] > (1ull << 31)) throw PimcError(kErrArg, "more than 2^31 attempts in one schedule entry");
         }
     }

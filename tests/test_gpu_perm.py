@@ -297,7 +297,40 @@ def test_sweep_chains_rejects_mismatched_chains(tmp_path, gpu_lib):
     b.set_path(path_b)
     with pytest.raises(PimcError):
         sweep_chains([a, b], [0, 1], [4, 4], 1)  # b has one move
-    sweep_chains([b, b], [0], [4], 1)  # chains without exchanges run one after another
+    with pytest.raises(PimcError):
+        sweep_chains([b, b], [0], [4], 1)  # one chain twice
+    sweep_chains([b], [0], [4], 2)
     assert b.move_stats(0)[0] == 8
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("pair", ["BarePairAction", "IlkkaPairAction"])
+def test_sweep_chains_plain_bisection_any_actions(tmp_path, gpu_lib, oracle_mod, pair):
+    """Chains without exchanges (the electron gas with its Ewald sums, bare or Ilkka pair action)
+    also run in one launch, on the permutation kernel's plain bisection; each chain replays the
+    oracle."""
+    sims, refs = [], []
+    for c in range(3):
+        d = tmp_path / f"egas{c}"
+        xml, path = electron_gas(d, n_part=14, n_bead=16, n_level=2, rs=2.0, k_cut_units=4.0, seed=9 + c, pair=pair)
+        L = ((4.0 * math.pi * 14 / 3.0) ** (1.0 / 3.0)) * 2.0
+        path = np.random.default_rng(50 + c).uniform(-L / 2, L / 2, size=path.shape)
+        g = Simulation(xml, base_dir=d, chain=c)
+        o = oracle_mod.OracleSim(xml, base_dir=d, chain=c)
+        g.set_path(path)
+        o.set_path(path)
+        sims.append(g)
+        refs.append(o)
+    sweep_chains(sims, [0, 1], [7, 7], 6)
+    for g, o in zip(sims, refs):
+        for _ in range(6):
+            o.move_attempts(0, 7)
+            o.move_attempts(1, 7)
+        for m in range(2):
+            assert g.move_stats(m) == o.move_stats(m), m
+        assert np.max(np.abs(g.get_path(1) - o.get_path(1))) < 1e-9
+        for s in range(2):
+            assert np.max(np.abs(g.rho_k(s) - o.rho_k(s))) < 1e-9
+        g.close()
+        o.close()
