@@ -1355,17 +1355,16 @@ struct IlkkaPairAction : PairAction {
 // src/actions/pair_action/david_pair_action_class.h:7-361. The squarer's expansion
 //   U = (u_00(r) + u_00(r'))/2 + sum_{k=1..n} sum_{j=0..k} u_kj(q) z^(2j) s^(2(k-j)),
 // q = (r + r')/2, z = r - r', on one radial grid; component 0 of every multi-spline is the potential.
-// Tables for the time step tau only (max_level 0, the setting of the reference's inputs).
+// One table per level up to max_level (n_tau = max_level + 1); level l reads table l (u_kj(level)).
 struct DavidPairAction : PairAction {
     uint32_t n_order = 0, n_val = 0;
     double r_min = 0., r_max = 0.;
     double du_long_k_0 = 0., du_long_r_0 = 0., v_long_k_0 = 0., v_long_r_0 = 0.;
     std::vector<double> u_long_k, du_long_k, v_long_k;
-    std::vector<Spline> u_kj, du_kj;  // n_val + 1 components
+    std::vector<std::vector<Spline>> u_kj, du_kj;  // [level][n_val + 1 components]
 
     DavidPairAction(Path& p, const Input& in, const std::string& base_dir) : PairAction(p, in) {
         n_order = in.GetAttribute<uint32_t>("n_order", 0);  // pair_action_class.h:208
-        if (max_level != 0) throw InputError("DavidPairAction: tables for one time step (max_level 0)");
         std::string file = in.GetAttribute<std::string>("file");
         if (!file.empty() && file[0] != '/' && !base_dir.empty()) file = base_dir + "/" + file;
         TableFile t = TableFile::Load(file);
@@ -1376,22 +1375,25 @@ struct DavidPairAction : PairAction {
             throw InputError("table '" + file + "': inconsistent grid");
         r_min = grid.front();
         r_max = grid.back();
-        const auto& taus = t.Vec(pre + "/taus");  // :234-246
+        const size_t n_tau = (size_t)max_level + 1;  // :234-246
+        const auto& taus = t.Vec(pre + "/taus");
+        if (taus.size() < n_tau) throw InputError("table '" + file + "': fewer taus than max_level + 1");
         bool found = false;
-        for (double x : taus) found |= std::fabs(x - p.tau) < 1.0e-6;
+        for (size_t i = 0; i < n_tau; ++i) found |= std::fabs(taus[i] - p.tau) < 1.0e-6;
         if (!found) throw InputError("table '" + file + "': tau of the path not found");
         const auto& V = t.Vec("potential/data");
         n_val = 1;
         for (uint32_t i = 1; i <= n_order; ++i) n_val += 1 + i;  // :252-255
-        auto load = [&](const std::string& key, std::vector<Spline>& out) {  // :257-316
-            const auto& d = t.Vec(key);
-            if (d.size() < (size_t)n_val * n_grid || V.size() != n_grid) throw InputError("table '" + file + "': short " + key);
-            out.assign(n_val + 1, Spline());
+        auto load = [&](const std::string& key, std::vector<std::vector<Spline>>& out) {  // :257-316
+            const auto& d = t.Vec(key);  // n_val x n_grid x n_tau, value index fastest
+            if (d.size() < (size_t)n_val * n_grid * n_tau || V.size() != n_grid) throw InputError("table '" + file + "': short " + key);
+            out.assign(n_tau, std::vector<Spline>(n_val + 1));
             std::vector<double> col(n_grid);
-            for (uint32_t v = 0; v <= n_val; ++v) {
-                for (size_t g = 0; g < n_grid; ++g) col[g] = v == 0 ? V[g] : d[(v - 1) + g * n_val];
-                out[v].Build(grid, col, false);
-            }
+            for (size_t l = 0; l < n_tau; ++l)
+                for (uint32_t v = 0; v <= n_val; ++v) {
+                    for (size_t g = 0; g < n_grid; ++g) col[g] = v == 0 ? V[g] : d[(v - 1) + g * n_val + l * n_val * n_grid];
+                    out[l][v].Build(grid, col, false);
+                }
         };
         load(pre + "/data", u_kj);
         load(dpre + "/data", du_kj);
@@ -1456,25 +1458,27 @@ struct DavidPairAction : PairAction {
         return tot;
     }
 
-    double CalcV(double r, double rp, uint32_t) override {  // :34-47
+    double CalcV(double r, double rp, uint32_t level) override {  // :34-47
         SetLimits(r_min, r_max, r, rp);
-        return 0.5 * (u_kj[0].Eval(r) + u_kj[0].Eval(rp));
+        return 0.5 * (u_kj[level][0].Eval(r) + u_kj[level][0].Eval(rp));
     }
     double CalcVLong() override { return KSum(v_long_k, 0, path.n_bead, 1) + v_long_k_0 + v_long_r_0; }  // :50-66
-    double CalcU(double r, double rp, double s, uint32_t) override {  // :69-102
+    double CalcU(double r, double rp, double s, uint32_t level) override {  // :69-102
         double q = 0.5 * (r + rp), z = r - rp;
         SetLimits(r_min, r_max, r, rp);
-        double u = 0.5 * (u_kj[1].Eval(r) + u_kj[1].Eval(rp));
-        if (s > 0.0 && q < r_max) u += OffDiagonal(u_kj, q, z, s);
+        const auto& t = u_kj[level];
+        double u = 0.5 * (t[1].Eval(r) + t[1].Eval(rp));
+        if (s > 0.0 && q < r_max) u += OffDiagonal(t, q, z, s);
         return u;
     }
     double CalcULong(uint32_t b0, uint32_t b1, uint32_t level) override { return KSum(u_long_k, b0, b1, 1u << level); }  // :105-123
-    double CalcdUdBeta(double r, double rp, double s, uint32_t) override {  // :126-167
+    double CalcdUdBeta(double r, double rp, double s, uint32_t level) override {  // :126-167
         double q = 0.5 * (r + rp), z = r - rp;
         SetLimits(r_min, r_max, r, rp);
-        double v = 0.5 * (du_kj[0].Eval(r) + du_kj[0].Eval(rp));
-        double du = 0.5 * (du_kj[1].Eval(r) + du_kj[1].Eval(rp)) + v;
-        if (s > 0.0 && q < r_max) du += OffDiagonal(du_kj, q, z, s);
+        const auto& t = du_kj[level];
+        double v = 0.5 * (t[0].Eval(r) + t[0].Eval(rp));
+        double du = 0.5 * (t[1].Eval(r) + t[1].Eval(rp)) + v;
+        if (s > 0.0 && q < r_max) du += OffDiagonal(t, q, z, s);
         return du;
     }
     double CalcdUdBetaLong() override { return KSum(du_long_k, 0, path.n_bead, 1) + du_long_k_0 + du_long_r_0; }  // :170-186

@@ -29,27 +29,27 @@ from .tables import coulomb_table, david_table, ilkka_table
 
 def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_level=3, seed=1234, coulomb=True,
                     n_step_inner=100, n_step_outer=10, gr_bins=200, gr_rmax=5.0, virial=False, path_seed=None,
-                    write_table=True, pair="BarePairAction", n_order=2):
+                    write_table=True, pair="BarePairAction", n_order=2, pair_max_level=0):
     workdir = Path(workdir)
     workdir.mkdir(parents=True, exist_ok=True)
     if pair == "DavidPairAction":
-        tab = workdir / f"david_open_{n_bead}_{beta}_{n_order}.pat"
+        tab = workdir / f"david_open_{n_bead}_{beta}_{n_order}_{pair_max_level}.pat"
         if write_table or not tab.exists():
-            david_table(tab, tau=beta / n_bead, n_order=n_order, lam=0.5, z_ab=1.0, L=0.0)
+            david_table(tab, tau=beta / n_bead, n_order=n_order, lam=0.5, z_ab=1.0, L=0.0, n_tau=pair_max_level + 1)
         pair_xml = (f'<Action name="Coulomb" type="DavidPairAction" file="{tab.name}" n_order="{n_order}" species_a="e" '
-                    f'species_b="e" max_level="0" use_long_range="0" />')
+                    f'species_b="e" max_level="{pair_max_level}" use_long_range="0" />')
     elif pair == "IlkkaPairAction":
         tab = workdir / f"ilkka_open_{n_bead}_{beta}.pat"
         if write_table or not tab.exists():
             ilkka_table(tab, tau=beta / n_bead, lam=0.5, z_ab=1.0, L=0.0)
         pair_xml = (f'<Action name="Coulomb" type="IlkkaPairAction" file="{tab.name}" species_a="e" species_b="e" '
-                    f'max_level="0" use_long_range="0" />')
+                    f'max_level="{pair_max_level}" use_long_range="0" />')
     else:
         tab = workdir / "coulomb_open.pat"
         if write_table or not tab.exists():
             coulomb_table(tab, z_ab=1.0, L=0.0)
         pair_xml = (f'<Action name="Coulomb" type="BarePairAction" file="{tab.name}" is_coulomb="1" species_a="e" '
-                    f'species_b="e" max_level="0" use_long_range="0" />')
+                    f'species_b="e" max_level="{pair_max_level}" use_long_range="0" />')
     pair = pair_xml if coulomb else ""
     energy = ('<Observable name="Energy" type="Energy" use_virial_estimator="1" />' if virial
               else '<Observable name="Energy" type="Energy" />')
@@ -91,14 +91,15 @@ def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_leve
 
 
 def electron_gas(workdir, *, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_units=12.0, n_level=4, seed=4321,
-                 n_step_inner=10, n_step_outer=4, path_seed=None, structure_factor=False, pair="BarePairAction", n_order=2):
+                 n_step_inner=10, n_step_outer=4, path_seed=None, structure_factor=False, pair="BarePairAction", n_order=2,
+                 pair_max_level=0):
     workdir = Path(workdir)
     workdir.mkdir(parents=True, exist_ok=True)
     L = (4.0 * math.pi * n_part / 3.0) ** (1.0 / 3.0) * rs
     k_cut = k_cut_units * 2.0 * math.pi / L
     if pair == "DavidPairAction":
         tab = workdir / f"david_ewald_{n_part}_{rs}_{n_bead}_{beta}_{n_order}.pat"
-        david_table(tab, tau=beta / n_bead, n_order=n_order, lam=0.5, z_ab=1.0, L=L, k_cut=k_cut)
+        david_table(tab, tau=beta / n_bead, n_order=n_order, lam=0.5, z_ab=1.0, L=L, k_cut=k_cut, n_tau=pair_max_level + 1)
         extra = f' n_order="{n_order}"'
     elif pair == "IlkkaPairAction":
         tab = workdir / f"ilkka_ewald_{n_part}_{rs}_{n_bead}_{beta}.pat"
@@ -124,9 +125,9 @@ def electron_gas(workdir, *, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_unit
   <Actions>
     <Action name="KineticU" type="Kinetic" n_images="0" species="eU" />
     <Action name="KineticD" type="Kinetic" n_images="0" species="eD" />
-    <Action name="CoulombUU" type="{pair}" file="{tab.name}"{extra} species_a="eU" species_b="eU" max_level="0" use_long_range="1" />
-    <Action name="CoulombDD" type="{pair}" file="{tab.name}"{extra} species_a="eD" species_b="eD" max_level="0" use_long_range="1" />
-    <Action name="CoulombUD" type="{pair}" file="{tab.name}"{extra} species_a="eU" species_b="eD" max_level="0" use_long_range="1" />
+    <Action name="CoulombUU" type="{pair}" file="{tab.name}"{extra} species_a="eU" species_b="eU" max_level="{pair_max_level}" use_long_range="1" />
+    <Action name="CoulombDD" type="{pair}" file="{tab.name}"{extra} species_a="eD" species_b="eD" max_level="{pair_max_level}" use_long_range="1" />
+    <Action name="CoulombUD" type="{pair}" file="{tab.name}"{extra} species_a="eU" species_b="eD" max_level="{pair_max_level}" use_long_range="1" />
   </Actions>
   <Moves>
     <Move name="BisectU" type="Bisect" species="eU" n_level="{n_level}" />

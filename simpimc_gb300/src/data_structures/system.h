@@ -137,8 +137,10 @@ struct PairDev {
     const double* u_long_k = nullptr;          // [K] (also DavidPairAction)
     const double* du_long_k = nullptr;         // [K] (also DavidPairAction)
     // DavidPairAction only
-    MultiCubic u_kj, du_kj;                    // n_val + 1 components, component 0 the potential
-    uint32_t n_order = 0;
+    MultiCubic u_kj, du_kj;                    // (max_level + 1) x (n_val + 1) components: the table of
+                                               // level l from component l * kj_stride, its component 0
+                                               // the potential
+    uint32_t n_order = 0, kj_stride = 0;       // kj_stride = n_val + 1
     double r_d_min = 0., r_d_max = 0.;         // the grid's ends (GetLimits)
 };
 

@@ -176,6 +176,8 @@ class Context {
     uint32_t perm_pending_ = 0;  // moves with permutation launches not yet folded into their counters
     void* MoveDescriptors();  // double-float move descriptors on the device (sweep.cu)
     bool PermutingSpecies(uint32_t s) const;
+    bool LevelPairTerms(uint32_t m) const;  // Bisect move with pair terms above level 0 (sweep.cu)
+    void RequireLevelZeroDensities(uint32_t m) const;  // refuses Ewald parts above level 0 (sweep.cu)
     // The path permutation: perm[g] = particle whose slice-0 bead follows bead (g, M - 1), global
     // indices; the host copy is refreshed after every device update.
     void SyncPermHost();

@@ -541,7 +541,6 @@ void Context::BuildActions(const Input& in) {
         } else if (h.type == "DavidPairAction") {
             // david_pair_action_class.h:190-358
             if (sys.n_pair >= kMaxPair) throw PimcError(kErrUnsupported, "too many pair actions");
-            if (max_level != 0) throw PimcError(kErrUnsupported, "DavidPairAction: tables for one time step (max_level 0)");
             PairDev& p = sys.pair[sys.n_pair];
             p.kind = kPairDavid;
             p.sa = SpeciesIndex(species_names, a.GetAttribute<std::string>("species_a"));
@@ -559,20 +558,28 @@ void Context::BuildActions(const Input& in) {
             const size_t n_grid = grid.size();
             if ((size_t)tf.Scalar(pre + "/grid/n_grid_points") != n_grid || n_grid < 2)
                 throw PimcError(kErrInput, "table '" + file + "': inconsistent grid");
+            // :234-246: n_tau = max_level + 1 tables; the path's tau must be among the first n_tau taus,
+            // and level l reads table l whatever its tau.
+            const size_t n_tau = (size_t)max_level + 1;
+            const auto& taus = tf.Vec(pre + "/taus");
+            if (taus.size() < n_tau) throw PimcError(kErrInput, "table '" + file + "': fewer taus than max_level + 1");
             bool found = false;
-            for (double t : tf.Vec(pre + "/taus")) found |= std::fabs(t - sys.tau) < 1.0e-6;
+            for (size_t i = 0; i < n_tau; ++i) found |= std::fabs(taus[i] - sys.tau) < 1.0e-6;
             if (!found) throw PimcError(kErrInput, "table '" + file + "': tau of the path not found");
             const auto& V = tf.Vec("potential/data");
             uint32_t n_val = 1;
             for (uint32_t i = 1; i <= p.n_order; ++i) n_val += 1 + i;
-            auto comps = [&](const std::string& key) {
+            p.kj_stride = n_val + 1;
+            auto comps = [&](const std::string& key) {  // value index fastest, then grid, then tau
                 const auto& d = tf.Vec(key);
-                if (d.size() < (size_t)n_val * n_grid || V.size() != n_grid) throw PimcError(kErrInput, "table '" + file + "': short " + key);
-                std::vector<std::vector<double>> out(n_val + 1, std::vector<double>(n_grid));
-                for (size_t g = 0; g < n_grid; ++g) {
-                    out[0][g] = V[g];
-                    for (uint32_t v = 1; v <= n_val; ++v) out[v][g] = d[(v - 1) + g * n_val];
-                }
+                if (d.size() < (size_t)n_val * n_grid * n_tau || V.size() != n_grid)
+                    throw PimcError(kErrInput, "table '" + file + "': short " + key);
+                std::vector<std::vector<double>> out(n_tau * (n_val + 1), std::vector<double>(n_grid));
+                for (size_t l = 0; l < n_tau; ++l)
+                    for (size_t g = 0; g < n_grid; ++g) {
+                        out[l * (n_val + 1)][g] = V[g];
+                        for (uint32_t v = 1; v <= n_val; ++v) out[l * (n_val + 1) + v][g] = d[(v - 1) + g * n_val + l * n_val * n_grid];
+                    }
                 return out;
             };
             p.u_kj = BuildMultiCubic(grid, comps(pre + "/data"));

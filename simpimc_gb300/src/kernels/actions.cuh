@@ -8,13 +8,16 @@ namespace pimc {
 /// DavidPairAction: the endpoint terms of component `diag` at r and r' (clamped to the grid), plus
 /// the off-diagonal expansion sum_{k=1..n} sum_{j=0..k} c_kj(q) z^2j s^2(k-j) at q = (r + r')/2
 /// (clamped) when s > 0 and q < r_max (david_pair_action_class.h:69-102, 126-167). With `add_v` the
-/// potential's endpoint terms (component 0) are added, as CalcdUdBeta does.
-__device__ __forceinline__ double DavidLink(const PairDev& pa, const MultiCubic& t, double r, double rp, double s, bool add_v) {
+/// potential's endpoint terms (component 0) are added, as CalcdUdBeta does. `level` picks the table
+/// u_kj(level) of the time step tau 2^level (the multi-spline's components from level * kj_stride).
+__device__ __forceinline__ double DavidLink(const PairDev& pa, const MultiCubic& t, double r, double rp, double s, bool add_v,
+                                            uint32_t level = 0) {
     const double q = 0.5 * (r + rp), z = r - rp;
+    const int b = (int)(level * pa.kj_stride);
     double ur, urp;
     const int i = MultiInterval(t, r, ur), ip = MultiInterval(t, rp, urp);
-    double u = 0.5 * (MultiComp(t, i, ur, 1) + MultiComp(t, ip, urp, 1));
-    if (add_v) u += 0.5 * (MultiComp(t, i, ur, 0) + MultiComp(t, ip, urp, 0));
+    double u = 0.5 * (MultiComp(t, i, ur, b + 1) + MultiComp(t, ip, urp, b + 1));
+    if (add_v) u += 0.5 * (MultiComp(t, i, ur, b) + MultiComp(t, ip, urp, b));
     if (s > 0. && q < pa.r_d_max) {
         double uq;
         const int iq = MultiInterval(t, q, uq);
@@ -23,7 +26,7 @@ __device__ __forceinline__ double DavidLink(const PairDev& pa, const MultiCubic&
         for (uint32_t k = 1; k <= pa.n_order; ++k) {
             double z2j = 1., cs = s2k;
             for (uint32_t j = 0; j <= k; ++j) {
-                u += MultiComp(t, iq, uq, (int)(k * (k + 1) / 2 + j + 1)) * z2j * cs;
+                u += MultiComp(t, iq, uq, b + (int)(k * (k + 1) / 2 + j + 1)) * z2j * cs;
                 z2j *= z2;
                 cs *= is2;
             }
@@ -66,10 +69,10 @@ __device__ __forceinline__ double PairV(const PairDev& pa, double r, double rp) 
 ///    tau at level 0 and zero above; that behaviour is kept.
 ///  * IlkkaPairAction (ilkka_pair_action_class.h:77-101): u(q + s/2, q - s/2), q = (r + r')/2, minus
 ///    half the long-range action at each end (clamped to its grid) when the action has an Ewald part.
-///  * DavidPairAction (david_pair_action_class.h:69-102): DavidLink of its action components; the
-///    tables are for the time step tau (max_level 0).
+///  * DavidPairAction (david_pair_action_class.h:69-102): DavidLink of the action components of the
+///    level's table u_kj(level).
 __device__ __forceinline__ double PairU(const PairDev& pa, double r, double rp, double s, uint32_t level, double tau) {
-    if (pa.kind == kPairDavid) return DavidLink(pa, pa.u_kj, r, rp, s, false);
+    if (pa.kind == kPairDavid) return DavidLink(pa, pa.u_kj, r, rp, s, false, level);
     if (pa.kind == kPairIlkka) {
         const double q = 0.5 * (r + rp);
         double u = EvalBicubic(pa.u_xy, q + 0.5 * s, q - 0.5 * s);

@@ -178,12 +178,13 @@ __device__ __forceinline__ void DrDrpDrrpDD(const dd* A0, const dd* C0, const dd
 /// CalcU of one link (bare_pair_action_class.h:146-150 with level_tau; ilkka_pair_action_class.h:77-101;
 /// david_pair_action_class.h:69-102).
 __device__ __forceinline__ dd PairUDD(const PairDD& pa, dd r, dd rp, dd s, int level, dd tau) {
-    if (pa.kind == kPairDavid) {
+    if (pa.kind == kPairDavid) {  // the table u_kj(level)
+        const int base = level * (int)pa.kj_stride;
         dd u0, u1;
         const int i0 = MultiIntervalDD(pa.u_kj, r, u0), i1 = MultiIntervalDD(pa.u_kj, rp, u1);
-        dd f = Scale2(Add(MultiCompDD(pa.u_kj, i0, u0, 1), MultiCompDD(pa.u_kj, i1, u1, 1)), 0.5f);
+        dd f = Scale2(Add(MultiCompDD(pa.u_kj, i0, u0, base + 1), MultiCompDD(pa.u_kj, i1, u1, base + 1)), 0.5f);
         const dd q = Scale2(Add(r, rp), 0.5f);
-        if (s.hi > 0.f && Less(q, pa.u_kj.x1)) f = Add(f, DavidOffDiagDD(pa, q, Sub(r, rp), s));
+        if (s.hi > 0.f && Less(q, pa.u_kj.x1)) f = Add(f, DavidOffDiagDD(pa, q, Sub(r, rp), s, base));
         return f;
     }
     if (pa.kind == kPairIlkka) {

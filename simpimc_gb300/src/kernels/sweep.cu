@@ -82,8 +82,8 @@ struct PairDD {
     CubicDD u_long_r;
     dd rumin, rumax;
     // DavidPairAction
-    MultiCubicDD u_kj;
-    uint32_t n_order;
+    MultiCubicDD u_kj;  // the table of level l from component l * kj_stride
+    uint32_t n_order, kj_stride;
 };
 
 constexpr int kMoveKinetic = 2;
@@ -234,8 +234,9 @@ __device__ __forceinline__ dd MultiCompDD(const MultiCubicDD& t, int i, dd u, in
     return Add(dd{a.x, a.y}, Mul(u, v));
 }
 
-/// DavidPairAction::CalcU's off-diagonal expansion at q (david_pair_action_class.h:80-99).
-__device__ __forceinline__ dd DavidOffDiagDD(const PairDD& pa, dd q, dd z, dd s) {
+/// DavidPairAction::CalcU's off-diagonal expansion at q (david_pair_action_class.h:80-99), with the
+/// table whose components start at `base`.
+__device__ __forceinline__ dd DavidOffDiagDD(const PairDD& pa, dd q, dd z, dd s, int base) {
     dd uq;
     const int iq = MultiIntervalDD(pa.u_kj, q, uq);
     const dd z2 = Sqr(z), s2 = Sqr(s), is2 = Div(DD(1.f), s2);
@@ -243,7 +244,7 @@ __device__ __forceinline__ dd DavidOffDiagDD(const PairDD& pa, dd q, dd z, dd s)
     for (uint32_t k = 1; k <= pa.n_order; ++k) {
         dd z2j = DD(1.f), cs = s2k;
         for (uint32_t j = 0; j <= k; ++j) {
-            tot = Add(tot, Mul(Mul(MultiCompDD(pa.u_kj, iq, uq, (int)(k * (k + 1) / 2 + j + 1)), z2j), cs));
+            tot = Add(tot, Mul(Mul(MultiCompDD(pa.u_kj, iq, uq, base + (int)(k * (k + 1) / 2 + j + 1)), z2j), cs));
             z2j = Mul(z2j, z2);
             cs = Mul(cs, is2);
         }
@@ -455,7 +456,7 @@ __device__ __forceinline__ dd PairLinkU4(const PairDD* s_pairs, const MoveDD& mv
                 f = Scale2(MultiCompDD(pa.u_kj, i, u, 1), 0.5f);
             } else if (ql == 2) {
                 const dd sl = Sqrt(ss2), q = Scale2(Add(r, rp), 0.5f);
-                if (sl.hi > 0.f && Less(q, pa.u_kj.x1)) f = DavidOffDiagDD(pa, q, Sub(r, rp), sl);
+                if (sl.hi > 0.f && Less(q, pa.u_kj.x1)) f = DavidOffDiagDD(pa, q, Sub(r, rp), sl, 0);
             }
         } else if (!ilkka) {
             if (ql < 2) f = PairHalfV(pa, Sqrt(ql == 0 ? rv2 : rq2));
@@ -1392,6 +1393,7 @@ void Context::BuildSweepTables() {
         q.rumin = q.rumax = dd{0.f, 0.f};
         q.u_kj = MultiCubicDD();
         q.n_order = p.n_order;
+        q.kj_stride = p.kj_stride;
         if (p.kind == kPairDavid) q.u_kj = MakeMultiCubicDD(*this, p.u_kj, keep_);
         if (p.kind == kPairIlkka) {
             q.u_xy = MakeBicubicDD(*this, p.u_xy, keep_);
@@ -1481,12 +1483,47 @@ void* Context::MoveDescriptors() {
     return sweep_desc_->ptr;
 }
 
+// Whether a Bisect move has pair terms above level 0: a pair action with max_level > 0 whose CalcU
+// is non-zero there (pair_action_class.h:267-291), i.e. the table actions (Ilkka, David); the bare
+// CalcU is zero above level 0, and Ewald parts above level 0 are refused (RequireLevelZeroDensities).
+// The sweep kernel forms pair terms at level 0 only, so such moves run on the permutation kernel's
+// plain variant.
+bool Context::LevelPairTerms(uint32_t m) const {
+    const MoveDev& d = moves[m].dev;
+    if (moves[m].kind != 0 || d.n_level < 2) return false;
+    for (int i = 0; i < d.n_pair; ++i) {
+        const PairDev& p = sys.pair[d.pair[i]];
+        if (p.max_level > 0 && !p.is_constant && p.kind != kPairBare) return true;
+    }
+    return false;
+}
+
+// A long-range pair action with max_level > 0 in a move of more than one level is refused. There the
+// reference updates the densities once per attempt, at the first level that reaches the action and on
+// that level's slices only, and then latches them (need_update_rho_k_, pair_action_class.h:293-298,
+// species_class.h:406-425, marked FIXME). The densities then drift from the positions through the
+// per-bead stores, which this layout does not keep.
+void Context::RequireLevelZeroDensities(uint32_t m) const {
+    const MoveDev& d = moves[m].dev;
+    if (moves[m].kind == 1 || d.n_level < 2) return;
+    for (int i = 0; i < d.n_pair; ++i) {
+        const PairDev& p = sys.pair[d.pair[i]];
+        if (p.use_long_range && p.max_level > 0 && !p.is_constant)
+            throw PimcError(kErrUnsupported, "long-range pair action with max_level > 0 (the reference latches its densities above level 0)");
+    }
+}
+
 void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep) {
     if (n_entries == 0 || n_rep == 0) return;
     if (n_entries > 1024) throw PimcError(kErrArg, "schedule longer than 1024 entries");
+    for (uint32_t e = 0; e < n_entries; ++e) {
+        if (mv[e] >= moves.size()) throw PimcError(kErrArg, "move index out of range");
+        RequireLevelZeroDensities(mv[e]);
+    }
     bool own_launches = false;
     auto on_perm_kernel = [&](uint32_t m) {
-        return moves[m].kind == 2 || moves[m].kind == 3 || (moves[m].kind == 0 && PermutingSpecies(moves[m].dev.species));
+        return moves[m].kind == 2 || moves[m].kind == 3 ||
+               (moves[m].kind == 0 && (PermutingSpecies(moves[m].dev.species) || LevelPairTerms(m)));
     };
     for (uint32_t e = 0; e < n_entries; ++e) {
         if (mv[e] >= moves.size()) throw PimcError(kErrArg, "move index out of range");
@@ -1526,12 +1563,9 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
         const MoveDev& d = moves[m].dev;
         if (d.n_level > 8) throw PimcError(kErrUnsupported, "bisection level above 8 in the sweep kernel");
         max_level = std::max(max_level, d.n_level);
-        for (int i = 0; i < d.n_pair; ++i) {
-            const PairDev& p = sys.pair[d.pair[i]];
-            if (p.use_long_range && p.max_level > 0)
-                throw PimcError(kErrUnsupported, "long-range pair action with max_level > 0 in the sweep kernel");
-        }
     }
+    for (uint32_t e = 0; e < n_entries; ++e)
+        if (LevelPairTerms(mv[e])) throw PimcError(kErrState, "pair terms above level 0 in the sweep kernel");
     char* base = static_cast<char*>(MoveDescriptors());
     MoveDD* dmoves = reinterpret_cast<MoveDD*>(base);
     uint32_t* dsm = reinterpret_cast<uint32_t*>(base + sizeof(MoveDD) * kMaxMoves);
@@ -1752,7 +1786,8 @@ void Context::PermArgs(uint32_t m, void* out, size_t* smem_out) {
     PermArgsDD& a = *static_cast<PermArgsDD*>(out);
     MoveHost& mh = moves[m];
     const uint32_t sp = mh.dev.species, N = sys.sp_n[sp], M = sys.M;
-    if (N > kPermMaxPart) throw PimcError(kErrUnsupported, "exchanging species of at most 512 particles");
+    if (N > kPermMaxPart)
+        throw PimcError(kErrUnsupported, "the permutation kernel (exchanges; pair terms above level 0) takes species of at most 512 particles");
     if (precision == 32 && sys.sp_rho[sp] >= 0 && sys.K)
         throw PimcError(kErrUnsupported, "the permutation kernel keeps double-float densities: set precision 64");
     const uint32_t B = 1u << mh.dev.n_level;
@@ -1849,6 +1884,7 @@ void SweepChains(const std::vector<Context*>& cs, const uint32_t* mv, const uint
         if (c->moves.size() != cs[0]->moves.size()) throw PimcError(kErrArg, "chains with different move lists");
         for (uint32_t e = 0; e < n_entries; ++e) {
             if (mv[e] >= c->moves.size()) throw PimcError(kErrArg, "move index out of range");
+            c->RequireLevelZeroDensities(mv[e]);
             const MoveHost& mh = c->moves[mv[e]];
             // every bisection and permuting move fits the one-CTA kernel (its plain variant replays the
             // sweep kernel's draws); HMC, species above kPermMaxPart and the FP32 density mode do not

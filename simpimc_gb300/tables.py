@@ -189,7 +189,7 @@ def ilkka_table(path, *, tau: float, lam: float = 0.5, z_ab: float = 1.0, L: flo
 
 def david_table(path, *, tau: float, n_order: int = 2, lam: float = 0.5, z_ab: float = 1.0, L: float = 0.0,
                 k_cut: float = 0.0, n_d: int = 3, n_grid: int = 200, r_max: float | None = None,
-                alpha: float | None = None) -> dict:
+                alpha: float | None = None, n_tau: int = 1) -> dict:
     """Write a DavidPairAction table (src/actions/pair_action/david_pair_action_class.h:190-358).
 
     The squarer that writes these tables is not part of the reference, so the table is synthetic:
@@ -204,7 +204,8 @@ def david_table(path, *, tau: float, n_order: int = 2, lam: float = 0.5, z_ab: f
       reads LOG, LINEAR and LOGLIN grid types, whose knots the points give);
     * ``u_kj_n/taus``, ``potential/data``;
     * ``u_kj_n/data`` and ``du_kj_dbeta_n/data``: n_val x n_grid x n_tau values, value index
-      fastest (Armadillo's cube order), n_val = sum_{i=0..n} (i + 1);
+      fastest (Armadillo's cube order), n_val = sum_{i=0..n} (i + 1). Table l is made for the time
+      step tau 2^l (the bisection's level l with max_level = n_tau - 1), with the potential of tau;
     * with ``L > 0`` and ``k_cut > 0``: ``long_range/{k_cut, n_k, k_points, u_k}`` (V u_k is the
       k-space Ewald potential, listed with k = 0 for its constant) and ``squarer/v_image``.
     """
@@ -217,22 +218,30 @@ def david_table(path, *, tau: float, n_order: int = 2, lam: float = 0.5, z_ab: f
     V = z_ab * erf(r / a) / r
     w = z_ab * np.exp(-(r / a) ** 2) / (2.0 * a)
     n_val = sum(i + 1 for i in range(n_order + 1))
-    u = np.zeros((n_val, n_grid))
-    du = np.zeros((n_val, n_grid))
-    u[0] = tau * V + tau * tau * w
-    du[0] = 2.0 * tau * w  # d u_00 / d tau - V
-    for k in range(1, n_order + 1):
-        for j in range(k + 1):
-            c = (-1.0) ** (k + j) / (4.0 ** k * (j + 1))
-            idx = k * (k + 1) // 2 + j
-            u[idx] = tau ** k * c * V / a ** (2 * k)
-            du[idx] = k * tau ** (k - 1) * c * V / a ** (2 * k)
+    us, dus, taus = [], [], []
+    for lvl in range(n_tau):
+        tl = tau * 2 ** lvl
+        al = math.sqrt(4.0 * lam * tl)
+        wl = z_ab * np.exp(-(r / al) ** 2) / (2.0 * al)
+        u = np.zeros((n_val, n_grid))
+        du = np.zeros((n_val, n_grid))
+        u[0] = tl * V + tl * tl * wl
+        du[0] = 2.0 * tl * wl  # d u_00 / d tau - V
+        for k in range(1, n_order + 1):
+            for j in range(k + 1):
+                c = (-1.0) ** (k + j) / (4.0 ** k * (j + 1))
+                idx = k * (k + 1) // 2 + j
+                u[idx] = tl ** k * c * V / al ** (2 * k)
+                du[idx] = k * tl ** (k - 1) * c * V / al ** (2 * k)
+        us.append(u.T.ravel())  # value index fastest
+        dus.append(du.T.ravel())
+        taus.append(tl)
     pre = f"u_kj_{n_order}"
     ds = {
         f"{pre}/grid/start": r[0], f"{pre}/grid/end": r[-1], f"{pre}/grid/n_grid_points": n_grid, f"{pre}/grid/grid_points": r,
-        f"{pre}/taus": tau, "potential/data": V,
-        f"{pre}/data": u.T.ravel(),  # value index fastest
-        f"du_kj_dbeta_{n_order}/data": du.T.ravel(),
+        f"{pre}/taus": tau if n_tau == 1 else np.array(taus), "potential/data": V,
+        f"{pre}/data": np.concatenate(us),  # then grid, then tau
+        f"du_kj_dbeta_{n_order}/data": np.concatenate(dus),
     }
     if L > 0 and k_cut > 0:
         al = ewald_alpha(L, k_cut) if alpha is None else alpha

@@ -17,10 +17,11 @@ scipy_interp = pytest.importorskip("scipy.interpolate")
 class Multi:
     """Component splines of a David table (component 0 the potential), argument clamped to the grid."""
 
-    def __init__(self, ds, key, n_order):
+    def __init__(self, ds, key, n_order, level=0):
         g = np.asarray(ds[f"u_kj_{n_order}/grid/grid_points"])
         n_val = sum(i + 1 for i in range(n_order + 1))
-        data = np.asarray(ds[key]).reshape(len(g), n_val)  # value index fastest
+        block = len(g) * n_val  # one table per tau: value index fastest, then grid, then tau
+        data = np.asarray(ds[key])[level * block:(level + 1) * block].reshape(len(g), n_val)
         cols = [np.asarray(ds["potential/data"])] + [data[:, v] for v in range(n_val)]
         self.lo, self.hi = g[0], g[-1]
         self.s = [scipy_interp.CubicSpline(g, c, bc_type="natural") for c in cols]
@@ -146,3 +147,40 @@ def test_oracle_david_ewald_action(tmp_path):
     got = c.get_action(2, b0, b1, [(0, p)], 0, 0)
     assert abs(got - want) <= 1e-10 * max(1.0, abs(want)), (got, want)
     c.close()
+
+
+def test_oracle_david_level_tables(tmp_path):
+    """max_level 2: level l sums links of stride 2^l with the table of index l (u_kj(level)), and the
+    action above max_level is zero (pair_action_class.h:267-291, david_pair_action_class.h:63-102)."""
+    xml, path = trapped_coulomb(tmp_path, n_part=5, n_bead=16, n_level=3, seed=5, pair="DavidPairAction", n_order=2,
+                                pair_max_level=2)
+    ds = david_table(tmp_path / "check.pat", tau=2.0 / 16, n_order=2, lam=0.5, z_ab=1.0, L=0.0, n_tau=3)
+    c = oracle.OracleSim(xml, base_dir=tmp_path)
+    c.set_path(path)
+    N, M, _ = path.shape
+    seen = []
+    for level in range(3):
+        u = Multi(ds, "u_kj_2/data", 2, level)
+        skip = 1 << level
+        for p, b0, b1 in [(1, 0, 8), (4, 12, 20)]:
+            want = 0.0
+            for b in range(b0, b1, skip):
+                for q in range(N):
+                    if q != p:
+                        want += link(u, *dists(path[q, b % M], path[p, b % M], path[q, (b + skip) % M],
+                                               path[p, (b + skip) % M], 0.0), 1, False)
+            got = c.get_action(2, b0, b1, [(0, p)], level, 0)
+            assert abs(got - want) <= 1e-12 * max(1.0, abs(want)), (level, got, want)
+            seen.append(got)
+    assert len(set(seen)) == len(seen)
+    assert c.get_action(2, 0, 8, [(0, 1)], 3, 0) == 0.0
+    c.close()
+
+
+def test_oracle_david_refuses_missing_level_tables(tmp_path):
+    """A table with fewer taus than max_level + 1 is an input error (david_pair_action_class.h:234-246)."""
+    xml, _ = trapped_coulomb(tmp_path, n_part=5, n_bead=16, n_level=3, seed=5, pair="DavidPairAction", n_order=2,
+                             pair_max_level=2)
+    david_table(tmp_path / "david_open_16_2.0_2_2.pat", tau=2.0 / 16, n_order=2, lam=0.5, z_ab=1.0, L=0.0, n_tau=2)
+    with pytest.raises(RuntimeError, match="fewer taus"):
+        oracle.OracleSim(xml, base_dir=tmp_path)
