@@ -261,9 +261,12 @@ __device__ __forceinline__ void CopyToShared(void* dst, const void* src, size_t 
 __device__ void PermRun(const PermArgsDD& a_in, uint64_t attempt0, uint32_t n_attempts, unsigned char* dyn, PermSharedDD& sh) {
     // The arguments, the move descriptor and its pair descriptors in shared memory: the phases of an
     // attempt read them on their dependent chains.
+    // (raw storage for the descriptors: their members have initialisers, which __shared__ cannot run)
     __shared__ PermArgsDD s_args;
-    __shared__ MoveDD s_mv;
-    __shared__ PairDD s_pairs[kMaxPair];
+    __shared__ __align__(16) unsigned char s_mv_raw[sizeof(MoveDD)];
+    __shared__ __align__(16) unsigned char s_pairs_raw[sizeof(PairDD) * kMaxPair];
+    MoveDD& s_mv = *reinterpret_cast<MoveDD*>(s_mv_raw);
+    PairDD* s_pairs = reinterpret_cast<PairDD*>(s_pairs_raw);
     __syncthreads();  // the previous entry of a many-chain schedule is done with them
     CopyToShared(&s_args, &a_in, sizeof(PermArgsDD));
     CopyToShared(&s_mv, a_in.mv, sizeof(MoveDD));

@@ -1525,10 +1525,7 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
         return moves[m].kind == 2 || moves[m].kind == 3 ||
                (moves[m].kind == 0 && (PermutingSpecies(moves[m].dev.species) || LevelPairTerms(m)));
     };
-    for (uint32_t e = 0; e < n_entries; ++e) {
-        if (mv[e] >= moves.size()) throw PimcError(kErrArg, "move index out of range");
-        own_launches |= moves[mv[e]].kind == 1 || on_perm_kernel(mv[e]);
-    }
+    for (uint32_t e = 0; e < n_entries; ++e) own_launches |= moves[mv[e]].kind == 1 || on_perm_kernel(mv[e]);
     bool all_perm = true;
     for (uint32_t e = 0; e < n_entries; ++e) all_perm &= on_perm_kernel(mv[e]);
     if (all_perm) {  // every entry on the permutation kernel: enqueue them all, wait once
