@@ -107,7 +107,11 @@ int pimc_virial_energy(pimc_ctx* ctx, uint32_t action, double window, double* ou
  * gradient, Metropolis on the energy change. */
 int pimc_move_attempts(pimc_ctx* ctx, uint32_t move, uint64_t n);
 /* A schedule of moves, (moves[i], counts[i]) in order, repeated n_rep times, in one launch
- * (the body of a Loop of Move events, loop_class.h:269-274). */
+ * (the body of a Loop of Move events, loop_class.h:269-274). A Bisect move whose Ilkka or David pair
+ * action has max_level > 0 runs on the permutation kernel, which forms the pair terms of every
+ * level (pair_action_class.h:267-291). A long-range pair action with max_level > 0 in a move of
+ * more than one level makes the call fail with PIMC_ERR_UNSUPPORTED before any attempt runs: the
+ * reference latches its densities there (pair_action_class.h:293-298). */
 int pimc_sweep(pimc_ctx* ctx, const uint32_t* moves, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep);
 /* out[5] = {total attempts, attempts in block, accepts in block, total accepts, total attempts
  * that reached the level-0 test} (counters of move_class.h:226-228). */
