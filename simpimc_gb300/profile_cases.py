@@ -5,6 +5,8 @@
     python -m simpimc_gb300.profile_cases large32  # 1024-electron gas, FP32 mode: 1 + 1 launches of 64 attempts
     python -m simpimc_gb300.profile_cases bosons   # 32 trapped bosons: Bisect and PermBisectIterative, 1 + 1 sweeps
     python -m simpimc_gb300.profile_cases chains   # 608 such chains: 1 + 1 launches of one sweep each (pimc_sweep_chains)
+    python -m simpimc_gb300.profile_cases egas_chains  # 38, 152 and 304 66-electron-gas chains: a warm-up
+                                                       # launch, then one timed sweep each (pimc_sweep_chains)
 
 The first two hold well under 100 MB on the device, the third about 1.3 GB; a capture of the
 second launch (`-k regex:<Kernel> -s 1 -c 1`) ends in seconds (the large case with one or two
@@ -88,10 +90,39 @@ def chains_case(d):
     print(f"chains ok: {sum(s.move_counters(0)[0] + s.move_counters(1)[0] for s in sims)} attempts")
 
 
+def egas_chains_case(d):
+    """Throughput of many 66-electron-gas chains (r_s = 2, beta = 8, M = 128, level 4) in one
+    launch: one sweep is 33 attempts of each species' move, 8 times (528 attempts, 15
+    moved beads each). Wall clock around the call, which returns after its launch has finished."""
+    import os
+    import time
+
+    from . import Simulation, sweep_chains
+    from .configs import electron_gas
+    for nc in (38, 152, 304):
+        sims = []
+        for c in range(nc):
+            dc = os.path.join(d, f"c{nc}_{c}")
+            xml, path = electron_gas(dc, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_units=12.0, n_level=4, seed=20261203 + c)
+            s = Simulation(xml, base_dir=dc, chain=c)
+            s.set_path(path)
+            sims.append(s)
+        sweep_chains(sims, [0, 1], [33, 33], 1)  # warm-up
+        b0 = sum(s.move_counters(0)[0] + s.move_counters(1)[0] for s in sims)
+        t0 = time.perf_counter()
+        sweep_chains(sims, [0, 1], [33, 33], 8)
+        el = time.perf_counter() - t0
+        att = sum(s.move_counters(0)[0] + s.move_counters(1)[0] for s in sims) - b0
+        print(f"{nc} chains: {att * 15 / el / 1e6:.3f} M bead-moves/s, {el:.3f} s per sweep", flush=True)
+        for s in sims:
+            s.close()
+
+
 def main(argv):
     case = argv[1] if len(argv) > 1 else "batch"
     with tempfile.TemporaryDirectory() as d:
-        {"batch": batch_case, "egas": egas_case, "large32": large32_case, "bosons": bosons_case, "chains": chains_case}[case](d)
+        {"batch": batch_case, "egas": egas_case, "large32": large32_case, "bosons": bosons_case, "chains": chains_case,
+         "egas_chains": egas_chains_case}[case](d)
 
 
 if __name__ == "__main__":
