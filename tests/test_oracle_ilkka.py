@@ -174,3 +174,27 @@ def test_oracle_ilkka_ewald_action(tmp_path):
     got = c.get_action(2, b0, b1, [(0, p)], 0, 0)  # KineticU, KineticD, then CoulombUU
     assert abs(got - want) <= 1e-10 * max(1.0, abs(want)), (got, want)
     c.close()
+
+
+def test_oracle_ilkka_levels_use_stride(tmp_path):
+    """max_level 1: the level-1 action sums links of stride 2 with the one table; level 2 is zero
+    (pair_action_class.h:267-291; ilkka_pair_action_class.h:77-101 takes no level)."""
+    xml, path = trapped_coulomb(tmp_path, n_part=5, n_bead=16, n_level=3, seed=7, pair="IlkkaPairAction", pair_max_level=1)
+    ds = ilkka_table(tmp_path / "check.pat", tau=2.0 / 16, lam=0.5, z_ab=1.0, L=0.0)
+    u, _ = tables(ds)
+    c = oracle.OracleSim(xml, base_dir=tmp_path)
+    c.set_path(path)
+    N, M, _ = path.shape
+    for level in (0, 1):
+        skip = 1 << level
+        for p, b0, b1 in [(2, 0, 8), (4, 10, 18)]:
+            want = 0.0
+            for b in range(b0, b1, skip):
+                for q in range(N):
+                    if q != p:
+                        want += link_u(u, None, *dr_drp_drrp(path[q, b % M], path[p, b % M], path[q, (b + skip) % M],
+                                                             path[p, (b + skip) % M], 0.0))
+            got = c.get_action(2, b0, b1, [(0, p)], level, 0)
+            assert abs(got - want) <= 1e-12 * max(1.0, abs(want)), (level, p, got, want)
+    assert c.get_action(2, 0, 8, [(0, 2)], 2, 0) == 0.0
+    c.close()
