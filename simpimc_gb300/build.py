@@ -1,7 +1,7 @@
 """Builds the CUDA library (sm_103a) in-tree: simpimc_gb300/lib/libsimpimc_gb300.so.
 
 Translation units compile in parallel with nvcc; the result links the CUDA runtime statically so
-the shared object only needs the driver at load time.
+the shared object only needs the CUDA driver library (libcuda) at load time.
 """
 from __future__ import annotations
 
