@@ -184,3 +184,17 @@ def test_oracle_david_refuses_missing_level_tables(tmp_path):
     david_table(tmp_path / "david_open_16_2.0_2_2.pat", tau=2.0 / 16, n_order=2, lam=0.5, z_ab=1.0, L=0.0, n_tau=2)
     with pytest.raises(RuntimeError, match="fewer taus"):
         oracle.OracleSim(xml, base_dir=tmp_path)
+
+
+def test_david_table_levels_layout(tmp_path):
+    """n_tau tables for tau 2^l, value index fastest, then grid, then tau; the first block equals the
+    one-table file's (the levels share the grid and the potential)."""
+    one = david_table(tmp_path / "one.pat", tau=0.125, n_order=2, n_grid=50)
+    three = david_table(tmp_path / "three.pat", tau=0.125, n_order=2, n_grid=50, n_tau=3)
+    assert np.allclose(three["u_kj_2/taus"], [0.125, 0.25, 0.5])
+    n_val = 6
+    for key in ("u_kj_2/data", "du_kj_dbeta_2/data"):
+        assert len(three[key]) == 3 * 50 * n_val
+        assert np.array_equal(three[key][:50 * n_val], one[key])
+        assert not np.array_equal(three[key][50 * n_val:100 * n_val], one[key])
+    assert np.array_equal(three["potential/data"], one["potential/data"])
