@@ -39,20 +39,20 @@ typedef struct pimc_info {
     int32_t pbc;
 } pimc_info;
 
-/* Framework + Simulation construction (src/framework/framework_class.h:87-128,
+/* Framework + Simulation construction (src/framework/framework_class.h:39-79,
  * src/framework/simulation_class.h:16-39). `base_dir` resolves relative table paths; `chain`
- * selects the independent random stream (the reference's clone index, framework_class.h:96). */
+ * selects the independent random stream (the reference's clone index, framework_class.h:104). */
 int pimc_create(const char* xml_text, const char* base_dir, int device, uint32_t chain, pimc_ctx** out);
 void pimc_destroy(pimc_ctx* ctx);
 const char* pimc_last_error(const pimc_ctx* ctx);
 int pimc_get_info(pimc_ctx* ctx, pimc_info* out);
-/* Overrides the <RNG seed> (framework_class.h:132-147). */
+/* Overrides the <RNG seed> (framework_class.h:84-101). */
 int pimc_set_seed(pimc_ctx* ctx, uint32_t seed);
 /* Names: kind 0 species, 1 action, 2 move, 3 observable. */
 int pimc_get_name(pimc_ctx* ctx, int kind, uint32_t index, char* buf, size_t cap);
 int pimc_species_info(pimc_ctx* ctx, uint32_t species, uint32_t* n_part, uint32_t* offset, double* lambda);
 
-/* Path state: Bead::SetR / StoreR and Species::InitRhoK (bead_class.h:255-302,
+/* Path state: Bead::SetR / StoreR and Species::InitRhoK (bead_class.h:57-101,
  * species_class.h:236-244,380-403). which: 0 the stored ("old") copy, 1 the working ("new") copy,
  * 2 both (then the per-slice charge densities are recomputed from the positions). */
 int pimc_set_path(pimc_ctx* ctx, int which, const double* pos);
@@ -64,7 +64,7 @@ int pimc_get_kvecs(pimc_ctx* ctx, double* out);
 
 /* Action interface (src/actions/action_class.h:37-52). Particles are (species, index) pairs as
  * in the reference's std::vector<std::pair<std::shared_ptr<Species>, uint32_t>>. mode 0 reads the
- * stored copy (OLD_MODE), 1 the working copy (NEW_MODE, bead_class.h:204-206). */
+ * stored copy (OLD_MODE), 1 the working copy (NEW_MODE, bead_class.h:7-8, 98). */
 /* Action::GetAction (action_class.h:43) */
 int pimc_get_action(pimc_ctx* ctx, uint32_t action, uint32_t b0, uint32_t b1, const uint32_t* species, const uint32_t* particles,
                     uint32_t n_particles, uint32_t level, int mode, double* out);
@@ -100,21 +100,21 @@ int pimc_potential(pimc_ctx* ctx, uint32_t action, double* out);
 /* Action::VirialEnergy (action_class.h:40) */
 int pimc_virial_energy(pimc_ctx* ctx, uint32_t action, double window, double* out);
 
-/* Moves: Move::DoEvent repeated (move_class.h:277-293, bisect_class.h:24-139). Runs n attempts
+/* Moves: Move::DoEvent repeated (move_class.h:61-77, bisect_class.h:24-139). Runs n attempts
  * of move `move` on the device in one launch. Besides Bisect, a <Move type="HMC" step_size="0.01"
  * n_steps="10" [species="..."]/> (no reference counterpart) moves the whole path of one or every
  * species by hybrid Monte Carlo: Gaussian momenta, leapfrog on S(R) + |P|^2/2 with the exact
  * gradient, Metropolis on the energy change. */
 int pimc_move_attempts(pimc_ctx* ctx, uint32_t move, uint64_t n);
 /* A schedule of moves, (moves[i], counts[i]) in order, repeated n_rep times, in one launch
- * (the body of a Loop of Move events, loop_class.h:269-274). A Bisect move whose Ilkka or David pair
+ * (the body of a Loop of Move events, loop_class.h:55-60). A Bisect move whose Ilkka or David pair
  * action has max_level > 0 runs on the permutation kernel, which forms the pair terms of every
  * level (pair_action_class.h:267-291). A long-range pair action with max_level > 0 in a move of
  * more than one level makes the call fail with PIMC_ERR_UNSUPPORTED before any attempt runs: the
  * reference latches its densities there (pair_action_class.h:293-298). */
 int pimc_sweep(pimc_ctx* ctx, const uint32_t* moves, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep);
 /* out[5] = {total attempts, attempts in block, accepts in block, total accepts, total attempts
- * that reached the level-0 test} (counters of move_class.h:226-228). */
+ * that reached the level-0 test} (counters of move_class.h:11-12). */
 int pimc_move_stats(pimc_ctx* ctx, uint32_t move, uint64_t* out);
 
 /* Path permutation of a species (the bead links at the ring closure, bead_class.h:38-41 after the
@@ -135,9 +135,9 @@ int pimc_sweep_chains(pimc_ctx** ctxs, uint32_t n_ctx, const uint32_t* moves, co
  * block (perm_bisect_class.h:25-26, 59-90); N = the move's species particle count. */
 int pimc_perm_stats(pimc_ctx* ctx, uint32_t move, uint64_t* out, size_t cap);
 
-/* Observables: Observable::DoEvent / Write (observable_class.h:421-432). pimc_observable_block
+/* Observables: Observable::DoEvent / Write (observable_class.h:93-104). pimc_observable_block
  * returns the normalised values Write() would append (energy_class.h:232-325,
- * pair_correlation_class.h:89-123, structure_factor_class.h:195-211) and resets the block. */
+ * pair_correlation_class.h:89-123, structure_factor_class.h:69-85) and resets the block. */
 int pimc_observable_accumulate(pimc_ctx* ctx, uint32_t observable);
 int pimc_observable_block(pimc_ctx* ctx, uint32_t observable, double* out, size_t cap, size_t* n);
 
@@ -210,7 +210,7 @@ int pimc_batch_get_path(pimc_batch* b, uint32_t chain, double* pos);
  * laid out on the device. A non-finite coordinate makes set_paths return PIMC_ERR_ARG. */
 int pimc_batch_set_paths(pimc_batch* b, const double* all);
 int pimc_batch_get_paths(pimc_batch* b, double* all);
-/* n bisection attempts (Move::DoEvent, move_class.h:277-293) on every chain. */
+/* n bisection attempts (Move::DoEvent, move_class.h:61-77) on every chain. */
 int pimc_batch_attempts(pimc_batch* b, uint64_t n);
 /* n sweeps on every chain; a sweep of a chain is n_part * ceil(n_bead / 2^n_level) attempts. */
 int pimc_batch_sweeps(pimc_batch* b, uint64_t n);

@@ -147,7 +147,7 @@ static void boxmuller(uint32_t w0, uint32_t w1, float& z0, float& z1) {
 
 // ---------------------------------------------------------------------------------------------
 // Natural cubic interpolating spline (stands in for einspline UBspline_1d_d / NUBspline_1d_d with
-// {NATURAL, NATURAL} boundary conditions: free_spline_class.h:177-180, bare_pair_action_class.h:36-67).
+// {NATURAL, NATURAL} boundary conditions: free_spline_class.h:64-67, bare_pair_action_class.h:36-67).
 struct Spline {
     std::vector<double> x, y, m;  // knots, values, second derivatives
     bool uniform = false;
@@ -368,7 +368,7 @@ struct Species {
     bool need_update_rho_k = true;
     // Per-slice charge densities and their copies (species_class.h:23-24): [b][k].
     std::vector<cplx> rho_k, rho_k_c;
-    // Per-bead charge densities and their copies (bead_class.h:218-219): [p][b][k].
+    // Per-bead charge densities and their copies (bead_class.h:20-21): [p][b][k].
     std::vector<cplx> bead_rho_k, bead_rho_k_c;
     // Bead links (bead_class.h:38-41, 98-111): bead (p, b) is followed by bead (nxt[p M + b], b + 1 mod M);
     // OLD mode reads the copy nxt_c. Between moves every link keeps its particle label except at the
@@ -540,7 +540,7 @@ struct Path {
         r_r_p_mag = std::sqrt(c);
     }
 
-    // bead_class.h:323-331 — rho_k of one bead from the current-mode position.
+    // bead_class.h:125-133 — rho_k of one bead from the current-mode position.
     void CalcBeadRhoK(Species& s, uint32_t p, uint32_t b, cplx* out) {
         ks.CalcC(GetR(s, p, b));
         for (size_t k = 0; k < ks.K(); ++k) {
@@ -694,7 +694,7 @@ struct Action {
     virtual void Reject() {}
 };
 
-// src/actions/single_action/single_action_class.h:245-262
+// src/actions/single_action/single_action_class.h:7-24
 struct SingleAction : Action {
     double i_4_lambda_tau;
     Species* species;
@@ -2440,13 +2440,13 @@ struct PairCorrelation : Observable {
         r_max = in.GetAttribute<double>("r_max", p.L / 2.);
         n_r = in.GetAttribute<uint32_t>("n_r", 100);
         if (n_r < 2) throw InputError("n_r must be at least 2");
-        dr = (r_max - r_min) / (n_r - 1.);  // observable_class.h:357-366
+        dr = (r_max - r_min) / (n_r - 1.);  // observable_class.h:29-38
         d_ir = 1. / dr;
         rs.resize(n_r);
         for (uint32_t i = 0; i < n_r; ++i) rs[i] = r_min + i * dr;
         gr.assign(n_r, 0.);
     }
-    // observable_class.h:384-390
+    // observable_class.h:56-62
     uint32_t ReverseMap(double r) const { return (uint32_t)std::nearbyint((r - r_min) * d_ir - 0.5); }
     void Accumulate() override {
         path.mode = NEW_MODE;
@@ -2487,7 +2487,7 @@ struct PairCorrelation : Observable {
     }
 };
 
-// structure_factor_class.h:7-212
+// structure_factor_class.h:7-86
 struct StructureFactor : Observable {
     Path& path;
     Species *sa, *sb;
@@ -2531,7 +2531,7 @@ struct StructureFactor : Observable {
     }
 };
 
-// sign_class.h:7-51: the block mean of the path's sign.
+// sign_class.h:7-48: the block mean of the path's sign.
 struct SignObs : Observable {
     Path& path;
     double sign = 0.;
@@ -2756,7 +2756,7 @@ struct Simulation {
                             found = true;
                         }
                 }
-                if (!found) continue;  // loop_class.h:254-258 warns and skips
+                if (!found) continue;  // loop_class.h:40-44 warns and skips
             } else if (t == "Write") {
                 ch.kind = 3;
             } else if (t == "Loop") {
@@ -2783,7 +2783,7 @@ struct Simulation {
                 if (c.kind == 0) RunNode(c);
                 else if (c.kind == 1) moves[c.index]->DoEvent();
                 else if (c.kind == 2)
-                    observables[c.index]->Accumulate();  // observable_class.h:421-429 ignores `skip`
+                    observables[c.index]->Accumulate();  // observable_class.h:93-101 ignores `skip`
                 else
                     Write();
             }

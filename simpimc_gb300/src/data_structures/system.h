@@ -15,7 +15,7 @@
 //   kidx  [K]            int32    packed lattice indices (n_x, n_y, n_z) of the stored half-space
 //                                  k-vectors, 8 bits each with an offset of 128.
 //
-// The reference's per-bead charge densities (bead_class.h:218-219, N*M*K complex numbers: 481 MB
+// The reference's per-bead charge densities (bead_class.h:20-21, N*M*K complex numbers: 481 MB
 // for the 66-electron gas and 426 GB for the 1024-electron one) are not stored: the density of a
 // bead is recomputed from its position when it is needed, with the same per-dimension phase
 // recurrence (k_space_class.h:83-94).

@@ -67,12 +67,12 @@ struct MoveHost {
     double target_ratio = 0.;
     bool first_block = true;
     uint64_t attempts = 0;       // total attempts (Philox attempt counter)
-    uint64_t block_attempt = 0;  // counters since the last Write (move_class.h:253-256)
+    uint64_t block_attempt = 0;  // counters since the last Write (move_class.h:37-40)
     uint64_t block_accept = 0;
     double last_ratio = 0.;      // acceptance ratio of the last completed block
     uint64_t total_accept = 0;   // accepted attempts since construction
     uint64_t total_level0 = 0;   // attempts whose proposal reached the level-0 evaluation
-    // Per Write event (move_class.h:296-310, bisect_class.h:193-213): the block's counters, its
+    // Per Write event (move_class.h:80-94, bisect_class.h:193-213): the block's counters, its
     // acceptance ratio and the bisection level in force.
     std::vector<double> out_attempt, out_accept, out_ratio, out_level;
     // Hybrid Monte Carlo move (no reference counterpart): leapfrog on the whole path driven by
@@ -105,7 +105,7 @@ struct ObservableHost {
     uint32_t sa = 0, sb = 0, n_r = 0;
     double r_min = 0., r_max = 0., dr = 0., d_ir = 0.;
     std::unique_ptr<DeviceBuffer> hist;  // unsigned long long [n_r]
-    // StructureFactor (structure_factor_class.h:7-212)
+    // StructureFactor (structure_factor_class.h:7-86)
     double k_cut = 0.;
     std::unique_ptr<DeviceBuffer> sk;    // double [K]
     // PathDump (path_dump_class.h:7-70): every `skip`-th Write stores each species' positions as
@@ -114,7 +114,7 @@ struct ObservableHost {
     uint64_t n_write_calls = 0;
     std::vector<std::vector<std::vector<double>>> dumps;  // [species][dump] positions
     std::vector<std::vector<std::vector<double>>> dump_perms;  // [species][dump] (prev, next) per particle
-    // Sign (sign_class.h:7-51) and Permutation (permutation_class.h:7-119): the block's sign sum,
+    // Sign (sign_class.h:7-48) and Permutation (permutation_class.h:7-119): the block's sign sum,
     // cycle-length counts and sector of each measurement; the partitions of N in sector order.
     double sign_sum = 0.;
     uint32_t species = 0, sector_max = 0;

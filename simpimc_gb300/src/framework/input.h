@@ -8,7 +8,7 @@
 //
 // Semantics kept from the reference: attribute names are case-sensitive; a missing attribute
 // without a default is an error; a missing child yields an empty node named "null" (the
-// reference tests `rng_in.node.name == "null"`, src/framework/framework_class.h:134).
+// reference tests `rng_in.node.name == "null"`, src/framework/framework_class.h:86).
 #pragma once
 
 #include <cctype>

@@ -1,7 +1,7 @@
 // Run output and restart.
 //
 // The reference writes its output through IO (HDF5) under fixed dataset paths: Moves/<name>/*
-// (move_class.h:45-53, 286-293; bisect_class.h:193-213) and Observables/<name>/* (observable_class.h:
+// (move_class.h:49-53, 80-94; bisect_class.h:193-213) and Observables/<name>/* (observable_class.h:
 // 79-88; energy_class.h:232-272; pair_correlation_class.h:76-120; structure_factor_class.h:56-82;
 // path_dump_class.h:28-66), one value appended per Write event to its extendable datasets. HDF5 is
 // not part of this build: the same paths are written to the table container of table_io.h, a

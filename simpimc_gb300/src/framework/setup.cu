@@ -406,7 +406,7 @@ struct KSet {
 
 void Context::BuildActions(const Input& in) {
     // k-space: the System cutoff, then every long-range action and structure factor may raise it
-    // (path_class.h:58-62, pair_action_class.h:216-222, structure_factor_class.h:175-180).
+    // (path_class.h:58-62, pair_action_class.h:216-222, structure_factor_class.h:49-54).
     KSet ks;
     Input sysin = in.GetChild("System");
     if (sys.pbc) ks.Setup(sysin.GetAttribute<double>("k_cut", 2. * M_PI / sys.L), sys.L, sys.n_d);
@@ -903,7 +903,7 @@ void Context::BuildObservables(const Input& in) {
 }
 
 void Context::ReadLoop(const Input& in, LoopNode& node) {
-    // loop_class.h:248-266
+    // loop_class.h:34-52
     for (auto& c : in.GetChildList()) {
         const std::string& t = c.GetName();
         LoopNode ch;

@@ -132,7 +132,7 @@ __device__ __forceinline__ int MultiInterval(const MultiCubic& t, double x, doub
     return i;
 }
 
-/// Free-particle log density with periodic-image correction (free_spline_class.h:189-197):
+/// Free-particle log density with periodic-image correction (free_spline_class.h:76-84):
 /// -sum_d image(dr_d) - |dr|^2 / (4 lambda tau).
 __device__ __forceinline__ double LogRhoFree(const double* dr, uint32_t n_d, double i4lt, const CubicTable* image, int has_images) {
     double tot = 0., r2 = 0.;
@@ -144,7 +144,7 @@ __device__ __forceinline__ double LogRhoFree(const double* dr, uint32_t n_d, dou
 }
 
 // -------------------------------------------------------------------------------------------
-// Charge-density phases (k_space_class.h:83-94, bead_class.h:323-331).
+// Charge-density phases (k_space_class.h:83-94, bead_class.h:125-133).
 
 __device__ __forceinline__ double2 CMul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 

@@ -104,7 +104,7 @@ __global__ void PairCorrelationKernel(const SystemDev sys, uint32_t sa, uint32_t
         LoadBead(sys.pos, sys.n_pad, sys.n_d, b, sys.sp_off[sa] + p, ra);
         LoadBead(sys.pos, sys.n_pad, sys.n_d, b, sys.sp_off[sb] + q, rb);
         const double r = DistMinImage(ra, rb, sys.n_d, sys.L, sys.iL);
-        // observable_class.h:384-390; a negative index wraps as the reference's unsigned cast does.
+        // observable_class.h:56-62; a negative index wraps as the reference's unsigned cast does.
         const uint32_t i = (uint32_t)(long long)rint((r - r_min) * d_ir - 0.5);
         if (i < n_r) atomicAdd(&counts[i], 1u);
     }
@@ -297,7 +297,7 @@ double Context::GetAction(uint32_t ai, uint32_t b0, uint32_t b1, const uint32_t*
         bool check = false;
         for (uint32_t i = 0; i < n; ++i) check |= (sp[i] == t.species);
         if (!check) return 0.;
-        // trap_class.h:224-229 reads the trap species' bead with every listed particle's index.
+        // trap_class.h:53-58 reads the trap species' bead with every listed particle's index.
         std::vector<uint32_t> list;
         for (uint32_t i = 0; i < n; ++i) {
             if (p[i] >= sys.sp_n[t.species]) throw PimcError(kErrArg, "particle index out of range for the trap species");

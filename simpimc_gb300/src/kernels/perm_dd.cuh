@@ -148,7 +148,7 @@ __device__ __forceinline__ dd LoadPos(const float2* pos, uint32_t np, uint32_t b
     return LoadDD(&pos[((size_t)b * 3 + d) * np + g]);
 }
 
-/// Free-particle log density of a displacement: -|dr|^2 i4 - images (free_spline_class.h:189-197).
+/// Free-particle log density of a displacement: -|dr|^2 i4 - images (free_spline_class.h:76-84).
 __device__ __forceinline__ dd LogRhoFreeDD(const dd* dr, uint32_t n_d, dd i4, const CubicDD* image, int has_images) {
     dd q{0.f, 0.f};
     for (uint32_t d = 0; d < n_d; ++d) q = Add(q, Sqr(dr[d]));

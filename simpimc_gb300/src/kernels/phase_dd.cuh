@@ -1,5 +1,5 @@
 // Double-float bead phases exp(i k x) for the charge densities (k_space_class.h:83-94,
-// bead_class.h:323-331): per-dimension rows exp(2 pi i n x / L), n = 0..max_index, and their
+// bead_class.h:125-133): per-dimension rows exp(2 pi i n x / L), n = 0..max_index, and their
 // products over dimensions for a packed k-vector.
 #pragma once
 

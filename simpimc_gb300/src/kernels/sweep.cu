@@ -338,7 +338,7 @@ __device__ __forceinline__ uint32_t LevelFirst(uint32_t nl, int lvl, uint32_t B)
 
 /// Level sums of one copy of the segment (warp-cooperative; every lane receives the totals):
 ///   lsp   = sampling log-probability of the copy's midpoints, -i4s |d|^2 - images(d)
-///           (free_spline_class.h:189-197 with tau' = tau 2^l / 2, bisect_class.h:85-94);
+///           (free_spline_class.h:76-84 with tau' = tau 2^l / 2, bisect_class.h:85-94);
 ///   small = kinetic action of the links j -> j + skip (kinetic_class.h:105-122) plus the trap
 ///           action of slices j at stride skip (trap_class.h:37-61, when lvl <= max_level).
 /// A segment spanning the whole ring (B == M) has no kinetic links: the reference walks from the
@@ -1973,7 +1973,7 @@ void Context::MoveAttempts(uint32_t m, uint64_t n) {
     Sweep(&m, &one, 1, 1);
 }
 
-// Bisect::Reset (bisect_class.h:142-155) and Move::Write/Reset (move_class.h:296-310); PathDump::Write
+// Bisect::Reset (bisect_class.h:142-155) and Move::Write/Reset (move_class.h:80-94); PathDump::Write
 // (path_dump_class.h:28-66) on every skip-th call.
 void Context::WriteBlock() {
     std::vector<double> host;
@@ -2028,7 +2028,7 @@ void Context::WriteBlock() {
     }
 }
 
-// Loop::DoEvent (loop_class.h:269-274). Consecutive move events run as one launch.
+// Loop::DoEvent (loop_class.h:55-60). Consecutive move events run as one launch.
 void Context::RunNode(const LoopNode& n) {
     bool only_moves = !n.children.empty();
     for (auto& c : n.children) only_moves &= (c.kind == 1);

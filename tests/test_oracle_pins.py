@@ -160,7 +160,7 @@ def test_ewald_potential_matches_brute_force(tmp_path):
 
 def test_kinetic_image_spline_known_answer(tmp_path):
     # Periodic box smaller than the thermal wavelength, so images matter: the kinetic action of a
-    # link equals -log of the image sum of the free propagator (free_spline_class.h:156-176).
+    # link equals -log of the image sum of the free propagator (free_spline_class.h:40-63).
     L, lam, beta, M = 2.0, 0.5, 4.0, 4
     tau = beta / M
     xml = f"""<Input><RNG seed="1"/><System n_d="3" n_bead="{M}" beta="{beta}" L="{L}" pbc="1"/>
