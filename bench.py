@@ -61,9 +61,16 @@ WORKLOAD = ("256 independent harmonic-trap Coulomb chains (omega=1, beta=2, open
 EGAS = dict(n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_units=12.0, n_level=4)
 
 
-def chains_workload(tmp):
+def rank_chain_seed0(rank):
+    """First chain seed of a rank's replica: rank r runs chains seeded SEED0 + r N_CHAINS + c, the same
+    shapes as every other rank (drawn from SEED0) but independent Markov chains, as the reference's
+    clones each draw their own seed (framework_class.h:84-101)."""
+    return SEED0 + rank * N_CHAINS
+
+
+def chains_workload(tmp, rank=0):
     from simpimc_gb300.configs import batched_trap_chains
-    return batched_trap_chains(tmp, n_chains=N_CHAINS, seed0=SEED0, n_level=CHAIN_LEVEL)
+    return batched_trap_chains(tmp, n_chains=N_CHAINS, seed0=SEED0, n_level=CHAIN_LEVEL, chain_seed0=rank_chain_seed0(rank))
 
 
 def clocks_sampler(out_path):
@@ -479,8 +486,11 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
+    if args.gpus != world:
+        raise SystemExit(f"--gpus {args.gpus} needs {args.gpus} ranks (launch with torchrun --nproc-per-node {args.gpus}); "
+                         f"WORLD_SIZE is {world}")
     tmp = tempfile.mkdtemp(prefix="pimc_bench_")
-    items = chains_workload(tmp)
+    items = chains_workload(tmp, rank)
     flat0 = np.concatenate([p.ravel() for _, p in items])
     batch = ChainBatch([x for x, _ in items], base_dir=tmp, device=local)
     batch.set_paths(flat0)

@@ -165,6 +165,14 @@ int pimc_synchronize(pimc_ctx* ctx);
 /* Tuning: CTAs of the cooperative sweep (0 = automatic) and the device wait limit. */
 int pimc_set_sweep_grid(pimc_ctx* ctx, int grid);
 int pimc_set_timeout_ns(pimc_ctx* ctx, uint64_t ns);
+/* Failure-path check of the device wait limit: one wait of the sweep's bounded grid barrier that
+ * no block can complete, limited to timeout_ns (at most 10 s). It returns PIMC_ERR_TIMEOUT with
+ * the device-measured wait in *waited_ns (may be NULL) and leaves the context usable; the path is
+ * not touched. When a real launch times out, its blocks may have committed parts of an attempt:
+ * every call that reads or moves the path then returns PIMC_ERR_STATE until
+ * pimc_set_path(ctx, 2, ...). The reference has no counterpart (its errors exit the process,
+ * actions.h:32-33). */
+int pimc_check_wait_limit(pimc_ctx* ctx, uint64_t timeout_ns, uint64_t* waited_ns);
 /* Bisection attempts in flight per round of the sweep (1..8; 0, the default, = automatic): the
  * blocks split into that many groups, and each round runs the longest prefix of the schedule's next
  * attempts in which no attempt reads what an earlier one may change (no earlier attempt's inner

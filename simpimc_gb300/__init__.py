@@ -86,6 +86,7 @@ SIGNATURES = {
     "pimc_synchronize": (C.c_int, [_P]),
     "pimc_set_sweep_grid": (C.c_int, [_P, C.c_int]),
     "pimc_set_timeout_ns": (C.c_int, [_P, C.c_uint64]),
+    "pimc_check_wait_limit": (C.c_int, [_P, C.c_uint64, _U64P]),
     "pimc_set_sweep_wave": (C.c_int, [_P, C.c_int]),
     "pimc_stream": (_P, [_P]),
     "pimc_sweep_timing": (C.c_int, [_P, C.c_int, _U64P]),
@@ -206,6 +207,13 @@ class Simulation:
 
     def set_timeout_ns(self, ns: int):
         self._check(self._lib.pimc_set_timeout_ns(self._h, ns))
+
+    def check_wait_limit(self, ns: int):
+        """One bounded device wait that nothing completes: returns (status code, device-measured
+        wait in ns). The status is PIMC_ERR_TIMEOUT (-4) when the limit works."""
+        w = C.c_uint64()
+        rc = self._lib.pimc_check_wait_limit(self._h, ns, C.byref(w))
+        return rc, w.value
 
     def synchronize(self):
         self._check(self._lib.pimc_synchronize(self._h))

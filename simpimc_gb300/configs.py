@@ -158,18 +158,19 @@ def electron_gas(workdir, *, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_unit
 
 
 def batched_trap_chains(workdir, *, n_chains=256, seed0=1000, n_range=(16, 128), bead_choices=(32, 64, 128),
-                        n_level=3, beta=2.0, omega=1.0):
-    """Independent trapped Coulomb chains with uneven sizes: chain c has seed ``seed0 + c``,
-    N drawn uniformly from ``n_range`` (inclusive) and M from ``bead_choices`` by a generator
-    seeded with ``seed0``; beads i.i.d. N(0, 1) from the chain's seed. Returns a list of
-    ``(xml_text, initial_path)``."""
+                        n_level=3, beta=2.0, omega=1.0, chain_seed0=None):
+    """Independent trapped Coulomb chains with uneven sizes: chain c has seed ``chain_seed0 + c``
+    (``chain_seed0`` defaults to ``seed0``), N drawn uniformly from ``n_range`` (inclusive) and M
+    from ``bead_choices`` by a generator seeded with ``seed0``; beads i.i.d. N(0, 1) from the
+    chain's seed. Returns a list of ``(xml_text, initial_path)``."""
+    cs0 = seed0 if chain_seed0 is None else chain_seed0
     rng = np.random.default_rng(seed0)
     ns = rng.integers(n_range[0], n_range[1] + 1, size=n_chains)
     ms = rng.choice(np.asarray(bead_choices), size=n_chains)
     out = []
     for c in range(n_chains):
         out.append(trapped_coulomb(workdir, n_part=int(ns[c]), n_bead=int(ms[c]), n_level=n_level, beta=beta,
-                                   omega=omega, seed=seed0 + c, write_table=(c == 0)))
+                                   omega=omega, seed=cs0 + c, write_table=(c == 0)))
     return out
 
 

@@ -39,9 +39,10 @@ int pimc_create(const char* xml_text, const char* base_dir, int device, uint32_t
     *out = nullptr;
     try {
         pimc::Input in = pimc::Input::FromString(xml_text);
-        auto* h = new pimc_ctx();
+        std::unique_ptr<pimc_ctx> h(new pimc_ctx());
         h->c.reset(new pimc::Context(in, base_dir ? base_dir : "", device, chain));
-        *out = h;
+        pimc::NoAllocPrepare(device);
+        *out = h.release();
         return PIMC_OK;
     } catch (const pimc::PimcError& e) {
         g_create_error = e.what();
@@ -296,6 +297,10 @@ int pimc_set_sweep_wave(pimc_ctx* ctx, int wave) {
 
 int pimc_set_timeout_ns(pimc_ctx* ctx, uint64_t ns) {
     return Guard(ctx, [&](pimc::Context& c) { c.timeout_ns = ns; });
+}
+
+int pimc_check_wait_limit(pimc_ctx* ctx, uint64_t timeout_ns, uint64_t* waited_ns) {
+    return Guard(ctx, [&](pimc::Context& c) { c.CheckWaitLimit(timeout_ns, waited_ns); });
 }
 
 void* pimc_stream(pimc_ctx* ctx) { return ctx && ctx->c ? (void*)ctx->c->stream : nullptr; }

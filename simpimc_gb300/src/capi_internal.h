@@ -7,6 +7,12 @@
 
 #include "framework/context.h"
 
+namespace pimc {
+/// Loads the no-allocation entry point's module (its fixed scratch array) and every kernel that
+/// entry point launches on `device`, so that its calls allocate nothing (noalloc.cu).
+void NoAllocPrepare(int device);
+}  // namespace pimc
+
 struct pimc_ctx {
     std::unique_ptr<pimc::Context> c;
     std::string err;

@@ -35,6 +35,8 @@ enum : int {
 };
 
 void CudaCheck(cudaError_t e, const char* what);
+/// Loads the FP64 conversion kernels of the sweep (EnsureFP64) ahead of their first launch.
+void PreloadConversionKernels();
 
 /// Owning device allocation.
 struct DeviceBuffer {
@@ -306,7 +308,14 @@ class Context {
     uint32_t* Pairs(size_t n_pairs);
     double2* RhoTmp(size_t n);
     uint32_t* Parts(size_t n);
-    void CheckDeviceError();
+    /// Reads and clears the device error word; a timeout of a launch that writes the path marks the
+    /// path as lost (path_lost) until the next pimc_set_path(ctx, 2, ...).
+    void CheckDeviceError(bool path_written = true);
+    void RequirePath() const;  // throws PIMC_ERR_STATE while path_lost
+    bool path_lost = false;
+    /// One bounded device wait that no block can complete (the sweep's grid barrier at a generation
+    /// nobody reaches); returns the device-measured wait and throws PIMC_ERR_TIMEOUT as a sweep would.
+    void CheckWaitLimit(uint64_t timeout_ns, uint64_t* waited_ns);
     void Sync();
 };
 

@@ -1004,7 +1004,7 @@ uint32_t* Context::Parts(size_t n) {
 
 void Context::Sync() { CudaCheck(cudaStreamSynchronize(stream), "stream synchronize"); }
 
-void Context::CheckDeviceError() {
+void Context::CheckDeviceError(bool path_written) {
     int e = 0;
     CudaCheck(cudaMemcpyAsync(&e, err_->ptr, sizeof(int), cudaMemcpyDeviceToHost, stream), "read error word");
     Sync();
@@ -1012,10 +1012,20 @@ void Context::CheckDeviceError() {
         int zero = 0;
         CudaCheck(cudaMemcpyAsync(err_->ptr, &zero, sizeof(int), cudaMemcpyHostToDevice, stream), "clear error word");
         Sync();
-        if (e == kDevErrTimeout) throw PimcError(kErrTimeout, "device wait timed out (grid barrier)");
+        if (e == kDevErrTimeout) {
+            // Blocks that gave up left the launch mid-attempt: some may have committed beads or
+            // densities that others did not.
+            if (path_written) path_lost = true;
+            throw PimcError(kErrTimeout, "device wait timed out (grid barrier)");
+        }
         if (e == kDevErrNonFinite) throw PimcError(kErrNonFinite, "non-finite value in the path");
         throw PimcError(kErrState, "device reported error " + std::to_string(e));
     }
+}
+
+void Context::RequirePath() const {
+    if (path_lost)
+        throw PimcError(kErrState, "the path is undefined after a launch that timed out; set it again with pimc_set_path(ctx, 2, ...)");
 }
 
 void Context::SetPath(int which, const double* h) {
@@ -1036,6 +1046,7 @@ void Context::SetPath(int which, const double* h) {
     if (which != 1) dd_valid = false;
     if (which == 2) {
         for (auto& a : actions) a.is_first_time = true;
+        path_lost = false;
         InitRhoK();
     }
 }

@@ -245,6 +245,16 @@ static uint32_t CountLinks(uint32_t b0, uint32_t b1, uint32_t skip, uint32_t M) 
     return n;
 }
 
+// The pair links of slices b0, b0 + skip, ... (ns of them) reach slice b0 + ns skip, and the
+// gradient's backward links slice b + M - skip (pair_action_class.h:281-283, 320-322). The reference
+// wraps those indices once (bead_loop, species_class.h:101) and reads past its bead array beyond
+// 2M; such ranges are refused here.
+static void CheckPairSlices(uint32_t b0, uint32_t ns, uint32_t skip, uint32_t M, bool gradient) {
+    uint64_t hi = (uint64_t)b0 + (uint64_t)ns * skip;
+    if (gradient && ns) hi = std::max<uint64_t>(hi, (uint64_t)b0 + (uint64_t)(ns - 1) * skip + M - skip);
+    if (hi >= 2ull * M) throw PimcError(kErrArg, "slice range reaches past one wrap of the ring at this level");
+}
+
 double Context::GetAction(uint32_t ai, uint32_t b0, uint32_t b1, const uint32_t* sp, const uint32_t* p, uint32_t n, uint32_t level, int mode) {
     EnsureFP64();
     if (ai >= actions.size()) throw PimcError(kErrArg, "action index out of range");
@@ -326,9 +336,10 @@ double Context::GetAction(uint32_t ai, uint32_t b0, uint32_t b1, const uint32_t*
     GenPairs(*this, pa, sp, p, n, la, lb, pairs);
     const uint32_t npairs = (uint32_t)(pairs.size() / 2);
     if (npairs == 0) return 0.;
+    const uint32_t ns = (b1 - b0 + skip - 1) / skip;
+    CheckPairSlices(b0, ns, skip, M, false);
     uint32_t* dp = Pairs(npairs);
     CudaCheck(cudaMemcpyAsync(dp, pairs.data(), pairs.size() * 4, cudaMemcpyHostToDevice, stream), "pairs upload");
-    const uint32_t ns = (b1 - b0 + skip - 1) / skip;
     const uint32_t offa = sys.sp_off[pa.sa], offb = sys.sp_off[pa.sb];
     const double tau = sys.tau;
     double tot = 0.;
@@ -464,9 +475,10 @@ void Context::GetActionGradient(uint32_t ai, uint32_t b0, uint32_t b1, const uin
     GenPairs(*this, pa, sp, p, n, la, lb, pairs);
     const uint32_t npairs = (uint32_t)(pairs.size() / 2);
     if (npairs == 0) return;
+    const uint32_t ns = (b1 - b0 + skip - 1) / skip;
+    CheckPairSlices(b0, ns, skip, M, true);
     uint32_t* dp = Pairs(npairs);
     CudaCheck(cudaMemcpyAsync(dp, pairs.data(), pairs.size() * 4, cudaMemcpyHostToDevice, stream), "pairs upload");
-    const uint32_t ns = (b1 - b0 + skip - 1) / skip;
     const uint32_t offa = sys.sp_off[pa.sa], offb = sys.sp_off[pa.sb];
     const double tau = sys.tau;
     if (pa.kind == kPairIlkka) {

@@ -1165,6 +1165,7 @@ __device__ __forceinline__ void Split53(uint32_t w0, uint32_t w1, dd& u) {
 // ---------------------------------------------------------------------------------------------
 
 void Context::EnsureDD() {
+    RequirePath();
     if (dd_valid) return;
     const size_t n_pos = (size_t)sys.M * 3 * sys.n_pad;
     const size_t n_rho = (rho_slots && sys.K) ? (size_t)rho_slots * sys.M * sys.K : 0;
@@ -1189,7 +1190,14 @@ void Context::SetPrecision(int bits) {
     dd_valid = false;
 }
 
+void PreloadConversionKernels() {
+    cudaFuncAttributes fa;
+    CudaCheck(cudaFuncGetAttributes(&fa, FromDDKernel), "loading FromDDKernel");
+    CudaCheck(cudaFuncGetAttributes(&fa, FromF32Kernel), "loading FromF32Kernel");
+}
+
 void Context::EnsureFP64() {
+    RequirePath();
     if (fp64_valid) return;
     const size_t n_pos = (size_t)sys.M * 3 * sys.n_pad;
     const size_t n_rho = (rho_slots && sys.K) ? (size_t)rho_slots * sys.M * sys.K : 0;
@@ -1513,8 +1521,31 @@ void Context::RequireLevelZeroDensities(uint32_t m) const {
     }
 }
 
+// Every block arrives once at generation 1 of a fresh counter and waits for generation 2, which no
+// block reaches: the wait ends only by its time limit (or the iteration cap) and sets the error word.
+__global__ void WaitLimitKernel(unsigned long long* ctr, int* err, uint64_t timeout_ns, unsigned long long* waited) {
+    const uint64_t t0 = GlobalTimerNs();
+    GridBarrier(ctr, 2, err, timeout_ns);
+    if (threadIdx.x == 0) atomicMax(waited, (unsigned long long)(GlobalTimerNs() - t0));
+}
+
+void Context::CheckWaitLimit(uint64_t timeout_ns, uint64_t* waited_ns) {
+    if (timeout_ns > 10000000000ull) throw PimcError(kErrArg, "wait limit above 10 s");
+    unsigned long long* w = reinterpret_cast<unsigned long long*>(Result());
+    CudaCheck(cudaMemsetAsync(Barrier(), 0, sizeof(unsigned long long), stream), "reset barrier");
+    CudaCheck(cudaMemsetAsync(w, 0, sizeof(unsigned long long), stream), "reset wait");
+    WaitLimitKernel<<<2, 32, 0, stream>>>(Barrier(), ErrWord(), timeout_ns, w);
+    CudaCheck(cudaGetLastError(), "wait-limit launch");
+    unsigned long long h = 0;
+    CudaCheck(cudaMemcpyAsync(&h, w, sizeof(h), cudaMemcpyDeviceToHost, stream), "read wait");
+    Sync();
+    if (waited_ns) *waited_ns = h;
+    CheckDeviceError(false);
+}
+
 void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep) {
     if (n_entries == 0 || n_rep == 0) return;
+    RequirePath();
     if (n_entries > 1024) throw PimcError(kErrArg, "schedule longer than 1024 entries");
     for (uint32_t e = 0; e < n_entries; ++e) {
         if (mv[e] >= moves.size()) throw PimcError(kErrArg, "move index out of range");
@@ -1915,13 +1946,6 @@ void SweepChains(const std::vector<Context*>& cs, const uint32_t* mv, const uint
             before[mv[e]] += counts[e];
             stride[ci * n_entries + e] = per_rep[mv[e]];
         }
-        for (uint32_t e = 0; e < n_entries; ++e) {
-            MoveHost& mh = c.moves[mv[e]];
-            mh.attempts += counts[e] * n_rep;
-            mh.block_attempt += counts[e] * n_rep;
-            c.perm_pending_ |= 1u << mv[e];
-        }
-        c.fp64_valid = false;
         c.Sync();  // the double-float copies each context prepared on its own stream
     }
     Context& c0 = *cs[0];
@@ -1930,6 +1954,16 @@ void SweepChains(const std::vector<Context*>& cs, const uint32_t* mv, const uint
     if (!optin) optin = PermSmemOptin(c0.device);
     if (smem > (size_t)optin) throw PimcError(kErrUnsupported, "permutation kernel shared memory above the device limit");
     DeviceBuffer dargs(args.size() * sizeof(PermArgsDD) + stride.size() * sizeof(uint64_t));
+    // The counters change only once nothing can refuse the launch any more.
+    for (Context* cp : cs) {
+        for (uint32_t e = 0; e < n_entries; ++e) {
+            MoveHost& mh = cp->moves[mv[e]];
+            mh.attempts += counts[e] * n_rep;
+            mh.block_attempt += counts[e] * n_rep;
+            cp->perm_pending_ |= 1u << mv[e];
+        }
+        cp->fp64_valid = false;
+    }
     CudaCheck(cudaMemcpyAsync(dargs.ptr, args.data(), args.size() * sizeof(PermArgsDD), cudaMemcpyHostToDevice, c0.stream), "chain arguments");
     uint64_t* dstride = reinterpret_cast<uint64_t*>(dargs.as<char>() + args.size() * sizeof(PermArgsDD));
     CudaCheck(cudaMemcpyAsync(dstride, stride.data(), stride.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, c0.stream), "chain arguments");

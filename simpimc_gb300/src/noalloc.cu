@@ -8,20 +8,20 @@
 // every temporary (pair list, particle lists, the proposal's charge densities, the reduction
 // partials and the result slot) in one fixed device array declared in this file.
 //
-// The array is kNoAllocScratchBytes = 4 MiB. Every GPU that loads the library holds it until the
-// process exits. A request needs, each part rounded up to 256 bytes: 8 bytes per particle pair,
-// 4 bytes per listed particle, 16 bytes per (slice, k-vector) and species for NEW-mode
-// long-range actions, and 8 bytes per reduction block plus 64 bytes; anything larger is refused
-// with PIMC_ERR_ARG and a message stating the need.
+// The array is kNoAllocScratchBytes = 4 MiB. CUDA loads a module's device variables and kernels
+// lazily by default, so pimc_create calls NoAllocPrepare: it looks up the array's address (which
+// loads this file's module and so places the array on the GPU) and loads every kernel the entry
+// point launches, including the FP64 conversion kernels of the sweep. From then on the GPU holds
+// the array until the process exits, and a call allocates nothing. A request needs, each part
+// rounded up to 256 bytes: 8 bytes per particle pair, 4 bytes per listed particle, 16 bytes per
+// (slice, k-vector) and species for NEW-mode long-range actions, and 8 bytes per reduction block
+// plus 64 bytes; anything larger is refused with PIMC_ERR_ARG and a message stating the need.
 //
 // All calls share the array and it keeps whatever the last call left in it. Nothing in it has to
 // start at zero: every region is fully written before it is read. Two calls whose GPU work
 // overlaps (for example from two contexts on one device, driven by different host threads) race
 // on the array; calls on one context are serialised by its stream and by the synchronisation at
 // the end of each call.
-//
-// The first call on a device looks up the array's device address (cudaGetSymbolAddress) with that
-// device current and caches it; make that first call before capturing any stream.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -116,6 +116,51 @@ __global__ void NoAllocProposalRhoKernel(const pimc::SystemDev sys, uint32_t spe
     }
 }
 
+// One (slice, pair) link of PairAction::GetAction (pair_action_class.h:278-289).
+struct NoAllocPairTerm {
+    pimc::PairDev pa;
+    const double* pos;
+    const uint32_t* pairs;
+    uint32_t npairs, b0, skip, M, n_d, np, offa, offb, level;
+    double L, iL, tau;
+    __device__ double operator()(uint64_t i) const {
+        const uint32_t j = (uint32_t)(i / npairs), q = (uint32_t)(i % npairs);
+        const uint32_t bi = Loop(b0 + j * skip, M), bj = Loop(b0 + j * skip + skip, M);
+        double A0[3], C0[3], A1[3], C1[3];
+        pimc::LoadBead(pos, np, n_d, bi, offb + pairs[2 * q + 1], A0);
+        pimc::LoadBead(pos, np, n_d, bi, offa + pairs[2 * q], C0);
+        pimc::LoadBead(pos, np, n_d, bj, offb + pairs[2 * q + 1], A1);
+        pimc::LoadBead(pos, np, n_d, bj, offa + pairs[2 * q], C1);
+        double r, rp, s;
+        pimc::DrDrpDrrp(A0, C0, A1, C1, n_d, L, iL, r, rp, s);
+        return pimc::PairU(pa, r, rp, s, level, tau);
+    }
+};
+
+// One (k-vector, slice) term of the long-range sum v_k Re(rho_a conj(rho_b)) (bare_pair_action_class.h:
+// 126-144): from the proposal densities `ra`/`rb` (NEW mode) or the committed per-slice densities.
+struct NoAllocLongTerm {
+    const double2* ra;
+    const double2* rb;
+    const double2* rho;
+    const double* vk;
+    uint32_t K, ns, b0, skip, M;
+    int slot_a, slot_b;
+    __device__ double operator()(uint64_t i) const {
+        const uint32_t k = (uint32_t)(i / ns), j = (uint32_t)(i % ns);
+        double2 a, b;
+        if (ra) {
+            a = ra[(size_t)j * K + k];
+            b = rb[(size_t)j * K + k];
+        } else {
+            const uint32_t bb = Loop(b0 + j * skip, M);
+            a = rho[((size_t)slot_a * M + bb) * K + k];
+            b = rho[((size_t)slot_b * M + bb) * K + k];
+        }
+        return vk[k] * (a.x * b.x + a.y * b.y);
+    }
+};
+
 /// Sum f over [0, n) into *result using `partials` (capacity `cap` doubles) in the scratch array.
 template <class F>
 double NoAllocSum(pimc::Context& c, uint64_t n, F f, double* partials, size_t cap, double* result) {
@@ -179,6 +224,10 @@ double GetActionNoAlloc(pimc::Context& c, uint32_t ai, uint32_t b0, uint32_t b1,
     if (npairs == 0) return 0.;
     const uint32_t skip = 1u << level;
     const uint32_t ns = (b1 - b0 + skip - 1) / skip;
+    // The last link's far slice, b0 + ns skip, must lie within one wrap of the ring: the reference's
+    // bead_loop subtracts M once (species_class.h:101), so beyond that it reads past its bead array.
+    if ((uint64_t)b0 + (uint64_t)ns * skip >= 2ull * sys.M)
+        throw PimcError(PIMC_ERR_ARG, "slice range reaches past one wrap of the ring at this level");
     const bool lr_new = pa.use_long_range && mode;
     const int n_species = pa.sa == pa.sb ? 1 : 2;
 
@@ -213,18 +262,23 @@ double GetActionNoAlloc(pimc::Context& c, uint32_t ai, uint32_t b0, uint32_t b1,
     const uint32_t M = sys.M, n_d = sys.n_d, np = sys.n_pad;
     const double L = sys.L, iL = sys.iL, tau = sys.tau;
     const uint32_t offa = sys.sp_off[pa.sa], offb = sys.sp_off[pa.sb];
-    double tot = NoAllocSum(c, (uint64_t)ns * npairs, [=] __device__(uint64_t i) -> double {
-        const uint32_t j = (uint32_t)(i / npairs), q = (uint32_t)(i % npairs);
-        const uint32_t bi = Loop(b0 + j * skip, M), bj = Loop(b0 + j * skip + skip, M);
-        double A0[3], C0[3], A1[3], C1[3];
-        pimc::LoadBead(pos, np, n_d, bi, offb + dp[2 * q + 1], A0);
-        pimc::LoadBead(pos, np, n_d, bi, offa + dp[2 * q], C0);
-        pimc::LoadBead(pos, np, n_d, bj, offb + dp[2 * q + 1], A1);
-        pimc::LoadBead(pos, np, n_d, bj, offa + dp[2 * q], C1);
-        double r, rp, s;
-        pimc::DrDrpDrrp(A0, C0, A1, C1, n_d, L, iL, r, rp, s);
-        return pimc::PairU(pa, r, rp, s, level, tau);
-    }, partials, max_blocks, result);
+    NoAllocPairTerm pt;
+    pt.pa = pa;
+    pt.pos = pos;
+    pt.pairs = dp;
+    pt.npairs = npairs;
+    pt.b0 = b0;
+    pt.skip = skip;
+    pt.M = M;
+    pt.n_d = n_d;
+    pt.np = np;
+    pt.offa = offa;
+    pt.offb = offb;
+    pt.level = level;
+    pt.L = L;
+    pt.iL = iL;
+    pt.tau = tau;
+    double tot = NoAllocSum(c, (uint64_t)ns * npairs, pt, partials, max_blocks, result);
 
     if (pa.use_long_range) {
         const uint32_t K = sys.K;
@@ -243,22 +297,19 @@ double GetActionNoAlloc(pimc::Context& c, uint32_t ai, uint32_t b0, uint32_t b1,
             ra = tmp;
             rb = n_species == 1 ? tmp : tmp + (size_t)ns * K;
         }
-        const double2* rho = sys.rho_k;
-        const int slot_a = sys.sp_rho[pa.sa], slot_b = sys.sp_rho[pa.sb];
-        const double* vk = pa.kind != pimc::kPairBare ? pa.u_long_k : pa.v_long_k;
-        double lr = NoAllocSum(c, (uint64_t)K * ns, [=] __device__(uint64_t i) -> double {
-            const uint32_t k = (uint32_t)(i / ns), j = (uint32_t)(i % ns);
-            double2 a, b;
-            if (ra) {
-                a = ra[(size_t)j * K + k];
-                b = rb[(size_t)j * K + k];
-            } else {
-                const uint32_t bb = Loop(b0 + j * skip, M);
-                a = rho[((size_t)slot_a * M + bb) * K + k];
-                b = rho[((size_t)slot_b * M + bb) * K + k];
-            }
-            return vk[k] * (a.x * b.x + a.y * b.y);
-        }, partials, max_blocks, result);
+        NoAllocLongTerm lt;
+        lt.ra = ra;
+        lt.rb = rb;
+        lt.rho = sys.rho_k;
+        lt.vk = pa.kind != pimc::kPairBare ? pa.u_long_k : pa.v_long_k;
+        lt.K = K;
+        lt.ns = ns;
+        lt.b0 = b0;
+        lt.skip = skip;
+        lt.M = M;
+        lt.slot_a = sys.sp_rho[pa.sa];
+        lt.slot_b = sys.sp_rho[pa.sb];
+        double lr = NoAllocSum(c, (uint64_t)K * ns, lt, partials, max_blocks, result);
         if (pa.sa != pa.sb) lr *= 2.;
         tot += pa.kind != pimc::kPairBare ? lr : skip * sys.tau * lr;
     }
@@ -266,6 +317,37 @@ double GetActionNoAlloc(pimc::Context& c, uint32_t ai, uint32_t b0, uint32_t b1,
 }
 
 }  // namespace
+
+namespace pimc {
+
+void NoAllocPrepare(int device) {
+    static bool prepared[kNoAllocMaxDevices] = {false};
+    ScratchAddress(device);  // loads this file's module: the scratch array is placed on the GPU here
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (prepared[device]) return;
+    int prev = 0;
+    CudaCheck(cudaGetDevice(&prev), "cudaGetDevice");
+    CudaCheck(cudaSetDevice(device), "cudaSetDevice");
+    // cudaFuncGetAttributes loads a kernel that lazy loading would otherwise load at its first launch.
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, NoAllocSumKernel<NoAllocPairTerm>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, NoAllocSumKernel<NoAllocLongTerm>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, NoAllocFinalKernel);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, NoAllocProposalRhoKernel);
+    if (e == cudaSuccess) {
+        try {
+            PreloadConversionKernels();
+        } catch (...) {
+            cudaSetDevice(prev);
+            throw;
+        }
+    }
+    cudaSetDevice(prev);
+    CudaCheck(e, "loading the no-allocation kernels");
+    prepared[device] = true;
+}
+
+}  // namespace pimc
 
 extern "C" int pimc_get_action_noalloc(pimc_ctx* ctx, uint32_t action, uint32_t b0, uint32_t b1, const uint32_t* species,
                                        const uint32_t* particles, uint32_t n_particles, uint32_t level, int mode, double* out) {

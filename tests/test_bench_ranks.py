@@ -1,7 +1,8 @@
 """Multi-process (replica) logic of bench.py on CPU: world size 2 over gloo on 127.0.0.1.
 
-Chains are independent Markov chains, one per GPU (the reference's MPI clones,
-framework_class.h:44-53): the only collective is the maximum of the per-rank timings."""
+Chains are independent Markov chains, one set per GPU (the reference's MPI clones,
+framework_class.h:44-53): the only collective is the maximum of the per-rank timings, and every
+rank runs its own chains, with seeds no other rank uses."""
 import os
 import socket
 
@@ -41,6 +42,45 @@ def test_reduce_max_over_two_ranks():
         p.join(120)
         assert p.exitcode == 0
     assert out[0] == out[1] == [2.0, 10.0, 3.0]
+
+
+def _seed_worker(rank, world, port, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import re
+    import tempfile
+
+    import bench
+    with tempfile.TemporaryDirectory() as d:
+        items = bench.chains_workload(d, int(os.environ["RANK"]))
+        seeds = [int(re.search(r'<RNG seed="(\d+)"', x).group(1)) for x, _ in items]
+        shapes = [p.shape for _, p in items]
+        first = items[0][1][0, 0].tolist()
+    gathered = [None] * world
+    dist.all_gather_object(gathered, seeds)
+    out[rank] = (seeds, shapes, first, gathered)
+    dist.destroy_process_group()
+
+
+def test_ranks_run_disjoint_chains():
+    """Rank r's replica: the same chain shapes on every rank, chain seeds SEED0 + r N_CHAINS + c."""
+    ctx = mp.get_context("spawn")
+    manager = ctx.Manager()
+    out = manager.dict()
+    port = _free_port()
+    procs = [ctx.Process(target=_seed_worker, args=(r, 2, port, out)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(300)
+        assert p.exitcode == 0
+    s0, sh0, f0, g0 = out[0]
+    s1, sh1, f1, _ = out[1]
+    assert len(s0) == len(s1) == 256
+    assert not set(s0) & set(s1)
+    assert g0[0] == s0 and g0[1] == s1
+    assert sh0 == sh1
+    assert f0 != f1  # different starting beads
 
 
 def test_single_process_is_identity():
