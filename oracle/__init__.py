@@ -25,8 +25,10 @@ def build(force: bool = False) -> Path:
     LIB.parent.mkdir(exist_ok=True)
     if force or not LIB.exists() or any(d.stat().st_mtime > LIB.stat().st_mtime for d in DEPS):
         cxx = os.environ.get("CXX") or shutil.which("g++") or "c++"
-        cmd = [cxx, "-std=c++17", "-O3", "-ffp-contract=off", "-fPIC", "-shared", str(SRC), "-o", str(LIB)]
+        cmd = [cxx, "-std=c++17", "-O3", "-ffp-contract=off", "-fPIC", "-shared", "-fopenmp", str(SRC), "-o", str(LIB)]
         r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:  # without OpenMP the lean-density sums run on one thread
+            r = subprocess.run([c for c in cmd if c != "-fopenmp"], capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"oracle build failed:\n{r.stderr}")
     return LIB
@@ -73,6 +75,7 @@ def lib():
             "oracle_perm_stats": [C.c_void_p, C.c_uint32, _U64P],
             "oracle_get_perm": [C.c_void_p, C.c_uint32, _U32P],
             "oracle_set_perm": [C.c_void_p, C.c_uint32, _U32P],
+            "oracle_set_lean_densities": [C.c_int],
         }.items():
             fn = getattr(L, name)
             fn.argtypes = args
@@ -106,12 +109,21 @@ def philox(ctr, key):
 
 
 class OracleSim:
-    """Same surface as simpimc_gb300.Simulation, evaluated by the CPU restatement."""
+    """Same surface as simpimc_gb300.Simulation, evaluated by the CPU restatement.
 
-    def __init__(self, xml: str, base_dir=".", chain: int = 0):
+    lean_densities=True keeps only the per-slice charge densities and recomputes each bead's density
+    from its position (identical results; needed where the reference's per-bead storage, N M K
+    complex numbers twice, does not fit in host memory)."""
+
+    def __init__(self, xml: str, base_dir=".", chain: int = 0, lean_densities: bool = False):
         L = lib()
         h = C.c_void_p()
-        if L.oracle_create(xml.encode(), str(base_dir).encode(), chain, C.byref(h)) != 0:
+        L.oracle_set_lean_densities(1 if lean_densities else 0)
+        try:
+            rc = L.oracle_create(xml.encode(), str(base_dir).encode(), chain, C.byref(h))
+        finally:
+            L.oracle_set_lean_densities(0)
+        if rc != 0:
             raise RuntimeError(L.oracle_last_error().decode())
         self._L, self._h = L, h
         info = np.zeros(8, dtype=np.uint32)
@@ -246,11 +258,12 @@ class OracleSim:
 
     def blocks(self, obs, cap=1 << 20):
         n = C.c_uint64()
-        self._L.oracle_n_blocks(self._h, obs, C.byref(n))
+        if self._L.oracle_n_blocks(self._h, obs, C.byref(n)) != 0:
+            raise IndexError(f"observable {obs} out of range")
         buf = np.zeros(cap, dtype=np.float64)
         out = []
         for b in range(n.value):
             m = C.c_uint64()
-            self._L.oracle_get_block(self._h, obs, b, buf.ctypes.data_as(_DP), cap, C.byref(m))
+            self._ok(self._L.oracle_get_block(self._h, obs, b, buf.ctypes.data_as(_DP), cap, C.byref(m)))
             out.append(buf[: m.value].copy())
         return out

@@ -338,15 +338,16 @@ struct KSpace {
     }
 
     // k_space_class.h:83-94.
-    void CalcC(const double* r) {
+    void CalcC(const double* r) { CalcCInto(r, c_k); }
+    void CalcCInto(const double* r, std::vector<std::vector<cplx>>& ck) const {
         for (uint32_t d = 0; d < box.size(); ++d) {
             double phi = r[d] * box[d];
             cplx t(std::cos(phi), std::sin(phi));
             int m = max_index[d];
-            c_k[d][m] = 1.;
+            ck[d][m] = 1.;
             for (int k = 1; k <= m; ++k) {
-                c_k[d][m + k] = t * c_k[d][m + k - 1];
-                c_k[d][m - k] = std::conj(c_k[d][m + k]);
+                ck[d][m + k] = t * ck[d][m + k - 1];
+                ck[d][m - k] = std::conj(ck[d][m + k]);
             }
         }
     }
@@ -378,8 +379,18 @@ struct Species {
     uint32_t bead_loop(uint32_t b) const { return b >= n_bead ? b - n_bead : b; }  // species_class.h:101
 };
 
+// Lean densities (no reference counterpart; a memory option of this oracle): the reference keeps every
+// bead's density and its copy (bead_class.h:20-21), N M K complex numbers twice, which is 426 GB for
+// N = 1024, M = 512, K = 25398. With lean densities on, a Path keeps only the per-slice densities
+// and recomputes a bead's density from its position wherever the reference reads the stored one.
+// The stored density always equals CalcRhoK of the bead's position of that copy, so the results are
+// identical bit for bit. The per-slice sums at initialisation run over slices in parallel (OpenMP),
+// each slice summing its particles in order as the reference does. Set before oracle_create.
+static bool g_lean_densities = false;
+
 struct Path {
     uint32_t n_d = 3, n_bead = 0;
+    bool lean_rho = g_lean_densities;
     double beta = 0., L = 0., iL = 0., vol = 1., tau = 0.;
     bool pbc = true;
     Mode mode = NEW_MODE;
@@ -550,8 +561,27 @@ struct Path {
         }
     }
 
-    cplx* BeadRhoK(Species& s, uint32_t p, uint32_t b, Mode m) {
+    // Density of bead (p, b) of copy m from its position, into `out` with the caller's phase tables.
+    void BeadRhoKAt(Species& s, uint32_t p, uint32_t b, Mode m, cplx* out, std::vector<std::vector<cplx>>& ck) const {
+        const double* rr = (m == NEW_MODE ? r.data() : r_c.data()) + ((size_t)(s.offset + p) * n_bead + s.bead_loop(b)) * n_d;
+        ks.CalcCInto(rr, ck);
+        for (size_t k = 0; k < ks.K(); ++k) {
+            cplx f = 1.;
+            for (uint32_t d = 0; d < ks.n_d; ++d) f *= ck[d][ks.indices[k][d]];
+            out[k] = f;
+        }
+    }
+
+    // The stored density of bead (p, b) of copy m; with lean densities, recomputed into `tmp`.
+    cplx* BeadRhoK(Species& s, uint32_t p, uint32_t b, Mode m, std::vector<cplx>* tmp = nullptr) {
         size_t K = ks.K();
+        if (lean_rho) {
+            if (!tmp) throw std::logic_error("lean densities need a buffer");
+            tmp->resize(K);
+            std::vector<std::vector<cplx>> ck = ks.c_k;
+            BeadRhoKAt(s, p, b, m, tmp->data(), ck);
+            return tmp->data();
+        }
         size_t off = ((size_t)p * n_bead + s.bead_loop(b)) * K;
         return (m == NEW_MODE ? s.bead_rho_k.data() : s.bead_rho_k_c.data()) + off;
     }
@@ -560,6 +590,25 @@ struct Path {
     void InitRhoK(Species& s) {
         size_t K = ks.K();
         s.rho_k.assign((size_t)n_bead * K, cplx(0., 0.));
+        if (lean_rho && K) {
+            std::vector<cplx>().swap(s.bead_rho_k);
+            std::vector<cplx>().swap(s.bead_rho_k_c);
+#pragma omp parallel
+            {
+                std::vector<std::vector<cplx>> ck = ks.c_k;
+                std::vector<cplx> br(K);
+#pragma omp for schedule(dynamic, 1)
+                for (int64_t b = 0; b < (int64_t)n_bead; ++b) {
+                    cplx* sr = &s.rho_k[(size_t)b * K];
+                    for (uint32_t p = 0; p < s.n_part; ++p) {
+                        BeadRhoKAt(s, p, (uint32_t)b, NEW_MODE, br.data(), ck);
+                        for (size_t k = 0; k < K; ++k) sr[k] += br[k];
+                    }
+                }
+            }
+            s.rho_k_c = s.rho_k;
+            return;
+        }
         s.bead_rho_k.assign((size_t)s.n_part * n_bead * K, cplx(0., 0.));
         if (K == 0) {
             s.rho_k_c = s.rho_k;
@@ -589,11 +638,12 @@ struct Path {
             uint32_t bb = s.bead_loop(b);
             std::copy(s.rho_k_c.begin() + (size_t)bb * K, s.rho_k_c.begin() + (size_t)(bb + 1) * K, s.rho_k.begin() + (size_t)bb * K);
         }
+        std::vector<cplx> tn, to;
         for (uint32_t p : parts) {
             for (uint32_t b = b0; b < b1; b += skip) {
-                cplx* nw = BeadRhoK(s, p, b, NEW_MODE);
-                CalcBeadRhoK(s, p, b, nw);
-                const cplx* od = BeadRhoK(s, p, b, OLD_MODE);
+                cplx* nw = BeadRhoK(s, p, b, NEW_MODE, &tn);
+                if (!lean_rho) CalcBeadRhoK(s, p, b, nw);  // lean: already formed from the NEW position
+                const cplx* od = BeadRhoK(s, p, b, OLD_MODE, &to);
                 cplx* sr = &s.rho_k[(size_t)s.bead_loop(b) * K];
                 for (size_t k = 0; k < K; ++k) sr[k] += nw[k] - od[k];
             }
@@ -1338,8 +1388,9 @@ struct IlkkaPairAction : PairAction {
         size_t K = path.ks.K();
         uint32_t skip = 1u << level;
         double tot[3] = {0., 0., 0.};
+        std::vector<cplx> tmp;
         for (uint32_t b = b0; b < b1; b += skip) {
-            const cplx* ri = path.BeadRhoK(*species_a, pi, b, path.mode);
+            const cplx* ri = path.BeadRhoK(*species_a, pi, b, path.mode, &tmp);
             for (size_t k = 0; k < K; ++k) {
                 const cplx& rbk = rb[(size_t)species_b->bead_loop(b) * K + k];
                 double f = u_long_k[k] * (ri[k].real() * rbk.imag() - ri[k].imag() * rbk.real());
@@ -1389,9 +1440,12 @@ struct DavidPairAction : PairAction {
             if (d.size() < (size_t)n_val * n_grid * n_tau || V.size() != n_grid) throw InputError("table '" + file + "': short " + key);
             out.assign(n_tau, std::vector<Spline>(n_val + 1));
             std::vector<double> col(n_grid);
+            // :262-271 fill the grid points below the last one only (the zeroing of the last one is
+            // commented out); the zero-initialised arrays leave zero there for every component.
             for (size_t l = 0; l < n_tau; ++l)
                 for (uint32_t v = 0; v <= n_val; ++v) {
-                    for (size_t g = 0; g < n_grid; ++g) col[g] = v == 0 ? V[g] : d[(v - 1) + g * n_val + l * n_val * n_grid];
+                    for (size_t g = 0; g < n_grid; ++g)
+                        col[g] = g + 1 == n_grid ? 0. : v == 0 ? V[g] : d[(v - 1) + g * n_val + l * n_val * n_grid];
                     out[l][v].Build(grid, col, false);
                 }
         };
@@ -1865,7 +1919,7 @@ struct Bisect : Move {
             double* r = path.GetRMode(*species, pb.first, pb.second, NEW_MODE);
             double* rc = path.GetRMode(*species, pb.first, pb.second, OLD_MODE);
             std::copy(r, r + path.n_d, rc);
-            if (K) {
+            if (K && !path.lean_rho) {
                 cplx* nw = path.BeadRhoK(*species, pb.first, pb.second, NEW_MODE);
                 cplx* od = path.BeadRhoK(*species, pb.first, pb.second, OLD_MODE);
                 std::copy(nw, nw + K, od);
@@ -1886,7 +1940,7 @@ struct Bisect : Move {
             double* r = path.GetRMode(*species, pb.first, pb.second, NEW_MODE);
             double* rc = path.GetRMode(*species, pb.first, pb.second, OLD_MODE);
             std::copy(rc, rc + path.n_d, r);
-            if (K) {
+            if (K && !path.lean_rho) {
                 cplx* nw = path.BeadRhoK(*species, pb.first, pb.second, NEW_MODE);
                 cplx* od = path.BeadRhoK(*species, pb.first, pb.second, OLD_MODE);
                 std::copy(od, od + K, nw);
@@ -2166,7 +2220,7 @@ struct PermBisect : Bisect {
                 const uint32_t q = src[(size_t)p * M + b];
                 std::copy(r0.begin() + path.Idx(*species, q, b), r0.begin() + path.Idx(*species, q, b) + nd, path.r.begin() + path.Idx(*species, p, b));
                 std::copy(rc0.begin() + path.Idx(*species, q, b), rc0.begin() + path.Idx(*species, q, b) + nd, path.r_c.begin() + path.Idx(*species, p, b));
-                if (K) {
+                if (K && !path.lean_rho) {
                     std::copy(k0.begin() + ((size_t)q * M + b) * K, k0.begin() + ((size_t)q * M + b + 1) * K, species->bead_rho_k.begin() + ((size_t)p * M + b) * K);
                     std::copy(kc0.begin() + ((size_t)q * M + b) * K, kc0.begin() + ((size_t)q * M + b + 1) * K, species->bead_rho_k_c.begin() + ((size_t)p * M + b) * K);
                 }
@@ -3043,12 +3097,14 @@ int oracle_run(void* h) {
 }
 
 int oracle_n_blocks(void* h, uint32_t o, uint64_t* n) {
-    *n = S(h)->blocks.at(o).size();
+    if (o >= S(h)->blocks.size()) return -1;
+    *n = S(h)->blocks[o].size();
     return 0;
 }
 
 int oracle_get_block(void* h, uint32_t o, uint64_t blk, double* out, uint64_t cap, uint64_t* n) {
-    const auto& v = S(h)->blocks.at(o).at(blk);
+    if (o >= S(h)->blocks.size() || blk >= S(h)->blocks[o].size()) return -1;
+    const auto& v = S(h)->blocks[o][blk];
     *n = v.size();
     for (size_t i = 0; i < v.size() && i < cap; ++i) out[i] = v[i];
     return 0;
@@ -3070,6 +3126,12 @@ int oracle_bisect_draws(uint32_t seed, uint32_t chain, uint32_t move, uint64_t a
         orc::boxmuller(w.w[2], w.w[3], z[3 * i + 2], z3);
     }
     for (uint32_t li = 0; li < n_level; ++li) logu[li] = orc::logf_spec(orc::u24(st.block(1u + (B - 1u) + li).w[0]));
+    return 0;
+}
+
+// Lean densities for every sim created afterwards (see g_lean_densities).
+int oracle_set_lean_densities(int on) {
+    orc::g_lean_densities = on != 0;
     return 0;
 }
 

@@ -29,7 +29,7 @@ from .tables import coulomb_table, david_table, ilkka_table
 
 def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_level=3, seed=1234, coulomb=True,
                     n_step_inner=100, n_step_outer=10, gr_bins=200, gr_rmax=5.0, virial=False, path_seed=None,
-                    write_table=True, pair="BarePairAction", n_order=2, pair_max_level=0):
+                    write_table=True, pair="BarePairAction", n_order=2, pair_max_level=0, adaptive=False, target_ratio=0.5):
     workdir = Path(workdir)
     workdir.mkdir(parents=True, exist_ok=True)
     if pair == "DavidPairAction":
@@ -53,6 +53,7 @@ def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_leve
     pair = pair_xml if coulomb else ""
     energy = ('<Observable name="Energy" type="Energy" use_virial_estimator="1" />' if virial
               else '<Observable name="Energy" type="Energy" />')
+    adapt = f' adaptive="1" target_ratio="{target_ratio!r}"' if adaptive else ""
     xml = f"""<Input>
   <RNG seed="{seed}" />
   <IO output_prefix="trap" />
@@ -67,7 +68,7 @@ def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_leve
     {pair}
   </Actions>
   <Moves>
-    <Move name="Bisect" type="Bisect" species="e" n_level="{n_level}" />
+    <Move name="Bisect" type="Bisect" species="e" n_level="{n_level}"{adapt} />
   </Moves>
   <Observables>
     {energy}
@@ -92,7 +93,7 @@ def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_leve
 
 def electron_gas(workdir, *, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_units=12.0, n_level=4, seed=4321,
                  n_step_inner=10, n_step_outer=4, path_seed=None, structure_factor=False, pair="BarePairAction", n_order=2,
-                 pair_max_level=0):
+                 pair_max_level=0, n_images=0):
     workdir = Path(workdir)
     workdir.mkdir(parents=True, exist_ok=True)
     L = (4.0 * math.pi * n_part / 3.0) ** (1.0 / 3.0) * rs
@@ -112,6 +113,7 @@ def electron_gas(workdir, *, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_unit
 
     n_up = n_part // 2
     n_dn = n_part - n_up
+    img = f' n_images="{n_images}"' if n_images else ""
     sk = ('<Observable name="sk" type="StructureFactor" species_a="eU" species_b="eU" />' if structure_factor else "")
     xml = f"""<Input>
   <RNG seed="{seed}" />
@@ -123,15 +125,15 @@ def electron_gas(workdir, *, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_unit
     <Species name="eD" n_part="{n_dn}" lambda="0.5" fermi="0" init_type="File" file_name="init.xyz" all_beads="1" />
   </Particles>
   <Actions>
-    <Action name="KineticU" type="Kinetic" n_images="0" species="eU" />
-    <Action name="KineticD" type="Kinetic" n_images="0" species="eD" />
+    <Action name="KineticU" type="Kinetic" n_images="{n_images}" species="eU" />
+    <Action name="KineticD" type="Kinetic" n_images="{n_images}" species="eD" />
     <Action name="CoulombUU" type="{pair}" file="{tab.name}"{extra} species_a="eU" species_b="eU" max_level="{pair_max_level}" use_long_range="1" />
     <Action name="CoulombDD" type="{pair}" file="{tab.name}"{extra} species_a="eD" species_b="eD" max_level="{pair_max_level}" use_long_range="1" />
     <Action name="CoulombUD" type="{pair}" file="{tab.name}"{extra} species_a="eU" species_b="eD" max_level="{pair_max_level}" use_long_range="1" />
   </Actions>
   <Moves>
-    <Move name="BisectU" type="Bisect" species="eU" n_level="{n_level}" />
-    <Move name="BisectD" type="Bisect" species="eD" n_level="{n_level}" />
+    <Move name="BisectU" type="Bisect" species="eU" n_level="{n_level}"{img} />
+    <Move name="BisectD" type="Bisect" species="eD" n_level="{n_level}"{img} />
   </Moves>
   <Observables>
     <Observable name="Energy" type="Energy" />

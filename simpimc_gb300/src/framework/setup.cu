@@ -570,13 +570,17 @@ void Context::BuildActions(const Input& in) {
             uint32_t n_val = 1;
             for (uint32_t i = 1; i <= p.n_order; ++i) n_val += 1 + i;
             p.kj_stride = n_val + 1;
-            auto comps = [&](const std::string& key) {  // value index fastest, then grid, then tau
+            // Value index fastest, then grid, then tau. The reference fills its spline data for the
+            // grid points below the last one only (david_pair_action_class.h:262-271, the zeroing of
+            // the last one commented out); its array library zero-initialises, so every component,
+            // the potential included, is zero at the last grid point.
+            auto comps = [&](const std::string& key) {
                 const auto& d = tf.Vec(key);
                 if (d.size() < (size_t)n_val * n_grid * n_tau || V.size() != n_grid)
                     throw PimcError(kErrInput, "table '" + file + "': short " + key);
-                std::vector<std::vector<double>> out(n_tau * (n_val + 1), std::vector<double>(n_grid));
+                std::vector<std::vector<double>> out(n_tau * (n_val + 1), std::vector<double>(n_grid, 0.));
                 for (size_t l = 0; l < n_tau; ++l)
-                    for (size_t g = 0; g < n_grid; ++g) {
+                    for (size_t g = 0; g + 1 < n_grid; ++g) {
                         out[l * (n_val + 1)][g] = V[g];
                         for (uint32_t v = 1; v <= n_val; ++v) out[l * (n_val + 1) + v][g] = d[(v - 1) + g * n_val + l * n_val * n_grid];
                     }

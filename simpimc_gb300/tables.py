@@ -200,8 +200,8 @@ def david_table(path, *, tau: float, n_order: int = 2, lam: float = 0.5, z_ab: f
     tau derivatives at fixed a, with the potential taken out of the diagonal one as in the
     reference's files (du_00 - V). Datasets, with ``n = n_order``:
 
-    * ``u_kj_n/grid/{start, end, n_grid_points, grid_points}``: a general grid (the reference also
-      reads LOG, LINEAR and LOGLIN grid types, whose knots the points give);
+    * ``u_kj_n/grid/{start, end, n_grid_points, type, grid_points}``: a general grid, type "GENERAL"
+      (the reference also reads LOG, LINEAR and LOGLIN grid types, whose knots the points give);
     * ``u_kj_n/taus``, ``potential/data``;
     * ``u_kj_n/data`` and ``du_kj_dbeta_n/data``: n_val x n_grid x n_tau values, value index
       fastest (Armadillo's cube order), n_val = sum_{i=0..n} (i + 1). Table l is made for the time
@@ -238,7 +238,8 @@ def david_table(path, *, tau: float, n_order: int = 2, lam: float = 0.5, z_ab: f
         taus.append(tl)
     pre = f"u_kj_{n_order}"
     ds = {
-        f"{pre}/grid/start": r[0], f"{pre}/grid/end": r[-1], f"{pre}/grid/n_grid_points": n_grid, f"{pre}/grid/grid_points": r,
+        f"{pre}/grid/start": r[0], f"{pre}/grid/end": r[-1], f"{pre}/grid/n_grid_points": n_grid, f"{pre}/grid/type": "GENERAL",
+        f"{pre}/grid/grid_points": r,
         f"{pre}/taus": tau if n_tau == 1 else np.array(taus), "potential/data": V,
         f"{pre}/data": np.concatenate(us),  # then grid, then tau
         f"du_kj_dbeta_{n_order}/data": np.concatenate(dus),

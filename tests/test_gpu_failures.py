@@ -4,8 +4,8 @@ hangs the GPU.
 The reference reports every failure by printing and exiting (actions.h:32-33). Here each call returns
 a status code and the context stays usable:
 - a device wait that nothing completes gives up at its time limit (PIMC_ERR_TIMEOUT);
-- a non-finite action difference inside the sweep (two particles on one point under bare Coulomb:
-  1/r is infinite) sets the device error word, and the call returns PIMC_ERR_NONFINITE;
+- a non-finite action difference inside the sweep (a coordinate whose square overflows the sweep's
+  double-float representation) sets the device error word, and the call returns PIMC_ERR_NONFINITE;
 - non-finite coordinates are refused at upload, single chain and batched;
 - a missing pair-action table is refused at creation (PIMC_ERR_INPUT).
 """
@@ -46,9 +46,13 @@ def test_wait_limit_gives_up_and_context_recovers(tmp_path, gpu_lib, oracle_mod)
 
 
 def test_sweep_reports_nonfinite_action_difference(tmp_path, gpu_lib):
+    """The sweep keeps positions as double-float pairs of FP32 numbers, so squares of coordinates and
+    displacements above ~3e38 overflow there (in FP64 they would not). One bead at 1e20 makes every
+    attempt whose segment reaches it form a non-finite action difference; the sweep stops and the
+    call returns PIMC_ERR_NONFINITE instead of accepting or rejecting on it."""
     xml, path = trapped_coulomb(tmp_path, n_part=4, n_bead=16, n_level=2, seed=13)
     path = np.array(path)
-    path[1] = path[0]  # particles 0 and 1 on the same point of every slice: 1/r is infinite
+    path[0, 6, 0] = 1.0e20
     g = Simulation(xml, base_dir=tmp_path)
     g.set_path(path)
     with pytest.raises(PimcError) as e:

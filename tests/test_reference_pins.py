@@ -1,0 +1,60 @@
+"""The oracle against the reference itself (CPU).
+
+tests/golden/reference_*.npz hold the answers of simpimc's own Action, Bisect and Observable classes
+— the reference checkout's headers, unmodified, compiled against the shim in oracle/refshim/ — on
+seeded inputs: GetAction / GetActionGradient queries, DActionDBeta, Potential, VirialEnergy, and the
+input's whole Algorithm loop (bisection with the oracle's random stream, measurements, Write events,
+adaptive bisection levels). Cases: the 8-particle trapped Coulomb system (N = 8, M = 32, level 3), an
+adaptive-level trap, DavidPairAction with tables at levels 0-2, and 14-electron gases with the bare
+Ewald, Ilkka and David pair actions and one with periodic images in the kinetic action
+(n_images = 10 on a small box).
+
+The oracle must reproduce every number (tolerances in tests/reference_cases.py). Where the reference
+checkout is present, the fixtures are also regenerated from it and must equal the committed files,
+which pins the fixtures to the reference code as built here.
+"""
+import numpy as np
+import pytest
+
+from reference_cases import check_against_fixture, fixture_names, generator, load, n_observables
+
+
+def _oracle_blocks(sim, xml):
+    sim.run()
+    return {o: sim.blocks(o) for o in range(n_observables(xml))}
+
+
+@pytest.mark.parametrize("name", fixture_names())
+def test_oracle_matches_reference_fixture(tmp_path, oracle_mod, name):
+    def make(xml, d):
+        return oracle_mod.OracleSim(xml, base_dir=d)
+
+    sim, errs = check_against_fixture(make, name, tmp_path, _oracle_blocks, lambda s: s.get_path(1))
+    sim.close()
+    assert not errs, errs[:10]
+
+
+def test_fixture_cases_cover_the_hot_path_classes():
+    names = fixture_names()
+    assert len(names) >= 7
+    xmls = " ".join(str(load(n)["xml"]) for n in names)
+    for cls in ("Kinetic", "HarmonicTrap", "BarePairAction", "IlkkaPairAction", "DavidPairAction", 'adaptive="1"', 'n_images="10"',
+                "StructureFactor", "PairCorrelation", "use_virial_estimator"):
+        assert cls in xmls, cls
+
+
+@pytest.mark.parametrize("name", fixture_names())
+def test_reference_build_reproduces_fixture(tmp_path, name):
+    """Regenerates one fixture from the reference checkout (skipped where it is absent)."""
+    from oracle import ref
+    if not ref.available():
+        pytest.skip("reference checkout absent")
+    gen = generator()
+    fresh = gen.reference_answers(name, str(tmp_path))
+    old = load(name)
+    assert sorted(fresh) == sorted(old)
+    for k, v in fresh.items():
+        if k in ("xml", "action_queries", "gradient_queries"):
+            assert str(v) == str(old[k]), k
+        else:
+            np.testing.assert_array_equal(np.asarray(v), old[k], err_msg=k)
