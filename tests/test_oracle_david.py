@@ -15,14 +15,18 @@ scipy_interp = pytest.importorskip("scipy.interpolate")
 
 
 class Multi:
-    """Component splines of a David table (component 0 the potential), argument clamped to the grid."""
+    """Component splines of a David table (component 0 the potential), argument clamped to the grid.
+    Every component is zero at the last grid point: the reference fills its spline data below that
+    point only (david_pair_action_class.h:262-271) and leaves the zero-initialised value there."""
 
     def __init__(self, ds, key, n_order, level=0):
         g = np.asarray(ds[f"u_kj_{n_order}/grid/grid_points"])
         n_val = sum(i + 1 for i in range(n_order + 1))
         block = len(g) * n_val  # one table per tau: value index fastest, then grid, then tau
         data = np.asarray(ds[key])[level * block:(level + 1) * block].reshape(len(g), n_val)
-        cols = [np.asarray(ds["potential/data"])] + [data[:, v] for v in range(n_val)]
+        cols = [np.asarray(ds["potential/data"], dtype=float).copy()] + [data[:, v].copy() for v in range(n_val)]
+        for c in cols:
+            c[-1] = 0.0
         self.lo, self.hi = g[0], g[-1]
         self.s = [scipy_interp.CubicSpline(g, c, bc_type="natural") for c in cols]
         self.n_order = n_order
