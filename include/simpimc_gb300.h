@@ -236,6 +236,20 @@ int pimc_batch_reset_energy(pimc_batch* b);
 int pimc_batch_last_energy(pimc_batch* b, double* out);
 /* Per-chain attempt and acceptance counters (arrays of n_chains; either may be NULL). */
 int pimc_batch_counters(pimc_batch* b, uint64_t* attempts, uint64_t* accepts);
+/* Hybrid Monte Carlo on the batch ("batched + adjoint"; no reference counterpart): a chain's input
+ * may hold one <Move type="HMC" step_size="..." n_steps="..."/> besides its Bisect move. Each
+ * attempt draws Gaussian momenta for every bead from the move's stream (keyed by its index in the
+ * input, as in a single-chain context), runs the leapfrog on S(R) + |P|^2/2 with the exact gradient
+ * of the whole-ring kinetic, trap and bare Coulomb action (pimc_action_gradient_path), and accepts
+ * with probability min(1, exp(-dH)). Positions, momenta and forces are FP32; both energies are
+ * double-float sums of exact differences and dH is FP64. One block per chain holds the chain's path
+ * in shared memory, which limits such a chain to 12 n_part n_bead bytes of it (n_part n_bead <=
+ * 18,000 or so). pimc_batch_hmc_attempts runs n attempts on every chain with the move;
+ * pimc_batch_hmc_counters reads their attempt and accept counters; pimc_batch_set_hmc_per_cycle adds
+ * n attempts to every measurement cycle of pimc_batch_run (after the sweeps). */
+int pimc_batch_hmc_attempts(pimc_batch* b, uint64_t n);
+int pimc_batch_hmc_counters(pimc_batch* b, uint64_t* attempts, uint64_t* accepts);
+int pimc_batch_set_hmc_per_cycle(pimc_batch* b, uint64_t n);
 /* Tiles: one attempt wants ceil((n_part-1)(2^n_level-1) / (32 items_per_lane)) warps for its pair
  * items; with wave = 1 a chain gets that many, at most max_warps (<= 16). With wave = W > 1 (<= 4)
  * a chain runs up to W attempts at once on W groups of such warps (at least 2 each, W times at

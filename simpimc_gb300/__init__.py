@@ -107,6 +107,9 @@ SIGNATURES = {
     "pimc_batch_energy": (C.c_int, [_P, C.c_uint32, _DP, C.c_uint64, _U64P]),
     "pimc_batch_reset_energy": (C.c_int, [_P]),
     "pimc_batch_counters": (C.c_int, [_P, _U64P, _U64P]),
+    "pimc_batch_hmc_attempts": (C.c_int, [_P, C.c_uint64]),
+    "pimc_batch_hmc_counters": (C.c_int, [_P, _U64P, _U64P]),
+    "pimc_batch_set_hmc_per_cycle": (C.c_int, [_P, C.c_uint64]),
     "pimc_batch_set_tiles": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32]),
     "pimc_batch_autotune": (C.c_int, [_P, C.c_uint32, _U32P, _U32P, _U32P, _DP]),
     "pimc_batch_stats": (C.c_int, [_P, _U64P]),
@@ -492,6 +495,20 @@ class ChainBatch:
         acc = np.zeros(self.n_chains, dtype=np.uint64)
         self._check(self._lib.pimc_batch_counters(self._h, att.ctypes.data_as(_U64P), acc.ctypes.data_as(_U64P)))
         return att, acc
+
+    def hmc_attempts(self, n: int):
+        """n hybrid Monte Carlo attempts on every chain whose input has an HMC move."""
+        self._check(self._lib.pimc_batch_hmc_attempts(self._h, n))
+
+    def hmc_counters(self):
+        att = np.zeros(self.n_chains, dtype=np.uint64)
+        acc = np.zeros(self.n_chains, dtype=np.uint64)
+        self._check(self._lib.pimc_batch_hmc_counters(self._h, att.ctypes.data_as(_U64P), acc.ctypes.data_as(_U64P)))
+        return att, acc
+
+    def set_hmc_per_cycle(self, n: int):
+        """HMC attempts in every measurement cycle of run() (after the sweeps)."""
+        self._check(self._lib.pimc_batch_set_hmc_per_cycle(self._h, n))
 
     def set_tiles(self, items_per_lane: int, max_warps: int, wave: int = 1):
         self._check(self._lib.pimc_batch_set_tiles(self._h, items_per_lane, max_warps, wave))

@@ -29,7 +29,8 @@ from .tables import coulomb_table, david_table, ilkka_table
 
 def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_level=3, seed=1234, coulomb=True,
                     n_step_inner=100, n_step_outer=10, gr_bins=200, gr_rmax=5.0, virial=False, path_seed=None,
-                    write_table=True, pair="BarePairAction", n_order=2, pair_max_level=0, adaptive=False, target_ratio=0.5):
+                    write_table=True, pair="BarePairAction", n_order=2, pair_max_level=0, adaptive=False, target_ratio=0.5,
+                    hmc=None):
     workdir = Path(workdir)
     workdir.mkdir(parents=True, exist_ok=True)
     if pair == "DavidPairAction":
@@ -54,6 +55,8 @@ def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_leve
     energy = ('<Observable name="Energy" type="Energy" use_virial_estimator="1" />' if virial
               else '<Observable name="Energy" type="Energy" />')
     adapt = f' adaptive="1" target_ratio="{target_ratio!r}"' if adaptive else ""
+    # hmc = (step_size, n_steps): the library's whole-path hybrid Monte Carlo move besides Bisect
+    hmc_xml = (f'\n    <Move name="HMC" type="HMC" species="e" step_size="{hmc[0]!r}" n_steps="{int(hmc[1])}" />' if hmc else "")
     xml = f"""<Input>
   <RNG seed="{seed}" />
   <IO output_prefix="trap" />
@@ -68,7 +71,7 @@ def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_leve
     {pair}
   </Actions>
   <Moves>
-    <Move name="Bisect" type="Bisect" species="e" n_level="{n_level}"{adapt} />
+    <Move name="Bisect" type="Bisect" species="e" n_level="{n_level}"{adapt} />{hmc_xml}
   </Moves>
   <Observables>
     {energy}
@@ -160,11 +163,12 @@ def electron_gas(workdir, *, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_unit
 
 
 def batched_trap_chains(workdir, *, n_chains=256, seed0=1000, n_range=(16, 128), bead_choices=(32, 64, 128),
-                        n_level=3, beta=2.0, omega=1.0, chain_seed0=None):
+                        n_level=3, beta=2.0, omega=1.0, chain_seed0=None, hmc=None):
     """Independent trapped Coulomb chains with uneven sizes: chain c has seed ``chain_seed0 + c``
     (``chain_seed0`` defaults to ``seed0``), N drawn uniformly from ``n_range`` (inclusive) and M
     from ``bead_choices`` by a generator seeded with ``seed0``; beads i.i.d. N(0, 1) from the
-    chain's seed. Returns a list of ``(xml_text, initial_path)``."""
+    chain's seed; ``hmc = (step_size, n_steps)`` adds the HMC move to every chain. Returns a list of
+    ``(xml_text, initial_path)``."""
     cs0 = seed0 if chain_seed0 is None else chain_seed0
     rng = np.random.default_rng(seed0)
     ns = rng.integers(n_range[0], n_range[1] + 1, size=n_chains)
@@ -172,7 +176,7 @@ def batched_trap_chains(workdir, *, n_chains=256, seed0=1000, n_range=(16, 128),
     out = []
     for c in range(n_chains):
         out.append(trapped_coulomb(workdir, n_part=int(ns[c]), n_bead=int(ms[c]), n_level=n_level, beta=beta,
-                                   omega=omega, seed=cs0 + c, write_table=(c == 0)))
+                                   omega=omega, seed=cs0 + c, write_table=(c == 0), hmc=hmc))
     return out
 
 

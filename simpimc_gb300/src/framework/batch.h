@@ -10,7 +10,8 @@
 //
 // Supported chains (anything else is rejected at creation): one species in three dimensions;
 // Kinetic (n_images 0); optional HarmonicTrap; optional BarePairAction with is_coulomb=1 and no
-// long-range part between the species and itself; one non-adaptive Bisect move with n_level <= 5;
+// long-range part between the species and itself; one non-adaptive Bisect move with n_level <= 5
+// and optionally one HMC move of the species (the library's whole-path hybrid Monte Carlo move);
 // open or periodic boundaries.
 //
 // Arithmetic: positions and per-term action values in FP32; every sum of terms compensated
@@ -53,11 +54,16 @@ struct ChainDev {
     int32_t pbc, has_trap, has_pair, trap_max_level;
     float trap_cofa, r2_min, r2_max, pad1;  // pair clamp r in [r_min, r_max] as r^2
     double trap_cofb, kin_const, i4ltt;     // DActionDBeta constants (trap_class.h, kinetic_class.h)
+    float hmc_eps;                          // HMC leapfrog step (0: the chain has no HMC move)
+    uint32_t hmc_steps, hmc_move, pad4;     // leapfrog steps; the HMC move's index in its input
 };
 
 /// Host view of one chain's input.
 struct ChainSpec {
     uint32_t n_part = 0, n_bead = 0, n_level = 0, seed = 0, move = 0;
+    bool has_hmc = false;             // a <Move type="HMC"> besides the Bisect move
+    uint32_t hmc_move = 0, hmc_steps = 0;
+    double hmc_eps = 0.;
     double beta = 0., tau = 0., L = 0., lambda = 0., omega = 0., r_min = 0., r_max = 0.;
     bool pbc = true, has_trap = false, has_pair = false;
     uint32_t trap_max_level = 0;
@@ -80,6 +86,9 @@ class ChainBatch {
     void GetPaths(double* all);
     void LastEnergy(double* out);      // [n_chains][4]: the latest measurement of every chain
     void Attempts(uint64_t n);                // n bisection attempts on every chain
+    void HmcAttempts(uint64_t n);             // n HMC attempts on every chain that has the move
+    void ReadHmcCounters(uint64_t* attempts, uint64_t* accepts);
+    void SetHmcPerCycle(uint64_t n);          // HMC attempts in each graph-replayed cycle
     void Sweeps(uint64_t n);                  // n sweeps on every chain (one launch)
     void Measure();                           // one energy measurement on every chain
     void Run(uint64_t n_cycles, uint64_t sweeps_per_measure);  // graph-replayed cycles
@@ -98,6 +107,9 @@ class ChainBatch {
     std::vector<ChainDev> chains;
     std::vector<uint32_t> order;   // block -> chain, most expensive first
     uint64_t bead_moves_per_sweep = 0;
+    uint64_t bead_moves_per_hmc = 0;  // beads one HMC attempt of every chain moves (n_part n_bead each)
+    uint64_t hmc_per_cycle = 0;
+    size_t hmc_smem = 0;              // shared memory of the HMC launch (largest chain's path planes)
     uint64_t path_doubles = 0;  // sum of n_part * n_bead * 3 over the chains
     uint64_t kernel_launches = 0;
     size_t stage_cap = 0;     // shared memory a sweep block may take for a staged path
@@ -106,14 +118,16 @@ class ChainBatch {
    private:
     void Upload();
     void LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts);
+    void LaunchHmc(uint64_t n_attempts);
     void LaunchMeasure();
     void ResetGraph();
     std::unique_ptr<DeviceBuffer> pos_, chains_dev_, order_dev_, att_, acc_, series_, n_meas_, err_, last_;
+    std::unique_ptr<DeviceBuffer> mom_, hmc_att_, hmc_acc_;  // HMC momenta (layout of pos_), counters
     std::vector<uint64_t> path_off_;  // first double of each chain in the concatenated host layout
     std::unique_ptr<DeviceBuffer> dstage_, path_off_dev_;  // host-layout doubles on the device, offsets
     size_t pos_float4 = 0;
     cudaGraphExec_t graph_ = nullptr;
-    uint64_t graph_sweeps_ = 0;
+    uint64_t graph_sweeps_ = 0, graph_hmc_ = 0;
     uint32_t launches_per_cycle_ = 3;  // sweep + energy parts + energy finish
     std::unique_ptr<DeviceBuffer> energy_tasks_, energy_first_, energy_part_;
     uint32_t n_energy_tasks_ = 0;

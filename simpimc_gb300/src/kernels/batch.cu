@@ -837,6 +837,207 @@ __global__ void BatchEnergyFinishKernel(BatchArgs a, const uint32_t* __restrict_
     a.n_meas[ci] = n + 1;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Hybrid Monte Carlo on every chain (the library's whole-path HMC move; no reference counterpart).
+// One block per chain runs its attempts: momenta P ~ N(0, 1) per coordinate from the attempt's
+// counter-based stream (normal j of the path-ordered coordinates (p, b, d) is component j % 4 of
+// Philox block 1 + j / 4, as the single-chain move draws them); leapfrog on H = S(R) + |P|^2 / 2
+// with the exact gradient of the whole-ring action at level 0
+//   S = sum_{p,b} |r_{b+1} - r_b|^2 / (4 lambda tau)        (Kinetic, n_images 0)
+//     + cofactor_a sum_{p,b} r^2                           (HarmonicTrap)
+//     + tau sum_b sum_{p<q} V(|r_p - r_q|), V = 1/r clamped to the table's r range (BarePairAction);
+// then acceptance with probability min(1, exp(-dH)) against the log-uniform of block 0, word 0.
+// The path sits in shared memory as three FP32 planes [M][N]; momenta live in global memory in the
+// layout of the positions. Forces and leapfrog updates are FP32 (each thread owns fixed beads);
+// both energies are sums of exact differences and products in double-float, and dH is formed in
+// FP64 from them, so the decision sees the trajectory's energy change to ~1e-6 absolute.
+constexpr uint32_t kHmcThreads = 1024;
+
+struct HmcArgs {
+    float4* mom;     // per chain, the layout of pos: [n_bead][n_pad] (x, y, z, 0)
+    uint64_t* att;   // per chain: HMC attempts (the move's Philox attempt counter)
+    uint64_t* acc;
+    uint32_t n_attempts;
+};
+
+/// Block-wide double-float sums of four quantities (fixed tree; every thread receives them).
+__device__ __forceinline__ void BlockSum4DD(dd v[4], dd (*s_red)[kHmcThreads / 32]) {
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, nw = blockDim.x >> 5;
+    for (int q = 0; q < 4; ++q) v[q] = WarpSumDD(v[q]);
+    __syncthreads();
+    if (lane == 0)
+        for (int q = 0; q < 4; ++q) s_red[q][warp] = v[q];
+    __syncthreads();
+    for (int q = 0; q < 4; ++q) v[q] = WarpSumDD(lane < nw ? s_red[q][lane] : DD(0.f));
+}
+
+/// Gradient dS/dr of bead i = b N + p (FP32) and, when `with_energy`, its share of S: the link
+/// b -> b+1, its trap term and half its pair sum (every pair is met twice).
+template <bool kPbc>
+__device__ __forceinline__ void HmcBead(const ChainDev& c, const float* __restrict__ sx, const float* __restrict__ sy,
+                                        const float* __restrict__ sz, uint32_t N, uint32_t M, uint32_t i, float i4, float cofa, float tau,
+                                        float& gx, float& gy, float& gz, bool with_energy, dd& e_kin, dd& e_trap, Comp& e_pair) {
+    const uint32_t b = i / N, p = i - b * N;
+    const uint32_t bp = b == 0 ? M - 1 : b - 1, bn = b + 1 == M ? 0 : b + 1;
+    const float x = sx[i], y = sy[i], z = sz[i];
+    const uint32_t ip = bp * N + p, in_ = bn * N + p;
+    // links (b-1 -> b) and (b -> b+1): d/dr_b of |r_{b+1} - r_b|^2 i4 summed = 2 i4 (d_{b-1} - d_b)
+    const float dpx = Img<kPbc>(__fsub_rn(x, sx[ip]), c.L, c.iL), dpy = Img<kPbc>(__fsub_rn(y, sy[ip]), c.L, c.iL),
+                dpz = Img<kPbc>(__fsub_rn(z, sz[ip]), c.L, c.iL);
+    const float dnx = Img<kPbc>(__fsub_rn(sx[in_], x), c.L, c.iL), dny = Img<kPbc>(__fsub_rn(sy[in_], y), c.L, c.iL),
+                dnz = Img<kPbc>(__fsub_rn(sz[in_], z), c.L, c.iL);
+    const float k2 = 2.f * i4;
+    gx = __fmul_rn(k2, __fsub_rn(dpx, dnx));
+    gy = __fmul_rn(k2, __fsub_rn(dpy, dny));
+    gz = __fmul_rn(k2, __fsub_rn(dpz, dnz));
+    if (c.has_trap) {
+        const float t2 = 2.f * cofa;
+        gx = __fmaf_rn(t2, x, gx);
+        gy = __fmaf_rn(t2, y, gy);
+        gz = __fmaf_rn(t2, z, gz);
+    }
+    if (with_energy) {
+        dd ex = TwoSum(sx[in_], -x), ey = TwoSum(sy[in_], -y), ez = TwoSum(sz[in_], -z);
+        if (kPbc) {
+            ex = Sub(ex, DD(__fmul_rn(c.L, rintf(__fmul_rn(ex.hi, c.iL)))));
+            ey = Sub(ey, DD(__fmul_rn(c.L, rintf(__fmul_rn(ey.hi, c.iL)))));
+            ez = Sub(ez, DD(__fmul_rn(c.L, rintf(__fmul_rn(ez.hi, c.iL)))));
+        }
+        e_kin = Add(e_kin, Add(Add(Sqr(ex), Sqr(ey)), Sqr(ez)));
+        e_trap = AddSq(AddSq(AddSq(e_trap, x), y), z);
+    }
+    if (c.has_pair) {
+        const float* rx = sx + b * N;
+        const float* ry = sy + b * N;
+        const float* rz = sz + b * N;
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        for (uint32_t q = 0; q < N; ++q) {
+            if (q == p) continue;
+            const float ux = Img<kPbc>(__fsub_rn(x, rx[q]), c.L, c.iL);
+            const float uy = Img<kPbc>(__fsub_rn(y, ry[q]), c.L, c.iL);
+            const float uz = Img<kPbc>(__fsub_rn(z, rz[q]), c.L, c.iL);
+            const float r2 = Sq3(ux, uy, uz);
+            const float rc2 = fminf(fmaxf(r2, c.r2_min), c.r2_max);
+            const float inv = rsqrtf(rc2);
+            if (with_energy) CompAdd(e_pair, inv);
+            // tau V'(r) (r_p - r_q) / r with V' = -1/r^2 inside the table's range, 0 where clamped
+            const float f = (r2 >= c.r2_min && r2 <= c.r2_max) ? __fmul_rn(__fmul_rn(inv, inv), inv) : 0.f;
+            fx = __fmaf_rn(f, ux, fx);
+            fy = __fmaf_rn(f, uy, fy);
+            fz = __fmaf_rn(f, uz, fz);
+        }
+        gx = __fmaf_rn(-tau, fx, gx);
+        gy = __fmaf_rn(-tau, fy, gy);
+        gz = __fmaf_rn(-tau, fz, gz);
+    }
+}
+
+template <bool kPbc>
+__device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c, uint32_t ci, float* sx, float* sy, float* sz,
+                         dd (*s_red)[kHmcThreads / 32], int* s_accept) {
+    const uint32_t N = c.n_part, M = c.n_bead, n_pad = c.n_pad, E = N * M;
+    const uint32_t t = threadIdx.x, T = blockDim.x;
+    float4* pos = a.pos + c.pos_off;
+    float4* mom = h.mom + c.pos_off;
+    const float i4 = c.i4lt_level[0], cofa = c.trap_cofa, tau = c.tau, eps = c.hmc_eps;
+    const double i4d = 1. / (4. * (double)c.lambda * (double)c.tau), taud = (double)c.tau;
+    uint64_t att = h.att[ci], acc = 0;
+    for (uint32_t it = 0; it < h.n_attempts; ++it, ++att) {
+        const MoveStream st{c.seed, c.chain_id, c.hmc_move, att};
+        // path into the planes; momenta from the stream
+        for (uint32_t i = t; i < E; i += T) {
+            const uint32_t b = i / N, p = i - b * N;
+            const float4 r = pos[(size_t)b * n_pad + p];
+            sx[i] = r.x;
+            sy[i] = r.y;
+            sz[i] = r.z;
+            float z3[3];
+            const uint32_t j0 = (p * M + b) * 3u;
+            for (uint32_t d = 0; d < 3; ++d) {
+                const uint32_t j = j0 + d;
+                const Philox4 w = st.Block(1u + (j >> 2));
+                float z0, z1;
+                if ((j & 3u) < 2u) BoxMullerF(w.v[0], w.v[1], z0, z1);
+                else BoxMullerF(w.v[2], w.v[3], z0, z1);
+                z3[d] = (j & 1u) ? z1 : z0;
+            }
+            mom[(size_t)b * n_pad + p] = make_float4(z3[0], z3[1], z3[2], 0.f);
+        }
+        __syncthreads();
+        double h_start = 0., h_end = 0.;
+        const uint32_t n_steps = c.hmc_steps;
+        for (uint32_t s = 0; s <= n_steps; ++s) {
+            // gradient at the current R; energy at the start (s = 0) and the end (s = n_steps)
+            const bool with_energy = s == 0 || s == n_steps;
+            const float f = (s == 0 || s == n_steps) ? 0.5f * eps : eps;
+            dd ek = DD(0.f), et = DD(0.f), ep = DD(0.f), em = DD(0.f);
+            Comp cp{0.f, 0.f};
+            for (uint32_t i = t; i < E; i += T) {
+                float gx, gy, gz;
+                HmcBead<kPbc>(c, sx, sy, sz, N, M, i, i4, cofa, tau, gx, gy, gz, with_energy, ek, et, cp);
+                const uint32_t b = i / N, p = i - b * N;
+                float4 m4 = mom[(size_t)b * n_pad + p];
+                if (s == 0) em = AddSq(AddSq(AddSq(em, m4.x), m4.y), m4.z);  // |P|^2 before the first kick
+                m4.x = __fmaf_rn(-f, gx, m4.x);
+                m4.y = __fmaf_rn(-f, gy, m4.y);
+                m4.z = __fmaf_rn(-f, gz, m4.z);
+                if (s == n_steps) em = AddSq(AddSq(AddSq(em, m4.x), m4.y), m4.z);  // |P|^2 after the last kick
+                mom[(size_t)b * n_pad + p] = m4;
+            }
+            if (with_energy) {
+                ep = CompDD(cp);
+                dd v[4] = {ek, et, ep, em};
+                BlockSum4DD(v, s_red);
+                const double hv = i4d * ToDouble(v[0]) + (c.has_trap ? (double)cofa * ToDouble(v[1]) : 0.) +
+                                  0.5 * taud * ToDouble(v[2]) + 0.5 * ToDouble(v[3]);
+                if (s == 0) h_start = hv;
+                else h_end = hv;
+            }
+            __syncthreads();  // every gradient read of R is done
+            if (s == n_steps) break;
+            for (uint32_t i = t; i < E; i += T) {  // drift
+                const uint32_t b = i / N, p = i - b * N;
+                const float4 m4 = mom[(size_t)b * n_pad + p];
+                sx[i] = __fmaf_rn(eps, m4.x, sx[i]);
+                sy[i] = __fmaf_rn(eps, m4.y, sy[i]);
+                sz[i] = __fmaf_rn(eps, m4.z, sz[i]);
+            }
+            __syncthreads();
+        }
+        if (t == 0) {
+            const double log_accept = -(h_end - h_start);
+            const double logu = (double)LogF(U24(st.Block(0).v[0]));
+            *s_accept = (isfinite(log_accept) && !(log_accept < logu)) ? 1 : 0;
+        }
+        __syncthreads();
+        if (*s_accept) {
+            for (uint32_t i = t; i < E; i += T) {
+                const uint32_t b = i / N, p = i - b * N;
+                pos[(size_t)b * n_pad + p] = make_float4(sx[i], sy[i], sz[i], 0.f);
+            }
+            ++acc;
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        h.att[ci] = att;
+        h.acc[ci] += acc;
+    }
+}
+
+__global__ void __launch_bounds__(kHmcThreads) BatchHmcKernel(BatchArgs a, HmcArgs h) {
+    const uint32_t ci = a.order[blockIdx.x];
+    const ChainDev& c = a.chains[ci];
+    if (c.hmc_eps == 0.f) return;  // the chain has no HMC move
+    __shared__ dd s_red[4][kHmcThreads / 32];
+    __shared__ int s_accept;
+    extern __shared__ float4 hmc_stage[];
+    float* sx = reinterpret_cast<float*>(hmc_stage);
+    const uint32_t E = c.n_part * c.n_bead;
+    if (c.pbc) HmcChain<true>(a, h, c, ci, sx, sx + E, sx + 2 * E, s_red, &s_accept);
+    else HmcChain<false>(a, h, c, ci, sx, sx + E, sx + 2 * E, s_red, &s_accept);
+}
+
 /// Host layout (every chain's [n_part][n_bead][3] doubles, concatenated) to the device float4
 /// layout, one block per chain; a non-finite coordinate sets kDevErrNonFinite and is not stored.
 __global__ void HostLayoutToPosKernel(const double* __restrict__ src, const ChainDev* __restrict__ chains, const uint64_t* __restrict__ path_off,
@@ -926,16 +1127,35 @@ ChainSpec ParseChain(const std::string& xml, const std::string& base_dir) {
         }
     }
     if (!has_kinetic) throw PimcError(kErrUnsupported, "batched chains need a Kinetic action");
+    // One Bisect move and at most one HMC move; each keeps its index in the input as the key of its
+    // random stream, as in a single-chain context.
     const auto moves = in.GetChild("Moves").GetChildList("Move");
-    if (moves.size() != 1 || moves[0].GetAttribute<std::string>("type") != "Bisect")
-        throw PimcError(kErrUnsupported, "batched chains need exactly one Bisect move");
-    if (moves[0].GetAttribute<std::string>("species") != sp) throw PimcError(kErrInput, "Bisect on an unknown species");
-    if (moves[0].GetAttribute<bool>("adaptive", false) || moves[0].GetAttribute<int>("n_images", 0) != 0)
+    int bisect = -1;
+    for (size_t i = 0; i < moves.size(); ++i) {
+        const std::string type = moves[i].GetAttribute<std::string>("type");
+        if (type == "Bisect" && bisect < 0) {
+            bisect = (int)i;
+        } else if (type == "HMC" && !s.has_hmc) {
+            const std::string hs = moves[i].GetAttribute<std::string>("species", "");
+            if (!hs.empty() && hs != sp) throw PimcError(kErrInput, "HMC on an unknown species");
+            s.has_hmc = true;
+            s.hmc_move = (uint32_t)i;
+            s.hmc_eps = moves[i].GetAttribute<double>("step_size", 0.01);
+            s.hmc_steps = moves[i].GetAttribute<uint32_t>("n_steps", 10);
+            if (!(s.hmc_eps > 0.) || s.hmc_steps < 1 || s.hmc_steps > 100000) throw PimcError(kErrInput, "HMC needs step_size > 0, n_steps >= 1");
+        } else {
+            throw PimcError(kErrUnsupported, "batched chains take one Bisect move and at most one HMC move");
+        }
+    }
+    if (bisect < 0) throw PimcError(kErrUnsupported, "batched chains need exactly one Bisect move");
+    const Input& bm = moves[(size_t)bisect];
+    if (bm.GetAttribute<std::string>("species") != sp) throw PimcError(kErrInput, "Bisect on an unknown species");
+    if (bm.GetAttribute<bool>("adaptive", false) || bm.GetAttribute<int>("n_images", 0) != 0)
         throw PimcError(kErrUnsupported, "batched Bisect: fixed level, n_images = 0");
-    s.n_level = moves[0].GetAttribute<uint32_t>("n_level");
+    s.n_level = bm.GetAttribute<uint32_t>("n_level");
     if (s.n_level < 1 || s.n_level > kBatchMaxLevels) throw PimcError(kErrUnsupported, "batched Bisect needs 1 <= n_level <= 5");
     if ((1u << s.n_level) > s.n_bead) throw PimcError(kErrInput, "bisection segment longer than the path");
-    s.move = 0;
+    s.move = (uint32_t)bisect;
     return s;
 }
 
@@ -991,6 +1211,13 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
         c.r2_max = (float)(s.r_max * s.r_max);
         c.kin_const = (double)s.n_part * s.n_bead * 3. / (2. * s.tau);  // kinetic_class.h:13
         c.i4ltt = 1. / (4. * s.lambda * s.tau * s.tau);
+        if (s.has_hmc) {
+            c.hmc_eps = (float)s.hmc_eps;
+            c.hmc_steps = s.hmc_steps;
+            c.hmc_move = s.hmc_move;
+            bead_moves_per_hmc += (uint64_t)s.n_part * s.n_bead;
+            hmc_smem = std::max(hmc_smem, (size_t)12 * s.n_part * s.n_bead);
+        }
         bead_moves_per_sweep += c.attempts_per_sweep * (B - 1);
         path_off_.push_back(path_doubles);
         path_doubles += (uint64_t)s.n_part * s.n_bead * 3;
@@ -1012,6 +1239,21 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
     n_meas_.reset(new DeviceBuffer(n_chains * sizeof(uint64_t)));
     series_.reset(new DeviceBuffer((size_t)n_chains * series_cap * kBatchSeriesComponents * sizeof(double)));
     err_.reset(new DeviceBuffer(sizeof(int)));
+    if (bead_moves_per_hmc) {
+        int optin_h = 0;
+        cudaFuncAttributes fh{};
+        CudaCheck(cudaDeviceGetAttribute(&optin_h, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "device attribute");
+        CudaCheck(cudaFuncGetAttributes(&fh, BatchHmcKernel), "kernel attributes");
+        if (hmc_smem + fh.sharedSizeBytes > (size_t)optin_h)
+            throw PimcError(kErrUnsupported, "a batched HMC chain's path (12 n_part n_bead bytes) exceeds the shared memory of one block");
+        CudaCheck(cudaFuncSetAttribute(BatchHmcKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hmc_smem), "smem attribute");
+        mom_.reset(new DeviceBuffer(off * sizeof(float4)));
+        hmc_att_.reset(new DeviceBuffer(n_chains * sizeof(uint64_t)));
+        hmc_acc_.reset(new DeviceBuffer(n_chains * sizeof(uint64_t)));
+        CudaCheck(cudaMemset(mom_->ptr, 0, off * sizeof(float4)), "memset");
+        CudaCheck(cudaMemset(hmc_att_->ptr, 0, n_chains * sizeof(uint64_t)), "memset");
+        CudaCheck(cudaMemset(hmc_acc_->ptr, 0, n_chains * sizeof(uint64_t)), "memset");
+    }
     CudaCheck(cudaMemset(att_->ptr, 0, n_chains * sizeof(uint64_t)), "memset");
     CudaCheck(cudaMemset(acc_->ptr, 0, n_chains * sizeof(uint64_t)), "memset");
     CudaCheck(cudaMemset(n_meas_->ptr, 0, n_chains * sizeof(uint64_t)), "memset");
@@ -1181,6 +1423,35 @@ void ChainBatch::LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts) {
     ++kernel_launches;
 }
 
+void ChainBatch::LaunchHmc(uint64_t n_attempts) {
+    if (!bead_moves_per_hmc) throw PimcError(kErrState, "no chain of the batch has an HMC move");
+    const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, series_cap);
+    for (uint64_t done = 0; done < n_attempts;) {
+        const uint32_t k = (uint32_t)std::min<uint64_t>(n_attempts - done, 1u << 20);
+        const HmcArgs h{mom_->as<float4>(), hmc_att_->as<uint64_t>(), hmc_acc_->as<uint64_t>(), k};
+        BatchHmcKernel<<<n_chains, kHmcThreads, hmc_smem, stream>>>(a, h);
+        CudaCheck(cudaGetLastError(), "batch HMC launch");
+        ++kernel_launches;
+        done += k;
+    }
+}
+
+void ChainBatch::HmcAttempts(uint64_t n) {
+    if (n) LaunchHmc(n);
+}
+
+void ChainBatch::ReadHmcCounters(uint64_t* attempts, uint64_t* accepts) {
+    if (!bead_moves_per_hmc) throw PimcError(kErrState, "no chain of the batch has an HMC move");
+    Sync();
+    if (attempts) CudaCheck(cudaMemcpy(attempts, hmc_att_->ptr, n_chains * sizeof(uint64_t), cudaMemcpyDeviceToHost), "read attempts");
+    if (accepts) CudaCheck(cudaMemcpy(accepts, hmc_acc_->ptr, n_chains * sizeof(uint64_t), cudaMemcpyDeviceToHost), "read accepts");
+}
+
+void ChainBatch::SetHmcPerCycle(uint64_t n) {
+    if (n && !bead_moves_per_hmc) throw PimcError(kErrState, "no chain of the batch has an HMC move");
+    hmc_per_cycle = n;
+}
+
 void ChainBatch::LaunchMeasure() {
     const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, series_cap);
     BatchEnergyPartKernel<<<n_energy_tasks_, kEnergyThreads, energy_smem_, stream>>>(a, energy_tasks_->as<EnergyTask>(), energy_part_->as<float2>());
@@ -1202,20 +1473,22 @@ void ChainBatch::Measure() { LaunchMeasure(); }
 
 void ChainBatch::Run(uint64_t n_cycles, uint64_t spm) {
     if (spm == 0) throw PimcError(kErrArg, "sweeps_per_measure must be positive");
-    if (!graph_ || graph_sweeps_ != spm) {
+    if (!graph_ || graph_sweeps_ != spm || graph_hmc_ != hmc_per_cycle) {
         ResetGraph();
         cudaGraph_t g = nullptr;
         CudaCheck(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
         const uint64_t before = kernel_launches;
         LaunchSweep(spm, 0);
+        if (hmc_per_cycle) LaunchHmc(hmc_per_cycle);
         LaunchMeasure();
+        launches_per_cycle_ = (uint32_t)(kernel_launches - before);
         kernel_launches = before;
         CudaCheck(cudaStreamEndCapture(stream, &g), "end capture");
-        launches_per_cycle_ = 3;
         const cudaError_t e = cudaGraphInstantiate(&graph_, g, 0);
         cudaGraphDestroy(g);
         CudaCheck(e, "graph instantiate");
         graph_sweeps_ = spm;
+        graph_hmc_ = hmc_per_cycle;
     }
     for (uint64_t i = 0; i < n_cycles; ++i) {
         CudaCheck(cudaGraphLaunch(graph_, stream), "graph launch");
@@ -1436,6 +1709,18 @@ int pimc_batch_reset_energy(pimc_batch* h) {
 
 int pimc_batch_counters(pimc_batch* h, uint64_t* attempts, uint64_t* accepts) {
     return BatchGuard(h, [&](pimc::ChainBatch& b) { b.ReadCounters(attempts, accepts); });
+}
+
+int pimc_batch_hmc_attempts(pimc_batch* h, uint64_t n) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.HmcAttempts(n); });
+}
+
+int pimc_batch_hmc_counters(pimc_batch* h, uint64_t* attempts, uint64_t* accepts) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.ReadHmcCounters(attempts, accepts); });
+}
+
+int pimc_batch_set_hmc_per_cycle(pimc_batch* h, uint64_t n) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.SetHmcPerCycle(n); });
 }
 
 int pimc_batch_set_tiles(pimc_batch* h, uint32_t items_per_lane, uint32_t max_warps, uint32_t wave) {
