@@ -18,7 +18,11 @@ void CudaCheck(cudaError_t e, const char* what) {
 DeviceBuffer::DeviceBuffer(size_t n) : bytes(n) {
     if (n == 0) n = 16;
     CudaCheck(cudaMalloc(&ptr, n), "cudaMalloc");
+    // cudaMemset runs on the legacy default stream and returns before it completes; the contexts'
+    // streams are non-blocking, so without this wait a copy enqueued on a context stream right after
+    // the allocation could land first and then be zeroed.
     CudaCheck(cudaMemset(ptr, 0, n), "cudaMemset");
+    CudaCheck(cudaStreamSynchronize(cudaStreamLegacy), "cudaMemset completion");
 }
 
 DeviceBuffer::~DeviceBuffer() {

@@ -873,10 +873,10 @@ __device__ __forceinline__ void BlockSum4DD(dd v[4], dd (*s_red)[kHmcThreads / 3
 
 /// Gradient dS/dr of bead i = b N + p (FP32) and, when `with_energy`, its share of S: the link
 /// b -> b+1, its trap term and half its pair sum (every pair is met twice).
-template <bool kPbc>
+template <bool kPbc, bool kEnergy>
 __device__ __forceinline__ void HmcBead(const ChainDev& c, const float* __restrict__ sx, const float* __restrict__ sy,
                                         const float* __restrict__ sz, uint32_t N, uint32_t M, uint32_t i, float i4, float cofa, float tau,
-                                        float& gx, float& gy, float& gz, bool with_energy, dd& e_kin, dd& e_trap, Comp& e_pair) {
+                                        float& gx, float& gy, float& gz, dd& e_kin, dd& e_trap, Comp& e_pair) {
     const uint32_t b = i / N, p = i - b * N;
     const uint32_t bp = b == 0 ? M - 1 : b - 1, bn = b + 1 == M ? 0 : b + 1;
     const float x = sx[i], y = sy[i], z = sz[i];
@@ -896,7 +896,7 @@ __device__ __forceinline__ void HmcBead(const ChainDev& c, const float* __restri
         gy = __fmaf_rn(t2, y, gy);
         gz = __fmaf_rn(t2, z, gz);
     }
-    if (with_energy) {
+    if constexpr (kEnergy) {
         dd ex = TwoSum(sx[in_], -x), ey = TwoSum(sy[in_], -y), ez = TwoSum(sz[in_], -z);
         if (kPbc) {
             ex = Sub(ex, DD(__fmul_rn(c.L, rintf(__fmul_rn(ex.hi, c.iL)))));
@@ -911,17 +911,18 @@ __device__ __forceinline__ void HmcBead(const ChainDev& c, const float* __restri
         const float* ry = sy + b * N;
         const float* rz = sz + b * N;
         float fx = 0.f, fy = 0.f, fz = 0.f;
+        const float r2lo = c.r2_min, r2hi = c.r2_max;
+#pragma unroll 4
         for (uint32_t q = 0; q < N; ++q) {
-            if (q == p) continue;
+            // q = p contributes nothing (both of its terms are masked)
             const float ux = Img<kPbc>(__fsub_rn(x, rx[q]), c.L, c.iL);
             const float uy = Img<kPbc>(__fsub_rn(y, ry[q]), c.L, c.iL);
             const float uz = Img<kPbc>(__fsub_rn(z, rz[q]), c.L, c.iL);
             const float r2 = Sq3(ux, uy, uz);
-            const float rc2 = fminf(fmaxf(r2, c.r2_min), c.r2_max);
-            const float inv = rsqrtf(rc2);
-            if (with_energy) CompAdd(e_pair, inv);
+            const float inv = rsqrtf(fminf(fmaxf(r2, r2lo), r2hi));
+            if constexpr (kEnergy) CompAdd(e_pair, q == p ? 0.f : inv);
             // tau V'(r) (r_p - r_q) / r with V' = -1/r^2 inside the table's range, 0 where clamped
-            const float f = (r2 >= c.r2_min && r2 <= c.r2_max) ? __fmul_rn(__fmul_rn(inv, inv), inv) : 0.f;
+            const float f = (r2 >= r2lo && r2 <= r2hi && q != p) ? __fmul_rn(__fmul_rn(inv, inv), inv) : 0.f;
             fx = __fmaf_rn(f, ux, fx);
             fy = __fmaf_rn(f, uy, fy);
             fz = __fmaf_rn(f, uz, fz);
@@ -974,7 +975,8 @@ __device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c
             Comp cp{0.f, 0.f};
             for (uint32_t i = t; i < E; i += T) {
                 float gx, gy, gz;
-                HmcBead<kPbc>(c, sx, sy, sz, N, M, i, i4, cofa, tau, gx, gy, gz, with_energy, ek, et, cp);
+                if (with_energy) HmcBead<kPbc, true>(c, sx, sy, sz, N, M, i, i4, cofa, tau, gx, gy, gz, ek, et, cp);
+                else HmcBead<kPbc, false>(c, sx, sy, sz, N, M, i, i4, cofa, tau, gx, gy, gz, ek, et, cp);
                 const uint32_t b = i / N, p = i - b * N;
                 float4 m4 = mom[(size_t)b * n_pad + p];
                 if (s == 0) em = AddSq(AddSq(AddSq(em, m4.x), m4.y), m4.z);  // |P|^2 before the first kick
@@ -1258,6 +1260,7 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
     CudaCheck(cudaMemset(acc_->ptr, 0, n_chains * sizeof(uint64_t)), "memset");
     CudaCheck(cudaMemset(n_meas_->ptr, 0, n_chains * sizeof(uint64_t)), "memset");
     CudaCheck(cudaMemset(err_->ptr, 0, sizeof(int)), "memset");
+    CudaCheck(cudaStreamSynchronize(cudaStreamLegacy), "memset completion");  // before any work on `stream`
     // Energy tasks: kEnergySlices slices of one chain each, chains in index order.
     std::vector<EnergyTask> tasks;
     std::vector<uint32_t> first(n_chains + 1, 0);
@@ -1386,7 +1389,8 @@ void ChainBatch::SetPaths(const double* all) {
     CudaCheck(cudaMemcpyAsync(&e, err_->ptr, sizeof(int), cudaMemcpyDeviceToHost, stream), "read error word");
     CudaCheck(cudaStreamSynchronize(stream), "sync");
     if (e & kDevErrNonFinite) {
-        CudaCheck(cudaMemset(err_->ptr, 0, sizeof(int)), "clear error");
+        CudaCheck(cudaMemsetAsync(err_->ptr, 0, sizeof(int), stream), "clear error");
+        CudaCheck(cudaStreamSynchronize(stream), "sync");
         throw PimcError(kErrArg, "non-finite position");
     }
 }

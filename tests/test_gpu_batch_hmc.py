@@ -19,7 +19,7 @@ pytestmark = pytest.mark.gpu
 SHAPES = [(5, 16, 2), (17, 32, 3), (33, 64, 3), (64, 32, 2), (40, 128, 3)]
 
 
-def _items(tmp_path, hmc=(0.005, 8)):
+def _items(tmp_path, hmc=(0.03, 10)):
     out = []
     for c, (n, m, lvl) in enumerate(SHAPES):
         xml, p = trapped_coulomb(tmp_path, n_part=n, n_bead=m, n_level=lvl, seed=300 + c, hmc=hmc)
