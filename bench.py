@@ -1,20 +1,26 @@
 #!/usr/bin/env python3
-"""Benchmark: bead-moves/s of path-integral Monte Carlo bisection sweeps on one GB300.
+"""Benchmark: bead-moves/s of path-integral Monte Carlo on one GB300, batched + adjoint.
 
-Headline workload (one "step" = one measurement cycle, replayed as a CUDA graph: one sweep of
-every chain, then one thermal-energy measurement of every chain): 256 independent chains of
-distinguishable unit-mass particles in an isotropic 3-D harmonic trap (omega = 1) with bare
-Coulomb repulsion (primitive action), open boundaries, beta = 2; chain c has seed 1000 + c,
-N drawn uniformly from {16..128} and M from {32, 64, 128} by a generator seeded with 1000;
-bisection level 3 (7 resampled beads per attempt); a sweep of a chain is N ceil(M / 8) attempts.
-FP32 positions and action terms, compensated sums, double-float acceptance, FP64 estimators.
-Synthetic data: beads i.i.d. N(0, 1) from each chain's seed, then untimed warm-up cycles.
+Headline workload (one "step" = one measurement cycle, replayed as a CUDA graph: one bisection sweep
+of every chain, one hybrid Monte Carlo attempt of every chain on the exact (adjoint) gradient, then
+one thermal-energy measurement of every chain): 256 independent chains of distinguishable unit-mass
+particles in an isotropic 3-D harmonic trap (omega = 1) with bare Coulomb repulsion (primitive
+action), open boundaries, beta = 2; chain c has seed 1000 + c, N drawn uniformly from {16..128} and
+M from {32, 64, 128} by a generator seeded with 1000. Bisection level 3 (7 resampled beads per
+attempt; a sweep of a chain is N ceil(M / 8) attempts); HMC step 0.005 with 10 leapfrog steps
+(every one of the chain's N M beads moves per attempt). FP32 positions, action terms and forces,
+compensated sums, double-float acceptance, FP64 estimators. Synthetic data: beads i.i.d. N(0, 1)
+from each chain's seed, then untimed warm-up cycles.
 
 Also reported on the same line:
-  plain_same_system  the single-chain FP64 sweep kernel run on a sample of the same chains, one
-                     chain at a time (what the batched kernel replaces);
+  components         the bisection sweep kernel and the HMC kernel timed alone (bead-moves/s each,
+                     HMC acceptance), with a roofline for each;
+  plain_same_system  the single-chain GPU path (double-float sweep kernel, FP64 HMC) running the
+                     same cycle on a sample of the same chains, one chain at a time (what the
+                     batched kernels replace);
   energy_gate        per-chain energies and blocking error bars of the batched FP32 chains
-                     against the single-chain FP64 path on the same chains and seeds;
+                     against the single-chain path on the same chains and seeds, after an
+                     equilibration of the paths;
   plain_electron_gas the single-chain FP64 kernel on the 66-electron gas (r_s = 2, beta = 8,
                      M = 128, Ewald |k| < 12 (2 pi / L), 3561 half-space k-vectors, level 4);
   exchange_bosons    32 trapped bosons with PermBisectIterative on the permutation kernel, with
@@ -28,9 +34,10 @@ Arms:
   (default)          the CUDA library. `value` = device-timed cycles with the paths resident in
                      HBM; `e2e` = the same cycles through the C interface with every chain's path
                      uploaded from and downloaded to host memory and the energies read back.
-  --impl reference   the CPU restatement of the reference hot path (the reference itself does not
-                     build here: its scaffold/einspline/Armadillo/HDF5 dependencies are absent) on
-                     the same chains, one chain per host thread, on a bounded sample per step.
+  --impl reference   the FP64 CPU restatement of the reference hot path (the reference's own headers
+                     build only against oracle/refshim where its checkout exists, not on the GPU box;
+                     the restatement is pinned to that build) running the same cycle on the same
+                     chains, one group of chains per host thread, on a bounded sample per step.
 """
 from __future__ import annotations
 
@@ -55,9 +62,11 @@ from simpimc_gb300.stats import blocking_error  # noqa: E402
 
 METRIC = "bead-moves/s"
 N_CHAINS, SEED0, CHAIN_LEVEL = 256, 1000, 3
+HMC = (0.005, 10)  # leapfrog step, steps per attempt
 WORKLOAD = ("256 independent harmonic-trap Coulomb chains (omega=1, beta=2, open), N~U{16..128}, M in {32,64,128}, "
-            "bisection level 3, seeds 1000+c; one step = one sweep of every chain + one energy measurement (CUDA graph); "
-            "FP32 action terms, compensated sums, double-float acceptance")
+            "seeds 1000+c; one step = one bisection sweep (level 3) + one HMC attempt (step 0.005 x 10, exact gradient) "
+            "of every chain + one energy measurement (CUDA graph); FP32 positions/terms/forces, compensated sums, "
+            "double-float acceptance")
 EGAS = dict(n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_units=12.0, n_level=4)
 
 
@@ -70,7 +79,31 @@ def rank_chain_seed0(rank):
 
 def chains_workload(tmp, rank=0):
     from simpimc_gb300.configs import batched_trap_chains
-    return batched_trap_chains(tmp, n_chains=N_CHAINS, seed0=SEED0, n_level=CHAIN_LEVEL, chain_seed0=rank_chain_seed0(rank))
+    return batched_trap_chains(tmp, n_chains=N_CHAINS, seed0=SEED0, n_level=CHAIN_LEVEL, chain_seed0=rank_chain_seed0(rank), hmc=HMC)
+
+
+def chain_cycle_moves(n, m):
+    """Bead-moves of one chain's cycle: a bisection sweep (N ceil(M / 2^l) attempts of 2^l - 1
+    beads) and one HMC attempt (all N M beads)."""
+    B = 1 << CHAIN_LEVEL
+    return n * math.ceil(m / B) * (B - 1) + n * m
+
+
+def hmc_pair_flops(shapes):
+    """Algorithmic FP32 flops of one HMC attempt of every chain: (steps + 1) gradient passes, each
+    N (N - 1) M pair evaluations of 16 flops (3 differences, r^2 in 5, r^-3 in 2, three force FMAs in
+    6, an FMA counted as two) plus N M beads of 24 flops (kinetic links and trap)."""
+    per = 0
+    for n, m, _ in shapes:
+        per += n * (n - 1) * m * 16 + n * m * 24
+    return (HMC[1] + 1) * per
+
+
+def fp32_peak_tflops(device, sm_mhz):
+    """Nominal FP32 CUDA-core peak: SMs x 128 FP32 lanes x 2 flops (FMA) x SM clock."""
+    import torch
+    n_sm = torch.cuda.get_device_properties(device).multi_processor_count
+    return n_sm * 128 * 2 * sm_mhz * 1e6 / 1e12
 
 
 def clocks_sampler(out_path):
@@ -137,8 +170,9 @@ def batch_algorithmic_bytes(batch, att, acc):
     return total
 
 
-def time_plain_chains(items, tmp, local, sample, sweeps=2):
-    """The single-chain FP64 sweep kernel on `sample` chains, one after the other (device time)."""
+def time_plain_chains(items, tmp, local, sample, cycles=2):
+    """The single-chain GPU path (double-float sweep kernel, FP64 HMC) running the batch's cycle on
+    `sample` chains, one after the other: device time and bead-moves."""
     import torch
     from simpimc_gb300 import Simulation
     moves, secs = 0, 0.0
@@ -146,54 +180,63 @@ def time_plain_chains(items, tmp, local, sample, sweeps=2):
         xml, path = items[c]
         s = Simulation(xml, base_dir=tmp, device=local, chain=c)
         s.set_path(path)
-        reps = s.species_info(0)[0] * math.ceil(s.n_bead / (1 << CHAIN_LEVEL))
+        n, m = s.species_info(0)[0], s.n_bead
+        reps = n * math.ceil(m / (1 << CHAIN_LEVEL))
         st = torch.cuda.ExternalStream(s._lib.pimc_stream(s._h), device=torch.device("cuda", local))
-        s.sweep([0], [1], reps)  # warm-up
+        s.sweep([0, 1], [reps, 1], 1)  # warm-up cycle
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st)
-        s.sweep([0], [1], reps * sweeps)
+        s.sweep([0, 1], [reps, 1], cycles)
         e1.record(st)
         e1.synchronize()
         secs += e0.elapsed_time(e1) / 1e3
-        moves += reps * sweeps * ((1 << CHAIN_LEVEL) - 1)
+        moves += cycles * chain_cycle_moves(n, m)
         s.close()
     return moves, secs
 
 
-def energy_gate(items, tmp, local, chains, sweeps):
-    """Batched FP32 chains against the single-chain FP64 path on the same chains and seeds: per
-    chain the mean energy and its blocking error bar over `sweeps` measurements."""
+def energy_gate(items, tmp, local, chains, equil, cycles):
+    """Batched FP32 chains against the single-chain path (double-float bisection, FP64 HMC) on the same
+    chains and seeds: `equil` untimed cycles to equilibrate the paths, then per chain the mean energy
+    and its blocking error bar over `cycles` measurements (one per cycle)."""
     from simpimc_gb300 import ChainBatch, Simulation
     sub = [items[c] for c in chains]
     b = ChainBatch([x for x, _ in sub], base_dir=tmp, device=local)
-    # The batch numbers its chains 0..k-1; the FP64 contexts use the same chain indices.
+    # The batch numbers its chains 0..k-1; the single-chain contexts use the same chain indices.
     for i, (_, p) in enumerate(sub):
         b.set_path(i, p)
-    b.run(sweeps, 1)
+    b.set_hmc_per_cycle(1)
+    b.run(equil, 1)
+    b.reset_energy()
+    b.run(cycles, 1)
     rows = []
     for i, (xml, p) in enumerate(sub):
-        e32, n = b.energy(i, cap=sweeps)
+        e32, n = b.energy(i, cap=cycles)
         s = Simulation(xml, base_dir=tmp, device=local, chain=i)
         s.set_path(p)
         reps = s.species_info(0)[0] * math.ceil(s.n_bead / (1 << CHAIN_LEVEL))
+        s.sweep([0, 1], [reps, 1], equil)
         e64 = []
-        for _ in range(sweeps):
-            s.sweep([0], [1], reps)
+        for _ in range(cycles):
+            s.sweep([0, 1], [reps, 1], 1)
             s.observable_accumulate(0)
             e64.append(s.observable_block(0)[0])
+        hacc = s.move_counters(1)[3]
         s.close()
         a32, a64 = e32[:, 0], np.asarray(e64)
         err32, err64 = blocking_error(a32), blocking_error(a64)
         rows.append({"chain": chains[i], "shape": list(b.shapes[i][:2]), "E_fp32": float(a32.mean()), "err_fp32": err32,
                      "E_fp64": float(a64.mean()), "err_fp64": err64,
                      "err_ratio": err32 / err64 if err64 > 0 else None,
-                     "max_abs_diff_per_measurement": float(np.max(np.abs(a32 - a64)))})
+                     "max_abs_diff_per_measurement": float(np.max(np.abs(a32 - a64))),
+                     "hmc_acceptance": hacc / max(equil + cycles, 1)})
     b.close()
     ratios = [r["err_ratio"] for r in rows if r["err_ratio"]]
-    return {"sweeps": sweeps, "chains": rows,
+    return {"equilibration_cycles": equil, "cycles": cycles, "chains": rows,
             "max_err_ratio_deviation": max(abs(r - 1.0) for r in ratios) if ratios else None,
-            "note": "chain i of the batch and the FP64 context with chain=i draw the same random stream"}
+            "note": "chain i of the batch and the single-chain context with chain=i draw the same random streams; "
+                    "the paths are equilibrated before the measured cycles"}
 
 
 def egas_plain(local, steps, warmup, tmp, flush):
@@ -454,7 +497,8 @@ def exchange_bosons_chains(local, tmp, n_chains=608, sweeps=10):
 
 
 def cpu_oracle_chains(items, tmp, seconds, chains):
-    """The oracle on one host core, cycling through `chains` in chunks of attempts."""
+    """The oracle on one host core, running the batch's cycle (bisection sweep + HMC attempt) on
+    `chains` round robin."""
     import oracle
     oracle.build()
     sims = []
@@ -462,16 +506,37 @@ def cpu_oracle_chains(items, tmp, seconds, chains):
         xml, p = items[c]
         o = oracle.OracleSim(xml, base_dir=tmp, chain=c)
         o.set_path(p)
-        sims.append(o)
-    moves, t0 = 0, time.perf_counter()
+        n, m = p.shape[0], p.shape[1]
+        sims.append((o, n * math.ceil(m / (1 << CHAIN_LEVEL)), chain_cycle_moves(n, m)))
+    moves, cycles, t0 = 0, 0, time.perf_counter()
     while time.perf_counter() - t0 < seconds:
-        for o in sims:
-            o.move_attempts(0, 64)
-            moves += 64 * ((1 << CHAIN_LEVEL) - 1)
+        for o, reps, mv in sims:
+            o.move_attempts(0, reps)
+            o.move_attempts(1, 1)
+            moves += mv
+            cycles += 1
+            if time.perf_counter() - t0 >= seconds:
+                break
     el = time.perf_counter() - t0
-    for o in sims:
+    for o, _, _ in sims:
         o.close()
-    return moves, el
+    return moves, el, cycles
+
+
+def time_launches(stream, flush, steps, fn):
+    """Device milliseconds of `steps` calls of fn() on `stream`, with an L2 flush before each."""
+    import torch
+    ms = 0.0
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        ms += e0.elapsed_time(e1)
+    return ms
 
 
 def run_ours(args):
@@ -496,48 +561,36 @@ def run_ours(args):
     batch.set_paths(flat0)
     stream = torch.cuda.ExternalStream(batch.stream(), device=torch.device("cuda", local))
     per_sweep = batch.stats()["bead_moves_per_sweep"]
+    per_hmc = sum(n * m for n, m, _ in batch.shapes)
+    per_step = per_sweep + per_hmc
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
 
-    # Clock samples cover the autotuner, the warm-up and the three timed loops below (the timed
-    # loops alone are too short for the sampler's period); the GPU runs the same kernels throughout.
+    # Clock samples cover the autotuner, the warm-up and the timed loops below (the timed loops alone
+    # are too short for the sampler's period); the GPU runs the same kernels throughout.
     clk_file = Path(tmp) / "clocks.csv"
     sampler = clocks_sampler(clk_file) if rank == 0 else None
     ipl, mw, wave, tune_s = batch.autotune(2)
+    batch.set_hmc_per_cycle(1)
     batch.run(args.warmup, 1)
     batch.synchronize()
     att0, acc0 = batch.counters()
+    hatt0, hacc0 = batch.hmc_counters()
     launches0 = batch.stats()["kernel_launches"]
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    ms = 0.0
     t_wall = time.perf_counter()
-    for _ in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.zero_()  # L2 flush between timed steps (untimed)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        batch.run(1, 1)
-        e1.record(stream)
-        e1.synchronize()
-        ms += e0.elapsed_time(e1)
+    ms = time_launches(stream, flush, args.steps, lambda: batch.run(1, 1))
     torch.cuda.synchronize()
     wall = time.perf_counter() - t_wall
     launches = batch.stats()["kernel_launches"] - launches0
     att1, acc1 = batch.counters()
+    hatt1, hacc1 = batch.hmc_counters()
 
-    # Sweep kernel alone (for its roofline): one launch per step, same flush.
-    k_ms = 0.0
-    for _ in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        batch.sweeps(1)
-        e1.record(stream)
-        e1.synchronize()
-        k_ms += e0.elapsed_time(e1)
+    # The two kernels alone (for their rooflines): one launch per step, same flush.
+    k_ms = time_launches(stream, flush, args.steps, lambda: batch.sweeps(1))
     att2, acc2 = batch.counters()
+    h_ms = time_launches(stream, flush, args.steps, lambda: batch.hmc_attempts(1))
 
     # e2e: every chain's path from pinned host memory, one cycle, energies and paths back, every step.
     host = torch.empty(batch.get_paths().size, dtype=torch.float64, pin_memory=True).numpy()
@@ -558,14 +611,15 @@ def run_ours(args):
         sampler.wait()
     assert np.all(np.isfinite(energies))
 
-    ms_max, e2e_max, k_max = reduce_max_over_ranks([ms, e2e_ms, k_ms], dist, device=f"cuda:{local}")
-    value = per_sweep * args.steps * world / (ms_max / 1e3)
-    e2e_value = per_sweep * args.steps * world / (e2e_max / 1e3)
+    ms_max, e2e_max, k_max, h_max = reduce_max_over_ranks([ms, e2e_ms, k_ms, h_ms], dist, device=f"cuda:{local}")
+    value = per_step * args.steps * world / (ms_max / 1e3)
+    e2e_value = per_step * args.steps * world / (e2e_max / 1e3)
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return
 
+    clocks = clocks_summary(clk_file, local)
     peak, peak_kind = measured_hbm_peak()
     alg = batch_algorithmic_bytes(batch, att2 - att1, acc2 - acc1) / args.steps
     achieved = alg / (k_max / args.steps / 1e3) / 1e9
@@ -573,12 +627,27 @@ def run_ours(args):
     tf = ROOT / "profiles" / "batch_sweep_traffic.json"
     if tf.exists():
         traffic = json.loads(tf.read_text()).get("dram_bytes_per_sweep")
+    sweep_roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                  "peak_kind": peak_kind, "kernel": "BatchSweepKernel", "algorithmic_bytes_per_launch": alg,
+                  "ms_per_launch": k_max / args.steps,
+                  "note": "operands are re-read from shared memory and L2; the kernel is bound by its longest chain's serial "
+                          "rounds (SM issue), see profiles/batch_sweep_256chains.md"}
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
+    fp32_peak = fp32_peak_tflops(local, sm_mhz)
+    flops = hmc_pair_flops(batch.shapes)
+    h_achieved = flops / (h_max / args.steps / 1e3) / 1e12
+    hmc_roof = {"bound": "fp32", "achieved": h_achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": h_achieved / fp32_peak,
+                "traffic": None, "peak_kind": "nominal: SMs x 128 FP32 lanes x 2 flops (FMA) x the median sampled SM clock "
+                                             "(no measured FP32 peak in MEASURED_PEAKS.json)",
+                "kernel": "BatchHmcKernel", "algorithmic_flops_per_launch": flops, "ms_per_launch": h_max / args.steps}
+    dominant = hmc_roof if h_max >= k_max else sweep_roof
     sample = list(range(0, N_CHAINS, N_CHAINS // 8))
     pm, psec = time_plain_chains(items, tmp, local, sample)
     plain = {"value": pm / psec, "unit": METRIC, "chains": sample,
-             "note": "single-chain FP64 sweep kernel, one chain after another, device time"}
-    cheap = sorted(range(N_CHAINS), key=lambda c: batch.shapes[c][0] ** 2 * batch.shapes[c][1])[:4]
-    gate = energy_gate(items, tmp, local, chains=cheap, sweeps=args.gate_sweeps)
+             "note": "single-chain path (double-float sweep kernel + FP64 HMC), the same cycle, one chain after another, device time"}
+    mid = sorted(range(N_CHAINS), key=lambda c: batch.shapes[c][0] ** 2 * batch.shapes[c][1])
+    gate_chains = [mid[len(mid) // 8], mid[len(mid) // 4], mid[3 * len(mid) // 8], mid[len(mid) // 2]]
+    gate = energy_gate(items, tmp, local, chains=gate_chains, equil=args.gate_equil, cycles=args.gate_sweeps)
     eg, _, _, _ = egas_plain(local, args.steps, args.warmup, tmp, flush)
     large = large_mixed_precision(local, tmp) if not args.no_large else None
     hmc = hmc_adjoint(local, tmp) if not args.no_large else None
@@ -586,27 +655,33 @@ def run_ours(args):
     exch["many_chains"] = exchange_bosons_chains(local, tmp)
     cpu = None
     if not args.no_cpu_baseline:
-        moves, el = cpu_oracle_chains(items, tmp, 12.0, sample)
+        moves, el, cyc = cpu_oracle_chains(items, tmp, 12.0, sample)
         cpu = {"value": moves / el, "unit": METRIC, "cores": 1, "kind": "port",
-               "sample": f"{moves // 7} bisection attempts ({el:.1f} s) on chains {sample}, round robin in chunks of 64"}
+               "sample": f"{cyc} chain cycles (bisection sweep + HMC attempt, {el:.1f} s) on chains {sample}, round robin"}
     path_bytes_h2d = int(host.nbytes)  # every chain's path as doubles, copied as they are
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Gaussian beads per chain, warmed up)",
-        "config": {"workload": WORKLOAD, "n_chains": N_CHAINS, "bead_moves_per_step": per_sweep,
+        "config": {"workload": WORKLOAD, "n_chains": N_CHAINS, "bead_moves_per_step": per_step,
+                   "bead_moves_per_step_bisection": per_sweep, "bead_moves_per_step_hmc": per_hmc,
                    "tile": {"items_per_lane": ipl, "max_warps": mw, "wave": wave, "autotune_s_per_sweep": tune_s},
-                   "acceptance": float((acc1 - acc0).sum() / max((att1 - att0).sum(), 1)),
+                   "bisection_acceptance": float((acc1 - acc0).sum() / max((att1 - att0).sum(), 1)),
+                   "hmc_acceptance": float((hacc1 - hacc0).sum() / max((hatt1 - hatt0).sum(), 1)),
                    "l2": "256 MB flush between timed steps", "parallelism": "replicas (independent chains per GPU)"},
-        "clocks": dict(clocks_summary(clk_file, local), window="autotune, warm-up and the three timed loops, 50 ms period"),
+        "clocks": dict(clocks, window="autotune, warm-up and the timed loops, 50 ms period"),
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": path_bytes_h2d,
                 "d2h_bytes_per_step": path_bytes_h2d + N_CHAINS * 4 * 8,
                 "note": "pimc_batch_set_paths + pimc_batch_run(1 cycle) + pimc_batch_last_energy + pimc_batch_get_paths per step, "
                         "paths in pinned host memory"},
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_kind": peak_kind, "kernel": "BatchSweepKernel",
-                     "algorithmic_bytes_per_launch": alg, "ms_per_launch": k_max / args.steps},
+        "roofline": dominant,
+        "components": {
+            "bisection_sweep": {"value": per_sweep / (k_max / args.steps / 1e3), "unit": METRIC, "ms_per_launch": k_max / args.steps,
+                                "roofline": sweep_roof},
+            "hmc": {"value": per_hmc / (h_max / args.steps / 1e3), "unit": METRIC, "ms_per_launch": h_max / args.steps,
+                    "leapfrog": {"step": HMC[0], "n_steps": HMC[1]}, "roofline": hmc_roof},
+        },
         "cpu_baseline": cpu,
         "plain_same_system": plain,
         "speedup_vs_plain_same_system": value / plain["value"],
@@ -623,20 +698,26 @@ def run_ours(args):
 
 
 def _oracle_worker(items, tmp, chains, seconds, results, idx):
+    """One host thread: the oracle running the batch's cycle (bisection sweep + HMC attempt) on its
+    share of the chains, round robin, for `seconds`."""
     import oracle
     sims = []
     for c in chains:
         xml, p = items[c]
         o = oracle.OracleSim(xml, base_dir=tmp, chain=c)
         o.set_path(p)
-        sims.append(o)
+        n, m = p.shape[0], p.shape[1]
+        sims.append((o, n * math.ceil(m / (1 << CHAIN_LEVEL)), chain_cycle_moves(n, m)))
     moves, t0 = 0, time.perf_counter()
     while time.perf_counter() - t0 < seconds:
-        for o in sims:
-            o.move_attempts(0, 64)
-            moves += 64 * ((1 << CHAIN_LEVEL) - 1)
+        for o, reps, mv in sims:
+            o.move_attempts(0, reps)
+            o.move_attempts(1, 1)
+            moves += mv
+            if time.perf_counter() - t0 >= seconds:
+                break
     results[idx] = (moves, time.perf_counter() - t0)
-    for o in sims:
+    for o, _, _ in sims:
         o.close()
 
 
@@ -657,12 +738,12 @@ def run_reference(args):
         res = [None] * threads
         groups = [list(range(i, N_CHAINS, threads)) for i in range(threads)]
         ths = [threading.Thread(target=_oracle_worker, args=(items, tmp, groups[i], per_step_s, res, i)) for i in range(threads)]
-        t0 = time.perf_counter()
         for t in ths:
             t.start()
         for t in ths:
             t.join()
-        total_s += time.perf_counter() - t0
+        # each thread times its own cycles (after building its chains); the step lasts as long as the slowest
+        total_s += max(r[1] for r in res)
         total_moves += sum(r[0] for r in res)
     value = total_moves / total_s
     line = {
@@ -671,8 +752,10 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian beads per chain)",
         "config": {"workload": WORKLOAD, "n_chains": N_CHAINS, "l2": "n/a (host)"}, "impl": "reference",
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
-                         "sample": f"{threads} threads, each cycling through its share of the 256 chains for {per_step_s:.0f} s per "
-                                   "step (CPU restatement; the reference's own build needs absent dependencies)"},
+                         "sample": f"{threads} threads, each running the cycle (bisection sweep + HMC attempt) on its share of "
+                                   f"the 256 chains for {per_step_s:.0f} s per step (the FP64 CPU restatement: the reference's "
+                                   "own headers build only against oracle/refshim with the reference checkout, absent on the GPU "
+                                   "box; tests/test_reference_pins.py pins the restatement to that build)"},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -685,7 +768,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--gate-sweeps", type=int, default=400)
+    ap.add_argument("--gate-sweeps", type=int, default=300, help="measured cycles of the energy gate")
+    ap.add_argument("--gate-equil", type=int, default=100, help="equilibration cycles of the energy gate")
     ap.add_argument("--no-large", action="store_true", help="skip the N=1024 mixed-precision leg")
     args = ap.parse_args()
     if args.warmup < 3:
