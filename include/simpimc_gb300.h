@@ -242,14 +242,22 @@ int pimc_batch_counters(pimc_batch* b, uint64_t* attempts, uint64_t* accepts);
  * input, as in a single-chain context), runs the leapfrog on S(R) + |P|^2/2 with the exact gradient
  * of the whole-ring kinetic, trap and bare Coulomb action (pimc_action_gradient_path), and accepts
  * with probability min(1, exp(-dH)). Positions, momenta and forces are FP32; both energies are
- * double-float sums of exact differences and dH is FP64. One block per chain holds the chain's path
- * in shared memory, which limits such a chain to 12 n_part n_bead bytes of it (n_part n_bead <=
- * 18,000 or so). pimc_batch_hmc_attempts runs n attempts on every chain with the move;
+ * double-float sums of exact differences and dH is FP64. Each chain runs on a thread-block cluster
+ * of k = 1, 2, 4 or 8 blocks (one k for the launch; it must divide every HMC chain's n_bead): block r
+ * holds slices [r n_bead / k, (r + 1) n_bead / k) with one halo slice on each side and their momenta
+ * in shared memory, 24 n_part (n_bead / k + 1) bytes, and reads the halos from its neighbours'
+ * shared memory after every drift. The trajectory does not depend on k (every bead's force and
+ * update is the same FP32 sequence); the energies' last bits may. pimc_batch_hmc_attempts runs n
+ * attempts on every chain with the move;
  * pimc_batch_hmc_counters reads their attempt and accept counters; pimc_batch_set_hmc_per_cycle adds
- * n attempts to every measurement cycle of pimc_batch_run (after the sweeps). */
+ * n attempts to every measurement cycle of pimc_batch_run (after the sweeps);
+ * pimc_batch_set_hmc_cluster / pimc_batch_get_hmc_cluster set and read k (pimc_batch_autotune picks
+ * the fastest that fits; error kErrUnsupported where k does not divide an n_bead or does not fit). */
 int pimc_batch_hmc_attempts(pimc_batch* b, uint64_t n);
 int pimc_batch_hmc_counters(pimc_batch* b, uint64_t* attempts, uint64_t* accepts);
 int pimc_batch_set_hmc_per_cycle(pimc_batch* b, uint64_t n);
+int pimc_batch_set_hmc_cluster(pimc_batch* b, uint32_t k);
+int pimc_batch_get_hmc_cluster(pimc_batch* b, uint32_t* k);
 /* Tiles: one attempt wants ceil((n_part-1)(2^n_level-1) / (32 items_per_lane)) warps for its pair
  * items; with wave = 1 a chain gets that many, at most max_warps (<= 16). With wave = W > 1 (<= 4)
  * a chain runs up to W attempts at once on W groups of such warps (at least 2 each, W times at

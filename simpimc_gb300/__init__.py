@@ -110,6 +110,8 @@ SIGNATURES = {
     "pimc_batch_hmc_attempts": (C.c_int, [_P, C.c_uint64]),
     "pimc_batch_hmc_counters": (C.c_int, [_P, _U64P, _U64P]),
     "pimc_batch_set_hmc_per_cycle": (C.c_int, [_P, C.c_uint64]),
+    "pimc_batch_set_hmc_cluster": (C.c_int, [_P, C.c_uint32]),
+    "pimc_batch_get_hmc_cluster": (C.c_int, [_P, _U32P]),
     "pimc_batch_set_tiles": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32]),
     "pimc_batch_autotune": (C.c_int, [_P, C.c_uint32, _U32P, _U32P, _U32P, _DP]),
     "pimc_batch_stats": (C.c_int, [_P, _U64P]),
@@ -509,6 +511,17 @@ class ChainBatch:
     def set_hmc_per_cycle(self, n: int):
         """HMC attempts in every measurement cycle of run() (after the sweeps)."""
         self._check(self._lib.pimc_batch_set_hmc_per_cycle(self._h, n))
+
+    @property
+    def hmc_cluster(self) -> int:
+        """Thread blocks per chain (one cluster) of the HMC launch."""
+        k = C.c_uint32()
+        self._check(self._lib.pimc_batch_get_hmc_cluster(self._h, C.byref(k)))
+        return k.value
+
+    @hmc_cluster.setter
+    def hmc_cluster(self, k: int):
+        self._check(self._lib.pimc_batch_set_hmc_cluster(self._h, k))
 
     def set_tiles(self, items_per_lane: int, max_warps: int, wave: int = 1):
         self._check(self._lib.pimc_batch_set_tiles(self._h, items_per_lane, max_warps, wave))

@@ -89,6 +89,8 @@ class ChainBatch {
     void HmcAttempts(uint64_t n);             // n HMC attempts on every chain that has the move
     void ReadHmcCounters(uint64_t* attempts, uint64_t* accepts);
     void SetHmcPerCycle(uint64_t n);          // HMC attempts in each graph-replayed cycle
+    void SetHmcCluster(uint32_t k);           // thread blocks per chain in the HMC launch (1, 2, 4, 8)
+    size_t HmcSmem(uint32_t k) const;         // dynamic shared memory of one HMC block; 0 if k is invalid
     void Sweeps(uint64_t n);                  // n sweeps on every chain (one launch)
     void Measure();                           // one energy measurement on every chain
     void Run(uint64_t n_cycles, uint64_t sweeps_per_measure);  // graph-replayed cycles
@@ -96,7 +98,7 @@ class ChainBatch {
     void ResetEnergy();
     void ReadCounters(uint64_t* attempts, uint64_t* accepts);
     void SetTiles(uint32_t items_per_lane, uint32_t max_warps, uint32_t wave);
-    double Autotune(uint32_t trial_sweeps);   // returns the best trial's seconds per sweep
+    double Autotune(uint32_t trial_sweeps);   // returns the best trial's seconds per sweep (also picks hmc_cluster)
     void Sync();
 
     uint32_t n_chains = 0, series_cap = 0;
@@ -109,7 +111,8 @@ class ChainBatch {
     uint64_t bead_moves_per_sweep = 0;
     uint64_t bead_moves_per_hmc = 0;  // beads one HMC attempt of every chain moves (n_part n_bead each)
     uint64_t hmc_per_cycle = 0;
-    size_t hmc_smem = 0;              // shared memory of the HMC launch (largest chain's path planes)
+    uint32_t hmc_cluster = 1;         // thread blocks (one cluster) per chain in the HMC launch
+    size_t hmc_smem_cap = 0;          // dynamic shared memory a block of the HMC launch may take
     uint64_t path_doubles = 0;  // sum of n_part * n_bead * 3 over the chains
     uint64_t kernel_launches = 0;
     size_t stage_cap = 0;     // shared memory a sweep block may take for a staged path
@@ -122,7 +125,8 @@ class ChainBatch {
     void LaunchMeasure();
     void ResetGraph();
     std::unique_ptr<DeviceBuffer> pos_, chains_dev_, order_dev_, att_, acc_, series_, n_meas_, err_, last_;
-    std::unique_ptr<DeviceBuffer> mom_, hmc_att_, hmc_acc_;  // HMC momenta (layout of pos_), counters
+    std::unique_ptr<DeviceBuffer> hmc_att_, hmc_acc_;  // HMC counters per chain
+    bool HmcClusterFits(uint32_t k) const;
     std::vector<uint64_t> path_off_;  // first double of each chain in the concatenated host layout
     std::unique_ptr<DeviceBuffer> dstage_, path_off_dev_;  // host-layout doubles on the device, offsets
     size_t pos_float4 = 0;

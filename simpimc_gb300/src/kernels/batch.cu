@@ -26,6 +26,8 @@
 #include <ctime>
 #include <numeric>
 
+#include <cooperative_groups.h>
+
 #include "../../../include/simpimc_gb300.h"
 #include "../common/philox.h"
 #include "../framework/batch.h"
@@ -839,23 +841,25 @@ __global__ void BatchEnergyFinishKernel(BatchArgs a, const uint32_t* __restrict_
 
 // ---------------------------------------------------------------------------------------------
 // Hybrid Monte Carlo on every chain (the library's whole-path HMC move; no reference counterpart).
-// One block per chain runs its attempts: momenta P ~ N(0, 1) per coordinate from the attempt's
-// counter-based stream (normal j of the path-ordered coordinates (p, b, d) is component j % 4 of
-// Philox block 1 + j / 4, as the single-chain move draws them); leapfrog on H = S(R) + |P|^2 / 2
-// with the exact gradient of the whole-ring action at level 0
+// Each chain runs on a cluster of k thread blocks (k = 1, 2, 4 or 8, the same for the launch): block
+// r of the cluster owns slices [r M / k, (r + 1) M / k). Per attempt: momenta P ~ N(0, 1) per
+// coordinate from the attempt's counter-based stream (normal j of the path-ordered coordinates
+// (p, b, d) is component j % 4 of Philox block 1 + j / 4, as the single-chain move draws them);
+// leapfrog on H = S(R) + |P|^2 / 2 with the exact gradient of the whole-ring action at level 0
 //   S = sum_{p,b} |r_{b+1} - r_b|^2 / (4 lambda tau)        (Kinetic, n_images 0)
 //     + cofactor_a sum_{p,b} r^2                           (HarmonicTrap)
 //     + tau sum_b sum_{p<q} V(|r_p - r_q|), V = 1/r clamped to the table's r range (BarePairAction);
 // then acceptance with probability min(1, exp(-dH)) against the log-uniform of block 0, word 0.
-// The path sits in shared memory as three FP32 planes [M][N]; momenta live in global memory in the
-// layout of the positions. Forces and leapfrog updates are FP32 (each thread owns fixed beads);
-// both energies are sums of exact differences and products in double-float, and dH is formed in
-// FP64 from them, so the decision sees the trajectory's energy change to ~1e-6 absolute.
-constexpr uint32_t kHmcThreads = 1024;
+// A block keeps its slices and one halo slice on each side in shared memory as three FP32 planes
+// [nb + 2][N], and its beads' momenta as three planes [nb][N]; after every drift the halos are read
+// from the neighbouring blocks' shared memory (distributed shared memory, between two cluster
+// barriers). Forces and leapfrog updates are FP32 (each thread owns fixed beads); both energies are
+// sums of exact differences and products in double-float, reduced over the cluster in block order,
+// and dH is formed in FP64, so the decision sees the trajectory's energy change to ~1e-6 absolute.
+constexpr uint32_t kHmcThreads = 512;
 
 struct HmcArgs {
-    float4* mom;     // per chain, the layout of pos: [n_bead][n_pad] (x, y, z, 0)
-    uint64_t* att;   // per chain: HMC attempts (the move's Philox attempt counter)
+    uint64_t* att;  // per chain: HMC attempts (the move's Philox attempt counter)
     uint64_t* acc;
     uint32_t n_attempts;
 };
@@ -871,16 +875,15 @@ __device__ __forceinline__ void BlockSum4DD(dd v[4], dd (*s_red)[kHmcThreads / 3
     for (int q = 0; q < 4; ++q) v[q] = WarpSumDD(lane < nw ? s_red[q][lane] : DD(0.f));
 }
 
-/// Gradient dS/dr of bead i = b N + p (FP32) and, when `with_energy`, its share of S: the link
-/// b -> b+1, its trap term and half its pair sum (every pair is met twice).
+/// Gradient dS/dr (FP32) of the bead in row `row` (1..nb), particle p, of the block's planes and,
+/// with kEnergy, its share of S: the link to the next slice, its trap term and half its pair sum
+/// (every pair is met twice). Rows row - 1 and row + 1 hold the neighbouring slices.
 template <bool kPbc, bool kEnergy>
 __device__ __forceinline__ void HmcBead(const ChainDev& c, const float* __restrict__ sx, const float* __restrict__ sy,
-                                        const float* __restrict__ sz, uint32_t N, uint32_t M, uint32_t i, float i4, float cofa, float tau,
+                                        const float* __restrict__ sz, uint32_t N, uint32_t row, uint32_t p, float i4, float cofa, float tau,
                                         float& gx, float& gy, float& gz, dd& e_kin, dd& e_trap, Comp& e_pair) {
-    const uint32_t b = i / N, p = i - b * N;
-    const uint32_t bp = b == 0 ? M - 1 : b - 1, bn = b + 1 == M ? 0 : b + 1;
+    const uint32_t i = row * N + p, ip = i - N, in_ = i + N;
     const float x = sx[i], y = sy[i], z = sz[i];
-    const uint32_t ip = bp * N + p, in_ = bn * N + p;
     // links (b-1 -> b) and (b -> b+1): d/dr_b of |r_{b+1} - r_b|^2 i4 summed = 2 i4 (d_{b-1} - d_b)
     const float dpx = Img<kPbc>(__fsub_rn(x, sx[ip]), c.L, c.iL), dpy = Img<kPbc>(__fsub_rn(y, sy[ip]), c.L, c.iL),
                 dpz = Img<kPbc>(__fsub_rn(z, sz[ip]), c.L, c.iL);
@@ -907,9 +910,9 @@ __device__ __forceinline__ void HmcBead(const ChainDev& c, const float* __restri
         e_trap = AddSq(AddSq(AddSq(e_trap, x), y), z);
     }
     if (c.has_pair) {
-        const float* rx = sx + b * N;
-        const float* ry = sy + b * N;
-        const float* rz = sz + b * N;
+        const float* rx = sx + row * N;
+        const float* ry = sy + row * N;
+        const float* rz = sz + row * N;
         float fx = 0.f, fy = 0.f, fz = 0.f;
         const float r2lo = c.r2_min, r2hi = c.r2_max;
 #pragma unroll 4
@@ -933,25 +936,51 @@ __device__ __forceinline__ void HmcBead(const ChainDev& c, const float* __restri
     }
 }
 
+struct HmcShared {
+    dd red[4][kHmcThreads / 32];
+    dd part[4];   // this block's energy sums, read by the whole cluster
+    int accept;
+};
+
+/// Halo rows 0 and nb + 1 from the neighbouring blocks' last and first own rows (the ring wraps).
+__device__ __forceinline__ void HmcHalos(cooperative_groups::cluster_group& cl, float* planes, uint32_t N, uint32_t nb, uint32_t RW) {
+    const uint32_t k = cl.num_blocks(), r = cl.block_rank();
+    const float* left = cl.map_shared_rank(planes, (r + k - 1) % k);
+    const float* right = cl.map_shared_rank(planes, (r + 1) % k);
+    for (uint32_t i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+        const uint32_t d = i / N, p = i - d * N;
+        planes[d * RW + p] = left[d * RW + nb * N + p];
+        planes[d * RW + (nb + 1) * N + p] = right[d * RW + N + p];
+    }
+}
+
 template <bool kPbc>
-__device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c, uint32_t ci, float* sx, float* sy, float* sz,
-                         dd (*s_red)[kHmcThreads / 32], int* s_accept) {
-    const uint32_t N = c.n_part, M = c.n_bead, n_pad = c.n_pad, E = N * M;
+__device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c, uint32_t ci, float* planes, HmcShared& sh) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const uint32_t k = cl.num_blocks(), r = cl.block_rank();
+    const uint32_t N = c.n_part, M = c.n_bead, n_pad = c.n_pad;
+    const uint32_t nb = M / k, b_lo = r * nb, E = nb * N, RW = (nb + 2) * N;
+    float* sx = planes;
+    float* sy = planes + RW;
+    float* sz = planes + 2 * RW;
+    float* px = planes + 3 * RW;
+    float* py = px + E;
+    float* pz = py + E;
     const uint32_t t = threadIdx.x, T = blockDim.x;
     float4* pos = a.pos + c.pos_off;
-    float4* mom = h.mom + c.pos_off;
     const float i4 = c.i4lt_level[0], cofa = c.trap_cofa, tau = c.tau, eps = c.hmc_eps;
     const double i4d = 1. / (4. * (double)c.lambda * (double)c.tau), taud = (double)c.tau;
     uint64_t att = h.att[ci], acc = 0;
     for (uint32_t it = 0; it < h.n_attempts; ++it, ++att) {
         const MoveStream st{c.seed, c.chain_id, c.hmc_move, att};
-        // path into the planes; momenta from the stream
+        // own slices from the committed path (this block wrote them last); momenta from the stream
         for (uint32_t i = t; i < E; i += T) {
-            const uint32_t b = i / N, p = i - b * N;
-            const float4 r = pos[(size_t)b * n_pad + p];
-            sx[i] = r.x;
-            sy[i] = r.y;
-            sz[i] = r.z;
+            const uint32_t lb = i / N, p = i - lb * N, b = b_lo + lb;
+            const float4 rv = pos[(size_t)b * n_pad + p];
+            sx[i + N] = rv.x;
+            sy[i + N] = rv.y;
+            sz[i + N] = rv.z;
             float z3[3];
             const uint32_t j0 = (p * M + b) * 3u;
             for (uint32_t d = 0; d < 3; ++d) {
@@ -962,82 +991,97 @@ __device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c
                 else BoxMullerF(w.v[2], w.v[3], z0, z1);
                 z3[d] = (j & 1u) ? z1 : z0;
             }
-            mom[(size_t)b * n_pad + p] = make_float4(z3[0], z3[1], z3[2], 0.f);
+            px[i] = z3[0];
+            py[i] = z3[1];
+            pz[i] = z3[2];
         }
-        __syncthreads();
+        cl.sync();
+        HmcHalos(cl, planes, N, nb, RW);
+        cl.sync();
         double h_start = 0., h_end = 0.;
         const uint32_t n_steps = c.hmc_steps;
         for (uint32_t s = 0; s <= n_steps; ++s) {
             // gradient at the current R; energy at the start (s = 0) and the end (s = n_steps)
             const bool with_energy = s == 0 || s == n_steps;
-            const float f = (s == 0 || s == n_steps) ? 0.5f * eps : eps;
-            dd ek = DD(0.f), et = DD(0.f), ep = DD(0.f), em = DD(0.f);
+            const float f = with_energy ? 0.5f * eps : eps;
+            dd ek = DD(0.f), et = DD(0.f), em = DD(0.f);
             Comp cp{0.f, 0.f};
             for (uint32_t i = t; i < E; i += T) {
+                const uint32_t lb = i / N, p = i - lb * N;
                 float gx, gy, gz;
-                if (with_energy) HmcBead<kPbc, true>(c, sx, sy, sz, N, M, i, i4, cofa, tau, gx, gy, gz, ek, et, cp);
-                else HmcBead<kPbc, false>(c, sx, sy, sz, N, M, i, i4, cofa, tau, gx, gy, gz, ek, et, cp);
-                const uint32_t b = i / N, p = i - b * N;
-                float4 m4 = mom[(size_t)b * n_pad + p];
-                if (s == 0) em = AddSq(AddSq(AddSq(em, m4.x), m4.y), m4.z);  // |P|^2 before the first kick
-                m4.x = __fmaf_rn(-f, gx, m4.x);
-                m4.y = __fmaf_rn(-f, gy, m4.y);
-                m4.z = __fmaf_rn(-f, gz, m4.z);
-                if (s == n_steps) em = AddSq(AddSq(AddSq(em, m4.x), m4.y), m4.z);  // |P|^2 after the last kick
-                mom[(size_t)b * n_pad + p] = m4;
+                if (with_energy) HmcBead<kPbc, true>(c, sx, sy, sz, N, lb + 1, p, i4, cofa, tau, gx, gy, gz, ek, et, cp);
+                else HmcBead<kPbc, false>(c, sx, sy, sz, N, lb + 1, p, i4, cofa, tau, gx, gy, gz, ek, et, cp);
+                float mx = px[i], my = py[i], mz = pz[i];
+                if (s == 0) em = AddSq(AddSq(AddSq(em, mx), my), mz);  // |P|^2 before the first kick
+                mx = __fmaf_rn(-f, gx, mx);
+                my = __fmaf_rn(-f, gy, my);
+                mz = __fmaf_rn(-f, gz, mz);
+                if (s == n_steps) em = AddSq(AddSq(AddSq(em, mx), my), mz);  // |P|^2 after the last kick
+                px[i] = mx;
+                py[i] = my;
+                pz[i] = mz;
             }
             if (with_energy) {
-                ep = CompDD(cp);
-                dd v[4] = {ek, et, ep, em};
-                BlockSum4DD(v, s_red);
-                const double hv = i4d * ToDouble(v[0]) + (c.has_trap ? (double)cofa * ToDouble(v[1]) : 0.) +
-                                  0.5 * taud * ToDouble(v[2]) + 0.5 * ToDouble(v[3]);
-                if (s == 0) h_start = hv;
-                else h_end = hv;
+                dd v[4] = {ek, et, CompDD(cp), em};
+                BlockSum4DD(v, sh.red);
+                if (t == 0)
+                    for (int q = 0; q < 4; ++q) sh.part[q] = v[q];
+                cl.sync();
+                if (t == 0) {
+                    dd tot[4] = {DD(0.f), DD(0.f), DD(0.f), DD(0.f)};
+                    for (uint32_t rr = 0; rr < k; ++rr) {  // block order: the same sum in every block
+                        const dd* pr = cl.map_shared_rank(sh.part, rr);
+                        for (int q = 0; q < 4; ++q) tot[q] = Add(tot[q], pr[q]);
+                    }
+                    const double hv = i4d * ToDouble(tot[0]) + (c.has_trap ? (double)cofa * ToDouble(tot[1]) : 0.) +
+                                      0.5 * taud * ToDouble(tot[2]) + 0.5 * ToDouble(tot[3]);
+                    if (s == 0) h_start = hv;
+                    else h_end = hv;
+                }
             }
             __syncthreads();  // every gradient read of R is done
             if (s == n_steps) break;
             for (uint32_t i = t; i < E; i += T) {  // drift
-                const uint32_t b = i / N, p = i - b * N;
-                const float4 m4 = mom[(size_t)b * n_pad + p];
-                sx[i] = __fmaf_rn(eps, m4.x, sx[i]);
-                sy[i] = __fmaf_rn(eps, m4.y, sy[i]);
-                sz[i] = __fmaf_rn(eps, m4.z, sz[i]);
+                sx[i + N] = __fmaf_rn(eps, px[i], sx[i + N]);
+                sy[i + N] = __fmaf_rn(eps, py[i], sy[i + N]);
+                sz[i + N] = __fmaf_rn(eps, pz[i], sz[i + N]);
             }
-            __syncthreads();
+            cl.sync();  // every block drifted its slices
+            HmcHalos(cl, planes, N, nb, RW);
+            cl.sync();  // every block read its halos before the next drift
         }
         if (t == 0) {
             const double log_accept = -(h_end - h_start);
             const double logu = (double)LogF(U24(st.Block(0).v[0]));
-            *s_accept = (isfinite(log_accept) && !(log_accept < logu)) ? 1 : 0;
+            sh.accept = (isfinite(log_accept) && !(log_accept < logu)) ? 1 : 0;
         }
         __syncthreads();
-        if (*s_accept) {
+        if (sh.accept) {
             for (uint32_t i = t; i < E; i += T) {
-                const uint32_t b = i / N, p = i - b * N;
-                pos[(size_t)b * n_pad + p] = make_float4(sx[i], sy[i], sz[i], 0.f);
+                const uint32_t lb = i / N, p = i - lb * N;
+                pos[(size_t)(b_lo + lb) * n_pad + p] = make_float4(sx[i + N], sy[i + N], sz[i + N], 0.f);
             }
             ++acc;
         }
-        __syncthreads();
+        cl.sync();  // no block reads its part of a later attempt's sums before every block used these
     }
-    if (t == 0) {
+    if (t == 0 && r == 0) {
         h.att[ci] = att;
         h.acc[ci] += acc;
     }
 }
 
-__global__ void __launch_bounds__(kHmcThreads) BatchHmcKernel(BatchArgs a, HmcArgs h) {
-    const uint32_t ci = a.order[blockIdx.x];
+__global__ void __launch_bounds__(kHmcThreads, 2) BatchHmcKernel(BatchArgs a, HmcArgs h) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const uint32_t ci = a.order[blockIdx.x / cl.num_blocks()];
     const ChainDev& c = a.chains[ci];
-    if (c.hmc_eps == 0.f) return;  // the chain has no HMC move
-    __shared__ dd s_red[4][kHmcThreads / 32];
-    __shared__ int s_accept;
+    if (c.hmc_eps == 0.f) return;  // the chain has no HMC move (every block of its cluster returns)
+    __shared__ HmcShared sh;
     extern __shared__ float4 hmc_stage[];
-    float* sx = reinterpret_cast<float*>(hmc_stage);
-    const uint32_t E = c.n_part * c.n_bead;
-    if (c.pbc) HmcChain<true>(a, h, c, ci, sx, sx + E, sx + 2 * E, s_red, &s_accept);
-    else HmcChain<false>(a, h, c, ci, sx, sx + E, sx + 2 * E, s_red, &s_accept);
+    float* planes = reinterpret_cast<float*>(hmc_stage);
+    if (c.pbc) HmcChain<true>(a, h, c, ci, planes, sh);
+    else HmcChain<false>(a, h, c, ci, planes, sh);
 }
 
 /// Host layout (every chain's [n_part][n_bead][3] doubles, concatenated) to the device float4
@@ -1218,7 +1262,6 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
             c.hmc_steps = s.hmc_steps;
             c.hmc_move = s.hmc_move;
             bead_moves_per_hmc += (uint64_t)s.n_part * s.n_bead;
-            hmc_smem = std::max(hmc_smem, (size_t)12 * s.n_part * s.n_bead);
         }
         bead_moves_per_sweep += c.attempts_per_sweep * (B - 1);
         path_off_.push_back(path_doubles);
@@ -1246,13 +1289,24 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
         cudaFuncAttributes fh{};
         CudaCheck(cudaDeviceGetAttribute(&optin_h, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "device attribute");
         CudaCheck(cudaFuncGetAttributes(&fh, BatchHmcKernel), "kernel attributes");
-        if (hmc_smem + fh.sharedSizeBytes > (size_t)optin_h)
-            throw PimcError(kErrUnsupported, "a batched HMC chain's path (12 n_part n_bead bytes) exceeds the shared memory of one block");
-        CudaCheck(cudaFuncSetAttribute(BatchHmcKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hmc_smem), "smem attribute");
-        mom_.reset(new DeviceBuffer(off * sizeof(float4)));
+        hmc_smem_cap = (size_t)optin_h > fh.sharedSizeBytes ? (size_t)optin_h - fh.sharedSizeBytes : 0;
+        size_t need = 0;
+        for (uint32_t k = 1; k <= 8; k *= 2)
+            if (HmcSmem(k) && HmcSmem(k) <= hmc_smem_cap) need = std::max(need, HmcSmem(k));
+        if (!need)
+            throw PimcError(kErrUnsupported, "a batched HMC chain's path (24 n_part (n_bead / k + 1) bytes per block of a cluster of k <= 8) "
+                                             "exceeds the shared memory of one block");
+        CudaCheck(cudaFuncSetAttribute(BatchHmcKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need), "smem attribute");
+        // Default split: the fewest blocks per chain that still give every SM a few blocks.
+        hmc_cluster = 0;
+        for (uint32_t k = 1; k <= 8; k *= 2)
+            if (HmcClusterFits(k)) {
+                hmc_cluster = k;
+                if ((uint64_t)n_chains * k >= 4ull * (uint64_t)n_sm) break;
+            }
+        if (!hmc_cluster) throw PimcError(kErrUnsupported, "no thread-block cluster of 1-8 blocks fits the batched HMC launch");
         hmc_att_.reset(new DeviceBuffer(n_chains * sizeof(uint64_t)));
         hmc_acc_.reset(new DeviceBuffer(n_chains * sizeof(uint64_t)));
-        CudaCheck(cudaMemset(mom_->ptr, 0, off * sizeof(float4)), "memset");
         CudaCheck(cudaMemset(hmc_att_->ptr, 0, n_chains * sizeof(uint64_t)), "memset");
         CudaCheck(cudaMemset(hmc_acc_->ptr, 0, n_chains * sizeof(uint64_t)), "memset");
     }
@@ -1427,14 +1481,67 @@ void ChainBatch::LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts) {
     ++kernel_launches;
 }
 
+size_t ChainBatch::HmcSmem(uint32_t k) const {
+    // per block: R planes with one halo row on each side, P planes for its own rows
+    size_t bytes = 0;
+    for (const auto& s : specs) {
+        if (!s.has_hmc) continue;
+        if (k == 0 || s.n_bead % k != 0) return 0;
+        const size_t nb = s.n_bead / k;
+        bytes = std::max(bytes, (size_t)12 * s.n_part * (2 * nb + 2));
+    }
+    return bytes;
+}
+
+bool ChainBatch::HmcClusterFits(uint32_t k) const {
+    const size_t smem = HmcSmem(k);
+    if (!smem || smem > hmc_smem_cap) return false;
+    cudaLaunchConfig_t cfg{};
+    cudaLaunchAttribute attr{};
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = k;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.gridDim = dim3(n_chains * k);
+    cfg.blockDim = dim3(kHmcThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, BatchHmcKernel, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return clusters > 0;
+}
+
+void ChainBatch::SetHmcCluster(uint32_t k) {
+    if (!bead_moves_per_hmc) throw PimcError(kErrState, "no chain of the batch has an HMC move");
+    if (k != 1 && k != 2 && k != 4 && k != 8) throw PimcError(kErrArg, "HMC cluster size must be 1, 2, 4 or 8");
+    if (!HmcClusterFits(k)) throw PimcError(kErrUnsupported, "this HMC cluster size does not divide every HMC chain's n_bead or does not fit");
+    if (k != hmc_cluster) ResetGraph();
+    hmc_cluster = k;
+}
+
 void ChainBatch::LaunchHmc(uint64_t n_attempts) {
     if (!bead_moves_per_hmc) throw PimcError(kErrState, "no chain of the batch has an HMC move");
     const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, series_cap);
+    cudaLaunchAttribute attr{};
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = hmc_cluster;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(n_chains * hmc_cluster);
+    cfg.blockDim = dim3(kHmcThreads);
+    cfg.dynamicSmemBytes = HmcSmem(hmc_cluster);
+    cfg.stream = stream;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
     for (uint64_t done = 0; done < n_attempts;) {
         const uint32_t k = (uint32_t)std::min<uint64_t>(n_attempts - done, 1u << 20);
-        const HmcArgs h{mom_->as<float4>(), hmc_att_->as<uint64_t>(), hmc_acc_->as<uint64_t>(), k};
-        BatchHmcKernel<<<n_chains, kHmcThreads, hmc_smem, stream>>>(a, h);
-        CudaCheck(cudaGetLastError(), "batch HMC launch");
+        const HmcArgs h{hmc_att_->as<uint64_t>(), hmc_acc_->as<uint64_t>(), k};
+        CudaCheck(cudaLaunchKernelEx(&cfg, BatchHmcKernel, a, h), "batch HMC launch");
         ++kernel_launches;
         done += k;
     }
@@ -1574,9 +1681,37 @@ double ChainBatch::Autotune(uint32_t trial_sweeps) {
             copy(*att_, att_save);
             copy(*acc_, acc_save);
         }
+    SetTiles(best_ipl, best_mw, best_wave);
+    if (bead_moves_per_hmc) {
+        // blocks per chain of the HMC launch: one attempt per trial, the state put back after each
+        DeviceBuffer hatt_save(hmc_att_->bytes), hacc_save(hmc_acc_->bytes);
+        copy(hatt_save, *hmc_att_);
+        copy(hacc_save, *hmc_acc_);
+        float best_h = 1e30f;
+        uint32_t best_k = hmc_cluster;
+        for (uint32_t k = 1; k <= 8; k *= 2) {
+            if (!HmcClusterFits(k)) continue;
+            SetHmcCluster(k);
+            LaunchHmc(1);  // warm-up of this shape
+            CudaCheck(cudaEventRecord(e0, stream), "event");
+            LaunchHmc(1);
+            CudaCheck(cudaEventRecord(e1, stream), "event");
+            CudaCheck(cudaEventSynchronize(e1), "event sync");
+            float ms = 0.f;
+            CudaCheck(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+            if (ms < best_h) {
+                best_h = ms;
+                best_k = k;
+            }
+            copy(*pos_, pos_save);
+            copy(*hmc_att_, hatt_save);
+            copy(*hmc_acc_, hacc_save);
+        }
+        SetHmcCluster(best_k);
+        CudaCheck(cudaStreamSynchronize(stream), "sync");
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    SetTiles(best_ipl, best_mw, best_wave);
     CudaCheck(cudaStreamSynchronize(stream), "sync");
     return best;
 }
@@ -1725,6 +1860,18 @@ int pimc_batch_hmc_counters(pimc_batch* h, uint64_t* attempts, uint64_t* accepts
 
 int pimc_batch_set_hmc_per_cycle(pimc_batch* h, uint64_t n) {
     return BatchGuard(h, [&](pimc::ChainBatch& b) { b.SetHmcPerCycle(n); });
+}
+
+int pimc_batch_set_hmc_cluster(pimc_batch* h, uint32_t k) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.SetHmcCluster(k); });
+}
+
+int pimc_batch_get_hmc_cluster(pimc_batch* h, uint32_t* k) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) {
+        if (!k) throw pimc::PimcError(pimc::kErrArg, "null output");
+        if (!b.bead_moves_per_hmc) throw pimc::PimcError(pimc::kErrState, "no chain of the batch has an HMC move");
+        *k = b.hmc_cluster;
+    });
 }
 
 int pimc_batch_set_tiles(pimc_batch* h, uint32_t items_per_lane, uint32_t max_warps, uint32_t wave) {

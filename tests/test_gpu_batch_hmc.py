@@ -6,7 +6,8 @@ action, Metropolis on dH). The batch computes it in FP32 with double-float energ
 restates it in FP64 with the same counter-based draws. The tests replay both: identical accept counts
 and positions within 1e-4 (FP32 positions, as the batched bisection tests), bisection sweeps
 interleaved, and the graph-replayed measurement cycle with HMC attempts equal to the same calls
-made one by one.
+made one by one. A chain runs on a cluster of k thread blocks split by slices; the trajectory is the
+same FP32 sequence for every k, so paths and accept counts are identical across k = 1, 2, 4, 8.
 """
 import numpy as np
 import pytest
@@ -34,9 +35,12 @@ def _batch(tmp_path, items):
     return b
 
 
-def test_batch_hmc_replays_oracle(tmp_path, gpu_lib, oracle_mod):
+@pytest.mark.parametrize("k", [1, 8])
+def test_batch_hmc_replays_oracle(tmp_path, gpu_lib, oracle_mod, k):
     items = _items(tmp_path)
     b = _batch(tmp_path, items)
+    b.hmc_cluster = k
+    assert b.hmc_cluster == k
     # smooth the N(0, 1) starting paths with bisection sweeps, then alternate HMC and bisection
     schedule = [("sweeps", 10), ("hmc", 6), ("bisect", 40), ("hmc", 6)]
     for kind, n in schedule:
@@ -88,6 +92,42 @@ def test_batch_hmc_cycle_graph_equals_calls(tmp_path, gpu_lib):
     assert np.array_equal(g.hmc_counters()[1], s.hmc_counters()[1])
     g.close()
     s.close()
+
+
+def test_batch_hmc_cluster_size_leaves_trajectory_unchanged(tmp_path, gpu_lib):
+    items = _items(tmp_path)
+    runs = []
+    for k in (1, 2, 4, 8):
+        b = _batch(tmp_path, items)
+        b.hmc_cluster = k
+        b.sweeps(5)
+        b.hmc_attempts(4)
+        b.attempts(20)
+        b.hmc_attempts(4)
+        runs.append(([b.get_path(c) for c in range(len(items))], b.hmc_counters()[1].copy()))
+        b.close()
+    for paths, acc in runs[1:]:
+        assert np.array_equal(acc, runs[0][1])
+        for c in range(len(items)):
+            assert np.array_equal(paths[c], runs[0][0][c]), c
+
+
+def test_batch_hmc_cluster_size_must_divide_n_bead(tmp_path, gpu_lib):
+    from simpimc_gb300 import PimcError
+    xml_a, pa = trapped_coulomb(tmp_path, n_part=6, n_bead=12, n_level=2, seed=1, hmc=(0.03, 4))
+    xml_b, pb = trapped_coulomb(tmp_path, n_part=5, n_bead=16, n_level=2, seed=2, hmc=(0.03, 4))
+    b = ChainBatch([xml_a, xml_b], base_dir=tmp_path)
+    b.set_path(0, pa)
+    b.set_path(1, pb)
+    for bad in (3, 16):
+        with pytest.raises(PimcError, match="1, 2, 4 or 8"):
+            b.hmc_cluster = bad
+    with pytest.raises(PimcError, match="divide"):
+        b.hmc_cluster = 8  # 12 slices do not split over 8 blocks
+    b.hmc_cluster = 4
+    b.hmc_attempts(3)
+    assert np.all(b.hmc_counters()[0] == 3)
+    b.close()
 
 
 def test_batch_hmc_needs_the_move(tmp_path, gpu_lib):
