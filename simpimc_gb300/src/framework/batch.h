@@ -37,7 +37,7 @@ namespace pimc {
 constexpr uint32_t kBatchMaxLevels = 5;        // segment of at most 32 beads
 constexpr uint32_t kBatchMaxWarps = 16;        // warps per chain (block size 512)
 constexpr uint32_t kBatchSeriesComponents = 4; // E, kinetic, trap, pair (each / M)
-constexpr uint32_t kMaxWave = 4;               // attempts of one chain in flight at once
+constexpr uint32_t kMaxWave = 8;               // attempts of one chain in flight at once
 
 /// Per-chain parameters read by the batched kernels.
 struct ChainDev {

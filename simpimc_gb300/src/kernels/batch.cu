@@ -167,8 +167,8 @@ struct PathView {
 
 /// Draws of one attempt (particle, first bead, normals, log-uniforms; philox.h stream layout) into
 /// shared buffers, by one warp; with `seg` also the moved particle's segment as it is now.
-__device__ __forceinline__ void DrawAttempt(const MoveStream& st, uint32_t lane, uint32_t N, uint32_t M, uint32_t B, uint32_t NL, uint32_t n_pad,
-                                            const float4* __restrict__ pos, float* z, float* logu, float4* seg, uint32_t* pb) {
+__device__ __forceinline__ uint2 DrawAttempt(const MoveStream& st, uint32_t lane, uint32_t N, uint32_t M, uint32_t B, uint32_t NL, uint32_t n_pad,
+                                             const float4* __restrict__ pos, float* z, float* logu, float4* seg, uint32_t* pb) {
     const Philox4 w0 = st.Block(0);
     const uint32_t p = UniformIndex(w0.v[0], N), b0 = UniformIndex(w0.v[1], M);
     if (seg) {
@@ -191,6 +191,7 @@ __device__ __forceinline__ void DrawAttempt(const MoveStream& st, uint32_t lane,
             logu[NL - 1 - li] = BisectLogU(st, B, li);
         }
     }
+    return make_uint2(p, b0);
 }
 
 /// Warp work of one attempt (bisect_class.h:39-124 above level 0): lane k enters with bead k of
@@ -510,21 +511,27 @@ __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_
 }
 
 // ---------------------------------------------------------------------------------------------
-// Several attempts of one chain at a time. Attempt j (later in the chain) does not see attempt i's
-// changes when they share nothing it reads: a different particle whose inner slices miss i's
-// inner slices (its pair terms read the others only there), or the same particle with its whole
-// segment clear of i's inner slices. A round takes the longest prefix of the next W drawn
-// attempts in which every attempt is clear of all earlier ones; they run concurrently, one per
-// sub-group of warps, and commit disjoint beads. The result is the sequential chain's.
+// Several attempts of one chain at a time. Two attempts commute when neither reads what the other
+// writes: different particles whose inner slices are disjoint (an attempt's pair terms read the
+// other particles only at its inner slices), or the same particle with each attempt's whole
+// segment clear of the other's inner slices. A scoreboard keeps the next kWindow drawn attempts;
+// each carries a mask of the attempts before it (up to kWindow - 1 back) that it does not commute
+// with. A round runs the first W attempts of the window, in attempt order, that commute with every
+// earlier attempt not yet run, one per sub-group of warps; they commit disjoint beads. Every
+// attempt therefore reads what it reads in the sequential chain, and the result is the sequential
+// chain's: the same accept decisions and the same path.
 
-constexpr uint32_t kRing = 2 * kMaxWave;  // ring of drawn attempts, slot = attempt mod kRing
+constexpr uint32_t kWindow = 16;          // attempts the scheduler considers per round
+constexpr uint32_t kRing = 2 * kWindow;   // drawn attempts, slot = attempt mod kRing
 static_assert((kRing & (kRing - 1)) == 0, "the drawn-attempt ring is indexed by a mask");
+static_assert(kMaxWave <= kWindow && kWindow <= 32, "a round's attempts come from the window; one lane per window entry");
 
 struct WaveShared {
     ChainDev c;
     float z[kRing][3 * (kMaxB - 1)];
     float logu[kRing][kBatchMaxLevels];
     uint32_t pb[kRing][2];
+    uint32_t dep[kRing];  // bit d: the attempt does not commute with the one d before it
     float2 on_[kMaxWave][3 * (kMaxB + 1)];
     Comp part[kMaxWave][kBatchMaxWarps];
     dd base0[kMaxWave];
@@ -536,18 +543,29 @@ __device__ __forceinline__ bool CircOverlap(uint32_t s1, uint32_t l1, uint32_t s
     return Wrap(s2 + M - s1, M) < l1 || Wrap(s1 + M - s2, M) < l2;
 }
 
-/// Does attempt j (later) read anything attempt i changes?
-__device__ __forceinline__ bool Conflicts(uint32_t pi, uint32_t bi, uint32_t pj, uint32_t bj, uint32_t B, uint32_t M) {
-    const uint32_t si = Wrap(bi + 1u, M);  // inner slices of i: [bi+1, bi+B-1]
-    if (pi == pj) return B + 1 > M || CircOverlap(si, B - 1, bj, B + 1, M);
-    return CircOverlap(si, B - 1, Wrap(bj + 1u, M), B - 1, M);
+/// Does either attempt read what the other writes? (Inner slices [b+1, b+B-1] are written; the
+/// segment [b, b+B] of the moved particle and the inner slices of every particle are read.)
+__device__ __forceinline__ bool Interact(uint32_t pi, uint32_t bi, uint32_t pj, uint32_t bj, uint32_t B, uint32_t M) {
+    const uint32_t si = Wrap(bi + 1u, M), sj = Wrap(bj + 1u, M);
+    if (pi == pj) return B + 1 > M || CircOverlap(si, B - 1, bj, B + 1, M) || CircOverlap(sj, B - 1, bi, B + 1, M);
+    return CircOverlap(si, B - 1, sj, B - 1, M);
 }
 
-/// Pairs (i, j), i < j < kMaxWave, in the order k = j (j - 1) / 2 + i; PairJ(k) = j. Pairs of a
-/// smaller j come first, so the lowest conflicting pair names the first attempt that conflicts.
-constexpr uint32_t kPairsMax = kMaxWave * (kMaxWave - 1) / 2;
-static_assert(kMaxWave == 4, "PairJ covers the pairs of a window of four");
-__device__ __forceinline__ uint32_t PairJ(uint32_t k) { return 1u + (k >= 1u ? 1u : 0u) + (k >= 3u ? 1u : 0u); }
+/// DrawAttempt for attempt y into ring slot `sl`, plus its scoreboard mask: lane d (1 <= d <
+/// kWindow) recomputes the particle and first bead of attempt y - d from its stream (block 0).
+__device__ __forceinline__ void DrawScored(WaveShared& sh, uint64_t y, uint32_t lane, uint32_t N, uint32_t M, uint32_t B, uint32_t NL,
+                                           uint32_t n_pad, const float4* __restrict__ pos) {
+    const ChainDev& c = sh.c;
+    const uint32_t sl = (uint32_t)y & (kRing - 1u);
+    const uint2 pb = DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, y}, lane, N, M, B, NL, n_pad, pos, sh.z[sl], sh.logu[sl], nullptr, sh.pb[sl]);
+    bool hit = false;
+    if (lane >= 1 && lane < kWindow && y >= lane) {
+        const Philox4 w = MoveStream{c.seed, c.chain_id, c.move, y - lane}.Block(0);
+        hit = Interact(UniformIndex(w.v[0], N), UniformIndex(w.v[1], M), pb.x, pb.y, B, M);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, hit);
+    if (lane == 0) sh.dep[sl] = m;
+}
 
 __device__ __forceinline__ void SubSync(uint32_t id, uint32_t n_warps) {
     if (n_warps == 1) __syncwarp();
@@ -558,7 +576,7 @@ template <bool kPbc, bool kStaged>
 __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchArgs a, uint32_t ci, uint64_t n_sweeps, uint64_t n_attempts) {
     const ChainDev& c = sh.c;
     const uint32_t W = c.n_wave, Gs = c.sub_warps, G = W * Gs;
-    constexpr uint32_t kMask = kRing - 1;  // 2W <= kRing: the window and the next one never share a slot
+    constexpr uint32_t kMask = kRing - 1;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     // Warp w belongs to sub-group w mod W: the leaders (warps 0..W-1), whose phases are the
     // serial part of a round, sit on different SM sub-partitions.
@@ -587,63 +605,54 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
         it_q[j] = i - it_k[j] * nm1;
     }
 
-    uint64_t A = a.attempts[ci];
-    const uint64_t end = A + (n_sweeps ? n_sweeps * c.attempts_per_sweep : n_attempts);
+    uint64_t H = a.attempts[ci];  // the first attempt not yet run
+    const uint64_t end = H + (n_sweeps ? n_sweeps * c.attempts_per_sweep : n_attempts);
+    uint32_t U = 0xffffffffu;     // bit i: attempt H + i not yet run
     if (threadIdx.x == 0) sh.accepts = 0;
-    // Prologue: the first 2W attempts' draws, attempt A + x by sub-group x mod W.
+    // Prologue: the first window's draws, attempt H + x by sub-group x mod W.
     if (ws == draw_warp)
-        for (uint64_t x = A + sg; x < end && x < A + 2 * W; x += W) {
-            const uint32_t sl = (uint32_t)x & kMask;
-            DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, x}, lane, N, M, B, NL, n_pad, pos, sh.z[sl], sh.logu[sl], nullptr, sh.pb[sl]);
-        }
+        for (uint64_t y = H + sg; y < end && y < H + kWindow; y += W) DrawScored(sh, y, lane, N, M, B, NL, n_pad, pos);
     SubSync(15, G);
 
-    while (A < end) {
-        // Attempt A + sg's beads, loaded before the round's prefix is known (the previous round's
-        // commits are visible after its closing barrier; unused if the prefix stops earlier).
-        const uint32_t a0 = (uint32_t)A & kMask;
-        const bool drawn = A + sg < end;
-        const uint32_t slot = (a0 + sg) & kMask;
-        const uint32_t p = drawn ? sh.pb[slot][0] : 0u, b0 = drawn ? sh.pb[slot][1] : 0u;
-        float3 pre[kItems];
-        if constexpr (!kStaged) {  // global beads: the first items' partners in flight during the leader
+    while (H < end) {
+        // The round's attempts: the first W of the window that commute with every earlier attempt
+        // not yet run (the same on every lane of every warp; attempt H always qualifies).
+        bool ok = false;
+        if (lane < kWindow && H + lane < end && ((U >> lane) & 1u)) {
+            const uint32_t dep = sh.dep[(uint32_t)(H + lane) & kMask];
+            ok = ((__brev(dep) >> (31u - lane)) & U) == 0u;  // bit lane - d <- bit d of dep
+        }
+        const unsigned elig = __ballot_sync(0xffffffffu, ok);
+        unsigned rest = elig, mine = 0u;
+        for (uint32_t k = 0; k < W && rest; ++k) {
+            if (k == sg) mine = rest & (0u - rest);
+            rest &= rest - 1u;
+        }
+        const unsigned sel = elig ^ rest;
+        const unsigned U_next = U & ~sel;
+        const uint32_t adv = (uint32_t)__ffs(U_next) - 1u;  // attempts at the head that are now run
+        if (mine) {
+            const uint32_t pos_in_window = (uint32_t)__ffs(mine) - 1u;
+            const uint64_t y = H + pos_in_window;
+            const uint32_t slot = (uint32_t)y & kMask;
+            const uint32_t p = sh.pb[slot][0], b0 = sh.pb[slot][1];
+            float3 pre[kItems];
+            if constexpr (!kStaged) {  // global beads: the first items' partners in flight during the leader
 #pragma unroll
-            for (uint32_t j = 0; j < kItems; ++j)
-                if (drawn && ts + j * Ts < n_items) pre[j] = path.Load(Wrap(b0 + 1u + it_k[j], M), it_q[j] + (it_q[j] >= p ? 1u : 0u));
-        }
-        float3 sv = make_float3(0.f, 0.f, 0.f), se = sv;
-        if (drawn && ws == 0) {
-            sv = path.Load(Wrap(b0 + (lane <= B ? lane : B), M), p);
-            se = path.Load(Wrap(b0 + B, M), p);
-        }
-        // The round's attempts: the longest conflict-free prefix of the next W (same on all lanes).
-        // Lane k tests pair k = j (j - 1) / 2 + i (i < j < W) and one ballot collects them.
-        const uint32_t left = end - A < (uint64_t)W ? (uint32_t)(end - A) : W;
-        uint32_t w = left;
-        if (left > 1) {
-            bool hit = false;
-            if (lane < kPairsMax) {
-                const uint32_t j = PairJ(lane), i = lane - j * (j - 1) / 2;
-                if (j < left) {
-                    const uint32_t* pi = sh.pb[(a0 + i) & kMask];
-                    const uint32_t* pj = sh.pb[(a0 + j) & kMask];
-                    hit = Conflicts(pi[0], pi[1], pj[0], pj[1], B, M);
-                }
+                for (uint32_t j = 0; j < kItems; ++j)
+                    if (ts + j * Ts < n_items) pre[j] = path.Load(Wrap(b0 + 1u + it_k[j], M), it_q[j] + (it_q[j] >= p ? 1u : 0u));
             }
-            const unsigned m = __ballot_sync(0xffffffffu, hit);
-            if (m) w = PairJ((uint32_t)__ffs(m) - 1u);  // the first later attempt that conflicts ends the prefix
-        }
-        if (sg < w) {
             float nx = 0.f, ny = 0.f, nz = 0.f;
-            if (ws == 0)
+            if (ws == 0) {
+                const float3 sv = path.Load(Wrap(b0 + (lane <= B ? lane : B), M), p);
+                const float3 se = path.Load(Wrap(b0 + B, M), p);
                 LeaderPhase<kPbc>(c, lane, NL, M, sv.x, sv.y, sv.z, se.x, se.y, se.z, sh.z[slot], sh.logu[slot], sh.on_[sg],
                                   &sh.base0[sg], &sh.upper_ok[sg], nx, ny, nz);
-            // The draw that completes the next window: attempt A + W + sg (its slot is not in use).
-            if (ws == draw_warp && A + W + sg < end) {
-                const uint64_t y = A + W + sg;
-                const uint32_t sl = (uint32_t)y & kMask;
+            }
+            // Draws that refill the window behind the head's advance (their slots are not in use).
+            if (ws == draw_warp) {
                 if (draw_warp == 0) __syncwarp();
-                DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, y}, lane, N, M, B, NL, n_pad, pos, sh.z[sl], sh.logu[sl], nullptr, sh.pb[sl]);
+                for (uint64_t yd = H + kWindow + sg; yd < H + kWindow + adv && yd < end; yd += W) DrawScored(sh, yd, lane, N, M, B, NL, n_pad, pos);
             }
             SubSync(1 + sg, Gs);
             const bool upper_ok = sh.upper_ok[sg] != 0;
@@ -657,9 +666,12 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
                 if (accepted && lane >= 1 && lane < B) path.Store(Wrap(b0 + lane, M), p, nx, ny, nz);
                 if (accepted && lane == 0) atomicAdd(&sh.accepts, 1u);
             }
+        } else if (ws == draw_warp) {
+            for (uint64_t yd = H + kWindow + sg; yd < H + kWindow + adv && yd < end; yd += W) DrawScored(sh, yd, lane, N, M, B, NL, n_pad, pos);
         }
         SubSync(15, G);
-        A += w;
+        U = adv ? (U_next >> adv) | (0xffffffffu << (32u - adv)) : U_next;
+        H += adv;
     }
     if constexpr (kStaged)  // every round ended with a block barrier: all commits are visible
         for (uint32_t i = threadIdx.x; i < N * M; i += G * 32u) {
@@ -667,7 +679,7 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
             pos[(size_t)b * n_pad + q] = make_float4(stage[i], stage[N * M + i], stage[2 * N * M + i], 0.f);
         }
     if (threadIdx.x == 0) {
-        a.attempts[ci] = A;
+        a.attempts[ci] = H;
         a.accepts[ci] += sh.accepts;
     }
 }
@@ -1355,7 +1367,7 @@ void ChainBatch::ResetGraph() {
 /// Blocks are ordered by descending work so the longest chains start first.
 void ChainBatch::SetTiles(uint32_t ipl, uint32_t mw, uint32_t wave) {
     if (ipl < 1 || mw < 1 || mw > kBatchMaxWarps || wave < 1 || wave > kMaxWave)
-        throw PimcError(kErrArg, "tile: items_per_lane >= 1, 1 <= max_warps <= 16, 1 <= wave <= 4");
+        throw PimcError(kErrArg, "tile: items_per_lane >= 1, 1 <= max_warps <= 16, 1 <= wave <= 8");
     items_per_lane = ipl;
     max_warps = mw;
     this->wave = wave;
@@ -1656,7 +1668,7 @@ double ChainBatch::Autotune(uint32_t trial_sweeps) {
     CudaCheck(cudaEventCreate(&e1), "event");
     const uint32_t ipls[] = {2, 4, 8};
     const uint32_t mws[] = {4, 8, 16};
-    const uint32_t waves[] = {1, 2, 4};
+    const uint32_t waves[] = {1, 2, 4, 8};
     double best = 1e300;
     uint32_t best_ipl = items_per_lane, best_mw = max_warps, best_wave = wave;
     for (uint32_t wv : waves)
