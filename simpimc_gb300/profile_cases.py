@@ -1,6 +1,7 @@
 """Small fixed workloads for profiler captures (one warm-up launch, then the launches to capture).
 
     python -m simpimc_gb300.profile_cases batch    # 256 uneven trapped-Coulomb chains: 1 + 1 sweep launches
+    python -m simpimc_gb300.profile_cases hmc      # the same chains with the HMC move: 1 + 1 HMC launches
     python -m simpimc_gb300.profile_cases egas     # 66-electron gas: 1 + 1 sweep launches (528 attempts each)
     python -m simpimc_gb300.profile_cases large32  # 1024-electron gas, FP32 mode: 1 + 1 launches of 64 attempts
     python -m simpimc_gb300.profile_cases bosons   # 32 trapped bosons: Bisect and PermBisectIterative, 1 + 1 sweeps
@@ -27,12 +28,28 @@ def batch_case(d):
     items = batched_trap_chains(d, n_chains=256, seed0=1000, n_level=3)
     b = ChainBatch([x for x, _ in items], base_dir=d)
     b.set_paths(np.concatenate([p.ravel() for _, p in items]))
-    b.set_tiles(4, 16, 4)
+    b.set_tiles(8, 16, 8)
     b.sweeps(1)
     b.sweeps(1)
     b.synchronize()
     att, acc = b.counters()
     print(f"batch ok: {int(att.sum())} attempts, acceptance {acc.sum() / att.sum():.4f}")
+
+
+def hmc_case(d):
+    """One HMC attempt per chain (leapfrog step 0.005, 10 steps) on clusters of 2 blocks per chain."""
+    from . import ChainBatch
+    from .configs import batched_trap_chains
+    items = batched_trap_chains(d, n_chains=256, seed0=1000, n_level=3, hmc=(0.005, 10))
+    b = ChainBatch([x for x, _ in items], base_dir=d)
+    b.set_paths(np.concatenate([p.ravel() for _, p in items]))
+    b.sweeps(2)
+    b.hmc_cluster = 2
+    b.hmc_attempts(1)
+    b.hmc_attempts(1)
+    b.synchronize()
+    att, acc = b.hmc_counters()
+    print(f"hmc ok: {int(att.sum())} attempts, acceptance {acc.sum() / att.sum():.4f}")
 
 
 def egas_case(d):
@@ -121,7 +138,7 @@ def egas_chains_case(d):
 def main(argv):
     case = argv[1] if len(argv) > 1 else "batch"
     with tempfile.TemporaryDirectory() as d:
-        {"batch": batch_case, "egas": egas_case, "large32": large32_case, "bosons": bosons_case, "chains": chains_case,
+        {"batch": batch_case, "hmc": hmc_case, "egas": egas_case, "large32": large32_case, "bosons": bosons_case, "chains": chains_case,
          "egas_chains": egas_chains_case}[case](d)
 
 

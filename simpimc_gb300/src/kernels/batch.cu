@@ -364,10 +364,24 @@ __device__ __forceinline__ Comp PairPhase(const ChainDev& c, uint32_t t, uint32_
         CompAdd(acc_u, __fsub_rn(rsqrtf(r2n), rsqrtf(r2o)));
     };
     if constexpr (kStaged) {  // beads in shared memory: no prefetch, loads batched by the unrolled loop
+        const uint32_t nk = n_items / nm1;  // inner slices
+        if ((nm1 + T - 1) / T * nk * 4u <= (n_items + T - 1) / T * 5u) {
+            // lane = partner particle, inner slices in a loop: no index division per item
+            for (uint32_t qi = t; qi < nm1; qi += T) {
+                const uint32_t q = qi + (qi >= p ? 1u : 0u);
+                uint32_t b = Wrap(b0 + 1u, M);
 #pragma unroll 4
-        for (uint32_t i = t; i < n_items; i += T) {
-            const uint32_t k = FastDivD(i, nm1, magic), qq = i - k * nm1;
-            item(k, path.Load(Wrap(b0 + 1u + k, M), qq + (qq >= p ? 1u : 0u)));
+                for (uint32_t k = 0; k < nk; ++k) {
+                    item(k, path.Load(b, q));
+                    b = b + 1u == M ? 0u : b + 1u;
+                }
+            }
+        } else {
+#pragma unroll 4
+            for (uint32_t i = t; i < n_items; i += T) {
+                const uint32_t k = FastDivD(i, nm1, magic), qq = i - k * nm1;
+                item(k, path.Load(Wrap(b0 + 1u + k, M), qq + (qq >= p ? 1u : 0u)));
+            }
         }
     } else {
 #pragma unroll
@@ -623,12 +637,9 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
             ok = ((__brev(dep) >> (31u - lane)) & U) == 0u;  // bit lane - d <- bit d of dep
         }
         const unsigned elig = __ballot_sync(0xffffffffu, ok);
-        unsigned rest = elig, mine = 0u;
-        for (uint32_t k = 0; k < W && rest; ++k) {
-            if (k == sg) mine = rest & (0u - rest);
-            rest &= rest - 1u;
-        }
-        const unsigned sel = elig ^ rest;
+        const uint32_t rank = __popc(elig & ((1u << lane) - 1u));  // eligible attempts before this lane's
+        const unsigned sel = __ballot_sync(0xffffffffu, ok && rank < W);
+        const unsigned mine = __ballot_sync(0xffffffffu, ok && rank == sg);
         const unsigned U_next = U & ~sel;
         const uint32_t adv = (uint32_t)__ffs(U_next) - 1u;  // attempts at the head that are now run
         if (mine) {
@@ -887,64 +898,108 @@ __device__ __forceinline__ void BlockSum4DD(dd v[4], dd (*s_red)[kHmcThreads / 3
     for (int q = 0; q < 4; ++q) v[q] = WarpSumDD(lane < nw ? s_red[q][lane] : DD(0.f));
 }
 
-/// Gradient dS/dr (FP32) of the bead in row `row` (1..nb), particle p, of the block's planes and,
-/// with kEnergy, its share of S: the link to the next slice, its trap term and half its pair sum
-/// (every pair is met twice). Rows row - 1 and row + 1 hold the neighbouring slices.
+/// Kinetic and trap gradient dS/dr (FP32) of bead `i` (row >= 1) of the block's rows and, with
+/// kEnergy, its share of S: the link to the next slice and its trap term. Rows i - N and i + N hold
+/// the neighbouring slices' beads.
 template <bool kPbc, bool kEnergy>
-__device__ __forceinline__ void HmcBead(const ChainDev& c, const float* __restrict__ sx, const float* __restrict__ sy,
-                                        const float* __restrict__ sz, uint32_t N, uint32_t row, uint32_t p, float i4, float cofa, float tau,
-                                        float& gx, float& gy, float& gz, dd& e_kin, dd& e_trap, Comp& e_pair) {
-    const uint32_t i = row * N + p, ip = i - N, in_ = i + N;
-    const float x = sx[i], y = sy[i], z = sz[i];
+__device__ __forceinline__ float3 HmcBeadTerms(const ChainDev& c, const float4* __restrict__ R, uint32_t N, uint32_t i, float i4, float cofa,
+                                               dd& e_kin, dd& e_trap) {
+    const float4 r = R[i], rp = R[i - N], rn = R[i + N];
     // links (b-1 -> b) and (b -> b+1): d/dr_b of |r_{b+1} - r_b|^2 i4 summed = 2 i4 (d_{b-1} - d_b)
-    const float dpx = Img<kPbc>(__fsub_rn(x, sx[ip]), c.L, c.iL), dpy = Img<kPbc>(__fsub_rn(y, sy[ip]), c.L, c.iL),
-                dpz = Img<kPbc>(__fsub_rn(z, sz[ip]), c.L, c.iL);
-    const float dnx = Img<kPbc>(__fsub_rn(sx[in_], x), c.L, c.iL), dny = Img<kPbc>(__fsub_rn(sy[in_], y), c.L, c.iL),
-                dnz = Img<kPbc>(__fsub_rn(sz[in_], z), c.L, c.iL);
+    const float dpx = Img<kPbc>(__fsub_rn(r.x, rp.x), c.L, c.iL), dpy = Img<kPbc>(__fsub_rn(r.y, rp.y), c.L, c.iL),
+                dpz = Img<kPbc>(__fsub_rn(r.z, rp.z), c.L, c.iL);
+    const float dnx = Img<kPbc>(__fsub_rn(rn.x, r.x), c.L, c.iL), dny = Img<kPbc>(__fsub_rn(rn.y, r.y), c.L, c.iL),
+                dnz = Img<kPbc>(__fsub_rn(rn.z, r.z), c.L, c.iL);
     const float k2 = 2.f * i4;
-    gx = __fmul_rn(k2, __fsub_rn(dpx, dnx));
-    gy = __fmul_rn(k2, __fsub_rn(dpy, dny));
-    gz = __fmul_rn(k2, __fsub_rn(dpz, dnz));
+    float3 g = make_float3(__fmul_rn(k2, __fsub_rn(dpx, dnx)), __fmul_rn(k2, __fsub_rn(dpy, dny)), __fmul_rn(k2, __fsub_rn(dpz, dnz)));
     if (c.has_trap) {
         const float t2 = 2.f * cofa;
-        gx = __fmaf_rn(t2, x, gx);
-        gy = __fmaf_rn(t2, y, gy);
-        gz = __fmaf_rn(t2, z, gz);
+        g.x = __fmaf_rn(t2, r.x, g.x);
+        g.y = __fmaf_rn(t2, r.y, g.y);
+        g.z = __fmaf_rn(t2, r.z, g.z);
     }
     if constexpr (kEnergy) {
-        dd ex = TwoSum(sx[in_], -x), ey = TwoSum(sy[in_], -y), ez = TwoSum(sz[in_], -z);
+        dd ex = TwoSum(rn.x, -r.x), ey = TwoSum(rn.y, -r.y), ez = TwoSum(rn.z, -r.z);
         if (kPbc) {
             ex = Sub(ex, DD(__fmul_rn(c.L, rintf(__fmul_rn(ex.hi, c.iL)))));
             ey = Sub(ey, DD(__fmul_rn(c.L, rintf(__fmul_rn(ey.hi, c.iL)))));
             ez = Sub(ez, DD(__fmul_rn(c.L, rintf(__fmul_rn(ez.hi, c.iL)))));
         }
         e_kin = Add(e_kin, Add(Add(Sqr(ex), Sqr(ey)), Sqr(ez)));
-        e_trap = AddSq(AddSq(AddSq(e_trap, x), y), z);
+        e_trap = AddSq(AddSq(AddSq(e_trap, r.x), r.y), r.z);
     }
-    if (c.has_pair) {
-        const float* rx = sx + row * N;
-        const float* ry = sy + row * N;
-        const float* rz = sz + row * N;
-        float fx = 0.f, fy = 0.f, fz = 0.f;
-        const float r2lo = c.r2_min, r2hi = c.r2_max;
+    return g;
+}
+
+/// Pair forces on two beads of one row at once (particles p0 and p1; f32x2 arithmetic, each half
+/// rounding as the scalar form does): sum over q of V'(r)/r (r_p - r_q) with V = 1/r clamped to the
+/// table's range, so V' = -1/r^2 inside it and 0 where clamped (q = p: r = 0 is below the range,
+/// whose lower end is positive). With kEnergy also the sum over q != p of V(r) for both beads. Without
+/// `two` the second half repeats p0 and only its forces are formed (and discarded).
+template <bool kPbc, bool kEnergy>
+__device__ __forceinline__ void HmcPairs2(const ChainDev& c, const float4* __restrict__ row, uint32_t N, uint32_t p0, uint32_t p1, bool two,
+                                          float2& fx, float2& fy, float2& fz, Comp& e_pair) {
+    if (!two) p1 = p0;
+    const float4 a0 = row[p0], a1 = row[p1];
+    const float2 X = make_float2(a0.x, a1.x), Y = make_float2(a0.y, a1.y), Z = make_float2(a0.z, a1.z);
+    const float r2lo = c.r2_min, r2hi = c.r2_max;
+    fx = fy = fz = make_float2(0.f, 0.f);
 #pragma unroll 4
-        for (uint32_t q = 0; q < N; ++q) {
-            // q = p contributes nothing (both of its terms are masked)
-            const float ux = Img<kPbc>(__fsub_rn(x, rx[q]), c.L, c.iL);
-            const float uy = Img<kPbc>(__fsub_rn(y, ry[q]), c.L, c.iL);
-            const float uz = Img<kPbc>(__fsub_rn(z, rz[q]), c.L, c.iL);
-            const float r2 = Sq3(ux, uy, uz);
-            const float inv = rsqrtf(fminf(fmaxf(r2, r2lo), r2hi));
-            if constexpr (kEnergy) CompAdd(e_pair, q == p ? 0.f : inv);
-            // tau V'(r) (r_p - r_q) / r with V' = -1/r^2 inside the table's range, 0 where clamped
-            const float f = (r2 >= r2lo && r2 <= r2hi && q != p) ? __fmul_rn(__fmul_rn(inv, inv), inv) : 0.f;
-            fx = __fmaf_rn(f, ux, fx);
-            fy = __fmaf_rn(f, uy, fy);
-            fz = __fmaf_rn(f, uz, fz);
+    for (uint32_t q = 0; q < N; ++q) {
+        const float4 b = row[q];
+        const float2 ux = Img2<kPbc>(Sub2(X, make_float2(b.x, b.x)), c.L, c.iL);
+        const float2 uy = Img2<kPbc>(Sub2(Y, make_float2(b.y, b.y)), c.L, c.iL);
+        const float2 uz = Img2<kPbc>(Sub2(Z, make_float2(b.z, b.z)), c.L, c.iL);
+        const float2 r2 = Sq3x2(ux, uy, uz);
+        const float c0 = fminf(fmaxf(r2.x, r2lo), r2hi), c1 = fminf(fmaxf(r2.y, r2lo), r2hi);
+        const float2 inv = make_float2(rsqrtf(c0), rsqrtf(c1));
+        if constexpr (kEnergy) {
+            CompAdd(e_pair, q == p0 ? 0.f : inv.x);
+            CompAdd(e_pair, (q == p1 || !two) ? 0.f : inv.y);
         }
-        gx = __fmaf_rn(-tau, fx, gx);
-        gy = __fmaf_rn(-tau, fy, gy);
-        gz = __fmaf_rn(-tau, fz, gz);
+        float2 f = Mul2(Mul2(inv, inv), inv);
+        f.x = c0 == r2.x ? f.x : 0.f;
+        f.y = c1 == r2.y ? f.y : 0.f;
+        fx = Fma2(f, ux, fx);
+        fy = Fma2(f, uy, fy);
+        fz = Fma2(f, uz, fz);
+    }
+}
+
+/// One kick P -= f dS/dR for the block's beads, task = (row, particles h and h + hN); with kEnergy
+/// also the block's shares of S and |P|^2 (before the kick when `p2_before`, after it when
+/// `p2_after`).
+template <bool kPbc, bool kEnergy>
+__device__ __forceinline__ void HmcKick(const ChainDev& c, const float4* __restrict__ R, float* px, float* py, float* pz, uint32_t N, uint32_t hN,
+                                        uint32_t n_tasks, float f, bool p2_before, bool p2_after, dd& ek, dd& et, Comp& cp, dd& em) {
+    const float i4 = c.i4lt_level[0], cofa = c.trap_cofa, tau = c.tau;
+    for (uint32_t task = threadIdx.x; task < n_tasks; task += blockDim.x) {
+        const uint32_t lb = task / hN, p0 = task - lb * hN, p1 = p0 + hN;
+        const bool two = p1 < N;
+        const uint32_t rowi = (lb + 1) * N;
+        float2 fx = make_float2(0.f, 0.f), fy = fx, fz = fx;
+        if (c.has_pair) HmcPairs2<kPbc, kEnergy>(c, R + rowi, N, p0, p1, two, fx, fy, fz, cp);
+#pragma unroll
+        for (uint32_t u = 0; u < 2; ++u) {
+            if (u == 1 && !two) break;
+            const uint32_t pp = u ? p1 : p0;
+            float3 g = HmcBeadTerms<kPbc, kEnergy>(c, R, N, rowi + pp, i4, cofa, ek, et);
+            if (c.has_pair) {
+                g.x = __fmaf_rn(-tau, u ? fx.y : fx.x, g.x);
+                g.y = __fmaf_rn(-tau, u ? fy.y : fy.x, g.y);
+                g.z = __fmaf_rn(-tau, u ? fz.y : fz.x, g.z);
+            }
+            const uint32_t i = lb * N + pp;
+            float mx = px[i], my = py[i], mz = pz[i];
+            if (kEnergy && p2_before) em = AddSq(AddSq(AddSq(em, mx), my), mz);  // |P|^2 before the first kick
+            mx = __fmaf_rn(-f, g.x, mx);
+            my = __fmaf_rn(-f, g.y, my);
+            mz = __fmaf_rn(-f, g.z, mz);
+            if (kEnergy && p2_after) em = AddSq(AddSq(AddSq(em, mx), my), mz);  // |P|^2 after the last kick
+            px[i] = mx;
+            py[i] = my;
+            pz[i] = mz;
+        }
     }
 }
 
@@ -955,33 +1010,30 @@ struct HmcShared {
 };
 
 /// Halo rows 0 and nb + 1 from the neighbouring blocks' last and first own rows (the ring wraps).
-__device__ __forceinline__ void HmcHalos(cooperative_groups::cluster_group& cl, float* planes, uint32_t N, uint32_t nb, uint32_t RW) {
+__device__ __forceinline__ void HmcHalos(cooperative_groups::cluster_group& cl, float4* R, uint32_t N, uint32_t nb) {
     const uint32_t k = cl.num_blocks(), r = cl.block_rank();
-    const float* left = cl.map_shared_rank(planes, (r + k - 1) % k);
-    const float* right = cl.map_shared_rank(planes, (r + 1) % k);
-    for (uint32_t i = threadIdx.x; i < 3 * N; i += blockDim.x) {
-        const uint32_t d = i / N, p = i - d * N;
-        planes[d * RW + p] = left[d * RW + nb * N + p];
-        planes[d * RW + (nb + 1) * N + p] = right[d * RW + N + p];
+    const float4* left = cl.map_shared_rank(R, (r + k - 1) % k);
+    const float4* right = cl.map_shared_rank(R, (r + 1) % k);
+    for (uint32_t p = threadIdx.x; p < N; p += blockDim.x) {
+        R[p] = left[nb * N + p];
+        R[(nb + 1) * N + p] = right[N + p];
     }
 }
 
 template <bool kPbc>
-__device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c, uint32_t ci, float* planes, HmcShared& sh) {
+__device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c, uint32_t ci, float4* R, HmcShared& sh) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
     const uint32_t k = cl.num_blocks(), r = cl.block_rank();
     const uint32_t N = c.n_part, M = c.n_bead, n_pad = c.n_pad;
-    const uint32_t nb = M / k, b_lo = r * nb, E = nb * N, RW = (nb + 2) * N;
-    float* sx = planes;
-    float* sy = planes + RW;
-    float* sz = planes + 2 * RW;
-    float* px = planes + 3 * RW;
+    const uint32_t nb = M / k, b_lo = r * nb, E = nb * N;
+    const uint32_t hN = (N + 1) / 2, n_tasks = nb * hN;  // task: (row, particles h and h + hN)
+    float* px = reinterpret_cast<float*>(R + (nb + 2) * N);
     float* py = px + E;
     float* pz = py + E;
     const uint32_t t = threadIdx.x, T = blockDim.x;
     float4* pos = a.pos + c.pos_off;
-    const float i4 = c.i4lt_level[0], cofa = c.trap_cofa, tau = c.tau, eps = c.hmc_eps;
+    const float cofa = c.trap_cofa, eps = c.hmc_eps;
     const double i4d = 1. / (4. * (double)c.lambda * (double)c.tau), taud = (double)c.tau;
     uint64_t att = h.att[ci], acc = 0;
     for (uint32_t it = 0; it < h.n_attempts; ++it, ++att) {
@@ -989,10 +1041,7 @@ __device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c
         // own slices from the committed path (this block wrote them last); momenta from the stream
         for (uint32_t i = t; i < E; i += T) {
             const uint32_t lb = i / N, p = i - lb * N, b = b_lo + lb;
-            const float4 rv = pos[(size_t)b * n_pad + p];
-            sx[i + N] = rv.x;
-            sy[i + N] = rv.y;
-            sz[i + N] = rv.z;
+            R[N + i] = pos[(size_t)b * n_pad + p];
             float z3[3];
             const uint32_t j0 = (p * M + b) * 3u;
             for (uint32_t d = 0; d < 3; ++d) {
@@ -1008,7 +1057,7 @@ __device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c
             pz[i] = z3[2];
         }
         cl.sync();
-        HmcHalos(cl, planes, N, nb, RW);
+        HmcHalos(cl, R, N, nb);
         cl.sync();
         double h_start = 0., h_end = 0.;
         const uint32_t n_steps = c.hmc_steps;
@@ -1018,21 +1067,8 @@ __device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c
             const float f = with_energy ? 0.5f * eps : eps;
             dd ek = DD(0.f), et = DD(0.f), em = DD(0.f);
             Comp cp{0.f, 0.f};
-            for (uint32_t i = t; i < E; i += T) {
-                const uint32_t lb = i / N, p = i - lb * N;
-                float gx, gy, gz;
-                if (with_energy) HmcBead<kPbc, true>(c, sx, sy, sz, N, lb + 1, p, i4, cofa, tau, gx, gy, gz, ek, et, cp);
-                else HmcBead<kPbc, false>(c, sx, sy, sz, N, lb + 1, p, i4, cofa, tau, gx, gy, gz, ek, et, cp);
-                float mx = px[i], my = py[i], mz = pz[i];
-                if (s == 0) em = AddSq(AddSq(AddSq(em, mx), my), mz);  // |P|^2 before the first kick
-                mx = __fmaf_rn(-f, gx, mx);
-                my = __fmaf_rn(-f, gy, my);
-                mz = __fmaf_rn(-f, gz, mz);
-                if (s == n_steps) em = AddSq(AddSq(AddSq(em, mx), my), mz);  // |P|^2 after the last kick
-                px[i] = mx;
-                py[i] = my;
-                pz[i] = mz;
-            }
+            if (with_energy) HmcKick<kPbc, true>(c, R, px, py, pz, N, hN, n_tasks, f, s == 0, s == n_steps, ek, et, cp, em);
+            else HmcKick<kPbc, false>(c, R, px, py, pz, N, hN, n_tasks, f, false, false, ek, et, cp, em);
             if (with_energy) {
                 dd v[4] = {ek, et, CompDD(cp), em};
                 BlockSum4DD(v, sh.red);
@@ -1054,12 +1090,14 @@ __device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c
             __syncthreads();  // every gradient read of R is done
             if (s == n_steps) break;
             for (uint32_t i = t; i < E; i += T) {  // drift
-                sx[i + N] = __fmaf_rn(eps, px[i], sx[i + N]);
-                sy[i + N] = __fmaf_rn(eps, py[i], sy[i + N]);
-                sz[i + N] = __fmaf_rn(eps, pz[i], sz[i + N]);
+                float4 v = R[N + i];
+                v.x = __fmaf_rn(eps, px[i], v.x);
+                v.y = __fmaf_rn(eps, py[i], v.y);
+                v.z = __fmaf_rn(eps, pz[i], v.z);
+                R[N + i] = v;
             }
             cl.sync();  // every block drifted its slices
-            HmcHalos(cl, planes, N, nb, RW);
+            HmcHalos(cl, R, N, nb);
             cl.sync();  // every block read its halos before the next drift
         }
         if (t == 0) {
@@ -1071,7 +1109,7 @@ __device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c
         if (sh.accept) {
             for (uint32_t i = t; i < E; i += T) {
                 const uint32_t lb = i / N, p = i - lb * N;
-                pos[(size_t)(b_lo + lb) * n_pad + p] = make_float4(sx[i + N], sy[i + N], sz[i + N], 0.f);
+                pos[(size_t)(b_lo + lb) * n_pad + p] = R[N + i];
             }
             ++acc;
         }
@@ -1091,9 +1129,8 @@ __global__ void __launch_bounds__(kHmcThreads, 2) BatchHmcKernel(BatchArgs a, Hm
     if (c.hmc_eps == 0.f) return;  // the chain has no HMC move (every block of its cluster returns)
     __shared__ HmcShared sh;
     extern __shared__ float4 hmc_stage[];
-    float* planes = reinterpret_cast<float*>(hmc_stage);
-    if (c.pbc) HmcChain<true>(a, h, c, ci, planes, sh);
-    else HmcChain<false>(a, h, c, ci, planes, sh);
+    if (c.pbc) HmcChain<true>(a, h, c, ci, hmc_stage, sh);
+    else HmcChain<false>(a, h, c, ci, hmc_stage, sh);
 }
 
 /// Host layout (every chain's [n_part][n_bead][3] doubles, concatenated) to the device float4
@@ -1214,6 +1251,8 @@ ChainSpec ParseChain(const std::string& xml, const std::string& base_dir) {
     if (s.n_level < 1 || s.n_level > kBatchMaxLevels) throw PimcError(kErrUnsupported, "batched Bisect needs 1 <= n_level <= 5");
     if ((1u << s.n_level) > s.n_bead) throw PimcError(kErrInput, "bisection segment longer than the path");
     s.move = (uint32_t)bisect;
+    // the HMC force leaves a particle's own term (r = 0) out by the clamp at the table's first point
+    if (s.has_hmc && s.has_pair && !(s.r_min > 0.)) throw PimcError(kErrUnsupported, "batched HMC needs a pair table starting at r > 0");
     return s;
 }
 
@@ -1494,13 +1533,13 @@ void ChainBatch::LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts) {
 }
 
 size_t ChainBatch::HmcSmem(uint32_t k) const {
-    // per block: R planes with one halo row on each side, P planes for its own rows
+    // per block: R rows (float4) with one halo row on each side, three P planes for its own rows
     size_t bytes = 0;
     for (const auto& s : specs) {
         if (!s.has_hmc) continue;
         if (k == 0 || s.n_bead % k != 0) return 0;
         const size_t nb = s.n_bead / k;
-        bytes = std::max(bytes, (size_t)12 * s.n_part * (2 * nb + 2));
+        bytes = std::max(bytes, (size_t)16 * s.n_part * (nb + 2) + (size_t)12 * s.n_part * nb);
     }
     return bytes;
 }
