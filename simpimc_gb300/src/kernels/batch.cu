@@ -535,15 +535,25 @@ __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_
 // attempt therefore reads what it reads in the sequential chain, and the result is the sequential
 // chain's: the same accept decisions and the same path.
 
-constexpr uint32_t kWindow = 16;          // attempts the scheduler considers per round
+constexpr uint32_t kWindow = 32;          // attempts the scheduler considers per round (one lane each)
 constexpr uint32_t kRing = 2 * kWindow;   // drawn attempts, slot = attempt mod kRing
 static_assert((kRing & (kRing - 1)) == 0, "the drawn-attempt ring is indexed by a mask");
 static_assert(kMaxWave <= kWindow && kWindow <= 32, "a round's attempts come from the window; one lane per window entry");
 
+/// A ring slot's normals (3 (B - 1) floats) and log-uniforms (n_level floats) live in dynamic
+/// shared memory after the staged path.
+__host__ __device__ constexpr size_t RingBytes(uint32_t B, uint32_t n_level) { return (size_t)kRing * (3 * (B - 1) + n_level) * sizeof(float); }
+
+struct WaveRing {
+    float* z;   // [kRing][3 (B - 1)]
+    float* lu;  // [kRing][n_level]
+    uint32_t zs, ls;
+    __device__ __forceinline__ float* Z(uint32_t slot) const { return z + slot * zs; }
+    __device__ __forceinline__ float* LU(uint32_t slot) const { return lu + slot * ls; }
+};
+
 struct WaveShared {
     ChainDev c;
-    float z[kRing][3 * (kMaxB - 1)];
-    float logu[kRing][kBatchMaxLevels];
     uint32_t pb[kRing][2];
     uint32_t dep[kRing];  // bit d: the attempt does not commute with the one d before it
     float2 on_[kMaxWave][3 * (kMaxB + 1)];
@@ -567,11 +577,11 @@ __device__ __forceinline__ bool Interact(uint32_t pi, uint32_t bi, uint32_t pj, 
 
 /// DrawAttempt for attempt y into ring slot `sl`, plus its scoreboard mask: lane d (1 <= d <
 /// kWindow) recomputes the particle and first bead of attempt y - d from its stream (block 0).
-__device__ __forceinline__ void DrawScored(WaveShared& sh, uint64_t y, uint32_t lane, uint32_t N, uint32_t M, uint32_t B, uint32_t NL,
-                                           uint32_t n_pad, const float4* __restrict__ pos) {
+__device__ __forceinline__ void DrawScored(WaveShared& sh, const WaveRing& ring, uint64_t y, uint32_t lane, uint32_t N, uint32_t M, uint32_t B,
+                                           uint32_t NL, uint32_t n_pad, const float4* __restrict__ pos) {
     const ChainDev& c = sh.c;
     const uint32_t sl = (uint32_t)y & (kRing - 1u);
-    const uint2 pb = DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, y}, lane, N, M, B, NL, n_pad, pos, sh.z[sl], sh.logu[sl], nullptr, sh.pb[sl]);
+    const uint2 pb = DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, y}, lane, N, M, B, NL, n_pad, pos, ring.Z(sl), ring.LU(sl), nullptr, sh.pb[sl]);
     bool hit = false;
     if (lane >= 1 && lane < kWindow && y >= lane) {
         const Philox4 w = MoveStream{c.seed, c.chain_id, c.move, y - lane}.Block(0);
@@ -607,6 +617,8 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
             stage[N * M + i] = v.y;
             stage[2 * N * M + i] = v.z;
         }
+    float* const ring_base = stage + (kStaged ? 3 * N * M : 0u);
+    const WaveRing ring{ring_base, ring_base + kRing * 3 * (B - 1), 3 * (B - 1), NL};
 
     const uint32_t nm1 = N > 1 ? N - 1 : 1;
     const uint32_t n_items = c.has_pair && N > 1 ? (N - 1) * (B - 1) : 0u;
@@ -621,11 +633,11 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
 
     uint64_t H = a.attempts[ci];  // the first attempt not yet run
     const uint64_t end = H + (n_sweeps ? n_sweeps * c.attempts_per_sweep : n_attempts);
-    uint32_t U = 0xffffffffu;     // bit i: attempt H + i not yet run
+    uint64_t U = ~0ull;           // bit i: attempt H + i not yet run (bits kWindow.. stay set)
     if (threadIdx.x == 0) sh.accepts = 0;
     // Prologue: the first window's draws, attempt H + x by sub-group x mod W.
     if (ws == draw_warp)
-        for (uint64_t y = H + sg; y < end && y < H + kWindow; y += W) DrawScored(sh, y, lane, N, M, B, NL, n_pad, pos);
+        for (uint64_t y = H + sg; y < end && y < H + kWindow; y += W) DrawScored(sh, ring, y, lane, N, M, B, NL, n_pad, pos);
     SubSync(15, G);
 
     while (H < end) {
@@ -634,14 +646,14 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
         bool ok = false;
         if (lane < kWindow && H + lane < end && ((U >> lane) & 1u)) {
             const uint32_t dep = sh.dep[(uint32_t)(H + lane) & kMask];
-            ok = ((__brev(dep) >> (31u - lane)) & U) == 0u;  // bit lane - d <- bit d of dep
+            ok = ((__brev(dep) >> (31u - lane)) & (uint32_t)U) == 0u;  // bit lane - d <- bit d of dep
         }
         const unsigned elig = __ballot_sync(0xffffffffu, ok);
         const uint32_t rank = __popc(elig & ((1u << lane) - 1u));  // eligible attempts before this lane's
         const unsigned sel = __ballot_sync(0xffffffffu, ok && rank < W);
         const unsigned mine = __ballot_sync(0xffffffffu, ok && rank == sg);
-        const unsigned U_next = U & ~sel;
-        const uint32_t adv = (uint32_t)__ffs(U_next) - 1u;  // attempts at the head that are now run
+        const uint64_t U_next = U & ~(uint64_t)sel;
+        const uint32_t adv = (uint32_t)__ffsll((long long)U_next) - 1u;  // attempts at the head that are now run (<= kWindow)
         if (mine) {
             const uint32_t pos_in_window = (uint32_t)__ffs(mine) - 1u;
             const uint64_t y = H + pos_in_window;
@@ -657,13 +669,13 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
             if (ws == 0) {
                 const float3 sv = path.Load(Wrap(b0 + (lane <= B ? lane : B), M), p);
                 const float3 se = path.Load(Wrap(b0 + B, M), p);
-                LeaderPhase<kPbc>(c, lane, NL, M, sv.x, sv.y, sv.z, se.x, se.y, se.z, sh.z[slot], sh.logu[slot], sh.on_[sg],
+                LeaderPhase<kPbc>(c, lane, NL, M, sv.x, sv.y, sv.z, se.x, se.y, se.z, ring.Z(slot), ring.LU(slot), sh.on_[sg],
                                   &sh.base0[sg], &sh.upper_ok[sg], nx, ny, nz);
             }
             // Draws that refill the window behind the head's advance (their slots are not in use).
             if (ws == draw_warp) {
                 if (draw_warp == 0) __syncwarp();
-                for (uint64_t yd = H + kWindow + sg; yd < H + kWindow + adv && yd < end; yd += W) DrawScored(sh, yd, lane, N, M, B, NL, n_pad, pos);
+                for (uint64_t yd = H + kWindow + sg; yd < H + kWindow + adv && yd < end; yd += W) DrawScored(sh, ring, yd, lane, N, M, B, NL, n_pad, pos);
             }
             SubSync(1 + sg, Gs);
             const bool upper_ok = sh.upper_ok[sg] != 0;
@@ -673,15 +685,15 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
             }
             SubSync(1 + sg, Gs);
             if (ws == 0) {
-                const bool accepted = upper_ok && Level0Accepts(c, lane, Gs, sh.part[sg], n_items != 0, sh.base0[sg], sh.logu[slot][0]);
+                const bool accepted = upper_ok && Level0Accepts(c, lane, Gs, sh.part[sg], n_items != 0, sh.base0[sg], ring.LU(slot)[0]);
                 if (accepted && lane >= 1 && lane < B) path.Store(Wrap(b0 + lane, M), p, nx, ny, nz);
                 if (accepted && lane == 0) atomicAdd(&sh.accepts, 1u);
             }
         } else if (ws == draw_warp) {
-            for (uint64_t yd = H + kWindow + sg; yd < H + kWindow + adv && yd < end; yd += W) DrawScored(sh, yd, lane, N, M, B, NL, n_pad, pos);
+            for (uint64_t yd = H + kWindow + sg; yd < H + kWindow + adv && yd < end; yd += W) DrawScored(sh, ring, yd, lane, N, M, B, NL, n_pad, pos);
         }
         SubSync(15, G);
-        U = adv ? (U_next >> adv) | (0xffffffffu << (32u - adv)) : U_next;
+        U = adv ? (U_next >> adv) | (~0ull << (64u - adv)) : U_next;
         H += adv;
     }
     if constexpr (kStaged)  // every round ended with a block barrier: all commits are visible
@@ -898,64 +910,77 @@ __device__ __forceinline__ void BlockSum4DD(dd v[4], dd (*s_red)[kHmcThreads / 3
     for (int q = 0; q < 4; ++q) v[q] = WarpSumDD(lane < nw ? s_red[q][lane] : DD(0.f));
 }
 
-/// Kinetic and trap gradient dS/dr (FP32) of bead `i` (row >= 1) of the block's rows and, with
-/// kEnergy, its share of S: the link to the next slice and its trap term. Rows i - N and i + N hold
-/// the neighbouring slices' beads.
+/// The block's beads: three coordinate planes of rows [nb + 2][N2] (row 0 and row nb + 1 are the
+/// neighbouring blocks' edge slices; N2 = N rounded up to even so that partner pairs load as float2).
+struct HmcRows {
+    float* x;
+    float* y;
+    float* z;
+    uint32_t N, N2;
+};
+
+/// Kinetic and trap gradient dS/dr (FP32) of bead (row, p), row >= 1, and, with kEnergy, its share
+/// of S: the link to the next slice and its trap term.
 template <bool kPbc, bool kEnergy>
-__device__ __forceinline__ float3 HmcBeadTerms(const ChainDev& c, const float4* __restrict__ R, uint32_t N, uint32_t i, float i4, float cofa,
-                                               dd& e_kin, dd& e_trap) {
-    const float4 r = R[i], rp = R[i - N], rn = R[i + N];
+__device__ __forceinline__ float3 HmcBeadTerms(const ChainDev& c, const HmcRows& R, uint32_t i, float i4, float cofa, dd& e_kin, dd& e_trap) {
+    const uint32_t ip = i - R.N2, in_ = i + R.N2;
+    const float x = R.x[i], y = R.y[i], z = R.z[i];
+    const float xp = R.x[ip], yp = R.y[ip], zp = R.z[ip], xn = R.x[in_], yn = R.y[in_], zn = R.z[in_];
     // links (b-1 -> b) and (b -> b+1): d/dr_b of |r_{b+1} - r_b|^2 i4 summed = 2 i4 (d_{b-1} - d_b)
-    const float dpx = Img<kPbc>(__fsub_rn(r.x, rp.x), c.L, c.iL), dpy = Img<kPbc>(__fsub_rn(r.y, rp.y), c.L, c.iL),
-                dpz = Img<kPbc>(__fsub_rn(r.z, rp.z), c.L, c.iL);
-    const float dnx = Img<kPbc>(__fsub_rn(rn.x, r.x), c.L, c.iL), dny = Img<kPbc>(__fsub_rn(rn.y, r.y), c.L, c.iL),
-                dnz = Img<kPbc>(__fsub_rn(rn.z, r.z), c.L, c.iL);
+    const float dpx = Img<kPbc>(__fsub_rn(x, xp), c.L, c.iL), dpy = Img<kPbc>(__fsub_rn(y, yp), c.L, c.iL),
+                dpz = Img<kPbc>(__fsub_rn(z, zp), c.L, c.iL);
+    const float dnx = Img<kPbc>(__fsub_rn(xn, x), c.L, c.iL), dny = Img<kPbc>(__fsub_rn(yn, y), c.L, c.iL),
+                dnz = Img<kPbc>(__fsub_rn(zn, z), c.L, c.iL);
     const float k2 = 2.f * i4;
     float3 g = make_float3(__fmul_rn(k2, __fsub_rn(dpx, dnx)), __fmul_rn(k2, __fsub_rn(dpy, dny)), __fmul_rn(k2, __fsub_rn(dpz, dnz)));
     if (c.has_trap) {
         const float t2 = 2.f * cofa;
-        g.x = __fmaf_rn(t2, r.x, g.x);
-        g.y = __fmaf_rn(t2, r.y, g.y);
-        g.z = __fmaf_rn(t2, r.z, g.z);
+        g.x = __fmaf_rn(t2, x, g.x);
+        g.y = __fmaf_rn(t2, y, g.y);
+        g.z = __fmaf_rn(t2, z, g.z);
     }
     if constexpr (kEnergy) {
-        dd ex = TwoSum(rn.x, -r.x), ey = TwoSum(rn.y, -r.y), ez = TwoSum(rn.z, -r.z);
+        dd ex = TwoSum(xn, -x), ey = TwoSum(yn, -y), ez = TwoSum(zn, -z);
         if (kPbc) {
             ex = Sub(ex, DD(__fmul_rn(c.L, rintf(__fmul_rn(ex.hi, c.iL)))));
             ey = Sub(ey, DD(__fmul_rn(c.L, rintf(__fmul_rn(ey.hi, c.iL)))));
             ez = Sub(ez, DD(__fmul_rn(c.L, rintf(__fmul_rn(ez.hi, c.iL)))));
         }
         e_kin = Add(e_kin, Add(Add(Sqr(ex), Sqr(ey)), Sqr(ez)));
-        e_trap = AddSq(AddSq(AddSq(e_trap, r.x), r.y), r.z);
+        e_trap = AddSq(AddSq(AddSq(e_trap, x), y), z);
     }
     return g;
 }
 
-/// Pair forces on two beads of one row at once (particles p0 and p1; f32x2 arithmetic, each half
-/// rounding as the scalar form does): sum over q of V'(r)/r (r_p - r_q) with V = 1/r clamped to the
-/// table's range, so V' = -1/r^2 inside it and 0 where clamped (q = p: r = 0 is below the range,
-/// whose lower end is positive). With kEnergy also the sum over q != p of V(r) for both beads. Without
-/// `two` the second half repeats p0 and only its forces are formed (and discarded).
+/// Pair force on bead (row, p): sum over q of V'(r)/r (r_p - r_q), V = 1/r clamped to the table's
+/// range, so V' = -1/r^2 inside it and 0 where clamped (q = p: r = 0 is below the range, whose lower
+/// end is positive). Partners go two at a time (q, q + 1) in f32x2 arithmetic, each half rounding
+/// as the scalar form does; the even and odd partners' sums are added at the end (an odd N's last
+/// partner joins the odd sum). With kEnergy also the sum over q != p of V(r).
 template <bool kPbc, bool kEnergy>
-__device__ __forceinline__ void HmcPairs2(const ChainDev& c, const float4* __restrict__ row, uint32_t N, uint32_t p0, uint32_t p1, bool two,
-                                          float2& fx, float2& fy, float2& fz, Comp& e_pair) {
-    if (!two) p1 = p0;
-    const float4 a0 = row[p0], a1 = row[p1];
-    const float2 X = make_float2(a0.x, a1.x), Y = make_float2(a0.y, a1.y), Z = make_float2(a0.z, a1.z);
+__device__ __forceinline__ float3 HmcPairForce(const ChainDev& c, const HmcRows& R, uint32_t row0, uint32_t p, Comp& e_pair) {
+    const float* __restrict__ rx = R.x + row0;
+    const float* __restrict__ ry = R.y + row0;
+    const float* __restrict__ rz = R.z + row0;
+    const float x = rx[p], y = ry[p], z = rz[p];
+    const float2 X = make_float2(x, x), Y = make_float2(y, y), Z = make_float2(z, z);
     const float r2lo = c.r2_min, r2hi = c.r2_max;
-    fx = fy = fz = make_float2(0.f, 0.f);
-#pragma unroll 4
-    for (uint32_t q = 0; q < N; ++q) {
-        const float4 b = row[q];
-        const float2 ux = Img2<kPbc>(Sub2(X, make_float2(b.x, b.x)), c.L, c.iL);
-        const float2 uy = Img2<kPbc>(Sub2(Y, make_float2(b.y, b.y)), c.L, c.iL);
-        const float2 uz = Img2<kPbc>(Sub2(Z, make_float2(b.z, b.z)), c.L, c.iL);
+    const uint32_t N = R.N, Ne = N & ~1u;
+    float2 fx = make_float2(0.f, 0.f), fy = fx, fz = fx;
+#pragma unroll 2
+    for (uint32_t q = 0; q < Ne; q += 2) {
+        const float2 bx = *reinterpret_cast<const float2*>(rx + q);
+        const float2 by = *reinterpret_cast<const float2*>(ry + q);
+        const float2 bz = *reinterpret_cast<const float2*>(rz + q);
+        const float2 ux = Img2<kPbc>(Sub2(X, bx), c.L, c.iL);
+        const float2 uy = Img2<kPbc>(Sub2(Y, by), c.L, c.iL);
+        const float2 uz = Img2<kPbc>(Sub2(Z, bz), c.L, c.iL);
         const float2 r2 = Sq3x2(ux, uy, uz);
         const float c0 = fminf(fmaxf(r2.x, r2lo), r2hi), c1 = fminf(fmaxf(r2.y, r2lo), r2hi);
         const float2 inv = make_float2(rsqrtf(c0), rsqrtf(c1));
         if constexpr (kEnergy) {
-            CompAdd(e_pair, q == p0 ? 0.f : inv.x);
-            CompAdd(e_pair, (q == p1 || !two) ? 0.f : inv.y);
+            CompAdd(e_pair, q == p ? 0.f : inv.x);
+            CompAdd(e_pair, q + 1 == p ? 0.f : inv.y);
         }
         float2 f = Mul2(Mul2(inv, inv), inv);
         f.x = c0 == r2.x ? f.x : 0.f;
@@ -964,42 +989,48 @@ __device__ __forceinline__ void HmcPairs2(const ChainDev& c, const float4* __res
         fy = Fma2(f, uy, fy);
         fz = Fma2(f, uz, fz);
     }
+    if (N & 1u) {
+        const uint32_t q = N - 1;
+        const float ux = Img<kPbc>(__fsub_rn(x, rx[q]), c.L, c.iL), uy = Img<kPbc>(__fsub_rn(y, ry[q]), c.L, c.iL),
+                    uz = Img<kPbc>(__fsub_rn(z, rz[q]), c.L, c.iL);
+        const float r2 = Sq3(ux, uy, uz);
+        const float cq = fminf(fmaxf(r2, r2lo), r2hi);
+        const float inv = rsqrtf(cq);
+        if constexpr (kEnergy) CompAdd(e_pair, q == p ? 0.f : inv);
+        const float f = cq == r2 ? __fmul_rn(__fmul_rn(inv, inv), inv) : 0.f;
+        fx.y = __fmaf_rn(f, ux, fx.y);
+        fy.y = __fmaf_rn(f, uy, fy.y);
+        fz.y = __fmaf_rn(f, uz, fz.y);
+    }
+    return make_float3(__fadd_rn(fx.x, fx.y), __fadd_rn(fy.x, fy.y), __fadd_rn(fz.x, fz.y));
 }
 
-/// One kick P -= f dS/dR for the block's beads, task = (row, particles h and h + hN); with kEnergy
-/// also the block's shares of S and |P|^2 (before the kick when `p2_before`, after it when
-/// `p2_after`).
+/// One kick P -= f dS/dR for the block's beads; with kEnergy also the block's shares of S and
+/// |P|^2 (before the kick when `p2_before`, after it when `p2_after`).
 template <bool kPbc, bool kEnergy>
-__device__ __forceinline__ void HmcKick(const ChainDev& c, const float4* __restrict__ R, float* px, float* py, float* pz, uint32_t N, uint32_t hN,
-                                        uint32_t n_tasks, float f, bool p2_before, bool p2_after, dd& ek, dd& et, Comp& cp, dd& em) {
+__device__ __forceinline__ void HmcKick(const ChainDev& c, const HmcRows& R, float* px, float* py, float* pz, uint32_t E, float f, bool p2_before,
+                                        bool p2_after, dd& ek, dd& et, Comp& cp, dd& em) {
     const float i4 = c.i4lt_level[0], cofa = c.trap_cofa, tau = c.tau;
-    for (uint32_t task = threadIdx.x; task < n_tasks; task += blockDim.x) {
-        const uint32_t lb = task / hN, p0 = task - lb * hN, p1 = p0 + hN;
-        const bool two = p1 < N;
-        const uint32_t rowi = (lb + 1) * N;
-        float2 fx = make_float2(0.f, 0.f), fy = fx, fz = fx;
-        if (c.has_pair) HmcPairs2<kPbc, kEnergy>(c, R + rowi, N, p0, p1, two, fx, fy, fz, cp);
-#pragma unroll
-        for (uint32_t u = 0; u < 2; ++u) {
-            if (u == 1 && !two) break;
-            const uint32_t pp = u ? p1 : p0;
-            float3 g = HmcBeadTerms<kPbc, kEnergy>(c, R, N, rowi + pp, i4, cofa, ek, et);
-            if (c.has_pair) {
-                g.x = __fmaf_rn(-tau, u ? fx.y : fx.x, g.x);
-                g.y = __fmaf_rn(-tau, u ? fy.y : fy.x, g.y);
-                g.z = __fmaf_rn(-tau, u ? fz.y : fz.x, g.z);
-            }
-            const uint32_t i = lb * N + pp;
-            float mx = px[i], my = py[i], mz = pz[i];
-            if (kEnergy && p2_before) em = AddSq(AddSq(AddSq(em, mx), my), mz);  // |P|^2 before the first kick
-            mx = __fmaf_rn(-f, g.x, mx);
-            my = __fmaf_rn(-f, g.y, my);
-            mz = __fmaf_rn(-f, g.z, mz);
-            if (kEnergy && p2_after) em = AddSq(AddSq(AddSq(em, mx), my), mz);  // |P|^2 after the last kick
-            px[i] = mx;
-            py[i] = my;
-            pz[i] = mz;
+    const uint32_t N = R.N, N2 = R.N2;
+    for (uint32_t i = threadIdx.x; i < E; i += blockDim.x) {
+        const uint32_t lb = i / N, p = i - lb * N;
+        const uint32_t row0 = (lb + 1) * N2;
+        float3 g = HmcBeadTerms<kPbc, kEnergy>(c, R, row0 + p, i4, cofa, ek, et);
+        if (c.has_pair) {
+            const float3 fp = HmcPairForce<kPbc, kEnergy>(c, R, row0, p, cp);
+            g.x = __fmaf_rn(-tau, fp.x, g.x);
+            g.y = __fmaf_rn(-tau, fp.y, g.y);
+            g.z = __fmaf_rn(-tau, fp.z, g.z);
         }
+        float mx = px[i], my = py[i], mz = pz[i];
+        if (kEnergy && p2_before) em = AddSq(AddSq(AddSq(em, mx), my), mz);  // |P|^2 before the first kick
+        mx = __fmaf_rn(-f, g.x, mx);
+        my = __fmaf_rn(-f, g.y, my);
+        mz = __fmaf_rn(-f, g.z, mz);
+        if (kEnergy && p2_after) em = AddSq(AddSq(AddSq(em, mx), my), mz);  // |P|^2 after the last kick
+        px[i] = mx;
+        py[i] = my;
+        pz[i] = mz;
     }
 }
 
@@ -1010,25 +1041,28 @@ struct HmcShared {
 };
 
 /// Halo rows 0 and nb + 1 from the neighbouring blocks' last and first own rows (the ring wraps).
-__device__ __forceinline__ void HmcHalos(cooperative_groups::cluster_group& cl, float4* R, uint32_t N, uint32_t nb) {
-    const uint32_t k = cl.num_blocks(), r = cl.block_rank();
-    const float4* left = cl.map_shared_rank(R, (r + k - 1) % k);
-    const float4* right = cl.map_shared_rank(R, (r + 1) % k);
-    for (uint32_t p = threadIdx.x; p < N; p += blockDim.x) {
-        R[p] = left[nb * N + p];
-        R[(nb + 1) * N + p] = right[N + p];
+__device__ __forceinline__ void HmcHalos(cooperative_groups::cluster_group& cl, const HmcRows& R, uint32_t nb) {
+    const uint32_t k = cl.num_blocks(), r = cl.block_rank(), N = R.N, N2 = R.N2;
+    float* planes[3] = {R.x, R.y, R.z};
+    for (uint32_t i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+        const uint32_t d = i / N, p = i - d * N;
+        float* mine = planes[d];
+        const float* left = cl.map_shared_rank(mine, (r + k - 1) % k);
+        const float* right = cl.map_shared_rank(mine, (r + 1) % k);
+        mine[p] = left[nb * N2 + p];
+        mine[(nb + 1) * N2 + p] = right[N2 + p];
     }
 }
 
 template <bool kPbc>
-__device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c, uint32_t ci, float4* R, HmcShared& sh) {
+__device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c, uint32_t ci, float* smem, HmcShared& sh) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
     const uint32_t k = cl.num_blocks(), r = cl.block_rank();
-    const uint32_t N = c.n_part, M = c.n_bead, n_pad = c.n_pad;
-    const uint32_t nb = M / k, b_lo = r * nb, E = nb * N;
-    const uint32_t hN = (N + 1) / 2, n_tasks = nb * hN;  // task: (row, particles h and h + hN)
-    float* px = reinterpret_cast<float*>(R + (nb + 2) * N);
+    const uint32_t N = c.n_part, M = c.n_bead, n_pad = c.n_pad, N2 = N + (N & 1u);
+    const uint32_t nb = M / k, b_lo = r * nb, E = nb * N, RW = (nb + 2) * N2;
+    const HmcRows R{smem, smem + RW, smem + 2 * RW, N, N2};
+    float* px = smem + 3 * RW;
     float* py = px + E;
     float* pz = py + E;
     const uint32_t t = threadIdx.x, T = blockDim.x;
@@ -1040,8 +1074,11 @@ __device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c
         const MoveStream st{c.seed, c.chain_id, c.hmc_move, att};
         // own slices from the committed path (this block wrote them last); momenta from the stream
         for (uint32_t i = t; i < E; i += T) {
-            const uint32_t lb = i / N, p = i - lb * N, b = b_lo + lb;
-            R[N + i] = pos[(size_t)b * n_pad + p];
+            const uint32_t lb = i / N, p = i - lb * N, b = b_lo + lb, ri = (lb + 1) * N2 + p;
+            const float4 v = pos[(size_t)b * n_pad + p];
+            R.x[ri] = v.x;
+            R.y[ri] = v.y;
+            R.z[ri] = v.z;
             float z3[3];
             const uint32_t j0 = (p * M + b) * 3u;
             for (uint32_t d = 0; d < 3; ++d) {
@@ -1057,7 +1094,7 @@ __device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c
             pz[i] = z3[2];
         }
         cl.sync();
-        HmcHalos(cl, R, N, nb);
+        HmcHalos(cl, R, nb);
         cl.sync();
         double h_start = 0., h_end = 0.;
         const uint32_t n_steps = c.hmc_steps;
@@ -1067,8 +1104,8 @@ __device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c
             const float f = with_energy ? 0.5f * eps : eps;
             dd ek = DD(0.f), et = DD(0.f), em = DD(0.f);
             Comp cp{0.f, 0.f};
-            if (with_energy) HmcKick<kPbc, true>(c, R, px, py, pz, N, hN, n_tasks, f, s == 0, s == n_steps, ek, et, cp, em);
-            else HmcKick<kPbc, false>(c, R, px, py, pz, N, hN, n_tasks, f, false, false, ek, et, cp, em);
+            if (with_energy) HmcKick<kPbc, true>(c, R, px, py, pz, E, f, s == 0, s == n_steps, ek, et, cp, em);
+            else HmcKick<kPbc, false>(c, R, px, py, pz, E, f, false, false, ek, et, cp, em);
             if (with_energy) {
                 dd v[4] = {ek, et, CompDD(cp), em};
                 BlockSum4DD(v, sh.red);
@@ -1090,14 +1127,13 @@ __device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c
             __syncthreads();  // every gradient read of R is done
             if (s == n_steps) break;
             for (uint32_t i = t; i < E; i += T) {  // drift
-                float4 v = R[N + i];
-                v.x = __fmaf_rn(eps, px[i], v.x);
-                v.y = __fmaf_rn(eps, py[i], v.y);
-                v.z = __fmaf_rn(eps, pz[i], v.z);
-                R[N + i] = v;
+                const uint32_t lb = i / N, ri = (lb + 1) * N2 + (i - lb * N);
+                R.x[ri] = __fmaf_rn(eps, px[i], R.x[ri]);
+                R.y[ri] = __fmaf_rn(eps, py[i], R.y[ri]);
+                R.z[ri] = __fmaf_rn(eps, pz[i], R.z[ri]);
             }
             cl.sync();  // every block drifted its slices
-            HmcHalos(cl, R, N, nb);
+            HmcHalos(cl, R, nb);
             cl.sync();  // every block read its halos before the next drift
         }
         if (t == 0) {
@@ -1108,8 +1144,8 @@ __device__ void HmcChain(const BatchArgs& a, const HmcArgs& h, const ChainDev& c
         __syncthreads();
         if (sh.accept) {
             for (uint32_t i = t; i < E; i += T) {
-                const uint32_t lb = i / N, p = i - lb * N;
-                pos[(size_t)(b_lo + lb) * n_pad + p] = R[N + i];
+                const uint32_t lb = i / N, p = i - lb * N, ri = (lb + 1) * N2 + p;
+                pos[(size_t)(b_lo + lb) * n_pad + p] = make_float4(R.x[ri], R.y[ri], R.z[ri], 0.f);
             }
             ++acc;
         }
@@ -1129,8 +1165,9 @@ __global__ void __launch_bounds__(kHmcThreads, 2) BatchHmcKernel(BatchArgs a, Hm
     if (c.hmc_eps == 0.f) return;  // the chain has no HMC move (every block of its cluster returns)
     __shared__ HmcShared sh;
     extern __shared__ float4 hmc_stage[];
-    if (c.pbc) HmcChain<true>(a, h, c, ci, hmc_stage, sh);
-    else HmcChain<false>(a, h, c, ci, hmc_stage, sh);
+    float* smem = reinterpret_cast<float*>(hmc_stage);
+    if (c.pbc) HmcChain<true>(a, h, c, ci, smem, sh);
+    else HmcChain<false>(a, h, c, ci, smem, sh);
 }
 
 /// Host layout (every chain's [n_part][n_bead][3] doubles, concatenated) to the device float4
@@ -1420,8 +1457,9 @@ void ChainBatch::SetTiles(uint32_t ipl, uint32_t mw, uint32_t wave) {
             c.n_wave = W;
             c.sub_warps = gs;
             c.n_warps = W * gs;
-            // The path in shared memory (three FP32 planes) when it fits next to the static part.
-            c.staged = (size_t)12 * c.n_part * c.n_bead <= stage_cap ? 1u : 0u;
+            // The path in shared memory (three FP32 planes) when it fits next to the static part and
+            // the ring of drawn attempts.
+            c.staged = (size_t)12 * c.n_part * c.n_bead + RingBytes(1u << c.n_level, c.n_level) <= stage_cap ? 1u : 0u;
         } else {
             c.n_wave = 1;
             c.n_warps = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(g, mw));
@@ -1431,7 +1469,8 @@ void ChainBatch::SetTiles(uint32_t ipl, uint32_t mw, uint32_t wave) {
     }
     stage_bytes = 0;
     for (const auto& c : chains)
-        if (c.staged) stage_bytes = std::max(stage_bytes, (size_t)12 * c.n_part * c.n_bead);
+        if (c.n_wave > 1)
+            stage_bytes = std::max(stage_bytes, (c.staged ? (size_t)12 * c.n_part * c.n_bead : 0) + RingBytes(1u << c.n_level, c.n_level));
     stage_bytes = (stage_bytes + 15) & ~size_t(15);
     CudaCheck(cudaFuncSetAttribute(BatchSweepKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_bytes), "smem attribute");
     order.resize(n_chains);
@@ -1533,13 +1572,14 @@ void ChainBatch::LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts) {
 }
 
 size_t ChainBatch::HmcSmem(uint32_t k) const {
-    // per block: R rows (float4) with one halo row on each side, three P planes for its own rows
+    // per block: three R planes of rows padded to an even length with one halo row on each side,
+    // three P planes for its own beads
     size_t bytes = 0;
     for (const auto& s : specs) {
         if (!s.has_hmc) continue;
         if (k == 0 || s.n_bead % k != 0) return 0;
-        const size_t nb = s.n_bead / k;
-        bytes = std::max(bytes, (size_t)16 * s.n_part * (nb + 2) + (size_t)12 * s.n_part * nb);
+        const size_t nb = s.n_bead / k, n2 = s.n_part + (s.n_part & 1u);
+        bytes = std::max(bytes, (size_t)12 * n2 * (nb + 2) + (size_t)12 * s.n_part * nb);
     }
     return bytes;
 }
