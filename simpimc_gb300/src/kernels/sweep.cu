@@ -127,7 +127,7 @@ struct SweepArgs {
     unsigned long long* bar;
     int* err;
     float2* partials;         // [2][gridDim.x]
-    float4* level_out;        // [2][kMaxLevels]: (diff, small) of each level from its designated block
+    float4* level_out;        // [2][kWaveSlots][kMaxLevels]: (diff, small) of each level from its designated block
     uint64_t timeout_ns;
     unsigned long long* phase_cycles;  // optional [kSweepPhases]: block 0's cycles per phase, summed
     // Concurrent attempts: `wave` groups of `group_ctas` blocks; the schedule flattened per
@@ -345,32 +345,32 @@ __device__ __forceinline__ uint32_t LevelFirst(uint32_t nl, int lvl, uint32_t B)
 /// first bead to GetNextBead(B), which is the first bead itself (kinetic_class.h:111-117).
 __device__ __forceinline__ void LevelSums(const MoveDD& mv, int lvl, uint32_t B, bool kin_links, const dd* seg, const dd* disp,
                                           uint32_t first, uint32_t n_d, dd L, dd iL, int lane, dd& lsp, dd& small) {
-    const uint32_t skip = 1u << lvl, nm = B / (2 * skip);
+    // Every term is a sum over dimensions (|d|^2 and the image splines), so one lane takes one
+    // (item, dimension) pair: the latency of a lane is one dimension's spline evaluation.
+    const uint32_t skip = 1u << lvl, nm = B / (2 * skip), nj = (B + skip - 1) / skip;
     dd sp{0.f, 0.f}, sm{0.f, 0.f};
-    for (uint32_t t = lane; t < nm; t += 32) {
-        dd q{0.f, 0.f};
-        for (uint32_t d = 0; d < n_d; ++d) q = Add(q, Sqr(disp[3 * (first + t) + d]));
-        dd v = Mul(q, mv.i4s[lvl]);
-        if (mv.has_images) v = Add(v, ImageSum(mv.sample_image[lvl], &disp[3 * (first + t)], n_d));
+    for (uint32_t i = lane; i < nm * n_d; i += 32) {
+        const uint32_t tt = i / n_d, d = i - tt * n_d;
+        const dd x = disp[3 * (first + tt) + d];
+        dd v = Mul(Sqr(x), mv.i4s[lvl]);
+        if (mv.has_images) v = Add(v, EvalCubicDD(mv.sample_image[lvl], x));
         sp = Add(sp, v);
     }
     for (int ki = 0; ki < (kin_links ? mv.n_kin : 0); ++ki)
-        for (uint32_t j = lane * skip; j < B; j += 32 * skip) {
-            dd dr[3];
-            dd q{0.f, 0.f};
-            for (uint32_t d = 0; d < n_d; ++d) {
-                dr[d] = MinImageDD(Sub(seg[3 * j + d], seg[3 * (j + skip) + d]), L, iL);
-                q = Add(q, Sqr(dr[d]));
-            }
-            dd v = Mul(q, mv.kin_i4[ki][lvl]);
-            if (mv.kin_has_images[ki]) v = Add(v, ImageSum(mv.kin_image[ki][lvl], dr, n_d));
+        for (uint32_t i = lane; i < nj * n_d; i += 32) {
+            const uint32_t jt = i / n_d, d = i - jt * n_d, j = jt * skip;
+            const dd dr = MinImageDD(Sub(seg[3 * j + d], seg[3 * (j + skip) + d]), L, iL);
+            dd v = Mul(Sqr(dr), mv.kin_i4[ki][lvl]);
+            if (mv.kin_has_images[ki]) v = Add(v, EvalCubicDD(mv.kin_image[ki][lvl], dr));
             sm = Add(sm, v);
         }
     for (int ti = 0; ti < mv.n_trap; ++ti) {
         if ((uint32_t)lvl > mv.trap_max_level[ti]) continue;
         dd acc{0.f, 0.f};
-        for (uint32_t j = lane * skip; j < B; j += 32 * skip)
-            for (uint32_t d = 0; d < n_d; ++d) acc = Add(acc, Sqr(seg[3 * j + d]));
+        for (uint32_t i = lane; i < nj * n_d; i += 32) {
+            const uint32_t jt = i / n_d, d = i - jt * n_d;
+            acc = Add(acc, Sqr(seg[3 * (jt * skip) + d]));
+        }
         sm = Add(sm, MulF(Mul(acc, mv.trap_cofa[ti]), (float)skip));
     }
     WarpSum2DD(sp, sm);
@@ -887,20 +887,29 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                         return;
                     }
                     PIMC_PHASE(4);
-                    if (warp == 0) {
+                    // The group's partials, one per thread in a single round trip, summed per warp
+                    // and then over the warps in order (the same total in every block).
+                    const uint32_t n_pw = (Gg + 31) / 32;
+                    if ((uint32_t)warp < n_pw) {
+                        const uint32_t c2 = (uint32_t)tid;
                         dd t{0.f, 0.f};
-                        for (uint32_t c2 = grp * Gg + lane; c2 < (grp + 1) * Gg; c2 += 32) {
-                            const float2 pv = __ldcg(&a.partials[(nbar & 1ull) * G + c2]);
-                            t = Add(t, dd{pv.x, pv.y});
+                        if (c2 < Gg) {
+                            const float2 pv = __ldcg(&a.partials[(nbar & 1ull) * G + grp * Gg + c2]);
+                            t = dd{pv.x, pv.y};
                         }
                         t = WarpSumDD(t);
+                        if (lane == 0) s_red[warp] = t;
+                    } else if ((uint32_t)warp == n_pw && lane < (int)nl) {
+                        // level sums from the designated blocks (written before their arrival)
+                        const float4 v = __ldcg(&a.level_out[((nbar & 1ull) * kWaveSlots + grp) * kMaxLevels + lane]);
+                        s_lvl_diff[lane] = dd{v.x, v.y};
+                        s_lvl_small[lane] = dd{v.z, v.w};
+                    }
+                    __syncthreads();
+                    if (warp == 0) {
+                        dd t = (uint32_t)lane < n_pw ? s_red[lane] : dd{0.f, 0.f};
+                        t = WarpSumDD(t);
                         if (lane == 0) s_big = t;
-                        if (lane < (int)nl) {
-                            // level sums from the designated blocks (written before their arrival)
-                            const float4 v = __ldcg(&a.level_out[((nbar & 1ull) * kWaveSlots + grp) * kMaxLevels + lane]);
-                            s_lvl_diff[lane] = dd{v.x, v.y};
-                            s_lvl_small[lane] = dd{v.z, v.w};
-                        }
                     }
                     __syncthreads();
                     PIMC_PHASE(5);
@@ -1010,44 +1019,64 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
         // Rounds of concurrent attempts: the longest prefix of the next `wave` attempts of the
         // schedule in which no attempt reads what an earlier one may change; group j runs attempt
         // j (the sequential chain's result), and a second grid barrier makes every commit visible
-        // before the next round reads. Idle groups keep the barrier count.
+        // before the next round reads, unless the next round reads nothing this round changes
+        // (its own first barrier then orders these commits before any later round). Idle groups
+        // keep the barrier count.
         const uint64_t total = a.n_rep * a.per_rep;
+        const uint32_t W = a.wave;  // <= kWaveSlots = 8: lanes 0..2W-1 hold this round's and the next round's candidates
         uint64_t A = 0;
         while (A < total) {
-            uint32_t wm[kWaveSlots], wb0[kWaveSlots], wB[kWaveSlots];
-            uint64_t wc[kWaveSlots];
-            uint32_t w = 0;
-            for (uint32_t j = 0; j < a.wave && A + j < total; ++j) {
-                const uint64_t x = A + j, rep = x / a.per_rep, r = x - rep * a.per_rep;
+            // Lane x: attempt A + x of the schedule (move, counter, first slice, length) and the
+            // mask of the earlier candidates it conflicts with (the same on every warp).
+            const uint32_t x = (uint32_t)lane;
+            const bool valid = x < 2 * W && A + x < total;
+            uint32_t m = 0, bj = 0, Bj = 1;
+            uint64_t actr = 0;
+            if (valid) {
+                const uint64_t xx = A + x, rep = xx / a.per_rep, r = xx - rep * a.per_rep;
                 uint32_t lo = 0, hi = a.n_entries;  // the entry holding position r of a repetition
                 while (hi - lo > 1) {
                     const uint32_t mid = (lo + hi) >> 1;
                     if (a.sched_prefix[mid] <= r) lo = mid;
                     else hi = mid;
                 }
-                const uint32_t m = a.sched_move[lo];
-                const uint64_t actr = a.attempt_base[m] + rep * a.per_rep_move[m] + a.move_before[lo] + (r - a.sched_prefix[lo]);
+                m = a.sched_move[lo];
+                actr = a.attempt_base[m] + rep * a.per_rep_move[m] + a.move_before[lo] + (r - a.sched_prefix[lo]);
                 const Philox4 w0 = MoveStream{a.seed, a.chain, m, actr}.Block(0);
-                const uint32_t bj = UniformIndex(w0.v[1], M);  // the attempt's first slice
-                const uint32_t Bj = 1u << s_moves[m].n_level;
-                bool clear = true;
-                for (uint32_t i = 0; i < j && clear; ++i) clear = !Conflicts(wb0[i], wB[i], bj, Bj, M);
-                if (!clear) break;
-                wm[j] = m;
-                wc[j] = actr;
-                wb0[j] = bj;
-                wB[j] = Bj;
-                ++w;
+                bj = UniformIndex(w0.v[1], M);  // the attempt's first slice
+                Bj = 1u << s_moves[m].n_level;
             }
+            uint32_t cmask = 0;  // bit i: attempt A + i (i < x) changes what attempt A + x reads
+            for (uint32_t i = 0; i < 2 * W; ++i) {
+                const uint32_t bi = __shfl_sync(0xffffffffu, bj, (int)i), Bi = __shfl_sync(0xffffffffu, Bj, (int)i);
+                if (valid && i < x && Conflicts(bi, Bi, bj, Bj, M)) cmask |= 1u << i;
+            }
+            const uint32_t n_valid = (uint32_t)__popc(__ballot_sync(0xffffffffu, valid));
+            // This round: the longest prefix of [0, W) in which no attempt conflicts with an earlier one.
+            const unsigned end_r = __ballot_sync(0xffffffffu, valid && x >= 1 && x < W && (cmask & ((1u << x) - 1u)) != 0u);
+            const uint32_t w = end_r ? (uint32_t)__ffs(end_r) - 1u : min(W, n_valid);
+            // The next round: its prefix from w; the commit barrier is skipped when none of its
+            // attempts reads what this round's attempts change.
+            const uint32_t below_next = (1u << (w + (x > w ? x - w : 0u))) - 1u;  // candidates w .. x - 1
+            const unsigned end_n = __ballot_sync(0xffffffffu, valid && x > w && x < w + W && (cmask & below_next & ~((1u << w) - 1u)) != 0u);
+            const uint32_t w_next = end_n ? (uint32_t)__ffs(end_n) - 1u - w : min(W, n_valid - w);
+            const unsigned cross = __ballot_sync(0xffffffffu, valid && x >= w && x < w + w_next && (cmask & ((1u << w) - 1u)) != 0u);
+            const bool commit_barrier = cross != 0u || w_next == 0u;
+            const uint32_t my_m = __shfl_sync(0xffffffffu, m, (int)(grp < w ? grp : 0u));
+            const uint64_t my_c = __shfl_sync(0xffffffffu, actr, (int)(grp < w ? grp : 0u));
             if (grp < w) {
-                attempt(wm[grp], wc[grp]);
+                attempt(my_m, my_c);
                 if (abort) return;
             } else {
                 ++nbar;
                 if (!GridBarrier(a.bar, nbar, a.err, a.timeout_ns)) return;
             }
-            ++nbar;
-            if (!GridBarrier(a.bar, nbar, a.err, a.timeout_ns)) return;
+            if (commit_barrier) {
+                ++nbar;
+                if (!GridBarrier(a.bar, nbar, a.err, a.timeout_ns)) return;
+            } else {
+                __syncthreads();  // the block's own commits before its next round's reads
+            }
             A += w;
         }
     }
@@ -1654,6 +1683,7 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
     const uint32_t Gg = (uint32_t)G0 / wave;
     const int G = (int)(Gg * wave);
     if (Gg < max_level + 1) throw PimcError(kErrArg, "sweep grid (per concurrent attempt) smaller than the bisection level count");
+    if (Gg + 32 > (uint32_t)kThreads) throw PimcError(kErrArg, "sweep grid per concurrent attempt above 480 blocks (one partial per thread)");
     uint32_t R = 1;
     while (R * 2 <= (1u << max_level) && R * 2 <= Gg) R *= 2;
     const uint32_t spc = std::max<uint32_t>(1, (1u << max_level) / R);
