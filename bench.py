@@ -18,6 +18,8 @@ Also reported on the same line:
   plain_same_system  the single-chain GPU path (double-float sweep kernel, FP64 HMC) running the
                      same cycle on a sample of the same chains, one chain at a time (what the
                      batched kernels replace);
+  same_shape_chains  152 chains of the heaviest shape (N = 127, M = 128) swept as one batch and as
+                     single-chain contexts through pimc_sweep_chains (one CTA per chain);
   energy_gate        per-chain energies and blocking error bars of the batched FP32 chains
                      against the single-chain path on the same chains and seeds, after an
                      equilibration of the paths;
@@ -496,6 +498,53 @@ def exchange_bosons_chains(local, tmp, n_chains=608, sweeps=10):
             "note": "pimc_sweep_chains: one launch, one CTA per chain; wall-clock time including argument upload and counter reads"}
 
 
+def same_shape_chains(local, tmp, n_chains=152, sweeps=2, shape=(127, 128)):
+    """Bisection sweeps of n_chains trapped Coulomb chains of one shape (the headline's heaviest,
+    N = 127, M = 128, level 3; seeds 5000 + c), as one ChainBatch and as n_chains single-chain
+    contexts swept by pimc_sweep_chains (one launch, one CTA per chain, double-float): device time
+    of `sweeps` sweeps on each side, after a warm-up sweep."""
+    import torch
+    from simpimc_gb300 import ChainBatch, Simulation, sweep_chains
+    from simpimc_gb300.configs import trapped_coulomb
+    n, m = shape
+    d = Path(tmp) / "same_shape"
+    items = [trapped_coulomb(d, n_part=n, n_bead=m, n_level=CHAIN_LEVEL, seed=5000 + c, write_table=(c == 0)) for c in range(n_chains)]
+    reps = n * math.ceil(m / (1 << CHAIN_LEVEL))
+    b = ChainBatch([x for x, _ in items], base_dir=d, device=local)
+    for c, (_, p) in enumerate(items):
+        b.set_path(c, p)
+    b.autotune(1)
+    b.sweeps(1)
+    st = torch.cuda.ExternalStream(b.stream(), device=torch.device("cuda", local))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    b.sweeps(sweeps)
+    e1.record(st)
+    e1.synchronize()
+    batch_s = e0.elapsed_time(e1) / 1e3
+    b.close()
+    sims = []
+    for c, (x, p) in enumerate(items):
+        s = Simulation(x, base_dir=d, device=local, chain=c)
+        s.set_path(p)
+        sims.append(s)
+    sweep_chains(sims, [0], [reps], 1)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sweep_chains(sims, [0], [reps], sweeps)
+    torch.cuda.synchronize()
+    chains_s = time.perf_counter() - t0
+    for s in sims:
+        s.close()
+    moves = n_chains * sweeps * reps * ((1 << CHAIN_LEVEL) - 1)
+    return {"workload": f"{n_chains} trapped Coulomb chains N={n} M={m} level {CHAIN_LEVEL}, bisection sweeps", "sweeps": sweeps,
+            "batch": {"value": moves / batch_s, "unit": METRIC, "seconds": batch_s, "note": "ChainBatch, FP32 positions, device time"},
+            "sweep_chains": {"value": moves / chains_s, "unit": METRIC, "seconds": chains_s,
+                             "note": "pimc_sweep_chains on single-chain contexts (double-float), one CTA per chain; wall-clock "
+                                     "time of the call with the device synchronised on both sides"},
+            "ratio": chains_s / batch_s}
+
+
 def cpu_oracle_chains(items, tmp, seconds, chains):
     """The oracle on one host core, running the batch's cycle (bisection sweep + HMC attempt) on
     `chains` round robin."""
@@ -588,8 +637,10 @@ def run_ours(args):
     hatt1, hacc1 = batch.hmc_counters()
 
     # The two kernels alone (for their rooflines): one launch per step, same flush.
+    rounds1 = batch.rounds()
     k_ms = time_launches(stream, flush, args.steps, lambda: batch.sweeps(1))
     att2, acc2 = batch.counters()
+    rounds2 = batch.rounds()
     h_ms = time_launches(stream, flush, args.steps, lambda: batch.hmc_attempts(1))
 
     # e2e: every chain's path from pinned host memory, one cycle, energies and paths back, every step.
@@ -630,9 +681,21 @@ def run_ours(args):
     sweep_roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                   "peak_kind": peak_kind, "kernel": "BatchSweepKernel", "algorithmic_bytes_per_launch": alg,
                   "ms_per_launch": k_max / args.steps,
-                  "note": "operands are re-read from shared memory and L2; the kernel is bound by its longest chain's serial "
-                          "rounds (SM issue), see profiles/batch_sweep_256chains.md"}
+                  "note": "secondary view: operands are re-read from shared memory and L2, so HBM does not bind this "
+                          "kernel; its bound is the heaviest chain's serial rounds (critical_path)"}
     sm_mhz = clocks.get("sm_mhz") or 2070.0
+    # The sweep launch's binding resource: the heaviest chain's serial scheduling rounds on its SM.
+    d_rounds = (rounds2 - rounds1).astype(np.float64) / args.steps
+    d_att = (att2 - att1).astype(np.float64) / args.steps
+    crit = int(np.argmax(d_rounds))
+    launch_cycles = k_max / args.steps * 1e-3 * sm_mhz * 1e6
+    critical_path = {"bound": "sm-issue: the heaviest chain's scheduling rounds, one SM", "chain": crit,
+                     "shape": list(batch.shapes[crit]), "attempts_per_sweep": float(d_att[crit]), "rounds_per_sweep": float(d_rounds[crit]),
+                     "attempts_per_round": float(d_att[crit] / d_rounds[crit]) if d_rounds[crit] else None,
+                     "cycles_per_round": launch_cycles / d_rounds[crit] if d_rounds[crit] else None,
+                     "mean_attempts_per_round_all_chains": float(d_att.sum() / d_rounds.sum()) if d_rounds.sum() else None,
+                     "note": "cycles_per_round = launch time x median SM clock / the heaviest chain's rounds: the launch ends "
+                             "with that chain; ncu issue and occupancy figures in profiles/batch_sweep_256chains.md"}
     fp32_peak = fp32_peak_tflops(local, sm_mhz)
     flops = hmc_pair_flops(batch.shapes)
     h_achieved = flops / (h_max / args.steps / 1e3) / 1e12
@@ -653,6 +716,7 @@ def run_ours(args):
     hmc = hmc_adjoint(local, tmp) if not args.no_large else None
     exch = exchange_bosons(local, tmp)
     exch["many_chains"] = exchange_bosons_chains(local, tmp)
+    same_shape = same_shape_chains(local, tmp)
     cpu = None
     if not args.no_cpu_baseline:
         moves, el, cyc = cpu_oracle_chains(items, tmp, 12.0, sample)
@@ -679,12 +743,13 @@ def run_ours(args):
         "roofline": dominant,
         "components": {
             "bisection_sweep": {"value": per_sweep / (k_max / args.steps / 1e3), "unit": METRIC, "ms_per_launch": k_max / args.steps,
-                                "roofline": sweep_roof},
+                                "critical_path": critical_path, "roofline": sweep_roof},
             "hmc": {"value": per_hmc / (h_max / args.steps / 1e3), "unit": METRIC, "ms_per_launch": h_max / args.steps,
                     "leapfrog": {"step": HMC[0], "n_steps": HMC[1]}, "roofline": hmc_roof},
         },
         "cpu_baseline": cpu,
         "plain_same_system": plain,
+        "same_shape_chains": same_shape,
         "speedup_vs_plain_same_system": value / plain["value"],
         "energy_gate": gate,
         "plain_electron_gas": eg,

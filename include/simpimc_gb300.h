@@ -236,6 +236,11 @@ int pimc_batch_reset_energy(pimc_batch* b);
 int pimc_batch_last_energy(pimc_batch* b, double* out);
 /* Per-chain attempt and acceptance counters (arrays of n_chains; either may be NULL). */
 int pimc_batch_counters(pimc_batch* b, uint64_t* attempts, uint64_t* accepts);
+/* Scheduling rounds of the bisection sweep kernel per chain (array of n_chains) since creation: a
+ * round runs up to `wave` commuting attempts of the chain at once, so attempts / rounds is the
+ * chain's concurrency and the heaviest chain's rounds set the sweep launch's critical path. No
+ * reference counterpart (a diagnostic of this library's scheduler). */
+int pimc_batch_rounds(pimc_batch* b, uint64_t* rounds);
 /* Hybrid Monte Carlo on the batch ("batched + adjoint"; no reference counterpart): a chain's input
  * may hold one <Move type="HMC" step_size="..." n_steps="..."/> besides its Bisect move. Each
  * attempt draws Gaussian momenta for every bead from the move's stream (keyed by its index in the

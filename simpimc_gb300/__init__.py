@@ -107,6 +107,7 @@ SIGNATURES = {
     "pimc_batch_energy": (C.c_int, [_P, C.c_uint32, _DP, C.c_uint64, _U64P]),
     "pimc_batch_reset_energy": (C.c_int, [_P]),
     "pimc_batch_counters": (C.c_int, [_P, _U64P, _U64P]),
+    "pimc_batch_rounds": (C.c_int, [_P, _U64P]),
     "pimc_batch_hmc_attempts": (C.c_int, [_P, C.c_uint64]),
     "pimc_batch_hmc_counters": (C.c_int, [_P, _U64P, _U64P]),
     "pimc_batch_set_hmc_per_cycle": (C.c_int, [_P, C.c_uint64]),
@@ -497,6 +498,12 @@ class ChainBatch:
         acc = np.zeros(self.n_chains, dtype=np.uint64)
         self._check(self._lib.pimc_batch_counters(self._h, att.ctypes.data_as(_U64P), acc.ctypes.data_as(_U64P)))
         return att, acc
+
+    def rounds(self):
+        """Scheduling rounds of the bisection sweep kernel per chain (attempts / rounds = concurrency)."""
+        r = np.zeros(self.n_chains, dtype=np.uint64)
+        self._check(self._lib.pimc_batch_rounds(self._h, r.ctypes.data_as(_U64P)))
+        return r
 
     def hmc_attempts(self, n: int):
         """n hybrid Monte Carlo attempts on every chain whose input has an HMC move."""

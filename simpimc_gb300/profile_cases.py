@@ -37,14 +37,14 @@ def batch_case(d):
 
 
 def hmc_case(d):
-    """One HMC attempt per chain (leapfrog step 0.005, 10 steps) on clusters of 2 blocks per chain."""
+    """One HMC attempt per chain (leapfrog step 0.005, 10 steps) on clusters of 4 blocks per chain."""
     from . import ChainBatch
     from .configs import batched_trap_chains
     items = batched_trap_chains(d, n_chains=256, seed0=1000, n_level=3, hmc=(0.005, 10))
     b = ChainBatch([x for x, _ in items], base_dir=d)
     b.set_paths(np.concatenate([p.ravel() for _, p in items]))
     b.sweeps(2)
-    b.hmc_cluster = 2
+    b.hmc_cluster = 4
     b.hmc_attempts(1)
     b.hmc_attempts(1)
     b.synchronize()

@@ -97,6 +97,7 @@ class ChainBatch {
     uint64_t ReadEnergy(uint32_t chain, double* out, uint64_t cap);  // series [n][4]
     void ResetEnergy();
     void ReadCounters(uint64_t* attempts, uint64_t* accepts);
+    void ReadRounds(uint64_t* rounds);        // scheduling rounds of the sweep kernel per chain
     void SetTiles(uint32_t items_per_lane, uint32_t max_warps, uint32_t wave);
     double Autotune(uint32_t trial_sweeps);   // returns the best trial's seconds per sweep (also picks hmc_cluster)
     void Sync();
@@ -124,7 +125,7 @@ class ChainBatch {
     void LaunchHmc(uint64_t n_attempts);
     void LaunchMeasure();
     void ResetGraph();
-    std::unique_ptr<DeviceBuffer> pos_, chains_dev_, order_dev_, att_, acc_, series_, n_meas_, err_, last_;
+    std::unique_ptr<DeviceBuffer> pos_, chains_dev_, order_dev_, att_, acc_, series_, n_meas_, err_, last_, rounds_;
     std::unique_ptr<DeviceBuffer> hmc_att_, hmc_acc_;  // HMC counters per chain
     bool HmcClusterFits(uint32_t k) const;
     std::vector<uint64_t> path_off_;  // first double of each chain in the concatenated host layout

@@ -48,6 +48,7 @@ struct BatchArgs {
     uint64_t* n_meas;    // per chain
     double* last;        // [chain][kBatchSeriesComponents]: latest measurement
     int* err;
+    uint64_t* rounds;    // per chain: scheduling rounds of the sweep kernel (one per attempt at wave 1)
     uint32_t series_cap;
 };
 
@@ -519,6 +520,7 @@ __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_
         GroupSync(G);
     }
     if (t == 0) {
+        a.rounds[ci] += att - a.attempts[ci];
         a.attempts[ci] = att;
         a.accepts[ci] = acc;
     }
@@ -634,6 +636,7 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
     uint64_t H = a.attempts[ci];  // the first attempt not yet run
     const uint64_t end = H + (n_sweeps ? n_sweeps * c.attempts_per_sweep : n_attempts);
     uint64_t U = ~0ull;           // bit i: attempt H + i not yet run (bits kWindow.. stay set)
+    uint64_t n_rounds = 0;
     if (threadIdx.x == 0) sh.accepts = 0;
     // Prologue: the first window's draws, attempt H + x by sub-group x mod W.
     if (ws == draw_warp)
@@ -693,6 +696,7 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
             for (uint64_t yd = H + kWindow + sg; yd < H + kWindow + adv && yd < end; yd += W) DrawScored(sh, ring, yd, lane, N, M, B, NL, n_pad, pos);
         }
         SubSync(15, G);
+        ++n_rounds;
         U = adv ? (U_next >> adv) | (~0ull << (64u - adv)) : U_next;
         H += adv;
     }
@@ -704,6 +708,7 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
     if (threadIdx.x == 0) {
         a.attempts[ci] = H;
         a.accepts[ci] += sh.accepts;
+        a.rounds[ci] += n_rounds;
     }
 }
 
@@ -1372,6 +1377,8 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
     n_meas_.reset(new DeviceBuffer(n_chains * sizeof(uint64_t)));
     series_.reset(new DeviceBuffer((size_t)n_chains * series_cap * kBatchSeriesComponents * sizeof(double)));
     err_.reset(new DeviceBuffer(sizeof(int)));
+    rounds_.reset(new DeviceBuffer(n_chains * sizeof(uint64_t)));
+    CudaCheck(cudaMemset(rounds_->ptr, 0, n_chains * sizeof(uint64_t)), "memset");
     if (bead_moves_per_hmc) {
         int optin_h = 0;
         cudaFuncAttributes fh{};
@@ -1556,16 +1563,16 @@ void ChainBatch::LastEnergy(double* out) {
 
 namespace {
 BatchArgs MakeArgs(DeviceBuffer& pos, DeviceBuffer& ch, DeviceBuffer& ord, DeviceBuffer& att, DeviceBuffer& acc, DeviceBuffer& ser,
-                   DeviceBuffer& nm, DeviceBuffer& last, DeviceBuffer& err, uint32_t cap) {
+                   DeviceBuffer& nm, DeviceBuffer& last, DeviceBuffer& err, DeviceBuffer& rounds, uint32_t cap) {
     return BatchArgs{pos.as<float4>(), ch.as<ChainDev>(), ord.as<uint32_t>(), att.as<uint64_t>(), acc.as<uint64_t>(),
-                     ser.as<double>(), nm.as<uint64_t>(), last.as<double>(), err.as<int>(), cap};
+                     ser.as<double>(), nm.as<uint64_t>(), last.as<double>(), err.as<int>(), rounds.as<uint64_t>(), cap};
 }
 }  // namespace
 
 void ChainBatch::LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts) {
     uint32_t warps = 1;
     for (const auto& c : chains) warps = std::max(warps, c.n_warps);
-    const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, series_cap);
+    const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, *rounds_, series_cap);
     BatchSweepKernel<<<n_chains, warps * 32, stage_bytes, stream>>>(a, n_sweeps, n_attempts);
     CudaCheck(cudaGetLastError(), "batch sweep launch");
     ++kernel_launches;
@@ -1616,7 +1623,7 @@ void ChainBatch::SetHmcCluster(uint32_t k) {
 
 void ChainBatch::LaunchHmc(uint64_t n_attempts) {
     if (!bead_moves_per_hmc) throw PimcError(kErrState, "no chain of the batch has an HMC move");
-    const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, series_cap);
+    const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, *rounds_, series_cap);
     cudaLaunchAttribute attr{};
     attr.id = cudaLaunchAttributeClusterDimension;
     attr.val.clusterDim.x = hmc_cluster;
@@ -1655,7 +1662,7 @@ void ChainBatch::SetHmcPerCycle(uint64_t n) {
 }
 
 void ChainBatch::LaunchMeasure() {
-    const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, series_cap);
+    const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, *rounds_, series_cap);
     BatchEnergyPartKernel<<<n_energy_tasks_, kEnergyThreads, energy_smem_, stream>>>(a, energy_tasks_->as<EnergyTask>(), energy_part_->as<float2>());
     CudaCheck(cudaGetLastError(), "batch energy launch");
     BatchEnergyFinishKernel<<<(n_chains + 7) / 8, 256, 0, stream>>>(a, energy_first_->as<uint32_t>(), energy_part_->as<float2>(), n_chains);
@@ -1725,6 +1732,11 @@ void ChainBatch::ResetEnergy() {
     CudaCheck(cudaStreamSynchronize(stream), "sync");
 }
 
+void ChainBatch::ReadRounds(uint64_t* rounds) {
+    Sync();
+    CudaCheck(cudaMemcpy(rounds, rounds_->ptr, n_chains * sizeof(uint64_t), cudaMemcpyDeviceToHost), "read rounds");
+}
+
 void ChainBatch::ReadCounters(uint64_t* attempts, uint64_t* accepts) {
     Sync();
     if (attempts) CudaCheck(cudaMemcpy(attempts, att_->ptr, n_chains * sizeof(uint64_t), cudaMemcpyDeviceToHost), "read attempts");
@@ -1735,13 +1747,14 @@ void ChainBatch::ReadCounters(uint64_t* attempts, uint64_t* accepts) {
 /// state, restores the state after each trial and keeps the fastest tile.
 double ChainBatch::Autotune(uint32_t trial_sweeps) {
     if (trial_sweeps == 0) trial_sweeps = 1;
-    DeviceBuffer pos_save(pos_->bytes), att_save(att_->bytes), acc_save(acc_->bytes);
+    DeviceBuffer pos_save(pos_->bytes), att_save(att_->bytes), acc_save(acc_->bytes), rounds_save(rounds_->bytes);
     auto copy = [&](DeviceBuffer& dst, const DeviceBuffer& src) {
         CudaCheck(cudaMemcpyAsync(dst.ptr, src.ptr, src.bytes, cudaMemcpyDeviceToDevice, stream), "state copy");
     };
     copy(pos_save, *pos_);
     copy(att_save, *att_);
     copy(acc_save, *acc_);
+    copy(rounds_save, *rounds_);
     cudaEvent_t e0, e1;
     CudaCheck(cudaEventCreate(&e0), "event");
     CudaCheck(cudaEventCreate(&e1), "event");
@@ -1771,6 +1784,7 @@ double ChainBatch::Autotune(uint32_t trial_sweeps) {
             copy(*pos_, pos_save);
             copy(*att_, att_save);
             copy(*acc_, acc_save);
+            copy(*rounds_, rounds_save);
         }
     SetTiles(best_ipl, best_mw, best_wave);
     if (bead_moves_per_hmc) {
@@ -1939,6 +1953,13 @@ int pimc_batch_reset_energy(pimc_batch* h) {
 
 int pimc_batch_counters(pimc_batch* h, uint64_t* attempts, uint64_t* accepts) {
     return BatchGuard(h, [&](pimc::ChainBatch& b) { b.ReadCounters(attempts, accepts); });
+}
+
+int pimc_batch_rounds(pimc_batch* h, uint64_t* rounds) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) {
+        if (!rounds) throw pimc::PimcError(pimc::kErrArg, "null output");
+        b.ReadRounds(rounds);
+    });
 }
 
 int pimc_batch_hmc_attempts(pimc_batch* h, uint64_t n) {

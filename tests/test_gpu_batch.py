@@ -193,3 +193,22 @@ def test_uneven_batch_runs(tmp_path, gpu_lib):
     assert np.all(acc > 0)
     b.close()
 
+
+
+def test_rounds_count_the_scheduler(chains):
+    """pimc_batch_rounds: one round per attempt at wave 1; at wave 8 every round runs at least one
+    attempt and the chains with room for concurrent attempts run several per round."""
+    d, items = chains
+    b = make_batch(d, items)
+    b.set_tiles(2, 16, 1)
+    b.attempts(40)
+    r1 = b.rounds()
+    assert np.array_equal(r1, np.full(len(items), 40, dtype=np.uint64))
+    b.set_tiles(2, 16, 8)
+    b.attempts(200)
+    r2 = b.rounds() - r1
+    att, _ = b.counters()
+    assert np.all(att == 240) and np.all(r2 >= 1) and np.all(r2 <= 200)
+    long_chains = [c for c, (n, m, lvl) in enumerate(SHAPES) if m >= 4 * (1 << lvl) and n >= 16]
+    assert long_chains and all(int(r2[c]) < 170 for c in long_chains), [(c, int(r2[c])) for c in long_chains]
+    b.close()
