@@ -3,6 +3,8 @@
     python -m simpimc_gb300.profile_cases batch    # 256 uneven trapped-Coulomb chains: 1 + 1 sweep launches
     python -m simpimc_gb300.profile_cases hmc      # the same chains with the HMC move: 1 + 1 HMC launches
     python -m simpimc_gb300.profile_cases egas     # 66-electron gas: 1 + 1 sweep launches (528 attempts each)
+    python -m simpimc_gb300.profile_cases egas_phases  # the same system: per-attempt phase cycles of the
+                                                       # sweep kernel's block 0 at one and two groups
     python -m simpimc_gb300.profile_cases large32  # 1024-electron gas, FP32 mode: 1 + 1 launches of 64 attempts
     python -m simpimc_gb300.profile_cases bosons   # 32 trapped bosons: Bisect and PermBisectIterative, 1 + 1 sweeps
     python -m simpimc_gb300.profile_cases chains   # 608 such chains: 1 + 1 launches of one sweep each (pimc_sweep_chains)
@@ -63,6 +65,30 @@ def egas_case(d):
     s.sweep([0, 1], [1, 1], reps)
     s.synchronize()
     print(f"egas ok: {s.move_counters(0)[0] + s.move_counters(1)[0]} attempts")
+
+
+def egas_phases_case(d):
+    """Per-attempt cycles of each phase of the sweep kernel's block 0 (pimc_sweep_timing) on the
+    66-electron gas, one sweep at one group (wave 1) and at the automatic group count."""
+    from . import Simulation
+    from .configs import electron_gas
+    xml, path = electron_gas(d, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_units=12.0, n_level=4, seed=20261203)
+    s = Simulation(xml, base_dir=d)
+    s.set_path(path)
+    reps = 33 * math.ceil(128 / 16)
+    for wave in (1, 0):
+        s.set_sweep_wave(wave)
+        s.sweep([0, 1], [1, 1], reps)  # warm-up
+        s.synchronize()
+        s.sweep_timing(1)
+        a0 = s.move_counters(0)[0] + s.move_counters(1)[0]
+        s.sweep([0, 1], [1, 1], reps)
+        s.synchronize()
+        n = s.move_counters(0)[0] + s.move_counters(1)[0] - a0
+        ph = s.sweep_timing(0)
+        print(f"wave {wave or 'auto'}: cycles per attempt of block 0 over {n} attempts")
+        print("  " + ", ".join(f"{k} {v / n:.0f}" for k, v in ph.items() if v))
+    s.close()
 
 
 def large32_case(d):
@@ -138,7 +164,7 @@ def egas_chains_case(d):
 def main(argv):
     case = argv[1] if len(argv) > 1 else "batch"
     with tempfile.TemporaryDirectory() as d:
-        {"batch": batch_case, "hmc": hmc_case, "egas": egas_case, "large32": large32_case, "bosons": bosons_case, "chains": chains_case,
+        {"batch": batch_case, "hmc": hmc_case, "egas": egas_case, "egas_phases": egas_phases_case, "large32": large32_case, "bosons": bosons_case, "chains": chains_case,
          "egas_chains": egas_chains_case}[case](d)
 
 
