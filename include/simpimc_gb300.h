@@ -241,6 +241,14 @@ int pimc_batch_counters(pimc_batch* b, uint64_t* attempts, uint64_t* accepts);
  * chain's concurrency and the heaviest chain's rounds set the sweep launch's critical path. No
  * reference counterpart (a diagnostic of this library's scheduler). */
 int pimc_batch_rounds(pimc_batch* b, uint64_t* rounds);
+/* Split chains: the n most expensive chains whose tile uses 16 warps with a wave and a path staged in
+ * shared memory each run on a cluster of two blocks (four groups of four warps per block, both
+ * blocks holding the path and the same scheduler; a round runs up to eight commuting attempts and
+ * every commit is written into both blocks' copies); the other chains pair up, two per cluster. The
+ * Markov chains are unchanged. pimc_batch_get_split returns how many chains qualified and were
+ * split (0: the plain one-block-per-chain launch); pimc_batch_autotune tries 0, 8, 16 and 32. */
+int pimc_batch_set_split(pimc_batch* b, uint32_t n);
+int pimc_batch_get_split(pimc_batch* b, uint32_t* n);
 /* Hybrid Monte Carlo on the batch ("batched + adjoint"; no reference counterpart): a chain's input
  * may hold one <Move type="HMC" step_size="..." n_steps="..."/> besides its Bisect move. Each
  * attempt draws Gaussian momenta for every bead from the move's stream (keyed by its index in the

@@ -108,6 +108,8 @@ SIGNATURES = {
     "pimc_batch_reset_energy": (C.c_int, [_P]),
     "pimc_batch_counters": (C.c_int, [_P, _U64P, _U64P]),
     "pimc_batch_rounds": (C.c_int, [_P, _U64P]),
+    "pimc_batch_set_split": (C.c_int, [_P, C.c_uint32]),
+    "pimc_batch_get_split": (C.c_int, [_P, _U32P]),
     "pimc_batch_hmc_attempts": (C.c_int, [_P, C.c_uint64]),
     "pimc_batch_hmc_counters": (C.c_int, [_P, _U64P, _U64P]),
     "pimc_batch_set_hmc_per_cycle": (C.c_int, [_P, C.c_uint64]),
@@ -498,6 +500,17 @@ class ChainBatch:
         acc = np.zeros(self.n_chains, dtype=np.uint64)
         self._check(self._lib.pimc_batch_counters(self._h, att.ctypes.data_as(_U64P), acc.ctypes.data_as(_U64P)))
         return att, acc
+
+    @property
+    def split(self) -> int:
+        """Chains running on two-block clusters (the most expensive ones that qualify)."""
+        n = C.c_uint32()
+        self._check(self._lib.pimc_batch_get_split(self._h, C.byref(n)))
+        return n.value
+
+    @split.setter
+    def split(self, n: int):
+        self._check(self._lib.pimc_batch_set_split(self._h, n))
 
     def rounds(self):
         """Scheduling rounds of the bisection sweep kernel per chain (attempts / rounds = concurrency)."""

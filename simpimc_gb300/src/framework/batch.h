@@ -99,12 +99,15 @@ class ChainBatch {
     void ReadCounters(uint64_t* attempts, uint64_t* accepts);
     void ReadRounds(uint64_t* rounds);        // scheduling rounds of the sweep kernel per chain
     void SetTiles(uint32_t items_per_lane, uint32_t max_warps, uint32_t wave);
+    void SetSplit(uint32_t n);                // the n most expensive chains on two blocks each
     double Autotune(uint32_t trial_sweeps);   // returns the best trial's seconds per sweep (also picks hmc_cluster)
     void Sync();
 
     uint32_t n_chains = 0, series_cap = 0;
     int device = 0, n_sm = 0;
     uint32_t items_per_lane = 2, max_warps = 16, wave = 1;  // pair tile and attempts in flight per chain
+    uint32_t split_request = 0;       // chains asked to run on two-block clusters
+    uint32_t n_split_ = 0, n_clusters_ = 0;  // chains split, clusters of the launch (0: plain launch)
     cudaStream_t stream = nullptr;
     std::vector<ChainSpec> specs;
     std::vector<ChainDev> chains;
@@ -122,11 +125,14 @@ class ChainBatch {
    private:
     void Upload();
     void LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts);
+    void ApplySplit();
     void LaunchHmc(uint64_t n_attempts);
     void LaunchMeasure();
     void ResetGraph();
     std::unique_ptr<DeviceBuffer> pos_, chains_dev_, order_dev_, att_, acc_, series_, n_meas_, err_, last_, rounds_;
     std::unique_ptr<DeviceBuffer> hmc_att_, hmc_acc_;  // HMC counters per chain
+    std::unique_ptr<DeviceBuffer> cluster_tasks_;      // uint2 per cluster of the split launch
+    std::vector<uint2> cluster_tasks_host_;
     bool HmcClusterFits(uint32_t k) const;
     std::vector<uint64_t> path_off_;  // first double of each chain in the concatenated host layout
     std::unique_ptr<DeviceBuffer> dstage_, path_off_dev_;  // host-layout doubles on the device, offsets

@@ -49,6 +49,8 @@ struct BatchArgs {
     double* last;        // [chain][kBatchSeriesComponents]: latest measurement
     int* err;
     uint64_t* rounds;    // per chain: scheduling rounds of the sweep kernel (one per attempt at wave 1)
+    const uint2* cluster_tasks;  // sweep launched as clusters of two blocks: the chains of cluster j's
+                                 // blocks (x == y: one chain split over both); null: block -> order[]
     uint32_t series_cap;
 };
 
@@ -180,15 +182,24 @@ __device__ __forceinline__ uint2 DrawAttempt(const MoveStream& st, uint32_t lane
         pb[0] = p;
         pb[1] = b0;
     }
-    for (uint32_t j = lane; j < (B - 1) + NL; j += 32) {
-        if (j < B - 1) {
-            float zz[3];
-            BisectNormals(st, j, zz);
-            z[3 * j] = zz[0];
-            z[3 * j + 1] = zz[1];
-            z[3 * j + 2] = zz[2];
+    // Two lanes per resampled bead (BisectNormals' two Box-Muller transforms of its Philox block:
+    // z0, z1 from words 0-1 on the even lane, z2 from words 2-3 on the odd one), one per level's
+    // log-uniform: the draw's latency is one transform's.
+    for (uint32_t j = lane; j < 2 * (B - 1) + NL; j += 32) {
+        if (j < 2 * (B - 1)) {
+            const uint32_t i = j >> 1;
+            const Philox4 w = st.Block(1u + i);
+            float z0, z1;
+            if ((j & 1u) == 0) {
+                BoxMullerF(w.v[0], w.v[1], z0, z1);
+                z[3 * i] = z0;
+                z[3 * i + 1] = z1;
+            } else {
+                BoxMullerF(w.v[2], w.v[3], z0, z1);
+                z[3 * i + 2] = z0;
+            }
         } else {
-            const uint32_t li = j - (B - 1);  // 0 = top level
+            const uint32_t li = j - 2 * (B - 1);  // 0 = top level
             logu[NL - 1 - li] = BisectLogU(st, B, li);
         }
     }
@@ -205,7 +216,7 @@ __device__ __forceinline__ uint2 DrawAttempt(const MoveStream& st, uint32_t lane
 template <bool kPbc, uint32_t NL>
 __device__ __forceinline__ void LeaderPhaseL(const ChainDev& c, uint32_t lane, uint32_t M, float ox, float oy, float oz, float ex, float ey,
                                              float ez, const float* zb, const float* logu, float2* s_on, dd* base0_out,
-                                             int* upper_out, float& nx, float& ny, float& nz) {
+                                             int* upper_out, float& nx, float& ny, float& nz, bool& upper_reg, dd& base0_reg) {
     constexpr uint32_t B = 1u << NL;
     const float L = c.L, iL = c.iL;
     const bool kin_links = B != M;  // whole-ring segment: no kinetic links (kinetic_class.h:111-117)
@@ -327,6 +338,10 @@ __device__ __forceinline__ void LeaderPhaseL(const ChainDev& c, uint32_t lane, u
     if (!isfinite(la.hi)) la.hi = -INFINITY;
     const bool fail = lane >= 1 && lane < NL && Less(la, DD(logu[lane]));
     const unsigned fails = __ballot_sync(0xffffffffu, fail);
+    // The leader warp keeps both results in registers (lane 0's base0 is level 0's); the shared
+    // copies serve the group's other warps.
+    upper_reg = fails == 0u;
+    base0_reg = la;
     if (lane == 0) {
         *upper_out = fails == 0u;
         *base0_out = la;
@@ -336,13 +351,13 @@ __device__ __forceinline__ void LeaderPhaseL(const ChainDev& c, uint32_t lane, u
 template <bool kPbc>
 __device__ __forceinline__ void LeaderPhase(const ChainDev& c, uint32_t lane, uint32_t NL, uint32_t M, float ox, float oy, float oz, float ex,
                                             float ey, float ez, const float* zb, const float* logu, float2* s_on, dd* base0_out,
-                                            int* upper_out, float& nx, float& ny, float& nz) {
+                                            int* upper_out, float& nx, float& ny, float& nz, bool& upper_reg, dd& base0_reg) {
     switch (NL) {
-        case 1: LeaderPhaseL<kPbc, 1>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_on, base0_out, upper_out, nx, ny, nz); break;
-        case 2: LeaderPhaseL<kPbc, 2>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_on, base0_out, upper_out, nx, ny, nz); break;
-        case 3: LeaderPhaseL<kPbc, 3>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_on, base0_out, upper_out, nx, ny, nz); break;
-        case 4: LeaderPhaseL<kPbc, 4>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_on, base0_out, upper_out, nx, ny, nz); break;
-        default: LeaderPhaseL<kPbc, 5>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_on, base0_out, upper_out, nx, ny, nz); break;
+        case 1: LeaderPhaseL<kPbc, 1>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_on, base0_out, upper_out, nx, ny, nz, upper_reg, base0_reg); break;
+        case 2: LeaderPhaseL<kPbc, 2>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_on, base0_out, upper_out, nx, ny, nz, upper_reg, base0_reg); break;
+        case 3: LeaderPhaseL<kPbc, 3>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_on, base0_out, upper_out, nx, ny, nz, upper_reg, base0_reg); break;
+        case 4: LeaderPhaseL<kPbc, 4>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_on, base0_out, upper_out, nx, ny, nz, upper_reg, base0_reg); break;
+        default: LeaderPhaseL<kPbc, 5>(c, lane, M, ox, oy, oz, ex, ey, ez, zb, logu, s_on, base0_out, upper_out, nx, ny, nz, upper_reg, base0_reg); break;
     }
 }
 
@@ -353,7 +368,7 @@ __device__ __forceinline__ void LeaderPhase(const ChainDev& c, uint32_t lane, ui
 template <bool kPbc, bool kStaged>
 __device__ __forceinline__ Comp PairPhase(const ChainDev& c, uint32_t t, uint32_t T, uint32_t n_items, uint32_t magic, uint32_t nm1, uint32_t p,
                                           uint32_t b0, uint32_t M, const PathView<kStaged>& path, const uint32_t* it_k, const float3* pre,
-                                          const float2* s_on) {
+                                          const float2* s_on, uint32_t partner_major_nk) {
     const float L = c.L, iL = c.iL, r2_min = c.r2_min, r2_max = c.r2_max;
     Comp acc_u{0.f, 0.f};
     auto item = [&](uint32_t k, float3 rq) {
@@ -365,8 +380,8 @@ __device__ __forceinline__ Comp PairPhase(const ChainDev& c, uint32_t t, uint32_
         CompAdd(acc_u, __fsub_rn(rsqrtf(r2n), rsqrtf(r2o)));
     };
     if constexpr (kStaged) {  // beads in shared memory: no prefetch, loads batched by the unrolled loop
-        const uint32_t nk = n_items / nm1;  // inner slices
-        if ((nm1 + T - 1) / T * nk * 4u <= (n_items + T - 1) / T * 5u) {
+        const uint32_t nk = partner_major_nk;  // inner slices (0: items flattened)
+        if (nk) {
             // lane = partner particle, inner slices in a loop: no index division per item
             for (uint32_t qi = t; qi < nm1; qi += T) {
                 const uint32_t q = qi + (qi >= p ? 1u : 0u);
@@ -455,6 +470,8 @@ __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_
     GroupSync(G);
 
     float nx = 0.f, ny = 0.f, nz = 0.f;  // warp 0, lane k: new position of bead k of the last attempt
+    bool lead_upper = false;             // warp 0: the upper levels passed (and lane 0's level-0 base)
+    dd lead_base0 = DD(0.f);
     uint32_t p_prev = 0xffffffffu, b0_prev = 0;
     bool acc_prev = false;
     for (uint64_t it = 0; it < n_att; ++it, ++att) {
@@ -495,22 +512,22 @@ __device__ __forceinline__ void SweepChain(SweepShared& sh, BatchArgs a, uint32_
                 }
             }
             LeaderPhase<kPbc>(c, lane, NL, M, ox, oy, oz, ex, ey, ez, sh.z[buf], sh.logu[buf], sh.on_, &sh.base0, &sh.upper_ok,
-                              nx, ny, nz);
+                              nx, ny, nz, lead_upper, lead_base0);
         } else if (ahead && warp == 1 && it + 1 < n_att) {
             DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, att + 1}, lane, N, M, B, NL, n_pad, pos, sh.z[buf ^ 1u], sh.logu[buf ^ 1u],
                         sh.seg[buf ^ 1u], sh.pb[buf ^ 1u]);
         }
         GroupSync(G);
-        const bool upper_ok = sh.upper_ok != 0;
+        const bool upper_ok = warp == 0 ? lead_upper : sh.upper_ok != 0;
 
         if (upper_ok && n_items) {
-            const Comp u = CompWarpSum(PairPhase<kPbc, false>(c, t, T, n_items, magic, nm1, p, b0, M, gpath, it_k, pre, sh.on_), 32);
+            const Comp u = CompWarpSum(PairPhase<kPbc, false>(c, t, T, n_items, magic, nm1, p, b0, M, gpath, it_k, pre, sh.on_, 0u), 32);
             if (lane == 0) sh.part[warp] = u;
         }
         GroupSync(G);
 
         if (warp == 0) {
-            const bool accepted = upper_ok && Level0Accepts(c, lane, G, sh.part, n_items != 0, sh.base0, sh.logu[buf][0]);
+            const bool accepted = upper_ok && Level0Accepts(c, lane, G, sh.part, n_items != 0, lead_base0, sh.logu[buf][0]);
             if (accepted && lane >= 1 && lane < B) pos[(size_t)Wrap(b0 + lane, M) * n_pad + p] = make_float4(nx, ny, nz, 0.f);
             acc += accepted ? 1u : 0u;
             acc_prev = accepted;
@@ -583,14 +600,15 @@ __device__ __forceinline__ void DrawScored(WaveShared& sh, const WaveRing& ring,
                                            uint32_t NL, uint32_t n_pad, const float4* __restrict__ pos) {
     const ChainDev& c = sh.c;
     const uint32_t sl = (uint32_t)y & (kRing - 1u);
-    const uint2 pb = DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, y}, lane, N, M, B, NL, n_pad, pos, ring.Z(sl), ring.LU(sl), nullptr, sh.pb[sl]);
+    const Philox4 w0 = MoveStream{c.seed, c.chain_id, c.move, y}.Block(0);
     bool hit = false;
     if (lane >= 1 && lane < kWindow && y >= lane) {
         const Philox4 w = MoveStream{c.seed, c.chain_id, c.move, y - lane}.Block(0);
-        hit = Interact(UniformIndex(w.v[0], N), UniformIndex(w.v[1], M), pb.x, pb.y, B, M);
+        hit = Interact(UniformIndex(w.v[0], N), UniformIndex(w.v[1], M), UniformIndex(w0.v[0], N), UniformIndex(w0.v[1], M), B, M);
     }
     const unsigned m = __ballot_sync(0xffffffffu, hit);
     if (lane == 0) sh.dep[sl] = m;
+    DrawAttempt(MoveStream{c.seed, c.chain_id, c.move, y}, lane, N, M, B, NL, n_pad, pos, ring.Z(sl), ring.LU(sl), nullptr, sh.pb[sl]);
 }
 
 __device__ __forceinline__ void SubSync(uint32_t id, uint32_t n_warps) {
@@ -598,8 +616,20 @@ __device__ __forceinline__ void SubSync(uint32_t id, uint32_t n_warps) {
     else asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n_warps * 32u) : "memory");
 }
 
-template <bool kPbc, bool kStaged>
-__device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchArgs a, uint32_t ci, uint64_t n_sweeps, uint64_t n_attempts) {
+/// Barrier over the two blocks of a cluster (release/acquire: each block's shared-memory writes,
+/// local and remote, are visible to both after it).
+__device__ __forceinline__ void ClusterPairSync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+/// kSplit: the chain runs on both blocks of a two-block cluster (crank = this block's rank). Both
+/// hold the staged path and the same scoreboard; a round takes the first 2W eligible attempts and
+/// block r runs those of rank r, r + 2, ...; an accepted attempt writes its beads into both blocks'
+/// planes, and a cluster barrier closes each round.
+template <bool kPbc, bool kStaged, bool kSplit>
+__device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchArgs a, uint32_t ci, uint64_t n_sweeps, uint64_t n_attempts,
+                                            uint32_t crank) {
+    static_assert(!kSplit || kStaged, "a split chain is staged in both blocks");
     const ChainDev& c = sh.c;
     const uint32_t W = c.n_wave, Gs = c.sub_warps, G = W * Gs;
     constexpr uint32_t kMask = kRing - 1;
@@ -621,6 +651,9 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
         }
     float* const ring_base = stage + (kStaged ? 3 * N * M : 0u);
     const WaveRing ring{ring_base, ring_base + kRing * 3 * (B - 1), 3 * (B - 1), NL};
+    float* peer_stage = stage;  // the other block's planes at the same offset (distributed shared memory)
+    if constexpr (kSplit) peer_stage = cooperative_groups::this_cluster().map_shared_rank(stage, crank ^ 1u);
+    const PathView<kStaged> peer{pos, peer_stage, n_pad, N, N * M};
 
     const uint32_t nm1 = N > 1 ? N - 1 : 1;
     const uint32_t n_items = c.has_pair && N > 1 ? (N - 1) * (B - 1) : 0u;
@@ -632,6 +665,9 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
         it_k[j] = FastDivD(i, nm1, magic);
         it_q[j] = i - it_k[j] * nm1;
     }
+    // Staged paths with enough partners for the group's lanes: partner-major pair loop, whose
+    // per-lane item count (ceil(nm1 / Ts) (B - 1)) is within 5/4 of the flattened loop's.
+    const uint32_t pmk = (kStaged && n_items && (nm1 + Ts - 1) / Ts * (B - 1) * 4u <= (n_items + Ts - 1) / Ts * 5u) ? B - 1 : 0u;
 
     uint64_t H = a.attempts[ci];  // the first attempt not yet run
     const uint64_t end = H + (n_sweeps ? n_sweeps * c.attempts_per_sweep : n_attempts);
@@ -641,7 +677,9 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
     // Prologue: the first window's draws, attempt H + x by sub-group x mod W.
     if (ws == draw_warp)
         for (uint64_t y = H + sg; y < end && y < H + kWindow; y += W) DrawScored(sh, ring, y, lane, N, M, B, NL, n_pad, pos);
-    SubSync(15, G);
+    if constexpr (kSplit) ClusterPairSync();  // both blocks staged before either commits into the other
+    else SubSync(15, G);
+    constexpr uint32_t kWays = kSplit ? 2u : 1u;  // blocks sharing the chain's rounds
 
     while (H < end) {
         // The round's attempts: the first W of the window that commute with every earlier attempt
@@ -653,8 +691,8 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
         }
         const unsigned elig = __ballot_sync(0xffffffffu, ok);
         const uint32_t rank = __popc(elig & ((1u << lane) - 1u));  // eligible attempts before this lane's
-        const unsigned sel = __ballot_sync(0xffffffffu, ok && rank < W);
-        const unsigned mine = __ballot_sync(0xffffffffu, ok && rank == sg);
+        const unsigned sel = __ballot_sync(0xffffffffu, ok && rank < kWays * W);
+        const unsigned mine = __ballot_sync(0xffffffffu, ok && rank == kWays * sg + crank);
         const uint64_t U_next = U & ~(uint64_t)sel;
         const uint32_t adv = (uint32_t)__ffsll((long long)U_next) - 1u;  // attempts at the head that are now run (<= kWindow)
         if (mine) {
@@ -669,11 +707,13 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
                     if (ts + j * Ts < n_items) pre[j] = path.Load(Wrap(b0 + 1u + it_k[j], M), it_q[j] + (it_q[j] >= p ? 1u : 0u));
             }
             float nx = 0.f, ny = 0.f, nz = 0.f;
+            bool lead_upper = false;
+            dd lead_base0 = DD(0.f);
             if (ws == 0) {
                 const float3 sv = path.Load(Wrap(b0 + (lane <= B ? lane : B), M), p);
                 const float3 se = path.Load(Wrap(b0 + B, M), p);
                 LeaderPhase<kPbc>(c, lane, NL, M, sv.x, sv.y, sv.z, se.x, se.y, se.z, ring.Z(slot), ring.LU(slot), sh.on_[sg],
-                                  &sh.base0[sg], &sh.upper_ok[sg], nx, ny, nz);
+                                  &sh.base0[sg], &sh.upper_ok[sg], nx, ny, nz, lead_upper, lead_base0);
             }
             // Draws that refill the window behind the head's advance (their slots are not in use).
             if (ws == draw_warp) {
@@ -681,34 +721,45 @@ __device__ __forceinline__ void SweepChainW(WaveShared& sh, float* stage, BatchA
                 for (uint64_t yd = H + kWindow + sg; yd < H + kWindow + adv && yd < end; yd += W) DrawScored(sh, ring, yd, lane, N, M, B, NL, n_pad, pos);
             }
             SubSync(1 + sg, Gs);
-            const bool upper_ok = sh.upper_ok[sg] != 0;
+            const bool upper_ok = ws == 0 ? lead_upper : sh.upper_ok[sg] != 0;
             if (upper_ok && n_items) {
-                const Comp u = CompWarpSum(PairPhase<kPbc, kStaged>(c, ts, Ts, n_items, magic, nm1, p, b0, M, path, it_k, pre, sh.on_[sg]), 32);
+                const Comp u = CompWarpSum(PairPhase<kPbc, kStaged>(c, ts, Ts, n_items, magic, nm1, p, b0, M, path, it_k, pre, sh.on_[sg], pmk), 32);
                 if (lane == 0) sh.part[sg][ws] = u;
             }
             SubSync(1 + sg, Gs);
             if (ws == 0) {
-                const bool accepted = upper_ok && Level0Accepts(c, lane, Gs, sh.part[sg], n_items != 0, sh.base0[sg], ring.LU(slot)[0]);
-                if (accepted && lane >= 1 && lane < B) path.Store(Wrap(b0 + lane, M), p, nx, ny, nz);
+                const bool accepted = upper_ok && Level0Accepts(c, lane, Gs, sh.part[sg], n_items != 0, lead_base0, ring.LU(slot)[0]);
+                if (accepted && lane >= 1 && lane < B) {
+                    path.Store(Wrap(b0 + lane, M), p, nx, ny, nz);
+                    if constexpr (kSplit) peer.Store(Wrap(b0 + lane, M), p, nx, ny, nz);
+                }
                 if (accepted && lane == 0) atomicAdd(&sh.accepts, 1u);
             }
         } else if (ws == draw_warp) {
             for (uint64_t yd = H + kWindow + sg; yd < H + kWindow + adv && yd < end; yd += W) DrawScored(sh, ring, yd, lane, N, M, B, NL, n_pad, pos);
         }
-        SubSync(15, G);
+        if constexpr (kSplit) ClusterPairSync();  // both blocks' commits, local and remote, before the next round
+        else SubSync(15, G);
         ++n_rounds;
         U = adv ? (U_next >> adv) | (~0ull << (64u - adv)) : U_next;
         H += adv;
     }
-    if constexpr (kStaged)  // every round ended with a block barrier: all commits are visible
-        for (uint32_t i = threadIdx.x; i < N * M; i += G * 32u) {
-            const uint32_t b = i / N, q = i - b * N;
-            pos[(size_t)b * n_pad + q] = make_float4(stage[i], stage[N * M + i], stage[2 * N * M + i], 0.f);
-        }
+    if constexpr (kStaged)  // every round ended with a block (cluster) barrier: all commits are visible
+        if (crank == 0)     // a split chain's two copies are identical
+            for (uint32_t i = threadIdx.x; i < N * M; i += G * 32u) {
+                const uint32_t b = i / N, q = i - b * N;
+                pos[(size_t)b * n_pad + q] = make_float4(stage[i], stage[N * M + i], stage[2 * N * M + i], 0.f);
+            }
     if (threadIdx.x == 0) {
-        a.attempts[ci] = H;
-        a.accepts[ci] += sh.accepts;
-        a.rounds[ci] += n_rounds;
+        if (kSplit) {
+            atomicAdd(reinterpret_cast<unsigned long long*>(&a.accepts[ci]), (unsigned long long)sh.accepts);
+        } else {
+            a.accepts[ci] += sh.accepts;
+        }
+        if (crank == 0) {
+            a.attempts[ci] = H;
+            a.rounds[ci] += n_rounds;
+        }
     }
 }
 
@@ -718,10 +769,20 @@ union BatchShared {
 };
 
 __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArgs a, uint64_t n_sweeps, uint64_t n_attempts) {
-    const uint32_t ci = a.order[blockIdx.x];
+    uint32_t ci, crank = 0;
+    bool split = false;
+    if (a.cluster_tasks) {  // clusters of two blocks: cluster j runs tasks[j]
+        const uint2 task = a.cluster_tasks[blockIdx.x >> 1];
+        crank = blockIdx.x & 1u;  // the block's rank in its cluster
+        split = task.x == task.y;
+        ci = crank ? task.y : task.x;
+        if (ci == 0xffffffffu) return;  // the last cluster's second block when the chain count is odd
+    } else {
+        ci = a.order[blockIdx.x];
+    }
     const uint32_t warp = threadIdx.x >> 5;
     const uint32_t G = a.chains[ci].n_warps;
-    if (warp >= G) return;
+    if (warp >= G) return;  // a split chain uses every warp of the block (no early exit before its cluster barriers)
     __shared__ BatchShared sh;
     extern __shared__ float4 batch_stage[];  // staged path planes (chains with `staged` set)
     {
@@ -732,12 +793,15 @@ __global__ void __launch_bounds__(kBatchMaxWarps * 32) BatchSweepKernel(BatchArg
     GroupSync(G);
     if (sh.one.c.n_wave > 1) {
         float* stage = reinterpret_cast<float*>(batch_stage);
-        if (sh.one.c.staged) {
-            if (sh.one.c.pbc) SweepChainW<true, true>(sh.wave, stage, a, ci, n_sweeps, n_attempts);
-            else SweepChainW<false, true>(sh.wave, stage, a, ci, n_sweeps, n_attempts);
+        if (split) {  // the host splits only staged chains with a wave
+            if (sh.one.c.pbc) SweepChainW<true, true, true>(sh.wave, stage, a, ci, n_sweeps, n_attempts, crank);
+            else SweepChainW<false, true, true>(sh.wave, stage, a, ci, n_sweeps, n_attempts, crank);
+        } else if (sh.one.c.staged) {
+            if (sh.one.c.pbc) SweepChainW<true, true, false>(sh.wave, stage, a, ci, n_sweeps, n_attempts, 0);
+            else SweepChainW<false, true, false>(sh.wave, stage, a, ci, n_sweeps, n_attempts, 0);
         } else {
-            if (sh.one.c.pbc) SweepChainW<true, false>(sh.wave, stage, a, ci, n_sweeps, n_attempts);
-            else SweepChainW<false, false>(sh.wave, stage, a, ci, n_sweeps, n_attempts);
+            if (sh.one.c.pbc) SweepChainW<true, false, false>(sh.wave, stage, a, ci, n_sweeps, n_attempts, 0);
+            else SweepChainW<false, false, false>(sh.wave, stage, a, ci, n_sweeps, n_attempts, 0);
         }
     } else {
         if (sh.one.c.pbc) SweepChain<true>(sh.one, a, ci, G, n_sweeps, n_attempts);
@@ -1487,6 +1551,7 @@ void ChainBatch::SetTiles(uint32_t ipl, uint32_t mw, uint32_t wave) {
         const double wy = (double)chains[y].attempts_per_sweep * chains[y].n_part;
         return wx > wy;
     });
+    ApplySplit();
     Upload();
     ResetGraph();
 }
@@ -1565,17 +1630,88 @@ namespace {
 BatchArgs MakeArgs(DeviceBuffer& pos, DeviceBuffer& ch, DeviceBuffer& ord, DeviceBuffer& att, DeviceBuffer& acc, DeviceBuffer& ser,
                    DeviceBuffer& nm, DeviceBuffer& last, DeviceBuffer& err, DeviceBuffer& rounds, uint32_t cap) {
     return BatchArgs{pos.as<float4>(), ch.as<ChainDev>(), ord.as<uint32_t>(), att.as<uint64_t>(), acc.as<uint64_t>(),
-                     ser.as<double>(), nm.as<uint64_t>(), last.as<double>(), err.as<int>(), rounds.as<uint64_t>(), cap};
+                     ser.as<double>(), nm.as<uint64_t>(), last.as<double>(), err.as<int>(), rounds.as<uint64_t>(), nullptr, cap};
 }
 }  // namespace
 
 void ChainBatch::LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts) {
     uint32_t warps = 1;
     for (const auto& c : chains) warps = std::max(warps, c.n_warps);
-    const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, *rounds_, series_cap);
-    BatchSweepKernel<<<n_chains, warps * 32, stage_bytes, stream>>>(a, n_sweeps, n_attempts);
-    CudaCheck(cudaGetLastError(), "batch sweep launch");
+    BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, *rounds_, series_cap);
+    if (n_split_ > 0) {
+        // Clusters of two blocks: a split chain on both, otherwise two chains side by side.
+        a.cluster_tasks = cluster_tasks_->as<uint2>();
+        cudaLaunchAttribute attr{};
+        attr.id = cudaLaunchAttributeClusterDimension;
+        attr.val.clusterDim.x = 2;
+        attr.val.clusterDim.y = 1;
+        attr.val.clusterDim.z = 1;
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(2 * n_clusters_);
+        cfg.blockDim = dim3(warps * 32);
+        cfg.dynamicSmemBytes = stage_bytes;
+        cfg.stream = stream;
+        cfg.attrs = &attr;
+        cfg.numAttrs = 1;
+        CudaCheck(cudaLaunchKernelEx(&cfg, BatchSweepKernel, a, n_sweeps, n_attempts), "batch sweep launch");
+    } else {
+        BatchSweepKernel<<<n_chains, warps * 32, stage_bytes, stream>>>(a, n_sweeps, n_attempts);
+        CudaCheck(cudaGetLastError(), "batch sweep launch");
+    }
     ++kernel_launches;
+}
+
+/// The `split` most expensive chains that qualify (a wave tile of 16 warps and a staged path) run on
+/// two blocks each with four groups of four warps per block; the others pair up, two chains per
+/// cluster, in descending order of work. Called after every tile change.
+void ChainBatch::ApplySplit() {
+    n_split_ = 0;
+    cluster_tasks_host_.clear();
+    if (split_request == 0) return;
+    std::vector<char> is_split(n_chains, 0);
+    for (uint32_t i = 0; i < n_chains && n_split_ < split_request; ++i) {
+        ChainDev& c = chains[order[i]];
+        if (c.n_wave <= 1 || !c.staged || c.n_warps != kBatchMaxWarps) continue;
+        c.n_wave = 4;
+        c.sub_warps = 4;
+        c.n_warps = 16;
+        is_split[order[i]] = 1;
+        cluster_tasks_host_.push_back(make_uint2(order[i], order[i]));
+        ++n_split_;
+    }
+    if (n_split_ == 0) return;
+    std::vector<uint32_t> rest;
+    for (uint32_t i = 0; i < n_chains; ++i)
+        if (!is_split[order[i]]) rest.push_back(order[i]);
+    for (size_t i = 0; i < rest.size(); i += 2)
+        cluster_tasks_host_.push_back(make_uint2(rest[i], i + 1 < rest.size() ? rest[i + 1] : 0xffffffffu));
+    n_clusters_ = (uint32_t)cluster_tasks_host_.size();
+    if (!cluster_tasks_ || cluster_tasks_->bytes < n_clusters_ * sizeof(uint2)) cluster_tasks_.reset(new DeviceBuffer(n_chains * sizeof(uint2)));
+    CudaCheck(cudaMemcpyAsync(cluster_tasks_->ptr, cluster_tasks_host_.data(), n_clusters_ * sizeof(uint2), cudaMemcpyHostToDevice, stream),
+              "upload cluster tasks");
+    // Every cluster must be schedulable with the launch's shared memory.
+    cudaLaunchAttribute attr{};
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = 2;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(2 * n_clusters_);
+    cfg.blockDim = dim3(kBatchMaxWarps * 32);
+    cfg.dynamicSmemBytes = stage_bytes;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, BatchSweepKernel, &cfg) != cudaSuccess || clusters < 1) {
+        cudaGetLastError();
+        throw PimcError(kErrUnsupported, "two-block clusters of the batch sweep do not fit this device");
+    }
+}
+
+void ChainBatch::SetSplit(uint32_t n) {
+    if (n > n_chains) throw PimcError(kErrArg, "more split chains than chains");
+    split_request = n;
+    SetTiles(items_per_lane, max_warps, wave);
 }
 
 size_t ChainBatch::HmcSmem(uint32_t k) const {
@@ -1787,6 +1923,34 @@ double ChainBatch::Autotune(uint32_t trial_sweeps) {
             copy(*rounds_, rounds_save);
         }
     SetTiles(best_ipl, best_mw, best_wave);
+    {
+        // chains split over two-block clusters: none, or the 8, 16, 32 most expensive
+        double best_s = best;
+        uint32_t best_n = split_request;
+        for (uint32_t n : {0u, 8u, 16u, 32u}) {
+            if (n > n_chains) continue;
+            SetSplit(n);
+            if (n > 0 && n_split_ == 0) continue;
+            LaunchSweep(1, 0);  // warm-up of this shape
+            CudaCheck(cudaEventRecord(e0, stream), "event");
+            LaunchSweep(trial_sweeps, 0);
+            CudaCheck(cudaEventRecord(e1, stream), "event");
+            CudaCheck(cudaEventSynchronize(e1), "event sync");
+            float ms = 0.f;
+            CudaCheck(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+            const double sec = ms * 1e-3 / trial_sweeps;
+            if (n == 0 || sec < best_s) {
+                best_s = sec;
+                best_n = n;
+            }
+            copy(*pos_, pos_save);
+            copy(*att_, att_save);
+            copy(*acc_, acc_save);
+            copy(*rounds_, rounds_save);
+        }
+        SetSplit(best_n);
+        best = best_s;
+    }
     if (bead_moves_per_hmc) {
         // blocks per chain of the HMC launch: one attempt per trial, the state put back after each
         DeviceBuffer hatt_save(hmc_att_->bytes), hacc_save(hmc_acc_->bytes);
@@ -1953,6 +2117,17 @@ int pimc_batch_reset_energy(pimc_batch* h) {
 
 int pimc_batch_counters(pimc_batch* h, uint64_t* attempts, uint64_t* accepts) {
     return BatchGuard(h, [&](pimc::ChainBatch& b) { b.ReadCounters(attempts, accepts); });
+}
+
+int pimc_batch_set_split(pimc_batch* h, uint32_t n) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) { b.SetSplit(n); });
+}
+
+int pimc_batch_get_split(pimc_batch* h, uint32_t* n) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) {
+        if (!n) throw pimc::PimcError(pimc::kErrArg, "null output");
+        *n = b.n_split_;
+    });
 }
 
 int pimc_batch_rounds(pimc_batch* h, uint64_t* rounds) {

@@ -212,3 +212,28 @@ def test_rounds_count_the_scheduler(chains):
     long_chains = [c for c, (n, m, lvl) in enumerate(SHAPES) if m >= 4 * (1 << lvl) and n >= 16]
     assert long_chains and all(int(r2[c]) < 170 for c in long_chains), [(c, int(r2[c])) for c in long_chains]
     b.close()
+
+
+@pytest.mark.parametrize("n_split", [1, 4, 9])
+def test_split_chains_match_one_block_per_chain(chains, n_split):
+    """The most expensive chains on two-block clusters (both blocks hold the path; a round runs up
+    to eight commuting attempts, commits written into both copies) make the same moves as the
+    one-block launch: identical accept counts and paths, bit for bit; odd and even chain counts."""
+    d, items = chains
+    ref = make_batch(d, items)
+    ref.set_tiles(2, 16, 8)
+    ref.attempts(150)
+    ref.sweeps(2)
+    b = make_batch(d, items)
+    b.set_tiles(2, 16, 8)
+    b.split = n_split
+    assert b.split == n_split
+    b.attempts(150)
+    b.sweeps(2)
+    a0, c0 = ref.counters()
+    a1, c1 = b.counters()
+    assert np.array_equal(a0, a1) and np.array_equal(c0, c1)
+    for c in range(len(items)):
+        assert np.array_equal(ref.get_path(c), b.get_path(c)), c
+    ref.close()
+    b.close()
