@@ -621,7 +621,21 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                         seg_new[i] = v;
                     }
                 } else if (warp < 4) {
-                    for (uint32_t i = tid - 64; i < B - 1; i += 64) BisectNormals(st, i, &zs[3 * i]);
+                    // two lanes per resampled bead: BisectNormals' two Box-Muller transforms of its
+                    // Philox block (z0, z1 from words 0-1 on the even lane, z2 from words 2-3)
+                    for (uint32_t j = tid - 64; j < 2 * (B - 1); j += 64) {
+                        const uint32_t i = j >> 1;
+                        const Philox4 w = st.Block(1u + i);
+                        float z0, z1;
+                        if ((j & 1u) == 0) {
+                            BoxMullerF(w.v[0], w.v[1], z0, z1);
+                            zs[3 * i] = z0;
+                            zs[3 * i + 1] = z1;
+                        } else {
+                            BoxMullerF(w.v[2], w.v[3], z0, z1);
+                            zs[3 * i + 2] = z0;
+                        }
+                    }
                 } else if (warp == 4) {
                     if (lane < (int)nl) logu[lane] = BisectLogU(st, B, (uint32_t)lane);
                 } else if (warp == 5) {
@@ -1668,11 +1682,11 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
 
     // Concurrent attempts need every scheduled move to have a grid phase (a non-constant pair
     // action) and segments of at most half the ring; otherwise one attempt at a time. Automatic:
-    // two groups when an attempt's density work is small (66-electron gas, 16 slices x 3.6k
-    // k-vectors: 1.35x faster per sweep), one when it fills the grid (1024 electrons, 16 x 25k:
-    // two and four groups were slower).
+    // three groups when an attempt's density work is small (66-electron gas, 16 slices x 3.6k
+    // k-vectors: 9.1 us per attempt against 9.7 with two groups and 11.2 with one), one when it
+    // fills the grid (1024 electrons, 16 x 25k: two and four groups were slower).
     uint32_t wave = sweep_wave > 0 ? (uint32_t)std::min(sweep_wave, (int)kWaveSlots)
-                                   : ((uint64_t(1) << max_level) * sys.K <= (uint64_t(1) << 17) ? 2u : 1u);
+                                   : ((uint64_t(1) << max_level) * sys.K <= (uint64_t(1) << 17) ? 3u : 1u);
     for (uint32_t e = 0; e < n_entries; ++e) {
         const MoveDev& d = moves[mv[e]].dev;
         bool gw = false;
