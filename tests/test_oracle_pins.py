@@ -19,6 +19,7 @@ import numpy as np
 import pytest
 
 import oracle
+from exact_energies import blocked_error, exact_sho_energy
 from simpimc_gb300.configs import electron_gas, trapped_coulomb
 from simpimc_gb300.tables import coulomb_table, lattice_k_magnitudes
 
@@ -56,27 +57,6 @@ def test_normals_statistics():
     zs = np.concatenate([oracle.bisect_draws(5, 0, 0, a, 8, 32, 5)[1].ravel() for a in range(400)])
     assert abs(zs.mean()) < 0.02 and abs(zs.std() - 1.0) < 0.02
     assert abs(np.mean(zs ** 4) - 3.0) < 0.15
-
-
-def exact_sho_energy(beta, M, omega, lam=0.5):
-    """Exact energy of one Cartesian degree of freedom under the reference's discretised action
-    S = sum_b [(x_{b+1} - x_b)^2 / (4 lam tau) + cofactor_a x_b^2] (kinetic_class.h, trap_class.h):
-    E = -d ln Z_M / d beta from the circulant normal modes."""
-    tau = beta / M
-    a = 1.0 / (4 * lam * tau)
-    c = 0.5 * tau * omega ** 2 * (1 + tau ** 2 * omega ** 2 / 12)
-    cb = 0.5 * omega ** 2 * (1 + 3 * tau ** 2 * omega ** 2 / 12)
-    s2 = np.sin(np.pi * np.arange(M) / M) ** 2
-    mu = 4 * a * s2 + c
-    dmu = -4 * s2 / (4 * lam * tau ** 2) + cb
-    return 1.0 / (2 * tau) + np.sum(dmu / mu) / (2 * M)
-
-
-def blocked_error(x, n_blocks=20):
-    x = np.asarray(x)
-    nb = len(x) // n_blocks
-    means = x[: nb * n_blocks].reshape(n_blocks, nb).mean(axis=1)
-    return means.std(ddof=1) / math.sqrt(n_blocks)
 
 
 def run_energy_series(o, n_sweeps, attempts_per_sweep, n_warm):
