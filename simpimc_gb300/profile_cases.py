@@ -2,6 +2,7 @@
 
     python -m simpimc_gb300.profile_cases batch    # 256 uneven trapped-Coulomb chains: 1 + 1 sweep launches
     python -m simpimc_gb300.profile_cases hmc      # the same chains with the HMC move: 1 + 1 HMC launches
+    python -m simpimc_gb300.profile_cases hmc_egas # single-chain HMC on the 128-electron gas: 1 + 1 attempts
     python -m simpimc_gb300.profile_cases egas     # 66-electron gas: 1 + 1 sweep launches (528 attempts each)
     python -m simpimc_gb300.profile_cases egas_phases  # the same system: per-attempt phase cycles of the
                                                        # sweep kernel's block 0 at one and two groups
@@ -65,6 +66,25 @@ def egas_case(d):
     s.sweep([0, 1], [1, 1], reps)
     s.synchronize()
     print(f"egas ok: {s.move_counters(0)[0] + s.move_counters(1)[0]} attempts")
+
+
+def hmc_egas_case(d):
+    """The single-chain HMC move (leapfrog 0.01 x 10 on the exact gradient, FP64) on the 128-electron
+    gas (r_s = 4, beta = 16, M = 256, |k| < 17 (2 pi / L)) after two bisection sweeps."""
+    from . import Simulation
+    from .configs import electron_gas
+    xml, path = electron_gas(d, n_part=128, rs=4.0, beta=16.0, n_bead=256, k_cut_units=17.0, n_level=4, seed=4242)
+    xml = xml.replace('<Move name="BisectD" type="Bisect" species="eD" n_level="4" />',
+                      '<Move name="BisectD" type="Bisect" species="eD" n_level="4" />\n'
+                      '    <Move name="HMC" type="HMC" step_size="0.01" n_steps="10" />')
+    s = Simulation(xml, base_dir=d)
+    s.set_path(path)
+    s.sweep([0, 1], [1, 1], 2 * 64 * 16)
+    s.move_attempts(2, 1)
+    s.move_attempts(2, 1)
+    s.synchronize()
+    print(f"hmc_egas ok: {s.move_counters(2)[0]} attempts, {s.n_k} k-vectors")
+    s.close()
 
 
 def egas_phases_case(d):
@@ -164,7 +184,7 @@ def egas_chains_case(d):
 def main(argv):
     case = argv[1] if len(argv) > 1 else "batch"
     with tempfile.TemporaryDirectory() as d:
-        {"batch": batch_case, "hmc": hmc_case, "egas": egas_case, "egas_phases": egas_phases_case, "large32": large32_case, "bosons": bosons_case, "chains": chains_case,
+        {"batch": batch_case, "hmc": hmc_case, "egas": egas_case, "egas_phases": egas_phases_case, "hmc_egas": hmc_egas_case, "large32": large32_case, "bosons": bosons_case, "chains": chains_case,
          "egas_chains": egas_chains_case}[case](d)
 
 

@@ -141,6 +141,7 @@ struct SweepArgs {
     // Shared-memory staging (byte offsets into the dynamic shared block).
     uint32_t n_moves, n_pairs;
     uint32_t off_moves, off_pairs, off_phase, off_work;
+    uint32_t off_rho_stage, rho_cpt;  // density staging: cells per thread (0: read from global memory)
     uint32_t n_stage;
     const float2* stage_x[kMaxPair];
     const float4* stage_c[kMaxPair];
@@ -484,6 +485,42 @@ __device__ __forceinline__ void CopyWords(void* dst, const void* src, uint32_t b
 /// kF32: FP32 mode. Per-slice densities are FP32 (a.rho32), bead phases are FP32 (PhaseF), and
 /// each thread's Ewald differences are summed with a cascaded compensated sum before they join the
 /// double-float acceptance pipeline; positions, pair links and level sums stay double-float.
+/// A thread's Ewald cells it = tid, tid + T, ... of an attempt's (owned slice, k-chunk) grid, as
+/// (slice index, k offset) advanced without a division per cell.
+struct CellIter {
+    uint32_t si, kk, dq, dr, nk;
+    __device__ __forceinline__ CellIter(uint32_t tid, uint32_t T, uint32_t nk_) : nk(nk_ ? nk_ : 1u) {
+        si = tid / nk;
+        kk = tid - si * nk;
+        dq = T / nk;
+        dr = T - dq * nk;
+    }
+    __device__ __forceinline__ void Next() {
+        kk += dr;
+        si += dq;
+        if (kk >= nk) {
+            kk -= nk;
+            ++si;
+        }
+    }
+};
+
+/// Slice b0 + jj of an M-slice ring (b0 < M, jj < M).
+__device__ __forceinline__ uint32_t RingSlice(uint32_t b0, uint32_t jj, uint32_t M) {
+    const uint32_t b = b0 + jj;
+    return b >= M ? b - M : b;
+}
+
+/// Asynchronous global -> shared copies (cp.async), completed by CpAsyncWaitAll of the issuing thread.
+__device__ __forceinline__ void CpAsync8(void* smem, const void* gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void CpAsync16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void CpAsyncCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void CpAsyncWaitAll() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 template <bool kF32>
 __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_constant__ SweepArgs a) {
     extern __shared__ float4 smem4[];
@@ -660,7 +697,31 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                 // the sampling phases and are consumed in the grid phase.
                 const uint32_t nk_own = k_hi - k_lo;
                 float4 pre_rho = make_float4(0.f, 0.f, 0.f, 0.f), pre_rho_o = pre_rho;
-                if (any_lr && (uint32_t)tid < n_own * nk_own) {
+                // Density staging: every Ewald cell this thread evaluates (cell ci = tid + ci blockDim),
+                // the moved species' and the first other species' densities, copied asynchronously into
+                // shared memory now and read in the grid phase, so that no cell's load sits on it.
+                const bool staged_rho = a.rho_cpt > 0 && n_own * nk_own <= a.rho_cpt * blockDim.x;  // else read global memory
+                float2* st_f = reinterpret_cast<float2*>(sbase + a.off_rho_stage);  // FP32: [cpt][blockDim][2]
+                float4* st_d = reinterpret_cast<float4*>(sbase + a.off_rho_stage);  // double-float: [cpt][blockDim][2]
+                if (staged_rho) {
+                    if (any_lr) {
+                        uint32_t ci = 0;
+                        CellIter cell(tid, blockDim.x, nk_own);
+                        for (uint32_t it = tid; it < n_own * nk_own; it += blockDim.x, ++ci, cell.Next()) {
+                            const uint32_t k = k_lo + cell.kk;
+                            const uint32_t b = RingSlice(bead0, s_slice_jj[cell.si], M);
+                            const size_t e = 2 * ((size_t)ci * blockDim.x + tid);
+                            if constexpr (kF32) {
+                                CpAsync8(st_f + e, &a.rho32[((size_t)slot_s * M + b) * K + k]);
+                                if (slot_o_first >= 0) CpAsync8(st_f + e + 1, &a.rho32[((size_t)slot_o_first * M + b) * K + k]);
+                            } else {
+                                CpAsync16(st_d + e, &a.rho[((size_t)slot_s * M + b) * K + k]);
+                                if (slot_o_first >= 0) CpAsync16(st_d + e + 1, &a.rho[((size_t)slot_o_first * M + b) * K + k]);
+                            }
+                        }
+                    }
+                    CpAsyncCommit();
+                } else if (any_lr && (uint32_t)tid < n_own * nk_own) {
                     const uint32_t k = k_lo + tid % nk_own;
                     const uint32_t b = (bead0 + s_slice_jj[tid / nk_own]) % M;
                     if constexpr (kF32) {
@@ -819,11 +880,18 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                         // This cell's densities (the first ones were loaded at the top of the
                         // attempt); the next cell's are requested before this one's arithmetic.
                         float2 rho_nx = make_float2(pre_rho.x, pre_rho.y), ro_nx = make_float2(pre_rho_o.x, pre_rho_o.y);
-                        for (uint32_t it = tid; it < n_own * nk; it += blockDim.x, ++ci) {
-                            const uint32_t si = it / nk, k = k_lo + it % nk;
-                            const uint32_t b = (bead0 + s_slice_jj[si]) % M;
+                        if (staged_rho) CpAsyncWaitAll();
+                        CellIter cell(tid, blockDim.x, nk);
+                        for (uint32_t it = tid; it < n_own * nk; it += blockDim.x, ++ci, cell.Next()) {
+                            const uint32_t si = cell.si, k = k_lo + cell.kk;
+                            const uint32_t b = RingSlice(bead0, s_slice_jj[si], M);
+                            if (staged_rho) {
+                                const float2* e = st_f + 2 * ((size_t)ci * blockDim.x + tid);
+                                rho_nx = e[0];
+                                ro_nx = e[1];
+                            }
                             const float2 rho = rho_nx, ro_first = ro_nx;
-                            if (it + blockDim.x < n_own * nk) {
+                            if (!staged_rho && it + blockDim.x < n_own * nk) {
                                 const uint32_t it2 = it + blockDim.x, si2 = it2 / nk, k2 = k_lo + it2 % nk;
                                 const uint32_t b2 = (bead0 + s_slice_jj[si2]) % M;
                                 rho_nx = a.rho32[((size_t)slot_s * M + b2) * K + k2];
@@ -855,14 +923,17 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                         const uint32_t nk = nk_own;
                         dd lr{0.f, 0.f};
                         uint32_t ci = 0;
-                        for (uint32_t it = tid; it < n_own * nk; it += blockDim.x, ++ci) {
-                            const uint32_t si = it / nk, k = k_lo + it % nk;
-                            const uint32_t b = (bead0 + s_slice_jj[si]) % M;
+                        if (staged_rho) CpAsyncWaitAll();
+                        CellIter cell(tid, blockDim.x, nk);
+                        for (uint32_t it = tid; it < n_own * nk; it += blockDim.x, ++ci, cell.Next()) {
+                            const uint32_t si = cell.si, k = k_lo + cell.kk;
+                            const uint32_t b = RingSlice(bead0, s_slice_jj[si], M);
                             const int32_t pk = a.kidx[k];
                             const ddc en = PhaseProductDD(tab_new + (size_t)si * 3 * stride, stride, n_d, pk);
                             const ddc eo = (ci == 0 && eo_done) ? pre_eo : PhaseProductDD(tab_old + (size_t)si * 3 * stride, stride, n_d, pk);
                             const ddc dl = CSub(en, eo);
-                            const ddc rho = Unpack(ci == 0 ? pre_rho : a.rho[((size_t)slot_s * M + b) * K + k]);
+                            const float4* e = st_d + 2 * ((size_t)ci * blockDim.x + tid);
+                            const ddc rho = Unpack(staged_rho ? e[0] : (ci == 0 ? pre_rho : a.rho[((size_t)slot_s * M + b) * K + k]));
                             if (ci < kDeltaCache) delta_cache[ci] = CAdd(rho, dl);  // the committed value on acceptance
                             for (int pi = 0; pi < mv.n_pair; ++pi) {
                                 const PairDD& pa = s_pairs[mv.pair[pi]];
@@ -875,8 +946,8 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                                     lr = Add(lr, Mul(vk, t));
                                 } else {
                                     const int slot_o = pa.sa == s ? pa.slot_b : pa.slot_a;
-                                    const ddc ro = Unpack((ci == 0 && slot_o == slot_o_first) ? pre_rho_o
-                                                                                              : a.rho[((size_t)slot_o * M + b) * K + k]);
+                                    const ddc ro = Unpack(slot_o == slot_o_first ? (staged_rho ? e[1] : (ci == 0 ? pre_rho_o : a.rho[((size_t)slot_o * M + b) * K + k]))
+                                                                                 : a.rho[((size_t)slot_o * M + b) * K + k]);
                                     const dd t = Add(Mul(dl.re, ro.re), Mul(dl.im, ro.im));
                                     lr = Add(lr, Scale2(Mul(vk, t), 2.f));
                                 }
@@ -977,9 +1048,10 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                     if (any_lr) {
                         const uint32_t nk = k_hi - k_lo;
                         uint32_t ci = 0;
-                        for (uint32_t it = tid; it < n_own * nk; it += blockDim.x, ++ci) {
-                            const uint32_t si = it / nk, k = k_lo + it % nk;
-                            const uint32_t b = (bead0 + s_slice_jj[si]) % M;
+                        CellIter cell(tid, blockDim.x, nk);
+                        for (uint32_t it = tid; it < n_own * nk; it += blockDim.x, ++ci, cell.Next()) {
+                            const uint32_t si = cell.si, k = k_lo + cell.kk;
+                            const uint32_t b = RingSlice(bead0, s_slice_jj[si], M);
                             // The first kDeltaCache cells of the thread store the value formed in the
                             // grid phase (the cell as loaded there plus the change); later ones re-form it.
                             if constexpr (kF32) {
@@ -991,7 +1063,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                                     const float2 en = PhaseProductF(tf_new + (size_t)si * 3 * stride, stride, n_d, pk);
                                     const float2 eo = PhaseProductF(tf_old + (size_t)si * 3 * stride, stride, n_d, pk);
                                     const float2 dl = make_float2(__fsub_rn(en.x, eo.x), __fsub_rn(en.y, eo.y));
-                                    const float2 c0 = *cell;
+                                    const float2 c0 = staged_rho ? st_f[2 * ((size_t)ci * blockDim.x + tid)] : *cell;
                                     *cell = make_float2(__fadd_rn(c0.x, dl.x), __fadd_rn(c0.y, dl.y));
                                 }
                             } else {
@@ -1002,7 +1074,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                                     const int32_t pk = a.kidx[k];
                                     const ddc dl = CSub(PhaseProductDD(tab_new + (size_t)si * 3 * stride, stride, n_d, pk),
                                                         PhaseProductDD(tab_old + (size_t)si * 3 * stride, stride, n_d, pk));
-                                    *cell = Pack(CAdd(Unpack(*cell), dl));
+                                    *cell = Pack(CAdd(Unpack(staged_rho ? st_d[2 * ((size_t)ci * blockDim.x + tid)] : *cell), dl));
                                 }
                             }
                         }
@@ -1727,8 +1799,19 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
     }
     // Shared layout: [move descriptors][pair descriptors][phase table][staged splines][work area].
     auto align16 = [](size_t x) { return (x + 15) & ~size_t(15); };
-    const size_t work = (size_t)2 * spc * 3 * args->tab_stride * sizeof(ddc) + (size_t)4 * 3 * args->seg_cap * sizeof(dd) +
-                        (size_t)3 * args->seg_cap * sizeof(float) + kMaxLevels * sizeof(float);
+    const size_t work0 = align16((size_t)2 * spc * 3 * args->tab_stride * sizeof(ddc) + (size_t)4 * 3 * args->seg_cap * sizeof(dd) +
+                                 (size_t)3 * args->seg_cap * sizeof(float) + kMaxLevels * sizeof(float));
+    // Density staging: the cells a thread evaluates in one attempt, for both species read (owned
+    // slices per attempt at most spc + 1 when M is not a multiple of R, k-chunk ceil(K / Q)).
+    {
+        const uint32_t own_max = std::min<uint32_t>(kMaxOwned, sys.M % R == 0 ? spc : spc + 1);
+        const uint64_t cells = (uint64_t)own_max * ((sys.K + args->Q - 1) / args->Q);
+        const uint32_t cpt = sys.K && rho_slots ? (uint32_t)((cells + kThreads - 1) / kThreads) : 0u;
+        const size_t bytes = (size_t)cpt * kThreads * 2 * (precision == 32 ? sizeof(float2) : sizeof(float4));
+        args->rho_cpt = bytes <= (size_t)112 * 1024 ? cpt : 0u;  // larger k-chunks read global memory
+    }
+    const size_t rho_stage = (size_t)args->rho_cpt * kThreads * 2 * (precision == 32 ? sizeof(float2) : sizeof(float4));
+    const size_t work = work0 + rho_stage;
     size_t off = 0;
     args->n_moves = (uint32_t)moves.size();
     args->n_pairs = (uint32_t)sys.n_pair;
@@ -1752,6 +1835,7 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
         off = align16(off + bx + bc);
     }
     args->off_work = (uint32_t)off;
+    args->off_rho_stage = (uint32_t)(off + work0);
     const size_t smem = off + work;
     const void* kfn = precision == 32 ? (const void*)BisectSweepKernel<true> : (const void*)BisectSweepKernel<false>;
     CudaCheck(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attribute");
