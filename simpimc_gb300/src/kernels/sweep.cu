@@ -142,6 +142,7 @@ struct SweepArgs {
     uint32_t n_moves, n_pairs;
     uint32_t off_moves, off_pairs, off_phase, off_work;
     uint32_t off_rho_stage, rho_cpt;  // density staging: cells per thread (0: read from global memory)
+    uint32_t off_kstage, kstage_n;    // the block's k-chunk of kidx and v_k (0: read from global memory)
     uint32_t n_stage;
     const float2* stage_x[kMaxPair];
     const float4* stage_c[kMaxPair];
@@ -577,6 +578,23 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
     const bool owns_k = q_own < a.Q;
     const uint32_t k_lo = owns_k ? (uint32_t)(((uint64_t)K * q_own) / a.Q) : 0u;
     const uint32_t k_hi = owns_k ? (uint32_t)(((uint64_t)K * (q_own + 1)) / a.Q) : 0u;
+    // The block's k-chunk of the k-vector indices and of every long-range action's v_k (FP32 mode:
+    // the leading float of each), staged once per launch: the chunk is the same in every attempt.
+    int32_t* s_kidx = reinterpret_cast<int32_t*>(sbase + a.off_kstage);
+    float* s_vkf = reinterpret_cast<float*>(s_kidx + a.kstage_n);    // FP32: [n_pairs][kstage_n]
+    float2* s_vkd = reinterpret_cast<float2*>(s_kidx + a.kstage_n);  // double-float: [n_pairs][kstage_n]
+    const bool kstaged = a.kstage_n > 0 && k_hi - k_lo <= a.kstage_n;
+    if (kstaged) {
+        for (uint32_t i = threadIdx.x; i < k_hi - k_lo; i += blockDim.x) s_kidx[i] = a.kidx[k_lo + i];
+        for (uint32_t p = 0; p < a.n_pairs; ++p)
+            if (s_pairs[p].use_lr && !s_pairs[p].is_constant)
+                for (uint32_t i = threadIdx.x; i < k_hi - k_lo; i += blockDim.x) {
+                    if constexpr (kF32) s_vkf[(size_t)p * a.kstage_n + i] = s_pairs[p].vk[k_lo + i].x;
+                    else s_vkd[(size_t)p * a.kstage_n + i] = s_pairs[p].vk[k_lo + i];
+                }
+    }
+    __syncthreads();
+    auto kidx_of = [&](uint32_t k) { return kstaged ? s_kidx[k - k_lo] : a.kidx[k]; };
 
     uint64_t ctr[kMaxMoves];
     unsigned long long n_acc[kMaxMoves], n_l0[kMaxMoves];
@@ -845,8 +863,8 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                         PIMC_ROLE_END(rt3, 5);
                     } else if (any_lr && (uint32_t)tid < n_own * nk_own) {
                         // Old-position phase of this thread's first Ewald cell (tables built above).
-                        if constexpr (kF32) pre_eo_f = PhaseProductF(tf_old + (size_t)(tid / nk_own) * 3 * stride, stride, n_d, a.kidx[k_lo + tid % nk_own]);
-                        else pre_eo = PhaseProductDD(tab_old + (size_t)(tid / nk_own) * 3 * stride, stride, n_d, a.kidx[k_lo + tid % nk_own]);
+                        if constexpr (kF32) pre_eo_f = PhaseProductF(tf_old + (size_t)(tid / nk_own) * 3 * stride, stride, n_d, kidx_of(k_lo + tid % nk_own));
+                        else pre_eo = PhaseProductDD(tab_old + (size_t)(tid / nk_own) * 3 * stride, stride, n_d, kidx_of(k_lo + tid % nk_own));
                         eo_done = true;
                         PIMC_ROLE_END(rt3, 6);
                     }
@@ -897,7 +915,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                                 rho_nx = a.rho32[((size_t)slot_s * M + b2) * K + k2];
                                 if (slot_o_first >= 0) ro_nx = a.rho32[((size_t)slot_o_first * M + b2) * K + k2];
                             }
-                            const int32_t pk = a.kidx[k];
+                            const int32_t pk = kidx_of(k);
                             const float2 en = PhaseProductF(tf_new + (size_t)si * 3 * stride, stride, n_d, pk);
                             const float2 eo = (ci == 0 && eo_done) ? pre_eo_f : PhaseProductF(tf_old + (size_t)si * 3 * stride, stride, n_d, pk);
                             const float2 dl = make_float2(__fsub_rn(en.x, eo.x), __fsub_rn(en.y, eo.y));
@@ -906,7 +924,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                             for (int pi = 0; pi < mv.n_pair; ++pi) {
                                 const PairDD& pa = s_pairs[mv.pair[pi]];
                                 if (!pa.use_lr || pa.is_constant) continue;
-                                const float vk = pa.vk[k].x;
+                                const float vk = kstaged ? s_vkf[(size_t)mv.pair[pi] * a.kstage_n + (k - k_lo)] : pa.vk[k].x;
                                 if (pa.sa == pa.sb) {
                                     const float t = __fmaf_rn(dl.x, __fmaf_rn(2.f, rho.x, dl.x), __fmul_rn(dl.y, __fmaf_rn(2.f, rho.y, dl.y)));
                                     CompAdd(lr32, __fmul_rn(vk, t));
@@ -928,7 +946,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                         for (uint32_t it = tid; it < n_own * nk; it += blockDim.x, ++ci, cell.Next()) {
                             const uint32_t si = cell.si, k = k_lo + cell.kk;
                             const uint32_t b = RingSlice(bead0, s_slice_jj[si], M);
-                            const int32_t pk = a.kidx[k];
+                            const int32_t pk = kidx_of(k);
                             const ddc en = PhaseProductDD(tab_new + (size_t)si * 3 * stride, stride, n_d, pk);
                             const ddc eo = (ci == 0 && eo_done) ? pre_eo : PhaseProductDD(tab_old + (size_t)si * 3 * stride, stride, n_d, pk);
                             const ddc dl = CSub(en, eo);
@@ -938,7 +956,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                             for (int pi = 0; pi < mv.n_pair; ++pi) {
                                 const PairDD& pa = s_pairs[mv.pair[pi]];
                                 if (!pa.use_lr || pa.is_constant) continue;
-                                const float2 vkf = pa.vk[k];
+                                const float2 vkf = kstaged ? s_vkd[(size_t)mv.pair[pi] * a.kstage_n + (k - k_lo)] : pa.vk[k];
                                 const dd vk{vkf.x, vkf.y};
                                 if (pa.sa == pa.sb) {
                                     // |rho + D|^2 - |rho|^2 = D.re (2 rho.re + D.re) + D.im (2 rho.im + D.im)
@@ -1059,7 +1077,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                                 if (ci < kDeltaCache) {
                                     *cell = delta_f[ci];
                                 } else {
-                                    const int32_t pk = a.kidx[k];
+                                    const int32_t pk = kidx_of(k);
                                     const float2 en = PhaseProductF(tf_new + (size_t)si * 3 * stride, stride, n_d, pk);
                                     const float2 eo = PhaseProductF(tf_old + (size_t)si * 3 * stride, stride, n_d, pk);
                                     const float2 dl = make_float2(__fsub_rn(en.x, eo.x), __fsub_rn(en.y, eo.y));
@@ -1071,7 +1089,7 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                                 if (ci < kDeltaCache) {
                                     *cell = Pack(delta_cache[ci]);
                                 } else {
-                                    const int32_t pk = a.kidx[k];
+                                    const int32_t pk = kidx_of(k);
                                     const ddc dl = CSub(PhaseProductDD(tab_new + (size_t)si * 3 * stride, stride, n_d, pk),
                                                         PhaseProductDD(tab_old + (size_t)si * 3 * stride, stride, n_d, pk));
                                     *cell = Pack(CAdd(Unpack(staged_rho ? st_d[2 * ((size_t)ci * blockDim.x + tid)] : *cell), dl));
@@ -1811,7 +1829,18 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
         args->rho_cpt = bytes <= (size_t)112 * 1024 ? cpt : 0u;  // larger k-chunks read global memory
     }
     const size_t rho_stage = (size_t)args->rho_cpt * kThreads * 2 * (precision == 32 ? sizeof(float2) : sizeof(float4));
-    const size_t work = work0 + rho_stage;
+    // The block's k-chunk of kidx and of every pair action's v_k, when some action has a long range.
+    {
+        bool any_long = false;
+        for (int i = 0; i < sys.n_pair; ++i) any_long |= sys.pair[i].use_long_range && !sys.pair[i].is_constant;
+        const uint32_t n_chunk = sys.K ? (uint32_t)((sys.K + args->Q - 1) / args->Q + 1) & ~1u : 0u;  // even: keeps v_k 8-byte aligned
+        const size_t kbytes = (size_t)n_chunk * (sizeof(int32_t) + (size_t)sys.n_pair * (precision == 32 ? sizeof(float) : sizeof(float2)));
+        args->kstage_n = (any_long && kbytes <= (size_t)64 * 1024 && work0 + rho_stage + align16(kbytes) <= (size_t)190 * 1024) ? n_chunk : 0u;
+    }
+    const size_t kstage = args->kstage_n ? align16((size_t)args->kstage_n * (sizeof(int32_t) + (size_t)sys.n_pair *
+                                                                                (precision == 32 ? sizeof(float) : sizeof(float2))))
+                                         : 0;
+    const size_t work = work0 + rho_stage + kstage;
     size_t off = 0;
     args->n_moves = (uint32_t)moves.size();
     args->n_pairs = (uint32_t)sys.n_pair;
@@ -1836,6 +1865,7 @@ void Context::Sweep(const uint32_t* mv, const uint64_t* counts, uint32_t n_entri
     }
     args->off_work = (uint32_t)off;
     args->off_rho_stage = (uint32_t)(off + work0);
+    args->off_kstage = (uint32_t)(off + work0 + rho_stage);
     const size_t smem = off + work;
     const void* kfn = precision == 32 ? (const void*)BisectSweepKernel<true> : (const void*)BisectSweepKernel<false>;
     CudaCheck(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attribute");
