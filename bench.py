@@ -730,7 +730,7 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "n_chains": N_CHAINS, "bead_moves_per_step": per_step,
                    "bead_moves_per_step_bisection": per_sweep, "bead_moves_per_step_hmc": per_hmc,
                    "tile": {"items_per_lane": ipl, "max_warps": mw, "wave": wave, "autotune_s_per_sweep": tune_s},
-                   "hmc_cluster": batch.hmc_cluster,
+                   "hmc_cluster": batch.hmc_cluster, "overlap_heavy_chains": batch.overlap, "split_chains": batch.split,
                    "bisection_acceptance": float((acc1 - acc0).sum() / max((att1 - att0).sum(), 1)),
                    "hmc_acceptance": float((hacc1 - hacc0).sum() / max((hatt1 - hatt0).sum(), 1)),
                    "l2": "256 MB flush between timed steps", "parallelism": "replicas (independent chains per GPU)"},

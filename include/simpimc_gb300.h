@@ -249,6 +249,14 @@ int pimc_batch_rounds(pimc_batch* b, uint64_t* rounds);
  * split (0: the plain one-block-per-chain launch); pimc_batch_autotune tries 0, 8, 16 and 32. */
 int pimc_batch_set_split(pimc_batch* b, uint32_t n);
 int pimc_batch_get_split(pimc_batch* b, uint32_t* n);
+/* Overlapped measurement cycle: with heavy = H > 0 and HMC attempts in the cycle, pimc_batch_run's
+ * graph runs the H most expensive chains' sweeps and HMC attempts on one stream and the other
+ * chains' on a second stream at the same time (each chain's kernels in order, then one energy
+ * measurement of every chain), so the lighter chains' HMC fills the SMs their sweeps leave while the
+ * heavy sweeps finish. The Markov chains are unchanged; pimc_batch_autotune tries H = 0, 16, 32,
+ * 48, 64, 96 (0: one stream). */
+int pimc_batch_set_overlap(pimc_batch* b, uint32_t heavy);
+int pimc_batch_get_overlap(pimc_batch* b, uint32_t* heavy);
 /* Hybrid Monte Carlo on the batch ("batched + adjoint"; no reference counterpart): a chain's input
  * may hold one <Move type="HMC" step_size="..." n_steps="..."/> besides its Bisect move. Each
  * attempt draws Gaussian momenta for every bead from the move's stream (keyed by its index in the

@@ -108,6 +108,8 @@ SIGNATURES = {
     "pimc_batch_reset_energy": (C.c_int, [_P]),
     "pimc_batch_counters": (C.c_int, [_P, _U64P, _U64P]),
     "pimc_batch_rounds": (C.c_int, [_P, _U64P]),
+    "pimc_batch_set_overlap": (C.c_int, [_P, C.c_uint32]),
+    "pimc_batch_get_overlap": (C.c_int, [_P, _U32P]),
     "pimc_batch_set_split": (C.c_int, [_P, C.c_uint32]),
     "pimc_batch_get_split": (C.c_int, [_P, _U32P]),
     "pimc_batch_hmc_attempts": (C.c_int, [_P, C.c_uint64]),
@@ -500,6 +502,17 @@ class ChainBatch:
         acc = np.zeros(self.n_chains, dtype=np.uint64)
         self._check(self._lib.pimc_batch_counters(self._h, att.ctypes.data_as(_U64P), acc.ctypes.data_as(_U64P)))
         return att, acc
+
+    @property
+    def overlap(self) -> int:
+        """Heaviest chains run beside the others in the measurement cycle's graph (0: one stream)."""
+        n = C.c_uint32()
+        self._check(self._lib.pimc_batch_get_overlap(self._h, C.byref(n)))
+        return n.value
+
+    @overlap.setter
+    def overlap(self, heavy: int):
+        self._check(self._lib.pimc_batch_set_overlap(self._h, heavy))
 
     @property
     def split(self) -> int:

@@ -107,6 +107,7 @@ class ChainBatch {
     int device = 0, n_sm = 0;
     uint32_t items_per_lane = 2, max_warps = 16, wave = 1;  // pair tile and attempts in flight per chain
     uint32_t split_request = 0;       // chains asked to run on two-block clusters
+    uint32_t overlap_heavy = 0;       // cycle graph: the heaviest chains' sweep beside the others' sweep and HMC
     uint32_t n_split_ = 0, n_clusters_ = 0;  // chains split, clusters of the launch (0: plain launch)
     cudaStream_t stream = nullptr;
     std::vector<ChainSpec> specs;
@@ -124,9 +125,10 @@ class ChainBatch {
 
    private:
     void Upload();
-    void LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts);
+    // chains order[first .. first + count) on stream s (the batch's stream when null)
+    void LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts, uint32_t first = 0, uint32_t count = 0xffffffffu, cudaStream_t s = nullptr);
     void ApplySplit();
-    void LaunchHmc(uint64_t n_attempts);
+    void LaunchHmc(uint64_t n_attempts, uint32_t first = 0, uint32_t count = 0xffffffffu, cudaStream_t s = nullptr);
     void LaunchMeasure();
     void ResetGraph();
     std::unique_ptr<DeviceBuffer> pos_, chains_dev_, order_dev_, att_, acc_, series_, n_meas_, err_, last_, rounds_;
@@ -139,6 +141,9 @@ class ChainBatch {
     size_t pos_float4 = 0;
     cudaGraphExec_t graph_ = nullptr;
     uint64_t graph_sweeps_ = 0, graph_hmc_ = 0;
+    uint32_t graph_heavy_ = 0;
+    cudaStream_t side_ = nullptr;                      // second stream of the overlapped cycle
+    cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
     uint32_t launches_per_cycle_ = 3;  // sweep + energy parts + energy finish
     std::unique_ptr<DeviceBuffer> energy_tasks_, energy_first_, energy_part_;
     uint32_t n_energy_tasks_ = 0;

@@ -1426,6 +1426,9 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
     }
     series_cap = 4096;
     CudaCheck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream create");
+    CudaCheck(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking), "stream create");
+    CudaCheck(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming), "event create");
+    CudaCheck(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming), "event create");
     pos_.reset(new DeviceBuffer(off * sizeof(float4)));
     pos_float4 = off;
     CudaCheck(cudaMemset(pos_->ptr, 0, off * sizeof(float4)), "memset");
@@ -1501,6 +1504,9 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
 
 ChainBatch::~ChainBatch() {
     if (graph_) cudaGraphExecDestroy(graph_);
+    if (ev_fork_) cudaEventDestroy(ev_fork_);
+    if (ev_join_) cudaEventDestroy(ev_join_);
+    if (side_) cudaStreamDestroy(side_);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -1634,11 +1640,15 @@ BatchArgs MakeArgs(DeviceBuffer& pos, DeviceBuffer& ch, DeviceBuffer& ord, Devic
 }
 }  // namespace
 
-void ChainBatch::LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts) {
+void ChainBatch::LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts, uint32_t first, uint32_t count, cudaStream_t s) {
     uint32_t warps = 1;
     for (const auto& c : chains) warps = std::max(warps, c.n_warps);
     BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, *rounds_, series_cap);
+    if (!s) s = stream;
+    count = std::min(count, n_chains - std::min(first, n_chains));
+    if (count == 0) return;
     if (n_split_ > 0) {
+        if (first != 0 || count != n_chains) throw PimcError(kErrState, "split chains run in the whole-batch launch only");
         // Clusters of two blocks: a split chain on both, otherwise two chains side by side.
         a.cluster_tasks = cluster_tasks_->as<uint2>();
         cudaLaunchAttribute attr{};
@@ -1650,12 +1660,13 @@ void ChainBatch::LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts) {
         cfg.gridDim = dim3(2 * n_clusters_);
         cfg.blockDim = dim3(warps * 32);
         cfg.dynamicSmemBytes = stage_bytes;
-        cfg.stream = stream;
+        cfg.stream = s;
         cfg.attrs = &attr;
         cfg.numAttrs = 1;
         CudaCheck(cudaLaunchKernelEx(&cfg, BatchSweepKernel, a, n_sweeps, n_attempts), "batch sweep launch");
     } else {
-        BatchSweepKernel<<<n_chains, warps * 32, stage_bytes, stream>>>(a, n_sweeps, n_attempts);
+        a.order = order_dev_->as<uint32_t>() + first;  // blocks run chains order[first .. first + count)
+        BatchSweepKernel<<<count, warps * 32, stage_bytes, s>>>(a, n_sweeps, n_attempts);
         CudaCheck(cudaGetLastError(), "batch sweep launch");
     }
     ++kernel_launches;
@@ -1757,19 +1768,23 @@ void ChainBatch::SetHmcCluster(uint32_t k) {
     hmc_cluster = k;
 }
 
-void ChainBatch::LaunchHmc(uint64_t n_attempts) {
+void ChainBatch::LaunchHmc(uint64_t n_attempts, uint32_t first, uint32_t count, cudaStream_t s) {
     if (!bead_moves_per_hmc) throw PimcError(kErrState, "no chain of the batch has an HMC move");
-    const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, *rounds_, series_cap);
+    BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, *rounds_, series_cap);
+    if (!s) s = stream;
+    count = std::min(count, n_chains - std::min(first, n_chains));
+    if (count == 0) return;
+    a.order = order_dev_->as<uint32_t>() + first;  // clusters run chains order[first .. first + count)
     cudaLaunchAttribute attr{};
     attr.id = cudaLaunchAttributeClusterDimension;
     attr.val.clusterDim.x = hmc_cluster;
     attr.val.clusterDim.y = 1;
     attr.val.clusterDim.z = 1;
     cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(n_chains * hmc_cluster);
+    cfg.gridDim = dim3(count * hmc_cluster);
     cfg.blockDim = dim3(kHmcThreads);
     cfg.dynamicSmemBytes = HmcSmem(hmc_cluster);
-    cfg.stream = stream;
+    cfg.stream = s;
     cfg.attrs = &attr;
     cfg.numAttrs = 1;
     for (uint64_t done = 0; done < n_attempts;) {
@@ -1818,13 +1833,28 @@ void ChainBatch::Measure() { LaunchMeasure(); }
 
 void ChainBatch::Run(uint64_t n_cycles, uint64_t spm) {
     if (spm == 0) throw PimcError(kErrArg, "sweeps_per_measure must be positive");
-    if (!graph_ || graph_sweeps_ != spm || graph_hmc_ != hmc_per_cycle) {
+    if (!graph_ || graph_sweeps_ != spm || graph_hmc_ != hmc_per_cycle || graph_heavy_ != overlap_heavy) {
         ResetGraph();
         cudaGraph_t g = nullptr;
         CudaCheck(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
         const uint64_t before = kernel_launches;
-        LaunchSweep(spm, 0);
-        if (hmc_per_cycle) LaunchHmc(hmc_per_cycle);
+        const uint32_t heavy = overlap_heavy;
+        if (hmc_per_cycle && n_split_ == 0 && heavy > 0 && heavy < n_chains) {
+            // The heavy chains' sweep and HMC on the main stream, the others' sweep and HMC on the
+            // side stream at the same time: a light chain's HMC fills SMs that its sweep left while
+            // the heavy sweeps finish. Each chain's own kernels stay in order.
+            CudaCheck(cudaEventRecord(ev_fork_, stream), "fork");
+            CudaCheck(cudaStreamWaitEvent(side_, ev_fork_, 0), "fork wait");
+            LaunchSweep(spm, 0, 0, heavy, stream);
+            LaunchSweep(spm, 0, heavy, n_chains - heavy, side_);
+            LaunchHmc(hmc_per_cycle, heavy, n_chains - heavy, side_);
+            LaunchHmc(hmc_per_cycle, 0, heavy, stream);
+            CudaCheck(cudaEventRecord(ev_join_, side_), "join");
+            CudaCheck(cudaStreamWaitEvent(stream, ev_join_, 0), "join wait");
+        } else {
+            LaunchSweep(spm, 0);
+            if (hmc_per_cycle) LaunchHmc(hmc_per_cycle);
+        }
         LaunchMeasure();
         launches_per_cycle_ = (uint32_t)(kernel_launches - before);
         kernel_launches = before;
@@ -1834,6 +1864,7 @@ void ChainBatch::Run(uint64_t n_cycles, uint64_t spm) {
         CudaCheck(e, "graph instantiate");
         graph_sweeps_ = spm;
         graph_hmc_ = hmc_per_cycle;
+        graph_heavy_ = overlap_heavy;
     }
     for (uint64_t i = 0; i < n_cycles; ++i) {
         CudaCheck(cudaGraphLaunch(graph_, stream), "graph launch");
@@ -1978,6 +2009,45 @@ double ChainBatch::Autotune(uint32_t trial_sweeps) {
         }
         SetHmcCluster(best_k);
         CudaCheck(cudaStreamSynchronize(stream), "sync");
+        if (n_split_ == 0) {
+            // The measurement cycle with the heaviest H chains beside the others (H = 0: one stream).
+            DeviceBuffer meas_save(n_meas_->bytes), last_save(last_->bytes);
+            copy(hatt_save, *hmc_att_);
+            copy(hacc_save, *hmc_acc_);
+            copy(meas_save, *n_meas_);
+            copy(last_save, *last_);
+            const uint64_t hpc = hmc_per_cycle;
+            hmc_per_cycle = 1;
+            float best_c = 1e30f;
+            uint32_t best_h = 0;
+            for (uint32_t hv : {0u, 16u, 32u, 48u, 64u, 96u}) {
+                if (hv >= n_chains) continue;
+                overlap_heavy = hv;
+                Run(1, 1);  // builds the cycle's graph
+                CudaCheck(cudaEventRecord(e0, stream), "event");
+                Run(trial_sweeps + 1, 1);
+                CudaCheck(cudaEventRecord(e1, stream), "event");
+                CudaCheck(cudaEventSynchronize(e1), "event sync");
+                float ms = 0.f;
+                CudaCheck(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+                if (ms < best_c) {
+                    best_c = ms;
+                    best_h = hv;
+                }
+                copy(*pos_, pos_save);
+                copy(*att_, att_save);
+                copy(*acc_, acc_save);
+                copy(*rounds_, rounds_save);
+                copy(*hmc_att_, hatt_save);
+                copy(*hmc_acc_, hacc_save);
+                copy(*n_meas_, meas_save);
+                copy(*last_, last_save);
+            }
+            hmc_per_cycle = hpc;
+            overlap_heavy = best_h;
+            ResetGraph();
+            CudaCheck(cudaStreamSynchronize(stream), "sync");
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -2117,6 +2187,20 @@ int pimc_batch_reset_energy(pimc_batch* h) {
 
 int pimc_batch_counters(pimc_batch* h, uint64_t* attempts, uint64_t* accepts) {
     return BatchGuard(h, [&](pimc::ChainBatch& b) { b.ReadCounters(attempts, accepts); });
+}
+
+int pimc_batch_set_overlap(pimc_batch* h, uint32_t heavy) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) {
+        if (heavy > b.n_chains) throw pimc::PimcError(pimc::kErrArg, "more heavy chains than chains");
+        b.overlap_heavy = heavy;
+    });
+}
+
+int pimc_batch_get_overlap(pimc_batch* h, uint32_t* heavy) {
+    return BatchGuard(h, [&](pimc::ChainBatch& b) {
+        if (!heavy) throw pimc::PimcError(pimc::kErrArg, "null output");
+        *heavy = b.overlap_heavy;
+    });
 }
 
 int pimc_batch_set_split(pimc_batch* h, uint32_t n) {

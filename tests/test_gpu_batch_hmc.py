@@ -74,10 +74,15 @@ def test_batch_hmc_replays_oracle(tmp_path, gpu_lib, oracle_mod, k):
     b.close()
 
 
-def test_batch_hmc_cycle_graph_equals_calls(tmp_path, gpu_lib):
+@pytest.mark.parametrize("heavy", [0, 2])
+def test_batch_hmc_cycle_graph_equals_calls(tmp_path, gpu_lib, heavy):
+    """The cycle's graph (with `heavy` > 0: the heaviest chains on one stream beside the others on a
+    second) gives the same bits as the same calls made one by one."""
     items = _items(tmp_path)
     g = _batch(tmp_path, items)
     s = _batch(tmp_path, items)
+    g.overlap = heavy
+    assert g.overlap == heavy
     g.set_hmc_per_cycle(2)
     g.run(3, 1)
     for _ in range(3):
@@ -136,4 +141,26 @@ def test_batch_hmc_needs_the_move(tmp_path, gpu_lib):
     b = _batch(tmp_path, items)
     with pytest.raises(PimcError):
         b.hmc_attempts(1)
+    b.close()
+
+
+def test_autotune_with_hmc_keeps_state(tmp_path, gpu_lib):
+    """The autotuner's trials (tiles, split chains, cluster sizes, overlapped cycles) leave the
+    paths, every counter and the energy series as they were."""
+    items = _items(tmp_path)
+    b = _batch(tmp_path, items)
+    b.set_hmc_per_cycle(1)
+    b.run(2, 1)
+    before = [b.get_path(c) for c in range(len(items))]
+    cnt0, hcnt0 = b.counters(), b.hmc_counters()
+    e0 = [b.energy(c) for c in range(len(items))]
+    b.autotune(1)
+    assert b.hmc_cluster in (1, 2, 4, 8) and 0 <= b.overlap < len(items)
+    cnt1, hcnt1 = b.counters(), b.hmc_counters()
+    for x, y in zip(cnt0 + hcnt0, cnt1 + hcnt1):
+        assert np.array_equal(x, y)
+    for c in range(len(items)):
+        assert np.array_equal(before[c], b.get_path(c))
+        e1 = b.energy(c)
+        assert e1[1] == e0[c][1] == 2 and np.array_equal(e1[0], e0[c][0])
     b.close()
