@@ -253,8 +253,8 @@ int pimc_batch_get_split(pimc_batch* b, uint32_t* n);
  * graph runs the H most expensive chains' sweeps and HMC attempts on one stream and the other
  * chains' on a second stream at the same time (each chain's kernels in order, then one energy
  * measurement of every chain), so the lighter chains' HMC fills the SMs their sweeps leave while the
- * heavy sweeps finish. The Markov chains are unchanged; pimc_batch_autotune tries H = 0, 16, 32,
- * 48, 64, 96 (0: one stream). */
+ * heavy sweeps finish. The Markov chains are unchanged; pimc_batch_autotune tries H = 0, n/8, n/4,
+ * 3n/8, n/2 and 5n/8 of the n chains (0: one stream), timing each by the median of five cycles. */
 int pimc_batch_set_overlap(pimc_batch* b, uint32_t heavy);
 int pimc_batch_get_overlap(pimc_batch* b, uint32_t* heavy);
 /* Hybrid Monte Carlo on the batch ("batched + adjoint"; no reference counterpart): a chain's input

@@ -129,7 +129,7 @@ class ChainBatch {
     void LaunchSweep(uint64_t n_sweeps, uint64_t n_attempts, uint32_t first = 0, uint32_t count = 0xffffffffu, cudaStream_t s = nullptr);
     void ApplySplit();
     void LaunchHmc(uint64_t n_attempts, uint32_t first = 0, uint32_t count = 0xffffffffu, cudaStream_t s = nullptr);
-    void LaunchMeasure();
+    void LaunchMeasure(uint32_t i0 = 0, uint32_t i1 = 0xffffffffu, cudaStream_t s = nullptr);  // chains order[i0 .. i1)
     void ResetGraph();
     std::unique_ptr<DeviceBuffer> pos_, chains_dev_, order_dev_, att_, acc_, series_, n_meas_, err_, last_, rounds_;
     std::unique_ptr<DeviceBuffer> hmc_att_, hmc_acc_;  // HMC counters per chain
@@ -147,6 +147,7 @@ class ChainBatch {
     uint32_t launches_per_cycle_ = 3;  // sweep + energy parts + energy finish
     std::unique_ptr<DeviceBuffer> energy_tasks_, energy_first_, energy_part_;
     uint32_t n_energy_tasks_ = 0;
+    std::vector<uint32_t> energy_first_host_;  // first energy task of each order position (n_chains + 1)
     size_t energy_smem_ = 0;  // dynamic shared memory of the energy kernel
 };
 

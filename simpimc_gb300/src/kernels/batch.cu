@@ -909,11 +909,15 @@ __global__ void __launch_bounds__(kEnergyThreads) BatchEnergyPartKernel(BatchArg
 
 /// One warp per chain: its tasks' sums in task order, then E and its parts (FP64) into the
 /// series and the latest-measurement record.
-__global__ void BatchEnergyFinishKernel(BatchArgs a, const uint32_t* __restrict__ first_task, const float2* __restrict__ part, uint32_t n_chains) {
-    const uint32_t ci = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31u;
-    if (ci >= n_chains) return;
+/// One warp per chain of order positions [i0, i1): its tasks [first_task[i], first_task[i + 1]) are
+/// summed in task order.
+__global__ void BatchEnergyFinishKernel(BatchArgs a, const uint32_t* __restrict__ first_task, const float2* __restrict__ part, uint32_t i0,
+                                        uint32_t i1) {
+    const uint32_t i = i0 + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31u;
+    if (i >= i1) return;
+    const uint32_t ci = a.order[i];
     const ChainDev& c = a.chains[ci];
-    const uint32_t t0 = first_task[ci], t1 = first_task[ci + 1];
+    const uint32_t t0 = first_task[i], t1 = first_task[i + 1];
     dd s[3] = {DD(0.f), DD(0.f), DD(0.f)};
     for (uint32_t t = t0 + lane; t < t1; t += 32)
         for (int q = 0; q < 3; ++q) {
@@ -1477,11 +1481,21 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
     CudaCheck(cudaMemset(n_meas_->ptr, 0, n_chains * sizeof(uint64_t)), "memset");
     CudaCheck(cudaMemset(err_->ptr, 0, sizeof(int)), "memset");
     CudaCheck(cudaStreamSynchronize(cudaStreamLegacy), "memset completion");  // before any work on `stream`
-    // Energy tasks: kEnergySlices slices of one chain each, chains in index order.
+    // Energy tasks: kEnergySlices slices of one chain each, chains in the launch order (most
+    // expensive first, as SetTiles orders the blocks), so that a contiguous range of order positions
+    // has a contiguous range of tasks.
+    order.resize(n_chains);
+    std::iota(order.begin(), order.end(), 0u);
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+        const double wx = (double)chains[x].attempts_per_sweep * chains[x].n_part;
+        const double wy = (double)chains[y].attempts_per_sweep * chains[y].n_part;
+        return wx > wy;
+    });
     std::vector<EnergyTask> tasks;
     std::vector<uint32_t> first(n_chains + 1, 0);
-    for (uint32_t ci = 0; ci < n_chains; ++ci) {
-        first[ci] = (uint32_t)tasks.size();
+    for (uint32_t i = 0; i < n_chains; ++i) {
+        const uint32_t ci = order[i];
+        first[i] = (uint32_t)tasks.size();
         for (uint32_t b0 = 0; b0 < chains[ci].n_bead; b0 += kEnergySlices)
             tasks.push_back(EnergyTask{ci, b0, std::min(kEnergySlices, chains[ci].n_bead - b0), 0});
     }
@@ -1499,6 +1513,7 @@ ChainBatch::ChainBatch(const std::vector<std::string>& xml, const std::string& b
     energy_part_.reset(new DeviceBuffer(tasks.size() * 3 * sizeof(float2)));
     CudaCheck(cudaMemcpy(energy_tasks_->ptr, tasks.data(), tasks.size() * sizeof(EnergyTask), cudaMemcpyHostToDevice), "energy tasks");
     CudaCheck(cudaMemcpy(energy_first_->ptr, first.data(), first.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "energy tasks");
+    energy_first_host_ = first;
     SetTiles(items_per_lane, max_warps, wave);
 }
 
@@ -1550,14 +1565,7 @@ void ChainBatch::SetTiles(uint32_t ipl, uint32_t mw, uint32_t wave) {
             stage_bytes = std::max(stage_bytes, (c.staged ? (size_t)12 * c.n_part * c.n_bead : 0) + RingBytes(1u << c.n_level, c.n_level));
     stage_bytes = (stage_bytes + 15) & ~size_t(15);
     CudaCheck(cudaFuncSetAttribute(BatchSweepKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_bytes), "smem attribute");
-    order.resize(n_chains);
-    std::iota(order.begin(), order.end(), 0u);
-    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
-        const double wx = (double)chains[x].attempts_per_sweep * chains[x].n_part;
-        const double wy = (double)chains[y].attempts_per_sweep * chains[y].n_part;
-        return wx > wy;
-    });
-    ApplySplit();
+    ApplySplit();  // `order` (most expensive first) was fixed at creation
     Upload();
     ResetGraph();
 }
@@ -1812,11 +1820,15 @@ void ChainBatch::SetHmcPerCycle(uint64_t n) {
     hmc_per_cycle = n;
 }
 
-void ChainBatch::LaunchMeasure() {
+void ChainBatch::LaunchMeasure(uint32_t i0, uint32_t i1, cudaStream_t s) {
     const BatchArgs a = MakeArgs(*pos_, *chains_dev_, *order_dev_, *att_, *acc_, *series_, *n_meas_, *last_, *err_, *rounds_, series_cap);
-    BatchEnergyPartKernel<<<n_energy_tasks_, kEnergyThreads, energy_smem_, stream>>>(a, energy_tasks_->as<EnergyTask>(), energy_part_->as<float2>());
+    if (!s) s = stream;
+    i1 = std::min(i1, n_chains);
+    if (i0 >= i1) return;
+    const uint32_t t0 = energy_first_host_[i0], t1 = energy_first_host_[i1];
+    BatchEnergyPartKernel<<<t1 - t0, kEnergyThreads, energy_smem_, s>>>(a, energy_tasks_->as<EnergyTask>() + t0, energy_part_->as<float2>() + (size_t)t0 * 3);
     CudaCheck(cudaGetLastError(), "batch energy launch");
-    BatchEnergyFinishKernel<<<(n_chains + 7) / 8, 256, 0, stream>>>(a, energy_first_->as<uint32_t>(), energy_part_->as<float2>(), n_chains);
+    BatchEnergyFinishKernel<<<(i1 - i0 + 7) / 8, 256, 0, s>>>(a, energy_first_->as<uint32_t>(), energy_part_->as<float2>(), i0, i1);
     CudaCheck(cudaGetLastError(), "batch energy launch");
     kernel_launches += 2;
 }
@@ -1848,14 +1860,16 @@ void ChainBatch::Run(uint64_t n_cycles, uint64_t spm) {
             LaunchSweep(spm, 0, 0, heavy, stream);
             LaunchSweep(spm, 0, heavy, n_chains - heavy, side_);
             LaunchHmc(hmc_per_cycle, heavy, n_chains - heavy, side_);
+            LaunchMeasure(heavy, n_chains, side_);
             LaunchHmc(hmc_per_cycle, 0, heavy, stream);
+            LaunchMeasure(0, heavy, stream);
             CudaCheck(cudaEventRecord(ev_join_, side_), "join");
             CudaCheck(cudaStreamWaitEvent(stream, ev_join_, 0), "join wait");
         } else {
             LaunchSweep(spm, 0);
             if (hmc_per_cycle) LaunchHmc(hmc_per_cycle);
+            LaunchMeasure();
         }
-        LaunchMeasure();
         launches_per_cycle_ = (uint32_t)(kernel_launches - before);
         kernel_launches = before;
         CudaCheck(cudaStreamEndCapture(stream, &g), "end capture");
@@ -2020,16 +2034,22 @@ double ChainBatch::Autotune(uint32_t trial_sweeps) {
             hmc_per_cycle = 1;
             float best_c = 1e30f;
             uint32_t best_h = 0;
-            for (uint32_t hv : {0u, 16u, 32u, 48u, 64u, 96u}) {
-                if (hv >= n_chains) continue;
+            for (uint32_t eighths = 0; eighths <= 5; ++eighths) {  // H = 0, n/8, ..., 5n/8
+                const uint32_t hv = n_chains * eighths / 8;
+                if (eighths > 0 && (hv == 0 || hv >= n_chains)) continue;
                 overlap_heavy = hv;
                 Run(1, 1);  // builds the cycle's graph
-                CudaCheck(cudaEventRecord(e0, stream), "event");
-                Run(trial_sweeps + 1, 1);
-                CudaCheck(cudaEventRecord(e1, stream), "event");
-                CudaCheck(cudaEventSynchronize(e1), "event sync");
-                float ms = 0.f;
-                CudaCheck(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+                // the median of five single cycles: two streams schedule differently from run to run
+                float cyc[5];
+                for (float& ms : cyc) {
+                    CudaCheck(cudaEventRecord(e0, stream), "event");
+                    Run(1, 1);
+                    CudaCheck(cudaEventRecord(e1, stream), "event");
+                    CudaCheck(cudaEventSynchronize(e1), "event sync");
+                    CudaCheck(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+                }
+                std::sort(cyc, cyc + 5);
+                const float ms = cyc[2];
                 if (ms < best_c) {
                     best_c = ms;
                     best_h = hv;
