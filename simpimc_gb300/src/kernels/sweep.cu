@@ -1055,6 +1055,16 @@ __global__ void __launch_bounds__(kThreads, 1) BisectSweepKernel(const __grid_co
                     return;
                 }
                 if (s_result & 4) n_l0[m] += 1;
+                if (!grid_work) {
+                    // Every block ran this attempt on the same inputs and commits the same beads;
+                    // without a grid phase no barrier has yet kept a fast block's commit from
+                    // reaching a slow block that still reads them.
+                    ++nbar;
+                    if (!GridBarrier(a.bar, nbar, a.err, a.timeout_ns)) {
+                        abort = true;
+                        return;
+                    }
+                }
 
                 // ---- 6. commit ---------------------------------------------------------------
                 if (res == 1) {

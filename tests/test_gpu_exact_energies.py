@@ -89,3 +89,25 @@ def test_free_particles_in_a_box_match_the_lattice_sum(tmp_path, gpu_lib):
     assert abs(vals.mean() - exact) < 2 * err, (vals.mean(), exact, err)
     classical = 3 * n / (2 * beta)
     assert abs(vals.mean() - classical) > 10 * err  # the box's quantisation is resolved
+
+
+def test_free_particles_replay_the_oracle(tmp_path, gpu_lib, oracle_mod):
+    """Attempts without a grid phase (no pair action) on the single-chain sweep kernel: every block
+    runs them and commits the same beads, after a grid barrier that keeps a fast block's commit from
+    a slow block's reads. The oracle's accept count and path, on the same draws."""
+    n, m, beta, L, lvl = 4, 16, 2.0, 3.0, 3
+    xml = _free_box_xml(n, m, beta, L, lvl, 2, seed=8102)
+    rng = np.random.default_rng(8102)
+    path = np.repeat(rng.uniform(-L / 2, L / 2, size=(n, 1, 3)), m, axis=1)
+    (tmp_path / "init.xyz").write_text("")
+    s = Simulation(xml, base_dir=tmp_path)
+    o = oracle_mod.OracleSim(xml, base_dir=tmp_path)
+    s.set_path(path)
+    o.set_path(path)
+    per_sweep = n * (m // (1 << lvl))
+    s.sweep([0], [per_sweep], 300)
+    o.move_attempts(0, 300 * per_sweep)
+    assert s.move_counters(0)[3] == o.move_stats(0)[2], (s.move_counters(0), o.move_stats(0))
+    assert np.max(np.abs(s.get_path(1) - o.get_path())) < 1e-9
+    s.close()
+    o.close()
