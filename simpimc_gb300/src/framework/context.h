@@ -283,6 +283,7 @@ class Context {
     std::unique_ptr<DeviceBuffer> pos_, pos_new_, rho_, kidx_;
     std::unique_ptr<DeviceBuffer> grad_, mom_, pos_save_, rho_scratch_, phase_tab_;  // adjoint / HMC work arrays
     std::vector<std::unique_ptr<DeviceBuffer>> adj_vk_;                              // double-float v_k per action
+    std::unique_ptr<DeviceBuffer> ewald_w_, ewald_terms_;  // per-species Ewald weight W_s; its terms (v_k pointers, slots)
     std::unique_ptr<DeviceBuffer> partials_, result_, bar_, err_, pairs_, rho_tmp_, parts_, kmag_dev_, sched_, accepts_;
     std::unique_ptr<DeviceBuffer> perm_, perm_inv_, perm_t_, perm_cyc_, perm_drho_, perm_hold_, perm_cnt_, perm_prop_, perm_segold_;
     size_t partials_cap_ = 0, pairs_cap_ = 0, rho_tmp_cap_ = 0, parts_cap_ = 0;

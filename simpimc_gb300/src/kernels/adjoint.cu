@@ -204,6 +204,60 @@ __global__ void EwaldGradDDKernel(const SystemDev sys, const double* __restrict_
     }
 }
 
+/// The Ewald force on a bead of species s from every selected long-range pair action is
+/// -2 tau box_d sum_k k_d Im(conj(W_s(k)) e^{i k r}) with W_s = sum_a v^a_k rho_{o(a)}(k), o(a) the
+/// action's other species (s itself for a homologous action): the actions' terms are linear in the
+/// densities, so one pass over k per bead covers them all. One thread per (slice, k) forms W_s.
+__global__ void EwaldWeightKernel(const SystemDev sys, const float4* __restrict__ rho, const float2* const* __restrict__ vk, const int* __restrict__ other_slot,
+                                  uint32_t n_terms, float4* __restrict__ w) {
+    const uint64_t n = (uint64_t)sys.M * sys.K;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t k = (uint32_t)(i % sys.K);
+        ddc acc{{0.f, 0.f}, {0.f, 0.f}};
+        for (uint32_t a = 0; a < n_terms; ++a) {
+            const float2 v = vk[a][k];
+            const ddc r = Unpack(rho[(size_t)other_slot[a] * sys.M * sys.K + i]);
+            const dd vv{v.x, v.y};
+            acc = CAdd(acc, ddc{Mul(vv, r.re), Mul(vv, r.im)});
+        }
+        w[i] = Pack(acc);
+    }
+}
+
+/// Ewald forces on the beads of one species from its weight W_s (EwaldWeightKernel): one warp per
+/// (slice, particle), lanes over the k-vectors in double-float, the particle's per-dimension phase
+/// rows in shared memory.
+__global__ void EwaldGradSpeciesKernel(const SystemDev sys, const double* __restrict__ pos, uint32_t species, const float4* __restrict__ w,
+                                       const float4* __restrict__ tab256, dd iL, dd two_pi, double* __restrict__ grad) {
+    extern __shared__ ddc etab_s[];  // [warps][3][stride]
+    const uint32_t stride = (uint32_t)max(max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
+    const uint32_t warps = blockDim.x >> 5, wi = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    ddc* my = etab_s + (size_t)wi * 3 * stride;
+    const uint32_t ns = sys.sp_n[species], off = sys.sp_off[species], M = sys.M, np = sys.n_pad, K = sys.K, n_d = sys.n_d;
+    for (uint64_t it = (uint64_t)blockIdx.x * warps + wi; it < (uint64_t)ns * M; it += (uint64_t)gridDim.x * warps) {
+        const uint32_t b = (uint32_t)(it / ns), g = off + (uint32_t)(it % ns);
+        const float4* wb = w + (size_t)b * K;
+        __syncwarp();
+        for (uint32_t t = lane; t < 3 * stride; t += 32) {
+            const uint32_t d = t / stride, n = t - d * stride;
+            if (d < n_d && (int)n <= sys.max_index[d]) my[t] = PhaseDD(SplitDD(PosAt(pos, np, b, d, g)), (int)n, iL, two_pi, tab256);
+        }
+        __syncwarp();
+        dd acc[3] = {DD(0.f), DD(0.f), DD(0.f)};
+        for (uint32_t k = lane; k < K; k += 32) {
+            const int32_t pk = sys.kidx[k];
+            const ddc e = PhaseProductDD(my, stride, n_d, pk);
+            const ddc r = Unpack(wb[k]);
+            const dd f = Sub(Mul(r.re, e.im), Mul(r.im, e.re));  // Im(conj(W) e)
+            for (uint32_t d = 0; d < n_d; ++d) acc[d] = Add(acc[d], MulF(f, (float)KIdx(pk, (int)d)));
+        }
+        for (uint32_t d = 0; d < n_d; ++d) {
+            const dd s = WarpSumDD(acc[d]);
+            if (lane == 0) grad[GIdx(b, d, g, np)] += -2. * sys.tau * sys.box[d] * ToDouble(s);
+        }
+    }
+}
+
 /// HMC momenta: standard normals for every coordinate of the moving particles, in the path order
 /// (moving particle, slice, dimension); normal j is component j % 4 of Philox block 1 + j / 4
 /// of the attempt's stream (two Box-Muller pairs per block).
@@ -370,6 +424,8 @@ void Context::GradientDev(int a, const double* pos, const float4* rho, double* g
     const size_t n = (size_t)sys.M * 3 * sys.n_pad;
     CudaCheck(cudaMemsetAsync(grad, 0, n * sizeof(double), stream), "grad clear");
     const int th = 256;
+    // Several actions selected: the Ewald forces per species in one pass (EwaldWeightKernel).
+    const bool fused_ewald = a < 0 && rho && sys.K;
     for (size_t i = 0; i < actions.size(); ++i) {
         const ActionHost& ah = actions[i];
         if (!Selected(ah, a, (int)i)) continue;
@@ -384,7 +440,7 @@ void Context::GradientDev(int a, const double* pos, const float4* rho, double* g
             if (pa.is_constant) continue;
             const uint64_t ng = (uint64_t)(pa.sa == pa.sb ? sys.sp_n[pa.sa] : sys.sp_n[pa.sa] + sys.sp_n[pa.sb]) * sys.M;
             PairGradKernel<<<Blocks(*this, ng, th), th, 0, stream>>>(sys, pos, pa, grad);
-            if (pa.use_long_range && rho && sys.K) {
+            if (pa.use_long_range && rho && sys.K && !fused_ewald) {
                 const float4* ra = rho + (size_t)sys.sp_rho[pa.sa] * sys.M * sys.K;
                 const float4* rb = rho + (size_t)sys.sp_rho[pa.sb] * sys.M * sys.K;
                 const int stride = std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
@@ -399,6 +455,43 @@ void Context::GradientDev(int a, const double* pos, const float4* rho, double* g
             }
         }
         CudaCheck(cudaGetLastError(), "gradient launch");
+    }
+    if (fused_ewald) {
+        const int stride = std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
+        const int warps = 8;
+        const size_t smem = (size_t)warps * 3 * stride * sizeof(ddc);
+        dd iL, two_pi;
+        SplitDouble(sys.iL, iL.hi, iL.lo);
+        SplitDouble(2. * M_PI, two_pi.hi, two_pi.lo);
+        const size_t mk = (size_t)sys.M * sys.K;
+        for (uint32_t s = 0; s < sys.S; ++s) {
+            // the selected long-range actions acting on species s, each with its other species' densities
+            std::vector<const float2*> vks;
+            std::vector<int> slots;
+            for (size_t i = 0; i < actions.size(); ++i) {
+                const ActionHost& ah = actions[i];
+                if (!Selected(ah, a, (int)i) || ah.kind != 2) continue;
+                const PairDev& pa = sys.pair[ah.index];
+                if (pa.is_constant || !pa.use_long_range || (pa.sa != s && pa.sb != s)) continue;
+                const uint32_t o = pa.sa == s ? pa.sb : pa.sa;
+                vks.push_back(adj_vk_[i]->as<float2>());
+                slots.push_back(sys.sp_rho[o]);
+            }
+            if (vks.empty()) continue;
+            if (!ewald_w_ || ewald_w_->bytes < mk * sizeof(float4)) ewald_w_.reset(new DeviceBuffer(mk * sizeof(float4)));
+            if (!ewald_terms_) ewald_terms_.reset(new DeviceBuffer(kMaxPair * (sizeof(const float2*) + sizeof(int))));
+            if (vks.size() > (size_t)kMaxPair) throw PimcError(kErrUnsupported, "more long-range actions on a species than the fused Ewald gradient takes");
+            const float2** dv = reinterpret_cast<const float2**>(ewald_terms_->ptr);
+            int* ds = reinterpret_cast<int*>(static_cast<char*>(ewald_terms_->ptr) + kMaxPair * sizeof(const float2*));
+            CudaCheck(cudaMemcpyAsync(dv, vks.data(), vks.size() * sizeof(const float2*), cudaMemcpyHostToDevice, stream), "ewald terms");
+            CudaCheck(cudaMemcpyAsync(ds, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice, stream), "ewald terms");
+            EwaldWeightKernel<<<Blocks(*this, mk, th), th, 0, stream>>>(sys, rho, dv, ds, (uint32_t)vks.size(), ewald_w_->as<float4>());
+            const uint64_t nbeads = (uint64_t)sys.sp_n[s] * sys.M;
+            const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((nbeads + warps - 1) / warps, (uint64_t)n_sm * 16));
+            EwaldGradSpeciesKernel<<<blocks, warps * 32, smem, stream>>>(sys, pos, s, ewald_w_->as<float4>(), phase_tab_->as<float4>(), iL, two_pi, grad);
+            CudaCheck(cudaGetLastError(), "ewald gradient launch");
+            // (the next species' terms and weight reuse both buffers after these kernels, in stream order)
+        }
     }
 }
 
