@@ -280,12 +280,13 @@ int pimc_batch_set_hmc_per_cycle(pimc_batch* b, uint64_t n);
 int pimc_batch_set_hmc_cluster(pimc_batch* b, uint32_t k);
 int pimc_batch_get_hmc_cluster(pimc_batch* b, uint32_t* k);
 /* Tiles: one attempt wants ceil((n_part-1)(2^n_level-1) / (32 items_per_lane)) warps for its pair
- * items; with wave = 1 a chain gets that many, at most max_warps (<= 16). With wave = W > 1 (<= 4)
+ * items; with wave = 1 a chain gets that many, at most max_warps (<= 16). With wave = W > 1 (<= 8)
  * a chain runs up to W attempts at once on W groups of such warps (at least 2 each, W times at
- * most max_warps in all): the longest prefix of its next W draws in which no attempt reads what an
- * earlier one may change, so the Markov chain is the sequential one. pimc_batch_autotune times
- * `trial_sweeps` sweeps of every candidate on a saved copy of the chains' state, restores it, and
- * keeps the fastest. */
+ * most max_warps in all): of its next 32 drawn attempts, the first W that commute with every
+ * earlier attempt not yet run (neither reads what the other writes), possibly out of order, so the
+ * Markov chain is the sequential one. pimc_batch_autotune times `trial_sweeps` sweeps of every
+ * candidate (and the split-chain counts, HMC cluster sizes and overlapped cycles) on a saved copy of
+ * the chains' state, restores it, and keeps the fastest. */
 int pimc_batch_set_tiles(pimc_batch* b, uint32_t items_per_lane, uint32_t max_warps, uint32_t wave);
 int pimc_batch_autotune(pimc_batch* b, uint32_t trial_sweeps, uint32_t* items_per_lane, uint32_t* max_warps, uint32_t* wave,
                         double* sec_per_sweep);
