@@ -138,19 +138,30 @@ __device__ __forceinline__ dd SplitDD(double x) {
     return dd{h, (float)(x - (double)h)};
 }
 
-/// Per-slice densities of every kept species from one position copy, in double-float: one thread
-/// per k-vector of a 128-wide chunk, one block per (chunk, slice, slot), particles in order in
-/// chunks whose phase rows sit in shared memory (species_class.h:380-403).
+/// Per-slice densities of every kept species from one position copy, in double-float: one block per
+/// (k-range of kRhoDDThreads x kRhoDDKPerThread k-vectors, slice, slot), each thread summing its
+/// kRhoDDKPerThread k-vectors over the particles in order, in chunks whose phase rows sit in
+/// shared memory (species_class.h:380-403). A wide k-range keeps the phase rows, which every block
+/// of a slice forms again, to a few per thread.
 constexpr uint32_t kRhoDDChunk = 32;
+constexpr uint32_t kRhoDDThreads = 128;
+constexpr uint32_t kRhoDDKPerThread = 8;
 
-__global__ void RhoDDKernel(const SystemDev sys, const double* __restrict__ pos, const int* __restrict__ slot_species, const float4* __restrict__ tab256,
-                            dd iL, dd two_pi, float4* __restrict__ rho) {
+__global__ void __launch_bounds__(kRhoDDThreads) RhoDDKernel(const SystemDev sys, const double* __restrict__ pos, const int* __restrict__ slot_species,
+                                                             const float4* __restrict__ tab256, dd iL, dd two_pi, float4* __restrict__ rho) {
     extern __shared__ ddc rtab[];  // [kRhoDDChunk][3][stride]
     const uint32_t stride = (uint32_t)max(max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y, slot = blockIdx.z;
+    const uint32_t b = blockIdx.y, slot = blockIdx.z;
     const uint32_t s = (uint32_t)slot_species[slot], ns = sys.sp_n[s], off = sys.sp_off[s], K = sys.K, np = sys.n_pad, n_d = sys.n_d;
-    const int32_t pk = k < K ? sys.kidx[k] : 0;
-    ddc acc{DD(0.f), DD(0.f)};
+    const uint32_t k0 = blockIdx.x * (kRhoDDThreads * kRhoDDKPerThread) + threadIdx.x;
+    int32_t pk[kRhoDDKPerThread];
+    ddc acc[kRhoDDKPerThread];
+#pragma unroll
+    for (uint32_t j = 0; j < kRhoDDKPerThread; ++j) {
+        const uint32_t k = k0 + j * kRhoDDThreads;
+        pk[j] = k < K ? sys.kidx[k] : 0;
+        acc[j] = ddc{DD(0.f), DD(0.f)};
+    }
     for (uint32_t p0 = 0; p0 < ns; p0 += kRhoDDChunk) {
         const uint32_t cnt = min(kRhoDDChunk, ns - p0);
         __syncthreads();
@@ -159,10 +170,16 @@ __global__ void RhoDDKernel(const SystemDev sys, const double* __restrict__ pos,
             if (d < n_d && (int)n <= sys.max_index[d]) rtab[t] = PhaseDD(SplitDD(PosAt(pos, np, b, d, off + p0 + pi)), (int)n, iL, two_pi, tab256);
         }
         __syncthreads();
-        if (k < K)
-            for (uint32_t pi = 0; pi < cnt; ++pi) acc = CAdd(acc, PhaseProductDD(rtab + (size_t)pi * 3 * stride, stride, n_d, pk));
+        for (uint32_t pi = 0; pi < cnt; ++pi)
+#pragma unroll
+            for (uint32_t j = 0; j < kRhoDDKPerThread; ++j)
+                if (k0 + j * kRhoDDThreads < K) acc[j] = CAdd(acc[j], PhaseProductDD(rtab + (size_t)pi * 3 * stride, stride, n_d, pk[j]));
     }
-    if (k < K) rho[((size_t)slot * sys.M + b) * K + k] = Pack(acc);
+#pragma unroll
+    for (uint32_t j = 0; j < kRhoDDKPerThread; ++j) {
+        const uint32_t k = k0 + j * kRhoDDThreads;
+        if (k < K) rho[((size_t)slot * sys.M + b) * K + k] = Pack(acc[j]);
+    }
 }
 
 /// Ewald forces: one warp per (slice, particle), lanes over the stored k-vectors in double-float;
@@ -323,7 +340,8 @@ const float4* Context::ScratchRho(const double* pos) {
     dd iL, two_pi;
     SplitDouble(sys.iL, iL.hi, iL.lo);
     SplitDouble(2. * M_PI, two_pi.hi, two_pi.lo);
-    RhoDDKernel<<<dim3((sys.K + 127) / 128, sys.M, rho_slots), 128, smem, stream>>>(sys, pos, reinterpret_cast<const int*>(dss),
+    const uint32_t k_per_block = kRhoDDThreads * kRhoDDKPerThread;
+    RhoDDKernel<<<dim3((sys.K + k_per_block - 1) / k_per_block, sys.M, rho_slots), kRhoDDThreads, smem, stream>>>(sys, pos, reinterpret_cast<const int*>(dss),
                                                                                      phase_tab_->as<float4>(), iL, two_pi, rho_scratch_->as<float4>());
     CudaCheck(cudaGetLastError(), "rho launch");
     return rho_scratch_->as<float4>();
