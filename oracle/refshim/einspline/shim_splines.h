@@ -1,5 +1,5 @@
 // Reference build shim (test infrastructure): the einspline entry points simpimc's headers call
-// (SURVEY-listed call sites in free_spline_class.h, bare/ilkka/david_pair_action_class.h). einspline
+// (call sites in free_spline_class.h and bare/ilkka/david_pair_action_class.h). einspline
 // is fetched from an unpinned tarball at configure time and is not in the checkout, so its
 // {NATURAL, NATURAL} interpolants are restated from their mathematical definition: the natural
 // cubic spline through the data (second derivative zero at both ends), here in the first-derivative
