@@ -19,43 +19,16 @@ namespace {
 __device__ __forceinline__ uint32_t BeadLoop(uint32_t b, uint32_t M) { return b >= M ? b - M : b; }
 
 // InitRhoK (species_class.h:380-403): rho(b, k) = sum over particles in index order of the bead
-// phases. One block per (slot, slice); particles are processed in chunks whose phase tables are
-// staged in shared memory.
-constexpr int kRhoChunk = 16;
-
-__global__ void InitRhoKernel(const SystemDev sys, const int* __restrict__ slot_species) {
-    extern __shared__ double2 tab[];  // [kRhoChunk][3][stride]
-    const int slot = blockIdx.y;
-    const uint32_t b = blockIdx.x;
-    const uint32_t s = (uint32_t)slot_species[slot];
-    const int stride = max(max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
-    double2* rho = sys.rho_k + ((size_t)slot * sys.M + b) * sys.K;
-    for (uint32_t k = threadIdx.x; k < sys.K; k += blockDim.x) rho[k] = make_double2(0., 0.);
-    const uint32_t np = sys.sp_n[s];
-    for (uint32_t p0 = 0; p0 < np; p0 += kRhoChunk) {
-        const uint32_t cnt = min((uint32_t)kRhoChunk, np - p0);
-        __syncthreads();
-        for (uint32_t t = threadIdx.x; t < cnt * sys.n_d; t += blockDim.x) {
-            const uint32_t pi = t / sys.n_d, d = t % sys.n_d;
-            const double x = PosAt(sys.pos, sys.n_pad, b, d, sys.sp_off[s] + p0 + pi);
-            PhaseRow(x, sys.box[d], sys.max_index[d], tab + ((size_t)pi * 3 + d) * stride);
-        }
-        __syncthreads();
-        for (uint32_t k = threadIdx.x; k < sys.K; k += blockDim.x) {
-            const int32_t pk = sys.kidx[k];
-            double2 acc = rho[k];
-            for (uint32_t pi = 0; pi < cnt; ++pi) {
-                const double2 e = PhaseProduct(tab + (size_t)pi * 3 * stride, stride, sys.n_d, pk);
-                acc.x += e.x;
-                acc.y += e.y;
-            }
-            rho[k] = acc;
-        }
+// phases, formed in double-float by the densities kernel of the adjoint (Context::ScratchRho: one
+// block per (1024 k-vectors, slice, slot), the particles' phase rows staged in shared memory) and
+// rounded to FP64 here.
+__global__ void DDToDoubleKernel(const float4* __restrict__ in, double2* __restrict__ out, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float4 v = in[i];
+        out[i] = make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
     }
 }
 
-// Per-slice densities of a proposal (species_class.h:406-425 in NEW mode): for each slice of the
-// segment, the committed density plus (new - old) phases of the listed particles, in list order.
 __global__ void ProposalRhoKernel(const SystemDev sys, uint32_t species, const uint32_t* __restrict__ parts, uint32_t n_parts,
                                   uint32_t b0, uint32_t skip, double2* __restrict__ out) {
     extern __shared__ double2 tab[];  // [2][3][stride]
@@ -173,17 +146,9 @@ __global__ void IlkkaLongGradKernel(const SystemDev sys, const double* __restric
 // ---------------------------------------------------------------------------------------------
 void Context::ComputeRho(const double* pos, double2* out) {
     if (!rho_slots || !sys.K) return;
-    std::vector<int> slot_species(rho_slots, 0);
-    for (uint32_t s = 0; s < sys.S; ++s)
-        if (sys.sp_rho[s] >= 0) slot_species[sys.sp_rho[s]] = (int)s;
-    uint32_t* dss = Parts(rho_slots);
-    CudaCheck(cudaMemcpyAsync(dss, slot_species.data(), rho_slots * sizeof(int), cudaMemcpyHostToDevice, stream), "slot upload");
-    const int stride = std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
-    const size_t smem = (size_t)kRhoChunk * 3 * stride * sizeof(double2);
-    SystemDev s2 = sys;
-    s2.pos = const_cast<double*>(pos);
-    s2.rho_k = out;
-    InitRhoKernel<<<dim3(sys.M, rho_slots), 256, smem, stream>>>(s2, reinterpret_cast<const int*>(dss));
+    const float4* r = ScratchRho(pos);
+    const size_t n = (size_t)rho_slots * sys.M * sys.K;
+    DDToDoubleKernel<<<(unsigned)std::min<size_t>((n + 255) / 256, (size_t)n_sm * 16), 256, 0, stream>>>(r, out, n);
     CudaCheck(cudaGetLastError(), "init rho_k launch");
     Sync();
 }
