@@ -15,7 +15,7 @@ from each chain's seed, then untimed warm-up cycles.
 Also reported on the same line:
   components         the bisection sweep kernel and the HMC kernel timed alone (bead-moves/s each,
                      HMC acceptance), with a roofline for each;
-  plain_same_system  the single-chain GPU path (double-float sweep kernel, FP64 HMC) running the
+  plain_same_system  the single-chain GPU path (double-float sweep kernel, FP64-grade HMC) running the
                      same cycle on a sample of the same chains, one chain at a time (what the
                      batched kernels replace);
   same_shape_chains  152 chains of the heaviest shape (N = 127, M = 128) swept as one batch and as
@@ -175,7 +175,7 @@ def batch_algorithmic_bytes(batch, att, acc):
 
 
 def time_plain_chains(items, tmp, local, sample, cycles=2):
-    """The single-chain GPU path (double-float sweep kernel, FP64 HMC) running the batch's cycle on
+    """The single-chain GPU path (double-float sweep kernel, FP64-grade HMC) running the batch's cycle on
     `sample` chains, one after the other: device time and bead-moves."""
     import torch
     from simpimc_gb300 import Simulation
@@ -201,7 +201,7 @@ def time_plain_chains(items, tmp, local, sample, cycles=2):
 
 
 def energy_gate(items, tmp, local, chains, equil, cycles, hmc=True):
-    """Batched FP32 chains against the single-chain path (double-float bisection, FP64 HMC) on the same
+    """Batched FP32 chains against the single-chain path (double-float bisection, FP64-grade HMC) on the same
     chains and seeds: `equil` untimed cycles to equilibrate the paths, then per chain the mean energy
     and its blocking error bar over `cycles` measurements (one per cycle). With hmc=False the cycle is
     the bisection sweep alone: both paths then make the same accept decisions, so the two series
@@ -410,7 +410,7 @@ def hmc_adjoint(local, tmp, attempts=4, equil_sweeps=10):
            "gradient_s_host_timed": grad_s, "acceptance": (c1[3] - c0[3]) / max(c1[0] - c0[0], 1),
            "value": beads * attempts / (ms / 1e3), "unit": METRIC,
            "equilibration": f"{equil_sweeps} bisection sweeps (level 4) from the classical start",
-           "note": "one HMC attempt moves all 32768 beads; 11 gradient and 2 whole-ring action evaluations per attempt, FP64"}
+           "note": "one HMC attempt moves all 32768 beads; 11 gradient and 2 whole-ring action evaluations per attempt; densities, Ewald sums and pair forces in double-float, other terms and totals FP64"}
     s.close()
     return out
 
@@ -721,7 +721,7 @@ def run_ours(args):
     sample = list(range(0, N_CHAINS, N_CHAINS // 8))
     pm, psec = time_plain_chains(items, tmp, local, sample)
     plain = {"value": pm / psec, "unit": METRIC, "chains": sample,
-             "note": "single-chain path (double-float sweep kernel + FP64 HMC), the same cycle, one chain after another, device time"}
+             "note": "single-chain path (double-float sweep kernel + FP64-grade HMC), the same cycle, one chain after another, device time"}
     mid = sorted(range(N_CHAINS), key=lambda c: batch.shapes[c][0] ** 2 * batch.shapes[c][1])
     gate_chains = [mid[len(mid) // 8], mid[len(mid) // 4], mid[3 * len(mid) // 8], mid[len(mid) // 2]]
     gate = energy_gate(items, tmp, local, chains=gate_chains, equil=args.gate_equil, cycles=args.gate_sweeps)

@@ -280,6 +280,7 @@ class Context {
     };
     std::vector<StageTable> stage_tables_;  // spline tables the sweep may copy into shared memory
     void BuildSweepTables();
+    void PairGradDD(uint32_t pair, const double* pos, double* grad);  // double-float short-range pair forces (sweep.cu)
     std::unique_ptr<DeviceBuffer> pos_, pos_new_, rho_, kidx_;
     std::unique_ptr<DeviceBuffer> grad_, mom_, pos_save_, rho_scratch_, phase_tab_;  // adjoint / HMC work arrays
     std::vector<std::unique_ptr<DeviceBuffer>> adj_vk_;                              // double-float v_k per action

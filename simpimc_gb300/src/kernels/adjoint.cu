@@ -100,39 +100,6 @@ __global__ void TrapGradKernel(const SystemDev sys, const double* __restrict__ p
     }
 }
 
-/// Short-range pair forces: one thread per (slice, particle of either species of the action).
-__global__ void PairGradKernel(const SystemDev sys, const double* __restrict__ pos, const PairDev pa, double* __restrict__ grad) {
-    const uint32_t na = sys.sp_n[pa.sa], nb = sys.sp_n[pa.sb], M = sys.M, np = sys.n_pad, n_d = sys.n_d;
-    const bool hom = pa.sa == pa.sb;
-    const uint32_t ng = hom ? na : na + nb;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (uint64_t)ng * M; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t b = (uint32_t)(i / ng), j = (uint32_t)(i % ng);
-        const bool in_a = j < na;
-        const uint32_t g = in_a ? sys.sp_off[pa.sa] + j : sys.sp_off[pa.sb] + (j - na);
-        const uint32_t q0 = in_a ? sys.sp_off[pa.sb] : sys.sp_off[pa.sa];
-        const uint32_t nq = in_a ? nb : na;
-        double rg[3], G[3] = {0., 0., 0.};
-        for (uint32_t d = 0; d < n_d; ++d) rg[d] = PosAt(pos, np, b, d, g);
-        for (uint32_t qi = 0; qi < nq; ++qi) {
-            const uint32_t q = q0 + qi;
-            if (q == g) continue;
-            double dr[3], r2 = 0.;
-            for (uint32_t d = 0; d < n_d; ++d) {
-                dr[d] = MinImage(rg[d] - PosAt(pos, np, b, d, q), sys.L, sys.iL);
-                r2 += dr[d] * dr[d];
-            }
-            const double r = sqrt(r2);
-            double v, dv;
-            PairVBead(pa, r, v, dv);
-            if (r > 0.) {
-                const double f = sys.tau * dv / r;
-                for (uint32_t d = 0; d < n_d; ++d) G[d] += f * dr[d];
-            }
-        }
-        for (uint32_t d = 0; d < n_d; ++d) grad[GIdx(b, d, g, np)] += G[d];
-    }
-}
-
 __device__ __forceinline__ dd SplitDD(double x) {
     const float h = (float)x;
     return dd{h, (float)(x - (double)h)};
@@ -402,7 +369,7 @@ double Context::TotalActionDev(int a, const double* pos, const float4* rho) {
             const bool hom = pa.sa == pa.sb;
             // tau V(|d_b|) per pair and slice, d_b the minimum image on that slice: the two half
             // links of CalcU that meet at a bead, with each end's distance taken as its own minimum
-            // image (the function PairGradKernel differentiates).
+            // image (the function the double-float pair-force kernel differentiates).
             SumItems<1>(*this, (uint64_t)na * nb * M, [=] __device__(uint64_t it, double* v) {
                 const uint32_t q = (uint32_t)(it % nb);
                 const uint64_t r0 = it / nb;
@@ -456,9 +423,9 @@ void Context::GradientDev(int a, const double* pos, const float4* rho, double* g
         } else {
             const PairDev pa = sys.pair[ah.index];
             if (pa.is_constant) continue;
-            const uint64_t ng = (uint64_t)(pa.sa == pa.sb ? sys.sp_n[pa.sa] : sys.sp_n[pa.sa] + sys.sp_n[pa.sb]) * sys.M;
-            PairGradKernel<<<Blocks(*this, ng, th), th, 0, stream>>>(sys, pos, pa, grad);
+            PairGradDD(ah.index, pos, grad);
             if (pa.use_long_range && rho && sys.K && !fused_ewald) {
+                const uint64_t ng = (uint64_t)(pa.sa == pa.sb ? sys.sp_n[pa.sa] : sys.sp_n[pa.sa] + sys.sp_n[pa.sb]) * sys.M;
                 const float4* ra = rho + (size_t)sys.sp_rho[pa.sa] * sys.M * sys.K;
                 const float4* rb = rho + (size_t)sys.sp_rho[pa.sb] * sys.M * sys.K;
                 const int stride = std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;

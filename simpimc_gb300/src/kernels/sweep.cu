@@ -195,6 +195,75 @@ __device__ __forceinline__ dd EvalCubicDD(const CubicDD& t, dd x) {
     return Add(dd{a.x, a.y}, Mul(u, v));
 }
 
+/// d/dx of EvalCubicDD: zero outside the grid, where EvalCubicDD holds the end value.
+__device__ __forceinline__ dd EvalCubicDerivDD(const CubicDD& t, dd x) {
+    if (Less(x, t.x0) || Less(t.x1, x)) return DD(0.f);
+    int i;
+    if (t.uniform) {
+        i = (int)floorf(__fmul_rn(__fsub_rn(x.hi, t.x0f), t.inv_dxf));
+        i = min(max(i, 0), t.n - 2);
+    } else {
+        int j = (int)floorf(__fmul_rn(__fsub_rn(x.hi, t.x0f), t.inv_dxf));
+        j = min(max(j, 0), t.n_bucket - 1);
+        i = t.bucket[j];
+    }
+    while (i < t.n - 2 && !Less(x, LoadDD(&t.x[i + 1]))) ++i;
+    while (i > 0 && Less(x, LoadDD(&t.x[i]))) --i;
+    const float4 a = t.c[2 * i], b = t.c[2 * i + 1];
+    const dd u = Sub(x, LoadDD(&t.x[i]));
+    // c1 + u (2 c2 + 3 u c3)
+    return Add(dd{a.z, a.w}, Mul(u, Add(Scale2(dd{b.x, b.y}, 2.f), Mul(u, MulF(dd{b.z, b.w}, 3.f)))));
+}
+
+__device__ __forceinline__ dd SplitToDD(double x) {
+    const float h = (float)x;
+    return dd{h, (float)(x - (double)h)};
+}
+
+/// Short-range pair forces of the whole-ring action in double-float (BarePairAction::CalcV's
+/// per-bead V(r) with the reference's two clamps, bare_pair_action_class.h:98-111): one thread per
+/// (slice, particle of either species), tau V'(r) / r (r_g - r_q) summed over the partners in order.
+__global__ void PairGradDDKernel(const SystemDev sys, const double* __restrict__ pos, const PairDD* __restrict__ pdd, uint32_t pair,
+                                 double* __restrict__ grad) {
+    const PairDD& pa = pdd[pair];
+    const uint32_t na = sys.sp_n[pa.sa], nb = sys.sp_n[pa.sb], M = sys.M, np = sys.n_pad, n_d = sys.n_d;
+    const bool hom = pa.sa == pa.sb;
+    const uint32_t ng = hom ? na : na + nb;
+    const dd L = SplitToDD(sys.L), iL = SplitToDD(sys.iL), tau = SplitToDD(sys.tau);
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (uint64_t)ng * M; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = (uint32_t)(i / ng), j = (uint32_t)(i % ng);
+        const bool in_a = j < na;
+        const uint32_t g = in_a ? sys.sp_off[pa.sa] + j : sys.sp_off[pa.sb] + (j - na);
+        const uint32_t q0 = in_a ? sys.sp_off[pa.sb] : sys.sp_off[pa.sa];
+        const uint32_t nq = in_a ? nb : na;
+        dd rg[3], G[3] = {DD(0.f), DD(0.f), DD(0.f)};
+#pragma unroll
+        for (uint32_t d = 0; d < 3; ++d) rg[d] = d < n_d ? SplitToDD(PosAt(pos, np, b, d, g)) : DD(0.f);
+        for (uint32_t qi = 0; qi < nq; ++qi) {
+            const uint32_t q = q0 + qi;
+            if (q == g) continue;
+            dd dr[3], r2 = DD(0.f);
+#pragma unroll
+            for (uint32_t d = 0; d < 3; ++d) {
+                dr[d] = d < n_d ? MinImageDD(Sub(rg[d], SplitToDD(PosAt(pos, np, b, d, q))), L, iL) : DD(0.f);
+                r2 = Add(r2, Sqr(dr[d]));
+            }
+            if (!(r2.hi > 0.f)) continue;  // coincident beads: no direction (the FP64 form skips r = 0)
+            const dd r = Sqrt(r2);
+            const bool in1 = !Less(r, pa.rvmin) && !Less(pa.rvmax, r);
+            if (!in1) continue;  // V is clamped there: no force from either part
+            dd dv = pa.is_coulomb ? Neg(Div(DD(1.f), r2)) : EvalCubicDerivDD(pa.v_r, r);
+            if (pa.use_lr && !Less(r, pa.rvlmin) && !Less(pa.rvlmax, r)) dv = Sub(dv, EvalCubicDerivDD(pa.v_long_r, r));
+            const dd f = Div(Mul(tau, dv), r);
+#pragma unroll
+            for (uint32_t d = 0; d < 3; ++d) G[d] = Add(G[d], Mul(f, dr[d]));
+        }
+#pragma unroll
+        for (uint32_t d = 0; d < 3; ++d)
+            if (d < n_d) grad[((size_t)b * 3 + d) * np + g] += ToDouble(G[d]);
+    }
+}
+
 /// Cell of one 2-D table axis holding x (the last knot at or below x, within [0, n - 2]).
 __device__ __forceinline__ int GridCellDD(const float2* g, const int32_t* bucket, int n, int nb, float x0f, float inv_dxf, dd x0, dd x1, dd x) {
     const dd xc = Min(Max(x, x0), x1);
@@ -1588,6 +1657,17 @@ void Context::BuildSweepTables() {
 // cofactors, pair indices) in the sweep's descriptor buffer, rebuilt when a level changes
 // (adaptive bisection between blocks). Returns the buffer: [kMaxMoves] MoveDD, then the schedule
 // and counters the sweep kernel uses.
+void Context::PairGradDD(uint32_t pair, const double* pos, double* grad) {
+    BuildSweepTables();
+    const PairDD* pdd = reinterpret_cast<const PairDD*>(sweep_tables_->as<char>() + sizeof(float4) * 256);
+    const PairDev& pa = sys.pair[pair];
+    const uint64_t ng = (uint64_t)(pa.sa == pa.sb ? sys.sp_n[pa.sa] : sys.sp_n[pa.sa] + sys.sp_n[pa.sb]) * sys.M;
+    const int th = 128;
+    const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((ng + th - 1) / th, (uint64_t)n_sm * 32));
+    PairGradDDKernel<<<blocks, th, 0, stream>>>(sys, pos, pdd, pair, grad);
+    CudaCheck(cudaGetLastError(), "pair gradient launch");
+}
+
 void* Context::MoveDescriptors() {
     BuildSweepTables();
     for (size_t m = 0; m < moves.size(); ++m)
