@@ -71,6 +71,7 @@ def lib():
             "oracle_run": [C.c_void_p],
             "oracle_n_blocks": [C.c_void_p, C.c_uint32, _U64P],
             "oracle_get_block": [C.c_void_p, C.c_uint32, C.c_uint64, _DP, C.c_uint64, _U64P],
+            "oracle_move_writes": [C.c_void_p, C.c_uint32, C.POINTER(C.c_int64), C.c_uint64, _U64P, _U64P],
             "oracle_philox": [_U32P, _U32P, _U32P],
             "oracle_perm_stats": [C.c_void_p, C.c_uint32, _U64P],
             "oracle_get_perm": [C.c_void_p, C.c_uint32, _U32P],
@@ -98,6 +99,27 @@ def bisect_draws(seed, chain, move, attempt, n_part, n_bead, n_level):
     fn(seed, chain, move, attempt, n_part, n_bead, n_level, pb.ctypes.data_as(_U32P), z.ctypes.data_as(C.POINTER(C.c_float)),
        lu.ctypes.data_as(C.POINTER(C.c_float)))
     return pb, z, lu
+
+
+def perm_draws(seed, chain, move, attempt, n_part, n_bead, n_level):
+    """Draws of one permuting-bisection attempt in the order the reference's moves consume them:
+    (first bead, iterative cycle's first particle), the iterative walk's uniforms [N, 2]
+    (continuation, choice per step), the table's selection uniform, normals [N (2^l - 1), 3] in
+    sampling order, the level tests' log-uniforms (top level first) and the table's final uniform."""
+    L = lib()
+    fn = L.oracle_perm_draws
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, _U32P, _DP,
+                   C.POINTER(C.c_float), C.POINTER(C.c_float), _DP]
+    B = 1 << n_level
+    idx = np.zeros(2, dtype=np.uint32)
+    sel = np.zeros(2 * n_part + 1)
+    z = np.zeros((n_part * (B - 1), 3), dtype=np.float32)
+    lu = np.zeros(n_level, dtype=np.float32)
+    fin = np.zeros(1)
+    fn(seed, chain, move, attempt, n_part, n_bead, n_level, idx.ctypes.data_as(_U32P), sel.ctypes.data_as(_DP),
+       z.ctypes.data_as(C.POINTER(C.c_float)), lu.ctypes.data_as(C.POINTER(C.c_float)), fin.ctypes.data_as(_DP))
+    return idx, sel[:2 * n_part].reshape(n_part, 2), float(sel[2 * n_part]), z, lu, float(fin[0])
 
 
 def philox(ctr, key):
@@ -255,6 +277,14 @@ class OracleSim:
 
     def run(self):
         self._ok(self._L.oracle_run(self._h))
+
+    def move_writes(self, move, cap=1 << 20):
+        """Rows recorded at each Write of run(): (n_attempt, n_accept, level or -1), then for a
+        permuting move its per-cycle-length attempts and accepts."""
+        buf = np.zeros(cap, dtype=np.int64)
+        n, k = C.c_uint64(), C.c_uint64()
+        self._ok(self._L.oracle_move_writes(self._h, move, buf.ctypes.data_as(C.POINTER(C.c_int64)), cap, C.byref(n), C.byref(k)))
+        return buf[: n.value * k.value].reshape(n.value, k.value).copy()
 
     def blocks(self, obs, cap=1 << 20):
         n = C.c_uint64()

@@ -2727,6 +2727,10 @@ struct Simulation {
     std::vector<uint64_t> obs_calls;
     LoopNode main_loop;
     std::vector<std::vector<std::vector<double>>> blocks;  // per observable, per block
+    // per move, per Write: {n_attempt, n_accept, bisection level (adaptive moves; else -1)}, then the
+    // per-cycle-length attempts and accepts of a permuting move (move_class.h:80-94,
+    // perm_bisect_class.h:119-132)
+    std::vector<std::vector<std::vector<int64_t>>> move_writes;
 
     Simulation(const Input& in, const std::string& bd, uint32_t chain_id) : base_dir(bd), chain(chain_id) {
         Input rng = in.GetChild("RNG");
@@ -2828,7 +2832,19 @@ struct Simulation {
             auto v = observables[i]->Block();
             if (!v.empty()) blocks[i].push_back(v);
         }
-        for (auto& m : moves) m->ResetBlock();
+        move_writes.resize(moves.size());
+        for (size_t i = 0; i < moves.size(); ++i) {
+            Move* m = moves[i].get();
+            std::vector<int64_t> row{(int64_t)m->n_attempt, (int64_t)m->n_accept, -1};
+            if (auto* b = dynamic_cast<Bisect*>(m))
+                if (b->adaptive) row[2] = b->n_level;
+            if (auto* pb = dynamic_cast<PermBisect*>(m)) {
+                row.insert(row.end(), pb->perm_attempt.begin(), pb->perm_attempt.end());
+                row.insert(row.end(), pb->perm_accept.begin(), pb->perm_accept.end());
+            }
+            move_writes[i].push_back(row);
+            m->ResetBlock();
+        }
     }
 
     void RunNode(const LoopNode& n) {
@@ -3102,6 +3118,20 @@ int oracle_n_blocks(void* h, uint32_t o, uint64_t* n) {
     return 0;
 }
 
+// Rows recorded at each Write of the last run for move m: {n_attempt, n_accept, level or -1}, and
+// for a permuting move its per-cycle-length attempts then accepts (N each); row-major into out.
+int oracle_move_writes(void* h, uint32_t m, int64_t* out, uint64_t cap, uint64_t* n_rows, uint64_t* row_len) {
+    auto* s = S(h);
+    if (m >= s->moves.size()) return -1;
+    *n_rows = m < s->move_writes.size() ? s->move_writes[m].size() : 0;
+    *row_len = *n_rows ? s->move_writes[m][0].size() : 0;
+    uint64_t k = 0;
+    for (uint64_t r = 0; r < *n_rows; ++r)
+        for (int64_t v : s->move_writes[m][r])
+            if (k < cap) out[k++] = v;
+    return 0;
+}
+
 int oracle_get_block(void* h, uint32_t o, uint64_t blk, double* out, uint64_t cap, uint64_t* n) {
     if (o >= S(h)->blocks.size() || blk >= S(h)->blocks[o].size()) return -1;
     const auto& v = S(h)->blocks[o][blk];
@@ -3126,6 +3156,38 @@ int oracle_bisect_draws(uint32_t seed, uint32_t chain, uint32_t move, uint64_t a
         orc::boxmuller(w.w[2], w.w[3], z[3 * i + 2], z3);
     }
     for (uint32_t li = 0; li < n_level; ++li) logu[li] = orc::logf_spec(orc::u24(st.block(1u + (B - 1u) + li).w[0]));
+    return 0;
+}
+
+// Draws of one permuting-bisection attempt (the layout above PermBisect), in the order the
+// reference's PermBisectIterative / PermBisectTable consume them: idx = {first bead, the iterative
+// cycle's first particle}; sel[2 N] = each cycle step's continuation and choice uniforms, then
+// sel[2 N] = the table's selection uniform; z = the 3 normals of each of the N (B - 1) midpoints in
+// sampling order; logu = the level tests' logarithms, top level first; fin = the table's final
+// uniform.
+int oracle_perm_draws(uint32_t seed, uint32_t chain, uint32_t move, uint64_t attempt, uint32_t n_part, uint32_t n_bead, uint32_t n_level,
+                      uint32_t* idx, double* sel, float* z, float* logu, double* fin) {
+    orc::Stream st{seed, chain, move, attempt};
+    const orc::RNG4 w0 = st.block(0);
+    const uint32_t N = n_part, B = 1u << n_level;
+    idx[0] = orc::uidx(w0.w[0], n_bead);
+    idx[1] = orc::uidx(w0.w[1], N);
+    for (uint32_t j = 0; j < N; ++j) {
+        const orc::RNG4 w = st.block(1u + j);
+        sel[2 * j] = orc::u53(w.w[0], w.w[1]);
+        sel[2 * j + 1] = orc::u53(w.w[2], w.w[3]);
+    }
+    sel[2 * N] = orc::u53(w0.w[2], w0.w[3]);
+    const uint32_t base_m = 1u + N, base_u = base_m + N * (B - 1u);
+    for (uint32_t c = 0; c < N * (B - 1u); ++c) {
+        const orc::RNG4 w = st.block(base_m + c);
+        float z3;
+        orc::boxmuller(w.w[0], w.w[1], z[3 * c], z[3 * c + 1]);
+        orc::boxmuller(w.w[2], w.w[3], z[3 * c + 2], z3);
+    }
+    for (uint32_t l = 0; l < n_level; ++l) logu[l] = orc::logf_spec(orc::u24(st.block(base_u + l).w[0]));
+    const orc::RNG4 wf = st.block(base_u + n_level);
+    fin[0] = orc::u53(wf.w[0], wf.w[1]);
     return 0;
 }
 

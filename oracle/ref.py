@@ -70,6 +70,9 @@ def lib():
             "refsim_virial_energy": [C.c_void_p, C.c_uint32, C.c_double, _DP],
             "refsim_move_attempt": [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, _DP, C.c_uint32, _DP, C.c_uint32],
             "refsim_move_counters": [C.c_void_p, C.c_uint32, _U64P],
+            "refsim_perm_attempt": [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, _DP, C.c_uint32, _DP, C.c_uint32, _DP, C.c_uint32],
+            "refsim_perm_counters": [C.c_void_p, C.c_uint32, _U64P],
+            "refsim_get_perm": [C.c_void_p, C.c_uint32, _U32P],
             "refsim_move_write": [C.c_void_p, C.c_uint32, C.POINTER(C.c_int64)],
             "refsim_obs_accumulate": [C.c_void_p, C.c_uint32],
             "refsim_obs_write": [C.c_void_p, C.c_uint32, _DP, C.c_uint64, _U64P],
@@ -88,17 +91,22 @@ def _seed_of(xml: str) -> int:
     return int(m.group(1)) if m else 0
 
 
-def _bisect_moves(xml: str):
-    """(species name, n_level) of each Bisect move, in input order."""
+MOVE_TYPES = ("Bisect", "PermBisectIterative", "PermBisectTable")
+
+
+def _moves(xml: str):
+    """(type, species name, n_level) of each move the harness builds, in input order."""
     import re
     out = []
     for m in re.finditer(r"<Move\s[^>]*>", xml):
         tag = m.group(0)
-        if 'type="Bisect"' not in tag:
+        t = re.search(r'type="([^"]+)"', tag)
+        if t is None or t.group(1) not in MOVE_TYPES:  # the Algorithm's event tags carry no type
             continue
+        t = t.group(1)
         sp = re.search(r'species="([^"]+)"', tag).group(1)
         lvl = int(re.search(r'n_level="(\d+)"', tag).group(1))
-        out.append((sp, lvl))
+        out.append((t, sp, lvl))
     return out
 
 
@@ -119,7 +127,7 @@ class RefSim:
         import re
         names = re.findall(r'<Species\s[^>]*name="([^"]+)"[^>]*n_part="(\d+)"', xml)
         self._species = {n: (i, int(c)) for i, (n, c) in enumerate(names)}
-        self._moves = _bisect_moves(xml)
+        self._moves = _moves(xml)
         self._attempts = [0] * len(self._moves)
 
     def _ok(self, rc):
@@ -196,18 +204,40 @@ class RefSim:
         return out.value
 
     def move_attempts(self, move, n):
-        """n Move::DoEvent calls of Bisect move `move` with the oracle's draws for its next attempts."""
+        """n Move::DoEvent calls of move `move` (Bisect or a permuting bisection) with the oracle's
+        draws for its next attempts."""
         import oracle
-        sp_name, _ = self._moves[move]
+        kind, sp_name, _ = self._moves[move]
         _, n_part = self._species[sp_name]
         for _ in range(n):
             n_level = self.move_level(move)
-            pb, z, lu = oracle.bisect_draws(self._seed, self._chain, move, self._attempts[move], n_part, self.n_bead, n_level)
-            zz = np.ascontiguousarray(z, dtype=np.float64)
-            uu = np.exp(np.asarray(lu, dtype=np.float64))
-            self._ok(self._L.refsim_move_attempt(self._h, move, int(pb[0]), int(pb[1]), zz.ctypes.data_as(_DP), len(zz),
-                                                 uu.ctypes.data_as(_DP), len(uu)))
+            a = self._attempts[move]
+            if kind == "Bisect":
+                pb, z, lu = oracle.bisect_draws(self._seed, self._chain, move, a, n_part, self.n_bead, n_level)
+                zz = np.ascontiguousarray(z, dtype=np.float64)
+                uu = np.exp(np.asarray(lu, dtype=np.float64))
+                self._ok(self._L.refsim_move_attempt(self._h, move, int(pb[0]), int(pb[1]), zz.ctypes.data_as(_DP), len(zz),
+                                                     uu.ctypes.data_as(_DP), len(uu)))
+            else:
+                idx, steps, sel_table, z, lu, fin = oracle.perm_draws(self._seed, self._chain, move, a, n_part, self.n_bead, n_level)
+                sel = np.ascontiguousarray(steps.reshape(-1) if kind == "PermBisectIterative" else [sel_table], dtype=np.float64)
+                zz = np.ascontiguousarray(z, dtype=np.float64)
+                uu = np.ascontiguousarray(np.concatenate([np.exp(np.asarray(lu, dtype=np.float64)), [fin]]))
+                self._ok(self._L.refsim_perm_attempt(self._h, move, int(idx[0]), int(idx[1]), zz.ctypes.data_as(_DP), len(zz),
+                                                     sel.ctypes.data_as(_DP), len(sel), uu.ctypes.data_as(_DP), len(uu)))
             self._attempts[move] += 1
+
+    def perm_stats(self, move, n_part):
+        """Per cycle length: the permuting move's attempts and accepts in its current block."""
+        out = np.zeros(2 * n_part, dtype=np.uint64)
+        self._ok(self._L.refsim_perm_counters(self._h, move, out.ctypes.data_as(_U64P)))
+        return out[:n_part].astype(np.int64), out[n_part:].astype(np.int64)
+
+    def get_perm(self, species, n_part):
+        """The path permutation at the ring closure (particle p's last bead links to slice 0 of out[p])."""
+        out = np.zeros(n_part, dtype=np.uint32)
+        self._ok(self._L.refsim_get_perm(self._h, species, out.ctypes.data_as(_U32P)))
+        return out.astype(np.int64)
 
     def _counters(self, move):
         out = np.zeros(3, dtype=np.uint64)
@@ -242,13 +272,15 @@ class RefSim:
         """Simulation::Run (simulation_class.h:42-45): the input's <Algorithm> loop of Move, Observable
         and Write events (loop_class.h:34-60; a Write writes every move, then every observable,
         write_class.h:31-42), one attempt per Move event. Returns ({move: [(n_attempt, n_accept,
-        n_level)] per Write}, {observable: [block] per Write that appended one})."""
+        n_level)] per Write}, {observable: [block] per Write that appended one}, {permuting move:
+        [(attempts, accepts) per cycle length] per Write})."""
         import xml.etree.ElementTree as ET
         root = ET.fromstring(xml)
-        moves = [m.get("name") for m in root.find("Moves") if m.get("type") == "Bisect"]
+        moves = [m.get("name") for m in root.find("Moves") if m.get("type") in MOVE_TYPES]
         obs = [o.get("name") for o in root.find("Observables") if o.get("type") in ("Energy", "PairCorrelation", "StructureFactor")]
         mstats = {i: [] for i in range(len(moves))}
         blocks = {i: [] for i in range(len(obs))}
+        pstats = {i: [] for i, mv in enumerate(self._moves) if mv[0] != "Bisect"}
 
         def loop(node):
             for _ in range(int(node.get("n_step", "1"))):
@@ -259,6 +291,8 @@ class RefSim:
                         self.observable_accumulate(obs.index(ev.get("name")))
                     elif ev.tag == "Write":
                         for m in range(len(moves)):
+                            if m in pstats:  # the block's counters, which the Write appends and resets
+                                pstats[m].append(np.stack(self.perm_stats(m, self._species[self._moves[m][1]][1])))
                             mstats[m].append(self.move_write(m))
                         for o in range(len(obs)):
                             b = self.observable_block(o)
@@ -268,4 +302,4 @@ class RefSim:
                         loop(ev)
 
         loop(root.find("Algorithm"))
-        return mstats, blocks
+        return mstats, blocks, pstats

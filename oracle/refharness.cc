@@ -7,8 +7,8 @@
 //
 // Set-up follows Simulation's constructor (framework/simulation_class.h:16-39) with the factories
 // of actions.h, moves.h and observables.h restricted to the hot path's classes: Kinetic,
-// HarmonicTrap, BarePairAction, IlkkaPairAction, DavidPairAction; Bisect; Energy, PairCorrelation,
-// StructureFactor. Species start as init_type "Line" (species_class.h:311-321) and take their
+// HarmonicTrap, BarePairAction, IlkkaPairAction, DavidPairAction; Bisect, PermBisectIterative,
+// PermBisectTable; Energy, PairCorrelation, StructureFactor. Species start as init_type "Line" (species_class.h:311-321) and take their
 // positions from refsim_set_path. Move draws are scripted (refshim/scaffold/rng/rng.h).
 #include <sys/time.h>
 
@@ -44,6 +44,8 @@ using namespace scaffold::rand;
 #include "actions/single_action/trap_class.h"
 #include "data_structures/path_class.h"
 #include "events/moves/single_species_move/bisect/bisect_class.h"
+#include "events/moves/single_species_move/bisect/perm_bisect/perm_bisect_iterative_class.h"
+#include "events/moves/single_species_move/bisect/perm_bisect/perm_bisect_table_class.h"
 #include "events/observables/energy_class.h"
 #include "events/observables/pair_correlation_class.h"
 #include "events/observables/structure_factor_class.h"
@@ -108,6 +110,11 @@ struct MoveCounterAccess : Move {
 struct BisectLevelAccess : Bisect {
     static uint32_t Bisect::*Level() { return &BisectLevelAccess::n_level; }
 };
+// The per-cycle-length counters of PermBisect (perm_bisect_class.h:25-26).
+struct PermCounterAccess : PermBisect {
+    static vec<uint32_t> PermBisect::*Attempts() { return &PermCounterAccess::perm_attempt; }
+    static vec<uint32_t> PermBisect::*Accepts() { return &PermCounterAccess::perm_accept; }
+};
 
 }  // namespace
 
@@ -125,8 +132,11 @@ int refsim_create(const char* xml, const char* dir, void** out) {
         s->path.reset(new Path(0, s->in, s->out, s->rng));
         for (auto& a : s->in.GetChild("Actions").GetChildList("Action")) s->actions.push_back(MakeAction(a, s->out, *s->path));
         for (auto& m : s->in.GetChild("Moves").GetChildList("Move")) {
-            if (m.GetAttribute<std::string>("type") != "Bisect") continue;
-            s->moves.push_back(std::make_shared<Bisect>(*s->path, s->rng, s->actions, m, s->out));
+            const std::string type = m.GetAttribute<std::string>("type");
+            if (type == "Bisect") s->moves.push_back(std::make_shared<Bisect>(*s->path, s->rng, s->actions, m, s->out));
+            else if (type == "PermBisectIterative") s->moves.push_back(std::make_shared<PermBisectIterative>(*s->path, s->rng, s->actions, m, s->out));
+            else if (type == "PermBisectTable") s->moves.push_back(std::make_shared<PermBisectTable>(*s->path, s->rng, s->actions, m, s->out));
+            else continue;
             s->move_names.push_back(m.GetAttribute<std::string>("name"));
         }
         for (auto& o : s->in.GetChild("Observables").GetChildList("Observable")) {
@@ -281,6 +291,57 @@ int refsim_move_attempt(void* h, uint32_t m, uint32_t particle, uint32_t bead0, 
         for (uint32_t i = 0; i < n_u; ++i) s.rng.QueueUniform(u[i]);
         s.moves.at(m)->DoEvent();
         s.rng.Clear();
+    });
+}
+
+/// One Move::DoEvent of permuting move m (PermBisectIterative or PermBisectTable) with its draws:
+/// the first bead (0-based), the cycle's first particle (iterative only; ignored otherwise),
+/// `n_z` normal triples in sampling order (level, cycle particle, position along the path), the
+/// `n_sel` uniforms of the cycle selection (iterative: continuation and choice of each step in
+/// turn; table: the selection uniform) and the `n_u` uniforms drawn after sampling starts (level
+/// tests, top level first, then the table's final test).
+int refsim_perm_attempt(void* h, uint32_t m, uint32_t bead0, uint32_t particle, const double* z, uint32_t n_z, const double* sel,
+                        uint32_t n_sel, const double* u, uint32_t n_u) {
+    return Guard([&] {
+        RefSim& s = *S(h);
+        Move* mv = s.moves.at(m).get();
+        const bool iterative = dynamic_cast<PermBisectIterative*>(mv) != nullptr;
+        if (!iterative && !dynamic_cast<PermBisectTable*>(mv)) throw std::invalid_argument("not a permuting move");
+        s.rng.Clear();
+        s.rng.QueueIndex(bead0 + 1);
+        if (iterative) s.rng.QueueIndex(particle + 1);
+        for (uint32_t i = 0; i < n_z; ++i) s.rng.QueueNormal({z[3 * i], z[3 * i + 1], z[3 * i + 2]});
+        for (uint32_t i = 0; i < n_sel; ++i) s.rng.QueueSelectionUniform(sel[i]);
+        for (uint32_t i = 0; i < n_u; ++i) s.rng.QueueUniform(u[i]);
+        mv->DoEvent();
+        s.rng.Clear();
+    });
+}
+
+/// out[2 N] = the permuting move's attempts, then accepts, per cycle length in its current block.
+int refsim_perm_counters(void* h, uint32_t m, uint64_t* out) {
+    return Guard([&] {
+        auto* mv = dynamic_cast<PermBisect*>(S(h)->moves.at(m).get());
+        if (!mv) throw std::invalid_argument("not a permuting move");
+        const vec<uint32_t>& att = mv->*PermCounterAccess::Attempts();
+        const vec<uint32_t>& acc = mv->*PermCounterAccess::Accepts();
+        for (size_t i = 0; i < att.size(); ++i) {
+            out[i] = att(i);
+            out[att.size() + i] = acc(i);
+        }
+    });
+}
+
+/// out[p] = the particle whose slice-0 bead follows particle p's last bead (the committed links,
+/// bead_class.h:107): the path permutation at the ring closure.
+int refsim_get_perm(void* h, uint32_t species, uint32_t* out) {
+    return Guard([&] {
+        Path& path = *S(h)->path;
+        auto& s = path.GetSpecies().at(species);
+        const ModeType keep = path.GetMode();
+        path.SetMode(OLD_MODE);
+        for (uint32_t p = 0; p < s->GetNPart(); ++p) out[p] = s->GetBead(p, path.GetNBead() - 1)->GetNextBead(1)->GetP();
+        path.SetMode(keep);
     });
 }
 

@@ -4,10 +4,16 @@
 //                 structure_factor_class.h:23);
 //   fequal(a,b,t) |a - b| < t, the k-magnitude matching of the pair-action tables;
 //   CompareVec    strict weak order of vectors (map keys of permutation sectors);
-//   GenCombPermK  all k-tuples of the distinct values of a set, in lexicographic order. KSpace::Setup
-//                 passes the concatenated index ranges of every dimension and k = n_d
-//                 (k_space_class.h:59-64) and keeps each integer vector once; the scaffold order is
-//                 unknown, so the tuples come in the order the oracle enumerates them.
+//   GenCombPermK  (set, k, repeat = false, ordered = true): all k-tuples of the distinct values of a
+//                 set, in lexicographic order. KSpace::Setup passes the concatenated index ranges of
+//                 every dimension and k = n_d (k_space_class.h:59-64) and keeps each integer vector
+//                 once. (set, k, false, false): the k-element subsets of the set's elements, each
+//                 in the set's order, subsets in lexicographic order of positions — the particle
+//                 sets of PermBisectTable's cycles (perm_bisect_table_class.h:80-86). The scaffold
+//                 orders are unknown, so both come in the order the oracle enumerates them.
+//   GenPerm       every permutation of a vector, lexicographic from its given order (the
+//                 permutation types of PermBisectTable, perm_bisect_table_class.h:55-61), the
+//                 oracle's order.
 #pragma once
 
 #include <algorithm>
@@ -31,7 +37,37 @@ struct CompareVec {
 };
 
 template <class T>
-void GenCombPermK(std::vector<std::vector<T>>& out, const std::vector<T>& set, uint32_t k, bool /*unused*/, bool /*unused*/) {
+void GenPerm(std::vector<std::vector<T>>& out, const std::vector<T>& v) {
+    out.clear();
+    std::vector<size_t> idx(v.size());
+    for (size_t i = 0; i < idx.size(); ++i) idx[i] = i;
+    do {
+        std::vector<T> p(v.size());
+        for (size_t i = 0; i < idx.size(); ++i) p[i] = v[idx[i]];
+        out.push_back(p);
+    } while (std::next_permutation(idx.begin(), idx.end()));
+}
+
+template <class T>
+void GenCombPermK(std::vector<std::vector<T>>& out, const std::vector<T>& set, uint32_t k, bool repeat, bool ordered) {
+    if (!repeat && !ordered) {  // subsets of k positions, lexicographic
+        out.clear();
+        const size_t n = set.size();
+        if (k == 0 || k > n) return;
+        std::vector<size_t> c(k);
+        for (uint32_t i = 0; i < k; ++i) c[i] = i;
+        for (;;) {
+            std::vector<T> t(k);
+            for (uint32_t i = 0; i < k; ++i) t[i] = set[c[i]];
+            out.push_back(t);
+            int i = (int)k - 1;
+            while (i >= 0 && c[i] == n - k + (size_t)i) --i;
+            if (i < 0) break;
+            ++c[i];
+            for (uint32_t j = (uint32_t)i + 1; j < k; ++j) c[j] = c[j - 1] + 1;
+        }
+        return;
+    }
     std::vector<T> vals(set);
     std::sort(vals.begin(), vals.end());
     vals.erase(std::unique(vals.begin(), vals.end()), vals.end());

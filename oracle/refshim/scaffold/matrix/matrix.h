@@ -247,6 +247,20 @@ class field {
     std::vector<T> d_;
 };
 
+/// Matrix-vector product (PermBisectTable forms inverse permutations as a permutation matrix times
+/// an index vector, perm_bisect_table_class.h:67-77).
+template <class T>
+vec<T> operator*(const mat<T>& m, const vec<T>& v) {
+    if (m.n_cols != v.size()) throw std::logic_error("mat * vec: size mismatch");
+    vec<T> r(m.n_rows);
+    for (size_t i = 0; i < m.n_rows; ++i) {
+        T t = T();
+        for (size_t j = 0; j < m.n_cols; ++j) t += m(i, j) * v(j);
+        r(i) = t;
+    }
+    return r;
+}
+
 template <class V>
 V zeros(size_t n) {
     return V(n);

@@ -10,7 +10,14 @@ and the reference's answers on it:
   with a long-range part reads its table-ordered v_long_k by the stored k-vector index,
   david_pair_action_class.h:60-61, past the end of that array);
 - the input's Algorithm loop (Simulation::Run) with bisection draws from the oracle's counter-based
-  stream: every Write's move counters and bisection level, every observable block, the final path.
+  stream: every Write's move counters and bisection level, every observable block, the final path;
+  for the permuting moves (PermBisectIterative, PermBisectTable) also every Write's per-cycle-length
+  counters and the final path permutation at the ring closure.
+
+PermBisectTable's case cycles every particle of its species (n_perm_part = N): with fewer, the
+reference leaves the particles owning the end beads out of the action's particle list when the
+segment passes a permuted ring closure (perm_bisect_table_class.h:133-141, against
+perm_bisect_iterative_class.h:141-146), which the oracle and the GPU library do not copy.
 
 The tests compare the oracle (tests/test_reference_pins.py, CPU) and the GPU library
 (tests/test_gpu_reference_fixtures.py) with these numbers; neither needs the reference checkout.
@@ -46,6 +53,10 @@ CASES = {
                                         n_step_outer=2, n_step_inner=30), 0.3),
     "david_egas": ("electron_gas", dict(n_part=14, n_bead=16, n_level=2, rs=2.0, k_cut_units=4.0, seed=13, pair="DavidPairAction",
                                         n_order=1, n_step_outer=2, n_step_inner=30), 0.3),
+    "bosons_iterative": ("trapped_bosons", dict(n_part=5, n_bead=16, n_level=2, seed=31, coulomb=True, perm="PermBisectIterative",
+                                                n_step_outer=3, n_step_inner=80), 0.0),
+    "bosons_table": ("trapped_bosons", dict(n_part=4, n_bead=16, n_level=2, seed=37, coulomb=True, perm="PermBisectTable", n_perm_part=4,
+                                            n_step_outer=3, n_step_inner=80), 0.0),
 }
 
 
@@ -141,12 +152,16 @@ def reference_answers(name, workdir):
     out["dactiondbeta"] = np.array([value(r.dactiondbeta, a) for a in range(n_actions)])
     out["potential"] = np.array([value(r.potential, a) for a in range(n_actions)])
     out["virial_energy"] = np.array([[value(r.virial_energy, a, w) for w in (M, 4)] for a in range(n_actions)])
-    mstats, blocks = r.run(xml)
+    mstats, blocks, pstats = r.run(xml)
     for m, rows in mstats.items():
         out[f"move_writes_{m}"] = np.array(rows, dtype=np.int64)  # (n_attempt, n_accept, n_level or -1) per Write
+    for m, rows in pstats.items():
+        out[f"perm_writes_{m}"] = np.array(rows, dtype=np.int64)  # (attempts, accepts) per cycle length, per Write
     for o, rows in blocks.items():
         out[f"blocks_{o}"] = np.array(rows)
     out["final_path"] = r.get_path(1)
+    if pstats:
+        out["final_perm"] = r.get_perm(0, path.shape[0])
     r.close()
     return out
 

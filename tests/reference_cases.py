@@ -5,7 +5,8 @@ object with the Simulation / OracleSim surface and compares the answers with the
 own classes gave (tests/golden/make_reference_fixtures.py). Tolerances are the parity tests' FP64
 ones: action values, dS/dbeta, potentials, virial energies and energy blocks 1e-10 relative; the
 central-difference pair gradients (eps = 1e-4, pair_action_class.h:135-155) 1e-8 relative; path
-coordinates 1e-9; g(r) and S(k) blocks 1e-10 relative; move counters and bisection levels exact.
+coordinates 1e-9; g(r) and S(k) blocks 1e-10 relative; move counters, bisection levels, the permuting
+moves' per-cycle-length counters and the final path permutation exact.
 """
 from __future__ import annotations
 
@@ -47,9 +48,12 @@ def _close(a, b, rel):
     return a.shape == b.shape and bool(np.all(np.abs(a - b) <= rel * np.maximum(1.0, np.abs(b))))
 
 
-def check_against_fixture(make_sim, name, workdir, run_blocks, final_path, move_writes=None, grad_rel=1e-8):
+def check_against_fixture(make_sim, name, workdir, run_blocks, final_path, move_writes=None, grad_rel=1e-8, perm_writes=None,
+                          final_perm=None):
     """make_sim(xml, workdir) -> a fresh simulation; run_blocks(sim, xml) -> {obs: [blocks]} after
-    running the Algorithm; final_path(sim) -> positions; move_writes(sim, xml) -> {move: rows} or None."""
+    running the Algorithm; final_path(sim) -> positions; move_writes(sim, xml) -> {move: rows} or None;
+    perm_writes(sim, xml) -> {permuting move: [Write, (attempts, accepts), cycle length]} and
+    final_perm(sim) -> the first species' path permutation, required when the fixture has them."""
     gen = generator()
     fx = load(name)
     xml, path = gen.build_case(name, workdir)
@@ -105,6 +109,18 @@ def check_against_fixture(make_sim, name, workdir, run_blocks, final_path, move_
                 want, got = want[:, :2], got[:, :2]
             if not np.array_equal(got, want):
                 errs.append(("move writes", m, got.tolist(), want.tolist()))
+    perm_keys = [k for k in fx if k.startswith("perm_writes_")]
+    if perm_keys:
+        assert perm_writes is not None and final_perm is not None, "a permuting-move fixture needs its counters and permutation"
+        got_pw = perm_writes(sim, xml)
+        for k in perm_keys:
+            m = int(k[len("perm_writes_"):])
+            got = np.asarray(got_pw.get(m, []), dtype=np.int64)
+            if not np.array_equal(got, fx[k]):
+                errs.append(("perm writes", m, got.tolist(), fx[k].tolist()))
+        got = np.asarray(final_perm(sim), dtype=np.int64)
+        if not np.array_equal(got, fx["final_perm"]):
+            errs.append(("final perm", got.tolist(), fx["final_perm"].tolist()))
     fp = final_path(sim)
     if not (fp.shape == fx["final_path"].shape and np.max(np.abs(fp - fx["final_path"])) < 1e-9):
         errs.append(("final path", float(np.max(np.abs(fp - fx["final_path"]))) if fp.shape == fx["final_path"].shape else None))

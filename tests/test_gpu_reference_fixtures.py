@@ -7,7 +7,9 @@ counter-based draws, measurements, Write events, adaptive bisection levels); the
 number (tolerances in tests/reference_cases.py: FP64 parity 1e-10 relative, FD gradients 1e-8, path
 1e-9, move counters and levels exact). The cases cover the kinetic action with and without periodic
 images, the trap, the bare Coulomb action with and without Ewald sums, IlkkaPairAction,
-DavidPairAction at levels 0-2 and with Ewald sums, and the adaptive bisection level.
+DavidPairAction at levels 0-2 and with Ewald sums, the adaptive bisection level, and the permuting
+moves PermBisectIterative and PermBisectTable (their per-cycle-length counters at every Write and the
+final path permutation, exact).
 """
 import xml.etree.ElementTree as ET
 
@@ -30,10 +32,13 @@ def test_gpu_matches_reference_fixture(tmp_path, gpu_lib, name):
         sim.run()
         return {o: sim.blocks(o) for o in range(n_observables(xml))}
 
-    def move_writes(sim, xml):
+    def output(sim):
         out = tmp_path / "run.pat"
         sim.write_output(out)
-        t = read_table(out)
+        return read_table(out)
+
+    def move_writes(sim, xml):
+        t = output(sim)
         rows = {}
         names = [m.get("name") for m in ET.fromstring(xml).find("Moves")]
         for i, n in enumerate(names):
@@ -42,7 +47,19 @@ def test_gpu_matches_reference_fixture(tmp_path, gpu_lib, name):
             rows[i] = np.stack([att, acc, lvl], axis=1).astype(np.int64)
         return rows
 
-    sim, errs = check_against_fixture(make, name, tmp_path, blocks, lambda s: s.get_path(1), move_writes)
+    def perm_writes(sim, xml):
+        t = output(sim)
+        n_part = sim.get_path(1).shape[0]
+        rows = {}
+        for i, m in enumerate(ET.fromstring(xml).find("Moves")):
+            if m.get("type") in ("PermBisectIterative", "PermBisectTable"):
+                att = np.asarray(t[f"Moves/{m.get('name')}/perm_attempt"]).reshape(-1, n_part)
+                acc = np.asarray(t[f"Moves/{m.get('name')}/perm_accept"]).reshape(-1, n_part)
+                rows[i] = np.stack([att, acc], axis=1).astype(np.int64)
+        return rows
+
+    sim, errs = check_against_fixture(make, name, tmp_path, blocks, lambda s: s.get_path(1), move_writes, perm_writes=perm_writes,
+                                      final_perm=lambda s: s.get_perm(0))
     sim_xml_types = [a.get("type") for a in ET.fromstring(str(load(name)["xml"])).find("Actions")]
     sim.close()
     # IlkkaPairAction's long-range gradient in NEW mode: the reference reads species b's NEW-copy

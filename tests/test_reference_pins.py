@@ -5,9 +5,11 @@ tests/golden/reference_*.npz hold the answers of simpimc's own Action, Bisect an
 seeded inputs: GetAction / GetActionGradient queries, DActionDBeta, Potential, VirialEnergy, and the
 input's whole Algorithm loop (bisection with the oracle's random stream, measurements, Write events,
 adaptive bisection levels). Cases: the 8-particle trapped Coulomb system (N = 8, M = 32, level 3), an
-adaptive-level trap, DavidPairAction with tables at levels 0-2, and 14-electron gases with the bare
+adaptive-level trap, DavidPairAction with tables at levels 0-2, 14-electron gases with the bare
 Ewald, Ilkka and David pair actions and one with periodic images in the kinetic action
-(n_images = 10 on a small box).
+(n_images = 10 on a small box), and trapped Coulomb bosons with the permuting moves
+(PermBisectIterative; PermBisectTable over every particle), whose per-cycle-length counters and
+final path permutation are compared too.
 
 The oracle must reproduce every number (tolerances in tests/reference_cases.py). Where the reference
 checkout is present, the fixtures are also regenerated from it and must equal the committed files,
@@ -24,22 +26,36 @@ def _oracle_blocks(sim, xml):
     return {o: sim.blocks(o) for o in range(n_observables(xml))}
 
 
+def _oracle_move_writes(sim, xml):
+    return {m: sim.move_writes(m)[:, :3] for m in range(sim.n_moves)}
+
+
+def _oracle_perm_writes(sim, xml):
+    out = {}
+    for m in range(sim.n_moves):
+        rows = sim.move_writes(m)
+        if rows.shape[1] > 3:
+            out[m] = rows[:, 3:].reshape(rows.shape[0], 2, -1)
+    return out
+
+
 @pytest.mark.parametrize("name", fixture_names())
 def test_oracle_matches_reference_fixture(tmp_path, oracle_mod, name):
     def make(xml, d):
         return oracle_mod.OracleSim(xml, base_dir=d)
 
-    sim, errs = check_against_fixture(make, name, tmp_path, _oracle_blocks, lambda s: s.get_path(1))
+    sim, errs = check_against_fixture(make, name, tmp_path, _oracle_blocks, lambda s: s.get_path(1), _oracle_move_writes,
+                                      perm_writes=_oracle_perm_writes, final_perm=lambda s: s.get_perm(0, s.get_path(1).shape[0]))
     sim.close()
     assert not errs, errs[:10]
 
 
 def test_fixture_cases_cover_the_hot_path_classes():
     names = fixture_names()
-    assert len(names) >= 7
+    assert len(names) >= 9
     xmls = " ".join(str(load(n)["xml"]) for n in names)
     for cls in ("Kinetic", "HarmonicTrap", "BarePairAction", "IlkkaPairAction", "DavidPairAction", 'adaptive="1"', 'n_images="10"',
-                "StructureFactor", "PairCorrelation", "use_virial_estimator"):
+                "StructureFactor", "PairCorrelation", "use_virial_estimator", "PermBisectIterative", "PermBisectTable"):
         assert cls in xmls, cls
 
 
