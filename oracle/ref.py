@@ -92,6 +92,7 @@ def _seed_of(xml: str) -> int:
 
 
 MOVE_TYPES = ("Bisect", "PermBisectIterative", "PermBisectTable")
+OBSERVABLE_TYPES = ("Energy", "PairCorrelation", "StructureFactor", "Sign")
 
 
 def _moves(xml: str):
@@ -272,14 +273,16 @@ class RefSim:
         """Simulation::Run (simulation_class.h:42-45): the input's <Algorithm> loop of Move, Observable
         and Write events (loop_class.h:34-60; a Write writes every move, then every observable,
         write_class.h:31-42), one attempt per Move event. Returns ({move: [(n_attempt, n_accept,
-        n_level)] per Write}, {observable: [block] per Write that appended one}, {permuting move:
+        n_level)] per Write}, {observable (its place among the input's observables): [block] per Write
+        that appended one}, {permuting move:
         [(attempts, accepts) per cycle length] per Write})."""
         import xml.etree.ElementTree as ET
         root = ET.fromstring(xml)
         moves = [m.get("name") for m in root.find("Moves") if m.get("type") in MOVE_TYPES]
-        obs = [o.get("name") for o in root.find("Observables") if o.get("type") in ("Energy", "PairCorrelation", "StructureFactor")]
+        all_obs = [o.get("name") for o in root.find("Observables")]
+        obs = [o.get("name") for o in root.find("Observables") if o.get("type") in OBSERVABLE_TYPES]
         mstats = {i: [] for i in range(len(moves))}
-        blocks = {i: [] for i in range(len(obs))}
+        blocks = {all_obs.index(n): [] for n in obs}  # keyed by the observable's place in the input
         pstats = {i: [] for i, mv in enumerate(self._moves) if mv[0] != "Bisect"}
 
         def loop(node):
@@ -297,7 +300,7 @@ class RefSim:
                         for o in range(len(obs)):
                             b = self.observable_block(o)
                             if b.size:
-                                blocks[o].append(b)
+                                blocks[all_obs.index(obs[o])].append(b)
                     elif ev.tag == "Loop":
                         loop(ev)
 

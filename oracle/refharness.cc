@@ -8,7 +8,7 @@
 // Set-up follows Simulation's constructor (framework/simulation_class.h:16-39) with the factories
 // of actions.h, moves.h and observables.h restricted to the hot path's classes: Kinetic,
 // HarmonicTrap, BarePairAction, IlkkaPairAction, DavidPairAction; Bisect, PermBisectIterative,
-// PermBisectTable; Energy, PairCorrelation, StructureFactor. Species start as init_type "Line" (species_class.h:311-321) and take their
+// PermBisectTable; Energy, PairCorrelation, StructureFactor, Sign. Species start as init_type "Line" (species_class.h:311-321) and take their
 // positions from refsim_set_path. Move draws are scripted (refshim/scaffold/rng/rng.h).
 #include <sys/time.h>
 
@@ -48,6 +48,7 @@ using namespace scaffold::rand;
 #include "events/moves/single_species_move/bisect/perm_bisect/perm_bisect_table_class.h"
 #include "events/observables/energy_class.h"
 #include "events/observables/pair_correlation_class.h"
+#include "events/observables/sign_class.h"
 #include "events/observables/structure_factor_class.h"
 
 namespace {
@@ -145,6 +146,7 @@ int refsim_create(const char* xml, const char* dir, void** out) {
             if (type == "Energy") ob = std::make_shared<Energy>(*s->path, s->actions, o, s->out);
             else if (type == "PairCorrelation") ob = std::make_shared<PairCorrelation>(*s->path, o, s->out);
             else if (type == "StructureFactor") ob = std::make_shared<StructureFactor>(*s->path, o, s->out);
+            else if (type == "Sign") ob = std::make_shared<Sign>(*s->path, o, s->out);
             else continue;
             s->observables.push_back(ob);
             s->obs_names.push_back(o.GetAttribute<std::string>("name"));
@@ -383,7 +385,8 @@ int refsim_obs_write(void* h, uint32_t o, double* out, uint64_t cap, uint64_t* n
     return Guard([&] {
         RefSim& s = *S(h);
         const std::string pre = "Observables/" + s.obs_names.at(o) + "/";
-        const std::string key = s.obs_types[o] == "Energy" ? pre + "total/x" : pre + "y";
+        const std::string& type = s.obs_types[o];
+        const std::string key = type == "Energy" ? pre + "total/x" : type == "Sign" ? pre + "x" : pre + "y";
         auto rows = [&]() -> size_t {
             auto* r = s.out.Appended(key);
             return r ? r->size() : 0;
@@ -400,7 +403,7 @@ int refsim_obs_write(void* h, uint32_t o, double* out, uint64_t cap, uint64_t* n
                 if (r) vals.push_back(r->back()[0]);
             }
         } else {
-            vals = s.out.Appended(pre + "y")->back();
+            vals = s.out.Appended(key)->back();
         }
         *n = vals.size();
         for (size_t i = 0; i < vals.size() && i < cap; ++i) out[i] = vals[i];

@@ -12,7 +12,10 @@ and the reference's answers on it:
 - the input's Algorithm loop (Simulation::Run) with bisection draws from the oracle's counter-based
   stream: every Write's move counters and bisection level, every observable block, the final path;
   for the permuting moves (PermBisectIterative, PermBisectTable) also every Write's per-cycle-length
-  counters and the final path permutation at the ring closure.
+  counters and the final path permutation at the ring closure. Observable blocks are keyed by the
+  observable's place in the input; the Permutation observable is left out (the reference's sector
+  lookup has no entries: species_class.h:178-180 generates the sectors only when some already
+  exist), and the Sign observable and the sign cofactor of the energy are in the fermion case.
 
 PermBisectTable's case cycles every particle of its species (n_perm_part = N): with fewer, the
 reference leaves the particles owning the end beads out of the action's particle list when the
@@ -57,6 +60,8 @@ CASES = {
                                                 n_step_outer=3, n_step_inner=80), 0.0),
     "bosons_table": ("trapped_bosons", dict(n_part=4, n_bead=16, n_level=2, seed=37, coulomb=True, perm="PermBisectTable", n_perm_part=4,
                                             n_step_outer=3, n_step_inner=80), 0.0),
+    "fermions_iterative": ("trapped_bosons", dict(n_part=4, n_bead=16, n_level=2, seed=43, coulomb=True, fermi=True,
+                                                  perm="PermBisectIterative", n_step_outer=3, n_step_inner=80), 0.0),
 }
 
 

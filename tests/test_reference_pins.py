@@ -7,9 +7,10 @@ input's whole Algorithm loop (bisection with the oracle's random stream, measure
 adaptive bisection levels). Cases: the 8-particle trapped Coulomb system (N = 8, M = 32, level 3), an
 adaptive-level trap, DavidPairAction with tables at levels 0-2, 14-electron gases with the bare
 Ewald, Ilkka and David pair actions and one with periodic images in the kinetic action
-(n_images = 10 on a small box), and trapped Coulomb bosons with the permuting moves
+(n_images = 10 on a small box), trapped Coulomb bosons with the permuting moves
 (PermBisectIterative; PermBisectTable over every particle), whose per-cycle-length counters and
-final path permutation are compared too.
+final path permutation are compared too, and trapped Coulomb fermions (the Sign observable and the
+energy's sign cofactor).
 
 The oracle must reproduce every number (tolerances in tests/reference_cases.py). Where the reference
 checkout is present, the fixtures are also regenerated from it and must equal the committed files,
@@ -52,10 +53,10 @@ def test_oracle_matches_reference_fixture(tmp_path, oracle_mod, name):
 
 def test_fixture_cases_cover_the_hot_path_classes():
     names = fixture_names()
-    assert len(names) >= 9
+    assert len(names) >= 10
     xmls = " ".join(str(load(n)["xml"]) for n in names)
     for cls in ("Kinetic", "HarmonicTrap", "BarePairAction", "IlkkaPairAction", "DavidPairAction", 'adaptive="1"', 'n_images="10"',
-                "StructureFactor", "PairCorrelation", "use_virial_estimator", "PermBisectIterative", "PermBisectTable"):
+                "StructureFactor", "PairCorrelation", "use_virial_estimator", "PermBisectIterative", "PermBisectTable", 'fermi="1"', 'type="Sign"'):
         assert cls in xmls, cls
 
 
