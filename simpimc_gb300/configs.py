@@ -27,30 +27,34 @@ import numpy as np
 from .tables import coulomb_table, david_table, ilkka_table
 
 
+def _open_pair_xml(workdir, species, pair, n_bead, beta, n_order, pair_max_level, write_table):
+    """The Coulomb pair action of an open-boundary species (its table written into `workdir`)."""
+    if pair == "DavidPairAction":
+        tab = workdir / f"david_open_{n_bead}_{beta}_{n_order}_{pair_max_level}.pat"
+        if write_table or not tab.exists():
+            david_table(tab, tau=beta / n_bead, n_order=n_order, lam=0.5, z_ab=1.0, L=0.0, n_tau=pair_max_level + 1)
+        return (f'<Action name="Coulomb" type="DavidPairAction" file="{tab.name}" n_order="{n_order}" species_a="{species}" '
+                f'species_b="{species}" max_level="{pair_max_level}" use_long_range="0" />')
+    if pair == "IlkkaPairAction":
+        tab = workdir / f"ilkka_open_{n_bead}_{beta}.pat"
+        if write_table or not tab.exists():
+            ilkka_table(tab, tau=beta / n_bead, lam=0.5, z_ab=1.0, L=0.0)
+        return (f'<Action name="Coulomb" type="IlkkaPairAction" file="{tab.name}" species_a="{species}" species_b="{species}" '
+                f'max_level="{pair_max_level}" use_long_range="0" />')
+    tab = workdir / "coulomb_open.pat"
+    if write_table or not tab.exists():
+        coulomb_table(tab, z_ab=1.0, L=0.0)
+    return (f'<Action name="Coulomb" type="BarePairAction" file="{tab.name}" is_coulomb="1" species_a="{species}" '
+            f'species_b="{species}" max_level="{pair_max_level}" use_long_range="0" />')
+
+
 def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_level=3, seed=1234, coulomb=True,
                     n_step_inner=100, n_step_outer=10, gr_bins=200, gr_rmax=5.0, virial=False, path_seed=None,
                     write_table=True, pair="BarePairAction", n_order=2, pair_max_level=0, adaptive=False, target_ratio=0.5,
                     hmc=None):
     workdir = Path(workdir)
     workdir.mkdir(parents=True, exist_ok=True)
-    if pair == "DavidPairAction":
-        tab = workdir / f"david_open_{n_bead}_{beta}_{n_order}_{pair_max_level}.pat"
-        if write_table or not tab.exists():
-            david_table(tab, tau=beta / n_bead, n_order=n_order, lam=0.5, z_ab=1.0, L=0.0, n_tau=pair_max_level + 1)
-        pair_xml = (f'<Action name="Coulomb" type="DavidPairAction" file="{tab.name}" n_order="{n_order}" species_a="e" '
-                    f'species_b="e" max_level="{pair_max_level}" use_long_range="0" />')
-    elif pair == "IlkkaPairAction":
-        tab = workdir / f"ilkka_open_{n_bead}_{beta}.pat"
-        if write_table or not tab.exists():
-            ilkka_table(tab, tau=beta / n_bead, lam=0.5, z_ab=1.0, L=0.0)
-        pair_xml = (f'<Action name="Coulomb" type="IlkkaPairAction" file="{tab.name}" species_a="e" species_b="e" '
-                    f'max_level="{pair_max_level}" use_long_range="0" />')
-    else:
-        tab = workdir / "coulomb_open.pat"
-        if write_table or not tab.exists():
-            coulomb_table(tab, z_ab=1.0, L=0.0)
-        pair_xml = (f'<Action name="Coulomb" type="BarePairAction" file="{tab.name}" is_coulomb="1" species_a="e" '
-                    f'species_b="e" max_level="{pair_max_level}" use_long_range="0" />')
+    pair_xml = _open_pair_xml(workdir, "e", pair, n_bead, beta, n_order, pair_max_level, write_table)
     pair = pair_xml if coulomb else ""
     energy = ('<Observable name="Energy" type="Energy" use_virial_estimator="1" />' if virial
               else '<Observable name="Energy" type="Energy" />')
@@ -188,17 +192,13 @@ def sweep_schedule(sim_or_counts, n_bisect_beads: int, n_bead: int):
 
 def trapped_bosons(workdir, *, n_part=3, beta=2.0, n_bead=16, omega=1.0, n_level=2, seed=1234, coulomb=False,
                    perm="PermBisectIterative", n_perm_part=2, fermi=False, n_step_inner=100, n_step_outer=10,
-                   path_seed=None, perm_level=None, sector_max=0):
+                   path_seed=None, perm_level=None, sector_max=0, pair="BarePairAction", n_order=2, pair_max_level=0):
     """Identical particles with exchange: the permuting move's species carries the path
-    permutation. Observables: Energy (thermal), Permutation (cycle histogram and sectors), Sign."""
+    permutation. Observables: Energy (thermal), Permutation (cycle histogram and sectors), Sign.
+    With coulomb, `pair` chooses the Coulomb pair action as in trapped_coulomb."""
     workdir = Path(workdir)
     workdir.mkdir(parents=True, exist_ok=True)
-    pair_xml = ""
-    if coulomb:
-        tab = workdir / "coulomb_open.pat"
-        coulomb_table(tab, z_ab=1.0, L=0.0)
-        pair_xml = (f'<Action name="Coulomb" type="BarePairAction" file="{tab.name}" is_coulomb="1" species_a="b" '
-                    f'species_b="b" max_level="0" use_long_range="0" />')
+    pair_xml = _open_pair_xml(workdir, "b", pair, n_bead, beta, n_order, pair_max_level, True) if coulomb else ""
     extra = f' n_perm_part="{n_perm_part}"' if perm == "PermBisectTable" else ""
     perm_level = n_level if perm_level is None else perm_level
     xml = f"""<Input>

@@ -62,6 +62,10 @@ CASES = {
                                             n_step_outer=3, n_step_inner=80), 0.0),
     "fermions_iterative": ("trapped_bosons", dict(n_part=4, n_bead=16, n_level=2, seed=43, coulomb=True, fermi=True,
                                                   perm="PermBisectIterative", n_step_outer=3, n_step_inner=80), 0.0),
+    "david_bosons": ("trapped_bosons", dict(n_part=4, n_bead=16, n_level=2, seed=53, coulomb=True, perm="PermBisectIterative",
+                                            pair="DavidPairAction", n_order=2, pair_max_level=2, n_step_outer=3, n_step_inner=80), 0.0),
+    "ilkka_bosons": ("trapped_bosons", dict(n_part=4, n_bead=16, n_level=2, seed=59, coulomb=True, perm="PermBisectIterative",
+                                            pair="IlkkaPairAction", pair_max_level=2, n_step_outer=3, n_step_inner=80), 0.0),
 }
 
 

@@ -9,7 +9,7 @@ number (tolerances in tests/reference_cases.py: FP64 parity 1e-10 relative, FD g
 images, the trap, the bare Coulomb action with and without Ewald sums, IlkkaPairAction,
 DavidPairAction at levels 0-2 and with Ewald sums, the adaptive bisection level, and the permuting
 moves PermBisectIterative and PermBisectTable (their per-cycle-length counters at every Write and the
-final path permutation, exact).
+final path permutation, exact) with bare, David and Ilkka pair actions, for bosons and fermions.
 """
 import xml.etree.ElementTree as ET
 

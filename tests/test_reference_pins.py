@@ -9,8 +9,9 @@ adaptive-level trap, DavidPairAction with tables at levels 0-2, 14-electron gase
 Ewald, Ilkka and David pair actions and one with periodic images in the kinetic action
 (n_images = 10 on a small box), trapped Coulomb bosons with the permuting moves
 (PermBisectIterative; PermBisectTable over every particle), whose per-cycle-length counters and
-final path permutation are compared too, and trapped Coulomb fermions (the Sign observable and the
-energy's sign cofactor).
+final path permutation are compared too, trapped Coulomb fermions (the Sign observable and the
+energy's sign cofactor), and trapped bosons with DavidPairAction / IlkkaPairAction tables above
+level 0 under PermBisectIterative.
 
 The oracle must reproduce every number (tolerances in tests/reference_cases.py). Where the reference
 checkout is present, the fixtures are also regenerated from it and must equal the committed files,
@@ -53,7 +54,7 @@ def test_oracle_matches_reference_fixture(tmp_path, oracle_mod, name):
 
 def test_fixture_cases_cover_the_hot_path_classes():
     names = fixture_names()
-    assert len(names) >= 10
+    assert len(names) >= 12
     xmls = " ".join(str(load(n)["xml"]) for n in names)
     for cls in ("Kinetic", "HarmonicTrap", "BarePairAction", "IlkkaPairAction", "DavidPairAction", 'adaptive="1"', 'n_images="10"',
                 "StructureFactor", "PairCorrelation", "use_virial_estimator", "PermBisectIterative", "PermBisectTable", 'fermi="1"', 'type="Sign"'):
