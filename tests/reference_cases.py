@@ -42,6 +42,21 @@ def n_observables(xml):
     return len(list(ET.fromstring(xml).find("Observables")))
 
 
+def species_counts(xml):
+    """n_part of each species, in input order."""
+    import xml.etree.ElementTree as ET
+    return [int(s.get("n_part")) for s in ET.fromstring(xml).find("Particles")]
+
+
+def permuting_moves(xml):
+    """{move index: species index} of the input's permuting moves."""
+    import xml.etree.ElementTree as ET
+    root = ET.fromstring(xml)
+    names = [s.get("name") for s in root.find("Particles")]
+    return {i: names.index(m.get("species")) for i, m in enumerate(root.find("Moves"))
+            if m.get("type") in ("PermBisectIterative", "PermBisectTable")}
+
+
 def _close(a, b, rel):
     a = np.asarray(a, dtype=float)
     b = np.asarray(b, dtype=float)
@@ -53,7 +68,7 @@ def check_against_fixture(make_sim, name, workdir, run_blocks, final_path, move_
     """make_sim(xml, workdir) -> a fresh simulation; run_blocks(sim, xml) -> {obs: [blocks]} after
     running the Algorithm; final_path(sim) -> positions; move_writes(sim, xml) -> {move: rows} or None;
     perm_writes(sim, xml) -> {permuting move: [Write, (attempts, accepts), cycle length]} and
-    final_perm(sim) -> the first species' path permutation, required when the fixture has them."""
+    final_perm(sim, xml) -> the first species' path permutation, required when the fixture has them."""
     gen = generator()
     fx = load(name)
     xml, path = gen.build_case(name, workdir)
@@ -118,7 +133,7 @@ def check_against_fixture(make_sim, name, workdir, run_blocks, final_path, move_
             got = np.asarray(got_pw.get(m, []), dtype=np.int64)
             if not np.array_equal(got, fx[k]):
                 errs.append(("perm writes", m, got.tolist(), fx[k].tolist()))
-        got = np.asarray(final_perm(sim), dtype=np.int64)
+        got = np.asarray(final_perm(sim, xml), dtype=np.int64)
         if not np.array_equal(got, fx["final_perm"]):
             errs.append(("final perm", got.tolist(), fx["final_perm"].tolist()))
     fp = final_path(sim)

@@ -16,7 +16,7 @@ import xml.etree.ElementTree as ET
 import numpy as np
 import pytest
 
-from reference_cases import check_against_fixture, fixture_names, load, n_observables
+from reference_cases import check_against_fixture, fixture_names, load, n_observables, permuting_moves, species_counts
 from simpimc_gb300 import Simulation
 from simpimc_gb300.tables import read_table
 
@@ -49,17 +49,17 @@ def test_gpu_matches_reference_fixture(tmp_path, gpu_lib, name):
 
     def perm_writes(sim, xml):
         t = output(sim)
-        n_part = sim.get_path(1).shape[0]
+        counts = species_counts(xml)
+        names = [m.get("name") for m in ET.fromstring(xml).find("Moves")]
         rows = {}
-        for i, m in enumerate(ET.fromstring(xml).find("Moves")):
-            if m.get("type") in ("PermBisectIterative", "PermBisectTable"):
-                att = np.asarray(t[f"Moves/{m.get('name')}/perm_attempt"]).reshape(-1, n_part)
-                acc = np.asarray(t[f"Moves/{m.get('name')}/perm_accept"]).reshape(-1, n_part)
-                rows[i] = np.stack([att, acc], axis=1).astype(np.int64)
+        for i, sp in permuting_moves(xml).items():
+            att = np.asarray(t[f"Moves/{names[i]}/perm_attempt"]).reshape(-1, counts[sp])
+            acc = np.asarray(t[f"Moves/{names[i]}/perm_accept"]).reshape(-1, counts[sp])
+            rows[i] = np.stack([att, acc], axis=1).astype(np.int64)
         return rows
 
     sim, errs = check_against_fixture(make, name, tmp_path, blocks, lambda s: s.get_path(1), move_writes, perm_writes=perm_writes,
-                                      final_perm=lambda s: s.get_perm(0))
+                                      final_perm=lambda s, xml: s.get_perm(0))
     sim_xml_types = [a.get("type") for a in ET.fromstring(str(load(name)["xml"])).find("Actions")]
     sim.close()
     # IlkkaPairAction's long-range gradient in NEW mode: the reference reads species b's NEW-copy

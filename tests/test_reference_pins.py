@@ -10,8 +10,8 @@ Ewald, Ilkka and David pair actions and one with periodic images in the kinetic 
 (n_images = 10 on a small box), trapped Coulomb bosons with the permuting moves
 (PermBisectIterative; PermBisectTable over every particle), whose per-cycle-length counters and
 final path permutation are compared too, trapped Coulomb fermions (the Sign observable and the
-energy's sign cofactor), and trapped bosons with DavidPairAction / IlkkaPairAction tables above
-level 0 under PermBisectIterative.
+energy's sign cofactor), trapped bosons with DavidPairAction / IlkkaPairAction tables above
+level 0 under PermBisectIterative, and an electron gas whose up spins exchange (Ewald sums).
 
 The oracle must reproduce every number (tolerances in tests/reference_cases.py). Where the reference
 checkout is present, the fixtures are also regenerated from it and must equal the committed files,
@@ -20,7 +20,7 @@ which pins the fixtures to the reference code as built here.
 import numpy as np
 import pytest
 
-from reference_cases import check_against_fixture, fixture_names, generator, load, n_observables
+from reference_cases import check_against_fixture, fixture_names, generator, load, n_observables, species_counts
 
 
 def _oracle_blocks(sim, xml):
@@ -47,14 +47,14 @@ def test_oracle_matches_reference_fixture(tmp_path, oracle_mod, name):
         return oracle_mod.OracleSim(xml, base_dir=d)
 
     sim, errs = check_against_fixture(make, name, tmp_path, _oracle_blocks, lambda s: s.get_path(1), _oracle_move_writes,
-                                      perm_writes=_oracle_perm_writes, final_perm=lambda s: s.get_perm(0, s.get_path(1).shape[0]))
+                                      perm_writes=_oracle_perm_writes, final_perm=lambda s, xml: s.get_perm(0, species_counts(xml)[0]))
     sim.close()
     assert not errs, errs[:10]
 
 
 def test_fixture_cases_cover_the_hot_path_classes():
     names = fixture_names()
-    assert len(names) >= 12
+    assert len(names) >= 13
     xmls = " ".join(str(load(n)["xml"]) for n in names)
     for cls in ("Kinetic", "HarmonicTrap", "BarePairAction", "IlkkaPairAction", "DavidPairAction", 'adaptive="1"', 'n_images="10"',
                 "StructureFactor", "PairCorrelation", "use_virial_estimator", "PermBisectIterative", "PermBisectTable", 'fermi="1"', 'type="Sign"'):
