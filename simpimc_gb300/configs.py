@@ -100,9 +100,10 @@ def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_leve
 
 def electron_gas(workdir, *, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_units=12.0, n_level=4, seed=4321,
                  n_step_inner=10, n_step_outer=4, path_seed=None, structure_factor=False, pair="BarePairAction", n_order=2,
-                 pair_max_level=0, n_images=0, perm=None):
+                 pair_max_level=0, n_images=0, perm=None, measure_all=False):
     """Two-spin electron gas in a periodic box with Ewald sums; `perm` (PermBisectIterative or
-    PermBisectTable over every up particle) adds a permuting move of the up spins."""
+    PermBisectTable over every up particle) adds a permuting move of the up spins; `measure_all`
+    accumulates g(r) (and S(k)) in the Algorithm besides the energy."""
     workdir = Path(workdir)
     workdir.mkdir(parents=True, exist_ok=True)
     L = (4.0 * math.pi * n_part / 3.0) ** (1.0 / 3.0) * rs
@@ -124,7 +125,9 @@ def electron_gas(workdir, *, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_unit
     n_dn = n_part - n_up
     img = f' n_images="{n_images}"' if n_images else ""
     sk = ('<Observable name="sk" type="StructureFactor" species_a="eU" species_b="eU" />' if structure_factor else "")
-    perm_move = perm_event = ""
+    perm_move = perm_event = more_events = ""
+    if measure_all:
+        more_events = '\n        <Observable name="gr" />' + ('\n        <Observable name="sk" />' if structure_factor else "")
     if perm:
         table = f' n_perm_part="{n_up}"' if perm == "PermBisectTable" else ""
         perm_move = f'\n    <Move name="PermU" type="{perm}" species="eU" n_level="{n_level}"{table}{img} />'
@@ -159,7 +162,7 @@ def electron_gas(workdir, *, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_unit
       <Loop n_step="{n_step_inner}">
         <Move name="BisectU" />
         <Move name="BisectD" />{perm_event}
-        <Observable name="Energy" />
+        <Observable name="Energy" />{more_events}
       </Loop>
       <Write />
     </Loop>
