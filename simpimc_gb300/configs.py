@@ -100,10 +100,11 @@ def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_leve
 
 def electron_gas(workdir, *, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_units=12.0, n_level=4, seed=4321,
                  n_step_inner=10, n_step_outer=4, path_seed=None, structure_factor=False, pair="BarePairAction", n_order=2,
-                 pair_max_level=0, n_images=0, perm=None, measure_all=False):
+                 pair_max_level=0, n_images=0, perm=None, measure_all=False, virial=False):
     """Two-spin electron gas in a periodic box with Ewald sums; `perm` (PermBisectIterative or
     PermBisectTable over every up particle) adds a permuting move of the up spins; `measure_all`
-    accumulates g(r) (and S(k)) in the Algorithm besides the energy."""
+    accumulates g(r) (and S(k)) in the Algorithm besides the energy; `virial` measures the energy
+    with the virial estimator."""
     workdir = Path(workdir)
     workdir.mkdir(parents=True, exist_ok=True)
     L = (4.0 * math.pi * n_part / 3.0) ** (1.0 / 3.0) * rs
@@ -126,6 +127,7 @@ def electron_gas(workdir, *, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_unit
     img = f' n_images="{n_images}"' if n_images else ""
     sk = ('<Observable name="sk" type="StructureFactor" species_a="eU" species_b="eU" />' if structure_factor else "")
     perm_move = perm_event = more_events = ""
+    energy_opt = ' use_virial_estimator="1"' if virial else ""
     if measure_all:
         more_events = '\n        <Observable name="gr" />' + ('\n        <Observable name="sk" />' if structure_factor else "")
     if perm:
@@ -153,7 +155,7 @@ def electron_gas(workdir, *, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_unit
     <Move name="BisectD" type="Bisect" species="eD" n_level="{n_level}"{img} />{perm_move}
   </Moves>
   <Observables>
-    <Observable name="Energy" type="Energy" />
+    <Observable name="Energy" type="Energy"{energy_opt} />
     <Observable name="gr" type="PairCorrelation" species_a="eU" species_b="eD" n_r="100" />
     {sk}
   </Observables>

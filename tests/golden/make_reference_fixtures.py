@@ -68,6 +68,10 @@ CASES = {
                                             pair="IlkkaPairAction", pair_max_level=2, n_step_outer=3, n_step_inner=80), 0.0),
     "egas_observables": ("electron_gas", dict(n_part=14, n_bead=16, n_level=2, rs=1.5, beta=4.0, k_cut_units=4.0, seed=79,
                                               structure_factor=True, measure_all=True, n_step_outer=3, n_step_inner=20), 0.2),
+    "egas_virial": ("electron_gas", dict(n_part=14, n_bead=16, n_level=2, rs=2.0, k_cut_units=4.0, seed=83, virial=True,
+                                         n_step_outer=3, n_step_inner=20), 0.3),
+    "ilkka_trap_virial": ("trapped_coulomb", dict(n_part=6, n_bead=32, n_level=3, seed=89, pair="IlkkaPairAction", virial=True,
+                                                  n_step_outer=3, n_step_inner=40), 0.0),
     "egas_perm": ("electron_gas", dict(n_part=14, n_bead=16, n_level=2, rs=1.0, beta=4.0, k_cut_units=3.0, seed=71,
                                        perm="PermBisectIterative", structure_factor=True, n_step_outer=2, n_step_inner=40), 0.15),
 }
