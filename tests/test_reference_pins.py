@@ -8,7 +8,7 @@ adaptive bisection levels). Cases: the 8-particle trapped Coulomb system (N = 8,
 adaptive-level trap, DavidPairAction with tables at levels 0-2, 14-electron gases with the bare
 Ewald, Ilkka and David pair actions, one with periodic images in the kinetic action
 (n_images = 10 on a small box) and one measuring the periodic g(r) and S(k), the virial estimator
-on an electron gas and on an IlkkaPairAction trap, trapped Coulomb bosons with the permuting moves
+on an electron gas and on IlkkaPairAction and DavidPairAction traps, trapped Coulomb bosons with the permuting moves
 (PermBisectIterative; PermBisectTable over every particle), whose per-cycle-length counters and
 final path permutation are compared too, trapped Coulomb fermions (the Sign observable and the
 energy's sign cofactor), trapped bosons with DavidPairAction / IlkkaPairAction tables above
@@ -55,7 +55,7 @@ def test_oracle_matches_reference_fixture(tmp_path, oracle_mod, name):
 
 def test_fixture_cases_cover_the_hot_path_classes():
     names = fixture_names()
-    assert len(names) >= 16
+    assert len(names) >= 17
     xmls = " ".join(str(load(n)["xml"]) for n in names)
     for cls in ("Kinetic", "HarmonicTrap", "BarePairAction", "IlkkaPairAction", "DavidPairAction", 'adaptive="1"', 'n_images="10"',
                 "StructureFactor", "PairCorrelation", "use_virial_estimator", "PermBisectIterative", "PermBisectTable", 'fermi="1"', 'type="Sign"'):
