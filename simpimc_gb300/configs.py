@@ -51,7 +51,7 @@ def _open_pair_xml(workdir, species, pair, n_bead, beta, n_order, pair_max_level
 def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_level=3, seed=1234, coulomb=True,
                     n_step_inner=100, n_step_outer=10, gr_bins=200, gr_rmax=5.0, virial=False, path_seed=None,
                     write_table=True, pair="BarePairAction", n_order=2, pair_max_level=0, adaptive=False, target_ratio=0.5,
-                    hmc=None):
+                    hmc=None, trap_max_level=0):
     workdir = Path(workdir)
     workdir.mkdir(parents=True, exist_ok=True)
     pair_xml = _open_pair_xml(workdir, "e", pair, n_bead, beta, n_order, pair_max_level, write_table)
@@ -71,7 +71,7 @@ def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_leve
   </Particles>
   <Actions>
     <Action name="Kinetic" type="Kinetic" n_images="0" species="e" />
-    <Action name="Trap" type="HarmonicTrap" species="e" omega="{omega}" max_level="0" />
+    <Action name="Trap" type="HarmonicTrap" species="e" omega="{omega}" max_level="{trap_max_level}" />
     {pair}
   </Actions>
   <Moves>
@@ -175,6 +175,59 @@ def electron_gas(workdir, *, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_unit
     # point in the box per particle, shared by all of its beads.
     rng = np.random.default_rng(seed if path_seed is None else path_seed)
     path = np.repeat(rng.uniform(-L / 2, L / 2, size=(n_part, 1, 3)), n_bead, axis=1)
+    return xml, path
+
+
+def two_species_trap(workdir, *, n_a=3, n_b=3, lambda_a=0.5, lambda_b=0.25, z_ab=0.5, beta=2.0, n_bead=32, omega=1.0, n_level=3,
+                     seed=1234, n_step_inner=40, n_step_outer=3):
+    """Two distinguishable species of different masses (lambda = hbar^2 / 2m) in one harmonic trap, with
+    bare Coulomb actions within and between them (charge product z_ab across species) and a Bisect
+    move per species."""
+    workdir = Path(workdir)
+    workdir.mkdir(parents=True, exist_ok=True)
+    coulomb_table(workdir / "coulomb_open.pat", z_ab=1.0, L=0.0)
+    coulomb_table(workdir / "coulomb_open_ab.pat", z_ab=z_ab, L=0.0)
+    xml = f"""<Input>
+  <RNG seed="{seed}" />
+  <IO output_prefix="trap2" />
+  <Parallel procs_per_group="1" />
+  <System n_d="3" n_bead="{n_bead}" beta="{beta}" pbc="0" />
+  <Particles>
+    <Species name="a" n_part="{n_a}" lambda="{lambda_a!r}" fermi="0" init_type="File" file_name="init.xyz" all_beads="1" />
+    <Species name="b" n_part="{n_b}" lambda="{lambda_b!r}" fermi="0" init_type="File" file_name="init.xyz" all_beads="1" />
+  </Particles>
+  <Actions>
+    <Action name="KineticA" type="Kinetic" n_images="0" species="a" />
+    <Action name="KineticB" type="Kinetic" n_images="0" species="b" />
+    <Action name="TrapA" type="HarmonicTrap" species="a" omega="{omega}" max_level="0" />
+    <Action name="TrapB" type="HarmonicTrap" species="b" omega="{omega}" max_level="0" />
+    <Action name="CoulombAA" type="BarePairAction" file="coulomb_open.pat" is_coulomb="1" species_a="a" species_b="a" max_level="0" use_long_range="0" />
+    <Action name="CoulombBB" type="BarePairAction" file="coulomb_open.pat" is_coulomb="1" species_a="b" species_b="b" max_level="0" use_long_range="0" />
+    <Action name="CoulombAB" type="BarePairAction" file="coulomb_open_ab.pat" is_coulomb="0" species_a="a" species_b="b" max_level="0" use_long_range="0" />
+  </Actions>
+  <Moves>
+    <Move name="BisectA" type="Bisect" species="a" n_level="{n_level}" />
+    <Move name="BisectB" type="Bisect" species="b" n_level="{n_level}" />
+  </Moves>
+  <Observables>
+    <Observable name="Energy" type="Energy" />
+    <Observable name="gr" type="PairCorrelation" species_a="a" species_b="b" r_min="0." r_max="5.0" n_r="100" />
+  </Observables>
+  <Algorithm>
+    <Loop n_step="{n_step_outer}">
+      <Loop n_step="{n_step_inner}">
+        <Move name="BisectA" />
+        <Move name="BisectB" />
+        <Observable name="Energy" />
+        <Observable name="gr" />
+      </Loop>
+      <Write />
+    </Loop>
+  </Algorithm>
+</Input>
+"""
+    rng = np.random.default_rng(seed)
+    path = rng.standard_normal((n_a + n_b, n_bead, 3))
     return xml, path
 
 

@@ -5,7 +5,8 @@ tests/golden/reference_*.npz hold the answers of simpimc's own Action, Bisect an
 seeded inputs: GetAction / GetActionGradient queries, DActionDBeta, Potential, VirialEnergy, and the
 input's whole Algorithm loop (bisection with the oracle's random stream, measurements, Write events,
 adaptive bisection levels). Cases: the 8-particle trapped Coulomb system (N = 8, M = 32, level 3), an
-adaptive-level trap, DavidPairAction with tables at levels 0-2, 14-electron gases with the bare
+adaptive-level trap, a trap with actions of max_level 2, two species of different masses in one trap,
+DavidPairAction with tables at levels 0-2, 14-electron gases with the bare
 Ewald, Ilkka and David pair actions, one with periodic images in the kinetic action
 (n_images = 10 on a small box) and one measuring the periodic g(r) and S(k), the virial estimator
 on an electron gas and on IlkkaPairAction and DavidPairAction traps, trapped Coulomb bosons with the permuting moves
@@ -55,7 +56,7 @@ def test_oracle_matches_reference_fixture(tmp_path, oracle_mod, name):
 
 def test_fixture_cases_cover_the_hot_path_classes():
     names = fixture_names()
-    assert len(names) >= 17
+    assert len(names) >= 19
     xmls = " ".join(str(load(n)["xml"]) for n in names)
     for cls in ("Kinetic", "HarmonicTrap", "BarePairAction", "IlkkaPairAction", "DavidPairAction", 'adaptive="1"', 'n_images="10"',
                 "StructureFactor", "PairCorrelation", "use_virial_estimator", "PermBisectIterative", "PermBisectTable", 'fermi="1"', 'type="Sign"'):
