@@ -125,9 +125,9 @@ int pimc_move_stats(pimc_ctx* ctx, uint32_t move, uint64_t* out);
 int pimc_get_perm(pimc_ctx* ctx, uint32_t species, uint32_t* perm);
 int pimc_set_perm(pimc_ctx* ctx, uint32_t species, const uint32_t* perm);
 /* pimc_sweep on n_ctx independent chains (contexts of the same input structure on one device):
- * when every schedule entry is a Bisect or permuting move on a species of at most 512 particles
- * (64-bit mode when the species keeps densities), all chains go to one launch of the permutation
- * kernel with one CTA per chain, any action set included (the reference runs one chain per MPI
+ * when every schedule entry is a Bisect or permuting move on a species of at most 512 particles,
+ * all chains go to one launch of the permutation kernel with one CTA per chain, any action set and
+ * either precision included (in 32-bit mode the kernel forms FP32 densities and Ewald terms) (the reference runs one chain per MPI
  * process, framework_class.h:44-53); otherwise the chains run one after another. Errors are
  * reported on ctxs[0]. */
 int pimc_sweep_chains(pimc_ctx** ctxs, uint32_t n_ctx, const uint32_t* moves, const uint64_t* counts, uint32_t n_entries, uint64_t n_rep);
@@ -157,8 +157,9 @@ int pimc_get_block(pimc_ctx* ctx, uint32_t observable, size_t block, double* out
 /* Sweep precision (the reference's build-time PRECISION option, CMakeLists.txt:11-19, as a run-time
  * switch): 64 (default) keeps positions, per-slice densities and all action terms in double-float;
  * 32 keeps the per-slice densities, bead phases and Ewald differences in FP32 with compensated sums
- * (densities rebuilt from the positions at every sweep call), while positions, pair links, level
- * sums and the acceptance test stay double-float and estimators stay FP64. */
+ * (densities rebuilt from the positions at every sweep call, on the sweep kernel and on the
+ * permutation kernel alike), while positions, pair links, level sums and the acceptance test stay
+ * double-float and estimators stay FP64. */
 int pimc_set_precision(pimc_ctx* ctx, int bits);
 /* Synchronises the context stream and reports any device-side error (timeout, non-finite). */
 int pimc_synchronize(pimc_ctx* ctx);

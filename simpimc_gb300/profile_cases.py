@@ -11,6 +11,7 @@
     python -m simpimc_gb300.profile_cases chains   # 608 such chains: 1 + 1 launches of one sweep each (pimc_sweep_chains)
     python -m simpimc_gb300.profile_cases egas_chains  # 38, 152 and 304 66-electron-gas chains: a warm-up
                                                        # launch, then one timed sweep each (pimc_sweep_chains)
+    python -m simpimc_gb300.profile_cases egas_chains32  # the same in the FP32 density mode
 
 The first two hold well under 100 MB on the device, the third about 1.3 GB; a capture of the
 second launch (`-k regex:<Kernel> -s 1 -c 1`) ends in seconds (the large case with one or two
@@ -153,10 +154,11 @@ def chains_case(d):
     print(f"chains ok: {sum(s.move_counters(0)[0] + s.move_counters(1)[0] for s in sims)} attempts")
 
 
-def egas_chains_case(d):
+def egas_chains_case(d, precision=64):
     """Throughput of many 66-electron-gas chains (r_s = 2, beta = 8, M = 128, level 4) in one
     launch: one sweep is 33 attempts of each species' move, 8 times (528 attempts, 15
-    moved beads each). Wall clock around the call, which returns after its launch has finished."""
+    moved beads each). Wall clock around the call, which returns after its launch has finished.
+    precision=32: the chains' FP32 density mode."""
     import os
     import time
 
@@ -168,6 +170,7 @@ def egas_chains_case(d):
             dc = os.path.join(d, f"c{nc}_{c}")
             xml, path = electron_gas(dc, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_units=12.0, n_level=4, seed=20261203 + c)
             s = Simulation(xml, base_dir=dc, chain=c)
+            s.set_precision(precision)
             s.set_path(path)
             sims.append(s)
         sweep_chains(sims, [0, 1], [33, 33], 1)  # warm-up
@@ -185,7 +188,7 @@ def main(argv):
     case = argv[1] if len(argv) > 1 else "batch"
     with tempfile.TemporaryDirectory() as d:
         {"batch": batch_case, "hmc": hmc_case, "egas": egas_case, "egas_phases": egas_phases_case, "hmc_egas": hmc_egas_case, "large32": large32_case, "bosons": bosons_case, "chains": chains_case,
-         "egas_chains": egas_chains_case}[case](d)
+         "egas_chains": egas_chains_case, "egas_chains32": lambda dd: egas_chains_case(dd, 32)}[case](d)
 
 
 if __name__ == "__main__":

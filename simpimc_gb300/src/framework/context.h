@@ -174,6 +174,7 @@ class Context {
     void PermEnqueue(uint32_t m, uint64_t n);
     void PermFinish();
     void PermPrepare(const uint32_t* mv, uint32_t n_entries);
+    void PermDensities();  // FP32 mode: FP32 densities from the positions before permutation-kernel launches
     void PermArgs(uint32_t m, void* out, size_t* smem);  // the kernel's arguments for move m (sweep.cu)
     uint32_t perm_pending_ = 0;  // moves with permutation launches not yet folded into their counters
     void* MoveDescriptors();  // double-float move descriptors on the device (sweep.cu)

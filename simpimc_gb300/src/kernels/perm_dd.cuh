@@ -96,7 +96,8 @@ struct PermArgsDD {
     int32_t sp_rho[kMaxSpecies];
     int32_t max_index[3];
     float2* pos;              // committed positions [M][3][n_pad]
-    float4* rho;              // densities [slots][M][K]
+    float4* rho;              // densities [slots][M][K] (64-bit mode)
+    float2* rho32;            // FP32 mode: densities [slots][M][K]; drho then holds float2 [B][K]
     const int32_t* kidx;
     const float4* phase256;
     const MoveDD* mv;
@@ -572,20 +573,31 @@ __device__ void PermRun(const PermArgsDD& a_in, uint64_t attempt0, uint32_t n_at
             __syncthreads();
         }
         // density changes of the inner beads (species_class.h:406-425), from their final positions
+        // (FP32 mode: FP32 bead phases and density changes, as the sweep kernel's FP32 mode forms them)
         if (slot >= 0 && K > 0) {
+            float2* phf = reinterpret_cast<float2*>(ph);
+            float2* drho32 = reinterpret_cast<float2*>(a.drho);
             for (uint32_t t = 1; t < B; ++t)
                 for (uint32_t m = 0; m < n; ++m) {
                     for (uint32_t it = threadIdx.x; it < 2u * nd * stride; it += blockDim.x) {
                         const uint32_t nn = it % stride, rest = it / stride, d = rest % nd, which = rest / nd;
                         const dd x = which ? LoadDD(SN(m, t, d)) : LoadDD(SO(m, t, d));
-                        ph[((size_t)which * 3 + d) * stride + nn] = PhaseDD(x, (int)nn, a.iL, a.two_pi, a.phase256);
+                        if (a.rho32) phf[((size_t)which * 3 + d) * stride + nn] = PhaseF(x, (int)nn, a.iL, a.phase256);
+                        else ph[((size_t)which * 3 + d) * stride + nn] = PhaseDD(x, (int)nn, a.iL, a.two_pi, a.phase256);
                     }
                     __syncthreads();
                     for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) {
                         const int32_t pk = a.kidx[k];
-                        const ddc dv = CSub(PhaseProductDD(ph + 3 * stride, stride, nd, pk), PhaseProductDD(ph, stride, nd, pk));
-                        float4* cell = &a.drho[(size_t)t * K + k];
-                        *cell = Pack(m == 0 ? dv : CAdd(Unpack(*cell), dv));
+                        if (a.rho32) {
+                            const float2 en = PhaseProductF(phf + 3 * stride, stride, nd, pk), eo = PhaseProductF(phf, stride, nd, pk);
+                            const float2 dv = make_float2(__fsub_rn(en.x, eo.x), __fsub_rn(en.y, eo.y));
+                            float2* cell = &drho32[(size_t)t * K + k];
+                            *cell = m == 0 ? dv : make_float2(__fadd_rn(cell->x, dv.x), __fadd_rn(cell->y, dv.y));
+                        } else {
+                            const ddc dv = CSub(PhaseProductDD(ph + 3 * stride, stride, nd, pk), PhaseProductDD(ph, stride, nd, pk));
+                            float4* cell = &a.drho[(size_t)t * K + k];
+                            *cell = Pack(m == 0 ? dv : CAdd(Unpack(*cell), dv));
+                        }
                     }
                     __syncthreads();
                 }
@@ -667,19 +679,39 @@ __device__ void PermRun(const PermArgsDD& a_in, uint64_t attempt0, uint32_t n_at
                     const bool hom = pa.sa == pa.sb;
                     const int oslot = hom ? slot : a.sp_rho[pa.sa == sp ? pa.sb : pa.sa];
                     dd part_lr{0.f, 0.f};
-                    for (uint32_t it = threadIdx.x; it < ngrid * K; it += blockDim.x) {
-                        const uint32_t k = it % K, t = (it / K + 1u) * skip;
-                        const ddc ro = Unpack(a.rho[((size_t)slot * M + slice(t)) * K + k]);
-                        const ddc dv = Unpack(a.drho[(size_t)t * K + k]);
-                        dd dm;
-                        if (hom) {
-                            // |ro + dv|^2 - |ro|^2 = 2 Re(dv conj ro) + |dv|^2
-                            dm = Add(Scale2(Add(Mul(dv.re, ro.re), Mul(dv.im, ro.im)), 2.f), Add(Sqr(dv.re), Sqr(dv.im)));
-                        } else {
-                            const ddc rb = Unpack(a.rho[((size_t)oslot * M + slice(t)) * K + k]);
-                            dm = Add(Mul(dv.re, rb.re), Mul(dv.im, rb.im));
+                    if (a.rho32) {
+                        // FP32 mode: FP32 terms in a compensated sum, joined to the double-float total
+                        const float2* drho32 = reinterpret_cast<const float2*>(a.drho);
+                        Comp lr32{0.f, 0.f};
+                        for (uint32_t it = threadIdx.x; it < ngrid * K; it += blockDim.x) {
+                            const uint32_t k = it % K, t = (it / K + 1u) * skip;
+                            const float2 ro = a.rho32[((size_t)slot * M + slice(t)) * K + k];
+                            const float2 dv = drho32[(size_t)t * K + k];
+                            float tm;
+                            if (hom) {
+                                tm = __fmaf_rn(dv.x, __fmaf_rn(2.f, ro.x, dv.x), __fmul_rn(dv.y, __fmaf_rn(2.f, ro.y, dv.y)));
+                            } else {
+                                const float2 rb = a.rho32[((size_t)oslot * M + slice(t)) * K + k];
+                                tm = __fmaf_rn(dv.x, rb.x, __fmul_rn(dv.y, rb.y));
+                            }
+                            CompAdd(lr32, __fmul_rn(pa.vk[k].x, tm));
                         }
-                        part_lr = Add(part_lr, Mul(LoadDD(&pa.vk[k]), dm));
+                        part_lr = CompDD(lr32);
+                    } else {
+                        for (uint32_t it = threadIdx.x; it < ngrid * K; it += blockDim.x) {
+                            const uint32_t k = it % K, t = (it / K + 1u) * skip;
+                            const ddc ro = Unpack(a.rho[((size_t)slot * M + slice(t)) * K + k]);
+                            const ddc dv = Unpack(a.drho[(size_t)t * K + k]);
+                            dd dm;
+                            if (hom) {
+                                // |ro + dv|^2 - |ro|^2 = 2 Re(dv conj ro) + |dv|^2
+                                dm = Add(Scale2(Add(Mul(dv.re, ro.re), Mul(dv.im, ro.im)), 2.f), Add(Sqr(dv.re), Sqr(dv.im)));
+                            } else {
+                                const ddc rb = Unpack(a.rho[((size_t)oslot * M + slice(t)) * K + k]);
+                                dm = Add(Mul(dv.re, rb.re), Mul(dv.im, rb.im));
+                            }
+                            part_lr = Add(part_lr, Mul(LoadDD(&pa.vk[k]), dm));
+                        }
                     }
                     const float f = (hom ? 1.f : 2.f) * (pa.kind == kPairBare ? (float)skip : 1.f);
                     dS = Add(dS, MulF(Mul(a.tau, part_lr), f));
@@ -745,8 +777,14 @@ __device__ void PermRun(const PermArgsDD& a_in, uint64_t attempt0, uint32_t n_at
             if (slot >= 0 && K > 0)
                 for (uint32_t it = threadIdx.x; it < (B - 1u) * K; it += blockDim.x) {
                     const uint32_t k = it % K, t = it / K + 1u;
-                    float4* r = &a.rho[((size_t)slot * M + slice(t)) * K + k];
-                    *r = Pack(CAdd(Unpack(*r), Unpack(a.drho[(size_t)t * K + k])));
+                    if (a.rho32) {
+                        float2* r = &a.rho32[((size_t)slot * M + slice(t)) * K + k];
+                        const float2 dv = reinterpret_cast<const float2*>(a.drho)[(size_t)t * K + k];
+                        *r = make_float2(__fadd_rn(r->x, dv.x), __fadd_rn(r->y, dv.y));
+                    } else {
+                        float4* r = &a.rho[((size_t)slot * M + slice(t)) * K + k];
+                        *r = Pack(CAdd(Unpack(*r), Unpack(a.drho[(size_t)t * K + k])));
+                    }
                 }
         }
         __syncthreads();

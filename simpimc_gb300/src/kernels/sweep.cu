@@ -2027,6 +2027,7 @@ static int PermSmemOptin(int device) {
 // double-float permutation kernel (perm_dd.cuh): one CTA runs them in order, in launches of at
 // most 2048 attempts.
 void Context::PermAttempts(uint32_t m, uint64_t n_att) {
+    PermDensities();
     PermEnqueue(m, n_att);
     PermFinish();
 }
@@ -2064,8 +2065,6 @@ void Context::PermArgs(uint32_t m, void* out, size_t* smem_out) {
     const uint32_t sp = mh.dev.species, N = sys.sp_n[sp], M = sys.M;
     if (N > kPermMaxPart)
         throw PimcError(kErrUnsupported, "the permutation kernel (exchanges; pair terms above level 0) takes species of at most 512 particles");
-    if (precision == 32 && sys.sp_rho[sp] >= 0 && sys.K)
-        throw PimcError(kErrUnsupported, "the permutation kernel keeps double-float densities: set precision 64");
     const uint32_t B = 1u << mh.dev.n_level;
     MoveDD* dmoves = static_cast<MoveDD*>(MoveDescriptors());
     EnsureDD();
@@ -2104,7 +2103,8 @@ void Context::PermArgs(uint32_t m, void* out, size_t* smem_out) {
     }
     for (int d = 0; d < 3; ++d) a.max_index[d] = sys.max_index[d];
     a.pos = pos_dd_->as<float2>();
-    a.rho = (rho_slots && sys.K) ? rho_dd_->as<float4>() : nullptr;
+    a.rho = (rho_slots && sys.K && precision != 32) ? rho_dd_->as<float4>() : nullptr;
+    a.rho32 = (rho_slots && sys.K && precision == 32) ? rho32_->as<float2>() : nullptr;
     a.kidx = sys.kidx;
     a.phase256 = sweep_tables_->as<float4>();
     a.mv = dmoves + m;
@@ -2139,9 +2139,43 @@ void Context::PermArgs(uint32_t m, void* out, size_t* smem_out) {
                     .total;
 }
 
+// FP32 mode: the FP32 per-slice densities formed from the positions before the permutation kernel
+// runs, as every sweep-kernel call forms them (the kernel then updates them attempt by attempt).
+void Context::PermDensities() {
+    if (precision != 32 || !rho_slots || !sys.K) return;
+    EnsureDD();
+    BuildSweepTables();
+    SweepArgs a{};
+    a.n_d = sys.n_d;
+    a.M = sys.M;
+    a.n_pad = sys.n_pad;
+    a.K = sys.K;
+    Split(sys.iL, a.iL);
+    for (int s = 0; s < kMaxSpecies; ++s) {
+        a.sp_off[s] = sys.sp_off[s];
+        a.sp_n[s] = sys.sp_n[s];
+    }
+    for (int d = 0; d < 3; ++d) a.max_index[d] = sys.max_index[d];
+    a.pos = pos_dd_->as<float2>();
+    a.rho32 = rho32_->as<float2>();
+    a.kidx = sys.kidx;
+    a.phase256 = sweep_tables_->as<float4>();
+    a.tab_stride = (uint32_t)std::max(std::max(sys.max_index[0], sys.max_index[1]), sys.max_index[2]) + 1;
+    std::vector<int> slot_species(rho_slots, 0);
+    for (uint32_t sp = 0; sp < sys.S; ++sp)
+        if (sys.sp_rho[sp] >= 0) slot_species[sys.sp_rho[sp]] = (int)sp;
+    uint32_t* dss = Parts(rho_slots);
+    CudaCheck(cudaMemcpyAsync(dss, slot_species.data(), rho_slots * sizeof(int), cudaMemcpyHostToDevice, stream), "slot upload");
+    const size_t rsm = (size_t)kRho32Chunk * 3 * a.tab_stride * sizeof(float2);
+    CudaCheck(cudaFuncSetAttribute(InitRho32Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm), "smem attribute");
+    InitRho32Kernel<<<dim3((sys.K + 255) / 256, sys.M, rho_slots), 256, rsm, stream>>>(a, reinterpret_cast<const int*>(dss));
+    CudaCheck(cudaGetLastError(), "rho32 launch");
+}
+
 // Sizes the permutation kernel's scratch for every move of a schedule before any launch (a later
 // move's larger scratch must not replace buffers an earlier launch still uses).
 void Context::PermPrepare(const uint32_t* mv, uint32_t n_entries) {
+    PermDensities();
     for (uint32_t e = 0; e < n_entries; ++e) {
         PermArgsDD a;
         size_t smem;
@@ -2163,10 +2197,9 @@ void SweepChains(const std::vector<Context*>& cs, const uint32_t* mv, const uint
             c->RequireLevelZeroDensities(mv[e]);
             const MoveHost& mh = c->moves[mv[e]];
             // every bisection and permuting move fits the one-CTA kernel (its plain variant replays the
-            // sweep kernel's draws); HMC, species above kPermMaxPart and the FP32 density mode do not
+            // sweep kernel's draws, in either density precision); HMC and species above kPermMaxPart do not
             const uint32_t sp = mh.dev.species;
-            all_perm &= (mh.kind == 0 || mh.kind == 2 || mh.kind == 3) && c->sys.sp_n[sp] <= kPermMaxPart &&
-                        !(c->precision == 32 && c->sys.sp_rho[sp] >= 0 && c->sys.K);
+            all_perm &= (mh.kind == 0 || mh.kind == 2 || mh.kind == 3) && c->sys.sp_n[sp] <= kPermMaxPart;
             if (counts[e] > (1ull << 31)) throw PimcError(kErrArg, "more than 2^31 attempts in one schedule entry");
         }
     }
