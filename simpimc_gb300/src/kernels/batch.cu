@@ -1851,24 +1851,34 @@ void ChainBatch::Run(uint64_t n_cycles, uint64_t spm) {
         CudaCheck(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
         const uint64_t before = kernel_launches;
         const uint32_t heavy = overlap_heavy;
-        if (hmc_per_cycle && n_split_ == 0 && heavy > 0 && heavy < n_chains) {
-            // The heavy chains' sweep and HMC on the main stream, the others' sweep and HMC on the
-            // side stream at the same time: a light chain's HMC fills SMs that its sweep left while
-            // the heavy sweeps finish. Each chain's own kernels stay in order.
-            CudaCheck(cudaEventRecord(ev_fork_, stream), "fork");
-            CudaCheck(cudaStreamWaitEvent(side_, ev_fork_, 0), "fork wait");
-            LaunchSweep(spm, 0, 0, heavy, stream);
-            LaunchSweep(spm, 0, heavy, n_chains - heavy, side_);
-            LaunchHmc(hmc_per_cycle, heavy, n_chains - heavy, side_);
-            LaunchMeasure(heavy, n_chains, side_);
-            LaunchHmc(hmc_per_cycle, 0, heavy, stream);
-            LaunchMeasure(0, heavy, stream);
-            CudaCheck(cudaEventRecord(ev_join_, side_), "join");
-            CudaCheck(cudaStreamWaitEvent(stream, ev_join_, 0), "join wait");
-        } else {
-            LaunchSweep(spm, 0);
-            if (hmc_per_cycle) LaunchHmc(hmc_per_cycle);
-            LaunchMeasure();
+        try {
+            if (hmc_per_cycle && n_split_ == 0 && heavy > 0 && heavy < n_chains) {
+                // The heavy chains' sweep and HMC on the main stream, the others' sweep and HMC on
+                // the side stream at the same time: a light chain's HMC fills SMs that its sweep left
+                // while the heavy sweeps finish. Each chain's own kernels stay in order.
+                CudaCheck(cudaEventRecord(ev_fork_, stream), "fork");
+                CudaCheck(cudaStreamWaitEvent(side_, ev_fork_, 0), "fork wait");
+                LaunchSweep(spm, 0, 0, heavy, stream);
+                LaunchSweep(spm, 0, heavy, n_chains - heavy, side_);
+                LaunchHmc(hmc_per_cycle, heavy, n_chains - heavy, side_);
+                LaunchMeasure(heavy, n_chains, side_);
+                LaunchHmc(hmc_per_cycle, 0, heavy, stream);
+                LaunchMeasure(0, heavy, stream);
+                CudaCheck(cudaEventRecord(ev_join_, side_), "join");
+                CudaCheck(cudaStreamWaitEvent(stream, ev_join_, 0), "join wait");
+            } else {
+                LaunchSweep(spm, 0);
+                if (hmc_per_cycle) LaunchHmc(hmc_per_cycle);
+                LaunchMeasure();
+            }
+        } catch (...) {
+            // end the capture so the batch's stream takes work again, drop the partial graph
+            kernel_launches = before;
+            cudaGraph_t partial = nullptr;
+            cudaStreamEndCapture(stream, &partial);
+            if (partial) cudaGraphDestroy(partial);
+            cudaGetLastError();
+            throw;
         }
         launches_per_cycle_ = (uint32_t)(kernel_launches - before);
         kernel_launches = before;
