@@ -77,6 +77,8 @@ CASES = {
     "trap_levels": ("trapped_coulomb", dict(n_part=6, n_bead=32, n_level=3, seed=101, trap_max_level=2, pair_max_level=2,
                                             n_step_outer=3, n_step_inner=40), 0.0),
     "two_species_trap": ("two_species_trap", dict(seed=103), 0.0),
+    "egas_perm_table": ("electron_gas", dict(n_part=14, n_bead=16, n_level=2, rs=1.0, beta=4.0, k_cut_units=3.0, seed=107,
+                                             perm="PermBisectTable", n_step_outer=2, n_step_inner=30), 0.15),
     "egas_perm": ("electron_gas", dict(n_part=14, n_bead=16, n_level=2, rs=1.0, beta=4.0, k_cut_units=3.0, seed=71,
                                        perm="PermBisectIterative", structure_factor=True, n_step_outer=2, n_step_inner=40), 0.15),
 }

@@ -13,7 +13,8 @@ on an electron gas and on IlkkaPairAction and DavidPairAction traps, trapped Cou
 (PermBisectIterative; PermBisectTable over every particle), whose per-cycle-length counters and
 final path permutation are compared too, trapped Coulomb fermions (the Sign observable and the
 energy's sign cofactor), trapped bosons with DavidPairAction / IlkkaPairAction tables above
-level 0 under PermBisectIterative, and an electron gas whose up spins exchange (Ewald sums).
+level 0 under PermBisectIterative, and electron gases whose up spins exchange by either permuting
+move (Ewald sums).
 
 The oracle must reproduce every number (tolerances in tests/reference_cases.py). Where the reference
 checkout is present, the fixtures are also regenerated from it and must equal the committed files,
@@ -56,7 +57,7 @@ def test_oracle_matches_reference_fixture(tmp_path, oracle_mod, name):
 
 def test_fixture_cases_cover_the_hot_path_classes():
     names = fixture_names()
-    assert len(names) >= 19
+    assert len(names) >= 20
     xmls = " ".join(str(load(n)["xml"]) for n in names)
     for cls in ("Kinetic", "HarmonicTrap", "BarePairAction", "IlkkaPairAction", "DavidPairAction", 'adaptive="1"', 'n_images="10"',
                 "StructureFactor", "PairCorrelation", "use_virial_estimator", "PermBisectIterative", "PermBisectTable", 'fermi="1"', 'type="Sign"'):
