@@ -92,7 +92,7 @@ def _seed_of(xml: str) -> int:
 
 
 MOVE_TYPES = ("Bisect", "PermBisectIterative", "PermBisectTable")
-OBSERVABLE_TYPES = ("Energy", "PairCorrelation", "StructureFactor", "Sign")
+OBSERVABLE_TYPES = ("Energy", "PairCorrelation", "StructureFactor", "Sign", "PathDump")
 
 
 def _moves(xml: str):

@@ -8,7 +8,7 @@
 // Set-up follows Simulation's constructor (framework/simulation_class.h:16-39) with the factories
 // of actions.h, moves.h and observables.h restricted to the hot path's classes: Kinetic,
 // HarmonicTrap, BarePairAction, IlkkaPairAction, DavidPairAction; Bisect, PermBisectIterative,
-// PermBisectTable; Energy, PairCorrelation, StructureFactor, Sign. Species start as init_type "Line" (species_class.h:311-321) and take their
+// PermBisectTable; Energy, PairCorrelation, StructureFactor, Sign, PathDump. Species start as init_type "Line" (species_class.h:311-321) and take their
 // positions from refsim_set_path. Move draws are scripted (refshim/scaffold/rng/rng.h).
 #include <sys/time.h>
 
@@ -48,6 +48,7 @@ using namespace scaffold::rand;
 #include "events/moves/single_species_move/bisect/perm_bisect/perm_bisect_table_class.h"
 #include "events/observables/energy_class.h"
 #include "events/observables/pair_correlation_class.h"
+#include "events/observables/path_dump_class.h"
 #include "events/observables/sign_class.h"
 #include "events/observables/structure_factor_class.h"
 
@@ -147,6 +148,7 @@ int refsim_create(const char* xml, const char* dir, void** out) {
             else if (type == "PairCorrelation") ob = std::make_shared<PairCorrelation>(*s->path, o, s->out);
             else if (type == "StructureFactor") ob = std::make_shared<StructureFactor>(*s->path, o, s->out);
             else if (type == "Sign") ob = std::make_shared<Sign>(*s->path, o, s->out);
+            else if (type == "PathDump") ob = std::make_shared<PathDump>(*s->path, o, s->out);
             else continue;
             s->observables.push_back(ob);
             s->obs_names.push_back(o.GetAttribute<std::string>("name"));
@@ -386,6 +388,26 @@ int refsim_obs_write(void* h, uint32_t o, double* out, uint64_t cap, uint64_t* n
         RefSim& s = *S(h);
         const std::string pre = "Observables/" + s.obs_names.at(o) + "/";
         const std::string& type = s.obs_types[o];
+        if (type == "PathDump") {  // per species: the dump's positions (d fastest, then bead, then particle), then (prev, next) per particle
+            auto& species = s.path->GetSpecies();
+            auto rows = [&]() -> size_t {
+                auto* r = s.out.Appended(pre + species.at(0)->GetName() + "/positions");
+                return r ? r->size() : 0;
+            };
+            const size_t before = rows();
+            s.observables.at(o)->Write();
+            *n = 0;
+            if (rows() == before) return;
+            std::vector<double> vals;
+            for (auto& sp : species)
+                for (const char* what : {"/positions", "/permutation"}) {
+                    const auto& row = s.out.Appended(pre + sp->GetName() + what)->back();
+                    vals.insert(vals.end(), row.begin(), row.end());
+                }
+            *n = vals.size();
+            for (size_t i = 0; i < vals.size() && i < cap; ++i) out[i] = vals[i];
+            return;
+        }
         const std::string key = type == "Energy" ? pre + "total/x" : type == "Sign" ? pre + "x" : pre + "y";
         auto rows = [&]() -> size_t {
             auto* r = s.out.Appended(key);

@@ -51,7 +51,7 @@ def _open_pair_xml(workdir, species, pair, n_bead, beta, n_order, pair_max_level
 def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_level=3, seed=1234, coulomb=True,
                     n_step_inner=100, n_step_outer=10, gr_bins=200, gr_rmax=5.0, virial=False, path_seed=None,
                     write_table=True, pair="BarePairAction", n_order=2, pair_max_level=0, adaptive=False, target_ratio=0.5,
-                    hmc=None, trap_max_level=0):
+                    hmc=None, trap_max_level=0, path_dump=0):
     workdir = Path(workdir)
     workdir.mkdir(parents=True, exist_ok=True)
     pair_xml = _open_pair_xml(workdir, "e", pair, n_bead, beta, n_order, pair_max_level, write_table)
@@ -59,6 +59,8 @@ def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_leve
     energy = ('<Observable name="Energy" type="Energy" use_virial_estimator="1" />' if virial
               else '<Observable name="Energy" type="Energy" />')
     adapt = f' adaptive="1" target_ratio="{target_ratio!r}"' if adaptive else ""
+    # path_dump = skip: a PathDump observable (every skip-th Write dumps the path) after the others
+    dump_xml = f'\n    <Observable name="path_dump" type="PathDump" skip="{path_dump}" />' if path_dump else ""
     # hmc = (step_size, n_steps): the library's whole-path hybrid Monte Carlo move besides Bisect
     hmc_xml = (f'\n    <Move name="HMC" type="HMC" species="e" step_size="{hmc[0]!r}" n_steps="{int(hmc[1])}" />' if hmc else "")
     xml = f"""<Input>
@@ -79,7 +81,7 @@ def trapped_coulomb(workdir, *, n_part=8, beta=2.0, n_bead=32, omega=1.0, n_leve
   </Moves>
   <Observables>
     {energy}
-    <Observable name="gr" type="PairCorrelation" species_a="e" species_b="e" r_min="0." r_max="{gr_rmax}" n_r="{gr_bins}" />
+    <Observable name="gr" type="PairCorrelation" species_a="e" species_b="e" r_min="0." r_max="{gr_rmax}" n_r="{gr_bins}" />{dump_xml}
   </Observables>
   <Algorithm>
     <Loop n_step="{n_step_outer}">
@@ -257,7 +259,7 @@ def sweep_schedule(sim_or_counts, n_bisect_beads: int, n_bead: int):
 
 def trapped_bosons(workdir, *, n_part=3, beta=2.0, n_bead=16, omega=1.0, n_level=2, seed=1234, coulomb=False,
                    perm="PermBisectIterative", n_perm_part=2, fermi=False, n_step_inner=100, n_step_outer=10,
-                   path_seed=None, perm_level=None, sector_max=0, pair="BarePairAction", n_order=2, pair_max_level=0):
+                   path_seed=None, perm_level=None, sector_max=0, pair="BarePairAction", n_order=2, pair_max_level=0, path_dump=0):
     """Identical particles with exchange: the permuting move's species carries the path
     permutation. Observables: Energy (thermal), Permutation (cycle histogram and sectors), Sign.
     With coulomb, `pair` chooses the Coulomb pair action as in trapped_coulomb."""
@@ -266,6 +268,7 @@ def trapped_bosons(workdir, *, n_part=3, beta=2.0, n_bead=16, omega=1.0, n_level
     pair_xml = _open_pair_xml(workdir, "b", pair, n_bead, beta, n_order, pair_max_level, True) if coulomb else ""
     extra = f' n_perm_part="{n_perm_part}"' if perm == "PermBisectTable" else ""
     perm_level = n_level if perm_level is None else perm_level
+    dump_xml = f'\n    <Observable name="path_dump" type="PathDump" skip="{path_dump}" />' if path_dump else ""
     xml = f"""<Input>
   <RNG seed="{seed}" />
   <IO output_prefix="bosons" />
@@ -286,7 +289,7 @@ def trapped_bosons(workdir, *, n_part=3, beta=2.0, n_bead=16, omega=1.0, n_level
   <Observables>
     <Observable name="Energy" type="Energy" />
     <Observable name="Permutation" type="Permutation" species="b"{f' sector_max="{sector_max}"' if sector_max else ""} />
-    <Observable name="Sign" type="Sign" />
+    <Observable name="Sign" type="Sign" />{dump_xml}
   </Observables>
   <Algorithm>
     <Loop n_step="{n_step_outer}">

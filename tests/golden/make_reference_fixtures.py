@@ -15,7 +15,8 @@ and the reference's answers on it:
   counters and the final path permutation at the ring closure. Observable blocks are keyed by the
   observable's place in the input; the Permutation observable is left out (the reference's sector
   lookup has no entries: species_class.h:178-180 generates the sectors only when some already
-  exist), and the Sign observable and the sign cofactor of the energy are in the fermion case.
+  exist), and the Sign observable and the sign cofactor of the energy are in the fermion case. A
+  PathDump observable's dumps are kept under their own key (`path_dumps_<index>`).
 
 PermBisectTable's case cycles every particle of its species (n_perm_part = N): with fewer, the
 reference leaves the particles owning the end beads out of the action's particle list when the
@@ -79,6 +80,10 @@ CASES = {
     "two_species_trap": ("two_species_trap", dict(seed=103), 0.0),
     "egas_perm_table": ("electron_gas", dict(n_part=14, n_bead=16, n_level=2, rs=1.0, beta=4.0, k_cut_units=3.0, seed=107,
                                              perm="PermBisectTable", n_step_outer=2, n_step_inner=30), 0.15),
+    "trap_dump": ("trapped_coulomb", dict(n_part=5, n_bead=16, n_level=2, seed=109, path_dump=2, n_step_outer=5, n_step_inner=30),
+                  0.0),
+    "bosons_dump": ("trapped_bosons", dict(n_part=4, n_bead=16, n_level=2, seed=113, coulomb=True, perm="PermBisectIterative",
+                                           path_dump=1, n_step_outer=4, n_step_inner=60), 0.0),
     "egas_perm": ("electron_gas", dict(n_part=14, n_bead=16, n_level=2, rs=1.0, beta=4.0, k_cut_units=3.0, seed=71,
                                        perm="PermBisectIterative", structure_factor=True, n_step_outer=2, n_step_inner=40), 0.15),
 }
@@ -181,8 +186,11 @@ def reference_answers(name, workdir):
         out[f"move_writes_{m}"] = np.array(rows, dtype=np.int64)  # (n_attempt, n_accept, n_level or -1) per Write
     for m, rows in pstats.items():
         out[f"perm_writes_{m}"] = np.array(rows, dtype=np.int64)  # (attempts, accepts) per cycle length, per Write
+    import xml.etree.ElementTree as ET
+    obs_types = [o.get("type") for o in ET.fromstring(xml).find("Observables")]
     for o, rows in blocks.items():
-        out[f"blocks_{o}"] = np.array(rows)
+        # PathDump's rows are its dumps (positions, then (prev, next) per particle, per species)
+        out[f"path_dumps_{o}" if obs_types[o] == "PathDump" else f"blocks_{o}"] = np.array(rows)
     out["final_path"] = r.get_path(1)
     if pstats:
         first_species = min(r._species.values())  # (index, n_part) of species 0

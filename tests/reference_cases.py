@@ -64,11 +64,12 @@ def _close(a, b, rel):
 
 
 def check_against_fixture(make_sim, name, workdir, run_blocks, final_path, move_writes=None, grad_rel=1e-8, perm_writes=None,
-                          final_perm=None):
+                          final_perm=None, path_dumps=None):
     """make_sim(xml, workdir) -> a fresh simulation; run_blocks(sim, xml) -> {obs: [blocks]} after
     running the Algorithm; final_path(sim) -> positions; move_writes(sim, xml) -> {move: rows} or None;
     perm_writes(sim, xml) -> {permuting move: [Write, (attempts, accepts), cycle length]} and
-    final_perm(sim, xml) -> the first species' path permutation, required when the fixture has them."""
+    final_perm(sim, xml) -> the first species' path permutation, required when the fixture has them;
+    path_dumps(sim, xml) -> {PathDump observable: [dump, values]} (None: not compared)."""
     gen = generator()
     fx = load(name)
     xml, path = gen.build_case(name, workdir)
@@ -136,6 +137,13 @@ def check_against_fixture(make_sim, name, workdir, run_blocks, final_path, move_
         got = np.asarray(final_perm(sim, xml), dtype=np.int64)
         if not np.array_equal(got, fx["final_perm"]):
             errs.append(("final perm", got.tolist(), fx["final_perm"].tolist()))
+    if path_dumps is not None:
+        got_pd = path_dumps(sim, xml)
+        for k in [k for k in fx if k.startswith("path_dumps_")]:
+            o = int(k[len("path_dumps_"):])
+            got, want = np.asarray(got_pd.get(o, []), dtype=float), fx[k]
+            if got.shape != want.shape or np.max(np.abs(got - want)) >= 1e-9:
+                errs.append(("path dumps", o, got.shape, want.shape))
     fp = final_path(sim)
     if not (fp.shape == fx["final_path"].shape and np.max(np.abs(fp - fx["final_path"])) < 1e-9):
         errs.append(("final path", float(np.max(np.abs(fp - fx["final_path"]))) if fp.shape == fx["final_path"].shape else None))

@@ -58,8 +58,25 @@ def test_gpu_matches_reference_fixture(tmp_path, gpu_lib, name):
             rows[i] = np.stack([att, acc], axis=1).astype(np.int64)
         return rows
 
+    def path_dumps(sim, xml):
+        t = output(sim)
+        root = ET.fromstring(xml)
+        species = [sp.get("name") for sp in root.find("Particles")]
+        rows = {}
+        for o, ob in enumerate(root.find("Observables")):
+            if ob.get("type") != "PathDump":
+                continue
+            parts = []
+            for sp in species:
+                pre = f"Observables/{ob.get('name')}/{sp}/"
+                n_dump = int(np.asarray(t[pre + "n_dump"]).ravel()[0])
+                parts.append(np.asarray(t[pre + "positions"]).reshape(n_dump, -1))
+                parts.append(np.asarray(t[pre + "permutation"]).reshape(n_dump, -1))
+            rows[o] = np.concatenate(parts, axis=1)
+        return rows
+
     sim, errs = check_against_fixture(make, name, tmp_path, blocks, lambda s: s.get_path(1), move_writes, perm_writes=perm_writes,
-                                      final_perm=lambda s, xml: s.get_perm(0))
+                                      final_perm=lambda s, xml: s.get_perm(0), path_dumps=path_dumps)
     sim_xml_types = [a.get("type") for a in ET.fromstring(str(load(name)["xml"])).find("Actions")]
     sim.close()
     # IlkkaPairAction's long-range gradient in NEW mode: the reference reads species b's NEW-copy
