@@ -18,13 +18,14 @@ and the reference's answers on it:
   exist), and the Sign observable and the sign cofactor of the energy are in the fermion case. A
   PathDump observable's dumps are kept under their own key (`path_dumps_<index>`).
 
-PermBisectTable's case cycles every particle of its species (n_perm_part = N): with fewer, the
+PermBisectTable's cases cycle every particle of their species (n_perm_part = N): with fewer, the
 reference leaves the particles owning the end beads out of the action's particle list when the
 segment passes a permuted ring closure (perm_bisect_table_class.h:133-141, against
 perm_bisect_iterative_class.h:141-146), which the oracle and the GPU library do not copy.
 
 The tests compare the oracle (tests/test_reference_pins.py, CPU) and the GPU library
 (tests/test_gpu_reference_fixtures.py) with these numbers; neither needs the reference checkout.
+The path dumps are compared with the library's output only (the oracle writes none).
 
 Usage: python tests/golden/make_reference_fixtures.py   (needs the checkout; see oracle/ref.py)
 """
