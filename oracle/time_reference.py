@@ -12,7 +12,12 @@ prints both rates and their ratio. The two final paths must agree (same Markov c
 The reference's draws are decoded before its timed loop; the ctypes cost of its per-attempt calls
 is measured with a call of the same marshalling and subtracted.
 
+`--egas` times the single-chain 66-electron gas instead (N = 66, r_s = 2, beta = 8, M = 128, Ewald
+|k| < 12 (2 pi / L), level 4; the bench's plain_electron_gas workload): 200 attempts of each spin's
+Bisect, alternating, through both codes.
+
 Usage: python oracle/time_reference.py [chain ...]   (default: chains 0, 32, ..., 224)
+       python oracle/time_reference.py --egas
 """
 from __future__ import annotations
 
@@ -65,7 +70,48 @@ def time_chain(items, tmp, c):
     return n, m, moves / (t_ref - t_call), moves / t_port, same
 
 
+def time_egas(n_each=200):
+    """The 66-electron gas: n_each attempts of each spin's move, alternating, through the reference
+    and the restatement from the same start; returns (bead-moves/s of each, same path)."""
+    import oracle
+    from oracle import ref
+    from simpimc_gb300.configs import electron_gas
+    tmp = tempfile.mkdtemp(prefix="pimc_timeref_")
+    level = 4
+    xml, path = electron_gas(tmp, n_part=66, rs=2.0, beta=8.0, n_bead=128, k_cut_units=12.0, n_level=level, seed=20261203)
+    r = ref.RefSim(xml, base_dir=tmp)
+    r.set_path(path)
+    o = oracle.OracleSim(xml, base_dir=tmp)
+    o.set_path(path)
+    draws = []
+    for a in range(n_each):
+        for m in (0, 1):
+            pb, z, lu = oracle.bisect_draws(r._seed, 0, m, a, 33, 128, level)
+            draws.append((m, int(pb[0]), int(pb[1]), np.ascontiguousarray(z, dtype=np.float64), np.exp(np.asarray(lu, dtype=np.float64))))
+    L, h = r._L, r._h
+    t0 = time.perf_counter()
+    for m, pa, b0, zz, uu in draws:
+        if L.refsim_move_attempt(h, m, pa, b0, zz.ctypes.data_as(ref._DP), len(zz), uu.ctypes.data_as(ref._DP), len(uu)) != 0:
+            raise RuntimeError(L.refsim_last_error().decode())
+    t_ref = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for _ in range(n_each):
+        o.move_attempts(0, 1)
+        o.move_attempts(1, 1)
+    t_port = time.perf_counter() - t0
+    same = bool(np.allclose(o.get_path(1), r.get_path(1), rtol=0, atol=1e-9))
+    moves = 2 * n_each * ((1 << level) - 1)
+    return moves / t_ref, moves / t_port, same
+
+
 def main():
+    if sys.argv[1:] == ["--egas"]:
+        v_ref, v_port, same = time_egas()
+        if not same:
+            raise RuntimeError("the reference and the restatement left different paths")
+        print(f"66-electron gas: reference {v_ref / 1e3:.2f} k bead-moves/s, restatement {v_port / 1e3:.2f} k, "
+              f"restatement / reference {v_port / v_ref:.2f}")
+        return
     from simpimc_gb300.configs import batched_trap_chains
     chains = [int(a) for a in sys.argv[1:]] or list(range(0, N_CHAINS, N_CHAINS // 8))
     tmp = tempfile.mkdtemp(prefix="pimc_timeref_")
