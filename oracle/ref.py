@@ -16,7 +16,9 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-LIB = HERE / "_ref" / "libsimpimc_ref.so"
+# SIMPIMC_REF_OPENMP=1 selects the OpenMP build (timing only; the fixtures use the serial one)
+OPENMP = os.environ.get("SIMPIMC_REF_OPENMP", "0") == "1"
+LIB = HERE / "_ref" / ("libsimpimc_ref_omp.so" if OPENMP else "libsimpimc_ref.so")
 SOURCES = [HERE / "refharness.cc", HERE / "build_ref.sh", *sorted((HERE / "refshim").rglob("*.h"))]
 DEFAULT_REFERENCE = "/root/reference"
 
@@ -40,7 +42,8 @@ def build(force: bool = False) -> Path:
     if ref is None:
         raise RuntimeError("the reference checkout is not present; the reference harness cannot be built here")
     if force or not LIB.exists() or any(s.stat().st_mtime > LIB.stat().st_mtime for s in SOURCES):
-        r = subprocess.run(["sh", str(HERE / "build_ref.sh"), ref], capture_output=True, text=True)
+        env = dict(os.environ, REF_OPENMP="1" if OPENMP else "0")
+        r = subprocess.run(["sh", str(HERE / "build_ref.sh"), ref], capture_output=True, text=True, env=env)
         if r.returncode != 0:
             raise RuntimeError(f"reference harness build failed:\n{r.stderr}")
     return LIB
