@@ -836,8 +836,10 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
                          "sample": f"{threads} threads, each running the cycle (bisection sweep + HMC attempt) on its share of "
                                    f"the 256 chains for {per_step_s:.0f} s per step (the FP64 CPU restatement: the reference's "
-                                   "own headers build only against oracle/refshim with the reference checkout, absent on the GPU "
-                                   "box; tests/test_reference_pins.py pins the restatement to that build)"},
+                                   "own headers build only against oracle/refshim with the reference checkout, which is not "
+                                   "where the bench runs; tests/test_reference_pins.py pins the restatement to that build bit "
+                                   "for bit, and oracle/time_reference.py measured the restatement 2.6-3.3x faster than the "
+                                   "reference's Move::DoEvent on the same bisection attempts, one thread each)"},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
