@@ -39,8 +39,8 @@ Arms:
                      HBM; `e2e` = the same cycles through the C interface with every chain's path
                      uploaded from and downloaded to host memory and the energies read back.
   --impl reference   the FP64 CPU restatement of the reference hot path (the reference's own headers
-                     build only against oracle/refshim where its checkout exists, not on the GPU box;
-                     the restatement is pinned to that build) running the same cycle on the same
+                     build only against oracle/refshim where its checkout exists, which is not where
+                     the bench runs; the restatement is pinned to that build) running the same cycle on the same
                      chains, one group of chains per host thread, on a bounded sample per step.
 """
 from __future__ import annotations

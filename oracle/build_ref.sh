@@ -4,7 +4,7 @@
 # (CMakeLists.txt:57-75: -O3 -ffast-math, NDEBUG) but without -fopenmp: the OpenMP reductions of
 # the actions then run in loop order (deterministic fixtures), and an index error inside one of
 # those loops is reported instead of terminating the process. Output: oracle/_ref/libsimpimc_ref.so.
-# Test infrastructure only; needs the checkout, so it runs where that exists (not on the GPU machine).
+# Test infrastructure only; needs the checkout, so it runs only where that exists.
 # With REF_OPENMP=1 it builds oracle/_ref/libsimpimc_ref_omp.so instead, with -fopenmp as the
 # reference's release build has it: the timing of the reference's own OpenMP model (one chain, the
 # action loops over threads), not the fixtures.
