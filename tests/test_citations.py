@@ -16,7 +16,7 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 MANIFEST = os.path.join(ROOT, "tests", "golden", "reference_line_counts.json")
 # Of the documents, only this repository's own are checked; other parties' files are not its citations.
-OWN_DOCS = ("DESIGN.md", "INTEGRATION.md", "README.md")
+OWN_DOCS = ("DESIGN.md", "INTEGRATION.md", "README.md", "profiles/")
 SKIP_PREFIX = ("tests/golden/",)
 CITE = re.compile(r"([A-Za-z_][A-Za-z0-9_./-]*\.(?:h|cc|cpp|py|xml|cmake))(?::|\s+lines?\s+)(\d+)(?:\s*-\s*(\d+))?"
                   r"((?:\s*,\s*\d+(?:\s*-\s*\d+)?)*)")
@@ -38,7 +38,7 @@ def _tracked():
     try:
         out = subprocess.check_output(["git", "ls-files"], cwd=ROOT, text=True)
         return [f for f in out.split()
-                if not f.startswith(SKIP_PREFIX) and not f.endswith(".json") and (not f.endswith(".md") or f in OWN_DOCS)]
+                if not f.startswith(SKIP_PREFIX) and not f.endswith(".json") and (not f.endswith(".md") or f.startswith(OWN_DOCS))]
     except Exception:
         pytest.skip("not a git checkout")
 
